@@ -1,0 +1,204 @@
+/**
+ * @file openmoc_gb300.h
+ * @brief C ABI of the GB300 (sm_103a) method-of-characteristics transport
+ *        solver: the drop-in back end for OpenMOC's Solver hooks.
+ *
+ * Every entry point takes plain pointers and sizes and returns an int status
+ * (MOC_OK = 0, negative on error); nothing throws across the ABI.  The text
+ * of the last error on the calling thread is available from moc_last_error().
+ * The OpenMOC-side subclass (openmoc_gb300/adapter/GB300Solver.h) turns a
+ * non-zero status into log_printf(ERROR, ...), which throws std::logic_error
+ * exactly like OpenMOC's own validation failures (src/log.cpp:588-599).
+ *
+ * A context owns one problem on one GPU: packed tracks, cross sections and
+ * every flux array live in device memory until moc_destroy.  Host arrays
+ * passed in are copied during the call and may be freed afterwards.  A
+ * context is single-owner and not thread-safe.
+ *
+ * Array layouts (the packing done by openmoc_gb300/adapter/pack_reference.h
+ * from OpenMOC's TrackGenerator, Geometry and Material objects):
+ *   tracks are in UID order (src/TrackGenerator.cpp:1795-1818);
+ *   seg_len[S] float, seg_fsr[S] int32, seg_off[T+1] int64;
+ *   track_ang[T] int32: row of weights / inv_sin for the track;
+ *   next[2T] int64: next track at the forward / backward end;
+ *   flags[T] uint8: bit0 the forward exit enters its next track forward,
+ *     bit1 the backward exit enters forward, bit2 / bit3 the forward /
+ *     backward outgoing flux is transferred (REFLECTIVE or PERIODIC boundary);
+ *   weights[A][Ph], inv_sin[A][Ph] float (2D: A = num_azim/2,
+ *     Ph = num_polar/2; 3D: A = num_azim/2*num_polar, Ph = 1, inv_sin = 1);
+ *   sigma_t[M][G], sigma_s[M][G][G] ([dest][orig]), nu_sigma_f[M][G],
+ *     chi[M][G] float; fsr_mat[R] int32; fsr_vol[R] float;
+ *   scalar fluxes / sources [R][G] float; boundary angular fluxes
+ *     [T][2][F] float with F = G*Ph, polar-major within a direction
+ *     (src/Solver.h:49-54).
+ */
+#ifndef OPENMOC_GB300_H_
+#define OPENMOC_GB300_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MOC_OK 0
+#define MOC_ERR_ARG (-1)         /* invalid argument or inconsistent input */
+#define MOC_ERR_CUDA (-2)        /* a CUDA runtime call failed */
+#define MOC_ERR_STATE (-3)       /* call made in the wrong order */
+#define MOC_ERR_MEMORY (-4)      /* device memory budget exceeded */
+#define MOC_ERR_UNSUPPORTED (-5) /* feature not supported by this back end */
+#define MOC_ERR_TIMEOUT (-6)     /* a device-side bounded wait ran out */
+
+/* Residual types, same values as OpenMOC's residualType (src/Solver.h:82-92) */
+#define MOC_SCALAR_FLUX 0
+#define MOC_FISSION_SOURCE 1
+#define MOC_TOTAL_SOURCE 2
+
+/* Exponential evaluators for the attenuation factor 1 - exp(-tau/sin) */
+#define MOC_EXP_TABLE 0     /* shared-memory interpolation table (default) */
+#define MOC_EXP_INTRINSIC 1 /* hardware ex2 with a series below x = 1/16 */
+
+typedef struct moc_ctx moc_ctx;
+
+typedef struct {
+  int32_t num_groups;     /* G */
+  int32_t num_polar_half; /* Ph: polar values per track direction */
+  int32_t num_angles;     /* A: rows of the weight tables */
+  int32_t num_materials;  /* M */
+  int64_t num_fsrs;       /* R */
+  int64_t num_tracks;     /* T */
+  int64_t num_segments;   /* S */
+  int32_t solve_3d;       /* 1: explicit 3D tracks (weight per track) */
+  int32_t device;         /* CUDA device ordinal */
+} moc_dims;
+
+/** Text of the last error reported on this thread ("" if none). */
+const char* moc_last_error(void);
+
+/** Library version string. */
+const char* moc_version(void);
+
+/** Creates a context; replaces GPUSolver's constructor + device setup
+ *  (src/accel/cuda/GPUSolver.cu:771-796, src/accel/cuda/GPUQuery.cu). */
+int moc_create(const moc_dims* dims, moc_ctx** out);
+
+/** Frees every device buffer of the context (GPUSolver::~GPUSolver,
+ *  src/accel/cuda/GPUSolver.cu:798-825). */
+int moc_destroy(moc_ctx* ctx);
+
+/** Uploads packed tracks and segments; replaces GPUSolver::initializeTracks
+ *  and clone_track (src/accel/cuda/GPUSolver.cu:1312-1358,
+ *  src/accel/cuda/clone.cu:86-126).  Checks every index on the host. */
+int moc_upload_tracks(moc_ctx* ctx, const float* seg_len,
+                      const int32_t* seg_fsr, const int64_t* seg_off,
+                      const int32_t* track_ang, const int64_t* next,
+                      const uint8_t* flags);
+
+/** Uploads the quadrature tables; replaces GPUSolver::copyQuadrature
+ *  (src/accel/cuda/GPUSolver.cu:1098-1148) and
+ *  Quadrature::getWeightInline / getInvSinThetaInline (src/Quadrature.h:
+ *  317-336). */
+int moc_upload_quadrature(moc_ctx* ctx, const float* weights,
+                          const float* inv_sin);
+
+/** Uploads cross sections; replaces GPUSolver::initializeMaterials and
+ *  clone_material (src/accel/cuda/GPUSolver.cu:1253-1310,
+ *  src/accel/cuda/clone.cu:12-84). */
+int moc_upload_materials(moc_ctx* ctx, const float* sigma_t,
+                         const float* sigma_s, const float* nu_sigma_f,
+                         const float* chi);
+
+/** Optional fission cross sections sigma_f[M][G], needed only for
+ *  moc_compute_fsr_fission_rates with nu = 0 (Material::getSigmaF,
+ *  src/Material.h:81-103). */
+int moc_upload_sigma_f(moc_ctx* ctx, const float* sigma_f);
+
+/** Uploads FSR materials and volumes; replaces GPUSolver::initializeFSRs
+ *  (src/accel/cuda/GPUSolver.cu:1170-1251). */
+int moc_upload_fsrs(moc_ctx* ctx, const int32_t* fsr_mat,
+                    const float* fsr_vol);
+
+/** Sets (q != NULL) or clears (q == NULL) the [R][G] fixed sources;
+ *  Solver::setFixedSourceByFSR / resetFixedSources (src/Solver.h:481-485),
+ *  GPUSolver::initializeFixedSources (src/accel/cuda/GPUSolver.cu:1416). */
+int moc_set_fixed_sources(moc_ctx* ctx, const float* q);
+
+/** Solver::setConvergenceThreshold (src/Solver.cpp:461). */
+int moc_set_convergence_threshold(moc_ctx* ctx, double threshold);
+
+/** Selects the exponential evaluator (MOC_EXP_*);
+ *  Solver::useExponentialInterpolation / useExponentialIntrinsic
+ *  (src/Solver.cpp:575-595). */
+int moc_set_exponential(moc_ctx* ctx, int kind);
+
+/** Sweep kernel shape: lps lanes per track direction (power of two <= 32)
+ *  each carrying `slots` energy groups (lps * slots >= G, slots <= 9);
+ *  lps = 0 restores the built-in choice.  Replaces
+ *  GPUSolver::setNumThreadBlocks / setNumThreadsPerBlock
+ *  (src/accel/cuda/GPUSolver.cu:987-1015). */
+int moc_set_sweep_shape(moc_ctx* ctx, int lps, int slots);
+int moc_get_sweep_shape(moc_ctx* ctx, int* lps, int* slots);
+
+/** Iterations enqueued between two checks of the device convergence flag
+ *  (default 4). */
+int moc_set_iterations_per_sync(moc_ctx* ctx, int k);
+
+/* ---- whole solves, device-resident (Solver::computeEigenvalue,
+ *      computeSource, computeFlux; src/Solver.cpp:1352-1700) ------------- */
+int moc_compute_eigenvalue(moc_ctx* ctx, int max_iters, int res_type);
+int moc_compute_source(moc_ctx* ctx, int max_iters, double k_eff,
+                       int res_type);
+int moc_compute_flux(moc_ctx* ctx, int max_iters, int only_fixed_source);
+
+/* ---- results ------------------------------------------------------------ */
+int moc_get_keff(moc_ctx* ctx, double* keff);            /* Solver::getKeff */
+int moc_get_num_iterations(moc_ctx* ctx, int* iters);    /* getNumIterations */
+int moc_get_residual(moc_ctx* ctx, double* residual);
+/** Solver::getFluxes / GPUSolver::getFluxes (src/accel/cuda/GPUSolver.cu:
+ *  962-985): copies the [R][G] scalar flux to out (n = R*G). */
+int moc_get_fluxes(moc_ctx* ctx, float* out, int64_t n);
+/** Solver::setFluxes / GPUSolver::setFluxes (src/Solver.h:478,
+ *  src/accel/cuda/GPUSolver.cu:1075-1096): sets the scalar flux (and the stored flux). */
+int moc_set_fluxes(moc_ctx* ctx, const float* in, int64_t n);
+/** Wall time of transport sweeps since the last solve started (ms), and
+ *  the number of sweeps: Timer split "Transport Sweep"
+ *  (src/CPUSolver.cpp:2365-2378). */
+int moc_get_sweep_time(moc_ctx* ctx, double* ms, int64_t* num_sweeps);
+
+/* ---- the protected Solver hooks, one call each (src/Solver.h:334-431) --- */
+int moc_zero_track_fluxes(moc_ctx* ctx);
+int moc_flatten_fsr_fluxes(moc_ctx* ctx, float value);
+int moc_flatten_fsr_fluxes_chi(moc_ctx* ctx, int material);
+int moc_store_fsr_fluxes(moc_ctx* ctx);
+int moc_normalize_fluxes(moc_ctx* ctx, double* factor);
+int moc_compute_fsr_sources(moc_ctx* ctx, int iteration);
+int moc_transport_sweep(moc_ctx* ctx);
+int moc_add_source_to_scalar_flux(moc_ctx* ctx);
+int moc_compute_keff(moc_ctx* ctx);
+int moc_compute_residual(moc_ctx* ctx, int res_type, double* residual);
+int moc_set_keff(moc_ctx* ctx, double keff);
+/** Solver::computeFSRFissionRates (src/Solver.h:539-540,
+ *  src/accel/cuda/GPUSolver.cu:1970): volume-integrated
+ *  (nu-)fission rate per FSR. */
+int moc_compute_fsr_fission_rates(moc_ctx* ctx, double* rates, int64_t n,
+                                  int nu);
+
+/* ---- state access for tests and restart --------------------------------- */
+/** Reduced sources Q/(4 pi) per FSR and group (Solver::getFSRSource*4pi). */
+int moc_get_reduced_sources(moc_ctx* ctx, float* out, int64_t n);
+/** Old (stored) scalar flux. */
+int moc_get_old_fluxes(moc_ctx* ctx, float* out, int64_t n);
+int moc_set_old_fluxes(moc_ctx* ctx, const float* in, int64_t n);
+/** Track angular fluxes that the next sweep starts from ([T][2][F]), i.e.
+ *  OpenMOC's _start_flux (src/Solver.h:252-253). */
+int moc_get_start_flux(moc_ctx* ctx, float* out, int64_t n);
+int moc_set_start_flux(moc_ctx* ctx, const float* in, int64_t n);
+
+/** Number of CUDA kernels this library launched on the context so far. */
+int moc_get_launch_count(moc_ctx* ctx, int64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OPENMOC_GB300_H_ */

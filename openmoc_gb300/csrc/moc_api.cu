@@ -1,0 +1,1031 @@
+// Host side of libopenmoc_gb300.so: the solver context, uploads, the
+// device-resident iteration drivers and the C ABI of include/openmoc_gb300.h.
+//
+// The iteration drivers restate Solver::computeEigenvalue, computeSource and
+// computeFlux (src/Solver.cpp:1352-1700) with every per-iteration scalar kept
+// on the device (moc::DevScalars).  A block of iterations is enqueued
+// without host synchronisation; kernels of iterations after convergence
+// return at once (DevScalars::done), and the host checks the state once per
+// block, the only device-to-host traffic of a solve besides the result.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/openmoc_gb300.h"
+#include "moc_internal.cuh"
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int code, const std::string& msg) {
+  g_error = msg;
+  return code;
+}
+
+#define MOC_CUDA(call)                                                    \
+  do {                                                                    \
+    cudaError_t e_ = (call);                                              \
+    if (e_ != cudaSuccess)                                                \
+      return fail(MOC_ERR_CUDA, std::string(#call) + ": " +               \
+                                    cudaGetErrorString(e_));              \
+  } while (0)
+
+#define MOC_CHECK(cond, code, msg) \
+  do {                             \
+    if (!(cond)) return fail(code, msg); \
+  } while (0)
+
+#define MOC_TRY(expr)        \
+  do {                       \
+    int s_ = (expr);         \
+    if (s_ != MOC_OK) return s_; \
+  } while (0)
+
+template <typename T>
+int dalloc(T** p, size_t n) {
+  *p = nullptr;
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc((void**) p, n * sizeof(T));
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    return fail(MOC_ERR_MEMORY, "device memory exhausted allocating " +
+                                    std::to_string(n * sizeof(T)) + " bytes");
+  }
+  MOC_CUDA(e);
+  return MOC_OK;
+}
+
+template <typename T>
+void dfree(T*& p) {
+  if (p) cudaFree((void*) p);
+  p = nullptr;
+}
+
+}  // namespace
+
+struct moc_ctx {
+  moc_dims d{};
+  cudaStream_t stream = nullptr;
+
+  // tracks
+  int2* segs = nullptr;
+  int64_t* seg_off = nullptr;
+  int32_t* order = nullptr;
+  int32_t* track_ang = nullptr;
+  int32_t* next = nullptr;
+  uint8_t* flags = nullptr;
+  // quadrature
+  float* weights = nullptr;
+  float* inv_sin = nullptr;
+  // materials
+  float* sigma_t = nullptr;
+  float* sigma_s = nullptr;
+  float* nu_sigma_f = nullptr;
+  float* chi = nullptr;
+  float* scat_out = nullptr;
+  float* sigma_f = nullptr;
+  uint8_t* fissile = nullptr;
+  std::vector<uint8_t> h_fissile;
+  std::vector<float> h_chi;
+  // FSRs
+  int32_t* fsr_mat = nullptr;
+  float* fsr_vol = nullptr;
+  float* fixed = nullptr;
+  // state
+  float* phi = nullptr;
+  float* phi_old = nullptr;
+  float* qt = nullptr;
+  float* psi[2] = {nullptr, nullptr};
+  float* exp_table = nullptr;
+  double* rates = nullptr;
+  moc::DevScalars* sc = nullptr;      // device
+  moc::DevScalars* hsc = nullptr;     // pinned host mirror
+
+  bool have_tracks = false, have_quad = false, have_mats = false,
+       have_fsrs = false;
+  double threshold = 1e-5;
+  int exp_kind = MOC_EXP_TABLE;
+  int lps = 0, slots = 0;
+  int num_iterations = 0;
+  double keff = 1.0;
+  double residual = 0.0;
+  long long num_fissionable = 0;
+  int64_t launches = 0;
+  double sweep_ms = 0.0;
+  int64_t num_sweeps = 0;
+  int iters_per_sync = 4;
+  std::vector<cudaEvent_t> ev;   // event pairs around sweeps
+};
+
+namespace {
+
+int64_t fluxes_per_track(const moc_ctx* c) {
+  return (int64_t) c->d.num_groups * c->d.num_polar_half;
+}
+
+int64_t num_psi(const moc_ctx* c) {
+  return 2 * c->d.num_tracks * fluxes_per_track(c);
+}
+
+int64_t num_flux(const moc_ctx* c) {
+  return c->d.num_fsrs * c->d.num_groups;
+}
+
+moc::SweepArgs sweep_args(moc_ctx* c, int check_done) {
+  moc::SweepArgs a{};
+  a.segs = c->segs;
+  a.seg_off = c->seg_off;
+  a.order = c->order;
+  a.track_ang = c->track_ang;
+  a.next = c->next;
+  a.flags = c->flags;
+  a.weights = c->weights;
+  a.inv_sin = c->inv_sin;
+  a.sigma_t = c->sigma_t;
+  a.fsr_mat = c->fsr_mat;
+  a.qt = c->qt;
+  a.exp_table = c->exp_table;
+  a.phi = c->phi;
+  a.psi[0] = c->psi[0];
+  a.psi[1] = c->psi[1];
+  a.sc = c->sc;
+  a.num_tracks = c->d.num_tracks;
+  a.num_groups = c->d.num_groups;
+  a.num_materials = c->d.num_materials;
+  a.lps = c->lps;
+  a.check_done = check_done;
+  return a;
+}
+
+moc::SolverArgs solver_args(moc_ctx* c, int check_done) {
+  moc::SolverArgs a{};
+  a.sigma_t = c->sigma_t;
+  a.sigma_s = c->sigma_s;
+  a.nu_sigma_f = c->nu_sigma_f;
+  a.chi = c->chi;
+  a.fissile = c->fissile;
+  a.fsr_mat = c->fsr_mat;
+  a.fsr_vol = c->fsr_vol;
+  a.fixed = c->fixed;
+  a.scat_out = c->scat_out;
+  a.sigma_f = c->sigma_f;
+  a.phi = c->phi;
+  a.phi_old = c->phi_old;
+  a.qt = c->qt;
+  a.psi[0] = c->psi[0];
+  a.psi[1] = c->psi[1];
+  a.sc = c->sc;
+  a.num_fsrs = c->d.num_fsrs;
+  a.num_psi = num_psi(c);
+  a.num_groups = c->d.num_groups;
+  a.num_materials = c->d.num_materials;
+  a.check_done = check_done;
+  return a;
+}
+
+int ready(moc_ctx* c) {
+  MOC_CHECK(c != nullptr, MOC_ERR_ARG, "null context");
+  MOC_CHECK(c->have_tracks && c->have_quad && c->have_mats && c->have_fsrs,
+            MOC_ERR_STATE,
+            "tracks, quadrature, materials and FSRs must be uploaded first");
+  MOC_CUDA(cudaSetDevice(c->d.device));
+  return MOC_OK;
+}
+
+int pull(moc_ctx* c) {
+  MOC_CUDA(cudaMemcpyAsync(c->hsc, c->sc, sizeof(moc::DevScalars),
+                           cudaMemcpyDeviceToHost, c->stream));
+  MOC_CUDA(cudaStreamSynchronize(c->stream));
+  return MOC_OK;
+}
+
+int push(moc_ctx* c) {
+  MOC_CUDA(cudaMemcpyAsync(c->sc, c->hsc, sizeof(moc::DevScalars),
+                           cudaMemcpyHostToDevice, c->stream));
+  MOC_CUDA(cudaStreamSynchronize(c->stream));
+  return MOC_OK;
+}
+
+// Utilisation of lanes for G groups split over lps lanes.
+double lane_use(int G, int lps, int slots) {
+  return (double) G / (double) (lps * slots);
+}
+
+// Heuristic kernel shape: the most lanes per track direction whose lane
+// utilisation is within 5% of the best reachable with at most kMaxSlots
+// groups per lane.
+void pick_shape(int G, int* lps_out, int* slots_out) {
+  double best = 0.0;
+  for (int lps = 1; lps <= 32; lps *= 2) {
+    int slots = (G + lps - 1) / lps;
+    if (slots > moc::kMaxSlots) continue;
+    best = std::max(best, lane_use(G, lps, slots));
+  }
+  int chosen = 32;
+  for (int lps = 32; lps >= 1; lps /= 2) {
+    int slots = (G + lps - 1) / lps;
+    if (slots > moc::kMaxSlots) continue;
+    if (lane_use(G, lps, slots) >= 0.95 * best) {
+      chosen = lps;
+      break;
+    }
+  }
+  *lps_out = chosen;
+  *slots_out = (G + chosen - 1) / chosen;
+}
+
+int enqueue_sweep(moc_ctx* c, int check_done, bool timed, int ev_index) {
+  if (c->lps == 0) pick_shape(c->d.num_groups, &c->lps, &c->slots);
+  if (timed) {
+    while ((int) c->ev.size() < 2 * (ev_index + 1)) {
+      cudaEvent_t e;
+      MOC_CUDA(cudaEventCreate(&e));
+      c->ev.push_back(e);
+    }
+    MOC_CUDA(cudaEventRecord(c->ev[2 * ev_index], c->stream));
+  }
+  moc::SweepArgs a = sweep_args(c, check_done);
+  if (!moc::launch_sweep(a, c->d.num_polar_half, c->slots, c->exp_kind,
+                         c->stream))
+    return fail(MOC_ERR_UNSUPPORTED,
+                "no sweep kernel for " + std::to_string(c->d.num_polar_half) +
+                    " polar angles per half space and " +
+                    std::to_string(c->slots) + " groups per lane");
+  c->launches++;
+  MOC_CUDA(cudaGetLastError());
+  if (timed) MOC_CUDA(cudaEventRecord(c->ev[2 * ev_index + 1], c->stream));
+  return MOC_OK;
+}
+
+int collect_sweep_times(moc_ctx* c, int n) {
+  for (int i = 0; i < n; i++) {
+    float ms = 0.f;
+    MOC_CUDA(cudaEventElapsedTime(&ms, c->ev[2 * i], c->ev[2 * i + 1]));
+    c->sweep_ms += ms;
+  }
+  return MOC_OK;
+}
+
+// Resets the device state machine for a new solve.
+int begin_solve(moc_ctx* c, int mode, int max_iters, int res_type,
+                double keff) {
+  MOC_TRY(pull(c));
+  moc::DevScalars& s = *c->hsc;
+  s.keff = keff;
+  s.k_prev = keff;
+  s.factor = 1.0;
+  s.residual = 0.0;
+  s.accum_rate = 0.0;
+  s.accum_res = 0.0;
+  s.threshold = c->threshold;
+  s.ticket_rate = s.ticket_res = s.ticket_sweep = 0;
+  s.iteration = 0;
+  s.max_iters = max_iters;
+  s.done = 0;
+  s.converged = 0;
+  s.dk = 0;
+  s.mode = mode;
+  s.res_type = res_type;
+  s.neg_sources = 0;
+  s.neg_fluxes = 0;
+  s.num_fissionable = c->num_fissionable;
+  MOC_TRY(push(c));
+  c->sweep_ms = 0.0;
+  c->num_sweeps = 0;
+  return MOC_OK;
+}
+
+int zero_track_fluxes(moc_ctx* c) {
+  size_t bytes = sizeof(float) * (size_t) num_psi(c);
+  MOC_CUDA(cudaMemsetAsync(c->psi[0], 0, bytes, c->stream));
+  MOC_CUDA(cudaMemsetAsync(c->psi[1], 0, bytes, c->stream));
+  MOC_TRY(pull(c));
+  c->hsc->scale[0] = c->hsc->scale[1] = 1.0f;
+  c->hsc->cur = 0;
+  MOC_TRY(push(c));
+  return MOC_OK;
+}
+
+// The device loop: iterations of `kind` until the device reports done.
+int run_iterations(moc_ctx* c, int kind, int res_type) {
+  moc::SolverArgs a = solver_args(c, 1);
+  int completed = 0;
+  for (;;) {
+    const int k = c->iters_per_sync;
+    for (int i = 0; i < k; i++) {
+      if (kind == moc::kModeFlux) {
+        moc::launch_zero_phi(a, c->stream);
+      } else {
+        moc::launch_compute_sources(a, -1, 1, c->stream);
+      }
+      c->launches++;
+      MOC_TRY(enqueue_sweep(c, 1, true, i));
+      moc::launch_add_source(a, kind == moc::kModeEigen ? 1 : 0, c->stream);
+      moc::launch_residual(a, res_type, kind == moc::kModeEigen ? 1 : 0, 1, 1,
+                           c->stream);
+      c->launches += 2;
+      MOC_CUDA(cudaGetLastError());
+    }
+    MOC_TRY(pull(c));
+    // sweeps that returned at once after convergence still record events;
+    // count only the iterations the device performed
+    const int done_now = c->hsc->iteration - completed;
+    MOC_TRY(collect_sweep_times(c, std::min(done_now, k)));
+    c->num_sweeps += done_now;
+    completed = c->hsc->iteration;
+    if (c->hsc->done) break;
+  }
+  c->keff = c->hsc->keff;
+  c->residual = c->hsc->residual;
+  return MOC_OK;
+}
+
+void build_exp_table(std::vector<float>& t) {
+  t.resize(moc::kExpTableSize);
+  for (int i = 0; i < moc::kExpTableSize; i++)
+    t[i] = (float) (-std::expm1(-(double) i * (double) moc::kExpTableH));
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* moc_last_error(void) { return g_error.c_str(); }
+
+const char* moc_version(void) { return "openmoc_gb300 0.1 (sm_103a)"; }
+
+int moc_create(const moc_dims* dims, moc_ctx** out) {
+  MOC_CHECK(dims != nullptr && out != nullptr, MOC_ERR_ARG, "null argument");
+  *out = nullptr;
+  const moc_dims& d = *dims;
+  MOC_CHECK(d.num_groups >= 1 && d.num_groups <= 32 * moc::kMaxSlots,
+            MOC_ERR_ARG, "num_groups must be in [1, 288]");
+  MOC_CHECK(d.num_polar_half >= 1 && moc::sweep_max_slots(d.num_polar_half) > 0,
+            MOC_ERR_UNSUPPORTED,
+            "num_polar_half must be 1, 2 or 3 (2, 4 or 6 polar angles in 2D)");
+  MOC_CHECK(d.num_angles >= 1 && d.num_materials >= 1 && d.num_fsrs >= 1 &&
+                d.num_tracks >= 1 && d.num_segments >= 0,
+            MOC_ERR_ARG, "empty problem dimension");
+  MOC_CHECK(d.num_tracks < (1LL << 31) && d.num_fsrs < (1LL << 31),
+            MOC_ERR_ARG, "tracks and FSRs are limited to 2^31");
+  MOC_CHECK((int64_t) d.num_materials * d.num_groups <= 16384, MOC_ERR_ARG,
+            "num_materials * num_groups is limited to 16384");
+  int ndev = 0;
+  MOC_CUDA(cudaGetDeviceCount(&ndev));
+  MOC_CHECK(d.device >= 0 && d.device < ndev, MOC_ERR_ARG,
+            "no CUDA device " + std::to_string(d.device));
+  MOC_CUDA(cudaSetDevice(d.device));
+
+  moc_ctx* c = new moc_ctx();
+  c->d = d;
+  int st = MOC_OK;
+  auto bail = [&](int s) {
+    moc_destroy(c);
+    return s;
+  };
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) !=
+      cudaSuccess)
+    return bail(fail(MOC_ERR_CUDA, "cudaStreamCreate failed"));
+  const int64_t R = d.num_fsrs, G = d.num_groups;
+  const int64_t npsi = num_psi(c);
+  // memory budget: state arrays plus tracks
+  size_t need = sizeof(float) * (size_t) (3 * R * G + 2 * npsi) +
+                sizeof(int2) * (size_t) d.num_segments +
+                (sizeof(int64_t) + 4 * sizeof(int32_t) + 1) *
+                    (size_t) d.num_tracks;
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && need > free_b)
+    return bail(fail(MOC_ERR_MEMORY,
+                     "problem needs " + std::to_string(need) +
+                         " bytes of device memory, " +
+                         std::to_string(free_b) + " free"));
+  if ((st = dalloc(&c->phi, R * G)) || (st = dalloc(&c->phi_old, R * G)) ||
+      (st = dalloc(&c->qt, R * G)) || (st = dalloc(&c->psi[0], npsi)) ||
+      (st = dalloc(&c->psi[1], npsi)) ||
+      (st = dalloc(&c->exp_table, moc::kExpTableSize)) ||
+      (st = dalloc(&c->rates, R)) || (st = dalloc(&c->sc, 1)))
+    return bail(st);
+  if (cudaMallocHost((void**) &c->hsc, sizeof(moc::DevScalars)) !=
+      cudaSuccess)
+    return bail(fail(MOC_ERR_CUDA, "cudaMallocHost failed"));
+  std::memset(c->hsc, 0, sizeof(moc::DevScalars));
+  c->hsc->keff = 1.0;
+  c->hsc->k_prev = 1.0;
+  c->hsc->factor = 1.0;
+  c->hsc->scale[0] = c->hsc->scale[1] = 1.0f;
+  c->hsc->threshold = c->threshold;
+  std::vector<float> tab;
+  build_exp_table(tab);
+  if (cudaMemcpy(c->exp_table, tab.data(), sizeof(float) * tab.size(),
+                 cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(c->sc, c->hsc, sizeof(moc::DevScalars),
+                 cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemset(c->phi, 0, sizeof(float) * R * G) != cudaSuccess ||
+      cudaMemset(c->phi_old, 0, sizeof(float) * R * G) != cudaSuccess ||
+      cudaMemset(c->qt, 0, sizeof(float) * R * G) != cudaSuccess ||
+      cudaMemset(c->psi[0], 0, sizeof(float) * npsi) != cudaSuccess ||
+      cudaMemset(c->psi[1], 0, sizeof(float) * npsi) != cudaSuccess)
+    return bail(fail(MOC_ERR_CUDA, "device initialisation failed"));
+  *out = c;
+  return MOC_OK;
+}
+
+int moc_destroy(moc_ctx* c) {
+  if (!c) return MOC_OK;
+  cudaSetDevice(c->d.device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  dfree(c->segs);
+  dfree(c->seg_off);
+  dfree(c->order);
+  dfree(c->track_ang);
+  dfree(c->next);
+  dfree(c->flags);
+  dfree(c->weights);
+  dfree(c->inv_sin);
+  dfree(c->sigma_t);
+  dfree(c->sigma_s);
+  dfree(c->nu_sigma_f);
+  dfree(c->chi);
+  dfree(c->scat_out);
+  dfree(c->sigma_f);
+  dfree(c->fissile);
+  dfree(c->fsr_mat);
+  dfree(c->fsr_vol);
+  dfree(c->fixed);
+  dfree(c->phi);
+  dfree(c->phi_old);
+  dfree(c->qt);
+  dfree(c->psi[0]);
+  dfree(c->psi[1]);
+  dfree(c->exp_table);
+  dfree(c->rates);
+  dfree(c->sc);
+  if (c->hsc) cudaFreeHost(c->hsc);
+  for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return MOC_OK;
+}
+
+int moc_upload_tracks(moc_ctx* c, const float* seg_len, const int32_t* seg_fsr,
+                      const int64_t* seg_off, const int32_t* track_ang,
+                      const int64_t* next, const uint8_t* flags) {
+  MOC_CHECK(c && seg_off && track_ang && next && flags, MOC_ERR_ARG,
+            "null argument");
+  const int64_t T = c->d.num_tracks, S = c->d.num_segments;
+  const int64_t R = c->d.num_fsrs;
+  MOC_CHECK(S == 0 || (seg_len && seg_fsr), MOC_ERR_ARG, "null segments");
+  MOC_CHECK(seg_off[0] == 0 && seg_off[T] == S, MOC_ERR_ARG,
+            "seg_off must run from 0 to num_segments");
+  std::vector<int64_t> count(T);
+  for (int64_t t = 0; t < T; t++) {
+    count[t] = seg_off[t + 1] - seg_off[t];
+    MOC_CHECK(count[t] >= 0 && count[t] < (1LL << 31), MOC_ERR_ARG,
+              "bad segment count on track " + std::to_string(t));
+    MOC_CHECK(track_ang[t] >= 0 && track_ang[t] < c->d.num_angles,
+              MOC_ERR_ARG, "track angle index out of range");
+    for (int d = 0; d < 2; d++)
+      MOC_CHECK(next[2 * t + d] >= 0 && next[2 * t + d] < T, MOC_ERR_ARG,
+                "next-track index out of range on track " +
+                    std::to_string(t));
+  }
+  std::vector<int2> packed(S);
+  for (int64_t s = 0; s < S; s++) {
+    MOC_CHECK(seg_fsr[s] >= 0 && seg_fsr[s] < R, MOC_ERR_ARG,
+              "segment FSR id out of range at segment " + std::to_string(s));
+    MOC_CHECK(std::isfinite(seg_len[s]) && seg_len[s] >= 0.0f, MOC_ERR_ARG,
+              "bad segment length at segment " + std::to_string(s));
+    int2 v;
+    std::memcpy(&v.x, &seg_len[s], 4);
+    v.y = seg_fsr[s];
+    packed[s] = v;
+  }
+  // longest tracks first (stable, so equal lengths keep UID order)
+  std::vector<int32_t> order(T);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
+    return count[a] > count[b];
+  });
+  std::vector<int32_t> next32(2 * T);
+  for (int64_t i = 0; i < 2 * T; i++) next32[i] = (int32_t) next[i];
+  MOC_CUDA(cudaSetDevice(c->d.device));
+  dfree(c->segs);
+  dfree(c->seg_off);
+  dfree(c->order);
+  dfree(c->track_ang);
+  dfree(c->next);
+  dfree(c->flags);
+  MOC_TRY(dalloc(&c->segs, S));
+  MOC_TRY(dalloc(&c->seg_off, T + 1));
+  MOC_TRY(dalloc(&c->order, T));
+  MOC_TRY(dalloc(&c->track_ang, T));
+  MOC_TRY(dalloc(&c->next, 2 * T));
+  MOC_TRY(dalloc(&c->flags, T));
+  MOC_CUDA(cudaMemcpy(c->segs, packed.data(), sizeof(int2) * S,
+                      cudaMemcpyHostToDevice));
+  MOC_CUDA(cudaMemcpy(c->seg_off, seg_off, sizeof(int64_t) * (T + 1),
+                      cudaMemcpyHostToDevice));
+  MOC_CUDA(cudaMemcpy(c->order, order.data(), sizeof(int32_t) * T,
+                      cudaMemcpyHostToDevice));
+  MOC_CUDA(cudaMemcpy(c->track_ang, track_ang, sizeof(int32_t) * T,
+                      cudaMemcpyHostToDevice));
+  MOC_CUDA(cudaMemcpy(c->next, next32.data(), sizeof(int32_t) * 2 * T,
+                      cudaMemcpyHostToDevice));
+  MOC_CUDA(cudaMemcpy(c->flags, flags, T, cudaMemcpyHostToDevice));
+  c->have_tracks = true;
+  return MOC_OK;
+}
+
+int moc_upload_quadrature(moc_ctx* c, const float* weights,
+                          const float* inv_sin) {
+  MOC_CHECK(c && weights && inv_sin, MOC_ERR_ARG, "null argument");
+  const int64_t n = (int64_t) c->d.num_angles * c->d.num_polar_half;
+  for (int64_t i = 0; i < n; i++)
+    MOC_CHECK(std::isfinite(weights[i]) && std::isfinite(inv_sin[i]) &&
+                  inv_sin[i] >= 1.0f,
+              MOC_ERR_ARG, "bad quadrature entry " + std::to_string(i));
+  MOC_CUDA(cudaSetDevice(c->d.device));
+  dfree(c->weights);
+  dfree(c->inv_sin);
+  MOC_TRY(dalloc(&c->weights, n));
+  MOC_TRY(dalloc(&c->inv_sin, n));
+  MOC_CUDA(cudaMemcpy(c->weights, weights, sizeof(float) * n,
+                      cudaMemcpyHostToDevice));
+  MOC_CUDA(cudaMemcpy(c->inv_sin, inv_sin, sizeof(float) * n,
+                      cudaMemcpyHostToDevice));
+  c->have_quad = true;
+  return MOC_OK;
+}
+
+static void count_fissionable(moc_ctx* c, const int32_t* fsr_mat) {
+  c->num_fissionable = 0;
+  for (int64_t r = 0; r < c->d.num_fsrs; r++)
+    c->num_fissionable += c->h_fissile[fsr_mat[r]] ? 1 : 0;
+}
+
+int moc_upload_materials(moc_ctx* c, const float* sigma_t,
+                         const float* sigma_s, const float* nu_sigma_f,
+                         const float* chi) {
+  MOC_CHECK(c && sigma_t && sigma_s && nu_sigma_f && chi, MOC_ERR_ARG,
+            "null argument");
+  const int M = c->d.num_materials, G = c->d.num_groups;
+  const int64_t MG = (int64_t) M * G;
+  std::vector<float> scat_out(MG, 0.0f);
+  std::vector<uint8_t> fis(M, 0);
+  for (int m = 0; m < M; m++) {
+    for (int g = 0; g < G; g++) {
+      const int64_t i = (int64_t) m * G + g;
+      MOC_CHECK(std::isfinite(sigma_t[i]) && sigma_t[i] > 0.0f, MOC_ERR_ARG,
+                "sigma_t must be positive and finite (material " +
+                    std::to_string(m) + ", group " + std::to_string(g + 1) +
+                    ")");
+      MOC_CHECK(std::isfinite(nu_sigma_f[i]) && std::isfinite(chi[i]),
+                MOC_ERR_ARG, "non-finite fission data in material " +
+                                 std::to_string(m));
+      if (nu_sigma_f[i] > 0.0f) fis[m] = 1;
+    }
+    for (int gd = 0; gd < G; gd++)
+      for (int g = 0; g < G; g++) {
+        const float v = sigma_s[((int64_t) m * G + gd) * G + g];
+        MOC_CHECK(std::isfinite(v), MOC_ERR_ARG,
+                  "non-finite scattering data in material " +
+                      std::to_string(m));
+        scat_out[(int64_t) m * G + g] += v;
+      }
+  }
+  MOC_CUDA(cudaSetDevice(c->d.device));
+  dfree(c->sigma_t);
+  dfree(c->sigma_s);
+  dfree(c->nu_sigma_f);
+  dfree(c->chi);
+  dfree(c->scat_out);
+  dfree(c->fissile);
+  MOC_TRY(dalloc(&c->sigma_t, MG));
+  MOC_TRY(dalloc(&c->sigma_s, MG * G));
+  MOC_TRY(dalloc(&c->nu_sigma_f, MG));
+  MOC_TRY(dalloc(&c->chi, MG));
+  MOC_TRY(dalloc(&c->scat_out, MG));
+  MOC_TRY(dalloc(&c->fissile, M));
+  MOC_CUDA(cudaMemcpy(c->sigma_t, sigma_t, 4 * MG, cudaMemcpyHostToDevice));
+  MOC_CUDA(cudaMemcpy(c->sigma_s, sigma_s, 4 * MG * G, cudaMemcpyHostToDevice));
+  MOC_CUDA(cudaMemcpy(c->nu_sigma_f, nu_sigma_f, 4 * MG,
+                      cudaMemcpyHostToDevice));
+  MOC_CUDA(cudaMemcpy(c->chi, chi, 4 * MG, cudaMemcpyHostToDevice));
+  MOC_CUDA(cudaMemcpy(c->scat_out, scat_out.data(), 4 * MG,
+                      cudaMemcpyHostToDevice));
+  MOC_CUDA(cudaMemcpy(c->fissile, fis.data(), M, cudaMemcpyHostToDevice));
+  c->h_fissile = fis;
+  c->h_chi.assign(chi, chi + MG);
+  c->have_mats = true;
+  return MOC_OK;
+}
+
+int moc_upload_sigma_f(moc_ctx* c, const float* sigma_f) {
+  MOC_CHECK(c && sigma_f, MOC_ERR_ARG, "null argument");
+  const int64_t MG = (int64_t) c->d.num_materials * c->d.num_groups;
+  MOC_CUDA(cudaSetDevice(c->d.device));
+  dfree(c->sigma_f);
+  MOC_TRY(dalloc(&c->sigma_f, MG));
+  MOC_CUDA(cudaMemcpy(c->sigma_f, sigma_f, 4 * MG, cudaMemcpyHostToDevice));
+  return MOC_OK;
+}
+
+int moc_upload_fsrs(moc_ctx* c, const int32_t* fsr_mat, const float* fsr_vol) {
+  MOC_CHECK(c && fsr_mat && fsr_vol, MOC_ERR_ARG, "null argument");
+  MOC_CHECK(c->have_mats, MOC_ERR_STATE, "upload materials before FSRs");
+  const int64_t R = c->d.num_fsrs;
+  for (int64_t r = 0; r < R; r++) {
+    MOC_CHECK(fsr_mat[r] >= 0 && fsr_mat[r] < c->d.num_materials, MOC_ERR_ARG,
+              "FSR material index out of range at FSR " + std::to_string(r));
+    MOC_CHECK(std::isfinite(fsr_vol[r]) && fsr_vol[r] >= 0.0f, MOC_ERR_ARG,
+              "bad FSR volume at FSR " + std::to_string(r));
+  }
+  MOC_CUDA(cudaSetDevice(c->d.device));
+  dfree(c->fsr_mat);
+  dfree(c->fsr_vol);
+  MOC_TRY(dalloc(&c->fsr_mat, R));
+  MOC_TRY(dalloc(&c->fsr_vol, R));
+  MOC_CUDA(cudaMemcpy(c->fsr_mat, fsr_mat, 4 * R, cudaMemcpyHostToDevice));
+  MOC_CUDA(cudaMemcpy(c->fsr_vol, fsr_vol, 4 * R, cudaMemcpyHostToDevice));
+  count_fissionable(c, fsr_mat);
+  c->have_fsrs = true;
+  return MOC_OK;
+}
+
+int moc_set_fixed_sources(moc_ctx* c, const float* q) {
+  MOC_CHECK(c, MOC_ERR_ARG, "null context");
+  MOC_CUDA(cudaSetDevice(c->d.device));
+  if (!q) {
+    dfree(c->fixed);
+    return MOC_OK;
+  }
+  const int64_t n = num_flux(c);
+  for (int64_t i = 0; i < n; i++)
+    MOC_CHECK(std::isfinite(q[i]), MOC_ERR_ARG, "non-finite fixed source");
+  if (!c->fixed) MOC_TRY(dalloc(&c->fixed, n));
+  MOC_CUDA(cudaMemcpy(c->fixed, q, 4 * n, cudaMemcpyHostToDevice));
+  return MOC_OK;
+}
+
+int moc_set_convergence_threshold(moc_ctx* c, double threshold) {
+  MOC_CHECK(c, MOC_ERR_ARG, "null context");
+  MOC_CHECK(threshold > 0.0 && std::isfinite(threshold), MOC_ERR_ARG,
+            "the convergence threshold must be positive");
+  c->threshold = threshold;
+  return MOC_OK;
+}
+
+int moc_set_exponential(moc_ctx* c, int kind) {
+  MOC_CHECK(c, MOC_ERR_ARG, "null context");
+  MOC_CHECK(kind == MOC_EXP_TABLE || kind == MOC_EXP_INTRINSIC, MOC_ERR_ARG,
+            "unknown exponential evaluator");
+  c->exp_kind = kind;
+  return MOC_OK;
+}
+
+int moc_set_sweep_shape(moc_ctx* c, int lps, int slots) {
+  MOC_CHECK(c, MOC_ERR_ARG, "null context");
+  if (lps == 0) {
+    c->lps = 0;
+    c->slots = 0;
+    return MOC_OK;
+  }
+  MOC_CHECK(lps >= 1 && lps <= 32 && (lps & (lps - 1)) == 0, MOC_ERR_ARG,
+            "lanes per track direction must be a power of two <= 32");
+  MOC_CHECK(slots >= 1 && slots <= moc::kMaxSlots &&
+                (int64_t) lps * slots >= c->d.num_groups,
+            MOC_ERR_ARG, "lanes x groups-per-lane must cover every group");
+  c->lps = lps;
+  c->slots = slots;
+  return MOC_OK;
+}
+
+int moc_get_sweep_shape(moc_ctx* c, int* lps, int* slots) {
+  MOC_CHECK(c && lps && slots, MOC_ERR_ARG, "null argument");
+  if (c->lps == 0) pick_shape(c->d.num_groups, &c->lps, &c->slots);
+  *lps = c->lps;
+  *slots = c->slots;
+  return MOC_OK;
+}
+
+int moc_set_iterations_per_sync(moc_ctx* c, int k) {
+  MOC_CHECK(c && k >= 1 && k <= 1024, MOC_ERR_ARG, "k must be in [1, 1024]");
+  c->iters_per_sync = k;
+  return MOC_OK;
+}
+
+// ---------------------------------------------------------------- solves
+int moc_compute_eigenvalue(moc_ctx* c, int max_iters, int res_type) {
+  MOC_TRY(ready(c));
+  MOC_CHECK(max_iters >= 1, MOC_ERR_ARG, "max_iters must be positive");
+  MOC_CHECK(res_type >= 0 && res_type <= 2, MOC_ERR_ARG, "bad residual type");
+  MOC_CHECK(res_type != MOC_FISSION_SOURCE || c->num_fissionable > 0,
+            MOC_ERR_ARG,
+            "The Solver is unable to compute a FISSION_SOURCE residual "
+            "without fissionable FSRs");
+  MOC_CHECK(c->num_fissionable > 0, MOC_ERR_ARG,
+            "an eigenvalue solve needs fissionable material");
+  // Solver::computeInitialFluxGuess: flat flux 1, normalised, stored;
+  // zero boundary fluxes (src/Solver.cpp:1710-1757)
+  MOC_TRY(zero_track_fluxes(c));
+  MOC_TRY(begin_solve(c, moc::kModeEigen, max_iters, res_type, 1.0));
+  moc::SolverArgs a = solver_args(c, 0);
+  moc::launch_fill(c->phi, num_flux(c), 1.0f, c->stream);
+  moc::launch_fission_rate(a, 1, c->stream);
+  moc::launch_scale_phi(a, c->stream);
+  c->launches += 3;
+  MOC_CUDA(cudaMemcpyAsync(c->phi_old, c->phi, 4 * num_flux(c),
+                           cudaMemcpyDeviceToDevice, c->stream));
+  MOC_CUDA(cudaGetLastError());
+  MOC_TRY(run_iterations(c, moc::kModeEigen, res_type));
+  c->num_iterations = c->hsc->iteration;
+  return MOC_OK;
+}
+
+int moc_compute_source(moc_ctx* c, int max_iters, double k_eff,
+                       int res_type) {
+  MOC_TRY(ready(c));
+  MOC_CHECK(max_iters >= 1, MOC_ERR_ARG, "max_iters must be positive");
+  MOC_CHECK(k_eff > 0.0, MOC_ERR_ARG,
+            "The Solver is unable to compute the source with a non-positive "
+            "keff");
+  MOC_CHECK(res_type >= 0 && res_type <= 2, MOC_ERR_ARG, "bad residual type");
+  MOC_TRY(zero_track_fluxes(c));
+  MOC_TRY(begin_solve(c, moc::kModeSource, max_iters, res_type, k_eff));
+  moc::launch_fill(c->phi, num_flux(c), 1.0f, c->stream);
+  c->launches++;
+  MOC_CUDA(cudaMemcpyAsync(c->phi_old, c->phi, 4 * num_flux(c),
+                           cudaMemcpyDeviceToDevice, c->stream));
+  MOC_TRY(run_iterations(c, moc::kModeSource, res_type));
+  c->num_iterations =
+      c->hsc->converged ? c->hsc->iteration - 1 : max_iters;
+  return MOC_OK;
+}
+
+int moc_compute_flux(moc_ctx* c, int max_iters, int only_fixed_source) {
+  MOC_TRY(ready(c));
+  MOC_CHECK(max_iters >= 1, MOC_ERR_ARG, "max_iters must be positive");
+  MOC_CHECK(only_fixed_source, MOC_ERR_UNSUPPORTED,
+            "computeFlux without only_fixed_source needs a previous "
+            "eigenvalue solve; use the hooks");
+  MOC_TRY(zero_track_fluxes(c));
+  MOC_TRY(begin_solve(c, moc::kModeFlux, max_iters, MOC_SCALAR_FLUX, 1.0));
+  moc::SolverArgs a = solver_args(c, 0);
+  moc::launch_fill(c->phi, num_flux(c), 0.0f, c->stream);
+  MOC_CUDA(cudaMemcpyAsync(c->phi_old, c->phi, 4 * num_flux(c),
+                           cudaMemcpyDeviceToDevice, c->stream));
+  moc::launch_compute_sources(a, 0, 0, c->stream);
+  c->launches += 2;
+  MOC_TRY(run_iterations(c, moc::kModeFlux, MOC_SCALAR_FLUX));
+  c->num_iterations =
+      c->hsc->converged ? c->hsc->iteration - 1 : max_iters;
+  return MOC_OK;
+}
+
+// --------------------------------------------------------------- results
+int moc_get_keff(moc_ctx* c, double* keff) {
+  MOC_CHECK(c && keff, MOC_ERR_ARG, "null argument");
+  MOC_TRY(pull(c));
+  *keff = c->hsc->keff;
+  return MOC_OK;
+}
+
+int moc_get_num_iterations(moc_ctx* c, int* iters) {
+  MOC_CHECK(c && iters, MOC_ERR_ARG, "null argument");
+  *iters = c->num_iterations;
+  return MOC_OK;
+}
+
+int moc_get_residual(moc_ctx* c, double* residual) {
+  MOC_CHECK(c && residual, MOC_ERR_ARG, "null argument");
+  MOC_TRY(pull(c));
+  *residual = c->hsc->residual;
+  return MOC_OK;
+}
+
+static int copy_out(moc_ctx* c, const float* src, float* out, int64_t n,
+                    int64_t expected) {
+  MOC_CHECK(c && out, MOC_ERR_ARG, "null argument");
+  MOC_CHECK(n == expected, MOC_ERR_ARG,
+            "expected " + std::to_string(expected) + " values, got " +
+                std::to_string(n));
+  MOC_CUDA(cudaSetDevice(c->d.device));
+  MOC_CUDA(cudaMemcpyAsync(out, src, 4 * n, cudaMemcpyDeviceToHost, c->stream));
+  MOC_CUDA(cudaStreamSynchronize(c->stream));
+  return MOC_OK;
+}
+
+static int copy_in(moc_ctx* c, float* dst, const float* in, int64_t n,
+                   int64_t expected) {
+  MOC_CHECK(c && in, MOC_ERR_ARG, "null argument");
+  MOC_CHECK(n == expected, MOC_ERR_ARG,
+            "expected " + std::to_string(expected) + " values, got " +
+                std::to_string(n));
+  MOC_CUDA(cudaSetDevice(c->d.device));
+  MOC_CUDA(cudaMemcpyAsync(dst, in, 4 * n, cudaMemcpyHostToDevice, c->stream));
+  MOC_CUDA(cudaStreamSynchronize(c->stream));
+  return MOC_OK;
+}
+
+int moc_get_fluxes(moc_ctx* c, float* out, int64_t n) {
+  MOC_CHECK(c, MOC_ERR_ARG, "null context");
+  return copy_out(c, c->phi, out, n, num_flux(c));
+}
+
+int moc_set_fluxes(moc_ctx* c, const float* in, int64_t n) {
+  MOC_CHECK(c, MOC_ERR_ARG, "null context");
+  MOC_TRY(copy_in(c, c->phi, in, n, num_flux(c)));
+  return copy_in(c, c->phi_old, in, n, num_flux(c));
+}
+
+int moc_get_old_fluxes(moc_ctx* c, float* out, int64_t n) {
+  MOC_CHECK(c, MOC_ERR_ARG, "null context");
+  return copy_out(c, c->phi_old, out, n, num_flux(c));
+}
+
+int moc_set_old_fluxes(moc_ctx* c, const float* in, int64_t n) {
+  MOC_CHECK(c, MOC_ERR_ARG, "null context");
+  return copy_in(c, c->phi_old, in, n, num_flux(c));
+}
+
+int moc_get_reduced_sources(moc_ctx* c, float* out, int64_t n) {
+  MOC_CHECK(c, MOC_ERR_ARG, "null context");
+  MOC_TRY(copy_out(c, c->qt, out, n, num_flux(c)));
+  // the device keeps Q / (4 pi sigma_t); report Q / (4 pi)
+  std::vector<float> st((size_t) c->d.num_materials * c->d.num_groups);
+  std::vector<int32_t> mat(c->d.num_fsrs);
+  MOC_CUDA(cudaMemcpy(st.data(), c->sigma_t, 4 * st.size(),
+                      cudaMemcpyDeviceToHost));
+  MOC_CUDA(cudaMemcpy(mat.data(), c->fsr_mat, 4 * mat.size(),
+                      cudaMemcpyDeviceToHost));
+  const int G = c->d.num_groups;
+  for (int64_t r = 0; r < c->d.num_fsrs; r++)
+    for (int g = 0; g < G; g++)
+      out[r * G + g] *= st[(int64_t) mat[r] * G + g];
+  return MOC_OK;
+}
+
+int moc_get_start_flux(moc_ctx* c, float* out, int64_t n) {
+  MOC_CHECK(c, MOC_ERR_ARG, "null context");
+  MOC_TRY(pull(c));
+  const int cur = c->hsc->cur;
+  const float scale = c->hsc->scale[cur];
+  MOC_TRY(copy_out(c, c->psi[cur], out, n, num_psi(c)));
+  if (scale != 1.0f)
+    for (int64_t i = 0; i < n; i++) out[i] *= scale;
+  return MOC_OK;
+}
+
+int moc_set_start_flux(moc_ctx* c, const float* in, int64_t n) {
+  MOC_CHECK(c, MOC_ERR_ARG, "null context");
+  MOC_TRY(copy_in(c, c->psi[0], in, n, num_psi(c)));
+  MOC_TRY(copy_in(c, c->psi[1], in, n, num_psi(c)));
+  MOC_TRY(pull(c));
+  c->hsc->scale[0] = c->hsc->scale[1] = 1.0f;
+  return push(c);
+}
+
+int moc_get_sweep_time(moc_ctx* c, double* ms, int64_t* num_sweeps) {
+  MOC_CHECK(c && ms && num_sweeps, MOC_ERR_ARG, "null argument");
+  *ms = c->sweep_ms;
+  *num_sweeps = c->num_sweeps;
+  return MOC_OK;
+}
+
+int moc_get_launch_count(moc_ctx* c, int64_t* launches) {
+  MOC_CHECK(c && launches, MOC_ERR_ARG, "null argument");
+  *launches = c->launches;
+  return MOC_OK;
+}
+
+// ----------------------------------------------------------------- hooks
+int moc_zero_track_fluxes(moc_ctx* c) {
+  MOC_TRY(ready(c));
+  return zero_track_fluxes(c);
+}
+
+int moc_flatten_fsr_fluxes(moc_ctx* c, float value) {
+  MOC_TRY(ready(c));
+  moc::launch_fill(c->phi, num_flux(c), value, c->stream);
+  c->launches++;
+  MOC_CUDA(cudaGetLastError());
+  return MOC_OK;
+}
+
+int moc_flatten_fsr_fluxes_chi(moc_ctx* c, int material) {
+  MOC_TRY(ready(c));
+  MOC_CHECK(material >= 0 && material < c->d.num_materials, MOC_ERR_ARG,
+            "chi spectrum material out of range");
+  float* d_chi = c->chi + (int64_t) material * c->d.num_groups;
+  moc::launch_fill_chi(c->phi, d_chi, c->d.num_fsrs, c->d.num_groups,
+                       c->stream);
+  c->launches++;
+  MOC_CUDA(cudaGetLastError());
+  return MOC_OK;
+}
+
+int moc_store_fsr_fluxes(moc_ctx* c) {
+  MOC_TRY(ready(c));
+  MOC_CUDA(cudaMemcpyAsync(c->phi_old, c->phi, 4 * num_flux(c),
+                           cudaMemcpyDeviceToDevice, c->stream));
+  return MOC_OK;
+}
+
+int moc_normalize_fluxes(moc_ctx* c, double* factor) {
+  MOC_TRY(ready(c));
+  moc::SolverArgs a = solver_args(c, 0);
+  moc::launch_fission_rate(a, 1, c->stream);
+  moc::launch_scale_phi(a, c->stream);
+  c->launches += 2;
+  MOC_CUDA(cudaGetLastError());
+  MOC_TRY(pull(c));
+  if (factor) *factor = c->hsc->factor;
+  return MOC_OK;
+}
+
+int moc_compute_fsr_sources(moc_ctx* c, int iteration) {
+  MOC_TRY(ready(c));
+  MOC_CHECK(iteration >= 0, MOC_ERR_ARG, "iteration must be non-negative");
+  moc::SolverArgs a = solver_args(c, 0);
+  moc::launch_compute_sources(a, iteration, 0, c->stream);
+  c->launches++;
+  MOC_CUDA(cudaGetLastError());
+  return MOC_OK;
+}
+
+int moc_transport_sweep(moc_ctx* c) {
+  MOC_TRY(ready(c));
+  MOC_CUDA(cudaMemsetAsync(c->phi, 0, 4 * num_flux(c), c->stream));
+  MOC_TRY(enqueue_sweep(c, 0, true, 0));
+  MOC_CUDA(cudaStreamSynchronize(c->stream));
+  MOC_TRY(collect_sweep_times(c, 1));
+  c->num_sweeps++;
+  return MOC_OK;
+}
+
+int moc_add_source_to_scalar_flux(moc_ctx* c) {
+  MOC_TRY(ready(c));
+  moc::SolverArgs a = solver_args(c, 0);
+  moc::launch_add_source(a, 0, c->stream);
+  c->launches++;
+  MOC_CUDA(cudaGetLastError());
+  return MOC_OK;
+}
+
+int moc_compute_keff(moc_ctx* c) {
+  MOC_TRY(ready(c));
+  moc::SolverArgs a = solver_args(c, 0);
+  moc::launch_fission_rate(a, 0, c->stream);
+  c->launches++;
+  MOC_CUDA(cudaGetLastError());
+  MOC_TRY(pull(c));
+  c->keff = c->hsc->keff;
+  return MOC_OK;
+}
+
+int moc_compute_residual(moc_ctx* c, int res_type, double* residual) {
+  MOC_TRY(ready(c));
+  MOC_CHECK(res_type >= 0 && res_type <= 2, MOC_ERR_ARG, "bad residual type");
+  moc::SolverArgs a = solver_args(c, 0);
+  moc::launch_residual(a, res_type, 0, 0, 0, c->stream);
+  c->launches++;
+  MOC_CUDA(cudaGetLastError());
+  MOC_TRY(pull(c));
+  if (residual) *residual = c->hsc->residual;
+  return MOC_OK;
+}
+
+int moc_set_keff(moc_ctx* c, double keff) {
+  MOC_CHECK(c, MOC_ERR_ARG, "null context");
+  MOC_CHECK(keff > 0.0 && std::isfinite(keff), MOC_ERR_ARG,
+            "keff must be positive");
+  MOC_TRY(pull(c));
+  c->hsc->keff = keff;
+  c->hsc->k_prev = keff;
+  c->keff = keff;
+  return push(c);
+}
+
+int moc_compute_fsr_fission_rates(moc_ctx* c, double* rates, int64_t n,
+                                  int nu) {
+  MOC_TRY(ready(c));
+  MOC_CHECK(rates && n == c->d.num_fsrs, MOC_ERR_ARG,
+            "rates must hold num_fsrs values");
+  MOC_CHECK(nu || c->sigma_f, MOC_ERR_STATE,
+            "fission (not nu-fission) rates need moc_upload_sigma_f");
+  moc::SolverArgs a = solver_args(c, 0);
+  moc::launch_fsr_rates(a, c->rates, nu, c->stream);
+  c->launches++;
+  MOC_CUDA(cudaGetLastError());
+  MOC_CUDA(cudaMemcpyAsync(rates, c->rates, 8 * n, cudaMemcpyDeviceToHost,
+                           c->stream));
+  MOC_CUDA(cudaStreamSynchronize(c->stream));
+  return MOC_OK;
+}
+
+}  // extern "C"

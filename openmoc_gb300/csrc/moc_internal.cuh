@@ -1,0 +1,128 @@
+// Internal declarations shared by the CUDA translation units of
+// libopenmoc_gb300.so.  Not part of the public ABI (include/openmoc_gb300.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace moc {
+
+// Exponential table for the attenuation factor g(x) = 1 - exp(-x): nodes at
+// x_i = i / kExpTableInvH, i < kExpTableSize.  Beyond the last node g = 1 in
+// float (exp(-20) = 2.1e-9).
+constexpr int kExpTableSize = 321;
+constexpr float kExpTableInvH = 16.0f;
+constexpr float kExpTableH = 1.0f / 16.0f;
+
+// Largest number of groups handled per lane and largest polar count.
+constexpr int kMaxSlots = 9;
+constexpr int kMaxPolarHalf = 5;
+constexpr int kSweepThreads = 128;
+
+enum ExpKind { kExpTable = 0, kExpIntrinsic = 1 };
+
+// Device-resident solver scalars: the iteration state machine that lets a
+// whole block of iterations run without host round trips.
+struct DevScalars {
+  double keff;            // current eigenvalue estimate
+  double k_prev;          // eigenvalue of the previous iteration
+  double factor;          // last normalisation factor
+  double residual;        // last residual
+  double accum_rate;      // fission-rate accumulator (reset by the last block)
+  double accum_res;       // residual accumulator (reset by the last block)
+  double threshold;       // convergence threshold
+  float scale[2];         // pending multiplier of each angular-flux buffer
+  unsigned int ticket_rate;
+  unsigned int ticket_res;
+  unsigned int ticket_sweep;
+  int cur;                // angular-flux buffer the next sweep reads
+  int iteration;          // iterations completed in this solve
+  int max_iters;
+  int done;               // 1: converged or out of iterations
+  int converged;
+  int dk;                 // 1e5 * (k - k_prev), truncated
+  int mode;               // SolveMode
+  int res_type;
+  unsigned long long neg_sources;
+  unsigned long long neg_fluxes;
+  long long num_fissionable;
+};
+
+enum SolveMode { kModeEigen = 0, kModeSource = 1, kModeFlux = 2, kModeHook = 3 };
+
+struct SweepArgs {
+  const int2* segs;          // [S] {float length bits, fsr}
+  const int64_t* seg_off;    // [T+1]
+  const int32_t* order;      // [T] tracks by decreasing segment count
+  const int32_t* track_ang;  // [T]
+  const int32_t* next;       // [2T]
+  const uint8_t* flags;      // [T]
+  const float* weights;      // [A][Ph]
+  const float* inv_sin;      // [A][Ph]
+  const float* sigma_t;      // [M][G]
+  const int32_t* fsr_mat;    // [R]
+  const float* qt;           // [R][G] reduced source / sigma_t
+  const float* exp_table;    // [kExpTableSize]
+  float* phi;                // [R][G] accumulated tallies
+  float* psi[2];             // [T][2][F] angular-flux buffers
+  DevScalars* sc;
+  int64_t num_tracks;
+  int num_groups;
+  int num_materials;
+  int lps;                   // lanes per track direction (1..32, power of 2)
+  int check_done;            // return at once if sc->done is set
+};
+
+struct SolverArgs {
+  const float* sigma_t;      // [M][G]
+  const float* sigma_s;      // [M][G][G] dest-major
+  const float* nu_sigma_f;   // [M][G]
+  const float* chi;          // [M][G]
+  const uint8_t* fissile;    // [M]
+  const int32_t* fsr_mat;    // [R]
+  const float* fsr_vol;      // [R]
+  const float* fixed;        // [R][G] or null
+  const float* scat_out;     // [M][G] total scattering out of each group
+  const float* sigma_f;      // [M][G] or null
+  float* phi;                // [R][G]
+  float* phi_old;            // [R][G]
+  float* qt;                 // [R][G]
+  float* psi[2];
+  DevScalars* sc;
+  int64_t num_fsrs;
+  int64_t num_psi;           // 2*T*F
+  int num_groups;
+  int num_materials;
+  int check_done;
+};
+
+// ---- launchers (sweep.cu) ------------------------------------------------
+// Chooses the kernel instance for (Ph, slots, exp kind).  Returns false if
+// no instance exists.
+bool launch_sweep(const SweepArgs& a, int polar_half, int slots, int exp_kind,
+                  cudaStream_t stream);
+int sweep_max_slots(int polar_half);
+
+// ---- launchers (solver_kernels.cu) ---------------------------------------
+// iteration < 0 reads the device iteration counter; fused also zeroes phi
+// after reading it (the tallies of the sweep that follows)
+void launch_compute_sources(const SolverArgs& a, int iteration, int fused,
+                            cudaStream_t s);
+// add-source + fission-rate reduction; update: 0 none, 1 eigen update of
+// keff / factor / buffer scale
+void launch_add_source(const SolverArgs& a, int update, cudaStream_t s);
+// normalise by sc->factor (if normalise), residual of res_type vs phi_old,
+// store phi into phi_old (if store), finish the iteration (if finish)
+void launch_residual(const SolverArgs& a, int res_type, int normalise,
+                     int store, int finish, cudaStream_t s);
+// fission-rate reduction of phi; what: 0 keff update, 1 normalise hook
+void launch_fission_rate(const SolverArgs& a, int what, cudaStream_t s);
+void launch_scale_phi(const SolverArgs& a, cudaStream_t s);
+void launch_zero_phi(const SolverArgs& a, cudaStream_t s);
+void launch_fill(float* p, int64_t n, float v, cudaStream_t s);
+void launch_fill_chi(float* phi, const float* chi, int64_t R, int G,
+                     cudaStream_t s);
+void launch_fsr_rates(const SolverArgs& a, double* out, int nu,
+                      cudaStream_t s);
+
+}  // namespace moc

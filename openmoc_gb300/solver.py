@@ -1,0 +1,393 @@
+"""Host-side mirror of OpenMOC's ``Solver`` interface over the GB300 C ABI.
+
+:class:`GB300Solver` exposes the names, argument meanings and error
+behaviour of ``openmoc.Solver`` (``src/Solver.h:433-585``): construct it,
+give it tracks with :meth:`setTrackGenerator`, then call
+:meth:`computeEigenvalue`, :meth:`computeSource` or :meth:`computeFlux`
+and read :meth:`getKeff`, :meth:`getFlux`, :meth:`getNumIterations`.
+Errors raise ``RuntimeError`` (:class:`openmoc_gb300._native.MOCError`), as
+OpenMOC's SWIG layer turns ``log_printf(ERROR, ...)`` into RuntimeError
+(``openmoc/swig/openmoc.i:106``).
+
+"Track generator" here is a :class:`openmoc_gb300.problem.Problem`: the
+packed tracks, segments, quadrature and cross sections that OpenMOC's
+``TrackGenerator`` / ``Geometry`` hold (packed from OpenMOC objects by
+``openmoc_gb300/adapter/pack_reference.h``, or produced by
+:mod:`openmoc_gb300.lattice`).
+
+Every solve runs on the GPU; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+from typing import Optional
+
+import numpy as np
+
+from . import _native
+from .problem import Problem
+
+# residualType values of src/Solver.h:82-92
+SCALAR_FLUX = 0
+FISSION_SOURCE = 1
+TOTAL_SOURCE = 2
+
+EXP_TABLE = 0
+EXP_INTRINSIC = 1
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+class GB300Solver:
+    """GB300 method-of-characteristics solver with OpenMOC's Solver API."""
+
+    def __init__(self, track_generator: Optional[Problem] = None, device: int = 0):
+        self._lib = _native.lib()
+        self._ctx = None
+        self._device = device
+        self._problem: Optional[Problem] = None
+        self._threshold = 1e-5
+        self._exp_kind = EXP_TABLE
+        self._fixed: dict = {}
+        self._fixed_by_material: dict = {}
+        self._num_iterations = 0
+        self._total_time = 0.0
+        self._keff = 1.0
+        self._shape = None
+        if track_generator is not None:
+            self.setTrackGenerator(track_generator)
+
+    # ------------------------------------------------------------ lifetime
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def close(self) -> None:
+        if self._ctx is not None:
+            self._lib.moc_destroy(self._ctx)
+            self._ctx = None
+
+    def _call(self, name: str, *args):
+        _native.check(getattr(self._lib, name)(self._ctx, *args))
+
+    def _need_ctx(self):
+        if self._ctx is None:
+            raise RuntimeError("The Solver is unable to compute since it does "
+                               "not contain a TrackGenerator")
+
+    # ---------------------------------------------------------- set up
+    def setTrackGenerator(self, track_generator: Problem) -> None:
+        """Uploads the packed tracks, quadrature, materials and FSRs
+        (Solver::setTrackGenerator, src/Solver.cpp:412-454)."""
+        p = track_generator
+        if not isinstance(p, Problem):
+            p = getattr(track_generator, "problem", None)
+            if not isinstance(p, Problem):
+                raise RuntimeError("setTrackGenerator needs a packed Problem")
+        p = p.contiguous()
+        try:
+            p.validate()
+        except ValueError as e:
+            raise _native.MOCError(-1, str(e)) from None
+        self.close()
+        dims = _native.Dims(p.num_groups, p.num_polar_half, p.num_angles,
+                            p.num_materials, p.num_fsrs, p.num_tracks,
+                            p.num_segments, p.solve_3d, self._device)
+        ctx = C.c_void_p()
+        _native.check(self._lib.moc_create(C.byref(dims), C.byref(ctx)))
+        self._ctx = ctx
+        self._problem = p
+        self._call("moc_upload_tracks", _ptr(p.seg_len), _ptr(p.seg_fsr),
+                   _ptr(p.seg_off), _ptr(p.track_ang), _ptr(p.next),
+                   _ptr(p.flags))
+        self._call("moc_upload_quadrature", _ptr(p.weights), _ptr(p.inv_sin))
+        self._call("moc_upload_materials", _ptr(p.sigma_t), _ptr(p.sigma_s),
+                   _ptr(p.nu_sigma_f), _ptr(p.chi))
+        self._call("moc_upload_fsrs", _ptr(p.fsr_mat), _ptr(p.fsr_vol))
+        self._call("moc_set_convergence_threshold", self._threshold)
+        self._call("moc_set_exponential", self._exp_kind)
+        if self._shape is not None:
+            self._call("moc_set_sweep_shape", *self._shape)
+        self._fixed = {}
+        self._fixed_by_material = {}
+        if p.fixed_sources is not None:
+            self._upload_fixed(np.asarray(p.fixed_sources, np.float32))
+
+    def getTrackGenerator(self) -> Optional[Problem]:
+        return self._problem
+
+    def setConvergenceThreshold(self, threshold: float) -> None:
+        """Solver::setConvergenceThreshold (src/Solver.cpp:461)."""
+        if threshold <= 0:
+            raise _native.MOCError(-1, "Unable to set the convergence threshold "
+                                       f"to {threshold} since it is not positive")
+        self._threshold = float(threshold)
+        if self._ctx is not None:
+            self._call("moc_set_convergence_threshold", self._threshold)
+
+    def getConvergenceThreshold(self) -> float:
+        return self._threshold
+
+    def useExponentialInterpolation(self) -> None:
+        """Shared-memory table evaluation of 1 - exp(-x) (the default)."""
+        self._exp_kind = EXP_TABLE
+        if self._ctx is not None:
+            self._call("moc_set_exponential", EXP_TABLE)
+
+    def useExponentialIntrinsic(self) -> None:
+        """Hardware ex2 evaluation of 1 - exp(-x)."""
+        self._exp_kind = EXP_INTRINSIC
+        if self._ctx is not None:
+            self._call("moc_set_exponential", EXP_INTRINSIC)
+
+    def setSweepShape(self, lanes_per_track_direction: int, groups_per_lane: int) -> None:
+        self._shape = (int(lanes_per_track_direction), int(groups_per_lane))
+        if self._ctx is not None:
+            self._call("moc_set_sweep_shape", *self._shape)
+
+    def getSweepShape(self):
+        self._need_ctx()
+        a, b = C.c_int(), C.c_int()
+        self._call("moc_get_sweep_shape", C.byref(a), C.byref(b))
+        return a.value, b.value
+
+    def setIterationsPerSync(self, k: int) -> None:
+        self._need_ctx()
+        self._call("moc_set_iterations_per_sync", int(k))
+
+    # ------------------------------------------------------- fixed sources
+    def setFixedSourceByFSR(self, fsr_id: int, group: int, source: float) -> None:
+        """Solver::setFixedSourceByFSR (src/Solver.cpp:479); group is
+        1-based."""
+        p = self._problem
+        if p is None:
+            raise RuntimeError("set a TrackGenerator before fixed sources")
+        if group <= 0 or group > p.num_groups:
+            raise _native.MOCError(-1, f"Unable to use fixed source for group {group} "
+                                       f"in a {p.num_groups} energy group problem")
+        if fsr_id < 0 or fsr_id >= p.num_fsrs:
+            raise _native.MOCError(-1, f"Unable to use fixed source for FSR {fsr_id} "
+                                       f"with only {p.num_fsrs} FSRs in the geometry")
+        self._fixed[(int(fsr_id), int(group))] = float(source)
+        self._push_fixed()
+
+    def setFixedSourceByMaterial(self, material: int, group: int, source: float) -> None:
+        """Solver::setFixedSourceByMaterial: every FSR of the material
+        (material given by its index in the packed problem)."""
+        p = self._problem
+        if p is None:
+            raise RuntimeError("set a TrackGenerator before fixed sources")
+        if material < 0 or material >= p.num_materials:
+            raise _native.MOCError(-1, f"no material {material}")
+        if group <= 0 or group > p.num_groups:
+            raise _native.MOCError(-1, f"Unable to use fixed source for group {group} "
+                                       f"in a {p.num_groups} energy group problem")
+        self._fixed_by_material[(int(material), int(group))] = float(source)
+        self._push_fixed()
+
+    def resetFixedSources(self) -> None:
+        self._fixed = {}
+        self._fixed_by_material = {}
+        if self._ctx is not None:
+            self._call("moc_set_fixed_sources", None)
+
+    def _push_fixed(self) -> None:
+        p = self._problem
+        q = np.zeros((p.num_fsrs, p.num_groups), np.float32)
+        for (m, g), v in self._fixed_by_material.items():
+            q[p.fsr_mat == m, g - 1] = v
+        for (r, g), v in self._fixed.items():
+            q[r, g - 1] = v
+        self._upload_fixed(q)
+
+    def _upload_fixed(self, q: np.ndarray) -> None:
+        q = np.ascontiguousarray(q, np.float32).ravel()
+        self._fixed_array = q
+        self._call("moc_set_fixed_sources", _ptr(q))
+
+    # ------------------------------------------------------------- solves
+    def computeEigenvalue(self, max_iters: int = 1000,
+                          res_type: int = FISSION_SOURCE) -> None:
+        """Solver::computeEigenvalue (src/Solver.cpp:1542-1700), run
+        device-resident."""
+        self._need_ctx()
+        t0 = time.perf_counter()
+        self._call("moc_compute_eigenvalue", int(max_iters), int(res_type))
+        self._total_time = time.perf_counter() - t0
+        self._after_solve()
+
+    def computeSource(self, max_iters: int = 1000, k_eff: float = 1.0,
+                      res_type: int = TOTAL_SOURCE) -> None:
+        """Solver::computeSource (src/Solver.cpp:1459-1535)."""
+        self._need_ctx()
+        if k_eff <= 0:
+            raise _native.MOCError(-1, f"The Solver is unable to compute the source with "
+                                       f"keff = {k_eff} since it is not a positive value")
+        t0 = time.perf_counter()
+        self._call("moc_compute_source", int(max_iters), float(k_eff), int(res_type))
+        self._total_time = time.perf_counter() - t0
+        self._after_solve()
+
+    def computeFlux(self, max_iters: int = 1000, only_fixed_source: bool = True) -> None:
+        """Solver::computeFlux (src/Solver.cpp:1352-1456)."""
+        self._need_ctx()
+        t0 = time.perf_counter()
+        self._call("moc_compute_flux", int(max_iters), int(bool(only_fixed_source)))
+        self._total_time = time.perf_counter() - t0
+        self._after_solve()
+
+    def _after_solve(self) -> None:
+        n = C.c_int()
+        self._call("moc_get_num_iterations", C.byref(n))
+        self._num_iterations = n.value
+        k = C.c_double()
+        self._call("moc_get_keff", C.byref(k))
+        self._keff = k.value
+
+    # ------------------------------------------------------------ results
+    def getKeff(self) -> float:
+        if self._ctx is not None:
+            k = C.c_double()
+            self._call("moc_get_keff", C.byref(k))
+            self._keff = k.value
+        return self._keff
+
+    def getNumIterations(self) -> int:
+        return self._num_iterations
+
+    def getTotalTime(self) -> float:
+        return self._total_time
+
+    def getResidual(self) -> float:
+        self._need_ctx()
+        r = C.c_double()
+        self._call("moc_get_residual", C.byref(r))
+        return r.value
+
+    def getSweepTime(self):
+        """(milliseconds of transport sweeps, number of sweeps) of the last
+        solve: the Timer split "Transport Sweep"."""
+        self._need_ctx()
+        ms, n = C.c_double(), C.c_int64()
+        self._call("moc_get_sweep_time", C.byref(ms), C.byref(n))
+        return ms.value, n.value
+
+    def getLaunchCount(self) -> int:
+        self._need_ctx()
+        n = C.c_int64()
+        self._call("moc_get_launch_count", C.byref(n))
+        return n.value
+
+    def getFluxes(self) -> np.ndarray:
+        """All scalar fluxes as an [R, G] array (Solver::getFluxes)."""
+        self._need_ctx()
+        p = self._problem
+        out = np.empty(p.num_fsrs * p.num_groups, np.float32)
+        self._call("moc_get_fluxes", _ptr(out), out.size)
+        return out.reshape(p.num_fsrs, p.num_groups)
+
+    def getFlux(self, fsr_id: int, group: int) -> float:
+        """Solver::getFlux (src/Solver.cpp:298-321); group is 1-based."""
+        self._need_ctx()
+        p = self._problem
+        if fsr_id >= p.num_fsrs:
+            raise _native.MOCError(-1, f"Unable to return a scalar flux for FSR ID = "
+                                       f"{fsr_id} since the max FSR ID = {p.num_fsrs - 1}")
+        if fsr_id < 0:
+            raise _native.MOCError(-1, f"Unable to return a scalar flux for FSR ID = "
+                                       f"{fsr_id} since FSRs do not have negative IDs")
+        if group - 1 >= p.num_groups:
+            raise _native.MOCError(-1, f"Unable to return a scalar flux in group {group} "
+                                       f"since there are only {p.num_groups} groups")
+        if group <= 0:
+            raise _native.MOCError(-1, f"Unable to return a scalar flux in group {group} "
+                                       f"since groups must be greater or equal to 1")
+        return float(self.getFluxes()[fsr_id, group - 1])
+
+    def setFluxes(self, fluxes) -> None:
+        """Solver::setFluxes: [R, G] (or flat) scalar fluxes."""
+        self._need_ctx()
+        a = np.ascontiguousarray(fluxes, np.float32).ravel()
+        self._call("moc_set_fluxes", _ptr(a), a.size)
+
+    def computeFSRFissionRates(self, num_FSRs: int, nu: bool = False) -> np.ndarray:
+        """Solver::computeFSRFissionRates (src/Solver.h:539-540)."""
+        self._need_ctx()
+        p = self._problem
+        if num_FSRs != p.num_fsrs:
+            raise _native.MOCError(-1, f"{num_FSRs} FSRs requested, the problem has "
+                                       f"{p.num_fsrs}")
+        out = np.empty(p.num_fsrs, np.float64)
+        self._call("moc_compute_fsr_fission_rates", _ptr(out), out.size, int(bool(nu)))
+        return out
+
+    # ------------------------------------------------- per-hook interface
+    # The protected hooks of src/Solver.h:334-431, exposed one call each so
+    # that a caller can drive (or test) one step of source iteration.
+    def zeroTrackFluxes(self):
+        self._call("moc_zero_track_fluxes")
+
+    def flattenFSRFluxes(self, value: float):
+        self._call("moc_flatten_fsr_fluxes", float(value))
+
+    def flattenFSRFluxesChiSpectrum(self, material: int):
+        self._call("moc_flatten_fsr_fluxes_chi", int(material))
+
+    def storeFSRFluxes(self):
+        self._call("moc_store_fsr_fluxes")
+
+    def normalizeFluxes(self) -> float:
+        f = C.c_double()
+        self._call("moc_normalize_fluxes", C.byref(f))
+        return f.value
+
+    def computeFSRSources(self, iteration: int):
+        self._call("moc_compute_fsr_sources", int(iteration))
+
+    def transportSweep(self):
+        self._call("moc_transport_sweep")
+
+    def addSourceToScalarFlux(self):
+        self._call("moc_add_source_to_scalar_flux")
+
+    def computeKeff(self):
+        self._call("moc_compute_keff")
+
+    def computeResidual(self, res_type: int) -> float:
+        r = C.c_double()
+        self._call("moc_compute_residual", int(res_type), C.byref(r))
+        return r.value
+
+    def setKeff(self, keff: float):
+        self._call("moc_set_keff", float(keff))
+
+    def getReducedSources(self) -> np.ndarray:
+        p = self._problem
+        out = np.empty(p.num_fsrs * p.num_groups, np.float32)
+        self._call("moc_get_reduced_sources", _ptr(out), out.size)
+        return out.reshape(p.num_fsrs, p.num_groups)
+
+    def getOldFluxes(self) -> np.ndarray:
+        p = self._problem
+        out = np.empty(p.num_fsrs * p.num_groups, np.float32)
+        self._call("moc_get_old_fluxes", _ptr(out), out.size)
+        return out.reshape(p.num_fsrs, p.num_groups)
+
+    def setOldFluxes(self, fluxes) -> None:
+        a = np.ascontiguousarray(fluxes, np.float32).ravel()
+        self._call("moc_set_old_fluxes", _ptr(a), a.size)
+
+    def getStartFlux(self) -> np.ndarray:
+        p = self._problem
+        out = np.empty(2 * p.num_tracks * p.fluxes_per_track, np.float32)
+        self._call("moc_get_start_flux", _ptr(out), out.size)
+        return out
+
+    def setStartFlux(self, psi) -> None:
+        a = np.ascontiguousarray(psi, np.float32).ravel()
+        self._call("moc_set_start_flux", _ptr(a), a.size)

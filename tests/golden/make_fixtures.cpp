@@ -1,0 +1,462 @@
+/*
+ * Generates the golden fixtures under tests/golden/ by running OpenMOC's own
+ * C++ library (compiled from the reference sources by oracle/ref.mk) on small
+ * problems.  Built twice, against the FP_PRECISION=float and =double builds,
+ * by tests/golden/make_fixtures.sh.
+ *
+ * For every case it writes <case>_<prec>.bin + <case>_<prec>.json:
+ *   - the packed tracks / quadrature / cross sections exactly as the GB300
+ *     adapter hands them to the C ABI (openmoc_gb300/adapter/pack_reference.h);
+ *   - the converged solve (iterations, keff, FSR scalar fluxes);
+ *   - (float build) a hook-by-hook probe from the converged state: the
+ *     reduced sources of computeFSRSources, the raw sweep tallies and the
+ *     outgoing boundary fluxes of one transportSweep, the flux after
+ *     addSourceToScalarFlux, keff after computeKeff, the normalisation factor
+ *     and the residual (src/CPUSolver.cpp:1860-2660).
+ * Track generation runs on one thread so FSR numbering is reproducible, as
+ * the reference test harness does (tests/testing_harness.py).
+ */
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "CPUSolver.h"
+#include "Geometry.h"
+#include "TrackGenerator.h"
+#include "log.h"
+
+#include "../../openmoc_gb300/adapter/pack_reference.h"
+#include "../../openmoc_gb300/csrc/synthetic_xs.h"
+
+using openmoc_gb300::MaterialXS;
+using openmoc_gb300::PackedProblem;
+
+#ifdef SINGLE
+static const char* PREC = "f32";
+#else
+static const char* PREC = "f64";
+#endif
+
+/* ------------------------------------------------------------------ output */
+struct Writer {
+  std::string bin_path, json_path;
+  std::ofstream bin;
+  std::stringstream arrays, scalars;
+  long offset = 0;
+  bool first_arr = true, first_sc = true;
+
+  Writer(const std::string& base) {
+    bin_path = base + ".bin";
+    json_path = base + ".json";
+    bin.open(bin_path.c_str(), std::ios::binary);
+  }
+  template <typename T>
+  void arr(const char* name, const char* dtype, const T* data, long n,
+           long rows = -1) {
+    while (offset % 16) { char z = 0; bin.write(&z, 1); offset++; }
+    bin.write((const char*) data, n * sizeof(T));
+    if (!first_arr) arrays << ",\n";
+    first_arr = false;
+    arrays << "    \"" << name << "\": {\"dtype\": \"" << dtype
+           << "\", \"offset\": " << offset << ", \"count\": " << n;
+    if (rows > 0) arrays << ", \"rows\": " << rows;
+    arrays << "}";
+    offset += n * sizeof(T);
+  }
+  void sc(const char* name, double v) {
+    if (!first_sc) scalars << ",\n";
+    first_sc = false;
+    char buf[64];
+    snprintf(buf, sizeof(buf), "%.17g", v);
+    scalars << "    \"" << name << "\": " << buf;
+  }
+  void close() {
+    bin.close();
+    std::ofstream js(json_path.c_str());
+    js << "{\n  \"precision\": \"" << PREC << "\",\n  \"arrays\": {\n"
+       << arrays.str() << "\n  },\n  \"scalars\": {\n" << scalars.str()
+       << "\n  }\n}\n";
+  }
+};
+
+static void write_problem(Writer& w, const PackedProblem& p) {
+  w.sc("num_groups", p.num_groups);
+  w.sc("num_polar_half", p.num_polar_half);
+  w.sc("num_angles", p.num_angles);
+  w.sc("num_materials", p.num_materials);
+  w.sc("solve_3d", p.solve_3d);
+  w.sc("num_fsrs", p.num_fsrs);
+  w.sc("num_tracks", p.num_tracks);
+  w.sc("num_segments", p.num_segments);
+  w.arr("seg_len", "f4", p.seg_len.data(), p.seg_len.size());
+  w.arr("seg_fsr", "i4", p.seg_fsr.data(), p.seg_fsr.size());
+  w.arr("seg_off", "i8", p.seg_off.data(), p.seg_off.size());
+  w.arr("track_ang", "i4", p.track_ang.data(), p.track_ang.size());
+  w.arr("next", "i8", p.next.data(), p.next.size());
+  w.arr("flags", "u1", p.flags.data(), p.flags.size());
+  w.arr("weights", "f4", p.weights.data(), p.weights.size());
+  w.arr("inv_sin", "f4", p.inv_sin.data(), p.inv_sin.size());
+  w.arr("sigma_t", "f4", p.sigma_t.data(), p.sigma_t.size());
+  w.arr("sigma_s", "f4", p.sigma_s.data(), p.sigma_s.size());
+  w.arr("nu_sigma_f", "f4", p.nu_sigma_f.data(), p.nu_sigma_f.size());
+  w.arr("chi", "f4", p.chi.data(), p.chi.size());
+  w.arr("fsr_mat", "i4", p.fsr_mat.data(), p.fsr_mat.size());
+  w.arr("fsr_vol", "f4", p.fsr_vol.data(), p.fsr_vol.size());
+}
+
+/* ---------------------------------------------- solver with hook access */
+class ProbeSolver : public CPUSolver {
+ public:
+  explicit ProbeSolver(TrackGenerator* tg) : CPUSolver(tg) {}
+
+  template <typename T>
+  static std::vector<float> tof(const T* a, long n) {
+    std::vector<float> v(n);
+    for (long i = 0; i < n; i++) v[i] = (float) a[i];
+    return v;
+  }
+  long nflux() const { return _num_FSRs * _num_groups; }
+  long nbound() const { return 2 * _tot_num_tracks * _fluxes_per_track; }
+
+  /* One pass of every hook from the converged state. */
+  void probe(Writer& w) {
+    w.sc("probe_keff_in", _k_eff);
+    std::vector<float> v = tof(_scalar_flux, nflux());
+    w.arr("probe_phi_in", "f4", v.data(), v.size());
+    std::vector<float> so = tof(_old_scalar_flux, nflux());
+    w.arr("probe_phi_old", "f4", so.data(), so.size());
+    computeFSRSources(100);
+    v = tof(_reduced_sources, nflux());
+    w.arr("probe_reduced_sources", "f4", v.data(), v.size());
+    w.arr("probe_start_flux_in", "f4", _start_flux, nbound());
+    transportSweep();
+    v = tof(_scalar_flux, nflux());
+    w.arr("probe_phi_sweep", "f4", v.data(), v.size());
+    w.arr("probe_start_flux_out", "f4", _start_flux, nbound());
+    addSourceToScalarFlux();
+    v = tof(_scalar_flux, nflux());
+    w.arr("probe_phi_addsrc", "f4", v.data(), v.size());
+    computeKeff();
+    w.sc("probe_keff_out", _k_eff);
+    double f = normalizeFluxes();
+    w.sc("probe_norm_factor", f);
+    v = tof(_scalar_flux, nflux());
+    w.arr("probe_phi_norm", "f4", v.data(), v.size());
+    w.sc("probe_residual_fission", computeResidual(FISSION_SOURCE));
+    w.sc("probe_residual_flux", computeResidual(SCALAR_FLUX));
+    w.sc("probe_residual_total", computeResidual(TOTAL_SOURCE));
+  }
+};
+
+/* ---------------------------------------------------------- model pieces */
+static Material* make_material(int id, const char* name, const MaterialXS& x) {
+  Material* m = new Material(id, name);
+  const int G = x.num_groups;
+  m->setNumEnergyGroups(G);
+  std::vector<double> t = x.sigma_t, s = x.sigma_s, nf = x.nu_sigma_f,
+                      f = x.sigma_f, c = x.chi;
+  m->setSigmaT(t.data(), G);
+  m->setSigmaS(s.data(), G * G);
+  m->setSigmaF(f.data(), G);
+  m->setNuSigmaF(nf.data(), G);
+  m->setChi(c.data(), G);
+  return m;
+}
+
+/* C5G7 UO2 and water 7-group data as listed in the reference's pin-cell
+ * driver (profile/models/pin-cell/pin-cell-3d.cpp:36-95); the published
+ * C5G7 benchmark data. */
+static MaterialXS c5g7(bool uo2) {
+  MaterialXS x;
+  x.num_groups = 7;
+  if (uo2) {
+    x.sigma_t = {0.177949, 0.329805, 0.480388, 0.554367, 0.311801, 0.395168,
+                 0.564406};
+    x.nu_sigma_f = {0.02005998, 0.002027303, 0.01570599, 0.04518301,
+                    0.04334208, 0.2020901, 0.5257105};
+    x.sigma_f = {0.00721206, 8.19301E-4, 0.0064532, 0.0185648, 0.0178084,
+                 0.0830348, 0.216004};
+    x.chi = {0.58791, 0.41176, 3.3906E-4, 1.1761E-7, 0.0, 0.0, 0.0};
+    x.sigma_s = {0.127537, 0.042378, 9.4374E-6, 5.5163E-9, 0, 0, 0,
+                 0, 0.324456, 0.0016314, 3.1427E-9, 0, 0, 0,
+                 0, 0, 0.45094, 0.0026792, 0, 0, 0,
+                 0, 0, 0, 0.452565, 0.0055664, 0, 0,
+                 0, 0, 0, 1.2525E-4, 0.271401, 0.010255, 1.0021E-8,
+                 0, 0, 0, 0, 0.0012968, 0.265802, 0.016809,
+                 0, 0, 0, 0, 0, 0.0085458, 0.27308};
+  } else {
+    x.sigma_t = {0.159206, 0.41297, 0.59031, 0.58435, 0.718, 1.25445,
+                 2.65038};
+    x.nu_sigma_f.assign(7, 0.0);
+    x.sigma_f.assign(7, 0.0);
+    x.chi.assign(7, 0.0);
+    x.sigma_s = {0.0444777, 0.1134, 7.2347E-4, 3.7499E-6, 5.3184E-8, 0, 0,
+                 0, 0.282334, 0.12994, 6.234E-4, 4.8002E-5, 7.4486E-6,
+                 1.0455E-6,
+                 0, 0, 0.345256, 0.22457, 0.016999, 0.0026443, 5.0344E-4,
+                 0, 0, 0, 0.0910284, 0.41551, 0.063732, 0.012139,
+                 0, 0, 0, 7.1437E-5, 0.139138, 0.51182, 0.061229,
+                 0, 0, 0, 0, 0.0022157, 0.699913, 0.53732,
+                 0, 0, 0, 0, 0, 0.13244, 2.4807};
+  }
+  return x;
+}
+
+static std::vector<double> linspace(double a, double b, int n) {
+  std::vector<double> v(n);
+  for (int i = 0; i < n; i++) v[i] = (n == 1) ? a : a + (b - a) * i / (n - 1);
+  return v;
+}
+
+/* The 70-group linspace data of tests/test_forward_pin_cell_70g. */
+static MaterialXS lin70(bool fuel) {
+  MaterialXS x;
+  x.num_groups = 70;
+  if (fuel) {
+    x.nu_sigma_f = linspace(0, 1, 70);
+    for (double& v : x.nu_sigma_f) v *= 7;
+    x.sigma_s = linspace(0, 1, 4900);
+    for (double& v : x.sigma_s) v /= 1000;
+    x.chi.assign(70, 1 / 70.);
+    x.sigma_t = linspace(2, 3, 70);
+  } else {
+    x.nu_sigma_f.assign(70, 0.0);
+    x.sigma_s = linspace(1, 2, 4900);
+    for (double& v : x.sigma_s) v /= 1000;
+    x.chi.assign(70, 0.0);
+    x.sigma_t = linspace(3, 4, 70);
+  }
+  x.sigma_f = x.nu_sigma_f;
+  return x;
+}
+
+struct PinSpec {
+  double radius, pitch;
+  int fuel_rings, fuel_sectors, mod_sectors;
+};
+
+/* A pin universe: fuel (-cylinder) and moderator (+cylinder). */
+static Universe* make_pin(Material* fuel, Material* mod, const PinSpec& ps) {
+  ZCylinder* cyl = new ZCylinder(0.0, 0.0, ps.radius);
+  Cell* f = new Cell();
+  f->setFill(fuel);
+  f->addSurface(-1, cyl);
+  if (ps.fuel_rings) f->setNumRings(ps.fuel_rings);
+  if (ps.fuel_sectors) f->setNumSectors(ps.fuel_sectors);
+  Cell* m = new Cell();
+  m->setFill(mod);
+  m->addSurface(+1, cyl);
+  if (ps.mod_sectors) m->setNumSectors(ps.mod_sectors);
+  Universe* u = new Universe();
+  u->addCell(f);
+  u->addCell(m);
+  return u;
+}
+
+/* Root universe: a box of half-width hw around a lattice or a single pin. */
+static Geometry* make_box_geometry(Universe* fill_or_null, Lattice* lat,
+                                   double hw, boundaryType bxmin,
+                                   boundaryType bxmax, boundaryType bymin,
+                                   boundaryType bymax) {
+  XPlane* xmin = new XPlane(-hw);
+  XPlane* xmax = new XPlane(hw);
+  YPlane* ymin = new YPlane(-hw);
+  YPlane* ymax = new YPlane(hw);
+  xmin->setBoundaryType(bxmin);
+  xmax->setBoundaryType(bxmax);
+  ymin->setBoundaryType(bymin);
+  ymax->setBoundaryType(bymax);
+  Cell* root = new Cell();
+  root->addSurface(+1, xmin);
+  root->addSurface(-1, xmax);
+  root->addSurface(+1, ymin);
+  root->addSurface(-1, ymax);
+  if (lat) root->setFill(lat);
+  else root->setFill(fill_or_null);
+  Universe* ru = new Universe();
+  ru->addCell(root);
+  Geometry* g = new Geometry();
+  g->setRootUniverse(ru);
+  return g;
+}
+
+/* The reference PinCellInput geometry (tests/input_set.py:95-137): r=1 pin
+ * in a +-2 cm reflective box, no rings or sectors. */
+static Geometry* pincell_input(Material* fuel, Material* water) {
+  ZCylinder* cyl = new ZCylinder(0.0, 0.0, 1.0);
+  XPlane* xmin = new XPlane(-2.0);
+  XPlane* xmax = new XPlane(2.0);
+  YPlane* ymin = new YPlane(-2.0);
+  YPlane* ymax = new YPlane(2.0);
+  xmin->setBoundaryType(REFLECTIVE);
+  xmax->setBoundaryType(REFLECTIVE);
+  ymin->setBoundaryType(REFLECTIVE);
+  ymax->setBoundaryType(REFLECTIVE);
+  Cell* f = new Cell();
+  f->setFill(fuel);
+  f->addSurface(-1, cyl);
+  Cell* m = new Cell();
+  m->setFill(water);
+  m->addSurface(+1, cyl);
+  m->addSurface(+1, xmin);
+  m->addSurface(-1, xmax);
+  m->addSurface(+1, ymin);
+  m->addSurface(-1, ymax);
+  Universe* ru = new Universe();
+  ru->addCell(f);
+  ru->addCell(m);
+  Geometry* g = new Geometry();
+  g->setRootUniverse(ru);
+  return g;
+}
+
+/* n x n lattice of pins; positions listed in water_pins hold a pin whose
+ * inner circle is filled with the moderator. */
+static Geometry* lattice_geometry(int n, Material* fuel, Material* mod,
+                                  const PinSpec& ps,
+                                  const std::vector<int>& water_pins,
+                                  boundaryType bxmin, boundaryType bxmax,
+                                  boundaryType bymin, boundaryType bymax) {
+  Universe* pin = make_pin(fuel, mod, ps);
+  Universe* wpin = make_pin(mod, mod, ps);
+  std::vector<Universe*> u(n * n, pin);
+  for (int k : water_pins) u[k] = wpin;
+  Lattice* lat = new Lattice();
+  lat->setWidth(ps.pitch, ps.pitch);
+  lat->setUniverses(1, n, n, u.data());
+  return make_box_geometry(NULL, lat, 0.5 * n * ps.pitch, bxmin, bxmax, bymin,
+                           bymax);
+}
+
+/* ------------------------------------------------------------------ runs */
+enum RunKind { EIGEN, SOURCE, FLUX };
+
+struct CaseSpec {
+  const char* name;
+  Geometry* geo;
+  int num_azim;
+  double spacing;
+  int max_iters;
+  double tol;
+  residualType res;
+  RunKind kind;
+  double k_source;
+  bool probe;
+};
+
+static void run_case(const CaseSpec& c, const std::string& outdir) {
+  c.geo->initializeFlatSourceRegions();
+  TrackGenerator tg(c.geo, c.num_azim, c.spacing);
+  tg.setNumThreads(1);
+  tg.generateTracks();
+
+  ProbeSolver solver(&tg);
+  solver.setNumThreads(1);
+  solver.setConvergenceThreshold(c.tol);
+  if (c.kind == EIGEN)
+    solver.computeEigenvalue(c.max_iters, c.res);
+  else if (c.kind == SOURCE)
+    solver.computeSource(c.max_iters, c.k_source, c.res);
+  else
+    solver.computeFlux(c.max_iters, true);
+
+  PackedProblem p;
+  openmoc_gb300::pack_tracks(&tg, p);
+  openmoc_gb300::pack_materials(c.geo, tg.getFSRVolumes(), p);
+
+  Writer w(outdir + "/" + c.name + "_" + PREC);
+  write_problem(w, p);
+  w.sc("num_azim", c.num_azim);
+  w.sc("spacing", c.spacing);
+  w.sc("max_iters", c.max_iters);
+  w.sc("tolerance", c.tol);
+  w.sc("res_type", (int) c.res);
+  w.sc("run_kind", (int) c.kind);
+  w.sc("k_source", c.k_source);
+  w.sc("iterations", solver.getNumIterations());
+  w.sc("keff", solver.getKeff());
+  const long R = p.num_fsrs;
+  const int G = p.num_groups;
+  std::vector<float> flux((size_t) R * G);
+  for (long r = 0; r < R; r++)
+    for (int g = 0; g < G; g++)
+      flux[(size_t) r * G + g] = (float) solver.getFlux(r, g + 1);
+  w.arr("flux", "f4", flux.data(), flux.size());
+  if (c.probe && c.kind == EIGEN) {
+#ifdef SINGLE
+    solver.probe(w);
+#endif
+  }
+  w.close();
+  printf("%s [%s]: R=%ld T=%ld S=%ld iters=%d keff=%.8f\n", c.name, PREC,
+         p.num_fsrs, p.num_tracks, p.num_segments, solver.getNumIterations(),
+         solver.getKeff());
+}
+
+int main(int argc, char** argv) {
+  std::string outdir = argc > 1 ? argv[1] : "tests/golden";
+  std::string only = argc > 2 ? argv[2] : "";
+  set_log_level("ERROR");
+  const boundaryType REF = REFLECTIVE, VAC = VACUUM;
+
+  std::vector<CaseSpec> cases;
+
+  /* 1. tests/test_forward_pin_cell: C5G7, 4 azimuthal, 0.1 cm, 1e-5 */
+  {
+    Material* fuel = make_material(1, "UO2", c5g7(true));
+    Material* water = make_material(2, "Water", c5g7(false));
+    cases.push_back({"pin_c5g7", pincell_input(fuel, water), 4, 0.1, 500,
+                     1e-5, FISSION_SOURCE, EIGEN, 1.0, true});
+  }
+  /* 2. tests/test_forward_pin_cell_70g: linspace 70-group data */
+  {
+    Material* fuel = make_material(3, "UO2-70", lin70(true));
+    Material* water = make_material(4, "Water-70", lin70(false));
+    cases.push_back({"pin_70g", pincell_input(fuel, water), 4, 0.1, 1000,
+                     1e-5, SCALAR_FLUX, EIGEN, 1.0, true});
+  }
+  /* 3. the 7-group synthetic pin cell: r=0.54 in 1.26 cm, 3 rings x 8
+   *    sectors in fuel, 8 moderator sectors, 32 azimuthal, 0.05 cm */
+  PinSpec pin = {0.54, 1.26, 3, 8, 8};
+  {
+    Material* fuel = make_material(5, "fuel7",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL, 7, true));
+    Material* mod = make_material(6, "mod7",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 1000, 7, false));
+    Lattice* lat = NULL;
+    Universe* u = make_pin(fuel, mod, pin);
+    cases.push_back({"pin7_synth", make_box_geometry(u, lat, 0.63, REF, REF,
+                     REF, REF), 32, 0.05, 1000, 1e-5, FISSION_SOURCE, EIGEN,
+                     1.0, true});
+  }
+  /* 4. 3x3 lattice, 2 groups, vacuum on +x and +y, centre pin water */
+  {
+    Material* fuel = make_material(7, "fuel2",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 2, 2, true));
+    Material* mod = make_material(8, "mod2",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 1002, 2, false));
+    cases.push_back({"lat3_g2_vac", lattice_geometry(3, fuel, mod, pin, {4},
+                     REF, VAC, REF, VAC), 16, 0.1, 1000, 1e-5,
+                     FISSION_SOURCE, EIGEN, 1.0, true});
+  }
+  /* 5. 2x2 lattice, 16 groups, reflective */
+  {
+    Material* fuel = make_material(9, "fuel16",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 3, 16, true));
+    Material* mod = make_material(10, "mod16",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 1003, 16, false));
+    cases.push_back({"lat2_g16", lattice_geometry(2, fuel, mod, pin, {3},
+                     REF, REF, REF, REF), 8, 0.1, 1000, 1e-5,
+                     FISSION_SOURCE, EIGEN, 1.0, true});
+  }
+
+  for (const CaseSpec& c : cases) {
+    if (!only.empty() && only != c.name) continue;
+    run_case(c, outdir);
+  }
+  return 0;
+}

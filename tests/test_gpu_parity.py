@@ -1,0 +1,130 @@
+"""Parity of the CUDA path (through the C ABI) with OpenMOC itself and with
+the FP64 oracle, on the fixtures OpenMOC's library wrote.
+
+Tolerances (the acceptance bar): keff within 1e-5 absolute and FSR scalar
+fluxes within 1e-4 max relative of OpenMOC's FP32 CPUSolver on identical
+inputs; the same bars against the FP64 build, with 1.5e-5 on keff because
+OpenMOC's own FP32 and FP64 builds differ by 1.1e-5 on the pin cell at the
+1e-5 convergence threshold.
+"""
+import numpy as np
+import pytest
+
+from conftest import CASES, load_case
+from openmoc_gb300 import GB300Solver
+from openmoc_gb300.solver import EXP_INTRINSIC, EXP_TABLE, FISSION_SOURCE, SCALAR_FLUX
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+KEFF_TOL = 1e-5
+FLUX_TOL = 1e-4
+
+
+def max_rel(a, b):
+    a = np.asarray(a, np.float64).ravel()
+    b = np.asarray(b, np.float64).ravel()
+    return float(np.max(np.abs(a - b) / np.abs(b)))
+
+
+def solve(case, exp_kind, precision="f32"):
+    p, sc, arr = load_case(case, precision)
+    s = GB300Solver(p)
+    s.setConvergenceThreshold(sc["tolerance"])
+    if exp_kind == EXP_INTRINSIC:
+        s.useExponentialIntrinsic()
+    s.computeEigenvalue(int(sc["max_iters"]), int(sc["res_type"]))
+    return s, p, sc, arr
+
+
+@pytest.mark.parametrize("exp_kind", [EXP_TABLE, EXP_INTRINSIC])
+@pytest.mark.parametrize("case", CASES)
+def test_eigenvalue_matches_openmoc(case, exp_kind):
+    s, p, sc, arr = solve(case, exp_kind)
+    _, sc64, arr64 = load_case(case, "f64")
+    k = s.getKeff()
+    flux = s.getFluxes()
+    assert abs(s.getNumIterations() - int(sc["iterations"])) <= 2
+    assert abs(k - sc["keff"]) <= KEFF_TOL, (k, sc["keff"])
+    assert max_rel(flux, arr["flux"]) <= FLUX_TOL
+    assert abs(k - sc64["keff"]) <= 1.5 * KEFF_TOL, (k, sc64["keff"])
+    assert max_rel(flux, arr64["flux"]) <= FLUX_TOL
+    # getFlux is 1-based in the group, like OpenMOC's
+    assert s.getFlux(0, 1) == pytest.approx(float(flux[0, 0]))
+
+
+@pytest.mark.parametrize("case", ["pin7_synth", "lat3_g2_vac", "lat2_g16", "pin_70g"])
+def test_tight_convergence_against_fp64_oracle(case):
+    """Converged further than the fixtures, the FP32 GPU sweep stays within
+    the bar of the FP64 oracle."""
+    p, _, _ = load_case(case, "f32")
+    o = Oracle(p, "f64")
+    o.compute_eigenvalue(2000, FISSION_SOURCE if case != "pin_70g" else SCALAR_FLUX, 1e-7)
+    s = GB300Solver(p)
+    s.setConvergenceThreshold(1e-7)
+    s.computeEigenvalue(2000, FISSION_SOURCE if case != "pin_70g" else SCALAR_FLUX)
+    assert abs(s.getKeff() - o.keff) <= KEFF_TOL
+    assert max_rel(s.getFluxes(), o.phi) <= FLUX_TOL
+
+
+@pytest.mark.parametrize("exp_kind", [EXP_TABLE, EXP_INTRINSIC])
+@pytest.mark.parametrize("case", CASES)
+def test_hooks_match_openmoc(case, exp_kind):
+    """One pass of each protected Solver hook from OpenMOC's converged state."""
+    p, sc, arr = load_case(case, "f32")
+    s = GB300Solver(p)
+    if exp_kind == EXP_INTRINSIC:
+        s.useExponentialIntrinsic()
+    R, G = p.num_fsrs, p.num_groups
+    s.setFluxes(arr["probe_phi_in"])
+    s.setOldFluxes(arr["probe_phi_old"])
+    s.setKeff(sc["probe_keff_in"])
+    s.setStartFlux(arr["probe_start_flux_in"])
+    s.computeFSRSources(100)
+    np.testing.assert_allclose(s.getReducedSources().ravel(),
+                               arr["probe_reduced_sources"], rtol=2e-6, atol=1e-30)
+    s.transportSweep()
+    ref = arr["probe_phi_sweep"].reshape(R, G)
+    got = s.getFluxes()
+    assert np.max(np.abs(got - ref) / np.abs(ref).max(axis=0)) < 5e-5
+    sref = arr["probe_start_flux_out"]
+    assert np.max(np.abs(s.getStartFlux() - sref)) <= 2e-4 * np.max(np.abs(sref))
+    s.addSourceToScalarFlux()
+    assert max_rel(s.getFluxes(), arr["probe_phi_addsrc"]) < 2e-5
+    s.computeKeff()
+    assert abs(s.getKeff() - sc["probe_keff_out"]) < 1e-6
+    f = s.normalizeFluxes()
+    assert abs(f / sc["probe_norm_factor"] - 1) < 1e-6
+    assert max_rel(s.getFluxes(), arr["probe_phi_norm"]) < 2e-5
+    assert s.computeResidual(1) == pytest.approx(sc["probe_residual_fission"], abs=1e-6)
+    assert s.computeResidual(0) == pytest.approx(sc["probe_residual_flux"], abs=1e-5)
+    assert s.computeResidual(2) == pytest.approx(sc["probe_residual_total"], abs=1e-6)
+
+
+@pytest.mark.parametrize("case", ["pin7_synth", "lat2_g16"])
+def test_sweep_matches_oracle_hook_for_hook(case):
+    """The sweep alone against the oracle from identical state, for every
+    sweep-kernel shape the library can pick for this group count."""
+    p, sc, arr = load_case(case, "f32")
+    G = p.num_groups
+    shapes = [(l, -(-G // l)) for l in (1, 2, 4, 8, 16, 32) if -(-G // l) <= 9]
+    o = Oracle(p, "f32")
+    o.phi[:] = arr["probe_phi_in"]
+    o.keff = sc["probe_keff_in"]
+    o.start[:] = arr["probe_start_flux_in"]
+    o.compute_sources(100)
+    o.sweep()
+    for lps, slots in shapes:
+        s = GB300Solver(p)
+        s.setSweepShape(lps, slots)
+        s.setFluxes(arr["probe_phi_in"])
+        s.setKeff(sc["probe_keff_in"])
+        s.setStartFlux(arr["probe_start_flux_in"])
+        s.computeFSRSources(100)
+        s.transportSweep()
+        ref = o.phi.reshape(p.num_fsrs, G)
+        got = s.getFluxes()
+        err = np.max(np.abs(got - ref) / np.abs(ref).max(axis=0))
+        assert err < 2e-5, (lps, slots, err)
+        assert np.max(np.abs(s.getStartFlux() - o.start)) <= 1e-5 * np.max(np.abs(o.start))
+        s.close()
