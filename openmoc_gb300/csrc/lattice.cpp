@@ -1,0 +1,496 @@
+// Track laydown and ray tracing for square lattices of pin cells: the
+// producer of the benchmark workloads on hosts that do not have OpenMOC.
+//
+// It restates, for this one geometry family, what OpenMOC's 2D
+// TrackGenerator and Geometry produce:
+//   - cyclic track laydown with corrected angles and spacings
+//     (TrackGenerator::initializeTracks, src/TrackGenerator.cpp:950-1083);
+//   - track connections and boundary conditions
+//     (TrackGenerator::initializeTrackReflections, :1086-1222);
+//   - UIDs in azimuth-major order (initializeTracksArray, :1795-1818);
+//   - segments between successive surface crossings
+//     (Geometry::segmentize2D, src/Geometry.cpp:2085-2230), with FSR ids in
+//     order of first touch over tracks in UID order (the single-thread
+//     numbering the reference test harness uses);
+//   - pin cells split into equal-area fuel rings (Cell::ringify,
+//     src/Cell.cpp:1397-1590) and sectors bounded by planes at
+//     pi/4 + i*2*pi/n (Cell::sectorize, src/Cell.cpp:1325-1390);
+//   - FSR volumes from segment lengths times the azimuthal weight and
+//     spacing (VolumeKernel, src/MOCKernel.cpp:86-170);
+//   - azimuthal weights and the Tabuchi-Yamamoto polar quadrature
+//     (Quadrature::precomputeWeights, src/Quadrature.cpp:674-745;
+//     TYPolarQuad, :797-895).
+// Segments are found analytically (circle, sector-line and lattice-line
+// crossings sorted along the ray, each sub-interval classified at its
+// midpoint), not by nudging a point across surfaces.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <unordered_map>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+thread_local std::string g_lat_error;
+
+struct Spec {
+  int32_t nx, ny;
+  double pitch;
+  double pin_radius;
+  int32_t fuel_rings;
+  int32_t fuel_sectors;
+  int32_t mod_sectors;
+  int32_t bc[4];          // xmin, xmax, ymin, ymax: 0 vacuum, 1 reflective
+  int32_t num_azim;       // multiple of 4
+  double spacing;
+  int32_t num_polar;      // 2, 4 or 6
+  int32_t moderator_material;
+  int32_t num_threads;
+};
+
+struct Track {
+  double x0, y0, x1, y1, phi;
+  int a;
+};
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kTinyMove = 1e-8;   // src/constants.h:41
+
+}  // namespace
+
+extern "C" {
+
+typedef struct {
+  int32_t nx, ny;
+  double pitch;
+  double pin_radius;
+  int32_t fuel_rings, fuel_sectors, mod_sectors;
+  int32_t bc[4];
+  int32_t num_azim;
+  double spacing;
+  int32_t num_polar;
+  int32_t moderator_material;
+  int32_t num_threads;
+  const int32_t* pin_material;   // [ny*nx], row 0 = top row (max y)
+} moc_lattice_spec;
+
+struct moc_lattice {
+  int64_t R = 0, T = 0, S = 0;
+  int32_t A = 0, Ph = 0, M = 0;
+  std::vector<float> seg_len;
+  std::vector<int32_t> seg_fsr;
+  std::vector<int64_t> seg_off;
+  std::vector<int32_t> track_ang;
+  std::vector<int64_t> next;
+  std::vector<uint8_t> flags;
+  std::vector<float> weights, inv_sin;
+  std::vector<int32_t> fsr_mat;
+  std::vector<float> fsr_vol;
+  std::vector<double> fsr_cx, fsr_cy;   // a point inside each FSR
+};
+
+const char* moc_lattice_last_error(void) { return g_lat_error.c_str(); }
+
+}  // extern "C"
+
+namespace {
+
+int lat_fail(const std::string& m) {
+  g_lat_error = m;
+  return -1;
+}
+
+// Region of a point relative to its pin-cell centre: ring index (0 =
+// outermost fuel ring, fuel_rings-1 = innermost; fuel_rings = moderator)
+// and sector index.
+struct Classifier {
+  int rings;
+  int fuel_sectors, mod_sectors;
+  std::vector<double> r2;   // squared ring radii, outer to inner
+  double beta_f, beta_m;    // first sector boundary angle
+
+  int sector_of(double ang, int n) const {
+    // sector boundaries at k*2pi/n - pi/4 (Cell::sectorize planes at
+    // pi/4 + k*2pi/n, sector k between planes k and k+1)
+    if (n <= 1) return 0;
+    const double d = 2.0 * kPi / n;
+    double x = ang + kPi / 4.0;
+    x = std::fmod(x, 2.0 * kPi);
+    if (x < 0) x += 2.0 * kPi;
+    int s = (int) std::floor(x / d);
+    if (s >= n) s = n - 1;
+    return s;
+  }
+  // returns (ring, sector) packed
+  uint32_t classify(double dx, double dy) const {
+    const double rr = dx * dx + dy * dy;
+    int ring = rings;  // moderator
+    if (rr < r2[0]) {
+      ring = 0;
+      for (int k = 1; k < rings; k++)
+        if (rr < r2[k]) ring = k;
+    }
+    const double ang = std::atan2(dy, dx);
+    const int sec = sector_of(ang, ring < rings ? fuel_sectors : mod_sectors);
+    return (uint32_t) ring << 16 | (uint32_t) sec;
+  }
+};
+
+void add_sector_lines(std::vector<double>& dirs, int n) {
+  if (n <= 1) return;
+  const double d = 2.0 * kPi / n;
+  for (int k = 0; k < n; k++) dirs.push_back(k * d - kPi / 4.0);
+}
+
+}  // namespace
+
+extern "C" int moc_lattice_generate(const moc_lattice_spec* sp,
+                                    moc_lattice** out) {
+  if (!sp || !out) return lat_fail("null argument");
+  *out = nullptr;
+  const moc_lattice_spec& s = *sp;
+  if (s.nx < 1 || s.ny < 1 || !(s.pitch > 0) || !(s.pin_radius > 0) ||
+      s.pin_radius >= 0.5 * s.pitch)
+    return lat_fail("bad lattice or pin dimensions");
+  if (s.num_azim < 4 || s.num_azim % 4)
+    return lat_fail("num_azim must be a positive multiple of 4");
+  if (!(s.spacing > 0)) return lat_fail("spacing must be positive");
+  if (s.num_polar != 2 && s.num_polar != 4 && s.num_polar != 6)
+    return lat_fail("num_polar must be 2, 4 or 6 (Tabuchi-Yamamoto)");
+  if (s.fuel_rings < 1 || s.fuel_sectors < 0 || s.mod_sectors < 0)
+    return lat_fail("bad ring / sector counts");
+  if (!s.pin_material) return lat_fail("pin_material is required");
+  for (int b = 0; b < 4; b++)
+    if (s.bc[b] != 0 && s.bc[b] != 1)
+      return lat_fail("boundary conditions are 0 (vacuum) or 1 (reflective)");
+
+  moc_lattice* L = new moc_lattice();
+  const int A = s.num_azim;
+  const double W = s.nx * s.pitch, H = s.ny * s.pitch;
+  const double xmin = -0.5 * W, ymin = -0.5 * H;
+
+  // ---- angles, spacings, counts (TrackGenerator::initializeTracks) ----
+  std::vector<int> num_x(A / 2), num_y(A / 2);
+  std::vector<double> phis(A / 2), dx_eff(A / 2), dy_eff(A / 2), spac(A / 2);
+  for (int a = 0; a < A / 4; a++) {
+    const double phi_d = 2.0 * kPi / A * (0.5 + a);
+    num_x[a] = (int) (std::fabs(W / s.spacing * std::sin(phi_d))) + 1;
+    num_y[a] = (int) (std::fabs(H / s.spacing * std::cos(phi_d))) + 1;
+    num_x[A / 2 - a - 1] = num_x[a];
+    num_y[A / 2 - a - 1] = num_y[a];
+    const double phi = std::atan((H * num_x[a]) / (W * num_y[a]));
+    phis[a] = phi;
+    phis[A / 2 - a - 1] = kPi - phi;
+    dx_eff[a] = dx_eff[A / 2 - a - 1] = W / num_x[a];
+    dy_eff[a] = dy_eff[A / 2 - a - 1] = H / num_y[a];
+    spac[a] = spac[A / 2 - a - 1] = dx_eff[a] * std::sin(phi);
+  }
+  // azimuthal weights (Quadrature::precomputeWeights)
+  std::vector<double> wa(A / 2);
+  for (int a = 0; a < A / 4; a++) {
+    double x1 = (a < A / 4 - 1) ? 0.5 * (phis[a + 1] - phis[a])
+                                : 0.5 * kPi - phis[a];
+    double x2 = (a >= 1) ? 0.5 * (phis[a] - phis[a - 1]) : phis[a];
+    wa[a] = wa[A / 2 - a - 1] = (x1 + x2) / kPi;
+  }
+  // Tabuchi-Yamamoto polar sets: sin(theta) and weight per half space
+  std::vector<double> sin_t, w_p;
+  if (s.num_polar == 2) {
+    sin_t = {0.798184};
+    w_p = {0.5};
+  } else if (s.num_polar == 4) {
+    sin_t = {0.363900, 0.899900};
+    w_p = {0.212854 / 2.0, 0.787146 / 2.0};
+  } else {
+    sin_t = {0.166648, 0.537707, 0.932954};
+    w_p = {0.046233 / 2.0, 0.283619 / 2.0, 0.670148 / 2.0};
+  }
+  const int Ph = s.num_polar / 2;
+  L->A = A / 2;
+  L->Ph = Ph;
+  L->weights.resize((size_t) (A / 2) * Ph);
+  L->inv_sin.resize((size_t) (A / 2) * Ph);
+  for (int a = 0; a < A / 2; a++)
+    for (int p = 0; p < Ph; p++) {
+      const double st = std::sin(std::asin(sin_t[p]));
+      const double w = 2.0 * kPi * wa[a] * spac[a] * w_p[p] * 2.0 * st;
+      L->weights[a * Ph + p] = (float) w;
+      L->inv_sin[a * Ph + p] = (float) (1.f / st);
+    }
+
+  // ---- tracks ----
+  std::vector<int64_t> first(A / 2 + 1, 0);
+  for (int a = 0; a < A / 2; a++) first[a + 1] = first[a] + num_x[a] + num_y[a];
+  const int64_t T = first[A / 2];
+  L->T = T;
+  std::vector<Track> tracks(T);
+  for (int a = 0; a < A / 2; a++) {
+    const int nx = num_x[a], ny = num_y[a];
+    const double dx = dx_eff[a], dy = dy_eff[a];
+    for (int i = 0; i < nx + ny; i++) {
+      Track& t = tracks[first[a] + i];
+      t.a = a;
+      t.phi = phis[a];
+      if (a < A / 4) {
+        if (i < nx) { t.x0 = xmin + W - dx * (i + 0.5); t.y0 = ymin; }
+        else { t.x0 = xmin; t.y0 = ymin + dy * (i - nx + 0.5); }
+        if (i < ny) { t.x1 = xmin + W; t.y1 = ymin + dy * (i + 0.5); }
+        else { t.x1 = xmin + W - dx * ((i - ny) + 0.5); t.y1 = ymin + H; }
+      } else {
+        if (i < nx) { t.x0 = xmin + dx * (i + 0.5); t.y0 = ymin; }
+        else { t.x0 = xmin + W; t.y0 = ymin + dy * (i - nx + 0.5); }
+        if (i < ny) { t.x1 = xmin; t.y1 = ymin + dy * (i + 0.5); }
+        else { t.x1 = xmin + dx * (i - ny + 0.5); t.y1 = ymin + H; }
+      }
+    }
+  }
+  // ---- connections (TrackGenerator::initializeTrackReflections) ----
+  L->next.assign(2 * T, 0);
+  L->flags.assign(T, 0);
+  L->track_ang.assign(T, 0);
+  const int BXMIN = s.bc[0], BXMAX = s.bc[1], BYMIN = s.bc[2], BYMAX = s.bc[3];
+  for (int a = 0; a < A / 2; a++) {
+    const int ac = A / 2 - a - 1;
+    const int nx = num_x[a], ny = num_y[a];
+    for (int i = 0; i < nx + ny; i++) {
+      const int64_t id = first[a] + i;
+      int bc_fwd, bc_bwd;
+      if (a < A / 4) {
+        bc_fwd = (i < ny) ? BXMAX : BYMAX;
+        bc_bwd = (i < nx) ? BYMIN : BXMIN;
+      } else {
+        bc_fwd = (i < ny) ? BXMIN : BYMAX;
+        bc_bwd = (i < nx) ? BYMIN : BXMAX;
+      }
+      bool fwd_fwd, bwd_fwd;
+      int64_t nf, nb;
+      if (i < ny) {
+        fwd_fwd = true;
+        nf = first[ac] + i + nx;
+      } else {
+        fwd_fwd = false;
+        nf = first[ac] + (nx + ny) - (i - ny) - 1;
+      }
+      if (i < nx) {
+        nb = first[ac] + nx - i - 1;
+        bwd_fwd = true;
+      } else {
+        bwd_fwd = false;
+        nb = first[ac] + i - nx;
+      }
+      L->next[2 * id] = nf;
+      L->next[2 * id + 1] = nb;
+      uint8_t f = 0;
+      if (fwd_fwd) f |= 1;
+      if (bwd_fwd) f |= 2;
+      if (bc_fwd == 1) f |= 4;
+      if (bc_bwd == 1) f |= 8;
+      L->flags[id] = f;
+      L->track_ang[id] = a;
+    }
+  }
+
+  // ---- segmentation ----
+  Classifier cls;
+  cls.rings = s.fuel_rings;
+  cls.fuel_sectors = s.fuel_sectors;
+  cls.mod_sectors = s.mod_sectors;
+  for (int k = 0; k < s.fuel_rings; k++) {
+    // equal-area rings: r_k = r * sqrt(1 - k/n)
+    const double r = s.pin_radius * std::sqrt(1.0 - (double) k / s.fuel_rings);
+    cls.r2.push_back(r * r);
+  }
+  std::vector<double> radii;
+  for (double v : cls.r2) radii.push_back(std::sqrt(v));
+  std::vector<double> line_dirs;
+  add_sector_lines(line_dirs, s.fuel_sectors);
+  add_sector_lines(line_dirs, s.mod_sectors);
+  std::sort(line_dirs.begin(), line_dirs.end());
+
+  std::vector<std::vector<float>> seg_len_t(T);
+  std::vector<std::vector<uint64_t>> seg_key_t(T);
+#ifdef _OPENMP
+  if (s.num_threads > 0) omp_set_num_threads(s.num_threads);
+#pragma omp parallel for schedule(dynamic, 16)
+#endif
+  for (int64_t t = 0; t < T; t++) {
+    const Track& tr = tracks[t];
+    const double ux = std::cos(tr.phi), uy = std::sin(tr.phi);
+    const double len =
+        std::sqrt((tr.x1 - tr.x0) * (tr.x1 - tr.x0) + (tr.y1 - tr.y0) * (tr.y1 - tr.y0));
+    std::vector<double> cuts;
+    cuts.push_back(0.0);
+    // lattice lines
+    for (int k = 1; k < s.nx; k++) {
+      if (std::fabs(ux) < 1e-300) break;
+      const double tt = (xmin + k * s.pitch - tr.x0) / ux;
+      if (tt > 0 && tt < len) cuts.push_back(tt);
+    }
+    for (int k = 1; k < s.ny; k++) {
+      if (std::fabs(uy) < 1e-300) break;
+      const double tt = (ymin + k * s.pitch - tr.y0) / uy;
+      if (tt > 0 && tt < len) cuts.push_back(tt);
+    }
+    cuts.push_back(len);
+    std::sort(cuts.begin(), cuts.end());
+    std::vector<double> pts;
+    std::vector<float>& out_len = seg_len_t[t];
+    std::vector<uint64_t>& out_key = seg_key_t[t];
+    for (size_t c = 0; c + 1 < cuts.size(); c++) {
+      const double ta = cuts[c], tb = cuts[c + 1];
+      if (tb - ta <= 0) continue;
+      const double tm = 0.5 * (ta + tb);
+      const double mx = tr.x0 + tm * ux, my = tr.y0 + tm * uy;
+      int ci = (int) std::floor((mx - xmin) / s.pitch);
+      int cj = (int) std::floor((my - ymin) / s.pitch);
+      ci = std::min(std::max(ci, 0), s.nx - 1);
+      cj = std::min(std::max(cj, 0), s.ny - 1);
+      const double cx = xmin + (ci + 0.5) * s.pitch;
+      const double cy = ymin + (cj + 0.5) * s.pitch;
+      pts.clear();
+      pts.push_back(ta);
+      const double px = tr.x0 - cx, py = tr.y0 - cy;
+      const double b = px * ux + py * uy;
+      const double pp = px * px + py * py;
+      for (double r : radii) {
+        const double disc = b * b - (pp - r * r);
+        if (disc <= 0) continue;
+        const double sq = std::sqrt(disc);
+        const double t1 = -b - sq, t2 = -b + sq;
+        if (t1 > ta && t1 < tb) pts.push_back(t1);
+        if (t2 > ta && t2 < tb) pts.push_back(t2);
+      }
+      for (double beta : line_dirs) {
+        const double vx = std::cos(beta), vy = std::sin(beta);
+        const double den = ux * vy - uy * vx;
+        if (std::fabs(den) < 1e-14) continue;
+        // P0 + t u = c + s v  ->  t = ((c - P0) x v) / (u x v)
+        const double qx = cx - tr.x0, qy = cy - tr.y0;
+        const double tt = (qx * vy - qy * vx) / den;
+        const double ss = (qx * uy - qy * ux) / den;
+        if (ss > 0 && tt > ta && tt < tb) pts.push_back(tt);
+      }
+      pts.push_back(tb);
+      std::sort(pts.begin(), pts.end());
+      const uint64_t cell = (uint64_t) ((int64_t) (s.ny - 1 - cj) * s.nx + ci);
+      for (size_t k = 0; k + 1 < pts.size(); k++) {
+        const double l = pts[k + 1] - pts[k];
+        if (l <= kTinyMove) {
+          // below the reference's surface nudge: absorbed by its neighbour
+          if (!out_len.empty()) out_len.back() += (float) 0;
+          continue;
+        }
+        const double mm = 0.5 * (pts[k] + pts[k + 1]);
+        const uint32_t rs =
+            cls.classify(tr.x0 + mm * ux - cx, tr.y0 + mm * uy - cy);
+        const uint64_t key = cell << 32 | rs;
+        if (!out_key.empty() && out_key.back() == key) {
+          out_len.back() = (float) ((double) out_len.back() + l);
+        } else {
+          out_key.push_back(key);
+          out_len.push_back((float) l);
+        }
+      }
+    }
+  }
+  // ---- FSR ids by first touch, UID order ----
+  std::unordered_map<uint64_t, int32_t> ids;
+  ids.reserve((size_t) s.nx * s.ny * 64);
+  std::vector<uint64_t> keys;
+  L->seg_off.assign(T + 1, 0);
+  for (int64_t t = 0; t < T; t++)
+    L->seg_off[t + 1] = L->seg_off[t] + (int64_t) seg_len_t[t].size();
+  const int64_t S = L->seg_off[T];
+  L->S = S;
+  L->seg_len.resize(S);
+  L->seg_fsr.resize(S);
+  for (int64_t t = 0; t < T; t++) {
+    const int64_t base = L->seg_off[t];
+    for (size_t k = 0; k < seg_len_t[t].size(); k++) {
+      const uint64_t key = seg_key_t[t][k];
+      auto it = ids.find(key);
+      int32_t id;
+      if (it == ids.end()) {
+        id = (int32_t) keys.size();
+        ids.emplace(key, id);
+        keys.push_back(key);
+      } else {
+        id = it->second;
+      }
+      L->seg_fsr[base + k] = id;
+      L->seg_len[base + k] = seg_len_t[t][k];
+    }
+    std::vector<float>().swap(seg_len_t[t]);
+    std::vector<uint64_t>().swap(seg_key_t[t]);
+  }
+  const int64_t R = (int64_t) keys.size();
+  L->R = R;
+  L->fsr_mat.resize(R);
+  L->fsr_vol.assign(R, 0.0f);
+  L->fsr_cx.resize(R);
+  L->fsr_cy.resize(R);
+  int32_t maxmat = s.moderator_material;
+  for (int64_t r = 0; r < R; r++) {
+    const uint64_t key = keys[r];
+    const int64_t cell = (int64_t) (key >> 32);
+    const int ring = (int) ((key >> 16) & 0xFFFF);
+    const int m = (ring < s.fuel_rings) ? s.pin_material[cell]
+                                        : s.moderator_material;
+    L->fsr_mat[r] = m;
+    maxmat = std::max(maxmat, m);
+  }
+  L->M = maxmat + 1;
+  // volumes: sum of segment lengths times azimuthal weight x spacing
+  std::vector<double> vol(R, 0.0);
+  for (int64_t t = 0; t < T; t++) {
+    const double w = spac[tracks[t].a] * wa[tracks[t].a];
+    for (int64_t k = L->seg_off[t]; k < L->seg_off[t + 1]; k++)
+      vol[L->seg_fsr[k]] += w * (double) L->seg_len[k];
+  }
+  for (int64_t r = 0; r < R; r++) L->fsr_vol[r] = (float) vol[r];
+  *out = L;
+  return 0;
+}
+
+extern "C" int moc_lattice_sizes(moc_lattice* L, int64_t* R, int64_t* T,
+                                 int64_t* S, int32_t* A, int32_t* Ph,
+                                 int32_t* M) {
+  if (!L) return lat_fail("null lattice");
+  *R = L->R;
+  *T = L->T;
+  *S = L->S;
+  *A = L->A;
+  *Ph = L->Ph;
+  *M = L->M;
+  return 0;
+}
+
+extern "C" int moc_lattice_export(moc_lattice* L, float* seg_len,
+                                  int32_t* seg_fsr, int64_t* seg_off,
+                                  int32_t* track_ang, int64_t* next,
+                                  uint8_t* flags, float* weights,
+                                  float* inv_sin, int32_t* fsr_mat,
+                                  float* fsr_vol) {
+  if (!L) return lat_fail("null lattice");
+  std::memcpy(seg_len, L->seg_len.data(), 4 * L->S);
+  std::memcpy(seg_fsr, L->seg_fsr.data(), 4 * L->S);
+  std::memcpy(seg_off, L->seg_off.data(), 8 * (L->T + 1));
+  std::memcpy(track_ang, L->track_ang.data(), 4 * L->T);
+  std::memcpy(next, L->next.data(), 8 * 2 * L->T);
+  std::memcpy(flags, L->flags.data(), L->T);
+  std::memcpy(weights, L->weights.data(), 4 * L->weights.size());
+  std::memcpy(inv_sin, L->inv_sin.data(), 4 * L->inv_sin.size());
+  std::memcpy(fsr_mat, L->fsr_mat.data(), 4 * L->R);
+  std::memcpy(fsr_vol, L->fsr_vol.data(), 4 * L->R);
+  return 0;
+}
+
+extern "C" int moc_lattice_destroy(moc_lattice* L) {
+  delete L;
+  return 0;
+}

@@ -653,6 +653,11 @@ int moc_upload_fsrs(moc_ctx* c, const int32_t* fsr_mat, const float* fsr_vol) {
   MOC_CUDA(cudaMemcpy(c->fsr_mat, fsr_mat, 4 * R, cudaMemcpyHostToDevice));
   MOC_CUDA(cudaMemcpy(c->fsr_vol, fsr_vol, 4 * R, cudaMemcpyHostToDevice));
   count_fissionable(c, fsr_mat);
+  // the FISSION_SOURCE residual norm is read on the device by every
+  // residual launch, hooks included
+  MOC_TRY(pull(c));
+  c->hsc->num_fissionable = c->num_fissionable;
+  MOC_TRY(push(c));
   c->have_fsrs = true;
   return MOC_OK;
 }
