@@ -1,0 +1,338 @@
+"""Benchmark: segment x group x polar integrations per second of MOC source
+iteration on the 17 x 17 pin lattice, 70 groups, 64 azimuthal angles,
+0.05 cm spacing, 3 polar angles per half space (TY-6), reflective.
+
+A step is one full source iteration (FSR sources, transport sweep, add
+source, keff + normalisation, residual) over the whole problem, inputs
+resident in HBM; integrations per step = 2 * F * S (F = G * polar/2), the
+count OpenMOC uses in its timer report (src/Solver.cpp:1901).  L2 is flushed
+(a 2 x L2 buffer is overwritten) before every timed step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times OpenMOC's CPU path on the host cores through the C
+restatement in oracle/ (OpenMOC itself cannot be built on the GPU host),
+with every host thread, on the same problem.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "17x17 pin lattice, 70 groups, 64 azimuthal, 0.05 cm, TY-6 (3 polar), reflective"
+METRIC = "segment*group*polar integrations/s"
+FLOPS_PER_INTEGRATION = 30   # FP32 flops of one integration (FMA = 2)
+
+
+def env_rank():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def algorithmic_bytes(p):
+    """Compulsory HBM bytes of one sweep: packed segments read once (8 B),
+    per-track offsets/links/flags (16 B), angular flux in and out for both
+    directions (16 B per track and flux value), sources read and tallies
+    written (8 B per FSR and group)."""
+    F = p.fluxes_per_track
+    return (8 * p.num_segments + 16 * p.num_tracks + 16 * p.num_tracks * F
+            + 8 * p.num_fsrs * p.num_groups)
+
+
+class Clocks:
+    """nvidia-smi clock / throttle samples during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "_work", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        os.remove(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r)
+                          if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows),
+                "sm_max_mhz": max(r[1] for r in rows), "reasons": reasons,
+                "samples": len(rows)}
+
+
+def build_problem():
+    from openmoc_gb300 import lattice
+    return lattice.assembly_17x17()
+
+
+def cpu_reference_rate(p, iters, threads):
+    """Integrations/s of the oracle's source iteration on the host cores."""
+    from oracle.oracle import Oracle
+    o = Oracle(p, "f32", num_threads=threads)
+    o.keff = 1.0
+    o.phi[:] = 1.0
+    o.normalize()
+    o.store()
+    t0 = time.perf_counter()
+    for i in range(iters):
+        o.compute_sources(i)
+        o.sweep()
+        o.add_source()
+        o.compute_keff()
+        o.normalize()
+        o.residual_of(1)
+        o.store()
+    dt = time.perf_counter() - t0
+    return p.integrations_per_sweep * iters / dt, dt
+
+
+def run_reference(args):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return
+    p = build_problem()
+    threads = os.cpu_count() or 1
+    rates = []
+    for _ in range(args.warmup):
+        cpu_reference_rate(p, 1, threads)
+    t_all = time.perf_counter()
+    for _ in range(args.steps):
+        r, _ = cpu_reference_rate(p, 1, threads)
+        rates.append(r)
+    elapsed = time.perf_counter() - t_all
+    value = float(np.mean(rates))
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value,
+        "unit": "integrations/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded cross sections, generated tracks)",
+        "config": {"workload": WORKLOAD, "fsrs": p.num_fsrs, "tracks": p.num_tracks,
+                   "segments": p.num_segments, "integrations_per_step": p.integrations_per_sweep},
+        "cpu_baseline": {"value": value, "unit": "integrations/s", "cores": threads,
+                         "kind": "port",
+                         "sample": f"{args.steps} full source iterations of the workload "
+                                   "(oracle/moc_oracle.c, OpenMP, FP32)"},
+        "e2e": {"value": value, "unit": "integrations/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def run_gpu(args):
+    import torch
+    rank, world, local = env_rank()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from openmoc_gb300 import GB300Solver
+    from openmoc_gb300.solver import FISSION_SOURCE
+
+    p = build_problem()
+    peaks, peak_kind = load_peaks()
+    s = GB300Solver(p, device=local)
+    lps, slots = s.getSweepShape()
+    launches0 = s.getLaunchCount()
+    # warm-up (also JIT-free: the library is ahead-of-time sm_103a code)
+    s.benchIterations(max(args.warmup, 3), FISSION_SOURCE, True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches_before = s.getLaunchCount()
+    with Clocks(local) as clk:
+        t_wall = time.perf_counter()
+        step_ms, sweep_ms = s.benchIterations(args.steps, FISSION_SOURCE, True)
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall
+    gpu_launches = s.getLaunchCount() - launches_before
+    clocks = clk.summary()
+    total_ms = float(np.sum(step_ms))
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+        dist.barrier()
+    ms_per_step = total_ms / args.steps
+    ints = p.integrations_per_sweep
+    value = world * ints * args.steps / (total_ms * 1e-3)
+
+    # roofline of the dominant kernel (the sweep)
+    sweep_avg = float(np.mean(sweep_ms))
+    nbytes = algorithmic_bytes(p)
+    achieved = nbytes / (sweep_avg * 1e-3) / 1e9
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "sweep_traffic.json")
+    if os.path.exists(tfile):
+        with open(tfile) as f:
+            traffic = json.load(f).get("dram_bytes_per_launch")
+    sm_mhz = clocks.get("sm_mhz") or float(peaks.get("sm_max_mhz", 2070.0))
+    props = torch.cuda.get_device_properties(local)
+    fp32_peak = props.multi_processor_count * 128 * 2 * sm_mhz * 1e6 / 1e12
+    fp32_achieved = ints * FLOPS_PER_INTEGRATION / (sweep_avg * 1e-3) / 1e12
+
+    # end to end through the public API: host buffers (pinned), upload,
+    # 20 iterations, fluxes back
+    e2e = None
+    if args.e2e_iters > 0:
+        e2e = end_to_end(p, args, local, torch)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        r, dt = cpu_reference_rate(p, args.cpu_iters, threads)
+        cpu = {"value": r, "unit": "integrations/s", "cores": threads, "kind": "port",
+               "sample": f"{args.cpu_iters} full source iterations of the workload "
+                         f"({dt:.1f} s, oracle/moc_oracle.c, OpenMP, FP32)"}
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": "integrations/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded cross sections, generated tracks)",
+            "config": {"workload": WORKLOAD, "fsrs": p.num_fsrs, "tracks": p.num_tracks,
+                       "segments": p.num_segments, "groups": p.num_groups,
+                       "integrations_per_step": ints, "l2": "flushed before every step",
+                       "sweep_shape": {"lanes_per_track_direction": lps,
+                                       "groups_per_lane": slots},
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+            "sweep_ms_per_step": sweep_avg,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
+                         "peak_source": f"{peak_kind} hbm_gbs",
+                         "algorithmic_bytes_per_launch": nbytes,
+                         "binding": {"bound": "fp32", "achieved": fp32_achieved,
+                                     "peak": fp32_peak, "unit": "TFLOP/s",
+                                     "frac": fp32_achieved / fp32_peak,
+                                     "flops_per_integration": FLOPS_PER_INTEGRATION}},
+            "clocks": clocks,
+            "gpu_launches": gpu_launches,
+            "wall_s": t_wall,
+        }
+        if e2e:
+            out["e2e"] = e2e
+        if cpu:
+            out["cpu_baseline"] = cpu
+        print(json.dumps(out), flush=True)
+    s.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def end_to_end(p, args, device, torch):
+    """The metric through GB300Solver: per step, upload the problem from
+    pinned host memory, run a fixed number of iterations, copy the fluxes
+    back."""
+    from openmoc_gb300 import GB300Solver, Problem
+    pinned = {}
+    h2d = 0
+    for k in ("seg_len", "seg_fsr", "seg_off", "track_ang", "next", "flags", "weights",
+              "inv_sin", "sigma_t", "sigma_s", "nu_sigma_f", "chi", "fsr_mat", "fsr_vol"):
+        a = getattr(p, k)
+        t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True)
+        t.numpy()[:] = a.view(np.uint8)
+        pinned[k] = (t, t.numpy().view(a.dtype))
+        h2d += a.nbytes
+    q = Problem(**{f: getattr(p, f) for f in p.__dataclass_fields__})
+    for k, (_, arr) in pinned.items():
+        setattr(q, k, arr)
+    d2h = p.num_fsrs * p.num_groups * 4
+    times = []
+    for i in range(args.e2e_steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s = GB300Solver(q, device=device)
+        s.setConvergenceThreshold(1e-30)
+        s.computeEigenvalue(args.e2e_iters)
+        flux = s.getFluxes()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        s.close()
+        if i > 0:
+            times.append(dt)
+        assert np.isfinite(flux).all()
+    t = float(np.mean(times))
+    return {"value": p.integrations_per_sweep * args.e2e_iters / t, "unit": "integrations/s",
+            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "iterations_per_step": args.e2e_iters, "seconds_per_step": t}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--e2e-iters", type=int, default=20)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-iters", type=int, default=3)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -194,6 +194,16 @@ int moc_set_old_fluxes(moc_ctx* ctx, const float* in, int64_t n);
 int moc_get_start_flux(moc_ctx* ctx, float* out, int64_t n);
 int moc_set_start_flux(moc_ctx* ctx, const float* in, int64_t n);
 
+/** Measurement: `steps` eigenvalue iterations from the initial flux guess
+ *  with the convergence exit disabled; step_ms[i] / sweep_ms[i] receive the
+ *  CUDA-event time of iteration i and of its transport sweep.  With
+ *  flush_l2 != 0 a buffer twice the L2 size is overwritten before each
+ *  iteration, outside the timed interval.  Plays the role of the "Transport
+ *  Sweep" timer split of Solver::printTimerReport (src/Solver.cpp:
+ *  1802-1970). */
+int moc_bench_iterations(moc_ctx* ctx, int steps, int res_type, int flush_l2,
+                         double* step_ms, double* sweep_ms);
+
 /** Number of CUDA kernels this library launched on the context so far. */
 int moc_get_launch_count(moc_ctx* ctx, int64_t* launches);
 

@@ -1,0 +1,65 @@
+/**
+ * @file openmoc_gb300_lattice.h
+ * @brief Workload producer for hosts without OpenMOC: 2D tracks and
+ *        segments of square pin-cell lattices, laid down and ray-traced the
+ *        way OpenMOC's TrackGenerator and Geometry do for that geometry
+ *        family (src/TrackGenerator.cpp:950-1222, src/Geometry.cpp:
+ *        2085-2230, src/Cell.cpp:1325-1590), plus seeded synthetic
+ *        cross sections.  Output arrays use the layout of openmoc_gb300.h.
+ *        Every function returns 0 on success, -1 on error
+ *        (moc_lattice_last_error gives the text).
+ */
+#ifndef OPENMOC_GB300_LATTICE_H_
+#define OPENMOC_GB300_LATTICE_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct moc_lattice moc_lattice;
+
+typedef struct {
+  int32_t nx, ny;          /* pin cells along x and y */
+  double pitch;            /* cm */
+  double pin_radius;       /* cm */
+  int32_t fuel_rings;      /* equal-area rings inside the pin */
+  int32_t fuel_sectors;    /* sectors inside the pin (0: none) */
+  int32_t mod_sectors;     /* sectors of the moderator around the pin */
+  int32_t bc[4];           /* xmin, xmax, ymin, ymax: 0 vacuum, 1 reflective */
+  int32_t num_azim;        /* multiple of 4 */
+  double spacing;          /* cm */
+  int32_t num_polar;       /* 2, 4 or 6 (Tabuchi-Yamamoto) */
+  int32_t moderator_material;
+  int32_t num_threads;     /* 0: OpenMP default */
+  const int32_t* pin_material; /* [ny*nx] material inside each pin; row 0 is
+                                  the top row, as Lattice::setUniverses
+                                  takes it (src/Universe.cpp:1604-1616) */
+} moc_lattice_spec;
+
+const char* moc_lattice_last_error(void);
+/** TrackGenerator::generateTracks for a pin lattice (2D, explicit). */
+int moc_lattice_generate(const moc_lattice_spec* spec, moc_lattice** out);
+int moc_lattice_sizes(moc_lattice* lat, int64_t* num_fsrs,
+                      int64_t* num_tracks, int64_t* num_segments,
+                      int32_t* num_angles, int32_t* num_polar_half,
+                      int32_t* num_materials);
+int moc_lattice_export(moc_lattice* lat, float* seg_len, int32_t* seg_fsr,
+                       int64_t* seg_off, int32_t* track_ang, int64_t* next,
+                       uint8_t* flags, float* weights, float* inv_sin,
+                       int32_t* fsr_mat, float* fsr_vol);
+int moc_lattice_destroy(moc_lattice* lat);
+
+/** Seeded synthetic multigroup data (sigma_s origin-major [orig*G+dest]),
+ *  optionally multiplied by lognormal(0, perturb_sigma) factors per group. */
+int moc_synthetic_xs(uint64_t seed, int32_t num_groups, int32_t fissile,
+                     uint64_t perturb_seed, double perturb_sigma,
+                     double* sigma_t, double* sigma_s, double* nu_sigma_f,
+                     double* sigma_f, double* chi);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -20,7 +20,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libopenmoc_gb300.so")
 
-SOURCES = ["sweep.cu", "solver_kernels.cu", "moc_api.cu"]
+SOURCES = ["sweep.cu", "solver_kernels.cu", "moc_api.cu", "lattice.cpp"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -60,10 +60,11 @@ def build(verbose: bool = False, ptxas_verbose: bool = False, force: bool = Fals
     jobs = []
     for s in SOURCES:
         src = os.path.join(CSRC, s)
-        obj = os.path.join(OUT, s.replace(".cu", ".o"))
+        obj = os.path.join(OUT, os.path.splitext(s)[0] + ".o")
         objs.append(obj)
         if force or _stale(obj, src):
-            jobs.append([cc] + _flags(ptxas_verbose) + ["-c", src, "-o", obj])
+            extra = ["-Xcompiler", "-fopenmp"] if s.endswith(".cpp") else []
+            jobs.append([cc] + _flags(ptxas_verbose) + extra + ["-c", src, "-o", obj])
 
     def run(cmd):
         if verbose:
@@ -79,7 +80,7 @@ def build(verbose: bool = False, ptxas_verbose: bool = False, force: bool = Fals
         list(ex.map(run, jobs))
     if jobs or not os.path.exists(LIB):
         tmp = LIB + ".tmp"
-        run([cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"])
+        run([cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lgomp"])
         os.replace(tmp, LIB)
     return LIB
 

@@ -38,21 +38,6 @@ namespace {
 
 thread_local std::string g_lat_error;
 
-struct Spec {
-  int32_t nx, ny;
-  double pitch;
-  double pin_radius;
-  int32_t fuel_rings;
-  int32_t fuel_sectors;
-  int32_t mod_sectors;
-  int32_t bc[4];          // xmin, xmax, ymin, ymax: 0 vacuum, 1 reflective
-  int32_t num_azim;       // multiple of 4
-  double spacing;
-  int32_t num_polar;      // 2, 4 or 6
-  int32_t moderator_material;
-  int32_t num_threads;
-};
-
 struct Track {
   double x0, y0, x1, y1, phi;
   int a;
@@ -91,7 +76,6 @@ struct moc_lattice {
   std::vector<float> weights, inv_sin;
   std::vector<int32_t> fsr_mat;
   std::vector<float> fsr_vol;
-  std::vector<double> fsr_cx, fsr_cy;   // a point inside each FSR
 };
 
 const char* moc_lattice_last_error(void) { return g_lat_error.c_str(); }
@@ -112,7 +96,6 @@ struct Classifier {
   int rings;
   int fuel_sectors, mod_sectors;
   std::vector<double> r2;   // squared ring radii, outer to inner
-  double beta_f, beta_m;    // first sector boundary angle
 
   int sector_of(double ang, int n) const {
     // sector boundaries at k*2pi/n - pi/4 (Cell::sectorize planes at
@@ -373,18 +356,18 @@ extern "C" int moc_lattice_generate(const moc_lattice_spec* sp,
         const double qx = cx - tr.x0, qy = cy - tr.y0;
         const double tt = (qx * vy - qy * vx) / den;
         const double ss = (qx * uy - qy * ux) / den;
-        if (ss > 0 && tt > ta && tt < tb) pts.push_back(tt);
+        // ss >= 0: a ray through the pin centre is cut there, where every
+        // sector plane meets
+        if (ss > -1e-12 && tt > ta && tt < tb) pts.push_back(tt);
       }
       pts.push_back(tb);
       std::sort(pts.begin(), pts.end());
       const uint64_t cell = (uint64_t) ((int64_t) (s.ny - 1 - cj) * s.nx + ci);
       for (size_t k = 0; k + 1 < pts.size(); k++) {
         const double l = pts[k + 1] - pts[k];
-        if (l <= kTinyMove) {
-          // below the reference's surface nudge: absorbed by its neighbour
-          if (!out_len.empty()) out_len.back() += (float) 0;
-          continue;
-        }
+        // sub-intervals below the reference's surface nudge do not form
+        // segments of their own
+        if (l <= kTinyMove) continue;
         const double mm = 0.5 * (pts[k] + pts[k + 1]);
         const uint32_t rs =
             cls.classify(tr.x0 + mm * ux - cx, tr.y0 + mm * uy - cy);
@@ -432,8 +415,6 @@ extern "C" int moc_lattice_generate(const moc_lattice_spec* sp,
   L->R = R;
   L->fsr_mat.resize(R);
   L->fsr_vol.assign(R, 0.0f);
-  L->fsr_cx.resize(R);
-  L->fsr_cy.resize(R);
   int32_t maxmat = s.moderator_material;
   for (int64_t r = 0; r < R; r++) {
     const uint64_t key = keys[r];
@@ -492,5 +473,28 @@ extern "C" int moc_lattice_export(moc_lattice* L, float* seg_len,
 
 extern "C" int moc_lattice_destroy(moc_lattice* L) {
   delete L;
+  return 0;
+}
+
+// ---- seeded synthetic cross sections (openmoc_gb300/csrc/synthetic_xs.h) --
+#include "synthetic_xs.h"
+
+extern "C" int moc_synthetic_xs(uint64_t seed, int32_t num_groups,
+                                int32_t fissile, uint64_t perturb_seed,
+                                double perturb_sigma, double* sigma_t,
+                                double* sigma_s, double* nu_sigma_f,
+                                double* sigma_f, double* chi) {
+  if (num_groups < 1 || !sigma_t || !sigma_s || !nu_sigma_f || !sigma_f || !chi)
+    return lat_fail("bad synthetic cross-section request");
+  openmoc_gb300::MaterialXS m =
+      openmoc_gb300::make_synthetic_xs(seed, num_groups, fissile != 0);
+  if (perturb_sigma > 0.0)
+    m = openmoc_gb300::perturb_xs(m, perturb_seed, perturb_sigma);
+  const int G = num_groups;
+  std::memcpy(sigma_t, m.sigma_t.data(), 8 * G);
+  std::memcpy(sigma_s, m.sigma_s.data(), 8 * (size_t) G * G);
+  std::memcpy(nu_sigma_f, m.nu_sigma_f.data(), 8 * G);
+  std::memcpy(sigma_f, m.sigma_f.data(), 8 * G);
+  std::memcpy(chi, m.chi.data(), 8 * G);
   return 0;
 }

@@ -103,6 +103,8 @@ struct moc_ctx {
   float* psi[2] = {nullptr, nullptr};
   float* exp_table = nullptr;
   double* rates = nullptr;
+  float* flush = nullptr;             // L2 flush buffer (measurement only)
+  int64_t flush_n = 0;
   moc::DevScalars* sc = nullptr;      // device
   moc::DevScalars* hsc = nullptr;     // pinned host mirror
 
@@ -464,6 +466,7 @@ int moc_destroy(moc_ctx* c) {
   dfree(c->psi[1]);
   dfree(c->exp_table);
   dfree(c->rates);
+  dfree(c->flush);
   dfree(c->sc);
   if (c->hsc) cudaFreeHost(c->hsc);
   for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
@@ -789,6 +792,63 @@ int moc_compute_flux(moc_ctx* c, int max_iters, int only_fixed_source) {
   MOC_TRY(run_iterations(c, moc::kModeFlux, MOC_SCALAR_FLUX));
   c->num_iterations =
       c->hsc->converged ? c->hsc->iteration - 1 : max_iters;
+  return MOC_OK;
+}
+
+// Fixed-count eigenvalue iterations for measurement: the loop body of
+// computeEigenvalue with the convergence exit disabled, each iteration
+// bracketed by CUDA events on the solver's stream (and its sweep by a second
+// pair).  With flush_l2, a buffer twice the L2 size is overwritten before
+// every iteration, outside the timed interval.
+int moc_bench_iterations(moc_ctx* c, int steps, int res_type, int flush_l2,
+                         double* step_ms, double* sweep_ms) {
+  MOC_TRY(ready(c));
+  MOC_CHECK(steps >= 1 && step_ms && sweep_ms, MOC_ERR_ARG, "bad arguments");
+  if (flush_l2 && !c->flush) {
+    int l2 = 0;
+    MOC_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize,
+                                    c->d.device));
+    c->flush_n = std::max<int64_t>(2 * (int64_t) l2 / 4, 1 << 20);
+    MOC_TRY(dalloc(&c->flush, c->flush_n));
+  }
+  // initial state as computeEigenvalue's first iteration sees it
+  MOC_TRY(zero_track_fluxes(c));
+  MOC_TRY(begin_solve(c, moc::kModeEigen, 1 << 30, res_type, 1.0));
+  c->hsc->threshold = -1.0;  // never converged: every iteration runs
+  MOC_TRY(push(c));
+  moc::SolverArgs a = solver_args(c, 1);
+  moc::launch_fill(c->phi, num_flux(c), 1.0f, c->stream);
+  moc::launch_fission_rate(a, 1, c->stream);
+  moc::launch_scale_phi(a, c->stream);
+  MOC_CUDA(cudaMemcpyAsync(c->phi_old, c->phi, 4 * num_flux(c),
+                           cudaMemcpyDeviceToDevice, c->stream));
+  std::vector<cudaEvent_t> ev(4 * steps);
+  for (auto& e : ev) MOC_CUDA(cudaEventCreate(&e));
+  for (int i = 0; i < steps; i++) {
+    if (flush_l2) moc::launch_fill(c->flush, c->flush_n, (float) i, c->stream);
+    MOC_CUDA(cudaEventRecord(ev[4 * i], c->stream));
+    moc::launch_compute_sources(a, -1, 1, c->stream);
+    MOC_CUDA(cudaEventRecord(ev[4 * i + 1], c->stream));
+    MOC_TRY(enqueue_sweep(c, 1, false, 0));
+    MOC_CUDA(cudaEventRecord(ev[4 * i + 2], c->stream));
+    moc::launch_add_source(a, 1, c->stream);
+    moc::launch_residual(a, res_type, 1, 1, 1, c->stream);
+    MOC_CUDA(cudaEventRecord(ev[4 * i + 3], c->stream));
+    c->launches += 3;
+  }
+  MOC_CUDA(cudaGetLastError());
+  MOC_CUDA(cudaStreamSynchronize(c->stream));
+  for (int i = 0; i < steps; i++) {
+    float t = 0.f, s = 0.f;
+    MOC_CUDA(cudaEventElapsedTime(&t, ev[4 * i], ev[4 * i + 3]));
+    MOC_CUDA(cudaEventElapsedTime(&s, ev[4 * i + 1], ev[4 * i + 2]));
+    step_ms[i] = t;
+    sweep_ms[i] = s;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  MOC_TRY(pull(c));
+  c->keff = c->hsc->keff;
+  c->num_iterations = c->hsc->iteration;
   return MOC_OK;
 }
 

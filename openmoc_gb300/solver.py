@@ -283,6 +283,18 @@ class GB300Solver:
         self._call("moc_get_launch_count", C.byref(n))
         return n.value
 
+    def benchIterations(self, steps: int, res_type: int = FISSION_SOURCE,
+                        flush_l2: bool = True):
+        """Times ``steps`` eigenvalue iterations (convergence exit off) with
+        CUDA events on the solver's stream; returns (step_ms, sweep_ms)
+        arrays."""
+        self._need_ctx()
+        st = np.zeros(steps, np.float64)
+        sw = np.zeros(steps, np.float64)
+        self._call("moc_bench_iterations", int(steps), int(res_type), int(bool(flush_l2)),
+                   _ptr(st), _ptr(sw))
+        return st, sw
+
     def getFluxes(self) -> np.ndarray:
         """All scalar fluxes as an [R, G] array (Solver::getFluxes)."""
         self._need_ctx()
