@@ -39,6 +39,8 @@ def _flags(ptxas_verbose: bool):
                 "-I", os.path.join(ROOT, "include"), "--expt-relaxed-constexpr"]
     if ptxas_verbose:
         f += ["-Xptxas", "-v"]
+    # extra nvcc flags (e.g. -DMOC_SWEEP_MIN_BLOCKS=6) for tuning builds
+    f += os.environ.get("MOC_NVCC_FLAGS", "").split()
     return f
 
 

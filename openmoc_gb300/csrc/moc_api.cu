@@ -108,6 +108,7 @@ struct moc_ctx {
   moc::DevScalars* sc = nullptr;      // device
   moc::DevScalars* hsc = nullptr;     // pinned host mirror
 
+  int mat_packed = 0;
   bool have_tracks = false, have_quad = false, have_mats = false,
        have_fsrs = false;
   double threshold = 1e-5;
@@ -160,6 +161,7 @@ moc::SweepArgs sweep_args(moc_ctx* c, int check_done) {
   a.num_groups = c->d.num_groups;
   a.num_materials = c->d.num_materials;
   a.lps = c->lps;
+  a.mat_packed = c->mat_packed;
   a.check_done = check_done;
   return a;
 }
@@ -344,6 +346,22 @@ int run_iterations(moc_ctx* c, int kind, int res_type) {
   }
   c->keff = c->hsc->keff;
   c->residual = c->hsc->residual;
+  return MOC_OK;
+}
+
+// Once tracks and FSR materials are both on the device, fold each
+// segment's material into its FSR word so the sweep needs no dependent
+// material lookup.
+int pack_materials(moc_ctx* c) {
+  c->mat_packed = 0;
+  if (!(c->have_tracks && c->have_fsrs)) return MOC_OK;
+  if (c->d.num_fsrs >= (1LL << 24) || c->d.num_materials > 256) return MOC_OK;
+  moc::launch_pack_materials(c->segs, c->d.num_segments, c->fsr_mat,
+                             c->stream);
+  c->launches++;
+  MOC_CUDA(cudaGetLastError());
+  MOC_CUDA(cudaStreamSynchronize(c->stream));
+  c->mat_packed = 1;
   return MOC_OK;
 }
 
@@ -541,6 +559,7 @@ int moc_upload_tracks(moc_ctx* c, const float* seg_len, const int32_t* seg_fsr,
                       cudaMemcpyHostToDevice));
   MOC_CUDA(cudaMemcpy(c->flags, flags, T, cudaMemcpyHostToDevice));
   c->have_tracks = true;
+  MOC_TRY(pack_materials(c));
   return MOC_OK;
 }
 
@@ -662,6 +681,7 @@ int moc_upload_fsrs(moc_ctx* c, const int32_t* fsr_mat, const float* fsr_vol) {
   c->hsc->num_fissionable = c->num_fissionable;
   MOC_TRY(push(c));
   c->have_fsrs = true;
+  MOC_TRY(pack_materials(c));
   return MOC_OK;
 }
 

@@ -18,6 +18,10 @@ constexpr float kExpTableH = 1.0f / 16.0f;
 constexpr int kMaxSlots = 9;
 constexpr int kMaxPolarHalf = 5;
 constexpr int kSweepThreads = 128;
+#ifndef MOC_SWEEP_MIN_BLOCKS
+#define MOC_SWEEP_MIN_BLOCKS 1
+#endif
+constexpr int kSweepMinBlocks = MOC_SWEEP_MIN_BLOCKS;
 
 enum ExpKind { kExpTable = 0, kExpIntrinsic = 1 };
 
@@ -71,6 +75,7 @@ struct SweepArgs {
   int num_materials;
   int lps;                   // lanes per track direction (1..32, power of 2)
   int check_done;            // return at once if sc->done is set
+  int mat_packed;            // segs[].y = fsr | material << 24
 };
 
 struct SolverArgs {
@@ -102,6 +107,10 @@ struct SolverArgs {
 bool launch_sweep(const SweepArgs& a, int polar_half, int slots, int exp_kind,
                   cudaStream_t stream);
 int sweep_max_slots(int polar_half);
+// Writes each segment's material into the top 8 bits of its FSR word
+// (valid when num_fsrs < 2^24 and num_materials <= 256); idempotent.
+void launch_pack_materials(int2* segs, int64_t num_segments,
+                           const int32_t* fsr_mat, cudaStream_t stream);
 
 // ---- launchers (solver_kernels.cu) ---------------------------------------
 // iteration < 0 reads the device iteration counter; fused also zeroes phi

@@ -70,7 +70,7 @@ struct AttenIntrinsic {
 };
 
 template <int PH, int SLOTS, int EXPK>
-__global__ void __launch_bounds__(kSweepThreads)
+__global__ void __launch_bounds__(kSweepThreads, kSweepMinBlocks)
 sweep_kernel(const SweepArgs a) {
   extern __shared__ float smem[];
   DevScalars* sc = a.sc;
@@ -124,21 +124,73 @@ sweep_kernel(const SweepArgs a) {
         psi[j][p] = (g < G) ? pin[p * G + g] * scale : 0.0f;
     }
 
+    // Segment stream, software-pipelined.  The lps lanes of a stream load
+    // lps consecutive segments with one coalesced access (a "chunk", one
+    // segment per lane) a whole chunk ahead of use; segment k reaches every
+    // lane of the stream by a shuffle from lane k % lps.  The sources of
+    // segment k+1 are gathered while segment k is integrated.
     const int2* seg = a.segs + b;
+    const unsigned gmask =
+        (lps == 32) ? 0xffffffffu
+                    : (((1u << lps) - 1u) << (lane & ~(lps - 1)));
+    auto fetch = [&](int kk) -> int2 {
+      return (kk < n) ? __ldg(seg + (dir ? n - 1 - kk : kk))
+                      : make_int2(0, 0);
+    };
+    auto unpack = [&](int2 sg, float& len, int& fsr, int& mat) {
+      len = __int_as_float(sg.x);
+      if (a.mat_packed) {
+        fsr = sg.y & 0xFFFFFF;
+        mat = (int) ((unsigned) sg.y >> 24);
+      } else {
+        fsr = sg.y;
+        mat = __ldg(a.fsr_mat + fsr);
+      }
+    };
+    int2 chunk = fetch(sub);
+    int2 chunk_next = fetch(lps + sub);
+    int2 sg;
+    sg.x = __shfl_sync(gmask, chunk.x, 0, lps);
+    sg.y = __shfl_sync(gmask, chunk.y, 0, lps);
+    float len;
+    int fsr, mat;
+    unpack(sg, len, fsr, mat);
+    float q[SLOTS];
+#pragma unroll
+    for (int j = 0; j < SLOTS; j++) {
+      const int g = sub + j * lps;
+      q[j] = (g < G && n > 0) ? __ldg(a.qt + (int64_t) fsr * G + g) : 0.0f;
+    }
     for (int k = 0; k < n; k++) {
-      const int2 sg = __ldg(seg + (dir ? n - 1 - k : k));
-      const float len = __int_as_float(sg.x);
-      const int fsr = sg.y;
-      const int mat = __ldg(a.fsr_mat + fsr);
+      // next segment: rotate chunks at chunk boundaries
+      const int kn = k + 1;
+      const int src = kn & (lps - 1);
+      if (src == 0) {
+        chunk = chunk_next;
+        chunk_next = fetch(kn + lps + sub);
+      }
+      int2 sgn;
+      sgn.x = __shfl_sync(gmask, chunk.x, src, lps);
+      sgn.y = __shfl_sync(gmask, chunk.y, src, lps);
+      float len_n;
+      int fsr_n, mat_n;
+      unpack(sgn, len_n, fsr_n, mat_n);
+      float qn[SLOTS];
+#pragma unroll
+      for (int j = 0; j < SLOTS; j++) {
+        const int g = sub + j * lps;
+        qn[j] = (g < G && kn < n) ? __ldg(a.qt + (int64_t) fsr_n * G + g)
+                                  : 0.0f;
+      }
+
       const float* st = s_st + mat * G;
-      const float* q = a.qt + (int64_t) fsr * G;
       float* ph = a.phi + (int64_t) fsr * G;
 #pragma unroll
       for (int j = 0; j < SLOTS; j++) {
         const int g = sub + j * lps;
         if (g < G) {
           const float tau = st[g] * len;
-          const float qv = __ldg(q + g);
+          const float qv = q[j];
           float tally = 0.0f;
 #pragma unroll
           for (int p = 0; p < PH; p++) {
@@ -152,6 +204,11 @@ sweep_kernel(const SweepArgs a) {
           atomicAdd(ph + g, tally);
         }
       }
+      len = len_n;
+      fsr = fsr_n;
+      mat = mat_n;
+#pragma unroll
+      for (int j = 0; j < SLOTS; j++) q[j] = qn[j];
     }
 
     // boundary-flux transfer to the connecting track, fused into the sweep
@@ -230,6 +287,24 @@ static bool dispatch_ph(const SweepArgs& a, int ph, int slots,
     case 3: return dispatch_slots<3, EXPK>(a, slots, s);
     default: return false;
   }
+}
+
+__global__ void pack_materials_kernel(int2* segs, int64_t n,
+                                      const int32_t* fsr_mat) {
+  for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t) gridDim.x * blockDim.x) {
+    const int fsr = segs[i].y & 0xFFFFFF;
+    segs[i].y = fsr | (fsr_mat[fsr] << 24);
+  }
+}
+
+void launch_pack_materials(int2* segs, int64_t num_segments,
+                           const int32_t* fsr_mat, cudaStream_t stream) {
+  if (num_segments == 0) return;
+  int64_t blocks = (num_segments + 255) / 256;
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  pack_materials_kernel<<<(unsigned) blocks, 256, 0, stream>>>(
+      segs, num_segments, fsr_mat);
 }
 
 int sweep_max_slots(int polar_half) {
