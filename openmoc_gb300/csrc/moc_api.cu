@@ -225,13 +225,13 @@ double lane_use(int G, int lps, int slots) {
 // groups per lane.
 void pick_shape(int G, int* lps_out, int* slots_out) {
   double best = 0.0;
-  for (int lps = 1; lps <= 32; lps *= 2) {
+  for (int lps = 2; lps <= 32; lps *= 2) {
     int slots = (G + lps - 1) / lps;
     if (slots > moc::kMaxSlots) continue;
     best = std::max(best, lane_use(G, lps, slots));
   }
   int chosen = 32;
-  for (int lps = 32; lps >= 1; lps /= 2) {
+  for (int lps = 32; lps >= 2; lps /= 2) {
     int slots = (G + lps - 1) / lps;
     if (slots > moc::kMaxSlots) continue;
     if (lane_use(G, lps, slots) >= 0.95 * best) {
@@ -365,10 +365,16 @@ int pack_materials(moc_ctx* c) {
   return MOC_OK;
 }
 
+// Nodes of the attenuation table: 1 - exp(-x_i) then exp(-x_i), both from
+// double precision, x_i = i * h.
 void build_exp_table(std::vector<float>& t) {
-  t.resize(moc::kExpTableSize);
-  for (int i = 0; i < moc::kExpTableSize; i++)
-    t[i] = (float) (-std::expm1(-(double) i * (double) moc::kExpTableH));
+  const int n = moc::kExpTableSize;
+  t.resize(2 * n);
+  for (int i = 0; i < n; i++) {
+    const double x = (double) i * (double) moc::kExpTableH;
+    t[i] = (float) (-std::expm1(-x));
+    t[n + i] = (float) std::exp(-x);
+  }
 }
 
 }  // namespace
@@ -427,7 +433,7 @@ int moc_create(const moc_dims* dims, moc_ctx** out) {
   if ((st = dalloc(&c->phi, R * G)) || (st = dalloc(&c->phi_old, R * G)) ||
       (st = dalloc(&c->qt, R * G)) || (st = dalloc(&c->psi[0], npsi)) ||
       (st = dalloc(&c->psi[1], npsi)) ||
-      (st = dalloc(&c->exp_table, moc::kExpTableSize)) ||
+      (st = dalloc(&c->exp_table, 2 * moc::kExpTableSize)) ||
       (st = dalloc(&c->rates, R)) || (st = dalloc(&c->sc, 1)))
     return bail(st);
   if (cudaMallocHost((void**) &c->hsc, sizeof(moc::DevScalars)) !=
@@ -723,8 +729,8 @@ int moc_set_sweep_shape(moc_ctx* c, int lps, int slots) {
     c->slots = 0;
     return MOC_OK;
   }
-  MOC_CHECK(lps >= 1 && lps <= 32 && (lps & (lps - 1)) == 0, MOC_ERR_ARG,
-            "lanes per track direction must be a power of two <= 32");
+  MOC_CHECK(moc::sweep_lps_supported(lps), MOC_ERR_ARG,
+            "lanes per track direction must be 2, 4, 8, 16 or 32");
   MOC_CHECK(slots >= 1 && slots <= moc::kMaxSlots &&
                 (int64_t) lps * slots >= c->d.num_groups,
             MOC_ERR_ARG, "lanes x groups-per-lane must cover every group");

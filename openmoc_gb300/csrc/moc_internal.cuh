@@ -18,10 +18,6 @@ constexpr float kExpTableH = 1.0f / 16.0f;
 constexpr int kMaxSlots = 9;
 constexpr int kMaxPolarHalf = 5;
 constexpr int kSweepThreads = 128;
-#ifndef MOC_SWEEP_MIN_BLOCKS
-#define MOC_SWEEP_MIN_BLOCKS 1
-#endif
-constexpr int kSweepMinBlocks = MOC_SWEEP_MIN_BLOCKS;
 
 enum ExpKind { kExpTable = 0, kExpIntrinsic = 1 };
 
@@ -66,7 +62,7 @@ struct SweepArgs {
   const float* sigma_t;      // [M][G]
   const int32_t* fsr_mat;    // [R]
   const float* qt;           // [R][G] reduced source / sigma_t
-  const float* exp_table;    // [kExpTableSize]
+  const float* exp_table;    // [2][kExpTableSize]: 1 - exp(-x_i), exp(-x_i)
   float* phi;                // [R][G] accumulated tallies
   float* psi[2];             // [T][2][F] angular-flux buffers
   DevScalars* sc;
@@ -107,6 +103,7 @@ struct SolverArgs {
 bool launch_sweep(const SweepArgs& a, int polar_half, int slots, int exp_kind,
                   cudaStream_t stream);
 int sweep_max_slots(int polar_half);
+bool sweep_lps_supported(int lps);
 // Writes each segment's material into the top 8 bits of its FSR word
 // (valid when num_fsrs < 2^24 and num_materials <= 256); idempotent.
 void launch_pack_materials(int2* segs, int64_t num_segments,

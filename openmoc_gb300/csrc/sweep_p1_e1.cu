@@ -1,0 +1,11 @@
+// Sweep kernel instances for 1 polar value(s) per track direction with
+// the hardware ex2 exponential (see sweep_kernel.cuh).
+#include "sweep_kernel.cuh"
+
+namespace moc {
+
+bool launch_sweep_p1_e1(const SweepArgs& a, int slots, cudaStream_t s) {
+  return dispatch_sweep_lps<1, 1>(a, slots, s);
+}
+
+}  // namespace moc

@@ -1,0 +1,11 @@
+// Sweep kernel instances for 3 polar value(s) per track direction with
+// the shared-memory table exponential (see sweep_kernel.cuh).
+#include "sweep_kernel.cuh"
+
+namespace moc {
+
+bool launch_sweep_p3_e0(const SweepArgs& a, int slots, cudaStream_t s) {
+  return dispatch_sweep_lps<3, 0>(a, slots, s);
+}
+
+}  // namespace moc
