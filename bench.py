@@ -187,8 +187,15 @@ def run_gpu(args):
     p = build_problem()
     peaks, peak_kind = load_peaks()
     s = GB300Solver(p, device=local)
-    lps, slots = s.getSweepShape()
-    launches0 = s.getLaunchCount()
+    if args.shape:
+        # a fixed kernel shape (e.g. to profile one instance)
+        lps, slots, exp_kind = (int(v) for v in args.shape.split(","))
+        s.setSweepShape(lps, slots)
+        (s.useExponentialIntrinsic if exp_kind else s.useExponentialInterpolation)()
+        tuning = []
+    else:
+        lps, slots, exp_kind = s.autotune()
+        tuning = s.getTuningLog()
     # warm-up (also JIT-free: the library is ahead-of-time sm_103a code)
     s.benchIterations(max(args.warmup, 3), FISSION_SOURCE, True)
     if dist:
@@ -252,7 +259,11 @@ def run_gpu(args):
                        "segments": p.num_segments, "groups": p.num_groups,
                        "integrations_per_step": ints, "l2": "flushed before every step",
                        "sweep_shape": {"lanes_per_track_direction": lps,
-                                       "groups_per_lane": slots},
+                                       "groups_per_lane": slots,
+                                       "exponential": ["shared-memory table",
+                                                       "hardware ex2"][exp_kind]},
+                       "autotune_ms": {f"{a}x{b}/{'table' if e == 0 else 'ex2'}": round(t, 4)
+                                       for a, b, e, t in tuning},
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
             "sweep_ms_per_step": sweep_avg,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak,
@@ -325,6 +336,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-iters", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--shape", default="",
+                    help="lanes,groups_per_lane,exp (0 table, 1 ex2) instead of autotuning")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -130,6 +130,19 @@ int moc_set_convergence_threshold(moc_ctx* ctx, double threshold);
  *  Solver::useExponentialInterpolation / useExponentialIntrinsic
  *  (src/Solver.cpp:575-595). */
 int moc_set_exponential(moc_ctx* ctx, int kind);
+int moc_get_exponential(moc_ctx* ctx, int* kind);
+
+/** Autotuner of the sweep kernel: times every lanes-per-track-direction
+ *  shape (and, unless moc_set_exponential fixed it, both exponential
+ *  evaluators) on this context's problem and keeps the fastest.  Runs by
+ *  itself at the first solve unless disabled with moc_set_autotune(ctx, 0)
+ *  or a shape is set with moc_set_sweep_shape; results are cached per
+ *  problem size for the process.  moc_autotune runs it now (and leaves zero
+ *  fluxes behind); moc_get_tuning_log reports every timed candidate. */
+int moc_set_autotune(moc_ctx* ctx, int on);
+int moc_autotune(moc_ctx* ctx, int* lps, int* slots, int* exp_kind);
+int moc_get_tuning_log(moc_ctx* ctx, int* lps, int* slots, int* exp_kind,
+                       float* ms, int capacity, int* count);
 
 /** Sweep kernel shape: lps lanes per track direction (power of two <= 32)
  *  each carrying `slots` energy groups (lps * slots >= G, slots <= 9);

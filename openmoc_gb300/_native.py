@@ -52,6 +52,11 @@ _SIGS = {
     "moc_set_fixed_sources": ([_P, _P], C.c_int),
     "moc_set_convergence_threshold": ([_P, C.c_double], C.c_int),
     "moc_set_exponential": ([_P, C.c_int], C.c_int),
+    "moc_get_exponential": ([_P, C.POINTER(C.c_int)], C.c_int),
+    "moc_set_autotune": ([_P, C.c_int], C.c_int),
+    "moc_autotune": ([_P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)],
+                     C.c_int),
+    "moc_get_tuning_log": ([_P, _P, _P, _P, _P, C.c_int, C.POINTER(C.c_int)], C.c_int),
     "moc_set_sweep_shape": ([_P, C.c_int, C.c_int], C.c_int),
     "moc_get_sweep_shape": ([_P, C.POINTER(C.c_int), C.POINTER(C.c_int)], C.c_int),
     "moc_set_iterations_per_sync": ([_P, C.c_int], C.c_int),

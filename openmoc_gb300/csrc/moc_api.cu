@@ -13,6 +13,9 @@
 #include <cstring>
 #include <numeric>
 #include <string>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "../../include/openmoc_gb300.h"
@@ -68,6 +71,12 @@ void dfree(T*& p) {
 
 }  // namespace
 
+// One timed sweep-kernel configuration of the autotuner.
+struct moc_tune_entry {
+  int lps, slots, exp_kind;
+  float ms;
+};
+
 struct moc_ctx {
   moc_dims d{};
   cudaStream_t stream = nullptr;
@@ -113,6 +122,11 @@ struct moc_ctx {
        have_fsrs = false;
   double threshold = 1e-5;
   int exp_kind = MOC_EXP_TABLE;
+  int exp_user_set = 0;      // evaluator fixed by the caller
+  int shape_user_set = 0;    // kernel shape fixed by the caller
+  int autotune = 1;          // time shapes / evaluators at the first solve
+  bool tuned = false;
+  std::vector<moc_tune_entry> tune_log;
   int lps = 0, slots = 0;
   int num_iterations = 0;
   double keff = 1.0;
@@ -263,6 +277,92 @@ int enqueue_sweep(moc_ctx* c, int check_done, bool timed, int ev_index) {
   c->launches++;
   MOC_CUDA(cudaGetLastError());
   if (timed) MOC_CUDA(cudaEventRecord(c->ev[2 * ev_index + 1], c->stream));
+  return MOC_OK;
+}
+
+// ---- autotuner: sweep kernel shape and exponential evaluator -----------
+// Candidate shapes are every lanes-per-track-direction count with at most
+// kMaxSlots groups per lane and at least half the lanes busy; each is timed
+// on the context's own problem (median of three sweeps after one warm-up).
+// Results are cached per problem size for the process.
+struct TuneKey {
+  int G, Ph, M, exp_fixed, exp_kind;
+  int64_t T, S, R;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(G, Ph, M, exp_fixed, exp_kind, T, S, R) <
+           std::tie(o.G, o.Ph, o.M, o.exp_fixed, o.exp_kind, o.T, o.S, o.R);
+  }
+};
+using TuneVal = moc_tune_entry;
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneVal> g_tune_cache;
+
+int time_sweep(moc_ctx* c, int reps, float* median_ms) {
+  std::vector<float> t;
+  MOC_TRY(enqueue_sweep(c, 0, true, 0));   // warm-up
+  for (int r = 0; r < reps; r++) {
+    MOC_TRY(enqueue_sweep(c, 0, true, r));
+  }
+  MOC_CUDA(cudaStreamSynchronize(c->stream));
+  for (int r = 0; r < reps; r++) {
+    float ms = 0.f;
+    MOC_CUDA(cudaEventElapsedTime(&ms, c->ev[2 * r], c->ev[2 * r + 1]));
+    t.push_back(ms);
+  }
+  std::sort(t.begin(), t.end());
+  *median_ms = t[t.size() / 2];
+  return MOC_OK;
+}
+
+// Leaves sweep tallies and angular-flux buffers in an undefined state: call
+// only before a solve initialises them.
+int autotune_sweep(moc_ctx* c, bool use_cache) {
+  TuneKey key{c->d.num_groups, c->d.num_polar_half, c->d.num_materials,
+              c->exp_user_set, c->exp_user_set ? c->exp_kind : -1,
+              c->d.num_tracks, c->d.num_segments, c->d.num_fsrs};
+  if (use_cache) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) {
+      c->lps = it->second.lps;
+      c->slots = it->second.slots;
+      c->exp_kind = it->second.exp_kind;
+      c->tuned = true;
+      return MOC_OK;
+    }
+  }
+  const int G = c->d.num_groups;
+  std::vector<int> kinds;
+  if (c->exp_user_set) kinds.push_back(c->exp_kind);
+  else kinds = {MOC_EXP_TABLE, MOC_EXP_INTRINSIC};
+  TuneVal best{0, 0, 0, 1e30f};
+  c->tune_log.clear();
+  for (int kind : kinds) {
+    for (int lps = 2; lps <= 32; lps *= 2) {
+      const int slots = (G + lps - 1) / lps;
+      if (slots > moc::kMaxSlots || lane_use(G, lps, slots) < 0.5) continue;
+      c->lps = lps;
+      c->slots = slots;
+      c->exp_kind = kind;
+      float ms = 0.f;
+      MOC_TRY(time_sweep(c, 3, &ms));
+      c->tune_log.push_back({lps, slots, kind, ms});
+      if (ms < best.ms) best = {lps, slots, kind, ms};
+    }
+  }
+  MOC_CHECK(best.lps > 0, MOC_ERR_UNSUPPORTED, "no sweep kernel shape fits");
+  c->lps = best.lps;
+  c->slots = best.slots;
+  c->exp_kind = best.exp_kind;
+  c->tuned = true;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune_cache[key] = best;
+  return MOC_OK;
+}
+
+int maybe_autotune(moc_ctx* c) {
+  if (c->autotune && !c->tuned && !c->shape_user_set)
+    return autotune_sweep(c, true);
   return MOC_OK;
 }
 
@@ -719,6 +819,51 @@ int moc_set_exponential(moc_ctx* c, int kind) {
   MOC_CHECK(kind == MOC_EXP_TABLE || kind == MOC_EXP_INTRINSIC, MOC_ERR_ARG,
             "unknown exponential evaluator");
   c->exp_kind = kind;
+  c->exp_user_set = 1;
+  c->tuned = false;
+  return MOC_OK;
+}
+
+int moc_get_exponential(moc_ctx* c, int* kind) {
+  MOC_CHECK(c && kind, MOC_ERR_ARG, "null argument");
+  *kind = c->exp_kind;
+  return MOC_OK;
+}
+
+int moc_set_autotune(moc_ctx* c, int on) {
+  MOC_CHECK(c, MOC_ERR_ARG, "null context");
+  c->autotune = on ? 1 : 0;
+  if (on) c->tuned = false;
+  return MOC_OK;
+}
+
+int moc_autotune(moc_ctx* c, int* lps, int* slots, int* exp_kind) {
+  MOC_TRY(ready(c));
+  c->tuned = false;
+  const int user_shape = c->shape_user_set;
+  c->shape_user_set = 0;
+  int st = autotune_sweep(c, false);
+  c->shape_user_set = user_shape;
+  MOC_TRY(st);
+  // the timing sweeps leave undefined tallies and angular fluxes behind
+  MOC_TRY(zero_track_fluxes(c));
+  MOC_CUDA(cudaMemsetAsync(c->phi, 0, 4 * num_flux(c), c->stream));
+  if (lps) *lps = c->lps;
+  if (slots) *slots = c->slots;
+  if (exp_kind) *exp_kind = c->exp_kind;
+  return MOC_OK;
+}
+
+int moc_get_tuning_log(moc_ctx* c, int* lps, int* slots, int* exp_kind,
+                       float* ms, int capacity, int* count) {
+  MOC_CHECK(c && count, MOC_ERR_ARG, "null argument");
+  *count = (int) c->tune_log.size();
+  for (int i = 0; i < (int) c->tune_log.size() && i < capacity; i++) {
+    lps[i] = c->tune_log[i].lps;
+    slots[i] = c->tune_log[i].slots;
+    exp_kind[i] = c->tune_log[i].exp_kind;
+    ms[i] = c->tune_log[i].ms;
+  }
   return MOC_OK;
 }
 
@@ -727,6 +872,8 @@ int moc_set_sweep_shape(moc_ctx* c, int lps, int slots) {
   if (lps == 0) {
     c->lps = 0;
     c->slots = 0;
+    c->shape_user_set = 0;
+    c->tuned = false;
     return MOC_OK;
   }
   MOC_CHECK(moc::sweep_lps_supported(lps), MOC_ERR_ARG,
@@ -736,6 +883,7 @@ int moc_set_sweep_shape(moc_ctx* c, int lps, int slots) {
             MOC_ERR_ARG, "lanes x groups-per-lane must cover every group");
   c->lps = lps;
   c->slots = slots;
+  c->shape_user_set = 1;
   return MOC_OK;
 }
 
@@ -764,6 +912,7 @@ int moc_compute_eigenvalue(moc_ctx* c, int max_iters, int res_type) {
             "without fissionable FSRs");
   MOC_CHECK(c->num_fissionable > 0, MOC_ERR_ARG,
             "an eigenvalue solve needs fissionable material");
+  MOC_TRY(maybe_autotune(c));
   // Solver::computeInitialFluxGuess: flat flux 1, normalised, stored;
   // zero boundary fluxes (src/Solver.cpp:1710-1757)
   MOC_TRY(zero_track_fluxes(c));
@@ -789,6 +938,7 @@ int moc_compute_source(moc_ctx* c, int max_iters, double k_eff,
             "The Solver is unable to compute the source with a non-positive "
             "keff");
   MOC_CHECK(res_type >= 0 && res_type <= 2, MOC_ERR_ARG, "bad residual type");
+  MOC_TRY(maybe_autotune(c));
   MOC_TRY(zero_track_fluxes(c));
   MOC_TRY(begin_solve(c, moc::kModeSource, max_iters, res_type, k_eff));
   moc::launch_fill(c->phi, num_flux(c), 1.0f, c->stream);
@@ -807,6 +957,7 @@ int moc_compute_flux(moc_ctx* c, int max_iters, int only_fixed_source) {
   MOC_CHECK(only_fixed_source, MOC_ERR_UNSUPPORTED,
             "computeFlux without only_fixed_source needs a previous "
             "eigenvalue solve; use the hooks");
+  MOC_TRY(maybe_autotune(c));
   MOC_TRY(zero_track_fluxes(c));
   MOC_TRY(begin_solve(c, moc::kModeFlux, max_iters, MOC_SCALAR_FLUX, 1.0));
   moc::SolverArgs a = solver_args(c, 0);
@@ -837,6 +988,7 @@ int moc_bench_iterations(moc_ctx* c, int steps, int res_type, int flush_l2,
     c->flush_n = std::max<int64_t>(2 * (int64_t) l2 / 4, 1 << 20);
     MOC_TRY(dalloc(&c->flush, c->flush_n));
   }
+  MOC_TRY(maybe_autotune(c));
   // initial state as computeEigenvalue's first iteration sees it
   MOC_TRY(zero_track_fluxes(c));
   MOC_TRY(begin_solve(c, moc::kModeEigen, 1 << 30, res_type, 1.0));

@@ -50,7 +50,7 @@ class GB300Solver:
         self._device = device
         self._problem: Optional[Problem] = None
         self._threshold = 1e-5
-        self._exp_kind = EXP_TABLE
+        self._exp_kind = None   # None: chosen by the autotuner
         self._fixed: dict = {}
         self._fixed_by_material: dict = {}
         self._num_iterations = 0
@@ -110,7 +110,8 @@ class GB300Solver:
                    _ptr(p.nu_sigma_f), _ptr(p.chi))
         self._call("moc_upload_fsrs", _ptr(p.fsr_mat), _ptr(p.fsr_vol))
         self._call("moc_set_convergence_threshold", self._threshold)
-        self._call("moc_set_exponential", self._exp_kind)
+        if self._exp_kind is not None:
+            self._call("moc_set_exponential", self._exp_kind)
         if self._shape is not None:
             self._call("moc_set_sweep_shape", *self._shape)
         self._fixed = {}
@@ -155,6 +156,41 @@ class GB300Solver:
         a, b = C.c_int(), C.c_int()
         self._call("moc_get_sweep_shape", C.byref(a), C.byref(b))
         return a.value, b.value
+
+    def getExponential(self) -> int:
+        """The evaluator in use (EXP_TABLE or EXP_INTRINSIC): the caller's
+        choice, or the autotuner's once a solve has run."""
+        self._need_ctx()
+        k = C.c_int()
+        self._call("moc_get_exponential", C.byref(k))
+        return k.value
+
+    def setAutotune(self, on: bool) -> None:
+        self._need_ctx()
+        self._call("moc_set_autotune", int(bool(on)))
+
+    def autotune(self):
+        """Times every sweep-kernel shape (and both exponential evaluators
+        unless one was chosen) on this problem and keeps the fastest;
+        returns (lanes per track direction, groups per lane, evaluator)."""
+        self._need_ctx()
+        a, b, e = C.c_int(), C.c_int(), C.c_int()
+        self._call("moc_autotune", C.byref(a), C.byref(b), C.byref(e))
+        return a.value, b.value, e.value
+
+    def getTuningLog(self):
+        """[(lanes, groups per lane, evaluator, sweep ms)] of the last tuning."""
+        self._need_ctx()
+        n = C.c_int()
+        cap = 64
+        a = np.zeros(cap, np.int32)
+        b = np.zeros(cap, np.int32)
+        e = np.zeros(cap, np.int32)
+        ms = np.zeros(cap, np.float32)
+        self._call("moc_get_tuning_log", _ptr(a), _ptr(b), _ptr(e), _ptr(ms), cap,
+                   C.byref(n))
+        return [(int(a[i]), int(b[i]), int(e[i]), float(ms[i]))
+                for i in range(min(n.value, cap))]
 
     def setIterationsPerSync(self, k: int) -> None:
         self._need_ctx()

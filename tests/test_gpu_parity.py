@@ -33,7 +33,10 @@ def solve(case, exp_kind, precision="f32"):
     s.setConvergenceThreshold(sc["tolerance"])
     if exp_kind == EXP_INTRINSIC:
         s.useExponentialIntrinsic()
+    else:
+        s.useExponentialInterpolation()
     s.computeEigenvalue(int(sc["max_iters"]), int(sc["res_type"]))
+    assert s.getExponential() == exp_kind
     return s, p, sc, arr
 
 
@@ -75,6 +78,8 @@ def test_hooks_match_openmoc(case, exp_kind):
     s = GB300Solver(p)
     if exp_kind == EXP_INTRINSIC:
         s.useExponentialIntrinsic()
+    else:
+        s.useExponentialInterpolation()
     R, G = p.num_fsrs, p.num_groups
     s.setFluxes(arr["probe_phi_in"])
     s.setOldFluxes(arr["probe_phi_old"])
@@ -128,3 +133,20 @@ def test_sweep_matches_oracle_hook_for_hook(case):
         assert err < 2e-5, (lps, slots, err)
         assert np.max(np.abs(s.getStartFlux() - o.start)) <= 1e-5 * np.max(np.abs(o.start))
         s.close()
+
+
+def test_autotuner_picks_a_timed_shape_and_keeps_parity():
+    """The autotuner times every shape (both evaluators when free), picks
+    the fastest, and the solve that follows still matches OpenMOC."""
+    p, sc, arr = load_case("lat2_g16", "f32")
+    s = GB300Solver(p)
+    lps, slots, kind = s.autotune()
+    log = s.getTuningLog()
+    assert len(log) >= 2 and {e for _, _, e, _ in log} == {EXP_TABLE, EXP_INTRINSIC}
+    fastest = min(log, key=lambda r: r[3])
+    assert (lps, slots, kind) == fastest[:3]
+    assert lps * slots >= p.num_groups
+    s.setConvergenceThreshold(sc["tolerance"])
+    s.computeEigenvalue(int(sc["max_iters"]), int(sc["res_type"]))
+    assert abs(s.getKeff() - sc["keff"]) <= KEFF_TOL
+    assert max_rel(s.getFluxes(), arr["flux"]) <= FLUX_TOL
