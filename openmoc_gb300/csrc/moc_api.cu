@@ -149,7 +149,19 @@ int64_t num_psi(const moc_ctx* c) {
   return 2 * c->d.num_tracks * fluxes_per_track(c);
 }
 
+// Row stride of the device [R][*] arrays: G rounded up to even, so that a
+// group pair is one aligned 8-byte access.
+int row_stride(const moc_ctx* c) {
+  return c->d.num_groups + (c->d.num_groups & 1);
+}
+
+// Elements of a device [R][ld] array.
 int64_t num_flux(const moc_ctx* c) {
+  return c->d.num_fsrs * row_stride(c);
+}
+
+// Elements of the host-side [R][G] view.
+int64_t num_host_flux(const moc_ctx* c) {
   return c->d.num_fsrs * c->d.num_groups;
 }
 
@@ -173,6 +185,7 @@ moc::SweepArgs sweep_args(moc_ctx* c, int check_done) {
   a.sc = c->sc;
   a.num_tracks = c->d.num_tracks;
   a.num_groups = c->d.num_groups;
+  a.ld = row_stride(c);
   a.num_materials = c->d.num_materials;
   a.lps = c->lps;
   a.mat_packed = c->mat_packed;
@@ -201,6 +214,7 @@ moc::SolverArgs solver_args(moc_ctx* c, int check_done) {
   a.num_fsrs = c->d.num_fsrs;
   a.num_psi = num_psi(c);
   a.num_groups = c->d.num_groups;
+  a.ld = row_stride(c);
   a.num_materials = c->d.num_materials;
   a.check_done = check_done;
   return a;
@@ -231,22 +245,28 @@ int push(moc_ctx* c) {
 
 // Utilisation of lanes for G groups split over lps lanes.
 double lane_use(int G, int lps, int slots) {
-  return (double) G / (double) (lps * slots);
+  return (double) G / (double) (2 * lps * slots);
+}
+
+// Group pairs per lane for G groups over lps lanes.
+int pair_slots(int G, int lps) {
+  const int pairs = (G + 1) / 2;
+  return (pairs + lps - 1) / lps;
 }
 
 // Heuristic kernel shape: the most lanes per track direction whose lane
 // utilisation is within 5% of the best reachable with at most kMaxSlots
-// groups per lane.
+// group pairs per lane.
 void pick_shape(int G, int* lps_out, int* slots_out) {
   double best = 0.0;
-  for (int lps = 2; lps <= 32; lps *= 2) {
-    int slots = (G + lps - 1) / lps;
+  for (int lps = 1; lps <= 32; lps *= 2) {
+    int slots = pair_slots(G, lps);
     if (slots > moc::kMaxSlots) continue;
     best = std::max(best, lane_use(G, lps, slots));
   }
   int chosen = 32;
-  for (int lps = 32; lps >= 2; lps /= 2) {
-    int slots = (G + lps - 1) / lps;
+  for (int lps = 32; lps >= 1; lps /= 2) {
+    int slots = pair_slots(G, lps);
     if (slots > moc::kMaxSlots) continue;
     if (lane_use(G, lps, slots) >= 0.95 * best) {
       chosen = lps;
@@ -254,7 +274,7 @@ void pick_shape(int G, int* lps_out, int* slots_out) {
     }
   }
   *lps_out = chosen;
-  *slots_out = (G + chosen - 1) / chosen;
+  *slots_out = pair_slots(G, chosen);
 }
 
 int enqueue_sweep(moc_ctx* c, int check_done, bool timed, int ev_index) {
@@ -338,8 +358,8 @@ int autotune_sweep(moc_ctx* c, bool use_cache) {
   TuneVal best{0, 0, 0, 1e30f};
   c->tune_log.clear();
   for (int kind : kinds) {
-    for (int lps = 2; lps <= 32; lps *= 2) {
-      const int slots = (G + lps - 1) / lps;
+    for (int lps = 1; lps <= 32; lps *= 2) {
+      const int slots = pair_slots(G, lps);
       if (slots > moc::kMaxSlots || lane_use(G, lps, slots) < 0.5) continue;
       c->lps = lps;
       c->slots = slots;
@@ -489,8 +509,8 @@ int moc_create(const moc_dims* dims, moc_ctx** out) {
   MOC_CHECK(dims != nullptr && out != nullptr, MOC_ERR_ARG, "null argument");
   *out = nullptr;
   const moc_dims& d = *dims;
-  MOC_CHECK(d.num_groups >= 1 && d.num_groups <= 32 * moc::kMaxSlots,
-            MOC_ERR_ARG, "num_groups must be in [1, 288]");
+  MOC_CHECK(d.num_groups >= 1 && d.num_groups <= 64 * moc::kMaxSlots,
+            MOC_ERR_ARG, "num_groups must be in [1, 384]");
   MOC_CHECK(d.num_polar_half >= 1 && moc::sweep_max_slots(d.num_polar_half) > 0,
             MOC_ERR_UNSUPPORTED,
             "num_polar_half must be 1, 2 or 3 (2, 4 or 6 polar angles in 2D)");
@@ -517,7 +537,7 @@ int moc_create(const moc_dims* dims, moc_ctx** out) {
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) !=
       cudaSuccess)
     return bail(fail(MOC_ERR_CUDA, "cudaStreamCreate failed"));
-  const int64_t R = d.num_fsrs, G = d.num_groups;
+  const int64_t R = d.num_fsrs, G = row_stride(c);
   const int64_t npsi = num_psi(c);
   // memory budget: state arrays plus tracks
   size_t need = sizeof(float) * (size_t) (3 * R * G + 2 * npsi) +
@@ -798,11 +818,16 @@ int moc_set_fixed_sources(moc_ctx* c, const float* q) {
     dfree(c->fixed);
     return MOC_OK;
   }
-  const int64_t n = num_flux(c);
+  const int64_t n = num_host_flux(c);
   for (int64_t i = 0; i < n; i++)
     MOC_CHECK(std::isfinite(q[i]), MOC_ERR_ARG, "non-finite fixed source");
-  if (!c->fixed) MOC_TRY(dalloc(&c->fixed, n));
-  MOC_CUDA(cudaMemcpy(c->fixed, q, 4 * n, cudaMemcpyHostToDevice));
+  if (!c->fixed) {
+    MOC_TRY(dalloc(&c->fixed, num_flux(c)));
+    MOC_CUDA(cudaMemset(c->fixed, 0, 4 * num_flux(c)));
+  }
+  const int G = c->d.num_groups, ld = row_stride(c);
+  MOC_CUDA(cudaMemcpy2D(c->fixed, 4 * ld, q, 4 * G, 4 * G, c->d.num_fsrs,
+                        cudaMemcpyHostToDevice));
   return MOC_OK;
 }
 
@@ -877,10 +902,11 @@ int moc_set_sweep_shape(moc_ctx* c, int lps, int slots) {
     return MOC_OK;
   }
   MOC_CHECK(moc::sweep_lps_supported(lps), MOC_ERR_ARG,
-            "lanes per track direction must be 2, 4, 8, 16 or 32");
+            "lanes per track direction must be 1, 2, 4, 8, 16 or 32");
   MOC_CHECK(slots >= 1 && slots <= moc::kMaxSlots &&
-                (int64_t) lps * slots >= c->d.num_groups,
-            MOC_ERR_ARG, "lanes x groups-per-lane must cover every group");
+                2 * (int64_t) lps * slots >= c->d.num_groups,
+            MOC_ERR_ARG,
+            "lanes x group pairs per lane must cover every group");
   c->lps = lps;
   c->slots = slots;
   c->shape_user_set = 1;
@@ -1075,30 +1101,57 @@ static int copy_in(moc_ctx* c, float* dst, const float* in, int64_t n,
   return MOC_OK;
 }
 
+// [R][G] host rows from / to the [R][ld] device layout.
+static int copy_rows_out(moc_ctx* c, const float* src, float* out, int64_t n) {
+  MOC_CHECK(c && out, MOC_ERR_ARG, "null argument");
+  MOC_CHECK(n == num_host_flux(c), MOC_ERR_ARG,
+            "expected " + std::to_string(num_host_flux(c)) + " values, got " +
+                std::to_string(n));
+  const int G = c->d.num_groups, ld = row_stride(c);
+  MOC_CUDA(cudaSetDevice(c->d.device));
+  MOC_CUDA(cudaMemcpy2DAsync(out, 4 * G, src, 4 * ld, 4 * G, c->d.num_fsrs,
+                             cudaMemcpyDeviceToHost, c->stream));
+  MOC_CUDA(cudaStreamSynchronize(c->stream));
+  return MOC_OK;
+}
+
+static int copy_rows_in(moc_ctx* c, float* dst, const float* in, int64_t n) {
+  MOC_CHECK(c && in, MOC_ERR_ARG, "null argument");
+  MOC_CHECK(n == num_host_flux(c), MOC_ERR_ARG,
+            "expected " + std::to_string(num_host_flux(c)) + " values, got " +
+                std::to_string(n));
+  const int G = c->d.num_groups, ld = row_stride(c);
+  MOC_CUDA(cudaSetDevice(c->d.device));
+  MOC_CUDA(cudaMemcpy2DAsync(dst, 4 * ld, in, 4 * G, 4 * G, c->d.num_fsrs,
+                             cudaMemcpyHostToDevice, c->stream));
+  MOC_CUDA(cudaStreamSynchronize(c->stream));
+  return MOC_OK;
+}
+
 int moc_get_fluxes(moc_ctx* c, float* out, int64_t n) {
   MOC_CHECK(c, MOC_ERR_ARG, "null context");
-  return copy_out(c, c->phi, out, n, num_flux(c));
+  return copy_rows_out(c, c->phi, out, n);
 }
 
 int moc_set_fluxes(moc_ctx* c, const float* in, int64_t n) {
   MOC_CHECK(c, MOC_ERR_ARG, "null context");
-  MOC_TRY(copy_in(c, c->phi, in, n, num_flux(c)));
-  return copy_in(c, c->phi_old, in, n, num_flux(c));
+  MOC_TRY(copy_rows_in(c, c->phi, in, n));
+  return copy_rows_in(c, c->phi_old, in, n);
 }
 
 int moc_get_old_fluxes(moc_ctx* c, float* out, int64_t n) {
   MOC_CHECK(c, MOC_ERR_ARG, "null context");
-  return copy_out(c, c->phi_old, out, n, num_flux(c));
+  return copy_rows_out(c, c->phi_old, out, n);
 }
 
 int moc_set_old_fluxes(moc_ctx* c, const float* in, int64_t n) {
   MOC_CHECK(c, MOC_ERR_ARG, "null context");
-  return copy_in(c, c->phi_old, in, n, num_flux(c));
+  return copy_rows_in(c, c->phi_old, in, n);
 }
 
 int moc_get_reduced_sources(moc_ctx* c, float* out, int64_t n) {
   MOC_CHECK(c, MOC_ERR_ARG, "null context");
-  MOC_TRY(copy_out(c, c->qt, out, n, num_flux(c)));
+  MOC_TRY(copy_rows_out(c, c->qt, out, n));
   // the device keeps Q / (4 pi sigma_t); report Q / (4 pi)
   std::vector<float> st((size_t) c->d.num_materials * c->d.num_groups);
   std::vector<int32_t> mat(c->d.num_fsrs);
@@ -1166,7 +1219,7 @@ int moc_flatten_fsr_fluxes_chi(moc_ctx* c, int material) {
             "chi spectrum material out of range");
   float* d_chi = c->chi + (int64_t) material * c->d.num_groups;
   moc::launch_fill_chi(c->phi, d_chi, c->d.num_fsrs, c->d.num_groups,
-                       c->stream);
+                       row_stride(c), c->stream);
   c->launches++;
   MOC_CUDA(cudaGetLastError());
   return MOC_OK;

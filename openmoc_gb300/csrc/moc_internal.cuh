@@ -14,8 +14,8 @@ constexpr int kExpTableSize = 321;
 constexpr float kExpTableInvH = 16.0f;
 constexpr float kExpTableH = 1.0f / 16.0f;
 
-// Largest number of groups handled per lane and largest polar count.
-constexpr int kMaxSlots = 9;
+// Largest number of group pairs handled per lane and largest polar count.
+constexpr int kMaxSlots = 6;
 constexpr int kMaxPolarHalf = 5;
 constexpr int kSweepThreads = 128;
 
@@ -61,13 +61,14 @@ struct SweepArgs {
   const float* inv_sin;      // [A][Ph]
   const float* sigma_t;      // [M][G]
   const int32_t* fsr_mat;    // [R]
-  const float* qt;           // [R][G] reduced source / sigma_t
+  const float* qt;           // [R][ld] reduced source / sigma_t
   const float* exp_table;    // [2][kExpTableSize]: 1 - exp(-x_i), exp(-x_i)
-  float* phi;                // [R][G] accumulated tallies
+  float* phi;                // [R][ld] accumulated tallies
   float* psi[2];             // [T][2][F] angular-flux buffers
   DevScalars* sc;
   int64_t num_tracks;
   int num_groups;
+  int ld;                    // row stride of phi / qt: G rounded up to even
   int num_materials;
   int lps;                   // lanes per track direction (1..32, power of 2)
   int check_done;            // return at once if sc->done is set
@@ -82,17 +83,18 @@ struct SolverArgs {
   const uint8_t* fissile;    // [M]
   const int32_t* fsr_mat;    // [R]
   const float* fsr_vol;      // [R]
-  const float* fixed;        // [R][G] or null
+  const float* fixed;        // [R][ld] or null
   const float* scat_out;     // [M][G] total scattering out of each group
   const float* sigma_f;      // [M][G] or null
-  float* phi;                // [R][G]
-  float* phi_old;            // [R][G]
-  float* qt;                 // [R][G]
+  float* phi;                // [R][ld]
+  float* phi_old;            // [R][ld]
+  float* qt;                 // [R][ld]
   float* psi[2];
   DevScalars* sc;
   int64_t num_fsrs;
   int64_t num_psi;           // 2*T*F
   int num_groups;
+  int ld;                    // row stride of the [R][*] arrays (even, >= G)
   int num_materials;
   int check_done;
 };
@@ -126,7 +128,7 @@ void launch_fission_rate(const SolverArgs& a, int what, cudaStream_t s);
 void launch_scale_phi(const SolverArgs& a, cudaStream_t s);
 void launch_zero_phi(const SolverArgs& a, cudaStream_t s);
 void launch_fill(float* p, int64_t n, float v, cudaStream_t s);
-void launch_fill_chi(float* phi, const float* chi, int64_t R, int G,
+void launch_fill_chi(float* phi, const float* chi, int64_t R, int G, int ld,
                      cudaStream_t s);
 void launch_fsr_rates(const SolverArgs& a, double* out, int nu,
                       cudaStream_t s);

@@ -87,7 +87,7 @@ compute_sources_kernel(const SolverArgs a, int iteration, int zero_phi) {
   for (int64_t r = (int64_t) blockIdx.x * wpb + warp; r < a.num_fsrs;
        r += (int64_t) gridDim.x * wpb) {
     const int m = a.fsr_mat[r];
-    float* phi = a.phi + r * G;
+    float* phi = a.phi + r * a.ld;
     for (int g = lane; g < G; g += 32) row[g] = phi[g];
     // fused: the sweep that follows starts from zero tallies; each lane
     // clears exactly the entries it staged
@@ -109,13 +109,13 @@ compute_sources_kernel(const SolverArgs a, int iteration, int zero_phi) {
       for (int g = 0; g < G; g++) s = fmaf(__ldg(srow + g), row[g], s);
       float q = (float) ((double) chi[gd] * (double) fr * inv_k);
       q += s;
-      if (a.fixed) q += a.fixed[r * G + gd];
+      if (a.fixed) q += a.fixed[r * a.ld + gd];
       q *= (float) kOneOverFourPi;
       if (q < 0.0f) {
         negatives++;
         if (iteration < 30) q = kFluxEpsilon;
       }
-      a.qt[r * G + gd] = q / st[gd];
+      a.qt[r * a.ld + gd] = q / st[gd];
     }
     __syncwarp();
   }
@@ -138,14 +138,15 @@ add_source_kernel(const SolverArgs a, int update) {
     const float vol0 = a.fsr_vol[r];
     const float vol = (vol0 < 1.0e-12f) ? 1.0e30f : vol0;
     const float st = a.sigma_t[(int64_t) m * G + g];
-    float v = a.phi[i];
+    const int64_t j = r * a.ld + g;
+    float v = a.phi[j];
     v /= (st * vol);
-    v += (float) kFourPi * a.qt[i];
+    v += (float) kFourPi * a.qt[j];
     if (v < 0.0f) {
       v = kFluxEpsilon;
       negatives++;
     }
-    a.phi[i] = v;
+    a.phi[j] = v;
     if (update)
       rate += (double) (a.nu_sigma_f[(int64_t) m * G + g] * v) * (double) vol0;
   }
@@ -192,12 +193,13 @@ residual_kernel(const SolverArgs a, int res_type, int normalise, int store,
     const float* so = a.scat_out + (int64_t) m * G;
     double nw = 0.0, od = 0.0, sq = 0.0, snw = 0.0, sod = 0.0;
     for (int g = lane; g < G; g += 32) {
-      float v = a.phi[r * G + g];
+      const int64_t j = r * a.ld + g;
+      float v = a.phi[j];
       if (normalise) {
         v = (float) ((double) v * factor);
-        a.phi[r * G + g] = v;
+        a.phi[j] = v;
       }
-      const float o = a.phi_old[r * G + g];
+      const float o = a.phi_old[j];
       if (res_type == 0) {
         if (o > 0.0f) {
           const double d = ((double) v - (double) o) / (double) o;
@@ -213,7 +215,7 @@ residual_kernel(const SolverArgs a, int res_type, int normalise, int store,
           sod += (double) so[g] * o;
         }
       }
-      if (store) a.phi_old[r * G + g] = v;
+      if (store) a.phi_old[j] = v;
     }
     if (res_type == 0) {
       sq = warp_sum_all_d(sq);
@@ -281,7 +283,8 @@ fission_rate_kernel(const SolverArgs a, int what) {
     const int64_t r = i / G;
     const int g = (int) (i - r * G);
     const int m = a.fsr_mat[r];
-    rate += (double) (a.nu_sigma_f[(int64_t) m * G + g] * a.phi[i]) *
+    rate += (double) (a.nu_sigma_f[(int64_t) m * G + g] *
+                      a.phi[r * a.ld + g]) *
             (double) a.fsr_vol[r];
   }
   DevScalars* sc = a.sc;
@@ -302,7 +305,7 @@ fission_rate_kernel(const SolverArgs a, int what) {
 
 __global__ void scale_phi_kernel(const SolverArgs a) {
   const double f = a.sc->factor;
-  const int64_t n = a.num_fsrs * a.num_groups;
+  const int64_t n = a.num_fsrs * a.ld;
   for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t) gridDim.x * blockDim.x)
     a.phi[i] = (float) ((double) a.phi[i] * f);
@@ -310,7 +313,7 @@ __global__ void scale_phi_kernel(const SolverArgs a) {
 
 __global__ void zero_phi_kernel(const SolverArgs a) {
   if (skip(a)) return;
-  const int64_t n = a.num_fsrs * a.num_groups;
+  const int64_t n = a.num_fsrs * a.ld;
   for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t) gridDim.x * blockDim.x)
     a.phi[i] = 0.0f;
@@ -323,11 +326,13 @@ __global__ void fill_kernel(float* p, int64_t n, float v) {
 }
 
 __global__ void fill_chi_kernel(float* phi, const float* chi, int64_t R,
-                                int G) {
-  const int64_t n = R * G;
+                                int G, int ld) {
+  const int64_t n = R * ld;
   for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t) gridDim.x * blockDim.x)
-    phi[i] = chi[i % G];
+       i += (int64_t) gridDim.x * blockDim.x) {
+    const int g = (int) (i % ld);
+    phi[i] = (g < G) ? chi[g] : 0.0f;
+  }
 }
 
 // Per-FSR volume-integrated (nu-)fission rate, one warp per FSR
@@ -341,7 +346,8 @@ __global__ void fsr_rates_kernel(const SolverArgs a, double* out, int nu) {
     const int m = a.fsr_mat[r];
     const float* xs = (nu ? a.nu_sigma_f : a.sigma_f) + (int64_t) m * G;
     double s = 0.0;
-    for (int g = lane; g < G; g += 32) s += (double) xs[g] * a.phi[r * G + g];
+    for (int g = lane; g < G; g += 32)
+      s += (double) xs[g] * a.phi[r * a.ld + g];
     s = warp_sum_all_d(s);
     if (lane == 0) out[r] = s * (double) a.fsr_vol[r];
   }
@@ -398,10 +404,10 @@ void launch_fill(float* p, int64_t n, float v, cudaStream_t s) {
   fill_kernel<<<grid_for(n, kThreads), kThreads, 0, s>>>(p, n, v);
 }
 
-void launch_fill_chi(float* phi, const float* chi, int64_t R, int G,
+void launch_fill_chi(float* phi, const float* chi, int64_t R, int G, int ld,
                      cudaStream_t s) {
-  fill_chi_kernel<<<grid_for(R * G, kThreads), kThreads, 0, s>>>(phi, chi, R,
-                                                                G);
+  fill_chi_kernel<<<grid_for(R * ld, kThreads), kThreads, 0, s>>>(phi, chi, R,
+                                                                 G, ld);
 }
 
 void launch_fsr_rates(const SolverArgs& a, double* out, int nu,

@@ -34,7 +34,8 @@ int sweep_max_slots(int polar_half) {
 }
 
 bool sweep_lps_supported(int lps) {
-  return lps == 2 || lps == 4 || lps == 8 || lps == 16 || lps == 32;
+  return lps == 1 || lps == 2 || lps == 4 || lps == 8 || lps == 16 ||
+         lps == 32;
 }
 
 bool launch_sweep(const SweepArgs& a, int polar_half, int slots, int exp_kind,

@@ -10,15 +10,16 @@
 //
 // Work decomposition: a "stream" is one direction of one track.  A warp
 // carries 32/LPS streams; the LPS lanes of a stream split the energy groups
-// (lane `sub` handles groups sub, sub+LPS, ..., SLOTS of them), and each
-// lane keeps the angular flux of its groups for all polar angles in
-// registers along the whole track.  The forward and backward streams of a
-// track are adjacent (they share segment cache lines).  Streams are ordered
-// by decreasing segment count so that the longest tracks start first.
-//
-// Per segment and group the lane sums the polar contributions in registers
-// and issues one fire-and-forget float reduction into the FSR tally; the
-// LPS lanes of a stream write LPS consecutive floats of one FSR row.
+// in pairs (lane `sub` handles group pairs sub, sub+LPS, ..., PS of them)
+// and keep the angular flux of those groups for every polar angle in
+// registers along the whole track.  Each pair is integrated with the packed
+// two-wide FP32 instructions of sm_100+ (FFMA2 / FADD2 / FMUL2), so one
+// instruction advances two groups; sources are read 8 bytes at a time and
+// tallies leave as one two-wide vector reduction (red.global.add.v2.f32)
+// per pair and segment.  Flux rows are padded to an even group count (ld).
+// The forward and backward streams of a track are adjacent (they share
+// segment cache lines), and streams are ordered by decreasing segment count
+// so that the longest tracks start first.
 //
 // Attenuation: delta = (psi - Q/sigma_t) * g(x), g(x) = 1 - exp(-x),
 // x = sigma_t * l / sin(theta): algebraically the reference's
@@ -28,6 +29,8 @@
 #include "moc_internal.cuh"
 
 namespace moc {
+
+__device__ __forceinline__ float2 f2(float v) { return make_float2(v, v); }
 
 // g(x) = 1 - exp(-x) from a shared-memory table of (g_i, 1 - g_i) at
 // x_i = i*h, h = 1/16, expanded around the node:
@@ -51,6 +54,11 @@ struct AttenTable {
     const float2 ge = tab[i];
     return fmaf(ge.y, q, ge.x);
   }
+  // two groups; x2 already scaled by 1/h
+  __device__ __forceinline__ static float2 eval2(float2 u2, float2 /*x2*/,
+                                                 const float2* tab) {
+    return make_float2(eval(u2.x, tab), eval(u2.y, tab));
+  }
 };
 
 // g(x) = 1 - exp(-x) from the hardware base-2 exponential, with the series
@@ -62,41 +70,47 @@ struct AttenIntrinsic {
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v));
     return r;
   }
-  __device__ __forceinline__ static float eval(float x) {
-    const float e = ex2(x * -1.4426950408889634f);
-    const float big = 1.0f - e;
-    const float small =
-        x * fmaf(x, fmaf(x, fmaf(x, fmaf(x, 1.0f / 120.0f, -1.0f / 24.0f),
-                                 1.0f / 6.0f), -0.5f), 1.0f);
-    return x < 0.25f ? small : big;
+  // u2 = -x * log2(e), x2 = x, for two groups
+  __device__ __forceinline__ static float2 eval2(float2 u2, float2 x2,
+                                                 const float2*) {
+    const float2 e = make_float2(ex2(u2.x), ex2(u2.y));
+    const float2 big = __ffma2_rn(e, f2(-1.0f), f2(1.0f));
+    float2 s = __ffma2_rn(x2, f2(1.0f / 120.0f), f2(-1.0f / 24.0f));
+    s = __ffma2_rn(x2, s, f2(1.0f / 6.0f));
+    s = __ffma2_rn(x2, s, f2(-0.5f));
+    s = __ffma2_rn(x2, s, f2(1.0f));
+    s = __fmul2_rn(x2, s);
+    return make_float2(x2.x < 0.25f ? s.x : big.x, x2.y < 0.25f ? s.y : big.y);
   }
 };
 
-// Registers available per thread: the busy instances keep 6 blocks of 128
+// Registers available per thread: the busy instances keep 5 blocks of 128
 // threads resident per SM, the small ones 8.
-template <int PH, int SLOTS>
+template <int PH, int PS>
 struct SweepOccupancy {
-  static constexpr int min_blocks = (PH * SLOTS > 12) ? 6 : 8;
+  static constexpr int min_blocks = (PH * PS > 6) ? 5 : 8;
 };
 
-template <int PH, int LPS, int SLOTS, int EXPK>
+template <int PH, int LPS, int PS, int EXPK>
 __global__ void __launch_bounds__(kSweepThreads,
-                                  (SweepOccupancy<PH, SLOTS>::min_blocks))
+                                  (SweepOccupancy<PH, PS>::min_blocks))
 sweep_kernel(const SweepArgs a) {
   extern __shared__ float smem[];
   DevScalars* sc = a.sc;
   if (a.check_done && *(volatile int*) &sc->done) return;
 
   const int G = a.num_groups;
-  const int MG = a.num_materials * G;
+  const int ld = a.ld;                       // even row stride >= G
   float2* s_tab = reinterpret_cast<float2*>(smem);
   float* s_st = smem + ((EXPK == kExpTable) ? 2 * kExpTableSize : 0);
-  for (int i = threadIdx.x; i < MG; i += blockDim.x) s_st[i] = a.sigma_t[i];
+  // sigma_t rows padded to ld; the padding group gets sigma_t = 1
+  for (int i = threadIdx.x; i < a.num_materials * ld; i += blockDim.x) {
+    const int m = i / ld, g = i - m * ld;
+    s_st[i] = (g < G) ? a.sigma_t[m * G + g] : 1.0f;
+  }
   if (EXPK == kExpTable)
-    for (int i = threadIdx.x; i < kExpTableSize; i += blockDim.x) {
-      const float gi = a.exp_table[i];
-      s_tab[i] = make_float2(gi, a.exp_table[kExpTableSize + i]);
-    }
+    for (int i = threadIdx.x; i < kExpTableSize; i += blockDim.x)
+      s_tab[i] = make_float2(a.exp_table[i], a.exp_table[kExpTableSize + i]);
   __syncthreads();
 
   const int cur = sc->cur;
@@ -109,6 +123,7 @@ sweep_kernel(const SweepArgs a) {
   const int64_t gwarp =
       ((int64_t) blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t stream = gwarp * (32 / LPS) + lane / LPS;
+  const int npairs = ld >> 1;
 
   if (stream < 2 * a.num_tracks) {
     const int t = a.order[stream >> 1];
@@ -118,22 +133,31 @@ sweep_kernel(const SweepArgs a) {
     const int ang = a.track_ang[t];
     const int F = G * PH;
 
-    float w[PH], xs[PH];
+    float2 w2[PH], xs2[PH], xl2[PH];
 #pragma unroll
     for (int p = 0; p < PH; p++) {
-      w[p] = a.weights[ang * PH + p];
+      w2[p] = f2(a.weights[ang * PH + p]);
       const float is = a.inv_sin[ang * PH + p];
-      xs[p] = (EXPK == kExpTable) ? is * kExpTableInvH : is;
+      if (EXPK == kExpTable) {
+        xs2[p] = f2(is * kExpTableInvH);
+      } else {
+        xs2[p] = f2(is);
+        xl2[p] = f2(is * -1.4426950408889634f);
+      }
     }
 
-    float psi[SLOTS][PH];
-    const float* pin = psi_in + ((int64_t) t * 2 + dir) * F + sub;
+    // angular flux of this lane's groups: pair s holds groups
+    // 2*(sub + s*LPS) and 2*(sub + s*LPS) + 1
+    float2 psi[PS][PH];
+    const float* pin = psi_in + ((int64_t) t * 2 + dir) * F;
 #pragma unroll
-    for (int j = 0; j < SLOTS; j++) {
-      const bool on = sub + j * LPS < G;
+    for (int s = 0; s < PS; s++) {
+      const int g0 = 2 * (sub + s * LPS);
 #pragma unroll
-      for (int p = 0; p < PH; p++)
-        psi[j][p] = on ? pin[p * G + j * LPS] * scale : 0.0f;
+      for (int p = 0; p < PH; p++) {
+        psi[s][p].x = (g0 < G) ? pin[p * G + g0] * scale : 0.0f;
+        psi[s][p].y = (g0 + 1 < G) ? pin[p * G + g0 + 1] * scale : 0.0f;
+      }
     }
 
     // Segment stream, software-pipelined.  The LPS lanes of a stream load
@@ -167,13 +191,13 @@ sweep_kernel(const SweepArgs a) {
     float len;
     int fsr, mat;
     unpack(sg, len, fsr, mat);
-    const float* qbase = a.qt + sub;
-    float q[SLOTS];
+    const float2* qbase = reinterpret_cast<const float2*>(a.qt) + sub;
+    float2 q[PS];
 #pragma unroll
-    for (int j = 0; j < SLOTS; j++)
-      q[j] = (sub + j * LPS < G && n > 0)
-                 ? __ldg(qbase + (int64_t) fsr * G + j * LPS)
-                 : 0.0f;
+    for (int s = 0; s < PS; s++)
+      q[s] = (sub + s * LPS < npairs && n > 0)
+                 ? __ldg(qbase + (int64_t) fsr * npairs + s * LPS)
+                 : f2(0.0f);
     for (int k = 0; k < n; k++) {
       // next segment: rotate chunks at chunk boundaries
       const int kn = k + 1;
@@ -188,37 +212,43 @@ sweep_kernel(const SweepArgs a) {
       float len_n;
       int fsr_n, mat_n;
       unpack(sgn, len_n, fsr_n, mat_n);
-      float qn[SLOTS];
-      const float* qrow = qbase + (int64_t) fsr_n * G;
+      float2 qn[PS];
+      const float2* qrow = qbase + (int64_t) fsr_n * npairs;
 #pragma unroll
-      for (int j = 0; j < SLOTS; j++)
-        qn[j] = (sub + j * LPS < G && kn < n) ? __ldg(qrow + j * LPS) : 0.0f;
+      for (int s = 0; s < PS; s++)
+        qn[s] = (sub + s * LPS < npairs && kn < n) ? __ldg(qrow + s * LPS)
+                                                   : f2(0.0f);
 
-      const float* st = s_st + mat * G + sub;
-      float* ph = a.phi + (int64_t) fsr * G + sub;
+      const float2* st =
+          reinterpret_cast<const float2*>(s_st + mat * ld) + sub;
+      float2* ph = reinterpret_cast<float2*>(a.phi + (int64_t) fsr * ld) + sub;
+      const float2 len2 = f2(len);
 #pragma unroll
-      for (int j = 0; j < SLOTS; j++) {
-        if (sub + j * LPS < G) {
-          const float tau = st[j * LPS] * len;
-          const float qv = q[j];
-          float tally = 0.0f;
+      for (int s = 0; s < PS; s++) {
+        if (sub + s * LPS < npairs) {
+          const float2 tau = __fmul2_rn(st[s * LPS], len2);
+          const float2 nq = make_float2(-q[s].x, -q[s].y);
+          float2 tally = f2(0.0f);
 #pragma unroll
           for (int p = 0; p < PH; p++) {
-            const float gx = (EXPK == kExpTable)
-                                 ? AttenTable::eval(tau * xs[p], s_tab)
-                                 : AttenIntrinsic::eval(tau * xs[p]);
-            const float d = (psi[j][p] - qv) * gx;
-            psi[j][p] -= d;
-            tally = fmaf(w[p], d, tally);
+            const float2 x2 = __fmul2_rn(tau, xs2[p]);
+            float2 gx;
+            if (EXPK == kExpTable)
+              gx = AttenTable::eval2(x2, x2, s_tab);
+            else
+              gx = AttenIntrinsic::eval2(__fmul2_rn(tau, xl2[p]), x2, s_tab);
+            const float2 d = __fmul2_rn(__fadd2_rn(psi[s][p], nq), gx);
+            psi[s][p] = __ffma2_rn(d, f2(-1.0f), psi[s][p]);
+            tally = __ffma2_rn(w2[p], d, tally);
           }
-          atomicAdd(ph + j * LPS, tally);
+          atomicAdd(ph + s * LPS, tally);
         }
       }
       len = len_n;
       fsr = fsr_n;
       mat = mat_n;
 #pragma unroll
-      for (int j = 0; j < SLOTS; j++) q[j] = qn[j];
+      for (int s = 0; s < PS; s++) q[s] = qn[s];
     }
 
     // boundary-flux transfer to the connecting track, fused into the sweep
@@ -227,12 +257,14 @@ sweep_kernel(const SweepArgs a) {
     if (f & (dir ? 8 : 4)) {
       const int nt = a.next[2 * t + dir];
       const int nd = (f & (dir ? 2 : 1)) ? 0 : 1;
-      float* po = psi_out + ((int64_t) nt * 2 + nd) * F + sub;
+      float* po = psi_out + ((int64_t) nt * 2 + nd) * F;
 #pragma unroll
-      for (int j = 0; j < SLOTS; j++) {
-        if (sub + j * LPS < G) {
+      for (int s = 0; s < PS; s++) {
+        const int g0 = 2 * (sub + s * LPS);
 #pragma unroll
-          for (int p = 0; p < PH; p++) po[p * G + j * LPS] = psi[j][p];
+        for (int p = 0; p < PH; p++) {
+          if (g0 < G) po[p * G + g0] = psi[s][p].x;
+          if (g0 + 1 < G) po[p * G + g0 + 1] = psi[s][p].y;
         }
       }
     }
@@ -256,22 +288,23 @@ sweep_kernel(const SweepArgs a) {
   }
 }
 
-template <int PH, int LPS, int SLOTS, int EXPK>
+template <int PH, int LPS, int PS, int EXPK>
 void launch_sweep_instance(const SweepArgs& a, cudaStream_t stream) {
   const int spw = 32 / LPS;
   const int64_t warps = (2 * a.num_tracks + spw - 1) / spw;
   const int wpb = kSweepThreads / 32;
   const int64_t blocks = (warps + wpb - 1) / wpb;
   const size_t smem =
-      sizeof(float) * ((size_t) a.num_materials * a.num_groups +
+      sizeof(float) * ((size_t) a.num_materials * a.ld +
                        (EXPK == kExpTable ? 2 * kExpTableSize : 0));
-  auto kern = sweep_kernel<PH, LPS, SLOTS, EXPK>;
+  auto kern = sweep_kernel<PH, LPS, PS, EXPK>;
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int) smem);
   kern<<<(unsigned) blocks, kSweepThreads, smem, stream>>>(a);
 }
 
+// slots = pairs of groups per lane
 template <int PH, int LPS, int EXPK>
 bool dispatch_sweep_slots(const SweepArgs& a, int slots, cudaStream_t s) {
   switch (slots) {
@@ -281,9 +314,6 @@ bool dispatch_sweep_slots(const SweepArgs& a, int slots, cudaStream_t s) {
     case 4: launch_sweep_instance<PH, LPS, 4, EXPK>(a, s); return true;
     case 5: launch_sweep_instance<PH, LPS, 5, EXPK>(a, s); return true;
     case 6: launch_sweep_instance<PH, LPS, 6, EXPK>(a, s); return true;
-    case 7: launch_sweep_instance<PH, LPS, 7, EXPK>(a, s); return true;
-    case 8: launch_sweep_instance<PH, LPS, 8, EXPK>(a, s); return true;
-    case 9: launch_sweep_instance<PH, LPS, 9, EXPK>(a, s); return true;
     default: return false;
   }
 }
@@ -291,6 +321,7 @@ bool dispatch_sweep_slots(const SweepArgs& a, int slots, cudaStream_t s) {
 template <int PH, int EXPK>
 bool dispatch_sweep_lps(const SweepArgs& a, int slots, cudaStream_t s) {
   switch (a.lps) {
+    case 1: return dispatch_sweep_slots<PH, 1, EXPK>(a, slots, s);
     case 2: return dispatch_sweep_slots<PH, 2, EXPK>(a, slots, s);
     case 4: return dispatch_sweep_slots<PH, 4, EXPK>(a, slots, s);
     case 8: return dispatch_sweep_slots<PH, 8, EXPK>(a, slots, s);
