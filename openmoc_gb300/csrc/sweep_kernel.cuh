@@ -61,10 +61,19 @@ struct AttenTable {
   }
 };
 
-// g(x) = 1 - exp(-x) from the hardware base-2 exponential, with the series
-// x - x^2/2 + x^3/6 - x^4/24 + x^5/120 below x = 1/4 where 1 - exp(-x)
-// would lose relative accuracy to cancellation.
+// g(x) = 1 - exp(-x) from the hardware base-2 exponential (relative error
+// about 2^-22) and the Taylor polynomial T5(x) = x - x^2/2 + x^3/6 - x^4/24
+// + x^5/120.  T5 never falls below g (its remainder is -exp(-z) x^6/720 for
+// some z in (0, x)), and it is accurate to 1e-9 relative below x = 0.1,
+// where 1 - exp(-x) loses relative accuracy to cancellation.  So
+//   g = min(T5(x), 1 + kBias - 2^(-x log2 e))
+// takes T5 for small x and the exponential for larger x (where T5 rises
+// away from g): one min instead of a compare and a select.  kBias lifts the
+// exponential branch above g by more than its own error, so the choice is
+// safe near the crossover; the absolute error is at most ~6.4e-7 there and
+// the relative error at most ~2.3e-6 for all x.
 struct AttenIntrinsic {
+  static constexpr float kBias = 4.0e-7f;
   __device__ __forceinline__ static float ex2(float v) {
     float r;
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v));
@@ -74,21 +83,25 @@ struct AttenIntrinsic {
   __device__ __forceinline__ static float2 eval2(float2 u2, float2 x2,
                                                  const float2*) {
     const float2 e = make_float2(ex2(u2.x), ex2(u2.y));
-    const float2 big = __ffma2_rn(e, f2(-1.0f), f2(1.0f));
+    const float2 big = __ffma2_rn(e, f2(-1.0f), f2(1.0f + kBias));
     float2 s = __ffma2_rn(x2, f2(1.0f / 120.0f), f2(-1.0f / 24.0f));
     s = __ffma2_rn(x2, s, f2(1.0f / 6.0f));
     s = __ffma2_rn(x2, s, f2(-0.5f));
     s = __ffma2_rn(x2, s, f2(1.0f));
     s = __fmul2_rn(x2, s);
-    return make_float2(x2.x < 0.25f ? s.x : big.x, x2.y < 0.25f ? s.y : big.y);
+    return make_float2(fminf(s.x, big.x), fminf(s.y, big.y));
   }
 };
 
 // Registers available per thread: the busy instances keep 5 blocks of 128
 // threads resident per SM, the small ones 8.
+#ifndef MOC_SWEEP_BIG_MIN_BLOCKS
+#define MOC_SWEEP_BIG_MIN_BLOCKS 5
+#endif
 template <int PH, int PS>
 struct SweepOccupancy {
-  static constexpr int min_blocks = (PH * PS > 6) ? 5 : 8;
+  static constexpr int min_blocks =
+      (PH * PS > 6) ? MOC_SWEEP_BIG_MIN_BLOCKS : 8;
 };
 
 template <int PH, int LPS, int PS, int EXPK>
@@ -192,12 +205,16 @@ sweep_kernel(const SweepArgs a) {
     int fsr, mat;
     unpack(sg, len, fsr, mat);
     const float2* qbase = reinterpret_cast<const float2*>(a.qt) + sub;
-    float2 q[PS];
-#pragma unroll
-    for (int s = 0; s < PS; s++)
-      q[s] = (sub + s * LPS < npairs && n > 0)
-                 ? __ldg(qbase + (int64_t) fsr * npairs + s * LPS)
-                 : f2(0.0f);
+    // The source row of the next segment is prefetched into L1 one segment
+    // ahead (no registers held); lanes of the stream split its cache lines.
+    const int row_bytes = ld * 4;
+    auto prefetch_row = [&](int r) {
+      const char* p0 = reinterpret_cast<const char*>(a.qt) + (int64_t) r * row_bytes;
+      const char* line = reinterpret_cast<const char*>(
+          reinterpret_cast<uintptr_t>(p0) & ~(uintptr_t) 127);
+      for (int l = sub; (int64_t) (line + 128 * l - p0) < row_bytes; l += LPS)
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(line + 128 * l));
+    };
     for (int k = 0; k < n; k++) {
       // next segment: rotate chunks at chunk boundaries
       const int kn = k + 1;
@@ -212,13 +229,9 @@ sweep_kernel(const SweepArgs a) {
       float len_n;
       int fsr_n, mat_n;
       unpack(sgn, len_n, fsr_n, mat_n);
-      float2 qn[PS];
-      const float2* qrow = qbase + (int64_t) fsr_n * npairs;
-#pragma unroll
-      for (int s = 0; s < PS; s++)
-        qn[s] = (sub + s * LPS < npairs && kn < n) ? __ldg(qrow + s * LPS)
-                                                   : f2(0.0f);
+      if (kn < n) prefetch_row(fsr_n);
 
+      const float2* qrow = qbase + (int64_t) fsr * npairs;
       const float2* st =
           reinterpret_cast<const float2*>(s_st + mat * ld) + sub;
       float2* ph = reinterpret_cast<float2*>(a.phi + (int64_t) fsr * ld) + sub;
@@ -226,8 +239,8 @@ sweep_kernel(const SweepArgs a) {
 #pragma unroll
       for (int s = 0; s < PS; s++) {
         if (sub + s * LPS < npairs) {
+          const float2 q = __ldg(qrow + s * LPS);
           const float2 tau = __fmul2_rn(st[s * LPS], len2);
-          const float2 nq = make_float2(-q[s].x, -q[s].y);
           float2 tally = f2(0.0f);
 #pragma unroll
           for (int p = 0; p < PH; p++) {
@@ -237,7 +250,8 @@ sweep_kernel(const SweepArgs a) {
               gx = AttenTable::eval2(x2, x2, s_tab);
             else
               gx = AttenIntrinsic::eval2(__fmul2_rn(tau, xl2[p]), x2, s_tab);
-            const float2 d = __fmul2_rn(__fadd2_rn(psi[s][p], nq), gx);
+            // d = (psi - q) * g;  psi -= d;  tally += w * d
+            const float2 d = __fmul2_rn(__ffma2_rn(q, f2(-1.0f), psi[s][p]), gx);
             psi[s][p] = __ffma2_rn(d, f2(-1.0f), psi[s][p]);
             tally = __ffma2_rn(w2[p], d, tally);
           }
@@ -247,8 +261,6 @@ sweep_kernel(const SweepArgs a) {
       len = len_n;
       fsr = fsr_n;
       mat = mat_n;
-#pragma unroll
-      for (int s = 0; s < PS; s++) q[s] = qn[s];
     }
 
     // boundary-flux transfer to the connecting track, fused into the sweep
