@@ -217,6 +217,12 @@ int moc_set_start_flux(moc_ctx* ctx, const float* in, int64_t n);
 int moc_bench_iterations(moc_ctx* ctx, int steps, int res_type, int flush_l2,
                          double* step_ms, double* sweep_ms);
 
+/** g = 1 - exp(-x) for n values with the sweep's evaluator `kind` (the
+ *  attenuation the sweep applies; ExpEvaluator::computeExponential returns
+ *  g(x)/x per unit path, src/ExpEvaluator.h:170-183).  For tests. */
+int moc_eval_attenuation(moc_ctx* ctx, int kind, const float* x, float* g,
+                         int64_t n);
+
 /** Number of CUDA kernels this library launched on the context so far. */
 int moc_get_launch_count(moc_ctx* ctx, int64_t* launches);
 

@@ -88,6 +88,7 @@ _SIGS = {
     "moc_set_start_flux": ([_P, _P, C.c_int64], C.c_int),
     "moc_get_launch_count": ([_P, C.POINTER(C.c_int64)], C.c_int),
     "moc_bench_iterations": ([_P, C.c_int, C.c_int, C.c_int, _P, _P], C.c_int),
+    "moc_eval_attenuation": ([_P, C.c_int, _P, _P, C.c_int64], C.c_int),
 }
 
 _lock = threading.Lock()

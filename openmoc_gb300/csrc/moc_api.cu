@@ -1193,6 +1193,36 @@ int moc_get_sweep_time(moc_ctx* c, double* ms, int64_t* num_sweeps) {
   return MOC_OK;
 }
 
+int moc_eval_attenuation(moc_ctx* c, int kind, const float* x, float* g,
+                         int64_t n) {
+  MOC_CHECK(c && x && g && n >= 0, MOC_ERR_ARG, "bad arguments");
+  MOC_CHECK(kind == MOC_EXP_TABLE || kind == MOC_EXP_INTRINSIC, MOC_ERR_ARG,
+            "unknown exponential evaluator");
+  if (n == 0) return MOC_OK;
+  MOC_CUDA(cudaSetDevice(c->d.device));
+  float *dx = nullptr, *dg = nullptr;
+  MOC_TRY(dalloc(&dx, n));
+  int st = dalloc(&dg, n);
+  if (st != MOC_OK) {
+    dfree(dx);
+    return st;
+  }
+  cudaError_t e = cudaMemcpyAsync(dx, x, 4 * n, cudaMemcpyHostToDevice,
+                                  c->stream);
+  if (e == cudaSuccess) {
+    moc::launch_attenuation(kind, dx, dg, n, c->exp_table, c->stream);
+    c->launches++;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(g, dg, 4 * n, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  dfree(dx);
+  dfree(dg);
+  MOC_CUDA(e);
+  return MOC_OK;
+}
+
 int moc_get_launch_count(moc_ctx* c, int64_t* launches) {
   MOC_CHECK(c && launches, MOC_ERR_ARG, "null argument");
   *launches = c->launches;

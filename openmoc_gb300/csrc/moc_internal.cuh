@@ -106,6 +106,8 @@ bool launch_sweep(const SweepArgs& a, int polar_half, int slots, int exp_kind,
                   cudaStream_t stream);
 int sweep_max_slots(int polar_half);
 bool sweep_lps_supported(int lps);
+void launch_attenuation(int kind, const float* x, float* g, int64_t n,
+                        const float* exp_table, cudaStream_t s);
 // Writes each segment's material into the top 8 bits of its FSR word
 // (valid when num_fsrs < 2^24 and num_materials <= 256); idempotent.
 void launch_pack_materials(int2* segs, int64_t num_segments,

@@ -61,19 +61,21 @@ struct AttenTable {
   }
 };
 
-// g(x) = 1 - exp(-x) from the hardware base-2 exponential (relative error
-// about 2^-22) and the Taylor polynomial T5(x) = x - x^2/2 + x^3/6 - x^4/24
-// + x^5/120.  T5 never falls below g (its remainder is -exp(-z) x^6/720 for
-// some z in (0, x)), and it is accurate to 1e-9 relative below x = 0.1,
-// where 1 - exp(-x) loses relative accuracy to cancellation.  So
-//   g = min(T5(x), 1 + kBias - 2^(-x log2 e))
+// g(x) = 1 - exp(-x) from the hardware base-2 exponential e ~ exp(-x)
+// (relative error about 2^-22) and the Taylor polynomial
+// T5(x) = x - x^2/2 + x^3/6 - x^4/24 + x^5/120.  T5 never falls below g
+// (its remainder is -exp(-z) x^6/720 for some z in (0, x)), and it is
+// accurate to 1e-9 relative below x = 0.1, where 1 - e loses relative
+// accuracy to cancellation.  So
+//   g = min(T5(x), 1 - (1 - kRel) e)
 // takes T5 for small x and the exponential for larger x (where T5 rises
-// away from g): one min instead of a compare and a select.  kBias lifts the
-// exponential branch above g by more than its own error, so the choice is
-// safe near the crossover; the absolute error is at most ~6.4e-7 there and
-// the relative error at most ~2.3e-6 for all x.
+// away from g): one min instead of a compare and a select.  The factor
+// 1 - kRel lifts the exponential branch above g by kRel*e, more than the
+// hardware error, so both branches overestimate and the min is the closer
+// one; the bias vanishes with e for optically thick segments.  The relative
+// error is below ~2e-6 for every x (largest near the crossover x ~ 0.26).
 struct AttenIntrinsic {
-  static constexpr float kBias = 4.0e-7f;
+  static constexpr float kRel = 5.0e-7f;
   __device__ __forceinline__ static float ex2(float v) {
     float r;
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v));
@@ -83,7 +85,7 @@ struct AttenIntrinsic {
   __device__ __forceinline__ static float2 eval2(float2 u2, float2 x2,
                                                  const float2*) {
     const float2 e = make_float2(ex2(u2.x), ex2(u2.y));
-    const float2 big = __ffma2_rn(e, f2(-1.0f), f2(1.0f + kBias));
+    const float2 big = __ffma2_rn(e, f2(kRel - 1.0f), f2(1.0f));
     float2 s = __ffma2_rn(x2, f2(1.0f / 120.0f), f2(-1.0f / 24.0f));
     s = __ffma2_rn(x2, s, f2(1.0f / 6.0f));
     s = __ffma2_rn(x2, s, f2(-0.5f));
@@ -205,16 +207,12 @@ sweep_kernel(const SweepArgs a) {
     int fsr, mat;
     unpack(sg, len, fsr, mat);
     const float2* qbase = reinterpret_cast<const float2*>(a.qt) + sub;
-    // The source row of the next segment is prefetched into L1 one segment
-    // ahead (no registers held); lanes of the stream split its cache lines.
-    const int row_bytes = ld * 4;
-    auto prefetch_row = [&](int r) {
-      const char* p0 = reinterpret_cast<const char*>(a.qt) + (int64_t) r * row_bytes;
-      const char* line = reinterpret_cast<const char*>(
-          reinterpret_cast<uintptr_t>(p0) & ~(uintptr_t) 127);
-      for (int l = sub; (int64_t) (line + 128 * l - p0) < row_bytes; l += LPS)
-        asm volatile("prefetch.global.L1 [%0];" ::"l"(line + 128 * l));
-    };
+    float2 q[PS];
+#pragma unroll
+    for (int s = 0; s < PS; s++)
+      q[s] = (sub + s * LPS < npairs && n > 0)
+                 ? __ldg(qbase + (int64_t) fsr * npairs + s * LPS)
+                 : f2(0.0f);
     for (int k = 0; k < n; k++) {
       // next segment: rotate chunks at chunk boundaries
       const int kn = k + 1;
@@ -229,9 +227,13 @@ sweep_kernel(const SweepArgs a) {
       float len_n;
       int fsr_n, mat_n;
       unpack(sgn, len_n, fsr_n, mat_n);
-      if (kn < n) prefetch_row(fsr_n);
+      float2 qn[PS];
+      const float2* qrow = qbase + (int64_t) fsr_n * npairs;
+#pragma unroll
+      for (int s = 0; s < PS; s++)
+        qn[s] = (sub + s * LPS < npairs && kn < n) ? __ldg(qrow + s * LPS)
+                                                   : f2(0.0f);
 
-      const float2* qrow = qbase + (int64_t) fsr * npairs;
       const float2* st =
           reinterpret_cast<const float2*>(s_st + mat * ld) + sub;
       float2* ph = reinterpret_cast<float2*>(a.phi + (int64_t) fsr * ld) + sub;
@@ -239,7 +241,7 @@ sweep_kernel(const SweepArgs a) {
 #pragma unroll
       for (int s = 0; s < PS; s++) {
         if (sub + s * LPS < npairs) {
-          const float2 q = __ldg(qrow + s * LPS);
+          const float2 qs = q[s];
           const float2 tau = __fmul2_rn(st[s * LPS], len2);
           float2 tally = f2(0.0f);
 #pragma unroll
@@ -251,7 +253,8 @@ sweep_kernel(const SweepArgs a) {
             else
               gx = AttenIntrinsic::eval2(__fmul2_rn(tau, xl2[p]), x2, s_tab);
             // d = (psi - q) * g;  psi -= d;  tally += w * d
-            const float2 d = __fmul2_rn(__ffma2_rn(q, f2(-1.0f), psi[s][p]), gx);
+            const float2 d =
+                __fmul2_rn(__ffma2_rn(qs, f2(-1.0f), psi[s][p]), gx);
             psi[s][p] = __ffma2_rn(d, f2(-1.0f), psi[s][p]);
             tally = __ffma2_rn(w2[p], d, tally);
           }
@@ -261,6 +264,8 @@ sweep_kernel(const SweepArgs a) {
       len = len_n;
       fsr = fsr_n;
       mat = mat_n;
+#pragma unroll
+      for (int s = 0; s < PS; s++) q[s] = qn[s];
     }
 
     // boundary-flux transfer to the connecting track, fused into the sweep

@@ -331,6 +331,14 @@ class GB300Solver:
                    _ptr(st), _ptr(sw))
         return st, sw
 
+    def evaluateAttenuation(self, x, kind: int) -> np.ndarray:
+        """1 - exp(-x) on the GPU with the sweep's evaluator ``kind``."""
+        self._need_ctx()
+        xa = np.ascontiguousarray(x, np.float32).ravel()
+        out = np.empty_like(xa)
+        self._call("moc_eval_attenuation", int(kind), _ptr(xa), _ptr(out), xa.size)
+        return out
+
     def getFluxes(self) -> np.ndarray:
         """All scalar fluxes as an [R, G] array (Solver::getFluxes)."""
         self._need_ctx()
