@@ -1,0 +1,85 @@
+/**
+ * @file GB300Solver.h
+ * @brief OpenMOC Solver subclass that runs the flat-source MOC hot path on a
+ *        GB300 GPU through libopenmoc_gb300.so (include/openmoc_gb300.h).
+ *
+ * Drop-in for OpenMOC's CPUSolver / GPUSolver (src/CPUSolver.h,
+ * src/accel/cuda/GPUSolver.h): it overrides the protected hooks of the
+ * abstract Solver (src/Solver.h:334-431) and the public virtuals used by
+ * callers (getFlux, getFluxes, setFluxes, resetFixedSources,
+ * computeFSRFissionRates), so OpenMOC's own Solver::computeEigenvalue /
+ * computeSource / computeFlux drive it hook by hook.  computeEigenvalue,
+ * computeSource and computeFlux are also redeclared here (hiding the base
+ * versions for callers that hold a GB300Solver) to run the whole source
+ * iteration device-resident, with the same initialisation sequence and
+ * convergence tests as src/Solver.cpp:1352-1700.
+ *
+ * Errors from the library become log_printf(ERROR, ...), which throws
+ * std::logic_error like every OpenMOC validation failure
+ * (src/log.cpp:588-599); SWIG maps that to a Python RuntimeError.
+ *
+ * Compiled against OpenMOC's headers and linked with its library and with
+ * libopenmoc_gb300.so (see INTEGRATION.md for the build lines).
+ */
+#ifndef OPENMOC_GB300_SOLVER_H_
+#define OPENMOC_GB300_SOLVER_H_
+
+#include "Solver.h"
+
+struct moc_ctx;
+
+class GB300Solver : public Solver {
+ protected:
+  moc_ctx* _ctx;
+  int _device;
+  int _exp_kind;           /* -1: chosen by the autotuner */
+  bool _uploaded;
+
+  void check(int status, const char* what);
+  void upload();
+  int materialIndex(Material* m);
+
+  /* Solver hooks (src/Solver.h:334-431) */
+  void initializeFluxArrays();
+  void initializeSourceArrays();
+  void initializeFSRs();
+  void zeroTrackFluxes();
+  void flattenFSRFluxes(FP_PRECISION value);
+  void flattenFSRFluxesChiSpectrum();
+  void storeFSRFluxes();
+  double normalizeFluxes();
+  void computeStabilizingFlux();
+  void stabilizeFlux();
+  void computeFSRSources(int iteration);
+  void computeFSRFissionSources();
+  void computeFSRScatterSources();
+  double computeResidual(residualType res_type);
+  void computeKeff();
+  void addSourceToScalarFlux();
+  void transportSweep();
+
+ public:
+  GB300Solver(TrackGenerator* track_generator = NULL, int device = 0);
+  virtual ~GB300Solver();
+
+  void setTrackGenerator(TrackGenerator* track_generator);
+  double getFlux(long fsr_id, int group);
+  void getFluxes(FP_PRECISION* out_fluxes, int num_fluxes);
+  void setFluxes(FP_PRECISION* in_fluxes, int num_fluxes);
+  void resetFixedSources();
+  void computeFSRFissionRates(double* fission_rates, long num_FSRs,
+                              bool nu = false);
+
+  /** Shared-memory table (0) or hardware ex2 (1) for 1 - exp(-x); the
+   *  default lets the autotuner pick the faster. */
+  void setExponentialEvaluator(int kind);
+
+  /* device-resident source iteration */
+  void computeEigenvalue(int max_iters = 1000,
+                         residualType res_type = FISSION_SOURCE);
+  void computeSource(int max_iters = 1000, double k_eff = 1.0,
+                     residualType res_type = TOTAL_SOURCE);
+  void computeFlux(int max_iters = 1000, bool only_fixed_source = true);
+};
+
+#endif
