@@ -223,6 +223,31 @@ int moc_bench_iterations(moc_ctx* ctx, int steps, int res_type, int flush_l2,
 int moc_eval_attenuation(moc_ctx* ctx, int kind, const float* x, float* g,
                          int64_t n);
 
+/** Largest num_fsrs that moc_fission_source_total_noalloc accepts. */
+#define MOC_NOALLOC_MAX_FSRS (1 << 19)
+
+/** No counterpart in the reference: an entry point that allocates nothing.
+ *  Writes to *total (one device double) the total volume-integrated
+ *  nu-fission source sum_r V_r sum_g nu_sigma_f[fsr_mat[r]][g] phi[r*ld+g],
+ *  the sum keff and the flux normalisation are built from, for callers that
+ *  own their device arrays but cannot allocate device memory: code whose
+ *  GPU memory is held by another framework's pool or caching allocator, and
+ *  code on a latency-critical path that cannot take cudaMalloc's implicit
+ *  device synchronisation.  All pointers are device memory of the current
+ *  device; stream is a cudaStream_t (NULL: the legacy default stream).
+ *  Scratch is a fixed 4 MiB per-FSR array inside the library (held by every
+ *  GPU that loads it), so num_fsrs may not exceed MOC_NOALLOC_MAX_FSRS; the
+ *  first call on a device looks up that array's address (make it before any
+ *  stream capture).  Calls share the array: calls that overlap on the GPU
+ *  (different streams, or threads) race and must be serialised.  The sum is
+ *  deterministic. */
+int moc_fission_source_total_noalloc(const float* phi, int64_t ld,
+                                     const float* nu_sigma_f,
+                                     const int32_t* fsr_mat,
+                                     const float* fsr_vol, int64_t num_fsrs,
+                                     int32_t num_groups, void* stream,
+                                     double* total);
+
 /** Number of CUDA kernels this library launched on the context so far. */
 int moc_get_launch_count(moc_ctx* ctx, int64_t* launches);
 

@@ -89,6 +89,8 @@ _SIGS = {
     "moc_get_launch_count": ([_P, C.POINTER(C.c_int64)], C.c_int),
     "moc_bench_iterations": ([_P, C.c_int, C.c_int, C.c_int, _P, _P], C.c_int),
     "moc_eval_attenuation": ([_P, C.c_int, _P, _P, C.c_int64], C.c_int),
+    "moc_fission_source_total_noalloc": ([_P, C.c_int64, _P, _P, _P, C.c_int64,
+                                          C.c_int32, _P, _P], C.c_int),
 }
 
 _lock = threading.Lock()

@@ -71,6 +71,10 @@ void dfree(T*& p) {
 
 }  // namespace
 
+namespace moc {
+int set_error(int code, const char* msg) { return fail(code, msg); }
+}  // namespace moc
+
 // One timed sweep-kernel configuration of the autotuner.
 struct moc_tune_entry {
   int lps, slots, exp_kind;

@@ -99,6 +99,9 @@ struct SolverArgs {
   int check_done;
 };
 
+// Records the text returned by moc_last_error on this thread; returns code.
+int set_error(int code, const char* msg);
+
 // ---- launchers (sweep.cu) ------------------------------------------------
 // Chooses the kernel instance for (Ph, slots, exp kind).  Returns false if
 // no instance exists.
