@@ -98,6 +98,7 @@ struct moc_ctx {
   // materials
   float* sigma_t = nullptr;
   float* sigma_s = nullptr;
+  float* sigma_s_T = nullptr;         // [M][orig][dest]
   float* nu_sigma_f = nullptr;
   float* chi = nullptr;
   float* scat_out = nullptr;
@@ -201,6 +202,7 @@ moc::SolverArgs solver_args(moc_ctx* c, int check_done) {
   moc::SolverArgs a{};
   a.sigma_t = c->sigma_t;
   a.sigma_s = c->sigma_s;
+  a.sigma_s_T = c->sigma_s_T;
   a.nu_sigma_f = c->nu_sigma_f;
   a.chi = c->chi;
   a.fissile = c->fissile;
@@ -599,6 +601,7 @@ int moc_destroy(moc_ctx* c) {
   dfree(c->inv_sin);
   dfree(c->sigma_t);
   dfree(c->sigma_s);
+  dfree(c->sigma_s_T);
   dfree(c->nu_sigma_f);
   dfree(c->chi);
   dfree(c->scat_out);
@@ -728,6 +731,7 @@ int moc_upload_materials(moc_ctx* c, const float* sigma_t,
   const int M = c->d.num_materials, G = c->d.num_groups;
   const int64_t MG = (int64_t) M * G;
   std::vector<float> scat_out(MG, 0.0f);
+  std::vector<float> ssT((size_t) MG * G);
   std::vector<uint8_t> fis(M, 0);
   for (int m = 0; m < M; m++) {
     for (int g = 0; g < G; g++) {
@@ -748,17 +752,22 @@ int moc_upload_materials(moc_ctx* c, const float* sigma_t,
                   "non-finite scattering data in material " +
                       std::to_string(m));
         scat_out[(int64_t) m * G + g] += v;
+        ssT[((int64_t) m * G + g) * G + gd] = v;
       }
   }
   MOC_CUDA(cudaSetDevice(c->d.device));
   dfree(c->sigma_t);
   dfree(c->sigma_s);
+  dfree(c->sigma_s_T);
   dfree(c->nu_sigma_f);
   dfree(c->chi);
   dfree(c->scat_out);
   dfree(c->fissile);
   MOC_TRY(dalloc(&c->sigma_t, MG));
   MOC_TRY(dalloc(&c->sigma_s, MG * G));
+  MOC_TRY(dalloc(&c->sigma_s_T, MG * G));
+  MOC_CUDA(cudaMemcpy(c->sigma_s_T, ssT.data(), 4 * MG * G,
+                      cudaMemcpyHostToDevice));
   MOC_TRY(dalloc(&c->nu_sigma_f, MG));
   MOC_TRY(dalloc(&c->chi, MG));
   MOC_TRY(dalloc(&c->scat_out, MG));

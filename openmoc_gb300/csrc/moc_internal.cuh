@@ -78,6 +78,7 @@ struct SweepArgs {
 struct SolverArgs {
   const float* sigma_t;      // [M][G]
   const float* sigma_s;      // [M][G][G] dest-major
+  const float* sigma_s_T;    // [M][G][G] origin-major (transposed)
   const float* nu_sigma_f;   // [M][G]
   const float* chi;          // [M][G]
   const uint8_t* fissile;    // [M]

@@ -9,9 +9,11 @@
 //   - keff *= (sum of nu-fission rates) / R and normalisation factor
 //     R / (total fission source), both in FP64;
 //   - FISSION_SOURCE, SCALAR_FLUX and TOTAL_SOURCE residuals in FP64.
-// All reductions are block reductions in double followed by one double
-// atomic per block; the last block (ticket counter) finishes the scalar
-// update on the device, so the host never reads intermediate sums.
+// Every kernel maps one warp to one FSR row (lanes over groups, no integer
+// division), runs on a grid of a few blocks per SM, and reduces in FP64:
+// warp shuffles, one shared-memory pass per block, one double atomic per
+// block; the last block (ticket counter) finishes the scalar update on the
+// device, so the host never reads intermediate sums.
 #include "moc_internal.cuh"
 
 namespace moc {
@@ -22,10 +24,11 @@ constexpr float kFluxEpsilon = 1.0e-25f;           // src/constants.h:15
 constexpr double kFourPi = 12.566370614359172;     // src/constants.h:27
 constexpr double kOneOverFourPi = 0.07957747154594767;
 constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
 
-__device__ __forceinline__ double warp_sum(double v) {
+__device__ __forceinline__ double warp_sum_all_d(double v) {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
 
@@ -35,19 +38,13 @@ __device__ __forceinline__ float warp_sum_all(float v) {
   return v;
 }
 
-__device__ __forceinline__ double warp_sum_all_d(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-// Sums v over the block, adds it to *accum and returns true in thread 0 of
-// the last block to do so (after which *accum holds the grid total).
+// Sums v (one value per warp, taken from lane 0) over the block, adds it to
+// *accum and returns true in thread 0 of the last block to do so (after
+// which *accum holds the grid total).
 __device__ bool block_accumulate(double v, double* accum,
                                  unsigned int* ticket) {
-  __shared__ double part[kThreads / 32];
+  __shared__ double part[kWarps];
   __shared__ int last;
-  v = warp_sum(v);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0) part[warp] = v;
   __syncthreads();
@@ -67,48 +64,87 @@ __device__ __forceinline__ bool skip(const SolverArgs& a) {
   return a.check_done && *(volatile int*) &a.sc->done;
 }
 
+__device__ __forceinline__ int64_t first_row() {
+  return ((int64_t) blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+}
+
+__device__ __forceinline__ int64_t row_step() {
+  return ((int64_t) gridDim.x * blockDim.x) >> 5;
+}
+
 // ---------------------------------------------------------------- sources
-// One warp per FSR: the FSR's flux row is staged in shared memory, the
-// nu-fission rate is a warp reduction and each lane produces the sources of
-// groups lane, lane+32, ... as dot products with rows of the
-// (destination-major) scattering matrix.
+// One warp per FSR: the flux row sits in registers (lane l holds groups
+// l, l+32, ...) and is broadcast group by group with shuffles; the
+// transposed scattering matrices of all materials ([m][orig][dest]) are
+// staged in shared memory, so each step reads one contiguous row of
+// destinations.  The fission term is rank one: chi[dest] * (nu_sigma_f .
+// phi) / k.  S = ceil(G / 32) destination groups per lane.
+template <int S>
 __global__ void __launch_bounds__(kThreads)
-compute_sources_kernel(const SolverArgs a, int iteration, int zero_phi) {
+compute_sources_kernel(const SolverArgs a, int iteration, int zero_phi,
+                       int staged) {
   if (skip(a)) return;
-  extern __shared__ float sm[];
+  extern __shared__ float s_ss[];
   const int G = a.num_groups;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int wpb = blockDim.x >> 5;
-  float* row = sm + warp * G;
+  const int GG = G * G;
+  if (staged) {
+    const int n = a.num_materials * GG;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s_ss[i] = a.sigma_s_T[i];
+    __syncthreads();
+  }
+  const float* ssT = staged ? s_ss : a.sigma_s_T;
+  const int lane = threadIdx.x & 31;
   const double inv_k = 1.0 / a.sc->keff;
   // iteration < 0: the device iteration counter of the running solve
   if (iteration < 0) iteration = a.sc->iteration;
   unsigned long long negatives = 0;
-  for (int64_t r = (int64_t) blockIdx.x * wpb + warp; r < a.num_fsrs;
-       r += (int64_t) gridDim.x * wpb) {
+  for (int64_t r = first_row(); r < a.num_fsrs; r += row_step()) {
     const int m = a.fsr_mat[r];
     float* phi = a.phi + r * a.ld;
-    for (int g = lane; g < G; g += 32) row[g] = phi[g];
-    // fused: the sweep that follows starts from zero tallies; each lane
-    // clears exactly the entries it staged
-    if (zero_phi)
-      for (int g = lane; g < G; g += 32) phi[g] = 0.0f;
-    __syncwarp();
+    float ph[S];
+#pragma unroll
+    for (int j = 0; j < S; j++) {
+      const int g = lane + 32 * j;
+      ph[j] = (g < G) ? phi[g] : 0.0f;
+    }
+    // fused: the sweep that follows starts from zero tallies
+    if (zero_phi) {
+#pragma unroll
+      for (int j = 0; j < S; j++)
+        if (lane + 32 * j < G) phi[lane + 32 * j] = 0.0f;
+    }
     float fr = 0.0f;
     if (a.fissile[m]) {
       const float* nf = a.nu_sigma_f + (int64_t) m * G;
-      for (int g = lane; g < G; g += 32) fr = fmaf(nf[g], row[g], fr);
+#pragma unroll
+      for (int j = 0; j < S; j++)
+        if (lane + 32 * j < G) fr = fmaf(nf[lane + 32 * j], ph[j], fr);
       fr = warp_sum_all(fr);
     }
-    const float* ss = a.sigma_s + (int64_t) m * G * G;
+    const float* mT = ssT + (int64_t) m * GG + lane;
+    float acc[S];
+#pragma unroll
+    for (int j = 0; j < S; j++) acc[j] = 0.0f;
+#pragma unroll
+    for (int js = 0; js < S; js++) {
+      const int gbase = 32 * js;
+      const int gcount = min(32, G - gbase);
+      for (int l = 0; l < gcount; l++) {
+        const float pg = __shfl_sync(0xffffffffu, ph[js], l);
+        const float* col = mT + (int64_t) (gbase + l) * G;
+#pragma unroll
+        for (int j = 0; j < S; j++)
+          if (lane + 32 * j < G) acc[j] = fmaf(col[32 * j], pg, acc[j]);
+      }
+    }
     const float* chi = a.chi + (int64_t) m * G;
     const float* st = a.sigma_t + (int64_t) m * G;
-    for (int gd = lane; gd < G; gd += 32) {
-      const float* srow = ss + (int64_t) gd * G;
-      float s = 0.0f;
-      for (int g = 0; g < G; g++) s = fmaf(__ldg(srow + g), row[g], s);
+#pragma unroll
+    for (int j = 0; j < S; j++) {
+      const int gd = lane + 32 * j;
+      if (gd >= G) continue;
       float q = (float) ((double) chi[gd] * (double) fr * inv_k);
-      q += s;
+      q += acc[j];
       if (a.fixed) q += a.fixed[r * a.ld + gd];
       q *= (float) kOneOverFourPi;
       if (q < 0.0f) {
@@ -117,47 +153,51 @@ compute_sources_kernel(const SolverArgs a, int iteration, int zero_phi) {
       }
       a.qt[r * a.ld + gd] = q / st[gd];
     }
-    __syncwarp();
   }
   if (negatives) atomicAdd(&a.sc->neg_sources, negatives);
 }
 
 // ------------------------------------------------------------- add source
+// update = 1: eigenvalue loop -- the nu-fission total also updates keff,
+// the normalisation factor and the next sweep's angular-flux scale
+// (CPUSolver::computeKeff then normalizeFluxes, src/CPUSolver.cpp:2327,
+// 1910: both use the same volume-integrated nu-fission total).
 __global__ void __launch_bounds__(kThreads)
 add_source_kernel(const SolverArgs a, int update) {
   if (skip(a)) return;
   const int G = a.num_groups;
-  const int64_t n = a.num_fsrs * G;
+  const int lane = threadIdx.x & 31;
   double rate = 0.0;
   unsigned long long negatives = 0;
-  for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t) gridDim.x * blockDim.x) {
-    const int64_t r = i / G;
-    const int g = (int) (i - r * G);
+  for (int64_t r = first_row(); r < a.num_fsrs; r += row_step()) {
     const int m = a.fsr_mat[r];
     const float vol0 = a.fsr_vol[r];
     const float vol = (vol0 < 1.0e-12f) ? 1.0e30f : vol0;
-    const float st = a.sigma_t[(int64_t) m * G + g];
-    const int64_t j = r * a.ld + g;
-    float v = a.phi[j];
-    v /= (st * vol);
-    v += (float) kFourPi * a.qt[j];
-    if (v < 0.0f) {
-      v = kFluxEpsilon;
-      negatives++;
+    const float* st = a.sigma_t + (int64_t) m * G;
+    const float* nf = a.nu_sigma_f + (int64_t) m * G;
+    float* phi = a.phi + r * a.ld;
+    const float* qt = a.qt + r * a.ld;
+    float rr = 0.0f;
+    for (int g = lane; g < G; g += 32) {
+      float v = phi[g];
+      v /= (st[g] * vol);
+      v += (float) kFourPi * qt[g];
+      if (v < 0.0f) {
+        v = kFluxEpsilon;
+        negatives++;
+      }
+      phi[g] = v;
+      rr = fmaf(nf[g], v, rr);
     }
-    a.phi[j] = v;
-    if (update)
-      rate += (double) (a.nu_sigma_f[(int64_t) m * G + g] * v) * (double) vol0;
+    if (update) rate += (double) rr * (double) vol0;
   }
   if (negatives) atomicAdd(&a.sc->neg_fluxes, negatives);
   if (!update) return;
+  rate = warp_sum_all_d(rate);
   DevScalars* sc = a.sc;
   if (block_accumulate(rate, &sc->accum_rate, &sc->ticket_rate)) {
     const double total = *(volatile double*) &sc->accum_rate;
     const double R = (double) a.num_fsrs;
-    // CPUSolver::computeKeff then normalizeFluxes (src/CPUSolver.cpp:2327,
-    // 1910): both use the same volume-integrated nu-fission total.
     sc->keff = sc->keff * (total / R);
     sc->factor = R / total;
     sc->scale[sc->cur] *= (float) sc->factor;
@@ -169,76 +209,68 @@ add_source_kernel(const SolverArgs a, int update) {
 
 // --------------------------------------------------------------- residual
 // One warp per FSR.  Optionally scales phi by sc->factor (the normalisation
-// of the eigenvalue loop), accumulates the residual of res_type against
+// of the eigenvalue loop), accumulates the residual of type RT against
 // phi_old, optionally stores phi into phi_old, and the last block finishes
 // the iteration: convergence test and counters
 // (Solver::computeEigenvalue / computeSource / computeFlux loop bodies,
 // src/Solver.cpp:1390-1450, 1500-1530, 1614-1685).
+template <int RT>
 __global__ void __launch_bounds__(kThreads)
-residual_kernel(const SolverArgs a, int res_type, int normalise, int store,
-                int finish) {
+residual_kernel(const SolverArgs a, int normalise, int store, int finish) {
   if (skip(a)) return;
   DevScalars* sc = a.sc;
   const int G = a.num_groups;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int wpb = blockDim.x >> 5;
+  const int lane = threadIdx.x & 31;
   const double factor = normalise ? sc->factor : 1.0;
   const double inv_k = 1.0 / sc->keff;
   double part = 0.0;
-  for (int64_t r = (int64_t) blockIdx.x * wpb + warp; r < a.num_fsrs;
-       r += (int64_t) gridDim.x * wpb) {
+  for (int64_t r = first_row(); r < a.num_fsrs; r += row_step()) {
     const int m = a.fsr_mat[r];
     const bool fis = a.fissile[m] != 0;
+    if (RT == 1 && !fis && !normalise && !store) continue;
     const float* nf = a.nu_sigma_f + (int64_t) m * G;
-    const float* so = a.scat_out + (int64_t) m * G;
-    double nw = 0.0, od = 0.0, sq = 0.0, snw = 0.0, sod = 0.0;
+    float* phi = a.phi + r * a.ld;
+    float* old = a.phi_old + r * a.ld;
+    double x = 0.0, y = 0.0;   // RT 0: sum of squares; else new and old
     for (int g = lane; g < G; g += 32) {
-      const int64_t j = r * a.ld + g;
-      float v = a.phi[j];
+      float v = phi[g];
       if (normalise) {
         v = (float) ((double) v * factor);
-        a.phi[j] = v;
+        phi[g] = v;
       }
-      const float o = a.phi_old[j];
-      if (res_type == 0) {
+      const float o = old[g];
+      if (RT == 0) {
         if (o > 0.0f) {
           const double d = ((double) v - (double) o) / (double) o;
-          sq += d * d;
+          x += d * d;
+        }
+      } else if (RT == 1) {
+        if (fis) {
+          x += (double) v * nf[g];
+          y += (double) o * nf[g];
         }
       } else {
-        if (fis) {
-          nw += (double) v * nf[g];
-          od += (double) o * nf[g];
-        }
-        if (res_type == 2) {
-          snw += (double) so[g] * v;
-          sod += (double) so[g] * o;
-        }
+        const float so = a.scat_out[(int64_t) m * G + g];
+        const double fv = fis ? (double) v * nf[g] * inv_k : 0.0;
+        const double fo = fis ? (double) o * nf[g] * inv_k : 0.0;
+        x += fv + (double) so * v;
+        y += fo + (double) so * o;
       }
-      if (store) a.phi_old[j] = v;
+      if (store) old[g] = v;
     }
-    if (res_type == 0) {
-      sq = warp_sum_all_d(sq);
-      if (lane == 0) part += sq;
+    x = warp_sum_all_d(x);
+    if (RT == 0) {
+      part += x;
     } else {
-      nw = warp_sum_all_d(nw);
-      od = warp_sum_all_d(od);
-      if (res_type == 2) {
-        snw = warp_sum_all_d(snw);
-        sod = warp_sum_all_d(sod);
-        nw = nw * inv_k + snw;
-        od = od * inv_k + sod;
-        if (lane == 0 && od > 0.0) part += ((nw - od) / od) * ((nw - od) / od);
-      } else if (lane == 0 && fis && od > 0.0) {
-        part += ((nw - od) / od) * ((nw - od) / od);
-      }
+      y = warp_sum_all_d(y);
+      if ((RT == 2 || fis) && y > 0.0) part += ((x - y) / y) * ((x - y) / y);
     }
   }
   if (block_accumulate(part, &sc->accum_res, &sc->ticket_res)) {
     double total = *(volatile double*) &sc->accum_res;
     if (total < 0.0) total = 0.0;
-    double norm = (res_type == 1) ? (double) sc->num_fissionable
-                                  : (double) a.num_fsrs;
+    double norm = (RT == 1) ? (double) sc->num_fissionable
+                            : (double) a.num_fsrs;
     if (norm <= 0.0) norm = 1.0;
     const double residual = sqrt(total / norm);
     sc->residual = residual;
@@ -276,17 +308,16 @@ residual_kernel(const SolverArgs a, int res_type, int normalise, int store,
 __global__ void __launch_bounds__(kThreads)
 fission_rate_kernel(const SolverArgs a, int what) {
   const int G = a.num_groups;
-  const int64_t n = a.num_fsrs * G;
+  const int lane = threadIdx.x & 31;
   double rate = 0.0;
-  for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t) gridDim.x * blockDim.x) {
-    const int64_t r = i / G;
-    const int g = (int) (i - r * G);
-    const int m = a.fsr_mat[r];
-    rate += (double) (a.nu_sigma_f[(int64_t) m * G + g] *
-                      a.phi[r * a.ld + g]) *
-            (double) a.fsr_vol[r];
+  for (int64_t r = first_row(); r < a.num_fsrs; r += row_step()) {
+    const float* nf = a.nu_sigma_f + (int64_t) a.fsr_mat[r] * G;
+    const float* phi = a.phi + r * a.ld;
+    double s = 0.0;
+    for (int g = lane; g < G; g += 32) s += (double) (nf[g] * phi[g]);
+    rate += s * (double) a.fsr_vol[r];
   }
+  rate = warp_sum_all_d(rate);
   DevScalars* sc = a.sc;
   if (block_accumulate(rate, &sc->accum_rate, &sc->ticket_rate)) {
     const double total = *(volatile double*) &sc->accum_rate;
@@ -339,10 +370,8 @@ __global__ void fill_chi_kernel(float* phi, const float* chi, int64_t R,
 // (GPUSolver::computeFSRFissionRates, src/accel/cuda/GPUSolver.cu:1970).
 __global__ void fsr_rates_kernel(const SolverArgs a, double* out, int nu) {
   const int G = a.num_groups;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int wpb = blockDim.x >> 5;
-  for (int64_t r = (int64_t) blockIdx.x * wpb + warp; r < a.num_fsrs;
-       r += (int64_t) gridDim.x * wpb) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t r = first_row(); r < a.num_fsrs; r += row_step()) {
     const int m = a.fsr_mat[r];
     const float* xs = (nu ? a.nu_sigma_f : a.sigma_f) + (int64_t) m * G;
     double s = 0.0;
@@ -360,34 +389,64 @@ int grid_for(int64_t n, int threads) {
   return (int) b;
 }
 
+// Row kernels: one warp per FSR, at most 4 blocks of 8 warps per SM.
+int row_grid(int64_t rows) {
+  int64_t b = (rows + kWarps - 1) / kWarps;
+  if (b > 152 * 4) b = 152 * 4;
+  if (b < 1) b = 1;
+  return (int) b;
+}
+
+template <int S>
+void launch_sources_s(const SolverArgs& a, int iteration, int fused,
+                      cudaStream_t s) {
+  const size_t need =
+      sizeof(float) * (size_t) a.num_materials * a.num_groups * a.num_groups;
+  const int staged = need <= 160 * 1024;
+  const size_t smem = staged ? need : 0;
+  auto kern = compute_sources_kernel<S>;
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int) smem);
+  // staging costs one matrix copy per block: keep the grid near one wave
+  int64_t blocks = (a.num_fsrs + kWarps - 1) / kWarps;
+  if (blocks > 152 * 2) blocks = 152 * 2;
+  kern<<<(unsigned) blocks, kThreads, smem, s>>>(a, iteration, fused, staged);
+}
+
 }  // namespace
 
 void launch_compute_sources(const SolverArgs& a, int iteration, int fused,
                             cudaStream_t s) {
-  const int wpb = kThreads / 32;
-  size_t smem = sizeof(float) * (size_t) a.num_groups * wpb;
-  int blocks = grid_for(a.num_fsrs, wpb);
-  if (smem > 48 * 1024)
-    cudaFuncSetAttribute(compute_sources_kernel,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int) smem);
-  compute_sources_kernel<<<blocks, kThreads, smem, s>>>(a, iteration, fused);
+  switch ((a.num_groups + 31) / 32) {
+    case 1: launch_sources_s<1>(a, iteration, fused, s); break;
+    case 2: launch_sources_s<2>(a, iteration, fused, s); break;
+    case 3: launch_sources_s<3>(a, iteration, fused, s); break;
+    case 4: launch_sources_s<4>(a, iteration, fused, s); break;
+    case 5: launch_sources_s<5>(a, iteration, fused, s); break;
+    case 6: launch_sources_s<6>(a, iteration, fused, s); break;
+    case 7: launch_sources_s<7>(a, iteration, fused, s); break;
+    default: launch_sources_s<12>(a, iteration, fused, s); break;
+  }
 }
 
 void launch_add_source(const SolverArgs& a, int update, cudaStream_t s) {
-  add_source_kernel<<<grid_for(a.num_fsrs * a.num_groups, kThreads), kThreads,
-                      0, s>>>(a, update);
+  add_source_kernel<<<row_grid(a.num_fsrs), kThreads, 0, s>>>(a, update);
 }
 
 void launch_residual(const SolverArgs& a, int res_type, int normalise,
                      int store, int finish, cudaStream_t s) {
-  residual_kernel<<<grid_for(a.num_fsrs, kThreads / 32), kThreads, 0, s>>>(
-      a, res_type, normalise, store, finish);
+  const int b = row_grid(a.num_fsrs);
+  if (res_type == 0)
+    residual_kernel<0><<<b, kThreads, 0, s>>>(a, normalise, store, finish);
+  else if (res_type == 1)
+    residual_kernel<1><<<b, kThreads, 0, s>>>(a, normalise, store, finish);
+  else
+    residual_kernel<2><<<b, kThreads, 0, s>>>(a, normalise, store, finish);
 }
 
 void launch_fission_rate(const SolverArgs& a, int what, cudaStream_t s) {
-  fission_rate_kernel<<<grid_for(a.num_fsrs * a.num_groups, kThreads),
-                        kThreads, 0, s>>>(a, what);
+  fission_rate_kernel<<<row_grid(a.num_fsrs), kThreads, 0, s>>>(a, what);
 }
 
 void launch_scale_phi(const SolverArgs& a, cudaStream_t s) {
@@ -412,8 +471,7 @@ void launch_fill_chi(float* phi, const float* chi, int64_t R, int G, int ld,
 
 void launch_fsr_rates(const SolverArgs& a, double* out, int nu,
                       cudaStream_t s) {
-  fsr_rates_kernel<<<grid_for(a.num_fsrs, kThreads / 32), kThreads, 0, s>>>(
-      a, out, nu);
+  fsr_rates_kernel<<<row_grid(a.num_fsrs), kThreads, 0, s>>>(a, out, nu);
 }
 
 }  // namespace moc
