@@ -765,7 +765,9 @@ int moc_upload_materials(moc_ctx* c, const float* sigma_t,
   dfree(c->fissile);
   MOC_TRY(dalloc(&c->sigma_t, MG));
   MOC_TRY(dalloc(&c->sigma_s, MG * G));
-  MOC_TRY(dalloc(&c->sigma_s_T, MG * G));
+  // padded to whole 16-byte words: the source kernel stages it as float4
+  MOC_TRY(dalloc(&c->sigma_s_T, MG * G + 4));
+  MOC_CUDA(cudaMemset(c->sigma_s_T, 0, 4 * (MG * G + 4)));
   MOC_CUDA(cudaMemcpy(c->sigma_s_T, ssT.data(), 4 * MG * G,
                       cudaMemcpyHostToDevice));
   MOC_TRY(dalloc(&c->nu_sigma_f, MG));

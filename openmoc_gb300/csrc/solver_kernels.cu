@@ -79,72 +79,78 @@ __device__ __forceinline__ int64_t row_step() {
 // staged in shared memory, so each step reads one contiguous row of
 // destinations.  The fission term is rank one: chi[dest] * (nu_sigma_f .
 // phi) / k.  S = ceil(G / 32) destination groups per lane.
+// Two FSR rows per warp pass give two independent accumulation chains.
 template <int S>
-__global__ void __launch_bounds__(kThreads)
-compute_sources_kernel(const SolverArgs a, int iteration, int zero_phi,
-                       int staged) {
-  if (skip(a)) return;
-  extern __shared__ float s_ss[];
+__device__ __forceinline__ void source_rows(const SolverArgs& a,
+                                            const float* ssT, int64_t r0,
+                                            int nrows, int zero_phi,
+                                            int iteration, float inv_k,
+                                            unsigned long long& negatives) {
   const int G = a.num_groups;
   const int GG = G * G;
-  if (staged) {
-    const int n = a.num_materials * GG;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) s_ss[i] = a.sigma_s_T[i];
-    __syncthreads();
-  }
-  const float* ssT = staged ? s_ss : a.sigma_s_T;
   const int lane = threadIdx.x & 31;
-  const double inv_k = 1.0 / a.sc->keff;
-  // iteration < 0: the device iteration counter of the running solve
-  if (iteration < 0) iteration = a.sc->iteration;
-  unsigned long long negatives = 0;
-  for (int64_t r = first_row(); r < a.num_fsrs; r += row_step()) {
-    const int m = a.fsr_mat[r];
+  float ph[2][S], acc[2][S], fr[2];
+  const float* mT[2];
+  int mat[2];
+#pragma unroll
+  for (int i = 0; i < 2; i++) {
+    const int64_t r = r0 + i;
+    const bool on = i < nrows;
+    mat[i] = on ? a.fsr_mat[r] : 0;
     float* phi = a.phi + r * a.ld;
-    float ph[S];
 #pragma unroll
     for (int j = 0; j < S; j++) {
       const int g = lane + 32 * j;
-      ph[j] = (g < G) ? phi[g] : 0.0f;
+      ph[i][j] = (on && g < G) ? phi[g] : 0.0f;
+      acc[i][j] = 0.0f;
     }
     // fused: the sweep that follows starts from zero tallies
-    if (zero_phi) {
+    if (on && zero_phi) {
 #pragma unroll
       for (int j = 0; j < S; j++)
         if (lane + 32 * j < G) phi[lane + 32 * j] = 0.0f;
     }
-    float fr = 0.0f;
-    if (a.fissile[m]) {
-      const float* nf = a.nu_sigma_f + (int64_t) m * G;
+    fr[i] = 0.0f;
+    if (on && a.fissile[mat[i]]) {
+      const float* nf = a.nu_sigma_f + (int64_t) mat[i] * G;
 #pragma unroll
       for (int j = 0; j < S; j++)
-        if (lane + 32 * j < G) fr = fmaf(nf[lane + 32 * j], ph[j], fr);
-      fr = warp_sum_all(fr);
+        if (lane + 32 * j < G) fr[i] = fmaf(nf[lane + 32 * j], ph[i][j], fr[i]);
     }
-    const float* mT = ssT + (int64_t) m * GG + lane;
-    float acc[S];
+    fr[i] = warp_sum_all(fr[i]);
+    mT[i] = ssT + (int64_t) mat[i] * GG + lane;
+  }
 #pragma unroll
-    for (int j = 0; j < S; j++) acc[j] = 0.0f;
+  for (int js = 0; js < S; js++) {
+    const int gbase = 32 * js;
+    const int gcount = min(32, G - gbase);
+#pragma unroll 4
+    for (int l = 0; l < gcount; l++) {
+      const float p0 = __shfl_sync(0xffffffffu, ph[0][js], l);
+      const float p1 = __shfl_sync(0xffffffffu, ph[1][js], l);
+      const float* c0 = mT[0] + (int64_t) (gbase + l) * G;
+      const float* c1 = mT[1] + (int64_t) (gbase + l) * G;
 #pragma unroll
-    for (int js = 0; js < S; js++) {
-      const int gbase = 32 * js;
-      const int gcount = min(32, G - gbase);
-      for (int l = 0; l < gcount; l++) {
-        const float pg = __shfl_sync(0xffffffffu, ph[js], l);
-        const float* col = mT + (int64_t) (gbase + l) * G;
-#pragma unroll
-        for (int j = 0; j < S; j++)
-          if (lane + 32 * j < G) acc[j] = fmaf(col[32 * j], pg, acc[j]);
-      }
+      for (int j = 0; j < S; j++)
+        if (lane + 32 * j < G) {
+          acc[0][j] = fmaf(c0[32 * j], p0, acc[0][j]);
+          acc[1][j] = fmaf(c1[32 * j], p1, acc[1][j]);
+        }
     }
-    const float* chi = a.chi + (int64_t) m * G;
-    const float* st = a.sigma_t + (int64_t) m * G;
+  }
+#pragma unroll
+  for (int i = 0; i < 2; i++) {
+    if (i >= nrows) break;
+    const int64_t r = r0 + i;
+    const float* chi = a.chi + (int64_t) mat[i] * G;
+    const float* st = a.sigma_t + (int64_t) mat[i] * G;
+    const float fk = fr[i] * inv_k;
 #pragma unroll
     for (int j = 0; j < S; j++) {
       const int gd = lane + 32 * j;
       if (gd >= G) continue;
-      float q = (float) ((double) chi[gd] * (double) fr * inv_k);
-      q += acc[j];
+      float q = chi[gd] * fk;
+      q += acc[i][j];
       if (a.fixed) q += a.fixed[r * a.ld + gd];
       q *= (float) kOneOverFourPi;
       if (q < 0.0f) {
@@ -153,6 +159,34 @@ compute_sources_kernel(const SolverArgs a, int iteration, int zero_phi,
       }
       a.qt[r * a.ld + gd] = q / st[gd];
     }
+  }
+}
+
+template <int S>
+__global__ void __launch_bounds__(kThreads)
+compute_sources_kernel(const SolverArgs a, int iteration, int zero_phi,
+                       int staged) {
+  if (skip(a)) return;
+  extern __shared__ float4 s_ss4[];
+  const int G = a.num_groups;
+  if (staged) {
+    // all materials' transposed matrices, 16 bytes per load, all in flight
+    const int n4 = (a.num_materials * G * G + 3) / 4;
+    const float4* src = reinterpret_cast<const float4*>(a.sigma_s_T);
+#pragma unroll 8
+    for (int i = threadIdx.x; i < n4; i += blockDim.x) s_ss4[i] = src[i];
+    __syncthreads();
+  }
+  const float* ssT =
+      staged ? reinterpret_cast<const float*>(s_ss4) : a.sigma_s_T;
+  const float inv_k = (float) (1.0 / a.sc->keff);
+  // iteration < 0: the device iteration counter of the running solve
+  if (iteration < 0) iteration = a.sc->iteration;
+  unsigned long long negatives = 0;
+  const int64_t warp = first_row(), warps = row_step();
+  for (int64_t r = 2 * warp; r < a.num_fsrs; r += 2 * warps) {
+    const int nrows = (r + 1 < a.num_fsrs) ? 2 : 1;
+    source_rows<S>(a, ssT, r, nrows, zero_phi, iteration, inv_k, negatives);
   }
   if (negatives) atomicAdd(&a.sc->neg_sources, negatives);
 }
@@ -221,8 +255,8 @@ residual_kernel(const SolverArgs a, int normalise, int store, int finish) {
   DevScalars* sc = a.sc;
   const int G = a.num_groups;
   const int lane = threadIdx.x & 31;
-  const double factor = normalise ? sc->factor : 1.0;
-  const double inv_k = 1.0 / sc->keff;
+  const float factor = normalise ? (float) sc->factor : 1.0f;
+  const float inv_k = (float) (1.0 / sc->keff);
   double part = 0.0;
   for (int64_t r = first_row(); r < a.num_fsrs; r += row_step()) {
     const int m = a.fsr_mat[r];
@@ -231,39 +265,44 @@ residual_kernel(const SolverArgs a, int normalise, int store, int finish) {
     const float* nf = a.nu_sigma_f + (int64_t) m * G;
     float* phi = a.phi + r * a.ld;
     float* old = a.phi_old + r * a.ld;
-    double x = 0.0, y = 0.0;   // RT 0: sum of squares; else new and old
+    // RT 0: sum of squared relative changes; otherwise x accumulates the
+    // source change from the exact differences v - o and y the old source,
+    // so the relative change keeps its accuracy near convergence
+    float x = 0.0f, y = 0.0f;
     for (int g = lane; g < G; g += 32) {
       float v = phi[g];
       if (normalise) {
-        v = (float) ((double) v * factor);
+        v *= factor;
         phi[g] = v;
       }
       const float o = old[g];
       if (RT == 0) {
         if (o > 0.0f) {
-          const double d = ((double) v - (double) o) / (double) o;
-          x += d * d;
+          const float d = (v - o) / o;
+          x = fmaf(d, d, x);
         }
       } else if (RT == 1) {
         if (fis) {
-          x += (double) v * nf[g];
-          y += (double) o * nf[g];
+          x = fmaf(v - o, nf[g], x);
+          y = fmaf(o, nf[g], y);
         }
       } else {
-        const float so = a.scat_out[(int64_t) m * G + g];
-        const double fv = fis ? (double) v * nf[g] * inv_k : 0.0;
-        const double fo = fis ? (double) o * nf[g] * inv_k : 0.0;
-        x += fv + (double) so * v;
-        y += fo + (double) so * o;
+        const float w = (fis ? nf[g] * inv_k : 0.0f) +
+                        a.scat_out[(int64_t) m * G + g];
+        x = fmaf(v - o, w, x);
+        y = fmaf(o, w, y);
       }
       if (store) old[g] = v;
     }
-    x = warp_sum_all_d(x);
+    x = warp_sum_all(x);
     if (RT == 0) {
-      part += x;
+      part += (double) x;
     } else {
-      y = warp_sum_all_d(y);
-      if ((RT == 2 || fis) && y > 0.0) part += ((x - y) / y) * ((x - y) / y);
+      y = warp_sum_all(y);
+      if ((RT == 2 || fis) && y > 0.0f) {
+        const double t = (double) x / (double) y;
+        part += t * t;
+      }
     }
   }
   if (block_accumulate(part, &sc->accum_res, &sc->ticket_res)) {
