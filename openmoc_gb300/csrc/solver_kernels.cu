@@ -25,6 +25,7 @@ constexpr double kFourPi = 12.566370614359172;     // src/constants.h:27
 constexpr double kOneOverFourPi = 0.07957747154594767;
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
+constexpr int kRowThreads = 1024;   // row kernels: 32 warps per block
 
 __device__ __forceinline__ double warp_sum_all_d(double v) {
 #pragma unroll
@@ -43,7 +44,7 @@ __device__ __forceinline__ float warp_sum_all(float v) {
 // which *accum holds the grid total).
 __device__ bool block_accumulate(double v, double* accum,
                                  unsigned int* ticket) {
-  __shared__ double part[kWarps];
+  __shared__ double part[32];
   __shared__ int last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0) part[warp] = v;
@@ -196,7 +197,7 @@ compute_sources_kernel(const SolverArgs a, int iteration, int zero_phi,
 // the normalisation factor and the next sweep's angular-flux scale
 // (CPUSolver::computeKeff then normalizeFluxes, src/CPUSolver.cpp:2327,
 // 1910: both use the same volume-integrated nu-fission total).
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kRowThreads)
 add_source_kernel(const SolverArgs a, int update) {
   if (skip(a)) return;
   const int G = a.num_groups;
@@ -249,7 +250,7 @@ add_source_kernel(const SolverArgs a, int update) {
 // (Solver::computeEigenvalue / computeSource / computeFlux loop bodies,
 // src/Solver.cpp:1390-1450, 1500-1530, 1614-1685).
 template <int RT>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kRowThreads)
 residual_kernel(const SolverArgs a, int normalise, int store, int finish) {
   if (skip(a)) return;
   DevScalars* sc = a.sc;
@@ -344,7 +345,7 @@ residual_kernel(const SolverArgs a, int normalise, int store, int finish) {
 // 2258-2333); what = 1: factor = R / total and the next sweep's angular
 // fluxes are scaled (CPUSolver::normalizeFluxes, src/CPUSolver.cpp:
 // 1860-1933).
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kRowThreads)
 fission_rate_kernel(const SolverArgs a, int what) {
   const int G = a.num_groups;
   const int lane = threadIdx.x & 31;
@@ -428,10 +429,12 @@ int grid_for(int64_t n, int threads) {
   return (int) b;
 }
 
-// Row kernels: one warp per FSR, at most 4 blocks of 8 warps per SM.
+// Row kernels: one warp per FSR, about one block per SM; few blocks keep
+// the grid-wide finish (one double atomic, a fence and a ticket per block)
+// short.
 int row_grid(int64_t rows) {
-  int64_t b = (rows + kWarps - 1) / kWarps;
-  if (b > 152 * 4) b = 152 * 4;
+  int64_t b = (rows + 2 * 32 - 1) / (2 * 32);
+  if (b > 152) b = 152;
   if (b < 1) b = 1;
   return (int) b;
 }
@@ -470,22 +473,22 @@ void launch_compute_sources(const SolverArgs& a, int iteration, int fused,
 }
 
 void launch_add_source(const SolverArgs& a, int update, cudaStream_t s) {
-  add_source_kernel<<<row_grid(a.num_fsrs), kThreads, 0, s>>>(a, update);
+  add_source_kernel<<<row_grid(a.num_fsrs), kRowThreads, 0, s>>>(a, update);
 }
 
 void launch_residual(const SolverArgs& a, int res_type, int normalise,
                      int store, int finish, cudaStream_t s) {
   const int b = row_grid(a.num_fsrs);
   if (res_type == 0)
-    residual_kernel<0><<<b, kThreads, 0, s>>>(a, normalise, store, finish);
+    residual_kernel<0><<<b, kRowThreads, 0, s>>>(a, normalise, store, finish);
   else if (res_type == 1)
-    residual_kernel<1><<<b, kThreads, 0, s>>>(a, normalise, store, finish);
+    residual_kernel<1><<<b, kRowThreads, 0, s>>>(a, normalise, store, finish);
   else
-    residual_kernel<2><<<b, kThreads, 0, s>>>(a, normalise, store, finish);
+    residual_kernel<2><<<b, kRowThreads, 0, s>>>(a, normalise, store, finish);
 }
 
 void launch_fission_rate(const SolverArgs& a, int what, cudaStream_t s) {
-  fission_rate_kernel<<<row_grid(a.num_fsrs), kThreads, 0, s>>>(a, what);
+  fission_rate_kernel<<<row_grid(a.num_fsrs), kRowThreads, 0, s>>>(a, what);
 }
 
 void launch_scale_phi(const SolverArgs& a, cudaStream_t s) {
@@ -510,7 +513,7 @@ void launch_fill_chi(float* phi, const float* chi, int64_t R, int G, int ld,
 
 void launch_fsr_rates(const SolverArgs& a, double* out, int nu,
                       cudaStream_t s) {
-  fsr_rates_kernel<<<row_grid(a.num_fsrs), kThreads, 0, s>>>(a, out, nu);
+  fsr_rates_kernel<<<row_grid(a.num_fsrs), kRowThreads, 0, s>>>(a, out, nu);
 }
 
 }  // namespace moc
