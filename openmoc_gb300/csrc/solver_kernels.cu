@@ -197,6 +197,10 @@ compute_sources_kernel(const SolverArgs a, int iteration, int zero_phi,
 // the normalisation factor and the next sweep's angular-flux scale
 // (CPUSolver::computeKeff then normalizeFluxes, src/CPUSolver.cpp:2327,
 // 1910: both use the same volume-integrated nu-fission total).
+// Row kernels keep a whole FSR row in registers (S = ceil(G/32) values per
+// lane): every load of the row is issued before the first store, so a row
+// costs one memory round trip.
+template <int S>
 __global__ void __launch_bounds__(kRowThreads)
 add_source_kernel(const SolverArgs a, int update) {
   if (skip(a)) return;
@@ -208,21 +212,30 @@ add_source_kernel(const SolverArgs a, int update) {
     const int m = a.fsr_mat[r];
     const float vol0 = a.fsr_vol[r];
     const float vol = (vol0 < 1.0e-12f) ? 1.0e30f : vol0;
-    const float* st = a.sigma_t + (int64_t) m * G;
-    const float* nf = a.nu_sigma_f + (int64_t) m * G;
-    float* phi = a.phi + r * a.ld;
-    const float* qt = a.qt + r * a.ld;
+    const float* __restrict__ st = a.sigma_t + (int64_t) m * G;
+    const float* __restrict__ nf = a.nu_sigma_f + (int64_t) m * G;
+    float* __restrict__ phi = a.phi + r * a.ld;
+    const float* __restrict__ qt = a.qt + r * a.ld;
+    float v[S], q[S];
+#pragma unroll
+    for (int j = 0; j < S; j++) {
+      const int g = lane + 32 * j;
+      v[j] = (g < G) ? phi[g] : 0.0f;
+      q[j] = (g < G) ? qt[g] : 0.0f;
+    }
     float rr = 0.0f;
-    for (int g = lane; g < G; g += 32) {
-      float v = phi[g];
-      v /= (st[g] * vol);
-      v += (float) kFourPi * qt[g];
-      if (v < 0.0f) {
-        v = kFluxEpsilon;
+#pragma unroll
+    for (int j = 0; j < S; j++) {
+      const int g = lane + 32 * j;
+      if (g >= G) continue;
+      float x = v[j] / (st[g] * vol);
+      x += (float) kFourPi * q[j];
+      if (x < 0.0f) {
+        x = kFluxEpsilon;
         negatives++;
       }
-      phi[g] = v;
-      rr = fmaf(nf[g], v, rr);
+      phi[g] = x;
+      rr = fmaf(nf[g], x, rr);
     }
     if (update) rate += (double) rr * (double) vol0;
   }
@@ -249,7 +262,7 @@ add_source_kernel(const SolverArgs a, int update) {
 // the iteration: convergence test and counters
 // (Solver::computeEigenvalue / computeSource / computeFlux loop bodies,
 // src/Solver.cpp:1390-1450, 1500-1530, 1614-1685).
-template <int RT>
+template <int RT, int S>
 __global__ void __launch_bounds__(kRowThreads)
 residual_kernel(const SolverArgs a, int normalise, int store, int finish) {
   if (skip(a)) return;
@@ -263,20 +276,30 @@ residual_kernel(const SolverArgs a, int normalise, int store, int finish) {
     const int m = a.fsr_mat[r];
     const bool fis = a.fissile[m] != 0;
     if (RT == 1 && !fis && !normalise && !store) continue;
-    const float* nf = a.nu_sigma_f + (int64_t) m * G;
-    float* phi = a.phi + r * a.ld;
-    float* old = a.phi_old + r * a.ld;
+    const float* __restrict__ nf = a.nu_sigma_f + (int64_t) m * G;
+    float* __restrict__ phi = a.phi + r * a.ld;
+    float* __restrict__ old = a.phi_old + r * a.ld;
+    float vv[S], oo[S];
+#pragma unroll
+    for (int j = 0; j < S; j++) {
+      const int g = lane + 32 * j;
+      vv[j] = (g < G) ? phi[g] : 0.0f;
+      oo[j] = (g < G) ? old[g] : 0.0f;
+    }
     // RT 0: sum of squared relative changes; otherwise x accumulates the
     // source change from the exact differences v - o and y the old source,
     // so the relative change keeps its accuracy near convergence
     float x = 0.0f, y = 0.0f;
-    for (int g = lane; g < G; g += 32) {
-      float v = phi[g];
+#pragma unroll
+    for (int j = 0; j < S; j++) {
+      const int g = lane + 32 * j;
+      if (g >= G) continue;
+      float v = vv[j];
       if (normalise) {
         v *= factor;
         phi[g] = v;
       }
-      const float o = old[g];
+      const float o = oo[j];
       if (RT == 0) {
         if (o > 0.0f) {
           const float d = (v - o) / o;
@@ -472,19 +495,55 @@ void launch_compute_sources(const SolverArgs& a, int iteration, int fused,
   }
 }
 
+namespace {
+
+template <int S>
+void launch_add_source_s(const SolverArgs& a, int update, cudaStream_t s) {
+  add_source_kernel<S><<<row_grid(a.num_fsrs), kRowThreads, 0, s>>>(a, update);
+}
+
+template <int S>
+void launch_residual_s(const SolverArgs& a, int res_type, int normalise,
+                       int store, int finish, cudaStream_t s) {
+  const int b = row_grid(a.num_fsrs);
+  if (res_type == 0)
+    residual_kernel<0, S><<<b, kRowThreads, 0, s>>>(a, normalise, store,
+                                                     finish);
+  else if (res_type == 1)
+    residual_kernel<1, S><<<b, kRowThreads, 0, s>>>(a, normalise, store,
+                                                     finish);
+  else
+    residual_kernel<2, S><<<b, kRowThreads, 0, s>>>(a, normalise, store,
+                                                     finish);
+}
+
+}  // namespace
+
 void launch_add_source(const SolverArgs& a, int update, cudaStream_t s) {
-  add_source_kernel<<<row_grid(a.num_fsrs), kRowThreads, 0, s>>>(a, update);
+  switch ((a.num_groups + 31) / 32) {
+    case 1: launch_add_source_s<1>(a, update, s); break;
+    case 2: launch_add_source_s<2>(a, update, s); break;
+    case 3: launch_add_source_s<3>(a, update, s); break;
+    case 4: launch_add_source_s<4>(a, update, s); break;
+    case 5: launch_add_source_s<5>(a, update, s); break;
+    case 6: launch_add_source_s<6>(a, update, s); break;
+    case 7: launch_add_source_s<7>(a, update, s); break;
+    default: launch_add_source_s<12>(a, update, s); break;
+  }
 }
 
 void launch_residual(const SolverArgs& a, int res_type, int normalise,
                      int store, int finish, cudaStream_t s) {
-  const int b = row_grid(a.num_fsrs);
-  if (res_type == 0)
-    residual_kernel<0><<<b, kRowThreads, 0, s>>>(a, normalise, store, finish);
-  else if (res_type == 1)
-    residual_kernel<1><<<b, kRowThreads, 0, s>>>(a, normalise, store, finish);
-  else
-    residual_kernel<2><<<b, kRowThreads, 0, s>>>(a, normalise, store, finish);
+  switch ((a.num_groups + 31) / 32) {
+    case 1: launch_residual_s<1>(a, res_type, normalise, store, finish, s); break;
+    case 2: launch_residual_s<2>(a, res_type, normalise, store, finish, s); break;
+    case 3: launch_residual_s<3>(a, res_type, normalise, store, finish, s); break;
+    case 4: launch_residual_s<4>(a, res_type, normalise, store, finish, s); break;
+    case 5: launch_residual_s<5>(a, res_type, normalise, store, finish, s); break;
+    case 6: launch_residual_s<6>(a, res_type, normalise, store, finish, s); break;
+    case 7: launch_residual_s<7>(a, res_type, normalise, store, finish, s); break;
+    default: launch_residual_s<12>(a, res_type, normalise, store, finish, s); break;
+  }
 }
 
 void launch_fission_rate(const SolverArgs& a, int what, cudaStream_t s) {
