@@ -32,6 +32,11 @@ sys.path.insert(0, ROOT)
 WORKLOAD = "17x17 pin lattice, 70 groups, 64 azimuthal, 0.05 cm, TY-6 (3 polar), reflective"
 METRIC = "segment*group*polar integrations/s"
 FLOPS_PER_INTEGRATION = 30   # FP32 flops of one integration (FMA = 2)
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one sweep launch
+# of this workload, from one ncu capture per sweep shape (lanes per track
+# direction, group pairs per lane, exponential kind); the summaries are under
+# profiles/ (sweep_kernel_17x17_70g.txt).
+SWEEP_DRAM_BYTES = {(8, 5, 1): 50_847_744 + 1_447_424}
 
 
 def env_rank():
@@ -224,11 +229,7 @@ def run_gpu(args):
     nbytes = algorithmic_bytes(p)
     achieved = nbytes / (sweep_avg * 1e-3) / 1e9
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    traffic = None
-    tfile = os.path.join(ROOT, "profiles", "sweep_traffic.json")
-    if os.path.exists(tfile):
-        with open(tfile) as f:
-            traffic = json.load(f).get("dram_bytes_per_launch")
+    traffic = SWEEP_DRAM_BYTES.get((lps, slots, exp_kind))
     sm_mhz = clocks.get("sm_mhz") or float(peaks.get("sm_max_mhz", 2070.0))
     props = torch.cuda.get_device_properties(local)
     fp32_peak = props.multi_processor_count * 128 * 2 * sm_mhz * 1e6 / 1e12
