@@ -46,6 +46,10 @@ struct DevScalars {
   unsigned long long neg_sources;
   unsigned long long neg_fluxes;
   long long num_fissionable;
+  // batched pools: this solve's FSR rows are [row0, row0 + nrows) of the
+  // pool's arrays; unused by single-problem contexts
+  long long row0;
+  long long nrows;
 };
 
 enum SolveMode { kModeEigen = 0, kModeSource = 1, kModeFlux = 2, kModeHook = 3 };
@@ -73,6 +77,12 @@ struct SweepArgs {
   int lps;                   // lanes per track direction (1..32, power of 2)
   int check_done;            // return at once if sc->done is set
   int mat_packed;            // segs[].y = fsr | material << 24
+  // Batched pools (null for a single problem): the solve each track belongs
+  // to, whose state supplies the pending angular-flux scale and the done
+  // flag; sc then only carries the pool's buffer index and ticket.
+  const int32_t* track_slot; // [T]
+  DevScalars* slots;         // [num_slots]
+  int num_slots;
 };
 
 struct SolverArgs {
@@ -98,6 +108,13 @@ struct SolverArgs {
   int ld;                    // row stride of the [R][*] arrays (even, >= G)
   int num_materials;
   int check_done;
+  // Batched pools (null for a single problem): the solve owning each FSR row
+  // (-1: unused row), the per-solve states, and one FP64 partial per row for
+  // the per-solve reductions.
+  const int32_t* row_slot;   // [R]
+  DevScalars* slots;         // [num_slots]
+  double* row_val;           // [R]
+  int num_slots;
 };
 
 // Records the text returned by moc_last_error on this thread; returns code.
@@ -138,5 +155,33 @@ void launch_fill_chi(float* phi, const float* chi, int64_t R, int G, int ld,
                      cudaStream_t s);
 void launch_fsr_rates(const SolverArgs& a, double* out, int nu,
                       cudaStream_t s);
+
+// ---- batched pools (solver_kernels.cu) -------------------------------------
+// The loop body of every live solve of a pool; a.num_fsrs is the end of the
+// highest row in use.  Sources take each row's keff and iteration from its
+// solve; add-source leaves each eigenvalue row's nu-fission rate in row_val;
+// rate_finish (one block per solve) updates keff, the normalisation factor
+// and the pending angular-flux scale; residual normalises, leaves each row's
+// residual term in row_val and stores phi_old; residual_finish ends the
+// iteration of every live solve (convergence, counters, done).
+void launch_batch_sources(const SolverArgs& a, cudaStream_t s);
+void launch_batch_add_source(const SolverArgs& a, cudaStream_t s);
+void launch_batch_rate_finish(const SolverArgs& a, cudaStream_t s);
+void launch_batch_residual(const SolverArgs& a, cudaStream_t s);
+void launch_batch_residual_finish(const SolverArgs& a, cudaStream_t s);
+// Initial state of one admitted solve: rows [r0, r0 + n) of phi and phi_old
+// set to value, qt zeroed.
+void launch_batch_init_rows(const SolverArgs& a, int64_t r0, int64_t n,
+                            float value, cudaStream_t s);
+// Rebases one admitted solve's track data from its own numbering to the
+// pool's: FSR ids (+r0) with the pool material of the FSR (fsr_mat, already
+// in pool numbering) packed into the top 8 bits, next-track links (+t0),
+// angle rows (+a0), segment offsets (+s0, T + 1 of them); track_slot of the
+// T + 1 track entries is set to slot.
+void launch_batch_rebase(int2* segs, int64_t S, const int32_t* fsr_mat,
+                         int32_t r0, int64_t* seg_off, int32_t* next,
+                         int32_t* track_ang, int32_t* track_slot, int64_t T,
+                         int64_t s0, int32_t t0, int32_t a0, int32_t slot,
+                         cudaStream_t s);
 
 }  // namespace moc

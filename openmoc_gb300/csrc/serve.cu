@@ -1,0 +1,1251 @@
+// The batched solve server of include/openmoc_gb300_serve.h: a
+// device-resident request loop that runs many independent solves of uneven
+// size on one GPU.
+//
+// Each pool (one group count and polar count) keeps the solves it holds in
+// shared device arrays.  A solve owns contiguous ranges of FSR rows, track
+// entries, segments, materials and angle rows, handed out by first-fit
+// allocators over the pool's capacity; its track data are uploaded in its
+// own numbering and rebased on the device.  An iteration of the pool is one
+// launch of each kernel for every live solve (solver_kernels.cu batch_*,
+// and the tuned sweep kernel over the concatenated track list, longest
+// tracks first), and blocks of iterations are replayed as captured CUDA
+// graphs.  Per solve, the loop body and convergence test are those of
+// Solver::computeEigenvalue / computeSource (src/Solver.cpp:1459-1700): the
+// same kernels' arithmetic, with reductions split per solve.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/openmoc_gb300.h"
+#include "../../include/openmoc_gb300_serve.h"
+#include "moc_internal.cuh"
+
+namespace {
+
+#define SV_FAIL(code, msg) moc::set_error(code, std::string(msg).c_str())
+
+#define SV_CHECK(cond, code, msg)          \
+  do {                                     \
+    if (!(cond)) return SV_FAIL(code, msg); \
+  } while (0)
+
+#define SV_CUDA(call)                                                     \
+  do {                                                                    \
+    cudaError_t e_ = (call);                                              \
+    if (e_ != cudaSuccess)                                                \
+      return SV_FAIL(MOC_ERR_CUDA,                                        \
+                     std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+#define SV_TRY(expr)               \
+  do {                             \
+    int s_ = (expr);               \
+    if (s_ != MOC_OK) return s_;   \
+  } while (0)
+
+double now_s() {
+  return std::chrono::duration<double>(
+             std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+
+template <typename T>
+int dev_alloc(T** p, size_t n) {
+  *p = nullptr;
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc((void**) p, n * sizeof(T));
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    return SV_FAIL(MOC_ERR_MEMORY, "device memory exhausted creating a pool (" +
+                                       std::to_string(n * sizeof(T)) +
+                                       " bytes)");
+  }
+  SV_CUDA(e);
+  return MOC_OK;
+}
+
+template <typename T>
+void dev_free(T*& p) {
+  if (p) cudaFree((void*) p);
+  p = nullptr;
+}
+
+// First-fit allocator of ranges of [0, capacity).
+class RangeAlloc {
+ public:
+  void reset(int64_t cap) {
+    cap_ = cap;
+    free_.clear();
+    if (cap > 0) free_[0] = cap;
+  }
+  // offset of a free range of n >= 1 entries, or -1
+  int64_t alloc(int64_t n) {
+    n = std::max<int64_t>(n, 1);
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+      if (it->second < n) continue;
+      const int64_t off = it->first, len = it->second;
+      free_.erase(it);
+      if (len > n) free_[off + n] = len - n;
+      return off;
+    }
+    return -1;
+  }
+  void release(int64_t off, int64_t n) {
+    n = std::max<int64_t>(n, 1);
+    auto next = free_.lower_bound(off);
+    if (next != free_.end() && next->first == off + n) {
+      n += next->second;
+      next = free_.erase(next);
+    }
+    if (next != free_.begin()) {
+      auto prev = std::prev(next);
+      if (prev->first + prev->second == off) {
+        prev->second += n;
+        return;
+      }
+    }
+    free_[off] = n;
+  }
+ private:
+  int64_t cap_ = 0;
+  std::map<int64_t, int64_t> free_;
+};
+
+// A validated request, packed in its own numbering, waiting for or holding
+// a pool slot.
+struct Staged {
+  int64_t ticket = 0;
+  moc_request req{};
+  int pool = -1;
+  int G = 0, Ph = 0, A = 0, M = 0, ld = 0;
+  int64_t R = 0, T = 0, S = 0;
+  std::vector<int2> segs;          // {length bits, local FSR}
+  std::vector<int64_t> seg_off;    // [T + 1]
+  std::vector<int32_t> next;       // [2T]
+  std::vector<int32_t> track_ang;  // [T]
+  std::vector<int32_t> nseg;       // [T]
+  std::vector<uint8_t> flags;      // [T + 1]
+  std::vector<float> weights, inv_sin;
+  std::vector<float> sigma_t, sigma_s_T, nu_sigma_f, chi, scat_out;
+  std::vector<uint8_t> fissile;
+  std::vector<int32_t> fsr_mat;
+  std::vector<float> fsr_vol;
+  std::vector<float> fixed;        // [R][ld] or empty
+  long long num_fissionable = 0;
+  double init_flux = 1.0;          // flat starting flux (normalised)
+  double t_submit = 0.0, t_admit = 0.0;
+
+  void release_arrays() {
+    std::vector<int2>().swap(segs);
+    std::vector<int64_t>().swap(seg_off);
+    std::vector<int32_t>().swap(next);
+    std::vector<int32_t>().swap(track_ang);
+    std::vector<uint8_t>().swap(flags);
+    std::vector<float>().swap(weights);
+    std::vector<float>().swap(inv_sin);
+    std::vector<float>().swap(sigma_t);
+    std::vector<float>().swap(sigma_s_T);
+    std::vector<float>().swap(nu_sigma_f);
+    std::vector<float>().swap(chi);
+    std::vector<float>().swap(scat_out);
+    std::vector<uint8_t>().swap(fissile);
+    std::vector<float>().swap(fsr_vol);
+    std::vector<float>().swap(fixed);
+  }
+};
+
+// Checks a request as moc_upload_* check a context's inputs and packs it.
+int stage_request(const moc_request& q, Staged& s) {
+  SV_CHECK(q.num_groups >= 1 && q.num_groups <= 64 * moc::kMaxSlots,
+           MOC_ERR_ARG, "num_groups must be in [1, 384]");
+  SV_CHECK(q.num_polar_half >= 1 && q.num_polar_half <= 3, MOC_ERR_UNSUPPORTED,
+           "num_polar_half must be 1, 2 or 3");
+  SV_CHECK(q.num_angles >= 1 && q.num_materials >= 1 && q.num_fsrs >= 1 &&
+               q.num_tracks >= 1 && q.num_segments >= 0,
+           MOC_ERR_ARG, "empty problem dimension");
+  SV_CHECK(q.num_materials <= 256 && q.num_fsrs < (1LL << 24) &&
+               q.num_tracks < (1LL << 30),
+           MOC_ERR_ARG, "request too large for a pool");
+  SV_CHECK(q.seg_off && q.track_ang && q.next && q.flags && q.weights &&
+               q.inv_sin && q.sigma_t && q.sigma_s && q.nu_sigma_f && q.chi &&
+               q.fsr_mat && q.fsr_vol && q.flux_out,
+           MOC_ERR_ARG, "null array in request");
+  SV_CHECK(q.num_segments == 0 || (q.seg_len && q.seg_fsr), MOC_ERR_ARG,
+           "null segments");
+  SV_CHECK(q.kind == MOC_SOLVE_EIGENVALUE || q.kind == MOC_SOLVE_SOURCE,
+           MOC_ERR_ARG, "unknown solve kind");
+  SV_CHECK(q.max_iters >= 1, MOC_ERR_ARG, "max_iters must be positive");
+  SV_CHECK(q.res_type >= 0 && q.res_type <= 2, MOC_ERR_ARG,
+           "bad residual type");
+  SV_CHECK(q.threshold > 0.0 && std::isfinite(q.threshold), MOC_ERR_ARG,
+           "the convergence threshold must be positive");
+  SV_CHECK(q.kind != MOC_SOLVE_SOURCE || q.k_eff > 0.0, MOC_ERR_ARG,
+           "The Solver is unable to compute the source with a non-positive "
+           "keff");
+  const int G = q.num_groups, M = q.num_materials, Ph = q.num_polar_half;
+  const int64_t R = q.num_fsrs, T = q.num_tracks, S = q.num_segments;
+  s.req = q;
+  s.G = G;
+  s.Ph = Ph;
+  s.A = q.num_angles;
+  s.M = M;
+  s.R = R;
+  s.T = T;
+  s.S = S;
+  s.ld = G + (G & 1);
+
+  // tracks
+  SV_CHECK(q.seg_off[0] == 0 && q.seg_off[T] == S, MOC_ERR_ARG,
+           "seg_off must run from 0 to num_segments");
+  s.seg_off.assign(q.seg_off, q.seg_off + T + 1);
+  s.nseg.resize(T);
+  s.next.resize(2 * T);
+  s.track_ang.resize(T);
+  s.flags.assign(q.flags, q.flags + T);
+  s.flags.push_back(0);
+  for (int64_t t = 0; t < T; t++) {
+    const int64_t n = q.seg_off[t + 1] - q.seg_off[t];
+    SV_CHECK(n >= 0 && n < (1LL << 31), MOC_ERR_ARG,
+             "bad segment count on track " + std::to_string(t));
+    s.nseg[t] = (int32_t) n;
+    SV_CHECK(q.track_ang[t] >= 0 && q.track_ang[t] < q.num_angles,
+             MOC_ERR_ARG, "track angle index out of range");
+    s.track_ang[t] = q.track_ang[t];
+    for (int d = 0; d < 2; d++) {
+      SV_CHECK(q.next[2 * t + d] >= 0 && q.next[2 * t + d] < T, MOC_ERR_ARG,
+               "next-track index out of range on track " + std::to_string(t));
+      s.next[2 * t + d] = (int32_t) q.next[2 * t + d];
+    }
+  }
+  s.segs.resize(S);
+  for (int64_t i = 0; i < S; i++) {
+    SV_CHECK(q.seg_fsr[i] >= 0 && q.seg_fsr[i] < R, MOC_ERR_ARG,
+             "segment FSR id out of range at segment " + std::to_string(i));
+    SV_CHECK(std::isfinite(q.seg_len[i]) && q.seg_len[i] >= 0.0f, MOC_ERR_ARG,
+             "bad segment length at segment " + std::to_string(i));
+    int2 v;
+    std::memcpy(&v.x, &q.seg_len[i], 4);
+    v.y = q.seg_fsr[i];
+    s.segs[i] = v;
+  }
+
+  // quadrature
+  const int64_t nq = (int64_t) q.num_angles * Ph;
+  s.weights.assign(q.weights, q.weights + nq);
+  s.inv_sin.assign(q.inv_sin, q.inv_sin + nq);
+  for (int64_t i = 0; i < nq; i++)
+    SV_CHECK(std::isfinite(q.weights[i]) && std::isfinite(q.inv_sin[i]) &&
+                 q.inv_sin[i] >= 1.0f,
+             MOC_ERR_ARG, "bad quadrature entry " + std::to_string(i));
+
+  // materials
+  const int64_t MG = (int64_t) M * G;
+  s.sigma_t.assign(q.sigma_t, q.sigma_t + MG);
+  s.nu_sigma_f.assign(q.nu_sigma_f, q.nu_sigma_f + MG);
+  s.chi.assign(q.chi, q.chi + MG);
+  s.scat_out.assign(MG, 0.0f);
+  s.sigma_s_T.assign(MG * G, 0.0f);
+  s.fissile.assign(M, 0);
+  for (int m = 0; m < M; m++) {
+    for (int g = 0; g < G; g++) {
+      const int64_t i = (int64_t) m * G + g;
+      SV_CHECK(std::isfinite(q.sigma_t[i]) && q.sigma_t[i] > 0.0f,
+               MOC_ERR_ARG, "sigma_t must be positive and finite (material " +
+                                std::to_string(m) + ")");
+      SV_CHECK(std::isfinite(q.nu_sigma_f[i]) && std::isfinite(q.chi[i]),
+               MOC_ERR_ARG, "non-finite fission data in material " +
+                                std::to_string(m));
+      if (q.nu_sigma_f[i] > 0.0f) s.fissile[m] = 1;
+    }
+    for (int gd = 0; gd < G; gd++)
+      for (int g = 0; g < G; g++) {
+        const float v = q.sigma_s[((int64_t) m * G + gd) * G + g];
+        SV_CHECK(std::isfinite(v), MOC_ERR_ARG,
+                 "non-finite scattering data in material " +
+                     std::to_string(m));
+        s.scat_out[(int64_t) m * G + g] += v;
+        s.sigma_s_T[((int64_t) m * G + g) * G + gd] = v;
+      }
+  }
+
+  // FSRs
+  s.fsr_mat.assign(q.fsr_mat, q.fsr_mat + R);
+  s.fsr_vol.assign(q.fsr_vol, q.fsr_vol + R);
+  double total = 0.0;
+  for (int64_t r = 0; r < R; r++) {
+    SV_CHECK(q.fsr_mat[r] >= 0 && q.fsr_mat[r] < M, MOC_ERR_ARG,
+             "FSR material index out of range at FSR " + std::to_string(r));
+    SV_CHECK(std::isfinite(q.fsr_vol[r]) && q.fsr_vol[r] >= 0.0f, MOC_ERR_ARG,
+             "bad FSR volume at FSR " + std::to_string(r));
+    const int m = q.fsr_mat[r];
+    if (s.fissile[m]) {
+      s.num_fissionable++;
+      double row = 0.0;
+      for (int g = 0; g < G; g++) row += (double) q.nu_sigma_f[(int64_t) m * G + g];
+      total += row * (double) q.fsr_vol[r];
+    }
+  }
+  if (q.kind == MOC_SOLVE_EIGENVALUE) {
+    SV_CHECK(s.num_fissionable > 0 && total > 0.0, MOC_ERR_ARG,
+             "an eigenvalue solve needs fissionable material");
+    // Solver::computeInitialFluxGuess then normalizeFluxes: a flat flux of
+    // one scaled by R / (total fission source)
+    s.init_flux = (double) (float) ((double) R / total);
+  } else {
+    s.init_flux = 1.0;
+  }
+  SV_CHECK(q.res_type != MOC_FISSION_SOURCE || s.num_fissionable > 0,
+           MOC_ERR_ARG,
+           "The Solver is unable to compute a FISSION_SOURCE residual "
+           "without fissionable FSRs");
+  if (q.fixed_source) {
+    s.fixed.assign((size_t) R * s.ld, 0.0f);
+    for (int64_t r = 0; r < R; r++)
+      for (int g = 0; g < G; g++) {
+        const float v = q.fixed_source[r * G + g];
+        SV_CHECK(std::isfinite(v), MOC_ERR_ARG, "non-finite fixed source");
+        s.fixed[r * s.ld + g] = v;
+      }
+  }
+  return MOC_OK;
+}
+
+}  // namespace
+
+struct moc_server;
+
+namespace {
+
+// A pool slot: one live solve and the ranges it owns.
+struct Slot {
+  std::unique_ptr<Staged> st;
+  int64_t r0 = 0, t0 = 0, s0 = 0;
+  int64_t m0 = 0, a0 = 0;
+  bool live = false;
+  bool uploaded = false;    // data copied into the pool's arrays
+  bool needs_init = false;  // starting state not yet written
+};
+
+struct Pool {
+  moc_pool_config cfg{};
+  int index = 0;
+  int G = 0, Ph = 0, ld = 0, F = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t block_done = nullptr;
+  std::vector<cudaEvent_t> tune_ev;
+
+  // device arrays over the pool's capacity
+  int2* segs = nullptr;
+  int64_t* seg_off = nullptr;
+  int32_t* order = nullptr;
+  int32_t* track_ang = nullptr;
+  int32_t* next = nullptr;
+  int32_t* track_slot = nullptr;
+  uint8_t* flags = nullptr;
+  float* weights = nullptr;
+  float* inv_sin = nullptr;
+  float* sigma_t = nullptr;
+  float* sigma_s_T = nullptr;
+  float* nu_sigma_f = nullptr;
+  float* chi = nullptr;
+  float* scat_out = nullptr;
+  uint8_t* fissile = nullptr;
+  int32_t* fsr_mat = nullptr;
+  int32_t* row_slot = nullptr;
+  float* fsr_vol = nullptr;
+  float* fixed = nullptr;
+  float* phi = nullptr;
+  float* phi_old = nullptr;
+  float* qt = nullptr;
+  float* psi[2] = {nullptr, nullptr};
+  float* exp_table = nullptr;
+  double* row_val = nullptr;
+  moc::DevScalars* sc = nullptr;       // pool: buffer index and ticket
+  moc::DevScalars* slots_d = nullptr;  // per-solve states
+  moc::DevScalars* slots_h = nullptr;  // pinned: states read back per block
+  moc::DevScalars* init_h = nullptr;   // pinned: states written at admission
+  float* retire_h = nullptr;           // pinned: fluxes of retired solves
+
+  RangeAlloc rows, tracks, segments, mats, angles;
+  std::vector<int> free_slots;
+  std::vector<Slot> slots;
+  std::deque<std::unique_ptr<Staged>> queue;  // guarded by the server mutex
+
+  bool in_flight = false;
+  bool dirty = false;
+  int64_t active_tracks = 0;
+  int64_t rows_hi = 0;
+  int64_t mats_hi = 0;
+  cudaGraphExec_t graph = nullptr;
+  int graph_iters = 0;
+
+  int lps = 0, pairs = 0, exp_kind = MOC_EXP_INTRINSIC;
+  bool tuned = false;
+};
+
+}  // namespace
+
+struct moc_server {
+  moc_server_config cfg{};
+  std::vector<std::unique_ptr<Pool>> pools;
+  std::mutex mu;                     // queues, results, counters
+  std::condition_variable cv;
+  std::map<int64_t, moc_result> results;
+  std::vector<int64_t> completed;    // since the last poll
+  int64_t next_ticket = 1;
+  moc_server_stats stats{};
+  std::thread loop;
+  std::atomic<bool> running{false};
+  std::string loop_error;
+  std::vector<float> exp_table_h;
+};
+
+namespace {
+
+void destroy_pool(Pool& p) {
+  if (p.stream) cudaStreamSynchronize(p.stream);
+  if (p.graph) cudaGraphExecDestroy(p.graph);
+  dev_free(p.segs);
+  dev_free(p.seg_off);
+  dev_free(p.order);
+  dev_free(p.track_ang);
+  dev_free(p.next);
+  dev_free(p.track_slot);
+  dev_free(p.flags);
+  dev_free(p.weights);
+  dev_free(p.inv_sin);
+  dev_free(p.sigma_t);
+  dev_free(p.sigma_s_T);
+  dev_free(p.nu_sigma_f);
+  dev_free(p.chi);
+  dev_free(p.scat_out);
+  dev_free(p.fissile);
+  dev_free(p.fsr_mat);
+  dev_free(p.row_slot);
+  dev_free(p.fsr_vol);
+  dev_free(p.fixed);
+  dev_free(p.phi);
+  dev_free(p.phi_old);
+  dev_free(p.qt);
+  dev_free(p.psi[0]);
+  dev_free(p.psi[1]);
+  dev_free(p.exp_table);
+  dev_free(p.row_val);
+  dev_free(p.sc);
+  dev_free(p.slots_d);
+  if (p.slots_h) cudaFreeHost(p.slots_h);
+  if (p.init_h) cudaFreeHost(p.init_h);
+  if (p.retire_h) cudaFreeHost(p.retire_h);
+  p.slots_h = p.init_h = nullptr;
+  p.retire_h = nullptr;
+  for (cudaEvent_t e : p.tune_ev) cudaEventDestroy(e);
+  if (p.block_done) cudaEventDestroy(p.block_done);
+  if (p.stream) cudaStreamDestroy(p.stream);
+  p.stream = nullptr;
+}
+
+int create_pool(moc_server* srv, const moc_pool_config& c, Pool& p) {
+  SV_CHECK(c.num_groups >= 1 && c.num_groups <= 64 * moc::kMaxSlots,
+           MOC_ERR_ARG, "num_groups must be in [1, 384]");
+  SV_CHECK(c.num_polar_half >= 1 && c.num_polar_half <= 3,
+           MOC_ERR_UNSUPPORTED, "num_polar_half must be 1, 2 or 3");
+  SV_CHECK(c.max_solves >= 1 && c.max_solves <= 4096 && c.max_materials >= 1 &&
+               c.max_materials <= 256 && c.max_angles >= 1 &&
+               c.max_fsrs >= 1 && c.max_fsrs < (1LL << 24) &&
+               c.max_tracks >= 2 && c.max_tracks < (1LL << 30) &&
+               c.max_segments >= 1,
+           MOC_ERR_ARG, "bad pool capacity");
+  const int ld = c.num_groups + (c.num_groups & 1);
+  SV_CHECK((int64_t) c.max_materials * ld * 4 <= 200 * 1024, MOC_ERR_ARG,
+           "max_materials x groups exceeds the sweep's shared-memory table");
+  if (c.lanes != 0) {
+    SV_CHECK(moc::sweep_lps_supported(c.lanes), MOC_ERR_ARG,
+             "lanes per track direction must be 1, 2, 4, 8, 16 or 32");
+    SV_CHECK(c.pairs >= 1 && c.pairs <= moc::kMaxSlots &&
+                 2 * (int64_t) c.lanes * c.pairs >= c.num_groups,
+             MOC_ERR_ARG, "lanes x group pairs per lane must cover every group");
+    SV_CHECK(c.exp_kind == MOC_EXP_TABLE || c.exp_kind == MOC_EXP_INTRINSIC,
+             MOC_ERR_ARG, "unknown exponential evaluator");
+  }
+  p.cfg = c;
+  p.G = c.num_groups;
+  p.Ph = c.num_polar_half;
+  p.ld = ld;
+  p.F = p.G * p.Ph;
+  if (c.lanes != 0) {
+    p.lps = c.lanes;
+    p.pairs = c.pairs;
+    p.exp_kind = c.exp_kind;
+    p.tuned = true;
+  }
+  SV_CUDA(cudaStreamCreateWithFlags(&p.stream, cudaStreamNonBlocking));
+  SV_CUDA(cudaEventCreateWithFlags(&p.block_done, cudaEventDisableTiming));
+  const int64_t R = c.max_fsrs, T = c.max_tracks, S = c.max_segments;
+  const int64_t M = c.max_materials, A = c.max_angles, N = c.max_solves;
+  const int64_t MG = M * p.G, npsi = T * 2 * p.F;
+  SV_TRY(dev_alloc(&p.segs, S));
+  SV_TRY(dev_alloc(&p.seg_off, T));
+  SV_TRY(dev_alloc(&p.order, T));
+  SV_TRY(dev_alloc(&p.track_ang, T));
+  SV_TRY(dev_alloc(&p.next, 2 * T));
+  SV_TRY(dev_alloc(&p.track_slot, T));
+  SV_TRY(dev_alloc(&p.flags, T));
+  SV_TRY(dev_alloc(&p.weights, A * p.Ph));
+  SV_TRY(dev_alloc(&p.inv_sin, A * p.Ph));
+  SV_TRY(dev_alloc(&p.sigma_t, MG));
+  SV_TRY(dev_alloc(&p.sigma_s_T, MG * p.G + 4));
+  SV_TRY(dev_alloc(&p.nu_sigma_f, MG));
+  SV_TRY(dev_alloc(&p.chi, MG));
+  SV_TRY(dev_alloc(&p.scat_out, MG));
+  SV_TRY(dev_alloc(&p.fissile, M));
+  SV_TRY(dev_alloc(&p.fsr_mat, R));
+  SV_TRY(dev_alloc(&p.row_slot, R));
+  SV_TRY(dev_alloc(&p.fsr_vol, R));
+  SV_TRY(dev_alloc(&p.fixed, R * ld));
+  SV_TRY(dev_alloc(&p.phi, R * ld));
+  SV_TRY(dev_alloc(&p.phi_old, R * ld));
+  SV_TRY(dev_alloc(&p.qt, R * ld));
+  SV_TRY(dev_alloc(&p.psi[0], npsi));
+  SV_TRY(dev_alloc(&p.psi[1], npsi));
+  SV_TRY(dev_alloc(&p.exp_table, 2 * moc::kExpTableSize));
+  SV_TRY(dev_alloc(&p.row_val, R));
+  SV_TRY(dev_alloc(&p.sc, 1));
+  SV_TRY(dev_alloc(&p.slots_d, N));
+  SV_CUDA(cudaMallocHost((void**) &p.slots_h, sizeof(moc::DevScalars) * N));
+  SV_CUDA(cudaMallocHost((void**) &p.init_h, sizeof(moc::DevScalars) * N));
+  SV_CUDA(cudaMallocHost((void**) &p.retire_h, sizeof(float) * R * ld));
+  // every slot starts free: done, so every kernel skips it
+  std::vector<moc::DevScalars> st(N);
+  std::memset(st.data(), 0, sizeof(moc::DevScalars) * N);
+  for (auto& s : st) {
+    s.done = 1;
+    s.keff = 1.0;
+    s.scale[0] = s.scale[1] = 1.0f;
+  }
+  std::memcpy(p.slots_h, st.data(), sizeof(moc::DevScalars) * N);
+  moc::DevScalars pool_sc;
+  std::memset(&pool_sc, 0, sizeof(pool_sc));
+  pool_sc.keff = 1.0;
+  pool_sc.scale[0] = pool_sc.scale[1] = 1.0f;
+  SV_CUDA(cudaMemcpy(p.slots_d, st.data(), sizeof(moc::DevScalars) * N,
+                     cudaMemcpyHostToDevice));
+  SV_CUDA(cudaMemcpy(p.sc, &pool_sc, sizeof(pool_sc), cudaMemcpyHostToDevice));
+  SV_CUDA(cudaMemcpy(p.exp_table, srv->exp_table_h.data(),
+                     sizeof(float) * srv->exp_table_h.size(),
+                     cudaMemcpyHostToDevice));
+  SV_CUDA(cudaMemset(p.row_slot, 0xFF, sizeof(int32_t) * R));
+  SV_CUDA(cudaMemset(p.fixed, 0, sizeof(float) * R * ld));
+  SV_CUDA(cudaMemset(p.phi, 0, sizeof(float) * R * ld));
+  SV_CUDA(cudaMemset(p.phi_old, 0, sizeof(float) * R * ld));
+  SV_CUDA(cudaMemset(p.qt, 0, sizeof(float) * R * ld));
+  SV_CUDA(cudaMemset(p.psi[0], 0, sizeof(float) * npsi));
+  SV_CUDA(cudaMemset(p.psi[1], 0, sizeof(float) * npsi));
+  SV_CUDA(cudaMemset(p.sigma_s_T, 0, sizeof(float) * (MG * p.G + 4)));
+  p.rows.reset(R);
+  p.tracks.reset(T);
+  p.segments.reset(S);
+  p.mats.reset(M);
+  p.angles.reset(A);
+  p.slots.resize(N);
+  for (int i = (int) N - 1; i >= 0; i--) p.free_slots.push_back(i);
+  return MOC_OK;
+}
+
+moc::SweepArgs pool_sweep_args(Pool& p) {
+  moc::SweepArgs a{};
+  a.segs = p.segs;
+  a.seg_off = p.seg_off;
+  a.order = p.order;
+  a.track_ang = p.track_ang;
+  a.next = p.next;
+  a.flags = p.flags;
+  a.weights = p.weights;
+  a.inv_sin = p.inv_sin;
+  a.sigma_t = p.sigma_t;
+  a.fsr_mat = p.fsr_mat;
+  a.qt = p.qt;
+  a.exp_table = p.exp_table;
+  a.phi = p.phi;
+  a.psi[0] = p.psi[0];
+  a.psi[1] = p.psi[1];
+  a.sc = p.sc;
+  a.num_tracks = p.active_tracks;
+  a.num_groups = p.G;
+  a.ld = p.ld;
+  a.num_materials = (int) std::max<int64_t>(p.mats_hi, 1);
+  a.lps = p.lps;
+  a.check_done = 0;
+  a.mat_packed = 1;
+  a.track_slot = p.track_slot;
+  a.slots = p.slots_d;
+  a.num_slots = p.cfg.max_solves;
+  return a;
+}
+
+moc::SolverArgs pool_solver_args(Pool& p) {
+  moc::SolverArgs a{};
+  a.sigma_t = p.sigma_t;
+  a.sigma_s = nullptr;
+  a.sigma_s_T = p.sigma_s_T;
+  a.nu_sigma_f = p.nu_sigma_f;
+  a.chi = p.chi;
+  a.fissile = p.fissile;
+  a.fsr_mat = p.fsr_mat;
+  a.fsr_vol = p.fsr_vol;
+  a.fixed = p.fixed;
+  a.scat_out = p.scat_out;
+  a.sigma_f = nullptr;
+  a.phi = p.phi;
+  a.phi_old = p.phi_old;
+  a.qt = p.qt;
+  a.psi[0] = p.psi[0];
+  a.psi[1] = p.psi[1];
+  a.sc = p.sc;
+  a.num_fsrs = p.rows_hi;
+  a.num_psi = p.cfg.max_tracks * 2 * p.F;
+  a.num_groups = p.G;
+  a.ld = p.ld;
+  a.num_materials = (int) std::max<int64_t>(p.mats_hi, 1);
+  a.check_done = 0;
+  a.row_slot = p.row_slot;
+  a.slots = p.slots_d;
+  a.row_val = p.row_val;
+  a.num_slots = p.cfg.max_solves;
+  return a;
+}
+
+}  // namespace
+
+namespace {
+
+void add_launches(moc_server* srv, int64_t n) {
+  std::lock_guard<std::mutex> lk(srv->mu);
+  srv->stats.kernel_launches += n;
+}
+
+void publish(moc_server* srv, const Staged& st, const moc_result& r) {
+  std::lock_guard<std::mutex> lk(srv->mu);
+  srv->results[st.ticket] = r;
+  srv->completed.push_back(st.ticket);
+  if (r.status == MOC_OK) srv->stats.completed++;
+  else srv->stats.failed++;
+  srv->stats.live--;
+  srv->cv.notify_all();
+}
+
+// Copies a solve's data into the ranges given to it and rebases them.
+int upload_slot(moc_server* srv, Pool& p, int slot_index) {
+  Slot& sl = p.slots[slot_index];
+  Staged& s = *sl.st;
+  cudaStream_t st = p.stream;
+  const int64_t T = s.T, S = s.S, R = s.R, G = s.G;
+  const int64_t MG = (int64_t) s.M * G;
+  std::vector<int32_t> mat(s.fsr_mat.size());
+  for (size_t i = 0; i < mat.size(); i++) mat[i] = s.fsr_mat[i] + (int32_t) sl.m0;
+  std::vector<int32_t> owner(R, slot_index);
+  if (S > 0)
+    SV_CUDA(cudaMemcpyAsync(p.segs + sl.s0, s.segs.data(), sizeof(int2) * S,
+                            cudaMemcpyHostToDevice, st));
+  SV_CUDA(cudaMemcpyAsync(p.seg_off + sl.t0, s.seg_off.data(),
+                          sizeof(int64_t) * (T + 1), cudaMemcpyHostToDevice, st));
+  SV_CUDA(cudaMemcpyAsync(p.next + 2 * sl.t0, s.next.data(),
+                          sizeof(int32_t) * 2 * T, cudaMemcpyHostToDevice, st));
+  SV_CUDA(cudaMemcpyAsync(p.track_ang + sl.t0, s.track_ang.data(),
+                          sizeof(int32_t) * T, cudaMemcpyHostToDevice, st));
+  SV_CUDA(cudaMemcpyAsync(p.flags + sl.t0, s.flags.data(), T + 1,
+                          cudaMemcpyHostToDevice, st));
+  SV_CUDA(cudaMemcpyAsync(p.weights + sl.a0 * p.Ph, s.weights.data(),
+                          sizeof(float) * s.weights.size(),
+                          cudaMemcpyHostToDevice, st));
+  SV_CUDA(cudaMemcpyAsync(p.inv_sin + sl.a0 * p.Ph, s.inv_sin.data(),
+                          sizeof(float) * s.inv_sin.size(),
+                          cudaMemcpyHostToDevice, st));
+  SV_CUDA(cudaMemcpyAsync(p.sigma_t + sl.m0 * G, s.sigma_t.data(),
+                          sizeof(float) * MG, cudaMemcpyHostToDevice, st));
+  SV_CUDA(cudaMemcpyAsync(p.sigma_s_T + sl.m0 * G * G, s.sigma_s_T.data(),
+                          sizeof(float) * MG * G, cudaMemcpyHostToDevice, st));
+  SV_CUDA(cudaMemcpyAsync(p.nu_sigma_f + sl.m0 * G, s.nu_sigma_f.data(),
+                          sizeof(float) * MG, cudaMemcpyHostToDevice, st));
+  SV_CUDA(cudaMemcpyAsync(p.chi + sl.m0 * G, s.chi.data(), sizeof(float) * MG,
+                          cudaMemcpyHostToDevice, st));
+  SV_CUDA(cudaMemcpyAsync(p.scat_out + sl.m0 * G, s.scat_out.data(),
+                          sizeof(float) * MG, cudaMemcpyHostToDevice, st));
+  SV_CUDA(cudaMemcpyAsync(p.fissile + sl.m0, s.fissile.data(), s.M,
+                          cudaMemcpyHostToDevice, st));
+  SV_CUDA(cudaMemcpyAsync(p.fsr_mat + sl.r0, mat.data(), sizeof(int32_t) * R,
+                          cudaMemcpyHostToDevice, st));
+  SV_CUDA(cudaMemcpyAsync(p.fsr_vol + sl.r0, s.fsr_vol.data(),
+                          sizeof(float) * R, cudaMemcpyHostToDevice, st));
+  if (s.fixed.empty())
+    SV_CUDA(cudaMemsetAsync(p.fixed + sl.r0 * p.ld, 0,
+                            sizeof(float) * R * p.ld, st));
+  else
+    SV_CUDA(cudaMemcpyAsync(p.fixed + sl.r0 * p.ld, s.fixed.data(),
+                            sizeof(float) * R * p.ld, cudaMemcpyHostToDevice,
+                            st));
+  moc::launch_batch_rebase(p.segs + sl.s0, S, p.fsr_mat, (int32_t) sl.r0,
+                           p.seg_off + sl.t0, p.next + 2 * sl.t0,
+                           p.track_ang + sl.t0, p.track_slot + sl.t0, T, sl.s0,
+                           (int32_t) sl.t0, (int32_t) sl.a0, slot_index, st);
+  SV_CUDA(cudaGetLastError());
+  // rows become visible to the row kernels only with their owner set, after
+  // the data above in stream order
+  SV_CUDA(cudaMemcpyAsync(p.row_slot + sl.r0, owner.data(),
+                          sizeof(int32_t) * R, cudaMemcpyHostToDevice, st));
+  add_launches(srv, 1);
+  return MOC_OK;
+}
+
+// Starting state of an admitted solve (Solver::computeEigenvalue /
+// computeSource before their loops, src/Solver.cpp:1459-1580): flat flux,
+// normalised for an eigenvalue solve, stored as the old flux; zero boundary
+// fluxes; keff 1 or the given one.
+int init_slot(moc_server* srv, Pool& p, int slot_index) {
+  Slot& sl = p.slots[slot_index];
+  Staged& s = *sl.st;
+  moc::SolverArgs a = pool_solver_args(p);
+  moc::launch_batch_init_rows(a, sl.r0, s.R, (float) s.init_flux, p.stream);
+  SV_CUDA(cudaGetLastError());
+  const size_t psi_bytes = sizeof(float) * (size_t) (s.T + 1) * 2 * p.F;
+  for (int b = 0; b < 2; b++)
+    SV_CUDA(cudaMemsetAsync(p.psi[b] + sl.t0 * 2 * p.F, 0, psi_bytes,
+                            p.stream));
+  moc::DevScalars& d = p.init_h[slot_index];
+  std::memset(&d, 0, sizeof(d));
+  const bool eigen = s.req.kind == MOC_SOLVE_EIGENVALUE;
+  d.keff = eigen ? 1.0 : s.req.k_eff;
+  d.k_prev = d.keff;
+  d.factor = 1.0;
+  d.threshold = s.req.threshold;
+  d.scale[0] = d.scale[1] = 1.0f;
+  d.max_iters = s.req.max_iters;
+  d.mode = eigen ? moc::kModeEigen : moc::kModeSource;
+  d.res_type = s.req.res_type;
+  d.num_fissionable = s.num_fissionable;
+  d.row0 = sl.r0;
+  d.nrows = s.R;
+  SV_CUDA(cudaMemcpyAsync(p.slots_d + slot_index, &d, sizeof(d),
+                          cudaMemcpyHostToDevice, p.stream));
+  sl.needs_init = false;
+  add_launches(srv, 1);
+  return MOC_OK;
+}
+
+// Admits queued requests while a slot and every range fit.
+int admit(moc_server* srv, Pool& p) {
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    for (auto it = p.queue.begin(); it != p.queue.end();) {
+      Staged& s = **it;
+      if (p.free_slots.empty()) break;
+      const int64_t r0 = p.rows.alloc(s.R);
+      const int64_t t0 = (r0 >= 0) ? p.tracks.alloc(s.T + 1) : -1;
+      const int64_t s0 = (t0 >= 0) ? p.segments.alloc(s.S) : -1;
+      const int64_t m0 = (s0 >= 0) ? p.mats.alloc(s.M) : -1;
+      const int64_t a0 = (m0 >= 0) ? p.angles.alloc(s.A) : -1;
+      if (a0 < 0) {
+        if (r0 >= 0) p.rows.release(r0, s.R);
+        if (t0 >= 0) p.tracks.release(t0, s.T + 1);
+        if (s0 >= 0) p.segments.release(s0, s.S);
+        if (m0 >= 0) p.mats.release(m0, s.M);
+        ++it;
+        continue;
+      }
+      const int idx = p.free_slots.back();
+      p.free_slots.pop_back();
+      Slot& sl = p.slots[idx];
+      sl.r0 = r0;
+      sl.t0 = t0;
+      sl.s0 = s0;
+      sl.m0 = m0;
+      sl.a0 = a0;
+      sl.live = true;
+      sl.uploaded = false;
+      sl.needs_init = true;
+      s.t_admit = now_s();
+      sl.st = std::move(*it);
+      it = p.queue.erase(it);
+      srv->stats.admitted++;
+      srv->stats.queued--;
+      srv->stats.live++;
+      p.dirty = true;
+    }
+  }
+  for (int i = 0; i < (int) p.slots.size(); i++) {
+    Slot& sl = p.slots[i];
+    if (!sl.live || sl.uploaded) continue;
+    SV_TRY(upload_slot(srv, p, i));
+    sl.uploaded = true;
+    // pageable copies are staged by the time cudaMemcpyAsync returns
+    sl.st->release_arrays();
+  }
+  return MOC_OK;
+}
+
+// Copies out and publishes every solve that the last block finished: all
+// their flux rows are copied into the pinned buffer at their own row
+// offsets, with one synchronisation.
+int retire(moc_server* srv, Pool& p) {
+  std::vector<int> done;
+  for (int i = 0; i < (int) p.slots.size(); i++) {
+    const Slot& sl = p.slots[i];
+    if (sl.live && !sl.needs_init && p.slots_h[i].done) done.push_back(i);
+  }
+  if (done.empty()) return MOC_OK;
+  for (int i : done) {
+    const Slot& sl = p.slots[i];
+    const int64_t R = sl.st->R;
+    SV_CUDA(cudaMemcpyAsync(p.retire_h + sl.r0 * p.ld, p.phi + sl.r0 * p.ld,
+                            sizeof(float) * R * p.ld, cudaMemcpyDeviceToHost,
+                            p.stream));
+    // the rows leave the row kernels' view before they are reused
+    SV_CUDA(cudaMemsetAsync(p.row_slot + sl.r0, 0xFF, sizeof(int32_t) * R,
+                            p.stream));
+  }
+  SV_CUDA(cudaStreamSynchronize(p.stream));
+  for (int i : done) {
+    Slot& sl = p.slots[i];
+    Staged& s = *sl.st;
+    const moc::DevScalars& d = p.slots_h[i];
+    const float* rows = p.retire_h + sl.r0 * p.ld;
+    for (int64_t r = 0; r < s.R; r++)
+      std::memcpy(s.req.flux_out + r * s.G, rows + r * p.ld,
+                  sizeof(float) * s.G);
+    moc_result res{};
+    res.status = MOC_OK;
+    res.converged = d.converged;
+    res.iterations = (s.req.kind == MOC_SOLVE_EIGENVALUE)
+                         ? d.iteration
+                         : (d.converged ? d.iteration - 1 : s.req.max_iters);
+    res.pool = p.index;
+    res.keff = d.keff;
+    res.residual = d.residual;
+    res.t_submit = s.t_submit;
+    res.t_admit = s.t_admit;
+    res.t_done = now_s();
+    p.rows.release(sl.r0, s.R);
+    p.tracks.release(sl.t0, s.T + 1);
+    p.segments.release(sl.s0, s.S);
+    p.mats.release(sl.m0, s.M);
+    p.angles.release(sl.a0, s.A);
+    sl.live = false;
+    publish(srv, s, res);
+    sl.st.reset();
+    p.free_slots.push_back(i);
+    p.dirty = true;
+  }
+  return MOC_OK;
+}
+
+}  // namespace
+
+namespace {
+
+// Track list of every live solve, longest tracks first, and the extents of
+// the rows and materials in use.
+int rebuild_order(Pool& p) {
+  std::vector<std::pair<int32_t, int32_t>> keyed;  // (-segments, track)
+  int64_t rows_hi = 0, mats_hi = 0;
+  for (const Slot& sl : p.slots) {
+    if (!sl.live) continue;
+    const Staged& s = *sl.st;
+    for (int64_t t = 0; t < s.T; t++)
+      keyed.emplace_back(-s.nseg[t], (int32_t) (sl.t0 + t));
+    rows_hi = std::max(rows_hi, sl.r0 + s.R);
+    mats_hi = std::max(mats_hi, sl.m0 + s.M);
+  }
+  std::sort(keyed.begin(), keyed.end());
+  std::vector<int32_t> order(keyed.size());
+  for (size_t i = 0; i < keyed.size(); i++) order[i] = keyed[i].second;
+  if (!order.empty())
+    SV_CUDA(cudaMemcpyAsync(p.order, order.data(),
+                            sizeof(int32_t) * order.size(),
+                            cudaMemcpyHostToDevice, p.stream));
+  p.active_tracks = (int64_t) order.size();
+  p.rows_hi = rows_hi;
+  p.mats_hi = mats_hi;
+  p.dirty = false;
+  if (p.graph) {
+    cudaGraphExecDestroy(p.graph);
+    p.graph = nullptr;
+  }
+  return MOC_OK;
+}
+
+// Group pairs per lane for G groups over lps lanes.
+int pairs_for(int G, int lps) { return ((G + 1) / 2 + lps - 1) / lps; }
+
+// Times every sweep shape with at most kMaxSlots pairs per lane and at
+// least half of its lanes busy, with both exponential evaluators, on the
+// pool's current solves (median of three sweeps after a warm-up), and keeps
+// the fastest.  Runs before those solves' starting state is written.
+int autotune_pool(moc_server* srv, Pool& p) {
+  if (p.tune_ev.empty()) {
+    p.tune_ev.resize(2);
+    for (auto& e : p.tune_ev) SV_CUDA(cudaEventCreate(&e));
+  }
+  float best_ms = 1e30f;
+  int best_lps = 0, best_pairs = 0, best_kind = MOC_EXP_INTRINSIC;
+  for (int kind : {MOC_EXP_TABLE, MOC_EXP_INTRINSIC}) {
+    for (int lps = 1; lps <= 32; lps *= 2) {
+      const int pairs = pairs_for(p.G, lps);
+      if (pairs > moc::kMaxSlots ||
+          (double) p.G / (2.0 * lps * pairs) < 0.5)
+        continue;
+      p.lps = lps;
+      moc::SweepArgs a = pool_sweep_args(p);
+      std::vector<float> ms;
+      for (int r = 0; r < 4; r++) {
+        SV_CUDA(cudaEventRecord(p.tune_ev[0], p.stream));
+        if (!moc::launch_sweep(a, p.Ph, pairs, kind, p.stream))
+          return SV_FAIL(MOC_ERR_UNSUPPORTED, "no sweep kernel for the pool");
+        SV_CUDA(cudaEventRecord(p.tune_ev[1], p.stream));
+        SV_CUDA(cudaEventSynchronize(p.tune_ev[1]));
+        float t = 0.f;
+        SV_CUDA(cudaEventElapsedTime(&t, p.tune_ev[0], p.tune_ev[1]));
+        if (r > 0) ms.push_back(t);
+      }
+      add_launches(srv, 4);
+      std::sort(ms.begin(), ms.end());
+      if (ms[1] < best_ms) {
+        best_ms = ms[1];
+        best_lps = lps;
+        best_pairs = pairs;
+        best_kind = kind;
+      }
+    }
+  }
+  SV_CHECK(best_lps > 0, MOC_ERR_UNSUPPORTED, "no sweep kernel shape fits");
+  p.lps = best_lps;
+  p.pairs = best_pairs;
+  p.exp_kind = best_kind;
+  p.tuned = true;
+  // the timing sweeps flipped the buffer index and wrote tallies and
+  // boundary fluxes that the starting state below overwrites
+  return MOC_OK;
+}
+
+// One source iteration of every live solve of the pool: six launches.
+int enqueue_iteration(Pool& p) {
+  moc::SolverArgs a = pool_solver_args(p);
+  moc::SweepArgs w = pool_sweep_args(p);
+  moc::launch_batch_sources(a, p.stream);
+  if (!moc::launch_sweep(w, p.Ph, p.pairs, p.exp_kind, p.stream))
+    return SV_FAIL(MOC_ERR_UNSUPPORTED, "no sweep kernel for the pool");
+  moc::launch_batch_add_source(a, p.stream);
+  moc::launch_batch_rate_finish(a, p.stream);
+  moc::launch_batch_residual(a, p.stream);
+  moc::launch_batch_residual_finish(a, p.stream);
+  SV_CUDA(cudaGetLastError());
+  return MOC_OK;
+}
+
+// Starts the next block of iterations of a pool and the read-back of its
+// solves' states.
+int launch_block(moc_server* srv, Pool& p) {
+  bool any = false;
+  for (const Slot& sl : p.slots) any = any || sl.live;
+  if (!any) return MOC_OK;
+  if (p.dirty) SV_TRY(rebuild_order(p));
+  for (int i = 0; i < (int) p.slots.size(); i++)
+    if (p.slots[i].live && p.slots[i].needs_init) SV_TRY(init_slot(srv, p, i));
+  if (!p.tuned) {
+    // every solve here is fresh: time the shapes on them, then write their
+    // starting state again
+    SV_TRY(autotune_pool(srv, p));
+    for (int i = 0; i < (int) p.slots.size(); i++)
+      if (p.slots[i].live) SV_TRY(init_slot(srv, p, i));
+  }
+  const int K = std::max(1, srv->cfg.iterations_per_poll);
+  if (srv->cfg.use_graphs) {
+    if (!p.graph || p.graph_iters != K) {
+      if (p.graph) cudaGraphExecDestroy(p.graph);
+      p.graph = nullptr;
+      cudaGraph_t g = nullptr;
+      SV_CUDA(cudaStreamBeginCapture(p.stream, cudaStreamCaptureModeRelaxed));
+      int st = MOC_OK;
+      for (int k = 0; k < K && st == MOC_OK; k++) st = enqueue_iteration(p);
+      cudaError_t e = cudaStreamEndCapture(p.stream, &g);
+      SV_TRY(st);
+      SV_CUDA(e);
+      e = cudaGraphInstantiate(&p.graph, g, 0);
+      cudaGraphDestroy(g);
+      SV_CUDA(e);
+      p.graph_iters = K;
+      std::lock_guard<std::mutex> lk(srv->mu);
+      srv->stats.graph_captures++;
+    }
+    SV_CUDA(cudaGraphLaunch(p.graph, p.stream));
+  } else {
+    for (int k = 0; k < K; k++) SV_TRY(enqueue_iteration(p));
+  }
+  SV_CUDA(cudaMemcpyAsync(p.slots_h, p.slots_d,
+                          sizeof(moc::DevScalars) * p.cfg.max_solves,
+                          cudaMemcpyDeviceToHost, p.stream));
+  SV_CUDA(cudaEventRecord(p.block_done, p.stream));
+  p.in_flight = true;
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    srv->stats.blocks++;
+    srv->stats.kernel_launches += 6 * K;
+  }
+  return MOC_OK;
+}
+
+// Fails every live and queued request of a pool after an error in the loop.
+void fail_pool(moc_server* srv, Pool& p, int status) {
+  std::vector<std::unique_ptr<Staged>> dead;
+  for (Slot& sl : p.slots)
+    if (sl.live) {
+      dead.push_back(std::move(sl.st));
+      sl.live = false;
+    }
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    for (auto& q : p.queue) {
+      dead.push_back(std::move(q));
+      srv->stats.queued--;
+      srv->stats.live++;
+    }
+    p.queue.clear();
+  }
+  for (auto& s : dead) {
+    moc_result r{};
+    r.status = status;
+    r.pool = p.index;
+    r.t_submit = s->t_submit;
+    r.t_admit = s->t_admit;
+    r.t_done = now_s();
+    publish(srv, *s, r);
+  }
+}
+
+// One pass over a pool; with wait, blocks on its running block.  Returns
+// the number of live and queued solves, or a negative status.
+int service(moc_server* srv, Pool& p, bool wait, bool* progressed) {
+  if (p.in_flight) {
+    if (wait) {
+      SV_CUDA(cudaEventSynchronize(p.block_done));
+    } else {
+      cudaError_t e = cudaEventQuery(p.block_done);
+      if (e == cudaErrorNotReady) return MOC_OK;
+      SV_CUDA(e);
+    }
+    p.in_flight = false;
+    SV_TRY(retire(srv, p));
+    *progressed = true;
+  }
+  SV_TRY(admit(srv, p));
+  const bool had = p.in_flight;
+  SV_TRY(launch_block(srv, p));
+  if (p.in_flight && !had) *progressed = true;
+  return MOC_OK;
+}
+
+int step_all(moc_server* srv, bool wait, bool* progressed) {
+  for (auto& pp : srv->pools) {
+    Pool& p = *pp;
+    cudaSetDevice(srv->cfg.device);
+    int st = service(srv, p, wait, progressed);
+    if (st != MOC_OK) {
+      const char* msg = moc_last_error();
+      {
+        std::lock_guard<std::mutex> lk(srv->mu);
+        srv->loop_error = msg ? msg : "";
+      }
+      cudaStreamSynchronize(p.stream);
+      p.in_flight = false;
+      fail_pool(srv, p, st);
+    }
+  }
+  return MOC_OK;
+}
+
+int64_t pending(moc_server* srv) {
+  std::lock_guard<std::mutex> lk(srv->mu);
+  return srv->stats.live + srv->stats.queued;
+}
+
+}  // namespace
+
+extern "C" {
+
+int moc_server_create(const moc_server_config* cfg, moc_server** out) {
+  SV_CHECK(cfg && out, MOC_ERR_ARG, "null argument");
+  *out = nullptr;
+  SV_CHECK(cfg->iterations_per_poll >= 1 && cfg->iterations_per_poll <= 1024,
+           MOC_ERR_ARG, "iterations_per_poll must be in [1, 1024]");
+  int ndev = 0;
+  SV_CUDA(cudaGetDeviceCount(&ndev));
+  SV_CHECK(cfg->device >= 0 && cfg->device < ndev, MOC_ERR_ARG,
+           "no CUDA device " + std::to_string(cfg->device));
+  SV_CUDA(cudaSetDevice(cfg->device));
+  moc_server* srv = new moc_server();
+  srv->cfg = *cfg;
+  // nodes of the attenuation table, as in moc_create
+  const int n = moc::kExpTableSize;
+  srv->exp_table_h.resize(2 * n);
+  for (int i = 0; i < n; i++) {
+    const double x = (double) i * (double) moc::kExpTableH;
+    srv->exp_table_h[i] = (float) (-std::expm1(-x));
+    srv->exp_table_h[n + i] = (float) std::exp(-x);
+  }
+  *out = srv;
+  return MOC_OK;
+}
+
+int moc_server_destroy(moc_server* srv) {
+  if (!srv) return MOC_OK;
+  moc_server_stop(srv);
+  cudaSetDevice(srv->cfg.device);
+  for (auto& p : srv->pools) destroy_pool(*p);
+  delete srv;
+  return MOC_OK;
+}
+
+int moc_server_add_pool(moc_server* srv, const moc_pool_config* cfg,
+                        int* pool) {
+  SV_CHECK(srv && cfg, MOC_ERR_ARG, "null argument");
+  SV_CHECK(!srv->running.load(), MOC_ERR_STATE,
+           "add pools before starting the loop");
+  for (auto& p : srv->pools)
+    SV_CHECK(p->G != cfg->num_groups || p->Ph != cfg->num_polar_half,
+             MOC_ERR_ARG, "a pool for this group and polar count exists");
+  SV_CUDA(cudaSetDevice(srv->cfg.device));
+  std::unique_ptr<Pool> p(new Pool());
+  p->index = (int) srv->pools.size();
+  int st = create_pool(srv, *cfg, *p);
+  if (st != MOC_OK) {
+    std::string msg = moc_last_error();
+    destroy_pool(*p);
+    return SV_FAIL(st, msg);
+  }
+  if (pool) *pool = p->index;
+  srv->pools.push_back(std::move(p));
+  return MOC_OK;
+}
+
+int moc_server_submit(moc_server* srv, const moc_request* req,
+                      int64_t* ticket) {
+  SV_CHECK(srv && req, MOC_ERR_ARG, "null argument");
+  Pool* target = nullptr;
+  for (auto& p : srv->pools)
+    if (p->G == req->num_groups && p->Ph == req->num_polar_half)
+      target = p.get();
+  SV_CHECK(target, MOC_ERR_UNSUPPORTED,
+           "no pool for " + std::to_string(req->num_groups) + " groups and " +
+               std::to_string(req->num_polar_half) + " polar angles");
+  std::unique_ptr<Staged> s(new Staged());
+  SV_TRY(stage_request(*req, *s));
+  const moc_pool_config& c = target->cfg;
+  SV_CHECK(s->R <= c.max_fsrs && s->T + 1 <= c.max_tracks &&
+               s->S <= c.max_segments && s->M <= c.max_materials &&
+               s->A <= c.max_angles,
+           MOC_ERR_MEMORY, "request exceeds its pool's capacity");
+  s->pool = target->index;
+  s->t_submit = now_s();
+  std::lock_guard<std::mutex> lk(srv->mu);
+  s->ticket = srv->next_ticket++;
+  if (ticket) *ticket = s->ticket;
+  srv->stats.submitted++;
+  srv->stats.queued++;
+  target->queue.push_back(std::move(s));
+  srv->cv.notify_all();
+  return MOC_OK;
+}
+
+int moc_server_step(moc_server* srv, int64_t* pend) {
+  SV_CHECK(srv, MOC_ERR_ARG, "null server");
+  SV_CHECK(!srv->running.load(), MOC_ERR_STATE,
+           "the loop thread is running");
+  bool progressed = false;
+  SV_TRY(step_all(srv, true, &progressed));
+  if (pend) *pend = pending(srv);
+  return MOC_OK;
+}
+
+int moc_server_start(moc_server* srv) {
+  SV_CHECK(srv, MOC_ERR_ARG, "null server");
+  SV_CHECK(!srv->running.load(), MOC_ERR_STATE, "already running");
+  srv->running.store(true);
+  srv->loop = std::thread([srv]() {
+    cudaSetDevice(srv->cfg.device);
+    while (srv->running.load()) {
+      bool progressed = false;
+      step_all(srv, false, &progressed);
+      if (!progressed) {
+        // nothing finished and nothing new: wait briefly for a submission
+        // or for the device
+        std::unique_lock<std::mutex> lk(srv->mu);
+        if (srv->stats.live == 0 && srv->running.load())
+          srv->cv.wait_for(lk, std::chrono::milliseconds(2));
+        else
+          std::this_thread::yield();
+      }
+    }
+  });
+  return MOC_OK;
+}
+
+int moc_server_stop(moc_server* srv) {
+  SV_CHECK(srv, MOC_ERR_ARG, "null server");
+  if (!srv->running.load()) return MOC_OK;
+  srv->running.store(false);
+  srv->cv.notify_all();
+  if (srv->loop.joinable()) srv->loop.join();
+  // finish the blocks in flight so that the server can be stepped or
+  // destroyed
+  for (auto& p : srv->pools)
+    if (p->stream) cudaStreamSynchronize(p->stream);
+  return MOC_OK;
+}
+
+int moc_server_wait(moc_server* srv, int64_t ticket, double timeout_s,
+                    moc_result* out) {
+  SV_CHECK(srv && out, MOC_ERR_ARG, "null argument");
+  std::unique_lock<std::mutex> lk(srv->mu);
+  SV_CHECK(ticket >= 1 && ticket < srv->next_ticket, MOC_ERR_ARG,
+           "unknown ticket");
+  auto ready = [&] { return srv->results.count(ticket) > 0; };
+  if (timeout_s < 0) {
+    srv->cv.wait(lk, ready);
+  } else if (!srv->cv.wait_for(lk, std::chrono::duration<double>(timeout_s),
+                               ready)) {
+    lk.unlock();
+    return SV_FAIL(MOC_ERR_TIMEOUT, "request not completed");
+  }
+  *out = srv->results[ticket];
+  return MOC_OK;
+}
+
+int moc_server_poll(moc_server* srv, int64_t* tickets, int capacity,
+                    int* count) {
+  SV_CHECK(srv && count && (capacity == 0 || tickets), MOC_ERR_ARG,
+           "null argument");
+  std::lock_guard<std::mutex> lk(srv->mu);
+  const int n = std::min<int>(capacity, (int) srv->completed.size());
+  for (int i = 0; i < n; i++) tickets[i] = srv->completed[i];
+  srv->completed.erase(srv->completed.begin(), srv->completed.begin() + n);
+  *count = n;
+  return MOC_OK;
+}
+
+int moc_server_stats_get(moc_server* srv, moc_server_stats* out) {
+  SV_CHECK(srv && out, MOC_ERR_ARG, "null argument");
+  std::lock_guard<std::mutex> lk(srv->mu);
+  *out = srv->stats;
+  return MOC_OK;
+}
+
+}  // extern "C"

@@ -14,6 +14,8 @@
 // warp shuffles, one shared-memory pass per block, one double atomic per
 // block; the last block (ticket counter) finishes the scalar update on the
 // device, so the host never reads intermediate sums.
+#include <algorithm>
+
 #include "moc_internal.cuh"
 
 namespace moc {
@@ -81,11 +83,14 @@ __device__ __forceinline__ int64_t row_step() {
 // destinations.  The fission term is rank one: chi[dest] * (nu_sigma_f .
 // phi) / k.  S = ceil(G / 32) destination groups per lane.
 // Two FSR rows per warp pass give two independent accumulation chains.
+// Row r0 + i is computed when bit i of `on` is set, with its own
+// 1 / keff and iteration count (those of its solve in a pool).
 template <int S>
 __device__ __forceinline__ void source_rows(const SolverArgs& a,
                                             const float* ssT, int64_t r0,
-                                            int nrows, int zero_phi,
-                                            int iteration, float inv_k,
+                                            int on_mask, int zero_phi,
+                                            int it0, int it1, float ik0,
+                                            float ik1,
                                             unsigned long long& negatives) {
   const int G = a.num_groups;
   const int GG = G * G;
@@ -96,7 +101,7 @@ __device__ __forceinline__ void source_rows(const SolverArgs& a,
 #pragma unroll
   for (int i = 0; i < 2; i++) {
     const int64_t r = r0 + i;
-    const bool on = i < nrows;
+    const bool on = (on_mask >> i) & 1;
     mat[i] = on ? a.fsr_mat[r] : 0;
     float* phi = a.phi + r * a.ld;
 #pragma unroll
@@ -141,11 +146,11 @@ __device__ __forceinline__ void source_rows(const SolverArgs& a,
   }
 #pragma unroll
   for (int i = 0; i < 2; i++) {
-    if (i >= nrows) break;
+    if (!((on_mask >> i) & 1)) continue;
     const int64_t r = r0 + i;
     const float* chi = a.chi + (int64_t) mat[i] * G;
     const float* st = a.sigma_t + (int64_t) mat[i] * G;
-    const float fk = fr[i] * inv_k;
+    const float fk = fr[i] * (i == 0 ? ik0 : ik1);
 #pragma unroll
     for (int j = 0; j < S; j++) {
       const int gd = lane + 32 * j;
@@ -156,7 +161,7 @@ __device__ __forceinline__ void source_rows(const SolverArgs& a,
       q *= (float) kOneOverFourPi;
       if (q < 0.0f) {
         negatives++;
-        if (iteration < 30) q = kFluxEpsilon;
+        if ((i == 0 ? it0 : it1) < 30) q = kFluxEpsilon;
       }
       a.qt[r * a.ld + gd] = q / st[gd];
     }
@@ -180,14 +185,35 @@ compute_sources_kernel(const SolverArgs a, int iteration, int zero_phi,
   }
   const float* ssT =
       staged ? reinterpret_cast<const float*>(s_ss4) : a.sigma_s_T;
-  const float inv_k = (float) (1.0 / a.sc->keff);
+  const float inv_k1 = a.row_slot ? 0.0f : (float) (1.0 / a.sc->keff);
   // iteration < 0: the device iteration counter of the running solve
-  if (iteration < 0) iteration = a.sc->iteration;
+  if (iteration < 0 && !a.row_slot) iteration = a.sc->iteration;
   unsigned long long negatives = 0;
   const int64_t warp = first_row(), warps = row_step();
   for (int64_t r = 2 * warp; r < a.num_fsrs; r += 2 * warps) {
-    const int nrows = (r + 1 < a.num_fsrs) ? 2 : 1;
-    source_rows<S>(a, ssT, r, nrows, zero_phi, iteration, inv_k, negatives);
+    int on = (r + 1 < a.num_fsrs) ? 3 : 1;
+    int it0 = iteration, it1 = iteration;
+    float ik0 = inv_k1, ik1 = inv_k1;
+    if (a.row_slot) {
+      // pool rows: each row's own solve; unused rows and finished solves
+      // are left untouched
+      const int s0 = a.row_slot[r];
+      const int s1 = (on & 2) ? a.row_slot[r + 1] : -1;
+      const DevScalars* p0 = (s0 >= 0) ? a.slots + s0 : nullptr;
+      const DevScalars* p1 = (s1 >= 0) ? a.slots + s1 : nullptr;
+      if (!p0 || p0->done) on &= ~1;
+      if (!p1 || p1->done) on &= ~2;
+      if (!on) continue;
+      if (on & 1) {
+        it0 = p0->iteration;
+        ik0 = (float) (1.0 / p0->keff);
+      }
+      if (on & 2) {
+        it1 = p1->iteration;
+        ik1 = (float) (1.0 / p1->keff);
+      }
+    }
+    source_rows<S>(a, ssT, r, on, zero_phi, it0, it1, ik0, ik1, negatives);
   }
   if (negatives) atomicAdd(&a.sc->neg_sources, negatives);
 }
@@ -445,6 +471,237 @@ __global__ void fsr_rates_kernel(const SolverArgs a, double* out, int nu) {
   }
 }
 
+// ------------------------------------------------------- batched pools
+// A pool holds many independent solves of one group count in shared
+// arrays: each solve owns a contiguous range of FSR rows, tracks, segments,
+// materials and angle rows.  The row kernels below are the add-source and
+// residual kernels above with every scalar taken from the row's solve, and
+// the grid-wide reductions split in two: each row leaves its FP64 term in
+// row_val, and one block per solve sums its rows in a fixed order and
+// updates the solve's state.
+
+// State of the solve owning row r; null for unused rows and finished solves.
+__device__ __forceinline__ DevScalars* live_slot(const SolverArgs& a,
+                                                 int64_t r) {
+  const int sl = a.row_slot[r];
+  if (sl < 0) return nullptr;
+  DevScalars* ss = a.slots + sl;
+  return ss->done ? nullptr : ss;
+}
+
+template <int S>
+__global__ void __launch_bounds__(kRowThreads)
+batch_add_source_kernel(const SolverArgs a) {
+  const int G = a.num_groups;
+  const int lane = threadIdx.x & 31;
+  for (int64_t r = first_row(); r < a.num_fsrs; r += row_step()) {
+    DevScalars* ss = live_slot(a, r);
+    if (!ss) continue;
+    const int m = a.fsr_mat[r];
+    const float vol0 = a.fsr_vol[r];
+    const float vol = (vol0 < 1.0e-12f) ? 1.0e30f : vol0;
+    const float* __restrict__ st = a.sigma_t + (int64_t) m * G;
+    const float* __restrict__ nf = a.nu_sigma_f + (int64_t) m * G;
+    float* __restrict__ phi = a.phi + r * a.ld;
+    const float* __restrict__ qt = a.qt + r * a.ld;
+    float v[S], q[S];
+#pragma unroll
+    for (int j = 0; j < S; j++) {
+      const int g = lane + 32 * j;
+      v[j] = (g < G) ? phi[g] : 0.0f;
+      q[j] = (g < G) ? qt[g] : 0.0f;
+    }
+    float rr = 0.0f;
+    int negatives = 0;
+#pragma unroll
+    for (int j = 0; j < S; j++) {
+      const int g = lane + 32 * j;
+      if (g >= G) continue;
+      float x = v[j] / (st[g] * vol);
+      x += (float) kFourPi * q[j];
+      if (x < 0.0f) {
+        x = kFluxEpsilon;
+        negatives++;
+      }
+      phi[g] = x;
+      rr = fmaf(nf[g], x, rr);
+    }
+    const double rate = warp_sum_all_d((double) rr * (double) vol0);
+    negatives = __reduce_add_sync(0xffffffffu, negatives);
+    if (lane == 0) {
+      a.row_val[r] = rate;
+      if (negatives) atomicAdd(&ss->neg_fluxes, (unsigned long long) negatives);
+    }
+  }
+}
+
+// Sum of row_val over the rows of solve blockIdx.x, in a fixed order;
+// valid in thread 0.
+__device__ double slot_row_sum(const SolverArgs& a, const DevScalars* ss) {
+  __shared__ double part[32];
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < ss->nrows; i += blockDim.x)
+    s += a.row_val[ss->row0 + i];
+  s = warp_sum_all_d(s);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) part[warp] = s;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int) (blockDim.x >> 5); i++) t += part[i];
+  return t;
+}
+
+// keff *= total / R, factor = R / total and the next sweep's angular-flux
+// scale, per eigenvalue solve (CPUSolver::computeKeff then normalizeFluxes,
+// src/CPUSolver.cpp:2327, 1910).
+__global__ void batch_rate_finish_kernel(const SolverArgs a) {
+  DevScalars* ss = a.slots + blockIdx.x;
+  if (ss->done || ss->mode != kModeEigen) return;
+  const double total = slot_row_sum(a, ss);
+  if (threadIdx.x == 0) {
+    const double R = (double) ss->nrows;
+    ss->keff = ss->keff * (total / R);
+    ss->factor = R / total;
+    ss->scale[a.sc->cur] *= (float) ss->factor;
+  }
+}
+
+// Residual terms per row: eigenvalue solves are normalised first; phi is
+// stored into phi_old.  The residual type is the solve's own.
+template <int S>
+__global__ void __launch_bounds__(kRowThreads)
+batch_residual_kernel(const SolverArgs a) {
+  const int G = a.num_groups;
+  const int lane = threadIdx.x & 31;
+  for (int64_t r = first_row(); r < a.num_fsrs; r += row_step()) {
+    const DevScalars* ss = live_slot(a, r);
+    if (!ss) continue;
+    const int RT = ss->res_type;
+    const bool normalise = ss->mode == kModeEigen;
+    const float factor = normalise ? (float) ss->factor : 1.0f;
+    const float inv_k = (float) (1.0 / ss->keff);
+    const int m = a.fsr_mat[r];
+    const bool fis = a.fissile[m] != 0;
+    const float* __restrict__ nf = a.nu_sigma_f + (int64_t) m * G;
+    float* __restrict__ phi = a.phi + r * a.ld;
+    float* __restrict__ old = a.phi_old + r * a.ld;
+    float vv[S], oo[S];
+#pragma unroll
+    for (int j = 0; j < S; j++) {
+      const int g = lane + 32 * j;
+      vv[j] = (g < G) ? phi[g] : 0.0f;
+      oo[j] = (g < G) ? old[g] : 0.0f;
+    }
+    float x = 0.0f, y = 0.0f;
+#pragma unroll
+    for (int j = 0; j < S; j++) {
+      const int g = lane + 32 * j;
+      if (g >= G) continue;
+      float v = vv[j];
+      if (normalise) {
+        v *= factor;
+        phi[g] = v;
+      }
+      const float o = oo[j];
+      if (RT == 0) {
+        if (o > 0.0f) {
+          const float d = (v - o) / o;
+          x = fmaf(d, d, x);
+        }
+      } else if (RT == 1) {
+        if (fis) {
+          x = fmaf(v - o, nf[g], x);
+          y = fmaf(o, nf[g], y);
+        }
+      } else {
+        const float w = (fis ? nf[g] * inv_k : 0.0f) +
+                        a.scat_out[(int64_t) m * G + g];
+        x = fmaf(v - o, w, x);
+        y = fmaf(o, w, y);
+      }
+      old[g] = v;
+    }
+    x = warp_sum_all(x);
+    y = warp_sum_all(y);
+    double part = 0.0;
+    if (RT == 0) {
+      part = (double) x;
+    } else if ((RT == 2 || fis) && y > 0.0f) {
+      const double t = (double) x / (double) y;
+      part = t * t;
+    }
+    if (lane == 0) a.row_val[r] = part;
+  }
+}
+
+// Residual, convergence test and counters per solve (the ends of
+// Solver::computeEigenvalue / computeSource loop bodies,
+// src/Solver.cpp:1500-1530, 1614-1685).
+__global__ void batch_residual_finish_kernel(const SolverArgs a) {
+  DevScalars* ss = a.slots + blockIdx.x;
+  if (ss->done) return;
+  double total = slot_row_sum(a, ss);
+  if (threadIdx.x != 0) return;
+  if (total < 0.0) total = 0.0;
+  double norm = (ss->res_type == 1) ? (double) ss->num_fissionable
+                                    : (double) ss->nrows;
+  if (norm <= 0.0) norm = 1.0;
+  const double residual = sqrt(total / norm);
+  ss->residual = residual;
+  const int i = ss->iteration;
+  if (ss->mode == kModeEigen) {
+    const int dk = (int) (1e5 * (ss->keff - ss->k_prev));
+    ss->dk = dk;
+    ss->k_prev = ss->keff;
+    ss->iteration = i + 1;
+    if (residual < ss->threshold && abs(dk) < 1) {
+      ss->converged = 1;
+      ss->done = 1;
+    }
+  } else {
+    ss->iteration = i + 1;
+    if (i > 1 && residual < ss->threshold) {
+      ss->converged = 1;
+      ss->done = 1;
+    }
+  }
+  if (ss->iteration >= ss->max_iters) ss->done = 1;
+}
+
+__global__ void batch_init_rows_kernel(const SolverArgs a, int64_t r0,
+                                       int64_t n, float value) {
+  const int64_t base = r0 * a.ld, count = n * a.ld;
+  for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+       i < count; i += (int64_t) gridDim.x * blockDim.x) {
+    a.phi[base + i] = value;
+    a.phi_old[base + i] = value;
+    a.qt[base + i] = 0.0f;
+  }
+}
+
+__global__ void batch_rebase_kernel(int2* segs, int64_t S,
+                                    const int32_t* fsr_mat, int32_t r0,
+                                    int64_t* seg_off, int32_t* next,
+                                    int32_t* track_ang, int32_t* track_slot,
+                                    int64_t T, int64_t s0, int32_t t0,
+                                    int32_t a0, int32_t slot) {
+  const int64_t n = (S > 2 * T + 2) ? S : 2 * T + 2;
+  for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t) gridDim.x * blockDim.x) {
+    if (i < S) {
+      const int f = segs[i].y + r0;
+      segs[i].y = f | (fsr_mat[f] << 24);
+    }
+    if (i <= T) {
+      seg_off[i] += s0;
+      track_slot[i] = slot;
+    }
+    if (i < T) track_ang[i] += a0;
+    if (i < 2 * T) next[i] += t0;
+  }
+}
+
 int grid_for(int64_t n, int threads) {
   int64_t b = (n + threads - 1) / threads;
   if (b > 152 * 16) b = 152 * 16;
@@ -465,8 +722,10 @@ int row_grid(int64_t rows) {
 template <int S>
 void launch_sources_s(const SolverArgs& a, int iteration, int fused,
                       cudaStream_t s) {
+  // staged as whole float4 words: round up to 16 bytes
   const size_t need =
-      sizeof(float) * (size_t) a.num_materials * a.num_groups * a.num_groups;
+      (sizeof(float) * (size_t) a.num_materials * a.num_groups * a.num_groups +
+       15) & ~(size_t) 15;
   const int staged = need <= 160 * 1024;
   const size_t smem = staged ? need : 0;
   auto kern = compute_sources_kernel<S>;
@@ -573,6 +832,64 @@ void launch_fill_chi(float* phi, const float* chi, int64_t R, int G, int ld,
 void launch_fsr_rates(const SolverArgs& a, double* out, int nu,
                       cudaStream_t s) {
   fsr_rates_kernel<<<row_grid(a.num_fsrs), kRowThreads, 0, s>>>(a, out, nu);
+}
+
+// ---- batched pools -------------------------------------------------------
+void launch_batch_sources(const SolverArgs& a, cudaStream_t s) {
+  launch_compute_sources(a, 0, 1, s);
+}
+
+void launch_batch_add_source(const SolverArgs& a, cudaStream_t s) {
+  const int b = row_grid(a.num_fsrs);
+  switch ((a.num_groups + 31) / 32) {
+    case 1: batch_add_source_kernel<1><<<b, kRowThreads, 0, s>>>(a); break;
+    case 2: batch_add_source_kernel<2><<<b, kRowThreads, 0, s>>>(a); break;
+    case 3: batch_add_source_kernel<3><<<b, kRowThreads, 0, s>>>(a); break;
+    case 4: batch_add_source_kernel<4><<<b, kRowThreads, 0, s>>>(a); break;
+    case 5: batch_add_source_kernel<5><<<b, kRowThreads, 0, s>>>(a); break;
+    case 6: batch_add_source_kernel<6><<<b, kRowThreads, 0, s>>>(a); break;
+    case 7: batch_add_source_kernel<7><<<b, kRowThreads, 0, s>>>(a); break;
+    default: batch_add_source_kernel<12><<<b, kRowThreads, 0, s>>>(a); break;
+  }
+}
+
+void launch_batch_rate_finish(const SolverArgs& a, cudaStream_t s) {
+  batch_rate_finish_kernel<<<a.num_slots, kThreads, 0, s>>>(a);
+}
+
+void launch_batch_residual(const SolverArgs& a, cudaStream_t s) {
+  const int b = row_grid(a.num_fsrs);
+  switch ((a.num_groups + 31) / 32) {
+    case 1: batch_residual_kernel<1><<<b, kRowThreads, 0, s>>>(a); break;
+    case 2: batch_residual_kernel<2><<<b, kRowThreads, 0, s>>>(a); break;
+    case 3: batch_residual_kernel<3><<<b, kRowThreads, 0, s>>>(a); break;
+    case 4: batch_residual_kernel<4><<<b, kRowThreads, 0, s>>>(a); break;
+    case 5: batch_residual_kernel<5><<<b, kRowThreads, 0, s>>>(a); break;
+    case 6: batch_residual_kernel<6><<<b, kRowThreads, 0, s>>>(a); break;
+    case 7: batch_residual_kernel<7><<<b, kRowThreads, 0, s>>>(a); break;
+    default: batch_residual_kernel<12><<<b, kRowThreads, 0, s>>>(a); break;
+  }
+}
+
+void launch_batch_residual_finish(const SolverArgs& a, cudaStream_t s) {
+  batch_residual_finish_kernel<<<a.num_slots, kThreads, 0, s>>>(a);
+}
+
+void launch_batch_init_rows(const SolverArgs& a, int64_t r0, int64_t n,
+                            float value, cudaStream_t s) {
+  batch_init_rows_kernel<<<grid_for(n * a.ld, kThreads), kThreads, 0, s>>>(
+      a, r0, n, value);
+}
+
+void launch_batch_rebase(int2* segs, int64_t S, const int32_t* fsr_mat,
+                         int32_t r0, int64_t* seg_off, int32_t* next,
+                         int32_t* track_ang, int32_t* track_slot, int64_t T,
+                         int64_t s0, int32_t t0, int32_t a0, int32_t slot,
+                         cudaStream_t s) {
+  const int64_t n = std::max<int64_t>(S, 2 * T + 2);
+  batch_rebase_kernel<<<grid_for(n, kThreads), kThreads, 0, s>>>(
+      segs, S, fsr_mat, r0, seg_off, next, track_ang, track_slot, T, s0, t0,
+      a0, slot);
 }
 
 }  // namespace moc

@@ -131,7 +131,6 @@ sweep_kernel(const SweepArgs a) {
   const int cur = sc->cur;
   const float* psi_in = a.psi[cur];
   float* psi_out = a.psi[cur ^ 1];
-  const float scale = sc->scale[cur];
 
   const int lane = threadIdx.x & 31;
   const int sub = lane & (LPS - 1);
@@ -140,8 +139,20 @@ sweep_kernel(const SweepArgs a) {
   const int64_t stream = gwarp * (32 / LPS) + lane / LPS;
   const int npairs = ld >> 1;
 
-  if (stream < 2 * a.num_tracks) {
-    const int t = a.order[stream >> 1];
+  // the solve of this track (a pool) or the context's own state; the LPS
+  // lanes of a stream share the track, so they agree on skipping it
+  int t = 0;
+  const DevScalars* ts = sc;
+  bool live = stream < 2 * a.num_tracks;
+  if (live) {
+    t = a.order[stream >> 1];
+    if (a.track_slot) {
+      ts = a.slots + a.track_slot[t];
+      live = ts->done == 0;
+    }
+  }
+  if (live) {
+    const float scale = ts->scale[cur];
     const int dir = (int) (stream & 1);
     const int64_t b = a.seg_off[t];
     const int n = (int) (a.seg_off[t + 1] - b);
@@ -297,11 +308,15 @@ sweep_kernel(const SweepArgs a) {
     last = (ticket == gridDim.x - 1);
   }
   __syncthreads();
-  if (last && threadIdx.x == 0) {
-    sc->ticket_sweep = 0;
-    sc->scale[cur ^ 1] = 1.0f;
-    sc->cur = cur ^ 1;
-    __threadfence();
+  if (last) {
+    for (int i = threadIdx.x; i < a.num_slots; i += blockDim.x)
+      a.slots[i].scale[cur ^ 1] = 1.0f;
+    if (threadIdx.x == 0) {
+      sc->ticket_sweep = 0;
+      sc->scale[cur ^ 1] = 1.0f;
+      sc->cur = cur ^ 1;
+      __threadfence();
+    }
   }
 }
 

@@ -1,5 +1,5 @@
 """The C ABI library builds for sm_103a, loads, and exports every entry
-point that include/openmoc_gb300.h declares (no GPU needed: nothing here
+point that the headers under include/ declare (no GPU needed: nothing here
 calls into the device)."""
 import ctypes
 import os
@@ -11,17 +11,24 @@ import pytest
 
 from conftest import ROOT
 
-HEADER = os.path.join(ROOT, "include", "openmoc_gb300.h")
+INCLUDE = os.path.join(ROOT, "include")
+HEADER = os.path.join(INCLUDE, "openmoc_gb300.h")
 
 
-def declared_functions():
-    text = open(HEADER).read()
-    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(moc_[a-z0-9_]+)\s*\(", text)))
+def declared_functions(header=None):
+    """Entry points declared by one header, or by every header."""
+    paths = [header] if header else [os.path.join(INCLUDE, f)
+                                     for f in sorted(os.listdir(INCLUDE))
+                                     if f.endswith(".h")]
+    names = set()
+    for path in paths:
+        text = re.sub(r"/\*.*?\*/", "", open(path).read(), flags=re.S)
+        names.update(re.findall(r"\b(moc_[a-z0-9_]+)\s*\(", text))
+    return sorted(names)
 
 
 def test_header_declares_entry_points():
-    names = declared_functions()
+    names = declared_functions(HEADER)
     assert "moc_create" in names and "moc_transport_sweep" in names
     assert len(names) >= 40
 
@@ -42,7 +49,13 @@ def test_library_builds_and_exports_every_declared_symbol():
 
 def test_python_binding_covers_the_header():
     from openmoc_gb300 import _native
-    assert set(_native.exported_symbols()) == set(declared_functions())
+    assert set(_native.exported_symbols()) == set(declared_functions(HEADER))
+
+
+def test_python_binding_covers_the_server_header():
+    from openmoc_gb300 import serving
+    header = os.path.join(INCLUDE, "openmoc_gb300_serve.h")
+    assert set(serving.exported_symbols()) == set(declared_functions(header))
 
 
 def test_library_is_sm_103a_only():

@@ -1,0 +1,199 @@
+"""The batched solve server (include/openmoc_gb300_serve.h) on the GPU.
+
+Each batched result must match OpenMOC's own on the fixtures (keff within
+1e-5, fluxes within 1e-4 relative, the parity bar) and the plain one-solve
+GB300Solver on generated problems, and a request must give the same result
+alone and in a mix of other requests (within the same tolerances; tally
+atomics make the last bits order-dependent).
+"""
+import time
+
+import numpy as np
+import pytest
+
+from conftest import CASES, load_case
+from openmoc_gb300 import GB300Solver, lattice
+from openmoc_gb300._native import MOCError
+from openmoc_gb300.serving import Server, pool_capacity
+
+pytestmark = pytest.mark.gpu
+
+KEFF_TOL = 1e-5
+FLUX_TOL = 1e-4
+
+
+def max_rel(a, b):
+    a = np.asarray(a, np.float64).ravel()
+    b = np.asarray(b, np.float64).ravel()
+    return float(np.max(np.abs(a - b) / np.abs(b)))
+
+
+def make_server(problems, max_solves, k=8, graphs=True, shape=None):
+    srv = Server(iterations_per_poll=k, use_graphs=graphs)
+    by_key = {}
+    for p in problems:
+        by_key.setdefault((p.num_groups, p.num_polar_half), []).append(p)
+    for (G, ph), ps in sorted(by_key.items()):
+        srv.add_pool(G, ph, shape=shape, **pool_capacity(ps, max_solves))
+    return srv
+
+
+def single(p, kind="eigenvalue", max_iters=1000, res_type=1, k_eff=1.0,
+           threshold=1e-5):
+    s = GB300Solver(p)
+    s.setConvergenceThreshold(threshold)
+    if kind == "eigenvalue":
+        s.computeEigenvalue(max_iters, res_type)
+    else:
+        s.computeSource(max_iters, k_eff, res_type)
+    out = dict(keff=s.getKeff(), flux=s.getFluxes(), iterations=s.getNumIterations())
+    s.close()
+    return out
+
+
+def test_fixtures_batched_match_openmoc():
+    cases = {c: load_case(c) for c in CASES}
+    srv = make_server([v[0] for v in cases.values()], 2)
+    tickets = {}
+    for c, (p, sc, _) in cases.items():
+        tickets[c] = srv.submit(p, "eigenvalue", int(sc["max_iters"]),
+                                int(sc["res_type"]), threshold=sc["tolerance"])
+    srv.run_until_idle()
+    for c, (p, sc, arr) in cases.items():
+        r = srv.wait(tickets[c], timeout=0)
+        _, sc64, arr64 = load_case(c, "f64")
+        assert r["converged"]
+        assert abs(r["iterations"] - int(sc["iterations"])) <= 2, c
+        assert abs(r["keff"] - sc["keff"]) <= KEFF_TOL, (c, r["keff"], sc["keff"])
+        assert max_rel(r["flux"], arr["flux"]) <= FLUX_TOL, c
+        assert abs(r["keff"] - sc64["keff"]) <= 1.5 * KEFF_TOL, c
+        assert max_rel(r["flux"], arr64["flux"]) <= FLUX_TOL, c
+    st = srv.stats()
+    assert st["completed"] == len(CASES) and st["failed"] == 0
+    assert st["graph_captures"] >= 1
+    srv.close()
+
+
+def mix(n_extra=6):
+    """A mix of uneven generated problems (pin cells and small lattices,
+    7 groups, perturbed cross sections)."""
+    ps = [lattice.pin_cell(7, 16 + 4 * (i % 3), 0.08, config=0, perturb=(100 + i, 0.05))
+          for i in range(n_extra // 2)]
+    ps += [lattice.square_lattice(3, 7, 16, 0.1, config=2, perturb=(200 + i, 0.05))
+           for i in range(n_extra - n_extra // 2)]
+    return ps
+
+
+def test_same_result_alone_and_in_the_mix():
+    target = lattice.square_lattice(3, 7, 24, 0.08, config=3, perturb=(7, 0.05))
+    others = mix(6)
+    alone = make_server([target] + others, 8)
+    ta = alone.submit(target)
+    alone.run_until_idle()
+    ra = alone.wait(ta, timeout=0)
+    alone.close()
+
+    crowd = make_server([target] + others, 8)
+    first = [crowd.submit(p) for p in others[:3]]
+    crowd.step()                       # others already running ...
+    tb = crowd.submit(target)          # ... when the target arrives
+    rest = [crowd.submit(p) for p in others[3:]]
+    crowd.run_until_idle()
+    rb = crowd.wait(tb, timeout=0)
+    for t in first + rest:
+        assert crowd.wait(t, timeout=0)["converged"]
+    crowd.close()
+
+    ref = single(target)
+    for r in (ra, rb):
+        assert abs(r["keff"] - ref["keff"]) <= KEFF_TOL
+        assert max_rel(r["flux"], ref["flux"]) <= FLUX_TOL
+        assert abs(r["iterations"] - ref["iterations"]) <= 2
+    assert abs(ra["keff"] - rb["keff"]) <= KEFF_TOL
+    assert max_rel(ra["flux"], rb["flux"]) <= FLUX_TOL
+
+
+def test_continuous_admission_with_two_slots():
+    ps = mix(6)
+    srv = make_server(ps, 2, k=4)
+    tickets = [srv.submit(p) for p in ps]
+    n_pending = srv.step()
+    assert n_pending == len(ps)         # two admitted, four queued
+    srv.run_until_idle()
+    for p, t in zip(ps, tickets):
+        r = srv.wait(t, timeout=0)
+        ref = single(p)
+        assert abs(r["keff"] - ref["keff"]) <= KEFF_TOL
+        assert max_rel(r["flux"], ref["flux"]) <= FLUX_TOL
+    st = srv.stats()
+    assert st["admitted"] == len(ps) and st["completed"] == len(ps)
+    assert st["graph_captures"] >= 3    # the set of live solves changed
+    srv.close()
+
+
+def test_fixed_source_requests():
+    p = lattice.square_lattice(3, 7, 16, 0.1, config=4)
+    q = np.zeros((p.num_fsrs, p.num_groups), np.float32)
+    fuel = np.nonzero(p.fsr_mat == 0)[0]
+    q[fuel, :] = 1.0
+    k_sub = 1.5   # above the lattice's own keff: a convergent source problem
+    srv = make_server([p], 4)
+    t1 = srv.submit(p, "source", 1000, 2, k_eff=k_sub, fixed_source=q)
+    t2 = srv.submit(p, "eigenvalue")
+    srv.run_until_idle()
+    r1 = srv.wait(t1, timeout=0)
+    r2 = srv.wait(t2, timeout=0)
+    srv.close()
+
+    s = GB300Solver(p)
+    s.setConvergenceThreshold(1e-5)
+    for f in fuel:
+        for g in range(p.num_groups):
+            s.setFixedSourceByFSR(int(f), g + 1, 1.0)
+    s.computeSource(1000, k_sub, 2)
+    ref_flux = s.getFluxes()
+    ref_iters = s.getNumIterations()
+    s.close()
+    assert r1["keff"] == pytest.approx(k_sub)
+    assert max_rel(r1["flux"], ref_flux) <= FLUX_TOL
+    assert abs(r1["iterations"] - ref_iters) <= 2
+    ref2 = single(p)
+    assert abs(r2["keff"] - ref2["keff"]) <= KEFF_TOL
+
+
+def test_loop_thread_and_graph_free_mode_agree():
+    ps = mix(4)
+    srv = make_server(ps, 4, k=8, graphs=True)
+    srv.start()
+    tickets = []
+    for p in ps:
+        tickets.append(srv.submit(p))
+        time.sleep(0.002)
+    res = [srv.wait(t, timeout=120) for t in tickets]
+    srv.stop()
+    assert sorted(srv.poll()) == sorted(tickets)
+    srv.close()
+
+    plain = make_server(ps, 4, k=8, graphs=False)
+    t2 = [plain.submit(p) for p in ps]
+    plain.run_until_idle()
+    for r, t in zip(res, t2):
+        r2 = plain.wait(t, timeout=0)
+        assert abs(r["keff"] - r2["keff"]) <= KEFF_TOL
+        assert max_rel(r["flux"], r2["flux"]) <= FLUX_TOL
+        assert r["t_submit"] <= r["t_admit"] <= r["t_done"]
+    plain.close()
+
+
+def test_bad_request_is_refused_on_submit():
+    p = lattice.pin_cell(7, 16, 0.1)
+    srv = make_server([p], 1)
+    with pytest.raises(MOCError, match="threshold"):
+        srv.submit(p, "eigenvalue", threshold=-1.0)
+    with pytest.raises(MOCError, match="no pool"):
+        srv.submit(lattice.pin_cell(2, 16, 0.1))     # no pool for 2 groups
+    big = lattice.square_lattice(3, 7, 16, 0.1, config=0)
+    with pytest.raises(MOCError, match="capacity"):
+        srv.submit(big)
+    assert srv.stats()["submitted"] == 0
+    srv.close()
