@@ -260,7 +260,7 @@ def run_gpu(args):
                        "segments": p.num_segments, "groups": p.num_groups,
                        "integrations_per_step": ints, "l2": "flushed before every step",
                        "sweep_shape": {"lanes_per_track_direction": lps,
-                                       "groups_per_lane": slots,
+                                       "group_pairs_per_lane": slots,
                                        "exponential": ["shared-memory table",
                                                        "hardware ex2"][exp_kind]},
                        "autotune_ms": {f"{a}x{b}/{'table' if e == 0 else 'ex2'}": round(t, 4)
@@ -327,6 +327,162 @@ def end_to_end(p, args, device, torch):
             "iterations_per_step": args.e2e_iters, "seconds_per_step": t}
 
 
+# ---------------------------------------------------------------- serving
+SERVING_WORKLOAD = ("request stream: Poisson arrivals, 70% eigenvalue / 30% fixed-source; "
+                    "pin cell, 3x3, 7x7 or 17x17 (guide tubes) lattice; 2, 7, 16 or 70 groups; "
+                    "lognormal(0, 0.05) cross-section factors; 16-64 azimuthal; 0.05-0.1 cm")
+SERVING_GEOMS = ("pin", "3x3", "7x7", "17x17")
+SERVING_GROUPS = (2, 7, 16, 70)
+SERVING_AZIM = (16, 32, 48, 64)
+SERVING_SPACING = (0.05, 0.075, 0.1)
+SOURCE_KEFF = 3.0   # fixed eigenvalue of the source solves, above every request's own k
+
+
+def serving_stream(n, seed, mean_gap_ms):
+    """n requests: arrival time, geometry, groups, quadrature, kind, seed."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for i in range(n):
+        t += rng.exponential(mean_gap_ms * 1e-3)
+        out.append(dict(
+            i=i, arrival=t, geom=SERVING_GEOMS[rng.integers(4)],
+            G=int(SERVING_GROUPS[rng.integers(4)]),
+            azim=int(SERVING_AZIM[rng.integers(4)]),
+            spacing=float(SERVING_SPACING[rng.integers(3)]),
+            kind="source" if rng.random() < 0.3 else "eigenvalue"))
+    return out
+
+
+def serving_problems(stream):
+    """Problems of a request stream; track laydowns are generated once per
+    (geometry, quadrature) and each request gets its own perturbed cross
+    sections (factor on sigma_t and the same row of scattering)."""
+    from openmoc_gb300 import lattice
+    tracks = {}
+    probs = []
+    for r in stream:
+        key = (r["geom"], r["azim"], r["spacing"])
+        if key not in tracks:
+            if r["geom"] == "pin":
+                tracks[key] = lattice.pin_cell(2, r["azim"], r["spacing"])
+            elif r["geom"] == "17x17":
+                tracks[key] = lattice.assembly_17x17(2, r["azim"], r["spacing"], config=0)
+            else:
+                n = int(r["geom"][0])
+                tracks[key] = lattice.square_lattice(n, 2, r["azim"], r["spacing"], config=0)
+        mats = lattice._fuel_mod(0, r["G"], 1, perturb=(1000 + r["i"], 0.05))
+        p = tracks[key].with_xs(*lattice.pack_materials(mats))
+        fs = None
+        if r["kind"] == "source":
+            fs = np.zeros((p.num_fsrs, p.num_groups), np.float32)
+            fs[p.fsr_mat == 0, :] = 1.0
+        probs.append((p, fs))
+    return probs
+
+
+def serve_plain(stream, probs, max_iters):
+    """The plain loop: one GB300Solver per request, one at a time, in
+    arrival order (upload, solve, fluxes back)."""
+    from openmoc_gb300 import GB300Solver
+    out = []
+    t0 = time.perf_counter()
+    clock = 0.0
+    for r, (p, fs) in zip(stream, probs):
+        now = time.perf_counter() - t0
+        if now < r["arrival"]:
+            time.sleep(r["arrival"] - now)
+        s = GB300Solver(p)
+        s.setAutotune(False)
+        s.useExponentialIntrinsic()
+        s.setConvergenceThreshold(1e-5)
+        if fs is not None:
+            s.setFixedSources(fs)
+            s.computeSource(max_iters, SOURCE_KEFF, 2)
+        else:
+            s.computeEigenvalue(max_iters, 1)
+        flux = s.getFluxes()
+        out.append(dict(keff=s.getKeff(), iterations=s.getNumIterations(), flux=flux))
+        s.close()
+        clock = time.perf_counter() - t0
+        out[-1]["latency"] = clock - r["arrival"]
+    return out, clock
+
+
+def serve_batched(stream, probs, max_iters, max_solves, k):
+    """The server: requests submitted at their arrival times from this
+    thread while the request loop runs on its own."""
+    from openmoc_gb300.serving import Server, pool_capacity
+    srv = Server(iterations_per_poll=k)
+    by_g = {}
+    for p, _ in probs:
+        by_g.setdefault(p.num_groups, []).append(p)
+    for G, ps in sorted(by_g.items()):
+        srv.add_pool(G, ps[0].num_polar_half, **pool_capacity(ps, max_solves))
+    srv.start()
+    t0 = time.perf_counter()
+    tickets = []
+    for r, (p, fs) in zip(stream, probs):
+        now = time.perf_counter() - t0
+        if now < r["arrival"]:
+            time.sleep(r["arrival"] - now)
+        if fs is not None:
+            t = srv.submit(p, "source", max_iters, 2, k_eff=SOURCE_KEFF, fixed_source=fs)
+        else:
+            t = srv.submit(p, "eigenvalue", max_iters, 1)
+        tickets.append(t)
+    res = [srv.wait(t) for t in tickets]
+    clock = time.perf_counter() - t0
+    stats = srv.stats()
+    srv.stop()
+    srv.close()
+    # submission happens at the arrival time
+    for x in res:
+        x["latency"] = x["t_done"] - x["t_submit"]
+    return res, clock, stats
+
+
+def run_serving(args):
+    import torch  # noqa: F401  (CUDA context and device checks)
+    stream = serving_stream(args.serving_requests, 0xC0FFEE + 2, args.serving_gap_ms)
+    t_prep = time.perf_counter()
+    probs = serving_problems(stream)
+    t_prep = time.perf_counter() - t_prep
+    # warm both paths (kernel loading, autotune caches) on a few requests
+    serve_plain(stream[:4], probs[:4], args.serving_iters)
+    batched, t_b, stats = serve_batched(stream, probs, args.serving_iters,
+                                        args.serving_slots, args.serving_k)
+    plain, t_p = serve_plain(stream, probs, args.serving_iters)
+    dk = max(abs(a["keff"] - b["keff"]) for a, b in zip(batched, plain))
+    df = max(float(np.max(np.abs(a["flux"].astype(np.float64) - b["flux"])
+                          / np.abs(b["flux"].astype(np.float64))))
+             for a, b in zip(batched, plain))
+    lat_b = np.array([x["latency"] for x in batched])
+    lat_p = np.array([x["latency"] for x in plain])
+    n = len(stream)
+    out = {
+        "metric": "solves/s (batched server vs plain per-solve loop)",
+        "value": n / t_b, "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
+        "data": "synthetic (seeded cross sections, generated tracks)",
+        "config": {"workload": SERVING_WORKLOAD, "requests": n,
+                   "mean_interarrival_ms": args.serving_gap_ms,
+                   "source_keff": SOURCE_KEFF, "max_iters": args.serving_iters,
+                   "solves_per_pool": args.serving_slots,
+                   "iterations_per_poll": args.serving_k,
+                   "problem_prep_s": t_prep},
+        "batched": {"solves_per_s": n / t_b, "makespan_s": t_b,
+                    "p50_latency_s": float(np.percentile(lat_b, 50)),
+                    "p99_latency_s": float(np.percentile(lat_b, 99)), "stats": stats},
+        "plain": {"solves_per_s": n / t_p, "makespan_s": t_p,
+                  "p50_latency_s": float(np.percentile(lat_p, 50)),
+                  "p99_latency_s": float(np.percentile(lat_p, 99))},
+        "speedup": t_p / t_b,
+        "agreement": {"max_abs_keff_diff": dk, "max_rel_flux_diff": df,
+                      "unconverged": int(sum(not x["converged"] for x in batched))},
+    }
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -338,12 +494,21 @@ def main():
     ap.add_argument("--cpu-iters", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--shape", default="",
-                    help="lanes,groups_per_lane,exp (0 table, 1 ex2) instead of autotuning")
+                    help="lanes,group_pairs_per_lane,exp (0 table, 1 ex2) instead of autotuning")
+    ap.add_argument("--serving", action="store_true",
+                    help="the request-stream benchmark (batched server vs plain loop)")
+    ap.add_argument("--serving-requests", type=int, default=512)
+    ap.add_argument("--serving-gap-ms", type=float, default=2.0)
+    ap.add_argument("--serving-iters", type=int, default=1000)
+    ap.add_argument("--serving-slots", type=int, default=32)
+    ap.add_argument("--serving-k", type=int, default=8)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.serving:
+        run_serving(args)
     else:
         run_gpu(args)
 

@@ -146,8 +146,9 @@ class GB300Solver:
         if self._ctx is not None:
             self._call("moc_set_exponential", EXP_INTRINSIC)
 
-    def setSweepShape(self, lanes_per_track_direction: int, groups_per_lane: int) -> None:
-        self._shape = (int(lanes_per_track_direction), int(groups_per_lane))
+    def setSweepShape(self, lanes_per_track_direction: int,
+                      group_pairs_per_lane: int) -> None:
+        self._shape = (int(lanes_per_track_direction), int(group_pairs_per_lane))
         if self._ctx is not None:
             self._call("moc_set_sweep_shape", *self._shape)
 
@@ -225,6 +226,20 @@ class GB300Solver:
                                        f"in a {p.num_groups} energy group problem")
         self._fixed_by_material[(int(material), int(group))] = float(source)
         self._push_fixed()
+
+    def setFixedSources(self, sources) -> None:
+        """Every FSR's fixed source at once ([R][G]): the bulk form of
+        setFixedSourceByFSR over all FSRs and groups."""
+        p = self._problem
+        if p is None:
+            raise RuntimeError("set a TrackGenerator before fixed sources")
+        q = np.asarray(sources, np.float32)
+        if q.size != p.num_fsrs * p.num_groups:
+            raise _native.MOCError(-1, f"fixed sources need {p.num_fsrs} x "
+                                       f"{p.num_groups} values, got {q.size}")
+        self._fixed = {}
+        self._fixed_by_material = {}
+        self._upload_fixed(q)
 
     def resetFixedSources(self) -> None:
         self._fixed = {}

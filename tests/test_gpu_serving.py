@@ -15,6 +15,7 @@ from conftest import CASES, load_case
 from openmoc_gb300 import GB300Solver, lattice
 from openmoc_gb300._native import MOCError
 from openmoc_gb300.serving import Server, pool_capacity
+from openmoc_gb300.solver import EXP_INTRINSIC
 
 pytestmark = pytest.mark.gpu
 
@@ -28,12 +29,19 @@ def max_rel(a, b):
     return float(np.max(np.abs(a - b) / np.abs(b)))
 
 
-def make_server(problems, max_solves, k=8, graphs=True, shape=None):
+# Sweep shapes (lanes per track direction, group pairs per lane) with the
+# hardware-ex2 evaluator: a pool and a single solver given the same
+# evaluator differ only in the order of the tally atomics.
+SHAPES = {2: (1, 1), 7: (4, 1), 16: (8, 1), 70: (8, 5)}
+
+
+def make_server(problems, max_solves, k=8, graphs=True, fixed_shape=True):
     srv = Server(iterations_per_poll=k, use_graphs=graphs)
     by_key = {}
     for p in problems:
         by_key.setdefault((p.num_groups, p.num_polar_half), []).append(p)
     for (G, ph), ps in sorted(by_key.items()):
+        shape = (*SHAPES[G], EXP_INTRINSIC) if fixed_shape else None
         srv.add_pool(G, ph, shape=shape, **pool_capacity(ps, max_solves))
     return srv
 
@@ -42,6 +50,8 @@ def single(p, kind="eigenvalue", max_iters=1000, res_type=1, k_eff=1.0,
            threshold=1e-5):
     s = GB300Solver(p)
     s.setConvergenceThreshold(threshold)
+    s.useExponentialIntrinsic()
+    s.setSweepShape(*SHAPES[p.num_groups])
     if kind == "eigenvalue":
         s.computeEigenvalue(max_iters, res_type)
     else:
@@ -53,7 +63,8 @@ def single(p, kind="eigenvalue", max_iters=1000, res_type=1, k_eff=1.0,
 
 def test_fixtures_batched_match_openmoc():
     cases = {c: load_case(c) for c in CASES}
-    srv = make_server([v[0] for v in cases.values()], 2)
+    # pools autotune their sweep shape and evaluator on the first batch
+    srv = make_server([v[0] for v in cases.values()], 2, fixed_shape=False)
     tickets = {}
     for c, (p, sc, _) in cases.items():
         tickets[c] = srv.submit(p, "eigenvalue", int(sc["max_iters"]),
@@ -125,9 +136,27 @@ def test_continuous_admission_with_two_slots():
         ref = single(p)
         assert abs(r["keff"] - ref["keff"]) <= KEFF_TOL
         assert max_rel(r["flux"], ref["flux"]) <= FLUX_TOL
+        assert abs(r["iterations"] - ref["iterations"]) <= 2
     st = srv.stats()
     assert st["admitted"] == len(ps) and st["completed"] == len(ps)
     assert st["graph_captures"] >= 3    # the set of live solves changed
+    srv.close()
+
+
+def test_unconverged_iterates_match_the_single_solver():
+    """Six iterations, far from convergence: every iterate of a solve that
+    reuses a freed slot must equal the single solver's to rounding, which
+    checks the starting state and the per-solve reductions directly."""
+    ps = mix(6)
+    srv = make_server(ps, 2, k=4)
+    tickets = [srv.submit(p, max_iters=6) for p in ps]
+    srv.run_until_idle()
+    for p, t in zip(ps, tickets):
+        r = srv.wait(t, timeout=0)
+        ref = single(p, max_iters=6)
+        assert r["iterations"] == ref["iterations"] == 6
+        assert abs(r["keff"] - ref["keff"]) <= 2e-6 * ref["keff"]
+        assert max_rel(r["flux"], ref["flux"]) <= 2e-5
     srv.close()
 
 
@@ -147,6 +176,8 @@ def test_fixed_source_requests():
 
     s = GB300Solver(p)
     s.setConvergenceThreshold(1e-5)
+    s.useExponentialIntrinsic()
+    s.setSweepShape(*SHAPES[p.num_groups])
     for f in fuel:
         for g in range(p.num_groups):
             s.setFixedSourceByFSR(int(f), g + 1, 1.0)
