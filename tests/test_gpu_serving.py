@@ -5,6 +5,12 @@ Each batched result must match OpenMOC's own on the fixtures (keff within
 GB300Solver on generated problems, and a request must give the same result
 alone and in a mix of other requests (within the same tolerances; tally
 atomics make the last bits order-dependent).
+
+Two solves stopped by the 1e-5 source criterion can differ by one
+iteration, and one iteration of a pin cell's slow upscatter groups moves
+the flux by about 2e-4: comparisons of generated problems therefore
+converge both sides to TIGHT (1e-6), where one iteration moves it ten
+times less.
 """
 import time
 
@@ -21,6 +27,7 @@ pytestmark = pytest.mark.gpu
 
 KEFF_TOL = 1e-5
 FLUX_TOL = 1e-4
+TIGHT = 1e-6
 
 
 def max_rel(a, b):
@@ -99,7 +106,7 @@ def test_same_result_alone_and_in_the_mix():
     target = lattice.square_lattice(3, 7, 24, 0.08, config=3, perturb=(7, 0.05))
     others = mix(6)
     alone = make_server([target] + others, 8)
-    ta = alone.submit(target)
+    ta = alone.submit(target, threshold=TIGHT)
     alone.run_until_idle()
     ra = alone.wait(ta, timeout=0)
     alone.close()
@@ -107,7 +114,7 @@ def test_same_result_alone_and_in_the_mix():
     crowd = make_server([target] + others, 8)
     first = [crowd.submit(p) for p in others[:3]]
     crowd.step()                       # others already running ...
-    tb = crowd.submit(target)          # ... when the target arrives
+    tb = crowd.submit(target, threshold=TIGHT)   # ... when the target arrives
     rest = [crowd.submit(p) for p in others[3:]]
     crowd.run_until_idle()
     rb = crowd.wait(tb, timeout=0)
@@ -115,7 +122,7 @@ def test_same_result_alone_and_in_the_mix():
         assert crowd.wait(t, timeout=0)["converged"]
     crowd.close()
 
-    ref = single(target)
+    ref = single(target, threshold=TIGHT)
     for r in (ra, rb):
         assert abs(r["keff"] - ref["keff"]) <= KEFF_TOL
         assert max_rel(r["flux"], ref["flux"]) <= FLUX_TOL
@@ -127,13 +134,13 @@ def test_same_result_alone_and_in_the_mix():
 def test_continuous_admission_with_two_slots():
     ps = mix(6)
     srv = make_server(ps, 2, k=4)
-    tickets = [srv.submit(p) for p in ps]
+    tickets = [srv.submit(p, threshold=TIGHT) for p in ps]
     n_pending = srv.step()
     assert n_pending == len(ps)         # two admitted, four queued
     srv.run_until_idle()
     for p, t in zip(ps, tickets):
         r = srv.wait(t, timeout=0)
-        ref = single(p)
+        ref = single(p, threshold=TIGHT)
         assert abs(r["keff"] - ref["keff"]) <= KEFF_TOL
         assert max_rel(r["flux"], ref["flux"]) <= FLUX_TOL
         assert abs(r["iterations"] - ref["iterations"]) <= 2
@@ -167,15 +174,16 @@ def test_fixed_source_requests():
     q[fuel, :] = 1.0
     k_sub = 1.5   # above the lattice's own keff: a convergent source problem
     srv = make_server([p], 4)
-    t1 = srv.submit(p, "source", 1000, 2, k_eff=k_sub, fixed_source=q)
-    t2 = srv.submit(p, "eigenvalue")
+    t1 = srv.submit(p, "source", 1000, 2, k_eff=k_sub, fixed_source=q,
+                    threshold=TIGHT)
+    t2 = srv.submit(p, "eigenvalue", threshold=TIGHT)
     srv.run_until_idle()
     r1 = srv.wait(t1, timeout=0)
     r2 = srv.wait(t2, timeout=0)
     srv.close()
 
     s = GB300Solver(p)
-    s.setConvergenceThreshold(1e-5)
+    s.setConvergenceThreshold(TIGHT)
     s.useExponentialIntrinsic()
     s.setSweepShape(*SHAPES[p.num_groups])
     for f in fuel:
@@ -188,8 +196,9 @@ def test_fixed_source_requests():
     assert r1["keff"] == pytest.approx(k_sub)
     assert max_rel(r1["flux"], ref_flux) <= FLUX_TOL
     assert abs(r1["iterations"] - ref_iters) <= 2
-    ref2 = single(p)
+    ref2 = single(p, threshold=TIGHT)
     assert abs(r2["keff"] - ref2["keff"]) <= KEFF_TOL
+    assert max_rel(r2["flux"], ref2["flux"]) <= FLUX_TOL
 
 
 def test_loop_thread_and_graph_free_mode_agree():
@@ -198,7 +207,7 @@ def test_loop_thread_and_graph_free_mode_agree():
     srv.start()
     tickets = []
     for p in ps:
-        tickets.append(srv.submit(p))
+        tickets.append(srv.submit(p, threshold=TIGHT))
         time.sleep(0.002)
     res = [srv.wait(t, timeout=120) for t in tickets]
     srv.stop()
@@ -206,7 +215,7 @@ def test_loop_thread_and_graph_free_mode_agree():
     srv.close()
 
     plain = make_server(ps, 4, k=8, graphs=False)
-    t2 = [plain.submit(p) for p in ps]
+    t2 = [plain.submit(p, threshold=TIGHT) for p in ps]
     plain.run_until_idle()
     for r, t in zip(res, t2):
         r2 = plain.wait(t, timeout=0)
