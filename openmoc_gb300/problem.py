@@ -156,13 +156,19 @@ class Problem:
             raise ValueError("fixed_sources must hold num_fsrs * num_groups")
 
     def with_xs(self, sigma_t, sigma_s, nu_sigma_f, chi) -> "Problem":
-        """A copy sharing the tracks but with other cross sections."""
+        """A copy sharing the tracks but with other cross sections (same
+        materials; the group count follows the new arrays)."""
         p = Problem(**{k: getattr(self, k) for k in self.__dataclass_fields__})
         p.sigma_t = np.ascontiguousarray(sigma_t, np.float32).ravel()
         p.sigma_s = np.ascontiguousarray(sigma_s, np.float32).ravel()
         p.nu_sigma_f = np.ascontiguousarray(nu_sigma_f, np.float32).ravel()
         p.chi = np.ascontiguousarray(chi, np.float32).ravel()
+        if p.sigma_t.size % p.num_materials:
+            raise ValueError("sigma_t must hold num_materials x groups values")
+        p.num_groups = p.sigma_t.size // p.num_materials
+        p.fixed_sources = None
         p.meta = dict(self.meta)
+        p.validate()
         return p
 
 

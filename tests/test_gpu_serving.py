@@ -6,11 +6,14 @@ GB300Solver on generated problems, and a request must give the same result
 alone and in a mix of other requests (within the same tolerances; tally
 atomics make the last bits order-dependent).
 
-Two solves stopped by the 1e-5 source criterion can differ by one
-iteration, and one iteration of a pin cell's slow upscatter groups moves
-the flux by about 2e-4: comparisons of generated problems therefore
-converge both sides to TIGHT (1e-6), where one iteration moves it ten
-times less.
+Two solves stopped by the source criterion can stop one iteration apart
+(the tally atomics decide which side of the threshold a residual falls),
+and near that point one iteration of a pin cell's slowly converging
+upscatter groups still moves the flux by about 2e-4 (the FP64 oracle moves
+keff by 3e-5 between the 1e-5 stop at 39 iterations and 1e-8 at 56).
+Comparisons of generated problems therefore run both sides for the same
+FIXED_ITERS iterations (a threshold no solve reaches), where only the order
+of the atomics differs.
 """
 import time
 
@@ -27,7 +30,8 @@ pytestmark = pytest.mark.gpu
 
 KEFF_TOL = 1e-5
 FLUX_TOL = 1e-4
-TIGHT = 1e-6
+FIXED_ITERS = 60
+NEVER = 1e-12   # threshold: stop at FIXED_ITERS
 
 
 def max_rel(a, b):
@@ -53,8 +57,8 @@ def make_server(problems, max_solves, k=8, graphs=True, fixed_shape=True):
     return srv
 
 
-def single(p, kind="eigenvalue", max_iters=1000, res_type=1, k_eff=1.0,
-           threshold=1e-5):
+def single(p, kind="eigenvalue", max_iters=FIXED_ITERS, res_type=1, k_eff=1.0,
+           threshold=NEVER):
     s = GB300Solver(p)
     s.setConvergenceThreshold(threshold)
     s.useExponentialIntrinsic()
@@ -106,7 +110,7 @@ def test_same_result_alone_and_in_the_mix():
     target = lattice.square_lattice(3, 7, 24, 0.08, config=3, perturb=(7, 0.05))
     others = mix(6)
     alone = make_server([target] + others, 8)
-    ta = alone.submit(target, threshold=TIGHT)
+    ta = alone.submit(target, max_iters=FIXED_ITERS, threshold=NEVER)
     alone.run_until_idle()
     ra = alone.wait(ta, timeout=0)
     alone.close()
@@ -114,7 +118,8 @@ def test_same_result_alone_and_in_the_mix():
     crowd = make_server([target] + others, 8)
     first = [crowd.submit(p) for p in others[:3]]
     crowd.step()                       # others already running ...
-    tb = crowd.submit(target, threshold=TIGHT)   # ... when the target arrives
+    tb = crowd.submit(target, max_iters=FIXED_ITERS,
+                      threshold=NEVER)   # ... when the target arrives
     rest = [crowd.submit(p) for p in others[3:]]
     crowd.run_until_idle()
     rb = crowd.wait(tb, timeout=0)
@@ -122,11 +127,11 @@ def test_same_result_alone_and_in_the_mix():
         assert crowd.wait(t, timeout=0)["converged"]
     crowd.close()
 
-    ref = single(target, threshold=TIGHT)
+    ref = single(target)
     for r in (ra, rb):
+        assert r["iterations"] == ref["iterations"] == FIXED_ITERS
         assert abs(r["keff"] - ref["keff"]) <= KEFF_TOL
         assert max_rel(r["flux"], ref["flux"]) <= FLUX_TOL
-        assert abs(r["iterations"] - ref["iterations"]) <= 2
     assert abs(ra["keff"] - rb["keff"]) <= KEFF_TOL
     assert max_rel(ra["flux"], rb["flux"]) <= FLUX_TOL
 
@@ -134,16 +139,16 @@ def test_same_result_alone_and_in_the_mix():
 def test_continuous_admission_with_two_slots():
     ps = mix(6)
     srv = make_server(ps, 2, k=4)
-    tickets = [srv.submit(p, threshold=TIGHT) for p in ps]
+    tickets = [srv.submit(p, max_iters=FIXED_ITERS, threshold=NEVER) for p in ps]
     n_pending = srv.step()
     assert n_pending == len(ps)         # two admitted, four queued
     srv.run_until_idle()
     for p, t in zip(ps, tickets):
         r = srv.wait(t, timeout=0)
-        ref = single(p, threshold=TIGHT)
+        ref = single(p)
+        assert r["iterations"] == ref["iterations"] == FIXED_ITERS
         assert abs(r["keff"] - ref["keff"]) <= KEFF_TOL
         assert max_rel(r["flux"], ref["flux"]) <= FLUX_TOL
-        assert abs(r["iterations"] - ref["iterations"]) <= 2
     st = srv.stats()
     assert st["admitted"] == len(ps) and st["completed"] == len(ps)
     assert st["graph_captures"] >= 3    # the set of live solves changed
@@ -156,7 +161,7 @@ def test_unconverged_iterates_match_the_single_solver():
     checks the starting state and the per-solve reductions directly."""
     ps = mix(6)
     srv = make_server(ps, 2, k=4)
-    tickets = [srv.submit(p, max_iters=6) for p in ps]
+    tickets = [srv.submit(p, max_iters=6, threshold=NEVER) for p in ps]
     srv.run_until_idle()
     for p, t in zip(ps, tickets):
         r = srv.wait(t, timeout=0)
@@ -174,29 +179,29 @@ def test_fixed_source_requests():
     q[fuel, :] = 1.0
     k_sub = 1.5   # above the lattice's own keff: a convergent source problem
     srv = make_server([p], 4)
-    t1 = srv.submit(p, "source", 1000, 2, k_eff=k_sub, fixed_source=q,
-                    threshold=TIGHT)
-    t2 = srv.submit(p, "eigenvalue", threshold=TIGHT)
+    t1 = srv.submit(p, "source", FIXED_ITERS, 2, k_eff=k_sub, fixed_source=q,
+                    threshold=NEVER)
+    t2 = srv.submit(p, "eigenvalue", FIXED_ITERS, threshold=NEVER)
     srv.run_until_idle()
     r1 = srv.wait(t1, timeout=0)
     r2 = srv.wait(t2, timeout=0)
     srv.close()
 
     s = GB300Solver(p)
-    s.setConvergenceThreshold(TIGHT)
+    s.setConvergenceThreshold(NEVER)
     s.useExponentialIntrinsic()
     s.setSweepShape(*SHAPES[p.num_groups])
     for f in fuel:
         for g in range(p.num_groups):
             s.setFixedSourceByFSR(int(f), g + 1, 1.0)
-    s.computeSource(1000, k_sub, 2)
+    s.computeSource(FIXED_ITERS, k_sub, 2)
     ref_flux = s.getFluxes()
     ref_iters = s.getNumIterations()
     s.close()
     assert r1["keff"] == pytest.approx(k_sub)
     assert max_rel(r1["flux"], ref_flux) <= FLUX_TOL
-    assert abs(r1["iterations"] - ref_iters) <= 2
-    ref2 = single(p, threshold=TIGHT)
+    assert r1["iterations"] == ref_iters == FIXED_ITERS
+    ref2 = single(p)
     assert abs(r2["keff"] - ref2["keff"]) <= KEFF_TOL
     assert max_rel(r2["flux"], ref2["flux"]) <= FLUX_TOL
 
@@ -207,7 +212,7 @@ def test_loop_thread_and_graph_free_mode_agree():
     srv.start()
     tickets = []
     for p in ps:
-        tickets.append(srv.submit(p, threshold=TIGHT))
+        tickets.append(srv.submit(p, max_iters=FIXED_ITERS, threshold=NEVER))
         time.sleep(0.002)
     res = [srv.wait(t, timeout=120) for t in tickets]
     srv.stop()
@@ -215,7 +220,7 @@ def test_loop_thread_and_graph_free_mode_agree():
     srv.close()
 
     plain = make_server(ps, 4, k=8, graphs=False)
-    t2 = [plain.submit(p, threshold=TIGHT) for p in ps]
+    t2 = [plain.submit(p, max_iters=FIXED_ITERS, threshold=NEVER) for p in ps]
     plain.run_until_idle()
     for r, t in zip(res, t2):
         r2 = plain.wait(t, timeout=0)
