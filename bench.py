@@ -392,6 +392,7 @@ def serve_plain(stream, probs, max_iters):
         now = time.perf_counter() - t0
         if now < r["arrival"]:
             time.sleep(r["arrival"] - now)
+        t_start = time.perf_counter()
         s = GB300Solver(p)
         s.setAutotune(False)
         s.useExponentialIntrinsic()
@@ -402,9 +403,11 @@ def serve_plain(stream, probs, max_iters):
         else:
             s.computeEigenvalue(max_iters, 1)
         flux = s.getFluxes()
-        out.append(dict(keff=s.getKeff(), iterations=s.getNumIterations(), flux=flux))
+        out.append(dict(keff=s.getKeff(), iterations=s.getNumIterations(), flux=flux,
+                        sweep_s=s.getSweepTime()[0] * 1e-3))
         s.close()
         clock = time.perf_counter() - t0
+        out[-1]["solve_s"] = time.perf_counter() - t_start
         out[-1]["latency"] = clock - r["arrival"]
     return out, clock
 
@@ -457,6 +460,16 @@ def run_serving(args):
     df = max(float(np.max(np.abs(a["flux"].astype(np.float64) - b["flux"])
                           / np.abs(b["flux"].astype(np.float64))))
              for a, b in zip(batched, plain))
+    classes = {}
+    for r, (p, _), a in zip(stream, probs, plain):
+        c = classes.setdefault(f'{r["geom"]}/{r["G"]}g', dict(
+            requests=0, plain_solve_s=0.0, plain_sweep_s=0.0, iterations=0,
+            integrations=0.0))
+        c["requests"] += 1
+        c["plain_solve_s"] += a["solve_s"]
+        c["plain_sweep_s"] += a["sweep_s"]
+        c["iterations"] += a["iterations"]
+        c["integrations"] += float(p.integrations_per_sweep) * a["iterations"]
     lat_b = np.array([x["latency"] for x in batched])
     lat_p = np.array([x["latency"] for x in plain])
     n = len(stream)
@@ -477,6 +490,7 @@ def run_serving(args):
                   "p50_latency_s": float(np.percentile(lat_p, 50)),
                   "p99_latency_s": float(np.percentile(lat_p, 99))},
         "speedup": t_p / t_b,
+        "plain_by_class": classes,
         "agreement": {"max_abs_keff_diff": dk, "max_rel_flux_diff": df,
                       "unconverged": int(sum(not x["converged"] for x in batched))},
     }
