@@ -21,8 +21,8 @@
  *     copied out and their ranges freed) and admits queued requests into the
  *     freed ranges (continuous batching); pools run on their own streams, so
  *     their work overlaps on the device;
- *   - the sweep shape (lanes per track, group pairs per lane, exponential
- *     evaluator) of a pool is autotuned on its first batch unless fixed.
+ *   - the sweep shape of a pool (lanes per track, group pairs per lane;
+ *     hardware-ex2 evaluator) is autotuned on its first batch unless fixed.
  *
  * Requests reference host arrays owned by the caller, which must stay valid
  * (and flux_out writable) until the request completes.  Every entry point
@@ -65,7 +65,7 @@ typedef struct {
   int64_t max_segments;   /* segments */
   int32_t lanes;          /* sweep lanes per track direction; 0: autotune */
   int32_t pairs;          /* group pairs per lane (with lanes) */
-  int32_t exp_kind;       /* MOC_EXP_* (with lanes) */
+  int32_t exp_kind;       /* with lanes: MOC_EXP_INTRINSIC (pools use ex2) */
 } moc_pool_config;
 
 typedef struct {
@@ -112,6 +112,10 @@ typedef struct {
   int64_t graph_captures;  /* CUDA graphs captured */
   int64_t kernel_launches; /* kernels run, graph nodes included */
   int64_t live, queued;
+  double gpu_busy_s;       /* device time of all blocks (pools overlap) */
+  double host_admit_s;     /* loop time spent uploading admitted solves */
+  double host_retire_s;    /* loop time spent copying out finished solves */
+  double host_graph_s;     /* loop time spent capturing CUDA graphs */
 } moc_server_stats;
 
 int moc_server_create(const moc_server_config* cfg, moc_server** out);

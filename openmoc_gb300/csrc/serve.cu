@@ -342,6 +342,7 @@ struct Pool {
   int index = 0;
   int G = 0, Ph = 0, ld = 0, F = 0;
   cudaStream_t stream = nullptr;
+  cudaEvent_t block_start = nullptr;
   cudaEvent_t block_done = nullptr;
   std::vector<cudaEvent_t> tune_ev;
 
@@ -450,6 +451,7 @@ void destroy_pool(Pool& p) {
   p.slots_h = p.init_h = nullptr;
   p.retire_h = nullptr;
   for (cudaEvent_t e : p.tune_ev) cudaEventDestroy(e);
+  if (p.block_start) cudaEventDestroy(p.block_start);
   if (p.block_done) cudaEventDestroy(p.block_done);
   if (p.stream) cudaStreamDestroy(p.stream);
   p.stream = nullptr;
@@ -475,8 +477,8 @@ int create_pool(moc_server* srv, const moc_pool_config& c, Pool& p) {
     SV_CHECK(c.pairs >= 1 && c.pairs <= moc::kMaxSlots &&
                  2 * (int64_t) c.lanes * c.pairs >= c.num_groups,
              MOC_ERR_ARG, "lanes x group pairs per lane must cover every group");
-    SV_CHECK(c.exp_kind == MOC_EXP_TABLE || c.exp_kind == MOC_EXP_INTRINSIC,
-             MOC_ERR_ARG, "unknown exponential evaluator");
+    SV_CHECK(c.exp_kind == MOC_EXP_INTRINSIC, MOC_ERR_UNSUPPORTED,
+             "pools sweep with the hardware-ex2 evaluator (MOC_EXP_INTRINSIC)");
   }
   p.cfg = c;
   p.G = c.num_groups;
@@ -490,7 +492,8 @@ int create_pool(moc_server* srv, const moc_pool_config& c, Pool& p) {
     p.tuned = true;
   }
   SV_CUDA(cudaStreamCreateWithFlags(&p.stream, cudaStreamNonBlocking));
-  SV_CUDA(cudaEventCreateWithFlags(&p.block_done, cudaEventDisableTiming));
+  SV_CUDA(cudaEventCreate(&p.block_start));
+  SV_CUDA(cudaEventCreate(&p.block_done));
   const int64_t R = c.max_fsrs, T = c.max_tracks, S = c.max_segments;
   const int64_t M = c.max_materials, A = c.max_angles, N = c.max_solves;
   const int64_t MG = M * p.G, npsi = T * 2 * p.F;
@@ -887,9 +890,9 @@ int rebuild_order(Pool& p) {
 int pairs_for(int G, int lps) { return ((G + 1) / 2 + lps - 1) / lps; }
 
 // Times every sweep shape with at most kMaxSlots pairs per lane and at
-// least half of its lanes busy, with both exponential evaluators, on the
-// pool's current solves (median of three sweeps after a warm-up), and keeps
-// the fastest.  Runs before those solves' starting state is written.
+// least half of its lanes busy on the pool's current solves (median of
+// three sweeps after a warm-up) and keeps the fastest.  Pools sweep with the
+// hardware-ex2 evaluator, the faster one on every workload measured.
 int autotune_pool(moc_server* srv, Pool& p) {
   if (p.tune_ev.empty()) {
     p.tune_ev.resize(2);
@@ -897,7 +900,7 @@ int autotune_pool(moc_server* srv, Pool& p) {
   }
   float best_ms = 1e30f;
   int best_lps = 0, best_pairs = 0, best_kind = MOC_EXP_INTRINSIC;
-  for (int kind : {MOC_EXP_TABLE, MOC_EXP_INTRINSIC}) {
+  for (int kind : {MOC_EXP_INTRINSIC}) {
     for (int lps = 1; lps <= 32; lps *= 2) {
       const int pairs = pairs_for(p.G, lps);
       if (pairs > moc::kMaxSlots ||
@@ -970,6 +973,7 @@ int launch_block(moc_server* srv, Pool& p) {
   const int K = std::max(1, srv->cfg.iterations_per_poll);
   if (srv->cfg.use_graphs) {
     if (!p.graph || p.graph_iters != K) {
+      const double t_cap = now_s();
       if (p.graph) cudaGraphExecDestroy(p.graph);
       p.graph = nullptr;
       cudaGraph_t g = nullptr;
@@ -985,9 +989,12 @@ int launch_block(moc_server* srv, Pool& p) {
       p.graph_iters = K;
       std::lock_guard<std::mutex> lk(srv->mu);
       srv->stats.graph_captures++;
+      srv->stats.host_graph_s += now_s() - t_cap;
     }
+    SV_CUDA(cudaEventRecord(p.block_start, p.stream));
     SV_CUDA(cudaGraphLaunch(p.graph, p.stream));
   } else {
+    SV_CUDA(cudaEventRecord(p.block_start, p.stream));
     for (int k = 0; k < K; k++) SV_TRY(enqueue_iteration(p));
   }
   SV_CUDA(cudaMemcpyAsync(p.slots_h, p.slots_d,
@@ -1043,10 +1050,25 @@ int service(moc_server* srv, Pool& p, bool wait, bool* progressed) {
       SV_CUDA(e);
     }
     p.in_flight = false;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p.block_start, p.block_done) == cudaSuccess) {
+      std::lock_guard<std::mutex> lk(srv->mu);
+      srv->stats.gpu_busy_s += 1e-3 * ms;
+    }
+    const double t_ret = now_s();
     SV_TRY(retire(srv, p));
+    {
+      std::lock_guard<std::mutex> lk(srv->mu);
+      srv->stats.host_retire_s += now_s() - t_ret;
+    }
     *progressed = true;
   }
+  const double t_adm = now_s();
   SV_TRY(admit(srv, p));
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    srv->stats.host_admit_s += now_s() - t_adm;
+  }
   const bool had = p.in_flight;
   SV_TRY(launch_block(srv, p));
   if (p.in_flight && !had) *progressed = true;

@@ -106,7 +106,9 @@ struct SweepOccupancy {
       (PH * PS > 6) ? MOC_SWEEP_BIG_MIN_BLOCKS : 8;
 };
 
-template <int PH, int LPS, int PS, int EXPK>
+// POOL: the tracks of many solves (a batched pool); each track takes its
+// pending angular-flux scale and done flag from its own solve's state.
+template <int PH, int LPS, int PS, int EXPK, bool POOL>
 __global__ void __launch_bounds__(kSweepThreads,
                                   (SweepOccupancy<PH, PS>::min_blocks))
 sweep_kernel(const SweepArgs a) {
@@ -139,20 +141,24 @@ sweep_kernel(const SweepArgs a) {
   const int64_t stream = gwarp * (32 / LPS) + lane / LPS;
   const int npairs = ld >> 1;
 
-  // the solve of this track (a pool) or the context's own state; the LPS
-  // lanes of a stream share the track, so they agree on skipping it
+  // the track and its pending scale; in a pool the solve of the track may
+  // be finished (the LPS lanes of a stream share the track, so they agree
+  // on skipping it)
   int t = 0;
-  const DevScalars* ts = sc;
+  float scale = 1.0f;
   bool live = stream < 2 * a.num_tracks;
-  if (live) {
-    t = a.order[stream >> 1];
-    if (a.track_slot) {
-      ts = a.slots + a.track_slot[t];
+  if (POOL) {
+    if (live) {
+      t = a.order[stream >> 1];
+      const DevScalars* ts = a.slots + a.track_slot[t];
       live = ts->done == 0;
+      scale = ts->scale[cur];
     }
+  } else {
+    scale = sc->scale[cur];
+    if (live) t = a.order[stream >> 1];
   }
   if (live) {
-    const float scale = ts->scale[cur];
     const int dir = (int) (stream & 1);
     const int64_t b = a.seg_off[t];
     const int n = (int) (a.seg_off[t + 1] - b);
@@ -309,8 +315,9 @@ sweep_kernel(const SweepArgs a) {
   }
   __syncthreads();
   if (last) {
-    for (int i = threadIdx.x; i < a.num_slots; i += blockDim.x)
-      a.slots[i].scale[cur ^ 1] = 1.0f;
+    if (POOL)
+      for (int i = threadIdx.x; i < a.num_slots; i += blockDim.x)
+        a.slots[i].scale[cur ^ 1] = 1.0f;
     if (threadIdx.x == 0) {
       sc->ticket_sweep = 0;
       sc->scale[cur ^ 1] = 1.0f;
@@ -320,7 +327,7 @@ sweep_kernel(const SweepArgs a) {
   }
 }
 
-template <int PH, int LPS, int PS, int EXPK>
+template <int PH, int LPS, int PS, int EXPK, bool POOL>
 void launch_sweep_instance(const SweepArgs& a, cudaStream_t stream) {
   const int spw = 32 / LPS;
   const int64_t warps = (2 * a.num_tracks + spw - 1) / spw;
@@ -329,7 +336,7 @@ void launch_sweep_instance(const SweepArgs& a, cudaStream_t stream) {
   const size_t smem =
       sizeof(float) * ((size_t) a.num_materials * a.ld +
                        (EXPK == kExpTable ? 2 * kExpTableSize : 0));
-  auto kern = sweep_kernel<PH, LPS, PS, EXPK>;
+  auto kern = sweep_kernel<PH, LPS, PS, EXPK, POOL>;
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int) smem);
@@ -337,17 +344,30 @@ void launch_sweep_instance(const SweepArgs& a, cudaStream_t stream) {
 }
 
 // slots = pairs of groups per lane
-template <int PH, int LPS, int EXPK>
-bool dispatch_sweep_slots(const SweepArgs& a, int slots, cudaStream_t s) {
+template <int PH, int LPS, int EXPK, bool POOL>
+bool launch_sweep_pairs(const SweepArgs& a, int slots, cudaStream_t s) {
   switch (slots) {
-    case 1: launch_sweep_instance<PH, LPS, 1, EXPK>(a, s); return true;
-    case 2: launch_sweep_instance<PH, LPS, 2, EXPK>(a, s); return true;
-    case 3: launch_sweep_instance<PH, LPS, 3, EXPK>(a, s); return true;
-    case 4: launch_sweep_instance<PH, LPS, 4, EXPK>(a, s); return true;
-    case 5: launch_sweep_instance<PH, LPS, 5, EXPK>(a, s); return true;
-    case 6: launch_sweep_instance<PH, LPS, 6, EXPK>(a, s); return true;
+    case 1: launch_sweep_instance<PH, LPS, 1, EXPK, POOL>(a, s); return true;
+    case 2: launch_sweep_instance<PH, LPS, 2, EXPK, POOL>(a, s); return true;
+    case 3: launch_sweep_instance<PH, LPS, 3, EXPK, POOL>(a, s); return true;
+    case 4: launch_sweep_instance<PH, LPS, 4, EXPK, POOL>(a, s); return true;
+    case 5: launch_sweep_instance<PH, LPS, 5, EXPK, POOL>(a, s); return true;
+    case 6: launch_sweep_instance<PH, LPS, 6, EXPK, POOL>(a, s); return true;
     default: return false;
   }
+}
+
+// Pools (a.track_slot set) have instances for the hardware-ex2 evaluator
+// only.
+template <int PH, int LPS, int EXPK>
+bool dispatch_sweep_slots(const SweepArgs& a, int slots, cudaStream_t s) {
+  if (a.track_slot) {
+    if constexpr (EXPK == kExpIntrinsic)
+      return launch_sweep_pairs<PH, LPS, EXPK, true>(a, slots, s);
+    else
+      return false;
+  }
+  return launch_sweep_pairs<PH, LPS, EXPK, false>(a, slots, s);
 }
 
 template <int PH, int EXPK>

@@ -79,7 +79,9 @@ class Result(C.Structure):
 class Stats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in (
         "submitted", "admitted", "completed", "failed", "blocks",
-        "graph_captures", "kernel_launches", "live", "queued")]
+        "graph_captures", "kernel_launches", "live", "queued")] + [
+        (n, C.c_double) for n in (
+            "gpu_busy_s", "host_admit_s", "host_retire_s", "host_graph_s")]
 
 
 _P = C.c_void_p
