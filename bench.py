@@ -420,8 +420,9 @@ def serve_batched(stream, probs, max_iters, max_solves, k):
     by_g = {}
     for p, _ in probs:
         by_g.setdefault(p.num_groups, []).append(p)
+    pools = []
     for G, ps in sorted(by_g.items()):
-        srv.add_pool(G, ps[0].num_polar_half, **pool_capacity(ps, max_solves))
+        pools.append(srv.add_pool(G, ps[0].num_polar_half, **pool_capacity(ps, max_solves)))
     srv.start()
     t0 = time.perf_counter()
     tickets = []
@@ -437,6 +438,7 @@ def serve_batched(stream, probs, max_iters, max_solves, k):
     res = [srv.wait(t) for t in tickets]
     clock = time.perf_counter() - t0
     stats = srv.stats()
+    stats["pools"] = [srv.pool_stats(i) for i in pools]
     srv.stop()
     srv.close()
     # submission happens at the arrival time
@@ -456,10 +458,17 @@ def run_serving(args):
     batched, t_b, stats = serve_batched(stream, probs, args.serving_iters,
                                         args.serving_slots, args.serving_k)
     plain, t_p = serve_plain(stream, probs, args.serving_iters)
-    dk = max(abs(a["keff"] - b["keff"]) for a, b in zip(batched, plain))
-    df = max(float(np.max(np.abs(a["flux"].astype(np.float64) - b["flux"])
-                          / np.abs(b["flux"].astype(np.float64))))
-             for a, b in zip(batched, plain))
+    diffs = []
+    for r, a, b in zip(stream, batched, plain):
+        fa, fb = a["flux"].astype(np.float64), b["flux"].astype(np.float64)
+        diffs.append(dict(
+            request=r["i"], cls=f'{r["geom"]}/{r["G"]}g/{r["kind"]}',
+            dk=abs(a["keff"] - b["keff"]),
+            dflux=float(np.max(np.abs(fa - fb) / np.abs(fb))),
+            iterations=(a["iterations"], b["iterations"])))
+    dk = max(d["dk"] for d in diffs)
+    df = max(d["dflux"] for d in diffs)
+    worst = sorted(diffs, key=lambda d: -d["dflux"])[:5]
     classes = {}
     for r, (p, _), a in zip(stream, probs, plain):
         c = classes.setdefault(f'{r["geom"]}/{r["G"]}g', dict(
@@ -492,7 +501,10 @@ def run_serving(args):
         "speedup": t_p / t_b,
         "plain_by_class": classes,
         "agreement": {"max_abs_keff_diff": dk, "max_rel_flux_diff": df,
-                      "unconverged": int(sum(not x["converged"] for x in batched))},
+                      "same_iterations": int(sum(d["iterations"][0] == d["iterations"][1]
+                                                 for d in diffs)),
+                      "unconverged": int(sum(not x["converged"] for x in batched)),
+                      "worst": worst},
     }
     print(json.dumps(out), flush=True)
 

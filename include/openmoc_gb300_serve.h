@@ -149,6 +149,17 @@ int moc_server_poll(moc_server* srv, int64_t* tickets, int capacity,
 
 int moc_server_stats_get(moc_server* srv, moc_server_stats* out);
 
+typedef struct {
+  int32_t num_groups, num_polar_half;
+  int32_t lanes, pairs, exp_kind; /* sweep shape in use (autotuned or fixed) */
+  int32_t live;
+  int64_t admitted, completed, blocks;
+  double gpu_busy_s;
+} moc_pool_stats;
+
+/** Statistics and sweep shape of one pool. */
+int moc_server_pool_stats(moc_server* srv, int pool, moc_pool_stats* out);
+
 #ifdef __cplusplus
 }
 #endif

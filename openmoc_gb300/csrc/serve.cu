@@ -393,6 +393,9 @@ struct Pool {
 
   int lps = 0, pairs = 0, exp_kind = MOC_EXP_INTRINSIC;
   bool tuned = false;
+  // counters (read under the server mutex)
+  int64_t n_admitted = 0, n_completed = 0, n_blocks = 0;
+  double busy_s = 0.0;
 };
 
 }  // namespace
@@ -780,6 +783,7 @@ int admit(moc_server* srv, Pool& p) {
       sl.st = std::move(*it);
       it = p.queue.erase(it);
       srv->stats.admitted++;
+      p.n_admitted++;
       srv->stats.queued--;
       srv->stats.live++;
       p.dirty = true;
@@ -843,6 +847,10 @@ int retire(moc_server* srv, Pool& p) {
     p.mats.release(sl.m0, s.M);
     p.angles.release(sl.a0, s.A);
     sl.live = false;
+    {
+      std::lock_guard<std::mutex> lk(srv->mu);
+      p.n_completed++;
+    }
     publish(srv, s, res);
     sl.st.reset();
     p.free_slots.push_back(i);
@@ -1005,6 +1013,7 @@ int launch_block(moc_server* srv, Pool& p) {
   {
     std::lock_guard<std::mutex> lk(srv->mu);
     srv->stats.blocks++;
+    p.n_blocks++;
     srv->stats.kernel_launches += 6 * K;
   }
   return MOC_OK;
@@ -1054,6 +1063,7 @@ int service(moc_server* srv, Pool& p, bool wait, bool* progressed) {
     if (cudaEventElapsedTime(&ms, p.block_start, p.block_done) == cudaSuccess) {
       std::lock_guard<std::mutex> lk(srv->mu);
       srv->stats.gpu_busy_s += 1e-3 * ms;
+      p.busy_s += 1e-3 * ms;
     }
     const double t_ret = now_s();
     SV_TRY(retire(srv, p));
@@ -1260,6 +1270,26 @@ int moc_server_poll(moc_server* srv, int64_t* tickets, int capacity,
   for (int i = 0; i < n; i++) tickets[i] = srv->completed[i];
   srv->completed.erase(srv->completed.begin(), srv->completed.begin() + n);
   *count = n;
+  return MOC_OK;
+}
+
+int moc_server_pool_stats(moc_server* srv, int pool, moc_pool_stats* out) {
+  SV_CHECK(srv && out, MOC_ERR_ARG, "null argument");
+  SV_CHECK(pool >= 0 && pool < (int) srv->pools.size(), MOC_ERR_ARG,
+           "no pool " + std::to_string(pool));
+  std::lock_guard<std::mutex> lk(srv->mu);
+  const Pool& p = *srv->pools[pool];
+  out->num_groups = p.G;
+  out->num_polar_half = p.Ph;
+  out->lanes = p.lps;
+  out->pairs = p.pairs;
+  out->exp_kind = p.exp_kind;
+  out->live = 0;
+  for (const Slot& sl : p.slots) out->live += sl.live ? 1 : 0;
+  out->admitted = p.n_admitted;
+  out->completed = p.n_completed;
+  out->blocks = p.n_blocks;
+  out->gpu_busy_s = p.busy_s;
   return MOC_OK;
 }
 

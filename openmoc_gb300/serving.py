@@ -84,6 +84,13 @@ class Stats(C.Structure):
             "gpu_busy_s", "host_admit_s", "host_retire_s", "host_graph_s")]
 
 
+class PoolStats(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in (
+        "num_groups", "num_polar_half", "lanes", "pairs", "exp_kind", "live")] + [
+        (n, C.c_int64) for n in ("admitted", "completed", "blocks")] + [
+        ("gpu_busy_s", C.c_double)]
+
+
 _P = C.c_void_p
 _SIGS = {
     "moc_server_create": ([C.POINTER(ServerConfig), C.POINTER(C.c_void_p)], C.c_int),
@@ -96,6 +103,7 @@ _SIGS = {
     "moc_server_wait": ([_P, C.c_int64, C.c_double, C.POINTER(Result)], C.c_int),
     "moc_server_poll": ([_P, _P, C.c_int, C.POINTER(C.c_int)], C.c_int),
     "moc_server_stats_get": ([_P, C.POINTER(Stats)], C.c_int),
+    "moc_server_pool_stats": ([_P, C.c_int, C.POINTER(PoolStats)], C.c_int),
 }
 
 _bound = False
@@ -257,6 +265,11 @@ class Server:
         s = Stats()
         _native.check(_lib().moc_server_stats_get(self._h, C.byref(s)))
         return {n: getattr(s, n) for n, _ in Stats._fields_}
+
+    def pool_stats(self, pool: int) -> dict:
+        s = PoolStats()
+        _native.check(_lib().moc_server_pool_stats(self._h, pool, C.byref(s)))
+        return {n: getattr(s, n) for n, _ in PoolStats._fields_}
 
     def close(self) -> None:
         if self._h:
