@@ -22,7 +22,9 @@
  *     freed ranges (continuous batching); pools run on their own streams, so
  *     their work overlaps on the device;
  *   - the sweep shape of a pool (lanes per track, group pairs per lane;
- *     hardware-ex2 evaluator) is autotuned on its first batch unless fixed.
+ *     hardware-ex2 evaluator) is autotuned on the live solves, once per
+ *     size class (power of two of live tracks), unless fixed; the timing
+ *     sweeps write into scratch buffers, so live state is untouched.
  *
  * Requests reference host arrays owned by the caller, which must stay valid
  * (and flux_out writable) until the request completes.  Every entry point
@@ -154,6 +156,7 @@ typedef struct {
   int32_t lanes, pairs, exp_kind; /* sweep shape in use (autotuned or fixed) */
   int32_t live;
   int64_t admitted, completed, blocks;
+  int64_t tunes;          /* autotuner runs (one per size class met) */
   double gpu_busy_s;
 } moc_pool_stats;
 

@@ -392,9 +392,15 @@ struct Pool {
   int graph_iters = 0;
 
   int lps = 0, pairs = 0, exp_kind = MOC_EXP_INTRINSIC;
-  bool tuned = false;
+  int graph_lps = 0, graph_pairs = 0;          // shape of the captured graph
+  std::map<int, std::pair<int, int>> shape_by_class;
+  // autotuner scratch outputs
+  float* tune_psi = nullptr;
+  float* tune_phi = nullptr;
+  moc::DevScalars* tune_sc = nullptr;
+  moc::DevScalars* tune_slots = nullptr;
   // counters (read under the server mutex)
-  int64_t n_admitted = 0, n_completed = 0, n_blocks = 0;
+  int64_t n_admitted = 0, n_completed = 0, n_blocks = 0, n_tunes = 0;
   double busy_s = 0.0;
 };
 
@@ -448,6 +454,10 @@ void destroy_pool(Pool& p) {
   dev_free(p.row_val);
   dev_free(p.sc);
   dev_free(p.slots_d);
+  dev_free(p.tune_psi);
+  dev_free(p.tune_phi);
+  dev_free(p.tune_sc);
+  dev_free(p.tune_slots);
   if (p.slots_h) cudaFreeHost(p.slots_h);
   if (p.init_h) cudaFreeHost(p.init_h);
   if (p.retire_h) cudaFreeHost(p.retire_h);
@@ -492,7 +502,6 @@ int create_pool(moc_server* srv, const moc_pool_config& c, Pool& p) {
     p.lps = c.lanes;
     p.pairs = c.pairs;
     p.exp_kind = c.exp_kind;
-    p.tuned = true;
   }
   SV_CUDA(cudaStreamCreateWithFlags(&p.stream, cudaStreamNonBlocking));
   SV_CUDA(cudaEventCreate(&p.block_start));
@@ -898,52 +907,94 @@ int rebuild_order(Pool& p) {
 int pairs_for(int G, int lps) { return ((G + 1) / 2 + lps - 1) / lps; }
 
 // Times every sweep shape with at most kMaxSlots pairs per lane and at
-// least half of its lanes busy on the pool's current solves (median of
-// three sweeps after a warm-up) and keeps the fastest.  Pools sweep with the
-// hardware-ex2 evaluator, the faster one on every workload measured.
+// least half of its lanes busy on the pool's current solves (the faster of
+// two sweeps after a warm-up) and keeps the fastest.  The timing sweeps read
+// the live tracks and sources but write tallies, angular fluxes, the buffer
+// index and the solves' scales into scratch copies, so the live state is
+// untouched and a pool can be retuned whenever its track count changes
+// scale.  Pools sweep with the hardware-ex2 evaluator, the faster one on
+// every workload measured.
 int autotune_pool(moc_server* srv, Pool& p) {
   if (p.tune_ev.empty()) {
     p.tune_ev.resize(2);
     for (auto& e : p.tune_ev) SV_CUDA(cudaEventCreate(&e));
   }
+  const int N = p.cfg.max_solves;
+  if (!p.tune_psi) {
+    const int64_t npsi = p.cfg.max_tracks * 2 * p.F;
+    SV_TRY(dev_alloc(&p.tune_psi, npsi));
+    SV_TRY(dev_alloc(&p.tune_phi, p.cfg.max_fsrs * p.ld));
+    SV_TRY(dev_alloc(&p.tune_sc, 1));
+    SV_TRY(dev_alloc(&p.tune_slots, N));
+    SV_CUDA(cudaMemsetAsync(p.tune_psi, 0, sizeof(float) * npsi, p.stream));
+  }
+  SV_CUDA(cudaMemcpyAsync(p.tune_sc, p.sc, sizeof(moc::DevScalars),
+                          cudaMemcpyDeviceToDevice, p.stream));
+  SV_CUDA(cudaMemcpyAsync(p.tune_slots, p.slots_d, sizeof(moc::DevScalars) * N,
+                          cudaMemcpyDeviceToDevice, p.stream));
   float best_ms = 1e30f;
-  int best_lps = 0, best_pairs = 0, best_kind = MOC_EXP_INTRINSIC;
-  for (int kind : {MOC_EXP_INTRINSIC}) {
-    for (int lps = 1; lps <= 32; lps *= 2) {
-      const int pairs = pairs_for(p.G, lps);
-      if (pairs > moc::kMaxSlots ||
-          (double) p.G / (2.0 * lps * pairs) < 0.5)
-        continue;
-      p.lps = lps;
-      moc::SweepArgs a = pool_sweep_args(p);
-      std::vector<float> ms;
-      for (int r = 0; r < 4; r++) {
-        SV_CUDA(cudaEventRecord(p.tune_ev[0], p.stream));
-        if (!moc::launch_sweep(a, p.Ph, pairs, kind, p.stream))
-          return SV_FAIL(MOC_ERR_UNSUPPORTED, "no sweep kernel for the pool");
-        SV_CUDA(cudaEventRecord(p.tune_ev[1], p.stream));
-        SV_CUDA(cudaEventSynchronize(p.tune_ev[1]));
-        float t = 0.f;
-        SV_CUDA(cudaEventElapsedTime(&t, p.tune_ev[0], p.tune_ev[1]));
-        if (r > 0) ms.push_back(t);
-      }
-      add_launches(srv, 4);
-      std::sort(ms.begin(), ms.end());
-      if (ms[1] < best_ms) {
-        best_ms = ms[1];
-        best_lps = lps;
-        best_pairs = pairs;
-        best_kind = kind;
-      }
+  int best_lps = 0, best_pairs = 0;
+  for (int lps = 1; lps <= 32; lps *= 2) {
+    const int pairs = pairs_for(p.G, lps);
+    if (pairs > moc::kMaxSlots || (double) p.G / (2.0 * lps * pairs) < 0.5)
+      continue;
+    p.lps = lps;
+    moc::SweepArgs a = pool_sweep_args(p);
+    a.phi = p.tune_phi;
+    a.psi[0] = a.psi[1] = p.tune_psi;
+    a.sc = p.tune_sc;
+    a.slots = p.tune_slots;
+    float best = 1e30f;
+    for (int r = 0; r < 3; r++) {
+      SV_CUDA(cudaEventRecord(p.tune_ev[0], p.stream));
+      if (!moc::launch_sweep(a, p.Ph, pairs, MOC_EXP_INTRINSIC, p.stream))
+        return SV_FAIL(MOC_ERR_UNSUPPORTED, "no sweep kernel for the pool");
+      SV_CUDA(cudaEventRecord(p.tune_ev[1], p.stream));
+      SV_CUDA(cudaEventSynchronize(p.tune_ev[1]));
+      float t = 0.f;
+      SV_CUDA(cudaEventElapsedTime(&t, p.tune_ev[0], p.tune_ev[1]));
+      if (r > 0) best = std::min(best, t);
+    }
+    add_launches(srv, 3);
+    if (best < best_ms) {
+      best_ms = best;
+      best_lps = lps;
+      best_pairs = pairs;
     }
   }
   SV_CHECK(best_lps > 0, MOC_ERR_UNSUPPORTED, "no sweep kernel shape fits");
   p.lps = best_lps;
   p.pairs = best_pairs;
-  p.exp_kind = best_kind;
-  p.tuned = true;
-  // the timing sweeps flipped the buffer index and wrote tallies and
-  // boundary fluxes that the starting state below overwrites
+  p.exp_kind = MOC_EXP_INTRINSIC;
+  std::lock_guard<std::mutex> lk(srv->mu);
+  p.n_tunes++;
+  return MOC_OK;
+}
+
+// Sweep shape for the pool's current track count: fixed by the pool's
+// configuration, or the autotuned one of its size class (a power of two of
+// live tracks), tuning that class on first use.
+int choose_shape(moc_server* srv, Pool& p) {
+  if (p.cfg.lanes != 0) return MOC_OK;
+  int cls = 0;
+  for (int64_t t = std::max<int64_t>(p.active_tracks, 1); t > 1; t >>= 1) cls++;
+  auto it = p.shape_by_class.find(cls);
+  int lps, pairs;
+  if (it == p.shape_by_class.end()) {
+    SV_TRY(autotune_pool(srv, p));
+    lps = p.lps;
+    pairs = p.pairs;
+    p.shape_by_class[cls] = std::make_pair(lps, pairs);
+  } else {
+    lps = it->second.first;
+    pairs = it->second.second;
+  }
+  if (lps != p.graph_lps || pairs != p.graph_pairs) {
+    if (p.graph) cudaGraphExecDestroy(p.graph);
+    p.graph = nullptr;
+  }
+  p.lps = lps;
+  p.pairs = pairs;
   return MOC_OK;
 }
 
@@ -971,13 +1022,7 @@ int launch_block(moc_server* srv, Pool& p) {
   if (p.dirty) SV_TRY(rebuild_order(p));
   for (int i = 0; i < (int) p.slots.size(); i++)
     if (p.slots[i].live && p.slots[i].needs_init) SV_TRY(init_slot(srv, p, i));
-  if (!p.tuned) {
-    // every solve here is fresh: time the shapes on them, then write their
-    // starting state again
-    SV_TRY(autotune_pool(srv, p));
-    for (int i = 0; i < (int) p.slots.size(); i++)
-      if (p.slots[i].live) SV_TRY(init_slot(srv, p, i));
-  }
+  SV_TRY(choose_shape(srv, p));
   const int K = std::max(1, srv->cfg.iterations_per_poll);
   if (srv->cfg.use_graphs) {
     if (!p.graph || p.graph_iters != K) {
@@ -995,6 +1040,8 @@ int launch_block(moc_server* srv, Pool& p) {
       cudaGraphDestroy(g);
       SV_CUDA(e);
       p.graph_iters = K;
+      p.graph_lps = p.lps;
+      p.graph_pairs = p.pairs;
       std::lock_guard<std::mutex> lk(srv->mu);
       srv->stats.graph_captures++;
       srv->stats.host_graph_s += now_s() - t_cap;
@@ -1289,6 +1336,7 @@ int moc_server_pool_stats(moc_server* srv, int pool, moc_pool_stats* out) {
   out->admitted = p.n_admitted;
   out->completed = p.n_completed;
   out->blocks = p.n_blocks;
+  out->tunes = p.n_tunes;
   out->gpu_busy_s = p.busy_s;
   return MOC_OK;
 }

@@ -87,7 +87,7 @@ class Stats(C.Structure):
 class PoolStats(C.Structure):
     _fields_ = [(n, C.c_int32) for n in (
         "num_groups", "num_polar_half", "lanes", "pairs", "exp_kind", "live")] + [
-        (n, C.c_int64) for n in ("admitted", "completed", "blocks")] + [
+        (n, C.c_int64) for n in ("admitted", "completed", "blocks", "tunes")] + [
         ("gpu_busy_s", C.c_double)]
 
 
