@@ -412,11 +412,11 @@ def serve_plain(stream, probs, max_iters):
     return out, clock
 
 
-def serve_batched(stream, probs, max_iters, max_solves, k):
+def serve_batched(stream, probs, max_iters, max_solves, k, priorities=True):
     """The server: requests submitted at their arrival times from this
     thread while the request loop runs on its own."""
     from openmoc_gb300.serving import Server, pool_capacity
-    srv = Server(iterations_per_poll=k)
+    srv = Server(iterations_per_poll=k, priorities=priorities)
     by_g = {}
     for p, _ in probs:
         by_g.setdefault(p.num_groups, []).append(p)
@@ -456,7 +456,8 @@ def run_serving(args):
     # warm both paths (kernel loading, autotune caches) on a few requests
     serve_plain(stream[:4], probs[:4], args.serving_iters)
     batched, t_b, stats = serve_batched(stream, probs, args.serving_iters,
-                                        args.serving_slots, args.serving_k)
+                                        args.serving_slots, args.serving_k,
+                                        not args.serving_no_priorities)
     plain, t_p = serve_plain(stream, probs, args.serving_iters)
     diffs = []
     for r, a, b in zip(stream, batched, plain):
@@ -493,6 +494,7 @@ def run_serving(args):
                    "source_keff": SOURCE_KEFF, "max_iters": args.serving_iters,
                    "solves_per_pool": args.serving_slots,
                    "iterations_per_poll": args.serving_k,
+                   "stream_priorities": not args.serving_no_priorities,
                    "problem_prep_s": t_prep},
         "batched": {"solves_per_s": n / t_b, "makespan_s": t_b,
                     "p50_latency_s": float(np.percentile(lat_b, 50)),
@@ -532,8 +534,9 @@ def main():
     ap.add_argument("--serving-requests", type=int, default=512)
     ap.add_argument("--serving-gap-ms", type=float, default=2.0)
     ap.add_argument("--serving-iters", type=int, default=1000)
-    ap.add_argument("--serving-slots", type=int, default=32)
+    ap.add_argument("--serving-slots", type=int, default=64)
     ap.add_argument("--serving-k", type=int, default=8)
+    ap.add_argument("--serving-no-priorities", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

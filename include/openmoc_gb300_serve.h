@@ -54,6 +54,9 @@ typedef struct {
   int32_t device;              /* CUDA device ordinal */
   int32_t iterations_per_poll; /* iterations per pool between host polls */
   int32_t use_graphs;          /* 1: replay each block as a CUDA graph */
+  int32_t priorities;          /* 1: pools of few fluxes per track (short,
+                                  latency-bound kernels) get the high
+                                  stream priority */
 } moc_server_config;
 
 typedef struct {

@@ -503,7 +503,13 @@ int create_pool(moc_server* srv, const moc_pool_config& c, Pool& p) {
     p.pairs = c.pairs;
     p.exp_kind = c.exp_kind;
   }
-  SV_CUDA(cudaStreamCreateWithFlags(&p.stream, cudaStreamNonBlocking));
+  // pools of few fluxes per track run short, latency-bound kernels: with
+  // priorities on they go ahead of the long sweeps of the wide pools
+  int prio_low = 0, prio_high = 0;
+  SV_CUDA(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
+  const bool high = srv->cfg.priorities && p.F <= 48;
+  SV_CUDA(cudaStreamCreateWithPriority(&p.stream, cudaStreamNonBlocking,
+                                       high ? prio_high : prio_low));
   SV_CUDA(cudaEventCreate(&p.block_start));
   SV_CUDA(cudaEventCreate(&p.block_done));
   const int64_t R = c.max_fsrs, T = c.max_tracks, S = c.max_segments;

@@ -36,7 +36,7 @@ _KINDS = {"eigenvalue": SOLVE_EIGENVALUE, "source": SOLVE_SOURCE}
 
 class ServerConfig(C.Structure):
     _fields_ = [("device", C.c_int32), ("iterations_per_poll", C.c_int32),
-                ("use_graphs", C.c_int32)]
+                ("use_graphs", C.c_int32), ("priorities", C.c_int32)]
 
 
 class PoolConfig(C.Structure):
@@ -147,9 +147,10 @@ class Server:
     arrays they reference are kept alive here until they complete."""
 
     def __init__(self, device: int = 0, iterations_per_poll: int = 8,
-                 use_graphs: bool = True):
+                 use_graphs: bool = True, priorities: bool = True):
         L = _lib()
-        cfg = ServerConfig(device, iterations_per_poll, 1 if use_graphs else 0)
+        cfg = ServerConfig(device, iterations_per_poll, 1 if use_graphs else 0,
+                           1 if priorities else 0)
         h = C.c_void_p()
         _native.check(L.moc_server_create(C.byref(cfg), C.byref(h)))
         self._h = h
