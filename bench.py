@@ -412,11 +412,12 @@ def serve_plain(stream, probs, max_iters):
     return out, clock
 
 
-def serve_batched(stream, probs, max_iters, max_solves, k, priorities=True):
+def serve_batched(stream, probs, max_iters, max_solves, k, priorities=True,
+                  hot_bytes=0):
     """The server: requests submitted at their arrival times from this
     thread while the request loop runs on its own."""
     from openmoc_gb300.serving import Server, pool_capacity
-    srv = Server(iterations_per_poll=k, priorities=priorities)
+    srv = Server(iterations_per_poll=k, priorities=priorities, hot_bytes=hot_bytes)
     by_g = {}
     for p, _ in probs:
         by_g.setdefault(p.num_groups, []).append(p)

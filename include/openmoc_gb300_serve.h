@@ -57,6 +57,11 @@ typedef struct {
   int32_t priorities;          /* 1: pools of few fluxes per track (short,
                                   latency-bound kernels) get the high
                                   stream priority */
+  int64_t hot_bytes;           /* cap on the sweep-gathered bytes (sources
+                                  and tallies, 8 B per FSR and group) of all
+                                  live solves, so that they stay in L2;
+                                  0: no cap.  A pool with no live solve
+                                  always admits one. */
 } moc_server_config;
 
 typedef struct {

@@ -408,6 +408,7 @@ struct Pool {
 
 struct moc_server {
   moc_server_config cfg{};
+  int64_t hot_live = 0;              // sweep-gathered bytes of live solves
   std::vector<std::unique_ptr<Pool>> pools;
   std::mutex mu;                     // queues, results, counters
   std::condition_variable cv;
@@ -665,6 +666,10 @@ void publish(moc_server* srv, const Staged& st, const moc_result& r) {
   srv->cv.notify_all();
 }
 
+// Bytes of a solve that the sweep gathers and scatters by FSR id: its
+// reduced sources and tallies.
+int64_t hot_bytes(const Staged& s) { return 8 * s.R * s.ld; }
+
 // Copies a solve's data into the ranges given to it and rebases them.
 int upload_slot(moc_server* srv, Pool& p, int slot_index) {
   Slot& sl = p.slots[slot_index];
@@ -767,9 +772,19 @@ int init_slot(moc_server* srv, Pool& p, int slot_index) {
 int admit(moc_server* srv, Pool& p) {
   {
     std::lock_guard<std::mutex> lk(srv->mu);
+    bool pool_empty = true;
+    for (const Slot& sl : p.slots) pool_empty = pool_empty && !sl.live;
     for (auto it = p.queue.begin(); it != p.queue.end();) {
       Staged& s = **it;
       if (p.free_slots.empty()) break;
+      // sources and tallies are gathered and scattered by FSR id in every
+      // sweep: admit while the live solves' share of them fits the budget
+      const int64_t hot = hot_bytes(s);
+      if (srv->cfg.hot_bytes > 0 && !pool_empty &&
+          srv->hot_live + hot > srv->cfg.hot_bytes) {
+        ++it;
+        continue;
+      }
       const int64_t r0 = p.rows.alloc(s.R);
       const int64_t t0 = (r0 >= 0) ? p.tracks.alloc(s.T + 1) : -1;
       const int64_t s0 = (t0 >= 0) ? p.segments.alloc(s.S) : -1;
@@ -797,6 +812,8 @@ int admit(moc_server* srv, Pool& p) {
       s.t_admit = now_s();
       sl.st = std::move(*it);
       it = p.queue.erase(it);
+      srv->hot_live += hot;
+      pool_empty = false;
       srv->stats.admitted++;
       p.n_admitted++;
       srv->stats.queued--;
@@ -861,6 +878,7 @@ int retire(moc_server* srv, Pool& p) {
     p.segments.release(sl.s0, s.S);
     p.mats.release(sl.m0, s.M);
     p.angles.release(sl.a0, s.A);
+    srv->hot_live -= hot_bytes(s);
     sl.live = false;
     {
       std::lock_guard<std::mutex> lk(srv->mu);
@@ -1077,6 +1095,7 @@ void fail_pool(moc_server* srv, Pool& p, int status) {
   std::vector<std::unique_ptr<Staged>> dead;
   for (Slot& sl : p.slots)
     if (sl.live) {
+      srv->hot_live -= hot_bytes(*sl.st);
       dead.push_back(std::move(sl.st));
       sl.live = false;
     }

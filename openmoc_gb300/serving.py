@@ -36,7 +36,8 @@ _KINDS = {"eigenvalue": SOLVE_EIGENVALUE, "source": SOLVE_SOURCE}
 
 class ServerConfig(C.Structure):
     _fields_ = [("device", C.c_int32), ("iterations_per_poll", C.c_int32),
-                ("use_graphs", C.c_int32), ("priorities", C.c_int32)]
+                ("use_graphs", C.c_int32), ("priorities", C.c_int32),
+                ("hot_bytes", C.c_int64)]
 
 
 class PoolConfig(C.Structure):
@@ -147,10 +148,14 @@ class Server:
     arrays they reference are kept alive here until they complete."""
 
     def __init__(self, device: int = 0, iterations_per_poll: int = 8,
-                 use_graphs: bool = True, priorities: bool = True):
+                 use_graphs: bool = True, priorities: bool = True,
+                 hot_bytes: int = 0):
+        """hot_bytes caps the sources and tallies (8 B per FSR and group)
+        of all live solves, to keep the sweep's gathers in L2 (0: no
+        cap)."""
         L = _lib()
         cfg = ServerConfig(device, iterations_per_poll, 1 if use_graphs else 0,
-                           1 if priorities else 0)
+                           1 if priorities else 0, int(hot_bytes))
         h = C.c_void_p()
         _native.check(L.moc_server_create(C.byref(cfg), C.byref(h)))
         self._h = h
