@@ -283,6 +283,13 @@ def run_gpu(args):
             out["e2e"] = e2e
         if cpu:
             out["cpu_baseline"] = cpu
+        if world == 1 and not args.no_serving:
+            # the second half of the headline: the request stream through the
+            # batched server against the plain per-solve loop
+            sv = run_serving(args)
+            out["serving"] = {k: sv[k] for k in ("metric", "value", "unit", "config",
+                                                 "batched", "plain", "speedup",
+                                                 "agreement")}
         print(json.dumps(out), flush=True)
     s.close()
     if dist:
@@ -458,7 +465,8 @@ def run_serving(args):
     serve_plain(stream[:4], probs[:4], args.serving_iters)
     batched, t_b, stats = serve_batched(stream, probs, args.serving_iters,
                                         args.serving_slots, args.serving_k,
-                                        not args.serving_no_priorities)
+                                        not args.serving_no_priorities,
+                                        args.serving_hot_mb << 20)
     plain, t_p = serve_plain(stream, probs, args.serving_iters)
     diffs = []
     for r, a, b in zip(stream, batched, plain):
@@ -496,6 +504,7 @@ def run_serving(args):
                    "solves_per_pool": args.serving_slots,
                    "iterations_per_poll": args.serving_k,
                    "stream_priorities": not args.serving_no_priorities,
+                   "hot_bytes_budget_mb": args.serving_hot_mb,
                    "problem_prep_s": t_prep},
         "batched": {"solves_per_s": n / t_b, "makespan_s": t_b,
                     "p50_latency_s": float(np.percentile(lat_b, 50)),
@@ -515,7 +524,7 @@ def run_serving(args):
                       "unconverged": int(sum(not x["converged"] for x in batched)),
                       "worst": worst},
     }
-    print(json.dumps(out), flush=True)
+    return out
 
 
 def main():
@@ -538,13 +547,17 @@ def main():
     ap.add_argument("--serving-slots", type=int, default=64)
     ap.add_argument("--serving-k", type=int, default=8)
     ap.add_argument("--serving-no-priorities", action="store_true")
+    ap.add_argument("--serving-hot-mb", type=int, default=32,
+                    help="L2 budget of the live solves' sources and tallies")
+    ap.add_argument("--no-serving", action="store_true",
+                    help="leave the request-stream benchmark out of the default line")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
     elif args.serving:
-        run_serving(args)
+        print(json.dumps(run_serving(args)), flush=True)
     else:
         run_gpu(args)
 
