@@ -197,8 +197,9 @@ def load_packed(base: str) -> Tuple[Problem, Dict[str, float], Dict[str, np.ndar
         solve_3d=int(sc["solve_3d"]),
         **{k: arrays[k] for k in _ARRAY_DTYPES},
     )
-    if "fixed_sources" in arrays:
-        p.fixed_sources = arrays["fixed_sources"]
+    for key in ("fixed_sources", "fixed_source"):
+        if key in arrays:
+            p.fixed_sources = arrays[key]
     p.meta = dict(sc)
     return p.contiguous(), sc, arrays
 

@@ -9,8 +9,10 @@ if ROOT not in sys.path:
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 
-# Cases produced by tests/golden/make_fixtures.cpp from OpenMOC itself.
+# Cases produced by tests/golden/make_fixtures.cpp from OpenMOC itself:
+# eigenvalue solves, and fixed-source solves (computeSource, computeFlux).
 CASES = ["pin_c5g7", "pin_70g", "pin7_synth", "lat3_g2_vac", "lat2_g16"]
+SRC_CASES = ["src3_g7", "flux3_g7"]
 
 
 def pytest_configure(config):

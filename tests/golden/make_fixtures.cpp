@@ -346,6 +346,8 @@ struct CaseSpec {
   RunKind kind;
   double k_source;
   bool probe;
+  Material* src_material;  /* fixed source in every group of this material */
+  double src_value;
 };
 
 static void run_case(const CaseSpec& c, const std::string& outdir) {
@@ -357,6 +359,10 @@ static void run_case(const CaseSpec& c, const std::string& outdir) {
   ProbeSolver solver(&tg);
   solver.setNumThreads(1);
   solver.setConvergenceThreshold(c.tol);
+  const int G0 = c.geo->getNumEnergyGroups();
+  if (c.src_material)
+    for (int g = 1; g <= G0; g++)
+      solver.setFixedSourceByMaterial(c.src_material, g, c.src_value);
   if (c.kind == EIGEN)
     solver.computeEigenvalue(c.max_iters, c.res);
   else if (c.kind == SOURCE)
@@ -386,6 +392,15 @@ static void run_case(const CaseSpec& c, const std::string& outdir) {
     for (int g = 0; g < G; g++)
       flux[(size_t) r * G + g] = (float) solver.getFlux(r, g + 1);
   w.arr("flux", "f4", flux.data(), flux.size());
+  if (c.src_material) {
+    /* the fixed source per FSR and group, as setFixedSourceByMaterial
+     * spreads it (Solver::initializeFixedSources, src/Solver.cpp:1100-1135) */
+    std::vector<float> q((size_t) R * G, 0.0f);
+    for (long r = 0; r < R; r++)
+      if (c.geo->findFSRMaterial(r) == c.src_material)
+        for (int g = 0; g < G; g++) q[(size_t) r * G + g] = (float) c.src_value;
+    w.arr("fixed_source", "f4", q.data(), q.size());
+  }
   if (c.probe && c.kind == EIGEN) {
 #ifdef SINGLE
     solver.probe(w);
@@ -410,14 +425,14 @@ int main(int argc, char** argv) {
     Material* fuel = make_material(1, "UO2", c5g7(true));
     Material* water = make_material(2, "Water", c5g7(false));
     cases.push_back({"pin_c5g7", pincell_input(fuel, water), 4, 0.1, 500,
-                     1e-5, FISSION_SOURCE, EIGEN, 1.0, true});
+                     1e-5, FISSION_SOURCE, EIGEN, 1.0, true, NULL, 0.0});
   }
   /* 2. tests/test_forward_pin_cell_70g: linspace 70-group data */
   {
     Material* fuel = make_material(3, "UO2-70", lin70(true));
     Material* water = make_material(4, "Water-70", lin70(false));
     cases.push_back({"pin_70g", pincell_input(fuel, water), 4, 0.1, 1000,
-                     1e-5, SCALAR_FLUX, EIGEN, 1.0, true});
+                     1e-5, SCALAR_FLUX, EIGEN, 1.0, true, NULL, 0.0});
   }
   /* 3. the 7-group synthetic pin cell: r=0.54 in 1.26 cm, 3 rings x 8
    *    sectors in fuel, 8 moderator sectors, 32 azimuthal, 0.05 cm */
@@ -431,7 +446,7 @@ int main(int argc, char** argv) {
     Universe* u = make_pin(fuel, mod, pin);
     cases.push_back({"pin7_synth", make_box_geometry(u, lat, 0.63, REF, REF,
                      REF, REF), 32, 0.05, 1000, 1e-5, FISSION_SOURCE, EIGEN,
-                     1.0, true});
+                     1.0, true, NULL, 0.0});
   }
   /* 4. 3x3 lattice, 2 groups, vacuum on +x and +y, centre pin water */
   {
@@ -441,7 +456,7 @@ int main(int argc, char** argv) {
         openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 1002, 2, false));
     cases.push_back({"lat3_g2_vac", lattice_geometry(3, fuel, mod, pin, {4},
                      REF, VAC, REF, VAC), 16, 0.1, 1000, 1e-5,
-                     FISSION_SOURCE, EIGEN, 1.0, true});
+                     FISSION_SOURCE, EIGEN, 1.0, true, NULL, 0.0});
   }
   /* 5. 2x2 lattice, 16 groups, reflective */
   {
@@ -451,7 +466,29 @@ int main(int argc, char** argv) {
         openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 1003, 16, false));
     cases.push_back({"lat2_g16", lattice_geometry(2, fuel, mod, pin, {3},
                      REF, REF, REF, REF), 8, 0.1, 1000, 1e-5,
-                     FISSION_SOURCE, EIGEN, 1.0, true});
+                     FISSION_SOURCE, EIGEN, 1.0, true, NULL, 0.0});
+  }
+  /* 6-7. fixed-source problems (tests/test_compute_source and
+   *      test_compute_flux run Solver::computeSource / computeFlux): a 3x3
+   *      lattice, 7 groups, vacuum on +x and +y, unit source in the fuel.
+   *      computeSource with keff 1 (the lattice's own keff is 0.3, so the
+   *      source iteration converges); computeFlux with the fixed source
+   *      alone. */
+  {
+    Material* fuel = make_material(11, "fuel7s",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 4, 7, true));
+    Material* mod = make_material(12, "mod7s",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 1004, 7, false));
+    cases.push_back({"src3_g7", lattice_geometry(3, fuel, mod, pin, {4},
+                     REF, VAC, REF, VAC), 16, 0.1, 1000, 1e-5,
+                     TOTAL_SOURCE, SOURCE, 1.0, false, fuel, 1.0});
+    Material* fuel2 = make_material(13, "fuel7f",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 4, 7, true));
+    Material* mod2 = make_material(14, "mod7f",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 1004, 7, false));
+    cases.push_back({"flux3_g7", lattice_geometry(3, fuel2, mod2, pin, {4},
+                     REF, VAC, REF, VAC), 16, 0.1, 1000, 1e-5,
+                     SCALAR_FLUX, FLUX, 1.0, false, fuel2, 1.0});
   }
 
   for (const CaseSpec& c : cases) {

@@ -10,7 +10,7 @@ OpenMOC's own FP32 and FP64 builds differ by 1.1e-5 on the pin cell at the
 import numpy as np
 import pytest
 
-from conftest import CASES, load_case
+from conftest import CASES, SRC_CASES, load_case
 from openmoc_gb300 import GB300Solver
 from openmoc_gb300.solver import EXP_INTRINSIC, EXP_TABLE, FISSION_SOURCE, SCALAR_FLUX
 from oracle.oracle import Oracle
@@ -151,3 +151,29 @@ def test_autotuner_picks_a_timed_shape_and_keeps_parity():
     s.computeEigenvalue(int(sc["max_iters"]), int(sc["res_type"]))
     assert abs(s.getKeff() - sc["keff"]) <= KEFF_TOL
     assert max_rel(s.getFluxes(), arr["flux"]) <= FLUX_TOL
+
+
+@pytest.mark.parametrize("exp_kind", [EXP_TABLE, EXP_INTRINSIC])
+@pytest.mark.parametrize("case", SRC_CASES)
+def test_fixed_source_matches_openmoc(case, exp_kind):
+    """computeSource (fixed keff) and computeFlux (fixed source alone) with
+    OpenMOC's own fixed sources, against its FP32 and FP64 solves."""
+    p, sc, arr = load_case(case)
+    _, sc64, arr64 = load_case(case, "f64")
+    assert p.fixed_sources is not None
+    s = GB300Solver(p)
+    s.setConvergenceThreshold(sc["tolerance"])
+    if exp_kind == EXP_INTRINSIC:
+        s.useExponentialIntrinsic()
+    else:
+        s.useExponentialInterpolation()
+    if int(sc["run_kind"]) == 1:
+        s.computeSource(int(sc["max_iters"]), sc["k_source"], int(sc["res_type"]))
+    else:
+        s.computeFlux(int(sc["max_iters"]), True)
+    flux = s.getFluxes()
+    assert abs(s.getNumIterations() - int(sc["iterations"])) <= 1
+    assert s.getKeff() == pytest.approx(sc["keff"])
+    assert max_rel(flux, arr["flux"]) <= FLUX_TOL
+    assert max_rel(flux, arr64["flux"]) <= FLUX_TOL
+    s.close()

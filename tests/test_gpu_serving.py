@@ -242,3 +242,26 @@ def test_bad_request_is_refused_on_submit():
         srv.submit(big)
     assert srv.stats()["submitted"] == 0
     srv.close()
+
+
+def test_fixed_source_fixture_through_a_pool():
+    """OpenMOC's computeSource fixture, solved in a pool beside eigenvalue
+    solves, against OpenMOC's FP32 and FP64 results."""
+    p, sc, arr = load_case("src3_g7")
+    _, _, arr64 = load_case("src3_g7", "f64")
+    others = mix(4)
+    srv = make_server([p] + others, 8, fixed_shape=False)
+    ts = [srv.submit(q) for q in others[:2]]
+    t = srv.submit(p, "source", int(sc["max_iters"]), int(sc["res_type"]),
+                   k_eff=sc["k_source"], threshold=sc["tolerance"])
+    ts += [srv.submit(q) for q in others[2:]]
+    srv.run_until_idle()
+    r = srv.wait(t, timeout=0)
+    for x in ts:
+        assert srv.wait(x, timeout=0)["converged"]
+    srv.close()
+    assert r["converged"]
+    assert abs(r["iterations"] - int(sc["iterations"])) <= 1
+    assert r["keff"] == pytest.approx(sc["k_source"])
+    assert max_rel(r["flux"], arr["flux"]) <= FLUX_TOL
+    assert max_rel(r["flux"], arr64["flux"]) <= FLUX_TOL

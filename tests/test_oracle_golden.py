@@ -16,7 +16,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import CASES, GOLDEN, load_case
+from conftest import CASES, GOLDEN, SRC_CASES, load_case
 from oracle.oracle import Oracle
 
 
@@ -25,7 +25,10 @@ def _solve(oracle, sc):
     if kind == 0:
         return oracle.compute_eigenvalue(int(sc["max_iters"]), int(sc["res_type"]),
                                          sc["tolerance"])
-    raise AssertionError("only eigenvalue fixtures are generated")
+    if kind == 1:
+        return oracle.compute_source(int(sc["max_iters"]), sc["k_source"],
+                                     int(sc["res_type"]), sc["tolerance"])
+    return oracle.compute_flux(int(sc["max_iters"]), sc["tolerance"])
 
 
 def test_reference_goldens_reproduced_by_reference_fixtures():
@@ -52,7 +55,7 @@ def test_oracle_matches_reference_goldens(precision):
         np.testing.assert_allclose(o.phi, d["fluxes"], rtol=2e-5)
 
 
-@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("case", CASES + SRC_CASES)
 @pytest.mark.parametrize("precision", ["f32", "f64"])
 def test_oracle_solve_matches_openmoc(case, precision):
     p, sc, arr = load_case(case, precision)
@@ -96,7 +99,7 @@ def test_oracle_hooks_match_openmoc(case):
 def test_fixture_fsr_ids_identical_across_precisions():
     """FSR numbering, tracks and links are integer data: the FP32 and FP64
     OpenMOC builds must produce them bit-identically."""
-    for case in CASES:
+    for case in CASES + SRC_CASES:
         a, _, _ = load_case(case, "f32")
         b, _, _ = load_case(case, "f64")
         for name in ("seg_fsr", "seg_off", "next", "flags", "track_ang", "fsr_mat"):
