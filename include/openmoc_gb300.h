@@ -58,6 +58,13 @@ extern "C" {
 #define MOC_EXP_TABLE 0     /* shared-memory interpolation table (default) */
 #define MOC_EXP_INTRINSIC 1 /* hardware ex2 with a series below x = 1/16 */
 
+/* Kernels of computeFSRSources (src/CPUSolver.cpp:1939-2025) */
+#define MOC_SOURCES_AUTO 0   /* tensor cores (3xTF32) at >= 70 groups */
+#define MOC_SOURCES_FP32 1   /* FP32 CUDA cores, one warp per FSR */
+#define MOC_SOURCES_TF32X3 2 /* per-material batched contraction on the
+                                tensor cores, TF32 high/low split products
+                                (64 to 96 groups) */
+
 typedef struct moc_ctx moc_ctx;
 
 typedef struct {
@@ -155,6 +162,13 @@ int moc_get_sweep_shape(moc_ctx* ctx, int* lps, int* slots);
 /** Iterations enqueued between two checks of the device convergence flag
  *  (default 4). */
 int moc_set_iterations_per_sync(moc_ctx* ctx, int k);
+
+/** Chooses the kernel of computeFSRSources (MOC_SOURCES_*); the group-count
+ *  preconditions of MOC_SOURCES_TF32X3 are checked here.  No counterpart in
+ *  the reference, which has one source kernel per back end. */
+int moc_set_source_kernel(moc_ctx* ctx, int kind);
+/** The kernel that computeFSRSources runs (MOC_SOURCES_FP32 or _TF32X3). */
+int moc_get_source_kernel(moc_ctx* ctx, int* kind);
 
 /* ---- whole solves, device-resident (Solver::computeEigenvalue,
  *      computeSource, computeFlux; src/Solver.cpp:1352-1700) ------------- */

@@ -60,6 +60,8 @@ _SIGS = {
     "moc_set_sweep_shape": ([_P, C.c_int, C.c_int], C.c_int),
     "moc_get_sweep_shape": ([_P, C.POINTER(C.c_int), C.POINTER(C.c_int)], C.c_int),
     "moc_set_iterations_per_sync": ([_P, C.c_int], C.c_int),
+    "moc_set_source_kernel": ([_P, C.c_int], C.c_int),
+    "moc_get_source_kernel": ([_P, C.POINTER(C.c_int)], C.c_int),
     "moc_compute_eigenvalue": ([_P, C.c_int, C.c_int], C.c_int),
     "moc_compute_source": ([_P, C.c_int, C.c_double, C.c_int], C.c_int),
     "moc_compute_flux": ([_P, C.c_int, C.c_int], C.c_int),

@@ -142,6 +142,13 @@ struct moc_ctx {
   int64_t num_sweeps = 0;
   int iters_per_sync = 4;
   std::vector<cudaEvent_t> ev;   // event pairs around sweeps
+  // 3xTF32 tensor-core sources: FSR ids by material in tiles, the material
+  // of each tile, the split scattering operands
+  int source_kind = MOC_SOURCES_AUTO;
+  int32_t* tc_rows = nullptr;
+  int32_t* tc_tile_mat = nullptr;
+  float* tc_b = nullptr;
+  int tc_tiles = 0;
 };
 
 namespace {
@@ -198,8 +205,23 @@ moc::SweepArgs sweep_args(moc_ctx* c, int check_done) {
   return a;
 }
 
+// Whether computeFSRSources runs on the tensor cores.
+bool use_tc_sources(const moc_ctx* c) {
+  if (!c->tc_b || !c->tc_rows || c->tc_tiles == 0) return false;
+  if (c->source_kind == MOC_SOURCES_TF32X3) return true;
+  return c->source_kind == MOC_SOURCES_AUTO && c->d.num_groups >= 70;
+}
+
 moc::SolverArgs solver_args(moc_ctx* c, int check_done) {
   moc::SolverArgs a{};
+  if (use_tc_sources(c)) {
+    a.tc_rows = c->tc_rows;
+    a.tc_tile_mat = c->tc_tile_mat;
+    a.tc_b = c->tc_b;
+    a.tc_tiles = c->tc_tiles;
+    a.tc_n = moc::tc_pad_n(c->d.num_groups);
+    a.tc_k = moc::tc_pad_k(c->d.num_groups);
+  }
   a.sigma_t = c->sigma_t;
   a.sigma_s = c->sigma_s;
   a.sigma_s_T = c->sigma_s_T;
@@ -462,6 +484,8 @@ int run_iterations(moc_ctx* c, int kind, int res_type) {
       MOC_CUDA(cudaGetLastError());
     }
     MOC_TRY(pull(c));
+    MOC_CHECK(!c->hsc->tc_error, MOC_ERR_TIMEOUT,
+              "a tensor-core source launch gave up waiting for its copies");
     // sweeps that returned at once after convergence still record events;
     // count only the iterations the device performed
     const int done_now = c->hsc->iteration - completed;
@@ -618,6 +642,9 @@ int moc_destroy(moc_ctx* c) {
   dfree(c->exp_table);
   dfree(c->rates);
   dfree(c->flush);
+  dfree(c->tc_rows);
+  dfree(c->tc_tile_mat);
+  dfree(c->tc_b);
   dfree(c->sc);
   if (c->hsc) cudaFreeHost(c->hsc);
   for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
@@ -782,6 +809,13 @@ int moc_upload_materials(moc_ctx* c, const float* sigma_t,
   MOC_CUDA(cudaMemcpy(c->scat_out, scat_out.data(), 4 * MG,
                       cudaMemcpyHostToDevice));
   MOC_CUDA(cudaMemcpy(c->fissile, fis.data(), M, cudaMemcpyHostToDevice));
+  dfree(c->tc_b);
+  if (moc::tc_sources_supported(G)) {
+    std::vector<float> b;
+    moc::tc_pack_scattering(sigma_s, M, G, b);
+    MOC_TRY(dalloc(&c->tc_b, b.size()));
+    MOC_CUDA(cudaMemcpy(c->tc_b, b.data(), 4 * b.size(), cudaMemcpyHostToDevice));
+  }
   c->h_fissile = fis;
   c->h_chi.assign(chi, chi + MG);
   c->have_mats = true;
@@ -816,6 +850,31 @@ int moc_upload_fsrs(moc_ctx* c, const int32_t* fsr_mat, const float* fsr_vol) {
   MOC_CUDA(cudaMemcpy(c->fsr_mat, fsr_mat, 4 * R, cudaMemcpyHostToDevice));
   MOC_CUDA(cudaMemcpy(c->fsr_vol, fsr_vol, 4 * R, cudaMemcpyHostToDevice));
   count_fissionable(c, fsr_mat);
+  // tensor-core source tiles: FSR ids grouped by material, each material's
+  // list padded to whole tiles with -1
+  dfree(c->tc_rows);
+  dfree(c->tc_tile_mat);
+  c->tc_tiles = 0;
+  if (moc::tc_sources_supported(c->d.num_groups)) {
+    std::vector<std::vector<int32_t>> by_mat(c->d.num_materials);
+    for (int64_t r = 0; r < R; r++) by_mat[fsr_mat[r]].push_back((int32_t) r);
+    std::vector<int32_t> rows, tile_mat;
+    for (int m = 0; m < c->d.num_materials; m++) {
+      const int64_t n = (int64_t) by_mat[m].size();
+      for (int64_t t0 = 0; t0 < n; t0 += moc::kTcRows) {
+        tile_mat.push_back(m);
+        for (int64_t i = 0; i < moc::kTcRows; i++)
+          rows.push_back(t0 + i < n ? by_mat[m][t0 + i] : -1);
+      }
+    }
+    c->tc_tiles = (int) tile_mat.size();
+    MOC_TRY(dalloc(&c->tc_rows, rows.size()));
+    MOC_TRY(dalloc(&c->tc_tile_mat, tile_mat.size()));
+    MOC_CUDA(cudaMemcpy(c->tc_rows, rows.data(), 4 * rows.size(),
+                        cudaMemcpyHostToDevice));
+    MOC_CUDA(cudaMemcpy(c->tc_tile_mat, tile_mat.data(), 4 * tile_mat.size(),
+                        cudaMemcpyHostToDevice));
+  }
   // the FISSION_SOURCE residual norm is read on the device by every
   // residual launch, hooks included
   MOC_TRY(pull(c));
@@ -933,6 +992,25 @@ int moc_get_sweep_shape(moc_ctx* c, int* lps, int* slots) {
   if (c->lps == 0) pick_shape(c->d.num_groups, &c->lps, &c->slots);
   *lps = c->lps;
   *slots = c->slots;
+  return MOC_OK;
+}
+
+int moc_set_source_kernel(moc_ctx* c, int kind) {
+  MOC_CHECK(c, MOC_ERR_ARG, "null context");
+  MOC_CHECK(kind == MOC_SOURCES_AUTO || kind == MOC_SOURCES_FP32 ||
+                kind == MOC_SOURCES_TF32X3,
+            MOC_ERR_ARG, "unknown source kernel");
+  MOC_CHECK(kind != MOC_SOURCES_TF32X3 ||
+                moc::tc_sources_supported(c->d.num_groups),
+            MOC_ERR_UNSUPPORTED,
+            "the tensor-core source kernel takes 64 to 96 groups");
+  c->source_kind = kind;
+  return MOC_OK;
+}
+
+int moc_get_source_kernel(moc_ctx* c, int* kind) {
+  MOC_CHECK(c && kind, MOC_ERR_ARG, "null argument");
+  *kind = use_tc_sources(c) ? MOC_SOURCES_TF32X3 : MOC_SOURCES_FP32;
   return MOC_OK;
 }
 

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 namespace moc {
 
 // Exponential table for the attenuation factor g(x) = 1 - exp(-x): nodes at
@@ -50,6 +52,7 @@ struct DevScalars {
   // pool's arrays; unused by single-problem contexts
   long long row0;
   long long nrows;
+  int tc_error;           // a tensor-core source launch gave up waiting
 };
 
 enum SolveMode { kModeEigen = 0, kModeSource = 1, kModeFlux = 2, kModeHook = 3 };
@@ -115,7 +118,19 @@ struct SolverArgs {
   DevScalars* slots;         // [num_slots]
   double* row_val;           // [R]
   int num_slots;
+  // 3xTF32 tensor-core source contraction (null / 0: CUDA-core kernel):
+  // FSR ids grouped by material in tiles of kTcRows (-1 pads a tile), the
+  // material of each tile, and per material the scattering matrix split
+  // into TF32 high and low parts in the MMA's operand layout.
+  const int32_t* tc_rows;    // [tc_tiles * kTcRows]
+  const int32_t* tc_tile_mat;// [tc_tiles]
+  const float* tc_b;         // [M][2][tc_n][tc_k]
+  int tc_tiles;
+  int tc_n, tc_k;            // padded destination / origin group counts
 };
+
+// Rows (FSRs) per tile of the tensor-core source kernel: the MMA's M.
+constexpr int kTcRows = 128;
 
 // Records the text returned by moc_last_error on this thread; returns code.
 int set_error(int code, const char* msg);
@@ -155,6 +170,18 @@ void launch_fill_chi(float* phi, const float* chi, int64_t R, int G, int ld,
                      cudaStream_t s);
 void launch_fsr_rates(const SolverArgs& a, double* out, int nu,
                       cudaStream_t s);
+
+// ---- tensor-core sources (sources_tc.cu) -----------------------------------
+// Group counts the 3xTF32 kernel takes, and its operand sizes.
+bool tc_sources_supported(int num_groups);
+int tc_pad_n(int num_groups);   // destination groups padded for the MMA's N
+int tc_pad_k(int num_groups);   // origin groups padded to the MMA's K step
+// Splits every material's [dest][orig] scattering matrix into TF32 high and
+// low parts laid out as the MMA's B operand (host side): out[M][2][n][k].
+void tc_pack_scattering(const float* sigma_s, int M, int G,
+                        std::vector<float>& out);
+void launch_sources_tc(const SolverArgs& a, int iteration, int zero_phi,
+                       cudaStream_t s);
 
 // ---- batched pools (solver_kernels.cu) -------------------------------------
 // The loop body of every live solve of a pool; a.num_fsrs is the end of the

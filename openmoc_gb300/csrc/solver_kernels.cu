@@ -742,6 +742,10 @@ void launch_sources_s(const SolverArgs& a, int iteration, int fused,
 
 void launch_compute_sources(const SolverArgs& a, int iteration, int fused,
                             cudaStream_t s) {
+  if (a.tc_tiles > 0 && !a.row_slot) {
+    launch_sources_tc(a, iteration, fused, s);
+    return;
+  }
   switch ((a.num_groups + 31) / 32) {
     case 1: launch_sources_s<1>(a, iteration, fused, s); break;
     case 2: launch_sources_s<2>(a, iteration, fused, s); break;

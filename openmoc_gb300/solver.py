@@ -57,6 +57,7 @@ class GB300Solver:
         self._total_time = 0.0
         self._keff = 1.0
         self._shape = None
+        self._source_kind = "auto"
         if track_generator is not None:
             self.setTrackGenerator(track_generator)
 
@@ -114,6 +115,8 @@ class GB300Solver:
             self._call("moc_set_exponential", self._exp_kind)
         if self._shape is not None:
             self._call("moc_set_sweep_shape", *self._shape)
+        if self._source_kind != "auto":
+            self._call("moc_set_source_kernel", self._SOURCE_KINDS[self._source_kind])
         self._fixed = {}
         self._fixed_by_material = {}
         if p.fixed_sources is not None:
@@ -192,6 +195,26 @@ class GB300Solver:
                    C.byref(n))
         return [(int(a[i]), int(b[i]), int(e[i]), float(ms[i]))
                 for i in range(min(n.value, cap))]
+
+    _SOURCE_KINDS = {"auto": 0, "fp32": 1, "tf32x3": 2}
+
+    def setSourceContraction(self, kind: str) -> None:
+        """Kernel of computeFSRSources: "fp32" (CUDA cores), "tf32x3" (the
+        per-material contraction on the tensor cores with TF32 high/low split
+        products, 64 to 96 groups) or "auto" (tf32x3 at >= 70 groups).  No
+        counterpart in OpenMOC."""
+        if kind not in self._SOURCE_KINDS:
+            raise _native.MOCError(-1, f"unknown source contraction {kind!r}")
+        self._source_kind = kind
+        if self._ctx is not None:
+            self._call("moc_set_source_kernel", self._SOURCE_KINDS[kind])
+
+    def getSourceContraction(self) -> str:
+        """The source kernel in use: "fp32" or "tf32x3"."""
+        self._need_ctx()
+        k = C.c_int()
+        self._call("moc_get_source_kernel", C.byref(k))
+        return {1: "fp32", 2: "tf32x3"}[k.value]
 
     def setIterationsPerSync(self, k: int) -> None:
         self._need_ctx()

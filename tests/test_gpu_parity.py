@@ -177,3 +177,42 @@ def test_fixed_source_matches_openmoc(case, exp_kind):
     assert max_rel(flux, arr["flux"]) <= FLUX_TOL
     assert max_rel(flux, arr64["flux"]) <= FLUX_TOL
     s.close()
+
+
+@pytest.mark.parametrize("case", ["pin_70g"])
+def test_tensor_core_sources_match_openmoc_and_fp32(case):
+    """computeFSRSources from OpenMOC's converged state: the 3xTF32
+    tensor-core contraction and the FP32 CUDA-core kernel against OpenMOC's
+    own reduced sources, and against each other."""
+    p, sc, arr = load_case(case, "f32")
+    got = {}
+    for kind in ("fp32", "tf32x3"):
+        s = GB300Solver(p)
+        s.setSourceContraction(kind)
+        assert s.getSourceContraction() == kind
+        s.setFluxes(arr["probe_phi_in"])
+        s.setKeff(sc["probe_keff_in"])
+        s.computeFSRSources(100)
+        got[kind] = s.getReducedSources().ravel()
+        s.close()
+    ref = arr["probe_reduced_sources"]
+    for kind, q in got.items():
+        np.testing.assert_allclose(q, ref, rtol=2e-6, atol=1e-30, err_msg=kind)
+    assert max_rel(got["tf32x3"], got["fp32"]) <= 1e-6
+
+
+def test_tensor_core_sources_eigenvalue_parity():
+    """A 70-group eigenvalue solve with the tensor-core sources against
+    OpenMOC's FP32 and FP64 results (auto selects them at 70 groups)."""
+    p, sc, arr = load_case("pin_70g")
+    _, sc64, arr64 = load_case("pin_70g", "f64")
+    s = GB300Solver(p)
+    assert s.getSourceContraction() == "tf32x3"
+    s.setConvergenceThreshold(sc["tolerance"])
+    s.computeEigenvalue(int(sc["max_iters"]), int(sc["res_type"]))
+    assert abs(s.getNumIterations() - int(sc["iterations"])) <= 2
+    assert abs(s.getKeff() - sc["keff"]) <= KEFF_TOL
+    assert max_rel(s.getFluxes(), arr["flux"]) <= FLUX_TOL
+    assert abs(s.getKeff() - sc64["keff"]) <= 1.5 * KEFF_TOL
+    assert max_rel(s.getFluxes(), arr64["flux"]) <= FLUX_TOL
+    s.close()
