@@ -213,6 +213,15 @@ def run_gpu(args):
         torch.cuda.synchronize()
         t_wall = time.perf_counter() - t_wall
     gpu_launches = s.getLaunchCount() - launches_before
+    # the source contraction both ways: 3xTF32 tensor cores (the default at
+    # 70 groups) against the FP32 CUDA-core kernel, same iterations
+    sources = {"kernel": s.getSourceContraction()}
+    for kind in ("fp32", "tf32x3"):
+        s.setSourceContraction(kind)
+        st, sw = s.benchIterations(max(args.steps // 2, 5), FISSION_SOURCE, True)
+        sources[f"{kind}_ms_per_step"] = float(np.mean(st))
+        sources[f"{kind}_non_sweep_ms"] = float(np.mean(np.asarray(st) - np.asarray(sw)))
+    s.setSourceContraction("auto")
     clocks = clk.summary()
     total_ms = float(np.sum(step_ms))
     if dist:
@@ -267,6 +276,7 @@ def run_gpu(args):
                                        for a, b, e, t in tuning},
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
             "sweep_ms_per_step": sweep_avg,
+            "sources": sources,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
                          "peak_source": f"{peak_kind} hbm_gbs",
