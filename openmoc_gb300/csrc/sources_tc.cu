@@ -178,29 +178,59 @@ sources_tc_kernel(const SolverArgs a, int iteration, int zero_phi) {
             : "memory");
   }
 
-  // operand A: the tile's flux rows, TF32 high and low parts
+  // operand A: the tile's flux rows, TF32 high and low parts.  A warp takes
+  // rows warp, warp + 4, ...; kRowBatch rows at a time with every load of
+  // the batch issued before the first is used (K <= 96: three per lane).
   const float* nf = a.nu_sigma_f + (size_t) m * G;
-  for (int i = warp; i < kTcRows; i += kTcThreads / 32) {
-    const int r = a.tc_rows[(size_t) tile * kTcRows + i];
-    float* phi = (r >= 0) ? a.phi + (size_t) r * a.ld : nullptr;
-    float fr = 0.0f;
-    for (int k = lane; k < K; k += 32) {
-      const float v = (phi && k < G) ? phi[k] : 0.0f;
-      if (k < G) fr = fmaf(nf[k], v, fr);
-      const float hi = tf32_round(v);
-      const float lo = tf32_round(v - hi);
-      const int off = core_offset(i, k, kc);
-      *reinterpret_cast<float*>(sa_hi + off) = hi;
-      *reinterpret_cast<float*>(sa_lo + off) = lo;
-    }
-    // fused: the sweep that follows starts from zero tallies
-    if (phi && zero_phi)
-      for (int k = lane; k < G; k += 32) phi[k] = 0.0f;
+  float nfl[3];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) fr += __shfl_xor_sync(0xffffffffu, fr, o);
-    if (lane == 0) {
-      s_fr[i] = fr;
-      s_row[i] = r;
+  for (int j = 0; j < 3; j++) {
+    const int k = lane + 32 * j;
+    nfl[j] = (k < G) ? nf[k] : 0.0f;
+  }
+  constexpr int kRowBatch = 8;
+  for (int i0 = warp; i0 < kTcRows; i0 += 4 * kRowBatch) {
+    float v[kRowBatch][3];
+    int rows[kRowBatch];
+#pragma unroll
+    for (int u = 0; u < kRowBatch; u++) {
+      const int i = i0 + 4 * u;
+      rows[u] = a.tc_rows[(size_t) tile * kTcRows + i];
+      const float* phi = a.phi + (size_t) (rows[u] >= 0 ? rows[u] : 0) * a.ld;
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        const int k = lane + 32 * j;
+        v[u][j] = (rows[u] >= 0 && k < G) ? phi[k] : 0.0f;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kRowBatch; u++) {
+      const int i = i0 + 4 * u;
+      float fr = 0.0f;
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        const int k = lane + 32 * j;
+        if (k >= K) continue;
+        fr = fmaf(nfl[j], v[u][j], fr);
+        const float hi = tf32_round(v[u][j]);
+        const float lo = tf32_round(v[u][j] - hi);
+        const int off = core_offset(i, k, kc);
+        *reinterpret_cast<float*>(sa_hi + off) = hi;
+        *reinterpret_cast<float*>(sa_lo + off) = lo;
+      }
+      // fused: the sweep that follows starts from zero tallies
+      if (rows[u] >= 0 && zero_phi) {
+        float* phi = a.phi + (size_t) rows[u] * a.ld;
+#pragma unroll
+        for (int j = 0; j < 3; j++)
+          if (lane + 32 * j < G) phi[lane + 32 * j] = 0.0f;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) fr += __shfl_xor_sync(0xffffffffu, fr, o);
+      if (lane == 0) {
+        s_fr[i] = fr;
+        s_row[i] = rows[u];
+      }
     }
   }
   // the generic-proxy stores above become visible to the tensor core
@@ -251,41 +281,56 @@ sources_tc_kernel(const SolverArgs a, int iteration, int zero_phi) {
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
-  // epilogue: thread t owns tile row t (accumulator lane t)
+  // epilogue, in two passes: thread t copies accumulator lane t (tile row
+  // t) into shared memory over the A operands, which the finished products
+  // no longer need (row stride N + 1 keeps the writes conflict-free); then
+  // each warp finishes whole rows with lanes over groups, so the source rows
+  // leave as coalesced stores.
+  float* s_acc = reinterpret_cast<float*>(smem);
   if (s_ok) {
     const uint32_t lane_base = tmem + ((uint32_t) (warp * 32) << 16);
-    const int t = threadIdx.x;
-    const int r = s_row[t];
-    const float inv_k = (float) (1.0 / sc->keff);
-    if (iteration < 0) iteration = sc->iteration;
-    const float fk = s_fr[t] * inv_k;
-    const float* chi = a.chi + (size_t) m * G;
-    const float* st = a.sigma_t + (size_t) m * G;
-    const float* fixed =
-        (a.fixed && r >= 0) ? a.fixed + (size_t) r * a.ld : nullptr;
-    float* qt = (r >= 0) ? a.qt + (size_t) r * a.ld : nullptr;
-    unsigned negatives = 0;
-    // 16 accumulator columns at a time (the loads are warp-collective, so
-    // every lane takes part, padding rows included)
 #pragma unroll
     for (int c = 0; c < N / 16; c++) {
       float acc[16];
-      __syncwarp();
+      __syncwarp();   // the loads are warp-collective
       tmem_load16(lane_base + c * 16, acc);
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-      for (int j = 0; j < 16; j++) {
-        const int d = 16 * c + j;
-        if (qt == nullptr || d >= G) continue;
-        float q = chi[d] * fk;
-        q += acc[j];
+      for (int j = 0; j < 16; j++)
+        s_acc[threadIdx.x * (N + 1) + 16 * c + j] = acc[j];
+    }
+  }
+  __syncthreads();
+  if (s_ok) {
+    const float inv_k = (float) (1.0 / sc->keff);
+    if (iteration < 0) iteration = sc->iteration;
+    float chil[3], stl[3];
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      const int d = lane + 32 * j;
+      chil[j] = (d < G) ? a.chi[(size_t) m * G + d] : 0.0f;
+      stl[j] = (d < G) ? a.sigma_t[(size_t) m * G + d] : 1.0f;
+    }
+    unsigned negatives = 0;
+    for (int i = warp; i < kTcRows; i += kTcThreads / 32) {
+      const int r = s_row[i];
+      if (r < 0) continue;
+      const float fk = s_fr[i] * inv_k;
+      const float* fixed = a.fixed ? a.fixed + (size_t) r * a.ld : nullptr;
+      float* qt = a.qt + (size_t) r * a.ld;
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        const int d = lane + 32 * j;
+        if (d >= G) continue;
+        float q = chil[j] * fk;
+        q += s_acc[i * (N + 1) + d];
         if (fixed) q += fixed[d];
         q *= (float) kTcOneOverFourPi;
         if (q < 0.0f) {
           negatives++;
           if (iteration < 30) q = kTcFluxEpsilon;
         }
-        qt[d] = q / st[d];
+        qt[d] = q / stl[j];
       }
     }
     if (negatives) atomicAdd(&sc->neg_sources, (unsigned long long) negatives);
