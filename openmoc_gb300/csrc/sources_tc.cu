@@ -38,6 +38,7 @@ namespace moc {
 namespace {
 
 constexpr int kTcThreads = 128;
+static_assert(kTcThreads == kTcRows, "one thread per tile row");
 constexpr int kTcColumns = 128;         // tensor-memory columns allocated
 constexpr float kTcFluxEpsilon = 1.0e-25f;
 constexpr double kTcOneOverFourPi = 0.07957747154594767;
@@ -145,6 +146,8 @@ sources_tc_kernel(const SolverArgs a, int iteration, int zero_phi) {
   const int m = a.tc_tile_mat[tile];
   const uint32_t bar_b = smem_addr(&bars[0]), bar_mma = smem_addr(&bars[1]);
 
+  // the tile's FSR ids, one per thread (kTcThreads == kTcRows)
+  s_row[threadIdx.x] = a.tc_rows[(size_t) tile * kTcRows + threadIdx.x];
   if (threadIdx.x == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_b));
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_mma));
@@ -180,7 +183,8 @@ sources_tc_kernel(const SolverArgs a, int iteration, int zero_phi) {
 
   // operand A: the tile's flux rows, TF32 high and low parts.  A warp takes
   // rows warp, warp + 4, ...; kRowBatch rows at a time with every load of
-  // the batch issued before the first is used (K <= 96: three per lane).
+  // the batch issued before the first is used (K <= 96: three per lane);
+  // the row ids were read into shared memory before the barrier above.
   const float* nf = a.nu_sigma_f + (size_t) m * G;
   float nfl[3];
 #pragma unroll
@@ -188,14 +192,14 @@ sources_tc_kernel(const SolverArgs a, int iteration, int zero_phi) {
     const int k = lane + 32 * j;
     nfl[j] = (k < G) ? nf[k] : 0.0f;
   }
-  constexpr int kRowBatch = 8;
+  constexpr int kRowBatch = 16;
   for (int i0 = warp; i0 < kTcRows; i0 += 4 * kRowBatch) {
     float v[kRowBatch][3];
     int rows[kRowBatch];
 #pragma unroll
     for (int u = 0; u < kRowBatch; u++) {
       const int i = i0 + 4 * u;
-      rows[u] = a.tc_rows[(size_t) tile * kTcRows + i];
+      rows[u] = s_row[i];
       const float* phi = a.phi + (size_t) (rows[u] >= 0 ? rows[u] : 0) * a.ld;
 #pragma unroll
       for (int j = 0; j < 3; j++) {
@@ -227,10 +231,7 @@ sources_tc_kernel(const SolverArgs a, int iteration, int zero_phi) {
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) fr += __shfl_xor_sync(0xffffffffu, fr, o);
-      if (lane == 0) {
-        s_fr[i] = fr;
-        s_row[i] = rows[u];
-      }
+      if (lane == 0) s_fr[i] = fr;
     }
   }
   // the generic-proxy stores above become visible to the tensor core
