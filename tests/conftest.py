@@ -13,6 +13,8 @@ GOLDEN = os.path.join(ROOT, "tests", "golden")
 # eigenvalue solves, and fixed-source solves (computeSource, computeFlux).
 CASES = ["pin_c5g7", "pin_70g", "pin7_synth", "lat3_g2_vac", "lat2_g16"]
 SRC_CASES = ["src3_g7", "flux3_g7"]
+# Explicit 3D tracks (TrackGenerator3D with EXPLICIT_3D segments).
+CASES_3D = ["pin3d_g7"]
 
 
 def pytest_configure(config):

@@ -27,6 +27,7 @@
 #include "CPUSolver.h"
 #include "Geometry.h"
 #include "TrackGenerator.h"
+#include "TrackGenerator3D.h"
 #include "log.h"
 
 #include "../../openmoc_gb300/adapter/pack_reference.h"
@@ -348,11 +349,24 @@ struct CaseSpec {
   bool probe;
   Material* src_material;  /* fixed source in every group of this material */
   double src_value;
+  int num_polar;           /* 3D cases: polar angles and axial spacing; */
+  double z_spacing;        /* 0 for 2D cases (omitted initialisers) */
 };
 
 static void run_case(const CaseSpec& c, const std::string& outdir) {
   c.geo->initializeFlatSourceRegions();
-  TrackGenerator tg(c.geo, c.num_azim, c.spacing);
+  TrackGenerator* tgp;
+  if (c.z_spacing > 0) {
+    /* explicit 3D segments (TrackGenerator3D, src/TrackGenerator3D.h) */
+    TrackGenerator3D* t3 = new TrackGenerator3D(c.geo, c.num_azim,
+                                                c.num_polar, c.spacing,
+                                                c.z_spacing);
+    t3->setSegmentFormation(EXPLICIT_3D);
+    tgp = t3;
+  } else {
+    tgp = new TrackGenerator(c.geo, c.num_azim, c.spacing);
+  }
+  TrackGenerator& tg = *tgp;
   tg.setNumThreads(1);
   tg.generateTracks();
 
@@ -410,6 +424,60 @@ static void run_case(const CaseSpec& c, const std::string& outdir) {
   printf("%s [%s]: R=%ld T=%ld S=%ld iters=%d keff=%.8f\n", c.name, PREC,
          p.num_fsrs, p.num_tracks, p.num_segments, solver.getNumIterations(),
          solver.getKeff());
+}
+
+/* An axially extruded pin cell: fuel pin and moderator for z < zf,
+ * homogeneous moderator above up to zt; reflective radially, vacuum at the
+ * bottom and top (the construction of the 3D benchmark, on one pin). */
+static Geometry* pin3d_geometry(Material* fuel, Material* mod, const PinSpec& ps,
+                                double zf, double zt) {
+  const double hw = 0.5 * ps.pitch;
+  ZCylinder* cyl = new ZCylinder(0.0, 0.0, ps.radius);
+  XPlane* xmin = new XPlane(-hw);
+  XPlane* xmax = new XPlane(hw);
+  YPlane* ymin = new YPlane(-hw);
+  YPlane* ymax = new YPlane(hw);
+  ZPlane* zmin = new ZPlane(0.0);
+  ZPlane* zmid = new ZPlane(zf);
+  ZPlane* zmax = new ZPlane(zt);
+  xmin->setBoundaryType(REFLECTIVE);
+  xmax->setBoundaryType(REFLECTIVE);
+  ymin->setBoundaryType(REFLECTIVE);
+  ymax->setBoundaryType(REFLECTIVE);
+  zmin->setBoundaryType(VACUUM);
+  zmax->setBoundaryType(VACUUM);
+  Cell* f = new Cell();
+  f->setFill(fuel);
+  f->addSurface(-1, cyl);
+  f->addSurface(+1, zmin);
+  f->addSurface(-1, zmid);
+  if (ps.fuel_rings) f->setNumRings(ps.fuel_rings);
+  if (ps.fuel_sectors) f->setNumSectors(ps.fuel_sectors);
+  Cell* m = new Cell();
+  m->setFill(mod);
+  m->addSurface(+1, cyl);
+  m->addSurface(+1, xmin);
+  m->addSurface(-1, xmax);
+  m->addSurface(+1, ymin);
+  m->addSurface(-1, ymax);
+  m->addSurface(+1, zmin);
+  m->addSurface(-1, zmid);
+  if (ps.mod_sectors) m->setNumSectors(ps.mod_sectors);
+  Cell* top = new Cell();
+  top->setFill(mod);
+  top->addSurface(+1, xmin);
+  top->addSurface(-1, xmax);
+  top->addSurface(+1, ymin);
+  top->addSurface(-1, ymax);
+  top->addSurface(+1, zmid);
+  top->addSurface(-1, zmax);
+  Universe* ru = new Universe();
+  ru->addCell(f);
+  ru->addCell(m);
+  ru->addCell(top);
+  Geometry* g = new Geometry();
+  g->setRootUniverse(ru);
+  return g;
 }
 
 int main(int argc, char** argv) {
@@ -489,6 +557,19 @@ int main(int argc, char** argv) {
     cases.push_back({"flux3_g7", lattice_geometry(3, fuel2, mod2, pin, {4},
                      REF, VAC, REF, VAC), 16, 0.1, 1000, 1e-5,
                      SCALAR_FLUX, FLUX, 1.0, false, fuel2, 1.0});
+  }
+
+  /* 8. explicit 3D: the pin extruded 2 cm, fuel below 1.6 cm, vacuum top
+   *    and bottom; 4 azimuthal, 4 polar, 0.1 cm radial, 0.4 cm axial */
+  {
+    Material* fuel = make_material(15, "fuel7z",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 5, 7, true));
+    Material* mod = make_material(16, "mod7z",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 1005, 7, false));
+    PinSpec p3 = {0.54, 1.26, 2, 4, 4};
+    cases.push_back({"pin3d_g7", pin3d_geometry(fuel, mod, p3, 1.6, 2.0), 4,
+                     0.1, 1000, 1e-5, FISSION_SOURCE, EIGEN, 1.0, false, NULL,
+                     0.0, 4, 0.4});
   }
 
   for (const CaseSpec& c : cases) {

@@ -10,7 +10,7 @@ OpenMOC's own FP32 and FP64 builds differ by 1.1e-5 on the pin cell at the
 import numpy as np
 import pytest
 
-from conftest import CASES, SRC_CASES, load_case
+from conftest import CASES, CASES_3D, SRC_CASES, load_case
 from openmoc_gb300 import GB300Solver
 from openmoc_gb300.solver import EXP_INTRINSIC, EXP_TABLE, FISSION_SOURCE, SCALAR_FLUX
 from oracle.oracle import Oracle
@@ -41,7 +41,7 @@ def solve(case, exp_kind, precision="f32"):
 
 
 @pytest.mark.parametrize("exp_kind", [EXP_TABLE, EXP_INTRINSIC])
-@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("case", CASES + CASES_3D)
 def test_eigenvalue_matches_openmoc(case, exp_kind):
     s, p, sc, arr = solve(case, exp_kind)
     _, sc64, arr64 = load_case(case, "f64")

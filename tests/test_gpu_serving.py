@@ -20,7 +20,7 @@ import time
 import numpy as np
 import pytest
 
-from conftest import CASES, load_case
+from conftest import CASES, CASES_3D, load_case
 from openmoc_gb300 import GB300Solver, lattice
 from openmoc_gb300._native import MOCError
 from openmoc_gb300.serving import Server, pool_capacity
@@ -73,7 +73,7 @@ def single(p, kind="eigenvalue", max_iters=FIXED_ITERS, res_type=1, k_eff=1.0,
 
 
 def test_fixtures_batched_match_openmoc():
-    cases = {c: load_case(c) for c in CASES}
+    cases = {c: load_case(c) for c in CASES + CASES_3D}
     # pools autotune their sweep shape and evaluator on the first batch
     srv = make_server([v[0] for v in cases.values()], 2, fixed_shape=False)
     tickets = {}
@@ -91,7 +91,7 @@ def test_fixtures_batched_match_openmoc():
         assert abs(r["keff"] - sc64["keff"]) <= 1.5 * KEFF_TOL, c
         assert max_rel(r["flux"], arr64["flux"]) <= FLUX_TOL, c
     st = srv.stats()
-    assert st["completed"] == len(CASES) and st["failed"] == 0
+    assert st["completed"] == len(cases) and st["failed"] == 0
     assert st["graph_captures"] >= 1
     srv.close()
 

@@ -16,7 +16,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import CASES, GOLDEN, SRC_CASES, load_case
+from conftest import CASES, CASES_3D, GOLDEN, SRC_CASES, load_case
 from oracle.oracle import Oracle
 
 
@@ -55,7 +55,7 @@ def test_oracle_matches_reference_goldens(precision):
         np.testing.assert_allclose(o.phi, d["fluxes"], rtol=2e-5)
 
 
-@pytest.mark.parametrize("case", CASES + SRC_CASES)
+@pytest.mark.parametrize("case", CASES + SRC_CASES + CASES_3D)
 @pytest.mark.parametrize("precision", ["f32", "f64"])
 def test_oracle_solve_matches_openmoc(case, precision):
     p, sc, arr = load_case(case, precision)
@@ -99,7 +99,7 @@ def test_oracle_hooks_match_openmoc(case):
 def test_fixture_fsr_ids_identical_across_precisions():
     """FSR numbering, tracks and links are integer data: the FP32 and FP64
     OpenMOC builds must produce them bit-identically."""
-    for case in CASES + SRC_CASES:
+    for case in CASES + SRC_CASES + CASES_3D:
         a, _, _ = load_case(case, "f32")
         b, _, _ = load_case(case, "f64")
         for name in ("seg_fsr", "seg_off", "next", "flags", "track_ang", "fsr_mat"):
