@@ -31,7 +31,8 @@ sys.path.insert(0, ROOT)
 
 WORKLOAD = "17x17 pin lattice, 70 groups, 64 azimuthal, 0.05 cm, TY-6 (3 polar), reflective"
 METRIC = "segment*group*polar integrations/s"
-FLOPS_PER_INTEGRATION = 30   # FP32 flops of one integration (FMA = 2)
+FLOPS_PER_INTEGRATION = 30     # FP32 flops of one 2D integration (FMA = 2)
+FLOPS_PER_INTEGRATION_3D = 28  # 3D: no 1/sin(theta) scaling
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one sweep launch
 # of this workload, from one ncu capture per sweep shape (lanes per track
 # direction, group pairs per lane, exponential kind); the summaries are under
@@ -119,8 +120,24 @@ class Clocks:
                 "samples": len(rows)}
 
 
-def build_problem():
+# The headline workload and the other single-solve configurations
+# (--workload): description, builder.
+WORKLOADS = {
+    "assembly70": WORKLOAD,
+    "core51": "51x51 pins (3x3 assemblies), 7 groups, 3 fuel sets in a checkerboard, "
+              "128 azimuthal, 0.03 cm, TY-6, vacuum on +x/+y, reflective on -x/-y",
+    "assembly3d": "17x17 assembly extruded to 20 cm (fuel below 16 cm, moderator above), "
+                  "7 groups, explicit 3D tracks: 16 azimuthal, 6 polar, 0.1 cm radial, "
+                  "0.5 cm axial; reflective radially, vacuum top and bottom",
+}
+
+
+def build_problem(workload="assembly70"):
     from openmoc_gb300 import lattice
+    if workload == "core51":
+        return lattice.core_51x51()
+    if workload == "assembly3d":
+        return lattice.assembly_17x17_3d()
     return lattice.assembly_17x17()
 
 
@@ -149,7 +166,7 @@ def run_reference(args):
     rank, world, _ = env_rank()
     if rank != 0:
         return
-    p = build_problem()
+    p = build_problem(args.workload)
     threads = os.cpu_count() or 1
     rates = []
     for _ in range(args.warmup):
@@ -166,8 +183,9 @@ def run_reference(args):
         "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded cross sections, generated tracks)",
-        "config": {"workload": WORKLOAD, "fsrs": p.num_fsrs, "tracks": p.num_tracks,
-                   "segments": p.num_segments, "integrations_per_step": p.integrations_per_sweep},
+        "config": {"workload": WORKLOADS[args.workload], "fsrs": p.num_fsrs,
+                   "tracks": p.num_tracks, "segments": p.num_segments,
+                   "integrations_per_step": p.integrations_per_sweep},
         "cpu_baseline": {"value": value, "unit": "integrations/s", "cores": threads,
                          "kind": "port",
                          "sample": f"{args.steps} full source iterations of the workload "
@@ -189,7 +207,7 @@ def run_gpu(args):
     from openmoc_gb300 import GB300Solver
     from openmoc_gb300.solver import FISSION_SOURCE
 
-    p = build_problem()
+    p = build_problem(args.workload)
     peaks, peak_kind = load_peaks()
     s = GB300Solver(p, device=local)
     if args.shape:
@@ -238,11 +256,13 @@ def run_gpu(args):
     nbytes = algorithmic_bytes(p)
     achieved = nbytes / (sweep_avg * 1e-3) / 1e9
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    traffic = SWEEP_DRAM_BYTES.get((lps, slots, exp_kind))
+    traffic = (SWEEP_DRAM_BYTES.get((lps, slots, exp_kind))
+               if args.workload == "assembly70" else None)
     sm_mhz = clocks.get("sm_mhz") or float(peaks.get("sm_max_mhz", 2070.0))
     props = torch.cuda.get_device_properties(local)
     fp32_peak = props.multi_processor_count * 128 * 2 * sm_mhz * 1e6 / 1e12
-    fp32_achieved = ints * FLOPS_PER_INTEGRATION / (sweep_avg * 1e-3) / 1e12
+    flops_per_int = FLOPS_PER_INTEGRATION_3D if p.solve_3d else FLOPS_PER_INTEGRATION
+    fp32_achieved = ints * flops_per_int / (sweep_avg * 1e-3) / 1e12
 
     # end to end through the public API: host buffers (pinned), upload,
     # 20 iterations, fluxes back
@@ -265,7 +285,8 @@ def run_gpu(args):
             "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded cross sections, generated tracks)",
-            "config": {"workload": WORKLOAD, "fsrs": p.num_fsrs, "tracks": p.num_tracks,
+            "config": {"workload": WORKLOADS[args.workload], "fsrs": p.num_fsrs,
+                       "tracks": p.num_tracks,
                        "segments": p.num_segments, "groups": p.num_groups,
                        "integrations_per_step": ints, "l2": "flushed before every step",
                        "sweep_shape": {"lanes_per_track_direction": lps,
@@ -284,7 +305,7 @@ def run_gpu(args):
                          "binding": {"bound": "fp32", "achieved": fp32_achieved,
                                      "peak": fp32_peak, "unit": "TFLOP/s",
                                      "frac": fp32_achieved / fp32_peak,
-                                     "flops_per_integration": FLOPS_PER_INTEGRATION}},
+                                     "flops_per_integration": flops_per_int}},
             "clocks": clocks,
             "gpu_launches": gpu_launches,
             "wall_s": t_wall,
@@ -293,7 +314,9 @@ def run_gpu(args):
             out["e2e"] = e2e
         if cpu:
             out["cpu_baseline"] = cpu
-        if world == 1 and not args.no_serving:
+        if args.batch > 0:
+            out["batched_instances"] = run_instances(p, args)
+        if world == 1 and not args.no_serving and args.workload == "assembly70":
             # the second half of the headline: the request stream through the
             # batched server against the plain per-solve loop
             sv = run_serving(args)
@@ -342,6 +365,39 @@ def end_to_end(p, args, device, torch):
     return {"value": p.integrations_per_sweep * args.e2e_iters / t, "unit": "integrations/s",
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
             "iterations_per_step": args.e2e_iters, "seconds_per_step": t}
+
+
+def run_instances(p, args, iters=10):
+    """args.batch cross-section-perturbed instances of `p` (the same tracks,
+    lognormal(0, 0.05) factors per material and group) in one server pool:
+    each kernel of an iteration is one launch over every instance.  Each
+    instance runs `iters` eigenvalue iterations; the rate counts the pool's
+    device time (CUDA events around every block) and the wall time from the
+    first submission (uploads included) to the last result."""
+    from openmoc_gb300 import lattice
+    from openmoc_gb300.serving import Server, pool_capacity
+    n = args.batch
+    insts = []
+    for i in range(n):
+        mats = lattice._fuel_mod(0, p.num_groups, 1, perturb=(7000 + i, 0.05))
+        insts.append(p.with_xs(*lattice.pack_materials(mats)))
+    srv = Server(iterations_per_poll=iters)
+    srv.add_pool(p.num_groups, p.num_polar_half, **pool_capacity(insts, n))
+    t0 = time.perf_counter()
+    tickets = [srv.submit(q, "eigenvalue", iters, 1, threshold=1e-30) for q in insts]
+    srv.run_until_idle()
+    res = [srv.wait(t, timeout=0) for t in tickets]
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    pool = srv.pool_stats(0)
+    srv.close()
+    total = sum(r["iterations"] for r in res) * p.integrations_per_sweep
+    return {"instances": n, "iterations_each": iters,
+            "integrations_per_s_device": total / st["gpu_busy_s"],
+            "integrations_per_s_wall": total / wall,
+            "device_s": st["gpu_busy_s"], "wall_s": wall,
+            "sweep_shape": [pool["lanes"], pool["pairs"]],
+            "keff": [r["keff"] for r in res]}
 
 
 # ---------------------------------------------------------------- serving
@@ -549,6 +605,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--shape", default="",
                     help="lanes,group_pairs_per_lane,exp (0 table, 1 ex2) instead of autotuning")
+    ap.add_argument("--workload", default="assembly70", choices=sorted(WORKLOADS),
+                    help="single-solve configuration (default: the headline one)")
+    ap.add_argument("--batch", type=int, default=0,
+                    help="with --workload: also run this many cross-section-perturbed "
+                         "instances in one server pool (one launch per kernel)")
     ap.add_argument("--serving", action="store_true",
                     help="the request-stream benchmark (batched server vs plain loop)")
     ap.add_argument("--serving-requests", type=int, default=512)

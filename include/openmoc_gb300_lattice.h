@@ -51,6 +51,19 @@ int moc_lattice_export(moc_lattice* lat, float* seg_len, int32_t* seg_fsr,
                        int32_t* fsr_mat, float* fsr_vol);
 int moc_lattice_destroy(moc_lattice* lat);
 
+/** Explicit 3D tracks of the lattice extruded to `height` (cm): its pins
+ *  below fuel_height, one homogeneous moderator region above; reflective
+ *  radially (required of the radial lattice), vacuum at bottom and top;
+ *  Gauss-Legendre polar angles (2, 4 or 6) and axial spacing z_spacing.
+ *  The workload shape of OpenMOC's TrackGenerator3D with EXPLICIT_3D
+ *  segments (src/TrackGenerator3D.cpp), with a laydown of its own whose 3D
+ *  links are exact.  The result has one polar value per track (3D layout of
+ *  include/openmoc_gb300.h) and is read with moc_lattice_sizes/export. */
+int moc_lattice_extrude(const moc_lattice* radial, double height,
+                        double fuel_height, double z_spacing,
+                        int32_t num_polar, int32_t num_threads,
+                        moc_lattice** out);
+
 /** Seeded synthetic multigroup data (sigma_s origin-major [orig*G+dest]),
  *  optionally multiplied by lognormal(0, perturb_sigma) factors per group. */
 int moc_synthetic_xs(uint64_t seed, int32_t num_groups, int32_t fissile,

@@ -76,6 +76,10 @@ struct moc_lattice {
   std::vector<float> weights, inv_sin;
   std::vector<int32_t> fsr_mat;
   std::vector<float> fsr_vol;
+  // per azimuthal index: effective spacing and azimuthal weight (used by the
+  // axial extrusion); moderator material
+  std::vector<double> az_spacing, az_weight;
+  int32_t moderator = 0;
 };
 
 const char* moc_lattice_last_error(void) { return g_lat_error.c_str(); }
@@ -434,6 +438,9 @@ extern "C" int moc_lattice_generate(const moc_lattice_spec* sp,
       vol[L->seg_fsr[k]] += w * (double) L->seg_len[k];
   }
   for (int64_t r = 0; r < R; r++) L->fsr_vol[r] = (float) vol[r];
+  L->az_spacing.assign(spac.begin(), spac.end());
+  L->az_weight.assign(wa.begin(), wa.end());
+  L->moderator = s.moderator_material;
   *out = L;
   return 0;
 }
@@ -496,5 +503,274 @@ extern "C" int moc_synthetic_xs(uint64_t seed, int32_t num_groups,
   std::memcpy(nu_sigma_f, m.nu_sigma_f.data(), 8 * G);
   std::memcpy(sigma_f, m.sigma_f.data(), 8 * G);
   std::memcpy(chi, m.chi.data(), 8 * G);
+  return 0;
+}
+
+// ---- axial extrusion into explicit 3D tracks ------------------------------
+// A lattice of height `height`, its pins for z < fuel_height and one
+// homogeneous moderator region above, reflective radially and vacuum at the
+// bottom and top: the shape of an axially extruded 3D benchmark with explicit
+// 3D segments (OpenMOC's TrackGenerator3D with EXPLICIT_3D,
+// src/TrackGenerator3D.cpp).  This is not OpenMOC's 3D laydown: it is a
+// laydown of its own on the same radial tracks, built so that every 3D link
+// is exact.
+//   - Radial tracks with reflective ends form closed cycles of directed 2D
+//     tracks; each cycle is unrolled into one periodic line coordinate s.
+//   - For each polar angle of a Gauss-Legendre set (mu = cos theta, half the
+//     angles upward), lines z = z0 + s cot(theta) start at the bottom (or
+//     top) at s_j = (j + 1/2) ds, with ds = L_cycle / n and
+//     n = round(L_cycle |cot theta| / dz): equally spaced along the cycle,
+//     vertical spacing dz' = ds |cot theta| close to dz.
+//   - A line is cut where it passes from one radial track to the next; each
+//     piece is a 3D track whose forward neighbour is the next piece (entered
+//     forward) and backward neighbour the previous one; the first and last
+//     pieces end on the vacuum bottom / top.
+//   - Segments: the radial segments under the piece, cut at z = fuel_height;
+//     above it the single moderator region (id R2); length = radial length /
+//     sin(theta).
+//   - Weights: one row per (cycle, polar angle): 2 pi w_a w_p d_a dz' sin(theta),
+//     w_a and d_a the azimuthal weight and spacing of the cycle's tracks, w_p
+//     the polar weight normalised to 1 over all polar angles (each 3D track is
+//     swept in both directions); FSR volumes are sum(w / 2 pi * length), as
+//     the radial laydown's volumes are sum(w_a d_a length).
+extern "C" int moc_lattice_extrude(const moc_lattice* L2, double height,
+                                   double fuel_height, double z_spacing,
+                                   int32_t num_polar, int32_t num_threads,
+                                   moc_lattice** out) {
+  if (!L2 || !out) return lat_fail("null argument");
+  *out = nullptr;
+  if (!(height > 0) || !(fuel_height > 0) || fuel_height > height ||
+      !(z_spacing > 0))
+    return lat_fail("bad axial dimensions");
+  if (num_polar != 2 && num_polar != 4 && num_polar != 6)
+    return lat_fail("num_polar must be 2, 4 or 6 (Gauss-Legendre)");
+  const int64_t T2 = L2->T;
+  for (int64_t t = 0; t < T2; t++)
+    if ((L2->flags[t] & 12) != 12)
+      return lat_fail("the extrusion needs reflective radial boundaries");
+  if (L2->az_spacing.empty()) return lat_fail("radial lattice has no spacings");
+
+  // Gauss-Legendre nodes and weights on [-1, 1] (sum of weights 2)
+  static const double gl_mu[3][3] = {{0.5773502691896258, 0, 0},
+                                     {0.3399810435848563, 0.8611363115940526, 0},
+                                     {0.2386191860831969, 0.6612093864662645,
+                                      0.9324695142031521}};
+  static const double gl_w[3][3] = {{1.0, 0, 0},
+                                    {0.6521451548625461, 0.3478548451374538, 0},
+                                    {0.4679139345726910, 0.3607615730481386,
+                                     0.1713244923791704}};
+  const int P = num_polar, half = P / 2, row = half - 1;
+  std::vector<double> mu(P), wp(P);
+  for (int k = 0; k < half; k++) {
+    mu[half - 1 - k] = -gl_mu[row][k];   // downward, steepest last
+    mu[half + k] = gl_mu[row][k];
+    wp[half - 1 - k] = wp[half + k] = 0.5 * gl_w[row][k];
+  }
+
+  // radial segment boundaries per track
+  std::vector<int64_t> off(L2->seg_off.begin(), L2->seg_off.end());
+  std::vector<double> cum((size_t) L2->S + T2);
+  std::vector<double> len2(T2);
+  for (int64_t t = 0; t < T2; t++) {
+    double c = 0;
+    cum[off[t] + t] = 0;
+    for (int64_t k = off[t]; k < off[t + 1]; k++) {
+      c += (double) L2->seg_len[k];
+      cum[k + 1 + t] = c;
+    }
+    len2[t] = c;
+  }
+  // cum of track t: cum[off[t] + t + i], i = 0..n_t
+
+  // cycles of directed tracks (t, d); the reverse cycle is left out
+  struct Cycle {
+    std::vector<int64_t> tr;
+    std::vector<int> dir;
+    std::vector<double> s0;
+    double len = 0;
+  };
+  std::vector<Cycle> cycles;
+  std::vector<uint8_t> seen(2 * T2, 0);
+  for (int64_t t0 = 0; t0 < T2; t0++)
+    for (int d0 = 0; d0 < 2; d0++) {
+      if (seen[2 * t0 + d0]) continue;
+      Cycle c;
+      int64_t t = t0;
+      int d = d0;
+      for (int64_t guard = 0;; guard++) {
+        if (guard > 2 * T2) return lat_fail("radial track links do not close");
+        c.tr.push_back(t);
+        c.dir.push_back(d);
+        c.s0.push_back(c.len);
+        c.len += len2[t];
+        seen[2 * t + d] = 1;
+        seen[2 * t + (1 - d)] = 1;
+        const int64_t nt = L2->next[2 * t + d];
+        const bool fwd = (L2->flags[t] & (d ? 2 : 1)) != 0;
+        t = nt;
+        d = fwd ? 0 : 1;
+        if (t == t0 && d == d0) break;
+      }
+      cycles.push_back(std::move(c));
+    }
+  const int64_t R2 = L2->R;
+  const int64_t nitems = (int64_t) cycles.size() * P;
+
+  // one work item per (cycle, polar angle): its tracks and segments
+  struct Item {
+    std::vector<float> seg_len;
+    std::vector<int32_t> seg_fsr;
+    std::vector<int32_t> nseg;
+    std::vector<uint8_t> first, last;   // first / last piece of its line
+    double weight = 0;
+  };
+  std::vector<Item> items(nitems);
+#ifdef _OPENMP
+  if (num_threads > 0) omp_set_num_threads(num_threads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+  for (int64_t it = 0; it < nitems; it++) {
+    const Cycle& c = cycles[it / P];
+    const int p = (int) (it % P);
+    Item& out_item = items[it];
+    const double sin_t = std::sqrt(1.0 - mu[p] * mu[p]);
+    const double cot = mu[p] / sin_t;          // dz / ds, signed
+    const double run = height / std::fabs(cot);
+    const int64_t n = std::max<int64_t>(
+        1, (int64_t) std::llround(c.len * std::fabs(cot) / z_spacing));
+    const double ds = c.len / (double) n;
+    const double dz_eff = ds * std::fabs(cot);
+    const int a = L2->track_ang[c.tr[0]];
+    out_item.weight = 2.0 * kPi * L2->az_weight[a] * wp[p] *
+                      L2->az_spacing[a] * dz_eff * sin_t;
+    const size_t ncyc = c.tr.size();
+    for (int64_t j = 0; j < n; j++) {
+      double s = (j + 0.5) * ds;
+      double z = (cot > 0) ? 0.0 : height;
+      double remaining = run;
+      size_t k = (size_t) (std::upper_bound(c.s0.begin(), c.s0.end(), s) -
+                           c.s0.begin()) - 1;
+      bool first_piece = true;
+      while (remaining > 1e-12) {
+        const int64_t t = c.tr[k];
+        const int d = c.dir[k];
+        const double L = len2[t];
+        const double a0 = std::max(0.0, s - c.s0[k]);
+        const double take = std::min(L - a0, remaining);
+        const double a1 = a0 + take;
+        // radial segments under [a0, a1] in traversal order, cut at the
+        // top of the fuel
+        const double* cb = cum.data() + off[t] + t;
+        const int64_t nsg = off[t + 1] - off[t];
+        const size_t seg_start = out_item.seg_len.size();
+        int32_t last_fsr = -1;
+        auto emit = [&](int32_t fsr, double l3) {
+          if (l3 <= 1e-10) return;
+          if (fsr == last_fsr && out_item.seg_len.size() > seg_start) {
+            out_item.seg_len.back() = (float) ((double) out_item.seg_len.back() + l3);
+          } else {
+            out_item.seg_fsr.push_back(fsr);
+            out_item.seg_len.push_back((float) l3);
+            last_fsr = fsr;
+          }
+        };
+        auto piece = [&](int32_t fsr2, double u0, double u1) {
+          // traversal interval [u0, u1] of one radial segment
+          const double z0 = z + (u0 - a0) * cot, z1 = z + (u1 - a0) * cot;
+          const double lo = std::min(z0, z1), hi = std::max(z0, z1);
+          if (hi <= fuel_height) {
+            emit(fsr2, (u1 - u0) / sin_t);
+          } else if (lo >= fuel_height) {
+            emit((int32_t) R2, (u1 - u0) / sin_t);
+          } else {
+            const double uc = u0 + (fuel_height - z0) / cot;
+            const bool below_first = z0 < fuel_height;
+            emit(below_first ? fsr2 : (int32_t) R2, (uc - u0) / sin_t);
+            emit(below_first ? (int32_t) R2 : fsr2, (u1 - uc) / sin_t);
+          }
+        };
+        if (d == 0) {
+          int64_t i = (int64_t) (std::upper_bound(cb, cb + nsg + 1, a0) - cb) - 1;
+          for (; i < nsg && cb[i] < a1; i++) {
+            const double u0 = std::max(a0, cb[i]), u1 = std::min(a1, cb[i + 1]);
+            if (u1 > u0) piece(L2->seg_fsr[off[t] + i], u0, u1);
+          }
+        } else {
+          // natural coordinate x = L - u
+          const double x0 = L - a1, x1 = L - a0;
+          int64_t i = (int64_t) (std::upper_bound(cb, cb + nsg + 1, x1) - cb) - 1;
+          if (i >= nsg) i = nsg - 1;
+          for (; i >= 0 && cb[i + 1] > x0; i--) {
+            const double v0 = std::max(x0, cb[i]), v1 = std::min(x1, cb[i + 1]);
+            if (v1 > v0) piece(L2->seg_fsr[off[t] + i], L - v1, L - v0);
+          }
+        }
+        out_item.nseg.push_back(
+            (int32_t) (out_item.seg_len.size() - seg_start));
+        remaining -= take;
+        z += take * cot;
+        out_item.first.push_back(first_piece ? 1 : 0);
+        out_item.last.push_back(remaining > 1e-12 ? 0 : 1);
+        first_piece = false;
+        k = (k + 1) % ncyc;
+        s = c.s0[k];
+      }
+    }
+  }
+
+  // concatenate in item order
+  moc_lattice* L = new moc_lattice();
+  int64_t T = 0, S = 0;
+  for (const Item& m : items) {
+    T += (int64_t) m.nseg.size();
+    S += (int64_t) m.seg_len.size();
+  }
+  if (T >= (1LL << 31) || S >= (1LL << 40)) {
+    delete L;
+    return lat_fail("extruded problem too large");
+  }
+  L->R = R2 + 1;
+  L->T = T;
+  L->S = S;
+  L->A = (int32_t) nitems;
+  L->Ph = 1;
+  L->M = L2->M;
+  L->seg_len.resize(S);
+  L->seg_fsr.resize(S);
+  L->seg_off.assign(T + 1, 0);
+  L->track_ang.resize(T);
+  L->next.resize(2 * T);
+  L->flags.resize(T);
+  L->weights.resize(nitems);
+  L->inv_sin.assign(nitems, 1.0f);
+  std::vector<double> vol(R2 + 1, 0.0);
+  int64_t tb = 0, sb = 0;
+  for (int64_t it = 0; it < nitems; it++) {
+    const Item& m = items[it];
+    L->weights[it] = (float) m.weight;
+    const double wv = m.weight / (2.0 * kPi);
+    std::memcpy(L->seg_len.data() + sb, m.seg_len.data(), 4 * m.seg_len.size());
+    std::memcpy(L->seg_fsr.data() + sb, m.seg_fsr.data(), 4 * m.seg_fsr.size());
+    for (size_t q = 0; q < m.seg_len.size(); q++)
+      vol[m.seg_fsr[q]] += wv * (double) m.seg_len[q];
+    for (size_t q = 0; q < m.nseg.size(); q++) {
+      const int64_t t = tb + (int64_t) q;
+      L->seg_off[t + 1] = L->seg_off[t] + m.nseg[q];
+      L->track_ang[t] = (int32_t) it;
+      uint8_t f = 1;                       // forward exit enters forward
+      if (!m.last[q]) f |= 4;              // transfer forward
+      if (!m.first[q]) f |= 8;             // transfer backward
+      L->flags[t] = f;                     // backward exit enters backward
+      L->next[2 * t] = m.last[q] ? t : t + 1;
+      L->next[2 * t + 1] = m.first[q] ? t : t - 1;
+    }
+    tb += (int64_t) m.nseg.size();
+    sb += (int64_t) m.seg_len.size();
+  }
+  L->fsr_mat.assign(L2->fsr_mat.begin(), L2->fsr_mat.end());
+  L->fsr_mat.push_back(L2->moderator);
+  L->fsr_vol.resize(R2 + 1);
+  for (int64_t r = 0; r <= R2; r++) L->fsr_vol[r] = (float) vol[r];
+  *out = L;
   return 0;
 }

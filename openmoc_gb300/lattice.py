@@ -62,6 +62,10 @@ def _lib():
         L.moc_lattice_sizes.restype = C.c_int
         L.moc_lattice_export.argtypes = [C.c_void_p] + [C.c_void_p] * 10
         L.moc_lattice_export.restype = C.c_int
+        L.moc_lattice_extrude.argtypes = [C.c_void_p, C.c_double, C.c_double,
+                                          C.c_double, C.c_int32, C.c_int32,
+                                          C.POINTER(C.c_void_p)]
+        L.moc_lattice_extrude.restype = C.c_int
         L.moc_lattice_destroy.argtypes = [C.c_void_p]
         L.moc_lattice_destroy.restype = C.c_int
         L.moc_lattice_last_error.restype = C.c_char_p
@@ -120,10 +124,13 @@ def lattice(nx: int, ny: int, pin_material: np.ndarray, materials: Sequence[Mate
             pitch: float = 1.26, pin_radius: float = 0.54, fuel_rings: int = 3,
             fuel_sectors: int = 8, mod_sectors: int = 8, num_polar: int = 6,
             bc=(REFLECTIVE, REFLECTIVE, REFLECTIVE, REFLECTIVE),
-            num_threads: int = 0) -> Problem:
+            num_threads: int = 0, extrude: Optional[dict] = None) -> Problem:
     """Tracks, segments and cross sections of an nx x ny pin lattice.
     ``pin_material[row, col]`` (row 0 = top) is the material inside each
-    pin; ``bc`` is (xmin, xmax, ymin, ymax)."""
+    pin; ``bc`` is (xmin, xmax, ymin, ymax).  ``extrude`` = dict(height,
+    fuel_height, z_spacing, num_polar) turns it into explicit 3D tracks of
+    the lattice extruded axially (moderator above fuel_height, vacuum at
+    bottom and top; ``num_polar`` Gauss-Legendre polar angles)."""
     L = _lib()
     pm = np.ascontiguousarray(np.asarray(pin_material, np.int32).reshape(ny, nx))
     spec = _Spec(nx, ny, pitch, pin_radius, fuel_rings, fuel_sectors, mod_sectors,
@@ -132,6 +139,17 @@ def lattice(nx: int, ny: int, pin_material: np.ndarray, materials: Sequence[Mate
     h = C.c_void_p()
     if L.moc_lattice_generate(C.byref(spec), C.byref(h)):
         raise RuntimeError(L.moc_lattice_last_error().decode())
+    if extrude is not None:
+        h3 = C.c_void_p()
+        rc = L.moc_lattice_extrude(h, float(extrude["height"]),
+                                   float(extrude["fuel_height"]),
+                                   float(extrude["z_spacing"]),
+                                   int(extrude["num_polar"]), num_threads,
+                                   C.byref(h3))
+        L.moc_lattice_destroy(h)
+        if rc:
+            raise RuntimeError(L.moc_lattice_last_error().decode())
+        h = h3
     try:
         R, T, S = C.c_int64(), C.c_int64(), C.c_int64()
         A, Ph, M = C.c_int32(), C.c_int32(), C.c_int32()
@@ -153,7 +171,8 @@ def lattice(nx: int, ny: int, pin_material: np.ndarray, materials: Sequence[Mate
     G = materials[0].num_groups
     p = Problem(num_groups=G, num_polar_half=Ph, num_angles=A,
                 num_materials=len(materials), num_fsrs=R, num_tracks=T,
-                num_segments=S, solve_3d=0, sigma_t=st, sigma_s=ss, nu_sigma_f=nf,
+                num_segments=S, solve_3d=0 if extrude is None else 1,
+                sigma_t=st, sigma_s=ss, nu_sigma_f=nf,
                 chi=ch, **arr)
     p.meta = dict(nx=nx, ny=ny, num_azim=num_azim, spacing=spacing, pitch=pitch,
                   num_polar=num_polar)
@@ -196,6 +215,22 @@ def assembly_17x17(num_groups: int = 70, num_azim: int = 64, spacing: float = 0.
     """17 x 17 assembly with 25 water-filled guide-tube positions."""
     return square_lattice(17, num_groups, num_azim, spacing, config,
                           GUIDE_TUBES_17x17, perturb)
+
+
+def assembly_17x17_3d(num_groups: int = 7, num_azim: int = 16, spacing: float = 0.1,
+                      num_polar: int = 6, z_spacing: float = 0.5, height: float = 20.0,
+                      fuel_height: float = 16.0, config: int = 4, perturb=None) -> Problem:
+    """The 17 x 17 assembly extruded axially: the lattice for z < 16 cm,
+    homogeneous moderator up to 20 cm, reflective radially, vacuum at the
+    bottom and top, explicit 3D tracks (16 azimuthal, 6 polar, 0.1 cm radial,
+    0.5 cm axial spacing)."""
+    mats = _fuel_mod(config, num_groups, 1, perturb)
+    pm = np.zeros((17, 17), np.int32)
+    for (r, c) in GUIDE_TUBES_17x17:
+        pm[r, c] = 1
+    return lattice(17, 17, pm, mats, 1, num_azim=num_azim, spacing=spacing,
+                   extrude=dict(height=height, fuel_height=fuel_height,
+                                z_spacing=z_spacing, num_polar=num_polar))
 
 
 def core_51x51(num_groups: int = 7, num_azim: int = 128, spacing: float = 0.03,
