@@ -234,7 +234,8 @@ def run_gpu(args):
     # the source contraction both ways: 3xTF32 tensor cores (the default at
     # 70 groups) against the FP32 CUDA-core kernel, same iterations
     sources = {"kernel": s.getSourceContraction()}
-    for kind in ("fp32", "tf32x3"):
+    kinds = ("fp32", "tf32x3") if 64 <= p.num_groups <= 96 else ()
+    for kind in kinds:
         s.setSourceContraction(kind)
         st, sw = s.benchIterations(max(args.steps // 2, 5), FISSION_SOURCE, True)
         sources[f"{kind}_ms_per_step"] = float(np.mean(st))
