@@ -149,6 +149,10 @@ struct moc_ctx {
   int32_t* tc_tile_mat = nullptr;
   float* tc_b = nullptr;
   int tc_tiles = 0;
+  // FSRs with the last ids that take a large share of the segments (the
+  // moderator above an extruded lattice): tallied in shared memory by the
+  // 3D sweep instances
+  int hot_base = 0, hot_count = 0;
 };
 
 namespace {
@@ -202,6 +206,8 @@ moc::SweepArgs sweep_args(moc_ctx* c, int check_done) {
   a.lps = c->lps;
   a.mat_packed = c->mat_packed;
   a.check_done = check_done;
+  a.hot_count = (c->d.num_polar_half == 1) ? c->hot_count : 0;
+  a.hot_base = a.hot_count ? c->hot_base : (int) c->d.num_fsrs;
   return a;
 }
 
@@ -675,6 +681,15 @@ int moc_upload_tracks(moc_ctx* c, const float* seg_len, const int32_t* seg_fsr,
                 "next-track index out of range on track " +
                     std::to_string(t));
   }
+  // trailing FSR ids crossed by at least 0.2 % of all segments each
+  std::vector<int64_t> per_fsr(R, 0);
+  for (int64_t s = 0; s < S; s++)
+    if (seg_fsr[s] >= 0 && seg_fsr[s] < R) per_fsr[seg_fsr[s]]++;
+  c->hot_count = 0;
+  while (c->hot_count < moc::kMaxHotFsrs && c->hot_count < R &&
+         per_fsr[R - 1 - c->hot_count] * 500 >= S && S > 0)
+    c->hot_count++;
+  c->hot_base = (int) (R - c->hot_count);
   std::vector<int2> packed(S);
   for (int64_t s = 0; s < S; s++) {
     MOC_CHECK(seg_fsr[s] >= 0 && seg_fsr[s] < R, MOC_ERR_ARG,

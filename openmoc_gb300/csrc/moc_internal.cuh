@@ -86,7 +86,15 @@ struct SweepArgs {
   const int32_t* track_slot; // [T]
   DevScalars* slots;         // [num_slots]
   int num_slots;
+  // FSRs [hot_base, hot_base + hot_count) take a large share of all
+  // segments (one region crossed by most tracks); each block tallies them in
+  // shared memory and adds its totals once at its end.  Used by the
+  // one-polar-value (3D) instances; hot_count = 0 elsewhere.
+  int hot_base;
+  int hot_count;             // 0 .. kMaxHotFsrs
 };
+
+constexpr int kMaxHotFsrs = 8;
 
 struct SolverArgs {
   const float* sigma_t;      // [M][G]

@@ -612,6 +612,8 @@ moc::SweepArgs pool_sweep_args(Pool& p) {
   a.track_slot = p.track_slot;
   a.slots = p.slots_d;
   a.num_slots = p.cfg.max_solves;
+  a.hot_base = 0x7FFFFFFF;   // no shared-memory tallies in pools
+  a.hot_count = 0;
   return a;
 }
 

@@ -120,11 +120,13 @@ sweep_kernel(const SweepArgs a) {
   const int ld = a.ld;                       // even row stride >= G
   float2* s_tab = reinterpret_cast<float2*>(smem);
   float* s_st = smem + ((EXPK == kExpTable) ? 2 * kExpTableSize : 0);
+  float* s_hot = s_st + a.num_materials * ld;   // [hot_count][ld]
   // sigma_t rows padded to ld; the padding group gets sigma_t = 1
   for (int i = threadIdx.x; i < a.num_materials * ld; i += blockDim.x) {
     const int m = i / ld, g = i - m * ld;
     s_st[i] = (g < G) ? a.sigma_t[m * G + g] : 1.0f;
   }
+  for (int i = threadIdx.x; i < a.hot_count * ld; i += blockDim.x) s_hot[i] = 0.0f;
   if (EXPK == kExpTable)
     for (int i = threadIdx.x; i < kExpTableSize; i += blockDim.x)
       s_tab[i] = make_float2(a.exp_table[i], a.exp_table[kExpTableSize + i]);
@@ -254,6 +256,9 @@ sweep_kernel(const SweepArgs a) {
       const float2* st =
           reinterpret_cast<const float2*>(s_st + mat * ld) + sub;
       float2* ph = reinterpret_cast<float2*>(a.phi + (int64_t) fsr * ld) + sub;
+      // a region crossed by most tracks tallies into this block's copy
+      // (3D problems only, PH == 1: one moderator region above the fuel)
+      const int hot = (PH == 1) ? fsr - a.hot_base : -1;
       const float2 len2 = f2(len);
 #pragma unroll
       for (int s = 0; s < PS; s++) {
@@ -275,7 +280,13 @@ sweep_kernel(const SweepArgs a) {
             psi[s][p] = __ffma2_rn(d, f2(-1.0f), psi[s][p]);
             tally = __ffma2_rn(w2[p], d, tally);
           }
-          atomicAdd(ph + s * LPS, tally);
+          if (PH == 1 && hot >= 0) {
+            float* hp = s_hot + hot * ld + 2 * (sub + s * LPS);
+            atomicAdd(hp, tally.x);
+            atomicAdd(hp + 1, tally.y);
+          } else {
+            atomicAdd(ph + s * LPS, tally);
+          }
         }
       }
       len = len_n;
@@ -308,6 +319,11 @@ sweep_kernel(const SweepArgs a) {
   // sc->cur by then.  The buffer just written starts with scale 1.
   __shared__ int last;
   __syncthreads();
+  // this block's totals of the shared-memory tallies
+  for (int i = threadIdx.x; i < a.hot_count * ld; i += blockDim.x) {
+    const float v = s_hot[i];
+    if (v != 0.0f) atomicAdd(a.phi + (int64_t) a.hot_base * ld + i, v);
+  }
   if (threadIdx.x == 0) {
     __threadfence();
     unsigned int ticket = atomicAdd(&sc->ticket_sweep, 1u);
@@ -334,7 +350,7 @@ void launch_sweep_instance(const SweepArgs& a, cudaStream_t stream) {
   const int wpb = kSweepThreads / 32;
   const int64_t blocks = (warps + wpb - 1) / wpb;
   const size_t smem =
-      sizeof(float) * ((size_t) a.num_materials * a.ld +
+      sizeof(float) * ((size_t) (a.num_materials + a.hot_count) * a.ld +
                        (EXPK == kExpTable ? 2 * kExpTableSize : 0));
   auto kern = sweep_kernel<PH, LPS, PS, EXPK, POOL>;
   if (smem > 48 * 1024)
