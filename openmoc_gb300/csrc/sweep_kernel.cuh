@@ -95,35 +95,22 @@ struct AttenIntrinsic {
   }
 };
 
-// Sources gathered this many segments ahead: two for the light instances
-// (few integrations per segment and lane, one or two group pairs), whose
-// loop is otherwise bound by load latency; one elsewhere.
-template <int PH, int LPS, int PS>
-struct SweepDepth {
-  static constexpr int value = (PH * PS <= 6 && PS <= 2 && LPS >= 2) ? 2 : 1;
-};
-
 // Registers available per thread: the busy instances keep 5 blocks of 128
-// threads resident per SM, the light ones 8, or 7 with the two-segment
-// look-ahead; one-polar instances with 3 to 6 pairs (and the shared-memory
-// tallies of 3D problems) 6.
+// threads resident per SM, the small ones 8.
 #ifndef MOC_SWEEP_BIG_MIN_BLOCKS
 #define MOC_SWEEP_BIG_MIN_BLOCKS 5
 #endif
-template <int PH, int LPS, int PS>
+template <int PH, int PS>
 struct SweepOccupancy {
   static constexpr int min_blocks =
-      (PH * PS > 6)           ? MOC_SWEEP_BIG_MIN_BLOCKS
-      : (PH == 1 && PS > 2)   ? 6
-      : (SweepDepth<PH, LPS, PS>::value == 2) ? 7
-                              : 8;
+      (PH * PS > 6) ? MOC_SWEEP_BIG_MIN_BLOCKS : 8;
 };
 
 // POOL: the tracks of many solves (a batched pool); each track takes its
 // pending angular-flux scale and done flag from its own solve's state.
 template <int PH, int LPS, int PS, int EXPK, bool POOL>
 __global__ void __launch_bounds__(kSweepThreads,
-                                  (SweepOccupancy<PH, LPS, PS>::min_blocks))
+                                  (SweepOccupancy<PH, PS>::min_blocks))
 sweep_kernel(const SweepArgs a) {
   extern __shared__ float smem[];
   DevScalars* sc = a.sc;
@@ -211,10 +198,7 @@ sweep_kernel(const SweepArgs a) {
     // LPS consecutive segments with one coalesced access (a "chunk", one
     // segment per lane) a whole chunk ahead of use; segment k reaches every
     // lane of the stream by a shuffle from lane k % LPS.  The sources of
-    // segment k + DEPTH are gathered while segment k is integrated: DEPTH 2
-    // for the light instances (few integrations per segment and lane), whose
-    // loop is otherwise bound by load latency.
-    constexpr int DEPTH = SweepDepth<PH, LPS, PS>::value;
+    // segment k+1 are gathered while segment k is integrated.
     const int2* seg = a.segs + b;
     const unsigned gmask =
         (LPS == 32) ? 0xffffffffu
@@ -235,48 +219,39 @@ sweep_kernel(const SweepArgs a) {
     };
     int2 chunk = fetch(sub);
     int2 chunk_next = fetch(LPS + sub);
-    int cb = 0;   // first segment of `chunk`; chunk_next holds the next LPS
-    // segment j, held by lane j % LPS of chunk or chunk_next (uniform over
-    // the stream's lanes)
-    auto word = [&](int j) -> int2 {
-      const int2 w = (j - cb < LPS) ? chunk : chunk_next;
-      int2 r;
-      r.x = __shfl_sync(gmask, w.x, j & (LPS - 1), LPS);
-      r.y = __shfl_sync(gmask, w.y, j & (LPS - 1), LPS);
-      return r;
-    };
+    int2 sg;
+    sg.x = __shfl_sync(gmask, chunk.x, 0, LPS);
+    sg.y = __shfl_sync(gmask, chunk.y, 0, LPS);
+    float len;
+    int fsr, mat;
+    unpack(sg, len, fsr, mat);
     const float2* qbase = reinterpret_cast<const float2*>(a.qt) + sub;
-    auto gather = [&](float2* qq, int f, bool valid) {
-      const float2* qrow = qbase + (int64_t) f * npairs;
+    float2 q[PS];
 #pragma unroll
-      for (int s = 0; s < PS; s++)
-        qq[s] = (sub + s * LPS < npairs && valid) ? __ldg(qrow + s * LPS)
-                                                  : f2(0.0f);
-    };
-    float len, len1 = 0.0f;
-    int fsr, mat, fsr1 = 0, mat1 = 0;
-    float2 q[PS], q1[PS];
-    unpack(word(0), len, fsr, mat);
-    gather(q, fsr, n > 0);
-    if (DEPTH == 2) {
-      // light instances keep two segments' sources in flight
-      unpack(word(1), len1, fsr1, mat1);
-      gather(q1, fsr1, n > 1);
-    }
+    for (int s = 0; s < PS; s++)
+      q[s] = (sub + s * LPS < npairs && n > 0)
+                 ? __ldg(qbase + (int64_t) fsr * npairs + s * LPS)
+                 : f2(0.0f);
     for (int k = 0; k < n; k++) {
-      // the segment DEPTH ahead: its word and its sources
-      const int ka = k + DEPTH;
+      // next segment: rotate chunks at chunk boundaries
+      const int kn = k + 1;
+      const int src = kn & (LPS - 1);
+      if (src == 0) {
+        chunk = chunk_next;
+        chunk_next = fetch(kn + LPS + sub);
+      }
+      int2 sgn;
+      sgn.x = __shfl_sync(gmask, chunk.x, src, LPS);
+      sgn.y = __shfl_sync(gmask, chunk.y, src, LPS);
       float len_n;
       int fsr_n, mat_n;
-      unpack(word(ka), len_n, fsr_n, mat_n);
+      unpack(sgn, len_n, fsr_n, mat_n);
       float2 qn[PS];
-      gather(qn, fsr_n, ka < n);
-      // rotate chunks once the look-ahead has reached chunk_next
-      if (ka - cb == LPS) {
-        chunk = chunk_next;
-        chunk_next = fetch(cb + 2 * LPS + sub);
-        cb += LPS;
-      }
+      const float2* qrow = qbase + (int64_t) fsr_n * npairs;
+#pragma unroll
+      for (int s = 0; s < PS; s++)
+        qn[s] = (sub + s * LPS < npairs && kn < n) ? __ldg(qrow + s * LPS)
+                                                   : f2(0.0f);
 
       const float2* st =
           reinterpret_cast<const float2*>(s_st + mat * ld) + sub;
@@ -314,25 +289,11 @@ sweep_kernel(const SweepArgs a) {
           }
         }
       }
-      if (DEPTH == 2) {
-        len = len1;
-        fsr = fsr1;
-        mat = mat1;
-        len1 = len_n;
-        fsr1 = fsr_n;
-        mat1 = mat_n;
+      len = len_n;
+      fsr = fsr_n;
+      mat = mat_n;
 #pragma unroll
-        for (int s = 0; s < PS; s++) {
-          q[s] = q1[s];
-          q1[s] = qn[s];
-        }
-      } else {
-        len = len_n;
-        fsr = fsr_n;
-        mat = mat_n;
-#pragma unroll
-        for (int s = 0; s < PS; s++) q[s] = qn[s];
-      }
+      for (int s = 0; s < PS; s++) q[s] = qn[s];
     }
 
     // boundary-flux transfer to the connecting track, fused into the sweep
