@@ -96,14 +96,19 @@ struct AttenIntrinsic {
 };
 
 // Registers available per thread: the busy instances keep 5 blocks of 128
-// threads resident per SM, the small ones 8.
+// threads resident per SM (4 at 18 pair-polar values per lane), the small
+// ones 8; one-polar (3D) instances with 3 or more pairs, whose shared-memory
+// tallies need a few registers more, 6.
 #ifndef MOC_SWEEP_BIG_MIN_BLOCKS
 #define MOC_SWEEP_BIG_MIN_BLOCKS 5
 #endif
 template <int PH, int PS>
 struct SweepOccupancy {
   static constexpr int min_blocks =
-      (PH * PS > 6) ? MOC_SWEEP_BIG_MIN_BLOCKS : 8;
+      (PH * PS >= 18)        ? 4
+      : (PH * PS > 6)        ? MOC_SWEEP_BIG_MIN_BLOCKS
+      : (PH == 1 && PS > 2)  ? 6
+                             : 8;
 };
 
 // POOL: the tracks of many solves (a batched pool); each track takes its
