@@ -45,6 +45,22 @@ def env_rank():
             int(os.environ.get("LOCAL_RANK", 0)))
 
 
+def max_over_ranks(x, dist, device):
+    """The largest value of x over the ranks (x itself without a process
+    group)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_step, steps, world, slowest_ms):
+    """Units of all `world` replicas per second of the slowest one."""
+    return world * units_per_step * steps / (slowest_ms * 1e-3)
+
+
 def load_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -242,15 +258,13 @@ def run_gpu(args):
         sources[f"{kind}_non_sweep_ms"] = float(np.mean(np.asarray(st) - np.asarray(sw)))
     s.setSourceContraction("auto")
     clocks = clk.summary()
-    total_ms = float(np.sum(step_ms))
+    # replicas: the slowest rank's time, every rank's integrations
+    total_ms = max_over_ranks(float(np.sum(step_ms)), dist, "cuda")
     if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
         dist.barrier()
     ms_per_step = total_ms / args.steps
     ints = p.integrations_per_sweep
-    value = world * ints * args.steps / (total_ms * 1e-3)
+    value = whole_job_rate(ints, args.steps, world, total_ms)
 
     # roofline of the dominant kernel (the sweep)
     sweep_avg = float(np.mean(sweep_ms))
