@@ -95,6 +95,30 @@ struct AttenIntrinsic {
   }
 };
 
+// Segments of look-ahead for the staged sources: bounded by the chunk
+// window (a segment word is reachable from chunk or chunk_next up to LPS
+// segments ahead of the current one).
+template <int LPS>
+struct SweepRing {
+  static constexpr int ahead = LPS < 3 ? LPS : 3;
+};
+
+__device__ __forceinline__ void cp_async8(void* smem_dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(
+                   (uint32_t) __cvta_generic_to_shared(smem_dst)),
+               "l"(src)
+               : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 // Registers available per thread: the busy instances keep 5 blocks of 128
 // threads resident per SM (4 at 18 pair-polar values per lane), the small
 // ones 8; one-polar (3D) instances with 3 or more pairs, whose shared-memory
@@ -126,6 +150,9 @@ sweep_kernel(const SweepArgs a) {
   float2* s_tab = reinterpret_cast<float2*>(smem);
   float* s_st = smem + ((EXPK == kExpTable) ? 2 * kExpTableSize : 0);
   float* s_hot = s_st + a.num_materials * ld;   // [hot_count][ld]
+  // [slot][pair][thread] ring of staged sources (8-byte aligned: every
+  // region before it is an even number of floats)
+  float2* s_ring = reinterpret_cast<float2*>(s_hot + a.hot_count * ld);
   // sigma_t rows padded to ld; the padding group gets sigma_t = 1
   for (int i = threadIdx.x; i < a.num_materials * ld; i += blockDim.x) {
     const int m = i / ld, g = i - m * ld;
@@ -203,7 +230,10 @@ sweep_kernel(const SweepArgs a) {
     // LPS consecutive segments with one coalesced access (a "chunk", one
     // segment per lane) a whole chunk ahead of use; segment k reaches every
     // lane of the stream by a shuffle from lane k % LPS.  The sources of
-    // segment k+1 are gathered while segment k is integrated.
+    // segment k + kAhead are copied into shared memory while segment k is
+    // integrated.
+    constexpr int kAhead = SweepRing<LPS>::ahead;
+    constexpr int kRing = kAhead + 1;
     const int2* seg = a.segs + b;
     const unsigned gmask =
         (LPS == 32) ? 0xffffffffu
@@ -224,39 +254,50 @@ sweep_kernel(const SweepArgs a) {
     };
     int2 chunk = fetch(sub);
     int2 chunk_next = fetch(LPS + sub);
-    int2 sg;
-    sg.x = __shfl_sync(gmask, chunk.x, 0, LPS);
-    sg.y = __shfl_sync(gmask, chunk.y, 0, LPS);
-    float len;
-    int fsr, mat;
-    unpack(sg, len, fsr, mat);
+    int cb = 0;   // first segment held by `chunk`; chunk_next the next LPS
+    // segment j (cb <= j < cb + 2 LPS) from lane j % LPS of chunk or
+    // chunk_next (uniform over the stream's lanes)
+    auto word = [&](int j) -> int2 {
+      const int2 w = (j - cb < LPS) ? chunk : chunk_next;
+      int2 r;
+      r.x = __shfl_sync(gmask, w.x, j & (LPS - 1), LPS);
+      r.y = __shfl_sync(gmask, w.y, j & (LPS - 1), LPS);
+      return r;
+    };
+    // The sources of segment j travel by asynchronous copies (8 bytes per
+    // group pair) into ring slot j % kRing of this thread, kAhead segments
+    // before use, so the look-ahead holds no registers; one copy group per
+    // segment (empty past the end of the track).
     const float2* qbase = reinterpret_cast<const float2*>(a.qt) + sub;
-    float2 q[PS];
+    auto slot = [&](int j, int s) -> float2* {
+      return s_ring + ((j % kRing) * PS + s) * kSweepThreads + threadIdx.x;
+    };
+    auto stage = [&](int j) {
+      if (j < n) {
+        float l;
+        int f, m;
+        unpack(word(j), l, f, m);
+        const float2* src = qbase + (int64_t) f * npairs;
 #pragma unroll
-    for (int s = 0; s < PS; s++)
-      q[s] = (sub + s * LPS < npairs && n > 0)
-                 ? __ldg(qbase + (int64_t) fsr * npairs + s * LPS)
-                 : f2(0.0f);
-    for (int k = 0; k < n; k++) {
-      // next segment: rotate chunks at chunk boundaries
-      const int kn = k + 1;
-      const int src = kn & (LPS - 1);
-      if (src == 0) {
-        chunk = chunk_next;
-        chunk_next = fetch(kn + LPS + sub);
+        for (int s = 0; s < PS; s++)
+          if (sub + s * LPS < npairs) cp_async8(slot(j, s), src + s * LPS);
       }
-      int2 sgn;
-      sgn.x = __shfl_sync(gmask, chunk.x, src, LPS);
-      sgn.y = __shfl_sync(gmask, chunk.y, src, LPS);
-      float len_n;
-      int fsr_n, mat_n;
-      unpack(sgn, len_n, fsr_n, mat_n);
-      float2 qn[PS];
-      const float2* qrow = qbase + (int64_t) fsr_n * npairs;
+      cp_async_commit();
+    };
 #pragma unroll
-      for (int s = 0; s < PS; s++)
-        qn[s] = (sub + s * LPS < npairs && kn < n) ? __ldg(qrow + s * LPS)
-                                                   : f2(0.0f);
+    for (int j = 0; j < kAhead; j++) stage(j);
+    for (int k = 0; k < n; k++) {
+      stage(k + kAhead);
+      float len;
+      int fsr, mat;
+      unpack(word(k), len, fsr, mat);
+      // rotate chunks once segment k + 1 leaves `chunk`
+      if (k + 1 - cb == LPS) {
+        chunk = chunk_next;
+        chunk_next = fetch(cb + 2 * LPS + sub);
+        cb += LPS;
+      }
+      cp_async_wait<kAhead>();   // segment k's sources have landed
 
       const float2* st =
           reinterpret_cast<const float2*>(s_st + mat * ld) + sub;
@@ -268,7 +309,7 @@ sweep_kernel(const SweepArgs a) {
 #pragma unroll
       for (int s = 0; s < PS; s++) {
         if (sub + s * LPS < npairs) {
-          const float2 qs = q[s];
+          const float2 qs = *slot(k, s);
           const float2 tau = __fmul2_rn(st[s * LPS], len2);
           float2 tally = f2(0.0f);
 #pragma unroll
@@ -294,11 +335,6 @@ sweep_kernel(const SweepArgs a) {
           }
         }
       }
-      len = len_n;
-      fsr = fsr_n;
-      mat = mat_n;
-#pragma unroll
-      for (int s = 0; s < PS; s++) q[s] = qn[s];
     }
 
     // boundary-flux transfer to the connecting track, fused into the sweep
@@ -356,7 +392,8 @@ void launch_sweep_instance(const SweepArgs& a, cudaStream_t stream) {
   const int64_t blocks = (warps + wpb - 1) / wpb;
   const size_t smem =
       sizeof(float) * ((size_t) (a.num_materials + a.hot_count) * a.ld +
-                       (EXPK == kExpTable ? 2 * kExpTableSize : 0));
+                       (EXPK == kExpTable ? 2 * kExpTableSize : 0)) +
+      sizeof(float2) * (SweepRing<LPS>::ahead + 1) * PS * kSweepThreads;
   auto kern = sweep_kernel<PH, LPS, PS, EXPK, POOL>;
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
