@@ -95,12 +95,17 @@ struct AttenIntrinsic {
   }
 };
 
-// Segments of look-ahead for the staged sources: bounded by the chunk
-// window (a segment word is reachable from chunk or chunk_next up to LPS
-// segments ahead of the current one).
-template <int LPS>
+// Source look-ahead.  The busy instances (more than 6 pair-polar values per
+// lane) stage the sources of the segments ahead in a shared-memory ring by
+// asynchronous copies, which hold no registers: up to three segments ahead,
+// bounded by the chunk window (a segment word is reachable from chunk or
+// chunk_next up to LPS segments ahead).  The light instances, whose loop is
+// short, keep the next segment's sources in registers (staging costs them
+// more instructions than it hides: 51x51 / 7 groups 2.12 -> 3.12 ms).
+template <int PH, int LPS, int PS>
 struct SweepRing {
-  static constexpr int ahead = LPS < 3 ? LPS : 3;
+  static constexpr bool staged = PH * PS > 6;
+  static constexpr int ahead = !staged ? 0 : (LPS < 3 ? LPS : 3);
 };
 
 __device__ __forceinline__ void cp_async8(void* smem_dst, const void* src) {
@@ -119,12 +124,12 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-// Registers available per thread: the busy instances keep 5 blocks of 128
+// Registers available per thread: the busy instances keep 6 blocks of 128
 // threads resident per SM (4 at 18 pair-polar values per lane), the small
 // ones 8; one-polar (3D) instances with 3 or more pairs, whose shared-memory
 // tallies need a few registers more, 6.
 #ifndef MOC_SWEEP_BIG_MIN_BLOCKS
-#define MOC_SWEEP_BIG_MIN_BLOCKS 5
+#define MOC_SWEEP_BIG_MIN_BLOCKS 6
 #endif
 template <int PH, int PS>
 struct SweepOccupancy {
@@ -232,7 +237,8 @@ sweep_kernel(const SweepArgs a) {
     // lane of the stream by a shuffle from lane k % LPS.  The sources of
     // segment k + kAhead are copied into shared memory while segment k is
     // integrated.
-    constexpr int kAhead = SweepRing<LPS>::ahead;
+    constexpr bool kStaged = SweepRing<PH, LPS, PS>::staged;
+    constexpr int kAhead = SweepRing<PH, LPS, PS>::ahead;
     constexpr int kRing = kAhead + 1;
     const int2* seg = a.segs + b;
     const unsigned gmask =
@@ -284,20 +290,54 @@ sweep_kernel(const SweepArgs a) {
       }
       cp_async_commit();
     };
+    // the register path: segment k + 1's word from `chunk` and its sources
+    // in registers, loaded while segment k is integrated
+    auto word_cur = [&](int j) -> int2 {
+      int2 r;
+      r.x = __shfl_sync(gmask, chunk.x, j & (LPS - 1), LPS);
+      r.y = __shfl_sync(gmask, chunk.y, j & (LPS - 1), LPS);
+      return r;
+    };
+    auto gather = [&](float2* qq, int f, bool valid) {
+      const float2* qrow = qbase + (int64_t) f * npairs;
 #pragma unroll
-    for (int j = 0; j < kAhead; j++) stage(j);
+      for (int s = 0; s < PS; s++)
+        qq[s] = (sub + s * LPS < npairs && valid) ? __ldg(qrow + s * LPS)
+                                                  : f2(0.0f);
+    };
+    float len = 0.0f;
+    int fsr = 0, mat = 0;
+    float2 q[PS];
+    if constexpr (kStaged) {
+#pragma unroll
+      for (int j = 0; j < kAhead; j++) stage(j);
+    } else {
+      unpack(word_cur(0), len, fsr, mat);
+      gather(q, fsr, n > 0);
+    }
     for (int k = 0; k < n; k++) {
-      stage(k + kAhead);
-      float len;
-      int fsr, mat;
-      unpack(word(k), len, fsr, mat);
-      // rotate chunks once segment k + 1 leaves `chunk`
-      if (k + 1 - cb == LPS) {
-        chunk = chunk_next;
-        chunk_next = fetch(cb + 2 * LPS + sub);
-        cb += LPS;
+      float len_n = 0.0f;
+      int fsr_n = 0, mat_n = 0;
+      float2 qn[PS];
+      if constexpr (kStaged) {
+        stage(k + kAhead);
+        unpack(word(k), len, fsr, mat);
+        // rotate chunks once segment k + 1 leaves `chunk`
+        if (k + 1 - cb == LPS) {
+          chunk = chunk_next;
+          chunk_next = fetch(cb + 2 * LPS + sub);
+          cb += LPS;
+        }
+        cp_async_wait<kAhead>();   // segment k's sources have landed
+      } else {
+        if (k + 1 - cb == LPS) {
+          chunk = chunk_next;
+          chunk_next = fetch(cb + 2 * LPS + sub);
+          cb += LPS;
+        }
+        unpack(word_cur(k + 1), len_n, fsr_n, mat_n);
+        gather(qn, fsr_n, k + 1 < n);
       }
-      cp_async_wait<kAhead>();   // segment k's sources have landed
 
       const float2* st =
           reinterpret_cast<const float2*>(s_st + mat * ld) + sub;
@@ -309,7 +349,7 @@ sweep_kernel(const SweepArgs a) {
 #pragma unroll
       for (int s = 0; s < PS; s++) {
         if (sub + s * LPS < npairs) {
-          const float2 qs = *slot(k, s);
+          const float2 qs = kStaged ? *slot(k, s) : q[s];
           const float2 tau = __fmul2_rn(st[s * LPS], len2);
           float2 tally = f2(0.0f);
 #pragma unroll
@@ -334,6 +374,13 @@ sweep_kernel(const SweepArgs a) {
             atomicAdd(ph + s * LPS, tally);
           }
         }
+      }
+      if constexpr (!kStaged) {
+        len = len_n;
+        fsr = fsr_n;
+        mat = mat_n;
+#pragma unroll
+        for (int s = 0; s < PS; s++) q[s] = qn[s];
       }
     }
 
@@ -393,7 +440,10 @@ void launch_sweep_instance(const SweepArgs& a, cudaStream_t stream) {
   const size_t smem =
       sizeof(float) * ((size_t) (a.num_materials + a.hot_count) * a.ld +
                        (EXPK == kExpTable ? 2 * kExpTableSize : 0)) +
-      sizeof(float2) * (SweepRing<LPS>::ahead + 1) * PS * kSweepThreads;
+      (SweepRing<PH, LPS, PS>::staged
+           ? sizeof(float2) * (SweepRing<PH, LPS, PS>::ahead + 1) * PS *
+                 kSweepThreads
+           : 0);
   auto kern = sweep_kernel<PH, LPS, PS, EXPK, POOL>;
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
