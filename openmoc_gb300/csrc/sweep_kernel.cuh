@@ -330,10 +330,10 @@ sweep_kernel(const SweepArgs a) {
         }
         cp_async_wait<kAhead>();   // segment k's sources have landed
       } else {
-        if (k + 1 - cb == LPS) {
+        // segment k + 1 opens a chunk: rotate
+        if (((k + 1) & (LPS - 1)) == 0) {
           chunk = chunk_next;
-          chunk_next = fetch(cb + 2 * LPS + sub);
-          cb += LPS;
+          chunk_next = fetch(k + 1 + LPS + sub);
         }
         unpack(word_cur(k + 1), len_n, fsr_n, mat_n);
         gather(qn, fsr_n, k + 1 < n);
