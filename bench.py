@@ -37,7 +37,7 @@ FLOPS_PER_INTEGRATION_3D = 28  # 3D: no 1/sin(theta) scaling
 # of this workload, from one ncu capture per sweep shape (lanes per track
 # direction, group pairs per lane, exponential kind); the summaries are under
 # profiles/ (sweep_kernel_17x17_70g.txt).
-SWEEP_DRAM_BYTES = {(8, 5, 1): 50_847_744 + 1_447_424}
+SWEEP_DRAM_BYTES = {(8, 5, 1): 50_853_120 + 1_411_328}
 
 
 def env_rank():
