@@ -681,26 +681,6 @@ int moc_upload_tracks(moc_ctx* c, const float* seg_len, const int32_t* seg_fsr,
                 "next-track index out of range on track " +
                     std::to_string(t));
   }
-  // trailing FSR ids crossed by at least 0.2 % of all segments each
-  std::vector<int64_t> per_fsr(R, 0);
-  for (int64_t s = 0; s < S; s++)
-    if (seg_fsr[s] >= 0 && seg_fsr[s] < R) per_fsr[seg_fsr[s]]++;
-  c->hot_count = 0;
-  while (c->hot_count < moc::kMaxHotFsrs && c->hot_count < R &&
-         per_fsr[R - 1 - c->hot_count] * 500 >= S && S > 0)
-    c->hot_count++;
-  c->hot_base = (int) (R - c->hot_count);
-  std::vector<int2> packed(S);
-  for (int64_t s = 0; s < S; s++) {
-    MOC_CHECK(seg_fsr[s] >= 0 && seg_fsr[s] < R, MOC_ERR_ARG,
-              "segment FSR id out of range at segment " + std::to_string(s));
-    MOC_CHECK(std::isfinite(seg_len[s]) && seg_len[s] >= 0.0f, MOC_ERR_ARG,
-              "bad segment length at segment " + std::to_string(s));
-    int2 v;
-    std::memcpy(&v.x, &seg_len[s], 4);
-    v.y = seg_fsr[s];
-    packed[s] = v;
-  }
   // longest tracks first (stable, so equal lengths keep UID order)
   std::vector<int32_t> order(T);
   std::iota(order.begin(), order.end(), 0);
@@ -717,13 +697,59 @@ int moc_upload_tracks(moc_ctx* c, const float* seg_len, const int32_t* seg_fsr,
   dfree(c->next);
   dfree(c->flags);
   MOC_TRY(dalloc(&c->segs, S));
+  // segments: raw lengths and FSR ids up, packed and checked on the device
+  {
+    float* d_len = nullptr;
+    int32_t* d_fsr = nullptr;
+    unsigned long long* d_chk = nullptr;   // [0] first bad index, [1..] tail
+    int st = dalloc(&d_len, S);
+    if (!st) st = dalloc(&d_fsr, S);
+    if (!st) st = dalloc(&d_chk, 1 + moc::kMaxHotFsrs);
+    std::vector<unsigned long long> chk(1 + moc::kMaxHotFsrs, 0);
+    chk[0] = ~0ull;
+    cudaError_t e = cudaSuccess;
+    if (!st && S > 0) {
+      e = cudaMemcpy(d_len, seg_len, 4 * S, cudaMemcpyHostToDevice);
+      if (e == cudaSuccess)
+        e = cudaMemcpy(d_fsr, seg_fsr, 4 * S, cudaMemcpyHostToDevice);
+      if (e == cudaSuccess)
+        e = cudaMemcpy(d_chk, chk.data(), 8 * chk.size(), cudaMemcpyHostToDevice);
+      if (e == cudaSuccess) {
+        moc::launch_pack_segments(d_len, d_fsr, c->segs, S, R, d_chk, d_chk + 1,
+                                  c->stream);
+        e = cudaStreamSynchronize(c->stream);
+      }
+      if (e == cudaSuccess)
+        e = cudaMemcpy(chk.data(), d_chk, 8 * chk.size(), cudaMemcpyDeviceToHost);
+    }
+    dfree(d_len);
+    dfree(d_fsr);
+    dfree(d_chk);
+    MOC_TRY(st);
+    MOC_CUDA(e);
+    if (chk[0] != ~0ull) {
+      const int64_t i = (int64_t) chk[0];
+      dfree(c->segs);
+      MOC_CHECK(seg_fsr[i] >= 0 && seg_fsr[i] < R, MOC_ERR_ARG,
+                "segment FSR id out of range at segment " + std::to_string(i));
+      return fail(MOC_ERR_ARG, "bad segment length at segment " +
+                                   std::to_string(i));
+    }
+    // trailing FSR ids crossed by at least 0.2 % of all segments each
+    c->hot_count = 0;
+    while (c->hot_count < moc::kMaxHotFsrs && c->hot_count < R && S > 0) {
+      const int64_t r = R - 1 - c->hot_count;          // FSR id
+      const int64_t slot = r - (R - moc::kMaxHotFsrs);  // its tail counter
+      if (slot < 0 || chk[1 + slot] * 500 < (unsigned long long) S) break;
+      c->hot_count++;
+    }
+    c->hot_base = (int) (R - c->hot_count);
+  }
   MOC_TRY(dalloc(&c->seg_off, T + 1));
   MOC_TRY(dalloc(&c->order, T));
   MOC_TRY(dalloc(&c->track_ang, T));
   MOC_TRY(dalloc(&c->next, 2 * T));
   MOC_TRY(dalloc(&c->flags, T));
-  MOC_CUDA(cudaMemcpy(c->segs, packed.data(), sizeof(int2) * S,
-                      cudaMemcpyHostToDevice));
   MOC_CUDA(cudaMemcpy(c->seg_off, seg_off, sizeof(int64_t) * (T + 1),
                       cudaMemcpyHostToDevice));
   MOC_CUDA(cudaMemcpy(c->order, order.data(), sizeof(int32_t) * T,

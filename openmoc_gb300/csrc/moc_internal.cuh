@@ -156,6 +156,12 @@ void launch_attenuation(int kind, const float* x, float* g, int64_t n,
 // (valid when num_fsrs < 2^24 and num_materials <= 256); idempotent.
 void launch_pack_materials(int2* segs, int64_t num_segments,
                            const int32_t* fsr_mat, cudaStream_t stream);
+// Packs and checks uploaded segments on the device (*bad = the first bad
+// index, or left as it was) and counts the segments of the last
+// kMaxHotFsrs FSR ids into tail[kMaxHotFsrs] (tail[i]: FSR R - kMaxHotFsrs + i).
+void launch_pack_segments(const float* len, const int32_t* fsr, int2* out,
+                          int64_t S, int64_t R, unsigned long long* bad,
+                          unsigned long long* tail, cudaStream_t stream);
 
 // ---- launchers (solver_kernels.cu) ---------------------------------------
 // iteration < 0 reads the device iteration counter; fused also zeroes phi

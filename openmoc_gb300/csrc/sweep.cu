@@ -20,6 +20,42 @@ __global__ void pack_materials_kernel(int2* segs, int64_t n,
   }
 }
 
+// Packs (length, FSR id) pairs into segment words, checking each (FSR id in
+// [0, R), length finite and non-negative): the first bad index goes to
+// *bad.  Counts the segments of the last kMaxHotFsrs FSR ids (block
+// counters in shared memory, one global add per block and counter).
+__global__ void pack_segments_kernel(const float* len, const int32_t* fsr,
+                                     int2* out, int64_t S, int64_t R,
+                                     unsigned long long* bad,
+                                     unsigned long long* tail) {
+  __shared__ unsigned int cnt[kMaxHotFsrs];
+  if (threadIdx.x < kMaxHotFsrs) cnt[threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t tail0 = R - kMaxHotFsrs;
+  for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < S;
+       i += (int64_t) gridDim.x * blockDim.x) {
+    const float l = len[i];
+    const int32_t f = fsr[i];
+    if (!(f >= 0 && f < R && isfinite(l) && l >= 0.0f))
+      atomicMin(bad, (unsigned long long) i);
+    out[i] = make_int2(__float_as_int(l), f);
+    if (f >= tail0 && f < R) atomicAdd(&cnt[f - tail0], 1u);
+  }
+  __syncthreads();
+  if (threadIdx.x < kMaxHotFsrs && cnt[threadIdx.x])
+    atomicAdd(&tail[threadIdx.x], (unsigned long long) cnt[threadIdx.x]);
+}
+
+void launch_pack_segments(const float* len, const int32_t* fsr, int2* out,
+                          int64_t S, int64_t R, unsigned long long* bad,
+                          unsigned long long* tail, cudaStream_t stream) {
+  if (S == 0) return;
+  int64_t blocks = (S + 255) / 256;
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  pack_segments_kernel<<<(unsigned) blocks, 256, 0, stream>>>(len, fsr, out, S,
+                                                              R, bad, tail);
+}
+
 void launch_pack_materials(int2* segs, int64_t num_segments,
                            const int32_t* fsr_mat, cudaStream_t stream) {
   if (num_segments == 0) return;

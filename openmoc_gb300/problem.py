@@ -112,9 +112,11 @@ class Problem:
             self.fixed_sources = np.ascontiguousarray(self.fixed_sources, np.float32)
         return self
 
-    def validate(self) -> None:
+    def validate(self, deep: bool = True) -> None:
         """Host-side checks of every packed index, raising ``ValueError``
-        the way OpenMOC's ``log_printf(ERROR, ...)`` raises."""
+        the way OpenMOC's ``log_printf(ERROR, ...)`` raises.  deep=False
+        checks the array sizes and dimensions only (the C ABI checks every
+        element again on upload, the segments on the device)."""
         G, R, T, S, M = (self.num_groups, self.num_fsrs, self.num_tracks,
                          self.num_segments, self.num_materials)
         A, Ph = self.num_angles, self.num_polar_half
@@ -130,6 +132,10 @@ class Problem:
                 raise ValueError(f"{name} has {a.size} entries, expected {n}")
         if G < 1 or Ph < 1 or R < 1 or T < 1 or M < 1:
             raise ValueError("empty problem dimension")
+        if self.fixed_sources is not None and self.fixed_sources.size != R * G:
+            raise ValueError("fixed_sources must hold num_fsrs * num_groups")
+        if not deep:
+            return
         if self.seg_off[0] != 0 or self.seg_off[-1] != S:
             raise ValueError("seg_off must start at 0 and end at num_segments")
         if np.any(np.diff(self.seg_off) < 0):
