@@ -34,6 +34,7 @@
 #ifndef OPENMOC_GB300_PACK_REFERENCE_H_
 #define OPENMOC_GB300_PACK_REFERENCE_H_
 
+#include <cmath>
 #include <cstdint>
 #include <map>
 #include <stdexcept>
@@ -76,6 +77,18 @@ struct PackedProblem {
 
   /* Dense index of every Material, keyed by the Material pointer. */
   std::map<Material*, int> material_index;
+
+  /* Linear-source geometry (pack_linear_source; 2D only):
+   *   seg_x[S], seg_y[S]  float   segment::_starting_position relative to
+   *                               the FSR centroid (RecenterSegments,
+   *                               src/TrackTraversingAlgorithms.cpp:1320-1331)
+   *   ang_dir[A][2]       double  cos(phi), sin(phi) of the tracks of each
+   *                               azimuthal index (Track::getPhi)
+   *   ang_wgt[A]          double  Quadrature::getAzimSpacing * getAzimWeight
+   *   pol_sin[A][Ph], pol_wgt[A][Ph]  double  getSinTheta, getPolarWeight
+   *   centroid[R][2]      double  Geometry::getFSRCentroid (for reporting) */
+  std::vector<float> seg_x, seg_y;
+  std::vector<double> ang_dir, ang_wgt, pol_sin, pol_wgt, centroid;
 };
 
 inline bool transfers_flux(boundaryType bc) {
@@ -195,6 +208,65 @@ inline void pack_tracks(TrackGenerator* tg, PackedProblem& out) {
         out.inv_sin[a * out.num_polar_half + p] =
             (float) quad->getInvSinThetaInline(a, p);
       }
+  }
+}
+
+/**
+ * Packs what the linear-source sweep reads beyond the flat-source arrays
+ * (CPULSSolver::tallyLSScalarFlux, src/CPULSSolver.cpp:542-741, and the
+ * LinearExpansionGenerator, src/TrackTraversingAlgorithms.cpp:470-830).
+ * Call after pack_tracks, once the segments have been re-centred on the FSR
+ * centroids (TrackGenerator::generateFSRCentroids, which
+ * Solver::initializeFSRs runs, src/Solver.cpp:865).  2D tracks only.
+ */
+inline void pack_linear_source(TrackGenerator* tg, PackedProblem& out) {
+  if (out.solve_3d)
+    throw std::runtime_error("linear-source packing takes 2D tracks only");
+  Geometry* geo = tg->getGeometry();
+  if (!geo->containsFSRCentroids())
+    throw std::runtime_error("FSR centroids have not been generated");
+  Quadrature* quad = tg->getQuadrature();
+  const int A = out.num_angles, Ph = out.num_polar_half;
+  const long T = out.num_tracks, R = geo->getNumFSRs();
+  Track** tracks = tg->get2DTracksArray();
+  out.seg_x.resize(out.num_segments);
+  out.seg_y.resize(out.num_segments);
+  out.ang_dir.assign(2 * (size_t) A, 0.0);
+  std::vector<char> seen(A, 0);
+  for (long t = 0; t < T; t++) {
+    segment* segs = tracks[t]->getSegments();
+    const long base = out.seg_off[t];
+    const int n = tracks[t]->getNumSegments();
+    for (int k = 0; k < n; k++) {
+      out.seg_x[base + k] = (float) segs[k]._starting_position[0];
+      out.seg_y[base + k] = (float) segs[k]._starting_position[1];
+    }
+    const int a = out.track_ang[t];
+    const double phi = tracks[t]->getPhi();
+    if (!seen[a]) {
+      seen[a] = 1;
+      out.ang_dir[2 * a] = std::cos(phi);
+      out.ang_dir[2 * a + 1] = std::sin(phi);
+    } else if (out.ang_dir[2 * a] != std::cos(phi) ||
+               out.ang_dir[2 * a + 1] != std::sin(phi)) {
+      throw std::runtime_error("tracks of one azimuthal index differ in phi");
+    }
+  }
+  out.ang_wgt.resize(A);
+  out.pol_sin.resize((size_t) A * Ph);
+  out.pol_wgt.resize((size_t) A * Ph);
+  for (int a = 0; a < A; a++) {
+    out.ang_wgt[a] = quad->getAzimSpacing(a) * quad->getAzimWeight(a);
+    for (int p = 0; p < Ph; p++) {
+      out.pol_sin[(size_t) a * Ph + p] = quad->getSinTheta(a, p);
+      out.pol_wgt[(size_t) a * Ph + p] = quad->getPolarWeight(a, p);
+    }
+  }
+  out.centroid.resize(2 * (size_t) R);
+  for (long r = 0; r < R; r++) {
+    Point* c = geo->getFSRCentroid(r);
+    out.centroid[2 * r] = c->getX();
+    out.centroid[2 * r + 1] = c->getY();
   }
 }
 

@@ -499,3 +499,459 @@ int oracle_compute_flux(const oracle_problem* p, oracle_state* s,
 }
 
 int oracle_real_size(void) { return (int) sizeof(real); }
+
+/* ================================================================ linear
+ * source.  CPULSSolver (src/CPULSSolver.cpp) restated for 2D tracks: the
+ * same source iteration with flux and source moments along x and y about
+ * each FSR centroid.  Layouts follow the reference: moments [R][3][G] (x, y,
+ * z; z stays 0 in 2D), src/CPULSSolver.h:20-23; the linear expansion matrix
+ * inverse [R][3] (xx, yy, xy) and the source constants [R][3][G].
+ *
+ * The exponential terms are evaluated in double from their definitions
+ * (series below x = 1, closed forms above), where the reference uses
+ * rational approximations (src/exponentials.h:101-323, accurate to 2e-7 and
+ * 1e-6), then rounded to ORACLE_REAL. */
+
+typedef struct {
+  const float* seg_x;     /* [S] segment start relative to its FSR centroid */
+  const float* seg_y;     /* [S] */
+  const double* ang_dir;  /* [A][2] cos(phi), sin(phi) */
+  const double* ang_wgt;  /* [A] azimuthal spacing x azimuthal weight */
+  const double* pol_sin;  /* [A][Ph] sin(theta_p) */
+  const double* pol_wgt;  /* [A][Ph] polar weight */
+} oracle_ls_geometry;
+
+typedef struct {
+  double* ilem;           /* [R][3] */
+  real* src_const;        /* [R][3][G] */
+  real* mom;              /* [R][3][G] flux moments */
+  real* red_xyz;          /* [R][3][G] reduced source moments */
+  const real* fixed_xy;   /* [R][2][G] fixed source moments, or NULL */
+  int32_t negative_allowed;
+  int32_t num_flat;       /* FSRs whose expansion matrix is singular */
+} oracle_ls_state;
+
+#define MIN_DET 1E-10     /* src/constants.h:70 */
+
+/* G(x) = (x - 1 + exp(-x)) / x^2 = sum_k (-x)^k / (k+2)! */
+static double exp_g(double x) {
+  if (x < 1.0) {
+    double term = 0.5, sum = 0.5;
+    for (int k = 1; k < 24; k++) {
+      term *= -x / (double) (k + 2);
+      sum += term;
+    }
+    return sum;
+  }
+  return (x + expm1(-x)) / (x * x);
+}
+
+/* G2(x) = 2/3 - (1 + 2/x) (1/x + 1/2 - (1 + 1/x)(1 - exp(-x))/x)
+ *       = sum_{m>=1} (-x)^m [(m+1)/(m+2)! - 2(m+2)/(m+3)!]
+ * (the quantity of src/exponentials.h:283-292). */
+static double exp_g2(double x) {
+  if (x < 1.0) {
+    double sum = 0.0, xm = 1.0, f2 = 2.0;   /* f2 = (m+2)!, m = 0 */
+    for (int m = 1; m < 26; m++) {
+      xm *= -x;
+      f2 *= (double) (m + 2);               /* (m+2)! */
+      double c = (double) (m + 1) / f2 - 2.0 * (double) (m + 2) /
+                                             (f2 * (double) (m + 3));
+      sum += c * xm;
+    }
+    return sum;
+  }
+  double f1 = -expm1(-x) / x;
+  return 2.0 / 3.0 - (1.0 + 2.0 / x) * (1.0 / x + 0.5 - (1.0 + 1.0 / x) * f1);
+}
+
+/* LinearExpansionGenerator::onTrack + execute for 2D tracks
+ * (src/TrackTraversingAlgorithms.cpp:543-640, :716-826): the volume
+ * moments of every FSR, their 2x2 inverse, and the source constants.
+ * Returns the number of FSRs left with a flat source (singular matrix). */
+int oracle_ls_constants(const oracle_problem* p, const oracle_ls_geometry* g,
+                        oracle_ls_state* s) {
+  const long R = p->num_fsrs;
+  const int G = p->num_groups, Ph = p->num_polar_half;
+  double* lem = (double*) calloc((size_t) R * 3, sizeof(double));
+  double* sc = (double*) calloc((size_t) R * 3 * G, sizeof(double));
+  for (long t = 0; t < p->num_tracks; t++) {
+    const int a = p->track_ang[t];
+    const double cph = g->ang_dir[2 * a], sph = g->ang_dir[2 * a + 1];
+    const double wgt = g->ang_wgt[a];
+    for (long k = p->seg_off[t]; k < p->seg_off[t + 1]; k++) {
+      const long r = p->seg_fsr[k];
+      const float* st = p->sigma_t + (long) p->fsr_mat[r] * G;
+      const double len = p->seg_len[k], vol = p->fsr_vol[r];
+      const double xc = (double) g->seg_x[k] + 0.5 * len * cph;
+      const double yc = (double) g->seg_y[k] + 0.5 * len * sph;
+      const double vol_impact = wgt * len / vol;
+      const double src_constant = vol_impact * len / 2.0;
+      for (int e = 0; e < G; e++) {
+        double c0 = vol_impact * xc * xc, c1 = vol_impact * yc * yc;
+        double c2 = vol_impact * xc * yc;
+        const double tau = len * (double) st[e];
+        for (int pp = 0; pp < Ph; pp++) {
+          const double sn = g->pol_sin[a * Ph + pp];
+          const double g2 = len * exp_g2(tau / sn) * src_constant * 2.0 *
+                            g->pol_wgt[a * Ph + pp] * sn;
+          c0 += cph * cph * g2;
+          c1 += sph * sph * g2;
+          c2 += sph * cph * g2;
+        }
+        sc[(r * 3 + 0) * G + e] += c0;
+        sc[(r * 3 + 1) * G + e] += c1;
+        sc[(r * 3 + 2) * G + e] += c2;
+      }
+      lem[r * 3 + 0] += wgt * len / vol * (xc * xc + cph * cph * len * len / 12.0);
+      lem[r * 3 + 1] += wgt * len / vol * (yc * yc + sph * sph * len * len / 12.0);
+      lem[r * 3 + 2] += wgt * len / vol * (xc * yc + sph * cph * len * len / 12.0);
+    }
+  }
+  int flat = 0;
+  for (long r = 0; r < R; r++) {
+    const double det = lem[r * 3] * lem[r * 3 + 1] - lem[r * 3 + 2] * lem[r * 3 + 2];
+    if (fabs(det) < MIN_DET) {
+      s->ilem[r * 3] = s->ilem[r * 3 + 1] = s->ilem[r * 3 + 2] = 0.0;
+      flat++;
+    } else {
+      s->ilem[r * 3 + 0] = lem[r * 3 + 1] / det;
+      s->ilem[r * 3 + 1] = lem[r * 3 + 0] / det;
+      s->ilem[r * 3 + 2] = -lem[r * 3 + 2] / det;
+    }
+  }
+  for (long i = 0; i < R * 3 * G; i++) s->src_const[i] = (real) sc[i];
+  free(lem);
+  free(sc);
+  s->num_flat = flat;
+  return flat;
+}
+
+/* CPULSSolver::flattenFSRFluxes, src/CPULSSolver.cpp:343-353 */
+void oracle_ls_flatten(const oracle_problem* p, oracle_state* s,
+                       oracle_ls_state* ls, double value) {
+  oracle_flatten(p, s, value);
+  memset(ls->mom, 0, sizeof(real) * p->num_fsrs * 3 * p->num_groups);
+}
+
+/* CPULSSolver::normalizeFluxes, src/CPULSSolver.cpp:362-378 */
+double oracle_ls_normalize(const oracle_problem* p, oracle_state* s,
+                           oracle_ls_state* ls) {
+  double f = oracle_normalize(p, s);
+  long n = p->num_fsrs * 3 * p->num_groups;
+  for (long i = 0; i < n; i++) ls->mom[i] *= f;
+  return f;
+}
+
+/* CPULSSolver::computeFSRSources (2D branch), src/CPULSSolver.cpp:386-527:
+ * the flat source of CPUSolver, then the x and y source moments through the
+ * inverse expansion matrix.  Returns the negative flat sources found. */
+long oracle_ls_compute_sources(const oracle_problem* p, oracle_state* s,
+                               oracle_ls_state* ls, int iteration) {
+  long neg = oracle_compute_sources(p, s, iteration, ls->negative_allowed);
+  const long R = p->num_fsrs;
+  const int G = p->num_groups;
+  set_threads(p);
+#pragma omp parallel for schedule(static)
+  for (long r = 0; r < R; r++) {
+    real buf[1024];
+    const int m = p->fsr_mat[r];
+    const float* ss = p->sigma_s + (long) m * G * G;
+    const float* nf = p->nu_sigma_f + (long) m * G;
+    const float* ch = p->chi + (long) m * G;
+    const int fissile = mat_fissile(p, m);
+    const double* il = ls->ilem + r * 3;
+    const real* mx = ls->mom + (r * 3 + 0) * G;
+    const real* my = ls->mom + (r * 3 + 1) * G;
+    for (int gd = 0; gd < G; gd++) {
+      double fis_x = 0.0, fis_y = 0.0;
+      if (fissile) {
+        for (int g = 0; g < G; g++) buf[g] = ((real) ch[gd] * (real) nf[g]) * mx[g];
+        fis_x = pairwise_sum_r(buf, G) / s->keff;
+        for (int g = 0; g < G; g++) buf[g] = ((real) ch[gd] * (real) nf[g]) * my[g];
+        fis_y = pairwise_sum_r(buf, G) / s->keff;
+      }
+      for (int g = 0; g < G; g++) buf[g] = (real) ss[gd * G + g] * mx[g];
+      double sca_x = pairwise_sum_r(buf, G);
+      for (int g = 0; g < G; g++) buf[g] = (real) ss[gd * G + g] * my[g];
+      double sca_y = pairwise_sum_r(buf, G);
+      real src_x = (real) (sca_x + fis_x), src_y = (real) (sca_y + fis_y);
+      if (ls->fixed_xy) {
+        src_x += ls->fixed_xy[(r * 2 + 0) * G + gd];
+        src_y += ls->fixed_xy[(r * 2 + 1) * G + gd];
+      }
+      real* rx = ls->red_xyz + (r * 3 + 0) * G + gd;
+      real* ry = ls->red_xyz + (r * 3 + 1) * G + gd;
+      if (ls->negative_allowed || s->reduced[r * G + gd] > 10 * FLUX_EPSILON ||
+          iteration > 29) {
+        *rx = (real) (ONE_OVER_FOUR_PI / 2 * (il[0] * src_x + il[2] * src_y));
+        *ry = (real) (ONE_OVER_FOUR_PI / 2 * (il[2] * src_x + il[1] * src_y));
+      } else {
+        *rx = 0;
+        *ry = 0;
+      }
+    }
+  }
+  return neg;
+}
+
+/* Linear-source attenuation along one segment, CPULSSolver::tallyLSScalarFlux
+ * 2D branch (src/CPULSSolver.cpp:653-741); pos is the segment's start in the
+ * direction of travel, dir the travel direction. */
+static void ls_tally_segment(const oracle_problem* p, const oracle_state* s,
+                             const oracle_ls_state* ls, long fsr, real length,
+                             int mat, int ang, const real pos[2],
+                             const real dir[2], real* buf, real* bx, real* by,
+                             float* psi) {
+  const int G = p->num_groups;
+  const int Ph = p->num_polar_half;
+  const float* st = p->sigma_t + (long) mat * G;
+  const real cx = 2 * pos[0] + length * dir[0];
+  const real cy = 2 * pos[1] + length * dir[1];
+  const real* qx = ls->red_xyz + (fsr * 3 + 0) * G;
+  const real* qy = ls->red_xyz + (fsr * 3 + 1) * G;
+  for (int pp = 0; pp < Ph; pp++) {
+    const real wgt = (real) p->weights[ang * Ph + pp];
+    const real inv_sin = (real) p->inv_sin[ang * Ph + pp];
+    for (int g = 0; g < G; g++) {
+      const int pe = pp * G + g;
+      const real tau = (real) st[g] * length;
+      double x = (double) (tau * inv_sin);
+      if (x < 1e-8) x = 1e-8;
+      const double gg = exp_g(x);
+      const double f1 = (1.0 - x * gg) * (double) inv_sin;
+      const double gs = gg * (double) inv_sin;
+      const real F1 = (real) f1, F2 = (real) (2.0 * gs - f1);
+      real H = (real) (f1 - gs);
+      const real src_flat = s->reduced[fsr * G + g] + qx[g] * cx + qy[g] * cy;
+      const real src_lin = dir[0] * qx[g] + dir[1] * qy[g];
+      H *= wgt * tau * length * (real) psi[pe];
+      real delta = (tau * (real) psi[pe] - length * src_flat) * F1 -
+                   length * length * src_lin * F2;
+      psi[pe] = (float) ((real) psi[pe] - delta);
+      delta *= wgt;
+      buf[g] += delta;
+      bx[g] += H * dir[0] + delta * pos[0];
+      by[g] += H * dir[1] + delta * pos[1];
+    }
+  }
+}
+
+/* CPULSSolver::accumulateLinearFluxContribution, src/CPULSSolver.cpp:749-781 */
+static void ls_flush(const oracle_problem* p, oracle_state* s,
+                     oracle_ls_state* ls, long fsr, real* buf, real* bx,
+                     real* by, void* locks) {
+  const int G = p->num_groups;
+#ifdef _OPENMP
+  omp_set_lock(&((omp_lock_t*) locks)[fsr]);
+#else
+  (void) locks;
+#endif
+  for (int g = 0; g < G; g++) {
+    s->phi[fsr * G + g] += buf[g];
+    ls->mom[(fsr * 3 + 0) * G + g] += bx[g];
+    ls->mom[(fsr * 3 + 1) * G + g] += by[g];
+  }
+#ifdef _OPENMP
+  omp_unset_lock(&((omp_lock_t*) locks)[fsr]);
+#endif
+  memset(buf, 0, sizeof(real) * G);
+  memset(bx, 0, sizeof(real) * G);
+  memset(by, 0, sizeof(real) * G);
+}
+
+/* CPUSolver::transportSweep with the linear-source tally (2D): as
+ * oracle_sweep, the direction of a track from its azimuthal angle
+ * (src/TrackTraversingAlgorithms.cpp:913-926), reversed for the backward
+ * pass, which starts each segment at its far end. */
+void oracle_ls_sweep(const oracle_problem* p, const oracle_ls_geometry* geo,
+                     oracle_state* s, oracle_ls_state* ls) {
+  const long R = p->num_fsrs;
+  const int G = p->num_groups;
+  const long T = p->num_tracks;
+  const int F = fluxes_per_track(p);
+  memset(s->phi, 0, sizeof(real) * R * G);
+  memset(ls->mom, 0, sizeof(real) * R * 3 * G);
+  memcpy(s->boundary, s->start, sizeof(float) * 2 * T * F);
+  set_threads(p);
+  void* locks = NULL;
+#ifdef _OPENMP
+  omp_lock_t* lk = (omp_lock_t*) malloc(sizeof(omp_lock_t) * R);
+  for (long r = 0; r < R; r++) omp_init_lock(&lk[r]);
+  locks = lk;
+#endif
+#pragma omp parallel
+  {
+    real* buf = (real*) calloc(3 * (size_t) G, sizeof(real));
+    real* bx = buf + G;
+    real* by = buf + 2 * G;
+#pragma omp for schedule(dynamic)
+    for (long t = 0; t < T; t++) {
+      const long b = p->seg_off[t];
+      const int n = (int) (p->seg_off[t + 1] - b);
+      const int ang = p->track_ang[t];
+      real dir[2] = {(real) geo->ang_dir[2 * ang], (real) geo->ang_dir[2 * ang + 1]};
+      float* psi = s->boundary + (t * 2) * (long) F;
+      for (int k = 0; k < n; k++) {
+        const long fsr = p->seg_fsr[b + k];
+        const real pos[2] = {(real) geo->seg_x[b + k], (real) geo->seg_y[b + k]};
+        ls_tally_segment(p, s, ls, fsr, (real) p->seg_len[b + k],
+                         p->fsr_mat[fsr], ang, pos, dir, buf, bx, by, psi);
+        if (k < n - 1 && fsr != p->seg_fsr[b + k + 1])
+          ls_flush(p, s, ls, fsr, buf, bx, by, locks);
+      }
+      transfer(p, s, t, 1, psi);
+      const real fdir[2] = {dir[0], dir[1]};
+      dir[0] = -dir[0];
+      dir[1] = -dir[1];
+      psi = s->boundary + (t * 2 + 1) * (long) F;
+      for (int k = n - 1; k >= 0; k--) {
+        const long fsr = p->seg_fsr[b + k];
+        const real len = (real) p->seg_len[b + k];
+        const real pos[2] = {(real) geo->seg_x[b + k] + fdir[0] * len,
+                             (real) geo->seg_y[b + k] + fdir[1] * len};
+        ls_tally_segment(p, s, ls, fsr, len, p->fsr_mat[fsr], ang, pos, dir,
+                         buf, bx, by, psi);
+        if (k == 0 || fsr != p->seg_fsr[b + k - 1])
+          ls_flush(p, s, ls, fsr, buf, bx, by, locks);
+      }
+      transfer(p, s, t, 0, psi);
+    }
+    free(buf);
+  }
+#ifdef _OPENMP
+  for (long r = 0; r < R; r++) omp_destroy_lock(&lk[r]);
+  free(lk);
+#endif
+}
+
+/* CPULSSolver::addSourceToScalarFlux (2D), src/CPULSSolver.cpp:787-882 */
+long oracle_ls_add_source(const oracle_problem* p, oracle_state* s,
+                          oracle_ls_state* ls) {
+  const long R = p->num_fsrs;
+  const int G = p->num_groups;
+  long neg = 0;
+  set_threads(p);
+#pragma omp parallel for schedule(static) reduction(+:neg)
+  for (long r = 0; r < R; r++) {
+    real vol = (real) p->fsr_vol[r];
+    if (vol < (real) ZERO_VOLUME) vol = (real) 1e30;
+    const float* st = p->sigma_t + (long) p->fsr_mat[r] * G;
+    const real* sc = ls->src_const + r * 3 * G;
+    for (int e = 0; e < G; e++) {
+      const real flux_const = (real) (FOUR_PI * 2);
+      const real qx = ls->red_xyz[(r * 3 + 0) * G + e];
+      const real qy = ls->red_xyz[(r * 3 + 1) * G + e];
+      real v = s->phi[r * G + e];
+      v /= vol;
+      v += (real) FOUR_PI * s->reduced[r * G + e];
+      v /= (real) st[e];
+      real mx = ls->mom[(r * 3 + 0) * G + e];
+      mx /= vol;
+      mx += flux_const * qx * sc[e];
+      mx += flux_const * qy * sc[2 * G + e];
+      real my = ls->mom[(r * 3 + 1) * G + e];
+      my /= vol;
+      my += flux_const * qx * sc[2 * G + e];
+      my += flux_const * qy * sc[G + e];
+      mx /= (real) st[e];
+      my /= (real) st[e];
+      if (v < (real) 0 && !ls->negative_allowed) {
+        neg++;
+        real old = s->phi_old[r * G + e];
+        v = old > FLUX_EPSILON ? old : FLUX_EPSILON;
+        mx = 0;
+        my = 0;
+      }
+      s->phi[r * G + e] = v;
+      ls->mom[(r * 3 + 0) * G + e] = mx;
+      ls->mom[(r * 3 + 1) * G + e] = my;
+    }
+  }
+  return neg;
+}
+
+/* Solver::computeEigenvalue with the linear-source hooks. */
+int oracle_ls_compute_eigenvalue(const oracle_problem* p,
+                                 const oracle_ls_geometry* geo,
+                                 oracle_state* s, oracle_ls_state* ls,
+                                 int max_iters, int res_type, double threshold,
+                                 double* residual_out) {
+  s->keff = 1.0;
+  oracle_ls_constants(p, geo, ls);
+  oracle_zero_track_fluxes(p, s);
+  oracle_ls_flatten(p, s, ls, 1.0);
+  oracle_ls_normalize(p, s, ls);
+  oracle_store(p, s);
+  double k_prev = s->keff;
+  double residual = 0.0;
+  int iters = 0;
+  for (int i = 0; i < max_iters; i++) {
+    oracle_ls_compute_sources(p, s, ls, i);
+    oracle_ls_sweep(p, geo, s, ls);
+    oracle_ls_add_source(p, s, ls);
+    oracle_compute_keff(p, s);
+    oracle_ls_normalize(p, s, ls);
+    residual = oracle_residual(p, s, res_type);
+    int dk = (int) (1e5 * (s->keff - k_prev));
+    k_prev = s->keff;
+    oracle_store(p, s);
+    iters++;
+    if (residual < threshold && abs(dk) < 1) break;
+  }
+  if (residual_out) *residual_out = residual;
+  return iters;
+}
+
+/* Solver::computeSource with the linear-source hooks. */
+int oracle_ls_compute_source(const oracle_problem* p,
+                             const oracle_ls_geometry* geo, oracle_state* s,
+                             oracle_ls_state* ls, int max_iters, double k_eff,
+                             int res_type, double threshold,
+                             double* residual_out) {
+  s->keff = k_eff;
+  oracle_ls_constants(p, geo, ls);
+  oracle_zero_track_fluxes(p, s);
+  oracle_ls_flatten(p, s, ls, 1.0);
+  oracle_store(p, s);
+  double residual = 0.0;
+  for (int i = 0; i < max_iters; i++) {
+    oracle_ls_compute_sources(p, s, ls, i);
+    oracle_ls_sweep(p, geo, s, ls);
+    oracle_ls_add_source(p, s, ls);
+    residual = oracle_residual(p, s, res_type);
+    oracle_store(p, s);
+    if (i > 1 && residual < threshold) {
+      if (residual_out) *residual_out = residual;
+      return i;
+    }
+  }
+  if (residual_out) *residual_out = residual;
+  return max_iters;
+}
+
+/* Solver::computeFlux (only the fixed source) with the linear-source hooks. */
+int oracle_ls_compute_flux(const oracle_problem* p,
+                           const oracle_ls_geometry* geo, oracle_state* s,
+                           oracle_ls_state* ls, int max_iters,
+                           double threshold, double* residual_out) {
+  s->keff = 1.0;
+  oracle_ls_constants(p, geo, ls);
+  oracle_zero_track_fluxes(p, s);
+  oracle_ls_flatten(p, s, ls, 0.0);
+  oracle_store(p, s);
+  oracle_ls_compute_sources(p, s, ls, 0);
+  double residual = 0.0;
+  for (int i = 0; i < max_iters; i++) {
+    oracle_ls_sweep(p, geo, s, ls);
+    oracle_ls_add_source(p, s, ls);
+    residual = oracle_residual(p, s, RES_SCALAR_FLUX);
+    oracle_store(p, s);
+    if (i > 1 && residual < threshold) {
+      if (residual_out) *residual_out = residual;
+      return i;
+    }
+  }
+  if (residual_out) *residual_out = residual;
+  return max_iters;
+}

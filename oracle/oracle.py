@@ -43,6 +43,19 @@ class _State(C.Structure):
     ]
 
 
+class _LSGeometry(C.Structure):
+    _fields_ = [("seg_x", C.c_void_p), ("seg_y", C.c_void_p),
+                ("ang_dir", C.c_void_p), ("ang_wgt", C.c_void_p),
+                ("pol_sin", C.c_void_p), ("pol_wgt", C.c_void_p)]
+
+
+class _LSState(C.Structure):
+    _fields_ = [("ilem", C.c_void_p), ("src_const", C.c_void_p),
+                ("mom", C.c_void_p), ("red_xyz", C.c_void_p),
+                ("fixed_xy", C.c_void_p), ("negative_allowed", C.c_int32),
+                ("num_flat", C.c_int32)]
+
+
 def build() -> None:
     subprocess.check_call(["bash", os.path.join(HERE, "build.sh")])
 
@@ -80,6 +93,27 @@ def _lib(precision: str):
         lib.oracle_flatten.argtypes = [P, S, C.c_double]
         lib.oracle_zero_track_fluxes.argtypes = [P, S]
         lib.oracle_real_size.restype = C.c_int
+        LG, LS = C.POINTER(_LSGeometry), C.POINTER(_LSState)
+        lib.oracle_ls_constants.argtypes = [P, LG, LS]
+        lib.oracle_ls_constants.restype = C.c_int
+        lib.oracle_ls_flatten.argtypes = [P, S, LS, C.c_double]
+        lib.oracle_ls_normalize.argtypes = [P, S, LS]
+        lib.oracle_ls_normalize.restype = C.c_double
+        lib.oracle_ls_compute_sources.argtypes = [P, S, LS, C.c_int]
+        lib.oracle_ls_compute_sources.restype = C.c_long
+        lib.oracle_ls_sweep.argtypes = [P, LG, S, LS]
+        lib.oracle_ls_add_source.argtypes = [P, S, LS]
+        lib.oracle_ls_add_source.restype = C.c_long
+        lib.oracle_ls_compute_eigenvalue.argtypes = [P, LG, S, LS, C.c_int, C.c_int,
+                                                     C.c_double, C.POINTER(C.c_double)]
+        lib.oracle_ls_compute_eigenvalue.restype = C.c_int
+        lib.oracle_ls_compute_source.argtypes = [P, LG, S, LS, C.c_int, C.c_double,
+                                                 C.c_int, C.c_double,
+                                                 C.POINTER(C.c_double)]
+        lib.oracle_ls_compute_source.restype = C.c_int
+        lib.oracle_ls_compute_flux.argtypes = [P, LG, S, LS, C.c_int, C.c_double,
+                                               C.POINTER(C.c_double)]
+        lib.oracle_ls_compute_flux.restype = C.c_int
         _LIBS[precision] = lib
     return _LIBS[precision]
 
@@ -169,3 +203,81 @@ class Oracle:
 
     def store(self) -> None:
         self.lib.oracle_store(C.byref(self._cp), C.byref(self._cs))
+
+
+class LSOracle(Oracle):
+    """The linear-source CPU solver (CPULSSolver, 2D) over one packed problem
+    plus its linear-source geometry: ``ls`` maps seg_x, seg_y, ang_dir,
+    ang_wgt, pol_sin, pol_wgt (the arrays of include/openmoc_gb300.h's
+    moc_ls_geometry) and optionally fixed_xy ([R][2][G] fixed source
+    moments)."""
+
+    def __init__(self, problem, ls, precision: str = "f32", num_threads: int = 0,
+                 negative_fluxes_allowed: bool = False):
+        super().__init__(problem, precision, num_threads)
+        R, G = problem.num_fsrs, problem.num_groups
+        self.geo_arrays = {
+            "seg_x": np.ascontiguousarray(ls["seg_x"], np.float32),
+            "seg_y": np.ascontiguousarray(ls["seg_y"], np.float32),
+            "ang_dir": np.ascontiguousarray(ls["ang_dir"], np.float64),
+            "ang_wgt": np.ascontiguousarray(ls["ang_wgt"], np.float64),
+            "pol_sin": np.ascontiguousarray(ls["pol_sin"], np.float64),
+            "pol_wgt": np.ascontiguousarray(ls["pol_wgt"], np.float64),
+        }
+        g = self.geo_arrays
+        self._cg = _LSGeometry(_ptr(g["seg_x"]), _ptr(g["seg_y"]), _ptr(g["ang_dir"]),
+                               _ptr(g["ang_wgt"]), _ptr(g["pol_sin"]),
+                               _ptr(g["pol_wgt"]))
+        self.ilem = np.zeros(R * 3, np.float64)
+        self.src_const = np.zeros(R * 3 * G, self.real)
+        self.mom = np.zeros(R * 3 * G, self.real)
+        self.red_xyz = np.zeros(R * 3 * G, self.real)
+        fx = ls.get("fixed_xy")
+        self.fixed_xy = None if fx is None else np.ascontiguousarray(fx, self.real)
+        self._cl = _LSState(_ptr(self.ilem), _ptr(self.src_const), _ptr(self.mom),
+                            _ptr(self.red_xyz), _ptr(self.fixed_xy),
+                            1 if negative_fluxes_allowed else 0, 0)
+
+    def constants(self) -> int:
+        return self.lib.oracle_ls_constants(C.byref(self._cp), C.byref(self._cg),
+                                            C.byref(self._cl))
+
+    def compute_eigenvalue(self, max_iters=1000, res_type=FISSION_SOURCE, tol=1e-5):
+        r = C.c_double()
+        self.num_iterations = self.lib.oracle_ls_compute_eigenvalue(
+            C.byref(self._cp), C.byref(self._cg), C.byref(self._cs), C.byref(self._cl),
+            max_iters, res_type, tol, C.byref(r))
+        self.residual = r.value
+        return self.num_iterations
+
+    def compute_source(self, max_iters=1000, k_eff=1.0, res_type=TOTAL_SOURCE, tol=1e-5):
+        r = C.c_double()
+        self.num_iterations = self.lib.oracle_ls_compute_source(
+            C.byref(self._cp), C.byref(self._cg), C.byref(self._cs), C.byref(self._cl),
+            max_iters, k_eff, res_type, tol, C.byref(r))
+        self.residual = r.value
+        return self.num_iterations
+
+    def compute_flux(self, max_iters=1000, tol=1e-5):
+        r = C.c_double()
+        self.num_iterations = self.lib.oracle_ls_compute_flux(
+            C.byref(self._cp), C.byref(self._cg), C.byref(self._cs), C.byref(self._cl),
+            max_iters, tol, C.byref(r))
+        self.residual = r.value
+        return self.num_iterations
+
+    def compute_sources(self, iteration: int) -> int:
+        return self.lib.oracle_ls_compute_sources(C.byref(self._cp), C.byref(self._cs),
+                                                  C.byref(self._cl), iteration)
+
+    def sweep(self) -> None:
+        self.lib.oracle_ls_sweep(C.byref(self._cp), C.byref(self._cg), C.byref(self._cs),
+                                 C.byref(self._cl))
+
+    def add_source(self) -> int:
+        return self.lib.oracle_ls_add_source(C.byref(self._cp), C.byref(self._cs),
+                                             C.byref(self._cl))
+
+    def normalize(self) -> float:
+        return self.lib.oracle_ls_normalize(C.byref(self._cp), C.byref(self._cs),
+                                            C.byref(self._cl))

@@ -15,6 +15,11 @@ CASES = ["pin_c5g7", "pin_70g", "pin7_synth", "lat3_g2_vac", "lat2_g16"]
 SRC_CASES = ["src3_g7", "flux3_g7"]
 # Explicit 3D tracks (TrackGenerator3D with EXPLICIT_3D segments).
 CASES_3D = ["pin3d_g7"]
+# Linear-source solves (CPULSSolver): the reference's own
+# test_2d_gradient_linear_source and test_fixed_linear_source replicas, an
+# eigenvalue pin cell and a computeSource lattice.
+LS_CASES = ["grad2d_ls", "fixls_c5g7", "pin7_ls", "src3_ls"]
+LS_PROBE_CASES = ["grad2d_ls", "pin7_ls"]
 
 
 def pytest_configure(config):
@@ -24,3 +29,13 @@ def pytest_configure(config):
 def load_case(name, precision="f32"):
     from openmoc_gb300.problem import load_packed
     return load_packed(os.path.join(GOLDEN, f"{name}_{precision}"))
+
+
+def ls_arrays(arr):
+    """The linear-source geometry of a fixture (and its fixed source moments,
+    if any) under the names of the oracle and of the solver API."""
+    d = {k[3:]: arr[k] for k in ("ls_seg_x", "ls_seg_y", "ls_ang_dir",
+                                 "ls_ang_wgt", "ls_pol_sin", "ls_pol_wgt")}
+    if "fixed_source_xy" in arr:
+        d["fixed_xy"] = arr["fixed_source_xy"]
+    return d

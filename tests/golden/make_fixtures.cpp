@@ -12,7 +12,13 @@
  *     reduced sources of computeFSRSources, the raw sweep tallies and the
  *     outgoing boundary fluxes of one transportSweep, the flux after
  *     addSourceToScalarFlux, keff after computeKeff, the normalisation factor
- *     and the residual (src/CPUSolver.cpp:1860-2660).
+ *     and the residual (src/CPUSolver.cpp:1860-2660);
+ *   - linear-source cases (CPULSSolver): the re-centred segment start
+ *     positions and angle data of pack_linear_source, OpenMOC's linear
+ *     expansion matrix inverse and source constants
+ *     (src/TrackTraversingAlgorithms.cpp:470-830), the converged flux moments,
+ *     and (float build, eigenvalue cases) the same hook-by-hook probe with the
+ *     moments of every step (src/CPULSSolver.cpp:343-886).
  * Track generation runs on one thread so FSR numbering is reproducible, as
  * the reference test harness does (tests/testing_harness.py).
  */
@@ -24,6 +30,7 @@
 #include <string>
 #include <vector>
 
+#include "CPULSSolver.h"
 #include "CPUSolver.h"
 #include "Geometry.h"
 #include "TrackGenerator.h"
@@ -150,6 +157,65 @@ class ProbeSolver : public CPUSolver {
     w.sc("probe_residual_fission", computeResidual(FISSION_SOURCE));
     w.sc("probe_residual_flux", computeResidual(SCALAR_FLUX));
     w.sc("probe_residual_total", computeResidual(TOTAL_SOURCE));
+  }
+};
+
+/* ----------------------------- linear-source solver with hook access */
+class ProbeLSSolver : public CPULSSolver {
+ public:
+  explicit ProbeLSSolver(TrackGenerator* tg) : CPULSSolver(tg) {}
+
+  long nflux() const { return _num_FSRs * _num_groups; }
+  long nbound() const { return 2 * _tot_num_tracks * _fluxes_per_track; }
+  /* flux moments [R][3][G] (x, y, z), src/CPULSSolver.h:20 */
+  std::vector<float> moments() const {
+    return ProbeSolver::tof(_scalar_flux_xyz, 3 * nflux());
+  }
+  std::vector<double> lin_exp() const {
+    std::vector<double> v(_FSR_lin_exp_matrix,
+                          _FSR_lin_exp_matrix + 3 * _num_FSRs);
+    return v;
+  }
+  std::vector<double> src_constants() const {
+    std::vector<double> v(3 * nflux());
+    for (long i = 0; i < 3 * nflux(); i++) v[i] = _FSR_source_constants[i];
+    return v;
+  }
+
+  void probe(Writer& w) {
+    w.sc("probe_keff_in", _k_eff);
+    std::vector<float> v = ProbeSolver::tof(_scalar_flux, nflux());
+    w.arr("probe_phi_in", "f4", v.data(), v.size());
+    v = moments();
+    w.arr("probe_mom_in", "f4", v.data(), v.size());
+    std::vector<float> so = ProbeSolver::tof(_old_scalar_flux, nflux());
+    w.arr("probe_phi_old", "f4", so.data(), so.size());
+    computeFSRSources(100);
+    v = ProbeSolver::tof(_reduced_sources, nflux());
+    w.arr("probe_reduced_sources", "f4", v.data(), v.size());
+    v = ProbeSolver::tof(_reduced_sources_xyz, 3 * nflux());
+    w.arr("probe_reduced_xyz", "f4", v.data(), v.size());
+    w.arr("probe_start_flux_in", "f4", _start_flux, nbound());
+    transportSweep();
+    v = ProbeSolver::tof(_scalar_flux, nflux());
+    w.arr("probe_phi_sweep", "f4", v.data(), v.size());
+    v = moments();
+    w.arr("probe_mom_sweep", "f4", v.data(), v.size());
+    w.arr("probe_start_flux_out", "f4", _start_flux, nbound());
+    addSourceToScalarFlux();
+    v = ProbeSolver::tof(_scalar_flux, nflux());
+    w.arr("probe_phi_addsrc", "f4", v.data(), v.size());
+    v = moments();
+    w.arr("probe_mom_addsrc", "f4", v.data(), v.size());
+    computeKeff();
+    w.sc("probe_keff_out", _k_eff);
+    double f = normalizeFluxes();
+    w.sc("probe_norm_factor", f);
+    v = ProbeSolver::tof(_scalar_flux, nflux());
+    w.arr("probe_phi_norm", "f4", v.data(), v.size());
+    v = moments();
+    w.arr("probe_mom_norm", "f4", v.data(), v.size());
+    w.sc("probe_residual_fission", computeResidual(FISSION_SOURCE));
   }
 };
 
@@ -333,6 +399,34 @@ static Geometry* lattice_geometry(int n, Material* fuel, Material* mod,
                            bymax);
 }
 
+/* The HomInfMedInput geometry of tests/input_set.py:52-92: a 10 x 10
+ * lattice of 0.25 cm cells in a 2.5 cm box, every cell a universe holding
+ * one cell filled with `mat`.  If src_pos >= 0 that lattice position
+ * ([row from the top][column], as Lattice::setUniverses takes it) holds a
+ * universe of its own whose cell is returned in *src_cell. */
+static Geometry* hom_lattice_geometry(Material* mat, Cell** src_cell,
+                                      int src_pos, boundaryType bxmin,
+                                      boundaryType bxmax, boundaryType bymin,
+                                      boundaryType bymax) {
+  Cell* fill = new Cell();
+  fill->setFill(mat);
+  Universe* fu = new Universe();
+  fu->addCell(fill);
+  std::vector<Universe*> u(100, fu);
+  if (src_pos >= 0) {
+    Cell* sc = new Cell();
+    sc->setFill(mat);
+    Universe* su = new Universe();
+    su->addCell(sc);
+    u[src_pos] = su;
+    *src_cell = sc;
+  }
+  Lattice* lat = new Lattice();
+  lat->setWidth(0.25, 0.25);
+  lat->setUniverses(1, 10, 10, u.data());
+  return make_box_geometry(NULL, lat, 1.25, bxmin, bxmax, bymin, bymax);
+}
+
 /* ------------------------------------------------------------------ runs */
 enum RunKind { EIGEN, SOURCE, FLUX };
 
@@ -351,6 +445,11 @@ struct CaseSpec {
   double src_value;
   int num_polar;           /* 3D cases: polar angles and axial spacing; */
   double z_spacing;        /* 0 for 2D cases (omitted initialisers) */
+  bool linear_source;      /* CPULSSolver instead of CPUSolver */
+  bool allow_negative;     /* Solver::allowNegativeFluxes(true) */
+  Cell* src_cell;          /* fixed source by cell: flat value per group */
+  std::vector<double> src_cell_flat;     /* [G] */
+  std::vector<double> src_cell_moments;  /* [G][3], empty: none */
 };
 
 static void run_case(const CaseSpec& c, const std::string& outdir) {
@@ -370,13 +469,41 @@ static void run_case(const CaseSpec& c, const std::string& outdir) {
   tg.setNumThreads(1);
   tg.generateTracks();
 
-  ProbeSolver solver(&tg);
+  /* Linear-source cases: re-centre the segments on the FSR centroids now
+   * (Solver::initializeFSRs does it again without moving them,
+   * src/TrackGenerator.cpp:1681-1710) and pack the start positions before
+   * the sweeps move them in place (src/CPULSSolver.cpp:738-740). */
+  PackedProblem p;
+  if (c.linear_source) {
+    tg.initializeFSRVolumesBuffer();
+    tg.generateFSRCentroids(tg.getFSRVolumes());
+    openmoc_gb300::pack_tracks(&tg, p);
+    openmoc_gb300::pack_linear_source(&tg, p);
+  }
+
+  ProbeSolver* flat = NULL;
+  ProbeLSSolver* ls = NULL;
+  CPUSolver* sp;
+  if (c.linear_source) sp = ls = new ProbeLSSolver(&tg);
+  else sp = flat = new ProbeSolver(&tg);
+  CPUSolver& solver = *sp;
   solver.setNumThreads(1);
   solver.setConvergenceThreshold(c.tol);
+  if (c.allow_negative) solver.allowNegativeFluxes(true);
   const int G0 = c.geo->getNumEnergyGroups();
   if (c.src_material)
     for (int g = 1; g <= G0; g++)
       solver.setFixedSourceByMaterial(c.src_material, g, c.src_value);
+  if (c.src_cell) {
+    for (int g = 1; g <= G0; g++)
+      if (c.src_cell_flat[g - 1] != 0.0)
+        solver.setFixedSourceByCell(c.src_cell, g, c.src_cell_flat[g - 1]);
+    for (int g = 1; ls && g <= G0 && !c.src_cell_moments.empty(); g++) {
+      const double* m = &c.src_cell_moments[3 * (g - 1)];
+      if (m[0] != 0.0 || m[1] != 0.0 || m[2] != 0.0)
+        ls->setFixedSourceMomentsByCell(c.src_cell, g, m[0], m[1], m[2]);
+    }
+  }
   if (c.kind == EIGEN)
     solver.computeEigenvalue(c.max_iters, c.res);
   else if (c.kind == SOURCE)
@@ -384,8 +511,15 @@ static void run_case(const CaseSpec& c, const std::string& outdir) {
   else
     solver.computeFlux(c.max_iters, true);
 
-  PackedProblem p;
-  openmoc_gb300::pack_tracks(&tg, p);
+  if (!c.linear_source) {
+    openmoc_gb300::pack_tracks(&tg, p);
+  } else {
+    /* the solve must not have split segments after the packing above */
+    PackedProblem q2;
+    openmoc_gb300::pack_tracks(&tg, q2);
+    if (q2.seg_len != p.seg_len || q2.seg_fsr != p.seg_fsr)
+      throw std::runtime_error("segments changed during the solve");
+  }
   openmoc_gb300::pack_materials(c.geo, tg.getFSRVolumes(), p);
 
   Writer w(outdir + "/" + c.name + "_" + PREC);
@@ -397,6 +531,8 @@ static void run_case(const CaseSpec& c, const std::string& outdir) {
   w.sc("res_type", (int) c.res);
   w.sc("run_kind", (int) c.kind);
   w.sc("k_source", c.k_source);
+  w.sc("linear_source", c.linear_source ? 1 : 0);
+  w.sc("allow_negative", c.allow_negative ? 1 : 0);
   w.sc("iterations", solver.getNumIterations());
   w.sc("keff", solver.getKeff());
   const long R = p.num_fsrs;
@@ -406,24 +542,61 @@ static void run_case(const CaseSpec& c, const std::string& outdir) {
     for (int g = 0; g < G; g++)
       flux[(size_t) r * G + g] = (float) solver.getFlux(r, g + 1);
   w.arr("flux", "f4", flux.data(), flux.size());
+  std::vector<float> q((size_t) R * G, 0.0f);
+  bool any_fixed = false;
   if (c.src_material) {
     /* the fixed source per FSR and group, as setFixedSourceByMaterial
      * spreads it (Solver::initializeFixedSources, src/Solver.cpp:1100-1135) */
-    std::vector<float> q((size_t) R * G, 0.0f);
     for (long r = 0; r < R; r++)
       if (c.geo->findFSRMaterial(r) == c.src_material)
         for (int g = 0; g < G; g++) q[(size_t) r * G + g] = (float) c.src_value;
-    w.arr("fixed_source", "f4", q.data(), q.size());
+    any_fixed = true;
+  }
+  if (c.src_cell) {
+    /* setFixedSourceByCell: every FSR of the cell (its id in the FSR key) */
+    std::vector<float> mom((size_t) R * 2 * G, 0.0f);
+    for (long r = 0; r < R; r++) {
+      if (c.geo->findCellContainingFSR(r) != c.src_cell) continue;
+      for (int g = 0; g < G; g++) {
+        q[(size_t) r * G + g] = (float) c.src_cell_flat[g];
+        if (!c.src_cell_moments.empty()) {
+          mom[((size_t) r * 2 + 0) * G + g] = (float) c.src_cell_moments[3 * g];
+          mom[((size_t) r * 2 + 1) * G + g] =
+              (float) c.src_cell_moments[3 * g + 1];
+        }
+      }
+    }
+    any_fixed = true;
+    if (!c.src_cell_moments.empty())
+      w.arr("fixed_source_xy", "f4", mom.data(), mom.size());
+  }
+  if (any_fixed) w.arr("fixed_source", "f4", q.data(), q.size());
+  if (ls) {
+    w.arr("ls_seg_x", "f4", p.seg_x.data(), p.seg_x.size());
+    w.arr("ls_seg_y", "f4", p.seg_y.data(), p.seg_y.size());
+    w.arr("ls_ang_dir", "f8", p.ang_dir.data(), p.ang_dir.size());
+    w.arr("ls_ang_wgt", "f8", p.ang_wgt.data(), p.ang_wgt.size());
+    w.arr("ls_pol_sin", "f8", p.pol_sin.data(), p.pol_sin.size());
+    w.arr("ls_pol_wgt", "f8", p.pol_wgt.data(), p.pol_wgt.size());
+    w.arr("ls_centroid", "f8", p.centroid.data(), p.centroid.size());
+    std::vector<double> ilem = ls->lin_exp();
+    w.arr("ls_ilem", "f8", ilem.data(), ilem.size());
+    std::vector<double> sc = ls->src_constants();
+    w.arr("ls_src_constants", "f8", sc.data(), sc.size());
+    std::vector<float> mom = ls->moments();
+    w.arr("ls_moments", "f4", mom.data(), mom.size());
   }
   if (c.probe && c.kind == EIGEN) {
 #ifdef SINGLE
-    solver.probe(w);
+    if (flat) flat->probe(w);
+    else ls->probe(w);
 #endif
   }
   w.close();
   printf("%s [%s]: R=%ld T=%ld S=%ld iters=%d keff=%.8f\n", c.name, PREC,
          p.num_fsrs, p.num_tracks, p.num_segments, solver.getNumIterations(),
          solver.getKeff());
+  delete sp;
 }
 
 /* An axially extruded pin cell: fuel pin and moderator for z < zf,
@@ -570,6 +743,62 @@ int main(int argc, char** argv) {
     cases.push_back({"pin3d_g7", pin3d_geometry(fuel, mod, p3, 1.6, 2.0), 4,
                      0.1, 1000, 1e-5, FISSION_SOURCE, EIGEN, 1.0, false, NULL,
                      0.0, 4, 0.4});
+  }
+
+  /* 9. tests/test_2d_gradient_linear_source: the 2-group homogeneous
+   *    medium of tests/input_set.py (HomInfMedInput, a 10 x 10 lattice of
+   *    one-cell universes in a 2.5 cm box) with vacuum on xmin and ymax,
+   *    CPULSSolver, 4 azimuthal, 0.1 cm, FISSION_SOURCE, 1e-5 */
+  {
+    MaterialXS x;
+    x.num_groups = 2;
+    x.sigma_f = {0.000625, 0.135416667};
+    x.nu_sigma_f = {0.0015, 0.325};
+    x.sigma_s = {0.1, 0.117, 0.0, 1.42};
+    x.chi = {1.0, 0.0};
+    x.sigma_t = {0.2208, 1.604};
+    Material* med = make_material(17, "2-group infinite medium", x);
+    cases.push_back({"grad2d_ls", hom_lattice_geometry(med, NULL, -1, VAC,
+                     REF, REF, VAC), 4, 0.1, 500, 1e-5, FISSION_SOURCE, EIGEN,
+                     1.0, true, NULL, 0.0, 0, 0.0, true, false, NULL});
+  }
+  /* 10. tests/test_fixed_linear_source: the same lattice, all vacuum, filled
+   *     with C5G7 water, one lattice cell holding a fixed source with flat
+   *     values and first moments; computeFlux with negative fluxes allowed */
+  {
+    Material* water = make_material(18, "Water", c5g7(false));
+    Cell* src = NULL;
+    Geometry* geo = hom_lattice_geometry(water, &src, 3 * 10 + 3, VAC, VAC,
+                                         VAC, VAC);
+    CaseSpec cs = {"fixls_c5g7", geo, 4, 0.1, 500, 1e-5, SCALAR_FLUX, FLUX,
+                   1.0, false, NULL, 0.0, 0, 0.0, true, true, src};
+    cs.src_cell_flat = {1.0, 0.5, 0.25, 1.0, 0.5, 0.25, 1.0};
+    cs.src_cell_moments = {0.01, 0.1, 0.2,  -0.1, 0.0, -0.04,  0.02, 0.0, 0.0,
+                           0, 0, 0,  0, 0, 0,  0, 0, 0,  0, 0, 0};
+    cases.push_back(cs);
+  }
+  /* 11. the 7-group synthetic pin cell of case 3 with the linear source */
+  {
+    Material* fuel = make_material(19, "fuel7ls",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL, 7, true));
+    Material* mod = make_material(20, "mod7ls",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 1000, 7, false));
+    Universe* u = make_pin(fuel, mod, pin);
+    cases.push_back({"pin7_ls", make_box_geometry(u, NULL, 0.63, REF, REF,
+                     REF, REF), 32, 0.05, 1000, 1e-5, FISSION_SOURCE, EIGEN,
+                     1.0, true, NULL, 0.0, 0, 0.0, true, false, NULL});
+  }
+  /* 12. the fixed-source 3x3 lattice of case 6 (computeSource, keff 1)
+   *     with the linear source */
+  {
+    Material* fuel = make_material(21, "fuel7sl",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 4, 7, true));
+    Material* mod = make_material(22, "mod7sl",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 1004, 7, false));
+    cases.push_back({"src3_ls", lattice_geometry(3, fuel, mod, pin, {4},
+                     REF, VAC, REF, VAC), 16, 0.1, 1000, 1e-5,
+                     TOTAL_SOURCE, SOURCE, 1.0, false, fuel, 1.0, 0, 0.0,
+                     true, false, NULL});
   }
 
   for (const CaseSpec& c : cases) {
