@@ -262,6 +262,51 @@ int moc_fission_source_total_noalloc(const float* phi, int64_t ld,
                                      int32_t num_groups, void* stream,
                                      double* total);
 
+/* ---- linear source (CPULSSolver, 2D tracks) ------------------------------
+ * Switches the context from OpenMOC's CPUSolver to its CPULSSolver
+ * semantics (src/CPULSSolver.cpp): flat plus linear (x, y) source and flux
+ * moments per FSR and group.  The arrays are what pack_linear_source
+ * (openmoc_gb300/adapter/pack_reference.h) reads from OpenMOC once the
+ * segments are re-centred on the FSR centroids. */
+typedef struct {
+  const float* seg_x;     /* [S] segment::_starting_position[0] relative to
+                             its FSR centroid (src/TrackTraversingAlgorithms.
+                             cpp:1320-1331) */
+  const float* seg_y;     /* [S] */
+  const double* ang_dir;  /* [A][2] cos(phi), sin(phi) of each angle row's
+                             tracks (Track::getPhi) */
+  const double* ang_wgt;  /* [A] Quadrature::getAzimSpacing * getAzimWeight */
+  const double* pol_sin;  /* [A][Ph] Quadrature::getSinTheta */
+  const double* pol_wgt;  /* [A][Ph] Quadrature::getPolarWeight */
+} moc_ls_geometry;
+
+/** Sets the linear-source geometry (g != NULL) and computes the linear
+ *  expansion matrices and source constants on the device
+ *  (CPULSSolver::initializeFSRs + LinearExpansionGenerator,
+ *  src/CPULSSolver.cpp:136-146, src/TrackTraversingAlgorithms.cpp:470-830);
+ *  g == NULL returns to the flat source.  Needs tracks, quadrature,
+ *  materials and FSRs uploaded; recomputed when materials or FSRs are
+ *  uploaded again, dropped when tracks are. */
+int moc_set_linear_source(moc_ctx* ctx, const moc_ls_geometry* g);
+/** Whether the linear source is on, and how many FSRs have a singular
+ *  expansion matrix (flat source there, as the reference warns). */
+int moc_get_linear_source(moc_ctx* ctx, int* enabled, int64_t* num_flat);
+/** Flux moments, reduced source moments (CPULSSolver::_scalar_flux_xyz,
+ *  _reduced_sources_xyz) and fixed source moments
+ *  (setFixedSourceMomentByFSR, src/CPULSSolver.cpp:280-307; NULL clears)
+ *  as [R][3][G] (x, y, z; z is 0 in 2D). */
+int moc_get_flux_moments(moc_ctx* ctx, float* out, int64_t n);
+int moc_set_flux_moments(moc_ctx* ctx, const float* in, int64_t n);
+int moc_get_source_moments(moc_ctx* ctx, float* out, int64_t n);
+int moc_set_fixed_source_moments(moc_ctx* ctx, const float* in, int64_t n);
+/** The inverse expansion matrices [R][3] (xx, yy, xy) and the source
+ *  constants [R][3][G] (CPULSSolver::getLinearExpansionCoeffsBuffer,
+ *  getSourceConstantsBuffer; either pointer may be NULL). */
+int moc_get_linear_expansion(moc_ctx* ctx, double* ilem, float* src_const);
+/** Solver::allowNegativeFluxes (src/Solver.cpp:623): no clamping of
+ *  negative sources or fluxes. */
+int moc_set_negative_fluxes_allowed(moc_ctx* ctx, int allowed);
+
 /** Number of CUDA kernels this library launched on the context so far. */
 int moc_get_launch_count(moc_ctx* ctx, int64_t* launches);
 

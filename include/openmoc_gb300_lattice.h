@@ -51,6 +51,16 @@ int moc_lattice_export(moc_lattice* lat, float* seg_len, int32_t* seg_fsr,
                        int32_t* fsr_mat, float* fsr_vol);
 int moc_lattice_destroy(moc_lattice* lat);
 
+/** Linear-source geometry of a 2D lattice (the arrays of moc_ls_geometry in
+ *  openmoc_gb300.h): each segment's start relative to its FSR centroid
+ *  (seg_x, seg_y [S]), the centroids [R][2] (CentroidGenerator's formula,
+ *  src/TrackTraversingAlgorithms.cpp:377-460), per angle row cos / sin phi
+ *  [A][2] and spacing x azimuthal weight [A], sin theta and polar weight
+ *  [A][Ph].  Fails for extruded 3D lattices. */
+int moc_lattice_export_ls(moc_lattice* lat, float* seg_x, float* seg_y,
+                          double* centroid, double* ang_dir, double* ang_wgt,
+                          double* pol_sin, double* pol_wgt);
+
 /** Explicit 3D tracks of the lattice extruded to `height` (cm): its pins
  *  below fuel_height, one homogeneous moderator region above; reflective
  *  radially (required of the radial lattice), vacuum at bottom and top;

@@ -38,6 +38,13 @@ class Dims(C.Structure):
     ]
 
 
+class LSGeometry(C.Structure):
+    """moc_ls_geometry: the linear-source arrays (pointers)."""
+    _fields_ = [("seg_x", C.c_void_p), ("seg_y", C.c_void_p),
+                ("ang_dir", C.c_void_p), ("ang_wgt", C.c_void_p),
+                ("pol_sin", C.c_void_p), ("pol_wgt", C.c_void_p)]
+
+
 _P = C.c_void_p
 _SIGS = {
     "moc_last_error": ([], C.c_char_p),
@@ -93,6 +100,14 @@ _SIGS = {
     "moc_eval_attenuation": ([_P, C.c_int, _P, _P, C.c_int64], C.c_int),
     "moc_fission_source_total_noalloc": ([_P, C.c_int64, _P, _P, _P, C.c_int64,
                                           C.c_int32, _P, _P], C.c_int),
+    "moc_set_linear_source": ([_P, C.POINTER(LSGeometry)], C.c_int),
+    "moc_get_linear_source": ([_P, C.POINTER(C.c_int), C.POINTER(C.c_int64)], C.c_int),
+    "moc_get_flux_moments": ([_P, _P, C.c_int64], C.c_int),
+    "moc_set_flux_moments": ([_P, _P, C.c_int64], C.c_int),
+    "moc_get_source_moments": ([_P, _P, C.c_int64], C.c_int),
+    "moc_set_fixed_source_moments": ([_P, _P, C.c_int64], C.c_int),
+    "moc_get_linear_expansion": ([_P, _P, _P], C.c_int),
+    "moc_set_negative_fluxes_allowed": ([_P, C.c_int], C.c_int),
 }
 
 _lock = threading.Lock()

@@ -80,6 +80,10 @@ struct moc_lattice {
   // axial extrusion); moderator material
   std::vector<double> az_spacing, az_weight;
   int32_t moderator = 0;
+  // 2D lattices: the tracks (start, angle) and the polar set, for the
+  // linear-source geometry (empty for extruded 3D lattices)
+  std::vector<Track> tracks;
+  std::vector<double> pol_sin, pol_wgt;
 };
 
 const char* moc_lattice_last_error(void) { return g_lat_error.c_str(); }
@@ -440,6 +444,11 @@ extern "C" int moc_lattice_generate(const moc_lattice_spec* sp,
   for (int64_t r = 0; r < R; r++) L->fsr_vol[r] = (float) vol[r];
   L->az_spacing.assign(spac.begin(), spac.end());
   L->az_weight.assign(wa.begin(), wa.end());
+  L->tracks = tracks;
+  for (int p = 0; p < Ph; p++) {
+    L->pol_sin.push_back(std::sin(std::asin(sin_t[p])));
+    L->pol_wgt.push_back(w_p[p]);
+  }
   L->moderator = s.moderator_material;
   *out = L;
   return 0;
@@ -475,6 +484,67 @@ extern "C" int moc_lattice_export(moc_lattice* L, float* seg_len,
   std::memcpy(inv_sin, L->inv_sin.data(), 4 * L->inv_sin.size());
   std::memcpy(fsr_mat, L->fsr_mat.data(), 4 * L->R);
   std::memcpy(fsr_vol, L->fsr_vol.data(), 4 * L->R);
+  return 0;
+}
+
+// Linear-source geometry of a 2D lattice: FSR centroids by
+// CentroidGenerator's formula (length- and azimuthal-weight-averaged segment
+// midpoints, src/TrackTraversingAlgorithms.cpp:377-460) and each segment's
+// start relative to its FSR's centroid (RecenterSegments, :1320-1331), with
+// starts walked along the track from its first point as the reference
+// walks them; per angle row cos / sin phi and spacing x azimuthal weight;
+// the polar set repeated per angle row.
+extern "C" int moc_lattice_export_ls(moc_lattice* L, float* seg_x,
+                                     float* seg_y, double* centroid,
+                                     double* ang_dir, double* ang_wgt,
+                                     double* pol_sin, double* pol_wgt) {
+  if (!L) return lat_fail("null lattice");
+  if (L->tracks.empty() || (int64_t) L->tracks.size() != L->T)
+    return lat_fail("the linear-source geometry needs a 2D lattice");
+  if (!seg_x || !seg_y || !centroid || !ang_dir || !ang_wgt || !pol_sin ||
+      !pol_wgt)
+    return lat_fail("null output array");
+  const int64_t T = L->T, R = L->R;
+  std::vector<double> cx(R, 0.0), cy(R, 0.0);
+  for (int pass = 0; pass < 2; pass++) {
+    for (int64_t t = 0; t < T; t++) {
+      const Track& tr = L->tracks[t];
+      const double c = std::cos(tr.phi), sn = std::sin(tr.phi);
+      const double w = L->az_spacing[tr.a] * L->az_weight[tr.a];
+      double x = tr.x0, y = tr.y0;
+      for (int64_t k = L->seg_off[t]; k < L->seg_off[t + 1]; k++) {
+        const int32_t r = L->seg_fsr[k];
+        const double l = (double) L->seg_len[k];
+        if (pass == 0) {
+          const double v = (double) L->fsr_vol[r];
+          cx[r] += w * (x + 0.5 * c * l) * l / v;
+          cy[r] += w * (y + 0.5 * sn * l) * l / v;
+        } else {
+          seg_x[k] = (float) (x - cx[r]);
+          seg_y[k] = (float) (y - cy[r]);
+        }
+        x += c * l;
+        y += sn * l;
+      }
+    }
+  }
+  for (int64_t r = 0; r < R; r++) {
+    centroid[2 * r] = cx[r];
+    centroid[2 * r + 1] = cy[r];
+  }
+  for (int a = 0; a < L->A; a++) {
+    ang_dir[2 * a] = ang_dir[2 * a + 1] = 0.0;
+    ang_wgt[a] = L->az_spacing[a] * L->az_weight[a];
+    for (int p = 0; p < L->Ph; p++) {
+      pol_sin[a * L->Ph + p] = L->pol_sin[p];
+      pol_wgt[a * L->Ph + p] = L->pol_wgt[p];
+    }
+  }
+  for (int64_t t = 0; t < T; t++) {
+    const Track& tr = L->tracks[t];
+    ang_dir[2 * tr.a] = std::cos(tr.phi);
+    ang_dir[2 * tr.a + 1] = std::sin(tr.phi);
+  }
   return 0;
 }
 

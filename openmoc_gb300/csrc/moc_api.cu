@@ -153,6 +153,23 @@ struct moc_ctx {
   // moderator above an extruded lattice): tallied in shared memory by the
   // 3D sweep instances
   int hot_base = 0, hot_count = 0;
+  // Linear source (moc_set_linear_source, 2D): 16-byte segment words with
+  // the start positions, per-angle FP64 data for the expansion constants
+  // (dir [A][2], azimuthal weight [A], sin theta [A][Ph], polar weight
+  // [A][Ph], one buffer), float directions, flux / source moments
+  // [R][ld][2], inverse expansion matrices [R][3], constants [R][3][ld] and
+  // fixed source moments [R][ld][2].
+  bool ls = false;
+  int4* segs_ls = nullptr;
+  double* ls_ang = nullptr;
+  float2* ls_dir = nullptr;
+  float* mom = nullptr;
+  float* qxy = nullptr;
+  float* ls_ilem = nullptr;
+  float* ls_const = nullptr;
+  float* fixed_xy = nullptr;
+  int64_t ls_num_flat = 0;
+  int negative_ok = 0;       // Solver::allowNegativeFluxes
 };
 
 namespace {
@@ -208,6 +225,12 @@ moc::SweepArgs sweep_args(moc_ctx* c, int check_done) {
   a.check_done = check_done;
   a.hot_count = (c->d.num_polar_half == 1) ? c->hot_count : 0;
   a.hot_base = a.hot_count ? c->hot_base : (int) c->d.num_fsrs;
+  if (c->ls) {
+    a.segs_ls = c->segs_ls;
+    a.ang_dir = c->ls_dir;
+    a.qxy = c->qxy;
+    a.mom = c->mom;
+  }
   return a;
 }
 
@@ -251,6 +274,14 @@ moc::SolverArgs solver_args(moc_ctx* c, int check_done) {
   a.ld = row_stride(c);
   a.num_materials = c->d.num_materials;
   a.check_done = check_done;
+  a.negative_ok = c->negative_ok;
+  if (c->ls) {
+    a.mom = c->mom;
+    a.qxy = c->qxy;
+    a.ls_ilem = c->ls_ilem;
+    a.ls_const = c->ls_const;
+    a.fixed_xy = c->fixed_xy;
+  }
   return a;
 }
 
@@ -289,19 +320,21 @@ int pair_slots(int G, int lps) {
 }
 
 // Heuristic kernel shape: the most lanes per track direction whose lane
-// utilisation is within 5% of the best reachable with at most kMaxSlots
-// group pairs per lane.
-void pick_shape(int G, int* lps_out, int* slots_out) {
+// utilisation is within 5% of the best reachable with at most max_slots
+// group pairs per lane (kMaxSlots for the flat-source sweep, kMaxLsSlots for
+// the linear-source sweep).
+void pick_shape(int G, int* lps_out, int* slots_out,
+                int max_slots = moc::kMaxSlots) {
   double best = 0.0;
   for (int lps = 1; lps <= 32; lps *= 2) {
     int slots = pair_slots(G, lps);
-    if (slots > moc::kMaxSlots) continue;
+    if (slots > max_slots) continue;
     best = std::max(best, lane_use(G, lps, slots));
   }
   int chosen = 32;
   for (int lps = 32; lps >= 1; lps /= 2) {
     int slots = pair_slots(G, lps);
-    if (slots > moc::kMaxSlots) continue;
+    if (slots > max_slots) continue;
     if (lane_use(G, lps, slots) >= 0.95 * best) {
       chosen = lps;
       break;
@@ -311,8 +344,13 @@ void pick_shape(int G, int* lps_out, int* slots_out) {
   *slots_out = pair_slots(G, chosen);
 }
 
+int max_slots(const moc_ctx* c) {
+  return c->ls ? moc::kMaxLsSlots : moc::kMaxSlots;
+}
+
 int enqueue_sweep(moc_ctx* c, int check_done, bool timed, int ev_index) {
-  if (c->lps == 0) pick_shape(c->d.num_groups, &c->lps, &c->slots);
+  if (c->lps == 0)
+    pick_shape(c->d.num_groups, &c->lps, &c->slots, max_slots(c));
   if (timed) {
     while ((int) c->ev.size() < 2 * (ev_index + 1)) {
       cudaEvent_t e;
@@ -322,10 +360,14 @@ int enqueue_sweep(moc_ctx* c, int check_done, bool timed, int ev_index) {
     MOC_CUDA(cudaEventRecord(c->ev[2 * ev_index], c->stream));
   }
   moc::SweepArgs a = sweep_args(c, check_done);
-  if (!moc::launch_sweep(a, c->d.num_polar_half, c->slots, c->exp_kind,
-                         c->stream))
+  const bool ok =
+      c->ls ? moc::launch_ls_sweep(a, c->d.num_polar_half, c->slots, c->stream)
+            : moc::launch_sweep(a, c->d.num_polar_half, c->slots, c->exp_kind,
+                                c->stream);
+  if (!ok)
     return fail(MOC_ERR_UNSUPPORTED,
-                "no sweep kernel for " + std::to_string(c->d.num_polar_half) +
+                std::string(c->ls ? "no linear-source" : "no") +
+                " sweep kernel for " + std::to_string(c->d.num_polar_half) +
                     " polar angles per half space and " +
                     std::to_string(c->slots) + " groups per lane");
   c->launches++;
@@ -414,7 +456,52 @@ int autotune_sweep(moc_ctx* c, bool use_cache) {
   return MOC_OK;
 }
 
+// the tallies and sources of the next sweep (fused: zero the tallies first)
+void enqueue_sources(moc_ctx* c, const moc::SolverArgs& a, int iteration,
+                     int fused) {
+  if (c->ls)
+    moc::launch_ls_sources(a, iteration, fused, c->stream);
+  else
+    moc::launch_compute_sources(a, iteration, fused, c->stream);
+  c->launches++;
+}
+
+// addSourceToScalarFlux; update = 1 also updates keff and the normalisation
+// (and, with a linear source, normalises the moments)
+void enqueue_add_source(moc_ctx* c, const moc::SolverArgs& a, int update) {
+  if (c->ls) {
+    moc::launch_ls_add_source(a, update, c->stream);
+    c->launches++;
+    if (update) {
+      moc::launch_ls_scale_moments(a, c->stream);
+      c->launches++;
+    }
+  } else {
+    moc::launch_add_source(a, update, c->stream);
+    c->launches++;
+  }
+}
+
+// zero flux tallies (and moments) without computing sources
+int enqueue_zero_tallies(moc_ctx* c, const moc::SolverArgs& a) {
+  moc::launch_zero_phi(a, c->stream);
+  c->launches++;
+  if (c->ls)
+    MOC_CUDA(cudaMemsetAsync(c->mom, 0, 8 * num_flux(c), c->stream));
+  return MOC_OK;
+}
+
+// the flux moments of a flattened flux are zero
+int zero_moments(moc_ctx* c) {
+  if (c->ls)
+    MOC_CUDA(cudaMemsetAsync(c->mom, 0, 8 * num_flux(c), c->stream));
+  return MOC_OK;
+}
+
 int maybe_autotune(moc_ctx* c) {
+  // the autotuner times flat-source sweeps; linear-source contexts keep
+  // the heuristic shape unless one is set
+  if (c->ls) return MOC_OK;
   if (c->autotune && !c->tuned && !c->shape_user_set)
     return autotune_sweep(c, true);
   return MOC_OK;
@@ -477,16 +564,15 @@ int run_iterations(moc_ctx* c, int kind, int res_type) {
     const int k = c->iters_per_sync;
     for (int i = 0; i < k; i++) {
       if (kind == moc::kModeFlux) {
-        moc::launch_zero_phi(a, c->stream);
+        MOC_TRY(enqueue_zero_tallies(c, a));
       } else {
-        moc::launch_compute_sources(a, -1, 1, c->stream);
+        enqueue_sources(c, a, -1, 1);
       }
-      c->launches++;
       MOC_TRY(enqueue_sweep(c, 1, true, i));
-      moc::launch_add_source(a, kind == moc::kModeEigen ? 1 : 0, c->stream);
+      enqueue_add_source(c, a, kind == moc::kModeEigen ? 1 : 0);
       moc::launch_residual(a, res_type, kind == moc::kModeEigen ? 1 : 0, 1, 1,
                            c->stream);
-      c->launches += 2;
+      c->launches++;
       MOC_CUDA(cudaGetLastError());
     }
     MOC_TRY(pull(c));
@@ -518,6 +604,60 @@ int pack_materials(moc_ctx* c) {
   MOC_CUDA(cudaGetLastError());
   MOC_CUDA(cudaStreamSynchronize(c->stream));
   c->mat_packed = 1;
+  return MOC_OK;
+}
+
+// Drops the linear source (new tracks invalidate the start positions).
+void ls_release(moc_ctx* c) {
+  dfree(c->segs_ls);
+  dfree(c->ls_ang);
+  dfree(c->ls_dir);
+  dfree(c->mom);
+  dfree(c->qxy);
+  dfree(c->ls_ilem);
+  dfree(c->ls_const);
+  dfree(c->fixed_xy);
+  if (c->ls && !c->shape_user_set) c->lps = c->slots = 0;
+  c->ls = false;
+  c->ls_num_flat = 0;
+}
+
+// The linear expansion constants from the uploaded segments, quadrature,
+// cross sections and volumes (re-run when any of the last two change).
+int ls_constants(moc_ctx* c) {
+  const int64_t R = c->d.num_fsrs, T = c->d.num_tracks;
+  const int G = c->d.num_groups, A = c->d.num_angles;
+  const int Ph = c->d.num_polar_half;
+  double* lem = nullptr;
+  double* acc = nullptr;
+  unsigned int* nflat = nullptr;
+  MOC_TRY(dalloc(&lem, 3 * R));
+  int st = dalloc(&acc, 3 * R * G);
+  if (st == MOC_OK) st = dalloc(&nflat, 1);
+  if (st != MOC_OK) {
+    dfree(lem);
+    dfree(acc);
+    return st;
+  }
+  const double* ang = c->ls_ang;
+  moc::launch_ls_constants(c->segs_ls, c->seg_off, c->track_ang, T, ang,
+                           ang + 2 * A, ang + 3 * A, ang + 3 * A + A * Ph, Ph,
+                           c->sigma_t, c->fsr_vol, R, G, row_stride(c), lem,
+                           acc, c->ls_ilem, c->ls_const, nflat, c->stream);
+  c->launches += 2;
+  unsigned int h = 0;
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&h, nflat, sizeof(h), cudaMemcpyDeviceToHost,
+                        c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  dfree(lem);
+  dfree(acc);
+  dfree(nflat);
+  if (e != cudaSuccess)
+    return fail(MOC_ERR_CUDA, std::string("linear expansion constants: ") +
+                                  cudaGetErrorString(e));
+  c->ls_num_flat = h;
   return MOC_OK;
 }
 
@@ -651,6 +791,14 @@ int moc_destroy(moc_ctx* c) {
   dfree(c->tc_rows);
   dfree(c->tc_tile_mat);
   dfree(c->tc_b);
+  dfree(c->segs_ls);
+  dfree(c->ls_ang);
+  dfree(c->ls_dir);
+  dfree(c->mom);
+  dfree(c->qxy);
+  dfree(c->ls_ilem);
+  dfree(c->ls_const);
+  dfree(c->fixed_xy);
   dfree(c->sc);
   if (c->hsc) cudaFreeHost(c->hsc);
   for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
@@ -759,6 +907,7 @@ int moc_upload_tracks(moc_ctx* c, const float* seg_len, const int32_t* seg_fsr,
   MOC_CUDA(cudaMemcpy(c->next, next32.data(), sizeof(int32_t) * 2 * T,
                       cudaMemcpyHostToDevice));
   MOC_CUDA(cudaMemcpy(c->flags, flags, T, cudaMemcpyHostToDevice));
+  ls_release(c);
   c->have_tracks = true;
   MOC_TRY(pack_materials(c));
   return MOC_OK;
@@ -860,6 +1009,7 @@ int moc_upload_materials(moc_ctx* c, const float* sigma_t,
   c->h_fissile = fis;
   c->h_chi.assign(chi, chi + MG);
   c->have_mats = true;
+  if (c->ls && c->have_fsrs) MOC_TRY(ls_constants(c));
   return MOC_OK;
 }
 
@@ -923,6 +1073,13 @@ int moc_upload_fsrs(moc_ctx* c, const int32_t* fsr_mat, const float* fsr_vol) {
   MOC_TRY(push(c));
   c->have_fsrs = true;
   MOC_TRY(pack_materials(c));
+  if (c->ls) {
+    // new FSR materials: refresh the material bits of the segment words
+    moc::launch_ls_refresh_ids(c->segs, c->segs_ls, c->d.num_segments,
+                               c->stream);
+    c->launches++;
+    MOC_TRY(ls_constants(c));
+  }
   return MOC_OK;
 }
 
@@ -988,6 +1145,7 @@ int moc_autotune(moc_ctx* c, int* lps, int* slots, int* exp_kind) {
   // the timing sweeps leave undefined tallies and angular fluxes behind
   MOC_TRY(zero_track_fluxes(c));
   MOC_CUDA(cudaMemsetAsync(c->phi, 0, 4 * num_flux(c), c->stream));
+  MOC_TRY(zero_moments(c));
   if (lps) *lps = c->lps;
   if (slots) *slots = c->slots;
   if (exp_kind) *exp_kind = c->exp_kind;
@@ -1018,7 +1176,7 @@ int moc_set_sweep_shape(moc_ctx* c, int lps, int slots) {
   }
   MOC_CHECK(moc::sweep_lps_supported(lps), MOC_ERR_ARG,
             "lanes per track direction must be 1, 2, 4, 8, 16 or 32");
-  MOC_CHECK(slots >= 1 && slots <= moc::kMaxSlots &&
+  MOC_CHECK(slots >= 1 && slots <= max_slots(c) &&
                 2 * (int64_t) lps * slots >= c->d.num_groups,
             MOC_ERR_ARG,
             "lanes x group pairs per lane must cover every group");
@@ -1030,7 +1188,8 @@ int moc_set_sweep_shape(moc_ctx* c, int lps, int slots) {
 
 int moc_get_sweep_shape(moc_ctx* c, int* lps, int* slots) {
   MOC_CHECK(c && lps && slots, MOC_ERR_ARG, "null argument");
-  if (c->lps == 0) pick_shape(c->d.num_groups, &c->lps, &c->slots);
+  if (c->lps == 0)
+    pick_shape(c->d.num_groups, &c->lps, &c->slots, max_slots(c));
   *lps = c->lps;
   *slots = c->slots;
   return MOC_OK;
@@ -1079,6 +1238,7 @@ int moc_compute_eigenvalue(moc_ctx* c, int max_iters, int res_type) {
   MOC_TRY(begin_solve(c, moc::kModeEigen, max_iters, res_type, 1.0));
   moc::SolverArgs a = solver_args(c, 0);
   moc::launch_fill(c->phi, num_flux(c), 1.0f, c->stream);
+  MOC_TRY(zero_moments(c));
   moc::launch_fission_rate(a, 1, c->stream);
   moc::launch_scale_phi(a, c->stream);
   c->launches += 3;
@@ -1102,6 +1262,7 @@ int moc_compute_source(moc_ctx* c, int max_iters, double k_eff,
   MOC_TRY(zero_track_fluxes(c));
   MOC_TRY(begin_solve(c, moc::kModeSource, max_iters, res_type, k_eff));
   moc::launch_fill(c->phi, num_flux(c), 1.0f, c->stream);
+  MOC_TRY(zero_moments(c));
   c->launches++;
   MOC_CUDA(cudaMemcpyAsync(c->phi_old, c->phi, 4 * num_flux(c),
                            cudaMemcpyDeviceToDevice, c->stream));
@@ -1122,10 +1283,11 @@ int moc_compute_flux(moc_ctx* c, int max_iters, int only_fixed_source) {
   MOC_TRY(begin_solve(c, moc::kModeFlux, max_iters, MOC_SCALAR_FLUX, 1.0));
   moc::SolverArgs a = solver_args(c, 0);
   moc::launch_fill(c->phi, num_flux(c), 0.0f, c->stream);
+  MOC_TRY(zero_moments(c));
   MOC_CUDA(cudaMemcpyAsync(c->phi_old, c->phi, 4 * num_flux(c),
                            cudaMemcpyDeviceToDevice, c->stream));
-  moc::launch_compute_sources(a, 0, 0, c->stream);
-  c->launches += 2;
+  enqueue_sources(c, a, 0, 0);
+  c->launches++;
   MOC_TRY(run_iterations(c, moc::kModeFlux, MOC_SCALAR_FLUX));
   c->num_iterations =
       c->hsc->converged ? c->hsc->iteration - 1 : max_iters;
@@ -1156,6 +1318,7 @@ int moc_bench_iterations(moc_ctx* c, int steps, int res_type, int flush_l2,
   MOC_TRY(push(c));
   moc::SolverArgs a = solver_args(c, 1);
   moc::launch_fill(c->phi, num_flux(c), 1.0f, c->stream);
+  MOC_TRY(zero_moments(c));
   moc::launch_fission_rate(a, 1, c->stream);
   moc::launch_scale_phi(a, c->stream);
   MOC_CUDA(cudaMemcpyAsync(c->phi_old, c->phi, 4 * num_flux(c),
@@ -1165,14 +1328,14 @@ int moc_bench_iterations(moc_ctx* c, int steps, int res_type, int flush_l2,
   for (int i = 0; i < steps; i++) {
     if (flush_l2) moc::launch_fill(c->flush, c->flush_n, (float) i, c->stream);
     MOC_CUDA(cudaEventRecord(ev[4 * i], c->stream));
-    moc::launch_compute_sources(a, -1, 1, c->stream);
+    enqueue_sources(c, a, -1, 1);
     MOC_CUDA(cudaEventRecord(ev[4 * i + 1], c->stream));
     MOC_TRY(enqueue_sweep(c, 1, false, 0));
     MOC_CUDA(cudaEventRecord(ev[4 * i + 2], c->stream));
-    moc::launch_add_source(a, 1, c->stream);
+    enqueue_add_source(c, a, 1);
     moc::launch_residual(a, res_type, 1, 1, 1, c->stream);
     MOC_CUDA(cudaEventRecord(ev[4 * i + 3], c->stream));
-    c->launches += 3;
+    c->launches++;
   }
   MOC_CUDA(cudaGetLastError());
   MOC_CUDA(cudaStreamSynchronize(c->stream));
@@ -1373,6 +1536,7 @@ int moc_flatten_fsr_fluxes(moc_ctx* c, float value) {
   MOC_TRY(ready(c));
   moc::launch_fill(c->phi, num_flux(c), value, c->stream);
   c->launches++;
+  MOC_TRY(zero_moments(c));
   MOC_CUDA(cudaGetLastError());
   return MOC_OK;
 }
@@ -1385,6 +1549,7 @@ int moc_flatten_fsr_fluxes_chi(moc_ctx* c, int material) {
   moc::launch_fill_chi(c->phi, d_chi, c->d.num_fsrs, c->d.num_groups,
                        row_stride(c), c->stream);
   c->launches++;
+  MOC_TRY(zero_moments(c));
   MOC_CUDA(cudaGetLastError());
   return MOC_OK;
 }
@@ -1402,6 +1567,10 @@ int moc_normalize_fluxes(moc_ctx* c, double* factor) {
   moc::launch_fission_rate(a, 1, c->stream);
   moc::launch_scale_phi(a, c->stream);
   c->launches += 2;
+  if (c->ls) {
+    moc::launch_ls_scale_moments(a, c->stream);
+    c->launches++;
+  }
   MOC_CUDA(cudaGetLastError());
   MOC_TRY(pull(c));
   if (factor) *factor = c->hsc->factor;
@@ -1412,8 +1581,7 @@ int moc_compute_fsr_sources(moc_ctx* c, int iteration) {
   MOC_TRY(ready(c));
   MOC_CHECK(iteration >= 0, MOC_ERR_ARG, "iteration must be non-negative");
   moc::SolverArgs a = solver_args(c, 0);
-  moc::launch_compute_sources(a, iteration, 0, c->stream);
-  c->launches++;
+  enqueue_sources(c, a, iteration, 0);
   MOC_CUDA(cudaGetLastError());
   return MOC_OK;
 }
@@ -1421,6 +1589,7 @@ int moc_compute_fsr_sources(moc_ctx* c, int iteration) {
 int moc_transport_sweep(moc_ctx* c) {
   MOC_TRY(ready(c));
   MOC_CUDA(cudaMemsetAsync(c->phi, 0, 4 * num_flux(c), c->stream));
+  MOC_TRY(zero_moments(c));
   MOC_TRY(enqueue_sweep(c, 0, true, 0));
   MOC_CUDA(cudaStreamSynchronize(c->stream));
   MOC_TRY(collect_sweep_times(c, 1));
@@ -1431,8 +1600,7 @@ int moc_transport_sweep(moc_ctx* c) {
 int moc_add_source_to_scalar_flux(moc_ctx* c) {
   MOC_TRY(ready(c));
   moc::SolverArgs a = solver_args(c, 0);
-  moc::launch_add_source(a, 0, c->stream);
-  c->launches++;
+  enqueue_add_source(c, a, 0);
   MOC_CUDA(cudaGetLastError());
   return MOC_OK;
 }
@@ -1485,6 +1653,227 @@ int moc_compute_fsr_fission_rates(moc_ctx* c, double* rates, int64_t n,
   MOC_CUDA(cudaMemcpyAsync(rates, c->rates, 8 * n, cudaMemcpyDeviceToHost,
                            c->stream));
   MOC_CUDA(cudaStreamSynchronize(c->stream));
+  return MOC_OK;
+}
+
+// ------------------------------------------------------------ linear source
+int moc_set_linear_source(moc_ctx* c, const moc_ls_geometry* g) {
+  MOC_TRY(ready(c));
+  if (!g) {
+    ls_release(c);
+    return MOC_OK;
+  }
+  MOC_CHECK(!c->d.solve_3d, MOC_ERR_UNSUPPORTED,
+            "the linear source takes 2D tracks");
+  MOC_CHECK(c->d.num_polar_half >= 1 && c->d.num_polar_half <= 3,
+            MOC_ERR_UNSUPPORTED,
+            "the linear-source sweep takes 1 to 3 polar angles per half space");
+  MOC_CHECK(c->mat_packed, MOC_ERR_UNSUPPORTED,
+            "the linear-source sweep needs fewer than 2^24 FSRs and at most "
+            "256 materials");
+  MOC_CHECK(g->seg_x && g->seg_y && g->ang_dir && g->ang_wgt && g->pol_sin &&
+                g->pol_wgt,
+            MOC_ERR_ARG, "null linear-source array");
+  const int64_t S = c->d.num_segments, R = c->d.num_fsrs;
+  const int A = c->d.num_angles, Ph = c->d.num_polar_half;
+  for (int64_t i = 0; i < S; i++)
+    MOC_CHECK(std::isfinite(g->seg_x[i]) && std::isfinite(g->seg_y[i]),
+              MOC_ERR_ARG,
+              "non-finite segment start position at segment " +
+                  std::to_string(i));
+  for (int a = 0; a < A; a++) {
+    const double cx = g->ang_dir[2 * a], cy = g->ang_dir[2 * a + 1];
+    MOC_CHECK(std::isfinite(cx) && std::isfinite(cy) &&
+                  std::fabs(cx * cx + cy * cy - 1.0) < 1e-6,
+              MOC_ERR_ARG,
+              "track direction of angle " + std::to_string(a) +
+                  " is not a unit vector");
+    MOC_CHECK(std::isfinite(g->ang_wgt[a]) && g->ang_wgt[a] > 0.0,
+              MOC_ERR_ARG, "azimuthal weight must be positive");
+    for (int p = 0; p < Ph; p++) {
+      const double sn = g->pol_sin[a * Ph + p], w = g->pol_wgt[a * Ph + p];
+      MOC_CHECK(std::isfinite(sn) && sn > 0.0 && sn <= 1.0, MOC_ERR_ARG,
+                "sin(theta) must lie in (0, 1]");
+      MOC_CHECK(std::isfinite(w) && w >= 0.0, MOC_ERR_ARG,
+                "polar weight must be non-negative");
+    }
+  }
+  ls_release(c);
+  const int64_t nf = num_flux(c);
+  const size_t nang = 3 * (size_t) A + 2 * (size_t) A * Ph;
+  std::vector<double> ang(nang);
+  std::vector<float2> dir(A);
+  for (int a = 0; a < A; a++) {
+    ang[2 * a] = g->ang_dir[2 * a];
+    ang[2 * a + 1] = g->ang_dir[2 * a + 1];
+    ang[2 * A + a] = g->ang_wgt[a];
+    dir[a] = make_float2((float) g->ang_dir[2 * a], (float) g->ang_dir[2 * a + 1]);
+    for (int p = 0; p < Ph; p++) {
+      ang[3 * A + a * Ph + p] = g->pol_sin[a * Ph + p];
+      ang[3 * A + A * Ph + a * Ph + p] = g->pol_wgt[a * Ph + p];
+    }
+  }
+  float* dx = nullptr;
+  float* dy = nullptr;
+  int st = MOC_OK;
+  auto step = [&](int r) { if (st == MOC_OK) st = r; };
+  step(dalloc(&c->segs_ls, S > 0 ? S : 1));
+  step(dalloc(&c->ls_ang, nang));
+  step(dalloc(&c->ls_dir, A));
+  step(dalloc(&c->mom, 2 * nf));
+  step(dalloc(&c->qxy, 2 * nf));
+  step(dalloc(&c->ls_ilem, 3 * R));
+  step(dalloc(&c->ls_const, 3 * nf));
+  step(dalloc(&dx, S > 0 ? S : 1));
+  step(dalloc(&dy, S > 0 ? S : 1));
+  if (st != MOC_OK) {
+    dfree(dx);
+    dfree(dy);
+    ls_release(c);
+    return st;
+  }
+  cudaError_t e = cudaMemcpy(dx, g->seg_x, 4 * S, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(dy, g->seg_y, 4 * S, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(c->ls_ang, ang.data(), 8 * nang, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(c->ls_dir, dir.data(), 8 * (size_t) A,
+                   cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(c->mom, 0, 8 * nf);
+  if (e == cudaSuccess) e = cudaMemset(c->qxy, 0, 8 * nf);
+  if (e == cudaSuccess) {
+    moc::launch_ls_pack_segments(c->segs, dx, dy, c->segs_ls, S, c->stream);
+    c->launches++;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  dfree(dx);
+  dfree(dy);
+  if (e != cudaSuccess) {
+    ls_release(c);
+    return fail(MOC_ERR_CUDA, std::string("linear source upload: ") +
+                                  cudaGetErrorString(e));
+  }
+  c->ls = true;
+  if (!c->shape_user_set) c->lps = c->slots = 0;
+  st = ls_constants(c);
+  if (st != MOC_OK) ls_release(c);
+  return st;
+}
+
+int moc_get_linear_source(moc_ctx* c, int* enabled, int64_t* num_flat) {
+  MOC_CHECK(c, MOC_ERR_ARG, "null context");
+  if (enabled) *enabled = c->ls ? 1 : 0;
+  if (num_flat) *num_flat = c->ls_num_flat;
+  return MOC_OK;
+}
+
+int moc_set_negative_fluxes_allowed(moc_ctx* c, int allowed) {
+  MOC_CHECK(c, MOC_ERR_ARG, "null context");
+  c->negative_ok = allowed ? 1 : 0;
+  return MOC_OK;
+}
+
+// host [R][3][G] (x, y, z) <-> device [R][ld][2] (x, y adjacent per group)
+static int moments_out(moc_ctx* c, const float* dev, float* out, int64_t n,
+                       float scale_by_sigma_t) {
+  const int64_t R = c->d.num_fsrs;
+  const int G = c->d.num_groups, ld = row_stride(c);
+  MOC_CHECK(out && n == 3 * R * G, MOC_ERR_ARG,
+            "moments need num_fsrs x 3 x num_groups values");
+  std::vector<float> h((size_t) 2 * R * ld);
+  MOC_CUDA(cudaMemcpyAsync(h.data(), dev, 8 * (size_t) R * ld,
+                           cudaMemcpyDeviceToHost, c->stream));
+  std::vector<float> st;
+  std::vector<int32_t> fm;
+  if (scale_by_sigma_t != 0.0f) {
+    st.resize((size_t) c->d.num_materials * G);
+    fm.resize(R);
+    MOC_CUDA(cudaMemcpyAsync(st.data(), c->sigma_t, 4 * st.size(),
+                             cudaMemcpyDeviceToHost, c->stream));
+    MOC_CUDA(cudaMemcpyAsync(fm.data(), c->fsr_mat, 4 * (size_t) R,
+                             cudaMemcpyDeviceToHost, c->stream));
+  }
+  MOC_CUDA(cudaStreamSynchronize(c->stream));
+  for (int64_t r = 0; r < R; r++)
+    for (int g = 0; g < G; g++) {
+      float x = h[(r * ld + g) * 2], y = h[(r * ld + g) * 2 + 1];
+      if (scale_by_sigma_t != 0.0f) {
+        const float s = st[(size_t) fm[r] * G + g];
+        x *= s;
+        y *= s;
+      }
+      out[(r * 3 + 0) * G + g] = x;
+      out[(r * 3 + 1) * G + g] = y;
+      out[(r * 3 + 2) * G + g] = 0.0f;
+    }
+  return MOC_OK;
+}
+
+static int moments_in(moc_ctx* c, float* dev, const float* in, int64_t n) {
+  const int64_t R = c->d.num_fsrs;
+  const int G = c->d.num_groups, ld = row_stride(c);
+  MOC_CHECK(in && n == 3 * R * G, MOC_ERR_ARG,
+            "moments need num_fsrs x 3 x num_groups values");
+  std::vector<float> h((size_t) 2 * R * ld, 0.0f);
+  for (int64_t r = 0; r < R; r++)
+    for (int g = 0; g < G; g++) {
+      const float x = in[(r * 3 + 0) * G + g], y = in[(r * 3 + 1) * G + g];
+      MOC_CHECK(std::isfinite(x) && std::isfinite(y), MOC_ERR_ARG,
+                "non-finite moment");
+      h[(r * ld + g) * 2] = x;
+      h[(r * ld + g) * 2 + 1] = y;
+    }
+  MOC_CUDA(cudaMemcpyAsync(dev, h.data(), 8 * (size_t) R * ld,
+                           cudaMemcpyHostToDevice, c->stream));
+  MOC_CUDA(cudaStreamSynchronize(c->stream));
+  return MOC_OK;
+}
+
+int moc_get_flux_moments(moc_ctx* c, float* out, int64_t n) {
+  MOC_TRY(ready(c));
+  MOC_CHECK(c->ls, MOC_ERR_STATE, "no linear source set");
+  return moments_out(c, c->mom, out, n, 0.0f);
+}
+
+int moc_set_flux_moments(moc_ctx* c, const float* in, int64_t n) {
+  MOC_TRY(ready(c));
+  MOC_CHECK(c->ls, MOC_ERR_STATE, "no linear source set");
+  return moments_in(c, c->mom, in, n);
+}
+
+int moc_get_source_moments(moc_ctx* c, float* out, int64_t n) {
+  MOC_TRY(ready(c));
+  MOC_CHECK(c->ls, MOC_ERR_STATE, "no linear source set");
+  return moments_out(c, c->qxy, out, n, 1.0f);
+}
+
+int moc_set_fixed_source_moments(moc_ctx* c, const float* in, int64_t n) {
+  MOC_TRY(ready(c));
+  MOC_CHECK(c->ls, MOC_ERR_STATE, "no linear source set");
+  if (!in) {
+    dfree(c->fixed_xy);
+    return MOC_OK;
+  }
+  if (!c->fixed_xy) MOC_TRY(dalloc(&c->fixed_xy, 2 * num_flux(c)));
+  return moments_in(c, c->fixed_xy, in, n);
+}
+
+int moc_get_linear_expansion(moc_ctx* c, double* ilem, float* src_const) {
+  MOC_TRY(ready(c));
+  MOC_CHECK(c->ls, MOC_ERR_STATE, "no linear source set");
+  const int64_t R = c->d.num_fsrs;
+  const int G = c->d.num_groups, ld = row_stride(c);
+  if (ilem) {
+    std::vector<float> h(3 * (size_t) R);
+    MOC_CUDA(cudaMemcpy(h.data(), c->ls_ilem, 4 * h.size(),
+                        cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < h.size(); i++) ilem[i] = h[i];
+  }
+  if (src_const)
+    MOC_CUDA(cudaMemcpy2D(src_const, 4 * G, c->ls_const, 4 * ld, 4 * G,
+                          3 * R, cudaMemcpyDeviceToHost));
   return MOC_OK;
 }
 

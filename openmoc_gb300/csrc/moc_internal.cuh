@@ -92,6 +92,16 @@ struct SweepArgs {
   // one-polar-value (3D) instances; hot_count = 0 elsewhere.
   int hot_base;
   int hot_count;             // 0 .. kMaxHotFsrs
+  // Linear source (2D; null for the flat-source sweep): per segment
+  // {length bits, fsr | material << 24, x bits, y bits} with (x, y) the
+  // segment's forward start relative to its FSR centroid; per angle row
+  // the forward direction (cos phi, sin phi); the reduced source moments
+  // divided by sigma_t and the flux moment tallies, both [R][ld][2] with x
+  // and y adjacent per group.
+  const int4* segs_ls;       // [S]
+  const float2* ang_dir;     // [A]
+  const float* qxy;          // [R][ld][2]
+  float* mom;                // [R][ld][2]
 };
 
 constexpr int kMaxHotFsrs = 8;
@@ -135,6 +145,16 @@ struct SolverArgs {
   const float* tc_b;         // [M][2][tc_n][tc_k]
   int tc_tiles;
   int tc_n, tc_k;            // padded destination / origin group counts
+  // Linear source (null: flat source): flux moments and reduced source
+  // moments / sigma_t ([R][ld][2], x and y adjacent per group), the inverse
+  // expansion matrix per FSR (xx, yy, xy), the source constants [R][3][ld]
+  // and the fixed source moments [R][ld][2] (or null).
+  float* mom;
+  float* qxy;
+  const float* ls_ilem;      // [R][3]
+  const float* ls_const;     // [R][3][ld]
+  const float* fixed_xy;
+  int negative_ok;           // Solver::allowNegativeFluxes
 };
 
 // Rows (FSRs) per tile of the tensor-core source kernel: the MMA's M.
@@ -196,6 +216,40 @@ void tc_pack_scattering(const float* sigma_s, int M, int G,
                         std::vector<float>& out);
 void launch_sources_tc(const SolverArgs& a, int iteration, int zero_phi,
                        cudaStream_t s);
+
+// ---- linear source (linear_source.cu, solver_kernels.cu, ls_sweep_*.cu) ----
+// Largest group pairs per lane of the linear-source sweep instances.
+constexpr int kMaxLsSlots = 5;
+// LinearExpansionGenerator (2D): volume moments and source constants
+// accumulated per FSR in FP64 over all segments, then inverted; outputs
+// ilem[R][3] and cst[R][3][ld] (float), returns through *num_flat the FSRs
+// whose matrix is singular (flat source there).  Scratch lem[R][3] and
+// acc[R][3][G] doubles are the caller's, zeroed here.
+void launch_ls_constants(const int4* segs_ls, const int64_t* seg_off,
+                         const int32_t* track_ang, int64_t T,
+                         const double* ang_dir, const double* ang_wgt,
+                         const double* pol_sin, const double* pol_wgt,
+                         int Ph, const float* sigma_t, const float* fsr_vol,
+                         int64_t R, int G, int ld, double* lem, double* acc,
+                         float* ilem, float* cst, unsigned int* num_flat,
+                         cudaStream_t s);
+// Builds segs_ls from the packed segments and the start positions.
+void launch_ls_pack_segments(const int2* segs, const float* x, const float* y,
+                             int4* out, int64_t S, cudaStream_t s);
+// Copies the FSR / material words of segs into segs_ls (after new FSR
+// materials were packed into segs).
+void launch_ls_refresh_ids(const int2* segs, int4* out, int64_t S,
+                           cudaStream_t s);
+// Flat + linear sources in one pass (CPULSSolver::computeFSRSources);
+// fused zeroes phi and the moments for the sweep that follows.
+void launch_ls_sources(const SolverArgs& a, int iteration, int fused,
+                       cudaStream_t s);
+// CPULSSolver::addSourceToScalarFlux; update as launch_add_source.
+void launch_ls_add_source(const SolverArgs& a, int update, cudaStream_t s);
+// Moments *= sc->factor (the normalisation of the eigenvalue loop).
+void launch_ls_scale_moments(const SolverArgs& a, cudaStream_t s);
+bool launch_ls_sweep(const SweepArgs& a, int polar_half, int slots,
+                     cudaStream_t stream);
 
 // ---- batched pools (solver_kernels.cu) -------------------------------------
 // The loop body of every live solve of a pool; a.num_fsrs is the end of the

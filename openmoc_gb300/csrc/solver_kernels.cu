@@ -161,7 +161,7 @@ __device__ __forceinline__ void source_rows(const SolverArgs& a,
       q *= (float) kOneOverFourPi;
       if (q < 0.0f) {
         negatives++;
-        if ((i == 0 ? it0 : it1) < 30) q = kFluxEpsilon;
+        if ((i == 0 ? it0 : it1) < 30 && !a.negative_ok) q = kFluxEpsilon;
       }
       a.qt[r * a.ld + gd] = q / st[gd];
     }
@@ -256,7 +256,7 @@ add_source_kernel(const SolverArgs a, int update) {
       if (g >= G) continue;
       float x = v[j] / (st[g] * vol);
       x += (float) kFourPi * q[j];
-      if (x < 0.0f) {
+      if (x < 0.0f && !a.negative_ok) {
         x = kFluxEpsilon;
         negatives++;
       }
@@ -468,6 +468,238 @@ __global__ void fsr_rates_kernel(const SolverArgs a, double* out, int nu) {
       s += (double) xs[g] * a.phi[r * a.ld + g];
     s = warp_sum_all_d(s);
     if (lane == 0) out[r] = s * (double) a.fsr_vol[r];
+  }
+}
+
+// ----------------------------------------------------------- linear source
+// CPULSSolver::computeFSRSources (src/CPULSSolver.cpp:386-527): one warp per
+// FSR computes the flat source of CPUSolver and, from the same pass over the
+// transposed scattering matrices, the scatter + fission sources of the x
+// and y flux moments; the moments go through the FSR's inverse expansion
+// matrix, times 1/(8 pi), and are zeroed where the flat source is not
+// above 1e-24 during the first 30 iterations (unless negative fluxes are
+// allowed).  Stores Q/sigma_t and (q_x, q_y)/sigma_t for the sweep; fused:
+// zeroes the flux and moment tallies.
+template <int S>
+__global__ void __launch_bounds__(kThreads)
+ls_sources_kernel(const SolverArgs a, int iteration, int zero, int staged) {
+  if (skip(a)) return;
+  extern __shared__ float4 s_ss4[];
+  const int G = a.num_groups;
+  if (staged) {
+    const int n4 = (a.num_materials * G * G + 3) / 4;
+    const float4* src = reinterpret_cast<const float4*>(a.sigma_s_T);
+#pragma unroll 8
+    for (int i = threadIdx.x; i < n4; i += blockDim.x) s_ss4[i] = src[i];
+    __syncthreads();
+  }
+  const float* ssT =
+      staged ? reinterpret_cast<const float*>(s_ss4) : a.sigma_s_T;
+  const float inv_k = (float) (1.0 / a.sc->keff);
+  if (iteration < 0) iteration = a.sc->iteration;
+  const int GG = G * G;
+  const int lane = threadIdx.x & 31;
+  const int ld = a.ld;
+  unsigned long long negatives = 0;
+  for (int64_t r = first_row(); r < a.num_fsrs; r += row_step()) {
+    const int m = a.fsr_mat[r];
+    float* phi = a.phi + r * ld;
+    float2* mom = reinterpret_cast<float2*>(a.mom + r * 2 * ld);
+    float ph[S], mx[S], my[S], s0[S], s1[S], s2[S];
+#pragma unroll
+    for (int j = 0; j < S; j++) {
+      const int g = lane + 32 * j;
+      const float2 mm = (g < G) ? mom[g] : make_float2(0.f, 0.f);
+      ph[j] = (g < G) ? phi[g] : 0.0f;
+      mx[j] = mm.x;
+      my[j] = mm.y;
+      s0[j] = s1[j] = s2[j] = 0.0f;
+    }
+    if (zero) {
+#pragma unroll
+      for (int j = 0; j < S; j++) {
+        const int g = lane + 32 * j;
+        if (g < G) {
+          phi[g] = 0.0f;
+          mom[g] = make_float2(0.f, 0.f);
+        }
+      }
+    }
+    float f0 = 0.0f, f1 = 0.0f, f2v = 0.0f;
+    if (a.fissile[m]) {
+      const float* nf = a.nu_sigma_f + (int64_t) m * G;
+#pragma unroll
+      for (int j = 0; j < S; j++) {
+        const int g = lane + 32 * j;
+        if (g < G) {
+          f0 = fmaf(nf[g], ph[j], f0);
+          f1 = fmaf(nf[g], mx[j], f1);
+          f2v = fmaf(nf[g], my[j], f2v);
+        }
+      }
+    }
+    f0 = warp_sum_all(f0) * inv_k;
+    f1 = warp_sum_all(f1) * inv_k;
+    f2v = warp_sum_all(f2v) * inv_k;
+    const float* mT = ssT + (int64_t) m * GG + lane;
+#pragma unroll
+    for (int js = 0; js < S; js++) {
+      const int gbase = 32 * js;
+      const int gcount = min(32, G - gbase);
+#pragma unroll 2
+      for (int l = 0; l < gcount; l++) {
+        const float p0 = __shfl_sync(0xffffffffu, ph[js], l);
+        const float p1 = __shfl_sync(0xffffffffu, mx[js], l);
+        const float p2 = __shfl_sync(0xffffffffu, my[js], l);
+        const float* c = mT + (int64_t) (gbase + l) * G;
+#pragma unroll
+        for (int j = 0; j < S; j++)
+          if (lane + 32 * j < G) {
+            const float cf = c[32 * j];
+            s0[j] = fmaf(cf, p0, s0[j]);
+            s1[j] = fmaf(cf, p1, s1[j]);
+            s2[j] = fmaf(cf, p2, s2[j]);
+          }
+      }
+    }
+    const float* chi = a.chi + (int64_t) m * G;
+    const float* st = a.sigma_t + (int64_t) m * G;
+    const float il0 = a.ls_ilem[3 * r], il1 = a.ls_ilem[3 * r + 1],
+                il2 = a.ls_ilem[3 * r + 2];
+    float2* qxy = reinterpret_cast<float2*>(a.qxy + r * 2 * ld);
+    const float2* fxy =
+        a.fixed_xy ? reinterpret_cast<const float2*>(a.fixed_xy + r * 2 * ld)
+                   : nullptr;
+#pragma unroll
+    for (int j = 0; j < S; j++) {
+      const int gd = lane + 32 * j;
+      if (gd >= G) continue;
+      float q = chi[gd] * f0;
+      q += s0[j];
+      if (a.fixed) q += a.fixed[r * ld + gd];
+      q *= (float) kOneOverFourPi;
+      if (q < 0.0f) {
+        negatives++;
+        if (iteration < 30 && !a.negative_ok) q = kFluxEpsilon;
+      }
+      float sx = fmaf(chi[gd], f1, s1[j]);
+      float sy = fmaf(chi[gd], f2v, s2[j]);
+      if (fxy) {
+        const float2 fx = fxy[gd];
+        sx += fx.x;
+        sy += fx.y;
+      }
+      float rx = 0.0f, ry = 0.0f;
+      if (a.negative_ok || q > 10.0f * kFluxEpsilon || iteration > 29) {
+        rx = (float) (kOneOverFourPi / 2) * fmaf(il0, sx, il2 * sy);
+        ry = (float) (kOneOverFourPi / 2) * fmaf(il2, sx, il1 * sy);
+      }
+      const float ist = 1.0f / st[gd];
+      a.qt[r * ld + gd] = q * ist;
+      qxy[gd] = make_float2(rx * ist, ry * ist);
+    }
+  }
+  if (negatives) atomicAdd(&a.sc->neg_sources, negatives);
+}
+
+// CPULSSolver::addSourceToScalarFlux (2D, src/CPULSSolver.cpp:787-882):
+//   phi = phi / (sigma_t V) + 4 pi Q / sigma_t,
+//   m_x = m_x / (sigma_t V) + 8 pi (q_x c_xx + q_y c_xy) / sigma_t,
+//   m_y = m_y / (sigma_t V) + 8 pi (q_x c_xy + q_y c_yy) / sigma_t,
+// a negative flux (unless allowed) becomes max(old flux, 1e-25) with zero
+// moments.  update = 1 also finishes the keff / normalisation update as
+// add_source_kernel does.
+template <int S>
+__global__ void __launch_bounds__(kRowThreads)
+ls_add_source_kernel(const SolverArgs a, int update) {
+  if (skip(a)) return;
+  const int G = a.num_groups;
+  const int ld = a.ld;
+  const int lane = threadIdx.x & 31;
+  double rate = 0.0;
+  unsigned long long negatives = 0;
+  for (int64_t r = first_row(); r < a.num_fsrs; r += row_step()) {
+    const int m = a.fsr_mat[r];
+    const float vol0 = a.fsr_vol[r];
+    const float vol = (vol0 < 1.0e-12f) ? 1.0e30f : vol0;
+    const float* __restrict__ st = a.sigma_t + (int64_t) m * G;
+    const float* __restrict__ nf = a.nu_sigma_f + (int64_t) m * G;
+    float* __restrict__ phi = a.phi + r * ld;
+    const float* __restrict__ qt = a.qt + r * ld;
+    const float* __restrict__ old = a.phi_old + r * ld;
+    float2* __restrict__ mom = reinterpret_cast<float2*>(a.mom + r * 2 * ld);
+    const float2* __restrict__ qm =
+        reinterpret_cast<const float2*>(a.qxy + r * 2 * ld);
+    const float* __restrict__ cst = a.ls_const + r * 3 * ld;
+    float v[S], q[S], o[S], c0[S], c1[S], c2[S];
+    float2 mm[S], qq[S];
+#pragma unroll
+    for (int j = 0; j < S; j++) {
+      const int g = lane + 32 * j;
+      const bool on = g < G;
+      v[j] = on ? phi[g] : 0.0f;
+      q[j] = on ? qt[g] : 0.0f;
+      o[j] = on ? old[g] : 0.0f;
+      mm[j] = on ? mom[g] : make_float2(0.f, 0.f);
+      qq[j] = on ? qm[g] : make_float2(0.f, 0.f);
+      c0[j] = on ? cst[g] : 0.0f;
+      c1[j] = on ? cst[ld + g] : 0.0f;
+      c2[j] = on ? cst[2 * ld + g] : 0.0f;
+    }
+    float rr = 0.0f;
+#pragma unroll
+    for (int j = 0; j < S; j++) {
+      const int g = lane + 32 * j;
+      if (g >= G) continue;
+      const float inv = 1.0f / (st[g] * vol);
+      float x = fmaf(v[j], inv, (float) kFourPi * q[j]);
+      float mx = fmaf(mm[j].x, inv, (float) (2 * kFourPi) *
+                                        fmaf(qq[j].x, c0[j], qq[j].y * c2[j]));
+      float my = fmaf(mm[j].y, inv, (float) (2 * kFourPi) *
+                                        fmaf(qq[j].x, c2[j], qq[j].y * c1[j]));
+      if (x < 0.0f && !a.negative_ok) {
+        x = fmaxf(o[j], kFluxEpsilon);
+        mx = 0.0f;
+        my = 0.0f;
+        negatives++;
+      }
+      phi[g] = x;
+      mom[g] = make_float2(mx, my);
+      rr = fmaf(nf[g], x, rr);
+    }
+    if (update) rate += (double) rr * (double) vol0;
+  }
+  if (negatives) atomicAdd(&a.sc->neg_fluxes, negatives);
+  if (!update) return;
+  rate = warp_sum_all_d(rate);
+  DevScalars* sc = a.sc;
+  if (block_accumulate(rate, &sc->accum_rate, &sc->ticket_rate)) {
+    const double total = *(volatile double*) &sc->accum_rate;
+    const double R = (double) a.num_fsrs;
+    sc->keff = sc->keff * (total / R);
+    sc->factor = R / total;
+    sc->scale[sc->cur] *= (float) sc->factor;
+    sc->accum_rate = 0.0;
+    sc->ticket_rate = 0;
+    __threadfence();
+  }
+}
+
+// The moments' share of CPULSSolver::normalizeFluxes (src/CPULSSolver.cpp:
+// 362-378): moments *= factor.
+__global__ void ls_scale_moments_kernel(const SolverArgs a) {
+  if (skip(a)) return;
+  const float f = (float) a.sc->factor;
+  const int64_t n = a.num_fsrs * 2 * a.ld;
+  float4* m4 = reinterpret_cast<float4*>(a.mom);
+  for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n / 4;
+       i += (int64_t) gridDim.x * blockDim.x) {
+    float4 v = m4[i];
+    v.x *= f;
+    v.y *= f;
+    v.z *= f;
+    v.w *= f;
+    m4[i] = v;
   }
 }
 
@@ -894,6 +1126,60 @@ void launch_batch_rebase(int2* segs, int64_t S, const int32_t* fsr_mat,
   batch_rebase_kernel<<<grid_for(n, kThreads), kThreads, 0, s>>>(
       segs, S, fsr_mat, r0, seg_off, next, track_ang, track_slot, T, s0, t0,
       a0, slot);
+}
+
+// ---- linear source ---------------------------------------------------------
+namespace {
+
+template <int S>
+void launch_ls_sources_s(const SolverArgs& a, int iteration, int fused,
+                         cudaStream_t s) {
+  const size_t need =
+      (sizeof(float) * (size_t) a.num_materials * a.num_groups * a.num_groups +
+       15) & ~(size_t) 15;
+  const int staged = need <= 160 * 1024;
+  const size_t smem = staged ? need : 0;
+  auto kern = ls_sources_kernel<S>;
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int) smem);
+  int64_t blocks = (a.num_fsrs + kWarps - 1) / kWarps;
+  if (blocks > 152 * 2) blocks = 152 * 2;
+  kern<<<(unsigned) blocks, kThreads, smem, s>>>(a, iteration, fused, staged);
+}
+
+template <int S>
+void launch_ls_add_source_s(const SolverArgs& a, int update, cudaStream_t s) {
+  ls_add_source_kernel<S><<<row_grid(a.num_fsrs), kRowThreads, 0, s>>>(a,
+                                                                       update);
+}
+
+}  // namespace
+
+void launch_ls_sources(const SolverArgs& a, int iteration, int fused,
+                       cudaStream_t s) {
+  switch ((a.num_groups + 31) / 32) {
+    case 1: launch_ls_sources_s<1>(a, iteration, fused, s); break;
+    case 2: launch_ls_sources_s<2>(a, iteration, fused, s); break;
+    case 3: launch_ls_sources_s<3>(a, iteration, fused, s); break;
+    case 4: launch_ls_sources_s<4>(a, iteration, fused, s); break;
+    default: launch_ls_sources_s<8>(a, iteration, fused, s); break;
+  }
+}
+
+void launch_ls_add_source(const SolverArgs& a, int update, cudaStream_t s) {
+  switch ((a.num_groups + 31) / 32) {
+    case 1: launch_ls_add_source_s<1>(a, update, s); break;
+    case 2: launch_ls_add_source_s<2>(a, update, s); break;
+    case 3: launch_ls_add_source_s<3>(a, update, s); break;
+    case 4: launch_ls_add_source_s<4>(a, update, s); break;
+    default: launch_ls_add_source_s<8>(a, update, s); break;
+  }
+}
+
+void launch_ls_scale_moments(const SolverArgs& a, cudaStream_t s) {
+  ls_scale_moments_kernel<<<grid_for(a.num_fsrs * a.ld / 2, kThreads),
+                            kThreads, 0, s>>>(a);
 }
 
 }  // namespace moc

@@ -66,6 +66,8 @@ def _lib():
                                           C.c_double, C.c_int32, C.c_int32,
                                           C.POINTER(C.c_void_p)]
         L.moc_lattice_extrude.restype = C.c_int
+        L.moc_lattice_export_ls.argtypes = [C.c_void_p] + [C.c_void_p] * 7
+        L.moc_lattice_export_ls.restype = C.c_int
         L.moc_lattice_destroy.argtypes = [C.c_void_p]
         L.moc_lattice_destroy.restype = C.c_int
         L.moc_lattice_last_error.restype = C.c_char_p
@@ -124,13 +126,19 @@ def lattice(nx: int, ny: int, pin_material: np.ndarray, materials: Sequence[Mate
             pitch: float = 1.26, pin_radius: float = 0.54, fuel_rings: int = 3,
             fuel_sectors: int = 8, mod_sectors: int = 8, num_polar: int = 6,
             bc=(REFLECTIVE, REFLECTIVE, REFLECTIVE, REFLECTIVE),
-            num_threads: int = 0, extrude: Optional[dict] = None) -> Problem:
+            num_threads: int = 0, extrude: Optional[dict] = None,
+            linear_source: bool = False) -> Problem:
     """Tracks, segments and cross sections of an nx x ny pin lattice.
     ``pin_material[row, col]`` (row 0 = top) is the material inside each
     pin; ``bc`` is (xmin, xmax, ymin, ymax).  ``extrude`` = dict(height,
     fuel_height, z_spacing, num_polar) turns it into explicit 3D tracks of
     the lattice extruded axially (moderator above fuel_height, vacuum at
-    bottom and top; ``num_polar`` Gauss-Legendre polar angles)."""
+    bottom and top; ``num_polar`` Gauss-Legendre polar angles).
+    ``linear_source`` also exports the linear-source geometry (2D only):
+    segment starts relative to the FSR centroids and the angle data, as
+    ``Problem.linear_source``."""
+    if linear_source and extrude is not None:
+        raise ValueError("the linear-source geometry needs 2D tracks")
     L = _lib()
     pm = np.ascontiguousarray(np.asarray(pin_material, np.int32).reshape(ny, nx))
     spec = _Spec(nx, ny, pitch, pin_radius, fuel_rings, fuel_sectors, mod_sectors,
@@ -165,6 +173,16 @@ def lattice(nx: int, ny: int, pin_material: np.ndarray, materials: Sequence[Mate
         L.moc_lattice_export(h, *[arr[k].ctypes.data for k in (
             "seg_len", "seg_fsr", "seg_off", "track_ang", "next", "flags", "weights",
             "inv_sin", "fsr_mat", "fsr_vol")])
+        ls = None
+        if linear_source:
+            ls = dict(seg_x=np.empty(S, np.float32), seg_y=np.empty(S, np.float32),
+                      centroid=np.empty(2 * R), ang_dir=np.empty(2 * A),
+                      ang_wgt=np.empty(A), pol_sin=np.empty(A * Ph),
+                      pol_wgt=np.empty(A * Ph))
+            if L.moc_lattice_export_ls(h, *[ls[k].ctypes.data for k in (
+                    "seg_x", "seg_y", "centroid", "ang_dir", "ang_wgt", "pol_sin",
+                    "pol_wgt")]):
+                raise RuntimeError(L.moc_lattice_last_error().decode())
     finally:
         L.moc_lattice_destroy(h)
     st, ss, nf, ch = pack_materials(materials)
@@ -174,6 +192,7 @@ def lattice(nx: int, ny: int, pin_material: np.ndarray, materials: Sequence[Mate
                 num_segments=S, solve_3d=0 if extrude is None else 1,
                 sigma_t=st, sigma_s=ss, nu_sigma_f=nf,
                 chi=ch, **arr)
+    p.linear_source = ls
     p.meta = dict(nx=nx, ny=ny, num_azim=num_azim, spacing=spacing, pitch=pitch,
                   num_polar=num_polar)
     return p.contiguous()
@@ -192,29 +211,30 @@ def _fuel_mod(config: int, G: int, n_fuel: int = 1, perturb=None):
 
 
 def pin_cell(num_groups: int = 7, num_azim: int = 32, spacing: float = 0.05,
-             config: int = 0, perturb=None) -> Problem:
+             config: int = 0, perturb=None, linear_source: bool = False) -> Problem:
     """One pin cell, all reflective (the 7-group pin-cell benchmark)."""
     mats = _fuel_mod(config, num_groups, 1, perturb)
     return lattice(1, 1, np.zeros((1, 1), np.int32), mats, 1,
-                   num_azim=num_azim, spacing=spacing)
+                   num_azim=num_azim, spacing=spacing, linear_source=linear_source)
 
 
 def square_lattice(n: int, num_groups: int, num_azim: int, spacing: float,
                    config: int, water_pins: Optional[List] = None,
-                   perturb=None) -> Problem:
+                   perturb=None, linear_source: bool = False) -> Problem:
     """n x n lattice of the pin; ``water_pins`` positions hold moderator."""
     mats = _fuel_mod(config, num_groups, 1, perturb)
     pm = np.zeros((n, n), np.int32)
     for (r, c) in (water_pins or []):
         pm[r, c] = 1
-    return lattice(n, n, pm, mats, 1, num_azim=num_azim, spacing=spacing)
+    return lattice(n, n, pm, mats, 1, num_azim=num_azim, spacing=spacing,
+                   linear_source=linear_source)
 
 
 def assembly_17x17(num_groups: int = 70, num_azim: int = 64, spacing: float = 0.05,
-                   config: int = 1, perturb=None) -> Problem:
+                   config: int = 1, perturb=None, linear_source: bool = False) -> Problem:
     """17 x 17 assembly with 25 water-filled guide-tube positions."""
     return square_lattice(17, num_groups, num_azim, spacing, config,
-                          GUIDE_TUBES_17x17, perturb)
+                          GUIDE_TUBES_17x17, perturb, linear_source)
 
 
 def assembly_17x17_3d(num_groups: int = 7, num_azim: int = 16, spacing: float = 0.1,

@@ -55,6 +55,11 @@ _ARRAY_DTYPES = {
     "fsr_vol": np.float32,
 }
 
+LS_KEYS = ("seg_x", "seg_y", "ang_dir", "ang_wgt", "pol_sin", "pol_wgt")
+LS_DTYPES = {"seg_x": np.float32, "seg_y": np.float32, "ang_dir": np.float64,
+             "ang_wgt": np.float64, "pol_sin": np.float64, "pol_wgt": np.float64,
+             "centroid": np.float64}
+
 FLAG_NEXT_FWD_IS_FWD = 1
 FLAG_NEXT_BWD_IS_FWD = 2
 FLAG_TRANSFER_FWD = 4
@@ -87,6 +92,11 @@ class Problem:
     fsr_vol: np.ndarray
     fixed_sources: Optional[np.ndarray] = None
     meta: Dict[str, float] = field(default_factory=dict)
+    # Linear-source geometry (2D; CPULSSolver): seg_x, seg_y [S] float32
+    # start of each segment relative to its FSR centroid; ang_dir [A][2]
+    # cos/sin phi, ang_wgt [A] azimuthal spacing x weight, pol_sin and
+    # pol_wgt [A][Ph] (float64); optionally centroid [R][2] (float64).
+    linear_source: Optional[Dict[str, np.ndarray]] = None
 
     @property
     def fluxes_per_track(self) -> int:
@@ -110,6 +120,9 @@ class Problem:
             setattr(self, name, np.ascontiguousarray(getattr(self, name), dtype=dt))
         if self.fixed_sources is not None:
             self.fixed_sources = np.ascontiguousarray(self.fixed_sources, np.float32)
+        if self.linear_source is not None:
+            self.linear_source = {k: np.ascontiguousarray(v, LS_DTYPES.get(k, v.dtype))
+                                  for k, v in self.linear_source.items()}
         return self
 
     def validate(self, deep: bool = True) -> None:
@@ -206,6 +219,9 @@ def load_packed(base: str) -> Tuple[Problem, Dict[str, float], Dict[str, np.ndar
     for key in ("fixed_sources", "fixed_source"):
         if key in arrays:
             p.fixed_sources = arrays[key]
+    if "ls_seg_x" in arrays:
+        p.linear_source = {k: arrays["ls_" + k] for k in LS_KEYS + ("centroid",)
+                           if "ls_" + k in arrays}
     p.meta = dict(sc)
     return p.contiguous(), sc, arrays
 
@@ -215,6 +231,9 @@ def save_packed(base: str, p: Problem, extra_scalars=None, extra_arrays=None) ->
     arrays = {k: getattr(p, k) for k in _ARRAY_DTYPES}
     if p.fixed_sources is not None:
         arrays["fixed_sources"] = p.fixed_sources
+    if p.linear_source is not None:
+        for k, v in p.linear_source.items():
+            arrays["ls_" + k] = np.ascontiguousarray(v, LS_DTYPES.get(k, v.dtype))
     if extra_arrays:
         arrays.update(extra_arrays)
     scalars = {k: getattr(p, k) for k in (

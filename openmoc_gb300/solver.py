@@ -58,6 +58,7 @@ class GB300Solver:
         self._keff = 1.0
         self._shape = None
         self._source_kind = "auto"
+        self._negative_ok = False
         if track_generator is not None:
             self.setTrackGenerator(track_generator)
 
@@ -117,6 +118,8 @@ class GB300Solver:
             self._call("moc_set_sweep_shape", *self._shape)
         if self._source_kind != "auto":
             self._call("moc_set_source_kernel", self._SOURCE_KINDS[self._source_kind])
+        if self._negative_ok:
+            self._call("moc_set_negative_fluxes_allowed", 1)
         self._fixed = {}
         self._fixed_by_material = {}
         if p.fixed_sources is not None:
@@ -136,6 +139,13 @@ class GB300Solver:
 
     def getConvergenceThreshold(self) -> float:
         return self._threshold
+
+    def allowNegativeFluxes(self, negative_fluxes_on: bool) -> None:
+        """Solver::allowNegativeFluxes (src/Solver.cpp:623): negative
+        sources and fluxes are kept instead of clamped."""
+        self._negative_ok = bool(negative_fluxes_on)
+        if self._ctx is not None:
+            self._call("moc_set_negative_fluxes_allowed", int(self._negative_ok))
 
     def useExponentialInterpolation(self) -> None:
         """Shared-memory table evaluation of 1 - exp(-x) (the default)."""
@@ -485,3 +495,140 @@ class GB300Solver:
     def setStartFlux(self, psi) -> None:
         a = np.ascontiguousarray(psi, np.float32).ravel()
         self._call("moc_set_start_flux", _ptr(a), a.size)
+
+
+class GB300LSSolver(GB300Solver):
+    """The linear-source solver with OpenMOC's CPULSSolver API
+    (``src/CPULSSolver.h``): flat plus linear (x, y) source and flux moments
+    per FSR, for 2D tracks.
+
+    The linear-source geometry -- each segment's start relative to its FSR
+    centroid, the track direction, azimuthal and polar weights of every angle
+    row -- comes from ``linear_source`` or from the problem's own
+    ``linear_source`` (``pack_linear_source`` in
+    ``openmoc_gb300/adapter/pack_reference.h``, or
+    :func:`openmoc_gb300.lattice.lattice`); the expansion matrices and source
+    constants are computed on the GPU when the tracks are set.
+    """
+
+    def __init__(self, track_generator: Optional[Problem] = None,
+                 linear_source: Optional[dict] = None, device: int = 0):
+        self._ls = linear_source
+        self._fixed_moments = {}
+        super().__init__(track_generator, device)
+
+    def setTrackGenerator(self, track_generator: Problem) -> None:
+        super().setTrackGenerator(track_generator)
+        ls = self._ls if self._ls is not None else self._problem.linear_source
+        if ls is None:
+            raise _native.MOCError(-1, "the linear-source solver needs segment "
+                                       "start positions and angle data")
+        self.setLinearSource(ls)
+
+    def setLinearSource(self, ls: dict) -> None:
+        """Uploads the linear-source geometry (the keys of
+        ``openmoc_gb300.problem.LS_KEYS``) and computes the expansion
+        constants."""
+        self._need_ctx()
+        p = self._problem
+        arrs = {}
+        for k, dt, n in (("seg_x", np.float32, p.num_segments),
+                         ("seg_y", np.float32, p.num_segments),
+                         ("ang_dir", np.float64, 2 * p.num_angles),
+                         ("ang_wgt", np.float64, p.num_angles),
+                         ("pol_sin", np.float64, p.num_angles * p.num_polar_half),
+                         ("pol_wgt", np.float64, p.num_angles * p.num_polar_half)):
+            if k not in ls:
+                raise _native.MOCError(-1, f"linear-source geometry lacks {k}")
+            a = np.ascontiguousarray(ls[k], dt).ravel()
+            if a.size != n:
+                raise _native.MOCError(-1, f"{k} has {a.size} values, expected {n}")
+            arrs[k] = a
+        self._ls_arrays = arrs
+        g = _native.LSGeometry(*(_ptr(arrs[k]) for k in ("seg_x", "seg_y", "ang_dir",
+                                                          "ang_wgt", "pol_sin",
+                                                          "pol_wgt")))
+        self._call("moc_set_linear_source", C.byref(g))
+        self._fixed_moments = {}
+
+    def getNumFlatSourceRegions(self) -> int:
+        """FSRs whose expansion matrix is singular (flat source there)."""
+        self._need_ctx()
+        on, n = C.c_int(), C.c_int64()
+        self._call("moc_get_linear_source", C.byref(on), C.byref(n))
+        return n.value
+
+    # ------------------------------------------------- fixed source moments
+    def setFixedSourceMomentByFSR(self, fsr_id: int, group: int, src_x: float,
+                                  src_y: float, src_z: float = 0.0) -> None:
+        """CPULSSolver::setFixedSourceMomentByFSR (src/CPULSSolver.cpp:
+        280-307); group is 1-based, z ignored for 2D tracks."""
+        p = self._problem
+        if group <= 0 or group > p.num_groups:
+            raise _native.MOCError(-1, f"Unable to set fixed source for group {group} "
+                                       f"in a {p.num_groups} energy group problem")
+        if fsr_id < 0 or fsr_id >= p.num_fsrs:
+            raise _native.MOCError(-1, f"Unable to set fixed source for FSR {fsr_id} "
+                                       f"with only {p.num_fsrs} FSRs in the geometry")
+        self._fixed_moments[(int(fsr_id), int(group))] = (float(src_x), float(src_y),
+                                                          float(src_z))
+        m = np.zeros((p.num_fsrs, 3, p.num_groups), np.float32)
+        for (r, g), v in self._fixed_moments.items():
+            m[r, :, g - 1] = v
+        self.setFixedSourceMoments(m)
+
+    def setFixedSourceMoments(self, moments) -> None:
+        """Every FSR's fixed source moments at once, [R, 3, G] (x, y, z)."""
+        self._need_ctx()
+        a = np.ascontiguousarray(moments, np.float32).ravel()
+        self._fixed_moment_array = a
+        self._call("moc_set_fixed_source_moments", _ptr(a), a.size)
+
+    def resetFixedSources(self) -> None:
+        super().resetFixedSources()
+        self._fixed_moments = {}
+        if self._ctx is not None:
+            self._call("moc_set_fixed_source_moments", None, 0)
+
+    # ------------------------------------------------------------- results
+    def _moments(self, fn: str) -> np.ndarray:
+        self._need_ctx()
+        p = self._problem
+        out = np.empty(p.num_fsrs * 3 * p.num_groups, np.float32)
+        self._call(fn, _ptr(out), out.size)
+        return out.reshape(p.num_fsrs, 3, p.num_groups)
+
+    def getFluxMoments(self) -> np.ndarray:
+        """The flux moments [R, 3, G] (x, y, z), CPULSSolver::_scalar_flux_xyz."""
+        return self._moments("moc_get_flux_moments")
+
+    def setFluxMoments(self, moments) -> None:
+        self._need_ctx()
+        a = np.ascontiguousarray(moments, np.float32).ravel()
+        self._call("moc_set_flux_moments", _ptr(a), a.size)
+
+    def getSourceMoments(self) -> np.ndarray:
+        """The reduced source moments [R, 3, G], _reduced_sources_xyz."""
+        return self._moments("moc_get_source_moments")
+
+    def getLinearExpansion(self):
+        """(inverse expansion matrices [R, 3] (xx, yy, xy), source constants
+        [R, 3, G]): getLinearExpansionCoeffsBuffer /
+        getSourceConstantsBuffer."""
+        self._need_ctx()
+        p = self._problem
+        il = np.empty(3 * p.num_fsrs, np.float64)
+        sc = np.empty(3 * p.num_fsrs * p.num_groups, np.float32)
+        self._call("moc_get_linear_expansion", _ptr(il), _ptr(sc))
+        return il.reshape(p.num_fsrs, 3), sc.reshape(p.num_fsrs, 3, p.num_groups)
+
+    def getFluxByPosition(self, fsr_id: int, dx: float, dy: float,
+                          group: int) -> float:
+        """The linear flux at offset (dx, dy) from the FSR's centroid:
+        CPULSSolver::getFluxByCoords (src/CPULSSolver.cpp:1082-1133) with the
+        point given relative to the centroid."""
+        il, _ = self.getLinearExpansion()
+        m = self.getFluxMoments()[fsr_id, :, group - 1]
+        flat = float(self.getFluxes()[fsr_id, group - 1])
+        a, b, c = il[fsr_id]
+        return flat + dx * (a * m[0] + c * m[1]) + dy * (c * m[0] + b * m[1])
