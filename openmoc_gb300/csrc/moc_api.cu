@@ -482,12 +482,11 @@ void enqueue_add_source(moc_ctx* c, const moc::SolverArgs& a, int update) {
   }
 }
 
-// zero flux tallies (and moments) without computing sources
+// zero flux tallies (and moments) without computing sources; skipped, like
+// every kernel of the loop, once the device reports the solve done
 int enqueue_zero_tallies(moc_ctx* c, const moc::SolverArgs& a) {
   moc::launch_zero_phi(a, c->stream);
   c->launches++;
-  if (c->ls)
-    MOC_CUDA(cudaMemsetAsync(c->mom, 0, 8 * num_flux(c), c->stream));
   return MOC_OK;
 }
 

@@ -431,12 +431,18 @@ __global__ void scale_phi_kernel(const SolverArgs a) {
     a.phi[i] = (float) ((double) a.phi[i] * f);
 }
 
+// zeroes the flux tallies (and the moment tallies of a linear source)
 __global__ void zero_phi_kernel(const SolverArgs a) {
   if (skip(a)) return;
   const int64_t n = a.num_fsrs * a.ld;
   for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t) gridDim.x * blockDim.x)
+       i += (int64_t) gridDim.x * blockDim.x) {
     a.phi[i] = 0.0f;
+    if (a.mom) {
+      a.mom[2 * i] = 0.0f;
+      a.mom[2 * i + 1] = 0.0f;
+    }
+  }
 }
 
 __global__ void fill_kernel(float* p, int64_t n, float v) {
@@ -1051,8 +1057,8 @@ void launch_scale_phi(const SolverArgs& a, cudaStream_t s) {
 }
 
 void launch_zero_phi(const SolverArgs& a, cudaStream_t s) {
-  zero_phi_kernel<<<grid_for(a.num_fsrs * a.num_groups, kThreads), kThreads,
-                    0, s>>>(a);
+  zero_phi_kernel<<<grid_for(a.num_fsrs * a.ld, kThreads), kThreads, 0, s>>>(
+      a);
 }
 
 void launch_fill(float* p, int64_t n, float v, cudaStream_t s) {
