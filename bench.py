@@ -33,6 +33,10 @@ WORKLOAD = "17x17 pin lattice, 70 groups, 64 azimuthal, 0.05 cm, TY-6 (3 polar),
 METRIC = "segment*group*polar integrations/s"
 FLOPS_PER_INTEGRATION = 30     # FP32 flops of one 2D integration (FMA = 2)
 FLOPS_PER_INTEGRATION_3D = 28  # 3D: no 1/sin(theta) scaling
+# linear source (2D): the rational G(x) (11 FMA, a reciprocal, a multiply),
+# F1/F2/H from it, the flat and linear source terms, the update and the
+# scalar-flux and x/y moment tallies, per (segment, group, polar)
+FLOPS_PER_LS_INTEGRATION = 48
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one sweep launch
 # of this workload, from one ncu capture per sweep shape (lanes per track
 # direction, group pairs per lane, exponential kind); the summaries are under
@@ -70,14 +74,15 @@ def load_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
 
 
-def algorithmic_bytes(p):
-    """Compulsory HBM bytes of one sweep: packed segments read once (8 B),
-    per-track offsets/links/flags (16 B), angular flux in and out for both
-    directions (16 B per track and flux value), sources read and tallies
-    written (8 B per FSR and group)."""
+def algorithmic_bytes(p, ls=False):
+    """Compulsory HBM bytes of one sweep: packed segments read once (8 B;
+    16 B with the linear source's start position), per-track
+    offsets/links/flags (16 B), angular flux in and out for both directions
+    (16 B per track and flux value), sources read and tallies written (8 B
+    per FSR and group; 24 B with the x / y source and flux moments)."""
     F = p.fluxes_per_track
-    return (8 * p.num_segments + 16 * p.num_tracks + 16 * p.num_tracks * F
-            + 8 * p.num_fsrs * p.num_groups)
+    return ((16 if ls else 8) * p.num_segments + 16 * p.num_tracks
+            + 16 * p.num_tracks * F + (24 if ls else 8) * p.num_fsrs * p.num_groups)
 
 
 class Clocks:
@@ -145,7 +150,12 @@ WORKLOADS = {
     "assembly3d": "17x17 assembly extruded to 20 cm (fuel below 16 cm, moderator above), "
                   "7 groups, explicit 3D tracks: 16 azimuthal, 6 polar, 0.1 cm radial, "
                   "0.5 cm axial; reflective radially, vacuum top and bottom",
+    "assembly70_ls": WORKLOAD + ", linear source (CPULSSolver)",
 }
+
+
+def is_ls(workload):
+    return workload.endswith("_ls")
 
 
 def build_problem(workload="assembly70"):
@@ -154,13 +164,20 @@ def build_problem(workload="assembly70"):
         return lattice.core_51x51()
     if workload == "assembly3d":
         return lattice.assembly_17x17_3d()
+    if workload == "assembly70_ls":
+        return lattice.assembly_17x17(linear_source=True)
     return lattice.assembly_17x17()
 
 
 def cpu_reference_rate(p, iters, threads):
-    """Integrations/s of the oracle's source iteration on the host cores."""
-    from oracle.oracle import Oracle
-    o = Oracle(p, "f32", num_threads=threads)
+    """Integrations/s of the oracle's source iteration on the host cores
+    (CPULSSolver's when the problem carries a linear source)."""
+    from oracle.oracle import LSOracle, Oracle
+    if p.linear_source is not None:
+        o = LSOracle(p, p.linear_source, "f32", num_threads=threads)
+        o.constants()
+    else:
+        o = Oracle(p, "f32", num_threads=threads)
     o.keff = 1.0
     o.phi[:] = 1.0
     o.normalize()
@@ -220,17 +237,19 @@ def run_gpu(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
-    from openmoc_gb300 import GB300Solver
+    from openmoc_gb300 import GB300LSSolver, GB300Solver
     from openmoc_gb300.solver import FISSION_SOURCE
 
     p = build_problem(args.workload)
+    ls = is_ls(args.workload)
     peaks, peak_kind = load_peaks()
-    s = GB300Solver(p, device=local)
+    s = (GB300LSSolver if ls else GB300Solver)(p, device=local)
     if args.shape:
         # a fixed kernel shape (e.g. to profile one instance)
         lps, slots, exp_kind = (int(v) for v in args.shape.split(","))
         s.setSweepShape(lps, slots)
-        (s.useExponentialIntrinsic if exp_kind else s.useExponentialInterpolation)()
+        if not ls:
+            (s.useExponentialIntrinsic if exp_kind else s.useExponentialInterpolation)()
         tuning = []
     else:
         lps, slots, exp_kind = s.autotune()
@@ -250,7 +269,7 @@ def run_gpu(args):
     # the source contraction both ways: 3xTF32 tensor cores (the default at
     # 70 groups) against the FP32 CUDA-core kernel, same iterations
     sources = {"kernel": s.getSourceContraction()}
-    kinds = ("fp32", "tf32x3") if 64 <= p.num_groups <= 96 else ()
+    kinds = ("fp32", "tf32x3") if 64 <= p.num_groups <= 96 and not ls else ()
     for kind in kinds:
         s.setSourceContraction(kind)
         st, sw = s.benchIterations(max(args.steps // 2, 5), FISSION_SOURCE, True)
@@ -268,7 +287,7 @@ def run_gpu(args):
 
     # roofline of the dominant kernel (the sweep)
     sweep_avg = float(np.mean(sweep_ms))
-    nbytes = algorithmic_bytes(p)
+    nbytes = algorithmic_bytes(p, ls)
     achieved = nbytes / (sweep_avg * 1e-3) / 1e9
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     traffic = (SWEEP_DRAM_BYTES.get((lps, slots, exp_kind))
@@ -276,7 +295,8 @@ def run_gpu(args):
     sm_mhz = clocks.get("sm_mhz") or float(peaks.get("sm_max_mhz", 2070.0))
     props = torch.cuda.get_device_properties(local)
     fp32_peak = props.multi_processor_count * 128 * 2 * sm_mhz * 1e6 / 1e12
-    flops_per_int = FLOPS_PER_INTEGRATION_3D if p.solve_3d else FLOPS_PER_INTEGRATION
+    flops_per_int = (FLOPS_PER_LS_INTEGRATION if ls else
+                     FLOPS_PER_INTEGRATION_3D if p.solve_3d else FLOPS_PER_INTEGRATION)
     fp32_achieved = ints * flops_per_int / (sweep_avg * 1e-3) / 1e12
 
     # end to end through the public API: host buffers (pinned), upload,
@@ -306,8 +326,10 @@ def run_gpu(args):
                        "integrations_per_step": ints, "l2": "flushed before every step",
                        "sweep_shape": {"lanes_per_track_direction": lps,
                                        "group_pairs_per_lane": slots,
-                                       "exponential": ["shared-memory table",
-                                                       "hardware ex2"][exp_kind]},
+                                       "exponential": ("rational G(x), F1/F2/H from it"
+                                                       if ls else
+                                                       ["shared-memory table",
+                                                        "hardware ex2"][exp_kind])},
                        "autotune_ms": {f"{a}x{b}/{'table' if e == 0 else 'ex2'}": round(t, 4)
                                        for a, b, e, t in tuning},
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
@@ -348,7 +370,7 @@ def end_to_end(p, args, device, torch):
     """The metric through GB300Solver: per step, upload the problem from
     pinned host memory, run a fixed number of iterations, copy the fluxes
     back."""
-    from openmoc_gb300 import GB300Solver, Problem
+    from openmoc_gb300 import GB300LSSolver, GB300Solver, Problem
     pinned = {}
     h2d = 0
     for k in ("seg_len", "seg_fsr", "seg_off", "track_ang", "next", "flags", "weights",
@@ -361,12 +383,23 @@ def end_to_end(p, args, device, torch):
     q = Problem(**{f: getattr(p, f) for f in p.__dataclass_fields__})
     for k, (_, arr) in pinned.items():
         setattr(q, k, arr)
+    if p.linear_source is not None:
+        q.linear_source = {}
+        for k, a in p.linear_source.items():
+            if k == "centroid":
+                continue
+            t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True)
+            t.numpy()[:] = a.view(np.uint8)
+            pinned["ls_" + k] = (t, t.numpy().view(a.dtype))
+            q.linear_source[k] = pinned["ls_" + k][1]
+            h2d += a.nbytes
     d2h = p.num_fsrs * p.num_groups * 4
     times = []
     for i in range(args.e2e_steps + 1):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        s = GB300Solver(q, device=device)
+        s = (GB300LSSolver if p.linear_source is not None else GB300Solver)(
+            q, device=device)
         s.setConvergenceThreshold(1e-30)
         s.computeEigenvalue(args.e2e_iters)
         flux = s.getFluxes()

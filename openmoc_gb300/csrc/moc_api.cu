@@ -382,11 +382,12 @@ int enqueue_sweep(moc_ctx* c, int check_done, bool timed, int ev_index) {
 // on the context's own problem (median of three sweeps after one warm-up).
 // Results are cached per problem size for the process.
 struct TuneKey {
-  int G, Ph, M, exp_fixed, exp_kind;
+  int G, Ph, M, exp_fixed, exp_kind, ls;
   int64_t T, S, R;
   bool operator<(const TuneKey& o) const {
-    return std::tie(G, Ph, M, exp_fixed, exp_kind, T, S, R) <
-           std::tie(o.G, o.Ph, o.M, o.exp_fixed, o.exp_kind, o.T, o.S, o.R);
+    return std::tie(G, Ph, M, exp_fixed, exp_kind, ls, T, S, R) <
+           std::tie(o.G, o.Ph, o.M, o.exp_fixed, o.exp_kind, o.ls, o.T, o.S,
+                    o.R);
   }
 };
 using TuneVal = moc_tune_entry;
@@ -415,7 +416,8 @@ int time_sweep(moc_ctx* c, int reps, float* median_ms) {
 int autotune_sweep(moc_ctx* c, bool use_cache) {
   TuneKey key{c->d.num_groups, c->d.num_polar_half, c->d.num_materials,
               c->exp_user_set, c->exp_user_set ? c->exp_kind : -1,
-              c->d.num_tracks, c->d.num_segments, c->d.num_fsrs};
+              c->ls ? 1 : 0, c->d.num_tracks, c->d.num_segments,
+              c->d.num_fsrs};
   if (use_cache) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune_cache.find(key);
@@ -429,14 +431,15 @@ int autotune_sweep(moc_ctx* c, bool use_cache) {
   }
   const int G = c->d.num_groups;
   std::vector<int> kinds;
-  if (c->exp_user_set) kinds.push_back(c->exp_kind);
+  // the linear-source sweep has one exponential evaluator
+  if (c->exp_user_set || c->ls) kinds.push_back(c->exp_kind);
   else kinds = {MOC_EXP_TABLE, MOC_EXP_INTRINSIC};
   TuneVal best{0, 0, 0, 1e30f};
   c->tune_log.clear();
   for (int kind : kinds) {
     for (int lps = 1; lps <= 32; lps *= 2) {
       const int slots = pair_slots(G, lps);
-      if (slots > moc::kMaxSlots || lane_use(G, lps, slots) < 0.5) continue;
+      if (slots > max_slots(c) || lane_use(G, lps, slots) < 0.5) continue;
       c->lps = lps;
       c->slots = slots;
       c->exp_kind = kind;
@@ -498,9 +501,6 @@ int zero_moments(moc_ctx* c) {
 }
 
 int maybe_autotune(moc_ctx* c) {
-  // the autotuner times flat-source sweeps; linear-source contexts keep
-  // the heuristic shape unless one is set
-  if (c->ls) return MOC_OK;
   if (c->autotune && !c->tuned && !c->shape_user_set)
     return autotune_sweep(c, true);
   return MOC_OK;
@@ -617,6 +617,7 @@ void ls_release(moc_ctx* c) {
   dfree(c->ls_const);
   dfree(c->fixed_xy);
   if (c->ls && !c->shape_user_set) c->lps = c->slots = 0;
+  if (c->ls) c->tuned = false;
   c->ls = false;
   c->ls_num_flat = 0;
 }
@@ -1756,6 +1757,7 @@ int moc_set_linear_source(moc_ctx* c, const moc_ls_geometry* g) {
   }
   c->ls = true;
   if (!c->shape_user_set) c->lps = c->slots = 0;
+  c->tuned = false;
   st = ls_constants(c);
   if (st != MOC_OK) ls_release(c);
   return st;
