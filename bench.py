@@ -268,7 +268,8 @@ def run_gpu(args):
     gpu_launches = s.getLaunchCount() - launches_before
     # the source contraction both ways: 3xTF32 tensor cores (the default at
     # 70 groups) against the FP32 CUDA-core kernel, same iterations
-    sources = {"kernel": s.getSourceContraction()}
+    sources = {"kernel": ("linear source: flat + x/y moments, FP32 CUDA cores" if ls
+                          else s.getSourceContraction())}
     kinds = ("fp32", "tf32x3") if 64 <= p.num_groups <= 96 and not ls else ()
     for kind in kinds:
         s.setSourceContraction(kind)

@@ -36,22 +36,19 @@ namespace {
 
 constexpr double kMinDet = 1e-10;   // src/constants.h:70
 
+// Series coefficients of G2 below: c_m = (m+1)/(m+2)! - 2(m+2)/(m+3)!,
+// m = 1..23, filled once by the host.
+__constant__ double c_g2_series[23];
+
 // G2(x) = 2/3 - (1 + 2/x)(1/x + 1/2 - (1 + 1/x)(1 - exp(-x))/x), the
 // quantity of the reference's expG2_fractional (src/exponentials.h:
-// 283-323); below x = 1 from its series
-//   sum_{m>=1} (-x)^m [(m+1)/(m+2)! - 2(m+2)/(m+3)!]
+// 283-323); below x = 1 from its series sum_{m>=1} c_m (-x)^m by Horner
 // (the closed form cancels there), above from the closed form in FP64.
 __device__ double ls_exp_g2(double x) {
   if (x < 1.0) {
-    double sum = 0.0, xm = 1.0, f = 2.0;   // f = (m+2)!
-    for (int m = 1; m < 24; m++) {
-      xm *= -x;
-      f *= (double) (m + 2);
-      const double c = (double) (m + 1) / f -
-                       2.0 * (double) (m + 2) / (f * (double) (m + 3));
-      sum = fma(c, xm, sum);
-    }
-    return sum;
+    double s = c_g2_series[22];
+    for (int m = 21; m >= 0; m--) s = fma(s, -x, c_g2_series[m]);
+    return -x * s;
   }
   const double f1 = -expm1(-x) / x;
   return 2.0 / 3.0 - (1.0 + 2.0 / x) * (1.0 / x + 0.5 - (1.0 + 1.0 / x) * f1);
@@ -165,6 +162,18 @@ void launch_ls_refresh_ids(const int2* segs, int4* out, int64_t S,
   ls_refresh_kernel<<<(unsigned) grid_for(S, 256), 256, 0, s>>>(segs, out, S);
 }
 
+// c_m for m = 1..23 (index m - 1)
+static void upload_g2_series(cudaStream_t s) {
+  double c[23];
+  double f = 2.0;   // (m+2)!
+  for (int m = 1; m <= 23; m++) {
+    f *= (double) (m + 2);
+    c[m - 1] = (double) (m + 1) / f - 2.0 * (double) (m + 2) / (f * (m + 3));
+  }
+  cudaMemcpyToSymbolAsync(c_g2_series, c, sizeof(c), 0,
+                          cudaMemcpyHostToDevice, s);
+}
+
 void launch_ls_constants(const int4* segs_ls, const int64_t* seg_off,
                          const int32_t* track_ang, int64_t T,
                          const double* ang_dir, const double* ang_wgt,
@@ -176,6 +185,7 @@ void launch_ls_constants(const int4* segs_ls, const int64_t* seg_off,
   cudaMemsetAsync(lem, 0, sizeof(double) * 3 * R, s);
   cudaMemsetAsync(acc, 0, sizeof(double) * 3 * R * G, s);
   cudaMemsetAsync(num_flat, 0, sizeof(unsigned int), s);
+  upload_g2_series(s);
   ls_moments_kernel<<<(unsigned) grid_for(32 * T, 256), 256, 0, s>>>(
       segs_ls, seg_off, track_ang, T, ang_dir, ang_wgt, pol_sin, pol_wgt, Ph,
       sigma_t, fsr_vol, G, lem, acc);

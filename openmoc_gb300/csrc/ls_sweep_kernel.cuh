@@ -40,7 +40,9 @@ namespace moc {
 // squares; openmoc_gb300/csrc/fit_ls_exponential.py derives the
 // coefficients), with P(0)/Q(0) = 1/2 and the leading coefficients equal so
 // that G ~ 1/x for large x.  Relative error 1.6e-7 in exact arithmetic,
-// below 6e-7 evaluated in FP32 (every x from 1e-7 to 5000).
+// below 6e-7 evaluated in FP32 (every x from 1e-7 to 5000).  neg_eval2
+// returns -G (the numerator's coefficients negated), which lets the sweep
+// form every term with plain fused multiply-adds.
 struct LsExpG {
   static constexpr float p0 = 5.0000000000e-01f;
   static constexpr float p1 = 1.7653049922e-01f;
@@ -59,12 +61,12 @@ struct LsExpG {
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v));
     return r;
   }
-  __device__ __forceinline__ static float2 eval2(float2 x) {
-    float2 n = __ffma2_rn(x, f2(p5), f2(p4));
-    n = __ffma2_rn(x, n, f2(p3));
-    n = __ffma2_rn(x, n, f2(p2));
-    n = __ffma2_rn(x, n, f2(p1));
-    n = __ffma2_rn(x, n, f2(p0));
+  __device__ __forceinline__ static float2 neg_eval2(float2 x) {
+    float2 n = __ffma2_rn(x, f2(-p5), f2(-p4));
+    n = __ffma2_rn(x, n, f2(-p3));
+    n = __ffma2_rn(x, n, f2(-p2));
+    n = __ffma2_rn(x, n, f2(-p1));
+    n = __ffma2_rn(x, n, f2(-p0));
     float2 d = __ffma2_rn(x, f2(q6), f2(q5));
     d = __ffma2_rn(x, d, f2(q4));
     d = __ffma2_rn(x, d, f2(q3));
@@ -74,10 +76,6 @@ struct LsExpG {
     return __fmul2_rn(n, make_float2(rcp(d.x), rcp(d.y)));
   }
 };
-
-__device__ __forceinline__ float2 neg2(float2 v) {
-  return make_float2(-v.x, -v.y);
-}
 
 // Blocks of 128 threads kept resident per SM: the register file bounds the
 // busy instances (PH * PS pair-polar values per lane).
@@ -219,24 +217,27 @@ ls_sweep_kernel(const SweepArgs a) {
               __ffma2_rn(qy, f2(c2y), __ffma2_rn(qx, f2(c2x), qf[s]));
           const float2 sl =
               __fmul2_rn(__ffma2_rn(qy, f2(dy), __fmul2_rn(qx, f2(dx))), len2);
+          // gn = -G, u = 1 - x G, m = u - 2 G = -(2G - u):
+          //   delta = (psi - s_f) x u + (s_l x) m
+          //   moment term w l x (u - G) psi = l tau (w / sin) (u + gn) psi
           float2 dacc = f2(0.0f), hacc = f2(0.0f);
 #pragma unroll
           for (int p = 0; p < PH; p++) {
             const float2 x = __fmul2_rn(tau, xs2[p]);
-            const float2 g = LsExpG::eval2(x);
-            const float2 u = __ffma2_rn(neg2(x), g, f2(1.0f));
+            const float2 gn = LsExpG::neg_eval2(x);
+            const float2 u = __ffma2_rn(x, gn, f2(1.0f));
             const float2 att = __fmul2_rn(x, u);
-            const float2 f2u = __ffma2_rn(f2(2.0f), g, neg2(u));
-            const float2 lin = __fmul2_rn(__fmul2_rn(sl, x), f2u);
-            const float2 e = __fadd2_rn(psi[s][p], neg2(sf));
-            const float2 d = __ffma2_rn(e, att, neg2(lin));
-            const float2 h = __fmul2_rn(__fadd2_rn(u, neg2(g)), psi[s][p]);
-            hacc = __ffma2_rn(h, __fmul2_rn(tau, xw2[p]), hacc);
-            psi[s][p] = __fadd2_rn(psi[s][p], neg2(d));
+            const float2 m = __ffma2_rn(f2(2.0f), gn, u);
+            const float2 e = __ffma2_rn(sf, f2(-1.0f), psi[s][p]);
+            const float2 d =
+                __ffma2_rn(e, att, __fmul2_rn(__fmul2_rn(sl, x), m));
+            hacc = __ffma2_rn(__fmul2_rn(__fadd2_rn(u, gn), psi[s][p]), xw2[p],
+                              hacc);
+            psi[s][p] = __ffma2_rn(d, f2(-1.0f), psi[s][p]);
             dacc = __ffma2_rn(w2[p], d, dacc);
           }
           atomicAdd(ph + s * LPS, dacc);
-          const float2 hl = __fmul2_rn(hacc, len2);
+          const float2 hl = __fmul2_rn(__fmul2_rn(hacc, tau), len2);
           const float2 mx = __ffma2_rn(dacc, f2(sx), __fmul2_rn(hl, f2(dx)));
           const float2 my = __ffma2_rn(dacc, f2(sy), __fmul2_rn(hl, f2(dy)));
           atomicAdd(pm + s * LPS, make_float4(mx.x, my.x, mx.y, my.y));
