@@ -104,10 +104,9 @@ void GB300Solver::upload() {
 }
 
 void GB300Solver::initializeFluxArrays() {
-  if (_negative_fluxes_allowed)
-    log_printf(ERROR, "GB300Solver clamps negative fluxes and sources as "
-               "OpenMOC's default does; allowNegativeFluxes is not supported");
   upload();
+  check(moc_set_negative_fluxes_allowed(_ctx, _negative_fluxes_allowed ? 1 : 0),
+        "allowNegativeFluxes");
   check(moc_zero_track_fluxes(_ctx), "zeroTrackFluxes");
 }
 
@@ -333,4 +332,90 @@ void GB300Solver::computeFlux(int max_iters, bool only_fixed_source) {
   check(moc_get_num_iterations(_ctx, &_num_iterations), "getNumIterations");
   _timer->stopTimer();
   _timer->recordSplit("Total time");
+}
+
+/* ---------------------------------------------------------- linear source */
+GB300LSSolver::GB300LSSolver(TrackGenerator* track_generator, int device)
+    : GB300Solver(track_generator, device) {}
+
+void GB300LSSolver::upload() {
+  GB300Solver::upload();
+  openmoc_gb300::PackedProblem p;
+  openmoc_gb300::pack_tracks(_track_generator, p);
+  try {
+    openmoc_gb300::pack_linear_source(_track_generator, p);
+  } catch (std::exception& e) {
+    log_printf(ERROR, "GB300LSSolver: %s", e.what());
+  }
+  moc_ls_geometry g;
+  g.seg_x = p.seg_x.data();
+  g.seg_y = p.seg_y.data();
+  g.ang_dir = p.ang_dir.data();
+  g.ang_wgt = p.ang_wgt.data();
+  g.pol_sin = p.pol_sin.data();
+  g.pol_wgt = p.pol_wgt.data();
+  check(moc_set_linear_source(_ctx, &g), "moc_set_linear_source");
+}
+
+void GB300LSSolver::initializeSourceArrays() {
+  GB300Solver::initializeSourceArrays();
+  if (!_ctx) return;
+  if (_fix_src_xyz_FSR_map.empty()) {
+    check(moc_set_fixed_source_moments(_ctx, NULL, 0), "resetFixedSources");
+    return;
+  }
+  std::vector<float> m((size_t) _num_FSRs * 3 * _num_groups, 0.f);
+  for (std::map<std::pair<long, int>, std::vector<double> >::iterator it =
+           _fix_src_xyz_FSR_map.begin();
+       it != _fix_src_xyz_FSR_map.end(); ++it) {
+    const long r = it->first.first;
+    const int g = it->first.second;
+    for (int i = 0; i < 3; i++)
+      m[((size_t) r * 3 + i) * _num_groups + g - 1] = (float) it->second[i];
+  }
+  check(moc_set_fixed_source_moments(_ctx, m.data(), (int64_t) m.size()),
+        "setFixedSourceMoments");
+}
+
+void GB300LSSolver::setFixedSourceMomentByFSR(long fsr_id, int group,
+                                              double src_x, double src_y,
+                                              double src_z) {
+  if (group <= 0 || group > _num_groups)
+    log_printf(ERROR, "Unable to set fixed source for group %d in "
+               "in a %d energy group problem", group, _num_groups);
+  if (fsr_id < 0 || fsr_id >= _num_FSRs)
+    log_printf(ERROR, "Unable to set fixed source for FSR %ld with only "
+               "%ld FSRs in the geometry", fsr_id, _num_FSRs);
+  std::vector<double>& v = _fix_src_xyz_FSR_map[std::make_pair(fsr_id, group)];
+  v.assign(3, 0.0);
+  v[0] = src_x;
+  v[1] = src_y;
+  v[2] = src_z;
+}
+
+void GB300LSSolver::resetFixedSources() {
+  GB300Solver::resetFixedSources();
+  _fix_src_xyz_FSR_map.clear();
+  if (_ctx) check(moc_set_fixed_source_moments(_ctx, NULL, 0), "resetFixedSources");
+}
+
+void GB300LSSolver::getFluxMoments(FP_PRECISION* out, long n) {
+  if (!_ctx) log_printf(ERROR, "no flux moments computed yet");
+  std::vector<float> f((size_t) n);
+  check(moc_get_flux_moments(_ctx, f.data(), n), "getFluxMoments");
+  for (long i = 0; i < n; i++) out[i] = f[i];
+}
+
+double GB300LSSolver::getFluxByOffset(long fsr_id, double dx, double dy,
+                                      int group) {
+  const double flat = getFlux(fsr_id, group);
+  std::vector<double> il((size_t) _num_FSRs * 3);
+  check(moc_get_linear_expansion(_ctx, il.data(), NULL), "getLinearExpansion");
+  std::vector<float> m((size_t) _num_FSRs * 3 * _num_groups);
+  check(moc_get_flux_moments(_ctx, m.data(), (int64_t) m.size()),
+        "getFluxMoments");
+  const double mx = m[((size_t) fsr_id * 3 + 0) * _num_groups + group - 1];
+  const double my = m[((size_t) fsr_id * 3 + 1) * _num_groups + group - 1];
+  const double* c = &il[(size_t) fsr_id * 3];
+  return flat + dx * (c[0] * mx + c[2] * my) + dy * (c[2] * mx + c[1] * my);
 }

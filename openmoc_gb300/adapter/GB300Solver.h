@@ -24,6 +24,9 @@
 #ifndef OPENMOC_GB300_SOLVER_H_
 #define OPENMOC_GB300_SOLVER_H_
 
+#include <map>
+#include <vector>
+
 #include "Solver.h"
 
 struct moc_ctx;
@@ -36,7 +39,7 @@ class GB300Solver : public Solver {
   bool _uploaded;
 
   void check(int status, const char* what);
-  void upload();
+  virtual void upload();
   int materialIndex(Material* m);
 
   /* Solver hooks (src/Solver.h:334-431) */
@@ -80,6 +83,35 @@ class GB300Solver : public Solver {
   void computeSource(int max_iters = 1000, double k_eff = 1.0,
                      residualType res_type = TOTAL_SOURCE);
   void computeFlux(int max_iters = 1000, bool only_fixed_source = true);
+};
+
+/**
+ * The linear-source counterpart (OpenMOC's CPULSSolver, src/CPULSSolver.h)
+ * for 2D tracks: the same hooks with flat plus x/y source and flux moments.
+ * upload() also packs the segments' start positions relative to the FSR
+ * centroids (re-centred by Solver::initializeFSRs) and the angle data
+ * (pack_linear_source) and hands them to moc_set_linear_source, which
+ * computes the linear expansion matrices and source constants on the GPU.
+ */
+class GB300LSSolver : public GB300Solver {
+ protected:
+  std::map<std::pair<long, int>, std::vector<double> > _fix_src_xyz_FSR_map;
+  void upload();
+  void initializeSourceArrays();
+
+ public:
+  GB300LSSolver(TrackGenerator* track_generator = NULL, int device = 0);
+
+  /** CPULSSolver::setFixedSourceMomentByFSR (src/CPULSSolver.cpp:280-307);
+   *  group is 1-based, src_z is ignored for 2D tracks. */
+  void setFixedSourceMomentByFSR(long fsr_id, int group, double src_x,
+                                 double src_y, double src_z);
+  void resetFixedSources();
+  /** Flux moments [R][3][G] (x, y, z), CPULSSolver::_scalar_flux_xyz. */
+  void getFluxMoments(FP_PRECISION* out, long n);
+  /** Flux at (x, y) relative to the FSR's centroid
+   *  (CPULSSolver::getFluxByCoords, src/CPULSSolver.cpp:1082-1133). */
+  double getFluxByOffset(long fsr_id, double dx, double dy, int group);
 };
 
 #endif

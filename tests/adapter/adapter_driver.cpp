@@ -76,5 +76,13 @@ int main() {
   } catch (std::exception& e) {
     printf("gb300 error: %s\n", e.what());
   }
+  try {
+    GB300LSSolver gpu_ls(&tg);
+    gpu_ls.computeEigenvalue(1000);
+    printf("gb300 ls keff %.8f iterations %d\n", gpu_ls.getKeff(),
+           gpu_ls.getNumIterations());
+  } catch (std::exception& e) {
+    printf("gb300 ls error: %s\n", e.what());
+  }
   return 0;
 }

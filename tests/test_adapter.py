@@ -48,3 +48,7 @@ def test_adapter_builds_and_runs(tmp_path):
         k_cpu = float(lines[0].split()[2])
         k_gpu = float(gpu[0].split()[2])
         assert abs(k_cpu - k_gpu) < 1e-5
+    ls = [l for l in lines if l.startswith("gb300 ls")]
+    assert ls, out.stdout
+    if ls[0].startswith("gb300 ls error"):
+        assert "moc_create failed" in ls[0]
