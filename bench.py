@@ -396,11 +396,13 @@ def end_to_end(p, args, device, torch):
             h2d += a.nbytes
     d2h = p.num_fsrs * p.num_groups * 4
     times = []
+    setups = []
     for i in range(args.e2e_steps + 1):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         s = (GB300LSSolver if p.linear_source is not None else GB300Solver)(
             q, device=device)
+        setup = time.perf_counter() - t0
         s.setConvergenceThreshold(1e-30)
         s.computeEigenvalue(args.e2e_iters)
         flux = s.getFluxes()
@@ -409,11 +411,13 @@ def end_to_end(p, args, device, torch):
         s.close()
         if i > 0:
             times.append(dt)
+            setups.append(setup)
         assert np.isfinite(flux).all()
     t = float(np.mean(times))
     return {"value": p.integrations_per_sweep * args.e2e_iters / t, "unit": "integrations/s",
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-            "iterations_per_step": args.e2e_iters, "seconds_per_step": t}
+            "iterations_per_step": args.e2e_iters, "seconds_per_step": t,
+            "setup_seconds_per_step": float(np.mean(setups))}
 
 
 def run_instances(p, args, iters=10):

@@ -11,9 +11,12 @@
 //   const[r][g] += w_a l / V_r (xc^2, yc^2, xc yc)
 //                + (cos^2, sin^2, sin cos) sum_p l G2(l sigma_t / sin_p)
 //                  w_a l^2 / (2 V_r) 2 w_p sin_p,
-// summed in FP64 (one warp per track, lanes over groups, FP64 atomics), then
-// the 2x2 inverse per FSR, or zeros where the determinant is below 1e-10
-// (the reference falls back to a flat source there).
+// summed in FP64 by one warp per FSR over its own segments (bucketed by FSR
+// first; lanes over groups, no atomics), then the 2x2 inverse per FSR, or
+// zeros where the determinant is below 1e-10 (the reference falls back to a
+// flat source there).
+#include <vector>
+
 #include "moc_internal.cuh"
 
 namespace moc {
@@ -36,22 +39,27 @@ namespace {
 
 constexpr double kMinDet = 1e-10;   // src/constants.h:70
 
-// Series coefficients of G2 below: c_m = (m+1)/(m+2)! - 2(m+2)/(m+3)!,
-// m = 1..23, filled once by the host.
-__constant__ double c_g2_series[23];
-
 // G2(x) = 2/3 - (1 + 2/x)(1/x + 1/2 - (1 + 1/x)(1 - exp(-x))/x), the
 // quantity of the reference's expG2_fractional (src/exponentials.h:
-// 283-323); below x = 1 from its series sum_{m>=1} c_m (-x)^m by Horner
-// (the closed form cancels there), above from the closed form in FP64.
-__device__ double ls_exp_g2(double x) {
-  if (x < 1.0) {
-    double s = c_g2_series[22];
-    for (int m = 21; m >= 0; m--) s = fma(s, -x, c_g2_series[m]);
-    return -x * s;
-  }
-  const double f1 = -expm1(-x) / x;
-  return 2.0 / 3.0 - (1.0 + 2.0 / x) * (1.0 / x + 0.5 - (1.0 + 1.0 / x) * f1);
+// 283-323), in FP32 by a rational x P5(x) / Q6(x) fitted here
+// (csrc/fit_ls_exponential.py): P(0) = -1/12, the slope of G2 at 0, and
+// p5 = q6 / 6 (G2 -> 1/6).  Evaluated in FP32: absolute error 3.3e-7,
+// relative 2.9e-6 where |G2| > 1e-3 and 4.3e-7 below x = 0.01 (the
+// reference's rational is quoted at 1e-6).
+__device__ __forceinline__ float ls_exp_g2(float x) {
+  constexpr float kP[6] = {-8.3333333333e-02f, 2.3162673964e-03f,
+                           1.5046986351e-03f, 5.4518176798e-04f,
+                           4.1676890852e-05f, 9.9593943274e-06f};
+  constexpr float kQ[7] = {1.0000000000e+00f, 6.7217634287e-01f,
+                           2.1929234424e-01f, 4.4564577781e-02f,
+                           6.5545427501e-03f, 6.0865601323e-04f,
+                           5.9756365965e-05f};
+  float n = kP[5], d = kQ[6];
+#pragma unroll
+  for (int k = 4; k >= 0; k--) n = fmaf(n, x, kP[k]);
+#pragma unroll
+  for (int k = 5; k >= 0; k--) d = fmaf(d, x, kQ[k]);
+  return x * n / d;
 }
 
 __global__ void ls_pack_kernel(const int2* segs, const float* x,
@@ -63,74 +71,121 @@ __global__ void ls_pack_kernel(const int2* segs, const float* x,
   }
 }
 
-// One warp per track; lane l takes groups l, l + 32, ...
-__global__ void ls_moments_kernel(const int4* segs, const int64_t* seg_off,
-                                  const int32_t* track_ang, int64_t T,
-                                  const double* ang_dir, const double* ang_wgt,
-                                  const double* pol_sin, const double* pol_wgt,
-                                  int Ph, const float* sigma_t,
-                                  const float* fsr_vol, int G, double* lem,
-                                  double* acc) {
+// The track of every segment (one warp per track).
+__global__ void ls_seg_track_kernel(const int64_t* seg_off, int64_t T,
+                                    int32_t* seg_track) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = ((int64_t) gridDim.x * blockDim.x) >> 5;
   for (int64_t t = ((int64_t) blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-       t < T; t += warps) {
-    const int a = track_ang[t];
-    const double cph = ang_dir[2 * a], sph = ang_dir[2 * a + 1];
-    const double wgt = ang_wgt[a];
-    for (int64_t k = seg_off[t]; k < seg_off[t + 1]; k++) {
-      const int4 w = segs[k];
-      const double len = (double) __int_as_float(w.x);
-      const int fsr = w.y & 0xFFFFFF;
-      const int mat = (int) ((unsigned) w.y >> 24);
-      const double xc = (double) __int_as_float(w.z) + 0.5 * len * cph;
-      const double yc = (double) __int_as_float(w.w) + 0.5 * len * sph;
-      const double vol = (double) fsr_vol[fsr];
-      const double vi = wgt * len / vol;
-      const double src_constant = vi * len / 2.0;
-      if (lane == 0) {
-        const double l2 = len * len / 12.0;
-        atomicAdd(lem + 3 * (int64_t) fsr + 0, vi * (xc * xc + cph * cph * l2));
-        atomicAdd(lem + 3 * (int64_t) fsr + 1, vi * (yc * yc + sph * sph * l2));
-        atomicAdd(lem + 3 * (int64_t) fsr + 2, vi * (xc * yc + sph * cph * l2));
-      }
-      const float* st = sigma_t + (int64_t) mat * G;
-      double* out = acc + (int64_t) fsr * 3 * G;
-      for (int g = lane; g < G; g += 32) {
-        const double tau = len * (double) st[g];
-        double k2 = 0.0;
-        for (int p = 0; p < Ph; p++) {
-          const double sn = pol_sin[a * Ph + p];
-          k2 += ls_exp_g2(tau / sn) * 2.0 * pol_wgt[a * Ph + p] * sn;
-        }
-        k2 *= len * src_constant;
-        atomicAdd(out + g, vi * xc * xc + cph * cph * k2);
-        atomicAdd(out + G + g, vi * yc * yc + sph * sph * k2);
-        atomicAdd(out + 2 * G + g, vi * xc * yc + sph * cph * k2);
-      }
-    }
+       t < T; t += warps)
+    for (int64_t k = seg_off[t] + lane; k < seg_off[t + 1]; k += 32)
+      seg_track[k] = (int32_t) t;
+}
+
+// Segments per FSR.
+__global__ void ls_count_kernel(const int4* segs, int64_t S, int64_t* count) {
+  for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < S;
+       i += (int64_t) gridDim.x * blockDim.x)
+    atomicAdd(reinterpret_cast<unsigned long long*>(count + (segs[i].y & 0xFFFFFF)),
+              1ull);
+}
+
+// Segment ids bucketed by FSR (start[r] .. start[r + 1]); fill counts up.
+__global__ void ls_bucket_kernel(const int4* segs, int64_t S,
+                                 const int64_t* start, int64_t* fill,
+                                 int32_t* list) {
+  for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < S;
+       i += (int64_t) gridDim.x * blockDim.x) {
+    const int r = segs[i].y & 0xFFFFFF;
+    const unsigned long long pos =
+        atomicAdd(reinterpret_cast<unsigned long long*>(fill + r), 1ull);
+    list[start[r] + (int64_t) pos] = (int32_t) i;
   }
 }
 
-__global__ void ls_invert_kernel(const double* lem, const double* acc,
-                                 int64_t R, int G, int ld, float* ilem,
-                                 float* cst, unsigned int* num_flat) {
-  for (int64_t r = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; r < R;
-       r += (int64_t) gridDim.x * blockDim.x) {
-    const double a = lem[3 * r], b = lem[3 * r + 1], c = lem[3 * r + 2];
-    const double det = a * b - c * c;
-    if (fabs(det) < kMinDet) {
-      ilem[3 * r] = ilem[3 * r + 1] = ilem[3 * r + 2] = 0.0f;
-      atomicAdd(num_flat, 1u);
-    } else {
-      ilem[3 * r] = (float) (b / det);
-      ilem[3 * r + 1] = (float) (a / det);
-      ilem[3 * r + 2] = (float) (-c / det);
+// One warp per FSR over its own segments, lanes over groups (S_ groups per
+// lane, G <= 32 S_), sums in FP64 registers: no atomics.  Writes the inverse
+// expansion matrix and the source constants of the FSR.
+template <int S_>
+__global__ void ls_constants_kernel(const int4* segs, const int32_t* list,
+                                    const int64_t* start,
+                                    const int32_t* seg_track,
+                                    const int32_t* track_ang,
+                                    const double* ang_dir,
+                                    const double* ang_wgt,
+                                    const double* pol_sin,
+                                    const double* pol_wgt, int Ph,
+                                    const float* sigma_t, const float* fsr_vol,
+                                    const int32_t* fsr_mat, int64_t R, int G,
+                                    int ld, float* ilem, float* cst,
+                                    unsigned int* num_flat) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t) gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = ((int64_t) blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+       r < R; r += warps) {
+    double l0 = 0.0, l1 = 0.0, l2 = 0.0;
+    double a0[S_], a1[S_], a2[S_];
+    float st[S_];
+    const int m = fsr_mat[r];
+#pragma unroll
+    for (int j = 0; j < S_; j++) {
+      const int g = lane + 32 * j;
+      a0[j] = a1[j] = a2[j] = 0.0;
+      st[j] = (g < G) ? sigma_t[(int64_t) m * G + g] : 0.0f;
     }
-    for (int i = 0; i < 3; i++)
-      for (int g = 0; g < ld; g++)
-        cst[(r * 3 + i) * ld + g] =
-            (g < G) ? (float) acc[(r * 3 + i) * G + g] : 0.0f;
+    const double vol = (double) fsr_vol[r];
+    for (int64_t e = start[r]; e < start[r + 1]; e++) {
+      const int k = list[e];
+      const int4 w = segs[k];
+      const int a = track_ang[seg_track[k]];
+      const double cph = ang_dir[2 * a], sph = ang_dir[2 * a + 1];
+      const double len = (double) __int_as_float(w.x);
+      const double xc = (double) __int_as_float(w.z) + 0.5 * len * cph;
+      const double yc = (double) __int_as_float(w.w) + 0.5 * len * sph;
+      const double vi = ang_wgt[a] * len / vol;
+      const double l12 = len * len / 12.0;
+      l0 += vi * (xc * xc + cph * cph * l12);
+      l1 += vi * (yc * yc + sph * sph * l12);
+      l2 += vi * (xc * yc + sph * cph * l12);
+      // per group: sum_p l G2(l sigma_t / sin_p) (vi l / 2) 2 w_p sin_p
+      const double k2f = len * vi * len / 2.0;
+      const float lenf = __int_as_float(w.x);
+#pragma unroll
+      for (int j = 0; j < S_; j++) {
+        const float tau = lenf * st[j];
+        float k2 = 0.0f;
+        for (int p = 0; p < Ph; p++) {
+          const float sn = (float) pol_sin[a * Ph + p];
+          k2 = fmaf(ls_exp_g2(tau / sn), (float) (2.0 * pol_wgt[a * Ph + p]) * sn,
+                    k2);
+        }
+        const double kk = k2f * (double) k2;
+        a0[j] += vi * xc * xc + cph * cph * kk;
+        a1[j] += vi * yc * yc + sph * sph * kk;
+        a2[j] += vi * xc * yc + sph * cph * kk;
+      }
+    }
+    if (lane == 0) {
+      const double det = l0 * l1 - l2 * l2;
+      if (fabs(det) < kMinDet) {
+        ilem[3 * r] = ilem[3 * r + 1] = ilem[3 * r + 2] = 0.0f;
+        atomicAdd(num_flat, 1u);
+      } else {
+        ilem[3 * r] = (float) (l1 / det);
+        ilem[3 * r + 1] = (float) (l0 / det);
+        ilem[3 * r + 2] = (float) (-l2 / det);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < S_; j++) {
+      const int g = lane + 32 * j;
+      if (g < ld) {
+        const bool on = g < G;
+        cst[(r * 3 + 0) * ld + g] = on ? (float) a0[j] : 0.0f;
+        cst[(r * 3 + 1) * ld + g] = on ? (float) a1[j] : 0.0f;
+        cst[(r * 3 + 2) * ld + g] = on ? (float) a2[j] : 0.0f;
+      }
+    }
   }
 }
 
@@ -162,35 +217,80 @@ void launch_ls_refresh_ids(const int2* segs, int4* out, int64_t S,
   ls_refresh_kernel<<<(unsigned) grid_for(S, 256), 256, 0, s>>>(segs, out, S);
 }
 
-// c_m for m = 1..23 (index m - 1)
-static void upload_g2_series(cudaStream_t s) {
-  double c[23];
-  double f = 2.0;   // (m+2)!
-  for (int m = 1; m <= 23; m++) {
-    f *= (double) (m + 2);
-    c[m - 1] = (double) (m + 1) / f - 2.0 * (double) (m + 2) / (f * (m + 3));
+int launch_ls_constants(const int4* segs_ls, const int64_t* seg_off,
+                        const int32_t* track_ang, int64_t T, int64_t S,
+                        const double* ang_dir, const double* ang_wgt,
+                        const double* pol_sin, const double* pol_wgt, int Ph,
+                        const float* sigma_t, const float* fsr_vol,
+                        const int32_t* fsr_mat, int64_t R, int G, int ld,
+                        float* ilem, float* cst, unsigned int* num_flat,
+                        cudaStream_t s) {
+  // segment buckets by FSR: counts, exclusive scan on the host, scatter
+  int64_t* count = nullptr;
+  int64_t* startp = nullptr;
+  int32_t* list = nullptr;
+  int32_t* seg_track = nullptr;
+  cudaError_t e = cudaMalloc(&count, sizeof(int64_t) * (R + 1));
+  if (e == cudaSuccess) e = cudaMalloc(&startp, sizeof(int64_t) * (R + 1));
+  if (e == cudaSuccess) e = cudaMalloc(&list, sizeof(int32_t) * (S > 0 ? S : 1));
+  if (e == cudaSuccess)
+    e = cudaMalloc(&seg_track, sizeof(int32_t) * (S > 0 ? S : 1));
+  std::vector<int64_t> h((size_t) R + 1, 0);
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(count, 0, sizeof(int64_t) * (R + 1), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(num_flat, 0, sizeof(unsigned), s);
+  if (e == cudaSuccess && S > 0) {
+    ls_count_kernel<<<(unsigned) grid_for(S, 256), 256, 0, s>>>(segs_ls, S,
+                                                               count);
+    ls_seg_track_kernel<<<(unsigned) grid_for(32 * T, 256), 256, 0, s>>>(
+        seg_off, T, seg_track);
+    e = cudaGetLastError();
   }
-  cudaMemcpyToSymbolAsync(c_g2_series, c, sizeof(c), 0,
-                          cudaMemcpyHostToDevice, s);
-}
-
-void launch_ls_constants(const int4* segs_ls, const int64_t* seg_off,
-                         const int32_t* track_ang, int64_t T,
-                         const double* ang_dir, const double* ang_wgt,
-                         const double* pol_sin, const double* pol_wgt,
-                         int Ph, const float* sigma_t, const float* fsr_vol,
-                         int64_t R, int G, int ld, double* lem, double* acc,
-                         float* ilem, float* cst, unsigned int* num_flat,
-                         cudaStream_t s) {
-  cudaMemsetAsync(lem, 0, sizeof(double) * 3 * R, s);
-  cudaMemsetAsync(acc, 0, sizeof(double) * 3 * R * G, s);
-  cudaMemsetAsync(num_flat, 0, sizeof(unsigned int), s);
-  upload_g2_series(s);
-  ls_moments_kernel<<<(unsigned) grid_for(32 * T, 256), 256, 0, s>>>(
-      segs_ls, seg_off, track_ang, T, ang_dir, ang_wgt, pol_sin, pol_wgt, Ph,
-      sigma_t, fsr_vol, G, lem, acc);
-  ls_invert_kernel<<<(unsigned) grid_for(R, 128), 128, 0, s>>>(
-      lem, acc, R, G, ld, ilem, cst, num_flat);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(h.data(), count, sizeof(int64_t) * R,
+                        cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess) {
+    int64_t run = 0;
+    for (int64_t r = 0; r < R; r++) {
+      const int64_t c = h[r];
+      h[r] = run;
+      run += c;
+    }
+    h[R] = run;
+    e = cudaMemcpyAsync(startp, h.data(), sizeof(int64_t) * (R + 1),
+                        cudaMemcpyHostToDevice, s);
+  }
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(count, 0, sizeof(int64_t) * (R + 1), s);
+  if (e == cudaSuccess && S > 0) {
+    ls_bucket_kernel<<<(unsigned) grid_for(S, 256), 256, 0, s>>>(
+        segs_ls, S, startp, count, list);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) {
+    const unsigned blocks = (unsigned) grid_for(32 * R, 256);
+#define MOC_LS_CONST(SS)                                                    \
+  ls_constants_kernel<SS><<<blocks, 256, 0, s>>>(                           \
+      segs_ls, list, startp, seg_track, track_ang, ang_dir, ang_wgt,        \
+      pol_sin, pol_wgt, Ph, sigma_t, fsr_vol, fsr_mat, R, G, ld, ilem, cst, \
+      num_flat)
+    switch ((ld + 31) / 32) {
+      case 1: MOC_LS_CONST(1); break;
+      case 2: MOC_LS_CONST(2); break;
+      case 3: MOC_LS_CONST(3); break;
+      case 4: MOC_LS_CONST(4); break;
+      default: MOC_LS_CONST(8); break;
+    }
+#undef MOC_LS_CONST
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(count);
+  cudaFree(startp);
+  cudaFree(list);
+  cudaFree(seg_track);
+  return e == cudaSuccess ? 0 : (int) e;
 }
 
 }  // namespace moc

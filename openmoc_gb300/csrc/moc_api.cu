@@ -628,31 +628,21 @@ int ls_constants(moc_ctx* c) {
   const int64_t R = c->d.num_fsrs, T = c->d.num_tracks;
   const int G = c->d.num_groups, A = c->d.num_angles;
   const int Ph = c->d.num_polar_half;
-  double* lem = nullptr;
-  double* acc = nullptr;
   unsigned int* nflat = nullptr;
-  MOC_TRY(dalloc(&lem, 3 * R));
-  int st = dalloc(&acc, 3 * R * G);
-  if (st == MOC_OK) st = dalloc(&nflat, 1);
-  if (st != MOC_OK) {
-    dfree(lem);
-    dfree(acc);
-    return st;
-  }
+  MOC_TRY(dalloc(&nflat, 1));
   const double* ang = c->ls_ang;
-  moc::launch_ls_constants(c->segs_ls, c->seg_off, c->track_ang, T, ang,
-                           ang + 2 * A, ang + 3 * A, ang + 3 * A + A * Ph, Ph,
-                           c->sigma_t, c->fsr_vol, R, G, row_stride(c), lem,
-                           acc, c->ls_ilem, c->ls_const, nflat, c->stream);
-  c->launches += 2;
+  const int rc = moc::launch_ls_constants(
+      c->segs_ls, c->seg_off, c->track_ang, T, c->d.num_segments, ang,
+      ang + 2 * A, ang + 3 * A, ang + 3 * A + A * Ph, Ph, c->sigma_t,
+      c->fsr_vol, c->fsr_mat, R, G, row_stride(c), c->ls_ilem, c->ls_const,
+      nflat, c->stream);
+  c->launches += 4;
   unsigned int h = 0;
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = (cudaError_t) rc;
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(&h, nflat, sizeof(h), cudaMemcpyDeviceToHost,
                         c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-  dfree(lem);
-  dfree(acc);
   dfree(nflat);
   if (e != cudaSuccess)
     return fail(MOC_ERR_CUDA, std::string("linear expansion constants: ") +
@@ -1671,6 +1661,9 @@ int moc_set_linear_source(moc_ctx* c, const moc_ls_geometry* g) {
   MOC_CHECK(c->mat_packed, MOC_ERR_UNSUPPORTED,
             "the linear-source sweep needs fewer than 2^24 FSRs and at most "
             "256 materials");
+  MOC_CHECK(c->d.num_groups <= 256 && c->d.num_segments < (1LL << 31),
+            MOC_ERR_UNSUPPORTED,
+            "the linear source takes at most 256 groups and 2^31 segments");
   MOC_CHECK(g->seg_x && g->seg_y && g->ang_dir && g->ang_wgt && g->pol_sin &&
                 g->pol_wgt,
             MOC_ERR_ARG, "null linear-source array");

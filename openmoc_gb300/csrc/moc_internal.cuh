@@ -220,19 +220,19 @@ void launch_sources_tc(const SolverArgs& a, int iteration, int zero_phi,
 // ---- linear source (linear_source.cu, solver_kernels.cu, ls_sweep_*.cu) ----
 // Largest group pairs per lane of the linear-source sweep instances.
 constexpr int kMaxLsSlots = 5;
-// LinearExpansionGenerator (2D): volume moments and source constants
-// accumulated per FSR in FP64 over all segments, then inverted; outputs
-// ilem[R][3] and cst[R][3][ld] (float), returns through *num_flat the FSRs
-// whose matrix is singular (flat source there).  Scratch lem[R][3] and
-// acc[R][3][G] doubles are the caller's, zeroed here.
-void launch_ls_constants(const int4* segs_ls, const int64_t* seg_off,
-                         const int32_t* track_ang, int64_t T,
-                         const double* ang_dir, const double* ang_wgt,
-                         const double* pol_sin, const double* pol_wgt,
-                         int Ph, const float* sigma_t, const float* fsr_vol,
-                         int64_t R, int G, int ld, double* lem, double* acc,
-                         float* ilem, float* cst, unsigned int* num_flat,
-                         cudaStream_t s);
+// LinearExpansionGenerator (2D): volume moments and source constants per
+// FSR summed in FP64 over the FSR's segments, then inverted; outputs
+// ilem[R][3] and cst[R][3][ld] (float) and through *num_flat the FSRs whose
+// matrix is singular (flat source there).  Allocates and frees its own
+// scratch (segment buckets by FSR); returns 0 or the cudaError_t.
+int launch_ls_constants(const int4* segs_ls, const int64_t* seg_off,
+                        const int32_t* track_ang, int64_t T, int64_t S,
+                        const double* ang_dir, const double* ang_wgt,
+                        const double* pol_sin, const double* pol_wgt, int Ph,
+                        const float* sigma_t, const float* fsr_vol,
+                        const int32_t* fsr_mat, int64_t R, int G, int ld,
+                        float* ilem, float* cst, unsigned int* num_flat,
+                        cudaStream_t s);
 // Builds segs_ls from the packed segments and the start positions.
 void launch_ls_pack_segments(const int2* segs, const float* x, const float* y,
                              int4* out, int64_t S, cudaStream_t s);
