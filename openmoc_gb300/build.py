@@ -69,6 +69,10 @@ def build(verbose: bool = False, ptxas_verbose: bool = False, force: bool = Fals
         objs.append(obj)
         if force or _stale(obj, src):
             extra = ["-Xcompiler", "-fopenmp"] if s.endswith(".cpp") else []
+            # the lattice ray tracer gives the same segments on the host and
+            # on the GPU, on x86 and Arm: no contraction of a*b+c into FMA
+            if s in ("lattice.cpp", "lattice_gpu.cu"):
+                extra += ["-Xcompiler", "-ffp-contract=off", "-fmad=false"]
             jobs.append([cc] + _flags(ptxas_verbose) + extra + ["-c", src, "-o", obj])
 
     def run(cmd):

@@ -34,68 +34,22 @@
 #include <omp.h>
 #endif
 
-namespace {
+#include "lattice_internal.h"
 
+namespace moc_lat {
+namespace {
 thread_local std::string g_lat_error;
-
-struct Track {
-  double x0, y0, x1, y1, phi;
-  int a;
-};
-
-constexpr double kPi = 3.14159265358979323846;
-constexpr double kTinyMove = 1e-8;   // src/constants.h:41
-
 }  // namespace
-
-extern "C" {
-
-typedef struct {
-  int32_t nx, ny;
-  double pitch;
-  double pin_radius;
-  int32_t fuel_rings, fuel_sectors, mod_sectors;
-  int32_t bc[4];
-  int32_t num_azim;
-  double spacing;
-  int32_t num_polar;
-  int32_t moderator_material;
-  int32_t num_threads;
-  const int32_t* pin_material;   // [ny*nx], row 0 = top row (max y)
-} moc_lattice_spec;
-
-struct moc_lattice {
-  int64_t R = 0, T = 0, S = 0;
-  int32_t A = 0, Ph = 0, M = 0;
-  std::vector<float> seg_len;
-  std::vector<int32_t> seg_fsr;
-  std::vector<int64_t> seg_off;
-  std::vector<int32_t> track_ang;
-  std::vector<int64_t> next;
-  std::vector<uint8_t> flags;
-  std::vector<float> weights, inv_sin;
-  std::vector<int32_t> fsr_mat;
-  std::vector<float> fsr_vol;
-  // per azimuthal index: effective spacing and azimuthal weight (used by the
-  // axial extrusion); moderator material
-  std::vector<double> az_spacing, az_weight;
-  int32_t moderator = 0;
-  // 2D lattices: the tracks (start, angle) and the polar set, for the
-  // linear-source geometry (empty for extruded 3D lattices)
-  std::vector<Track> tracks;
-  std::vector<double> pol_sin, pol_wgt;
-};
-
-const char* moc_lattice_last_error(void) { return g_lat_error.c_str(); }
-
-}  // extern "C"
-
-namespace {
 
 int lat_fail(const std::string& m) {
   g_lat_error = m;
   return -1;
 }
+
+
+
+namespace {
+
 
 // Region of a point relative to its pin-cell centre: ring index (0 =
 // outermost fuel ring, fuel_rings-1 = innermost; fuel_rings = moderator)
@@ -140,11 +94,7 @@ void add_sector_lines(std::vector<double>& dirs, int n) {
 
 }  // namespace
 
-extern "C" int moc_lattice_generate(const moc_lattice_spec* sp,
-                                    moc_lattice** out) {
-  if (!sp || !out) return lat_fail("null argument");
-  *out = nullptr;
-  const moc_lattice_spec& s = *sp;
+int lat_validate(const moc_lattice_spec& s) {
   if (s.nx < 1 || s.ny < 1 || !(s.pitch > 0) || !(s.pin_radius > 0) ||
       s.pin_radius >= 0.5 * s.pitch)
     return lat_fail("bad lattice or pin dimensions");
@@ -159,8 +109,10 @@ extern "C" int moc_lattice_generate(const moc_lattice_spec* sp,
   for (int b = 0; b < 4; b++)
     if (s.bc[b] != 0 && s.bc[b] != 1)
       return lat_fail("boundary conditions are 0 (vacuum) or 1 (reflective)");
+  return 0;
+}
 
-  moc_lattice* L = new moc_lattice();
+void lat_laydown(const moc_lattice_spec& s, moc_lattice* L, LatGeo& X) {
   const int A = s.num_azim;
   const double W = s.nx * s.pitch, H = s.ny * s.pitch;
   const double xmin = -0.5 * W, ymin = -0.5 * H;
@@ -285,23 +237,109 @@ extern "C" int moc_lattice_generate(const moc_lattice_spec* sp,
       L->track_ang[id] = a;
     }
   }
+  X.A = A / 2;
+  X.Ph = Ph;
+  X.T = T;
+  X.W = W;
+  X.H = H;
+  X.xmin = xmin;
+  X.ymin = ymin;
+  X.tracks = tracks;
+  X.spac = spac;
+  X.wa = wa;
+  X.sin_t = sin_t;
+  X.w_p = w_p;
+}
 
-  // ---- segmentation ----
-  Classifier cls;
-  cls.rings = s.fuel_rings;
-  cls.fuel_sectors = s.fuel_sectors;
-  cls.mod_sectors = s.mod_sectors;
+void lat_cells(const moc_lattice_spec& s, LatCells& c) {
+  c.rings = s.fuel_rings;
+  c.fuel_sectors = s.fuel_sectors;
+  c.mod_sectors = s.mod_sectors;
   for (int k = 0; k < s.fuel_rings; k++) {
     // equal-area rings: r_k = r * sqrt(1 - k/n)
     const double r = s.pin_radius * std::sqrt(1.0 - (double) k / s.fuel_rings);
-    cls.r2.push_back(r * r);
+    c.r2.push_back(r * r);
   }
-  std::vector<double> radii;
-  for (double v : cls.r2) radii.push_back(std::sqrt(v));
-  std::vector<double> line_dirs;
-  add_sector_lines(line_dirs, s.fuel_sectors);
-  add_sector_lines(line_dirs, s.mod_sectors);
-  std::sort(line_dirs.begin(), line_dirs.end());
+  for (double v : c.r2) c.radii.push_back(std::sqrt(v));
+  add_sector_lines(c.line_dirs, s.fuel_sectors);
+  add_sector_lines(c.line_dirs, s.mod_sectors);
+  std::sort(c.line_dirs.begin(), c.line_dirs.end());
+}
+
+void lat_finish(const moc_lattice_spec& s, moc_lattice* L, const LatGeo& X,
+                const std::vector<uint64_t>& keys, bool volumes) {
+  const std::vector<Track>& tracks = X.tracks;
+  const std::vector<double>& spac = X.spac;
+  const std::vector<double>& wa = X.wa;
+  const std::vector<double>& sin_t = X.sin_t;
+  const std::vector<double>& w_p = X.w_p;
+  const int Ph = X.Ph;
+  const int64_t T = X.T;
+  const int64_t R = (int64_t) keys.size();
+  L->R = R;
+  L->fsr_mat.resize(R);
+  if (volumes) L->fsr_vol.assign(R, 0.0f);
+  int32_t maxmat = s.moderator_material;
+  for (int64_t r = 0; r < R; r++) {
+    const uint64_t key = keys[r];
+    const int64_t cell = (int64_t) (key >> 32);
+    const int ring = (int) ((key >> 16) & 0xFFFF);
+    const int m = (ring < s.fuel_rings) ? s.pin_material[cell]
+                                        : s.moderator_material;
+    L->fsr_mat[r] = m;
+    maxmat = std::max(maxmat, m);
+  }
+  L->M = maxmat + 1;
+  // volumes: sum of segment lengths times azimuthal weight x spacing
+  if (volumes) {
+    std::vector<double> vol(R, 0.0);
+    for (int64_t t = 0; t < T; t++) {
+      const double w = spac[tracks[t].a] * wa[tracks[t].a];
+      for (int64_t k = L->seg_off[t]; k < L->seg_off[t + 1]; k++)
+        vol[L->seg_fsr[k]] += w * (double) L->seg_len[k];
+    }
+    for (int64_t r = 0; r < R; r++) L->fsr_vol[r] = (float) vol[r];
+  }
+  L->az_spacing.assign(spac.begin(), spac.end());
+  L->az_weight.assign(wa.begin(), wa.end());
+  L->tracks = tracks;
+  for (int p = 0; p < Ph; p++) {
+    L->pol_sin.push_back(std::sin(std::asin(sin_t[p])));
+    L->pol_wgt.push_back(w_p[p]);
+  }
+  L->moderator = s.moderator_material;
+  L->moderator = s.moderator_material;
+}
+
+}  // namespace moc_lat
+
+using namespace moc_lat;
+
+extern "C" const char* moc_lattice_last_error(void) {
+  return g_lat_error.c_str();
+}
+
+extern "C" int moc_lattice_generate(const moc_lattice_spec* sp,
+                                    moc_lattice** out) {
+  if (!sp || !out) return lat_fail("null argument");
+  *out = nullptr;
+  const moc_lattice_spec& s = *sp;
+  if (lat_validate(s)) return -1;
+  moc_lattice* L = new moc_lattice();
+  LatGeo X;
+  lat_laydown(s, L, X);
+  const std::vector<Track>& tracks = X.tracks;
+  const double xmin = X.xmin, ymin = X.ymin;
+  const int64_t T = X.T;
+  LatCells cells;
+  lat_cells(s, cells);
+  Classifier cls;
+  cls.rings = cells.rings;
+  cls.fuel_sectors = cells.fuel_sectors;
+  cls.mod_sectors = cells.mod_sectors;
+  cls.r2 = cells.r2;
+  const std::vector<double>& radii = cells.radii;
+  const std::vector<double>& line_dirs = cells.line_dirs;
 
   std::vector<std::vector<float>> seg_len_t(T);
   std::vector<std::vector<uint64_t>> seg_key_t(T);
@@ -419,37 +457,7 @@ extern "C" int moc_lattice_generate(const moc_lattice_spec* sp,
     std::vector<float>().swap(seg_len_t[t]);
     std::vector<uint64_t>().swap(seg_key_t[t]);
   }
-  const int64_t R = (int64_t) keys.size();
-  L->R = R;
-  L->fsr_mat.resize(R);
-  L->fsr_vol.assign(R, 0.0f);
-  int32_t maxmat = s.moderator_material;
-  for (int64_t r = 0; r < R; r++) {
-    const uint64_t key = keys[r];
-    const int64_t cell = (int64_t) (key >> 32);
-    const int ring = (int) ((key >> 16) & 0xFFFF);
-    const int m = (ring < s.fuel_rings) ? s.pin_material[cell]
-                                        : s.moderator_material;
-    L->fsr_mat[r] = m;
-    maxmat = std::max(maxmat, m);
-  }
-  L->M = maxmat + 1;
-  // volumes: sum of segment lengths times azimuthal weight x spacing
-  std::vector<double> vol(R, 0.0);
-  for (int64_t t = 0; t < T; t++) {
-    const double w = spac[tracks[t].a] * wa[tracks[t].a];
-    for (int64_t k = L->seg_off[t]; k < L->seg_off[t + 1]; k++)
-      vol[L->seg_fsr[k]] += w * (double) L->seg_len[k];
-  }
-  for (int64_t r = 0; r < R; r++) L->fsr_vol[r] = (float) vol[r];
-  L->az_spacing.assign(spac.begin(), spac.end());
-  L->az_weight.assign(wa.begin(), wa.end());
-  L->tracks = tracks;
-  for (int p = 0; p < Ph; p++) {
-    L->pol_sin.push_back(std::sin(std::asin(sin_t[p])));
-    L->pol_wgt.push_back(w_p[p]);
-  }
-  L->moderator = s.moderator_material;
+  lat_finish(s, L, X, keys, true);
   *out = L;
   return 0;
 }
