@@ -354,6 +354,8 @@ def run_gpu(args):
             out["cpu_baseline"] = cpu
         if args.batch > 0:
             out["batched_instances"] = run_instances(p, args)
+        if world == 1 and args.workload == "assembly70" and not args.no_raytrace:
+            out["ray_tracing"] = ray_tracing(local)
         if world == 1 and not args.no_serving and args.workload == "assembly70":
             # the second half of the headline: the request stream through the
             # batched server against the plain per-solve loop
@@ -365,6 +367,27 @@ def run_gpu(args):
     s.close()
     if dist:
         dist.destroy_process_group()
+
+
+def ray_tracing(device):
+    """Track generation of the 51x51 core on the host cores against the
+    device ray tracer (laydown on the host, segmentation, FSR numbering and
+    volumes on the GPU); both produce the same segments."""
+    from openmoc_gb300 import lattice as lat
+    lat.pin_cell(7, device=device)            # CUDA context and module load
+    t0 = time.perf_counter()
+    h = lat.core_51x51()
+    t_host = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    d = lat.core_51x51(device=device)
+    t_dev = time.perf_counter() - t0
+    same = all(np.array_equal(getattr(h, k), getattr(d, k)) for k in (
+        "seg_len", "seg_fsr", "seg_off", "track_ang", "next", "flags", "fsr_mat"))
+    return {"workload": "51x51 pins, 128 azimuthal, 0.03 cm, TY-6: "
+                        f"{d.num_tracks} tracks, {d.num_segments} segments",
+            "host_s": t_host, "host_threads": os.cpu_count(), "device_s": t_dev,
+            "segments_per_s_device": d.num_segments / t_dev,
+            "speedup": t_host / t_dev, "identical_segments": bool(same)}
 
 
 def end_to_end(p, args, device, torch):
@@ -673,6 +696,8 @@ def main():
     ap.add_argument("--serving-no-priorities", action="store_true")
     ap.add_argument("--serving-hot-mb", type=int, default=32,
                     help="L2 budget of the live solves' sources and tallies")
+    ap.add_argument("--no-raytrace", action="store_true",
+                    help="skip the track-generation timing (host vs device ray tracing)")
     ap.add_argument("--no-serving", action="store_true",
                     help="leave the request-stream benchmark out of the default line")
     args = ap.parse_args()

@@ -51,6 +51,15 @@ int moc_lattice_export(moc_lattice* lat, float* seg_len, int32_t* seg_fsr,
                        int32_t* fsr_mat, float* fsr_vol);
 int moc_lattice_destroy(moc_lattice* lat);
 
+/** moc_lattice_generate with the ray tracing on CUDA device `device`: the
+ *  laydown on the host, segmentation (one thread per track), FSR numbering
+ *  by first touch and FSR volumes on the GPU.  Segment lengths, FSR ids,
+ *  links and flags are bit-identical to moc_lattice_generate's; volumes are
+ *  summed in a different order (FP64 atomics).  At most 16 fuel rings and
+ *  64 sector lines per pin cell. */
+int moc_lattice_generate_device(const moc_lattice_spec* spec, int32_t device,
+                                moc_lattice** out);
+
 /** Linear-source geometry of a 2D lattice (the arrays of moc_ls_geometry in
  *  openmoc_gb300.h): each segment's start relative to its FSR centroid
  *  (seg_x, seg_y [S]), the centroids [R][2] (CentroidGenerator's formula,

@@ -21,7 +21,8 @@ OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libopenmoc_gb300.so")
 
 SOURCES = ["sweep.cu", "solver_kernels.cu", "moc_api.cu", "lattice.cpp",
-           "noalloc.cu", "serve.cu", "sources_tc.cu", "linear_source.cu"] + [
+           "noalloc.cu", "serve.cu", "sources_tc.cu", "linear_source.cu",
+           "lattice_gpu.cu"] + [
     f"sweep_p{ph}_e{e}.cu" for ph in (1, 2, 3) for e in (0, 1)] + [
     f"ls_sweep_p{ph}.cu" for ph in (1, 2, 3)]
 

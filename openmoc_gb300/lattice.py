@@ -66,6 +66,9 @@ def _lib():
                                           C.c_double, C.c_int32, C.c_int32,
                                           C.POINTER(C.c_void_p)]
         L.moc_lattice_extrude.restype = C.c_int
+        L.moc_lattice_generate_device.argtypes = [C.POINTER(_Spec), C.c_int32,
+                                                  C.POINTER(C.c_void_p)]
+        L.moc_lattice_generate_device.restype = C.c_int
         L.moc_lattice_export_ls.argtypes = [C.c_void_p] + [C.c_void_p] * 7
         L.moc_lattice_export_ls.restype = C.c_int
         L.moc_lattice_destroy.argtypes = [C.c_void_p]
@@ -127,7 +130,7 @@ def lattice(nx: int, ny: int, pin_material: np.ndarray, materials: Sequence[Mate
             fuel_sectors: int = 8, mod_sectors: int = 8, num_polar: int = 6,
             bc=(REFLECTIVE, REFLECTIVE, REFLECTIVE, REFLECTIVE),
             num_threads: int = 0, extrude: Optional[dict] = None,
-            linear_source: bool = False) -> Problem:
+            linear_source: bool = False, device: Optional[int] = None) -> Problem:
     """Tracks, segments and cross sections of an nx x ny pin lattice.
     ``pin_material[row, col]`` (row 0 = top) is the material inside each
     pin; ``bc`` is (xmin, xmax, ymin, ymax).  ``extrude`` = dict(height,
@@ -136,7 +139,8 @@ def lattice(nx: int, ny: int, pin_material: np.ndarray, materials: Sequence[Mate
     bottom and top; ``num_polar`` Gauss-Legendre polar angles).
     ``linear_source`` also exports the linear-source geometry (2D only):
     segment starts relative to the FSR centroids and the angle data, as
-    ``Problem.linear_source``."""
+    ``Problem.linear_source``.  ``device`` ray-traces on that CUDA device
+    (the same segments and FSR ids; moc_lattice_generate_device)."""
     if linear_source and extrude is not None:
         raise ValueError("the linear-source geometry needs 2D tracks")
     L = _lib()
@@ -145,7 +149,9 @@ def lattice(nx: int, ny: int, pin_material: np.ndarray, materials: Sequence[Mate
                  (C.c_int32 * 4)(*bc), num_azim, spacing, num_polar,
                  moderator_material, num_threads, pm.ctypes.data)
     h = C.c_void_p()
-    if L.moc_lattice_generate(C.byref(spec), C.byref(h)):
+    rc = (L.moc_lattice_generate(C.byref(spec), C.byref(h)) if device is None else
+          L.moc_lattice_generate_device(C.byref(spec), int(device), C.byref(h)))
+    if rc:
         raise RuntimeError(L.moc_lattice_last_error().decode())
     if extrude is not None:
         h3 = C.c_void_p()
@@ -211,30 +217,34 @@ def _fuel_mod(config: int, G: int, n_fuel: int = 1, perturb=None):
 
 
 def pin_cell(num_groups: int = 7, num_azim: int = 32, spacing: float = 0.05,
-             config: int = 0, perturb=None, linear_source: bool = False) -> Problem:
+             config: int = 0, perturb=None, linear_source: bool = False,
+             device: Optional[int] = None) -> Problem:
     """One pin cell, all reflective (the 7-group pin-cell benchmark)."""
     mats = _fuel_mod(config, num_groups, 1, perturb)
     return lattice(1, 1, np.zeros((1, 1), np.int32), mats, 1,
-                   num_azim=num_azim, spacing=spacing, linear_source=linear_source)
+                   num_azim=num_azim, spacing=spacing, linear_source=linear_source,
+                   device=device)
 
 
 def square_lattice(n: int, num_groups: int, num_azim: int, spacing: float,
                    config: int, water_pins: Optional[List] = None,
-                   perturb=None, linear_source: bool = False) -> Problem:
+                   perturb=None, linear_source: bool = False,
+                   device: Optional[int] = None) -> Problem:
     """n x n lattice of the pin; ``water_pins`` positions hold moderator."""
     mats = _fuel_mod(config, num_groups, 1, perturb)
     pm = np.zeros((n, n), np.int32)
     for (r, c) in (water_pins or []):
         pm[r, c] = 1
     return lattice(n, n, pm, mats, 1, num_azim=num_azim, spacing=spacing,
-                   linear_source=linear_source)
+                   linear_source=linear_source, device=device)
 
 
 def assembly_17x17(num_groups: int = 70, num_azim: int = 64, spacing: float = 0.05,
-                   config: int = 1, perturb=None, linear_source: bool = False) -> Problem:
+                   config: int = 1, perturb=None, linear_source: bool = False,
+                   device: Optional[int] = None) -> Problem:
     """17 x 17 assembly with 25 water-filled guide-tube positions."""
     return square_lattice(17, num_groups, num_azim, spacing, config,
-                          GUIDE_TUBES_17x17, perturb, linear_source)
+                          GUIDE_TUBES_17x17, perturb, linear_source, device)
 
 
 def assembly_17x17_3d(num_groups: int = 7, num_azim: int = 16, spacing: float = 0.1,
@@ -254,7 +264,7 @@ def assembly_17x17_3d(num_groups: int = 7, num_azim: int = 16, spacing: float = 
 
 
 def core_51x51(num_groups: int = 7, num_azim: int = 128, spacing: float = 0.03,
-               config: int = 3) -> Problem:
+               config: int = 3, device: Optional[int] = None) -> Problem:
     """3 x 3 assemblies of 17 x 17 pins, three fuel sets in a checkerboard,
     vacuum on +x and +y, reflective on -x and -y."""
     mats = _fuel_mod(config, num_groups, 3)
@@ -267,4 +277,4 @@ def core_51x51(num_groups: int = 7, num_azim: int = 128, spacing: float = 0.03,
                 block[r, c] = 3
             pm[17 * ar:17 * ar + 17, 17 * ac:17 * ac + 17] = block
     return lattice(51, 51, pm, mats, 3, num_azim=num_azim, spacing=spacing,
-                   bc=(REFLECTIVE, VACUUM, REFLECTIVE, VACUUM))
+                   bc=(REFLECTIVE, VACUUM, REFLECTIVE, VACUUM), device=device)
