@@ -232,7 +232,11 @@ __global__ void fill_kernel(GpuLattice g, const GpuTrack* tracks, int64_t T,
         seg_len[i] = (float) l;
         const int64_t d = dense_key(g, key);
         seg_dense[i] = (int32_t) d;
-        atomicMin(first_touch + d, (unsigned long long) i);
+        // the first touch only decreases: skip the atomic once a smaller
+        // index is already recorded (most segments, after the first tracks)
+        if (*(volatile unsigned long long*) (first_touch + d) >
+            (unsigned long long) i)
+          atomicMin(first_touch + d, (unsigned long long) i);
       }
     });
   }
