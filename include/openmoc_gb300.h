@@ -307,6 +307,36 @@ int moc_get_linear_expansion(moc_ctx* ctx, double* ilem, float* src_const);
  *  negative sources or fluxes. */
 int moc_set_negative_fluxes_allowed(moc_ctx* ctx, int allowed);
 
+/* ---- on-the-fly 3D segmentation ------------------------------------------
+ * For explicit 3D problems made by extruding a radial lattice
+ * (moc_lattice_extrude): instead of the stored 3D segments, every 3D track
+ * is cut from the radial segments under it during the sweep (the
+ * OTF_TRACKS segment formation of OpenMOC's TrackGenerator3D,
+ * src/TraverseSegments.cpp:151-265).  Arrays as moc_lattice_export_otf
+ * (include/openmoc_gb300_lattice.h) gives them. */
+typedef struct {
+  int64_t num_radial_tracks;     /* T2 */
+  int64_t num_radial_segments;   /* S2 */
+  const int32_t* trk;      /* [T][4] radial track, first radial segment
+                              crossed (in traversal order), count, 1 if the
+                              traversal runs against the radial track */
+  const float* trk_f;      /* [T][4] start a0 along the traversal, span,
+                              height above the cut at a0, 0 */
+  const float* ang;        /* [A][4] cot theta, 1 / cot theta, 1 / sin theta, 0 */
+  const float* rad_len;    /* [S2] radial segment lengths */
+  const int32_t* rad_fsr;  /* [S2] their FSR ids */
+  const int64_t* rad_off;  /* [T2 + 1] */
+  const float* rad_start;  /* [S2] start of each radial segment on its track */
+  const float* rad_total;  /* [T2] radial track lengths */
+  int32_t above_fsr;       /* the region above the cut plane */
+} moc_otf_tracks;
+
+/** Switches a 3D context (tracks, quadrature, materials and FSRs uploaded;
+ *  the explicit segments may be empty) to on-the-fly segmentation; NULL
+ *  returns to the stored segments.  Dropped when tracks are re-uploaded. */
+int moc_set_otf_tracks(moc_ctx* ctx, const moc_otf_tracks* tracks);
+int moc_get_otf_tracks(moc_ctx* ctx, int* enabled);
+
 /** Number of CUDA kernels this library launched on the context so far. */
 int moc_get_launch_count(moc_ctx* ctx, int64_t* launches);
 

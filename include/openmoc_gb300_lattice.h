@@ -83,6 +83,22 @@ int moc_lattice_extrude(const moc_lattice* radial, double height,
                         int32_t num_polar, int32_t num_threads,
                         moc_lattice** out);
 
+/** On-the-fly description of an extruded lattice's 3D tracks (the arrays
+ *  of moc_otf_tracks in openmoc_gb300.h): per 3D track [T][4] (radial
+ *  track, first radial segment crossed in traversal order, count, 1 if the
+ *  traversal runs against the radial track) and [T][4] floats (start a0
+ *  along the radial traversal, span, height above the fuel top at a0, 0);
+ *  per angle row [A][4] (cot theta, 1/cot theta, 1/sin theta, 0); the
+ *  radial segments (lengths, FSR ids, offsets, start of each segment on its
+ *  track, track lengths); above_fsr = the region above the fuel.
+ *  moc_lattice_otf_sizes gives T2 and S2 of the radial arrays. */
+int moc_lattice_otf_sizes(moc_lattice* lat, int64_t* num_radial_tracks,
+                          int64_t* num_radial_segments, int32_t* above_fsr);
+int moc_lattice_export_otf(moc_lattice* lat, int32_t* trk, float* trk_f,
+                           float* ang, float* rad_len, int32_t* rad_fsr,
+                           int64_t* rad_off, float* rad_start,
+                           float* rad_total);
+
 /** Seeded synthetic multigroup data (sigma_s origin-major [orig*G+dest]),
  *  optionally multiplied by lognormal(0, perturb_sigma) factors per group. */
 int moc_synthetic_xs(uint64_t seed, int32_t num_groups, int32_t fissile,

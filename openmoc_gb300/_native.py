@@ -45,6 +45,15 @@ class LSGeometry(C.Structure):
                 ("pol_sin", C.c_void_p), ("pol_wgt", C.c_void_p)]
 
 
+class OtfTracks(C.Structure):
+    """moc_otf_tracks: the on-the-fly description of extruded 3D tracks."""
+    _fields_ = [("num_radial_tracks", C.c_int64), ("num_radial_segments", C.c_int64),
+                ("trk", C.c_void_p), ("trk_f", C.c_void_p), ("ang", C.c_void_p),
+                ("rad_len", C.c_void_p), ("rad_fsr", C.c_void_p),
+                ("rad_off", C.c_void_p), ("rad_start", C.c_void_p),
+                ("rad_total", C.c_void_p), ("above_fsr", C.c_int32)]
+
+
 _P = C.c_void_p
 _SIGS = {
     "moc_last_error": ([], C.c_char_p),
@@ -108,6 +117,8 @@ _SIGS = {
     "moc_set_fixed_source_moments": ([_P, _P, C.c_int64], C.c_int),
     "moc_get_linear_expansion": ([_P, _P, _P], C.c_int),
     "moc_set_negative_fluxes_allowed": ([_P, C.c_int], C.c_int),
+    "moc_set_otf_tracks": ([_P, C.POINTER(OtfTracks)], C.c_int),
+    "moc_get_otf_tracks": ([_P, C.POINTER(C.c_int)], C.c_int),
 }
 
 _lock = threading.Lock()

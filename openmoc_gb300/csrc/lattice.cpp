@@ -556,6 +556,35 @@ extern "C" int moc_lattice_export_ls(moc_lattice* L, float* seg_x,
   return 0;
 }
 
+extern "C" int moc_lattice_otf_sizes(moc_lattice* L, int64_t* num_radial_tracks,
+                                     int64_t* num_radial_segments,
+                                     int32_t* above_fsr) {
+  if (!L || L->rad_off.empty())
+    return lat_fail("not an extruded 3D lattice");
+  *num_radial_tracks = (int64_t) L->rad_total.size();
+  *num_radial_segments = (int64_t) L->rad_len.size();
+  *above_fsr = L->above_fsr;
+  return 0;
+}
+
+extern "C" int moc_lattice_export_otf(moc_lattice* L, int32_t* trk,
+                                      float* trk_f, float* ang,
+                                      float* rad_len, int32_t* rad_fsr,
+                                      int64_t* rad_off, float* rad_start,
+                                      float* rad_total) {
+  if (!L || L->rad_off.empty())
+    return lat_fail("not an extruded 3D lattice");
+  std::memcpy(trk, L->otf_trk.data(), 4 * L->otf_trk.size());
+  std::memcpy(trk_f, L->otf_trk_f.data(), 4 * L->otf_trk_f.size());
+  std::memcpy(ang, L->otf_ang.data(), 4 * L->otf_ang.size());
+  std::memcpy(rad_len, L->rad_len.data(), 4 * L->rad_len.size());
+  std::memcpy(rad_fsr, L->rad_fsr.data(), 4 * L->rad_fsr.size());
+  std::memcpy(rad_off, L->rad_off.data(), 8 * L->rad_off.size());
+  std::memcpy(rad_start, L->rad_start.data(), 4 * L->rad_start.size());
+  std::memcpy(rad_total, L->rad_total.data(), 4 * L->rad_total.size());
+  return 0;
+}
+
 extern "C" int moc_lattice_destroy(moc_lattice* L) {
   delete L;
   return 0;
@@ -700,7 +729,10 @@ extern "C" int moc_lattice_extrude(const moc_lattice* L2, double height,
     std::vector<int32_t> seg_fsr;
     std::vector<int32_t> nseg;
     std::vector<uint8_t> first, last;   // first / last piece of its line
+    std::vector<int32_t> otf;           // per 3D track: t, first, count, rev
+    std::vector<float> otf_f;           // per 3D track: a0, span, w0, 0
     double weight = 0;
+    float cot = 0, sin_t = 0;
   };
   std::vector<Item> items(nitems);
 #ifdef _OPENMP
@@ -721,6 +753,8 @@ extern "C" int moc_lattice_extrude(const moc_lattice* L2, double height,
     const int a = L2->track_ang[c.tr[0]];
     out_item.weight = 2.0 * kPi * L2->az_weight[a] * wp[p] *
                       L2->az_spacing[a] * dz_eff * sin_t;
+    out_item.cot = (float) cot;
+    out_item.sin_t = (float) sin_t;
     const size_t ncyc = c.tr.size();
     for (int64_t j = 0; j < n; j++) {
       double s = (j + 0.5) * ds;
@@ -767,22 +801,34 @@ extern "C" int moc_lattice_extrude(const moc_lattice* L2, double height,
             emit(below_first ? (int32_t) R2 : fsr2, (u1 - uc) / sin_t);
           }
         };
+        // the radial segments crossed, for the on-the-fly description
+        int64_t i_first = 0, n_crossed = 0;
         if (d == 0) {
           int64_t i = (int64_t) (std::upper_bound(cb, cb + nsg + 1, a0) - cb) - 1;
+          i_first = i;
           for (; i < nsg && cb[i] < a1; i++) {
             const double u0 = std::max(a0, cb[i]), u1 = std::min(a1, cb[i + 1]);
             if (u1 > u0) piece(L2->seg_fsr[off[t] + i], u0, u1);
+            n_crossed++;
           }
         } else {
           // natural coordinate x = L - u
           const double x0 = L - a1, x1 = L - a0;
           int64_t i = (int64_t) (std::upper_bound(cb, cb + nsg + 1, x1) - cb) - 1;
           if (i >= nsg) i = nsg - 1;
+          i_first = i;
           for (; i >= 0 && cb[i + 1] > x0; i--) {
             const double v0 = std::max(x0, cb[i]), v1 = std::min(x1, cb[i + 1]);
             if (v1 > v0) piece(L2->seg_fsr[off[t] + i], L - v1, L - v0);
+            n_crossed++;
           }
         }
+        out_item.otf.insert(out_item.otf.end(),
+                            {(int32_t) t, (int32_t) i_first,
+                             (int32_t) n_crossed, (int32_t) d});
+        out_item.otf_f.insert(out_item.otf_f.end(),
+                              {(float) a0, (float) take,
+                               (float) (z - fuel_height), 0.0f});
         out_item.nseg.push_back(
             (int32_t) (out_item.seg_len.size() - seg_start));
         remaining -= take;
@@ -821,11 +867,21 @@ extern "C" int moc_lattice_extrude(const moc_lattice* L2, double height,
   L->flags.resize(T);
   L->weights.resize(nitems);
   L->inv_sin.assign(nitems, 1.0f);
+  L->otf_trk.resize(4 * (size_t) T);
+  L->otf_trk_f.resize(4 * (size_t) T);
+  L->otf_ang.resize(4 * (size_t) nitems);
   std::vector<double> vol(R2 + 1, 0.0);
   int64_t tb = 0, sb = 0;
   for (int64_t it = 0; it < nitems; it++) {
     const Item& m = items[it];
     L->weights[it] = (float) m.weight;
+    L->otf_ang[4 * it + 0] = m.cot;
+    L->otf_ang[4 * it + 1] = 1.0f / m.cot;
+    L->otf_ang[4 * it + 2] = 1.0f / m.sin_t;
+    L->otf_ang[4 * it + 3] = 0.0f;
+    std::memcpy(L->otf_trk.data() + 4 * tb, m.otf.data(), 4 * m.otf.size());
+    std::memcpy(L->otf_trk_f.data() + 4 * tb, m.otf_f.data(),
+                4 * m.otf_f.size());
     const double wv = m.weight / (2.0 * kPi);
     std::memcpy(L->seg_len.data() + sb, m.seg_len.data(), 4 * m.seg_len.size());
     std::memcpy(L->seg_fsr.data() + sb, m.seg_fsr.data(), 4 * m.seg_fsr.size());
@@ -847,6 +903,18 @@ extern "C" int moc_lattice_extrude(const moc_lattice* L2, double height,
   }
   L->fsr_mat.assign(L2->fsr_mat.begin(), L2->fsr_mat.end());
   L->fsr_mat.push_back(L2->moderator);
+  // the radial segments the on-the-fly tracks are cut from
+  L->rad_len = L2->seg_len;
+  L->rad_fsr = L2->seg_fsr;
+  L->rad_off = L2->seg_off;
+  L->rad_start.resize(L2->S);
+  L->rad_total.resize(T2);
+  for (int64_t t = 0; t < T2; t++) {
+    for (int64_t k = off[t]; k < off[t + 1]; k++)
+      L->rad_start[k] = (float) cum[k + t];
+    L->rad_total[t] = (float) len2[t];
+  }
+  L->above_fsr = (int32_t) R2;
   L->fsr_vol.resize(R2 + 1);
   for (int64_t r = 0; r <= R2; r++) L->fsr_vol[r] = (float) vol[r];
   *out = L;

@@ -67,4 +67,15 @@ struct moc_lattice {
   // linear-source geometry (empty for extruded 3D lattices)
   std::vector<moc_lat::Track> tracks;
   std::vector<double> pol_sin, pol_wgt;
+  // Extruded 3D lattices: the on-the-fly description of every 3D track
+  // (radial track, first radial segment in traversal order, count, 1 if
+  // reversed; a0, span, height above the cut at a0), per angle row cot,
+  // 1/cot, 1/sin, and the radial segments they are cut from.
+  std::vector<int32_t> otf_trk;     // [T][4]
+  std::vector<float> otf_trk_f;     // [T][4]
+  std::vector<float> otf_ang;       // [A][4]
+  std::vector<float> rad_len, rad_start, rad_total;
+  std::vector<int32_t> rad_fsr;
+  std::vector<int64_t> rad_off;
+  int32_t above_fsr = -1;
 };

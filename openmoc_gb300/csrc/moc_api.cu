@@ -170,6 +170,21 @@ struct moc_ctx {
   float* fixed_xy = nullptr;
   int64_t ls_num_flat = 0;
   int negative_ok = 0;       // Solver::allowNegativeFluxes
+  // On-the-fly 3D segmentation (moc_set_otf_tracks): 3D track descriptors,
+  // per-angle cot / 1/cot / 1/sin, the radial segments, and the track order
+  // by radial segments crossed
+  bool otf = false;
+  int4* otf_trk = nullptr;
+  float4* otf_trk_f = nullptr;
+  float4* otf_ang = nullptr;
+  int2* otf_rad = nullptr;
+  float* otf_rad_start = nullptr;
+  int64_t* otf_rad_off = nullptr;
+  float* otf_rad_total = nullptr;
+  int32_t* otf_order = nullptr;
+  int64_t otf_S2 = 0;
+  int otf_above_fsr = 0;
+  int otf_above_word = 0;    // above_fsr | material << 24
 };
 
 namespace {
@@ -345,7 +360,21 @@ void pick_shape(int G, int* lps_out, int* slots_out,
 }
 
 int max_slots(const moc_ctx* c) {
-  return c->ls ? moc::kMaxLsSlots : moc::kMaxSlots;
+  return c->ls ? moc::kMaxLsSlots : c->otf ? moc::kMaxOtfSlots : moc::kMaxSlots;
+}
+
+moc::OtfArgs otf_args(const moc_ctx* c) {
+  moc::OtfArgs o{};
+  o.trk = c->otf_trk;
+  o.trk_f = c->otf_trk_f;
+  o.ang = c->otf_ang;
+  o.rad_segs = c->otf_rad;
+  o.rad_start = c->otf_rad_start;
+  o.rad_off = c->otf_rad_off;
+  o.rad_total = c->otf_rad_total;
+  o.above_fsr = c->otf_above_fsr;
+  o.above = c->otf_above_word;
+  return o;
 }
 
 int enqueue_sweep(moc_ctx* c, int check_done, bool timed, int ev_index) {
@@ -360,10 +389,16 @@ int enqueue_sweep(moc_ctx* c, int check_done, bool timed, int ev_index) {
     MOC_CUDA(cudaEventRecord(c->ev[2 * ev_index], c->stream));
   }
   moc::SweepArgs a = sweep_args(c, check_done);
-  const bool ok =
-      c->ls ? moc::launch_ls_sweep(a, c->d.num_polar_half, c->slots, c->stream)
-            : moc::launch_sweep(a, c->d.num_polar_half, c->slots, c->exp_kind,
-                                c->stream);
+  bool ok;
+  if (c->otf) {
+    a.order = c->otf_order;
+    ok = moc::launch_otf_sweep(a, otf_args(c), c->slots, c->stream);
+  } else {
+    ok = c->ls ? moc::launch_ls_sweep(a, c->d.num_polar_half, c->slots,
+                                      c->stream)
+               : moc::launch_sweep(a, c->d.num_polar_half, c->slots,
+                                   c->exp_kind, c->stream);
+  }
   if (!ok)
     return fail(MOC_ERR_UNSUPPORTED,
                 std::string(c->ls ? "no linear-source" : "no") +
@@ -431,8 +466,8 @@ int autotune_sweep(moc_ctx* c, bool use_cache) {
   }
   const int G = c->d.num_groups;
   std::vector<int> kinds;
-  // the linear-source sweep has one exponential evaluator
-  if (c->exp_user_set || c->ls) kinds.push_back(c->exp_kind);
+  // the linear-source and on-the-fly sweeps have one exponential evaluator
+  if (c->exp_user_set || c->ls || c->otf) kinds.push_back(c->exp_kind);
   else kinds = {MOC_EXP_TABLE, MOC_EXP_INTRINSIC};
   TuneVal best{0, 0, 0, 1e30f};
   c->tune_log.clear();
@@ -603,6 +638,30 @@ int pack_materials(moc_ctx* c) {
   MOC_CUDA(cudaGetLastError());
   MOC_CUDA(cudaStreamSynchronize(c->stream));
   c->mat_packed = 1;
+  return MOC_OK;
+}
+
+// Drops the on-the-fly description (new tracks invalidate it).
+void otf_release(moc_ctx* c) {
+  dfree(c->otf_trk);
+  dfree(c->otf_trk_f);
+  dfree(c->otf_ang);
+  dfree(c->otf_rad);
+  dfree(c->otf_rad_start);
+  dfree(c->otf_rad_off);
+  dfree(c->otf_rad_total);
+  dfree(c->otf_order);
+  if (c->otf && !c->shape_user_set) c->lps = c->slots = 0;
+  if (c->otf) c->tuned = false;
+  c->otf = false;
+}
+
+// The material of the region above the cut, packed with its id.
+int otf_above_word(moc_ctx* c) {
+  int32_t m = 0;
+  MOC_CUDA(cudaMemcpy(&m, c->fsr_mat + c->otf_above_fsr, 4,
+                      cudaMemcpyDeviceToHost));
+  c->otf_above_word = c->otf_above_fsr | (m << 24);
   return MOC_OK;
 }
 
@@ -789,6 +848,14 @@ int moc_destroy(moc_ctx* c) {
   dfree(c->ls_ilem);
   dfree(c->ls_const);
   dfree(c->fixed_xy);
+  dfree(c->otf_trk);
+  dfree(c->otf_trk_f);
+  dfree(c->otf_ang);
+  dfree(c->otf_rad);
+  dfree(c->otf_rad_start);
+  dfree(c->otf_rad_off);
+  dfree(c->otf_rad_total);
+  dfree(c->otf_order);
   dfree(c->sc);
   if (c->hsc) cudaFreeHost(c->hsc);
   for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
@@ -898,6 +965,7 @@ int moc_upload_tracks(moc_ctx* c, const float* seg_len, const int32_t* seg_fsr,
                       cudaMemcpyHostToDevice));
   MOC_CUDA(cudaMemcpy(c->flags, flags, T, cudaMemcpyHostToDevice));
   ls_release(c);
+  otf_release(c);
   c->have_tracks = true;
   MOC_TRY(pack_materials(c));
   return MOC_OK;
@@ -1069,6 +1137,12 @@ int moc_upload_fsrs(moc_ctx* c, const int32_t* fsr_mat, const float* fsr_vol) {
                                c->stream);
     c->launches++;
     MOC_TRY(ls_constants(c));
+  }
+  if (c->otf) {
+    moc::launch_pack_materials(c->otf_rad, c->otf_S2, c->fsr_mat, c->stream);
+    c->launches++;
+    MOC_CUDA(cudaStreamSynchronize(c->stream));
+    MOC_TRY(otf_above_word(c));
   }
   return MOC_OK;
 }
@@ -1868,6 +1942,121 @@ int moc_get_linear_expansion(moc_ctx* c, double* ilem, float* src_const) {
   if (src_const)
     MOC_CUDA(cudaMemcpy2D(src_const, 4 * G, c->ls_const, 4 * ld, 4 * G,
                           3 * R, cudaMemcpyDeviceToHost));
+  return MOC_OK;
+}
+
+// ------------------------------------------------- on-the-fly 3D tracks
+int moc_set_otf_tracks(moc_ctx* c, const moc_otf_tracks* d) {
+  MOC_TRY(ready(c));
+  if (!d) {
+    otf_release(c);
+    return MOC_OK;
+  }
+  MOC_CHECK(c->d.solve_3d && c->d.num_polar_half == 1, MOC_ERR_UNSUPPORTED,
+            "on-the-fly segmentation takes 3D tracks");
+  MOC_CHECK(!c->ls, MOC_ERR_UNSUPPORTED,
+            "on-the-fly segmentation and the linear source do not combine");
+  MOC_CHECK(c->d.num_fsrs < (1LL << 24) && c->d.num_materials <= 256,
+            MOC_ERR_UNSUPPORTED,
+            "on-the-fly segmentation needs fewer than 2^24 FSRs and at most "
+            "256 materials");
+  MOC_CHECK(d->trk && d->trk_f && d->ang && d->rad_len && d->rad_fsr &&
+                d->rad_off && d->rad_start && d->rad_total,
+            MOC_ERR_ARG, "null on-the-fly array");
+  const int64_t T = c->d.num_tracks, T2 = d->num_radial_tracks;
+  const int64_t S2 = d->num_radial_segments, R = c->d.num_fsrs;
+  const int A = c->d.num_angles;
+  MOC_CHECK(T2 >= 1 && S2 >= 0 && d->rad_off[0] == 0 && d->rad_off[T2] == S2,
+            MOC_ERR_ARG, "radial segment offsets must run from 0 to S2");
+  MOC_CHECK(d->above_fsr >= 0 && d->above_fsr < R, MOC_ERR_ARG,
+            "above_fsr out of range");
+  for (int64_t t = 0; t < T2; t++)
+    MOC_CHECK(d->rad_off[t + 1] >= d->rad_off[t] && std::isfinite(d->rad_total[t]),
+              MOC_ERR_ARG, "bad radial track " + std::to_string(t));
+  for (int64_t k = 0; k < S2; k++)
+    MOC_CHECK(d->rad_fsr[k] >= 0 && d->rad_fsr[k] < R &&
+                  std::isfinite(d->rad_len[k]) && d->rad_len[k] >= 0.0f &&
+                  std::isfinite(d->rad_start[k]),
+              MOC_ERR_ARG, "bad radial segment " + std::to_string(k));
+  std::vector<int32_t> cnt(T);
+  for (int64_t t = 0; t < T; t++) {
+    const int32_t* q = d->trk + 4 * t;
+    const float* f = d->trk_f + 4 * t;
+    MOC_CHECK(q[0] >= 0 && q[0] < T2 && q[2] >= 0 && (q[3] == 0 || q[3] == 1),
+              MOC_ERR_ARG, "bad on-the-fly track " + std::to_string(t));
+    const int64_t n = d->rad_off[q[0] + 1] - d->rad_off[q[0]];
+    const int64_t lo = q[3] ? q[1] - q[2] + 1 : q[1];
+    const int64_t hi = q[3] ? q[1] : q[1] + q[2] - 1;
+    MOC_CHECK(q[2] == 0 || (lo >= 0 && hi < n), MOC_ERR_ARG,
+              "on-the-fly track " + std::to_string(t) +
+                  " crosses radial segments outside its radial track");
+    MOC_CHECK(std::isfinite(f[0]) && std::isfinite(f[1]) && f[1] >= 0.0f &&
+                  std::isfinite(f[2]),
+              MOC_ERR_ARG, "bad on-the-fly track " + std::to_string(t));
+    cnt[t] = q[2];
+  }
+  for (int a = 0; a < 4 * A; a++)
+    MOC_CHECK(std::isfinite(d->ang[a]), MOC_ERR_ARG, "bad on-the-fly angle data");
+  std::vector<int32_t> order(T);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int32_t x, int32_t y) { return cnt[x] > cnt[y]; });
+  std::vector<int2> rad(S2);
+  for (int64_t k = 0; k < S2; k++)
+    rad[k] = make_int2(__builtin_bit_cast(int, d->rad_len[k]), d->rad_fsr[k]);
+  otf_release(c);
+  int st = MOC_OK;
+  auto step = [&](int r) { if (st == MOC_OK) st = r; };
+  step(dalloc(&c->otf_trk, T > 0 ? T : 1));
+  step(dalloc(&c->otf_trk_f, T > 0 ? T : 1));
+  step(dalloc(&c->otf_ang, A));
+  step(dalloc(&c->otf_rad, S2 > 0 ? S2 : 1));
+  step(dalloc(&c->otf_rad_start, S2 > 0 ? S2 : 1));
+  step(dalloc(&c->otf_rad_off, T2 + 1));
+  step(dalloc(&c->otf_rad_total, T2));
+  step(dalloc(&c->otf_order, T > 0 ? T : 1));
+  if (st != MOC_OK) {
+    otf_release(c);
+    return st;
+  }
+  cudaError_t e = cudaMemcpy(c->otf_trk, d->trk, 16 * T, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(c->otf_trk_f, d->trk_f, 16 * T, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(c->otf_ang, d->ang, 16 * (size_t) A, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(c->otf_rad, rad.data(), 8 * S2, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(c->otf_rad_start, d->rad_start, 4 * S2,
+                   cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(c->otf_rad_off, d->rad_off, 8 * (T2 + 1),
+                   cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(c->otf_rad_total, d->rad_total, 4 * T2,
+                   cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(c->otf_order, order.data(), 4 * T, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    otf_release(c);
+    return fail(MOC_ERR_CUDA, std::string("on-the-fly upload: ") +
+                                  cudaGetErrorString(e));
+  }
+  c->otf_S2 = S2;
+  c->otf_above_fsr = d->above_fsr;
+  moc::launch_pack_materials(c->otf_rad, S2, c->fsr_mat, c->stream);
+  c->launches++;
+  MOC_CUDA(cudaStreamSynchronize(c->stream));
+  MOC_TRY(otf_above_word(c));
+  c->otf = true;
+  if (!c->shape_user_set) c->lps = c->slots = 0;
+  c->tuned = false;
+  return MOC_OK;
+}
+
+int moc_get_otf_tracks(moc_ctx* c, int* enabled) {
+  MOC_CHECK(c && enabled, MOC_ERR_ARG, "null argument");
+  *enabled = c->otf ? 1 : 0;
   return MOC_OK;
 }
 

@@ -217,6 +217,26 @@ void tc_pack_scattering(const float* sigma_s, int M, int G,
 void launch_sources_tc(const SolverArgs& a, int iteration, int zero_phi,
                        cudaStream_t s);
 
+// ---- on-the-fly 3D segmentation (otf_sweep.cu) ----------------------------
+// Extruded 3D tracks cut from their radial segments during the sweep.
+struct OtfArgs {
+  const int4* trk;          // [T] radial track, first radial segment (index
+                            //     within it, in traversal order), count,
+                            //     1 if the traversal runs against it
+  const float4* trk_f;      // [T] start a0 along the radial traversal, span
+                            //     A, height above the cut at a0, unused
+  const float4* ang;        // [A] cot(theta), 1 / cot(theta), 1 / sin(theta)
+  const int2* rad_segs;     // [S2] {length bits, fsr | material << 24}
+  const float* rad_start;   // [S2] start of each radial segment on its track
+  const int64_t* rad_off;   // [T2 + 1]
+  const float* rad_total;   // [T2] radial track lengths
+  int above;                // fsr | material << 24 of the region above the cut
+  int above_fsr;
+};
+bool launch_otf_sweep(const SweepArgs& a, const OtfArgs& o, int slots,
+                      cudaStream_t stream);
+constexpr int kMaxOtfSlots = 4;
+
 // ---- linear source (linear_source.cu, solver_kernels.cu, ls_sweep_*.cu) ----
 // Largest group pairs per lane of the linear-source sweep instances.
 constexpr int kMaxLsSlots = 5;

@@ -69,6 +69,11 @@ def _lib():
         L.moc_lattice_generate_device.argtypes = [C.POINTER(_Spec), C.c_int32,
                                                   C.POINTER(C.c_void_p)]
         L.moc_lattice_generate_device.restype = C.c_int
+        L.moc_lattice_otf_sizes.argtypes = [C.c_void_p, C.POINTER(C.c_int64),
+                                            C.POINTER(C.c_int64), C.POINTER(C.c_int32)]
+        L.moc_lattice_otf_sizes.restype = C.c_int
+        L.moc_lattice_export_otf.argtypes = [C.c_void_p] + [C.c_void_p] * 8
+        L.moc_lattice_export_otf.restype = C.c_int
         L.moc_lattice_export_ls.argtypes = [C.c_void_p] + [C.c_void_p] * 7
         L.moc_lattice_export_ls.restype = C.c_int
         L.moc_lattice_destroy.argtypes = [C.c_void_p]
@@ -179,6 +184,23 @@ def lattice(nx: int, ny: int, pin_material: np.ndarray, materials: Sequence[Mate
         L.moc_lattice_export(h, *[arr[k].ctypes.data for k in (
             "seg_len", "seg_fsr", "seg_off", "track_ang", "next", "flags", "weights",
             "inv_sin", "fsr_mat", "fsr_vol")])
+        otf = None
+        if extrude is not None:
+            T2, S2, above = C.c_int64(), C.c_int64(), C.c_int32()
+            if L.moc_lattice_otf_sizes(h, C.byref(T2), C.byref(S2), C.byref(above)):
+                raise RuntimeError(L.moc_lattice_last_error().decode())
+            T2, S2 = T2.value, S2.value
+            otf = dict(trk=np.empty(4 * T, np.int32), trk_f=np.empty(4 * T, np.float32),
+                       ang=np.empty(4 * A, np.float32),
+                       rad_len=np.empty(S2, np.float32), rad_fsr=np.empty(S2, np.int32),
+                       rad_off=np.empty(T2 + 1, np.int64),
+                       rad_start=np.empty(S2, np.float32),
+                       rad_total=np.empty(T2, np.float32),
+                       above_fsr=np.array([above.value], np.int32))
+            if L.moc_lattice_export_otf(h, *[otf[k].ctypes.data for k in (
+                    "trk", "trk_f", "ang", "rad_len", "rad_fsr", "rad_off",
+                    "rad_start", "rad_total")]):
+                raise RuntimeError(L.moc_lattice_last_error().decode())
         ls = None
         if linear_source:
             ls = dict(seg_x=np.empty(S, np.float32), seg_y=np.empty(S, np.float32),
@@ -199,6 +221,7 @@ def lattice(nx: int, ny: int, pin_material: np.ndarray, materials: Sequence[Mate
                 sigma_t=st, sigma_s=ss, nu_sigma_f=nf,
                 chi=ch, **arr)
     p.linear_source = ls
+    p.otf = otf
     p.meta = dict(nx=nx, ny=ny, num_azim=num_azim, spacing=spacing, pitch=pitch,
                   num_polar=num_polar)
     return p.contiguous()

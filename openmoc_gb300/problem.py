@@ -97,6 +97,10 @@ class Problem:
     # cos/sin phi, ang_wgt [A] azimuthal spacing x weight, pol_sin and
     # pol_wgt [A][Ph] (float64); optionally centroid [R][2] (float64).
     linear_source: Optional[Dict[str, np.ndarray]] = None
+    # On-the-fly description of extruded 3D tracks (moc_otf_tracks arrays:
+    # trk, trk_f, ang, rad_len, rad_fsr, rad_off, rad_start, rad_total,
+    # above_fsr); the explicit segments above stay valid.
+    otf: Optional[Dict[str, np.ndarray]] = None
 
     @property
     def fluxes_per_track(self) -> int:

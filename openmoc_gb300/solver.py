@@ -59,6 +59,7 @@ class GB300Solver:
         self._shape = None
         self._source_kind = "auto"
         self._negative_ok = False
+        self._formation = "explicit"
         if track_generator is not None:
             self.setTrackGenerator(track_generator)
 
@@ -120,6 +121,8 @@ class GB300Solver:
             self._call("moc_set_source_kernel", self._SOURCE_KINDS[self._source_kind])
         if self._negative_ok:
             self._call("moc_set_negative_fluxes_allowed", 1)
+        if self._formation == "otf":
+            self._set_otf()
         self._fixed = {}
         self._fixed_by_material = {}
         if p.fixed_sources is not None:
@@ -139,6 +142,36 @@ class GB300Solver:
 
     def getConvergenceThreshold(self) -> float:
         return self._threshold
+
+    def setSegmentFormation(self, formation: str) -> None:
+        """"explicit" (stored 3D segments) or "otf": 3D tracks of an extruded
+        lattice cut from their radial segments during the sweep
+        (TrackGenerator3D::setSegmentFormation(OTF_TRACKS),
+        src/TrackGenerator3D.h).  "otf" needs the problem's ``otf`` arrays."""
+        if formation not in ("explicit", "otf"):
+            raise _native.MOCError(-1, f"unknown segment formation {formation!r}")
+        self._formation = formation
+        if self._ctx is not None:
+            if formation == "otf":
+                self._set_otf()
+            else:
+                self._call("moc_set_otf_tracks", None)
+
+    def getSegmentFormation(self) -> str:
+        return self._formation
+
+    def _set_otf(self) -> None:
+        o = self._problem.otf
+        if o is None:
+            raise _native.MOCError(-1, "the problem has no on-the-fly track description")
+        arrs = {k: np.ascontiguousarray(v) for k, v in o.items()}
+        self._otf_arrays = arrs
+        d = _native.OtfTracks(arrs["rad_total"].size, arrs["rad_len"].size,
+                              *(_ptr(arrs[k]) for k in ("trk", "trk_f", "ang", "rad_len",
+                                                        "rad_fsr", "rad_off", "rad_start",
+                                                        "rad_total")),
+                              int(arrs["above_fsr"][0]))
+        self._call("moc_set_otf_tracks", C.byref(d))
 
     def allowNegativeFluxes(self, negative_fluxes_on: bool) -> None:
         """Solver::allowNegativeFluxes (src/Solver.cpp:623): negative

@@ -90,3 +90,69 @@ def test_extrusion_converges_towards_openmoc_3d_keff():
     o = Oracle(_extruded_pin(0.1, 6, 8, 0.05), "f64", num_threads=2)
     o.compute_eigenvalue(1000, 1, 1e-6)
     assert abs(o.keff - sc["keff"]) / sc["keff"] < 0.03
+
+
+def _otf_pieces(p):
+    """The pieces the on-the-fly sweep cuts for every 3D track, in traversal
+    order (a restatement of otf_sweep.cu's cut() in double precision),
+    merged like the explicit generator merges consecutive pieces of one
+    region."""
+    o = p.otf
+    trk = o["trk"].reshape(-1, 4)
+    tf = o["trk_f"].reshape(-1, 4).astype(np.float64)
+    ang = o["ang"].reshape(-1, 4).astype(np.float64)
+    above = int(o["above_fsr"][0])
+    out = []
+    for t in range(p.num_tracks):
+        t2, first, n, rev = (int(v) for v in trk[t])
+        a0, span, w0 = tf[t, 0], tf[t, 1], tf[t, 2]
+        cot, icot, isin = ang[p.track_ang[t], :3]
+        rb = int(o["rad_off"][t2])
+        total = float(o["rad_total"][t2])
+        pieces = []
+        for k in range(n):
+            idx = first - k if rev else first + k
+            l = float(o["rad_len"][rb + idx])
+            c0 = float(o["rad_start"][rb + idx])
+            s = (total - c0 - l) - a0 if rev else c0 - a0
+            us, ue = max(s, 0.0), min(s + l, span)
+            if not ue > us:
+                continue
+            ws, we = w0 + us * cot, w0 + ue * cot
+            below = int(o["rad_fsr"][rb + idx])
+            if max(ws, we) <= 0 or min(ws, we) >= 0:
+                pieces.append((below if max(ws, we) <= 0 else above, (ue - us) * isin))
+            else:
+                uc = us - ws * icot
+                a_, b_ = (below, above) if ws < 0 else (above, below)
+                pieces.append((a_, (uc - us) * isin))
+                pieces.append((b_, (ue - uc) * isin))
+        merged = []
+        for f, l in pieces:
+            if l <= 1e-10:
+                continue
+            if merged and merged[-1][0] == f:
+                merged[-1][1] += l
+            else:
+                merged.append([f, l])
+        out.append(merged)
+    return out
+
+
+def test_otf_description_reproduces_explicit_segments():
+    """The on-the-fly track description of an extruded lattice cuts the same
+    3D segments as the explicit generator stores (FSR ids exactly, lengths to
+    float rounding)."""
+    mats = lt._fuel_mod(4, 7, 1)
+    pm = np.zeros((2, 2), np.int32)
+    pm[0, 1] = 1
+    p = lt.lattice(2, 2, pm, mats, 1, num_azim=8, spacing=0.1,
+                        extrude=dict(height=2.0, fuel_height=1.6, z_spacing=0.4,
+                                     num_polar=4))
+    pieces = _otf_pieces(p)
+    for t in range(p.num_tracks):
+        b, e = p.seg_off[t], p.seg_off[t + 1]
+        got = pieces[t]
+        assert [f for f, _ in got] == list(p.seg_fsr[b:e]), t
+        np.testing.assert_allclose([l for _, l in got], p.seg_len[b:e], rtol=2e-5,
+                                   atol=2e-6)
