@@ -74,15 +74,21 @@ def load_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
 
 
-def algorithmic_bytes(p, ls=False):
+def algorithmic_bytes(p, ls=False, otf=False):
     """Compulsory HBM bytes of one sweep: packed segments read once (8 B;
     16 B with the linear source's start position), per-track
     offsets/links/flags (16 B), angular flux in and out for both directions
     (16 B per track and flux value), sources read and tallies written (8 B
     per FSR and group; 24 B with the x / y source and flux moments)."""
     F = p.fluxes_per_track
-    return ((16 if ls else 8) * p.num_segments + 16 * p.num_tracks
-            + 16 * p.num_tracks * F + (24 if ls else 8) * p.num_fsrs * p.num_groups)
+    if otf:
+        # a 32-byte description per 3D track and the radial segments (12 B)
+        # instead of the stored 3D segments
+        seg = 32 * p.num_tracks + 12 * p.otf["rad_len"].size
+    else:
+        seg = (16 if ls else 8) * p.num_segments
+    return (seg + 16 * p.num_tracks + 16 * p.num_tracks * F
+            + (24 if ls else 8) * p.num_fsrs * p.num_groups)
 
 
 class Clocks:
@@ -151,6 +157,9 @@ WORKLOADS = {
                   "7 groups, explicit 3D tracks: 16 azimuthal, 6 polar, 0.1 cm radial, "
                   "0.5 cm axial; reflective radially, vacuum top and bottom",
     "assembly70_ls": WORKLOAD + ", linear source (CPULSSolver)",
+    "assembly3d_otf": "17x17 assembly extruded to 20 cm (fuel below 16 cm, moderator above), "
+                      "7 groups, 16 azimuthal, 6 polar, 0.1 cm radial, 0.5 cm axial; 3D "
+                      "tracks cut from the radial segments during the sweep (on-the-fly)",
 }
 
 
@@ -162,7 +171,7 @@ def build_problem(workload="assembly70"):
     from openmoc_gb300 import lattice
     if workload == "core51":
         return lattice.core_51x51()
-    if workload == "assembly3d":
+    if workload in ("assembly3d", "assembly3d_otf"):
         return lattice.assembly_17x17_3d()
     if workload == "assembly70_ls":
         return lattice.assembly_17x17(linear_source=True)
@@ -243,7 +252,10 @@ def run_gpu(args):
     p = build_problem(args.workload)
     ls = is_ls(args.workload)
     peaks, peak_kind = load_peaks()
-    s = (GB300LSSolver if ls else GB300Solver)(p, device=local)
+    s = (GB300LSSolver if ls else GB300Solver)(device=local)
+    if args.workload.endswith("_otf"):
+        s.setSegmentFormation("otf")
+    s.setTrackGenerator(p)
     if args.shape:
         # a fixed kernel shape (e.g. to profile one instance)
         lps, slots, exp_kind = (int(v) for v in args.shape.split(","))
@@ -288,7 +300,8 @@ def run_gpu(args):
 
     # roofline of the dominant kernel (the sweep)
     sweep_avg = float(np.mean(sweep_ms))
-    nbytes = algorithmic_bytes(p, ls)
+    otf = args.workload.endswith("_otf")
+    nbytes = algorithmic_bytes(p, ls, otf)
     achieved = nbytes / (sweep_avg * 1e-3) / 1e9
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     traffic = (SWEEP_DRAM_BYTES.get((lps, slots, exp_kind))
@@ -304,7 +317,7 @@ def run_gpu(args):
     # 20 iterations, fluxes back
     e2e = None
     if args.e2e_iters > 0:
-        e2e = end_to_end(p, args, local, torch)
+        e2e = end_to_end(p, args, local, torch, otf=args.workload.endswith("_otf"))
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -390,7 +403,7 @@ def ray_tracing(device):
             "speedup": t_host / t_dev, "identical_segments": bool(same)}
 
 
-def end_to_end(p, args, device, torch):
+def end_to_end(p, args, device, torch, otf=False):
     """The metric through GB300Solver: per step, upload the problem from
     pinned host memory, run a fixed number of iterations, copy the fluxes
     back."""
@@ -407,6 +420,14 @@ def end_to_end(p, args, device, torch):
     q = Problem(**{f: getattr(p, f) for f in p.__dataclass_fields__})
     for k, (_, arr) in pinned.items():
         setattr(q, k, arr)
+    if otf:
+        q.otf = {}
+        for k, a in p.otf.items():
+            t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True)
+            t.numpy()[:] = a.view(np.uint8)
+            pinned["otf_" + k] = (t, t.numpy().view(a.dtype))
+            q.otf[k] = pinned["otf_" + k][1]
+            h2d += a.nbytes
     if p.linear_source is not None:
         q.linear_source = {}
         for k, a in p.linear_source.items():
@@ -424,7 +445,10 @@ def end_to_end(p, args, device, torch):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         s = (GB300LSSolver if p.linear_source is not None else GB300Solver)(
-            q, device=device)
+            device=device)
+        if otf:
+            s.setSegmentFormation("otf")
+        s.setTrackGenerator(q)
         setup = time.perf_counter() - t0
         s.setConvergenceThreshold(1e-30)
         s.computeEigenvalue(args.e2e_iters)
