@@ -72,9 +72,10 @@ def test_otf_without_stored_segments():
     q.seg_off = np.zeros(p.num_tracks + 1, np.int64)
     q.num_segments = 0
     k, f = _solve(q, "otf")
-    # tallies are float atomics: equal up to their summation order
-    assert abs(k - k_ref) < 1e-7
-    assert _rel(f, f_ref) < 1e-6
+    # tallies are float atomics (and the autotuner may pick another shape):
+    # equal up to summation order
+    assert abs(k - k_ref) < 1e-6
+    assert _rel(f, f_ref) < 1e-5
 
 
 def test_otf_bad_requests_raise():
