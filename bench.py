@@ -251,6 +251,7 @@ def run_gpu(args):
 
     p = build_problem(args.workload)
     ls = is_ls(args.workload)
+    otf = args.workload.endswith("_otf")
     peaks, peak_kind = load_peaks()
     s = (GB300LSSolver if ls else GB300Solver)(device=local)
     if args.workload.endswith("_otf"):
@@ -300,7 +301,6 @@ def run_gpu(args):
 
     # roofline of the dominant kernel (the sweep)
     sweep_avg = float(np.mean(sweep_ms))
-    otf = args.workload.endswith("_otf")
     nbytes = algorithmic_bytes(p, ls, otf)
     achieved = nbytes / (sweep_avg * 1e-3) / 1e9
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
@@ -341,9 +341,9 @@ def run_gpu(args):
                        "sweep_shape": {"lanes_per_track_direction": lps,
                                        "group_pairs_per_lane": slots,
                                        "exponential": ("rational G(x), F1/F2/H from it"
-                                                       if ls else
-                                                       ["shared-memory table",
-                                                        "hardware ex2"][exp_kind])},
+                                                       if ls else "hardware ex2" if otf
+                                                       else ["shared-memory table",
+                                                             "hardware ex2"][exp_kind])},
                        "autotune_ms": {f"{a}x{b}/{'table' if e == 0 else 'ex2'}": round(t, 4)
                                        for a, b, e, t in tuning},
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},

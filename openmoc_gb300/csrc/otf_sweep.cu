@@ -124,23 +124,21 @@ otf_sweep_kernel(const SweepArgs a, const OtfArgs o) {
       return p;
     };
 
-    auto integrate = [&](float len, int word) {
+    // one piece with its sources already loaded
+    auto integrate = [&](float len, int word, const float2* qv) {
       const int fsr = word & 0xFFFFFF;
       const int mat = (int) ((unsigned) word >> 24);
       const float2* st = reinterpret_cast<const float2*>(s_st + mat * ld) + sub;
-      const float2* qrow =
-          reinterpret_cast<const float2*>(a.qt + (int64_t) fsr * ld) + sub;
       const bool hot = fsr == o.above_fsr;
       const float2 len2 = f2(len);
 #pragma unroll
       for (int s = 0; s < PS; s++) {
         if (sub + s * LPS < npairs) {
-          const float2 qs = __ldg(qrow + s * LPS);
           const float2 tau = __fmul2_rn(st[s * LPS], len2);
           const float2 gx =
               AttenIntrinsic::eval2(__fmul2_rn(tau, xl2), tau, nullptr);
           const float2 d =
-              __fmul2_rn(__ffma2_rn(qs, f2(-1.0f), psi[s]), gx);
+              __fmul2_rn(__ffma2_rn(qv[s], f2(-1.0f), psi[s]), gx);
           psi[s] = __ffma2_rn(d, f2(-1.0f), psi[s]);
           const float2 tally = __fmul2_rn(w2, d);
           if (hot) {
@@ -155,19 +153,66 @@ otf_sweep_kernel(const SweepArgs a, const OtfArgs o) {
         }
       }
     };
+    auto load_q = [&](int word, float2* qv) {
+      const float2* qrow = reinterpret_cast<const float2*>(
+                               a.qt + (int64_t) (word & 0xFFFFFF) * ld) + sub;
+#pragma unroll
+      for (int s = 0; s < PS; s++)
+        qv[s] = (sub + s * LPS < npairs) ? __ldg(qrow + s * LPS) : f2(0.0f);
+    };
 
+    // Pieces of a chunk of LPS radial segments reach every lane of the
+    // stream by shuffles; where the registers allow (LPS x PS <= 4) the
+    // sources of all of a chunk's pieces are loaded before the first is
+    // integrated, else those of each radial segment's pieces.
+    constexpr bool kBatched = LPS * PS <= 4;
+    constexpr int kBatch = kBatched ? 2 * LPS : 1;
     Piece2 mine = cut(sub);
     for (int cb = 0; cb < nrad; cb += LPS) {
       const Piece2 nxt = cut(cb + LPS + sub);   // the next chunk, ahead
       const int m = min(LPS, nrad - cb);
-      for (int j = 0; j < m; j++) {
-        const int n = __shfl_sync(gmask, mine.n, j, LPS);
-        const float l0 = __shfl_sync(gmask, mine.l0, j, LPS);
-        const int w0 = __shfl_sync(gmask, mine.w0, j, LPS);
-        const float l1 = __shfl_sync(gmask, mine.l1, j, LPS);
-        const int w1 = __shfl_sync(gmask, mine.w1, j, LPS);
-        if (n > 0) integrate(l0, w0);
-        if (n > 1) integrate(l1, w1);
+      if constexpr (kBatched) {
+        float pl[kBatch];
+        int pw[kBatch];
+        float2 pq[kBatch][PS];
+        int np = 0;
+#pragma unroll
+        for (int j = 0; j < LPS; j++) {
+          if (j < m) {
+            const int n = __shfl_sync(gmask, mine.n, j, LPS);
+            const float l0 = __shfl_sync(gmask, mine.l0, j, LPS);
+            const int w0 = __shfl_sync(gmask, mine.w0, j, LPS);
+            const float l1 = __shfl_sync(gmask, mine.l1, j, LPS);
+            const int w1 = __shfl_sync(gmask, mine.w1, j, LPS);
+            pl[2 * j] = l0;
+            pw[2 * j] = (n > 0) ? w0 : -1;
+            pl[2 * j + 1] = l1;
+            pw[2 * j + 1] = (n > 1) ? w1 : -1;
+          } else {
+            pw[2 * j] = pw[2 * j + 1] = -1;
+            pl[2 * j] = pl[2 * j + 1] = 0.0f;
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < kBatch; i++)
+          if (pw[i] >= 0) load_q(pw[i], pq[i]);
+#pragma unroll
+        for (int i = 0; i < kBatch; i++)
+          if (pw[i] >= 0) integrate(pl[i], pw[i], pq[i]);
+        (void) np;
+      } else {
+        for (int j = 0; j < m; j++) {
+          const int n = __shfl_sync(gmask, mine.n, j, LPS);
+          const float l0 = __shfl_sync(gmask, mine.l0, j, LPS);
+          const int w0 = __shfl_sync(gmask, mine.w0, j, LPS);
+          const float l1 = __shfl_sync(gmask, mine.l1, j, LPS);
+          const int w1 = __shfl_sync(gmask, mine.w1, j, LPS);
+          float2 q0[PS], q1[PS];
+          if (n > 0) load_q(w0, q0);
+          if (n > 1) load_q(w1, q1);
+          if (n > 0) integrate(l0, w0, q0);
+          if (n > 1) integrate(l1, w1, q1);
+        }
       }
       mine = nxt;
     }
