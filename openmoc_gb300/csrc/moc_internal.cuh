@@ -102,6 +102,14 @@ struct SweepArgs {
   const float2* ang_dir;     // [A]
   const float* qxy;          // [R][ld][2]
   float* mom;                // [R][ld][2]
+  // CMFD (null: none): coarse cell of every FSR (iy * cm_nx + ix), outgoing
+  // partial currents [cells][4 faces][ld], and per track the boundary face
+  // crossed at its forward / backward end where the flux is not
+  // transferred (vacuum), else -1
+  const int32_t* cm_cell;    // [R]
+  float* cm_cur;             // [cells][4][ld]
+  const int8_t* cm_end;      // [T][2]
+  int cm_nx;
 };
 
 constexpr int kMaxHotFsrs = 8;

@@ -140,12 +140,16 @@ struct SweepOccupancy {
                              : 8;
 };
 
-// POOL: the tracks of many solves (a batched pool); each track takes its
+// MODE 1: the tracks of many solves (a batched pool); each track takes its
 // pending angular-flux scale and done flag from its own solve's state.
-template <int PH, int LPS, int PS, int EXPK, bool POOL>
+// MODE 2: one problem, also tallying the partial currents out of the
+// coarse-mesh cells for CMFD (a.cm_cell set).
+template <int PH, int LPS, int PS, int EXPK, int MODE>
 __global__ void __launch_bounds__(kSweepThreads,
                                   (SweepOccupancy<PH, PS>::min_blocks))
 sweep_kernel(const SweepArgs a) {
+  constexpr bool POOL = MODE == 1;
+  constexpr bool CMFD = MODE == 2;
   extern __shared__ float smem[];
   DevScalars* sc = a.sc;
   if (a.check_done && *(volatile int*) &sc->done) return;
@@ -308,6 +312,39 @@ sweep_kernel(const SweepArgs a) {
     float len = 0.0f;
     int fsr = 0, mat = 0;
     float2 q[PS];
+    // CMFD partial currents: faces 0 x-, 1 y-, 2 x+, 3 y+ of cell
+    // iy * nx + ix; each crossing adds sum_p w_p psi_p of the lane's pairs
+    auto add_current = [&](int cell, int face) {
+      float2* cp = reinterpret_cast<float2*>(
+                       a.cm_cur + ((int64_t) cell * 4 + face) * ld) + sub;
+#pragma unroll
+      for (int s2 = 0; s2 < PS; s2++) {
+        if (sub + s2 * LPS < npairs) {
+          float2 j = f2(0.0f);
+#pragma unroll
+          for (int p = 0; p < PH; p++) j = __ffma2_rn(w2[p], psi[s2][p], j);
+          atomicAdd(cp + s2 * LPS, j);
+        }
+      }
+    };
+    auto tally_current = [&](int f0, int f1, bool at_end) {
+      const int c0 = __ldg(a.cm_cell + f0);
+      if (f1 >= 0) {
+        const int c1 = __ldg(a.cm_cell + f1);
+        if (c1 == c0) return;
+        const int dx = c1 % a.cm_nx - c0 % a.cm_nx;
+        const int dy = c1 / a.cm_nx - c0 / a.cm_nx;
+        if (dx != 0) {
+          add_current(c0, dx > 0 ? 2 : 0);
+          if (dy != 0) add_current(c0 + dx, dy > 0 ? 3 : 1);
+        } else if (dy != 0) {
+          add_current(c0, dy > 0 ? 3 : 1);
+        }
+      } else if (at_end) {
+        const int face = a.cm_end[2 * t + dir];
+        if (face >= 0) add_current(c0, face);
+      }
+    };
     if constexpr (kStaged) {
 #pragma unroll
       for (int j = 0; j < kAhead; j++) stage(j);
@@ -375,6 +412,22 @@ sweep_kernel(const SweepArgs a) {
           }
         }
       }
+      if constexpr (CMFD) {
+        // partial current out of the coarse cell when the next segment lies
+        // in another one (through an intermediate cell at a corner), or out
+        // through the boundary at the end of a track that is not continued
+        int fsr_next = -1;
+        if (k + 1 < n) {
+          if constexpr (kStaged) {
+            float l2;
+            int m2;
+            unpack(word(k + 1), l2, fsr_next, m2);
+          } else {
+            fsr_next = fsr_n;
+          }
+        }
+        tally_current(fsr, fsr_next, k + 1 == n);
+      }
       if constexpr (!kStaged) {
         len = len_n;
         fsr = fsr_n;
@@ -431,7 +484,7 @@ sweep_kernel(const SweepArgs a) {
   }
 }
 
-template <int PH, int LPS, int PS, int EXPK, bool POOL>
+template <int PH, int LPS, int PS, int EXPK, int MODE>
 void launch_sweep_instance(const SweepArgs& a, cudaStream_t stream) {
   const int spw = 32 / LPS;
   const int64_t warps = (2 * a.num_tracks + spw - 1) / spw;
@@ -444,7 +497,7 @@ void launch_sweep_instance(const SweepArgs& a, cudaStream_t stream) {
            ? sizeof(float2) * (SweepRing<PH, LPS, PS>::ahead + 1) * PS *
                  kSweepThreads
            : 0);
-  auto kern = sweep_kernel<PH, LPS, PS, EXPK, POOL>;
+  auto kern = sweep_kernel<PH, LPS, PS, EXPK, MODE>;
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int) smem);
@@ -452,15 +505,15 @@ void launch_sweep_instance(const SweepArgs& a, cudaStream_t stream) {
 }
 
 // slots = pairs of groups per lane
-template <int PH, int LPS, int EXPK, bool POOL>
+template <int PH, int LPS, int EXPK, int MODE>
 bool launch_sweep_pairs(const SweepArgs& a, int slots, cudaStream_t s) {
   switch (slots) {
-    case 1: launch_sweep_instance<PH, LPS, 1, EXPK, POOL>(a, s); return true;
-    case 2: launch_sweep_instance<PH, LPS, 2, EXPK, POOL>(a, s); return true;
-    case 3: launch_sweep_instance<PH, LPS, 3, EXPK, POOL>(a, s); return true;
-    case 4: launch_sweep_instance<PH, LPS, 4, EXPK, POOL>(a, s); return true;
-    case 5: launch_sweep_instance<PH, LPS, 5, EXPK, POOL>(a, s); return true;
-    case 6: launch_sweep_instance<PH, LPS, 6, EXPK, POOL>(a, s); return true;
+    case 1: launch_sweep_instance<PH, LPS, 1, EXPK, MODE>(a, s); return true;
+    case 2: launch_sweep_instance<PH, LPS, 2, EXPK, MODE>(a, s); return true;
+    case 3: launch_sweep_instance<PH, LPS, 3, EXPK, MODE>(a, s); return true;
+    case 4: launch_sweep_instance<PH, LPS, 4, EXPK, MODE>(a, s); return true;
+    case 5: launch_sweep_instance<PH, LPS, 5, EXPK, MODE>(a, s); return true;
+    case 6: launch_sweep_instance<PH, LPS, 6, EXPK, MODE>(a, s); return true;
     default: return false;
   }
 }
@@ -471,11 +524,17 @@ template <int PH, int LPS, int EXPK>
 bool dispatch_sweep_slots(const SweepArgs& a, int slots, cudaStream_t s) {
   if (a.track_slot) {
     if constexpr (EXPK == kExpIntrinsic)
-      return launch_sweep_pairs<PH, LPS, EXPK, true>(a, slots, s);
+      return launch_sweep_pairs<PH, LPS, EXPK, 1>(a, slots, s);
     else
       return false;
   }
-  return launch_sweep_pairs<PH, LPS, EXPK, false>(a, slots, s);
+  if (a.cm_cell) {
+    if constexpr (EXPK == kExpIntrinsic)
+      return launch_sweep_pairs<PH, LPS, EXPK, 2>(a, slots, s);
+    else
+      return false;
+  }
+  return launch_sweep_pairs<PH, LPS, EXPK, 0>(a, slots, s);
 }
 
 template <int PH, int EXPK>
