@@ -337,6 +337,66 @@ typedef struct {
 int moc_set_otf_tracks(moc_ctx* ctx, const moc_otf_tracks* tracks);
 int moc_get_otf_tracks(moc_ctx* ctx, int* enabled);
 
+/* ---- CMFD acceleration ----------------------------------------------------
+ * Coarse-mesh finite-difference acceleration of moc_compute_eigenvalue
+ * (2D flat-source problems; replaces the reference's Cmfd, src/Cmfd.h, as
+ * Geometry::setCmfd attaches it and Solver::computeEigenvalue calls
+ * Cmfd::computeKeff in place of computeKeff, src/Solver.cpp:1597-1645).
+ * Every iteration the sweep also tallies the partial currents out of the
+ * coarse cells; the FSR fluxes are reduced on the mesh, the coarse
+ * diffusion eigenproblem (cross sections collapsed by flux, surface
+ * diffusion coefficients with Larsen's correction and the nonlinear
+ * correction term, relaxation, flux limiting) is solved in FP64 on the
+ * host, and the FSR fluxes are scaled by the ratio of the new to the old
+ * coarse flux.  The mesh must not cut an FSR: each FSR lies in one cell. */
+#define MOC_BC_VACUUM 0
+#define MOC_BC_REFLECTIVE 1
+typedef struct {
+  int32_t num_x, num_y;        /* Cmfd::setLatticeStructure */
+  const double* widths_x;      /* [num_x] cm (Cmfd::setWidths) */
+  const double* widths_y;      /* [num_y] cm */
+  const int32_t* fsr_cell;     /* [R] cell of every FSR: iy * num_x + ix,
+                                  iy counted from y-min (Cmfd::findCmfdCell,
+                                  src/Cmfd.cpp:2007-2026) */
+  const int8_t* track_end_face;/* [T][2] mesh boundary face crossed where the
+                                  forward / backward traversal of each track
+                                  leaves the geometry (0 x-min, 1 y-min,
+                                  2 x-max, 3 y-max), -1 none */
+  int32_t boundary[4];         /* x-min, y-min, x-max, y-max:
+                                  MOC_BC_VACUUM or MOC_BC_REFLECTIVE */
+  int32_t num_cmfd_groups;     /* E (Cmfd::setGroupStructure) */
+  const int32_t* group_of;     /* [G] coarse group of each group, 0 for the
+                                  first, rising by at most 1; NULL: E = G,
+                                  one coarse group per group */
+  int32_t num_edc_angles;      /* n > 0: Larsen's effective diffusion
+                                  coefficient correction over these angles
+                                  (azimuthal < num_azim / 2 x polar <
+                                  num_polar / 2); 0: no correction */
+  const double* edc_mu;        /* [n] cos theta */
+  const double* edc_weight;    /* [n] azimuthal x polar weight */
+  double relaxation;           /* setCMFDRelaxationFactor (reference 0.7) */
+  double sor_factor;           /* setSORRelaxationFactor (reference 1.5) */
+  int32_t flux_limiting;       /* useFluxLimiting (reference 1) */
+  int32_t num_unbounded_iterations; /* setNumUnboundedIterations (0) */
+} moc_cmfd_mesh;
+
+/** Attaches CMFD to the context (tracks, quadrature, materials and FSRs
+ *  uploaded; not with a linear source or on-the-fly segmentation); NULL
+ *  detaches it.  Dropped when tracks are re-uploaded.  Uses the hardware
+ *  exponential (MOC_ERR_UNSUPPORTED if the table was requested). */
+int moc_set_cmfd(moc_ctx* ctx, const moc_cmfd_mesh* mesh);
+/** Whether CMFD is attached, the last coarse eigenvalue, the coarse power
+ *  iterations and SOR sweeps of the last coarse solve, and its
+ *  prolongation ratio farthest from 1 (any pointer may be NULL). */
+int moc_get_cmfd_info(moc_ctx* ctx, int* enabled, double* keff,
+                      int* power_iterations, int* linear_iterations,
+                      double* max_ratio);
+/** The coarse fluxes of the last coarse solve, [cells][E], before (old) and
+ *  after (new) it, each normalised to unit total fission source
+ *  (Cmfd::rescaleFlux); either pointer may be NULL. */
+int moc_get_cmfd_fluxes(moc_ctx* ctx, double* old_flux, double* new_flux,
+                        int64_t n);
+
 /** Number of CUDA kernels this library launched on the context so far. */
 int moc_get_launch_count(moc_ctx* ctx, int64_t* launches);
 

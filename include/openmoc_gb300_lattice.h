@@ -49,6 +49,15 @@ int moc_lattice_export(moc_lattice* lat, float* seg_len, int32_t* seg_fsr,
                        int64_t* seg_off, int32_t* track_ang, int64_t* next,
                        uint8_t* flags, float* weights, float* inv_sin,
                        int32_t* fsr_mat, float* fsr_vol);
+/** What a CMFD mesh (moc_cmfd_mesh, openmoc_gb300.h) is laid over, for a
+ *  2D lattice: per FSR the box of its lattice cell [R][4] (xmin, xmax,
+ *  ymin, ymax), per track the boundary face at the end of its forward and
+ *  backward traversal [T][2] (0 x-min, 1 y-min, 2 x-max, 3 y-max; -1 none),
+ *  the Larsen-EDC quadrature [A][Ph] (cos theta; azimuthal x polar weight)
+ *  and the geometry's bounds [4] (xmin, xmax, ymin, ymax). */
+int moc_lattice_export_cmfd(moc_lattice* lat, double* fsr_box,
+                            int8_t* end_face, double* edc_mu, double* edc_w,
+                            double* bounds);
 int moc_lattice_destroy(moc_lattice* lat);
 
 /** moc_lattice_generate with the ray tracing on CUDA device `device`: the

@@ -7,10 +7,11 @@ OpenMOC's Solver interface.
     solver.computeEigenvalue()
     solver.getKeff(), solver.getFlux(fsr, group)
 """
+from .cmfd import Cmfd  # noqa: F401
 from .problem import Problem, load_packed, save_packed  # noqa: F401
 from .solver import (EXP_INTRINSIC, EXP_TABLE, FISSION_SOURCE,  # noqa: F401
                      SCALAR_FLUX, TOTAL_SOURCE, GB300LSSolver, GB300Solver)
 
-__all__ = ["GB300Solver", "GB300LSSolver", "Problem", "load_packed", "save_packed",
+__all__ = ["GB300Solver", "GB300LSSolver", "Cmfd", "Problem", "load_packed", "save_packed",
            "SCALAR_FLUX", "FISSION_SOURCE", "TOTAL_SOURCE", "EXP_TABLE",
            "EXP_INTRINSIC"]

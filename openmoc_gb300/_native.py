@@ -14,6 +14,8 @@ import threading
 from . import build as _build
 
 MOC_OK = 0
+MOC_ERR_ARG = -1
+MOC_ERR_UNSUPPORTED = -5
 ERRORS = {
     -1: "invalid argument",
     -2: "CUDA error",
@@ -52,6 +54,19 @@ class OtfTracks(C.Structure):
                 ("rad_len", C.c_void_p), ("rad_fsr", C.c_void_p),
                 ("rad_off", C.c_void_p), ("rad_start", C.c_void_p),
                 ("rad_total", C.c_void_p), ("above_fsr", C.c_int32)]
+
+
+class CmfdMesh(C.Structure):
+    """moc_cmfd_mesh: the coarse mesh and settings of CMFD acceleration."""
+    _fields_ = [("num_x", C.c_int32), ("num_y", C.c_int32),
+                ("widths_x", C.c_void_p), ("widths_y", C.c_void_p),
+                ("fsr_cell", C.c_void_p), ("track_end_face", C.c_void_p),
+                ("boundary", C.c_int32 * 4), ("num_cmfd_groups", C.c_int32),
+                ("group_of", C.c_void_p), ("num_edc_angles", C.c_int32),
+                ("edc_mu", C.c_void_p), ("edc_weight", C.c_void_p),
+                ("relaxation", C.c_double), ("sor_factor", C.c_double),
+                ("flux_limiting", C.c_int32),
+                ("num_unbounded_iterations", C.c_int32)]
 
 
 _P = C.c_void_p
@@ -119,6 +134,11 @@ _SIGS = {
     "moc_set_negative_fluxes_allowed": ([_P, C.c_int], C.c_int),
     "moc_set_otf_tracks": ([_P, C.POINTER(OtfTracks)], C.c_int),
     "moc_get_otf_tracks": ([_P, C.POINTER(C.c_int)], C.c_int),
+    "moc_set_cmfd": ([_P, C.POINTER(CmfdMesh)], C.c_int),
+    "moc_get_cmfd_info": ([_P, C.POINTER(C.c_int), C.POINTER(C.c_double),
+                           C.POINTER(C.c_int), C.POINTER(C.c_int),
+                           C.POINTER(C.c_double)], C.c_int),
+    "moc_get_cmfd_fluxes": ([_P, _P, _P, C.c_int64], C.c_int),
 }
 
 _lock = threading.Lock()

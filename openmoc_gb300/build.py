@@ -22,7 +22,7 @@ LIB = os.path.join(OUT, "libopenmoc_gb300.so")
 
 SOURCES = ["sweep.cu", "solver_kernels.cu", "moc_api.cu", "lattice.cpp",
            "noalloc.cu", "serve.cu", "sources_tc.cu", "linear_source.cu",
-           "lattice_gpu.cu", "otf_sweep.cu"] + [
+           "lattice_gpu.cu", "otf_sweep.cu", "cmfd.cu", "cmfd_solve.cpp"] + [
     f"sweep_p{ph}_e{e}.cu" for ph in (1, 2, 3) for e in (0, 1)] + [
     f"ls_sweep_p{ph}.cu" for ph in (1, 2, 3)]
 

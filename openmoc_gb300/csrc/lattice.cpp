@@ -308,7 +308,13 @@ void lat_finish(const moc_lattice_spec& s, moc_lattice* L, const LatGeo& X,
     L->pol_wgt.push_back(w_p[p]);
   }
   L->moderator = s.moderator_material;
-  L->moderator = s.moderator_material;
+  L->fsr_pin.resize(R);
+  for (int64_t r = 0; r < R; r++) L->fsr_pin[r] = (int32_t) (keys[r] >> 32);
+  L->nx = s.nx;
+  L->ny = s.ny;
+  L->pitch = s.pitch;
+  L->xmin = X.xmin;
+  L->ymin = X.ymin;
 }
 
 }  // namespace moc_lat
@@ -918,5 +924,52 @@ extern "C" int moc_lattice_extrude(const moc_lattice* L2, double height,
   L->fsr_vol.resize(R2 + 1);
   for (int64_t r = 0; r <= R2; r++) L->fsr_vol[r] = (float) vol[r];
   *out = L;
+  return 0;
+}
+
+extern "C" int moc_lattice_export_cmfd(moc_lattice* L, double* fsr_box,
+                                       int8_t* end_face, double* edc_mu,
+                                       double* edc_w, double* bounds) {
+  if (!L) return lat_fail("null lattice");
+  if (L->tracks.empty() || (int64_t) L->tracks.size() != L->T ||
+      (int64_t) L->fsr_pin.size() != L->R)
+    return lat_fail("the CMFD geometry needs a 2D lattice");
+  if (!fsr_box || !end_face || !edc_mu || !edc_w || !bounds)
+    return lat_fail("null output array");
+  const double W = L->nx * L->pitch, H = L->ny * L->pitch;
+  const double x0 = L->xmin, y0 = L->ymin;
+  for (int64_t r = 0; r < L->R; r++) {
+    const int pin = L->fsr_pin[r];
+    const int ci = pin % L->nx, row = pin / L->nx;
+    const int cj = L->ny - 1 - row;
+    fsr_box[4 * r] = x0 + ci * L->pitch;
+    fsr_box[4 * r + 1] = x0 + (ci + 1) * L->pitch;
+    fsr_box[4 * r + 2] = y0 + cj * L->pitch;
+    fsr_box[4 * r + 3] = y0 + (cj + 1) * L->pitch;
+  }
+  // the boundary face a track end lies on (x faces first at a corner)
+  const double tol = 1e-9 * std::max(W, H);
+  auto face = [&](double x, double y) -> int8_t {
+    if (std::fabs(x - x0) <= tol) return 0;
+    if (std::fabs(x - (x0 + W)) <= tol) return 2;
+    if (std::fabs(y - y0) <= tol) return 1;
+    if (std::fabs(y - (y0 + H)) <= tol) return 3;
+    return -1;
+  };
+  for (int64_t t = 0; t < L->T; t++) {
+    const Track& tr = L->tracks[t];
+    end_face[2 * t] = face(tr.x1, tr.y1);
+    end_face[2 * t + 1] = face(tr.x0, tr.y0);
+  }
+  for (int a = 0; a < L->A; a++)
+    for (int p = 0; p < L->Ph; p++) {
+      const double sn = L->pol_sin[p];
+      edc_mu[a * L->Ph + p] = std::sqrt(1.0 - sn * sn);
+      edc_w[a * L->Ph + p] = L->az_weight[a] * L->pol_wgt[p];
+    }
+  bounds[0] = x0;
+  bounds[1] = x0 + W;
+  bounds[2] = y0;
+  bounds[3] = y0 + H;
   return 0;
 }

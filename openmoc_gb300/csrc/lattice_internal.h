@@ -78,4 +78,9 @@ struct moc_lattice {
   std::vector<int32_t> rad_fsr;
   std::vector<int64_t> rad_off;
   int32_t above_fsr = -1;
+  // 2D lattices: the lattice cell of every FSR (row 0 at the top, as the
+  // FSR keys number them) and the lattice's placement, for CMFD meshes
+  std::vector<int32_t> fsr_pin;
+  int32_t nx = 0, ny = 0;
+  double pitch = 0.0, xmin = 0.0, ymin = 0.0;
 };

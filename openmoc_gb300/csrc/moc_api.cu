@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "../../include/openmoc_gb300.h"
+#include "cmfd_internal.h"
 #include "moc_internal.cuh"
 
 namespace {
@@ -185,6 +186,24 @@ struct moc_ctx {
   int64_t otf_S2 = 0;
   int otf_above_fsr = 0;
   int otf_above_word = 0;    // above_fsr | material << 24
+  // CMFD (moc_set_cmfd): the coarse cell of every FSR, the boundary face at
+  // each track end, outgoing partial currents [cells][4][ld], coarse group
+  // of each group, FSRs by (cell, material) pair (CSR), their FP64 flux
+  // sums [P][G] and the prolongation ratios [cells][E]; pinned host copies
+  // of the sums and currents; the host coarse solver
+  moc_cmfd::Solver* cmfd = nullptr;
+  std::vector<int32_t> h_cm_cell;
+  int32_t* cm_cell = nullptr;
+  int8_t* cm_end = nullptr;
+  float* cm_cur = nullptr;
+  int32_t* cm_group = nullptr;
+  int32_t* cm_pair_off = nullptr;
+  int32_t* cm_pair_fsr = nullptr;
+  double* cm_sums = nullptr;
+  double* cm_ratio = nullptr;
+  double* h_cm_sums = nullptr;
+  float* h_cm_cur = nullptr;
+  int64_t cm_sums_n = 0;
 };
 
 namespace {
@@ -245,6 +264,12 @@ moc::SweepArgs sweep_args(moc_ctx* c, int check_done) {
     a.ang_dir = c->ls_dir;
     a.qxy = c->qxy;
     a.mom = c->mom;
+  }
+  if (c->cmfd && !c->ls && !c->otf) {
+    a.cm_cell = c->cm_cell;
+    a.cm_cur = c->cm_cur;
+    a.cm_end = c->cm_end;
+    a.cm_nx = c->cmfd->cfg.nx;
   }
   return a;
 }
@@ -419,10 +444,11 @@ int enqueue_sweep(moc_ctx* c, int check_done, bool timed, int ev_index) {
 struct TuneKey {
   int G, Ph, M, exp_fixed, exp_kind, ls;
   int64_t T, S, R;
+  int cm;
   bool operator<(const TuneKey& o) const {
-    return std::tie(G, Ph, M, exp_fixed, exp_kind, ls, T, S, R) <
+    return std::tie(G, Ph, M, exp_fixed, exp_kind, ls, T, S, R, cm) <
            std::tie(o.G, o.Ph, o.M, o.exp_fixed, o.exp_kind, o.ls, o.T, o.S,
-                    o.R);
+                    o.R, o.cm);
   }
 };
 using TuneVal = moc_tune_entry;
@@ -452,7 +478,7 @@ int autotune_sweep(moc_ctx* c, bool use_cache) {
   TuneKey key{c->d.num_groups, c->d.num_polar_half, c->d.num_materials,
               c->exp_user_set, c->exp_user_set ? c->exp_kind : -1,
               c->ls ? 1 : 0, c->d.num_tracks, c->d.num_segments,
-              c->d.num_fsrs};
+              c->d.num_fsrs, c->cmfd ? 1 : 0};
   if (use_cache) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune_cache.find(key);
@@ -467,7 +493,8 @@ int autotune_sweep(moc_ctx* c, bool use_cache) {
   const int G = c->d.num_groups;
   std::vector<int> kinds;
   // the linear-source and on-the-fly sweeps have one exponential evaluator
-  if (c->exp_user_set || c->ls || c->otf) kinds.push_back(c->exp_kind);
+  if (c->exp_user_set || c->ls || c->otf || c->cmfd)
+    kinds.push_back(c->exp_kind);
   else kinds = {MOC_EXP_TABLE, MOC_EXP_INTRINSIC};
   TuneVal best{0, 0, 0, 1e30f};
   c->tune_log.clear();
@@ -638,6 +665,145 @@ int pack_materials(moc_ctx* c) {
   MOC_CUDA(cudaGetLastError());
   MOC_CUDA(cudaStreamSynchronize(c->stream));
   c->mat_packed = 1;
+  return MOC_OK;
+}
+
+void cmfd_release(moc_ctx* c) {
+  dfree(c->cm_cell);
+  dfree(c->cm_end);
+  dfree(c->cm_cur);
+  dfree(c->cm_group);
+  dfree(c->cm_pair_off);
+  dfree(c->cm_pair_fsr);
+  dfree(c->cm_sums);
+  dfree(c->cm_ratio);
+  if (c->h_cm_sums) cudaFreeHost(c->h_cm_sums);
+  if (c->h_cm_cur) cudaFreeHost(c->h_cm_cur);
+  c->h_cm_sums = nullptr;
+  c->h_cm_cur = nullptr;
+  c->cm_sums_n = 0;
+  c->h_cm_cell.clear();
+  delete c->cmfd;
+  c->cmfd = nullptr;
+}
+
+// Per solve: the cross sections and FSR data the coarse solve collapses
+// (read back from the device, so that any upload since is seen), the
+// (cell, material) pairs with their FSR lists, and the pair-sum buffers.
+int cmfd_prepare(moc_ctx* c) {
+  moc_cmfd::Solver& S = *c->cmfd;
+  const int M = c->d.num_materials, G = c->d.num_groups;
+  const int64_t R = c->d.num_fsrs;
+  const int64_t MG = (int64_t) M * G;
+  std::vector<float> st(MG), nf(MG), ss(MG * G), vol(R);
+  std::vector<int32_t> mat(R);
+  MOC_CUDA(cudaMemcpy(st.data(), c->sigma_t, 4 * MG, cudaMemcpyDeviceToHost));
+  MOC_CUDA(cudaMemcpy(nf.data(), c->nu_sigma_f, 4 * MG,
+                      cudaMemcpyDeviceToHost));
+  MOC_CUDA(cudaMemcpy(ss.data(), c->sigma_s, 4 * MG * G,
+                      cudaMemcpyDeviceToHost));
+  MOC_CUDA(cudaMemcpy(vol.data(), c->fsr_vol, 4 * R, cudaMemcpyDeviceToHost));
+  MOC_CUDA(cudaMemcpy(mat.data(), c->fsr_mat, 4 * R, cudaMemcpyDeviceToHost));
+  moc_cmfd::Fine& F = S.fine;
+  F.M = M;
+  F.st.assign(st.begin(), st.end());
+  F.nf.assign(nf.begin(), nf.end());
+  F.ss.assign(ss.begin(), ss.end());
+  F.chi.assign(c->h_chi.begin(), c->h_chi.end());
+  const int C = S.cfg.cells();
+  F.cell_vol.assign(C, 0.0);
+  // pair id of every (cell, material) in use, in cell-major order
+  std::vector<int32_t> pid((size_t) C * M, -1);
+  for (int64_t r = 0; r < R; r++) {
+    pid[(size_t) c->h_cm_cell[r] * M + mat[r]] = 0;
+    F.cell_vol[c->h_cm_cell[r]] += (double) vol[r];
+  }
+  F.pair_cell.clear();
+  F.pair_mat.clear();
+  for (int cell = 0; cell < C; cell++)
+    for (int m = 0; m < M; m++)
+      if (pid[(size_t) cell * M + m] == 0) {
+        pid[(size_t) cell * M + m] = F.pairs();
+        F.pair_cell.push_back(cell);
+        F.pair_mat.push_back(m);
+      }
+  const int P = F.pairs();
+  std::vector<int32_t> off(P + 1, 0), list(R);
+  for (int64_t r = 0; r < R; r++)
+    off[pid[(size_t) c->h_cm_cell[r] * M + mat[r]] + 1]++;
+  for (int p = 0; p < P; p++) off[p + 1] += off[p];
+  std::vector<int32_t> fill(off.begin(), off.end() - 1);
+  for (int64_t r = 0; r < R; r++)
+    list[fill[pid[(size_t) c->h_cm_cell[r] * M + mat[r]]]++] = (int32_t) r;
+  dfree(c->cm_pair_off);
+  dfree(c->cm_pair_fsr);
+  MOC_TRY(dalloc(&c->cm_pair_off, P + 1));
+  MOC_TRY(dalloc(&c->cm_pair_fsr, R));
+  MOC_CUDA(cudaMemcpy(c->cm_pair_off, off.data(), 4 * (P + 1),
+                      cudaMemcpyHostToDevice));
+  MOC_CUDA(cudaMemcpy(c->cm_pair_fsr, list.data(), 4 * R,
+                      cudaMemcpyHostToDevice));
+  const int64_t n = (int64_t) P * G;
+  if (n != c->cm_sums_n) {
+    dfree(c->cm_sums);
+    if (c->h_cm_sums) cudaFreeHost(c->h_cm_sums);
+    c->h_cm_sums = nullptr;
+    MOC_TRY(dalloc(&c->cm_sums, n));
+    MOC_CUDA(cudaMallocHost(&c->h_cm_sums, 8 * n));
+    c->cm_sums_n = n;
+  }
+  S.reset();
+  S.source_threshold = 0.1 * c->threshold;   // Solver::initializeCmfd
+  return MOC_OK;
+}
+
+// computeEigenvalue with CMFD (src/Solver.cpp:1591-1647): per iteration
+// sources, sweep with current tallies, addSourceToScalarFlux, the coarse
+// solve in place of computeKeff (flux sums and currents to the host, ratios
+// back, prolongation), normalizeFluxes, residual and store.  The host reads
+// the device state every iteration: the coarse solve needs its tallies.
+int run_cmfd_iterations(moc_ctx* c, int res_type) {
+  moc_cmfd::Solver& S = *c->cmfd;
+  moc::SolverArgs a = solver_args(c, 1);
+  const int C = S.cfg.cells(), E = S.cfg.E;
+  const int ld = row_stride(c);
+  const int64_t ncur = (int64_t) C * moc_cmfd::kFaces * ld;
+  for (int it = 0;; it++) {
+    enqueue_sources(c, a, -1, 1);
+    MOC_CUDA(cudaMemsetAsync(c->cm_cur, 0, 4 * ncur, c->stream));
+    MOC_TRY(enqueue_sweep(c, 1, true, 0));
+    enqueue_add_source(c, a, 0);
+    moc::launch_cmfd_pair_sums(c->phi, c->fsr_vol, c->cm_pair_off,
+                               c->cm_pair_fsr, S.fine.pairs(),
+                               c->d.num_groups, ld, c->cm_sums, c->stream);
+    c->launches++;
+    MOC_CUDA(cudaGetLastError());
+    MOC_CUDA(cudaMemcpyAsync(c->h_cm_sums, c->cm_sums, 8 * c->cm_sums_n,
+                             cudaMemcpyDeviceToHost, c->stream));
+    MOC_CUDA(cudaMemcpyAsync(c->h_cm_cur, c->cm_cur, 4 * ncur,
+                             cudaMemcpyDeviceToHost, c->stream));
+    MOC_CUDA(cudaStreamSynchronize(c->stream));
+    const double k = S.step(it, c->h_cm_sums, c->h_cm_cur, ld);
+    MOC_CUDA(cudaMemcpyAsync(c->cm_ratio, S.ratio.data(), 8 * (int64_t) C * E,
+                             cudaMemcpyHostToDevice, c->stream));
+    moc::launch_cmfd_prolong(c->phi, c->cm_cell, c->cm_group, c->cm_ratio,
+                             c->d.num_fsrs, c->d.num_groups, ld, E, c->sc, k,
+                             c->stream);
+    moc::launch_fission_rate(a, 1, c->stream);
+    moc::launch_residual(a, res_type, 1, 1, 1, c->stream);
+    c->launches += 3;
+    MOC_CUDA(cudaGetLastError());
+    MOC_TRY(pull(c));
+    MOC_TRY(collect_sweep_times(c, 1));
+    c->num_sweeps++;
+    // the coarse solve's tolerance follows the transport residual
+    double res = c->hsc->residual;
+    if (res <= 0.0) res = 1e-6;
+    S.source_threshold = 0.01 * res;
+    if (c->hsc->done) break;
+  }
+  c->keff = c->hsc->keff;
+  c->residual = c->hsc->residual;
   return MOC_OK;
 }
 
@@ -856,6 +1022,7 @@ int moc_destroy(moc_ctx* c) {
   dfree(c->otf_rad_off);
   dfree(c->otf_rad_total);
   dfree(c->otf_order);
+  cmfd_release(c);
   dfree(c->sc);
   if (c->hsc) cudaFreeHost(c->hsc);
   for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
@@ -966,6 +1133,7 @@ int moc_upload_tracks(moc_ctx* c, const float* seg_len, const int32_t* seg_fsr,
   MOC_CUDA(cudaMemcpy(c->flags, flags, T, cudaMemcpyHostToDevice));
   ls_release(c);
   otf_release(c);
+  cmfd_release(c);
   c->have_tracks = true;
   MOC_TRY(pack_materials(c));
   return MOC_OK;
@@ -1295,6 +1463,12 @@ int moc_compute_eigenvalue(moc_ctx* c, int max_iters, int res_type) {
             "without fissionable FSRs");
   MOC_CHECK(c->num_fissionable > 0, MOC_ERR_ARG,
             "an eigenvalue solve needs fissionable material");
+  if (c->cmfd) {
+    MOC_CHECK(!c->ls && !c->otf, MOC_ERR_UNSUPPORTED,
+              "CMFD acceleration of a linear-source or on-the-fly solve is "
+              "not supported");
+    MOC_TRY(cmfd_prepare(c));
+  }
   MOC_TRY(maybe_autotune(c));
   // Solver::computeInitialFluxGuess: flat flux 1, normalised, stored;
   // zero boundary fluxes (src/Solver.cpp:1710-1757)
@@ -1309,7 +1483,10 @@ int moc_compute_eigenvalue(moc_ctx* c, int max_iters, int res_type) {
   MOC_CUDA(cudaMemcpyAsync(c->phi_old, c->phi, 4 * num_flux(c),
                            cudaMemcpyDeviceToDevice, c->stream));
   MOC_CUDA(cudaGetLastError());
-  MOC_TRY(run_iterations(c, moc::kModeEigen, res_type));
+  if (c->cmfd)
+    MOC_TRY(run_cmfd_iterations(c, res_type));
+  else
+    MOC_TRY(run_iterations(c, moc::kModeEigen, res_type));
   c->num_iterations = c->hsc->iteration;
   return MOC_OK;
 }
@@ -2057,6 +2234,156 @@ int moc_set_otf_tracks(moc_ctx* c, const moc_otf_tracks* d) {
 int moc_get_otf_tracks(moc_ctx* c, int* enabled) {
   MOC_CHECK(c && enabled, MOC_ERR_ARG, "null argument");
   *enabled = c->otf ? 1 : 0;
+  return MOC_OK;
+}
+
+int moc_set_cmfd(moc_ctx* c, const moc_cmfd_mesh* m) {
+  MOC_TRY(ready(c));
+  if (!m) {
+    if (c->cmfd) {
+      cmfd_release(c);
+      c->tuned = false;
+      if (!c->exp_user_set) c->exp_kind = MOC_EXP_TABLE;
+    }
+    return MOC_OK;
+  }
+  MOC_CHECK(!c->ls && !c->otf, MOC_ERR_UNSUPPORTED,
+            "CMFD is supported for 2D flat-source solves with stored "
+            "segments");
+  MOC_CHECK(!(c->exp_user_set && c->exp_kind == MOC_EXP_TABLE),
+            MOC_ERR_UNSUPPORTED,
+            "CMFD current tallies use the hardware exponential");
+  const int64_t R = c->d.num_fsrs, T = c->d.num_tracks;
+  const int G = c->d.num_groups;
+  MOC_CHECK(m->num_x >= 1 && m->num_y >= 1 &&
+                (int64_t) m->num_x * m->num_y <= (1 << 24),
+            MOC_ERR_ARG, "bad CMFD lattice structure");
+  MOC_CHECK(m->widths_x && m->widths_y && m->fsr_cell && m->track_end_face,
+            MOC_ERR_ARG, "null CMFD mesh array");
+  const int C = m->num_x * m->num_y;
+  for (int i = 0; i < m->num_x; i++)
+    MOC_CHECK(std::isfinite(m->widths_x[i]) && m->widths_x[i] > 0.0,
+              MOC_ERR_ARG, "CMFD cell widths must be positive");
+  for (int i = 0; i < m->num_y; i++)
+    MOC_CHECK(std::isfinite(m->widths_y[i]) && m->widths_y[i] > 0.0,
+              MOC_ERR_ARG, "CMFD cell widths must be positive");
+  for (int64_t r = 0; r < R; r++)
+    MOC_CHECK(m->fsr_cell[r] >= 0 && m->fsr_cell[r] < C, MOC_ERR_ARG,
+              "CMFD cell out of range at FSR " + std::to_string(r));
+  for (int64_t i = 0; i < 2 * T; i++)
+    MOC_CHECK(m->track_end_face[i] >= -1 && m->track_end_face[i] < 4,
+              MOC_ERR_ARG, "bad track end face");
+  for (int f = 0; f < 4; f++)
+    MOC_CHECK(m->boundary[f] == MOC_BC_VACUUM ||
+                  m->boundary[f] == MOC_BC_REFLECTIVE,
+              MOC_ERR_UNSUPPORTED,
+              "CMFD boundaries must be vacuum or reflective");
+  const int E = m->group_of ? m->num_cmfd_groups : G;
+  MOC_CHECK(E >= 1 && E <= G, MOC_ERR_ARG, "bad number of CMFD groups");
+  std::vector<int> group_of(G);
+  for (int g = 0; g < G; g++) group_of[g] = m->group_of ? m->group_of[g] : g;
+  MOC_CHECK(group_of[0] == 0 && group_of[G - 1] == E - 1, MOC_ERR_ARG,
+            "CMFD groups must cover 0 .. E-1");
+  for (int g = 1; g < G; g++)
+    MOC_CHECK(group_of[g] == group_of[g - 1] ||
+                  group_of[g] == group_of[g - 1] + 1,
+              MOC_ERR_ARG,
+              "CMFD groups must be contiguous ranges of groups");
+  MOC_CHECK(m->num_edc_angles >= 0 &&
+                (m->num_edc_angles == 0 || (m->edc_mu && m->edc_weight)),
+            MOC_ERR_ARG, "bad EDC quadrature");
+  for (int i = 0; i < m->num_edc_angles; i++)
+    MOC_CHECK(m->edc_mu[i] > 0.0 && m->edc_mu[i] <= 1.0 &&
+                  std::isfinite(m->edc_weight[i]),
+              MOC_ERR_ARG, "bad EDC quadrature");
+  MOC_CHECK(std::isfinite(m->relaxation) && m->relaxation > 0.0 &&
+                m->relaxation <= 1.0,
+            MOC_ERR_ARG, "the CMFD relaxation factor must be in (0, 1]");
+  MOC_CHECK(std::isfinite(m->sor_factor) && m->sor_factor > 0.0 &&
+                m->sor_factor < 2.0,
+            MOC_ERR_ARG, "the SOR factor must be in (0, 2)");
+  MOC_CHECK(m->num_unbounded_iterations >= 0, MOC_ERR_ARG,
+            "negative number of unbounded iterations");
+  cmfd_release(c);
+  auto* S = new moc_cmfd::Solver();
+  moc_cmfd::Config& cf = S->cfg;
+  cf.nx = m->num_x;
+  cf.ny = m->num_y;
+  cf.G = G;
+  cf.E = E;
+  cf.wx.assign(m->widths_x, m->widths_x + m->num_x);
+  cf.wy.assign(m->widths_y, m->widths_y + m->num_y);
+  cf.group_of = group_of;
+  cf.gstart.assign(E + 1, G);
+  for (int g = G - 1; g >= 0; g--) cf.gstart[group_of[g]] = g;
+  cf.edc_mu.assign(m->edc_mu, m->edc_mu + m->num_edc_angles);
+  cf.edc_w.assign(m->edc_weight, m->edc_weight + m->num_edc_angles);
+  for (int f = 0; f < 4; f++) cf.bc[f] = m->boundary[f];
+  cf.relaxation = m->relaxation;
+  cf.sor = m->sor_factor;
+  cf.flux_limiting = m->flux_limiting != 0;
+  cf.unbounded = m->num_unbounded_iterations;
+  c->cmfd = S;
+  c->h_cm_cell.assign(m->fsr_cell, m->fsr_cell + R);
+  const int ld = row_stride(c);
+  const int64_t ncur = (int64_t) C * moc_cmfd::kFaces * ld;
+  int st = MOC_OK;
+  auto step = [&](int r) { if (st == MOC_OK) st = r; };
+  step(dalloc(&c->cm_cell, R));
+  step(dalloc(&c->cm_end, 2 * T));
+  step(dalloc(&c->cm_cur, ncur));
+  step(dalloc(&c->cm_group, G));
+  step(dalloc(&c->cm_ratio, (int64_t) C * E));
+  if (st == MOC_OK && cudaMallocHost(&c->h_cm_cur, 4 * ncur) != cudaSuccess)
+    st = fail(MOC_ERR_MEMORY, "pinned host buffer for CMFD currents");
+  if (st != MOC_OK) {
+    cmfd_release(c);
+    return st;
+  }
+  cudaError_t e = cudaMemcpy(c->cm_cell, m->fsr_cell, 4 * R,
+                             cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(c->cm_end, m->track_end_face, 2 * T,
+                   cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(c->cm_group, group_of.data(), 4 * G,
+                   cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(c->cm_cur, 0, 4 * ncur);
+  if (e != cudaSuccess) {
+    cmfd_release(c);
+    return fail(MOC_ERR_CUDA, cudaGetErrorString(e));
+  }
+  S->reset();
+  c->exp_kind = MOC_EXP_INTRINSIC;
+  c->tuned = false;
+  return MOC_OK;
+}
+
+int moc_get_cmfd_info(moc_ctx* c, int* enabled, double* keff,
+                      int* power_iterations, int* linear_iterations,
+                      double* max_ratio) {
+  MOC_CHECK(c, MOC_ERR_ARG, "null context");
+  const moc_cmfd::Solver* S = c->cmfd;
+  if (enabled) *enabled = S ? 1 : 0;
+  if (keff) *keff = S ? S->keff : 0.0;
+  if (power_iterations) *power_iterations = S ? S->stats.power_iterations : 0;
+  if (linear_iterations)
+    *linear_iterations = S ? S->stats.linear_iterations : 0;
+  if (max_ratio) *max_ratio = S ? S->stats.max_ratio : 1.0;
+  return MOC_OK;
+}
+
+int moc_get_cmfd_fluxes(moc_ctx* c, double* old_flux, double* new_flux,
+                        int64_t n) {
+  MOC_CHECK(c && c->cmfd, MOC_ERR_STATE, "CMFD is not attached");
+  const moc_cmfd::Solver& S = *c->cmfd;
+  const int64_t need = (int64_t) S.cfg.cells() * S.cfg.E;
+  MOC_CHECK(n == need, MOC_ERR_ARG,
+            "expected " + std::to_string(need) + " coarse fluxes");
+  if (old_flux && (int64_t) S.phi_old.size() == need)
+    std::copy(S.phi_old.begin(), S.phi_old.end(), old_flux);
+  if (new_flux && (int64_t) S.phi_new.size() == need)
+    std::copy(S.phi_new.begin(), S.phi_new.end(), new_flux);
   return MOC_OK;
 }
 

@@ -307,4 +307,16 @@ void launch_batch_rebase(int2* segs, int64_t S, const int32_t* fsr_mat,
                          int64_t s0, int32_t t0, int32_t a0, int32_t slot,
                          cudaStream_t s);
 
+// CMFD (cmfd.cu): per (coarse cell, material) pair the sums of phi * volume
+// over its FSRs, [P][G] FP64, from the CSR list pair_off [P + 1] /
+// pair_fsr [R]; and the prolongation phi[r][g] *= ratio[cell(r)][group(g)]
+// ([cells][E] FP64), which also sets sc->keff to the coarse eigenvalue.
+void launch_cmfd_pair_sums(const float* phi, const float* vol,
+                           const int32_t* pair_off, const int32_t* pair_fsr,
+                           int P, int G, int ld, double* out, cudaStream_t s);
+void launch_cmfd_prolong(float* phi, const int32_t* fsr_cell,
+                         const int32_t* group_of, const double* ratio,
+                         int64_t R, int G, int ld, int E, DevScalars* sc,
+                         double keff, cudaStream_t s);
+
 }  // namespace moc

@@ -314,7 +314,7 @@ sweep_kernel(const SweepArgs a) {
     float2 q[PS];
     // CMFD partial currents: faces 0 x-, 1 y-, 2 x+, 3 y+ of cell
     // iy * nx + ix; each crossing adds sum_p w_p psi_p of the lane's pairs
-    auto add_current = [&](int cell, int face) {
+    auto add_current = [&](int cell, int face, float frac) {
       float2* cp = reinterpret_cast<float2*>(
                        a.cm_cur + ((int64_t) cell * 4 + face) * ld) + sub;
 #pragma unroll
@@ -323,7 +323,7 @@ sweep_kernel(const SweepArgs a) {
           float2 j = f2(0.0f);
 #pragma unroll
           for (int p = 0; p < PH; p++) j = __ffma2_rn(w2[p], psi[s2][p], j);
-          atomicAdd(cp + s2 * LPS, j);
+          atomicAdd(cp + s2 * LPS, __fmul2_rn(j, f2(frac)));
         }
       }
     };
@@ -334,15 +334,21 @@ sweep_kernel(const SweepArgs a) {
         if (c1 == c0) return;
         const int dx = c1 % a.cm_nx - c0 % a.cm_nx;
         const int dy = c1 / a.cm_nx - c0 / a.cm_nx;
-        if (dx != 0) {
-          add_current(c0, dx > 0 ? 2 : 0);
-          if (dy != 0) add_current(c0 + dx, dy > 0 ? 3 : 1);
-        } else if (dy != 0) {
-          add_current(c0, dy > 0 ? 3 : 1);
+        const int fx = dx > 0 ? 2 : 0, fy = dy > 0 ? 3 : 1;
+        if (dx != 0 && dy != 0) {
+          // through a corner: half by the x neighbour, half by the y one
+          add_current(c0, fx, 0.5f);
+          add_current(c0 + dx, fy, 0.5f);
+          add_current(c0, fy, 0.5f);
+          add_current(c0 + dy * a.cm_nx, fx, 0.5f);
+        } else if (dx != 0) {
+          add_current(c0, fx, 1.0f);
+        } else {
+          add_current(c0, fy, 1.0f);
         }
       } else if (at_end) {
         const int face = a.cm_end[2 * t + dir];
-        if (face >= 0) add_current(c0, face);
+        if (face >= 0) add_current(c0, face, 1.0f);
       }
     };
     if constexpr (kStaged) {

@@ -76,6 +76,8 @@ def _lib():
         L.moc_lattice_export_otf.restype = C.c_int
         L.moc_lattice_export_ls.argtypes = [C.c_void_p] + [C.c_void_p] * 7
         L.moc_lattice_export_ls.restype = C.c_int
+        L.moc_lattice_export_cmfd.argtypes = [C.c_void_p] + [C.c_void_p] * 5
+        L.moc_lattice_export_cmfd.restype = C.c_int
         L.moc_lattice_destroy.argtypes = [C.c_void_p]
         L.moc_lattice_destroy.restype = C.c_int
         L.moc_lattice_last_error.restype = C.c_char_p
@@ -211,6 +213,17 @@ def lattice(nx: int, ny: int, pin_material: np.ndarray, materials: Sequence[Mate
                     "seg_x", "seg_y", "centroid", "ang_dir", "ang_wgt", "pol_sin",
                     "pol_wgt")]):
                 raise RuntimeError(L.moc_lattice_last_error().decode())
+        cm = None
+        if extrude is None:
+            cm = dict(fsr_box=np.empty(4 * R), end_face=np.empty(2 * T, np.int8),
+                      edc_mu=np.empty(A * Ph), edc_w=np.empty(A * Ph),
+                      bounds=np.empty(4))
+            if L.moc_lattice_export_cmfd(h, *[cm[k].ctypes.data for k in (
+                    "fsr_box", "end_face", "edc_mu", "edc_w", "bounds")]):
+                raise RuntimeError(L.moc_lattice_last_error().decode())
+            cm["fsr_box"] = cm["fsr_box"].reshape(R, 4)
+            # (x-min, y-min, x-max, y-max) from bc = (xmin, xmax, ymin, ymax)
+            cm["bc"] = np.array([bc[0], bc[2], bc[1], bc[3]], np.int32)
     finally:
         L.moc_lattice_destroy(h)
     st, ss, nf, ch = pack_materials(materials)
@@ -222,6 +235,7 @@ def lattice(nx: int, ny: int, pin_material: np.ndarray, materials: Sequence[Mate
                 chi=ch, **arr)
     p.linear_source = ls
     p.otf = otf
+    p.cmfd_geometry = cm
     p.meta = dict(nx=nx, ny=ny, num_azim=num_azim, spacing=spacing, pitch=pitch,
                   num_polar=num_polar)
     return p.contiguous()

@@ -101,6 +101,15 @@ class Problem:
     # trk, trk_f, ang, rad_len, rad_fsr, rad_off, rad_start, rad_total,
     # above_fsr); the explicit segments above stay valid.
     otf: Optional[Dict[str, np.ndarray]] = None
+    # What a CMFD mesh is laid over (2D): end_face [T][2] int8 boundary face
+    # crossed where each track's forward / backward traversal leaves the
+    # geometry (0 x-min, 1 y-min, 2 x-max, 3 y-max, -1 none); bounds [4]
+    # (xmin, xmax, ymin, ymax); bc [4] (x-min, y-min, x-max, y-max: 0 vacuum,
+    # 1 reflective); edc_mu / edc_w Larsen-EDC quadrature (cos theta and
+    # azimuthal x polar weight per angle pair); and either fsr_box [R][4]
+    # (xmin, xmax, ymin, ymax of the lattice cell holding each FSR) or a
+    # fixed mesh: fsr_cell [R] with widths_x, widths_y.
+    cmfd_geometry: Optional[Dict[str, np.ndarray]] = None
 
     @property
     def fluxes_per_track(self) -> int:
@@ -226,6 +235,8 @@ def load_packed(base: str) -> Tuple[Problem, Dict[str, float], Dict[str, np.ndar
     if "ls_seg_x" in arrays:
         p.linear_source = {k: arrays["ls_" + k] for k in LS_KEYS + ("centroid",)
                            if "ls_" + k in arrays}
+    if "cm_end_face" in arrays:
+        p.cmfd_geometry = {k[3:]: v for k, v in arrays.items() if k.startswith("cm_")}
     p.meta = dict(sc)
     return p.contiguous(), sc, arrays
 
@@ -238,6 +249,9 @@ def save_packed(base: str, p: Problem, extra_scalars=None, extra_arrays=None) ->
     if p.linear_source is not None:
         for k, v in p.linear_source.items():
             arrays["ls_" + k] = np.ascontiguousarray(v, LS_DTYPES.get(k, v.dtype))
+    if p.cmfd_geometry is not None:
+        for k, v in p.cmfd_geometry.items():
+            arrays["cm_" + k] = np.ascontiguousarray(v)
     if extra_arrays:
         arrays.update(extra_arrays)
     scalars = {k: getattr(p, k) for k in (

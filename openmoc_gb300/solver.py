@@ -60,6 +60,8 @@ class GB300Solver:
         self._source_kind = "auto"
         self._negative_ok = False
         self._formation = "explicit"
+        self._cmfd = None
+        self._cmfd_keep = None
         if track_generator is not None:
             self.setTrackGenerator(track_generator)
 
@@ -123,6 +125,8 @@ class GB300Solver:
             self._call("moc_set_negative_fluxes_allowed", 1)
         if self._formation == "otf":
             self._set_otf()
+        if self._cmfd is not None:
+            self._set_cmfd()
         self._fixed = {}
         self._fixed_by_material = {}
         if p.fixed_sources is not None:
@@ -172,6 +176,53 @@ class GB300Solver:
                                                         "rad_total")),
                               int(arrs["above_fsr"][0]))
         self._call("moc_set_otf_tracks", C.byref(d))
+
+    # ---------------------------------------------------------------- CMFD
+    def setCmfd(self, cmfd) -> None:
+        """Attaches CMFD acceleration (an ``openmoc_gb300.Cmfd``; None
+        detaches it) to computeEigenvalue, as ``Geometry::setCmfd`` does for
+        the reference's solvers (src/Geometry.cpp, src/Solver.cpp:1150-1185)."""
+        self._cmfd = cmfd
+        if self._ctx is not None:
+            if cmfd is None:
+                self._call("moc_set_cmfd", None)
+                self._cmfd_keep = None
+            else:
+                self._set_cmfd()
+
+    def getCmfd(self):
+        return self._cmfd
+
+    def _set_cmfd(self) -> None:
+        mesh, keep = self._cmfd.mesh(self._problem)
+        self._call("moc_set_cmfd", C.byref(mesh))
+        self._cmfd_keep = keep
+
+    def getCmfdInfo(self) -> dict:
+        """The last coarse solve: eigenvalue, power iterations, SOR sweeps
+        and the prolongation ratio farthest from 1."""
+        self._need_ctx()
+        en, k, pi, li, mr = (C.c_int(), C.c_double(), C.c_int(), C.c_int(),
+                             C.c_double())
+        self._call("moc_get_cmfd_info", C.byref(en), C.byref(k), C.byref(pi),
+                   C.byref(li), C.byref(mr))
+        return {"enabled": bool(en.value), "keff": k.value,
+                "power_iterations": pi.value, "linear_iterations": li.value,
+                "max_ratio": mr.value}
+
+    def getCmfdFluxes(self):
+        """(old, new) coarse fluxes of the last coarse solve, [cells][E],
+        each normalised to unit total fission source."""
+        self._need_ctx()
+        if self._cmfd is None:
+            raise _native.MOCError(-3, "CMFD is not attached")
+        mesh, _ = self._cmfd.mesh(self._problem)
+        n = mesh.num_x * mesh.num_y * mesh.num_cmfd_groups
+        old = np.zeros(n, np.float64)
+        new = np.zeros(n, np.float64)
+        self._call("moc_get_cmfd_fluxes", _ptr(old), _ptr(new), n)
+        E = mesh.num_cmfd_groups
+        return old.reshape(-1, E), new.reshape(-1, E)
 
     def allowNegativeFluxes(self, negative_fluxes_on: bool) -> None:
         """Solver::allowNegativeFluxes (src/Solver.cpp:623): negative

@@ -20,6 +20,9 @@ CASES_3D = ["pin3d_g7"]
 # eigenvalue pin cell and a computeSource lattice.
 LS_CASES = ["grad2d_ls", "fixls_c5g7", "pin7_ls", "src3_ls"]
 LS_PROBE_CASES = ["grad2d_ls", "pin7_ls"]
+# CMFD-accelerated eigenvalue solves (Geometry::setCmfd) and the coarse
+# group structure each case set (None: one coarse group per group).
+CMFD_CASES = {"cmfd_lat3": [[1, 2, 3], [4, 5, 6, 7]], "cmfd_lat5_vac": None}
 
 
 def pytest_configure(config):

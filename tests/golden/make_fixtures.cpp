@@ -31,6 +31,7 @@
 #include <vector>
 
 #include "CPULSSolver.h"
+#include "Cmfd.h"
 #include "CPUSolver.h"
 #include "Geometry.h"
 #include "TrackGenerator.h"
@@ -450,7 +451,74 @@ struct CaseSpec {
   Cell* src_cell;          /* fixed source by cell: flat value per group */
   std::vector<double> src_cell_flat;     /* [G] */
   std::vector<double> src_cell_moments;  /* [G][3], empty: none */
+  Cmfd* cmfd;              /* attached to geo before the FSRs are made */
 };
+
+/* What the CMFD mesh of a case is laid over, in the arrays
+ * Problem.cmfd_geometry reads (prefix cm_): the reference's own FSR-to-cell
+ * map (Cmfd::convertFSRIdToCmfdCell) on its uniform mesh, the boundary face
+ * at each track end, the Larsen-EDC quadrature (Cmfd::computeLarsensEDCFactor
+ * reads getSinTheta, getAzimWeight, getPolarWeight for azim < num_azim / 2,
+ * polar < num_polar / 2), the geometry's bounds and boundary types. */
+static void write_cmfd(Writer& w, const CaseSpec& c, TrackGenerator& tg,
+                       const PackedProblem& p) {
+  Cmfd* cm = c.cmfd;
+  Geometry* geo = c.geo;
+  const int nx = cm->getNumX(), ny = cm->getNumY();
+  const double x0 = geo->getMinX(), x1 = geo->getMaxX();
+  const double y0 = geo->getMinY(), y1 = geo->getMaxY();
+  const double wx = (x1 - x0) / nx, wy = (y1 - y0) / ny;
+  std::vector<int32_t> cell(p.num_fsrs);
+  for (long r = 0; r < p.num_fsrs; r++) {
+    cell[r] = cm->convertFSRIdToCmfdCell(r);
+    /* the cell numbering (y from y-min) checked on a point of the FSR */
+    Point* pt = geo->getFSRPoint(r);
+    const int ix = (int) std::floor((pt->getX() - x0) / wx);
+    const int iy = (int) std::floor((pt->getY() - y0) / wy);
+    if (ix >= 0 && ix < nx && iy >= 0 && iy < ny && cell[r] != iy * nx + ix)
+      throw std::runtime_error("unexpected CMFD cell numbering");
+  }
+  w.arr("cm_fsr_cell", "i4", cell.data(), cell.size());
+  std::vector<double> wxs(nx, wx), wys(ny, wy);
+  w.arr("cm_widths_x", "f8", wxs.data(), wxs.size());
+  w.arr("cm_widths_y", "f8", wys.data(), wys.size());
+  Track** tracks = tg.get2DTracksArray();
+  const long T = tg.getNum2DTracks();
+  const double tol = 1e-9 * std::max(x1 - x0, y1 - y0);
+  auto face = [&](Point* q) -> int8_t {
+    if (std::fabs(q->getX() - x0) <= tol) return 0;
+    if (std::fabs(q->getX() - x1) <= tol) return 2;
+    if (std::fabs(q->getY() - y0) <= tol) return 1;
+    if (std::fabs(q->getY() - y1) <= tol) return 3;
+    return -1;
+  };
+  std::vector<int8_t> ends(2 * T);
+  for (long t = 0; t < T; t++) {
+    ends[2 * t] = face(tracks[t]->getEnd());
+    ends[2 * t + 1] = face(tracks[t]->getStart());
+  }
+  w.arr("cm_end_face", "i1", ends.data(), ends.size());
+  Quadrature* q = tg.getQuadrature();
+  std::vector<double> mu, wt;
+  for (int a = 0; a < q->getNumAzimAngles() / 2; a++)
+    for (int pp = 0; pp < q->getNumPolarAngles() / 2; pp++) {
+      const double sn = q->getSinTheta(a, pp);
+      mu.push_back(std::sqrt(1.0 - sn * sn));
+      wt.push_back(q->getAzimWeight(a) * q->getPolarWeight(a, pp));
+    }
+  w.arr("cm_edc_mu", "f8", mu.data(), mu.size());
+  w.arr("cm_edc_w", "f8", wt.data(), wt.size());
+  double bounds[4] = {x0, x1, y0, y1};
+  w.arr("cm_bounds", "f8", bounds, 4);
+  auto code = [](boundaryType b) -> int32_t {
+    return b == VACUUM ? 0 : b == REFLECTIVE ? 1 : 2;
+  };
+  int32_t bc[4] = {code(geo->getMinXBoundaryType()),
+                   code(geo->getMinYBoundaryType()),
+                   code(geo->getMaxXBoundaryType()),
+                   code(geo->getMaxYBoundaryType())};
+  w.arr("cm_bc", "i4", bc, 4);
+}
 
 static void run_case(const CaseSpec& c, const std::string& outdir) {
   c.geo->initializeFlatSourceRegions();
@@ -586,6 +654,7 @@ static void run_case(const CaseSpec& c, const std::string& outdir) {
     std::vector<float> mom = ls->moments();
     w.arr("ls_moments", "f4", mom.data(), mom.size());
   }
+  if (c.cmfd) write_cmfd(w, c, tg, p);
   if (c.probe && c.kind == EIGEN) {
 #ifdef SINGLE
     if (flat) flat->probe(w);
@@ -799,6 +868,46 @@ int main(int argc, char** argv) {
                      REF, VAC, REF, VAC), 16, 0.1, 1000, 1e-5,
                      TOTAL_SOURCE, SOURCE, 1.0, false, fuel, 1.0, 0, 0.0,
                      true, false, NULL});
+  }
+
+  /* 13-14. CMFD acceleration (tests/test_cmfd_* set Cmfd up the same way:
+   *        setLatticeStructure, setGroupStructure, relaxation factors).
+   *        A 3x3 lattice, 7 groups, reflective, centre pin water, on a 3x3
+   *        mesh with two coarse groups; a 5x5 lattice, 7 groups, vacuum on
+   *        +x and +y, on a 5x5 mesh with a coarse group per group. */
+  {
+    Material* fuel = make_material(23, "fuel7c",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 5, 7, true));
+    Material* mod = make_material(24, "mod7c",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 1005, 7, false));
+    Geometry* geo = lattice_geometry(3, fuel, mod, pin, {4}, REF, REF, REF,
+                                     REF);
+    Cmfd* cm = new Cmfd();
+    cm->setLatticeStructure(3, 3);
+    cm->setGroupStructure({{1, 2, 3}, {4, 5, 6, 7}});
+    cm->setCMFDRelaxationFactor(0.7);
+    cm->setSORRelaxationFactor(1.5);
+    geo->setCmfd(cm);
+    CaseSpec cs = {"cmfd_lat3", geo, 16, 0.1, 1000, 1e-5, FISSION_SOURCE,
+                   EIGEN, 1.0, false, NULL, 0.0};
+    cs.cmfd = cm;
+    cases.push_back(cs);
+  }
+  {
+    Material* fuel = make_material(25, "fuel7v",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 6, 7, true));
+    Material* mod = make_material(26, "mod7v",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 1006, 7, false));
+    Geometry* geo = lattice_geometry(5, fuel, mod, pin, {6, 12, 18}, REF,
+                                     VAC, REF, VAC);
+    Cmfd* cm = new Cmfd();
+    cm->setLatticeStructure(5, 5);
+    cm->setSORRelaxationFactor(1.5);
+    geo->setCmfd(cm);
+    CaseSpec cs = {"cmfd_lat5_vac", geo, 16, 0.1, 1000, 1e-5, FISSION_SOURCE,
+                   EIGEN, 1.0, false, NULL, 0.0};
+    cs.cmfd = cm;
+    cases.push_back(cs);
   }
 
   for (const CaseSpec& c : cases) {

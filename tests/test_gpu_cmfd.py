@@ -1,0 +1,157 @@
+"""CMFD-accelerated eigenvalue solves on the GPU (GB300Solver.setCmfd)
+against OpenMOC's own CMFD-accelerated CPUSolver runs, and against the
+unaccelerated GPU solve.
+
+  * the reference fixtures (a reflective 3 x 3 lattice on a 3 x 3 mesh with
+    two coarse groups, a 5 x 5 lattice with vacuum on two sides on a 5 x 5
+    mesh): iterations within one, keff within 1e-5, fluxes within 1e-4;
+  * a generated 17 x 17 assembly: CMFD converges to the unaccelerated
+    answer in fewer iterations, with a pin-cell mesh and a coarser one;
+  * rejected requests.
+"""
+import numpy as np
+import pytest
+
+from conftest import CMFD_CASES, load_case
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(got, ref, floor):
+    got, ref = np.asarray(got, np.float64), np.asarray(ref, np.float64)
+    return float(np.max(np.abs(got - ref) /
+                        np.maximum(np.abs(ref), floor * np.abs(ref).max())))
+
+
+def _cmfd(p, groups):
+    from openmoc_gb300 import Cmfd
+    c = Cmfd()
+    nx = p.cmfd_geometry["widths_x"].size
+    ny = p.cmfd_geometry["widths_y"].size
+    c.setLatticeStructure(nx, ny)
+    if groups is not None:
+        c.setGroupStructure(groups)
+    c.setSORRelaxationFactor(1.5)
+    c.setCMFDRelaxationFactor(0.7)
+    return c
+
+
+@pytest.mark.parametrize("case", sorted(CMFD_CASES))
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+def test_gpu_cmfd_matches_openmoc(case, precision):
+    from openmoc_gb300 import GB300Solver
+    p, sc, arr = load_case(case, precision)
+    s = GB300Solver(device=0)
+    s.setConvergenceThreshold(sc["tolerance"])
+    s.setTrackGenerator(p)
+    s.setCmfd(_cmfd(p, CMFD_CASES[case]))
+    s.computeEigenvalue(int(sc["max_iters"]), int(sc["res_type"]))
+    info = s.getCmfdInfo()
+    assert info["enabled"] and info["power_iterations"] > 25
+    assert abs(s.getNumIterations() - int(sc["iterations"])) <= 1
+    assert abs(s.getKeff() - sc["keff"]) < 1e-5
+    assert _rel(s.getFluxes(), arr["flux"].reshape(p.num_fsrs, -1), 1e-4) < 1e-4
+    s.close()
+
+
+def _assembly(G=7):
+    from openmoc_gb300 import lattice as lat
+    return lat.assembly_17x17(num_groups=G, num_azim=16, spacing=0.1)
+
+
+@pytest.mark.parametrize("mesh", [17, 1])
+def test_gpu_cmfd_converges_to_unaccelerated_answer(mesh):
+    """A 17 x 17 assembly with vacuum on two sides: the CMFD solve (pin-cell
+    mesh, or one coarse cell per 17 x 17 block = no spatial coupling)
+    reaches the unaccelerated solution; the pin-cell mesh in far fewer
+    iterations."""
+    from openmoc_gb300 import Cmfd, GB300Solver
+    from openmoc_gb300 import lattice as lat
+    from openmoc_gb300.lattice import REFLECTIVE, VACUUM
+    mats = lat._fuel_mod(1, 7, 1)
+    pm = np.zeros((17, 17), np.int32)
+    for (r, c) in lat.GUIDE_TUBES_17x17:
+        pm[r, c] = 1
+    p = lat.lattice(17, 17, pm, mats, 1, num_azim=16, spacing=0.1,
+                    bc=(REFLECTIVE, VACUUM, REFLECTIVE, VACUUM))
+    tol = 1e-7
+    ref = GB300Solver(p, device=0)
+    ref.setConvergenceThreshold(tol)
+    ref.computeEigenvalue(3000, 1)
+    n_plain = ref.getNumIterations()
+    s = GB300Solver(device=0)
+    s.setConvergenceThreshold(tol)
+    s.setTrackGenerator(p)
+    c = Cmfd()
+    c.setLatticeStructure(mesh, mesh)
+    c.setGroupStructure([[1, 2, 3], [4, 5, 6, 7]])
+    s.setCmfd(c)
+    s.computeEigenvalue(3000, 1)
+    n_cmfd = s.getNumIterations()
+    assert abs(s.getKeff() - ref.getKeff()) < 2e-6
+    assert _rel(s.getFluxes(), ref.getFluxes(), 1e-3) < 1e-4
+    if mesh == 17:
+        assert n_cmfd < 0.5 * n_plain, (n_cmfd, n_plain)
+    old, new = s.getCmfdFluxes()
+    assert old.shape == (mesh * mesh, 2) and np.isfinite(new).all()
+    ref.close()
+    s.close()
+
+
+def test_gpu_cmfd_detach_restores_plain_solve():
+    from openmoc_gb300 import Cmfd, GB300Solver
+    from openmoc_gb300 import lattice as lat
+    p = lat.square_lattice(3, 7, 16, 0.1, 0, water_pins=[(1, 1)])
+    a = GB300Solver(p, device=0)
+    a.computeEigenvalue(1000, 1)
+    b = GB300Solver(p, device=0)
+    c = Cmfd()
+    c.setLatticeStructure(3, 3)
+    b.setCmfd(c)
+    b.computeEigenvalue(1000, 1)
+    assert b.getNumIterations() < a.getNumIterations()
+    b.setCmfd(None)
+    b.computeEigenvalue(1000, 1)
+    assert b.getNumIterations() == a.getNumIterations()
+    assert not b.getCmfdInfo()["enabled"]
+    a.close()
+    b.close()
+
+
+def test_gpu_cmfd_bad_requests_raise():
+    from openmoc_gb300 import Cmfd, GB300LSSolver, GB300Solver
+    from openmoc_gb300 import lattice as lat
+    from openmoc_gb300._native import MOCError
+    p = lat.square_lattice(3, 7, 16, 0.1, 0)
+    s = GB300Solver(p, device=0)
+    c = Cmfd()
+    c.setLatticeStructure(2, 2)          # mesh lines cut the pins
+    with pytest.raises(MOCError):
+        s.setCmfd(c)
+    c = Cmfd()
+    c.setLatticeStructure(3, 3)
+    c.setGroupStructure([[1, 2], [3]])   # does not cover 7 groups
+    with pytest.raises(MOCError):
+        s.setCmfd(c)
+    s.close()
+    pl = lat.pin_cell(7, linear_source=True)
+    ls = GB300LSSolver(pl, device=0)
+    c = Cmfd()
+    c.setLatticeStructure(1, 1)
+    with pytest.raises(MOCError):
+        ls.setCmfd(c)
+    ls.close()
+
+
+def test_gpu_cmfd_uses_native_library():
+    from openmoc_gb300 import Cmfd, GB300Solver
+    from openmoc_gb300 import lattice as lat
+    p = lat.square_lattice(3, 7, 16, 0.1, 0)
+    s = GB300Solver(p, device=0)
+    c = Cmfd()
+    c.setLatticeStructure(3, 3)
+    s.setCmfd(c)
+    n0 = s.getLaunchCount()
+    s.computeEigenvalue(3, 1)
+    assert s.getLaunchCount() >= n0 + 3 * 6
+    s.close()
