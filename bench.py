@@ -369,6 +369,8 @@ def run_gpu(args):
             out["batched_instances"] = run_instances(p, args)
         if world == 1 and args.workload == "assembly70" and not args.no_raytrace:
             out["ray_tracing"] = ray_tracing(local)
+        if world == 1 and args.workload == "assembly70" and not args.no_cmfd:
+            out["cmfd"] = cmfd_acceleration(p, local)
         if world == 1 and not args.no_serving and args.workload == "assembly70":
             # the second half of the headline: the request stream through the
             # batched server against the plain per-solve loop
@@ -380,6 +382,41 @@ def run_gpu(args):
     s.close()
     if dist:
         dist.destroy_process_group()
+
+
+def cmfd_acceleration(p, device, tol=1e-5):
+    """Time to solution of the headline problem, computeEigenvalue to a
+    1e-5 fission-source residual, without and with CMFD (pin-cell mesh,
+    the 70 groups condensed to 8 coarse groups of 9 or 8): iterations, wall
+    seconds, and the per-iteration cost of the coarse solve and its
+    host round trip."""
+    from openmoc_gb300 import Cmfd, GB300Solver
+    G = p.num_groups
+    bands = np.array_split(np.arange(1, G + 1), 8)
+    res = {"workload": f"{p.meta.get('nx', 17)}x{p.meta.get('ny', 17)} pins, {G} "
+                       f"groups; CMFD on the pin mesh with {len(bands)} coarse groups",
+           "tolerance": tol}
+    for name, use in (("plain", False), ("cmfd", True)):
+        s = GB300Solver(p, device=device)
+        s.setConvergenceThreshold(tol)
+        if use:
+            c = Cmfd()
+            c.setLatticeStructure(int(p.meta.get("nx", 17)), int(p.meta.get("ny", 17)))
+            c.setGroupStructure([b.tolist() for b in bands])
+            s.setCmfd(c)
+        s.computeEigenvalue(5, 1)                 # tuning and module load
+        t0 = time.perf_counter()
+        s.computeEigenvalue(5000, 1)
+        dt = time.perf_counter() - t0
+        res[name] = {"iterations": s.getNumIterations(), "seconds": dt,
+                     "ms_per_iteration": 1e3 * dt / max(1, s.getNumIterations()),
+                     "keff": s.getKeff()}
+        if use:
+            res[name]["coarse_power_iterations_last"] = s.getCmfdInfo()["power_iterations"]
+        s.close()
+    res["speedup"] = res["plain"]["seconds"] / res["cmfd"]["seconds"]
+    res["keff_difference"] = res["cmfd"]["keff"] - res["plain"]["keff"]
+    return res
 
 
 def ray_tracing(device):
@@ -722,6 +759,8 @@ def main():
                     help="L2 budget of the live solves' sources and tallies")
     ap.add_argument("--no-raytrace", action="store_true",
                     help="skip the track-generation timing (host vs device ray tracing)")
+    ap.add_argument("--no-cmfd", action="store_true",
+                    help="leave the CMFD time-to-solution comparison out")
     ap.add_argument("--no-serving", action="store_true",
                     help="leave the request-stream benchmark out of the default line")
     args = ap.parse_args()

@@ -265,7 +265,64 @@ static void transfer(const oracle_problem* p, oracle_state* s, long t, int fwd,
  * zero the scalar flux, copy the start fluxes into the boundary fluxes, then
  * sweep every track forward and backward, tallying FSR contributions in a
  * buffer that is flushed whenever the FSR changes. */
-void oracle_sweep(const oracle_problem* p, oracle_state* s) {
+/* CMFD partial currents (Cmfd::tallyCurrent, src/Cmfd.h:572-660): where a
+ * track leaves a coarse cell, sum_p w_p psi_p of the outgoing angular flux
+ * is added to [cell][face][group] (faces 0 x-min, 1 y-min, 2 x-max,
+ * 3 y-max); a crossing through a corner goes half by way of each
+ * neighbouring cell (Cmfd::splitEdgeCurrents, src/Cmfd.cpp:2249-2345).
+ * Track ends on the boundary add to the face given in end_face. */
+typedef struct {
+  const int* cell;              /* [R] coarse cell of every FSR */
+  const signed char* end_face;  /* [T][2] */
+  int nx;
+  double* cur;                  /* [cells][4][G] */
+} oracle_cmfd_tally;
+
+static void add_current(const oracle_problem* p, const oracle_cmfd_tally* cm,
+                        int cell, int face, double frac, int ang,
+                        const float* psi) {
+  const int G = p->num_groups, Ph = p->num_polar_half;
+  double* dst = cm->cur + ((long) cell * 4 + face) * G;
+  for (int g = 0; g < G; g++) {
+    double j = 0.0;
+    for (int pp = 0; pp < Ph; pp++)
+      j += (double) p->weights[ang * Ph + pp] * (double) psi[pp * G + g];
+#pragma omp atomic
+    dst[g] += frac * j;
+  }
+}
+
+static void tally_crossing(const oracle_problem* p,
+                           const oracle_cmfd_tally* cm, long fsr,
+                           long fsr_next, int end_face, int ang,
+                           const float* psi) {
+  const int c0 = cm->cell[fsr];
+  if (fsr_next < 0) {
+    if (end_face >= 0) add_current(p, cm, c0, end_face, 1.0, ang, psi);
+    return;
+  }
+  const int c1 = cm->cell[fsr_next];
+  if (c1 == c0) return;
+  const int dx = c1 % cm->nx - c0 % cm->nx, dy = c1 / cm->nx - c0 / cm->nx;
+  const int fx = dx > 0 ? 2 : 0, fy = dy > 0 ? 3 : 1;
+  if (dx != 0 && dy != 0) {
+    add_current(p, cm, c0, fx, 0.5, ang, psi);
+    add_current(p, cm, c0 + dx, fy, 0.5, ang, psi);
+    add_current(p, cm, c0, fy, 0.5, ang, psi);
+    add_current(p, cm, c0 + dy * cm->nx, fx, 0.5, ang, psi);
+  } else {
+    add_current(p, cm, c0, dx != 0 ? fx : fy, 1.0, ang, psi);
+  }
+}
+
+/* CPUSolver::transportSweep + TransportSweep::onTrack
+ * (src/CPUSolver.cpp:2338-2398, src/TrackTraversingAlgorithms.cpp:890-1052):
+ * zero the scalar flux, copy the start fluxes into the boundary fluxes, then
+ * sweep every track forward and backward, tallying FSR contributions in a
+ * buffer that is flushed whenever the FSR changes; with cm, also the CMFD
+ * partial currents (2D). */
+static void sweep_impl(const oracle_problem* p, oracle_state* s,
+                       const oracle_cmfd_tally* cm) {
   const long R = p->num_fsrs;
   const int G = p->num_groups;
   const long T = p->num_tracks;
@@ -293,6 +350,9 @@ void oracle_sweep(const oracle_problem* p, oracle_state* s) {
         long fsr = p->seg_fsr[b + k];
         tally_segment(p, s, fsr, (real) p->seg_len[b + k],
                       p->fsr_mat[fsr], ang, buf, psi);
+        if (cm)
+          tally_crossing(p, cm, fsr, k < n - 1 ? p->seg_fsr[b + k + 1] : -1,
+                         cm->end_face[2 * t], ang, psi);
         if (k < n - 1 && fsr != p->seg_fsr[b + k + 1])
           flush(p, s, fsr, weight, buf, locks);
       }
@@ -302,6 +362,9 @@ void oracle_sweep(const oracle_problem* p, oracle_state* s) {
         long fsr = p->seg_fsr[b + k];
         tally_segment(p, s, fsr, (real) p->seg_len[b + k],
                       p->fsr_mat[fsr], ang, buf, psi);
+        if (cm)
+          tally_crossing(p, cm, fsr, k > 0 ? p->seg_fsr[b + k - 1] : -1,
+                         cm->end_face[2 * t + 1], ang, psi);
         if (k == 0 || fsr != p->seg_fsr[b + k - 1])
           flush(p, s, fsr, weight, buf, locks);
       }
@@ -313,6 +376,19 @@ void oracle_sweep(const oracle_problem* p, oracle_state* s) {
   for (long r = 0; r < R; r++) omp_destroy_lock(&lk[r]);
   free(lk);
 #endif
+}
+
+void oracle_sweep(const oracle_problem* p, oracle_state* s) {
+  sweep_impl(p, s, NULL);
+}
+
+/* The sweep with the CMFD current tallies added into cur [cells][4][G]
+ * (zeroed by the caller). */
+void oracle_sweep_currents(const oracle_problem* p, oracle_state* s,
+                           const int* cell, const signed char* end_face,
+                           int nx, double* cur) {
+  oracle_cmfd_tally cm = {cell, end_face, nx, cur};
+  sweep_impl(p, s, &cm);
 }
 
 /* CPUSolver::addSourceToScalarFlux, src/CPUSolver.cpp:2608-2660 */

@@ -82,6 +82,8 @@ def _lib(precision: str):
         lib.oracle_compute_sources.argtypes = [P, S, C.c_int, C.c_int]
         lib.oracle_compute_sources.restype = C.c_long
         lib.oracle_sweep.argtypes = [P, S]
+        lib.oracle_sweep_currents.argtypes = [P, S, C.c_void_p, C.c_void_p, C.c_int,
+                                              C.c_void_p]
         lib.oracle_add_source.argtypes = [P, S, C.c_int]
         lib.oracle_add_source.restype = C.c_long
         lib.oracle_compute_keff.argtypes = [P, S]
@@ -188,6 +190,21 @@ class Oracle:
 
     def sweep(self) -> None:
         self.lib.oracle_sweep(C.byref(self._cp), C.byref(self._cs))
+
+    def sweep_currents(self, cell: np.ndarray, end_face: np.ndarray, nx: int,
+                       cur: np.ndarray) -> None:
+        """The sweep with CMFD partial currents added into cur [cells][4][G]
+        (FP64)."""
+        assert cell.dtype == np.int32 and end_face.dtype == np.int8
+        assert cur.dtype == np.float64 and cur.flags.c_contiguous
+        self.lib.oracle_sweep_currents(C.byref(self._cp), C.byref(self._cs),
+                                       _ptr(cell), _ptr(end_face), nx, _ptr(cur))
+
+    def flatten(self, value: float = 1.0) -> None:
+        self.lib.oracle_flatten(C.byref(self._cp), C.byref(self._cs), value)
+
+    def zero_track_fluxes(self) -> None:
+        self.lib.oracle_zero_track_fluxes(C.byref(self._cp), C.byref(self._cs))
 
     def add_source(self) -> int:
         return self.lib.oracle_add_source(C.byref(self._cp), C.byref(self._cs), 0)

@@ -155,3 +155,46 @@ def test_gpu_cmfd_uses_native_library():
     s.computeEigenvalue(3, 1)
     assert s.getLaunchCount() >= n0 + 3 * 6
     s.close()
+
+
+def test_gpu_cmfd_matches_oracle_step_by_step():
+    """A generated 5 x 5 lattice (vacuum on +x and +y, water pins) on a pin
+    mesh with two coarse groups, a fixed number of iterations: keff, fluxes
+    and the coarse fluxes of the last coarse solve against the FP64 oracle
+    CMFD (oracle/cmfd_oracle.py)."""
+    from openmoc_gb300 import Cmfd, GB300Solver
+    from openmoc_gb300 import lattice as lat
+    from openmoc_gb300.lattice import REFLECTIVE, VACUUM
+    from oracle.cmfd_oracle import CmfdOracle, cmfd_eigenvalue
+    from oracle.oracle import Oracle
+    mats = lat._fuel_mod(2, 7, 1)
+    pm = np.zeros((5, 5), np.int32)
+    for (r, c) in [(1, 1), (2, 3), (3, 2)]:
+        pm[r, c] = 1
+    p = lat.lattice(5, 5, pm, mats, 1, num_azim=16, spacing=0.1,
+                    bc=(REFLECTIVE, VACUUM, REFLECTIVE, VACUUM))
+    groups = [[1, 2, 3], [4, 5, 6, 7]]
+    c = Cmfd()
+    c.setLatticeStructure(5, 5)
+    c.setGroupStructure(groups)
+    mesh, keep = c.mesh(p)
+    g = p.cmfd_geometry
+    cm = CmfdOracle(p, 5, 5, keep[0], keep[1], keep[2], g["end_face"], g["bc"],
+                    keep[4], g["edc_mu"], g["edc_w"])
+    o = Oracle(p, "f64", num_threads=8)
+    iters = 8
+    cmfd_eigenvalue(o, cm, iters, 1, 1e-30)
+    s = GB300Solver(device=0)
+    s.setConvergenceThreshold(1e-30)
+    s.setTrackGenerator(p)
+    s.setCmfd(c)
+    s.computeEigenvalue(iters, 1)
+    assert s.getNumIterations() == iters
+    assert abs(s.getKeff() - o.keff) < 2e-6
+    R = p.num_fsrs
+    assert _rel(s.getFluxes(), o.phi.reshape(R, -1), 1e-4) < 2e-5
+    old, new = s.getCmfdFluxes()
+    assert np.max(np.abs(new - cm.new_flux)) < 1e-4 * np.abs(cm.new_flux).max()
+    assert np.max(np.abs(old - cm.old_flux)) < 1e-4 * np.abs(cm.old_flux).max()
+    assert abs(s.getCmfdInfo()["keff"] - cm.keff) < 2e-6
+    s.close()
