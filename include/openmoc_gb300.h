@@ -378,6 +378,11 @@ typedef struct {
   double sor_factor;           /* setSORRelaxationFactor (reference 1.5) */
   int32_t flux_limiting;       /* useFluxLimiting (reference 1) */
   int32_t num_unbounded_iterations; /* setNumUnboundedIterations (0) */
+  int32_t solve_on_host;       /* 0: the coarse solve runs on the GPU in
+                                  FP32 (as the reference's single-precision
+                                  build), with no host round trip; 1: on the
+                                  host in FP64, tallies read back every
+                                  iteration */
 } moc_cmfd_mesh;
 
 /** Attaches CMFD to the context (tracks, quadrature, materials and FSRs

@@ -66,7 +66,8 @@ class CmfdMesh(C.Structure):
                 ("edc_mu", C.c_void_p), ("edc_weight", C.c_void_p),
                 ("relaxation", C.c_double), ("sor_factor", C.c_double),
                 ("flux_limiting", C.c_int32),
-                ("num_unbounded_iterations", C.c_int32)]
+                ("num_unbounded_iterations", C.c_int32),
+                ("solve_on_host", C.c_int32)]
 
 
 _P = C.c_void_p

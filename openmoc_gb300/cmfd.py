@@ -36,6 +36,7 @@ class Cmfd:
         self._flux_limiting = True      # src/Cmfd.cpp:39
         self._unbounded = 0             # src/Cmfd.cpp:35
         self._edc = True
+        self._host = False
         self._fsr_cell: Optional[np.ndarray] = None
 
     # ------------------------------------------------------------ settings
@@ -106,6 +107,12 @@ class Cmfd:
         the reference's flat-source CMFD)."""
         self._edc = bool(on)
 
+    def useHostSolver(self, on: bool) -> None:
+        """Solve the coarse problem on the host in FP64 (the tallies go to
+        the host and the ratios back every iteration) instead of on the GPU
+        in FP32 (the default: one block, no host round trip)."""
+        self._host = bool(on)
+
     def setKNearest(self, k: int) -> None:
         """Cmfd::setKNearest (src/Cmfd.cpp:3417): k = 1 is the plain
         cell-average update; the centroid-weighted update is not built."""
@@ -175,7 +182,8 @@ class Cmfd:
                              (_native.C.c_int32 * 4)(*[int(b) for b in bc]),
                              E, ptr(group_of), int(mu.size), ptr(mu), ptr(w),
                              self._relaxation, self._sor,
-                             1 if self._flux_limiting else 0, self._unbounded)
+                             1 if self._flux_limiting else 0, self._unbounded,
+                             1 if self._host else 0)
         return m, keep
 
 

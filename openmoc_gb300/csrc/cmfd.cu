@@ -1,8 +1,18 @@
 // Device side of the CMFD accelerator: the flux reduction onto the coarse
-// mesh and the prolongation of the coarse solution back onto the FSRs.  The
-// partial currents are tallied by the sweep itself (sweep_kernel.cuh, mode
-// 2); the coarse solve runs on the host (cmfd_solve.cpp).
+// mesh, the coarse solve, and the prolongation of the coarse solution back
+// onto the FSRs.  The partial currents are tallied by the sweep itself
+// (sweep_kernel.cuh, mode 2).  cmfd_solve.cpp holds the same coarse solve on
+// the host in FP64.
+//
+// The coarse solve runs in one block: the coarse problem (a few thousand
+// unknowns) is far too small to fill the GPU, and the power iteration's
+// hundreds of red-black SOR sweeps are latency-bound, so they run between
+// __syncthreads barriers of a single block, with the operands in L1, instead
+// of as hundreds of dependent launches or host round trips.  Arithmetic is
+// FP32 with FP64 sums, as in the reference's single-precision build
+// (CMFD_PRECISION float, LINALG_TOL 1e-7).
 #include <algorithm>
+#include <cfloat>
 
 #include "moc_internal.cuh"
 
@@ -11,6 +21,16 @@ namespace moc {
 namespace {
 
 constexpr int kPairThreads = 256;
+constexpr int kSolveThreads = 1024;
+constexpr float kZeroSigmaT = 1e-6f;          // src/constants.h:34
+constexpr double kFluxEps = 1e-25;            // src/constants.h:15
+constexpr double kLinalgTol = 1e-7;           // LINALG_TOL, FP32 build
+constexpr int kMinIters = 25;                 // src/constants.h:74-81
+constexpr int kMaxPowerIters = 25000;
+constexpr int kMaxLinearIters = 10000;
+// Bound on the SOR sweeps of one coarse solve (about 0.1 s): past it the
+// solve counts as failed and the MOC iteration goes on without prolongation.
+constexpr int kMaxSweeps = 200000;
 
 // One warp per (coarse cell, material) pair: S[p][g] = sum over the pair's
 // FSRs of phi[r][g] * V[r] in FP64, lanes over groups, FSRs from the CSR
@@ -21,7 +41,8 @@ cmfd_pair_sums_kernel(const float* __restrict__ phi,
                       const float* __restrict__ vol,
                       const int32_t* __restrict__ pair_off,
                       const int32_t* __restrict__ pair_fsr, int P, int G,
-                      int ld, double* __restrict__ out) {
+                      int ld, double* __restrict__ out, const DevScalars* sc) {
+  if (*(volatile const int*) &sc->done) return;
   const int lane = threadIdx.x & 31;
   const int warps = (gridDim.x * blockDim.x) >> 5;
   for (int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < P;
@@ -41,23 +62,436 @@ cmfd_pair_sums_kernel(const float* __restrict__ phi,
 }
 
 // phi[r][g] *= ratio[cell(r)][coarse group(g)] (Cmfd::updateMOCFlux,
-// src/Cmfd.cpp:1509-1560); the first thread also installs the coarse
-// eigenvalue as the solver's keff (Solver::computeEigenvalue takes
-// Cmfd::computeKeff's result, src/Solver.cpp:1600-1604).
+// src/Cmfd.cpp:1509-1560).
 __global__ void cmfd_prolong_kernel(float* __restrict__ phi,
                                     const int32_t* __restrict__ fsr_cell,
                                     const int32_t* __restrict__ group_of,
-                                    const double* __restrict__ ratio,
+                                    const float* __restrict__ ratio,
                                     int64_t R, int G, int ld, int E,
-                                    DevScalars* sc, double keff) {
+                                    const DevScalars* sc) {
+  if (*(volatile const int*) &sc->done) return;
   const int64_t n = R * ld;
-  const int64_t i0 = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
-  if (i0 == 0) sc->keff = keff;
-  for (int64_t i = i0; i < n; i += (int64_t) gridDim.x * blockDim.x) {
+  for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t) gridDim.x * blockDim.x) {
     const int64_t r = i / ld;
     const int g = (int) (i - r * ld);
     if (g >= G) continue;
-    phi[i] *= (float) ratio[(int64_t) fsr_cell[r] * E + group_of[g]];
+    phi[i] *= ratio[(int64_t) fsr_cell[r] * E + group_of[g]];
+  }
+}
+
+// ------------------------------------------------------------ coarse solve
+// Sum of v over the block, returned to every thread.
+__device__ double block_sum(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __syncthreads();   // earlier readers of red are done
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  double t = 0.0;
+  const int nw = (blockDim.x + 31) >> 5;
+  for (int i = 0; i < nw; i++) t += red[i];
+  return t;
+}
+
+struct Work {
+  float *sig_t, *nu_f, *chi, *dif, *dlx, *dly, *phi_c;   // [C][E]
+  float *sig_s;                                           // [C][E][E] e -> g
+  float *J;                                               // [C][4][E]
+  float *A, *nb, *M;                                      // [C][E][E], [C][4][E]
+  float *x, *src_a, *src_b, *ls_a, *ls_b;                 // [C][E]
+};
+
+__device__ Work carve(float* w, int C, int E) {
+  const int64_t CE = (int64_t) C * E, CEE = CE * E, C4E = 4 * CE;
+  Work k;
+  k.sig_t = w; w += CE;
+  k.nu_f = w; w += CE;
+  k.chi = w; w += CE;
+  k.dif = w; w += CE;
+  k.dlx = w; w += CE;
+  k.dly = w; w += CE;
+  k.phi_c = w; w += CE;
+  k.sig_s = w; w += CEE;
+  k.J = w; w += C4E;
+  k.A = w; w += CEE;
+  k.nb = w; w += C4E;
+  k.M = w; w += CEE;
+  k.x = w; w += CE;
+  k.src_a = w; w += CE;
+  k.src_b = w; w += CE;
+  k.ls_a = w; w += CE;
+  k.ls_b = w;
+  return k;
+}
+
+__device__ __forceinline__ int neighbour(const CmfdArgs& a, int c, int f) {
+  const int ix = c % a.nx, iy = c / a.nx;
+  switch (f) {
+    case 0: return ix > 0 ? c - 1 : -1;
+    case 1: return iy > 0 ? c - a.nx : -1;
+    case 2: return ix + 1 < a.nx ? c + 1 : -1;
+    default: return iy + 1 < a.ny ? c + a.nx : -1;
+  }
+}
+
+// Larsen's effective diffusion coefficient factor
+// (Cmfd::computeLarsensEDCFactor, src/Cmfd.cpp:1625-1650).
+__device__ float larsen(const CmfdArgs& a, float d, float delta) {
+  double rho = 0.0;
+  for (int i = 0; i < a.n_edc; i++) {
+    const float mu = a.edc_mu[i];
+    const float e = expf(-delta / (3.0f * d * mu));
+    const float alpha = (1.0f + e) / (1.0f - e) - 2.0f * (3.0f * d * mu) / delta;
+    rho += 2.0 * mu * a.edc_w[i] * alpha;
+  }
+  return (float) (1.0 + delta * rho / (2.0 * d));
+}
+
+// out = M x, rows over the block (no barrier)
+__device__ void mat_fission(const CmfdArgs& a, const Work& k, const float* x,
+                            float* out) {
+  const int E = a.E, CE = a.C * a.E;
+  for (int r = threadIdx.x; r < CE; r += blockDim.x) {
+    const int c = r / E;
+    const float* m = k.M + (int64_t) r * E;
+    const float* xc = x + (int64_t) c * E;
+    float s = 0.0f;
+    for (int g = 0; g < E; g++) s += m[g] * xc[g];
+    out[r] = s;
+  }
+}
+
+__device__ double block_total(const float* v, int n, double* red) {
+  double t = 0.0;
+  for (int r = threadIdx.x; r < n; r += blockDim.x) t += v[r];
+  return block_sum(t, red);
+}
+
+// computeRMSE(integrated) (src/linalg.cpp:595-680)
+__device__ double rmse(const CmfdArgs& a, const float* x, const float* y,
+                       double* red) {
+  double part = 0.0;
+  for (int c = threadIdx.x; c < a.C; c += blockDim.x) {
+    double s = 0.0, t = 0.0;
+    for (int e = 0; e < a.E; e++) {
+      s += x[c * a.E + e];
+      t += y[c * a.E + e];
+    }
+    if (fabs(t) > kFluxEps) {
+      const float r = (float) ((s - t) / t);
+      part += (double) (r * r);
+    }
+  }
+  const double tot = block_sum(part, red);
+  return sqrt(tot / (double) max(a.C, 1));
+}
+
+// Cmfd::collapseXS (src/Cmfd.cpp:720-1000) for cell c, coarse group e, and
+// the coarse currents and Larsen-corrected diffusion coefficients.
+__device__ void collapse_one(const CmfdArgs& a, const Work& k, int c, int e) {
+  const int E = a.E, G = a.G;
+  const int ce = c * E + e;
+  const int p0 = a.cell_pair[c], p1 = a.cell_pair[c + 1];
+  double prod_tot = 0.0, chi_t = 0.0;
+  for (int p = p0; p < p1; p++) {
+    const int m = a.pair_mat[p];
+    const double* s = a.S + (int64_t) p * G;
+    double prod = 0.0;
+    for (int h = 0; h < G; h++) prod += (double) a.nf[m * G + h] * s[h];
+    chi_t += (double) a.chi_m[m * E + e] * prod;
+    prod_tot += prod;
+  }
+  float* ss_row = k.sig_s + (int64_t) ce * E;
+  for (int g = 0; g < E; g++) ss_row[g] = 0.0f;
+  double total = 0.0, nuf = 0.0, rxn = 0.0, dsum = 0.0;
+  for (int h = a.gstart[e]; h < a.gstart[e + 1]; h++) {
+    double r = 0.0, t = 0.0;
+    for (int p = p0; p < p1; p++) {
+      const int m = a.pair_mat[p];
+      const double s = a.S[(int64_t) p * G + h];
+      r += s;
+      t += (double) a.st[m * G + h] * s;
+      nuf += (double) a.nf[m * G + h] * s;
+      const float* sr = a.ss_m + ((int64_t) m * G + h) * E;
+      for (int g = 0; g < E; g++) ss_row[g] += (float) ((double) sr[g] * s);
+    }
+    total += t;
+    rxn += r;
+    if (fabs(t) > fabs(r) * (double) FLT_EPSILON) dsum += r / (3.0 * (t / r));
+  }
+  if (rxn <= 0.0) {
+    rxn = kZeroSigmaT;
+    dsum = kZeroSigmaT;
+    total = kZeroSigmaT;
+    if (nuf != 0.0) nuf = kZeroSigmaT;
+    for (int g = 0; g < E; g++) ss_row[g] = 0.0f;
+  }
+  k.sig_t[ce] = (float) (total / rxn);
+  k.nu_f[ce] = (float) (nuf / rxn);
+  k.dif[ce] = (float) (dsum / rxn);
+  k.chi[ce] = fabs(prod_tot) > 0.0 ? (float) (chi_t / prod_tot) : 0.0f;
+  k.phi_c[ce] = (float) (rxn / (double) a.cell_vol[c]);
+  for (int g = 0; g < E; g++) ss_row[g] = (float) ((double) ss_row[g] / rxn);
+  for (int f = 0; f < 4; f++) {
+    const float* src = a.cur + ((int64_t) c * 4 + f) * a.ld;
+    double j = 0.0;
+    for (int h = a.gstart[e]; h < a.gstart[e + 1]; h++) j += src[h];
+    k.J[((int64_t) c * 4 + f) * E + e] = (float) j;
+  }
+  const float d = k.dif[ce];
+  k.dlx[ce] = a.n_edc ? d * larsen(a, d, a.wx[c % a.nx]) : d;
+  k.dly[ce] = a.n_edc ? d * larsen(a, d, a.wy[c / a.nx]) : d;
+}
+
+// Cmfd::getSurfaceDiffusionCoefficient and Cmfd::constructMatrices
+// (src/Cmfd.cpp:1048-1170, 1353-1500): row (c, e) of A and M.
+__device__ void build_row(const CmfdArgs& a, const Work& k, int c, int e,
+                          int it, bool valid) {
+  const int E = a.E;
+  const int ce = c * E + e;
+  const int ix = c % a.nx, iy = c / a.nx;
+  const float V = a.cell_vol[c];
+  float* row = k.A + (int64_t) ce * E;
+  for (int g = 0; g < E; g++) {
+    const float v = -k.sig_s[((int64_t) c * E + g) * E + e] * V;
+    row[g] = fabsf(v) > FLT_EPSILON ? v : 0.0f;
+  }
+  float diag = row[e] + k.sig_t[ce] * V;
+  const float flux = k.phi_c[ce];
+  for (int f = 0; f < 4; f++) {
+    const bool xf = (f == 0 || f == 2);
+    const float width = xf ? a.wy[iy] : a.wx[ix];
+    const float delta = xf ? a.wx[ix] : a.wy[iy];
+    const float d = xf ? k.dlx[ce] : k.dly[ce];
+    const int n = neighbour(a, c, f);
+    const float j_out = k.J[((int64_t) c * 4 + f) * E + e];
+    float dh = 0.0f, dt = 0.0f;
+    if (n < 0) {
+      if (a.bc[f] == 0) {
+        const float cur_out = j_out / width;
+        dh = 2.0f * d / delta / (1.0f + 4.0f * d / delta);
+        dt = (dh * flux - cur_out) / flux;
+      }
+    } else {
+      const int ne = n * E + e;
+      const float delta_n = xf ? a.wx[n % a.nx] : a.wy[n / a.nx];
+      const float dn = xf ? k.dlx[ne] : k.dly[ne];
+      const float flux_n = k.phi_c[ne];
+      const float j_in = k.J[((int64_t) n * 4 + (f ^ 2)) * E + e];
+      dh = 2.0f * d * dn / (delta_n * d + delta * dn);
+      const float current = (j_out - j_in) / width;
+      dt = -(dh * (flux_n - flux) + current) / (flux_n + flux);
+      if (a.flux_limiting && it > 0 && fabsf(dt / dh) > 1.0f) {
+        dh = current > 0.0f ? fabsf(current / (2.0f * flux))
+                            : fabsf(current / (2.0f * flux_n));
+        dt = -(dh * (flux_n - flux) + current) / (flux_n + flux);
+        dh = fmaxf(dh, fabsf(dt));
+      }
+    }
+    float* old = a.dcorr_old + ((int64_t) c * 4 + f) * E + e;
+    if (valid) dt = a.relax * dt + (1.0f - a.relax) * *old;
+    if (it == 0) dt = 0.0f;
+    *old = dt;
+    diag += (dh - dt) * width;
+    k.nb[((int64_t) c * 4 + f) * E + e] = n >= 0 ? -(dh + dt) * width : 0.0f;
+  }
+  row[e] = diag;
+  float* mrow = k.M + (int64_t) ce * E;
+  for (int g = 0; g < E; g++) {
+    const float v = k.chi[ce] * k.nu_f[c * E + g] * V;
+    mrow[g] = fabsf(v) > FLT_EPSILON ? v : 0.0f;
+  }
+  k.x[ce] = flux;                  // the collapsed flux starts the solve
+}
+
+// One red-black half sweep of SOR over the cells of `color`.
+__device__ void sor_half(const CmfdArgs& a, const Work& k, const float* b,
+                         int color) {
+  const int E = a.E;
+  const float w = a.sor;
+  for (int c = threadIdx.x; c < a.C; c += blockDim.x) {
+    if (((c % a.nx) + (c / a.nx) + color) & 1) continue;
+    int nbc[4];
+    for (int f = 0; f < 4; f++) nbc[f] = neighbour(a, c, f);
+    for (int e = 0; e < E; e++) {
+      const int r = c * E + e;
+      const float* arow = k.A + (int64_t) r * E;
+      const float d = arow[e];
+      float v = (1.0f - w) * k.x[r] * (d / w);
+      for (int g = 0; g < E; g++)
+        if (g != e) v -= arow[g] * k.x[c * E + g];
+      for (int f = 0; f < 4; f++)
+        if (nbc[f] >= 0)
+          v -= k.nb[((int64_t) c * 4 + f) * E + e] * k.x[nbc[f] * E + e];
+      v += b[r];
+      k.x[r] = v * (w / d);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kSolveThreads, 1)
+cmfd_solve_kernel(const CmfdArgs a) {
+  DevScalars* sc = a.sc;
+  if (*(volatile int*) &sc->done) return;
+  __shared__ double red[32];
+  const int C = a.C, E = a.E;
+  const int CE = C * E;
+  const Work k = carve(a.work, C, E);
+  CmfdDevState* cm = a.cm;
+  const int it = sc->iteration;                 // MOC iteration
+  // the coarse tolerance follows the transport residual
+  // (Solver::computeEigenvalue, src/Solver.cpp:1671-1675)
+  double src_thr = 0.1 * sc->threshold;         // Solver::initializeCmfd
+  if (it > 0) src_thr = 0.01 * (sc->residual > 0.0 ? sc->residual : 1e-6);
+  const bool valid = cm->valid != 0;
+  double keff = cm->keff;
+
+  for (int ce = threadIdx.x; ce < CE; ce += blockDim.x)
+    collapse_one(a, k, ce / E, ce % E);
+  __syncthreads();
+  for (int ce = threadIdx.x; ce < CE; ce += blockDim.x)
+    build_row(a, k, ce / E, ce % E, it, valid);
+  __syncthreads();
+
+  // ---- eigenvalueSolve (src/linalg.cpp:25-176)
+  const double rows = (double) CE;
+  const double tol = fmax(kLinalgTol, src_thr);
+  const double lin_tol = fmax(kLinalgTol, tol * 1e-1);
+  float* src_old = k.src_a;
+  float* src_new = k.src_b;
+  mat_fission(a, k, k.x, src_old);
+  const double s0 = block_total(src_old, CE, red);
+  bool failed = !(s0 > 0.0) || !isfinite(s0);
+  int sweeps = 0, power = 0;
+  if (!failed) {
+    for (int r = threadIdx.x; r < CE; r += blockDim.x) {
+      src_old[r] = (float) (src_old[r] * (rows / s0));
+      k.x[r] = (float) (k.x[r] * (rows * keff / s0));
+    }
+    __syncthreads();
+    double initial = 0.0;
+    for (power = 0; power < kMaxPowerIters; power++) {
+      // ---- linearSolve (src/linalg.cpp:179-385): red-black SOR on
+      // A x = src_old
+      float* ls_old = k.ls_a;
+      float* ls_new = k.ls_b;
+      mat_fission(a, k, k.x, ls_old);
+      __syncthreads();
+      double lres = 0.0, linit = 0.0, min_res = 1e6;
+      int li = 0;
+      bool ok = true;
+      while (li < kMaxLinearIters) {
+        sor_half(a, k, src_old, 0);
+        __syncthreads();
+        sor_half(a, k, src_old, 1);
+        __syncthreads();
+        sweeps++;
+        mat_fission(a, k, k.x, ls_new);
+        __syncthreads();
+        if (li == 0) {
+          lres = rmse(a, ls_new, ls_old, red);
+          linit = lres;
+        }
+        li++;
+        if (li > kMinIters) {
+          lres = rmse(a, ls_new, ls_old, red);
+          min_res = fmin(min_res, lres);
+          if ((lres > 1e3 * min_res && min_res > 1e-10) || !isfinite(lres)) {
+            ok = false;
+            break;
+          }
+          const double q = linit > 0.0 ? lres / linit : INFINITY;
+          if (q < 0.1 || lres < lin_tol) break;
+        }
+        if (li > kMinIters - 1 && li < kMaxLinearIters) {
+          float* t = ls_old;
+          ls_old = ls_new;
+          ls_new = t;
+        }
+        if (sweeps >= kMaxSweeps) {
+          ok = false;
+          break;
+        }
+        __syncthreads();   // ls_new is rewritten by the next sweep
+      }
+      if (li == kMaxLinearIters) ok = false;
+      if (!ok) {
+        failed = true;
+        break;
+      }
+      mat_fission(a, k, k.x, src_new);
+      __syncthreads();
+      keff = block_total(src_new, CE, red) / rows;
+      for (int r = threadIdx.x; r < CE; r += blockDim.x)
+        src_new[r] = (float) (src_new[r] / keff);
+      __syncthreads();
+      const double res = rmse(a, src_new, src_old, red);
+      if (power == 0) initial = res < 1e-14 ? 1e-10 : res;
+      float* t = src_old;
+      src_old = src_new;
+      src_new = t;
+      if ((res / initial < 0.03 || res < kLinalgTol) && power > kMinIters) {
+        power++;
+        break;
+      }
+      __syncthreads();
+    }
+    if (!(fabs(keff + 1.0) > FLT_EPSILON) || !isfinite(keff)) failed = true;
+  }
+  __syncthreads();
+
+  // ---- Cmfd::rescaleFlux and the ratios of Cmfd::updateMOCFlux
+  // (src/Cmfd.cpp:1304-1350, 1509-1560, 3222-3300)
+  if (failed) {
+    for (int r = threadIdx.x; r < CE; r += blockDim.x) a.ratio[r] = 1.0f;
+    if (threadIdx.x == 0) {
+      cm->failed = 1;
+      cm->power_iters = power;
+      cm->linear_iters = sweeps;
+      cm->max_ratio = 1.0f;
+      cm->valid = 1;
+      sc->keff = cm->keff;          // the previous coarse eigenvalue stands
+    }
+    return;
+  }
+  mat_fission(a, k, k.x, k.src_a);
+  mat_fission(a, k, k.phi_c, k.src_b);
+  __syncthreads();
+  const double sn = block_total(k.src_a, CE, red);
+  const double so = block_total(k.src_b, CE, red);
+  float far = 1.0f;
+  for (int r = threadIdx.x; r < CE; r += blockDim.x) {
+    const float xn = (float) (k.x[r] / sn);
+    const float xo = (float) (k.phi_c[r] / so);
+    float q = fabs((double) xo) > kFluxEps ? xn / xo : 0.0f;
+    if (it > a.unbounded) q = fminf(20.0f, fmaxf(0.05f, q));
+    a.ratio[r] = q;
+    a.flux_new[r] = xn;
+    a.flux_old[r] = xo;
+    if (q > 0.0f && fabsf(logf(q)) > fabsf(logf(far))) far = q;
+  }
+  // the ratio farthest from 1 (log distance) over the block
+  for (int o = 16; o > 0; o >>= 1) {
+    const float y = __shfl_xor_sync(0xffffffffu, far, o);
+    if (fabsf(logf(y)) > fabsf(logf(far))) far = y;
+  }
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = (double) far;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float best = 1.0f;
+    for (int i = 0; i < (int) (blockDim.x >> 5); i++) {
+      const float y = (float) red[i];
+      if (fabsf(logf(y)) > fabsf(logf(best))) best = y;
+    }
+    cm->max_ratio = best;
+    cm->failed = 0;
+    cm->power_iters = power;
+    cm->linear_iters = sweeps;
+    cm->valid = 1;
+    cm->keff = keff;
+    sc->keff = keff;
   }
 }
 
@@ -74,28 +508,37 @@ int sm_count() {
 
 }  // namespace
 
+int64_t cmfd_work_floats(int C, int E) {
+  const int64_t CE = (int64_t) C * E;
+  return 12 * CE + 3 * CE * E + 8 * CE;
+}
+
 void launch_cmfd_pair_sums(const float* phi, const float* vol,
                            const int32_t* pair_off, const int32_t* pair_fsr,
-                           int P, int G, int ld, double* out,
+                           int P, int G, int ld, double* out, DevScalars* sc,
                            cudaStream_t s) {
   if (P <= 0) return;
-  const int64_t warps_needed = P;
   const int per_block = kPairThreads / 32;
-  int blocks = (int) std::min<int64_t>((warps_needed + per_block - 1) / per_block,
-                                       (int64_t) 8 * sm_count());
+  const int blocks = (int) std::min<int64_t>((P + per_block - 1) / per_block,
+                                             (int64_t) 8 * sm_count());
   cmfd_pair_sums_kernel<<<blocks, kPairThreads, 0, s>>>(phi, vol, pair_off,
-                                                        pair_fsr, P, G, ld, out);
+                                                        pair_fsr, P, G, ld, out,
+                                                        sc);
+}
+
+void launch_cmfd_solve(const CmfdArgs& a, cudaStream_t s) {
+  cmfd_solve_kernel<<<1, kSolveThreads, 0, s>>>(a);
 }
 
 void launch_cmfd_prolong(float* phi, const int32_t* fsr_cell,
-                         const int32_t* group_of, const double* ratio,
+                         const int32_t* group_of, const float* ratio,
                          int64_t R, int G, int ld, int E, DevScalars* sc,
-                         double keff, cudaStream_t s) {
+                         cudaStream_t s) {
   const int64_t n = R * ld;
   int blocks = (int) std::min<int64_t>((n + 255) / 256, (int64_t) 8 * sm_count());
   if (blocks < 1) blocks = 1;
   cmfd_prolong_kernel<<<blocks, 256, 0, s>>>(phi, fsr_cell, group_of, ratio, R,
-                                             G, ld, E, sc, keff);
+                                             G, ld, E, sc);
 }
 
 }  // namespace moc

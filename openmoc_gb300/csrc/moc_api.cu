@@ -200,10 +200,32 @@ struct moc_ctx {
   int32_t* cm_pair_off = nullptr;
   int32_t* cm_pair_fsr = nullptr;
   double* cm_sums = nullptr;
-  double* cm_ratio = nullptr;
+  float* cm_ratio = nullptr;
   double* h_cm_sums = nullptr;
   float* h_cm_cur = nullptr;
+  std::vector<float> h_cm_ratio;
   int64_t cm_sums_n = 0;
+  // the device coarse solve (default; cm_host: the FP64 host solve): its
+  // state, scratch, relaxation history, coarse fluxes, and the collapse
+  // inputs (pairs of each cell, pair materials, chi per coarse group and
+  // scattering into each coarse group by material, cell volumes, widths,
+  // coarse group starts, Larsen quadrature)
+  bool cm_host = false;
+  moc::CmfdDevState* cm_state = nullptr;
+  float* cm_work = nullptr;
+  float* cm_dcorr = nullptr;
+  float* cm_flux_old = nullptr;
+  float* cm_flux_new = nullptr;
+  int32_t* cm_cell_pair = nullptr;
+  int32_t* cm_pair_mat = nullptr;
+  float* cm_chi_m = nullptr;
+  float* cm_ss_m = nullptr;
+  float* cm_cell_vol = nullptr;
+  float* cm_wx = nullptr;
+  float* cm_wy = nullptr;
+  int32_t* cm_gstart = nullptr;
+  float* cm_edc_mu = nullptr;
+  float* cm_edc_w = nullptr;
 };
 
 namespace {
@@ -677,6 +699,21 @@ void cmfd_release(moc_ctx* c) {
   dfree(c->cm_pair_fsr);
   dfree(c->cm_sums);
   dfree(c->cm_ratio);
+  dfree(c->cm_state);
+  dfree(c->cm_work);
+  dfree(c->cm_dcorr);
+  dfree(c->cm_flux_old);
+  dfree(c->cm_flux_new);
+  dfree(c->cm_cell_pair);
+  dfree(c->cm_pair_mat);
+  dfree(c->cm_chi_m);
+  dfree(c->cm_ss_m);
+  dfree(c->cm_cell_vol);
+  dfree(c->cm_wx);
+  dfree(c->cm_wy);
+  dfree(c->cm_gstart);
+  dfree(c->cm_edc_mu);
+  dfree(c->cm_edc_w);
   if (c->h_cm_sums) cudaFreeHost(c->h_cm_sums);
   if (c->h_cm_cur) cudaFreeHost(c->h_cm_cur);
   c->h_cm_sums = nullptr;
@@ -749,57 +786,175 @@ int cmfd_prepare(moc_ctx* c) {
     if (c->h_cm_sums) cudaFreeHost(c->h_cm_sums);
     c->h_cm_sums = nullptr;
     MOC_TRY(dalloc(&c->cm_sums, n));
-    MOC_CUDA(cudaMallocHost(&c->h_cm_sums, 8 * n));
+    if (c->cm_host) MOC_CUDA(cudaMallocHost(&c->h_cm_sums, 8 * n));
     c->cm_sums_n = n;
   }
   S.reset();
   S.source_threshold = 0.1 * c->threshold;   // Solver::initializeCmfd
+  if (c->cm_host) return MOC_OK;
+  // the device solve's inputs
+  const moc_cmfd::Config& cf = S.cfg;
+  const int E = cf.E;
+  std::vector<int32_t> cell_pair(C + 1, 0);
+  for (int p = 0; p < P; p++) cell_pair[F.pair_cell[p] + 1]++;
+  for (int i = 0; i < C; i++) cell_pair[i + 1] += cell_pair[i];
+  std::vector<float> chi_m((size_t) M * E, 0.0f), ss_m((size_t) MG * E, 0.0f);
+  for (int m = 0; m < M; m++)
+    for (int h = 0; h < G; h++) {
+      chi_m[(size_t) m * E + cf.group_of[h]] += c->h_chi[(size_t) m * G + h];
+      // scattering from h into each coarse group (sigma_s is [m][dest][orig])
+      for (int g = 0; g < G; g++)
+        ss_m[((size_t) m * G + h) * E + cf.group_of[g]] +=
+            ss[((size_t) m * G + g) * G + h];
+    }
+  std::vector<float> cvol(F.cell_vol.begin(), F.cell_vol.end());
+  std::vector<float> wx(cf.wx.begin(), cf.wx.end()), wy(cf.wy.begin(), cf.wy.end());
+  std::vector<float> mu(cf.edc_mu.begin(), cf.edc_mu.end());
+  std::vector<float> ew(cf.edc_w.begin(), cf.edc_w.end());
+  std::vector<int32_t> gstart(cf.gstart.begin(), cf.gstart.end());
+  auto up = [&](auto** dst, const auto& v) -> int {
+    dfree(*dst);
+    MOC_TRY(dalloc(dst, std::max<int64_t>(1, (int64_t) v.size())));
+    if (!v.empty())
+      MOC_CUDA(cudaMemcpy(*dst, v.data(), sizeof(v[0]) * v.size(),
+                          cudaMemcpyHostToDevice));
+    return MOC_OK;
+  };
+  MOC_TRY(up(&c->cm_cell_pair, cell_pair));
+  MOC_TRY(up(&c->cm_pair_mat, F.pair_mat));
+  MOC_TRY(up(&c->cm_chi_m, chi_m));
+  MOC_TRY(up(&c->cm_ss_m, ss_m));
+  MOC_TRY(up(&c->cm_cell_vol, cvol));
+  MOC_TRY(up(&c->cm_wx, wx));
+  MOC_TRY(up(&c->cm_wy, wy));
+  MOC_TRY(up(&c->cm_gstart, gstart));
+  MOC_TRY(up(&c->cm_edc_mu, mu));
+  MOC_TRY(up(&c->cm_edc_w, ew));
+  const int64_t CE = (int64_t) C * E;
+  dfree(c->cm_work);
+  dfree(c->cm_dcorr);
+  dfree(c->cm_flux_old);
+  dfree(c->cm_flux_new);
+  dfree(c->cm_state);
+  MOC_TRY(dalloc(&c->cm_work, moc::cmfd_work_floats(C, E)));
+  MOC_TRY(dalloc(&c->cm_dcorr, 4 * CE));
+  MOC_TRY(dalloc(&c->cm_flux_old, CE));
+  MOC_TRY(dalloc(&c->cm_flux_new, CE));
+  MOC_TRY(dalloc(&c->cm_state, 1));
+  MOC_CUDA(cudaMemset(c->cm_dcorr, 0, 16 * CE));
+  MOC_CUDA(cudaMemset(c->cm_flux_old, 0, 4 * CE));
+  MOC_CUDA(cudaMemset(c->cm_flux_new, 0, 4 * CE));
+  moc::CmfdDevState st0{};
+  st0.keff = 1.0;
+  st0.max_ratio = 1.0f;
+  MOC_CUDA(cudaMemcpy(c->cm_state, &st0, sizeof(st0), cudaMemcpyHostToDevice));
   return MOC_OK;
+}
+
+moc::CmfdArgs cmfd_args(moc_ctx* c) {
+  const moc_cmfd::Config& cf = c->cmfd->cfg;
+  moc::CmfdArgs a{};
+  a.nx = cf.nx;
+  a.ny = cf.ny;
+  a.C = cf.cells();
+  a.E = cf.E;
+  a.G = cf.G;
+  a.P = c->cmfd->fine.pairs();
+  a.n_edc = (int) cf.edc_mu.size();
+  a.ld = row_stride(c);
+  for (int f = 0; f < 4; f++) a.bc[f] = cf.bc[f];
+  a.relax = (float) cf.relaxation;
+  a.sor = (float) cf.sor;
+  a.flux_limiting = cf.flux_limiting ? 1 : 0;
+  a.unbounded = cf.unbounded;
+  a.wx = c->cm_wx;
+  a.wy = c->cm_wy;
+  a.gstart = c->cm_gstart;
+  a.cell_pair = c->cm_cell_pair;
+  a.pair_mat = c->cm_pair_mat;
+  a.st = c->sigma_t;
+  a.nf = c->nu_sigma_f;
+  a.chi_m = c->cm_chi_m;
+  a.ss_m = c->cm_ss_m;
+  a.cell_vol = c->cm_cell_vol;
+  a.edc_mu = c->cm_edc_mu;
+  a.edc_w = c->cm_edc_w;
+  a.S = c->cm_sums;
+  a.cur = c->cm_cur;
+  a.work = c->cm_work;
+  a.dcorr_old = c->cm_dcorr;
+  a.ratio = c->cm_ratio;
+  a.flux_old = c->cm_flux_old;
+  a.flux_new = c->cm_flux_new;
+  a.cm = c->cm_state;
+  a.sc = c->sc;
+  return a;
 }
 
 // computeEigenvalue with CMFD (src/Solver.cpp:1591-1647): per iteration
 // sources, sweep with current tallies, addSourceToScalarFlux, the coarse
-// solve in place of computeKeff (flux sums and currents to the host, ratios
-// back, prolongation), normalizeFluxes, residual and store.  The host reads
-// the device state every iteration: the coarse solve needs its tallies.
+// solve in place of computeKeff and the prolongation, normalizeFluxes,
+// residual and store.  The device solve keeps the whole loop on the GPU
+// (the host checks the state once per block of iterations, as without
+// CMFD); the host solve reads the tallies back every iteration.
 int run_cmfd_iterations(moc_ctx* c, int res_type) {
   moc_cmfd::Solver& S = *c->cmfd;
   moc::SolverArgs a = solver_args(c, 1);
   const int C = S.cfg.cells(), E = S.cfg.E;
   const int ld = row_stride(c);
   const int64_t ncur = (int64_t) C * moc_cmfd::kFaces * ld;
-  for (int it = 0;; it++) {
-    enqueue_sources(c, a, -1, 1);
-    MOC_CUDA(cudaMemsetAsync(c->cm_cur, 0, 4 * ncur, c->stream));
-    MOC_TRY(enqueue_sweep(c, 1, true, 0));
-    enqueue_add_source(c, a, 0);
-    moc::launch_cmfd_pair_sums(c->phi, c->fsr_vol, c->cm_pair_off,
-                               c->cm_pair_fsr, S.fine.pairs(),
-                               c->d.num_groups, ld, c->cm_sums, c->stream);
-    c->launches++;
-    MOC_CUDA(cudaGetLastError());
-    MOC_CUDA(cudaMemcpyAsync(c->h_cm_sums, c->cm_sums, 8 * c->cm_sums_n,
-                             cudaMemcpyDeviceToHost, c->stream));
-    MOC_CUDA(cudaMemcpyAsync(c->h_cm_cur, c->cm_cur, 4 * ncur,
-                             cudaMemcpyDeviceToHost, c->stream));
-    MOC_CUDA(cudaStreamSynchronize(c->stream));
-    const double k = S.step(it, c->h_cm_sums, c->h_cm_cur, ld);
-    MOC_CUDA(cudaMemcpyAsync(c->cm_ratio, S.ratio.data(), 8 * (int64_t) C * E,
-                             cudaMemcpyHostToDevice, c->stream));
-    moc::launch_cmfd_prolong(c->phi, c->cm_cell, c->cm_group, c->cm_ratio,
-                             c->d.num_fsrs, c->d.num_groups, ld, E, c->sc, k,
-                             c->stream);
-    moc::launch_fission_rate(a, 1, c->stream);
-    moc::launch_residual(a, res_type, 1, 1, 1, c->stream);
-    c->launches += 3;
-    MOC_CUDA(cudaGetLastError());
+  const moc::CmfdArgs ca = cmfd_args(c);
+  int completed = 0;
+  for (;;) {
+    const int k = c->cm_host ? 1 : c->iters_per_sync;
+    for (int i = 0; i < k; i++) {
+      enqueue_sources(c, a, -1, 1);
+      MOC_CUDA(cudaMemsetAsync(c->cm_cur, 0, 4 * ncur, c->stream));
+      MOC_TRY(enqueue_sweep(c, 1, true, i));
+      enqueue_add_source(c, a, 0);
+      moc::launch_cmfd_pair_sums(c->phi, c->fsr_vol, c->cm_pair_off,
+                                 c->cm_pair_fsr, S.fine.pairs(),
+                                 c->d.num_groups, ld, c->cm_sums, c->sc,
+                                 c->stream);
+      c->launches += 3;
+      MOC_CUDA(cudaGetLastError());
+      if (c->cm_host) {
+        MOC_CUDA(cudaMemcpyAsync(c->h_cm_sums, c->cm_sums, 8 * c->cm_sums_n,
+                                 cudaMemcpyDeviceToHost, c->stream));
+        MOC_CUDA(cudaMemcpyAsync(c->h_cm_cur, c->cm_cur, 4 * ncur,
+                                 cudaMemcpyDeviceToHost, c->stream));
+        MOC_TRY(pull(c));
+        if (c->hsc->done) break;
+        S.source_threshold = c->hsc->iteration == 0
+                                 ? 0.1 * c->threshold
+                                 : 0.01 * (c->hsc->residual > 0.0
+                                               ? c->hsc->residual : 1e-6);
+        const double kc = S.step(c->hsc->iteration, c->h_cm_sums,
+                                 c->h_cm_cur, ld);
+        c->h_cm_ratio.assign(S.ratio.begin(), S.ratio.end());
+        MOC_CUDA(cudaMemcpyAsync(c->cm_ratio, c->h_cm_ratio.data(),
+                                 4 * (int64_t) C * E, cudaMemcpyHostToDevice,
+                                 c->stream));
+        c->hsc->keff = kc;
+        MOC_CUDA(cudaMemcpyAsync(&c->sc->keff, &c->hsc->keff, sizeof(double),
+                                 cudaMemcpyHostToDevice, c->stream));
+      } else {
+        moc::launch_cmfd_solve(ca, c->stream);
+        c->launches++;
+      }
+      moc::launch_cmfd_prolong(c->phi, c->cm_cell, c->cm_group, c->cm_ratio,
+                               c->d.num_fsrs, c->d.num_groups, ld, E, c->sc,
+                               c->stream);
+      moc::launch_fission_rate(a, 1, c->stream);
+      moc::launch_residual(a, res_type, 1, 1, 1, c->stream);
+      c->launches += 3;
+      MOC_CUDA(cudaGetLastError());
+    }
     MOC_TRY(pull(c));
-    MOC_TRY(collect_sweep_times(c, 1));
-    c->num_sweeps++;
-    // the coarse solve's tolerance follows the transport residual
-    double res = c->hsc->residual;
-    if (res <= 0.0) res = 1e-6;
-    S.source_threshold = 0.01 * res;
+    const int done_now = c->hsc->iteration - completed;
+    MOC_TRY(collect_sweep_times(c, std::min(done_now, k)));
+    c->num_sweeps += done_now;
+    completed = c->hsc->iteration;
     if (c->hsc->done) break;
   }
   c->keff = c->hsc->keff;
@@ -2324,6 +2479,7 @@ int moc_set_cmfd(moc_ctx* c, const moc_cmfd_mesh* m) {
   cf.flux_limiting = m->flux_limiting != 0;
   cf.unbounded = m->num_unbounded_iterations;
   c->cmfd = S;
+  c->cm_host = m->solve_on_host != 0;
   c->h_cm_cell.assign(m->fsr_cell, m->fsr_cell + R);
   const int ld = row_stride(c);
   const int64_t ncur = (int64_t) C * moc_cmfd::kFaces * ld;
@@ -2334,7 +2490,8 @@ int moc_set_cmfd(moc_ctx* c, const moc_cmfd_mesh* m) {
   step(dalloc(&c->cm_cur, ncur));
   step(dalloc(&c->cm_group, G));
   step(dalloc(&c->cm_ratio, (int64_t) C * E));
-  if (st == MOC_OK && cudaMallocHost(&c->h_cm_cur, 4 * ncur) != cudaSuccess)
+  if (st == MOC_OK && c->cm_host &&
+      cudaMallocHost(&c->h_cm_cur, 4 * ncur) != cudaSuccess)
     st = fail(MOC_ERR_MEMORY, "pinned host buffer for CMFD currents");
   if (st != MOC_OK) {
     cmfd_release(c);
@@ -2364,12 +2521,26 @@ int moc_get_cmfd_info(moc_ctx* c, int* enabled, double* keff,
                       double* max_ratio) {
   MOC_CHECK(c, MOC_ERR_ARG, "null context");
   const moc_cmfd::Solver* S = c->cmfd;
+  double k = S ? S->keff : 0.0, mr = 1.0;
+  int pi = S ? S->stats.power_iterations : 0;
+  int li = S ? S->stats.linear_iterations : 0;
+  if (S && !c->cm_host && c->cm_state) {
+    moc::CmfdDevState d{};
+    MOC_CUDA(cudaSetDevice(c->d.device));
+    MOC_CUDA(cudaStreamSynchronize(c->stream));
+    MOC_CUDA(cudaMemcpy(&d, c->cm_state, sizeof(d), cudaMemcpyDeviceToHost));
+    k = d.keff;
+    pi = d.power_iters;
+    li = d.linear_iters;
+    mr = d.max_ratio;
+  } else if (S) {
+    mr = S->stats.max_ratio;
+  }
   if (enabled) *enabled = S ? 1 : 0;
-  if (keff) *keff = S ? S->keff : 0.0;
-  if (power_iterations) *power_iterations = S ? S->stats.power_iterations : 0;
-  if (linear_iterations)
-    *linear_iterations = S ? S->stats.linear_iterations : 0;
-  if (max_ratio) *max_ratio = S ? S->stats.max_ratio : 1.0;
+  if (keff) *keff = k;
+  if (power_iterations) *power_iterations = pi;
+  if (linear_iterations) *linear_iterations = li;
+  if (max_ratio) *max_ratio = mr;
   return MOC_OK;
 }
 
@@ -2380,6 +2551,24 @@ int moc_get_cmfd_fluxes(moc_ctx* c, double* old_flux, double* new_flux,
   const int64_t need = (int64_t) S.cfg.cells() * S.cfg.E;
   MOC_CHECK(n == need, MOC_ERR_ARG,
             "expected " + std::to_string(need) + " coarse fluxes");
+  if (!c->cm_host) {
+    MOC_CHECK(c->cm_flux_old != nullptr, MOC_ERR_STATE,
+              "no coarse solve has run");
+    std::vector<float> t(need);
+    MOC_CUDA(cudaSetDevice(c->d.device));
+    MOC_CUDA(cudaStreamSynchronize(c->stream));
+    if (old_flux) {
+      MOC_CUDA(cudaMemcpy(t.data(), c->cm_flux_old, 4 * need,
+                          cudaMemcpyDeviceToHost));
+      std::copy(t.begin(), t.end(), old_flux);
+    }
+    if (new_flux) {
+      MOC_CUDA(cudaMemcpy(t.data(), c->cm_flux_new, 4 * need,
+                          cudaMemcpyDeviceToHost));
+      std::copy(t.begin(), t.end(), new_flux);
+    }
+    return MOC_OK;
+  }
   if (old_flux && (int64_t) S.phi_old.size() == need)
     std::copy(S.phi_old.begin(), S.phi_old.end(), old_flux);
   if (new_flux && (int64_t) S.phi_new.size() == need)

@@ -307,16 +307,65 @@ void launch_batch_rebase(int2* segs, int64_t S, const int32_t* fsr_mat,
                          int64_t s0, int32_t t0, int32_t a0, int32_t slot,
                          cudaStream_t s);
 
+// CMFD coarse solve on the device (cmfd.cu): state kept between
+// iterations of a solve, and the inputs of the single-block solver.
+struct CmfdDevState {
+  double keff;          // coarse eigenvalue of the previous solve (1 at start)
+  int valid;            // the relaxation history holds a previous step
+  int power_iters;      // power iterations of the last coarse solve
+  int linear_iters;     // SOR sweeps of the last coarse solve
+  int failed;           // the last coarse solve did not converge
+  float max_ratio;      // prolongation ratio farthest from 1
+  int pad;
+};
+
+struct CmfdArgs {
+  int nx, ny, C, E, G, P, n_edc, ld;
+  int bc[4];                    // faces x-min, y-min, x-max, y-max: 0 vacuum
+  float relax, sor;
+  int flux_limiting, unbounded;
+  const float* wx;              // [nx]
+  const float* wy;              // [ny]
+  const int32_t* gstart;        // [E + 1] first group of each coarse group
+  const int32_t* cell_pair;     // [C + 1] pairs of each cell (cell-major)
+  const int32_t* pair_mat;      // [P]
+  const float* st;              // [M][G] total cross sections
+  const float* nf;              // [M][G] nu-fission
+  const float* chi_m;           // [M][E] chi summed over each coarse group
+  const float* ss_m;            // [M][G][E] scattering from h into coarse g
+  const float* cell_vol;        // [C]
+  const float* edc_mu;          // [n_edc]
+  const float* edc_w;           // [n_edc]
+  const double* S;              // [P][G] sums of phi * V
+  const float* cur;             // [C][4][ld] partial currents
+  float* work;                  // scratch (cmfd_work_floats)
+  float* dcorr_old;             // [C][4][E] relaxation history
+  float* ratio;                 // [C][E] prolongation factors
+  float* flux_old;              // [C][E] coarse fluxes, unit fission source
+  float* flux_new;              // [C][E]
+  CmfdDevState* cm;
+  DevScalars* sc;
+};
+
+// Scratch floats the device coarse solve needs for C cells, E groups.
+int64_t cmfd_work_floats(int C, int E);
+// One coarse solve (Cmfd::computeKeff) on one block: collapse, matrices,
+// power iteration with red-black SOR, ratios; sets sc->keff.  Returns at
+// once when the solve is done.
+void launch_cmfd_solve(const CmfdArgs& a, cudaStream_t s);
+
 // CMFD (cmfd.cu): per (coarse cell, material) pair the sums of phi * volume
 // over its FSRs, [P][G] FP64, from the CSR list pair_off [P + 1] /
 // pair_fsr [R]; and the prolongation phi[r][g] *= ratio[cell(r)][group(g)]
 // ([cells][E] FP64), which also sets sc->keff to the coarse eigenvalue.
+// Both return at once when sc->done is set.
 void launch_cmfd_pair_sums(const float* phi, const float* vol,
                            const int32_t* pair_off, const int32_t* pair_fsr,
-                           int P, int G, int ld, double* out, cudaStream_t s);
+                           int P, int G, int ld, double* out, DevScalars* sc,
+                           cudaStream_t s);
 void launch_cmfd_prolong(float* phi, const int32_t* fsr_cell,
-                         const int32_t* group_of, const double* ratio,
+                         const int32_t* group_of, const float* ratio,
                          int64_t R, int G, int ld, int E, DevScalars* sc,
-                         double keff, cudaStream_t s);
+                         cudaStream_t s);
 
 }  // namespace moc

@@ -396,6 +396,7 @@ residual_kernel(const SolverArgs a, int normalise, int store, int finish) {
 // 1860-1933).
 __global__ void __launch_bounds__(kRowThreads)
 fission_rate_kernel(const SolverArgs a, int what) {
+  if (skip(a)) return;
   const int G = a.num_groups;
   const int lane = threadIdx.x & 31;
   double rate = 0.0;

@@ -23,9 +23,10 @@ def _rel(got, ref, floor):
                         np.maximum(np.abs(ref), floor * np.abs(ref).max())))
 
 
-def _cmfd(p, groups):
+def _cmfd(p, groups, host=False):
     from openmoc_gb300 import Cmfd
     c = Cmfd()
+    c.useHostSolver(host)
     nx = p.cmfd_geometry["widths_x"].size
     ny = p.cmfd_geometry["widths_y"].size
     c.setLatticeStructure(nx, ny)
@@ -38,13 +39,15 @@ def _cmfd(p, groups):
 
 @pytest.mark.parametrize("case", sorted(CMFD_CASES))
 @pytest.mark.parametrize("precision", ["f32", "f64"])
-def test_gpu_cmfd_matches_openmoc(case, precision):
+@pytest.mark.parametrize("host", [False, True])
+def test_gpu_cmfd_matches_openmoc(case, precision, host):
+    """The coarse solve on the GPU (FP32) or on the host (FP64)."""
     from openmoc_gb300 import GB300Solver
     p, sc, arr = load_case(case, precision)
     s = GB300Solver(device=0)
     s.setConvergenceThreshold(sc["tolerance"])
     s.setTrackGenerator(p)
-    s.setCmfd(_cmfd(p, CMFD_CASES[case]))
+    s.setCmfd(_cmfd(p, CMFD_CASES[case], host))
     s.computeEigenvalue(int(sc["max_iters"]), int(sc["res_type"]))
     info = s.getCmfdInfo()
     assert info["enabled"] and info["power_iterations"] > 25
@@ -92,6 +95,8 @@ def test_gpu_cmfd_converges_to_unaccelerated_answer(mesh):
     assert _rel(s.getFluxes(), ref.getFluxes(), 1e-3) < 1e-4
     if mesh == 17:
         assert n_cmfd < 0.5 * n_plain, (n_cmfd, n_plain)
+    info = s.getCmfdInfo()
+    assert info["power_iterations"] > 25 and info["linear_iterations"] > 25
     old, new = s.getCmfdFluxes()
     assert old.shape == (mesh * mesh, 2) and np.isfinite(new).all()
     ref.close()
@@ -157,7 +162,8 @@ def test_gpu_cmfd_uses_native_library():
     s.close()
 
 
-def test_gpu_cmfd_matches_oracle_step_by_step():
+@pytest.mark.parametrize("host", [False, True])
+def test_gpu_cmfd_matches_oracle_step_by_step(host):
     """A generated 5 x 5 lattice (vacuum on +x and +y, water pins) on a pin
     mesh with two coarse groups, a fixed number of iterations: keff, fluxes
     and the coarse fluxes of the last coarse solve against the FP64 oracle
@@ -177,6 +183,7 @@ def test_gpu_cmfd_matches_oracle_step_by_step():
     c = Cmfd()
     c.setLatticeStructure(5, 5)
     c.setGroupStructure(groups)
+    c.useHostSolver(host)
     mesh, keep = c.mesh(p)
     g = p.cmfd_geometry
     cm = CmfdOracle(p, 5, 5, keep[0], keep[1], keep[2], g["end_face"], g["bc"],
