@@ -21,7 +21,10 @@ namespace moc {
 namespace {
 
 constexpr int kPairThreads = 256;
-constexpr int kSolveThreads = 1024;
+constexpr int kSolveThreads = 512;
+// shared memory for the solve's vectors (x and four sources): up to 120 KB,
+// leaving the rest of the SM's 256 KB to L1 for the matrices
+constexpr int kSolveSmemMax = 120 * 1024;
 constexpr float kZeroSigmaT = 1e-6f;          // src/constants.h:34
 constexpr double kFluxEps = 1e-25;            // src/constants.h:15
 constexpr double kLinalgTol = 1e-7;           // LINALG_TOL, FP32 build
@@ -310,8 +313,10 @@ __device__ void sor_half(const CmfdArgs& a, const Work& k, const float* b,
                          int color) {
   const int E = a.E;
   const float w = a.sor;
-  for (int c = threadIdx.x; c < a.C; c += blockDim.x) {
-    if (((c % a.nx) + (c / a.nx) + color) & 1) continue;
+  const int j0 = color ? a.n_color0 : 0;
+  const int j1 = color ? a.C : a.n_color0;
+  for (int j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
+    const int c = a.color_cells[j];
     int nbc[4];
     for (int f = 0; f < 4; f++) nbc[f] = neighbour(a, c, f);
     for (int e = 0; e < E; e++) {
@@ -331,13 +336,23 @@ __device__ void sor_half(const CmfdArgs& a, const Work& k, const float* b,
 }
 
 __global__ void __launch_bounds__(kSolveThreads, 1)
-cmfd_solve_kernel(const CmfdArgs a) {
+cmfd_solve_kernel(const CmfdArgs a, int vec_in_smem) {
   DevScalars* sc = a.sc;
   if (*(volatile int*) &sc->done) return;
   __shared__ double red[32];
+  extern __shared__ float s_vec[];
   const int C = a.C, E = a.E;
   const int CE = C * E;
-  const Work k = carve(a.work, C, E);
+  Work k = carve(a.work, C, E);
+  if (vec_in_smem) {
+    // the iterate and the source vectors, rewritten every sweep, in shared
+    // memory; the matrices, read only, stay in L1
+    k.x = s_vec;
+    k.src_a = s_vec + CE;
+    k.src_b = s_vec + 2 * CE;
+    k.ls_a = s_vec + 3 * CE;
+    k.ls_b = s_vec + 4 * CE;
+  }
   CmfdDevState* cm = a.cm;
   const int it = sc->iteration;                 // MOC iteration
   // the coarse tolerance follows the transport residual
@@ -387,8 +402,12 @@ cmfd_solve_kernel(const CmfdArgs a) {
         sor_half(a, k, src_old, 1);
         __syncthreads();
         sweeps++;
-        mat_fission(a, k, k.x, ls_new);
-        __syncthreads();
+        // the new fission source is read at the first sweep and from the
+        // 25th on (residuals and the copy to the old source)
+        if (li == 0 || li + 1 >= kMinIters) {
+          mat_fission(a, k, k.x, ls_new);
+          __syncthreads();
+        }
         if (li == 0) {
           lres = rmse(a, ls_new, ls_old, red);
           linit = lres;
@@ -527,7 +546,20 @@ void launch_cmfd_pair_sums(const float* phi, const float* vol,
 }
 
 void launch_cmfd_solve(const CmfdArgs& a, cudaStream_t s) {
-  cmfd_solve_kernel<<<1, kSolveThreads, 0, s>>>(a);
+  // one thread per cell of a colour, at least four warps
+  int threads = (std::max(a.n_color0, a.C - a.n_color0) + 31) / 32 * 32;
+  threads = std::max(128, std::min(kSolveThreads, threads));
+  const int64_t vec_bytes = (int64_t) 5 * a.C * a.E * sizeof(float);
+  const int in_smem = vec_bytes <= kSolveSmemMax ? 1 : 0;
+  const int smem = in_smem ? (int) vec_bytes : 0;
+  static int configured = 0;
+  if (!configured) {
+    cudaFuncSetAttribute(cmfd_solve_kernel,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kSolveSmemMax);
+    configured = 1;
+  }
+  cmfd_solve_kernel<<<1, threads, smem, s>>>(a, in_smem);
 }
 
 void launch_cmfd_prolong(float* phi, const int32_t* fsr_cell,

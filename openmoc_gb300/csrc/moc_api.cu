@@ -217,6 +217,8 @@ struct moc_ctx {
   float* cm_flux_old = nullptr;
   float* cm_flux_new = nullptr;
   int32_t* cm_cell_pair = nullptr;
+  int32_t* cm_color_cells = nullptr;
+  int cm_n_color0 = 0;
   int32_t* cm_pair_mat = nullptr;
   float* cm_chi_m = nullptr;
   float* cm_ss_m = nullptr;
@@ -705,6 +707,7 @@ void cmfd_release(moc_ctx* c) {
   dfree(c->cm_flux_old);
   dfree(c->cm_flux_new);
   dfree(c->cm_cell_pair);
+  dfree(c->cm_color_cells);
   dfree(c->cm_pair_mat);
   dfree(c->cm_chi_m);
   dfree(c->cm_ss_m);
@@ -821,6 +824,13 @@ int cmfd_prepare(moc_ctx* c) {
     return MOC_OK;
   };
   MOC_TRY(up(&c->cm_cell_pair, cell_pair));
+  std::vector<int32_t> colors;
+  for (int k = 0; k < 2; k++) {
+    for (int cell = 0; cell < C; cell++)
+      if (((cell % cf.nx) + (cell / cf.nx)) % 2 == k) colors.push_back(cell);
+    if (k == 0) c->cm_n_color0 = (int) colors.size();
+  }
+  MOC_TRY(up(&c->cm_color_cells, colors));
   MOC_TRY(up(&c->cm_pair_mat, F.pair_mat));
   MOC_TRY(up(&c->cm_chi_m, chi_m));
   MOC_TRY(up(&c->cm_ss_m, ss_m));
@@ -871,6 +881,8 @@ moc::CmfdArgs cmfd_args(moc_ctx* c) {
   a.wy = c->cm_wy;
   a.gstart = c->cm_gstart;
   a.cell_pair = c->cm_cell_pair;
+  a.color_cells = c->cm_color_cells;
+  a.n_color0 = c->cm_n_color0;
   a.pair_mat = c->cm_pair_mat;
   a.st = c->sigma_t;
   a.nf = c->nu_sigma_f;

@@ -328,6 +328,8 @@ struct CmfdArgs {
   const float* wy;              // [ny]
   const int32_t* gstart;        // [E + 1] first group of each coarse group
   const int32_t* cell_pair;     // [C + 1] pairs of each cell (cell-major)
+  const int32_t* color_cells;   // [C] red cells ((ix + iy) even), then black
+  int n_color0;
   const int32_t* pair_mat;      // [P]
   const float* st;              // [M][G] total cross sections
   const float* nf;              // [M][G] nu-fission
