@@ -391,11 +391,12 @@ typedef struct {
  *  exponential (MOC_ERR_UNSUPPORTED if the table was requested). */
 int moc_set_cmfd(moc_ctx* ctx, const moc_cmfd_mesh* mesh);
 /** Whether CMFD is attached, the last coarse eigenvalue, the coarse power
- *  iterations and SOR sweeps of the last coarse solve, and its
- *  prolongation ratio farthest from 1 (any pointer may be NULL). */
+ *  iterations and SOR sweeps of the last coarse solve, its prolongation
+ *  ratio farthest from 1, and whether it failed to converge (no
+ *  prolongation that iteration); any pointer may be NULL. */
 int moc_get_cmfd_info(moc_ctx* ctx, int* enabled, double* keff,
                       int* power_iterations, int* linear_iterations,
-                      double* max_ratio);
+                      double* max_ratio, int* failed);
 /** The coarse fluxes of the last coarse solve, [cells][E], before (old) and
  *  after (new) it, each normalised to unit total fission source
  *  (Cmfd::rescaleFlux); either pointer may be NULL. */

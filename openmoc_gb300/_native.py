@@ -138,7 +138,7 @@ _SIGS = {
     "moc_set_cmfd": ([_P, C.POINTER(CmfdMesh)], C.c_int),
     "moc_get_cmfd_info": ([_P, C.POINTER(C.c_int), C.POINTER(C.c_double),
                            C.POINTER(C.c_int), C.POINTER(C.c_int),
-                           C.POINTER(C.c_double)], C.c_int),
+                           C.POINTER(C.c_double), C.POINTER(C.c_int)], C.c_int),
     "moc_get_cmfd_fluxes": ([_P, _P, _P, C.c_int64], C.c_int),
 }
 

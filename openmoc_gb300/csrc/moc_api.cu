@@ -2530,12 +2530,13 @@ int moc_set_cmfd(moc_ctx* c, const moc_cmfd_mesh* m) {
 
 int moc_get_cmfd_info(moc_ctx* c, int* enabled, double* keff,
                       int* power_iterations, int* linear_iterations,
-                      double* max_ratio) {
+                      double* max_ratio, int* failed) {
   MOC_CHECK(c, MOC_ERR_ARG, "null context");
   const moc_cmfd::Solver* S = c->cmfd;
   double k = S ? S->keff : 0.0, mr = 1.0;
   int pi = S ? S->stats.power_iterations : 0;
   int li = S ? S->stats.linear_iterations : 0;
+  int fl = S ? (S->stats.failed ? 1 : 0) : 0;
   if (S && !c->cm_host && c->cm_state) {
     moc::CmfdDevState d{};
     MOC_CUDA(cudaSetDevice(c->d.device));
@@ -2545,6 +2546,7 @@ int moc_get_cmfd_info(moc_ctx* c, int* enabled, double* keff,
     pi = d.power_iters;
     li = d.linear_iters;
     mr = d.max_ratio;
+    fl = d.failed;
   } else if (S) {
     mr = S->stats.max_ratio;
   }
@@ -2553,6 +2555,7 @@ int moc_get_cmfd_info(moc_ctx* c, int* enabled, double* keff,
   if (power_iterations) *power_iterations = pi;
   if (linear_iterations) *linear_iterations = li;
   if (max_ratio) *max_ratio = mr;
+  if (failed) *failed = fl;
   return MOC_OK;
 }
 

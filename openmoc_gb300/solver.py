@@ -202,13 +202,13 @@ class GB300Solver:
         """The last coarse solve: eigenvalue, power iterations, SOR sweeps
         and the prolongation ratio farthest from 1."""
         self._need_ctx()
-        en, k, pi, li, mr = (C.c_int(), C.c_double(), C.c_int(), C.c_int(),
-                             C.c_double())
+        en, k, pi, li, mr, fl = (C.c_int(), C.c_double(), C.c_int(), C.c_int(),
+                                 C.c_double(), C.c_int())
         self._call("moc_get_cmfd_info", C.byref(en), C.byref(k), C.byref(pi),
-                   C.byref(li), C.byref(mr))
+                   C.byref(li), C.byref(mr), C.byref(fl))
         return {"enabled": bool(en.value), "keff": k.value,
                 "power_iterations": pi.value, "linear_iterations": li.value,
-                "max_ratio": mr.value}
+                "max_ratio": mr.value, "failed": bool(fl.value)}
 
     def getCmfdFluxes(self):
         """(old, new) coarse fluxes of the last coarse solve, [cells][E],
