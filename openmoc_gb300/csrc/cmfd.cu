@@ -22,9 +22,10 @@ namespace {
 
 constexpr int kPairThreads = 256;
 constexpr int kSolveThreads = 512;
-// shared memory for the solve's vectors (x and four sources): up to 120 KB,
+// shared memory for the solve's vectors: up to 120 KB,
 // leaving the rest of the SM's 256 KB to L1 for the matrices
 constexpr int kSolveSmemMax = 120 * 1024;
+constexpr int kSmemVecs = 8;   // x, two sources, two SOR sources, rhs, two dd sources
 constexpr float kZeroSigmaT = 1e-6f;          // src/constants.h:34
 constexpr double kFluxEps = 1e-25;            // src/constants.h:15
 constexpr double kLinalgTol = 1e-7;           // LINALG_TOL, FP32 build
@@ -103,6 +104,7 @@ struct Work {
   float *J;                                               // [C][4][E]
   float *A, *nb, *M;                                      // [C][E][E], [C][4][E]
   float *x, *src_a, *src_b, *ls_a, *ls_b;                 // [C][E]
+  float *rhs, *dd_a, *dd_b, *ddv;                         // [C][E]
 };
 
 __device__ Work carve(float* w, int C, int E) {
@@ -124,7 +126,11 @@ __device__ Work carve(float* w, int C, int E) {
   k.src_a = w; w += CE;
   k.src_b = w; w += CE;
   k.ls_a = w; w += CE;
-  k.ls_b = w;
+  k.ls_b = w; w += CE;
+  k.rhs = w; w += CE;
+  k.dd_a = w; w += CE;
+  k.dd_b = w; w += CE;
+  k.ddv = w;
   return k;
 }
 
@@ -335,6 +341,103 @@ __device__ void sor_half(const CmfdArgs& a, const Work& k, const float* b,
   }
 }
 
+// linearSolve (src/linalg.cpp:179-385): red-black SOR on A x = b until the
+// fission source settles; false when it diverges or does not converge.
+// Uniform across the block (every branch depends on block-wide values).
+__device__ bool linear_solve(const CmfdArgs& a, const Work& k, const float* b,
+                             double tol, double* red, int& sweeps) {
+  tol = fmax(kLinalgTol, tol);
+  float* ls_old = k.ls_a;
+  float* ls_new = k.ls_b;
+  mat_fission(a, k, k.x, ls_old);
+  __syncthreads();
+  double lres = 0.0, linit = 0.0, min_res = 1e6;
+  int li = 0;
+  while (li < kMaxLinearIters) {
+    sor_half(a, k, b, 0);
+    __syncthreads();
+    sor_half(a, k, b, 1);
+    __syncthreads();
+    sweeps++;
+    // the new fission source is read at the first sweep and from the 25th
+    // on (residuals and the copy to the old source)
+    if (li == 0 || li + 1 >= kMinIters) {
+      mat_fission(a, k, k.x, ls_new);
+      __syncthreads();
+    }
+    if (li == 0) {
+      lres = rmse(a, ls_new, ls_old, red);
+      linit = lres;
+    }
+    li++;
+    if (li > kMinIters) {
+      lres = rmse(a, ls_new, ls_old, red);
+      min_res = fmin(min_res, lres);
+      if ((lres > 1e3 * min_res && min_res > 1e-10) || !isfinite(lres))
+        return false;
+      const double q = linit > 0.0 ? lres / linit : INFINITY;
+      if (q < 0.1 || lres < tol) return true;
+    }
+    if (li > kMinIters - 1 && li < kMaxLinearIters) {
+      float* t = ls_old;
+      ls_old = ls_new;
+      ls_new = t;
+    }
+    if (sweeps >= kMaxSweeps) return false;
+    __syncthreads();   // ls_new is rewritten by the next sweep
+  }
+  return false;
+}
+
+// ddLinearSolve (src/linalg.cpp:717-900): A made diagonally dominant by
+// adding dd = max(0, sum |off-diagonal| - diagonal) to each diagonal, the
+// difference moved to the right side (b + dd x) and linearSolve repeated
+// until the fission source settles; A is restored on success.
+__device__ bool dd_linear_solve(const CmfdArgs& a, const Work& k,
+                                const float* b, double tol, double* red,
+                                int& sweeps) {
+  const int E = a.E, CE = a.C * a.E;
+  for (int r = threadIdx.x; r < CE; r += blockDim.x) {
+    const int c = r / E, e = r % E;
+    float* arow = k.A + (int64_t) r * E;
+    double sum = 0.0;
+    for (int g = 0; g < E; g++)
+      if (g != e) sum += fabsf(arow[g]);
+    for (int f = 0; f < 4; f++) sum += fabsf(k.nb[((int64_t) c * 4 + f) * E + e]);
+    const float dd = sum > (double) arow[e] ? (float) (sum - arow[e]) : 0.0f;
+    k.ddv[r] = dd;
+    arow[e] += dd;
+  }
+  __syncthreads();
+  float* old_src = k.dd_a;
+  float* new_src = k.dd_b;
+  mat_fission(a, k, k.x, new_src);
+  __syncthreads();
+  double initial = 0.0, min_res = 1e6;
+  for (int it = 0; it < kMaxLinearIters; it++) {
+    float* t = old_src;
+    old_src = new_src;
+    new_src = t;
+    for (int r = threadIdx.x; r < CE; r += blockDim.x)
+      k.rhs[r] = b[r] + k.ddv[r] * k.x[r];
+    __syncthreads();
+    linear_solve(a, k, k.rhs, tol, red, sweeps);   // a failure is only noted
+    mat_fission(a, k, k.x, new_src);
+    __syncthreads();
+    const double res = rmse(a, new_src, old_src, red);
+    if (it == 0) initial = res < 1e-14 ? 1e-10 : res;
+    min_res = fmin(min_res, res);
+    if ((res > 1e3 * min_res && min_res > 1e-10) || !isfinite(res))
+      return false;
+    if (res / initial < 0.1 || res < tol) break;
+    if (sweeps >= kMaxSweeps) return false;
+  }
+  for (int r = threadIdx.x; r < CE; r += blockDim.x)
+    k.A[(int64_t) r * E + r % E] -= k.ddv[r];
+  __syncthreads();
+  return true;
+}
+
 __global__ void __launch_bounds__(kSolveThreads, 1)
 cmfd_solve_kernel(const CmfdArgs a, int vec_in_smem) {
   DevScalars* sc = a.sc;
@@ -352,6 +455,9 @@ cmfd_solve_kernel(const CmfdArgs a, int vec_in_smem) {
     k.src_b = s_vec + 2 * CE;
     k.ls_a = s_vec + 3 * CE;
     k.ls_b = s_vec + 4 * CE;
+    k.rhs = s_vec + 5 * CE;
+    k.dd_a = s_vec + 6 * CE;
+    k.dd_b = s_vec + 7 * CE;
   }
   CmfdDevState* cm = a.cm;
   const int it = sc->iteration;                 // MOC iteration
@@ -386,55 +492,16 @@ cmfd_solve_kernel(const CmfdArgs a, int vec_in_smem) {
     }
     __syncthreads();
     double initial = 0.0;
+    bool dd_mode = false;
     for (power = 0; power < kMaxPowerIters; power++) {
-      // ---- linearSolve (src/linalg.cpp:179-385): red-black SOR on
-      // A x = src_old
-      float* ls_old = k.ls_a;
-      float* ls_new = k.ls_b;
-      mat_fission(a, k, k.x, ls_old);
-      __syncthreads();
-      double lres = 0.0, linit = 0.0, min_res = 1e6;
-      int li = 0;
-      bool ok = true;
-      while (li < kMaxLinearIters) {
-        sor_half(a, k, src_old, 0);
-        __syncthreads();
-        sor_half(a, k, src_old, 1);
-        __syncthreads();
-        sweeps++;
-        // the new fission source is read at the first sweep and from the
-        // 25th on (residuals and the copy to the old source)
-        if (li == 0 || li + 1 >= kMinIters) {
-          mat_fission(a, k, k.x, ls_new);
-          __syncthreads();
-        }
-        if (li == 0) {
-          lres = rmse(a, ls_new, ls_old, red);
-          linit = lres;
-        }
-        li++;
-        if (li > kMinIters) {
-          lres = rmse(a, ls_new, ls_old, red);
-          min_res = fmin(min_res, lres);
-          if ((lres > 1e3 * min_res && min_res > 1e-10) || !isfinite(lres)) {
-            ok = false;
-            break;
-          }
-          const double q = linit > 0.0 ? lres / linit : INFINITY;
-          if (q < 0.1 || lres < lin_tol) break;
-        }
-        if (li > kMinIters - 1 && li < kMaxLinearIters) {
-          float* t = ls_old;
-          ls_old = ls_new;
-          ls_new = t;
-        }
-        if (sweeps >= kMaxSweeps) {
-          ok = false;
-          break;
-        }
-        __syncthreads();   // ls_new is rewritten by the next sweep
+      // eigenvalueSolve's linear solves: plain, or diagonally dominated
+      // from the first failure on
+      bool ok = false;
+      if (!dd_mode) ok = linear_solve(a, k, src_old, lin_tol, red, sweeps);
+      if (!ok) {
+        dd_mode = true;
+        ok = dd_linear_solve(a, k, src_old, lin_tol, red, sweeps);
       }
-      if (li == kMaxLinearIters) ok = false;
       if (!ok) {
         failed = true;
         break;
@@ -529,7 +596,7 @@ int sm_count() {
 
 int64_t cmfd_work_floats(int C, int E) {
   const int64_t CE = (int64_t) C * E;
-  return 12 * CE + 3 * CE * E + 8 * CE;
+  return 16 * CE + 3 * CE * E + 8 * CE;
 }
 
 void launch_cmfd_pair_sums(const float* phi, const float* vol,
@@ -549,7 +616,7 @@ void launch_cmfd_solve(const CmfdArgs& a, cudaStream_t s) {
   // one thread per cell of a colour, at least four warps
   int threads = (std::max(a.n_color0, a.C - a.n_color0) + 31) / 32 * 32;
   threads = std::max(128, std::min(kSolveThreads, threads));
-  const int64_t vec_bytes = (int64_t) 5 * a.C * a.E * sizeof(float);
+  const int64_t vec_bytes = (int64_t) kSmemVecs * a.C * a.E * sizeof(float);
   const int in_smem = vec_bytes <= kSolveSmemMax ? 1 : 0;
   const int smem = in_smem ? (int) vec_bytes : 0;
   static int configured = 0;

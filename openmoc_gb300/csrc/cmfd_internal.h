@@ -81,6 +81,8 @@ class Solver {
   void fission(const std::vector<double>& x, std::vector<double>& out) const;
   bool linear_solve(std::vector<double>& x, const std::vector<double>& b,
                     double tol);
+  bool dd_linear_solve(std::vector<double>& x, const std::vector<double>& b,
+                       double tol);
   double eigen_solve(std::vector<double>& x, double k, double tol);
   int neighbour(int cell, int face) const;
 };

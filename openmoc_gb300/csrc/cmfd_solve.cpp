@@ -313,6 +313,47 @@ bool Solver::linear_solve(std::vector<double>& x, const std::vector<double>& b,
   return ok;
 }
 
+// ddLinearSolve (src/linalg.cpp:717-900): A made diagonally dominant by
+// dd = max(0, sum |off-diagonal| - diagonal) on each diagonal, the
+// difference moved to the right side (b + dd x), linear solves repeated
+// until the fission source settles; A restored on success.
+bool Solver::dd_linear_solve(std::vector<double>& x,
+                             const std::vector<double>& b, double tol) {
+  const int C = cfg.cells(), E = cfg.E;
+  std::vector<double> dd((size_t) C * E, 0.0), rhs((size_t) C * E);
+  for (int c = 0; c < C; c++)
+    for (int e = 0; e < E; e++) {
+      const size_t r = (size_t) c * E + e;
+      double* row = a_blk.data() + r * E;
+      double sum = 0.0;
+      for (int g = 0; g < E; g++)
+        if (g != e) sum += std::fabs(row[g]);
+      for (int f = 0; f < kFaces; f++)
+        sum += std::fabs(a_nb[((size_t) c * kFaces + f) * E + e]);
+      if (sum > row[e]) dd[r] = sum - row[e];
+      row[e] += dd[r];
+    }
+  std::vector<double> old_src, new_src;
+  fission(x, new_src);
+  double initial = 0.0, min_res = 1e6;
+  for (int it = 0; it < kMaxLinearIters; it++) {
+    old_src = new_src;
+    for (size_t r = 0; r < rhs.size(); r++) rhs[r] = b[r] + dd[r] * x[r];
+    linear_solve(x, rhs, tol);      // a failure is only noted
+    fission(x, new_src);
+    const double res = rmse_integrated(new_src, old_src, C, E);
+    if (it == 0) initial = res < 1e-14 ? 1e-10 : res;
+    min_res = std::min(min_res, res);
+    if ((res > 1e3 * min_res && min_res > 1e-10) || !std::isfinite(res))
+      return false;
+    if (res / initial < 0.1 || res < tol) break;
+  }
+  for (int c = 0; c < C; c++)
+    for (int e = 0; e < E; e++)
+      a_blk[((size_t) c * E + e) * E + e] -= dd[(size_t) c * E + e];
+  return true;
+}
+
 // Power iteration; returns keff, or -1 when a linear solve fails.
 double Solver::eigen_solve(std::vector<double>& x, double k, double tol) {
   const int C = cfg.cells(), E = cfg.E;
@@ -327,8 +368,15 @@ double Solver::eigen_solve(std::vector<double>& x, double k, double tol) {
   for (double& v : x) v *= rows * k / s;
   double initial = 0.0;
   int iter;
+  bool dd_mode = false;
   for (iter = 0; iter < kMaxPowerIters; iter++) {
-    if (!linear_solve(x, old_src, tol * 1e-1)) {
+    // plain linear solves, diagonally dominated from the first failure on
+    bool ok = !dd_mode && linear_solve(x, old_src, tol * 1e-1);
+    if (!ok) {
+      dd_mode = true;
+      ok = dd_linear_solve(x, old_src, tol * 1e-1);
+    }
+    if (!ok) {
       stats.power_iterations = iter + 1;
       return -1.0;
     }

@@ -17,9 +17,10 @@ Each step follows the reference, per FSR as the reference loops:
     correction at the first iteration;
   * Cmfd::constructMatrices (src/Cmfd.cpp:1353-1500), entries below
     FLT_EPSILON dropped as there;
-  * eigenvalueSolve / linearSolve (src/linalg.cpp:25-176, 179-385): power
-    iteration over red-black SOR with computeRMSE's integrated residual,
-    at least 25 iterations of each, stop ratios 0.03 and 0.1;
+  * eigenvalueSolve / linearSolve / ddLinearSolve (src/linalg.cpp:25-176,
+    179-385, 717-900): power iteration over red-black SOR with
+    computeRMSE's integrated residual, at least 25 iterations of each, stop
+    ratios 0.03 and 0.1, the diagonally dominated solve after a failure;
   * Cmfd::rescaleFlux and Cmfd::updateMOCFlux (src/Cmfd.cpp:1304-1350,
     1509-1560): ratios of new to old coarse flux, bounded to [0.05, 20]
     after the unbounded iterations;
@@ -259,6 +260,31 @@ class CmfdOracle:
                 old_src = new_src
         return it < 10000, it
 
+    def _dd_linear_solve(self, A, nb, Mm, x, b, tol):
+        """ddLinearSolve (src/linalg.cpp:717-900)."""
+        E = self.E
+        idx = np.arange(E)
+        off = np.abs(A).sum(2) - np.abs(A[:, idx, idx]) + np.abs(nb).sum(1)
+        diag = A[:, idx, idx]
+        dd = np.where(off > diag, off - diag, 0.0)
+        A = A.copy()
+        A[:, idx, idx] += dd
+        new_src = np.einsum("ceg,cg->ce", Mm, x)
+        initial, min_res = 0.0, 1e6
+        for it in range(10000):
+            old_src = new_src
+            self._linear_solve(A, nb, Mm, x, b + dd * x, tol)
+            new_src = np.einsum("ceg,cg->ce", Mm, x)
+            res = self._rmse(new_src, old_src)
+            if it == 0:
+                initial = res if res >= 1e-14 else 1e-10
+            min_res = min(min_res, res)
+            if (res > 1e3 * min_res and min_res > 1e-10) or not np.isfinite(res):
+                return False
+            if res / initial < 0.1 or res < tol:
+                break
+        return True
+
     def _eigen_solve(self, A, nb, Mm, x, k, tol):
         tol = max(self.tol_min, tol)
         rows = x.size
@@ -267,8 +293,14 @@ class CmfdOracle:
         old_src *= rows / s
         x *= rows * k / s
         initial = 0.0
+        dd_mode = False
         for it in range(25000):
-            ok, _ = self._linear_solve(A, nb, Mm, x, old_src, tol * 1e-1)
+            ok = False
+            if not dd_mode:
+                ok, _ = self._linear_solve(A, nb, Mm, x, old_src, tol * 1e-1)
+            if not ok:
+                dd_mode = True
+                ok = self._dd_linear_solve(A, nb, Mm, x, old_src, tol * 1e-1)
             if not ok:
                 return -1.0, it + 1
             new_src = np.einsum("ceg,cg->ce", Mm, x)
