@@ -32,6 +32,12 @@ constexpr double kLinalgTol = 1e-7;           // LINALG_TOL, FP32 build
 constexpr int kMinIters = 25;                 // src/constants.h:74-81
 constexpr int kMaxPowerIters = 25000;
 constexpr int kMaxLinearIters = 10000;
+// Divergence of a linear solve is a thousandfold rise of the fission-source
+// change over its minimum (src/linalg.cpp:345-356); in FP32 a minimum below
+// the single-precision resolution is rounding noise, not a trend, so the
+// minimum must also exceed this floor (the reference's floor, 1e-10, is
+// meant for its double build).
+constexpr double kNoiseFloor = 1e-7;
 // Bound on the SOR sweeps of one coarse solve (about 0.1 s): past it the
 // solve counts as failed and the MOC iteration goes on without prolongation.
 constexpr int kMaxSweeps = 200000;
@@ -373,7 +379,7 @@ __device__ bool linear_solve(const CmfdArgs& a, const Work& k, const float* b,
     if (li > kMinIters) {
       lres = rmse(a, ls_new, ls_old, red);
       min_res = fmin(min_res, lres);
-      if ((lres > 1e3 * min_res && min_res > 1e-10) || !isfinite(lres))
+      if ((lres > 1e3 * min_res && min_res > kNoiseFloor) || !isfinite(lres))
         return false;
       const double q = linit > 0.0 ? lres / linit : INFINITY;
       if (q < 0.1 || lres < tol) return true;
@@ -427,7 +433,7 @@ __device__ bool dd_linear_solve(const CmfdArgs& a, const Work& k,
     const double res = rmse(a, new_src, old_src, red);
     if (it == 0) initial = res < 1e-14 ? 1e-10 : res;
     min_res = fmin(min_res, res);
-    if ((res > 1e3 * min_res && min_res > 1e-10) || !isfinite(res))
+    if ((res > 1e3 * min_res && min_res > kNoiseFloor) || !isfinite(res))
       return false;
     if (res / initial < 0.1 || res < tol) break;
     if (sweeps >= kMaxSweeps) return false;
