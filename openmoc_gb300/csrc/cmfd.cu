@@ -38,6 +38,12 @@ constexpr int kMaxLinearIters = 10000;
 // minimum must also exceed this floor (the reference's floor, 1e-10, is
 // meant for its double build).
 constexpr double kNoiseFloor = 1e-7;
+// Near convergence an FP32 iterate stops changing except for rounding: the
+// measured change then hovers at the single-precision resolution and may
+// never drop below the tolerance.  A change below kStallMax that has not
+// halved over kStallWindow checks counts as converged.
+constexpr double kStallMax = 1e-6;
+constexpr int kStallWindow = 8;
 // Bound on the SOR sweeps of one coarse solve (about 0.1 s): past it the
 // solve counts as failed and the MOC iteration goes on without prolongation.
 constexpr int kMaxSweeps = 200000;
@@ -357,8 +363,8 @@ __device__ bool linear_solve(const CmfdArgs& a, const Work& k, const float* b,
   float* ls_new = k.ls_b;
   mat_fission(a, k, k.x, ls_old);
   __syncthreads();
-  double lres = 0.0, linit = 0.0, min_res = 1e6;
-  int li = 0;
+  double lres = 0.0, linit = 0.0, min_res = 1e6, stall_res = INFINITY;
+  int li = 0, stall_li = 0;
   while (li < kMaxLinearIters) {
     sor_half(a, k, b, 0);
     __syncthreads();
@@ -383,6 +389,11 @@ __device__ bool linear_solve(const CmfdArgs& a, const Work& k, const float* b,
         return false;
       const double q = linit > 0.0 ? lres / linit : INFINITY;
       if (q < 0.1 || lres < tol) return true;
+      if (li - stall_li >= kStallWindow) {
+        if (lres < kStallMax && lres > 0.5 * stall_res) return true;
+        stall_res = lres;
+        stall_li = li;
+      }
     }
     if (li > kMinIters - 1 && li < kMaxLinearIters) {
       float* t = ls_old;
@@ -419,7 +430,8 @@ __device__ bool dd_linear_solve(const CmfdArgs& a, const Work& k,
   float* new_src = k.dd_b;
   mat_fission(a, k, k.x, new_src);
   __syncthreads();
-  double initial = 0.0, min_res = 1e6;
+  double initial = 0.0, min_res = 1e6, stall_res = INFINITY;
+  int stall_it = 0;
   for (int it = 0; it < kMaxLinearIters; it++) {
     float* t = old_src;
     old_src = new_src;
@@ -436,6 +448,11 @@ __device__ bool dd_linear_solve(const CmfdArgs& a, const Work& k,
     if ((res > 1e3 * min_res && min_res > kNoiseFloor) || !isfinite(res))
       return false;
     if (res / initial < 0.1 || res < tol) break;
+    if (it - stall_it >= kStallWindow) {
+      if (res < kStallMax && res > 0.5 * stall_res) break;
+      stall_res = res;
+      stall_it = it;
+    }
     if (sweeps >= kMaxSweeps) return false;
   }
   for (int r = threadIdx.x; r < CE; r += blockDim.x)
@@ -497,7 +514,8 @@ cmfd_solve_kernel(const CmfdArgs a, int vec_in_smem) {
       k.x[r] = (float) (k.x[r] * (rows * keff / s0));
     }
     __syncthreads();
-    double initial = 0.0;
+    double initial = 0.0, stall_res = INFINITY;
+    int stall_p = 0;
     bool dd_mode = false;
     for (power = 0; power < kMaxPowerIters; power++) {
       // eigenvalueSolve's linear solves: plain, or diagonally dominated
@@ -526,6 +544,14 @@ cmfd_solve_kernel(const CmfdArgs a, int vec_in_smem) {
       if ((res / initial < 0.03 || res < kLinalgTol) && power > kMinIters) {
         power++;
         break;
+      }
+      if (power > kMinIters && power - stall_p >= kStallWindow) {
+        if (res < kStallMax && res > 0.5 * stall_res) {
+          power++;
+          break;
+        }
+        stall_res = res;
+        stall_p = power;
       }
       __syncthreads();
     }
