@@ -412,7 +412,9 @@ def cmfd_acceleration(p, device, tol=1e-5):
                      "ms_per_iteration": 1e3 * dt / max(1, s.getNumIterations()),
                      "keff": s.getKeff()}
         if use:
-            res[name]["coarse_power_iterations_last"] = s.getCmfdInfo()["power_iterations"]
+            info = s.getCmfdInfo()
+            res[name]["coarse_power_iterations_last"] = info["power_iterations"]
+            res[name]["coarse_sor_sweeps_last"] = info["linear_iterations"]
         s.close()
     res["speedup"] = res["plain"]["seconds"] / res["cmfd"]["seconds"]
     res["keff_difference"] = res["cmfd"]["keff"] - res["plain"]["keff"]

@@ -22,10 +22,8 @@ namespace {
 
 constexpr int kPairThreads = 256;
 constexpr int kSolveThreads = 512;
-// shared memory for the solve's vectors: up to 120 KB,
-// leaving the rest of the SM's 256 KB to L1 for the matrices
-constexpr int kSolveSmemMax = 120 * 1024;
-constexpr int kSmemVecs = 8;   // x, two sources, two SOR sources, rhs, two dd sources
+// shared memory for the coarse system (vectors, A and couplings)
+constexpr int kSolveSmemMax = 216 * 1024;
 constexpr float kZeroSigmaT = 1e-6f;          // src/constants.h:34
 constexpr double kFluxEps = 1e-25;            // src/constants.h:15
 constexpr double kLinalgTol = 1e-7;           // LINALG_TOL, FP32 build
@@ -110,40 +108,51 @@ __device__ double block_sum(double v, double* red) {
   return t;
 }
 
+// The coarse system lives in colour order: j is a cell's position in the
+// list of red cells ((ix + iy) even) followed by black ones, so that the
+// threads of a half sweep take consecutive j.  Arrays are group-major:
+// vector element (e, j) at e * C + j, A(e, g) of cell j at (e * E + g) * C +
+// j, the coupling of face f at (f * E + e) * C + j, so a warp's loads are
+// contiguous.  The collapse works per cell, in cell order.
 struct Work {
-  float *sig_t, *nu_f, *chi, *dif, *dlx, *dly, *phi_c;   // [C][E]
-  float *sig_s;                                           // [C][E][E] e -> g
-  float *J;                                               // [C][4][E]
-  float *A, *nb, *M;                                      // [C][E][E], [C][4][E]
-  float *x, *src_a, *src_b, *ls_a, *ls_b;                 // [C][E]
-  float *rhs, *dd_a, *dd_b, *ddv;                         // [C][E]
+  // cell order [C][E] ([C][E][E] for sig_s, [C][4][E] for J)
+  float *sig_t, *nu_f, *chi, *dif, *dlx, *dly, *phi_c, *sig_s, *J;
+  // colour order
+  float *A, *nb, *M;                                  // [E][E][C], [4][E][C]
+  float *x, *phi_t, *src_a, *src_b, *ls_a, *ls_b;     // [E][C]
+  float *rhs, *dd_a, *dd_b, *ddv;                     // [E][C]
 };
+
+constexpr int kColourVecs = 10;   // x .. ddv
 
 __device__ Work carve(float* w, int C, int E) {
   const int64_t CE = (int64_t) C * E, CEE = CE * E, C4E = 4 * CE;
   Work k;
-  k.sig_t = w; w += CE;
-  k.nu_f = w; w += CE;
-  k.chi = w; w += CE;
-  k.dif = w; w += CE;
-  k.dlx = w; w += CE;
-  k.dly = w; w += CE;
-  k.phi_c = w; w += CE;
+  float** cell_order[] = {&k.sig_t, &k.nu_f, &k.chi, &k.dif, &k.dlx, &k.dly,
+                          &k.phi_c};
+  for (float** p : cell_order) { *p = w; w += CE; }
   k.sig_s = w; w += CEE;
   k.J = w; w += C4E;
   k.A = w; w += CEE;
   k.nb = w; w += C4E;
   k.M = w; w += CEE;
-  k.x = w; w += CE;
-  k.src_a = w; w += CE;
-  k.src_b = w; w += CE;
-  k.ls_a = w; w += CE;
-  k.ls_b = w; w += CE;
-  k.rhs = w; w += CE;
-  k.dd_a = w; w += CE;
-  k.dd_b = w; w += CE;
-  k.ddv = w;
+  float** vecs[] = {&k.x, &k.phi_t, &k.src_a, &k.src_b, &k.ls_a, &k.ls_b,
+                    &k.rhs, &k.dd_a, &k.dd_b, &k.ddv};
+  for (float** p : vecs) { *p = w; w += CE; }
   return k;
+}
+
+// Shared memory: level 2 holds the colour-order vectors, A and the
+// couplings; level 1 the vectors only; level 0 nothing (all in global).
+__device__ void place_in_smem(Work& k, float* s, int level, int C, int E) {
+  if (level < 1) return;
+  const int64_t CE = (int64_t) C * E;
+  float** vecs[] = {&k.x, &k.phi_t, &k.src_a, &k.src_b, &k.ls_a, &k.ls_b,
+                    &k.rhs, &k.dd_a, &k.dd_b, &k.ddv};
+  for (float** p : vecs) { *p = s; s += CE; }
+  if (level < 2) return;
+  k.A = s; s += CE * E;
+  k.nb = s;
 }
 
 __device__ __forceinline__ int neighbour(const CmfdArgs& a, int c, int f) {
@@ -169,16 +178,15 @@ __device__ float larsen(const CmfdArgs& a, float d, float delta) {
   return (float) (1.0 + delta * rho / (2.0 * d));
 }
 
-// out = M x, rows over the block (no barrier)
+// out = M x over all (e, j) (no barrier)
 __device__ void mat_fission(const CmfdArgs& a, const Work& k, const float* x,
                             float* out) {
-  const int E = a.E, CE = a.C * a.E;
+  const int E = a.E, C = a.C, CE = a.C * a.E;
   for (int r = threadIdx.x; r < CE; r += blockDim.x) {
-    const int c = r / E;
-    const float* m = k.M + (int64_t) r * E;
-    const float* xc = x + (int64_t) c * E;
+    const int e = r / C, j = r - e * C;
+    const float* m = k.M + (int64_t) e * E * C + j;
     float s = 0.0f;
-    for (int g = 0; g < E; g++) s += m[g] * xc[g];
+    for (int g = 0; g < E; g++) s += m[(int64_t) g * C] * x[g * C + j];
     out[r] = s;
   }
 }
@@ -193,11 +201,11 @@ __device__ double block_total(const float* v, int n, double* red) {
 __device__ double rmse(const CmfdArgs& a, const float* x, const float* y,
                        double* red) {
   double part = 0.0;
-  for (int c = threadIdx.x; c < a.C; c += blockDim.x) {
+  for (int j = threadIdx.x; j < a.C; j += blockDim.x) {
     double s = 0.0, t = 0.0;
     for (int e = 0; e < a.E; e++) {
-      s += x[c * a.E + e];
-      t += y[c * a.E + e];
+      s += x[e * a.C + j];
+      t += y[e * a.C + j];
     }
     if (fabs(t) > kFluxEps) {
       const float r = (float) ((s - t) / t);
@@ -266,19 +274,21 @@ __device__ void collapse_one(const CmfdArgs& a, const Work& k, int c, int e) {
 }
 
 // Cmfd::getSurfaceDiffusionCoefficient and Cmfd::constructMatrices
-// (src/Cmfd.cpp:1048-1170, 1353-1500): row (c, e) of A and M.
+// (src/Cmfd.cpp:1048-1170, 1353-1500): row (c, e) of A and M, written in
+// colour order.
 __device__ void build_row(const CmfdArgs& a, const Work& k, int c, int e,
                           int it, bool valid) {
-  const int E = a.E;
+  const int E = a.E, C = a.C;
   const int ce = c * E + e;
+  const int j = a.cell_pos[c];
   const int ix = c % a.nx, iy = c / a.nx;
   const float V = a.cell_vol[c];
-  float* row = k.A + (int64_t) ce * E;
+  float* arow = k.A + (int64_t) e * E * C + j;        // A(e, g) at g * C
   for (int g = 0; g < E; g++) {
     const float v = -k.sig_s[((int64_t) c * E + g) * E + e] * V;
-    row[g] = fabsf(v) > FLT_EPSILON ? v : 0.0f;
+    arow[(int64_t) g * C] = fabsf(v) > FLT_EPSILON ? v : 0.0f;
   }
-  float diag = row[e] + k.sig_t[ce] * V;
+  float diag = arow[(int64_t) e * C] + k.sig_t[ce] * V;
   const float flux = k.phi_c[ce];
   for (int f = 0; f < 4; f++) {
     const bool xf = (f == 0 || f == 2);
@@ -315,40 +325,40 @@ __device__ void build_row(const CmfdArgs& a, const Work& k, int c, int e,
     if (it == 0) dt = 0.0f;
     *old = dt;
     diag += (dh - dt) * width;
-    k.nb[((int64_t) c * 4 + f) * E + e] = n >= 0 ? -(dh + dt) * width : 0.0f;
+    k.nb[((int64_t) f * E + e) * C + j] = n >= 0 ? -(dh + dt) * width : 0.0f;
   }
-  row[e] = diag;
-  float* mrow = k.M + (int64_t) ce * E;
+  arow[(int64_t) e * C] = diag;
+  float* mrow = k.M + (int64_t) e * E * C + j;
   for (int g = 0; g < E; g++) {
     const float v = k.chi[ce] * k.nu_f[c * E + g] * V;
-    mrow[g] = fabsf(v) > FLT_EPSILON ? v : 0.0f;
+    mrow[(int64_t) g * C] = fabsf(v) > FLT_EPSILON ? v : 0.0f;
   }
-  k.x[ce] = flux;                  // the collapsed flux starts the solve
+  k.x[e * C + j] = flux;           // the collapsed flux starts the solve
+  k.phi_t[e * C + j] = flux;
 }
 
-// One red-black half sweep of SOR over the cells of `color`.
+// One red-black half sweep of SOR over the cells of `color` (colour order:
+// red j < n_color0, black after), groups in order within a cell.
 __device__ void sor_half(const CmfdArgs& a, const Work& k, const float* b,
                          int color) {
-  const int E = a.E;
+  const int E = a.E, C = a.C;
   const float w = a.sor;
   const int j0 = color ? a.n_color0 : 0;
   const int j1 = color ? a.C : a.n_color0;
   for (int j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
-    const int c = a.color_cells[j];
-    int nbc[4];
-    for (int f = 0; f < 4; f++) nbc[f] = neighbour(a, c, f);
+    int nbj[4];
+    for (int f = 0; f < 4; f++) nbj[f] = a.nbr_j[f * C + j];
     for (int e = 0; e < E; e++) {
-      const int r = c * E + e;
-      const float* arow = k.A + (int64_t) r * E;
-      const float d = arow[e];
-      float v = (1.0f - w) * k.x[r] * (d / w);
+      const float* arow = k.A + (int64_t) e * E * C + j;
+      const float d = arow[(int64_t) e * C];
+      float v = (1.0f - w) * k.x[e * C + j] * (d / w);
       for (int g = 0; g < E; g++)
-        if (g != e) v -= arow[g] * k.x[c * E + g];
+        if (g != e) v -= arow[(int64_t) g * C] * k.x[g * C + j];
       for (int f = 0; f < 4; f++)
-        if (nbc[f] >= 0)
-          v -= k.nb[((int64_t) c * 4 + f) * E + e] * k.x[nbc[f] * E + e];
-      v += b[r];
-      k.x[r] = v * (w / d);
+        if (nbj[f] >= 0)
+          v -= k.nb[((int64_t) f * E + e) * C + j] * k.x[e * C + nbj[f]];
+      v += b[e * C + j];
+      k.x[e * C + j] = v * (w / d);
     }
   }
 }
@@ -413,17 +423,18 @@ __device__ bool linear_solve(const CmfdArgs& a, const Work& k, const float* b,
 __device__ bool dd_linear_solve(const CmfdArgs& a, const Work& k,
                                 const float* b, double tol, double* red,
                                 int& sweeps) {
-  const int E = a.E, CE = a.C * a.E;
-  for (int r = threadIdx.x; r < CE; r += blockDim.x) {
-    const int c = r / E, e = r % E;
-    float* arow = k.A + (int64_t) r * E;
+  const int E = a.E, C = a.C, CE = a.C * a.E;
+  for (int r = threadIdx.x; r < CE; r += blockDim.x) {   // r = e * C + j
+    const int e = r / C, j = r - e * C;
+    float* arow = k.A + (int64_t) e * E * C + j;
     double sum = 0.0;
     for (int g = 0; g < E; g++)
-      if (g != e) sum += fabsf(arow[g]);
-    for (int f = 0; f < 4; f++) sum += fabsf(k.nb[((int64_t) c * 4 + f) * E + e]);
-    const float dd = sum > (double) arow[e] ? (float) (sum - arow[e]) : 0.0f;
+      if (g != e) sum += fabsf(arow[(int64_t) g * C]);
+    for (int f = 0; f < 4; f++) sum += fabsf(k.nb[((int64_t) f * E + e) * C + j]);
+    const float diag = arow[(int64_t) e * C];
+    const float dd = sum > (double) diag ? (float) (sum - diag) : 0.0f;
     k.ddv[r] = dd;
-    arow[e] += dd;
+    arow[(int64_t) e * C] = diag + dd;
   }
   __syncthreads();
   float* old_src = k.dd_a;
@@ -455,33 +466,24 @@ __device__ bool dd_linear_solve(const CmfdArgs& a, const Work& k,
     }
     if (sweeps >= kMaxSweeps) return false;
   }
-  for (int r = threadIdx.x; r < CE; r += blockDim.x)
-    k.A[(int64_t) r * E + r % E] -= k.ddv[r];
+  for (int r = threadIdx.x; r < CE; r += blockDim.x) {
+    const int e = r / C, j = r - e * C;
+    k.A[((int64_t) e * E + e) * C + j] -= k.ddv[r];
+  }
   __syncthreads();
   return true;
 }
 
 __global__ void __launch_bounds__(kSolveThreads, 1)
-cmfd_solve_kernel(const CmfdArgs a, int vec_in_smem) {
+cmfd_solve_kernel(const CmfdArgs a, int smem_level) {
   DevScalars* sc = a.sc;
   if (*(volatile int*) &sc->done) return;
   __shared__ double red[32];
-  extern __shared__ float s_vec[];
+  extern __shared__ float s_dyn[];
   const int C = a.C, E = a.E;
   const int CE = C * E;
   Work k = carve(a.work, C, E);
-  if (vec_in_smem) {
-    // the iterate and the source vectors, rewritten every sweep, in shared
-    // memory; the matrices, read only, stay in L1
-    k.x = s_vec;
-    k.src_a = s_vec + CE;
-    k.src_b = s_vec + 2 * CE;
-    k.ls_a = s_vec + 3 * CE;
-    k.ls_b = s_vec + 4 * CE;
-    k.rhs = s_vec + 5 * CE;
-    k.dd_a = s_vec + 6 * CE;
-    k.dd_b = s_vec + 7 * CE;
-  }
+  place_in_smem(k, s_dyn, smem_level, C, E);
   CmfdDevState* cm = a.cm;
   const int it = sc->iteration;                 // MOC iteration
   // the coarse tolerance follows the transport residual
@@ -574,19 +576,21 @@ cmfd_solve_kernel(const CmfdArgs a, int vec_in_smem) {
     return;
   }
   mat_fission(a, k, k.x, k.src_a);
-  mat_fission(a, k, k.phi_c, k.src_b);
+  mat_fission(a, k, k.phi_t, k.src_b);
   __syncthreads();
   const double sn = block_total(k.src_a, CE, red);
   const double so = block_total(k.src_b, CE, red);
   float far = 1.0f;
-  for (int r = threadIdx.x; r < CE; r += blockDim.x) {
+  for (int r = threadIdx.x; r < CE; r += blockDim.x) {   // r = e * C + j
+    const int e = r / C, j = r - e * C;
+    const int out = a.color_cells[j] * E + e;            // cell order
     const float xn = (float) (k.x[r] / sn);
-    const float xo = (float) (k.phi_c[r] / so);
+    const float xo = (float) (k.phi_t[r] / so);
     float q = fabs((double) xo) > kFluxEps ? xn / xo : 0.0f;
     if (it > a.unbounded) q = fminf(20.0f, fmaxf(0.05f, q));
-    a.ratio[r] = q;
-    a.flux_new[r] = xn;
-    a.flux_old[r] = xo;
+    a.ratio[out] = q;
+    a.flux_new[out] = xn;
+    a.flux_old[out] = xo;
     if (q > 0.0f && fabsf(logf(q)) > fabsf(logf(far))) far = q;
   }
   // the ratio farthest from 1 (log distance) over the block
@@ -628,7 +632,7 @@ int sm_count() {
 
 int64_t cmfd_work_floats(int C, int E) {
   const int64_t CE = (int64_t) C * E;
-  return 16 * CE + 3 * CE * E + 8 * CE;
+  return 7 * CE + 3 * CE * E + 8 * CE + 10 * CE;
 }
 
 void launch_cmfd_pair_sums(const float* phi, const float* vol,
@@ -648,9 +652,11 @@ void launch_cmfd_solve(const CmfdArgs& a, cudaStream_t s) {
   // one thread per cell of a colour, at least four warps
   int threads = (std::max(a.n_color0, a.C - a.n_color0) + 31) / 32 * 32;
   threads = std::max(128, std::min(kSolveThreads, threads));
-  const int64_t vec_bytes = (int64_t) kSmemVecs * a.C * a.E * sizeof(float);
-  const int in_smem = vec_bytes <= kSolveSmemMax ? 1 : 0;
-  const int smem = in_smem ? (int) vec_bytes : 0;
+  const int64_t CE = (int64_t) a.C * a.E;
+  const int64_t level1 = 4 * kColourVecs * CE;
+  const int64_t level2 = level1 + 4 * (CE * a.E + 4 * CE);
+  const int level = level2 <= kSolveSmemMax ? 2 : level1 <= kSolveSmemMax ? 1 : 0;
+  const int smem = level == 2 ? (int) level2 : level == 1 ? (int) level1 : 0;
   static int configured = 0;
   if (!configured) {
     cudaFuncSetAttribute(cmfd_solve_kernel,
@@ -658,7 +664,7 @@ void launch_cmfd_solve(const CmfdArgs& a, cudaStream_t s) {
                          kSolveSmemMax);
     configured = 1;
   }
-  cmfd_solve_kernel<<<1, threads, smem, s>>>(a, in_smem);
+  cmfd_solve_kernel<<<1, threads, smem, s>>>(a, level);
 }
 
 void launch_cmfd_prolong(float* phi, const int32_t* fsr_cell,

@@ -218,6 +218,8 @@ struct moc_ctx {
   float* cm_flux_new = nullptr;
   int32_t* cm_cell_pair = nullptr;
   int32_t* cm_color_cells = nullptr;
+  int32_t* cm_cell_pos = nullptr;
+  int32_t* cm_nbr_j = nullptr;
   int cm_n_color0 = 0;
   int32_t* cm_pair_mat = nullptr;
   float* cm_chi_m = nullptr;
@@ -708,6 +710,8 @@ void cmfd_release(moc_ctx* c) {
   dfree(c->cm_flux_new);
   dfree(c->cm_cell_pair);
   dfree(c->cm_color_cells);
+  dfree(c->cm_cell_pos);
+  dfree(c->cm_nbr_j);
   dfree(c->cm_pair_mat);
   dfree(c->cm_chi_m);
   dfree(c->cm_ss_m);
@@ -831,6 +835,18 @@ int cmfd_prepare(moc_ctx* c) {
     if (k == 0) c->cm_n_color0 = (int) colors.size();
   }
   MOC_TRY(up(&c->cm_color_cells, colors));
+  std::vector<int32_t> pos(C), nbr_j(4 * (size_t) C, -1);
+  for (int jj = 0; jj < C; jj++) pos[colors[jj]] = jj;
+  for (int jj = 0; jj < C; jj++) {
+    const int cell = colors[jj], ix = cell % cf.nx, iy = cell / cf.nx;
+    const int nb[4] = {ix > 0 ? cell - 1 : -1, iy > 0 ? cell - cf.nx : -1,
+                       ix + 1 < cf.nx ? cell + 1 : -1,
+                       iy + 1 < cf.ny ? cell + cf.nx : -1};
+    for (int f = 0; f < 4; f++)
+      nbr_j[(size_t) f * C + jj] = nb[f] >= 0 ? pos[nb[f]] : -1;
+  }
+  MOC_TRY(up(&c->cm_cell_pos, pos));
+  MOC_TRY(up(&c->cm_nbr_j, nbr_j));
   MOC_TRY(up(&c->cm_pair_mat, F.pair_mat));
   MOC_TRY(up(&c->cm_chi_m, chi_m));
   MOC_TRY(up(&c->cm_ss_m, ss_m));
@@ -882,6 +898,8 @@ moc::CmfdArgs cmfd_args(moc_ctx* c) {
   a.gstart = c->cm_gstart;
   a.cell_pair = c->cm_cell_pair;
   a.color_cells = c->cm_color_cells;
+  a.cell_pos = c->cm_cell_pos;
+  a.nbr_j = c->cm_nbr_j;
   a.n_color0 = c->cm_n_color0;
   a.pair_mat = c->cm_pair_mat;
   a.st = c->sigma_t;

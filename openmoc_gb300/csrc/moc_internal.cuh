@@ -329,6 +329,8 @@ struct CmfdArgs {
   const int32_t* gstart;        // [E + 1] first group of each coarse group
   const int32_t* cell_pair;     // [C + 1] pairs of each cell (cell-major)
   const int32_t* color_cells;   // [C] red cells ((ix + iy) even), then black
+  const int32_t* cell_pos;      // [C] position of each cell in color_cells
+  const int32_t* nbr_j;         // [4][C] neighbours by face, colour order
   int n_color0;
   const int32_t* pair_mat;      // [P]
   const float* st;              // [M][G] total cross sections
