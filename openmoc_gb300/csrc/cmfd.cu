@@ -178,15 +178,22 @@ __device__ float larsen(const CmfdArgs& a, float d, float delta) {
   return (float) (1.0 + delta * rho / (2.0 * d));
 }
 
-// out = M x over all (e, j) (no barrier)
+// out = M x over all (e, j) (no barrier); EC as in sor_half
+template <int EC>
 __device__ void mat_fission(const CmfdArgs& a, const Work& k, const float* x,
                             float* out) {
-  const int E = a.E, C = a.C, CE = a.C * a.E;
+  const int E = EC > 0 ? EC : a.E;
+  const int C = a.C, CE = a.C * E;
   for (int r = threadIdx.x; r < CE; r += blockDim.x) {
     const int e = r / C, j = r - e * C;
     const float* m = k.M + (int64_t) e * E * C + j;
     float s = 0.0f;
-    for (int g = 0; g < E; g++) s += m[(int64_t) g * C] * x[g * C + j];
+    if constexpr (EC > 0) {
+#pragma unroll
+      for (int g = 0; g < EC; g++) s += m[g * C] * x[g * C + j];
+    } else {
+      for (int g = 0; g < E; g++) s += m[(int64_t) g * C] * x[g * C + j];
+    }
     out[r] = s;
   }
 }
@@ -338,27 +345,55 @@ __device__ void build_row(const CmfdArgs& a, const Work& k, int c, int e,
 }
 
 // One red-black half sweep of SOR over the cells of `color` (colour order:
-// red j < n_color0, black after), groups in order within a cell.
+// red j < n_color0, black after), groups in order within a cell.  EC > 0:
+// the coarse group count fixed at compile time (loops unrolled, the cell's
+// iterate in registers); EC = 0: any count.
+template <int EC>
 __device__ void sor_half(const CmfdArgs& a, const Work& k, const float* b,
                          int color) {
-  const int E = a.E, C = a.C;
+  const int C = a.C;
   const float w = a.sor;
   const int j0 = color ? a.n_color0 : 0;
   const int j1 = color ? a.C : a.n_color0;
   for (int j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
     int nbj[4];
+#pragma unroll
     for (int f = 0; f < 4; f++) nbj[f] = a.nbr_j[f * C + j];
-    for (int e = 0; e < E; e++) {
-      const float* arow = k.A + (int64_t) e * E * C + j;
-      const float d = arow[(int64_t) e * C];
-      float v = (1.0f - w) * k.x[e * C + j] * (d / w);
-      for (int g = 0; g < E; g++)
-        if (g != e) v -= arow[(int64_t) g * C] * k.x[g * C + j];
-      for (int f = 0; f < 4; f++)
-        if (nbj[f] >= 0)
-          v -= k.nb[((int64_t) f * E + e) * C + j] * k.x[e * C + nbj[f]];
-      v += b[e * C + j];
-      k.x[e * C + j] = v * (w / d);
+    if constexpr (EC > 0) {
+      float xo[EC];
+#pragma unroll
+      for (int g = 0; g < EC; g++) xo[g] = k.x[g * C + j];
+#pragma unroll
+      for (int e = 0; e < EC; e++) {
+        const float* arow = k.A + e * EC * C + j;
+        float ar[EC];
+#pragma unroll
+        for (int g = 0; g < EC; g++) ar[g] = arow[g * C];
+        float v = (1.0f - w) * xo[e] * (ar[e] / w);
+#pragma unroll
+        for (int g = 0; g < EC; g++)
+          if (g != e) v -= ar[g] * xo[g];
+#pragma unroll
+        for (int f = 0; f < 4; f++)
+          if (nbj[f] >= 0) v -= k.nb[(f * EC + e) * C + j] * k.x[e * C + nbj[f]];
+        v += b[e * C + j];
+        xo[e] = v * (w / ar[e]);
+        k.x[e * C + j] = xo[e];
+      }
+    } else {
+      const int E = a.E;
+      for (int e = 0; e < E; e++) {
+        const float* arow = k.A + (int64_t) e * E * C + j;
+        const float d = arow[(int64_t) e * C];
+        float v = (1.0f - w) * k.x[e * C + j] * (d / w);
+        for (int g = 0; g < E; g++)
+          if (g != e) v -= arow[(int64_t) g * C] * k.x[g * C + j];
+        for (int f = 0; f < 4; f++)
+          if (nbj[f] >= 0)
+            v -= k.nb[((int64_t) f * E + e) * C + j] * k.x[e * C + nbj[f]];
+        v += b[e * C + j];
+        k.x[e * C + j] = v * (w / d);
+      }
     }
   }
 }
@@ -366,25 +401,26 @@ __device__ void sor_half(const CmfdArgs& a, const Work& k, const float* b,
 // linearSolve (src/linalg.cpp:179-385): red-black SOR on A x = b until the
 // fission source settles; false when it diverges or does not converge.
 // Uniform across the block (every branch depends on block-wide values).
+template <int EC>
 __device__ bool linear_solve(const CmfdArgs& a, const Work& k, const float* b,
                              double tol, double* red, int& sweeps) {
   tol = fmax(kLinalgTol, tol);
   float* ls_old = k.ls_a;
   float* ls_new = k.ls_b;
-  mat_fission(a, k, k.x, ls_old);
+  mat_fission<EC>(a, k, k.x, ls_old);
   __syncthreads();
   double lres = 0.0, linit = 0.0, min_res = 1e6, stall_res = INFINITY;
   int li = 0, stall_li = 0;
   while (li < kMaxLinearIters) {
-    sor_half(a, k, b, 0);
+    sor_half<EC>(a, k, b, 0);
     __syncthreads();
-    sor_half(a, k, b, 1);
+    sor_half<EC>(a, k, b, 1);
     __syncthreads();
     sweeps++;
     // the new fission source is read at the first sweep and from the 25th
     // on (residuals and the copy to the old source)
     if (li == 0 || li + 1 >= kMinIters) {
-      mat_fission(a, k, k.x, ls_new);
+      mat_fission<EC>(a, k, k.x, ls_new);
       __syncthreads();
     }
     if (li == 0) {
@@ -420,6 +456,7 @@ __device__ bool linear_solve(const CmfdArgs& a, const Work& k, const float* b,
 // adding dd = max(0, sum |off-diagonal| - diagonal) to each diagonal, the
 // difference moved to the right side (b + dd x) and linearSolve repeated
 // until the fission source settles; A is restored on success.
+template <int EC>
 __device__ bool dd_linear_solve(const CmfdArgs& a, const Work& k,
                                 const float* b, double tol, double* red,
                                 int& sweeps) {
@@ -439,7 +476,7 @@ __device__ bool dd_linear_solve(const CmfdArgs& a, const Work& k,
   __syncthreads();
   float* old_src = k.dd_a;
   float* new_src = k.dd_b;
-  mat_fission(a, k, k.x, new_src);
+  mat_fission<EC>(a, k, k.x, new_src);
   __syncthreads();
   double initial = 0.0, min_res = 1e6, stall_res = INFINITY;
   int stall_it = 0;
@@ -450,8 +487,8 @@ __device__ bool dd_linear_solve(const CmfdArgs& a, const Work& k,
     for (int r = threadIdx.x; r < CE; r += blockDim.x)
       k.rhs[r] = b[r] + k.ddv[r] * k.x[r];
     __syncthreads();
-    linear_solve(a, k, k.rhs, tol, red, sweeps);   // a failure is only noted
-    mat_fission(a, k, k.x, new_src);
+    linear_solve<EC>(a, k, k.rhs, tol, red, sweeps);   // a failure is only noted
+    mat_fission<EC>(a, k, k.x, new_src);
     __syncthreads();
     const double res = rmse(a, new_src, old_src, red);
     if (it == 0) initial = res < 1e-14 ? 1e-10 : res;
@@ -474,6 +511,7 @@ __device__ bool dd_linear_solve(const CmfdArgs& a, const Work& k,
   return true;
 }
 
+template <int EC>
 __global__ void __launch_bounds__(kSolveThreads, 1)
 cmfd_solve_kernel(const CmfdArgs a, int smem_level) {
   DevScalars* sc = a.sc;
@@ -506,7 +544,7 @@ cmfd_solve_kernel(const CmfdArgs a, int smem_level) {
   const double lin_tol = fmax(kLinalgTol, tol * 1e-1);
   float* src_old = k.src_a;
   float* src_new = k.src_b;
-  mat_fission(a, k, k.x, src_old);
+  mat_fission<EC>(a, k, k.x, src_old);
   const double s0 = block_total(src_old, CE, red);
   bool failed = !(s0 > 0.0) || !isfinite(s0);
   int sweeps = 0, power = 0;
@@ -523,16 +561,16 @@ cmfd_solve_kernel(const CmfdArgs a, int smem_level) {
       // eigenvalueSolve's linear solves: plain, or diagonally dominated
       // from the first failure on
       bool ok = false;
-      if (!dd_mode) ok = linear_solve(a, k, src_old, lin_tol, red, sweeps);
+      if (!dd_mode) ok = linear_solve<EC>(a, k, src_old, lin_tol, red, sweeps);
       if (!ok) {
         dd_mode = true;
-        ok = dd_linear_solve(a, k, src_old, lin_tol, red, sweeps);
+        ok = dd_linear_solve<EC>(a, k, src_old, lin_tol, red, sweeps);
       }
       if (!ok) {
         failed = true;
         break;
       }
-      mat_fission(a, k, k.x, src_new);
+      mat_fission<EC>(a, k, k.x, src_new);
       __syncthreads();
       keff = block_total(src_new, CE, red) / rows;
       for (int r = threadIdx.x; r < CE; r += blockDim.x)
@@ -575,8 +613,8 @@ cmfd_solve_kernel(const CmfdArgs a, int smem_level) {
     }
     return;
   }
-  mat_fission(a, k, k.x, k.src_a);
-  mat_fission(a, k, k.phi_t, k.src_b);
+  mat_fission<EC>(a, k, k.x, k.src_a);
+  mat_fission<EC>(a, k, k.phi_t, k.src_b);
   __syncthreads();
   const double sn = block_total(k.src_a, CE, red);
   const double so = block_total(k.src_b, CE, red);
@@ -615,6 +653,19 @@ cmfd_solve_kernel(const CmfdArgs a, int smem_level) {
     cm->keff = keff;
     sc->keff = keff;
   }
+}
+
+template <int EC>
+void solve_instance(const CmfdArgs& a, int threads, int smem, int level,
+                    cudaStream_t s) {
+  static bool configured = false;
+  if (!configured) {
+    cudaFuncSetAttribute(cmfd_solve_kernel<EC>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kSolveSmemMax);
+    configured = true;
+  }
+  cmfd_solve_kernel<EC><<<1, threads, smem, s>>>(a, level);
 }
 
 int sm_count() {
@@ -657,14 +708,17 @@ void launch_cmfd_solve(const CmfdArgs& a, cudaStream_t s) {
   const int64_t level2 = level1 + 4 * (CE * a.E + 4 * CE);
   const int level = level2 <= kSolveSmemMax ? 2 : level1 <= kSolveSmemMax ? 1 : 0;
   const int smem = level == 2 ? (int) level2 : level == 1 ? (int) level1 : 0;
-  static int configured = 0;
-  if (!configured) {
-    cudaFuncSetAttribute(cmfd_solve_kernel,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         kSolveSmemMax);
-    configured = 1;
+  switch (a.E) {
+    case 1: solve_instance<1>(a, threads, smem, level, s); break;
+    case 2: solve_instance<2>(a, threads, smem, level, s); break;
+    case 3: solve_instance<3>(a, threads, smem, level, s); break;
+    case 4: solve_instance<4>(a, threads, smem, level, s); break;
+    case 5: solve_instance<5>(a, threads, smem, level, s); break;
+    case 6: solve_instance<6>(a, threads, smem, level, s); break;
+    case 7: solve_instance<7>(a, threads, smem, level, s); break;
+    case 8: solve_instance<8>(a, threads, smem, level, s); break;
+    default: solve_instance<0>(a, threads, smem, level, s); break;
   }
-  cmfd_solve_kernel<<<1, threads, smem, s>>>(a, level);
 }
 
 void launch_cmfd_prolong(float* phi, const int32_t* fsr_cell,
