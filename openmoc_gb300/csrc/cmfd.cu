@@ -119,11 +119,13 @@ struct Work {
   float *sig_t, *nu_f, *chi, *dif, *dlx, *dly, *phi_c, *sig_s, *J;
   // colour order
   float *A, *nb, *M;                                  // [E][E][C], [4][E][C]
-  float *x, *phi_t, *src_a, *src_b, *ls_a, *ls_b;     // [E][C]
-  float *rhs, *dd_a, *dd_b, *ddv;                     // [E][C]
+  float *x, *src_a, *src_b, *ls_a, *ls_b;            // [E][C]
+  float *sa, *sb;        // per row (1 - w) d / w and w / d of the SOR update
+  float *phi_t, *rhs, *dd_a, *dd_b, *ddv;             // [E][C]
 };
 
-constexpr int kColourVecs = 10;   // x .. ddv
+constexpr int kHotVecs = 7;       // x .. sb: in shared memory when they fit
+constexpr int kColourVecs = 12;   // every colour-order vector
 
 __device__ Work carve(float* w, int C, int E) {
   const int64_t CE = (int64_t) C * E, CEE = CE * E, C4E = 4 * CE;
@@ -136,19 +138,18 @@ __device__ Work carve(float* w, int C, int E) {
   k.A = w; w += CEE;
   k.nb = w; w += C4E;
   k.M = w; w += CEE;
-  float** vecs[] = {&k.x, &k.phi_t, &k.src_a, &k.src_b, &k.ls_a, &k.ls_b,
-                    &k.rhs, &k.dd_a, &k.dd_b, &k.ddv};
+  float** vecs[] = {&k.x, &k.src_a, &k.src_b, &k.ls_a, &k.ls_b, &k.sa,
+                    &k.sb, &k.phi_t, &k.rhs, &k.dd_a, &k.dd_b, &k.ddv};
   for (float** p : vecs) { *p = w; w += CE; }
   return k;
 }
 
-// Shared memory: level 2 holds the colour-order vectors, A and the
+// Shared memory: level 2 holds the vectors of the SOR sweeps, A and the
 // couplings; level 1 the vectors only; level 0 nothing (all in global).
 __device__ void place_in_smem(Work& k, float* s, int level, int C, int E) {
   if (level < 1) return;
   const int64_t CE = (int64_t) C * E;
-  float** vecs[] = {&k.x, &k.phi_t, &k.src_a, &k.src_b, &k.ls_a, &k.ls_b,
-                    &k.rhs, &k.dd_a, &k.dd_b, &k.ddv};
+  float** vecs[] = {&k.x, &k.src_a, &k.src_b, &k.ls_a, &k.ls_b, &k.sa, &k.sb};
   for (float** p : vecs) { *p = s; s += CE; }
   if (level < 2) return;
   k.A = s; s += CE * E;
@@ -360,25 +361,27 @@ __device__ void sor_half(const CmfdArgs& a, const Work& k, const float* b,
 #pragma unroll
     for (int f = 0; f < 4; f++) nbj[f] = a.nbr_j[f * C + j];
     if constexpr (EC > 0) {
+      // a missing neighbour points at the cell itself with a zero coupling
+#pragma unroll
+      for (int f = 0; f < 4; f++) nbj[f] = nbj[f] < 0 ? j : nbj[f];
       float xo[EC];
 #pragma unroll
       for (int g = 0; g < EC; g++) xo[g] = k.x[g * C + j];
 #pragma unroll
       for (int e = 0; e < EC; e++) {
         const float* arow = k.A + e * EC * C + j;
-        float ar[EC];
-#pragma unroll
-        for (int g = 0; g < EC; g++) ar[g] = arow[g * C];
-        float v = (1.0f - w) * xo[e] * (ar[e] / w);
+        const int r = e * C + j;
+        // two partial sums: the cell's other groups, and the neighbours
+        float s0 = b[r], s1 = 0.0f;
 #pragma unroll
         for (int g = 0; g < EC; g++)
-          if (g != e) v -= ar[g] * xo[g];
+          if (g != e) s0 -= arow[g * C] * xo[g];
 #pragma unroll
         for (int f = 0; f < 4; f++)
-          if (nbj[f] >= 0) v -= k.nb[(f * EC + e) * C + j] * k.x[e * C + nbj[f]];
-        v += b[e * C + j];
-        xo[e] = v * (w / ar[e]);
-        k.x[e * C + j] = xo[e];
+          s1 -= k.nb[(f * EC + e) * C + j] * k.x[e * C + nbj[f]];
+        const float v = k.sa[r] * xo[e] + (s0 + s1);
+        xo[e] = v * k.sb[r];
+        k.x[r] = xo[e];
       }
     } else {
       const int E = a.E;
@@ -398,6 +401,19 @@ __device__ void sor_half(const CmfdArgs& a, const Work& k, const float* b,
   }
 }
 
+// The SOR update's diagonal factors for the current A (no barrier).
+template <int EC>
+__device__ void sor_prep(const CmfdArgs& a, const Work& k) {
+  const int E = EC > 0 ? EC : a.E, C = a.C, CE = a.C * E;
+  const float w = a.sor;
+  for (int r = threadIdx.x; r < CE; r += blockDim.x) {
+    const int e = r / C, j = r - e * C;
+    const float d = k.A[((int64_t) e * E + e) * C + j];
+    k.sa[r] = (1.0f - w) * (d / w);
+    k.sb[r] = w / d;
+  }
+}
+
 // linearSolve (src/linalg.cpp:179-385): red-black SOR on A x = b until the
 // fission source settles; false when it diverges or does not converge.
 // Uniform across the block (every branch depends on block-wide values).
@@ -407,6 +423,7 @@ __device__ bool linear_solve(const CmfdArgs& a, const Work& k, const float* b,
   tol = fmax(kLinalgTol, tol);
   float* ls_old = k.ls_a;
   float* ls_new = k.ls_b;
+  sor_prep<EC>(a, k);
   mat_fission<EC>(a, k, k.x, ls_old);
   __syncthreads();
   double lres = 0.0, linit = 0.0, min_res = 1e6, stall_res = INFINITY;
@@ -683,7 +700,7 @@ int sm_count() {
 
 int64_t cmfd_work_floats(int C, int E) {
   const int64_t CE = (int64_t) C * E;
-  return 7 * CE + 3 * CE * E + 8 * CE + 10 * CE;
+  return 7 * CE + 3 * CE * E + 8 * CE + kColourVecs * CE;
 }
 
 void launch_cmfd_pair_sums(const float* phi, const float* vol,
@@ -704,7 +721,7 @@ void launch_cmfd_solve(const CmfdArgs& a, cudaStream_t s) {
   int threads = (std::max(a.n_color0, a.C - a.n_color0) + 31) / 32 * 32;
   threads = std::max(128, std::min(kSolveThreads, threads));
   const int64_t CE = (int64_t) a.C * a.E;
-  const int64_t level1 = 4 * kColourVecs * CE;
+  const int64_t level1 = 4 * kHotVecs * CE;
   const int64_t level2 = level1 + 4 * (CE * a.E + 4 * CE);
   const int level = level2 <= kSolveSmemMax ? 2 : level1 <= kSolveSmemMax ? 1 : 0;
   const int smem = level == 2 ? (int) level2 : level == 1 ? (int) level1 : 0;
