@@ -364,25 +364,36 @@ __device__ void sor_half(const CmfdArgs& a, const Work& k, const float* b,
       // a missing neighbour points at the cell itself with a zero coupling
 #pragma unroll
       for (int f = 0; f < 4; f++) nbj[f] = nbj[f] < 0 ? j : nbj[f];
-      float xo[EC];
+      // everything that does not depend on this cell's update first (the
+      // neighbours are of the other colour), the stores last, so that no
+      // load waits behind a store
+      float xo[EC], t[EC], sa[EC], sb[EC];
 #pragma unroll
-      for (int g = 0; g < EC; g++) xo[g] = k.x[g * C + j];
+      for (int e = 0; e < EC; e++) {
+        const int r = e * C + j;
+        xo[e] = k.x[r];
+        sa[e] = k.sa[r];
+        sb[e] = k.sb[r];
+        float u = b[r];
+#pragma unroll
+        for (int f = 0; f < 4; f++)
+          u -= k.nb[(f * EC + e) * C + j] * k.x[e * C + nbj[f]];
+        t[e] = u;
+      }
 #pragma unroll
       for (int e = 0; e < EC; e++) {
         const float* arow = k.A + e * EC * C + j;
-        const int r = e * C + j;
-        // two partial sums: the cell's other groups, and the neighbours
-        float s0 = b[r], s1 = 0.0f;
+        float s0 = 0.0f, s1 = 0.0f;      // two partial sums over the groups
 #pragma unroll
         for (int g = 0; g < EC; g++)
-          if (g != e) s0 -= arow[g * C] * xo[g];
-#pragma unroll
-        for (int f = 0; f < 4; f++)
-          s1 -= k.nb[(f * EC + e) * C + j] * k.x[e * C + nbj[f]];
-        const float v = k.sa[r] * xo[e] + (s0 + s1);
-        xo[e] = v * k.sb[r];
-        k.x[r] = xo[e];
+          if (g != e) {
+            if (g & 1) s1 -= arow[g * C] * xo[g];
+            else s0 -= arow[g * C] * xo[g];
+          }
+        xo[e] = (sa[e] * xo[e] + (t[e] + (s0 + s1))) * sb[e];
       }
+#pragma unroll
+      for (int e = 0; e < EC; e++) k.x[e * C + j] = xo[e];
     } else {
       const int E = a.E;
       for (int e = 0; e < E; e++) {
