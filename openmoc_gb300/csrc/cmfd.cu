@@ -122,6 +122,7 @@ struct Work {
   float *x, *src_a, *src_b, *ls_a, *ls_b;            // [E][C]
   float *sa, *sb;        // per row (1 - w) d / w and w / d of the SOR update
   float *phi_t, *rhs, *dd_a, *dd_b, *ddv;             // [E][C]
+  const int32_t* nbr;    // [4][C] neighbours in colour order
 };
 
 constexpr int kHotVecs = 7;       // x .. sb: in shared memory when they fit
@@ -154,6 +155,16 @@ __device__ void place_in_smem(Work& k, float* s, int level, int C, int E) {
   if (level < 2) return;
   k.A = s; s += CE * E;
   k.nb = s;
+}
+
+// Bytes of dynamic shared memory at each level: the float arrays, then the
+// neighbour table (4 C ints).
+__host__ __device__ inline int64_t smem_bytes(int level, int C, int E) {
+  const int64_t CE = (int64_t) C * E;
+  if (level < 1) return 0;
+  int64_t f = 7 * CE;                      // kHotVecs
+  if (level >= 2) f += CE * E + 4 * CE;
+  return 4 * f + 16 * (int64_t) C;
 }
 
 __device__ __forceinline__ int neighbour(const CmfdArgs& a, int c, int f) {
@@ -359,7 +370,7 @@ __device__ void sor_half(const CmfdArgs& a, const Work& k, const float* b,
   for (int j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
     int nbj[4];
 #pragma unroll
-    for (int f = 0; f < 4; f++) nbj[f] = a.nbr_j[f * C + j];
+    for (int f = 0; f < 4; f++) nbj[f] = k.nbr[f * C + j];
     if constexpr (EC > 0) {
       // a missing neighbour points at the cell itself with a zero coupling
 #pragma unroll
@@ -550,6 +561,13 @@ cmfd_solve_kernel(const CmfdArgs a, int smem_level) {
   const int CE = C * E;
   Work k = carve(a.work, C, E);
   place_in_smem(k, s_dyn, smem_level, C, E);
+  k.nbr = a.nbr_j;
+  if (smem_level >= 1) {
+    int32_t* s_nbr = reinterpret_cast<int32_t*>(
+        reinterpret_cast<char*>(s_dyn) + smem_bytes(smem_level, C, E) - 16 * C);
+    for (int i = threadIdx.x; i < 4 * C; i += blockDim.x) s_nbr[i] = a.nbr_j[i];
+    k.nbr = s_nbr;             // read after the barrier below the collapse
+  }
   CmfdDevState* cm = a.cm;
   const int it = sc->iteration;                 // MOC iteration
   // the coarse tolerance follows the transport residual
@@ -731,11 +749,10 @@ void launch_cmfd_solve(const CmfdArgs& a, cudaStream_t s) {
   // one thread per cell of a colour, at least four warps
   int threads = (std::max(a.n_color0, a.C - a.n_color0) + 31) / 32 * 32;
   threads = std::max(128, std::min(kSolveThreads, threads));
-  const int64_t CE = (int64_t) a.C * a.E;
-  const int64_t level1 = 4 * kHotVecs * CE;
-  const int64_t level2 = level1 + 4 * (CE * a.E + 4 * CE);
+  const int64_t level1 = smem_bytes(1, a.C, a.E);
+  const int64_t level2 = smem_bytes(2, a.C, a.E);
   const int level = level2 <= kSolveSmemMax ? 2 : level1 <= kSolveSmemMax ? 1 : 0;
-  const int smem = level == 2 ? (int) level2 : level == 1 ? (int) level1 : 0;
+  const int smem = (int) smem_bytes(level, a.C, a.E);
   switch (a.E) {
     case 1: solve_instance<1>(a, threads, smem, level, s); break;
     case 2: solve_instance<2>(a, threads, smem, level, s); break;
