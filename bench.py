@@ -367,10 +367,17 @@ def run_gpu(args):
             out["cpu_baseline"] = cpu
         if args.batch > 0:
             out["batched_instances"] = run_instances(p, args)
+        core = None
         if world == 1 and args.workload == "assembly70" and not args.no_raytrace:
-            out["ray_tracing"] = ray_tracing(local)
+            out["ray_tracing"], core = ray_tracing(local)
         if world == 1 and args.workload == "assembly70" and not args.no_cmfd:
-            out["cmfd"] = cmfd_acceleration(p, local)
+            # the regime CMFD is for: a core whose sweeps are expensive and
+            # whose plain source iteration needs a thousand iterations
+            from openmoc_gb300 import lattice as lat
+            if core is None:
+                core = lat.core_51x51(device=local)
+            out["cmfd"] = cmfd_acceleration(core, local, coarse_groups=2,
+                                            label="51x51 core, 7 groups")
         if world == 1 and not args.no_serving and args.workload == "assembly70":
             # the second half of the headline: the request stream through the
             # batched server against the plain per-solve loop
@@ -384,17 +391,17 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
-def cmfd_acceleration(p, device, tol=1e-5):
-    """Time to solution of the headline problem, computeEigenvalue to a
-    1e-5 fission-source residual, without and with CMFD (pin-cell mesh,
-    the 70 groups condensed to 8 coarse groups of 9 or 8): iterations, wall
-    seconds, and the per-iteration cost of the coarse solve and its
-    host round trip."""
+def cmfd_acceleration(p, device, tol=1e-5, coarse_groups=8, label=None):
+    """Time to solution, computeEigenvalue to a 1e-5 fission-source
+    residual, without and with CMFD (pin-cell mesh, the groups condensed to
+    `coarse_groups` contiguous bands): iterations, wall seconds, and the
+    coarse solve's power iterations and SOR sweeps."""
     from openmoc_gb300 import Cmfd, GB300Solver
     G = p.num_groups
-    bands = np.array_split(np.arange(1, G + 1), 8)
-    res = {"workload": f"{p.meta.get('nx', 17)}x{p.meta.get('ny', 17)} pins, {G} "
-                       f"groups; CMFD on the pin mesh with {len(bands)} coarse groups",
+    bands = np.array_split(np.arange(1, G + 1), coarse_groups)
+    res = {"workload": (label or f"{p.meta.get('nx', 17)}x{p.meta.get('ny', 17)} pins, "
+                                 f"{G} groups")
+                       + f"; CMFD on the pin mesh with {len(bands)} coarse groups",
            "tolerance": tol}
     for name, use in (("plain", False), ("cmfd", True)):
         s = GB300Solver(p, device=device)
@@ -424,7 +431,8 @@ def cmfd_acceleration(p, device, tol=1e-5):
 def ray_tracing(device):
     """Track generation of the 51x51 core on the host cores against the
     device ray tracer (laydown on the host, segmentation, FSR numbering and
-    volumes on the GPU); both produce the same segments."""
+    volumes on the GPU); both produce the same segments.  Returns the
+    timings and the device-traced problem."""
     from openmoc_gb300 import lattice as lat
     lat.pin_cell(7, device=device)            # CUDA context and module load
     t0 = time.perf_counter()
@@ -435,11 +443,11 @@ def ray_tracing(device):
     t_dev = time.perf_counter() - t0
     same = all(np.array_equal(getattr(h, k), getattr(d, k)) for k in (
         "seg_len", "seg_fsr", "seg_off", "track_ang", "next", "flags", "fsr_mat"))
-    return {"workload": "51x51 pins, 128 azimuthal, 0.03 cm, TY-6: "
-                        f"{d.num_tracks} tracks, {d.num_segments} segments",
-            "host_s": t_host, "host_threads": os.cpu_count(), "device_s": t_dev,
-            "segments_per_s_device": d.num_segments / t_dev,
-            "speedup": t_host / t_dev, "identical_segments": bool(same)}
+    return ({"workload": "51x51 pins, 128 azimuthal, 0.03 cm, TY-6: "
+                         f"{d.num_tracks} tracks, {d.num_segments} segments",
+             "host_s": t_host, "host_threads": os.cpu_count(), "device_s": t_dev,
+             "segments_per_s_device": d.num_segments / t_dev,
+             "speedup": t_host / t_dev, "identical_segments": bool(same)}, d)
 
 
 def end_to_end(p, args, device, torch, otf=False):
