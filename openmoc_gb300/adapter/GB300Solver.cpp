@@ -17,16 +17,19 @@
  */
 #include "GB300Solver.h"
 
+#include <cmath>
 #include <cstring>
 #include <map>
 #include <vector>
 
 #include "../../include/openmoc_gb300.h"
+#include "Cmfd.h"
 #include "pack_reference.h"
 
 GB300Solver::GB300Solver(TrackGenerator* track_generator, int device)
     : Solver(NULL), _ctx(NULL), _device(device), _exp_kind(-1),
-      _uploaded(false) {
+      _uploaded(false), _cmfd_relaxation(0.7), _cmfd_sor(1.5),
+      _cmfd_flux_limiting(true), _cmfd_on_host(false), _cmfd_unbounded(0) {
   _gpu_solver = true;
   if (track_generator != NULL) setTrackGenerator(track_generator);
 }
@@ -50,6 +53,95 @@ void GB300Solver::setTrackGenerator(TrackGenerator* track_generator) {
 void GB300Solver::setExponentialEvaluator(int kind) {
   _exp_kind = kind;
   if (_ctx) check(moc_set_exponential(_ctx, kind), "setExponentialEvaluator");
+}
+
+void GB300Solver::setCmfdFactors(double relaxation, double sor,
+                                 bool flux_limiting, int unbounded_iterations,
+                                 bool on_host) {
+  _cmfd_relaxation = relaxation;
+  _cmfd_sor = sor;
+  _cmfd_flux_limiting = flux_limiting;
+  _cmfd_unbounded = unbounded_iterations;
+  _cmfd_on_host = on_host;
+}
+
+/* The Geometry's Cmfd (Solver::initializeCmfd, src/Solver.cpp:1145-1185)
+ * as a moc_cmfd_mesh: OpenMOC's own FSR-to-cell map, lattice widths,
+ * boundaries and group structure, the boundary face at each track end, and
+ * the quadrature of Cmfd::computeLarsensEDCFactor. */
+void GB300Solver::attachCmfd() {
+  initializeCmfd();
+  if (_cmfd == NULL || !_cmfd->isFluxUpdateOn()) {
+    check(moc_set_cmfd(_ctx, NULL), "moc_set_cmfd");
+    return;
+  }
+  if (_SOLVE_3D || _cmfd->getNumZ() > 1)
+    log_printf(ERROR, "GB300Solver supports CMFD on 2D meshes only");
+  if (_cmfd->isCentroidUpdateOn())
+    log_printf(ERROR, "GB300Solver supports the cell-average CMFD update "
+               "only (Cmfd::setKNearest(1))");
+  const int nx = _cmfd->getNumX(), ny = _cmfd->getNumY();
+  Lattice* lat = _cmfd->getLattice();
+  std::vector<double> wx(lat->getWidthsX()), wy(lat->getWidthsY());
+  if ((int) wx.size() != nx || (int) wy.size() != ny)
+    log_printf(ERROR, "GB300Solver: unexpected CMFD lattice widths");
+  std::vector<int32_t> cell(_num_FSRs);
+  for (long r = 0; r < _num_FSRs; r++)
+    cell[r] = _cmfd->convertFSRIdToCmfdCell(r);
+  const double x0 = _geometry->getMinX(), x1 = _geometry->getMaxX();
+  const double y0 = _geometry->getMinY(), y1 = _geometry->getMaxY();
+  const double tol = 1e-9 * std::max(x1 - x0, y1 - y0);
+  Track** tracks = _track_generator->get2DTracksArray();
+  const long T = _track_generator->getNum2DTracks();
+  std::vector<int8_t> ends(2 * T);
+  for (long t = 0; t < T; t++) {
+    Point* q[2] = {tracks[t]->getEnd(), tracks[t]->getStart()};
+    for (int d = 0; d < 2; d++) {
+      int8_t f = -1;
+      if (std::fabs(q[d]->getX() - x0) <= tol) f = 0;
+      else if (std::fabs(q[d]->getX() - x1) <= tol) f = 2;
+      else if (std::fabs(q[d]->getY() - y0) <= tol) f = 1;
+      else if (std::fabs(q[d]->getY() - y1) <= tol) f = 3;
+      ends[2 * t + d] = f;
+    }
+  }
+  const int sides[4] = {SURFACE_X_MIN, SURFACE_Y_MIN, SURFACE_X_MAX,
+                        SURFACE_Y_MAX};
+  moc_cmfd_mesh m;
+  std::memset(&m, 0, sizeof(m));
+  for (int f = 0; f < 4; f++) {
+    const int b = _cmfd->getBoundary(sides[f]);
+    if (b != VACUUM && b != REFLECTIVE)
+      log_printf(ERROR, "GB300Solver supports vacuum and reflective CMFD "
+                 "boundaries only");
+    m.boundary[f] = (b == VACUUM) ? MOC_BC_VACUUM : MOC_BC_REFLECTIVE;
+  }
+  std::vector<int32_t> group_of(_num_groups);
+  for (int g = 0; g < _num_groups; g++) group_of[g] = _cmfd->getCmfdGroup(g);
+  std::vector<double> mu, w;
+  for (size_t a = 0; a < _quad->getNumAzimAngles() / 2; a++)
+    for (size_t p = 0; p < _quad->getNumPolarAngles() / 2; p++) {
+      const double sn = _quad->getSinTheta(a, p);
+      mu.push_back(std::sqrt(1.0 - sn * sn));
+      w.push_back(_quad->getAzimWeight(a) * _quad->getPolarWeight(a, p));
+    }
+  m.num_x = nx;
+  m.num_y = ny;
+  m.widths_x = wx.data();
+  m.widths_y = wy.data();
+  m.fsr_cell = cell.data();
+  m.track_end_face = ends.data();
+  m.num_cmfd_groups = _cmfd->getNumCmfdGroups();
+  m.group_of = group_of.data();
+  m.num_edc_angles = (int32_t) mu.size();
+  m.edc_mu = mu.data();
+  m.edc_weight = w.data();
+  m.relaxation = _cmfd_relaxation;
+  m.sor_factor = _cmfd_sor;
+  m.flux_limiting = _cmfd_flux_limiting ? 1 : 0;
+  m.num_unbounded_iterations = _cmfd_unbounded;
+  m.solve_on_host = _cmfd_on_host ? 1 : 0;
+  check(moc_set_cmfd(_ctx, &m), "moc_set_cmfd");
 }
 
 int GB300Solver::materialIndex(Material* m) {
@@ -280,6 +372,7 @@ void GB300Solver::computeEigenvalue(int max_iters, residualType res_type) {
   initializeExpEvaluators();
   initializeFluxArrays();
   initializeSourceArrays();
+  attachCmfd();
   check(moc_compute_eigenvalue(_ctx, max_iters, (int) res_type),
         "computeEigenvalue");
   check(moc_get_keff(_ctx, &_k_eff), "getKeff");

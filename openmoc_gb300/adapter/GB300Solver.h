@@ -40,6 +40,12 @@ class GB300Solver : public Solver {
 
   void check(int status, const char* what);
   virtual void upload();
+  /* CMFD from the Geometry (Solver::initializeCmfd), attached to the
+   * context as moc_set_cmfd wants it */
+  void attachCmfd();
+  double _cmfd_relaxation, _cmfd_sor;
+  bool _cmfd_flux_limiting, _cmfd_on_host;
+  int _cmfd_unbounded;
   int materialIndex(Material* m);
 
   /* Solver hooks (src/Solver.h:334-431) */
@@ -76,6 +82,13 @@ class GB300Solver : public Solver {
   /** Shared-memory table (0) or hardware ex2 (1) for 1 - exp(-x); the
    *  default lets the autotuner pick the faster. */
   void setExponentialEvaluator(int kind);
+  /** The factors of the Geometry's Cmfd, which OpenMOC keeps private:
+   *  relaxation (Cmfd::setCMFDRelaxationFactor, default 0.7), SOR factor
+   *  (setSORRelaxationFactor, 1.5), flux limiting (useFluxLimiting, on),
+   *  unbounded iterations (setNumUnboundedIterations, 0); on_host runs the
+   *  coarse solve on the host in FP64 instead of on the GPU in FP32. */
+  void setCmfdFactors(double relaxation, double sor, bool flux_limiting,
+                      int unbounded_iterations, bool on_host = false);
 
   /* device-resident source iteration */
   void computeEigenvalue(int max_iters = 1000,
