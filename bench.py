@@ -428,6 +428,28 @@ def cmfd_acceleration(p, device, tol=1e-5, coarse_groups=8, label=None):
     return res
 
 
+def cmfd_core_solve(device=0):
+    """The CMFD-accelerated solve of cmfd_acceleration's core alone (pin
+    mesh, two coarse groups, 1e-5), on a device-traced core."""
+    from openmoc_gb300 import Cmfd, GB300Solver
+    from openmoc_gb300 import lattice as lat
+    p = lat.core_51x51(device=device)
+    s = GB300Solver(p, device=device)
+    s.setConvergenceThreshold(1e-5)
+    c = Cmfd()
+    c.setLatticeStructure(51, 51)
+    c.setGroupStructure([[1, 2, 3], [4, 5, 6, 7]])
+    s.setCmfd(c)
+    t0 = time.perf_counter()
+    s.computeEigenvalue(1000, 1)
+    dt = time.perf_counter() - t0
+    out = {"workload": "51x51 core, 7 groups; CMFD on the pin mesh with 2 coarse groups",
+           "iterations": s.getNumIterations(), "seconds": dt, "keff": s.getKeff(),
+           "cmfd": s.getCmfdInfo()}
+    s.close()
+    return out
+
+
 def ray_tracing(device):
     """Track generation of the 51x51 core on the host cores against the
     device ray tracer (laydown on the host, segmentation, FSR numbering and
@@ -771,12 +793,18 @@ def main():
                     help="skip the track-generation timing (host vs device ray tracing)")
     ap.add_argument("--no-cmfd", action="store_true",
                     help="leave the CMFD time-to-solution comparison out")
+    ap.add_argument("--cmfd-only", action="store_true",
+                    help="only the CMFD-accelerated solve of the 51x51 core (for "
+                         "profiling): prints its iterations, seconds and coarse-solve "
+                         "statistics")
     ap.add_argument("--no-serving", action="store_true",
                     help="leave the request-stream benchmark out of the default line")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.cmfd_only:
+        print(json.dumps(cmfd_core_solve()), flush=True)
+    elif args.impl == "reference":
         run_reference(args)
     elif args.serving:
         print(json.dumps(run_serving(args)), flush=True)
