@@ -376,8 +376,8 @@ def run_gpu(args):
             from openmoc_gb300 import lattice as lat
             if core is None:
                 core = lat.core_51x51(device=local)
-            out["cmfd"] = cmfd_acceleration(core, local, coarse_groups=2,
-                                            label="51x51 core, 7 groups")
+            out["cmfd"] = cmfd_acceleration(core, local, label="51x51 core, 7 groups",
+                                            groups=[[1, 2, 3], [4, 5, 6, 7]])
         if world == 1 and not args.no_serving and args.workload == "assembly70":
             # the second half of the headline: the request stream through the
             # batched server against the plain per-solve loop
@@ -391,14 +391,15 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
-def cmfd_acceleration(p, device, tol=1e-5, coarse_groups=8, label=None):
+def cmfd_acceleration(p, device, tol=1e-5, coarse_groups=8, label=None, groups=None):
     """Time to solution, computeEigenvalue to a 1e-5 fission-source
     residual, without and with CMFD (pin-cell mesh, the groups condensed to
     `coarse_groups` contiguous bands): iterations, wall seconds, and the
     coarse solve's power iterations and SOR sweeps."""
     from openmoc_gb300 import Cmfd, GB300Solver
     G = p.num_groups
-    bands = np.array_split(np.arange(1, G + 1), coarse_groups)
+    bands = ([np.array(g) for g in groups] if groups is not None
+             else np.array_split(np.arange(1, G + 1), coarse_groups))
     res = {"workload": (label or f"{p.meta.get('nx', 17)}x{p.meta.get('ny', 17)} pins, "
                                  f"{G} groups")
                        + f"; CMFD on the pin mesh with {len(bands)} coarse groups",

@@ -22,8 +22,6 @@ namespace {
 
 constexpr int kPairThreads = 256;
 constexpr int kSolveThreads = 512;
-// up to 4 coarse groups a thread needs few registers: twice the warps
-constexpr int solve_threads(int ec) { return (ec > 0 && ec <= 4) ? 1024 : kSolveThreads; }
 // shared memory for the coarse system (vectors, A and couplings)
 constexpr int kSolveSmemMax = 216 * 1024;
 constexpr float kZeroSigmaT = 1e-6f;          // src/constants.h:34
@@ -553,7 +551,7 @@ __device__ bool dd_linear_solve(const CmfdArgs& a, const Work& k,
 }
 
 template <int EC>
-__global__ void __launch_bounds__(solve_threads(EC), 1)
+__global__ void __launch_bounds__(kSolveThreads, 1)
 cmfd_solve_kernel(const CmfdArgs a, int smem_level) {
   DevScalars* sc = a.sc;
   if (*(volatile int*) &sc->done) return;
@@ -750,8 +748,7 @@ void launch_cmfd_pair_sums(const float* phi, const float* vol,
 void launch_cmfd_solve(const CmfdArgs& a, cudaStream_t s) {
   // one thread per cell of a colour, at least four warps
   int threads = (std::max(a.n_color0, a.C - a.n_color0) + 31) / 32 * 32;
-  const int cap = solve_threads(a.E <= 8 ? a.E : 0);
-  threads = std::max(128, std::min(cap, threads));
+  threads = std::max(128, std::min(kSolveThreads, threads));
   const int64_t level1 = smem_bytes(1, a.C, a.E);
   const int64_t level2 = smem_bytes(2, a.C, a.E);
   const int level = level2 <= kSolveSmemMax ? 2 : level1 <= kSolveSmemMax ? 1 : 0;
