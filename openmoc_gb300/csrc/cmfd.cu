@@ -119,14 +119,14 @@ struct Work {
   float *sig_t, *nu_f, *chi, *dif, *dlx, *dly, *phi_c, *sig_s, *J;
   // colour order
   float *A, *nb, *M;                                  // [E][E][C], [4][E][C]
-  float *x, *src_a, *src_b, *ls_a, *ls_b;            // [E][C]
+  float *x, *b;          // iterate, right side of the SOR sweeps [E][C]
+  float *src_a, *src_b, *ls_a, *ls_b;                 // [E][C]
   float *sa, *sb;        // per row (1 - w) d / w and w / d of the SOR update
   float *phi_t, *rhs, *dd_a, *dd_b, *ddv;             // [E][C]
   const int32_t* nbr;    // [4][C] neighbours in colour order
 };
 
-constexpr int kHotVecs = 7;       // x .. sb: in shared memory when they fit
-constexpr int kColourVecs = 12;   // every colour-order vector
+constexpr int kColourVecs = 13;   // every colour-order vector
 
 __device__ Work carve(float* w, int C, int E) {
   const int64_t CE = (int64_t) C * E, CEE = CE * E, C4E = 4 * CE;
@@ -139,32 +139,60 @@ __device__ Work carve(float* w, int C, int E) {
   k.A = w; w += CEE;
   k.nb = w; w += C4E;
   k.M = w; w += CEE;
-  float** vecs[] = {&k.x, &k.src_a, &k.src_b, &k.ls_a, &k.ls_b, &k.sa,
+  float** vecs[] = {&k.x, &k.b, &k.src_a, &k.src_b, &k.ls_a, &k.ls_b, &k.sa,
                     &k.sb, &k.phi_t, &k.rhs, &k.dd_a, &k.dd_b, &k.ddv};
   for (float** p : vecs) { *p = w; w += CE; }
   return k;
 }
 
-// Shared memory: level 2 holds the vectors of the SOR sweeps, A and the
-// couplings; level 1 the vectors only; level 0 nothing (all in global).
-__device__ void place_in_smem(Work& k, float* s, int level, int C, int E) {
-  if (level < 1) return;
+// Shared memory holds what every SOR sweep reads, in this order of
+// priority, each array while the budget lasts: x, b, sa, sb (C E floats
+// each), the couplings (4 C E), the neighbour table (4 C ints), A (C E E).
+constexpr int kSmemItems = 7;
+
+__host__ __device__ inline int64_t smem_item_bytes(int i, int C, int E) {
   const int64_t CE = (int64_t) C * E;
-  float** vecs[] = {&k.x, &k.src_a, &k.src_b, &k.ls_a, &k.ls_b, &k.sa, &k.sb};
-  for (float** p : vecs) { *p = s; s += CE; }
-  if (level < 2) return;
-  k.A = s; s += CE * E;
-  k.nb = s;
+  switch (i) {
+    case 4: return 16 * CE;
+    case 5: return 16 * (int64_t) C;
+    case 6: return 4 * CE * E;
+    default: return 4 * CE;
+  }
 }
 
-// Bytes of dynamic shared memory at each level: the float arrays, then the
-// neighbour table (4 C ints).
-__host__ __device__ inline int64_t smem_bytes(int level, int C, int E) {
-  const int64_t CE = (int64_t) C * E;
-  if (level < 1) return 0;
-  int64_t f = 7 * CE;                      // kHotVecs
-  if (level >= 2) f += CE * E + 4 * CE;
-  return 4 * f + 16 * (int64_t) C;
+// Items placed (bit i) and their bytes for a budget.
+inline int smem_plan(int C, int E, int64_t budget, int64_t* bytes) {
+  int mask = 0;
+  int64_t used = 0;
+  for (int i = 0; i < kSmemItems; i++) {
+    const int64_t n = smem_item_bytes(i, C, E);
+    if (used + n <= budget) {
+      mask |= 1 << i;
+      used += n;
+    }
+  }
+  *bytes = used;
+  return mask;
+}
+
+// Points the placed arrays at shared memory (the neighbour table is copied
+// in; the caller syncs before it is read).
+__device__ void place_in_smem(Work& k, char* s, int mask, const CmfdArgs& a) {
+  const int C = a.C, E = a.E;
+  float** vecs[] = {&k.x, &k.b, &k.sa, &k.sb, &k.nb};
+  for (int i = 0; i < kSmemItems; i++) {
+    if (!(mask & (1 << i))) continue;
+    if (i < 5) {
+      *vecs[i] = reinterpret_cast<float*>(s);
+    } else if (i == 5) {
+      int32_t* t = reinterpret_cast<int32_t*>(s);
+      for (int q = threadIdx.x; q < 4 * C; q += blockDim.x) t[q] = a.nbr_j[q];
+      k.nbr = t;
+    } else {
+      k.A = reinterpret_cast<float*>(s);
+    }
+    s += smem_item_bytes(i, C, E);
+  }
 }
 
 __device__ __forceinline__ int neighbour(const CmfdArgs& a, int c, int f) {
@@ -513,6 +541,9 @@ __device__ bool dd_linear_solve(const CmfdArgs& a, const Work& k,
     arow[(int64_t) e * C] = diag + dd;
   }
   __syncthreads();
+  // b (on chip) takes the right sides b0 + dd x; b0 waits in k.rhs
+  float* bw = const_cast<float*>(b);
+  for (int r = threadIdx.x; r < CE; r += blockDim.x) k.rhs[r] = b[r];
   float* old_src = k.dd_a;
   float* new_src = k.dd_b;
   mat_fission<EC>(a, k, k.x, new_src);
@@ -524,9 +555,9 @@ __device__ bool dd_linear_solve(const CmfdArgs& a, const Work& k,
     old_src = new_src;
     new_src = t;
     for (int r = threadIdx.x; r < CE; r += blockDim.x)
-      k.rhs[r] = b[r] + k.ddv[r] * k.x[r];
+      bw[r] = k.rhs[r] + k.ddv[r] * k.x[r];
     __syncthreads();
-    linear_solve<EC>(a, k, k.rhs, tol, red, sweeps);   // a failure is only noted
+    linear_solve<EC>(a, k, bw, tol, red, sweeps);   // a failure is only noted
     mat_fission<EC>(a, k, k.x, new_src);
     __syncthreads();
     const double res = rmse(a, new_src, old_src, red);
@@ -545,6 +576,7 @@ __device__ bool dd_linear_solve(const CmfdArgs& a, const Work& k,
   for (int r = threadIdx.x; r < CE; r += blockDim.x) {
     const int e = r / C, j = r - e * C;
     k.A[((int64_t) e * E + e) * C + j] -= k.ddv[r];
+    bw[r] = k.rhs[r];
   }
   __syncthreads();
   return true;
@@ -552,22 +584,17 @@ __device__ bool dd_linear_solve(const CmfdArgs& a, const Work& k,
 
 template <int EC>
 __global__ void __launch_bounds__(kSolveThreads, 1)
-cmfd_solve_kernel(const CmfdArgs a, int smem_level) {
+cmfd_solve_kernel(const CmfdArgs a, int smem_mask) {
   DevScalars* sc = a.sc;
   if (*(volatile int*) &sc->done) return;
   __shared__ double red[32];
-  extern __shared__ float s_dyn[];
+  extern __shared__ float4 s_dyn[];
   const int C = a.C, E = a.E;
   const int CE = C * E;
   Work k = carve(a.work, C, E);
-  place_in_smem(k, s_dyn, smem_level, C, E);
   k.nbr = a.nbr_j;
-  if (smem_level >= 1) {
-    int32_t* s_nbr = reinterpret_cast<int32_t*>(
-        reinterpret_cast<char*>(s_dyn) + smem_bytes(smem_level, C, E) - 16 * C);
-    for (int i = threadIdx.x; i < 4 * C; i += blockDim.x) s_nbr[i] = a.nbr_j[i];
-    k.nbr = s_nbr;             // read after the barrier below the collapse
-  }
+  // the neighbour table copy is read after the barrier below the collapse
+  place_in_smem(k, reinterpret_cast<char*>(s_dyn), smem_mask, a);
   CmfdDevState* cm = a.cm;
   const int it = sc->iteration;                 // MOC iteration
   // the coarse tolerance follows the transport residual
@@ -588,8 +615,8 @@ cmfd_solve_kernel(const CmfdArgs a, int smem_level) {
   const double rows = (double) CE;
   const double tol = fmax(kLinalgTol, src_thr);
   const double lin_tol = fmax(kLinalgTol, tol * 1e-1);
-  float* src_old = k.src_a;
-  float* src_new = k.src_b;
+  float* src_old = k.b;          // the SOR's right side, on chip if placed
+  float* src_new = k.src_a;
   mat_fission<EC>(a, k, k.x, src_old);
   const double s0 = block_total(src_old, CE, red);
   bool failed = !(s0 > 0.0) || !isfinite(s0);
@@ -624,9 +651,8 @@ cmfd_solve_kernel(const CmfdArgs a, int smem_level) {
       __syncthreads();
       const double res = rmse(a, src_new, src_old, red);
       if (power == 0) initial = res < 1e-14 ? 1e-10 : res;
-      float* t = src_old;
-      src_old = src_new;
-      src_new = t;
+      for (int r = threadIdx.x; r < CE; r += blockDim.x) src_old[r] = src_new[r];
+      __syncthreads();
       if ((res / initial < 0.03 || res < kLinalgTol) && power > kMinIters) {
         power++;
         break;
@@ -749,10 +775,9 @@ void launch_cmfd_solve(const CmfdArgs& a, cudaStream_t s) {
   // one thread per cell of a colour, at least four warps
   int threads = (std::max(a.n_color0, a.C - a.n_color0) + 31) / 32 * 32;
   threads = std::max(128, std::min(kSolveThreads, threads));
-  const int64_t level1 = smem_bytes(1, a.C, a.E);
-  const int64_t level2 = smem_bytes(2, a.C, a.E);
-  const int level = level2 <= kSolveSmemMax ? 2 : level1 <= kSolveSmemMax ? 1 : 0;
-  const int smem = (int) smem_bytes(level, a.C, a.E);
+  int64_t bytes = 0;
+  const int level = smem_plan(a.C, a.E, kSolveSmemMax, &bytes);   // item mask
+  const int smem = (int) bytes;
   switch (a.E) {
     case 1: solve_instance<1>(a, threads, smem, level, s); break;
     case 2: solve_instance<2>(a, threads, smem, level, s); break;
