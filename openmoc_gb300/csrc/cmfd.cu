@@ -78,6 +78,7 @@ cmfd_pair_sums_kernel(const float* __restrict__ phi,
 // phi[r][g] *= ratio[cell(r)][coarse group(g)] (Cmfd::updateMOCFlux,
 // src/Cmfd.cpp:1509-1560).
 __global__ void cmfd_prolong_kernel(float* __restrict__ phi,
+                                    float2* __restrict__ mom,
                                     const int32_t* __restrict__ fsr_cell,
                                     const int32_t* __restrict__ group_of,
                                     const float* __restrict__ ratio,
@@ -90,7 +91,12 @@ __global__ void cmfd_prolong_kernel(float* __restrict__ phi,
     const int64_t r = i / ld;
     const int g = (int) (i - r * ld);
     if (g >= G) continue;
-    phi[i] *= ratio[(int64_t) fsr_cell[r] * E + group_of[g]];
+    const float q = ratio[(int64_t) fsr_cell[r] * E + group_of[g]];
+    phi[i] *= q;
+    if (mom) {                 // linear source: the moments of the group too
+      float2 m = mom[i];
+      mom[i] = make_float2(m.x * q, m.y * q);
+    }
   }
 }
 
@@ -791,15 +797,16 @@ void launch_cmfd_solve(const CmfdArgs& a, cudaStream_t s) {
   }
 }
 
-void launch_cmfd_prolong(float* phi, const int32_t* fsr_cell,
+void launch_cmfd_prolong(float* phi, float* mom, const int32_t* fsr_cell,
                          const int32_t* group_of, const float* ratio,
                          int64_t R, int G, int ld, int E, DevScalars* sc,
                          cudaStream_t s) {
   const int64_t n = R * ld;
   int blocks = (int) std::min<int64_t>((n + 255) / 256, (int64_t) 8 * sm_count());
   if (blocks < 1) blocks = 1;
-  cmfd_prolong_kernel<<<blocks, 256, 0, s>>>(phi, fsr_cell, group_of, ratio, R,
-                                             G, ld, E, sc);
+  cmfd_prolong_kernel<<<blocks, 256, 0, s>>>(
+      phi, reinterpret_cast<float2*>(mom), fsr_cell, group_of, ratio, R, G, ld,
+      E, sc);
 }
 
 }  // namespace moc

@@ -84,7 +84,9 @@ struct LsOccupancy {
   static constexpr int min_blocks = (PH * PS >= 12) ? 4 : (PH * PS >= 6) ? 5 : 6;
 };
 
-template <int PH, int LPS, int PS>
+// CM: also the CMFD partial currents (a.cm_cell set), as the flat sweep's
+// mode 2.
+template <int PH, int LPS, int PS, bool CM>
 __global__ void __launch_bounds__(kSweepThreads,
                                   (LsOccupancy<PH, PS>::min_blocks))
 ls_sweep_kernel(const SweepArgs a) {
@@ -243,6 +245,11 @@ ls_sweep_kernel(const SweepArgs a) {
           atomicAdd(pm + s * LPS, make_float4(mx.x, my.x, mx.y, my.y));
         }
       }
+      if constexpr (CM) {
+        const int fsr_next = (k + 1 < n) ? (wnext.y & 0xFFFFFF) : -1;
+        cmfd_tally_crossing<PH, LPS, PS>(a, t, dir, fsr, fsr_next, k + 1 == n,
+                                         sub, npairs, ld, w2, psi);
+      }
       wcur = wnext;
     }
 
@@ -289,7 +296,8 @@ void launch_ls_instance(const SweepArgs& a, cudaStream_t stream) {
   const int wpb = kSweepThreads / 32;
   const int64_t blocks = (warps + wpb - 1) / wpb;
   const size_t smem = sizeof(float) * (size_t) a.num_materials * a.ld;
-  auto kern = ls_sweep_kernel<PH, LPS, PS>;
+  auto kern = a.cm_cell ? ls_sweep_kernel<PH, LPS, PS, true>
+                        : ls_sweep_kernel<PH, LPS, PS, false>;
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int) smem);

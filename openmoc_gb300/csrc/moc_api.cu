@@ -193,6 +193,7 @@ struct moc_ctx {
   // of the sums and currents; the host coarse solver
   moc_cmfd::Solver* cmfd = nullptr;
   std::vector<int32_t> h_cm_cell;
+  std::vector<double> cm_edc_mu_h, cm_edc_w_h;   // as given (flat source)
   int32_t* cm_cell = nullptr;
   int8_t* cm_end = nullptr;
   float* cm_cur = nullptr;
@@ -291,7 +292,7 @@ moc::SweepArgs sweep_args(moc_ctx* c, int check_done) {
     a.qxy = c->qxy;
     a.mom = c->mom;
   }
-  if (c->cmfd && !c->ls && !c->otf) {
+  if (c->cmfd && !c->otf) {
     a.cm_cell = c->cm_cell;
     a.cm_cur = c->cm_cur;
     a.cm_end = c->cm_end;
@@ -796,6 +797,10 @@ int cmfd_prepare(moc_ctx* c) {
     if (c->cm_host) MOC_CUDA(cudaMallocHost(&c->h_cm_sums, 8 * n));
     c->cm_sums_n = n;
   }
+  // Larsen's factor is for flat sources only (Cmfd::
+  // getSurfaceDiffusionCoefficient, src/Cmfd.cpp:1082-1083, 1125-1126)
+  S.cfg.edc_mu = c->ls ? std::vector<double>() : c->cm_edc_mu_h;
+  S.cfg.edc_w = c->ls ? std::vector<double>() : c->cm_edc_w_h;
   S.reset();
   S.source_threshold = 0.1 * c->threshold;   // Solver::initializeCmfd
   if (c->cm_host) return MOC_OK;
@@ -815,6 +820,7 @@ int cmfd_prepare(moc_ctx* c) {
             ss[((size_t) m * G + g) * G + h];
     }
   std::vector<float> cvol(F.cell_vol.begin(), F.cell_vol.end());
+  // (cf.edc_* were set for this solve above)
   std::vector<float> wx(cf.wx.begin(), cf.wx.end()), wy(cf.wy.begin(), cf.wy.end());
   std::vector<float> mu(cf.edc_mu.begin(), cf.edc_mu.end());
   std::vector<float> ew(cf.edc_w.begin(), cf.edc_w.end());
@@ -972,12 +978,17 @@ int run_cmfd_iterations(moc_ctx* c, int res_type) {
         moc::launch_cmfd_solve(ca, c->stream);
         c->launches++;
       }
-      moc::launch_cmfd_prolong(c->phi, c->cm_cell, c->cm_group, c->cm_ratio,
-                               c->d.num_fsrs, c->d.num_groups, ld, E, c->sc,
-                               c->stream);
+      moc::launch_cmfd_prolong(c->phi, c->ls ? c->mom : nullptr, c->cm_cell,
+                               c->cm_group, c->cm_ratio, c->d.num_fsrs,
+                               c->d.num_groups, ld, E, c->sc, c->stream);
       moc::launch_fission_rate(a, 1, c->stream);
+      c->launches += 2;
+      if (c->ls) {     // normalizeFluxes scales the moments too
+        moc::launch_ls_scale_moments(a, c->stream);
+        c->launches++;
+      }
       moc::launch_residual(a, res_type, 1, 1, 1, c->stream);
-      c->launches += 3;
+      c->launches++;
       MOC_CUDA(cudaGetLastError());
     }
     MOC_TRY(pull(c));
@@ -1649,9 +1660,8 @@ int moc_compute_eigenvalue(moc_ctx* c, int max_iters, int res_type) {
   MOC_CHECK(c->num_fissionable > 0, MOC_ERR_ARG,
             "an eigenvalue solve needs fissionable material");
   if (c->cmfd) {
-    MOC_CHECK(!c->ls && !c->otf, MOC_ERR_UNSUPPORTED,
-              "CMFD acceleration of a linear-source or on-the-fly solve is "
-              "not supported");
+    MOC_CHECK(!c->otf, MOC_ERR_UNSUPPORTED,
+              "CMFD acceleration of an on-the-fly solve is not supported");
     MOC_TRY(cmfd_prepare(c));
   }
   MOC_TRY(maybe_autotune(c));
@@ -2432,9 +2442,8 @@ int moc_set_cmfd(moc_ctx* c, const moc_cmfd_mesh* m) {
     }
     return MOC_OK;
   }
-  MOC_CHECK(!c->ls && !c->otf, MOC_ERR_UNSUPPORTED,
-            "CMFD is supported for 2D flat-source solves with stored "
-            "segments");
+  MOC_CHECK(!c->otf, MOC_ERR_UNSUPPORTED,
+            "CMFD is supported for 2D solves with stored segments");
   MOC_CHECK(!(c->exp_user_set && c->exp_kind == MOC_EXP_TABLE),
             MOC_ERR_UNSUPPORTED,
             "CMFD current tallies use the hardware exponential");
@@ -2501,8 +2510,8 @@ int moc_set_cmfd(moc_ctx* c, const moc_cmfd_mesh* m) {
   cf.group_of = group_of;
   cf.gstart.assign(E + 1, G);
   for (int g = G - 1; g >= 0; g--) cf.gstart[group_of[g]] = g;
-  cf.edc_mu.assign(m->edc_mu, m->edc_mu + m->num_edc_angles);
-  cf.edc_w.assign(m->edc_weight, m->edc_weight + m->num_edc_angles);
+  c->cm_edc_mu_h.assign(m->edc_mu, m->edc_mu + m->num_edc_angles);
+  c->cm_edc_w_h.assign(m->edc_weight, m->edc_weight + m->num_edc_angles);
   for (int f = 0; f < 4; f++) cf.bc[f] = m->boundary[f];
   cf.relaxation = m->relaxation;
   cf.sor = m->sor_factor;

@@ -367,7 +367,8 @@ void launch_cmfd_pair_sums(const float* phi, const float* vol,
                            const int32_t* pair_off, const int32_t* pair_fsr,
                            int P, int G, int ld, double* out, DevScalars* sc,
                            cudaStream_t s);
-void launch_cmfd_prolong(float* phi, const int32_t* fsr_cell,
+// mom (linear source, [R][ld][2]) is scaled with phi when not null.
+void launch_cmfd_prolong(float* phi, float* mom, const int32_t* fsr_cell,
                          const int32_t* group_of, const float* ratio,
                          int64_t R, int G, int ld, int E, DevScalars* sc,
                          cudaStream_t s);

@@ -140,6 +140,60 @@ struct SweepOccupancy {
                              : 8;
 };
 
+// CMFD partial currents (mode 2 of the sweeps): faces 0 x-, 1 y-, 2 x+,
+// 3 y+ of cell iy * nx + ix; a crossing adds sum_p w_p psi_p of the lane's
+// group pairs (Cmfd::tallyCurrent, src/Cmfd.h:572-660).
+template <int PH, int LPS, int PS>
+__device__ __forceinline__ void cmfd_add_current(
+    const SweepArgs& a, int cell, int face, float frac, int sub, int npairs,
+    int ld, const float2 (&w2)[PH], const float2 (&psi)[PS][PH]) {
+  float2* cp = reinterpret_cast<float2*>(
+                   a.cm_cur + ((int64_t) cell * 4 + face) * ld) + sub;
+#pragma unroll
+  for (int s2 = 0; s2 < PS; s2++) {
+    if (sub + s2 * LPS < npairs) {
+      float2 j = f2(0.0f);
+#pragma unroll
+      for (int p = 0; p < PH; p++) j = __ffma2_rn(w2[p], psi[s2][p], j);
+      atomicAdd(cp + s2 * LPS, __fmul2_rn(j, f2(frac)));
+    }
+  }
+}
+
+// The current out of segment f0's coarse cell when the next segment f1
+// lies in another (a corner crossing half by each neighbouring cell,
+// Cmfd::splitEdgeCurrents, src/Cmfd.cpp:2249-2345), or, at the end of the
+// track (f1 < 0), through the boundary face of the track end.
+template <int PH, int LPS, int PS>
+__device__ __forceinline__ void cmfd_tally_crossing(
+    const SweepArgs& a, int t, int dir, int f0, int f1, bool at_end, int sub,
+    int npairs, int ld, const float2 (&w2)[PH], const float2 (&psi)[PS][PH]) {
+  const int c0 = __ldg(a.cm_cell + f0);
+  if (f1 >= 0) {
+    const int c1 = __ldg(a.cm_cell + f1);
+    if (c1 == c0) return;
+    const int dx = c1 % a.cm_nx - c0 % a.cm_nx;
+    const int dy = c1 / a.cm_nx - c0 / a.cm_nx;
+    const int fx = dx > 0 ? 2 : 0, fy = dy > 0 ? 3 : 1;
+    if (dx != 0 && dy != 0) {
+      cmfd_add_current<PH, LPS, PS>(a, c0, fx, 0.5f, sub, npairs, ld, w2, psi);
+      cmfd_add_current<PH, LPS, PS>(a, c0 + dx, fy, 0.5f, sub, npairs, ld, w2,
+                                    psi);
+      cmfd_add_current<PH, LPS, PS>(a, c0, fy, 0.5f, sub, npairs, ld, w2, psi);
+      cmfd_add_current<PH, LPS, PS>(a, c0 + dy * a.cm_nx, fx, 0.5f, sub,
+                                    npairs, ld, w2, psi);
+    } else {
+      cmfd_add_current<PH, LPS, PS>(a, c0, dx != 0 ? fx : fy, 1.0f, sub, npairs,
+                                    ld, w2, psi);
+    }
+  } else if (at_end) {
+    const int face = a.cm_end[2 * t + dir];
+    if (face >= 0)
+      cmfd_add_current<PH, LPS, PS>(a, c0, face, 1.0f, sub, npairs, ld, w2,
+                                    psi);
+  }
+}
+
 // MODE 1: the tracks of many solves (a batched pool); each track takes its
 // pending angular-flux scale and done flag from its own solve's state.
 // MODE 2: one problem, also tallying the partial currents out of the
@@ -312,44 +366,9 @@ sweep_kernel(const SweepArgs a) {
     float len = 0.0f;
     int fsr = 0, mat = 0;
     float2 q[PS];
-    // CMFD partial currents: faces 0 x-, 1 y-, 2 x+, 3 y+ of cell
-    // iy * nx + ix; each crossing adds sum_p w_p psi_p of the lane's pairs
-    auto add_current = [&](int cell, int face, float frac) {
-      float2* cp = reinterpret_cast<float2*>(
-                       a.cm_cur + ((int64_t) cell * 4 + face) * ld) + sub;
-#pragma unroll
-      for (int s2 = 0; s2 < PS; s2++) {
-        if (sub + s2 * LPS < npairs) {
-          float2 j = f2(0.0f);
-#pragma unroll
-          for (int p = 0; p < PH; p++) j = __ffma2_rn(w2[p], psi[s2][p], j);
-          atomicAdd(cp + s2 * LPS, __fmul2_rn(j, f2(frac)));
-        }
-      }
-    };
     auto tally_current = [&](int f0, int f1, bool at_end) {
-      const int c0 = __ldg(a.cm_cell + f0);
-      if (f1 >= 0) {
-        const int c1 = __ldg(a.cm_cell + f1);
-        if (c1 == c0) return;
-        const int dx = c1 % a.cm_nx - c0 % a.cm_nx;
-        const int dy = c1 / a.cm_nx - c0 / a.cm_nx;
-        const int fx = dx > 0 ? 2 : 0, fy = dy > 0 ? 3 : 1;
-        if (dx != 0 && dy != 0) {
-          // through a corner: half by the x neighbour, half by the y one
-          add_current(c0, fx, 0.5f);
-          add_current(c0 + dx, fy, 0.5f);
-          add_current(c0, fy, 0.5f);
-          add_current(c0 + dy * a.cm_nx, fx, 0.5f);
-        } else if (dx != 0) {
-          add_current(c0, fx, 1.0f);
-        } else {
-          add_current(c0, fy, 1.0f);
-        }
-      } else if (at_end) {
-        const int face = a.cm_end[2 * t + dir];
-        if (face >= 0) add_current(c0, face, 1.0f);
-      }
+      cmfd_tally_crossing<PH, LPS, PS>(a, t, dir, f0, f1, at_end, sub, npairs,
+                                       ld, w2, psi);
     };
     if constexpr (kStaged) {
 #pragma unroll

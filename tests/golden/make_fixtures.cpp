@@ -910,6 +910,29 @@ int main(int argc, char** argv) {
     cases.push_back(cs);
   }
 
+  /* 15. the reflective 3x3 lattice of case 13 with the linear source
+   *     (CPULSSolver with CMFD: no Larsen factor, moments prolonged); SOR
+   *     factor 1.0 as tests/test_cmfd_linear_source sets it (at 1.5
+   *     OpenMOC's FP32 coarse solve fails on this case) */
+  {
+    Material* fuel = make_material(27, "fuel7cl",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 5, 7, true));
+    Material* mod = make_material(28, "mod7cl",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 1005, 7, false));
+    Geometry* geo = lattice_geometry(3, fuel, mod, pin, {4}, REF, REF, REF,
+                                     REF);
+    Cmfd* cm = new Cmfd();
+    cm->setLatticeStructure(3, 3);
+    cm->setGroupStructure({{1, 2, 3}, {4, 5, 6, 7}});
+    cm->setCMFDRelaxationFactor(0.7);
+    cm->setSORRelaxationFactor(1.0);
+    geo->setCmfd(cm);
+    CaseSpec cs = {"cmfd_lat3_ls", geo, 16, 0.1, 1000, 1e-5, FISSION_SOURCE,
+                   EIGEN, 1.0, false, NULL, 0.0, 0, 0.0, true, false, NULL};
+    cs.cmfd = cm;
+    cases.push_back(cs);
+  }
+
   for (const CaseSpec& c : cases) {
     if (!only.empty() && only != c.name) continue;
     run_case(c, outdir);

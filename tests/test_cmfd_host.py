@@ -82,6 +82,7 @@ def test_cmfd_fixtures_hold_a_mesh(case):
     from openmoc_gb300 import Cmfd
     p, sc, _ = load_case(case, "f32")
     g = p.cmfd_geometry
+    assert (p.linear_source is not None) == case.endswith("_ls")
     assert g["end_face"].size == 2 * p.num_tracks
     assert g["fsr_cell"].size == p.num_fsrs
     c = Cmfd()

@@ -12,7 +12,7 @@ unaccelerated GPU solve.
 import numpy as np
 import pytest
 
-from conftest import CMFD_CASES, load_case
+from conftest import CMFD_CASES, CMFD_SOR, load_case
 
 pytestmark = pytest.mark.gpu
 
@@ -23,7 +23,7 @@ def _rel(got, ref, floor):
                         np.maximum(np.abs(ref), floor * np.abs(ref).max())))
 
 
-def _cmfd(p, groups, host=False):
+def _cmfd(p, groups, host=False, sor=1.5):
     from openmoc_gb300 import Cmfd
     c = Cmfd()
     c.useHostSolver(host)
@@ -32,7 +32,7 @@ def _cmfd(p, groups, host=False):
     c.setLatticeStructure(nx, ny)
     if groups is not None:
         c.setGroupStructure(groups)
-    c.setSORRelaxationFactor(1.5)
+    c.setSORRelaxationFactor(sor)
     c.setCMFDRelaxationFactor(0.7)
     return c
 
@@ -41,13 +41,15 @@ def _cmfd(p, groups, host=False):
 @pytest.mark.parametrize("precision", ["f32", "f64"])
 @pytest.mark.parametrize("host", [False, True])
 def test_gpu_cmfd_matches_openmoc(case, precision, host):
-    """The coarse solve on the GPU (FP32) or on the host (FP64)."""
-    from openmoc_gb300 import GB300Solver
+    """The coarse solve on the GPU (FP32) or on the host (FP64); the
+    linear-source case through GB300LSSolver (moments prolonged, no Larsen
+    factor)."""
+    from openmoc_gb300 import GB300LSSolver, GB300Solver
     p, sc, arr = load_case(case, precision)
-    s = GB300Solver(device=0)
+    s = (GB300LSSolver if p.linear_source is not None else GB300Solver)(device=0)
     s.setConvergenceThreshold(sc["tolerance"])
     s.setTrackGenerator(p)
-    s.setCmfd(_cmfd(p, CMFD_CASES[case], host))
+    s.setCmfd(_cmfd(p, CMFD_CASES[case], host, CMFD_SOR[case]))
     s.computeEigenvalue(int(sc["max_iters"]), int(sc["res_type"]))
     info = s.getCmfdInfo()
     assert info["enabled"] and info["power_iterations"] > 25
@@ -125,7 +127,7 @@ def test_gpu_cmfd_detach_restores_plain_solve():
 
 
 def test_gpu_cmfd_bad_requests_raise():
-    from openmoc_gb300 import Cmfd, GB300LSSolver, GB300Solver
+    from openmoc_gb300 import Cmfd, GB300Solver
     from openmoc_gb300 import lattice as lat
     from openmoc_gb300._native import MOCError
     p = lat.square_lattice(3, 7, 16, 0.1, 0)
@@ -140,13 +142,6 @@ def test_gpu_cmfd_bad_requests_raise():
     with pytest.raises(MOCError):
         s.setCmfd(c)
     s.close()
-    pl = lat.pin_cell(7, linear_source=True)
-    ls = GB300LSSolver(pl, device=0)
-    c = Cmfd()
-    c.setLatticeStructure(1, 1)
-    with pytest.raises(MOCError):
-        ls.setCmfd(c)
-    ls.close()
 
 
 def test_gpu_cmfd_uses_native_library():
@@ -205,4 +200,39 @@ def test_gpu_cmfd_matches_oracle_step_by_step(host):
     assert np.max(np.abs(new - cm.new_flux)) < 1e-4 * np.abs(cm.new_flux).max()
     assert np.max(np.abs(old - cm.old_flux)) < 1e-4 * np.abs(cm.old_flux).max()
     assert abs(s.getCmfdInfo()["keff"] - cm.keff) < 2e-6
+    s.close()
+
+
+def test_gpu_cmfd_linear_source_converges_to_unaccelerated_answer():
+    """A generated 5 x 5 lattice with the linear source, vacuum on +x and
+    +y: CMFD (moments prolonged) reaches the unaccelerated linear-source
+    solution in fewer iterations."""
+    from openmoc_gb300 import Cmfd, GB300LSSolver
+    from openmoc_gb300 import lattice as lat
+    from openmoc_gb300.lattice import REFLECTIVE, VACUUM
+    mats = lat._fuel_mod(2, 7, 1)
+    pm = np.zeros((5, 5), np.int32)
+    for (r, c) in [(1, 1), (2, 3), (3, 2)]:
+        pm[r, c] = 1
+    p = lat.lattice(5, 5, pm, mats, 1, num_azim=16, spacing=0.1,
+                    bc=(REFLECTIVE, VACUUM, REFLECTIVE, VACUUM),
+                    linear_source=True)
+    ref = GB300LSSolver(p, device=0)
+    ref.setConvergenceThreshold(1e-6)
+    ref.computeEigenvalue(3000, 1)
+    s = GB300LSSolver(p, device=0)
+    s.setConvergenceThreshold(1e-6)
+    c = Cmfd()
+    c.setLatticeStructure(5, 5)
+    c.setGroupStructure([[1, 2, 3], [4, 5, 6, 7]])
+    c.setSORRelaxationFactor(1.0)
+    s.setCmfd(c)
+    s.computeEigenvalue(3000, 1)
+    assert s.getNumIterations() < ref.getNumIterations()
+    assert abs(s.getKeff() - ref.getKeff()) < 5e-6
+    assert _rel(s.getFluxes(), ref.getFluxes(), 1e-3) < 1e-4
+    R, G = p.num_fsrs, p.num_groups
+    m, mr = s.getFluxMoments(), ref.getFluxMoments()
+    assert np.max(np.abs(m - mr)) < 2e-4 * np.abs(mr).max()
+    ref.close()
     s.close()
