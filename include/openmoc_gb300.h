@@ -339,7 +339,7 @@ int moc_get_otf_tracks(moc_ctx* ctx, int* enabled);
 
 /* ---- CMFD acceleration ----------------------------------------------------
  * Coarse-mesh finite-difference acceleration of moc_compute_eigenvalue
- * (2D flat-source problems; replaces the reference's Cmfd, src/Cmfd.h, as
+ * (2D problems, flat or linear source; replaces the reference's Cmfd, src/Cmfd.h, as
  * Geometry::setCmfd attaches it and Solver::computeEigenvalue calls
  * Cmfd::computeKeff in place of computeKeff, src/Solver.cpp:1597-1645).
  * Every iteration the sweep also tallies the partial currents out of the
@@ -386,9 +386,11 @@ typedef struct {
 } moc_cmfd_mesh;
 
 /** Attaches CMFD to the context (tracks, quadrature, materials and FSRs
- *  uploaded; not with a linear source or on-the-fly segmentation); NULL
- *  detaches it.  Dropped when tracks are re-uploaded.  Uses the hardware
- *  exponential (MOC_ERR_UNSUPPORTED if the table was requested). */
+ *  uploaded; not with on-the-fly segmentation); NULL detaches it.  With the
+ *  linear source the flux moments are prolonged too and Larsen's factor is
+ *  not applied (CPULSSolver's CMFD).  Dropped when tracks are re-uploaded.
+ *  Uses the hardware exponential (MOC_ERR_UNSUPPORTED if the table was
+ *  requested). */
 int moc_set_cmfd(moc_ctx* ctx, const moc_cmfd_mesh* mesh);
 /** Whether CMFD is attached, the last coarse eigenvalue, the coarse power
  *  iterations and SOR sweeps of the last coarse solve, its prolongation

@@ -1,7 +1,7 @@
 """CMFD acceleration settings: the Python face of ``moc_cmfd_mesh``.
 
 Mirrors the reference's ``openmoc.Cmfd`` (src/Cmfd.h) for what its
-eigenvalue acceleration of 2D flat-source problems uses: lattice structure
+eigenvalue acceleration of 2D problems (flat or linear source) uses: lattice structure
 and widths, group structure, CMFD and SOR relaxation factors, flux
 limiting, unbounded iterations.  Attach it with ``GB300Solver.setCmfd``
 (the reference attaches it to the Geometry, ``Geometry::setCmfd``).
@@ -103,8 +103,8 @@ class Cmfd:
         self._unbounded = int(n)
 
     def useLarsenEDC(self, on: bool) -> None:
-        """Larsen's effective diffusion coefficient correction (always on in
-        the reference's flat-source CMFD)."""
+        """Larsen's effective diffusion coefficient correction (on in the
+        reference's flat-source CMFD; never applied with a linear source)."""
         self._edc = bool(on)
 
     def useHostSolver(self, on: bool) -> None:
