@@ -383,6 +383,13 @@ typedef struct {
                                   build), with no host round trip; 1: on the
                                   host in FP64, tallies read back every
                                   iteration */
+  int32_t k_nearest;           /* 0: each FSR takes its cell's ratio;
+                                  1..9: Cmfd::setKNearest, the ratio
+                                  weighted over the nearest of the 3 x 3
+                                  cells around it by centroid distance */
+  const double* fsr_centroid;  /* [R][2] (x, y), needed when k_nearest > 0
+                                  (TrackGenerator::generateFSRCentroids) */
+  double origin_x, origin_y;   /* the mesh's x-min / y-min corner */
 } moc_cmfd_mesh;
 
 /** Attaches CMFD to the context (tracks, quadrature, materials and FSRs

@@ -53,11 +53,12 @@ int moc_lattice_export(moc_lattice* lat, float* seg_len, int32_t* seg_fsr,
  *  2D lattice: per FSR the box of its lattice cell [R][4] (xmin, xmax,
  *  ymin, ymax), per track the boundary face at the end of its forward and
  *  backward traversal [T][2] (0 x-min, 1 y-min, 2 x-max, 3 y-max; -1 none),
- *  the Larsen-EDC quadrature [A][Ph] (cos theta; azimuthal x polar weight)
- *  and the geometry's bounds [4] (xmin, xmax, ymin, ymax). */
+ *  the Larsen-EDC quadrature [A][Ph] (cos theta; azimuthal x polar weight),
+ *  the geometry's bounds [4] (xmin, xmax, ymin, ymax) and, when centroid is
+ *  not NULL, the FSR centroids [R][2] for the k-nearest update. */
 int moc_lattice_export_cmfd(moc_lattice* lat, double* fsr_box,
                             int8_t* end_face, double* edc_mu, double* edc_w,
-                            double* bounds);
+                            double* bounds, double* centroid);
 int moc_lattice_destroy(moc_lattice* lat);
 
 /** moc_lattice_generate with the ray tracing on CUDA device `device`: the

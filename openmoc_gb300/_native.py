@@ -67,7 +67,9 @@ class CmfdMesh(C.Structure):
                 ("relaxation", C.c_double), ("sor_factor", C.c_double),
                 ("flux_limiting", C.c_int32),
                 ("num_unbounded_iterations", C.c_int32),
-                ("solve_on_host", C.c_int32)]
+                ("solve_on_host", C.c_int32), ("k_nearest", C.c_int32),
+                ("fsr_centroid", C.c_void_p), ("origin_x", C.c_double),
+                ("origin_y", C.c_double)]
 
 
 _P = C.c_void_p

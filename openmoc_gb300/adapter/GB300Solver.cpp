@@ -29,7 +29,8 @@
 GB300Solver::GB300Solver(TrackGenerator* track_generator, int device)
     : Solver(NULL), _ctx(NULL), _device(device), _exp_kind(-1),
       _uploaded(false), _cmfd_relaxation(0.7), _cmfd_sor(1.5),
-      _cmfd_flux_limiting(true), _cmfd_on_host(false), _cmfd_unbounded(0) {
+      _cmfd_flux_limiting(true), _cmfd_on_host(false), _cmfd_unbounded(0),
+      _cmfd_k_nearest(1) {
   _gpu_solver = true;
   if (track_generator != NULL) setTrackGenerator(track_generator);
 }
@@ -57,7 +58,8 @@ void GB300Solver::setExponentialEvaluator(int kind) {
 
 void GB300Solver::setCmfdFactors(double relaxation, double sor,
                                  bool flux_limiting, int unbounded_iterations,
-                                 bool on_host) {
+                                 bool on_host, int k_nearest) {
+  _cmfd_k_nearest = k_nearest;
   _cmfd_relaxation = relaxation;
   _cmfd_sor = sor;
   _cmfd_flux_limiting = flux_limiting;
@@ -77,9 +79,6 @@ void GB300Solver::attachCmfd() {
   }
   if (_SOLVE_3D || _cmfd->getNumZ() > 1)
     log_printf(ERROR, "GB300Solver supports CMFD on 2D meshes only");
-  if (_cmfd->isCentroidUpdateOn())
-    log_printf(ERROR, "GB300Solver supports the cell-average CMFD update "
-               "only (Cmfd::setKNearest(1))");
   const int nx = _cmfd->getNumX(), ny = _cmfd->getNumY();
   Lattice* lat = _cmfd->getLattice();
   std::vector<double> wx(lat->getWidthsX()), wy(lat->getWidthsY());
@@ -141,6 +140,21 @@ void GB300Solver::attachCmfd() {
   m.flux_limiting = _cmfd_flux_limiting ? 1 : 0;
   m.num_unbounded_iterations = _cmfd_unbounded;
   m.solve_on_host = _cmfd_on_host ? 1 : 0;
+  // the k-nearest update from the FSR centroids OpenMOC generated
+  // (Solver::initializeFSRs, src/Solver.cpp:865)
+  std::vector<double> cen;
+  if (_cmfd->isCentroidUpdateOn()) {
+    cen.resize(2 * _num_FSRs);
+    for (long r = 0; r < _num_FSRs; r++) {
+      Point* q = _geometry->getFSRCentroid(r);
+      cen[2 * r] = q->getX();
+      cen[2 * r + 1] = q->getY();
+    }
+    m.k_nearest = _cmfd_k_nearest;
+    m.fsr_centroid = cen.data();
+    m.origin_x = lat->getMinX();
+    m.origin_y = lat->getMinY();
+  }
   check(moc_set_cmfd(_ctx, &m), "moc_set_cmfd");
 }
 

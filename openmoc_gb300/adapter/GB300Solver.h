@@ -45,7 +45,7 @@ class GB300Solver : public Solver {
   void attachCmfd();
   double _cmfd_relaxation, _cmfd_sor;
   bool _cmfd_flux_limiting, _cmfd_on_host;
-  int _cmfd_unbounded;
+  int _cmfd_unbounded, _cmfd_k_nearest;
   int materialIndex(Material* m);
 
   /* Solver hooks (src/Solver.h:334-431) */
@@ -85,10 +85,13 @@ class GB300Solver : public Solver {
   /** The factors of the Geometry's Cmfd, which OpenMOC keeps private:
    *  relaxation (Cmfd::setCMFDRelaxationFactor, default 0.7), SOR factor
    *  (setSORRelaxationFactor, 1.5), flux limiting (useFluxLimiting, on),
-   *  unbounded iterations (setNumUnboundedIterations, 0); on_host runs the
-   *  coarse solve on the host in FP64 instead of on the GPU in FP32. */
+   *  unbounded iterations (setNumUnboundedIterations, 0), k of
+   *  setKNearest (used when the Cmfd's centroid update is on, default 1);
+   *  on_host runs the coarse solve on the host in FP64 instead of on the
+   *  GPU in FP32. */
   void setCmfdFactors(double relaxation, double sor, bool flux_limiting,
-                      int unbounded_iterations, bool on_host = false);
+                      int unbounded_iterations, bool on_host = false,
+                      int k_nearest = 1);
 
   /* device-resident source iteration */
   void computeEigenvalue(int max_iters = 1000,

@@ -37,6 +37,7 @@ class Cmfd:
         self._unbounded = 0             # src/Cmfd.cpp:35
         self._edc = True
         self._host = False
+        self._k_nearest = 0
         self._fsr_cell: Optional[np.ndarray] = None
 
     # ------------------------------------------------------------ settings
@@ -114,12 +115,13 @@ class Cmfd:
         self._host = bool(on)
 
     def setKNearest(self, k: int) -> None:
-        """Cmfd::setKNearest (src/Cmfd.cpp:3417): k = 1 is the plain
-        cell-average update; the centroid-weighted update is not built."""
-        if int(k) != 1:
-            raise _native.MOCError(_native.MOC_ERR_UNSUPPORTED,
-                                   "only the cell-average prolongation (k = 1) "
-                                   "is supported")
+        """Cmfd::setKNearest (src/Cmfd.cpp:3417): each FSR's update ratio
+        weighted over the k nearest of the 3 x 3 cells around it by the
+        distance from its centroid (k in 1..9)."""
+        if not 1 <= int(k) <= 9:
+            raise _native.MOCError(-1, "Unable to set CMFD k-nearest to "
+                                       f"{k}. k-nearest must be between 1 and 9.")
+        self._k_nearest = int(k)
 
     def setFSRCells(self, fsr_cell: np.ndarray) -> None:
         """The coarse cell of every FSR given directly (iy * num_x + ix, iy
@@ -176,14 +178,24 @@ class Cmfd:
         wx = np.ascontiguousarray(wx, np.float64)
         wy = np.ascontiguousarray(wy, np.float64)
         bc = np.asarray(geo["bc"], np.int32)
-        keep = [wx, wy, cell, end, group_of, mu, w]
+        cen = np.zeros(0, np.float64)
+        if self._k_nearest > 0:
+            if "fsr_centroid" in geo:
+                cen = np.ascontiguousarray(geo["fsr_centroid"], np.float64)
+            elif problem.linear_source is not None and "centroid" in problem.linear_source:
+                cen = np.ascontiguousarray(problem.linear_source["centroid"], np.float64)
+            else:
+                raise _native.MOCError(-1, "the k-nearest update needs the FSR "
+                                           "centroids")
+        keep = [wx, wy, cell, end, group_of, mu, w, cen]
         ptr = lambda a: a.ctypes.data if a.size else None  # noqa: E731
         m = _native.CmfdMesh(nx, ny, ptr(wx), ptr(wy), ptr(cell), ptr(end),
                              (_native.C.c_int32 * 4)(*[int(b) for b in bc]),
                              E, ptr(group_of), int(mu.size), ptr(mu), ptr(w),
                              self._relaxation, self._sor,
                              1 if self._flux_limiting else 0, self._unbounded,
-                             1 if self._host else 0)
+                             1 if self._host else 0, self._k_nearest, ptr(cen),
+                             float(bounds[0]), float(bounds[2]))
         return m, keep
 
 

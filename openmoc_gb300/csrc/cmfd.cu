@@ -82,16 +82,27 @@ __global__ void cmfd_prolong_kernel(float* __restrict__ phi,
                                     const int32_t* __restrict__ fsr_cell,
                                     const int32_t* __restrict__ group_of,
                                     const float* __restrict__ ratio,
-                                    int64_t R, int G, int ld, int E,
+                                    CmfdStencil st, int64_t R, int G, int ld,
+                                    int E, int unbounded,
                                     const DevScalars* sc) {
   if (*(volatile const int*) &sc->done) return;
+  const bool bound = sc->iteration > unbounded;
   const int64_t n = R * ld;
   for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t) gridDim.x * blockDim.x) {
     const int64_t r = i / ld;
     const int g = (int) (i - r * ld);
     if (g >= G) continue;
-    const float q = ratio[(int64_t) fsr_cell[r] * E + group_of[g]];
+    const int e = group_of[g];
+    float q;
+    if (st.off) {              // Cmfd::getUpdateRatio with k-nearest stencils
+      q = 0.0f;
+      for (int j = st.off[r]; j < st.off[r + 1]; j++)
+        q += st.coef[j] * ratio[(int64_t) st.cell[j] * E + e];
+    } else {
+      q = ratio[(int64_t) fsr_cell[r] * E + e];
+    }
+    if (bound) q = fminf(20.0f, fmaxf(0.05f, q));
     phi[i] *= q;
     if (mom) {                 // linear source: the moments of the group too
       float2 m = mom[i];
@@ -702,8 +713,8 @@ cmfd_solve_kernel(const CmfdArgs a, int smem_mask) {
     const int out = a.color_cells[j] * E + e;            // cell order
     const float xn = (float) (k.x[r] / sn);
     const float xo = (float) (k.phi_t[r] / so);
-    float q = fabs((double) xo) > kFluxEps ? xn / xo : 0.0f;
-    if (it > a.unbounded) q = fminf(20.0f, fmaxf(0.05f, q));
+    // bounded by the prolongation, after any k-nearest weighting
+    const float q = fabs((double) xo) > kFluxEps ? xn / xo : 0.0f;
     a.ratio[out] = q;
     a.flux_new[out] = xn;
     a.flux_old[out] = xo;
@@ -799,14 +810,15 @@ void launch_cmfd_solve(const CmfdArgs& a, cudaStream_t s) {
 
 void launch_cmfd_prolong(float* phi, float* mom, const int32_t* fsr_cell,
                          const int32_t* group_of, const float* ratio,
-                         int64_t R, int G, int ld, int E, DevScalars* sc,
+                         const CmfdStencil& st, int64_t R, int G, int ld,
+                         int E, int unbounded, DevScalars* sc,
                          cudaStream_t s) {
   const int64_t n = R * ld;
   int blocks = (int) std::min<int64_t>((n + 255) / 256, (int64_t) 8 * sm_count());
   if (blocks < 1) blocks = 1;
   cmfd_prolong_kernel<<<blocks, 256, 0, s>>>(
-      phi, reinterpret_cast<float2*>(mom), fsr_cell, group_of, ratio, R, G, ld,
-      E, sc);
+      phi, reinterpret_cast<float2*>(mom), fsr_cell, group_of, ratio, st, R, G,
+      ld, E, unbounded, sc);
 }
 
 }  // namespace moc

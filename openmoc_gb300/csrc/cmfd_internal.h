@@ -46,6 +46,17 @@ struct Stats {
   bool failed = false;              // the last coarse solve did not converge
 };
 
+// The k-nearest prolongation of Cmfd::getUpdateRatio (src/Cmfd.cpp:
+// 3178-3220) with the stencils of Cmfd::generateKNearestStencils
+// (src/Cmfd.cpp:2887-2960) as per-FSR coefficients: the update ratio of FSR
+// r is sum over j in [off[r], off[r+1]) of coef[j] * ratio[cell[j]].
+void knearest_coefficients(const Config& cfg, int k, double origin_x,
+                           double origin_y, const double* centroid,
+                           const int32_t* fsr_cell, int64_t R,
+                           std::vector<int32_t>& off,
+                           std::vector<int32_t>& cell,
+                           std::vector<float>& coef);
+
 class Solver {
  public:
   Config cfg;

@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <limits>
 
 namespace moc_cmfd {
 
@@ -428,14 +429,84 @@ double Solver::step(int moc_iter, const double* S, const float* cur, int ld) {
   for (double& v : phi_new) v /= sn;
   for (double& v : phi_old) v /= so;
   for (size_t i = 0; i < ratio.size(); i++) {
-    double r = std::fabs(phi_old[i]) > kFluxEpsilon ? phi_new[i] / phi_old[i]
-                                                    : 0.0;
-    if (moc_iter > cfg.unbounded) r = std::min(20.0, std::max(0.05, r));
+    // bounded to [0.05, 20] by the prolongation, after any k-nearest
+    // weighting (Cmfd::updateMOCFlux, src/Cmfd.cpp:1530-1540)
+    const double r = std::fabs(phi_old[i]) > kFluxEpsilon
+                         ? phi_new[i] / phi_old[i] : 0.0;
     ratio[i] = r;
     if (r > 0.0 && std::fabs(std::log(r)) > std::fabs(std::log(stats.max_ratio)))
       stats.max_ratio = r;
   }
   return keff;
+}
+
+void knearest_coefficients(const Config& cfg, int k, double origin_x,
+                           double origin_y, const double* centroid,
+                           const int32_t* fsr_cell, int64_t R,
+                           std::vector<int32_t>& off,
+                           std::vector<int32_t>& cell,
+                           std::vector<float>& coef) {
+  // cell centres from the accumulated widths
+  std::vector<double> cx(cfg.nx), cy(cfg.ny);
+  double acc = 0.0;
+  for (int i = 0; i < cfg.nx; i++) {
+    cx[i] = acc + cfg.wx[i] / 2;
+    acc += cfg.wx[i];
+  }
+  acc = 0.0;
+  for (int i = 0; i < cfg.ny; i++) {
+    cy[i] = acc + cfg.wy[i] / 2;
+    acc += cfg.wy[i];
+  }
+  constexpr double kFar = 1.0e300;   // FLT_INFINITY, src/constants.h:18
+  off.assign(R + 1, 0);
+  cell.clear();
+  coef.clear();
+  std::vector<std::pair<int, double>> st;
+  for (int64_t r = 0; r < R; r++) {
+    const int c = fsr_cell[r], ix = c % cfg.nx, iy = c / cfg.nx;
+    const double dx = centroid[2 * r] - origin_x;
+    const double dy = centroid[2 * r + 1] - origin_y;
+    // distances to the 3 x 3 cells around (stencil 0..8, row by row from
+    // y-min; 4 is the FSR's own cell), the missing ones infinitely far
+    st.clear();
+    for (int j = 0; j < 9; j++) {
+      const int sx = ix + j % 3 - 1, sy = iy + j / 3 - 1;
+      double d = std::numeric_limits<double>::max();
+      if (sx >= 0 && sx < cfg.nx && sy >= 0 && sy < cfg.ny)
+        d = std::pow(std::pow(dx - cx[sx], 2.0) + std::pow(dy - cy[sy], 2.0),
+                     0.5);
+      st.push_back(std::make_pair(j, d));
+    }
+    std::sort(st.begin(), st.end(),
+              [](const std::pair<int, double>& a,
+                 const std::pair<int, double>& b) {
+                return a.second < b.second;
+              });
+    st.erase(std::remove_if(st.begin(), st.end(),
+                            [&](const std::pair<int, double>& e) {
+                              return e.second > kFar;
+                            }),
+             st.end());
+    st.resize(std::min<size_t>((size_t) k, st.size()));
+    double total = 1.e-10;
+    for (const auto& e : st) total += e.second;
+    for (auto& e : st) e.second = 1.0 - e.second / total;
+    // Cmfd::getUpdateRatio: the stencil cells other than the FSR's own,
+    // then the own cell with the first entry's weight, all over (n - 1);
+    // a one-entry stencil adds the own cell's ratio undivided
+    const size_t n = st.size();
+    const double div = n == 1 ? 1.0 : (double) (n - 1);
+    for (const auto& e : st) {
+      if (e.first == 4) continue;
+      const int j = e.first;
+      cell.push_back((iy + j / 3 - 1) * cfg.nx + (ix + j % 3 - 1));
+      coef.push_back((float) (e.second / div));
+    }
+    cell.push_back(c);
+    coef.push_back(n == 1 ? 1.0f : (float) (st[0].second / div));
+    off[r + 1] = (int32_t) cell.size();
+  }
 }
 
 }  // namespace moc_cmfd

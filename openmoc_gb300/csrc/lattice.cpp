@@ -929,7 +929,8 @@ extern "C" int moc_lattice_extrude(const moc_lattice* L2, double height,
 
 extern "C" int moc_lattice_export_cmfd(moc_lattice* L, double* fsr_box,
                                        int8_t* end_face, double* edc_mu,
-                                       double* edc_w, double* bounds) {
+                                       double* edc_w, double* bounds,
+                                       double* centroid) {
   if (!L) return lat_fail("null lattice");
   if (L->tracks.empty() || (int64_t) L->tracks.size() != L->T ||
       (int64_t) L->fsr_pin.size() != L->R)
@@ -971,5 +972,30 @@ extern "C" int moc_lattice_export_cmfd(moc_lattice* L, double* fsr_box,
   bounds[1] = x0 + W;
   bounds[2] = y0;
   bounds[3] = y0 + H;
+  // FSR centroids (TrackGenerator::generateFSRCentroids,
+  // src/TrackGenerator.cpp:1681-1710): segment midpoints weighted by length,
+  // azimuthal spacing and weight, over the FSR volume
+  if (centroid) {
+    std::vector<double> cx(L->R, 0.0), cy(L->R, 0.0);
+    for (int64_t t = 0; t < L->T; t++) {
+      const Track& tr = L->tracks[t];
+      const double c = std::cos(tr.phi), sn = std::sin(tr.phi);
+      const double w = L->az_spacing[tr.a] * L->az_weight[tr.a];
+      double x = tr.x0, y = tr.y0;
+      for (int64_t k = L->seg_off[t]; k < L->seg_off[t + 1]; k++) {
+        const int32_t r = L->seg_fsr[k];
+        const double l = (double) L->seg_len[k];
+        const double v = (double) L->fsr_vol[r];
+        cx[r] += w * (x + 0.5 * c * l) * l / v;
+        cy[r] += w * (y + 0.5 * sn * l) * l / v;
+        x += c * l;
+        y += sn * l;
+      }
+    }
+    for (int64_t r = 0; r < L->R; r++) {
+      centroid[2 * r] = cx[r];
+      centroid[2 * r + 1] = cy[r];
+    }
+  }
   return 0;
 }

@@ -194,6 +194,9 @@ struct moc_ctx {
   moc_cmfd::Solver* cmfd = nullptr;
   std::vector<int32_t> h_cm_cell;
   std::vector<double> cm_edc_mu_h, cm_edc_w_h;   // as given (flat source)
+  int32_t* cm_pro_off = nullptr;     // k-nearest stencils (null: none)
+  int32_t* cm_pro_cell = nullptr;
+  float* cm_pro_coef = nullptr;
   int32_t* cm_cell = nullptr;
   int8_t* cm_end = nullptr;
   float* cm_cur = nullptr;
@@ -721,6 +724,9 @@ void cmfd_release(moc_ctx* c) {
   dfree(c->cm_wy);
   dfree(c->cm_gstart);
   dfree(c->cm_edc_mu);
+  dfree(c->cm_pro_off);
+  dfree(c->cm_pro_cell);
+  dfree(c->cm_pro_coef);
   dfree(c->cm_edc_w);
   if (c->h_cm_sums) cudaFreeHost(c->h_cm_sums);
   if (c->h_cm_cur) cudaFreeHost(c->h_cm_cur);
@@ -979,8 +985,11 @@ int run_cmfd_iterations(moc_ctx* c, int res_type) {
         c->launches++;
       }
       moc::launch_cmfd_prolong(c->phi, c->ls ? c->mom : nullptr, c->cm_cell,
-                               c->cm_group, c->cm_ratio, c->d.num_fsrs,
-                               c->d.num_groups, ld, E, c->sc, c->stream);
+                               c->cm_group, c->cm_ratio,
+                               moc::CmfdStencil{c->cm_pro_off, c->cm_pro_cell,
+                                                c->cm_pro_coef},
+                               c->d.num_fsrs, c->d.num_groups, ld, E,
+                               S.cfg.unbounded, c->sc, c->stream);
       moc::launch_fission_rate(a, 1, c->stream);
       c->launches += 2;
       if (c->ls) {     // normalizeFluxes scales the moments too
@@ -2498,6 +2507,14 @@ int moc_set_cmfd(moc_ctx* c, const moc_cmfd_mesh* m) {
             MOC_ERR_ARG, "the SOR factor must be in (0, 2)");
   MOC_CHECK(m->num_unbounded_iterations >= 0, MOC_ERR_ARG,
             "negative number of unbounded iterations");
+  MOC_CHECK(m->k_nearest >= 0 && m->k_nearest <= 9, MOC_ERR_ARG,
+            "k_nearest must be in 0..9 (Cmfd::setKNearest takes 1..9)");
+  MOC_CHECK(m->k_nearest == 0 || m->fsr_centroid, MOC_ERR_ARG,
+            "the k-nearest update needs the FSR centroids");
+  if (m->k_nearest > 0)
+    for (int64_t i = 0; i < 2 * R; i++)
+      MOC_CHECK(std::isfinite(m->fsr_centroid[i]), MOC_ERR_ARG,
+                "non-finite FSR centroid");
   cmfd_release(c);
   auto* S = new moc_cmfd::Solver();
   moc_cmfd::Config& cf = S->cfg;
@@ -2545,6 +2562,28 @@ int moc_set_cmfd(moc_ctx* c, const moc_cmfd_mesh* m) {
     e = cudaMemcpy(c->cm_group, group_of.data(), 4 * G,
                    cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(c->cm_cur, 0, 4 * ncur);
+  if (e == cudaSuccess && m->k_nearest > 0) {
+    std::vector<int32_t> off, cell;
+    std::vector<float> coef;
+    moc_cmfd::knearest_coefficients(cf, m->k_nearest, m->origin_x,
+                                    m->origin_y, m->fsr_centroid,
+                                    m->fsr_cell, R, off, cell, coef);
+    int st2 = dalloc(&c->cm_pro_off, R + 1);
+    if (st2 == MOC_OK) st2 = dalloc(&c->cm_pro_cell, (int64_t) cell.size());
+    if (st2 == MOC_OK) st2 = dalloc(&c->cm_pro_coef, (int64_t) coef.size());
+    if (st2 != MOC_OK) {
+      cmfd_release(c);
+      return st2;
+    }
+    e = cudaMemcpy(c->cm_pro_off, off.data(), 4 * (R + 1),
+                   cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(c->cm_pro_cell, cell.data(), 4 * cell.size(),
+                     cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(c->cm_pro_coef, coef.data(), 4 * coef.size(),
+                     cudaMemcpyHostToDevice);
+  }
   if (e != cudaSuccess) {
     cmfd_release(c);
     return fail(MOC_ERR_CUDA, cudaGetErrorString(e));

@@ -367,10 +367,18 @@ void launch_cmfd_pair_sums(const float* phi, const float* vol,
                            const int32_t* pair_off, const int32_t* pair_fsr,
                            int P, int G, int ld, double* out, DevScalars* sc,
                            cudaStream_t s);
-// mom (linear source, [R][ld][2]) is scaled with phi when not null.
+// k-nearest prolongation stencils (CSR per FSR; off null: none).
+struct CmfdStencil {
+  const int32_t* off;    // [R + 1]
+  const int32_t* cell;   // coarse cells
+  const float* coef;     // their weights
+};
+// mom (linear source, [R][ld][2]) is scaled with phi when not null; ratios
+// are bounded to [0.05, 20] from MOC iteration unbounded + 1 on.
 void launch_cmfd_prolong(float* phi, float* mom, const int32_t* fsr_cell,
                          const int32_t* group_of, const float* ratio,
-                         int64_t R, int G, int ld, int E, DevScalars* sc,
+                         const CmfdStencil& st, int64_t R, int G, int ld,
+                         int E, int unbounded, DevScalars* sc,
                          cudaStream_t s);
 
 }  // namespace moc

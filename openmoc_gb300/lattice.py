@@ -76,7 +76,7 @@ def _lib():
         L.moc_lattice_export_otf.restype = C.c_int
         L.moc_lattice_export_ls.argtypes = [C.c_void_p] + [C.c_void_p] * 7
         L.moc_lattice_export_ls.restype = C.c_int
-        L.moc_lattice_export_cmfd.argtypes = [C.c_void_p] + [C.c_void_p] * 5
+        L.moc_lattice_export_cmfd.argtypes = [C.c_void_p] + [C.c_void_p] * 6
         L.moc_lattice_export_cmfd.restype = C.c_int
         L.moc_lattice_destroy.argtypes = [C.c_void_p]
         L.moc_lattice_destroy.restype = C.c_int
@@ -217,9 +217,10 @@ def lattice(nx: int, ny: int, pin_material: np.ndarray, materials: Sequence[Mate
         if extrude is None:
             cm = dict(fsr_box=np.empty(4 * R), end_face=np.empty(2 * T, np.int8),
                       edc_mu=np.empty(A * Ph), edc_w=np.empty(A * Ph),
-                      bounds=np.empty(4))
+                      bounds=np.empty(4), fsr_centroid=np.empty(2 * R))
             if L.moc_lattice_export_cmfd(h, *[cm[k].ctypes.data for k in (
-                    "fsr_box", "end_face", "edc_mu", "edc_w", "bounds")]):
+                    "fsr_box", "end_face", "edc_mu", "edc_w", "bounds",
+                    "fsr_centroid")]):
                 raise RuntimeError(L.moc_lattice_last_error().decode())
             cm["fsr_box"] = cm["fsr_box"].reshape(R, 4)
             # (x-min, y-min, x-max, y-max) from bc = (xmin, xmax, ymin, ymax)

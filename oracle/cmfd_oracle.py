@@ -41,7 +41,8 @@ FLUX_EPSILON = 1e-25
 class CmfdOracle:
     def __init__(self, problem, nx, ny, widths_x, widths_y, fsr_cell, end_face,
                  bc, group_of=None, edc_mu=None, edc_w=None, relaxation=0.7,
-                 sor=1.5, flux_limiting=True, unbounded=0, linalg_tol=1e-7):
+                 sor=1.5, flux_limiting=True, unbounded=0, linalg_tol=1e-7,
+                 k_nearest=0, centroid=None, origin=(0.0, 0.0)):
         p = problem
         self.p = p
         self.nx, self.ny = int(nx), int(ny)
@@ -75,6 +76,11 @@ class CmfdOracle:
                              np.where(ix < self.nx - 1, c + 1, -1),
                              np.where(iy < self.ny - 1, c + self.nx, -1)], 1)
         self.colors = [c[(ix + iy) % 2 == k] for k in (0, 1)]
+        self.stencil = None
+        if k_nearest > 0:
+            self.stencil = knearest_stencils(self, int(k_nearest),
+                                              np.asarray(centroid, np.float64).reshape(-1, 2),
+                                              origin)
         self.reset()
 
     def reset(self, threshold=1e-5):
@@ -327,10 +333,53 @@ class CmfdOracle:
         new = x / np.einsum("ceg,cg->ce", Mm, x).sum()
         old = phi_c / np.einsum("ceg,cg->ce", Mm, phi_c).sum()
         ratio = np.where(np.abs(old) > FLUX_EPSILON, new / np.where(old == 0, 1, old), 0.0)
-        if it > self.unbounded:
-            ratio = np.clip(ratio, 0.05, 20.0)
         self.old_flux, self.new_flux = old, new
         return k, ratio
+
+    def update_ratios(self, it, ratio):
+        """Cmfd::updateMOCFlux's ratio per FSR and coarse group: the cell's,
+        or Cmfd::getUpdateRatio's k-nearest weighting; bounded to [0.05, 20]
+        after the unbounded iterations."""
+        if self.stencil is None:
+            q = ratio[self.cell]
+        else:
+            q = np.stack([sum(c * ratio[cell] for cell, c in st)
+                          for st in self.stencil])
+        if it > self.unbounded:
+            q = np.clip(q, 0.05, 20.0)
+        return q
+
+
+def knearest_stencils(cm, k, centroid, origin):
+    """Cmfd::generateKNearestStencils (src/Cmfd.cpp:2887-2960) and the
+    combination of Cmfd::getUpdateRatio (src/Cmfd.cpp:3178-3220), per FSR a
+    list of (coarse cell, coefficient)."""
+    cx = np.cumsum(cm.wx) - cm.wx / 2
+    cy = np.cumsum(cm.wy) - cm.wy / 2
+    out = []
+    for r in range(centroid.shape[0]):
+        c = int(cm.cell[r])
+        ix, iy = c % cm.nx, c // cm.nx
+        dx, dy = centroid[r, 0] - origin[0], centroid[r, 1] - origin[1]
+        st = []
+        for j in range(9):
+            sx, sy = ix + j % 3 - 1, iy + j // 3 - 1
+            if 0 <= sx < cm.nx and 0 <= sy < cm.ny:
+                d = ((dx - cx[sx]) ** 2 + (dy - cy[sy]) ** 2) ** 0.5
+            else:
+                d = np.finfo(np.float64).max
+            st.append((j, d))
+        st = sorted(st, key=lambda e: e[1])          # stable, as libstdc++'s
+        st = [e for e in st if e[1] <= 1e300][:k]    # insertion sort on 9
+        total = 1e-10 + sum(d for _, d in st)
+        st = [(j, 1.0 - d / total) for j, d in st]
+        n = len(st)
+        div = 1.0 if n == 1 else n - 1.0
+        terms = [((iy + j // 3 - 1) * cm.nx + ix + j % 3 - 1, w / div)
+                 for j, w in st if j != 4]
+        terms.append((c, 1.0 if n == 1 else st[0][1] / div))
+        out.append(terms)
+    return out
 
 
 def cmfd_eigenvalue(oracle, cm: CmfdOracle, max_iters=1000, res_type=1, tol=1e-5):
@@ -355,7 +404,7 @@ def cmfd_eigenvalue(oracle, cm: CmfdOracle, max_iters=1000, res_type=1, tol=1e-5
         phi = oracle.phi.reshape(R, G).astype(np.float64)
         k, ratio = cm.compute_keff(i, phi, cur)
         oracle.keff = k
-        scaled = phi * ratio[cm.cell][:, cm.group_of]
+        scaled = phi * cm.update_ratios(i, ratio)[:, cm.group_of]
         oracle.phi[:] = scaled.ravel().astype(oracle.phi.dtype)
         oracle.normalize()
         residual = oracle.residual_of(res_type)

@@ -23,9 +23,11 @@ LS_PROBE_CASES = ["grad2d_ls", "pin7_ls"]
 # CMFD-accelerated eigenvalue solves (Geometry::setCmfd) and the coarse
 # group structure each case set (None: one coarse group per group).
 CMFD_CASES = {"cmfd_lat3": [[1, 2, 3], [4, 5, 6, 7]], "cmfd_lat5_vac": None,
-              "cmfd_lat3_ls": [[1, 2, 3], [4, 5, 6, 7]]}
+              "cmfd_lat3_ls": [[1, 2, 3], [4, 5, 6, 7]],
+              "cmfd_lat3_k3": [[1, 2, 3], [4, 5, 6, 7]]}
 # SOR factor each case set (the linear-source case runs CPULSSolver)
-CMFD_SOR = {"cmfd_lat3": 1.5, "cmfd_lat5_vac": 1.5, "cmfd_lat3_ls": 1.0}
+CMFD_SOR = {"cmfd_lat3": 1.5, "cmfd_lat5_vac": 1.5, "cmfd_lat3_ls": 1.0,
+            "cmfd_lat3_k3": 1.5}
 
 
 def pytest_configure(config):

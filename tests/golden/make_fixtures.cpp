@@ -452,6 +452,7 @@ struct CaseSpec {
   std::vector<double> src_cell_flat;     /* [G] */
   std::vector<double> src_cell_moments;  /* [G][3], empty: none */
   Cmfd* cmfd;              /* attached to geo before the FSRs are made */
+  int k_nearest;           /* the Cmfd's setKNearest (0: not set) */
 };
 
 /* What the CMFD mesh of a case is laid over, in the arrays
@@ -518,6 +519,18 @@ static void write_cmfd(Writer& w, const CaseSpec& c, TrackGenerator& tg,
                    code(geo->getMaxXBoundaryType()),
                    code(geo->getMaxYBoundaryType())};
   w.arr("cm_bc", "i4", bc, 4);
+  if (cm->isCentroidUpdateOn()) {
+    /* the centroids the k-nearest stencils were built from */
+    std::vector<double> cen(2 * p.num_fsrs);
+    for (long r = 0; r < p.num_fsrs; r++) {
+      Point* q = geo->getFSRCentroid(r);
+      cen[2 * r] = q->getX();
+      cen[2 * r + 1] = q->getY();
+    }
+    w.arr("cm_fsr_centroid", "f8", cen.data(), cen.size());
+    int32_t k = c.k_nearest;
+    w.arr("cm_k_nearest", "i4", &k, 1);
+  }
 }
 
 static void run_case(const CaseSpec& c, const std::string& outdir) {
@@ -930,6 +943,29 @@ int main(int argc, char** argv) {
     CaseSpec cs = {"cmfd_lat3_ls", geo, 16, 0.1, 1000, 1e-5, FISSION_SOURCE,
                    EIGEN, 1.0, false, NULL, 0.0, 0, 0.0, true, false, NULL};
     cs.cmfd = cm;
+    cases.push_back(cs);
+  }
+
+  /* 16. case 13 with the k-nearest update (Cmfd::setKNearest(3), as
+   *     tests/test_cmfd_pwr_assembly sets it) */
+  {
+    Material* fuel = make_material(29, "fuel7ck",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 5, 7, true));
+    Material* mod = make_material(30, "mod7ck",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 1005, 7, false));
+    Geometry* geo = lattice_geometry(3, fuel, mod, pin, {4}, REF, REF, REF,
+                                     REF);
+    Cmfd* cm = new Cmfd();
+    cm->setLatticeStructure(3, 3);
+    cm->setGroupStructure({{1, 2, 3}, {4, 5, 6, 7}});
+    cm->setCMFDRelaxationFactor(0.7);
+    cm->setSORRelaxationFactor(1.5);
+    cm->setKNearest(3);
+    geo->setCmfd(cm);
+    CaseSpec cs = {"cmfd_lat3_k3", geo, 16, 0.1, 1000, 1e-5, FISSION_SOURCE,
+                   EIGEN, 1.0, false, NULL, 0.0};
+    cs.cmfd = cm;
+    cs.k_nearest = 3;
     cases.push_back(cs);
   }
 

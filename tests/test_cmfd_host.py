@@ -26,7 +26,7 @@ def test_cmfd_settings_validate():
     with pytest.raises(MOCError):
         c.setCMFDRelaxationFactor(0.0)
     with pytest.raises(MOCError):
-        c.setKNearest(3)
+        c.setKNearest(10)
     with pytest.raises(MOCError):
         c.setLatticeStructure(3, 3, 2)
     c.setKNearest(1)
@@ -92,3 +92,18 @@ def test_cmfd_fixtures_hold_a_mesh(case):
     m, keep = c.mesh(p)
     assert np.array_equal(keep[2], g["fsr_cell"])
     assert m.num_edc_angles == g["edc_mu"].size
+
+
+def test_cmfd_lattice_centroids_match_openmoc():
+    """The generated lattice's FSR centroids (the k-nearest update's input)
+    against OpenMOC's Geometry::getFSRCentroid for the same lattice, FSR by
+    FSR after matching FSRs by centroid (the two number FSRs differently)."""
+    p = _lat3()
+    q, sc, arr = load_case("cmfd_lat3_k3", "f64")
+    g = p.cmfd_geometry["fsr_centroid"].reshape(-1, 2)
+    r = q.cmfd_geometry["fsr_centroid"].reshape(-1, 2)
+    assert g.shape == r.shape
+    d = np.sqrt(((g[:, None, :] - r[None, :, :]) ** 2).sum(-1))
+    nearest = d.argmin(1)
+    assert np.unique(nearest).size == g.shape[0]      # one to one
+    assert d.min(1).max() < 2e-6

@@ -34,6 +34,8 @@ def _cmfd(p, groups, host=False, sor=1.5):
         c.setGroupStructure(groups)
     c.setSORRelaxationFactor(sor)
     c.setCMFDRelaxationFactor(0.7)
+    if "k_nearest" in p.cmfd_geometry:
+        c.setKNearest(int(p.cmfd_geometry["k_nearest"][0]))
     return c
 
 

@@ -16,6 +16,10 @@ def cmfd_oracle_for(p, groups, **kw):
     go = None
     if groups is not None:
         go = np.concatenate([[e] * len(gr) for e, gr in enumerate(groups)])
+    if "k_nearest" in g:
+        kw.setdefault("k_nearest", int(g["k_nearest"][0]))
+        kw.setdefault("centroid", g["fsr_centroid"])
+        kw.setdefault("origin", (g["bounds"][0], g["bounds"][2]))
     return CmfdOracle(p, g["widths_x"].size, g["widths_y"].size, g["widths_x"],
                       g["widths_y"], g["fsr_cell"], g["end_face"], g["bc"], go,
                       g["edc_mu"], g["edc_w"], **kw)
@@ -23,7 +27,8 @@ def cmfd_oracle_for(p, groups, **kw):
 
 @pytest.mark.parametrize("case,precision", [("cmfd_lat3", "f64"),
                                             ("cmfd_lat3", "f32"),
-                                            ("cmfd_lat5_vac", "f64")])
+                                            ("cmfd_lat5_vac", "f64"),
+                                            ("cmfd_lat3_k3", "f64")])
 def test_cmfd_oracle_matches_openmoc(case, precision):
     p, sc, arr = load_case(case, precision)
     cm = cmfd_oracle_for(p, CMFD_CASES[case])
