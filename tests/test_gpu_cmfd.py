@@ -160,8 +160,8 @@ def test_gpu_cmfd_uses_native_library():
     s.close()
 
 
-@pytest.mark.parametrize("host", [False, True])
-def test_gpu_cmfd_matches_oracle_step_by_step(host):
+@pytest.mark.parametrize("host,k", [(False, 0), (True, 0), (False, 3)])
+def test_gpu_cmfd_matches_oracle_step_by_step(host, k):
     """A generated 5 x 5 lattice (vacuum on +x and +y, water pins) on a pin
     mesh with two coarse groups, a fixed number of iterations: keff, fluxes
     and the coarse fluxes of the last coarse solve against the FP64 oracle
@@ -182,10 +182,13 @@ def test_gpu_cmfd_matches_oracle_step_by_step(host):
     c.setLatticeStructure(5, 5)
     c.setGroupStructure(groups)
     c.useHostSolver(host)
+    if k:
+        c.setKNearest(k)
     mesh, keep = c.mesh(p)
     g = p.cmfd_geometry
     cm = CmfdOracle(p, 5, 5, keep[0], keep[1], keep[2], g["end_face"], g["bc"],
-                    keep[4], g["edc_mu"], g["edc_w"])
+                    keep[4], g["edc_mu"], g["edc_w"], k_nearest=k,
+                    centroid=g["fsr_centroid"], origin=(g["bounds"][0], g["bounds"][2]))
     o = Oracle(p, "f64", num_threads=8)
     iters = 8
     cmfd_eigenvalue(o, cm, iters, 1, 1e-30)
