@@ -22,6 +22,11 @@ namespace {
 
 constexpr int kPairThreads = 256;
 constexpr int kSolveThreads = 512;
+// the solve kernel's block: up to 4 coarse groups a thread holds little, so
+// twice the warps
+constexpr int solve_threads(int ec) {
+  return (ec > 0 && ec <= 4) ? 1024 : kSolveThreads;
+}
 // shared memory for the coarse system (vectors, A and couplings)
 constexpr int kSolveSmemMax = 216 * 1024;
 constexpr float kZeroSigmaT = 1e-6f;          // src/constants.h:34
@@ -599,8 +604,33 @@ __device__ bool dd_linear_solve(const CmfdArgs& a, const Work& k,
   return true;
 }
 
+// Cmfd::collapseXS over the whole GPU, one thread per (cell, coarse group).
+__global__ void __launch_bounds__(256)
+cmfd_collapse_kernel(const CmfdArgs a) {
+  if (*(volatile const int*) &a.sc->done) return;
+  const Work k = carve(a.work, a.C, a.E);
+  const int CE = a.C * a.E;
+  for (int ce = blockIdx.x * blockDim.x + threadIdx.x; ce < CE;
+       ce += gridDim.x * blockDim.x)
+    collapse_one(a, k, ce / a.E, ce % a.E);
+}
+
+// The surface coefficients and matrices, one thread per row; reads the
+// neighbours' collapse, so it follows the collapse kernel.
+__global__ void __launch_bounds__(256)
+cmfd_build_kernel(const CmfdArgs a) {
+  if (*(volatile const int*) &a.sc->done) return;
+  const Work k = carve(a.work, a.C, a.E);
+  const int it = a.sc->iteration;
+  const bool valid = a.cm->valid != 0;
+  const int CE = a.C * a.E;
+  for (int ce = blockIdx.x * blockDim.x + threadIdx.x; ce < CE;
+       ce += gridDim.x * blockDim.x)
+    build_row(a, k, ce / a.E, ce % a.E, it, valid);
+}
+
 template <int EC>
-__global__ void __launch_bounds__(kSolveThreads, 1)
+__global__ void __launch_bounds__(solve_threads(EC), 1)
 cmfd_solve_kernel(const CmfdArgs a, int smem_mask) {
   DevScalars* sc = a.sc;
   if (*(volatile int*) &sc->done) return;
@@ -608,25 +638,26 @@ cmfd_solve_kernel(const CmfdArgs a, int smem_mask) {
   extern __shared__ float4 s_dyn[];
   const int C = a.C, E = a.E;
   const int CE = C * E;
-  Work k = carve(a.work, C, E);
+  const Work g = carve(a.work, C, E);   // as the build kernels wrote it
+  Work k = g;
   k.nbr = a.nbr_j;
-  // the neighbour table copy is read after the barrier below the collapse
   place_in_smem(k, reinterpret_cast<char*>(s_dyn), smem_mask, a);
+  // the placed matrices and the starting iterate onto the chip
+  const int64_t CEE = (int64_t) CE * E;
+  if (k.x != g.x)
+    for (int r = threadIdx.x; r < CE; r += blockDim.x) k.x[r] = g.x[r];
+  if (k.nb != g.nb)
+    for (int r = threadIdx.x; r < 4 * CE; r += blockDim.x) k.nb[r] = g.nb[r];
+  if (k.A != g.A)
+    for (int64_t r = threadIdx.x; r < CEE; r += blockDim.x) k.A[r] = g.A[r];
+  __syncthreads();
   CmfdDevState* cm = a.cm;
   const int it = sc->iteration;                 // MOC iteration
   // the coarse tolerance follows the transport residual
   // (Solver::computeEigenvalue, src/Solver.cpp:1671-1675)
   double src_thr = 0.1 * sc->threshold;         // Solver::initializeCmfd
   if (it > 0) src_thr = 0.01 * (sc->residual > 0.0 ? sc->residual : 1e-6);
-  const bool valid = cm->valid != 0;
   double keff = cm->keff;
-
-  for (int ce = threadIdx.x; ce < CE; ce += blockDim.x)
-    collapse_one(a, k, ce / E, ce % E);
-  __syncthreads();
-  for (int ce = threadIdx.x; ce < CE; ce += blockDim.x)
-    build_row(a, k, ce / E, ce % E, it, valid);
-  __syncthreads();
 
   // ---- eigenvalueSolve (src/linalg.cpp:25-176)
   const double rows = (double) CE;
@@ -790,8 +821,13 @@ void launch_cmfd_pair_sums(const float* phi, const float* vol,
 
 void launch_cmfd_solve(const CmfdArgs& a, cudaStream_t s) {
   // one thread per cell of a colour, at least four warps
+  // collapse and matrices over the GPU, then the solve on one block
+  const int CE = a.C * a.E;
+  const int nb = (int) std::min<int64_t>((CE + 255) / 256, (int64_t) 4 * sm_count());
+  cmfd_collapse_kernel<<<std::max(nb, 1), 256, 0, s>>>(a);
+  cmfd_build_kernel<<<std::max(nb, 1), 256, 0, s>>>(a);
   int threads = (std::max(a.n_color0, a.C - a.n_color0) + 31) / 32 * 32;
-  threads = std::max(128, std::min(kSolveThreads, threads));
+  threads = std::max(128, std::min(solve_threads(a.E <= 8 ? a.E : 0), threads));
   int64_t bytes = 0;
   const int level = smem_plan(a.C, a.E, kSolveSmemMax, &bytes);   // item mask
   const int smem = (int) bytes;

@@ -981,8 +981,8 @@ int run_cmfd_iterations(moc_ctx* c, int res_type) {
         MOC_CUDA(cudaMemcpyAsync(&c->sc->keff, &c->hsc->keff, sizeof(double),
                                  cudaMemcpyHostToDevice, c->stream));
       } else {
-        moc::launch_cmfd_solve(ca, c->stream);
-        c->launches++;
+        moc::launch_cmfd_solve(ca, c->stream);   // collapse, build, solve
+        c->launches += 3;
       }
       moc::launch_cmfd_prolong(c->phi, c->ls ? c->mom : nullptr, c->cm_cell,
                                c->cm_group, c->cm_ratio,
