@@ -85,7 +85,7 @@ void Solver::collapse(const double* S, const float* cur, int ld,
   // pairs of each cell
   std::vector<std::vector<int>> of_cell(C);
   for (int p = 0; p < P; p++) of_cell[fine.pair_cell[p]].push_back(p);
-  std::vector<double> chi_t(E), scat(E), rxn_h(G), trans_h(G);
+  std::vector<double> chi_t(E), scat(E);
   for (int c = 0; c < C; c++) {
     const std::vector<int>& ps = of_cell[c];
     // fission spectrum weighted by each pair's neutron production

@@ -826,7 +826,6 @@ int cmfd_prepare(moc_ctx* c) {
             ss[((size_t) m * G + g) * G + h];
     }
   std::vector<float> cvol(F.cell_vol.begin(), F.cell_vol.end());
-  // (cf.edc_* were set for this solve above)
   std::vector<float> wx(cf.wx.begin(), cf.wx.end()), wy(cf.wy.begin(), cf.wy.end());
   std::vector<float> mu(cf.edc_mu.begin(), cf.edc_mu.end());
   std::vector<float> ew(cf.edc_w.begin(), cf.edc_w.end());
