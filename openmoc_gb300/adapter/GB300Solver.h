@@ -18,8 +18,9 @@
  * std::logic_error like every OpenMOC validation failure
  * (src/log.cpp:588-599); SWIG maps that to a Python RuntimeError.
  *
- * Compiled against OpenMOC's headers and linked with its library and with
- * libopenmoc_gb300.so (see INTEGRATION.md for the build lines).
+ * Compiled against OpenMOC's headers (-I <openmoc>/src, with OpenMOC's
+ * FP_PRECISION / CMFD_PRECISION macros) and linked with its library and with
+ * libopenmoc_gb300.so and libcudart.
  */
 #ifndef OPENMOC_GB300_SOLVER_H_
 #define OPENMOC_GB300_SOLVER_H_
