@@ -146,6 +146,11 @@ struct Work {
   float *sa, *sb;        // per row (1 - w) d / w and w / d of the SOR update
   float *phi_t, *rhs, *dd_a, *dd_b, *ddv;             // [E][C]
   const int32_t* nbr;    // [4][C] neighbours in colour order
+  // on-chip copies for the SOR sweeps (null: not placed): the neighbour
+  // table in 16 bits, and A's off-diagonal part [e][g != e][C] (its
+  // diagonal lives in sa / sb)
+  const int16_t* nbr16;
+  const float* aoff;
 };
 
 constexpr int kColourVecs = 13;   // every colour-order vector
@@ -164,20 +169,24 @@ __device__ Work carve(float* w, int C, int E) {
   float** vecs[] = {&k.x, &k.b, &k.src_a, &k.src_b, &k.ls_a, &k.ls_b, &k.sa,
                     &k.sb, &k.phi_t, &k.rhs, &k.dd_a, &k.dd_b, &k.ddv};
   for (float** p : vecs) { *p = w; w += CE; }
+  k.nbr = nullptr;
+  k.nbr16 = nullptr;
+  k.aoff = nullptr;
   return k;
 }
 
 // Shared memory holds what every SOR sweep reads, in this order of
 // priority, each array while the budget lasts: x, b, sa, sb (C E floats
-// each), the couplings (4 C E), the neighbour table (4 C ints), A (C E E).
+// each), the couplings (4 C E), the neighbour table (4 C 16-bit ids; up to
+// 32767 cells), A's off-diagonal part (C E (E - 1)).
 constexpr int kSmemItems = 7;
 
 __host__ __device__ inline int64_t smem_item_bytes(int i, int C, int E) {
   const int64_t CE = (int64_t) C * E;
   switch (i) {
     case 4: return 16 * CE;
-    case 5: return 16 * (int64_t) C;
-    case 6: return 4 * CE * E;
+    case 5: return C <= 32767 ? 8 * (int64_t) C : 0;
+    case 6: return 4 * CE * (E - 1);
     default: return 4 * CE;
   }
 }
@@ -188,7 +197,7 @@ inline int smem_plan(int C, int E, int64_t budget, int64_t* bytes) {
   int64_t used = 0;
   for (int i = 0; i < kSmemItems; i++) {
     const int64_t n = smem_item_bytes(i, C, E);
-    if (used + n <= budget) {
+    if (n > 0 && used + n <= budget) {
       mask |= 1 << i;
       used += n;
     }
@@ -197,8 +206,9 @@ inline int smem_plan(int C, int E, int64_t budget, int64_t* bytes) {
   return mask;
 }
 
-// Points the placed arrays at shared memory (the neighbour table is copied
-// in; the caller syncs before it is read).
+// Points the placed arrays at shared memory and fills the neighbour table
+// and A's off-diagonal part (from A in global memory, written by the build
+// kernel); the caller syncs before they are read.
 __device__ void place_in_smem(Work& k, char* s, int mask, const CmfdArgs& a) {
   const int C = a.C, E = a.E;
   float** vecs[] = {&k.x, &k.b, &k.sa, &k.sb, &k.nb};
@@ -207,11 +217,20 @@ __device__ void place_in_smem(Work& k, char* s, int mask, const CmfdArgs& a) {
     if (i < 5) {
       *vecs[i] = reinterpret_cast<float*>(s);
     } else if (i == 5) {
-      int32_t* t = reinterpret_cast<int32_t*>(s);
-      for (int q = threadIdx.x; q < 4 * C; q += blockDim.x) t[q] = a.nbr_j[q];
-      k.nbr = t;
+      int16_t* t = reinterpret_cast<int16_t*>(s);
+      for (int q = threadIdx.x; q < 4 * C; q += blockDim.x)
+        t[q] = (int16_t) a.nbr_j[q];
+      k.nbr16 = t;
     } else {
-      k.A = reinterpret_cast<float*>(s);
+      float* t = reinterpret_cast<float*>(s);
+      const int n = C * E * (E - 1);
+      for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        // q = (e * (E - 1) + gi) * C + j, gi-th of the groups g != e
+        const int j = q % C, eg = q / C, e = eg / (E - 1), gi = eg % (E - 1);
+        const int g = gi < e ? gi : gi + 1;
+        t[q] = k.A[((int64_t) e * E + g) * C + j];
+      }
+      k.aoff = t;
     }
     s += smem_item_bytes(i, C, E);
   }
@@ -419,8 +438,13 @@ __device__ void sor_half(const CmfdArgs& a, const Work& k, const float* b,
   const int j1 = color ? a.C : a.n_color0;
   for (int j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
     int nbj[4];
+    if (k.nbr16) {
 #pragma unroll
-    for (int f = 0; f < 4; f++) nbj[f] = k.nbr[f * C + j];
+      for (int f = 0; f < 4; f++) nbj[f] = k.nbr16[f * C + j];
+    } else {
+#pragma unroll
+      for (int f = 0; f < 4; f++) nbj[f] = k.nbr[f * C + j];
+    }
     if constexpr (EC > 0) {
       // a missing neighbour points at the cell itself with a zero coupling
 #pragma unroll
@@ -443,14 +467,25 @@ __device__ void sor_half(const CmfdArgs& a, const Work& k, const float* b,
       }
 #pragma unroll
       for (int e = 0; e < EC; e++) {
-        const float* arow = k.A + e * EC * C + j;
         float s0 = 0.0f, s1 = 0.0f;      // two partial sums over the groups
+        if (k.aoff) {
+          const float* arow = k.aoff + e * (EC - 1) * C + j;
 #pragma unroll
-        for (int g = 0; g < EC; g++)
-          if (g != e) {
-            if (g & 1) s1 -= arow[g * C] * xo[g];
-            else s0 -= arow[g * C] * xo[g];
-          }
+          for (int g = 0; g < EC; g++)
+            if (g != e) {
+              const float v = arow[(g < e ? g : g - 1) * C] * xo[g];
+              if (g & 1) s1 -= v;
+              else s0 -= v;
+            }
+        } else {
+          const float* arow = k.A + e * EC * C + j;
+#pragma unroll
+          for (int g = 0; g < EC; g++)
+            if (g != e) {
+              if (g & 1) s1 -= arow[g * C] * xo[g];
+              else s0 -= arow[g * C] * xo[g];
+            }
+        }
         xo[e] = (sa[e] * xo[e] + (t[e] + (s0 + s1))) * sb[e];
       }
 #pragma unroll
@@ -642,14 +677,11 @@ cmfd_solve_kernel(const CmfdArgs a, int smem_mask) {
   Work k = g;
   k.nbr = a.nbr_j;
   place_in_smem(k, reinterpret_cast<char*>(s_dyn), smem_mask, a);
-  // the placed matrices and the starting iterate onto the chip
-  const int64_t CEE = (int64_t) CE * E;
+  // the placed couplings and the starting iterate onto the chip
   if (k.x != g.x)
     for (int r = threadIdx.x; r < CE; r += blockDim.x) k.x[r] = g.x[r];
   if (k.nb != g.nb)
     for (int r = threadIdx.x; r < 4 * CE; r += blockDim.x) k.nb[r] = g.nb[r];
-  if (k.A != g.A)
-    for (int64_t r = threadIdx.x; r < CEE; r += blockDim.x) k.A[r] = g.A[r];
   __syncthreads();
   CmfdDevState* cm = a.cm;
   const int it = sc->iteration;                 // MOC iteration
