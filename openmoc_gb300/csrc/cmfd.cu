@@ -9,8 +9,10 @@
 // hundreds of red-black SOR sweeps are latency-bound, so they run between
 // __syncthreads barriers of a single block, with the operands in L1, instead
 // of as hundreds of dependent launches or host round trips.  Arithmetic is
-// FP32 with FP64 sums, as in the reference's single-precision build
-// (CMFD_PRECISION float, LINALG_TOL 1e-7).
+// FP32, as in the reference's single-precision build (CMFD_PRECISION float,
+// LINALG_TOL 1e-7); block-wide sums are compensated FP32 within a thread,
+// FP32 within a warp and FP64 across warps, and the scalar work after them
+// runs in one thread, since FP64 issues at a small fraction of the FP32 rate.
 #include <algorithm>
 #include <cfloat>
 
@@ -117,17 +119,41 @@ __global__ void cmfd_prolong_kernel(float* __restrict__ phi,
 }
 
 // ------------------------------------------------------------ coarse solve
-// Sum of v over the block, returned to every thread.
-__device__ double block_sum(double v, double* red) {
+// Neumaier's compensated summation (A. Neumaier, ZAMM 54, 1974) in FP32: a
+// thread's partial sum over its share of a vector, accurate to a few units
+// in the last place however many values the thread adds.
+struct FSum {
+  float s = 0.0f, c = 0.0f;
+  __device__ void add(float v) {
+    const float t = s + v;
+    c += fabsf(s) >= fabsf(v) ? (s - t) + v : (v - t) + s;
+    s = t;
+  }
+  __device__ float value() const { return s + c; }
+};
+
+// Sum over the block of one FP32 value per thread: FP32 within each warp,
+// FP64 across the warps.  Thread 0 alone passes the total to `finish` and
+// every thread gets finish's result, so the FP64 arithmetic after a
+// reduction (a root, a quotient, a convergence test) runs once, not in each
+// of the block's threads: an SM issues FP64 at 1/64 of its FP32 rate, and
+// those per-thread copies were most of the coarse solve's time.  red holds
+// 33 doubles.
+template <class F>
+__device__ double block_sum(float v, double* red, F finish) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   __syncthreads();   // earlier readers of red are done
-  if (lane == 0) red[w] = v;
+  if (lane == 0) red[w] = (double) v;
   __syncthreads();
-  double t = 0.0;
-  const int nw = (blockDim.x + 31) >> 5;
-  for (int i = 0; i < nw; i++) t += red[i];
-  return t;
+  if (threadIdx.x == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    double t = 0.0;
+    for (int i = 0; i < nw; i++) t += red[i];
+    red[32] = finish(t);
+  }
+  __syncthreads();
+  return red[32];
 }
 
 // The coarse system lives in colour order: j is a cell's position in the
@@ -279,29 +305,44 @@ __device__ void mat_fission(const CmfdArgs& a, const Work& k, const float* x,
   }
 }
 
-__device__ double block_total(const float* v, int n, double* red) {
-  double t = 0.0;
-  for (int r = threadIdx.x; r < n; r += blockDim.x) t += v[r];
-  return block_sum(t, red);
+// finish(sum of v[0, n)) for every thread (block_sum)
+template <class F>
+__device__ double block_total(const float* v, int n, double* red, F finish) {
+  FSum t;
+  for (int r = threadIdx.x; r < n; r += blockDim.x) t.add(v[r]);
+  return block_sum(t.value(), red, finish);
 }
 
-// computeRMSE(integrated) (src/linalg.cpp:595-680)
+__device__ double block_total(const float* v, int n, double* red) {
+  return block_total(v, n, red, [](double s) { return s; });
+}
+
+// computeRMSE(integrated) (src/linalg.cpp:595-680): the root mean square
+// over the cells of the relative change of a cell's source summed over its
+// groups, handed to judge (thread 0); every thread gets judge's result.  A
+// cell's change is summed from its group differences, which FP32 subtracts
+// exactly while old and new are within a factor of two, so the quotient
+// keeps FP32 precision without the reference's double sums.
+template <class F>
 __device__ double rmse(const CmfdArgs& a, const float* x, const float* y,
-                       double* red) {
-  double part = 0.0;
+                       double* red, F judge) {
+  FSum part;
   for (int j = threadIdx.x; j < a.C; j += blockDim.x) {
-    double s = 0.0, t = 0.0;
+    float d = 0.0f, t = 0.0f;
     for (int e = 0; e < a.E; e++) {
-      s += x[e * a.C + j];
-      t += y[e * a.C + j];
+      const float yo = y[e * a.C + j];
+      d += x[e * a.C + j] - yo;
+      t += yo;
     }
-    if (fabs(t) > kFluxEps) {
-      const float r = (float) ((s - t) / t);
-      part += (double) (r * r);
+    if (fabsf(t) > (float) kFluxEps) {
+      const float r = d / t;
+      part.add(r * r);
     }
   }
-  const double tot = block_sum(part, red);
-  return sqrt(tot / (double) max(a.C, 1));
+  const int C = a.C;
+  return block_sum(part.value(), red, [&](double tot) {
+    return judge(sqrt(tot / (double) max(C, 1)));
+  });
 }
 
 // Cmfd::collapseXS (src/Cmfd.cpp:720-1000) for cell c, coarse group e, and
@@ -533,7 +574,8 @@ __device__ bool linear_solve(const CmfdArgs& a, const Work& k, const float* b,
   sor_prep<EC>(a, k);
   mat_fission<EC>(a, k, k.x, ls_old);
   __syncthreads();
-  double lres = 0.0, linit = 0.0, min_res = 1e6, stall_res = INFINITY;
+  // the convergence state lives in thread 0, which judges each residual
+  double linit = 0.0, min_res = 1e6, stall_res = INFINITY;
   int li = 0, stall_li = 0;
   while (li < kMaxLinearIters) {
     sor_half<EC>(a, k, b, 0);
@@ -547,23 +589,24 @@ __device__ bool linear_solve(const CmfdArgs& a, const Work& k, const float* b,
       mat_fission<EC>(a, k, k.x, ls_new);
       __syncthreads();
     }
-    if (li == 0) {
-      lres = rmse(a, ls_new, ls_old, red);
-      linit = lres;
-    }
+    if (li == 0) rmse(a, ls_new, ls_old, red, [&](double r) { return linit = r; });
     li++;
     if (li > kMinIters) {
-      lres = rmse(a, ls_new, ls_old, red);
-      min_res = fmin(min_res, lres);
-      if ((lres > 1e3 * min_res && min_res > kNoiseFloor) || !isfinite(lres))
-        return false;
-      const double q = linit > 0.0 ? lres / linit : INFINITY;
-      if (q < 0.1 || lres < tol) return true;
-      if (li - stall_li >= kStallWindow) {
-        if (lres < kStallMax && lres > 0.5 * stall_res) return true;
-        stall_res = lres;
-        stall_li = li;
-      }
+      // 1 converged, -1 diverged, 0 not yet
+      const double verdict = rmse(a, ls_new, ls_old, red, [&](double r) {
+        min_res = fmin(min_res, r);
+        if ((r > 1e3 * min_res && min_res > kNoiseFloor) || !isfinite(r)) return -1.0;
+        const double q = linit > 0.0 ? r / linit : INFINITY;
+        if (q < 0.1 || r < tol) return 1.0;
+        if (li - stall_li >= kStallWindow) {
+          if (r < kStallMax && r > 0.5 * stall_res) return 1.0;
+          stall_res = r;
+          stall_li = li;
+        }
+        return 0.0;
+      });
+      if (verdict < 0.0) return false;
+      if (verdict > 0.0) return true;
     }
     if (li > kMinIters - 1 && li < kMaxLinearIters) {
       float* t = ls_old;
@@ -617,17 +660,21 @@ __device__ bool dd_linear_solve(const CmfdArgs& a, const Work& k,
     linear_solve<EC>(a, k, bw, tol, red, sweeps);   // a failure is only noted
     mat_fission<EC>(a, k, k.x, new_src);
     __syncthreads();
-    const double res = rmse(a, new_src, old_src, red);
-    if (it == 0) initial = res < 1e-14 ? 1e-10 : res;
-    min_res = fmin(min_res, res);
-    if ((res > 1e3 * min_res && min_res > kNoiseFloor) || !isfinite(res))
-      return false;
-    if (res / initial < 0.1 || res < tol) break;
-    if (it - stall_it >= kStallWindow) {
-      if (res < kStallMax && res > 0.5 * stall_res) break;
-      stall_res = res;
-      stall_it = it;
-    }
+    // thread 0 judges: 1 settled, -1 diverged, 0 not yet
+    const double verdict = rmse(a, new_src, old_src, red, [&](double res) {
+      if (it == 0) initial = res < 1e-14 ? 1e-10 : res;
+      min_res = fmin(min_res, res);
+      if ((res > 1e3 * min_res && min_res > kNoiseFloor) || !isfinite(res)) return -1.0;
+      if (res / initial < 0.1 || res < tol) return 1.0;
+      if (it - stall_it >= kStallWindow) {
+        if (res < kStallMax && res > 0.5 * stall_res) return 1.0;
+        stall_res = res;
+        stall_it = it;
+      }
+      return 0.0;
+    });
+    if (verdict < 0.0) return false;
+    if (verdict > 0.0) break;
     if (sweeps >= kMaxSweeps) return false;
   }
   for (int r = threadIdx.x; r < CE; r += blockDim.x) {
@@ -669,7 +716,7 @@ __global__ void __launch_bounds__(solve_threads(EC), 1)
 cmfd_solve_kernel(const CmfdArgs a, int smem_mask) {
   DevScalars* sc = a.sc;
   if (*(volatile int*) &sc->done) return;
-  __shared__ double red[32];
+  __shared__ double red[33];
   extern __shared__ float4 s_dyn[];
   const int C = a.C, E = a.E;
   const int CE = C * E;
@@ -725,27 +772,27 @@ cmfd_solve_kernel(const CmfdArgs a, int smem_mask) {
       }
       mat_fission<EC>(a, k, k.x, src_new);
       __syncthreads();
-      keff = block_total(src_new, CE, red) / rows;
-      for (int r = threadIdx.x; r < CE; r += blockDim.x)
-        src_new[r] = (float) (src_new[r] / keff);
+      keff = block_total(src_new, CE, red, [&](double s) { return s / rows; });
+      const float kf = (float) keff;
+      for (int r = threadIdx.x; r < CE; r += blockDim.x) src_new[r] /= kf;
       __syncthreads();
-      const double res = rmse(a, src_new, src_old, red);
-      if (power == 0) initial = res < 1e-14 ? 1e-10 : res;
+      // thread 0 judges: 1 converged, 0 not yet
+      const double stop = rmse(a, src_new, src_old, red, [&](double res) {
+        if (power == 0) initial = res < 1e-14 ? 1e-10 : res;
+        if ((res / initial < 0.03 || res < kLinalgTol) && power > kMinIters) return 1.0;
+        if (power > kMinIters && power - stall_p >= kStallWindow) {
+          if (res < kStallMax && res > 0.5 * stall_res) return 1.0;
+          stall_res = res;
+          stall_p = power;
+        }
+        return 0.0;
+      });
       for (int r = threadIdx.x; r < CE; r += blockDim.x) src_old[r] = src_new[r];
       __syncthreads();
-      if ((res / initial < 0.03 || res < kLinalgTol) && power > kMinIters) {
+      if (stop > 0.0) {
         power++;
         break;
       }
-      if (power > kMinIters && power - stall_p >= kStallWindow) {
-        if (res < kStallMax && res > 0.5 * stall_res) {
-          power++;
-          break;
-        }
-        stall_res = res;
-        stall_p = power;
-      }
-      __syncthreads();
     }
     if (!(fabs(keff + 1.0) > FLT_EPSILON) || !isfinite(keff)) failed = true;
   }
@@ -768,14 +815,16 @@ cmfd_solve_kernel(const CmfdArgs a, int smem_mask) {
   mat_fission<EC>(a, k, k.x, k.src_a);
   mat_fission<EC>(a, k, k.phi_t, k.src_b);
   __syncthreads();
-  const double sn = block_total(k.src_a, CE, red);
-  const double so = block_total(k.src_b, CE, red);
+  // the reciprocals of the two source totals, formed once by thread 0
+  const auto inverse = [](double s) { return 1.0 / s; };
+  const double sn = block_total(k.src_a, CE, red, inverse);
+  const double so = block_total(k.src_b, CE, red, inverse);
   float far = 1.0f;
   for (int r = threadIdx.x; r < CE; r += blockDim.x) {   // r = e * C + j
     const int e = r / C, j = r - e * C;
     const int out = a.color_cells[j] * E + e;            // cell order
-    const float xn = (float) (k.x[r] / sn);
-    const float xo = (float) (k.phi_t[r] / so);
+    const float xn = (float) (k.x[r] * sn);
+    const float xo = (float) (k.phi_t[r] * so);
     // bounded by the prolongation, after any k-nearest weighting
     const float q = fabs((double) xo) > kFluxEps ? xn / xo : 0.0f;
     a.ratio[out] = q;
