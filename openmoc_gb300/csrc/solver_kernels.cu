@@ -204,14 +204,18 @@ compute_sources_kernel(const SolverArgs a, int iteration, int zero_phi,
       if (!p0 || p0->done) on &= ~1;
       if (!p1 || p1->done) on &= ~2;
       if (!on) continue;
+      // the FP64 reciprocals in one lane (the rows are the whole warp's)
+      const bool lane0 = (threadIdx.x & 31) == 0;
       if (on & 1) {
         it0 = p0->iteration;
-        ik0 = (float) (1.0 / p0->keff);
+        if (lane0) ik0 = (float) (1.0 / p0->keff);
       }
       if (on & 2) {
         it1 = p1->iteration;
-        ik1 = (float) (1.0 / p1->keff);
+        if (lane0) ik1 = (float) (1.0 / p1->keff);
       }
+      ik0 = __shfl_sync(0xffffffffu, ik0, 0);
+      ik1 = __shfl_sync(0xffffffffu, ik1, 0);
     }
     source_rows<S>(a, ssT, r, on, zero_phi, it0, it1, ik0, ik1, negatives);
   }
@@ -345,11 +349,13 @@ residual_kernel(const SolverArgs a, int normalise, int store, int finish) {
       if (store) old[g] = v;
     }
     x = warp_sum_all(x);
-    if (RT == 0) {
-      part += (double) x;
-    } else {
-      y = warp_sum_all(y);
-      if ((RT == 2 || fis) && y > 0.0f) {
+    if (RT != 0) y = warp_sum_all(y);
+    // block_accumulate takes lane 0's part: the FP64 quotient (1/64 of the
+    // FP32 issue rate) runs in that lane alone
+    if (lane == 0) {
+      if (RT == 0) {
+        part += (double) x;
+      } else if ((RT == 2 || fis) && y > 0.0f) {
         const double t = (double) x / (double) y;
         part += t * t;
       }
@@ -819,7 +825,12 @@ batch_residual_kernel(const SolverArgs a) {
     const int RT = ss->res_type;
     const bool normalise = ss->mode == kModeEigen;
     const float factor = normalise ? (float) ss->factor : 1.0f;
-    const float inv_k = (float) (1.0 / ss->keff);
+    // the FP64 reciprocal in one lane (RT is the same for the whole warp)
+    float inv_k = 0.0f;
+    if (RT == 2) {
+      if (lane == 0) inv_k = (float) (1.0 / ss->keff);
+      inv_k = __shfl_sync(0xffffffffu, inv_k, 0);
+    }
     const int m = a.fsr_mat[r];
     const bool fis = a.fissile[m] != 0;
     const float* __restrict__ nf = a.nu_sigma_f + (int64_t) m * G;
@@ -863,14 +874,16 @@ batch_residual_kernel(const SolverArgs a) {
     }
     x = warp_sum_all(x);
     y = warp_sum_all(y);
-    double part = 0.0;
-    if (RT == 0) {
-      part = (double) x;
-    } else if ((RT == 2 || fis) && y > 0.0f) {
-      const double t = (double) x / (double) y;
-      part = t * t;
+    if (lane == 0) {
+      double part = 0.0;
+      if (RT == 0) {
+        part = (double) x;
+      } else if ((RT == 2 || fis) && y > 0.0f) {
+        const double t = (double) x / (double) y;
+        part = t * t;
+      }
+      a.row_val[r] = part;
     }
-    if (lane == 0) a.row_val[r] = part;
   }
 }
 
