@@ -241,3 +241,31 @@ def test_gpu_cmfd_linear_source_converges_to_unaccelerated_answer():
     assert np.max(np.abs(m - mr)) < 2e-4 * np.abs(mr).max()
     ref.close()
     s.close()
+
+
+def test_gpu_cmfd_generic_instance_converges_to_unaccelerated_answer():
+    """More than 8 coarse groups take the generic instance of the device
+    coarse solve (512 threads, a cell's groups looped at run time): a
+    16-group assembly with every group its own coarse group reaches the
+    unaccelerated answer in fewer iterations."""
+    from openmoc_gb300 import Cmfd, GB300Solver
+    p = _assembly(16)
+    tol = 1e-6
+    ref = GB300Solver(p, device=0)
+    ref.setConvergenceThreshold(tol)
+    ref.computeEigenvalue(20000, 1)
+    n_plain = ref.getNumIterations()
+    assert n_plain < 20000
+    s = GB300Solver(p, device=0)
+    s.setConvergenceThreshold(tol)
+    c = Cmfd()
+    c.setLatticeStructure(17, 17)
+    s.setCmfd(c)
+    s.computeEigenvalue(20000, 1)
+    info = s.getCmfdInfo()
+    assert info["enabled"] and not info["failed"]
+    assert s.getNumIterations() < n_plain, (s.getNumIterations(), n_plain)
+    assert abs(s.getKeff() - ref.getKeff()) < 5e-6
+    assert _rel(s.getFluxes(), ref.getFluxes(), 1e-3) < 1e-4
+    ref.close()
+    s.close()
