@@ -10,9 +10,12 @@ count OpenMOC uses in its timer report (src/Solver.cpp:1901).  L2 is flushed
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
---impl reference times OpenMOC's CPU path on the host cores through the C
-restatement in oracle/ (OpenMOC itself cannot be built on the GPU host),
-with every host thread, on the same problem.
+--impl reference times OpenMOC's CPU path on the host cores with every host
+thread, on the same problem: OpenMOC's own CPUSolver (oracle/openmoc_run.cpp
+linked against OpenMOC's library, timed by its own Timer splits) where that
+build exists on the host, else the C restatement in oracle/moc_oracle.c.  It
+never loads the GPU library: its tracks come from a host-only build of the
+track generator (oracle/_build/libmoc_tracks.so).
 """
 from __future__ import annotations
 
@@ -22,6 +25,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -100,10 +104,10 @@ class Clocks:
     def __init__(self, device):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "_work", f"clocks_{os.getpid()}.csv")
+        fd, self.path = tempfile.mkstemp(prefix="moc_clocks_", suffix=".csv")
+        os.close(fd)
 
     def __enter__(self):
-        os.makedirs(os.path.dirname(self.path), exist_ok=True)
         try:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(
@@ -126,6 +130,8 @@ class Clocks:
 
     def summary(self):
         if self.proc is None or not os.path.exists(self.path):
+            if os.path.exists(self.path):
+                os.remove(self.path)
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         rows = []
         for line in open(self.path):
@@ -178,6 +184,47 @@ def build_problem(workload="assembly70"):
     return lattice.assembly_17x17()
 
 
+# Workloads OpenMOC's own driver (oracle/openmoc_run.cpp) can build
+OPENMOC_CONFIGS = {"assembly70": "assembly70", "core51": "core51"}
+OPENMOC_RUNNER = os.path.join(ROOT, "oracle", "_ref", "openmoc_run_f32")
+ORACLE_TRACKS = os.path.join(ROOT, "oracle", "_build", "libmoc_tracks.so")
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def bench_config(p, workload, world):
+    """The workload description both arms report (the same keys and values,
+    so the two lines compare like for like)."""
+    return {"workload": WORKLOADS[workload], "fsrs": p.num_fsrs, "tracks": p.num_tracks,
+            "segments": p.num_segments, "groups": p.num_groups,
+            "integrations_per_step": p.integrations_per_sweep,
+            "l2": "GPU: a 2 x L2 buffer is overwritten before every timed step",
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
+
+
+def openmoc_rate(workload, warmup, iters, threads):
+    """OpenMOC's own CPUSolver on the workload (FP32 build, OpenMP over
+    `threads`), timed by its Timer splits: integrations per second of whole
+    source iterations ("Total time" less "Solver initialization") and of the
+    "Transport Sweep" split alone.  None where the OpenMOC build is absent
+    or does not run on this host."""
+    if workload not in OPENMOC_CONFIGS or not os.access(OPENMOC_RUNNER, os.X_OK):
+        return None
+    try:
+        r = subprocess.run([OPENMOC_RUNNER, OPENMOC_CONFIGS[workload], "time",
+                            str(warmup), str(iters), str(threads)],
+                           capture_output=True, text=True, timeout=1800)
+    except OSError:
+        return None
+    if r.returncode != 0:
+        return None
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    iter_s = d["total_s"] - d["init_s"]
+    d["value"] = d["integrations_per_iteration"] * d["iterations"] / iter_s
+    d["sweep_value"] = d["integrations_per_iteration"] * d["iterations"] / d["transport_sweep_s"]
+    d["seconds_per_iteration"] = iter_s / d["iterations"]
+    return d
+
+
 def cpu_reference_rate(p, iters, threads):
     """Integrations/s of the oracle's source iteration on the host cores
     (CPULSSolver's when the problem carries a linear source)."""
@@ -204,36 +251,104 @@ def cpu_reference_rate(p, iters, threads):
     return p.integrations_per_sweep * iters / dt, dt
 
 
+def cpu_baseline(p, workload, iters):
+    """The CPU baseline beside the GPU number: OpenMOC's CPUSolver where it
+    was built on this host, else the oracle port; every host thread."""
+    threads = os.cpu_count() or 1
+    d = openmoc_rate(workload, 1, iters, threads)
+    if d is not None:
+        return {"value": d["value"], "unit": "integrations/s", "cores": threads,
+                "kind": "reference",
+                "sample": f"{iters} source iterations of OpenMOC's CPUSolver (FP32) on "
+                          f"the workload after 1 warm-up iteration, Timer splits; "
+                          f"transport sweep alone {d['sweep_value']:.4g}/s"}
+    r, dt = cpu_reference_rate(p, iters, threads)
+    return {"value": r, "unit": "integrations/s", "cores": threads, "kind": "port",
+            "sample": f"{iters} full source iterations of the workload "
+                      f"({dt:.1f} s, oracle/moc_oracle.c, OpenMP, FP32; OpenMOC's "
+                      "own build is absent on this host)"}
+
+
+def accuracy(p, workload, keff, flux, iters):
+    """Errors of a GPU result after `iters` source iterations from the flat
+    guess: against OpenMOC's FP64 CPUSolver at the same iteration count
+    (tests/golden/openmoc_<config>_f64.json: its 4096-flux sample and group
+    sums) and against the FP64 oracle's full flux."""
+    from oracle.oracle import FISSION_SOURCE, Oracle
+    out = {"iterations": iters}
+    flux = np.asarray(flux, np.float64).ravel()
+    path = os.path.join(GOLDEN, f"openmoc_{OPENMOC_CONFIGS.get(workload, '-')}_f64.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            g = json.load(f)
+        if int(g["iterations"]) == iters:
+            idx = np.asarray(g["flux_sample_index"], np.int64)
+            ref = np.asarray(g["flux_sample"], np.float64)
+            sums = flux.reshape(-1, p.num_groups).sum(axis=0)
+            rs = np.asarray(g["group_flux_sums"], np.float64)
+            out["vs_openmoc_fp64"] = {
+                "keff_abs_err": abs(keff - g["keff"]),
+                "flux_max_rel_err": float(np.max(np.abs(flux[idx] - ref) / np.abs(ref))),
+                "group_sum_max_rel_err": float(np.max(np.abs(sums - rs) / np.abs(rs))),
+                "fluxes_compared": int(idx.size) + p.num_groups}
+    o = Oracle(p, "f64", num_threads=os.cpu_count() or 1)
+    t0 = time.perf_counter()
+    o.compute_eigenvalue(iters, FISSION_SOURCE, 1e-30)
+    out["vs_fp64_oracle"] = {
+        "keff_abs_err": abs(keff - o.keff),
+        "flux_max_rel_err": float(np.max(np.abs(flux - o.phi) / np.abs(o.phi))),
+        "fluxes_compared": int(flux.size), "oracle_s": time.perf_counter() - t0}
+    out["bar"] = {"keff_abs": 1e-5, "flux_rel": 1e-4}
+    return out
+
+
 def run_reference(args):
     rank, world, _ = env_rank()
     if rank != 0:
         return
+    from openmoc_gb300 import lattice
+    if not os.path.exists(ORACLE_TRACKS):
+        subprocess.check_call(["bash", os.path.join(ROOT, "oracle", "build.sh")])
+    lattice.use_host_library(ORACLE_TRACKS)
     p = build_problem(args.workload)
     threads = os.cpu_count() or 1
-    rates = []
-    for _ in range(args.warmup):
-        cpu_reference_rate(p, 1, threads)
     t_all = time.perf_counter()
-    for _ in range(args.steps):
-        r, _ = cpu_reference_rate(p, 1, threads)
-        rates.append(r)
-    elapsed = time.perf_counter() - t_all
-    value = float(np.mean(rates))
+    d = openmoc_rate(args.workload, args.warmup, args.steps, threads)
+    if d is not None:
+        assert (d["fsrs"], d["tracks"], d["segments"]) == (
+            p.num_fsrs, p.num_tracks, p.num_segments), "OpenMOC built a different problem"
+        value = d["value"]
+        ms_per_step = 1e3 * d["seconds_per_iteration"]
+        base = {"kind": "reference",
+                "sample": f"{args.steps} source iterations of OpenMOC's CPUSolver (FP32 "
+                          f"build) after {args.warmup} warm-up iterations, timed by its "
+                          f"Timer splits; transport sweep alone {d['sweep_value']:.4g}/s"}
+    else:
+        rates = []
+        for _ in range(args.warmup):
+            cpu_reference_rate(p, 1, threads)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            r, _ = cpu_reference_rate(p, 1, threads)
+            rates.append(r)
+        value = float(np.mean(rates))
+        ms_per_step = 1e3 * (time.perf_counter() - t0) / args.steps
+        base = {"kind": "port",
+                "sample": f"{args.steps} full source iterations of the workload "
+                          "(oracle/moc_oracle.c, OpenMP, FP32): OpenMOC's own build "
+                          "does not exist on this host (no OpenMOC source tree here, "
+                          "and builds made elsewhere do not run on this CPU)"}
     out = {
         "impl": "reference", "metric": METRIC, "value": value,
         "unit": "integrations/s", "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded cross sections, generated tracks)",
-        "config": {"workload": WORKLOADS[args.workload], "fsrs": p.num_fsrs,
-                   "tracks": p.num_tracks, "segments": p.num_segments,
-                   "integrations_per_step": p.integrations_per_sweep},
-        "cpu_baseline": {"value": value, "unit": "integrations/s", "cores": threads,
-                         "kind": "port",
-                         "sample": f"{args.steps} full source iterations of the workload "
-                                   "(oracle/moc_oracle.c, OpenMP, FP32)"},
+        "config": bench_config(p, args.workload, world),
+        "cpu_baseline": dict(value=value, unit="integrations/s", cores=threads, **base),
         "e2e": {"value": value, "unit": "integrations/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
+        "wall_s": time.perf_counter() - t_all,
     }
     print(json.dumps(out), flush=True)
 
@@ -320,12 +435,16 @@ def run_gpu(args):
         e2e = end_to_end(p, args, local, torch, otf=args.workload.endswith("_otf"))
 
     cpu = None
+    acc = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        threads = os.cpu_count() or 1
-        r, dt = cpu_reference_rate(p, args.cpu_iters, threads)
-        cpu = {"value": r, "unit": "integrations/s", "cores": threads, "kind": "port",
-               "sample": f"{args.cpu_iters} full source iterations of the workload "
-                         f"({dt:.1f} s, oracle/moc_oracle.c, OpenMP, FP32)"}
+        cpu = cpu_baseline(p, args.workload, args.cpu_iters)
+        # the error of the end-to-end result against the FP64 references
+        if e2e is not None and not ls and not args.no_accuracy:
+            acc = accuracy(p, args.workload, e2e.pop("keff"), e2e.pop("flux"),
+                           args.e2e_iters)
+    if e2e is not None:
+        e2e.pop("keff", None)
+        e2e.pop("flux", None)
 
     if rank == 0:
         out = {
@@ -334,19 +453,15 @@ def run_gpu(args):
             "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded cross sections, generated tracks)",
-            "config": {"workload": WORKLOADS[args.workload], "fsrs": p.num_fsrs,
-                       "tracks": p.num_tracks,
-                       "segments": p.num_segments, "groups": p.num_groups,
-                       "integrations_per_step": ints, "l2": "flushed before every step",
-                       "sweep_shape": {"lanes_per_track_direction": lps,
-                                       "group_pairs_per_lane": slots,
-                                       "exponential": ("rational G(x), F1/F2/H from it"
-                                                       if ls else "hardware ex2" if otf
-                                                       else ["shared-memory table",
-                                                             "hardware ex2"][exp_kind])},
-                       "autotune_ms": {f"{a}x{b}/{'table' if e == 0 else 'ex2'}": round(t, 4)
-                                       for a, b, e, t in tuning},
-                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+            "config": bench_config(p, args.workload, world),
+            "sweep_shape": {"lanes_per_track_direction": lps,
+                            "group_pairs_per_lane": slots,
+                            "exponential": ("rational G(x), F1/F2/H from it"
+                                            if ls else "hardware ex2" if otf
+                                            else ["shared-memory table",
+                                                  "hardware ex2"][exp_kind])},
+            "autotune_ms": {f"{a}x{b}/{'table' if e == 0 else 'ex2'}": round(t, 4)
+                            for a, b, e, t in tuning},
             "sweep_ms_per_step": sweep_avg,
             "sources": sources,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak,
@@ -365,6 +480,8 @@ def run_gpu(args):
             out["e2e"] = e2e
         if cpu:
             out["cpu_baseline"] = cpu
+        if acc:
+            out["accuracy"] = acc
         if args.batch > 0:
             out["batched_instances"] = run_instances(p, args)
         core = None
@@ -525,6 +642,7 @@ def end_to_end(p, args, device, torch, otf=False):
         flux = s.getFluxes()
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
+        keff = s.getKeff()
         s.close()
         if i > 0:
             times.append(dt)
@@ -534,7 +652,8 @@ def end_to_end(p, args, device, torch, otf=False):
     return {"value": p.integrations_per_sweep * args.e2e_iters / t, "unit": "integrations/s",
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
             "iterations_per_step": args.e2e_iters, "seconds_per_step": t,
-            "setup_seconds_per_step": float(np.mean(setups))}
+            "setup_seconds_per_step": float(np.mean(setups)),
+            "keff": keff, "flux": flux}
 
 
 def run_instances(p, args, iters=10):
@@ -773,6 +892,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-iters", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="leave out the FP64 comparison of the end-to-end result")
     ap.add_argument("--shape", default="",
                     help="lanes,group_pairs_per_lane,exp (0 table, 1 ex2) instead of autotuning")
     ap.add_argument("--workload", default="assembly70", choices=sorted(WORKLOADS),

@@ -169,6 +169,13 @@ int moc_set_iterations_per_sync(moc_ctx* ctx, int k);
 int moc_set_source_kernel(moc_ctx* ctx, int kind);
 /** The kernel that computeFSRSources runs (MOC_SOURCES_FP32 or _TF32X3). */
 int moc_get_source_kernel(moc_ctx* ctx, int* kind);
+/** No counterpart in the reference.  How many times the tensor-core source
+ *  kernel polls an mbarrier (its operand copy, its products) before it gives
+ *  up: it then records the failure, waits once more with the full default
+ *  limit for the work in flight, frees its tensor memory and returns, and
+ *  the solve returns MOC_ERR_TIMEOUT.  polls < 0 restores the default
+ *  (2^22); 0 gives up at once (a way to exercise the failure path). */
+int moc_set_tensor_wait_limit(moc_ctx* ctx, int64_t polls);
 
 /* ---- whole solves, device-resident (Solver::computeEigenvalue,
  *      computeSource, computeFlux; src/Solver.cpp:1352-1700) ------------- */
@@ -249,14 +256,18 @@ int moc_eval_attenuation(moc_ctx* ctx, int kind, const float* x, float* g,
  *  code on a latency-critical path that cannot take cudaMalloc's implicit
  *  device synchronisation.  All pointers are device memory of the current
  *  device; stream is a cudaStream_t (NULL: the legacy default stream).
- *  Scratch is a fixed 4 MiB per-FSR array inside the library (held by every
- *  GPU that loads it), so num_fsrs may not exceed MOC_NOALLOC_MAX_FSRS; the
- *  first call on a device looks up that array's address (make it before any
- *  stream capture).  Calls share the array: calls that overlap on the GPU
- *  (different streams, or threads) race and must be serialised.  The sum is
- *  deterministic. */
+ *  nu_sigma_f holds num_materials rows of num_groups; an FSR whose
+ *  fsr_mat entry is outside [0, num_materials) reads nothing and makes
+ *  *total NaN.  Scratch is a fixed 4 MiB per-FSR array inside the library
+ *  (held by every GPU that loads it), so num_fsrs may not exceed
+ *  MOC_NOALLOC_MAX_FSRS; the first call in each CUDA context of a device
+ *  (again after cudaDeviceReset) looks up that array's address (make it
+ *  before any stream capture).  Calls share the array: calls that overlap
+ *  on the GPU (different streams, or threads) race and must be serialised.
+ *  The sum is deterministic. */
 int moc_fission_source_total_noalloc(const float* phi, int64_t ld,
                                      const float* nu_sigma_f,
+                                     int32_t num_materials,
                                      const int32_t* fsr_mat,
                                      const float* fsr_vol, int64_t num_fsrs,
                                      int32_t num_groups, void* stream,

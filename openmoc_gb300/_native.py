@@ -96,6 +96,7 @@ _SIGS = {
     "moc_set_iterations_per_sync": ([_P, C.c_int], C.c_int),
     "moc_set_source_kernel": ([_P, C.c_int], C.c_int),
     "moc_get_source_kernel": ([_P, C.POINTER(C.c_int)], C.c_int),
+    "moc_set_tensor_wait_limit": ([_P, C.c_int64], C.c_int),
     "moc_compute_eigenvalue": ([_P, C.c_int, C.c_int], C.c_int),
     "moc_compute_source": ([_P, C.c_int, C.c_double, C.c_int], C.c_int),
     "moc_compute_flux": ([_P, C.c_int, C.c_int], C.c_int),
@@ -125,8 +126,8 @@ _SIGS = {
     "moc_get_launch_count": ([_P, C.POINTER(C.c_int64)], C.c_int),
     "moc_bench_iterations": ([_P, C.c_int, C.c_int, C.c_int, _P, _P], C.c_int),
     "moc_eval_attenuation": ([_P, C.c_int, _P, _P, C.c_int64], C.c_int),
-    "moc_fission_source_total_noalloc": ([_P, C.c_int64, _P, _P, _P, C.c_int64,
-                                          C.c_int32, _P, _P], C.c_int),
+    "moc_fission_source_total_noalloc": ([_P, C.c_int64, _P, C.c_int32, _P, _P,
+                                          C.c_int64, C.c_int32, _P, _P], C.c_int),
     "moc_set_linear_source": ([_P, C.POINTER(LSGeometry)], C.c_int),
     "moc_get_linear_source": ([_P, C.POINTER(C.c_int), C.POINTER(C.c_int64)], C.c_int),
     "moc_get_flux_moments": ([_P, _P, C.c_int64], C.c_int),

@@ -150,6 +150,7 @@ struct moc_ctx {
   int32_t* tc_tile_mat = nullptr;
   float* tc_b = nullptr;
   int tc_tiles = 0;
+  int64_t tc_wait_limit = -1;  // < 0: the kernel's default
   // FSRs with the last ids that take a large share of the segments (the
   // moderator above an extruded lattice): tallied in shared memory by the
   // 3D sweep instances
@@ -320,6 +321,8 @@ moc::SolverArgs solver_args(moc_ctx* c, int check_done) {
     a.tc_tiles = c->tc_tiles;
     a.tc_n = moc::tc_pad_n(c->d.num_groups);
     a.tc_k = moc::tc_pad_k(c->d.num_groups);
+    a.tc_wait_limit = c->tc_wait_limit < 0 ? moc::kTcDefaultWaitLimit
+                                           : (unsigned) c->tc_wait_limit;
   }
   a.sigma_t = c->sigma_t;
   a.sigma_s = c->sigma_s;
@@ -630,6 +633,7 @@ int begin_solve(moc_ctx* c, int mode, int max_iters, int res_type,
   s.neg_sources = 0;
   s.neg_fluxes = 0;
   s.num_fissionable = c->num_fissionable;
+  s.tc_error = 0;
   MOC_TRY(push(c));
   c->sweep_ms = 0.0;
   c->num_sweeps = 0;
@@ -1628,6 +1632,14 @@ int moc_get_sweep_shape(moc_ctx* c, int* lps, int* slots) {
     pick_shape(c->d.num_groups, &c->lps, &c->slots, max_slots(c));
   *lps = c->lps;
   *slots = c->slots;
+  return MOC_OK;
+}
+
+int moc_set_tensor_wait_limit(moc_ctx* c, int64_t polls) {
+  MOC_CHECK(c, MOC_ERR_ARG, "null context");
+  MOC_CHECK(polls <= (int64_t) 0xFFFFFFFFu, MOC_ERR_ARG,
+            "the wait limit must fit 32 bits");
+  c->tc_wait_limit = polls < 0 ? -1 : polls;
   return MOC_OK;
 }
 

@@ -153,6 +153,9 @@ struct SolverArgs {
   const float* tc_b;         // [M][2][tc_n][tc_k]
   int tc_tiles;
   int tc_n, tc_k;            // padded destination / origin group counts
+  // polls of an mbarrier before the tensor-core source kernel gives up on
+  // its first wait (its drain waits use the full default limit)
+  unsigned tc_wait_limit;
   // Linear source (null: flat source): flux moments and reduced source
   // moments / sigma_t ([R][ld][2], x and y adjacent per group), the inverse
   // expansion matrix per FSR (xx, yy, xy), the source constants [R][3][ld]
@@ -167,6 +170,8 @@ struct SolverArgs {
 
 // Rows (FSRs) per tile of the tensor-core source kernel: the MMA's M.
 constexpr int kTcRows = 128;
+// mbarrier polls before a wait of the tensor-core source kernel gives up
+constexpr unsigned kTcDefaultWaitLimit = 1u << 22;
 
 // Records the text returned by moc_last_error on this thread; returns code.
 int set_error(int code, const char* msg);

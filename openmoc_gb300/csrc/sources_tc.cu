@@ -42,7 +42,6 @@ static_assert(kTcThreads == kTcRows, "one thread per tile row");
 constexpr int kTcColumns = 128;         // tensor-memory columns allocated
 constexpr float kTcFluxEpsilon = 1.0e-25f;
 constexpr double kTcOneOverFourPi = 0.07957747154594767;
-constexpr unsigned kTcWaitLimit = 1u << 22;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
   return (uint32_t) __cvta_generic_to_shared(p);
@@ -72,8 +71,9 @@ __host__ __device__ constexpr uint32_t tf32_idesc(int n) {
          ((uint32_t) (128 >> 4) << 24);
 }
 
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  for (unsigned i = 0; i < kTcWaitLimit; i++) {
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity,
+                                          unsigned limit) {
+  for (unsigned i = 0; i < limit; i++) {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
@@ -244,7 +244,7 @@ sources_tc_kernel(const SolverArgs a, int iteration, int zero_phi) {
   // one thread issues the products and waits for them; the others learn
   // the outcome at the barrier
   if (threadIdx.x == 0) {
-    if (mbar_wait(bar_b, 0)) {
+    if (mbar_wait(bar_b, 0, a.tc_wait_limit)) {
       const uint32_t idesc = tf32_idesc(N);
       const uint32_t a_hi = smem_addr(sa_hi), a_lo = smem_addr(sa_lo);
       const uint32_t b_hi = smem_addr(sb), b_lo = b_hi + b_bytes;
@@ -263,19 +263,20 @@ sources_tc_kernel(const SolverArgs a, int iteration, int zero_phi) {
           "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster."
           "b64 [%0];" ::"r"(bar_mma)
           : "memory");
-      if (!mbar_wait(bar_mma, 0)) {
-        // record it, and give the products a second bounded wait before
-        // the tensor memory is freed
+      if (!mbar_wait(bar_mma, 0, a.tc_wait_limit)) {
+        // record it, and give the products a second wait, bounded by the
+        // full default limit, before the tensor memory is freed
         sc->tc_error = 1;
         s_ok = 0;
-        mbar_wait(bar_mma, 0);
+        mbar_wait(bar_mma, 0, kTcDefaultWaitLimit);
       }
     } else {
-      // the bulk copy never completed: record it, and give it a second
-      // bounded wait before the shared memory goes away
+      // the bulk copy did not complete in time: record it, and give it a
+      // second wait, bounded by the full default limit, before the shared
+      // memory goes away
       sc->tc_error = 1;
       s_ok = 0;
-      mbar_wait(bar_b, 0);
+      mbar_wait(bar_b, 0, kTcDefaultWaitLimit);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");

@@ -52,8 +52,21 @@ class _Spec(C.Structure):
     ]
 
 
+_host_library = None
+
+
+def use_host_library(path: str) -> None:
+    """Binds the track generator and the cross-section builder to a
+    host-only build of ``csrc/lattice.cpp`` at ``path`` (the same
+    ``moc_lattice_*`` / ``moc_synthetic_xs`` entry points, no CUDA code)
+    instead of libopenmoc_gb300.so, for processes that must not load the GPU
+    library.  Device ray tracing (``device=``) is then unavailable."""
+    global _host_library
+    _host_library = C.CDLL(path)
+
+
 def _lib():
-    L = _native.lib()
+    L = _native.lib() if _host_library is None else _host_library
     if not getattr(L, "_lattice_sigs", False):
         L.moc_lattice_generate.argtypes = [C.POINTER(_Spec), C.POINTER(C.c_void_p)]
         L.moc_lattice_generate.restype = C.c_int
@@ -66,9 +79,10 @@ def _lib():
                                           C.c_double, C.c_int32, C.c_int32,
                                           C.POINTER(C.c_void_p)]
         L.moc_lattice_extrude.restype = C.c_int
-        L.moc_lattice_generate_device.argtypes = [C.POINTER(_Spec), C.c_int32,
-                                                  C.POINTER(C.c_void_p)]
-        L.moc_lattice_generate_device.restype = C.c_int
+        if hasattr(L, "moc_lattice_generate_device"):
+            L.moc_lattice_generate_device.argtypes = [C.POINTER(_Spec), C.c_int32,
+                                                      C.POINTER(C.c_void_p)]
+            L.moc_lattice_generate_device.restype = C.c_int
         L.moc_lattice_otf_sizes.argtypes = [C.c_void_p, C.POINTER(C.c_int64),
                                             C.POINTER(C.c_int64), C.POINTER(C.c_int32)]
         L.moc_lattice_otf_sizes.restype = C.c_int

@@ -310,6 +310,13 @@ class GB300Solver:
         self._call("moc_get_source_kernel", C.byref(k))
         return {1: "fp32", 2: "tf32x3"}[k.value]
 
+    def setTensorWaitLimit(self, polls: int) -> None:
+        """mbarrier polls before the tensor-core source kernel gives up
+        waiting (the solve then raises the timeout status); a negative value
+        restores the default.  No counterpart in OpenMOC."""
+        self._need_ctx()
+        self._call("moc_set_tensor_wait_limit", int(polls))
+
     def setIterationsPerSync(self, k: int) -> None:
         self._need_ctx()
         self._call("moc_set_iterations_per_sync", int(k))

@@ -8,8 +8,14 @@
 # infinite lattice z-width test in Lattice::getLatZ, src/Universe.cpp:1986),
 # which gcc 13 folds away under plain -ffast-math.
 #
-#   make -f oracle/ref.mk REF=/root/reference -j8
-REF ?= /root/reference
+# Also links oracle/openmoc_run.cpp (OpenMOC run on the benchmark
+# configurations: golden files and the timed CPU baseline) against each build.
+#
+#   make -f oracle/ref.mk REF=<OpenMOC source tree> -j8
+ifndef REF
+$(error REF must name an OpenMOC source tree (the directory holding src/))
+endif
+ORACLE := $(patsubst %/,%,$(dir $(lastword $(MAKEFILE_LIST))))
 OUT ?= oracle/_ref
 CXX ?= g++
 
@@ -21,15 +27,21 @@ SRCS := Cell Cmfd CPUSolver CPULSSolver ExpEvaluator Geometry linalg \
 
 COMMON := -O3 -ffast-math -fno-finite-math-only -fopenmp -std=c++11 -fpic -w -DGCC -DOPENMP \
           -DVEC_ALIGNMENT=64
-F32FLAGS := $(COMMON) -DFP_PRECISION=float -DSINGLE -DVEC_LENGTH=8 \
-            -DCMFD_PRECISION=float -DLINALG_TOL=1E-7
-F64FLAGS := $(COMMON) -DFP_PRECISION=double -DVEC_LENGTH=4 \
-            -DCMFD_PRECISION=double -DLINALG_TOL=1E-15
+F32DEFS := -DFP_PRECISION=float -DSINGLE -DVEC_LENGTH=8 -DCMFD_PRECISION=float \
+           -DLINALG_TOL=1E-7
+F64DEFS := -DFP_PRECISION=double -DVEC_LENGTH=4 -DCMFD_PRECISION=double \
+           -DLINALG_TOL=1E-15
+F32FLAGS := $(COMMON) $(F32DEFS)
+F64FLAGS := $(COMMON) $(F64DEFS)
+RUNFLAGS := -O2 -fopenmp -std=c++11 -w -DGCC -DOPENMP -DVEC_ALIGNMENT=64 -I$(REF)/src
 
 OBJ32 := $(addprefix $(OUT)/f32/,$(addsuffix .o,$(SRCS)))
 OBJ64 := $(addprefix $(OUT)/f64/,$(addsuffix .o,$(SRCS)))
+RUN_DEPS := $(ORACLE)/openmoc_run.cpp $(ORACLE)/../openmoc_gb300/adapter/pack_reference.h \
+            $(ORACLE)/../openmoc_gb300/csrc/synthetic_xs.h
 
-all: $(OUT)/libopenmoc_f32.a $(OUT)/libopenmoc_f64.a
+all: $(OUT)/libopenmoc_f32.a $(OUT)/libopenmoc_f64.a \
+     $(OUT)/openmoc_run_f32 $(OUT)/openmoc_run_f64
 
 $(OUT)/f32/%.o: $(REF)/src/%.cpp
 	@mkdir -p $(dir $@)
@@ -44,5 +56,11 @@ $(OUT)/libopenmoc_f32.a: $(OBJ32)
 
 $(OUT)/libopenmoc_f64.a: $(OBJ64)
 	ar rcs $@ $^
+
+$(OUT)/openmoc_run_f32: $(RUN_DEPS) $(OUT)/libopenmoc_f32.a
+	$(CXX) $(RUNFLAGS) $(F32DEFS) $< $(OUT)/libopenmoc_f32.a -o $@
+
+$(OUT)/openmoc_run_f64: $(RUN_DEPS) $(OUT)/libopenmoc_f64.a
+	$(CXX) $(RUNFLAGS) $(F64DEFS) $< $(OUT)/libopenmoc_f64.a -o $@
 
 .PHONY: all

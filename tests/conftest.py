@@ -47,3 +47,56 @@ def ls_arrays(arr):
     if "fixed_source_xy" in arr:
         d["fixed_xy"] = arr["fixed_source_xy"]
     return d
+
+
+def load_openmoc_config_golden(config):
+    """OpenMOC's FP64 CPUSolver on a benchmark configuration after a fixed
+    number of source iterations (tests/golden/make_config_goldens.sh):
+    track checksums, keff, per-group flux sums and a sample of FSR fluxes."""
+    import json
+    with open(os.path.join(GOLDEN, f"openmoc_{config}_f64.json")) as f:
+        return json.load(f)
+
+
+def track_checksum(a):
+    """The order-sensitive checksum oracle/openmoc_run.cpp writes: the sum
+    over i of (word_i + 1) * (2 i + 1) mod 2^64, word_i the i-th element's
+    bytes as a little-endian unsigned integer."""
+    import numpy as np
+    a = np.ascontiguousarray(a)
+    words = a.view({1: np.uint8, 4: np.uint32, 8: np.uint64}[a.itemsize]).astype(np.uint64)
+    i = np.arange(a.size, dtype=np.uint64)
+    return int(np.sum((words + np.uint64(1)) * (np.uint64(2) * i + np.uint64(1)),
+                      dtype=np.uint64))
+
+
+def quantised_sums(a, bits):
+    """The plain and the (i mod 1009 + 1)-weighted sum, mod 2^64, of
+    q_i = floor(a_i * 2^bits + 1/2): the exact integer sums
+    oracle/openmoc_run.cpp writes for segment lengths and volumes."""
+    import numpy as np
+    q = np.floor(np.asarray(a, np.float64) * 2.0 ** bits + 0.5).astype(np.int64)
+    q = q.view(np.uint64)
+    w = (np.arange(q.size) % 1009 + 1).astype(np.uint64)
+    return int(np.sum(q, dtype=np.uint64)), int(np.sum(w * q, dtype=np.uint64))
+
+
+def wrapped_difference(a, b):
+    """a - b for two sums kept mod 2^64, as a signed integer."""
+    d = (int(a) - int(b)) % (1 << 64)
+    return d - (1 << 64) if d >= (1 << 63) else d
+
+
+def errors_against_golden(keff, flux, golden):
+    """|keff - keff_ref|, the largest relative error over the golden's flux
+    sample and over its per-group flux sums."""
+    import numpy as np
+    flux = np.asarray(flux, np.float64).ravel()
+    G = int(golden["num_groups"])
+    idx = np.asarray(golden["flux_sample_index"], np.int64)
+    ref = np.asarray(golden["flux_sample"], np.float64)
+    sums = flux.reshape(-1, G).sum(axis=0)
+    ref_sums = np.asarray(golden["group_flux_sums"], np.float64)
+    return (abs(keff - golden["keff"]),
+            float(np.max(np.abs(flux[idx] - ref) / np.abs(ref))),
+            float(np.max(np.abs(sums - ref_sums) / np.abs(ref_sums))))

@@ -2,7 +2,8 @@
 flat-source eigenvalue path into tests/golden/reference_results.json, and
 those of its linear-source tests into tests/golden/reference_results_ls.json.
 
-Source files (read from the reference tree, REF, default /root/reference):
+Source files (read from the reference tree named by the environment
+variable REF):
   tests/test_forward_pin_cell/results_true.dat
   tests/test_forward_pin_cell_70g/results_true.dat
   tests/test_2d_gradient_linear_source/results_true.dat  (CPULSSolver)
@@ -16,7 +17,7 @@ import json
 import os
 import sys
 
-REF = os.environ.get("REF", "/root/reference")
+REF = os.environ.get("REF", "")
 HERE = os.path.dirname(os.path.abspath(__file__))
 CASES = {"pin_c5g7": "test_forward_pin_cell",
          "pin_70g": "test_forward_pin_cell_70g"}
@@ -42,6 +43,8 @@ def parse(path):
 
 
 def main():
+    if not REF:
+        sys.exit("set REF to the OpenMOC source tree")
     for cases, name in ((CASES, "reference_results.json"),
                         (LS_CASES, "reference_results_ls.json")):
         res = {}

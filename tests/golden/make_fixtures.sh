@@ -1,10 +1,10 @@
 #!/bin/bash
 # Regenerates the golden fixtures in tests/golden/ from OpenMOC's own C++
 # library, built from the reference sources by oracle/ref.mk.  Needs the
-# reference tree (REF, default /root/reference); run from the repo root:
+# reference tree (REF=<OpenMOC source tree>); run from the repo root:
 #   bash tests/golden/make_fixtures.sh [case]
 set -euo pipefail
-REF=${REF:-/root/reference}
+: "${REF:?REF must name an OpenMOC source tree}"
 HERE=$(cd "$(dirname "$0")" && pwd)
 ROOT=$(cd "$HERE/../.." && pwd)
 OUT=$ROOT/oracle/_ref

@@ -1,9 +1,10 @@
 """The OpenMOC-side drop-in (openmoc_gb300/adapter/GB300Solver.{h,cpp})
 compiles against OpenMOC's own headers, links with OpenMOC's library and
 libopenmoc_gb300.so, and runs through OpenMOC's API.  Needs OpenMOC's source
-tree (it is the reference project itself), so it is skipped where that tree
-is absent; without a GPU the driver reports the adapter's error instead of
-a result, which must be the ERROR-level exception OpenMOC raises."""
+tree (it is the reference project itself), named by the environment variable
+OPENMOC_SOURCE, so it is skipped where that is unset; without a GPU the
+driver reports the adapter's error instead of a result, which must be the
+ERROR-level exception OpenMOC raises."""
 import os
 import subprocess
 
@@ -11,11 +12,12 @@ import pytest
 
 from conftest import ROOT
 
-REF = os.environ.get("OPENMOC_SOURCE", "/root/reference")
+REF = os.environ.get("OPENMOC_SOURCE", "")
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "src")),
-                    reason="OpenMOC source tree not available")
+@pytest.mark.skipif(not REF or not os.path.isdir(os.path.join(REF, "src")),
+                    reason="set OPENMOC_SOURCE to an OpenMOC source tree to build the "
+                           "adapter against it")
 def test_adapter_builds_and_runs(tmp_path):
     from openmoc_gb300 import build
     lib = build.build()

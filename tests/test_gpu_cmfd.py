@@ -269,3 +269,61 @@ def test_gpu_cmfd_generic_instance_converges_to_unaccelerated_answer():
     assert _rel(s.getFluxes(), ref.getFluxes(), 1e-3) < 1e-4
     ref.close()
     s.close()
+
+
+def test_gpu_cmfd_core_mesh_matches_oracle_step_by_step():
+    """The regime of the 51 x 51 core's CMFD benchmark: a 51 x 51 pin mesh
+    (2,601 cells, 1,300 and 1,301 of each red-black colour, so each thread
+    of the device coarse solve updates two cells of a colour) with two
+    coarse groups, three fuel sets in a checkerboard of assemblies, vacuum
+    on +x and +y.  A fixed number of iterations (a coarser quadrature than
+    the benchmark's keeps the oracle quick): keff, fluxes, the coarse fluxes
+    and the coarse keff of the last coarse solve against the FP64 oracle
+    CMFD (oracle/cmfd_oracle.py)."""
+    from openmoc_gb300 import Cmfd, GB300Solver
+    from openmoc_gb300 import lattice as lat
+    from openmoc_gb300.lattice import REFLECTIVE, VACUUM
+    from oracle.cmfd_oracle import CmfdOracle, cmfd_eigenvalue
+    from oracle.oracle import Oracle
+    mats = lat._fuel_mod(3, 7, 3)
+    pm = np.zeros((51, 51), np.int32)
+    for ar in range(3):
+        for ac in range(3):
+            block = np.full((17, 17), (ar + ac) % 3, np.int32)
+            for (r, c) in lat.GUIDE_TUBES_17x17:
+                block[r, c] = 3
+            pm[17 * ar:17 * ar + 17, 17 * ac:17 * ac + 17] = block
+    p = lat.lattice(51, 51, pm, mats, 3, num_azim=8, spacing=0.1,
+                    bc=(REFLECTIVE, VACUUM, REFLECTIVE, VACUUM))
+    groups = [[1, 2, 3], [4, 5, 6, 7]]
+    c = Cmfd()
+    c.setLatticeStructure(51, 51)
+    c.setGroupStructure(groups)
+    mesh, keep = c.mesh(p)
+    g = p.cmfd_geometry
+    cm = CmfdOracle(p, 51, 51, keep[0], keep[1], keep[2], g["end_face"], g["bc"],
+                    keep[4], g["edc_mu"], g["edc_w"], centroid=g["fsr_centroid"],
+                    origin=(g["bounds"][0], g["bounds"][2]))
+    o = Oracle(p, "f64")
+    iters = 6
+    cmfd_eigenvalue(o, cm, iters, 1, 1e-30)
+    R = p.num_fsrs
+    # the FP32 device coarse solve and the FP64 host one
+    for host in (False, True):
+        c.useHostSolver(host)
+        s = GB300Solver(device=0)
+        s.setConvergenceThreshold(1e-30)
+        s.setTrackGenerator(p)
+        s.setCmfd(c)
+        s.computeEigenvalue(iters, 1)
+        info = s.getCmfdInfo()
+        assert s.getNumIterations() == iters
+        assert info["enabled"] and not info["failed"]
+        assert abs(s.getKeff() - o.keff) < 2e-6, host
+        assert _rel(s.getFluxes(), o.phi.reshape(R, -1), 1e-4) < 2e-5, host
+        old, new = s.getCmfdFluxes()
+        assert old.shape == (51 * 51, 2)
+        assert np.max(np.abs(new - cm.new_flux)) < 1e-4 * np.abs(cm.new_flux).max(), host
+        assert np.max(np.abs(old - cm.old_flux)) < 1e-4 * np.abs(cm.old_flux).max(), host
+        assert abs(info["keff"] - cm.keff) < 2e-6, host
+        s.close()

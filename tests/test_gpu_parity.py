@@ -218,6 +218,34 @@ def test_tensor_core_sources_eigenvalue_parity():
     s.close()
 
 
+def test_tensor_core_wait_timeout_is_reported_and_recovered():
+    """The tensor-core source kernel's bounded waits: with a limit of zero
+    polls its first wait gives up at once; it records the failure, drains
+    its copy with the default limit and frees its tensor memory, and the
+    solve reports the timeout status.  The same context then solves
+    normally (tensor memory was released), matching a fresh context."""
+    from openmoc_gb300._native import MOCError
+    p, sc, _ = load_case("pin_70g")
+    s = GB300Solver(p)
+    s.setSourceContraction("tf32x3")
+    s.setConvergenceThreshold(1e-30)
+    s.setTensorWaitLimit(0)
+    with pytest.raises(MOCError) as e:
+        s.computeEigenvalue(8, SCALAR_FLUX)
+    assert e.value.status == -6 and "gave up waiting" in str(e.value)
+    s.setTensorWaitLimit(-1)
+    s.computeEigenvalue(8, SCALAR_FLUX)
+    k, flux = s.getKeff(), s.getFluxes()
+    s.close()
+    t = GB300Solver(p)
+    t.setSourceContraction("tf32x3")
+    t.setConvergenceThreshold(1e-30)
+    t.computeEigenvalue(8, SCALAR_FLUX)
+    assert k == pytest.approx(t.getKeff(), abs=1e-7)
+    assert max_rel(flux, t.getFluxes()) <= 1e-5
+    t.close()
+
+
 def test_extruded_3d_lattice_matches_fp64_oracle():
     """A 2x2 lattice extruded into explicit 3D tracks by the axial
     extrusion (the generator of the 3D benchmark workload; its moderator
