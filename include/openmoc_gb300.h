@@ -152,8 +152,9 @@ int moc_get_tuning_log(moc_ctx* ctx, int* lps, int* slots, int* exp_kind,
                        float* ms, int capacity, int* count);
 
 /** Sweep kernel shape: lps lanes per track direction (power of two <= 32)
- *  each carrying `slots` energy groups (lps * slots >= G, slots <= 9);
- *  lps = 0 restores the built-in choice.  Replaces
+ *  each carrying `slots` pairs of energy groups (2 * lps * slots >= G,
+ *  slots at most the kernel's limit); lps = 0 restores the built-in choice.
+ *  Replaces
  *  GPUSolver::setNumThreadBlocks / setNumThreadsPerBlock
  *  (src/accel/cuda/GPUSolver.cu:987-1015). */
 int moc_set_sweep_shape(moc_ctx* ctx, int lps, int slots);
@@ -317,6 +318,40 @@ int moc_get_linear_expansion(moc_ctx* ctx, double* ilem, float* src_const);
 /** Solver::allowNegativeFluxes (src/Solver.cpp:623): no clamping of
  *  negative sources or fluxes. */
 int moc_set_negative_fluxes_allowed(moc_ctx* ctx, int allowed);
+
+/** Transport stabilization types (stabilizationType, src/Solver.h:103-113). */
+#define MOC_STABILIZE_DIAGONAL 0
+#define MOC_STABILIZE_YAMAMOTO 1
+#define MOC_STABILIZE_GLOBAL 2
+
+/** Solver::stabilizeTransport(factor, type) (src/Solver.cpp:676-681):
+ *  from the second eigenvalue iteration on, the flux after keff is blended
+ *  with the flux at the start of the iteration
+ *  (CPUSolver::computeStabilizingFlux + stabilizeFlux,
+ *  src/CPUSolver.cpp:2665-2810) before the normalisation.  on = 0 turns it
+ *  off.  Flat source only. */
+int moc_set_transport_stabilization(moc_ctx* ctx, int on, double factor,
+                                    int type);
+/** The protected hooks: CPUSolver::computeStabilizingFlux keeps the current
+ *  flux as the base of the correction; stabilizeFlux applies it
+ *  (src/CPUSolver.cpp:2665-2810). */
+int moc_compute_stabilizing_flux(moc_ctx* ctx);
+int moc_stabilize_flux(moc_ctx* ctx);
+/** CPUSolver::computeFSRFissionSources / computeFSRScatterSources
+ *  (src/CPUSolver.cpp:2030-2110): the reduced source holds the fission (or
+ *  the scattering) part alone, sum over g' of M[g][g'] phi[g'] / (4 pi), as
+ *  the Krylov solvers of openmoc.krylov use it; read it back with
+ *  moc_get_reduced_sources. */
+int moc_compute_fsr_fission_sources(moc_ctx* ctx);
+int moc_compute_fsr_scatter_sources(moc_ctx* ctx);
+
+/** Solver::setKeffFromNeutronBalance (src/Solver.cpp:2045-2048; used by
+ *  CPUSolver::computeKeff and transferBoundaryFlux, src/CPUSolver.cpp:
+ *  2258-2330, 2593-2600): on = 1 computes keff = fission / (absorption +
+ *  leakage), the leakage tallied by the sweep at vacuum track ends, instead
+ *  of keff *= fission / num_FSRs.  For the flat-source sweep of stored
+ *  segments; with CMFD the coarse solve's keff applies. */
+int moc_set_keff_from_neutron_balance(moc_ctx* ctx, int on);
 
 /* ---- on-the-fly 3D segmentation ------------------------------------------
  * For explicit 3D problems made by extruding a radial lattice

@@ -136,6 +136,12 @@ _SIGS = {
     "moc_set_fixed_source_moments": ([_P, _P, C.c_int64], C.c_int),
     "moc_get_linear_expansion": ([_P, _P, _P], C.c_int),
     "moc_set_negative_fluxes_allowed": ([_P, C.c_int], C.c_int),
+    "moc_set_keff_from_neutron_balance": ([_P, C.c_int], C.c_int),
+    "moc_set_transport_stabilization": ([_P, C.c_int, C.c_double, C.c_int], C.c_int),
+    "moc_compute_stabilizing_flux": ([_P], C.c_int),
+    "moc_stabilize_flux": ([_P], C.c_int),
+    "moc_compute_fsr_fission_sources": ([_P], C.c_int),
+    "moc_compute_fsr_scatter_sources": ([_P], C.c_int),
     "moc_set_otf_tracks": ([_P, C.POINTER(OtfTracks)], C.c_int),
     "moc_get_otf_tracks": ([_P, C.POINTER(C.c_int)], C.c_int),
     "moc_set_cmfd": ([_P, C.POINTER(CmfdMesh)], C.c_int),

@@ -13,6 +13,13 @@
  *   computeKeff            CPUSolver.cpp:2258  moc_compute_keff
  *   transportSweep         CPUSolver.cpp:2338  moc_transport_sweep
  *   addSourceToScalarFlux  CPUSolver.cpp:2608  moc_add_source_to_scalar_flux
+ *   computeStabilizingFlux CPUSolver.cpp:2665  moc_compute_stabilizing_flux
+ *   stabilizeFlux          CPUSolver.cpp:2736  moc_stabilize_flux
+ *   computeFSRFissionSources CPUSolver.cpp:2030 moc_compute_fsr_fission_sources
+ *   computeFSRScatterSources CPUSolver.cpp:2074 moc_compute_fsr_scatter_sources
+ * Solver::stabilizeTransport and setKeffFromNeutronBalance reach the device
+ * at initializeFluxArrays (moc_set_transport_stabilization,
+ * moc_set_keff_from_neutron_balance).
  * The host keeps no flux arrays: getFlux / getFluxes read the device.
  */
 #include "GB300Solver.h"
@@ -213,6 +220,12 @@ void GB300Solver::initializeFluxArrays() {
   upload();
   check(moc_set_negative_fluxes_allowed(_ctx, _negative_fluxes_allowed ? 1 : 0),
         "allowNegativeFluxes");
+  check(moc_set_keff_from_neutron_balance(_ctx, _keff_from_fission_rates ? 0 : 1),
+        "setKeffFromNeutronBalance");
+  check(moc_set_transport_stabilization(_ctx, _stabilize_transport ? 1 : 0,
+                                        _stabilization_factor,
+                                        (int) _stabilization_type),
+        "stabilizeTransport");
   check(moc_zero_track_fluxes(_ctx), "zeroTrackFluxes");
 }
 
@@ -264,11 +277,11 @@ double GB300Solver::normalizeFluxes() {
 }
 
 void GB300Solver::computeStabilizingFlux() {
-  log_printf(ERROR, "GB300Solver does not implement transport stabilization");
+  check(moc_compute_stabilizing_flux(_ctx), "computeStabilizingFlux");
 }
 
 void GB300Solver::stabilizeFlux() {
-  log_printf(ERROR, "GB300Solver does not implement transport stabilization");
+  check(moc_stabilize_flux(_ctx), "stabilizeFlux");
 }
 
 void GB300Solver::computeFSRSources(int iteration) {
@@ -277,13 +290,11 @@ void GB300Solver::computeFSRSources(int iteration) {
 }
 
 void GB300Solver::computeFSRFissionSources() {
-  log_printf(ERROR, "GB300Solver does not implement the fission-only source "
-             "(openmoc.krylov helper)");
+  check(moc_compute_fsr_fission_sources(_ctx), "computeFSRFissionSources");
 }
 
 void GB300Solver::computeFSRScatterSources() {
-  log_printf(ERROR, "GB300Solver does not implement the scatter-only source "
-             "(openmoc.krylov helper)");
+  check(moc_compute_fsr_scatter_sources(_ctx), "computeFSRScatterSources");
 }
 
 double GB300Solver::computeResidual(residualType res_type) {

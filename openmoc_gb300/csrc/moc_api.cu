@@ -172,6 +172,20 @@ struct moc_ctx {
   float* fixed_xy = nullptr;
   int64_t ls_num_flat = 0;
   int negative_ok = 0;       // Solver::allowNegativeFluxes
+  int keff_balance = 0;      // Solver::setKeffFromNeutronBalance
+  // transport stabilization (Solver::stabilizeTransport): type DIAGONAL 0,
+  // YAMAMOTO 1, GLOBAL 2; per material and group the pair (c1, c2), made
+  // from the host copies of sigma_t and the scattering diagonal and the
+  // materials the FSRs use; the flux saved by the computeStabilizingFlux
+  // hook
+  int stab_on = 0;
+  int stab_type = 0;
+  double stab_factor = 0.0;
+  bool stab_dirty = true;
+  float2* stab = nullptr;
+  float* stab_base = nullptr;
+  std::vector<float> h_sigma_t, h_scat_diag;
+  std::vector<uint8_t> h_mat_used;
   // On-the-fly 3D segmentation (moc_set_otf_tracks): 3D track descriptors,
   // per-angle cot / 1/cot / 1/sin, the radial segments, and the track order
   // by radial segments crossed
@@ -263,6 +277,57 @@ int64_t num_host_flux(const moc_ctx* c) {
   return c->d.num_fsrs * c->d.num_groups;
 }
 
+// keff from the neutron balance: the flat-source sweeps of stored
+// segments tally the leakage; CMFD supplies its own keff
+bool balance_keff(const moc_ctx* c) {
+  return c->keff_balance && !c->ls && !c->otf && !c->cmfd;
+}
+
+// The transport-stabilization coefficients (c1, c2) per material and group
+// (CPUSolver::computeStabilizingFlux / stabilizeFlux, src/CPUSolver.cpp:
+// 2665-2810), rebuilt after a material or FSR upload.
+int ensure_stab(moc_ctx* c) {
+  if (!c->stab_on || (!c->stab_dirty && c->stab)) return MOC_OK;
+  const int M = c->d.num_materials, G = c->d.num_groups, ld = row_stride(c);
+  MOC_CHECK((int) c->h_sigma_t.size() == M * G &&
+                (int) c->h_mat_used.size() == M,
+            MOC_ERR_STATE, "upload materials and FSRs before stabilizing");
+  const double f = c->stab_factor;
+  std::vector<float2> cf((size_t) M * ld, make_float2(0.0f, 1.0f));
+  if (c->stab_type == MOC_STABILIZE_YAMAMOTO) {
+    for (int g = 0; g < G; g++) {
+      float max_ratio = 0.0f;
+      for (int m = 0; m < M; m++) {
+        if (!c->h_mat_used[m]) continue;
+        const float ratio = std::abs(c->h_scat_diag[(int64_t) m * G + g] /
+                                     c->h_sigma_t[(int64_t) m * G + g]);
+        if (ratio > max_ratio) max_ratio = ratio;
+      }
+      const float mr = (float) (max_ratio * f);
+      for (int m = 0; m < M; m++)
+        cf[(int64_t) m * ld + g] = make_float2(mr, 1.0f / (1.0f + mr));
+    }
+  } else {
+    for (int m = 0; m < M; m++)
+      for (int g = 0; g < G; g++) {
+        const int64_t i = (int64_t) m * G + g;
+        if (c->stab_type == MOC_STABILIZE_GLOBAL) {
+          cf[(int64_t) m * ld + g] =
+              make_float2((float) (1.0 / f - 1.0), (float) f);
+        } else if (c->h_scat_diag[i] < 0.0f) {
+          const double r = f * c->h_scat_diag[i] / c->h_sigma_t[i];
+          cf[(int64_t) m * ld + g] =
+              make_float2((float) -r, (float) (1.0 / (1.0 - r)));
+        }
+      }
+  }
+  if (!c->stab) MOC_TRY(dalloc(&c->stab, (int64_t) M * ld));
+  MOC_CUDA(cudaMemcpy(c->stab, cf.data(), sizeof(float2) * cf.size(),
+                      cudaMemcpyHostToDevice));
+  c->stab_dirty = false;
+  return MOC_OK;
+}
+
 moc::SweepArgs sweep_args(moc_ctx* c, int check_done) {
   moc::SweepArgs a{};
   a.segs = c->segs;
@@ -302,6 +367,7 @@ moc::SweepArgs sweep_args(moc_ctx* c, int check_done) {
     a.cm_end = c->cm_end;
     a.cm_nx = c->cmfd->cfg.nx;
   }
+  if (balance_keff(c)) a.leakage = &c->sc->leakage;
   return a;
 }
 
@@ -348,6 +414,8 @@ moc::SolverArgs solver_args(moc_ctx* c, int check_done) {
   a.num_materials = c->d.num_materials;
   a.check_done = check_done;
   a.negative_ok = c->negative_ok;
+  a.keff_balance = balance_keff(c) ? 1 : 0;
+  a.stab = c->stab_on ? c->stab : nullptr;
   if (c->ls) {
     a.mom = c->mom;
     a.qxy = c->qxy;
@@ -634,6 +702,8 @@ int begin_solve(moc_ctx* c, int mode, int max_iters, int res_type,
   s.neg_fluxes = 0;
   s.num_fissionable = c->num_fissionable;
   s.tc_error = 0;
+  s.accum_abs = 0.0;
+  s.leakage = 0.0;
   MOC_TRY(push(c));
   c->sweep_ms = 0.0;
   c->num_sweeps = 0;
@@ -653,6 +723,7 @@ int zero_track_fluxes(moc_ctx* c) {
 
 // The device loop: iterations of `kind` until the device reports done.
 int run_iterations(moc_ctx* c, int kind, int res_type) {
+  MOC_TRY(ensure_stab(c));
   moc::SolverArgs a = solver_args(c, 1);
   int completed = 0;
   for (;;) {
@@ -664,7 +735,14 @@ int run_iterations(moc_ctx* c, int kind, int res_type) {
         enqueue_sources(c, a, -1, 1);
       }
       MOC_TRY(enqueue_sweep(c, 1, true, i));
-      enqueue_add_source(c, a, kind == moc::kModeEigen ? 1 : 0);
+      if (kind == moc::kModeEigen && c->stab_on) {
+        // keff first; the stabilized flux sets the normalisation
+        enqueue_add_source(c, a, 2);
+        moc::launch_stabilize(a, c->phi_old, 1, c->stream);
+        c->launches++;
+      } else {
+        enqueue_add_source(c, a, kind == moc::kModeEigen ? 1 : 0);
+      }
       moc::launch_residual(a, res_type, kind == moc::kModeEigen ? 1 : 0, 1, 1,
                            c->stream);
       c->launches++;
@@ -1214,6 +1292,8 @@ int moc_destroy(moc_ctx* c) {
   dfree(c->tc_rows);
   dfree(c->tc_tile_mat);
   dfree(c->tc_b);
+  dfree(c->stab);
+  dfree(c->stab_base);
   dfree(c->segs_ls);
   dfree(c->ls_ang);
   dfree(c->ls_dir);
@@ -1406,6 +1486,13 @@ int moc_upload_materials(moc_ctx* c, const float* sigma_t,
         ssT[((int64_t) m * G + g) * G + gd] = v;
       }
   }
+  c->h_sigma_t.assign(sigma_t, sigma_t + MG);
+  c->h_scat_diag.resize(MG);
+  for (int m = 0; m < M; m++)
+    for (int g = 0; g < G; g++)
+      c->h_scat_diag[(int64_t) m * G + g] =
+          sigma_s[((int64_t) m * G + g) * G + g];
+  c->stab_dirty = true;
   MOC_CUDA(cudaSetDevice(c->d.device));
   dfree(c->sigma_t);
   dfree(c->sigma_s);
@@ -1474,6 +1561,9 @@ int moc_upload_fsrs(moc_ctx* c, const int32_t* fsr_mat, const float* fsr_vol) {
   MOC_TRY(dalloc(&c->fsr_vol, R));
   MOC_CUDA(cudaMemcpy(c->fsr_mat, fsr_mat, 4 * R, cudaMemcpyHostToDevice));
   MOC_CUDA(cudaMemcpy(c->fsr_vol, fsr_vol, 4 * R, cudaMemcpyHostToDevice));
+  c->h_mat_used.assign(c->d.num_materials, 0);
+  for (int64_t r = 0; r < R; r++) c->h_mat_used[fsr_mat[r]] = 1;
+  c->stab_dirty = true;
   count_fissionable(c, fsr_mat);
   // tensor-core source tiles: FSR ids grouped by material, each material's
   // list padded to whole tiles with -1
@@ -2045,6 +2135,8 @@ int moc_compute_fsr_sources(moc_ctx* c, int iteration) {
 int moc_transport_sweep(moc_ctx* c) {
   MOC_TRY(ready(c));
   MOC_CUDA(cudaMemsetAsync(c->phi, 0, 4 * num_flux(c), c->stream));
+  // the leakage tally starts afresh with every sweep (src/CPUSolver.cpp:2360)
+  MOC_CUDA(cudaMemsetAsync(&c->sc->leakage, 0, sizeof(double), c->stream));
   MOC_TRY(zero_moments(c));
   MOC_TRY(enqueue_sweep(c, 0, true, 0));
   MOC_CUDA(cudaStreamSynchronize(c->stream));
@@ -2121,6 +2213,10 @@ int moc_set_linear_source(moc_ctx* c, const moc_ls_geometry* g) {
   }
   MOC_CHECK(!c->d.solve_3d, MOC_ERR_UNSUPPORTED,
             "the linear source takes 2D tracks");
+  MOC_CHECK(!c->keff_balance, MOC_ERR_UNSUPPORTED,
+            "keff from the neutron balance is built for the flat source");
+  MOC_CHECK(!c->stab_on, MOC_ERR_UNSUPPORTED,
+            "transport stabilization is built for the flat source");
   MOC_CHECK(c->d.num_polar_half >= 1 && c->d.num_polar_half <= 3,
             MOC_ERR_UNSUPPORTED,
             "the linear-source sweep takes 1 to 3 polar angles per half space");
@@ -2232,6 +2328,83 @@ int moc_get_linear_source(moc_ctx* c, int* enabled, int64_t* num_flat) {
 int moc_set_negative_fluxes_allowed(moc_ctx* c, int allowed) {
   MOC_CHECK(c, MOC_ERR_ARG, "null context");
   c->negative_ok = allowed ? 1 : 0;
+  return MOC_OK;
+}
+
+int moc_set_transport_stabilization(moc_ctx* c, int on, double factor,
+                                    int type) {
+  MOC_CHECK(c, MOC_ERR_ARG, "null context");
+  if (!on) {
+    c->stab_on = 0;
+    return MOC_OK;
+  }
+  MOC_CHECK(std::isfinite(factor) && factor > 0.0, MOC_ERR_ARG,
+            "the stabilization factor must be positive");
+  MOC_CHECK(type == MOC_STABILIZE_DIAGONAL || type == MOC_STABILIZE_YAMAMOTO ||
+                type == MOC_STABILIZE_GLOBAL,
+            MOC_ERR_ARG, "unknown stabilization type");
+  MOC_CHECK(!c->ls, MOC_ERR_UNSUPPORTED,
+            "transport stabilization is built for the flat source");
+  if (c->stab && c->d.num_materials > 0) {
+    // the coefficients depend on the factor and type
+    dfree(c->stab);
+    c->stab = nullptr;
+  }
+  c->stab_on = 1;
+  c->stab_factor = factor;
+  c->stab_type = type;
+  c->stab_dirty = true;
+  return MOC_OK;
+}
+
+int moc_compute_stabilizing_flux(moc_ctx* c) {
+  MOC_TRY(ready(c));
+  MOC_CHECK(c->stab_on, MOC_ERR_STATE, "transport stabilization is off");
+  MOC_TRY(ensure_stab(c));
+  if (!c->stab_base) MOC_TRY(dalloc(&c->stab_base, num_flux(c)));
+  MOC_CUDA(cudaMemcpyAsync(c->stab_base, c->phi, 4 * num_flux(c),
+                           cudaMemcpyDeviceToDevice, c->stream));
+  return MOC_OK;
+}
+
+int moc_stabilize_flux(moc_ctx* c) {
+  MOC_TRY(ready(c));
+  MOC_CHECK(c->stab_on, MOC_ERR_STATE, "transport stabilization is off");
+  MOC_CHECK(c->stab_base, MOC_ERR_STATE,
+            "computeStabilizingFlux must come before stabilizeFlux");
+  MOC_TRY(ensure_stab(c));
+  moc::SolverArgs a = solver_args(c, 0);
+  moc::launch_stabilize(a, c->stab_base, 0, c->stream);
+  c->launches++;
+  MOC_CUDA(cudaGetLastError());
+  return MOC_OK;
+}
+
+int moc_compute_fsr_fission_sources(moc_ctx* c) {
+  MOC_TRY(ready(c));
+  moc::SolverArgs a = solver_args(c, 0);
+  moc::launch_partial_sources(a, 0, c->stream);
+  c->launches++;
+  MOC_CUDA(cudaGetLastError());
+  return MOC_OK;
+}
+
+int moc_compute_fsr_scatter_sources(moc_ctx* c) {
+  MOC_TRY(ready(c));
+  moc::SolverArgs a = solver_args(c, 0);
+  moc::launch_partial_sources(a, 1, c->stream);
+  c->launches++;
+  MOC_CUDA(cudaGetLastError());
+  return MOC_OK;
+}
+
+int moc_set_keff_from_neutron_balance(moc_ctx* c, int on) {
+  MOC_CHECK(c, MOC_ERR_ARG, "null context");
+  MOC_CHECK(!on || (!c->ls && !c->otf), MOC_ERR_UNSUPPORTED,
+            "keff from the neutron balance is built for the flat-source sweep "
+            "of stored segments (not the linear source or on-the-fly 3D "
+            "segments)");
+  c->keff_balance = on ? 1 : 0;
   return MOC_OK;
 }
 
@@ -2348,6 +2521,8 @@ int moc_set_otf_tracks(moc_ctx* c, const moc_otf_tracks* d) {
             "on-the-fly segmentation takes 3D tracks");
   MOC_CHECK(!c->ls, MOC_ERR_UNSUPPORTED,
             "on-the-fly segmentation and the linear source do not combine");
+  MOC_CHECK(!c->keff_balance, MOC_ERR_UNSUPPORTED,
+            "keff from the neutron balance is built for stored segments");
   MOC_CHECK(c->d.num_fsrs < (1LL << 24) && c->d.num_materials <= 256,
             MOC_ERR_UNSUPPORTED,
             "on-the-fly segmentation needs fewer than 2^24 FSRs and at most "

@@ -53,6 +53,11 @@ struct DevScalars {
   long long row0;
   long long nrows;
   int tc_error;           // a tensor-core source launch gave up waiting
+  // keff from the neutron balance (Solver::setKeffFromNeutronBalance):
+  // absorption-rate accumulator and the leakage the last sweep tallied at
+  // vacuum track ends
+  double accum_abs;
+  double leakage;
 };
 
 enum SolveMode { kModeEigen = 0, kModeSource = 1, kModeFlux = 2, kModeHook = 3 };
@@ -110,6 +115,8 @@ struct SweepArgs {
   float* cm_cur;             // [cells][4][ld]
   const int8_t* cm_end;      // [T][2]
   int cm_nx;
+  // keff from the neutron balance: the leakage tally (null: not tallied)
+  double* leakage;
 };
 
 constexpr int kMaxHotFsrs = 8;
@@ -166,6 +173,13 @@ struct SolverArgs {
   const float* ls_const;     // [R][3][ld]
   const float* fixed_xy;
   int negative_ok;           // Solver::allowNegativeFluxes
+  // keff = fission / (absorption + leakage) instead of keff *= fission / R
+  // (Solver::setKeffFromNeutronBalance); absorption = sigma_t - scat_out
+  int keff_balance;
+  // transport stabilization (null: off): per material and group the pair
+  // (c1, c2) of phi = (phi + c1 * phi_start) * c2, phi_start the flux at
+  // the start of the iteration
+  const float2* stab;        // [M][ld]
 };
 
 // Rows (FSRs) per tile of the tensor-core source kernel: the MMA's M.
@@ -202,7 +216,8 @@ void launch_pack_segments(const float* len, const int32_t* fsr, int2* out,
 void launch_compute_sources(const SolverArgs& a, int iteration, int fused,
                             cudaStream_t s);
 // add-source + fission-rate reduction; update: 0 none, 1 eigen update of
-// keff / factor / buffer scale
+// keff / factor / buffer scale, 2 keff only (the factor follows the
+// stabilization)
 void launch_add_source(const SolverArgs& a, int update, cudaStream_t s);
 // normalise by sc->factor (if normalise), residual of res_type vs phi_old,
 // store phi into phi_old (if store), finish the iteration (if finish)
@@ -210,6 +225,16 @@ void launch_residual(const SolverArgs& a, int res_type, int normalise,
                      int store, int finish, cudaStream_t s);
 // fission-rate reduction of phi; what: 0 keff update, 1 normalise hook
 void launch_fission_rate(const SolverArgs& a, int what, cudaStream_t s);
+// transport stabilization of phi from `base` (the flux at the start of the
+// iteration); in_loop: only from the second iteration on, and the
+// normalisation factor of the stabilized flux is computed as
+// launch_fission_rate(what = 1) does
+void launch_stabilize(const SolverArgs& a, const float* base, int in_loop,
+                      cudaStream_t s);
+// the fission (which = 0) or scattering (which = 1) part of the reduced
+// source alone into qt (CPUSolver::computeFSRFissionSources /
+// computeFSRScatterSources)
+void launch_partial_sources(const SolverArgs& a, int which, cudaStream_t s);
 void launch_scale_phi(const SolverArgs& a, cudaStream_t s);
 void launch_zero_phi(const SolverArgs& a, cudaStream_t s);
 void launch_fill(float* p, int64_t n, float v, cudaStream_t s);

@@ -136,7 +136,7 @@ otf_sweep_kernel(const SweepArgs a, const OtfArgs o) {
         if (sub + s * LPS < npairs) {
           const float2 tau = __fmul2_rn(st[s * LPS], len2);
           const float2 gx =
-              AttenIntrinsic::eval2(__fmul2_rn(tau, xl2), tau, nullptr);
+              AttenIntrinsic::eval2(__fmul2_rn(tau, xl2));
           const float2 d =
               __fmul2_rn(__ffma2_rn(qv[s], f2(-1.0f), psi[s]), gx);
           psi[s] = __ffma2_rn(d, f2(-1.0f), psi[s]);

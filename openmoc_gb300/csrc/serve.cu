@@ -33,6 +33,9 @@
 
 namespace {
 
+// Group pairs per lane for G groups over lps lanes.
+int pairs_for(int G, int lps) { return ((G + 1) / 2 + lps - 1) / lps; }
+
 #define SV_FAIL(code, msg) moc::set_error(code, std::string(msg).c_str())
 
 #define SV_CHECK(cond, code, msg)          \
@@ -929,8 +932,6 @@ int rebuild_order(Pool& p) {
   return MOC_OK;
 }
 
-// Group pairs per lane for G groups over lps lanes.
-int pairs_for(int G, int lps) { return ((G + 1) / 2 + lps - 1) / lps; }
 
 // Times every sweep shape with at most kMaxSlots pairs per lane and at
 // least half of its lanes busy on the pool's current solves (the faster of

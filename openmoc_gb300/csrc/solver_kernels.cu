@@ -63,6 +63,44 @@ __device__ bool block_accumulate(double v, double* accum,
   return last && threadIdx.x == 0;
 }
 
+// block_accumulate for two sums sharing one ticket
+__device__ bool block_accumulate2(double v, double w, double* accum_v,
+                                  double* accum_w, unsigned int* ticket) {
+  __shared__ double part[2][32];
+  __shared__ int last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    part[0][warp] = v;
+    part[1][warp] = w;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0, t = 0.0;
+    for (int i = 0; i < (int) (blockDim.x >> 5); i++) {
+      s += part[0][i];
+      t += part[1][i];
+    }
+    atomicAdd(accum_v, s);
+    atomicAdd(accum_w, t);
+    __threadfence();
+    unsigned int k = atomicAdd(ticket, 1u);
+    last = (k == gridDim.x - 1);
+  }
+  __syncthreads();
+  return last && threadIdx.x == 0;
+}
+
+// keff from the neutron balance, fission / (absorption + leakage)
+// (CPUSolver::computeKeff, src/CPUSolver.cpp:2258-2330), by the last block
+// of a reduction that accumulated the absorption rate; the leakage is the
+// last sweep's tally
+__device__ void finish_balance_keff(DevScalars* sc, double fission) {
+  const double absorption = *(volatile double*) &sc->accum_abs;
+  const double leakage = *(volatile double*) &sc->leakage;
+  sc->keff = fission / (absorption + leakage);
+  sc->accum_abs = 0.0;
+}
+
 __device__ __forceinline__ bool skip(const SolverArgs& a) {
   return a.check_done && *(volatile int*) &a.sc->done;
 }
@@ -236,13 +274,15 @@ add_source_kernel(const SolverArgs a, int update) {
   if (skip(a)) return;
   const int G = a.num_groups;
   const int lane = threadIdx.x & 31;
-  double rate = 0.0;
+  double rate = 0.0, arate = 0.0;
   unsigned long long negatives = 0;
+  const bool balance = update && a.keff_balance;
   for (int64_t r = first_row(); r < a.num_fsrs; r += row_step()) {
     const int m = a.fsr_mat[r];
     const float vol0 = a.fsr_vol[r];
     const float vol = (vol0 < 1.0e-12f) ? 1.0e30f : vol0;
     const float* __restrict__ st = a.sigma_t + (int64_t) m * G;
+    const float* __restrict__ so = a.scat_out + (int64_t) m * G;
     const float* __restrict__ nf = a.nu_sigma_f + (int64_t) m * G;
     float* __restrict__ phi = a.phi + r * a.ld;
     const float* __restrict__ qt = a.qt + r * a.ld;
@@ -253,12 +293,13 @@ add_source_kernel(const SolverArgs a, int update) {
       v[j] = (g < G) ? phi[g] : 0.0f;
       q[j] = (g < G) ? qt[g] : 0.0f;
     }
-    float rr = 0.0f;
+    float rr = 0.0f, ra = 0.0f;
 #pragma unroll
     for (int j = 0; j < S; j++) {
       const int g = lane + 32 * j;
       if (g >= G) continue;
-      float x = v[j] / (st[g] * vol);
+      const float stg = st[g];
+      float x = v[j] / (stg * vol);
       x += (float) kFourPi * q[j];
       if (x < 0.0f && !a.negative_ok) {
         x = kFluxEpsilon;
@@ -266,17 +307,37 @@ add_source_kernel(const SolverArgs a, int update) {
       }
       phi[g] = x;
       rr = fmaf(nf[g], x, rr);
+      if (balance) ra = fmaf(stg - so[g], x, ra);
     }
     if (update) rate += (double) rr * (double) vol0;
+    if (balance) arate += (double) ra * (double) vol0;
   }
   if (negatives) atomicAdd(&a.sc->neg_fluxes, negatives);
   if (!update) return;
   rate = warp_sum_all_d(rate);
   DevScalars* sc = a.sc;
-  if (block_accumulate(rate, &sc->accum_rate, &sc->ticket_rate)) {
+  bool last;
+  if (balance)
+    last = block_accumulate2(rate, warp_sum_all_d(arate), &sc->accum_rate,
+                             &sc->accum_abs, &sc->ticket_rate);
+  else
+    last = block_accumulate(rate, &sc->accum_rate, &sc->ticket_rate);
+  if (last) {
     const double total = *(volatile double*) &sc->accum_rate;
     const double R = (double) a.num_fsrs;
-    sc->keff = sc->keff * (total / R);
+    if (balance) {
+      finish_balance_keff(sc, total);
+      sc->leakage = 0.0;   // the next sweep tallies afresh
+    } else {
+      sc->keff = sc->keff * (total / R);
+    }
+    if (update == 2) {
+      // the normalisation factor comes from the stabilized flux
+      sc->accum_rate = 0.0;
+      sc->ticket_rate = 0;
+      __threadfence();
+      return;
+    }
     sc->factor = R / total;
     sc->scale[sc->cur] *= (float) sc->factor;
     sc->accum_rate = 0.0;
@@ -405,20 +466,36 @@ fission_rate_kernel(const SolverArgs a, int what) {
   if (skip(a)) return;
   const int G = a.num_groups;
   const int lane = threadIdx.x & 31;
-  double rate = 0.0;
+  const bool balance = what == 0 && a.keff_balance;
+  double rate = 0.0, arate = 0.0;
   for (int64_t r = first_row(); r < a.num_fsrs; r += row_step()) {
-    const float* nf = a.nu_sigma_f + (int64_t) a.fsr_mat[r] * G;
+    const int m = a.fsr_mat[r];
+    const float* nf = a.nu_sigma_f + (int64_t) m * G;
+    const float* st = a.sigma_t + (int64_t) m * G;
+    const float* so = a.scat_out + (int64_t) m * G;
     const float* phi = a.phi + r * a.ld;
-    double s = 0.0;
-    for (int g = lane; g < G; g += 32) s += (double) (nf[g] * phi[g]);
+    double s = 0.0, t = 0.0;
+    for (int g = lane; g < G; g += 32) {
+      s += (double) (nf[g] * phi[g]);
+      if (balance) t += (double) ((st[g] - so[g]) * phi[g]);
+    }
     rate += s * (double) a.fsr_vol[r];
+    arate += t * (double) a.fsr_vol[r];
   }
   rate = warp_sum_all_d(rate);
   DevScalars* sc = a.sc;
-  if (block_accumulate(rate, &sc->accum_rate, &sc->ticket_rate)) {
+  bool last;
+  if (balance)
+    last = block_accumulate2(rate, warp_sum_all_d(arate), &sc->accum_rate,
+                             &sc->accum_abs, &sc->ticket_rate);
+  else
+    last = block_accumulate(rate, &sc->accum_rate, &sc->ticket_rate);
+  if (last) {
     const double total = *(volatile double*) &sc->accum_rate;
     const double R = (double) a.num_fsrs;
-    if (what == 0) {
+    if (balance) {
+      finish_balance_keff(sc, total);
+    } else if (what == 0) {
       sc->keff = sc->keff * (total / R);
     } else {
       sc->factor = R / total;
@@ -427,6 +504,90 @@ fission_rate_kernel(const SolverArgs a, int what) {
     sc->accum_rate = 0.0;
     sc->ticket_rate = 0;
     __threadfence();
+  }
+}
+
+// -------------------------------------------------- transport stabilization
+// CPUSolver::computeStabilizingFlux + stabilizeFlux (src/CPUSolver.cpp:
+// 2665-2810) in one pass: the stabilizing flux is c1 times the flux at the
+// start of the iteration (`base`), added to the new flux, the sum scaled by
+// c2; per material and group (DIAGONAL: c1 = -f sigma_s,gg / sigma_t,g,
+// c2 = 1 / (1 + c1) where sigma_s,gg < 0, else 0 and 1; YAMAMOTO: the
+// group's largest |sigma_s,gg / sigma_t,g| over the FSRs' materials times f,
+// c2 = 1 / (1 + c1); GLOBAL: c1 = 1 / f - 1, c2 = f).  In the eigenvalue
+// loop (in_loop) it applies from the second iteration on and then computes
+// the normalisation factor of the stabilized flux (normalizeFluxes follows
+// stabilizeFlux, src/Solver.cpp:1632-1640).
+__global__ void __launch_bounds__(kRowThreads)
+stabilize_kernel(const SolverArgs a, const float* base, int in_loop) {
+  if (skip(a)) return;
+  DevScalars* sc = a.sc;
+  const int G = a.num_groups;
+  const int lane = threadIdx.x & 31;
+  const bool apply = !in_loop || sc->iteration > 0;
+  double rate = 0.0;
+  for (int64_t r = first_row(); r < a.num_fsrs; r += row_step()) {
+    const int m = a.fsr_mat[r];
+    const float2* cf = a.stab + (int64_t) m * a.ld;
+    const float* nf = a.nu_sigma_f + (int64_t) m * G;
+    float* phi = a.phi + r * a.ld;
+    const float* b = base + r * a.ld;
+    double s = 0.0;
+    for (int g = lane; g < G; g += 32) {
+      float x = phi[g];
+      if (apply) {
+        const float2 c = cf[g];
+        x = (x + c.x * b[g]) * c.y;
+        phi[g] = x;
+      }
+      s += (double) (nf[g] * x);
+    }
+    rate += s * (double) a.fsr_vol[r];
+  }
+  if (!in_loop) return;
+  rate = warp_sum_all_d(rate);
+  if (block_accumulate(rate, &sc->accum_rate, &sc->ticket_rate)) {
+    const double total = *(volatile double*) &sc->accum_rate;
+    sc->factor = (double) a.num_fsrs / total;
+    sc->scale[sc->cur] *= (float) sc->factor;
+    sc->accum_rate = 0.0;
+    sc->ticket_rate = 0;
+    __threadfence();
+  }
+}
+
+// --------------------------------------------- fission / scatter sources
+// CPUSolver::computeFSRFissionSources / computeFSRScatterSources
+// (src/CPUSolver.cpp:2030-2110): one part of the reduced source alone,
+// sum over g' of M[g][g'] phi[g'] / (4 pi), M the fission matrix
+// chi[g] nu_sigma_f[g'] (which = 0) or the scattering matrix (which = 1);
+// no 1 / keff, fixed source or clamping.  Stored divided by sigma_t like
+// every reduced source on the device.
+__global__ void __launch_bounds__(kRowThreads)
+partial_sources_kernel(const SolverArgs a, int which) {
+  const int G = a.num_groups;
+  const int lane = threadIdx.x & 31;
+  for (int64_t r = first_row(); r < a.num_fsrs; r += row_step()) {
+    const int m = a.fsr_mat[r];
+    const float* phi = a.phi + r * a.ld;
+    const float* st = a.sigma_t + (int64_t) m * G;
+    float* qt = a.qt + r * a.ld;
+    double fis = 0.0;
+    if (which == 0 && a.fissile[m]) {
+      const float* nf = a.nu_sigma_f + (int64_t) m * G;
+      for (int g = lane; g < G; g += 32) fis += (double) (nf[g] * phi[g]);
+      fis = warp_sum_all_d(fis);
+    }
+    for (int gd = lane; gd < G; gd += 32) {
+      double q = 0.0;
+      if (which == 0) {
+        q = (double) a.chi[(int64_t) m * G + gd] * fis;
+      } else {
+        const float* row = a.sigma_s + ((int64_t) m * G + gd) * G;
+        for (int g = 0; g < G; g++) q += (double) (row[g] * phi[g]);
+      }
+      qt[gd] = (float) (q * kOneOverFourPi) / st[gd];
+    }
   }
 }
 
@@ -629,13 +790,15 @@ ls_add_source_kernel(const SolverArgs a, int update) {
   const int G = a.num_groups;
   const int ld = a.ld;
   const int lane = threadIdx.x & 31;
-  double rate = 0.0;
+  double rate = 0.0, arate = 0.0;
   unsigned long long negatives = 0;
+  const bool balance = update && a.keff_balance;
   for (int64_t r = first_row(); r < a.num_fsrs; r += row_step()) {
     const int m = a.fsr_mat[r];
     const float vol0 = a.fsr_vol[r];
     const float vol = (vol0 < 1.0e-12f) ? 1.0e30f : vol0;
     const float* __restrict__ st = a.sigma_t + (int64_t) m * G;
+    const float* __restrict__ so = a.scat_out + (int64_t) m * G;
     const float* __restrict__ nf = a.nu_sigma_f + (int64_t) m * G;
     float* __restrict__ phi = a.phi + r * ld;
     const float* __restrict__ qt = a.qt + r * ld;
@@ -1063,6 +1226,17 @@ void launch_residual(const SolverArgs& a, int res_type, int normalise,
 
 void launch_fission_rate(const SolverArgs& a, int what, cudaStream_t s) {
   fission_rate_kernel<<<row_grid(a.num_fsrs), kRowThreads, 0, s>>>(a, what);
+}
+
+void launch_stabilize(const SolverArgs& a, const float* base, int in_loop,
+                      cudaStream_t s) {
+  stabilize_kernel<<<row_grid(a.num_fsrs), kRowThreads, 0, s>>>(a, base,
+                                                               in_loop);
+}
+
+void launch_partial_sources(const SolverArgs& a, int which, cudaStream_t s) {
+  partial_sources_kernel<<<row_grid(a.num_fsrs), kRowThreads, 0, s>>>(a,
+                                                                     which);
 }
 
 void launch_scale_phi(const SolverArgs& a, cudaStream_t s) {

@@ -54,9 +54,8 @@ struct AttenTable {
     const float2 ge = tab[i];
     return fmaf(ge.y, q, ge.x);
   }
-  // two groups; x2 already scaled by 1/h
-  __device__ __forceinline__ static float2 eval2(float2 u2, float2 /*x2*/,
-                                                 const float2* tab) {
+  // two groups; u2 = x / h
+  __device__ __forceinline__ static float2 eval2(float2 u2, const float2* tab) {
     return make_float2(eval(u2.x, tab), eval(u2.y, tab));
   }
 };
@@ -74,23 +73,30 @@ struct AttenTable {
 // hardware error, so both branches overestimate and the min is the closer
 // one; the bias vanishes with e for optically thick segments.  The relative
 // error is below ~2e-6 for every x (largest near the crossover x ~ 0.26).
+// Both branches take the exponent u = -x log2(e) that ex2 needs: with
+// x = -u ln 2, T5 is the polynomial u (b1 + u (b2 + ... + u b5)),
+// b_i = -(ln 2)^i / i!, so x itself is never formed.
 struct AttenIntrinsic {
   static constexpr float kRel = 5.0e-7f;
+  static constexpr float b1 = -0.6931471805599453f;
+  static constexpr float b2 = -0.2402265069591007f;
+  static constexpr float b3 = -0.05550410866482158f;
+  static constexpr float b4 = -0.009618129107628477f;
+  static constexpr float b5 = -0.0013333558146428443f;
   __device__ __forceinline__ static float ex2(float v) {
     float r;
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v));
     return r;
   }
-  // u2 = -x * log2(e), x2 = x, for two groups
-  __device__ __forceinline__ static float2 eval2(float2 u2, float2 x2,
-                                                 const float2*) {
+  // u2 = -x * log2(e) for two groups
+  __device__ __forceinline__ static float2 eval2(float2 u2) {
     const float2 e = make_float2(ex2(u2.x), ex2(u2.y));
     const float2 big = __ffma2_rn(e, f2(kRel - 1.0f), f2(1.0f));
-    float2 s = __ffma2_rn(x2, f2(1.0f / 120.0f), f2(-1.0f / 24.0f));
-    s = __ffma2_rn(x2, s, f2(1.0f / 6.0f));
-    s = __ffma2_rn(x2, s, f2(-0.5f));
-    s = __ffma2_rn(x2, s, f2(1.0f));
-    s = __fmul2_rn(x2, s);
+    float2 s = __ffma2_rn(u2, f2(b5), f2(b4));
+    s = __ffma2_rn(u2, s, f2(b3));
+    s = __ffma2_rn(u2, s, f2(b2));
+    s = __ffma2_rn(u2, s, f2(b1));
+    s = __fmul2_rn(u2, s);
     return make_float2(fminf(s.x, big.x), fminf(s.y, big.y));
   }
 };
@@ -124,12 +130,14 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-// Registers available per thread: the busy instances keep 6 blocks of 128
+// Registers available per thread: the busy instances keep 5 blocks of 128
 // threads resident per SM (4 at 18 pair-polar values per lane), the small
 // ones 8; one-polar (3D) instances with 3 or more pairs, whose shared-memory
-// tallies need a few registers more, 6.
+// tallies need a few registers more, 6.  Measured on 17 x 17 / 70 groups
+// (8 lanes x 5 pairs, ex2, loop unrolled by 4): 5 blocks 485 us per sweep,
+// 6 blocks 513 us, 4 blocks 510 us.
 #ifndef MOC_SWEEP_BIG_MIN_BLOCKS
-#define MOC_SWEEP_BIG_MIN_BLOCKS 6
+#define MOC_SWEEP_BIG_MIN_BLOCKS 5
 #endif
 template <int PH, int PS>
 struct SweepOccupancy {
@@ -237,6 +245,8 @@ sweep_kernel(const SweepArgs a) {
       ((int64_t) blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t stream = gwarp * (32 / LPS) + lane / LPS;
   const int npairs = ld >> 1;
+  // pair s of this lane holds groups (the last lanes may have none)
+  auto live_pair = [&](int s) { return sub + s * LPS < npairs; };
 
   // the track and its pending scale; in a pool the solve of the track may
   // be finished (the LPS lanes of a stream share the track, so they agree
@@ -262,17 +272,17 @@ sweep_kernel(const SweepArgs a) {
     const int ang = a.track_ang[t];
     const int F = G * PH;
 
+    // the exponent scale of each polar angle: x / h for the table, -x log2 e
+    // for the hardware exponential
     float2 w2[PH], xs2[PH], xl2[PH];
 #pragma unroll
     for (int p = 0; p < PH; p++) {
       w2[p] = f2(a.weights[ang * PH + p]);
       const float is = a.inv_sin[ang * PH + p];
-      if (EXPK == kExpTable) {
+      if (EXPK == kExpTable)
         xs2[p] = f2(is * kExpTableInvH);
-      } else {
-        xs2[p] = f2(is);
+      else
         xl2[p] = f2(is * -1.4426950408889634f);
-      }
     }
 
     // angular flux of this lane's groups: pair s holds groups
@@ -344,7 +354,7 @@ sweep_kernel(const SweepArgs a) {
         const float2* src = qbase + (int64_t) f * npairs;
 #pragma unroll
         for (int s = 0; s < PS; s++)
-          if (sub + s * LPS < npairs) cp_async8(slot(j, s), src + s * LPS);
+          if (live_pair(s)) cp_async8(slot(j, s), src + s * LPS);
       }
       cp_async_commit();
     };
@@ -360,8 +370,7 @@ sweep_kernel(const SweepArgs a) {
       const float2* qrow = qbase + (int64_t) f * npairs;
 #pragma unroll
       for (int s = 0; s < PS; s++)
-        qq[s] = (sub + s * LPS < npairs && valid) ? __ldg(qrow + s * LPS)
-                                                  : f2(0.0f);
+        qq[s] = (live_pair(s) && valid) ? __ldg(qrow + s * LPS) : f2(0.0f);
     };
     float len = 0.0f;
     int fsr = 0, mat = 0;
@@ -377,6 +386,9 @@ sweep_kernel(const SweepArgs a) {
       unpack(word_cur(0), len, fsr, mat);
       gather(q, fsr, n > 0);
     }
+    // the staged loop unrolled by the ring's depth (4): the ring slots of
+    // the four copies are compile-time offsets
+#pragma unroll(kStaged ? 4 : 1)
     for (int k = 0; k < n; k++) {
       float len_n = 0.0f;
       int fsr_n = 0, mat_n = 0;
@@ -410,18 +422,17 @@ sweep_kernel(const SweepArgs a) {
       const float2 len2 = f2(len);
 #pragma unroll
       for (int s = 0; s < PS; s++) {
-        if (sub + s * LPS < npairs) {
+        if (live_pair(s)) {
           const float2 qs = kStaged ? *slot(k, s) : q[s];
           const float2 tau = __fmul2_rn(st[s * LPS], len2);
           float2 tally = f2(0.0f);
 #pragma unroll
           for (int p = 0; p < PH; p++) {
-            const float2 x2 = __fmul2_rn(tau, xs2[p]);
             float2 gx;
             if (EXPK == kExpTable)
-              gx = AttenTable::eval2(x2, x2, s_tab);
+              gx = AttenTable::eval2(__fmul2_rn(tau, xs2[p]), s_tab);
             else
-              gx = AttenIntrinsic::eval2(__fmul2_rn(tau, xl2[p]), x2, s_tab);
+              gx = AttenIntrinsic::eval2(__fmul2_rn(tau, xl2[p]));
             // d = (psi - q) * g;  psi -= d;  tally += w * d
             const float2 d =
                 __fmul2_rn(__ffma2_rn(qs, f2(-1.0f), psi[s][p]), gx);
@@ -463,8 +474,30 @@ sweep_kernel(const SweepArgs a) {
     }
 
     // boundary-flux transfer to the connecting track, fused into the sweep
-    // (CPUSolver::transferBoundaryFlux, src/CPUSolver.cpp:2560-2600)
+    // (CPUSolver::transferBoundaryFlux, src/CPUSolver.cpp:2560-2600); at a
+    // vacuum end, when keff comes from the neutron balance, the leakage:
+    // the outgoing angular flux of every polar value and group weighted by
+    // the quadrature weight of the track's polar index, which is 0 for 2D
+    // tracks (src/CPUSolver.cpp:2593-2600, src/TrackTraversingAlgorithms.cpp
+    // :895-905), summed over the stream's lanes, one FP64 atomic per stream
     const int f = a.flags[t];
+    if (!(f & (dir ? 8 : 4)) && a.leakage) {
+      float2 acc = f2(0.0f);
+#pragma unroll
+      for (int s = 0; s < PS; s++) {
+        const int g0 = 2 * (sub + s * LPS);
+#pragma unroll
+        for (int p = 0; p < PH; p++) {
+          if (g0 < G) acc.x += psi[s][p].x;
+          if (g0 + 1 < G) acc.y += psi[s][p].y;
+        }
+      }
+      float v = (acc.x + acc.y) * w2[0].x;
+#pragma unroll
+      for (int o = LPS / 2; o > 0; o >>= 1)
+        v += __shfl_xor_sync(gmask, v, o, LPS);
+      if (sub == 0) atomicAdd(a.leakage, (double) v);
+    }
     if (f & (dir ? 8 : 4)) {
       const int nt = a.next[2 * t + dir];
       const int nd = (f & (dir ? 2 : 1)) ? 0 : 1;

@@ -21,10 +21,9 @@ __global__ void attenuation_kernel(int kind, const float* x, float* g,
     const float2 x2 = make_float2(x[i], (i + 1 < n) ? x[i + 1] : 0.0f);
     float2 r;
     if (kind == kExpTable)
-      r = AttenTable::eval2(__fmul2_rn(x2, f2(kExpTableInvH)), x2, tab);
+      r = AttenTable::eval2(__fmul2_rn(x2, f2(kExpTableInvH)), tab);
     else
-      r = AttenIntrinsic::eval2(__fmul2_rn(x2, f2(-1.4426950408889634f)), x2,
-                                tab);
+      r = AttenIntrinsic::eval2(__fmul2_rn(x2, f2(-1.4426950408889634f)));
     g[i] = r.x;
     if (i + 1 < n) g[i + 1] = r.y;
   }

@@ -59,6 +59,8 @@ class GB300Solver:
         self._shape = None
         self._source_kind = "auto"
         self._negative_ok = False
+        self._keff_balance = False
+        self._stabilization = None
         self._formation = "explicit"
         self._cmfd = None
         self._cmfd_keep = None
@@ -123,6 +125,10 @@ class GB300Solver:
             self._call("moc_set_source_kernel", self._SOURCE_KINDS[self._source_kind])
         if self._negative_ok:
             self._call("moc_set_negative_fluxes_allowed", 1)
+        if self._keff_balance:
+            self._call("moc_set_keff_from_neutron_balance", 1)
+        if self._stabilization is not None:
+            self._call("moc_set_transport_stabilization", 1, *self._stabilization)
         if self._formation == "otf":
             self._set_otf()
         if self._cmfd is not None:
@@ -230,6 +236,28 @@ class GB300Solver:
         self._negative_ok = bool(negative_fluxes_on)
         if self._ctx is not None:
             self._call("moc_set_negative_fluxes_allowed", int(self._negative_ok))
+
+    def setKeffFromNeutronBalance(self) -> None:
+        """Solver::setKeffFromNeutronBalance (src/Solver.cpp:2045): keff =
+        fission / (absorption + leakage) with the leakage tallied at vacuum
+        track ends, instead of the ratio of successive fission sources."""
+        self._keff_balance = True
+        if self._ctx is not None:
+            self._call("moc_set_keff_from_neutron_balance", 1)
+
+    _STABILIZATION = {"DIAGONAL": 0, "YAMAMOTO": 1, "GLOBAL": 2}
+
+    def stabilizeTransport(self, stabilization_factor: float,
+                           stabilization_type="DIAGONAL") -> None:
+        """Solver::stabilizeTransport (src/Solver.cpp:676): DIAGONAL,
+        YAMAMOTO or GLOBAL (names, or 0, 1, 2 as openmoc.DIAGONAL ...)."""
+        t = (self._STABILIZATION.get(stabilization_type, -1)
+             if isinstance(stabilization_type, str) else int(stabilization_type))
+        if t not in (0, 1, 2):
+            raise _native.MOCError(-1, f"unknown stabilization type {stabilization_type!r}")
+        self._stabilization = (float(stabilization_factor), t)
+        if self._ctx is not None:
+            self._call("moc_set_transport_stabilization", 1, *self._stabilization)
 
     def useExponentialInterpolation(self) -> None:
         """Shared-memory table evaluation of 1 - exp(-x) (the default)."""
@@ -540,6 +568,18 @@ class GB300Solver:
         f = C.c_double()
         self._call("moc_normalize_fluxes", C.byref(f))
         return f.value
+
+    def computeStabilizingFlux(self):
+        self._call("moc_compute_stabilizing_flux")
+
+    def stabilizeFlux(self):
+        self._call("moc_stabilize_flux")
+
+    def computeFSRFissionSources(self):
+        self._call("moc_compute_fsr_fission_sources")
+
+    def computeFSRScatterSources(self):
+        self._call("moc_compute_fsr_scatter_sources")
 
     def computeFSRSources(self, iteration: int):
         self._call("moc_compute_fsr_sources", int(iteration))

@@ -70,6 +70,16 @@ typedef struct {
   float* boundary;  /* [T][2][F] incoming angular flux of this sweep */
   float* start;     /* [T][2][F] outgoing angular flux for the next sweep */
   double keff;
+  /* [T] leakage tallied at vacuum track ends, or NULL: keff from the ratio
+   * of fission sources (Solver::setKeffFromNeutronBalance switches to
+   * fission / (absorption + leakage)) */
+  real* leakage;
+  /* [R][G] stabilizing flux, or NULL: no transport stabilization
+   * (Solver::stabilizeTransport with stab_type 0 DIAGONAL, 1 YAMAMOTO,
+   * 2 GLOBAL and stab_factor) */
+  real* stab_flux;
+  int32_t stab_type;
+  double stab_factor;
 } oracle_state;
 
 /* ------------------------------------------------------------ utilities */
@@ -247,12 +257,19 @@ static void flush(const oracle_problem* p, oracle_state* s, long fsr,
   memset(buf, 0, sizeof(real) * G);
 }
 
-/* CPUSolver::transferBoundaryFlux, src/CPUSolver.cpp:2560-2600 */
+/* CPUSolver::transferBoundaryFlux, src/CPUSolver.cpp:2560-2600; the
+ * leakage at a vacuum end takes the quadrature weight of the track's polar
+ * index for every polar value, the index being 0 for 2D tracks
+ * (src/TrackTraversingAlgorithms.cpp:895-905). */
 static void transfer(const oracle_problem* p, oracle_state* s, long t, int fwd,
                      const float* psi) {
   const int F = fluxes_per_track(p);
   uint8_t f = p->flags[t];
   int moves = fwd ? (f & 4) : (f & 8);
+  if (!moves && s->leakage) {
+    real weight = (real) p->weights[(long) p->track_ang[t] * p->num_polar_half];
+    for (int pe = 0; pe < F; pe++) s->leakage[t] += weight * (real) psi[pe];
+  }
   if (!moves) return;
   long next = p->next[2 * t + (fwd ? 0 : 1)];
   int next_is_fwd = fwd ? (f & 1) : (f & 2);
@@ -328,6 +345,7 @@ static void sweep_impl(const oracle_problem* p, oracle_state* s,
   const long T = p->num_tracks;
   const int F = fluxes_per_track(p);
   memset(s->phi, 0, sizeof(real) * R * G);
+  if (s->leakage) memset(s->leakage, 0, sizeof(real) * T);
   memcpy(s->boundary, s->start, sizeof(float) * 2 * T * F);
   set_threads(p);
   void* locks = NULL;
@@ -433,8 +451,31 @@ void oracle_compute_keff(const oracle_problem* p, oracle_state* s) {
     rates[r] *= (real) p->fsr_vol[r];
   }
   double fission = pairwise_sum_d(rates, R);
+  if (!s->leakage) {
+    free(rates);
+    s->keff *= fission / (double) R;
+    return;
+  }
+  /* absorption = sigma_t less the scattering out of each group, formed as
+   * Material::getSigmaA does (src/Material.cpp:230-252) */
+#pragma omp parallel for schedule(static)
+  for (long r = 0; r < R; r++) {
+    real grp[1024];
+    const int m = p->fsr_mat[r];
+    const float* st = p->sigma_t + (long) m * G;
+    const float* ss = p->sigma_s + (long) m * G * G;
+    for (int g = 0; g < G; g++) {
+      real sa = (real) st[g];
+      for (int gd = 0; gd < G; gd++) sa -= (real) ss[gd * G + g];
+      grp[g] = sa * s->phi[r * G + g];
+    }
+    rates[r] = pairwise_sum_r(grp, G);
+    rates[r] *= (real) p->fsr_vol[r];
+  }
+  double absorption = pairwise_sum_d(rates, R);
   free(rates);
-  s->keff *= fission / (double) R;
+  double leakage = pairwise_sum_r(s->leakage, p->num_tracks);
+  s->keff = fission / (absorption + leakage);
 }
 
 /* CPUSolver::computeResidual, src/CPUSolver.cpp:2113-2255 */
@@ -494,11 +535,87 @@ double oracle_residual(const oracle_problem* p, oracle_state* s, int res_type) {
   return sqrt(total / (double) norm);
 }
 
+/* The largest |sigma_s,gg / sigma_t,g| over the FSRs' materials times the
+ * factor (the YAMAMOTO ratio of group g, src/CPUSolver.cpp:2697-2712). */
+static real yamamoto_ratio(const oracle_problem* p, const oracle_state* s,
+                           int g) {
+  const int G = p->num_groups;
+  float max_ratio = 0.0f;
+  for (long r = 0; r < p->num_fsrs; r++) {
+    const int m = p->fsr_mat[r];
+    const float scat = p->sigma_s[((long) m * G + g) * G + g];
+    const float total = p->sigma_t[(long) m * G + g];
+    const float ratio = fabsf(scat / total);
+    if (ratio > max_ratio) max_ratio = ratio;
+  }
+  return (real) (max_ratio * s->stab_factor);
+}
+
+/* CPUSolver::computeStabilizingFlux, src/CPUSolver.cpp:2665-2730 */
+void oracle_compute_stabilizing_flux(const oracle_problem* p, oracle_state* s) {
+  const long R = p->num_fsrs;
+  const int G = p->num_groups;
+  if (s->stab_type == 0) {
+    for (long r = 0; r < R; r++) {
+      const int m = p->fsr_mat[r];
+      for (int e = 0; e < G; e++) {
+        const real sigma_s = (real) p->sigma_s[((long) m * G + e) * G + e];
+        const real sigma_t = (real) p->sigma_t[(long) m * G + e];
+        if (sigma_s < 0)
+          s->stab_flux[r * G + e] = (real) (-s->phi[r * G + e] *
+                                            s->stab_factor * sigma_s / sigma_t);
+      }
+    }
+  } else if (s->stab_type == 1) {
+    for (int e = 0; e < G; e++) {
+      const real max_ratio = yamamoto_ratio(p, s, e);
+      for (long r = 0; r < R; r++)
+        s->stab_flux[r * G + e] = s->phi[r * G + e] * max_ratio;
+    }
+  } else {
+    const real mult = (real) (1.0 / s->stab_factor - 1.0);
+    for (long i = 0; i < R * G; i++) s->stab_flux[i] = mult * s->phi[i];
+  }
+}
+
+/* CPUSolver::stabilizeFlux, src/CPUSolver.cpp:2736-2810 */
+void oracle_stabilize_flux(const oracle_problem* p, oracle_state* s) {
+  const long R = p->num_fsrs;
+  const int G = p->num_groups;
+  if (s->stab_type == 0) {
+    for (long r = 0; r < R; r++) {
+      const int m = p->fsr_mat[r];
+      for (int e = 0; e < G; e++) {
+        const real sigma_s = (real) p->sigma_s[((long) m * G + e) * G + e];
+        const real sigma_t = (real) p->sigma_t[(long) m * G + e];
+        if (sigma_s < 0) {
+          s->phi[r * G + e] += s->stab_flux[r * G + e];
+          s->phi[r * G + e] = (real) (s->phi[r * G + e] /
+                                      (1.0 - s->stab_factor * sigma_s / sigma_t));
+        }
+      }
+    }
+  } else if (s->stab_type == 1) {
+    for (int e = 0; e < G; e++) {
+      const real max_ratio = yamamoto_ratio(p, s, e);
+      for (long r = 0; r < R; r++) {
+        s->phi[r * G + e] += s->stab_flux[r * G + e];
+        s->phi[r * G + e] /= (1 + max_ratio);
+      }
+    }
+  } else {
+    for (long i = 0; i < R * G; i++) {
+      s->phi[i] += s->stab_flux[i];
+      s->phi[i] = (real) (s->phi[i] * s->stab_factor);
+    }
+  }
+}
+
 /* ------------------------------------------------------------ drivers */
 
-/* Solver::computeEigenvalue without CMFD or stabilisation
- * (src/Solver.cpp:1542-1700; initial guess src/Solver.cpp:1710-1757).
- * Returns the number of iterations. */
+/* Solver::computeEigenvalue without CMFD (src/Solver.cpp:1542-1700;
+ * initial guess src/Solver.cpp:1710-1757), with transport stabilization
+ * when s->stab_flux is set.  Returns the number of iterations. */
 int oracle_compute_eigenvalue(const oracle_problem* p, oracle_state* s,
                               int max_iters, int res_type, double threshold,
                               double* residual_out) {
@@ -510,11 +627,15 @@ int oracle_compute_eigenvalue(const oracle_problem* p, oracle_state* s,
   double k_prev = s->keff;
   double residual = 0.0;
   int iters = 0;
+  if (s->stab_flux)
+    memset(s->stab_flux, 0, sizeof(real) * p->num_fsrs * p->num_groups);
   for (int i = 0; i < max_iters; i++) {
+    if (i > 0 && s->stab_flux) oracle_compute_stabilizing_flux(p, s);
     oracle_compute_sources(p, s, i, 0);
     oracle_sweep(p, s);
     oracle_add_source(p, s, 0);
     oracle_compute_keff(p, s);
+    if (i > 0 && s->stab_flux) oracle_stabilize_flux(p, s);
     oracle_normalize(p, s);
     residual = oracle_residual(p, s, res_type);
     int dk = (int) (1e5 * (s->keff - k_prev));

@@ -39,7 +39,8 @@ class _State(C.Structure):
     _fields_ = [
         ("phi", C.c_void_p), ("phi_old", C.c_void_p), ("reduced", C.c_void_p),
         ("fixed", C.c_void_p), ("boundary", C.c_void_p), ("start", C.c_void_p),
-        ("keff", C.c_double),
+        ("keff", C.c_double), ("leakage", C.c_void_p),
+        ("stab_flux", C.c_void_p), ("stab_type", C.c_int32), ("stab_factor", C.c_double),
     ]
 
 
@@ -92,6 +93,8 @@ def _lib(precision: str):
         lib.oracle_residual.argtypes = [P, S, C.c_int]
         lib.oracle_residual.restype = C.c_double
         lib.oracle_store.argtypes = [P, S]
+        lib.oracle_compute_stabilizing_flux.argtypes = [P, S]
+        lib.oracle_stabilize_flux.argtypes = [P, S]
         lib.oracle_flatten.argtypes = [P, S, C.c_double]
         lib.oracle_zero_track_fluxes.argtypes = [P, S]
         lib.oracle_real_size.restype = C.c_int
@@ -148,10 +151,26 @@ class Oracle:
             _ptr(pp.next), _ptr(pp.flags), _ptr(pp.weights), _ptr(pp.inv_sin),
             _ptr(pp.sigma_t), _ptr(pp.sigma_s), _ptr(pp.nu_sigma_f), _ptr(pp.chi),
             _ptr(pp.fsr_mat), _ptr(pp.fsr_vol), pp.solve_3d, num_threads)
+        self.leakage = None
         self._cs = _State(_ptr(self.phi), _ptr(self.phi_old), _ptr(self.reduced),
-                          _ptr(self.fixed), _ptr(self.boundary), _ptr(self.start), 1.0)
+                          _ptr(self.fixed), _ptr(self.boundary), _ptr(self.start), 1.0,
+                          None, None, 0, 0.0)
+        self.stab_flux = None
         self.num_iterations = 0
         self.residual = 0.0
+
+    def set_keff_from_neutron_balance(self) -> None:
+        """keff = fission / (absorption + leakage), the leakage tallied per
+        track at vacuum ends (Solver::setKeffFromNeutronBalance)."""
+        self.leakage = np.zeros(self.p.num_tracks, self.real)
+        self._cs.leakage = _ptr(self.leakage)
+
+    def stabilize_transport(self, factor: float, kind: int) -> None:
+        """Solver::stabilizeTransport: kind 0 DIAGONAL, 1 YAMAMOTO, 2 GLOBAL."""
+        self.stab_flux = np.zeros(self.p.num_fsrs * self.p.num_groups, self.real)
+        self._cs.stab_flux = _ptr(self.stab_flux)
+        self._cs.stab_type = int(kind)
+        self._cs.stab_factor = float(factor)
 
     @property
     def keff(self) -> float:
@@ -220,6 +239,20 @@ class Oracle:
 
     def store(self) -> None:
         self.lib.oracle_store(C.byref(self._cp), C.byref(self._cs))
+
+    def compute_stabilizing_flux(self) -> None:
+        self.lib.oracle_compute_stabilizing_flux(C.byref(self._cp), C.byref(self._cs))
+
+    def stabilize_flux(self) -> None:
+        self.lib.oracle_stabilize_flux(C.byref(self._cp), C.byref(self._cs))
+
+    def configure(self, scalars) -> None:
+        """The solver options a fixture was made with: keff from the neutron
+        balance, transport stabilization."""
+        if int(scalars.get("keff_balance", 0)):
+            self.set_keff_from_neutron_balance()
+        if int(scalars.get("stab_type", -1)) >= 0:
+            self.stabilize_transport(scalars["stab_factor"], int(scalars["stab_type"]))
 
 
 class LSOracle(Oracle):

@@ -15,6 +15,12 @@ CASES = ["pin_c5g7", "pin_70g", "pin7_synth", "lat3_g2_vac", "lat2_g16"]
 SRC_CASES = ["src3_g7", "flux3_g7"]
 # Explicit 3D tracks (TrackGenerator3D with EXPLICIT_3D segments).
 CASES_3D = ["pin3d_g7"]
+# keff from the neutron balance (Solver::setKeffFromNeutronBalance); its
+# probe also holds the fission / scattering source hooks.
+BALANCE_CASES = ["lat3_bal"]
+# Transport stabilization (Solver::stabilizeTransport): YAMAMOTO, GLOBAL,
+# DIAGONAL (a moderator with negative within-group scattering).
+STAB_CASES = ["pin7_stab_y", "pin7_stab_g", "lat3_stab_d"]
 # Linear-source solves (CPULSSolver): the reference's own
 # test_2d_gradient_linear_source and test_fixed_linear_source replicas, an
 # eigenvalue pin cell and a computeSource lattice.

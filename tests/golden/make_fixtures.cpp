@@ -131,8 +131,10 @@ class ProbeSolver : public CPUSolver {
   long nflux() const { return _num_FSRs * _num_groups; }
   long nbound() const { return 2 * _tot_num_tracks * _fluxes_per_track; }
 
-  /* One pass of every hook from the converged state. */
-  void probe(Writer& w) {
+  /* One pass of every hook from the converged state; with partial, then
+   * the fission and the scattering parts of the source alone from the
+   * normalised flux (computeFSRFissionSources / computeFSRScatterSources). */
+  void probe(Writer& w, bool partial = false) {
     w.sc("probe_keff_in", _k_eff);
     std::vector<float> v = tof(_scalar_flux, nflux());
     w.arr("probe_phi_in", "f4", v.data(), v.size());
@@ -158,6 +160,14 @@ class ProbeSolver : public CPUSolver {
     w.sc("probe_residual_fission", computeResidual(FISSION_SOURCE));
     w.sc("probe_residual_flux", computeResidual(SCALAR_FLUX));
     w.sc("probe_residual_total", computeResidual(TOTAL_SOURCE));
+    if (partial) {
+      computeFSRFissionSources();
+      v = tof(_reduced_sources, nflux());
+      w.arr("probe_fission_sources", "f4", v.data(), v.size());
+      computeFSRScatterSources();
+      v = tof(_reduced_sources, nflux());
+      w.arr("probe_scatter_sources", "f4", v.data(), v.size());
+    }
   }
 };
 
@@ -453,6 +463,10 @@ struct CaseSpec {
   std::vector<double> src_cell_moments;  /* [G][3], empty: none */
   Cmfd* cmfd;              /* attached to geo before the FSRs are made */
   int k_nearest;           /* the Cmfd's setKNearest (0: not set) */
+  bool keff_balance;       /* Solver::setKeffFromNeutronBalance */
+  int stab_type;           /* stabilizeTransport type + 1 (0: off) */
+  double stab_factor;
+  bool probe_partial;      /* probe the fission / scatter source hooks */
 };
 
 /* What the CMFD mesh of a case is laid over, in the arrays
@@ -571,6 +585,10 @@ static void run_case(const CaseSpec& c, const std::string& outdir) {
   solver.setNumThreads(1);
   solver.setConvergenceThreshold(c.tol);
   if (c.allow_negative) solver.allowNegativeFluxes(true);
+  if (c.keff_balance) solver.setKeffFromNeutronBalance();
+  if (c.stab_type > 0)
+    solver.stabilizeTransport(c.stab_factor,
+                              (stabilizationType) (c.stab_type - 1));
   const int G0 = c.geo->getNumEnergyGroups();
   if (c.src_material)
     for (int g = 1; g <= G0; g++)
@@ -614,6 +632,9 @@ static void run_case(const CaseSpec& c, const std::string& outdir) {
   w.sc("k_source", c.k_source);
   w.sc("linear_source", c.linear_source ? 1 : 0);
   w.sc("allow_negative", c.allow_negative ? 1 : 0);
+  w.sc("keff_balance", c.keff_balance ? 1 : 0);
+  w.sc("stab_type", c.stab_type - 1);
+  w.sc("stab_factor", c.stab_factor);
   w.sc("iterations", solver.getNumIterations());
   w.sc("keff", solver.getKeff());
   const long R = p.num_fsrs;
@@ -670,7 +691,7 @@ static void run_case(const CaseSpec& c, const std::string& outdir) {
   if (c.cmfd) write_cmfd(w, c, tg, p);
   if (c.probe && c.kind == EIGEN) {
 #ifdef SINGLE
-    if (flat) flat->probe(w);
+    if (flat) flat->probe(w, c.probe_partial);
     else ls->probe(w);
 #endif
   }
@@ -966,6 +987,55 @@ int main(int argc, char** argv) {
                    EIGEN, 1.0, false, NULL, 0.0};
     cs.cmfd = cm;
     cs.k_nearest = 3;
+    cases.push_back(cs);
+  }
+
+  /* 17. case 4 (3x3, 2 groups, vacuum on +x and +y) with keff from the
+   *     neutron balance (Solver::setKeffFromNeutronBalance); the probe also
+   *     takes the fission and scattering source hooks */
+  {
+    Material* fuel = make_material(31, "fuel2b",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 2, 2, true));
+    Material* mod = make_material(32, "mod2b",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 1002, 2, false));
+    CaseSpec cs = {"lat3_bal", lattice_geometry(3, fuel, mod, pin, {4}, REF,
+                   VAC, REF, VAC), 16, 0.1, 1000, 1e-5, FISSION_SOURCE, EIGEN,
+                   1.0, true, NULL, 0.0};
+    cs.keff_balance = true;
+    cs.probe_partial = true;
+    cases.push_back(cs);
+  }
+  /* 18-20. transport stabilization (Solver::stabilizeTransport): the
+   *     7-group pin cell of case 3 with YAMAMOTO (factor 0.5) and GLOBAL
+   *     (0.5); DIAGONAL on a 3x3 lattice, 7 groups, vacuum on +x and +y,
+   *     whose moderator has negative within-group scattering in its last two
+   *     groups (as transport-corrected data can), factor 1 */
+  for (int k = 0; k < 2; k++) {
+    Material* fuel = make_material(33 + 2 * k, "fuel7st",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL, 7, true));
+    Material* mod = make_material(34 + 2 * k, "mod7st",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 1000, 7, false));
+    Universe* u = make_pin(fuel, mod, pin);
+    CaseSpec cs = {k == 0 ? "pin7_stab_y" : "pin7_stab_g",
+                   make_box_geometry(u, NULL, 0.63, REF, REF, REF, REF), 32,
+                   0.05, 1000, 1e-5, FISSION_SOURCE, EIGEN, 1.0, false, NULL,
+                   0.0};
+    cs.stab_type = (k == 0 ? (int) YAMAMOTO : (int) GLOBAL) + 1;
+    cs.stab_factor = 0.5;
+    cases.push_back(cs);
+  }
+  {
+    Material* fuel = make_material(37, "fuel7sd",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 4, 7, true));
+    MaterialXS mx = openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 1004, 7,
+                                                     false);
+    for (int g = 5; g < 7; g++) mx.sigma_s[g * 7 + g] = -0.05 * mx.sigma_t[g];
+    Material* mod = make_material(38, "mod7sd", mx);
+    CaseSpec cs = {"lat3_stab_d", lattice_geometry(3, fuel, mod, pin, {4},
+                   REF, VAC, REF, VAC), 16, 0.1, 1000, 1e-5, FISSION_SOURCE,
+                   EIGEN, 1.0, false, NULL, 0.0};
+    cs.stab_type = (int) DIAGONAL + 1;
+    cs.stab_factor = 1.0;
     cases.push_back(cs);
   }
 

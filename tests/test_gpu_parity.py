@@ -10,7 +10,7 @@ OpenMOC's own FP32 and FP64 builds differ by 1.1e-5 on the pin cell at the
 import numpy as np
 import pytest
 
-from conftest import CASES, CASES_3D, SRC_CASES, load_case
+from conftest import BALANCE_CASES, CASES, CASES_3D, SRC_CASES, STAB_CASES, load_case
 from openmoc_gb300 import GB300Solver
 from openmoc_gb300.solver import EXP_INTRINSIC, EXP_TABLE, FISSION_SOURCE, SCALAR_FLUX
 from oracle.oracle import Oracle
@@ -265,4 +265,84 @@ def test_extruded_3d_lattice_matches_fp64_oracle():
     o.compute_eigenvalue(30, 1, 1e-30)
     assert abs(s.getKeff() - o.keff) <= 2e-6 * o.keff
     assert max_rel(s.getFluxes(), o.phi.reshape(p.num_fsrs, p.num_groups)) <= 2e-5
+    s.close()
+
+
+def _configure(s, sc):
+    if int(sc.get("keff_balance", 0)):
+        s.setKeffFromNeutronBalance()
+    if int(sc.get("stab_type", -1)) >= 0:
+        s.stabilizeTransport(sc["stab_factor"], int(sc["stab_type"]))
+
+
+@pytest.mark.parametrize("case", BALANCE_CASES + STAB_CASES)
+def test_balance_and_stabilization_match_openmoc(case):
+    """keff from the neutron balance (Solver::setKeffFromNeutronBalance)
+    and transport stabilization (Solver::stabilizeTransport: YAMAMOTO,
+    GLOBAL, DIAGONAL) against OpenMOC's FP32 and FP64 runs."""
+    p, sc, arr = load_case(case, "f32")
+    _, sc64, arr64 = load_case(case, "f64")
+    s = GB300Solver(p)
+    _configure(s, sc)
+    s.setConvergenceThreshold(sc["tolerance"])
+    s.computeEigenvalue(int(sc["max_iters"]), int(sc["res_type"]))
+    assert abs(s.getNumIterations() - int(sc["iterations"])) <= 2
+    assert abs(s.getKeff() - sc["keff"]) <= KEFF_TOL
+    assert max_rel(s.getFluxes(), arr["flux"]) <= FLUX_TOL
+    assert abs(s.getKeff() - sc64["keff"]) <= 1.5 * KEFF_TOL
+    assert max_rel(s.getFluxes(), arr64["flux"]) <= FLUX_TOL
+    s.close()
+
+
+@pytest.mark.parametrize("case", BALANCE_CASES)
+def test_balance_hooks_and_partial_sources_match_openmoc(case):
+    """From OpenMOC's converged state: the sweep's leakage tally feeds
+    computeKeff (fission / (absorption + leakage)); then the fission and the
+    scattering parts of the source alone (computeFSRFissionSources /
+    computeFSRScatterSources) from the normalised flux."""
+    p, sc, arr = load_case(case, "f32")
+    s = GB300Solver(p)
+    s.setKeffFromNeutronBalance()
+    s.setFluxes(arr["probe_phi_in"])
+    s.setOldFluxes(arr["probe_phi_old"])
+    s.setKeff(sc["probe_keff_in"])
+    s.setStartFlux(arr["probe_start_flux_in"])
+    s.computeFSRSources(100)
+    s.transportSweep()
+    s.addSourceToScalarFlux()
+    s.computeKeff()
+    assert abs(s.getKeff() - sc["probe_keff_out"]) < 2e-6
+    s.setFluxes(arr["probe_phi_norm"])
+    s.computeFSRFissionSources()
+    np.testing.assert_allclose(s.getReducedSources().ravel(), arr["probe_fission_sources"],
+                               rtol=2e-6, atol=1e-30)
+    s.computeFSRScatterSources()
+    np.testing.assert_allclose(s.getReducedSources().ravel(), arr["probe_scatter_sources"],
+                               rtol=2e-6, atol=1e-30)
+    s.close()
+
+
+@pytest.mark.parametrize("case", STAB_CASES)
+def test_stabilization_hooks_match_oracle(case):
+    """computeStabilizingFlux then stabilizeFlux from the same state on the
+    GPU and in the oracle (CPUSolver semantics, src/CPUSolver.cpp:
+    2665-2810)."""
+    p, sc, arr = load_case(case, "f32")
+    o = Oracle(p, "f32")
+    o.configure(sc)
+    R, G = p.num_fsrs, p.num_groups
+    rng = np.random.default_rng(5)
+    start = rng.uniform(0.5, 1.5, R * G).astype(np.float32)
+    after = rng.uniform(0.5, 1.5, R * G).astype(np.float32)
+    o.phi[:] = start
+    o.compute_stabilizing_flux()
+    o.phi[:] = after
+    o.stabilize_flux()
+    s = GB300Solver(p)
+    _configure(s, sc)
+    s.setFluxes(start)
+    s.computeStabilizingFlux()
+    s.setFluxes(after)
+    s.stabilizeFlux()
+    np.testing.assert_allclose(s.getFluxes().ravel(), o.phi, rtol=2e-6)
     s.close()

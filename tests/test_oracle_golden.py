@@ -16,7 +16,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import CASES, CASES_3D, GOLDEN, SRC_CASES, load_case
+from conftest import BALANCE_CASES, CASES, CASES_3D, GOLDEN, SRC_CASES, STAB_CASES, load_case
 from oracle.oracle import Oracle
 
 
@@ -55,21 +55,25 @@ def test_oracle_matches_reference_goldens(precision):
         np.testing.assert_allclose(o.phi, d["fluxes"], rtol=2e-5)
 
 
-@pytest.mark.parametrize("case", CASES + SRC_CASES + CASES_3D)
+@pytest.mark.parametrize("case", CASES + SRC_CASES + CASES_3D + BALANCE_CASES + STAB_CASES)
 @pytest.mark.parametrize("precision", ["f32", "f64"])
 def test_oracle_solve_matches_openmoc(case, precision):
+    """Including keff from the neutron balance and the three transport
+    stabilizations."""
     p, sc, arr = load_case(case, precision)
     o = Oracle(p, precision, num_threads=2)
+    o.configure(sc)
     it = _solve(o, sc)
     assert abs(it - int(sc["iterations"])) <= 1
     assert abs(o.keff - sc["keff"]) < 1e-5
     np.testing.assert_allclose(o.phi, arr["flux"], rtol=1e-5)
 
 
-@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("case", CASES + BALANCE_CASES)
 def test_oracle_hooks_match_openmoc(case):
     p, sc, arr = load_case(case, "f32")
     o = Oracle(p, "f32", num_threads=1)
+    o.configure(sc)
     o.phi[:] = arr["probe_phi_in"]
     o.phi_old[:] = arr["probe_phi_old"]
     o.keff = sc["probe_keff_in"]
