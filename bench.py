@@ -501,7 +501,7 @@ def run_gpu(args):
             sv = run_serving(args)
             out["serving"] = {k: sv[k] for k in ("metric", "value", "unit", "config",
                                                  "batched", "plain", "speedup",
-                                                 "agreement")}
+                                                 "ceiling", "by_class", "agreement")}
         print(json.dumps(out), flush=True)
     s.close()
     if dist:
@@ -846,9 +846,33 @@ def run_serving(args):
         c["plain_sweep_s"] += a["sweep_s"]
         c["iterations"] += a["iterations"]
         c["integrations"] += float(p.integrations_per_sweep) * a["iterations"]
+    # per class: the batched solves' latencies beside the plain loop's
+    for r, b in zip(stream, batched):
+        c = classes[f'{r["geom"]}/{r["G"]}g']
+        c.setdefault("batched_latency_s", []).append(b["latency"])
+    for c in classes.values():
+        lat = np.array(c.pop("batched_latency_s"))
+        c["batched_p50_latency_s"] = float(np.percentile(lat, 50))
+        c["batched_p99_latency_s"] = float(np.percentile(lat, 99))
+        c["plain_integrations_per_s"] = c["integrations"] / max(c["plain_sweep_s"], 1e-12)
     lat_b = np.array([x["latency"] for x in batched])
     lat_p = np.array([x["latency"] for x in plain])
     n = len(stream)
+    # The ceiling of the mix: every request's integrations at the rate the
+    # fastest class sweeps at alone (the large 70-group solves, FP32-bound),
+    # i.e. a batched makespan no shorter than the stream's total work at the
+    # best single-problem sweep rate; and the same at the FP32 peak.
+    total_int = sum(c["integrations"] for c in classes.values())
+    best_rate = max(c["plain_integrations_per_s"] for c in classes.values())
+    import torch
+    props = torch.cuda.get_device_properties(0)
+    fp32_rate = props.multi_processor_count * 128 * 2 * 2.07e9 / FLOPS_PER_INTEGRATION
+    ceiling = {"stream_integrations": total_int,
+               "best_single_problem_rate": best_rate,
+               "min_makespan_s_at_best_rate": total_int / best_rate,
+               "speedup_ceiling_at_best_rate": t_p / (total_int / best_rate),
+               "min_makespan_s_at_fp32_peak": total_int / fp32_rate,
+               "speedup_ceiling_at_fp32_peak": t_p / (total_int / fp32_rate)}
     out = {
         "metric": "solves/s (batched server vs plain per-solve loop)",
         "value": n / t_b, "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
@@ -868,7 +892,8 @@ def run_serving(args):
                   "p50_latency_s": float(np.percentile(lat_p, 50)),
                   "p99_latency_s": float(np.percentile(lat_p, 99))},
         "speedup": t_p / t_b,
-        "plain_by_class": classes,
+        "ceiling": ceiling,
+        "by_class": classes,
         # a request whose two solves stopped one iteration apart can differ
         # in fluxes that are still decaying from the flat guess (1e-9 of the
         # peak); df_same covers the requests that ran the same iterations

@@ -152,9 +152,9 @@ int moc_get_tuning_log(moc_ctx* ctx, int* lps, int* slots, int* exp_kind,
                        float* ms, int capacity, int* count);
 
 /** Sweep kernel shape: lps lanes per track direction (power of two <= 32)
- *  each carrying `slots` pairs of energy groups (2 * lps * slots >= G,
- *  slots at most the kernel's limit); lps = 0 restores the built-in choice.
- *  Replaces
+ *  each carrying `slots` pairs of energy groups, the fewest that cover the
+ *  groups (slots = ceil(ceil(G / 2) / lps), at most the kernel's limit);
+ *  lps = 0 restores the built-in choice.  Replaces
  *  GPUSolver::setNumThreadBlocks / setNumThreadsPerBlock
  *  (src/accel/cuda/GPUSolver.cu:987-1015). */
 int moc_set_sweep_shape(moc_ctx* ctx, int lps, int slots);

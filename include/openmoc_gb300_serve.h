@@ -74,7 +74,8 @@ typedef struct {
   int64_t max_tracks;     /* track entries (a solve uses T + 1) */
   int64_t max_segments;   /* segments */
   int32_t lanes;          /* sweep lanes per track direction; 0: autotune */
-  int32_t pairs;          /* group pairs per lane (with lanes) */
+  int32_t pairs;          /* group pairs per lane (with lanes): the fewest
+                             that cover the groups, ceil(ceil(G/2)/lanes) */
   int32_t exp_kind;       /* with lanes: MOC_EXP_INTRINSIC (pools use ex2) */
 } moc_pool_config;
 

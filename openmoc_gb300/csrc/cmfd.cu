@@ -139,18 +139,21 @@ struct FSum {
 // of the block's threads: an SM issues FP64 at 1/64 of its FP32 rate, and
 // those per-thread copies were most of the coarse solve's time.  red holds
 // 33 doubles.
+// The warp partials red[0..31] of the previous call were read by warp 0
+// before that call's last barrier, and its result red[32] is read by every
+// thread before it reaches this call's barrier, so writing the partials
+// needs no barrier of its own.  Warp 0 adds the partials as a shuffle tree.
 template <class F>
 __device__ double block_sum(float v, double* red, F finish) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  __syncthreads();   // earlier readers of red are done
   if (lane == 0) red[w] = (double) v;
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (w == 0) {
     const int nw = (blockDim.x + 31) >> 5;
-    double t = 0.0;
-    for (int i = 0; i < nw; i++) t += red[i];
-    red[32] = finish(t);
+    double t = lane < nw ? red[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) red[32] = finish(t);
   }
   __syncthreads();
   return red[32];
@@ -339,9 +342,10 @@ __device__ double rmse(const CmfdArgs& a, const float* x, const float* y,
       part.add(r * r);
     }
   }
-  const int C = a.C;
+  const double inv_c = 1.0 / (double) max(a.C, 1);
   return block_sum(part.value(), red, [&](double tot) {
-    return judge(sqrt(tot / (double) max(C, 1)));
+    // the root in FP32: the verdicts need a few digits, not FP64's 16
+    return judge((double) sqrtf((float) (tot * inv_c)));
   });
 }
 
@@ -575,7 +579,7 @@ __device__ bool linear_solve(const CmfdArgs& a, const Work& k, const float* b,
   mat_fission<EC>(a, k, k.x, ls_old);
   __syncthreads();
   // the convergence state lives in thread 0, which judges each residual
-  double linit = 0.0, min_res = 1e6, stall_res = INFINITY;
+  double linit = 0.0, inv_linit = INFINITY, min_res = 1e6, stall_res = INFINITY;
   int li = 0, stall_li = 0;
   while (li < kMaxLinearIters) {
     sor_half<EC>(a, k, b, 0);
@@ -589,14 +593,18 @@ __device__ bool linear_solve(const CmfdArgs& a, const Work& k, const float* b,
       mat_fission<EC>(a, k, k.x, ls_new);
       __syncthreads();
     }
-    if (li == 0) rmse(a, ls_new, ls_old, red, [&](double r) { return linit = r; });
+    if (li == 0)
+      rmse(a, ls_new, ls_old, red, [&](double r) {
+        inv_linit = r > 0.0 ? 1.0 / r : INFINITY;
+        return linit = r;
+      });
     li++;
     if (li > kMinIters) {
       // 1 converged, -1 diverged, 0 not yet
       const double verdict = rmse(a, ls_new, ls_old, red, [&](double r) {
         min_res = fmin(min_res, r);
         if ((r > 1e3 * min_res && min_res > kNoiseFloor) || !isfinite(r)) return -1.0;
-        const double q = linit > 0.0 ? r / linit : INFINITY;
+        const double q = linit > 0.0 ? r * inv_linit : INFINITY;
         if (q < 0.1 || r < tol) return 1.0;
         if (li - stall_li >= kStallWindow) {
           if (r < kStallMax && r > 0.5 * stall_res) return 1.0;
@@ -648,7 +656,7 @@ __device__ bool dd_linear_solve(const CmfdArgs& a, const Work& k,
   float* new_src = k.dd_b;
   mat_fission<EC>(a, k, k.x, new_src);
   __syncthreads();
-  double initial = 0.0, min_res = 1e6, stall_res = INFINITY;
+  double initial = 0.0, inv_initial = 0.0, min_res = 1e6, stall_res = INFINITY;
   int stall_it = 0;
   for (int it = 0; it < kMaxLinearIters; it++) {
     float* t = old_src;
@@ -662,10 +670,13 @@ __device__ bool dd_linear_solve(const CmfdArgs& a, const Work& k,
     __syncthreads();
     // thread 0 judges: 1 settled, -1 diverged, 0 not yet
     const double verdict = rmse(a, new_src, old_src, red, [&](double res) {
-      if (it == 0) initial = res < 1e-14 ? 1e-10 : res;
+      if (it == 0) {
+        initial = res < 1e-14 ? 1e-10 : res;
+        inv_initial = 1.0 / initial;
+      }
       min_res = fmin(min_res, res);
       if ((res > 1e3 * min_res && min_res > kNoiseFloor) || !isfinite(res)) return -1.0;
-      if (res / initial < 0.1 || res < tol) return 1.0;
+      if (res * inv_initial < 0.1 || res < tol) return 1.0;
       if (it - stall_it >= kStallWindow) {
         if (res < kStallMax && res > 0.5 * stall_res) return 1.0;
         stall_res = res;
@@ -754,7 +765,7 @@ cmfd_solve_kernel(const CmfdArgs a, int smem_mask) {
       k.x[r] = (float) (k.x[r] * (rows * keff / s0));
     }
     __syncthreads();
-    double initial = 0.0, stall_res = INFINITY;
+    double initial = 0.0, inv_initial = 0.0, stall_res = INFINITY;
     int stall_p = 0;
     bool dd_mode = false;
     for (power = 0; power < kMaxPowerIters; power++) {
@@ -778,8 +789,12 @@ cmfd_solve_kernel(const CmfdArgs a, int smem_mask) {
       __syncthreads();
       // thread 0 judges: 1 converged, 0 not yet
       const double stop = rmse(a, src_new, src_old, red, [&](double res) {
-        if (power == 0) initial = res < 1e-14 ? 1e-10 : res;
-        if ((res / initial < 0.03 || res < kLinalgTol) && power > kMinIters) return 1.0;
+        if (power == 0) {
+          initial = res < 1e-14 ? 1e-10 : res;
+          inv_initial = 1.0 / initial;
+        }
+        if ((res * inv_initial < 0.03 || res < kLinalgTol) && power > kMinIters)
+          return 1.0;
         if (power > kMinIters && power - stall_p >= kStallWindow) {
           if (res < kStallMax && res > 0.5 * stall_res) return 1.0;
           stall_res = res;

@@ -1710,6 +1710,9 @@ int moc_set_sweep_shape(moc_ctx* c, int lps, int slots) {
                 2 * (int64_t) lps * slots >= c->d.num_groups,
             MOC_ERR_ARG,
             "lanes x group pairs per lane must cover every group");
+  MOC_CHECK(slots == pair_slots(c->d.num_groups, lps), MOC_ERR_ARG,
+            "group pairs per lane must be the fewest that cover the groups, "
+            "ceil(ceil(G / 2) / lanes)");
   c->lps = lps;
   c->slots = slots;
   c->shape_user_set = 1;

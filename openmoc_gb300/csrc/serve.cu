@@ -494,6 +494,9 @@ int create_pool(moc_server* srv, const moc_pool_config& c, Pool& p) {
     SV_CHECK(c.pairs >= 1 && c.pairs <= moc::kMaxSlots &&
                  2 * (int64_t) c.lanes * c.pairs >= c.num_groups,
              MOC_ERR_ARG, "lanes x group pairs per lane must cover every group");
+    SV_CHECK(c.pairs == pairs_for(c.num_groups, c.lanes), MOC_ERR_ARG,
+             "group pairs per lane must be the fewest that cover the groups, "
+             "ceil(ceil(G / 2) / lanes)");
     SV_CHECK(c.exp_kind == MOC_EXP_INTRINSIC, MOC_ERR_UNSUPPORTED,
              "pools sweep with the hardware-ex2 evaluator (MOC_EXP_INTRINSIC)");
   }

@@ -245,8 +245,19 @@ sweep_kernel(const SweepArgs a) {
       ((int64_t) blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t stream = gwarp * (32 / LPS) + lane / LPS;
   const int npairs = ld >> 1;
-  // pair s of this lane holds groups (the last lanes may have none)
-  auto live_pair = [&](int s) { return sub + s * LPS < npairs; };
+  // Pair s of this lane holds groups.  The host gives an instance at least
+  // (PS - 1) * LPS group pairs (every shape it runs has PS = ceil(npairs /
+  // LPS), and moc_set_sweep_shape and the server check it), so only a
+  // lane's last pair can lie past the groups: in the busy (staged)
+  // instances the others need no test and no branch.  The light instances
+  // test every pair (holding the predicate costs them a spill).
+  const bool last_live = sub + (PS - 1) * LPS < npairs;
+  auto live_pair = [&](int s) {
+    if constexpr (SweepRing<PH, LPS, PS>::staged)
+      return s < PS - 1 || last_live;
+    else
+      return sub + s * LPS < npairs;
+  };
 
   // the track and its pending scale; in a pool the solve of the track may
   // be finished (the LPS lanes of a stream share the track, so they agree
