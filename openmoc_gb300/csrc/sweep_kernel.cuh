@@ -139,13 +139,16 @@ __device__ __forceinline__ void cp_async_wait() {
 #ifndef MOC_SWEEP_BIG_MIN_BLOCKS
 #define MOC_SWEEP_BIG_MIN_BLOCKS 5
 #endif
-template <int PH, int PS>
+// The busy instances of the CMFD mode, which also tally partial currents,
+// take 4 blocks (their registers would spill at 5).
+template <int PH, int PS, int MODE = 0>
 struct SweepOccupancy {
   static constexpr int min_blocks =
-      (PH * PS >= 18)        ? 4
-      : (PH * PS > 6)        ? MOC_SWEEP_BIG_MIN_BLOCKS
-      : (PH == 1 && PS > 2)  ? 6
-                             : 8;
+      (PH * PS >= 18)              ? 4
+      : (PH * PS > 6 && MODE == 2) ? 4
+      : (PH * PS > 6)              ? MOC_SWEEP_BIG_MIN_BLOCKS
+      : (PH == 1 && PS > 2)        ? 6
+                                   : 8;
 };
 
 // CMFD partial currents (mode 2 of the sweeps): faces 0 x-, 1 y-, 2 x+,
@@ -208,7 +211,7 @@ __device__ __forceinline__ void cmfd_tally_crossing(
 // coarse-mesh cells for CMFD (a.cm_cell set).
 template <int PH, int LPS, int PS, int EXPK, int MODE>
 __global__ void __launch_bounds__(kSweepThreads,
-                                  (SweepOccupancy<PH, PS>::min_blocks))
+                                  (SweepOccupancy<PH, PS, MODE>::min_blocks))
 sweep_kernel(const SweepArgs a) {
   constexpr bool POOL = MODE == 1;
   constexpr bool CMFD = MODE == 2;
@@ -339,11 +342,12 @@ sweep_kernel(const SweepArgs a) {
     };
     int2 chunk = fetch(sub);
     int2 chunk_next = fetch(LPS + sub);
-    int cb = 0;   // first segment held by `chunk`; chunk_next the next LPS
-    // segment j (cb <= j < cb + 2 LPS) from lane j % LPS of chunk or
-    // chunk_next (uniform over the stream's lanes)
+    // `chunk` holds the LPS-aligned run of segments containing the current
+    // segment k, chunk_next the run after it; segment j (k <= j < k + LPS)
+    // comes from lane j % LPS of the one that holds it
+    int kc = 0;   // the current segment
     auto word = [&](int j) -> int2 {
-      const int2 w = (j - cb < LPS) ? chunk : chunk_next;
+      const int2 w = ((j ^ kc) < LPS) ? chunk : chunk_next;
       int2 r;
       r.x = __shfl_sync(gmask, w.x, j & (LPS - 1), LPS);
       r.y = __shfl_sync(gmask, w.y, j & (LPS - 1), LPS);
@@ -405,13 +409,14 @@ sweep_kernel(const SweepArgs a) {
       int fsr_n = 0, mat_n = 0;
       float2 qn[PS];
       if constexpr (kStaged) {
+        kc = k;
         stage(k + kAhead);
-        unpack(word(k), len, fsr, mat);
-        // rotate chunks once segment k + 1 leaves `chunk`
-        if (k + 1 - cb == LPS) {
+        // segment k always lies in `chunk` here (it rotates below, once
+        // segment k + 1 leaves it)
+        unpack(word_cur(k), len, fsr, mat);
+        if (((k + 1) & (LPS - 1)) == 0) {
           chunk = chunk_next;
-          chunk_next = fetch(cb + 2 * LPS + sub);
-          cb += LPS;
+          chunk_next = fetch(k + 1 + LPS + sub);
         }
         cp_async_wait<kAhead>();   // segment k's sources have landed
       } else {
@@ -466,9 +471,10 @@ sweep_kernel(const SweepArgs a) {
         int fsr_next = -1;
         if (k + 1 < n) {
           if constexpr (kStaged) {
+            // segment k + 1 lies in `chunk` once the rotation above is done
             float l2;
             int m2;
-            unpack(word(k + 1), l2, fsr_next, m2);
+            unpack(word_cur(k + 1), l2, fsr_next, m2);
           } else {
             fsr_next = fsr_n;
           }
