@@ -45,7 +45,7 @@ FLOPS_PER_LS_INTEGRATION = 48
 # of this workload, from one ncu capture per sweep shape (lanes per track
 # direction, group pairs per lane, exponential kind); the summaries are under
 # profiles/ (sweep_kernel_17x17_70g.txt).
-SWEEP_DRAM_BYTES = {(8, 5, 1): 50_853_120 + 1_411_328}
+SWEEP_DRAM_BYTES = {(8, 5, 1): 50_877_440 + 1_314_560}
 
 
 def env_rank():
