@@ -47,6 +47,9 @@ extern "C" {
 /* Solve kinds of a request. */
 #define MOC_SOLVE_EIGENVALUE 0 /* Solver::computeEigenvalue */
 #define MOC_SOLVE_SOURCE 1     /* Solver::computeSource with a fixed keff */
+#define MOC_SOLVE_FLUX 2       /* Solver::computeFlux(max_iters, true): the
+                                  fixed source alone, computed once from a
+                                  zero flux; SCALAR_FLUX residual */
 
 typedef struct moc_server moc_server;
 

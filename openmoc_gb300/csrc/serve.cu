@@ -186,7 +186,8 @@ int stage_request(const moc_request& q, Staged& s) {
            MOC_ERR_ARG, "null array in request");
   SV_CHECK(q.num_segments == 0 || (q.seg_len && q.seg_fsr), MOC_ERR_ARG,
            "null segments");
-  SV_CHECK(q.kind == MOC_SOLVE_EIGENVALUE || q.kind == MOC_SOLVE_SOURCE,
+  SV_CHECK(q.kind == MOC_SOLVE_EIGENVALUE || q.kind == MOC_SOLVE_SOURCE ||
+               q.kind == MOC_SOLVE_FLUX,
            MOC_ERR_ARG, "unknown solve kind");
   SV_CHECK(q.max_iters >= 1, MOC_ERR_ARG, "max_iters must be positive");
   SV_CHECK(q.res_type >= 0 && q.res_type <= 2, MOC_ERR_ARG,
@@ -305,6 +306,11 @@ int stage_request(const moc_request& q, Staged& s) {
     // Solver::computeInitialFluxGuess then normalizeFluxes: a flat flux of
     // one scaled by R / (total fission source)
     s.init_flux = (double) (float) ((double) R / total);
+  } else if (q.kind == MOC_SOLVE_FLUX) {
+    // Solver::computeFlux: flattenFSRFluxes(0), and the SCALAR_FLUX
+    // residual whatever the request says (src/Solver.cpp:1380-1440)
+    s.init_flux = 0.0;
+    s.req.res_type = MOC_SCALAR_FLUX;
   } else {
     s.init_flux = 1.0;
   }
@@ -764,7 +770,9 @@ int init_slot(moc_server* srv, Pool& p, int slot_index) {
   d.threshold = s.req.threshold;
   d.scale[0] = d.scale[1] = 1.0f;
   d.max_iters = s.req.max_iters;
-  d.mode = eigen ? moc::kModeEigen : moc::kModeSource;
+  d.mode = eigen ? moc::kModeEigen
+                 : s.req.kind == MOC_SOLVE_FLUX ? moc::kModeFlux
+                                                : moc::kModeSource;
   d.res_type = s.req.res_type;
   d.num_fissionable = s.num_fissionable;
   d.row0 = sl.r0;

@@ -241,6 +241,19 @@ compute_sources_kernel(const SolverArgs a, int iteration, int zero_phi,
       const DevScalars* p1 = (s1 >= 0) ? a.slots + s1 : nullptr;
       if (!p0 || p0->done) on &= ~1;
       if (!p1 || p1->done) on &= ~2;
+      // a computeFlux solve keeps the sources of its first iteration (the
+      // fixed source; Solver::computeFlux computes them once): its rows only
+      // get their tallies zeroed
+      int keep = 0;
+      if ((on & 1) && p0->mode == kModeFlux && p0->iteration > 0) keep |= 1;
+      if ((on & 2) && p1->mode == kModeFlux && p1->iteration > 0) keep |= 2;
+      if (keep && zero_phi) {
+        const int lane = threadIdx.x & 31;
+        for (int i = 0; i < 2; i++)
+          if ((keep >> i) & 1)
+            for (int g = lane; g < G; g += 32) a.phi[(r + i) * a.ld + g] = 0.0f;
+      }
+      on &= ~keep;
       if (!on) continue;
       // the FP64 reciprocals in one lane (the rows are the whole warp's)
       const bool lane0 = (threadIdx.x & 31) == 0;

@@ -31,7 +31,8 @@ from .problem import Problem
 
 SOLVE_EIGENVALUE = 0
 SOLVE_SOURCE = 1
-_KINDS = {"eigenvalue": SOLVE_EIGENVALUE, "source": SOLVE_SOURCE}
+SOLVE_FLUX = 2
+_KINDS = {"eigenvalue": SOLVE_EIGENVALUE, "source": SOLVE_SOURCE, "flux": SOLVE_FLUX}
 
 
 class ServerConfig(C.Structure):
@@ -185,7 +186,9 @@ class Server:
         """Queues a solve of `p`; returns its ticket.  kind "eigenvalue" is
         Solver.computeEigenvalue(max_iters, res_type); "source" is
         Solver.computeSource(max_iters, k_eff, res_type) with fixed_source
-        (default: p.fixed_sources) as [R][G] source."""
+        (default: p.fixed_sources) as [R][G] source; "flux" is
+        Solver.computeFlux(max_iters, True): that fixed source alone,
+        SCALAR_FLUX residual."""
         arrs = dict(
             seg_len=np.ascontiguousarray(p.seg_len, np.float32),
             seg_fsr=np.ascontiguousarray(p.seg_fsr, np.int32),

@@ -265,3 +265,34 @@ def test_fixed_source_fixture_through_a_pool():
     assert r["keff"] == pytest.approx(sc["k_source"])
     assert max_rel(r["flux"], arr["flux"]) <= FLUX_TOL
     assert max_rel(r["flux"], arr64["flux"]) <= FLUX_TOL
+
+
+def test_fixed_flux_fixture_through_a_pool():
+    """OpenMOC's computeFlux fixture (the fixed source alone, computed once
+    from a zero flux; SCALAR_FLUX residual) solved in a pool beside
+    eigenvalue and computeSource solves, against OpenMOC's FP32 and FP64
+    results, and the same request alone against the single-problem solver."""
+    p, sc, arr = load_case("flux3_g7")
+    _, _, arr64 = load_case("flux3_g7", "f64")
+    ps, _, _ = load_case("src3_g7")
+    others = mix(4)
+    srv = make_server([p, ps] + others, 8, fixed_shape=False)
+    ts = [srv.submit(q) for q in others[:2]]
+    t = srv.submit(p, "flux", int(sc["max_iters"]), threshold=sc["tolerance"])
+    ts.append(srv.submit(ps, "source", 1000, 2, k_eff=1.0, threshold=1e-5))
+    ts += [srv.submit(q) for q in others[2:]]
+    srv.run_until_idle()
+    r = srv.wait(t, timeout=0)
+    for x in ts:
+        assert srv.wait(x, timeout=0)["converged"]
+    srv.close()
+    assert r["converged"]
+    assert abs(r["iterations"] - int(sc["iterations"])) <= 1
+    assert max_rel(r["flux"], arr["flux"]) <= FLUX_TOL
+    assert max_rel(r["flux"], arr64["flux"]) <= FLUX_TOL
+    s = GB300Solver(p)
+    s.setConvergenceThreshold(sc["tolerance"])
+    s.computeFlux(int(sc["max_iters"]), True)
+    assert r["iterations"] == s.getNumIterations()
+    assert max_rel(r["flux"], s.getFluxes()) <= 1e-5
+    s.close()
