@@ -658,18 +658,52 @@ def end_to_end(p, args, device, torch, otf=False):
 
 def run_instances(p, args, iters=10):
     """args.batch cross-section-perturbed instances of `p` (the same tracks,
-    lognormal(0, 0.05) factors per material and group) in one server pool:
-    each kernel of an iteration is one launch over every instance.  Each
-    instance runs `iters` eigenvalue iterations; the rate counts the pool's
-    device time (CUDA events around every block) and the wall time from the
-    first submission (uploads included) to the last result."""
-    from openmoc_gb300 import lattice
+    lognormal(0, 0.05) factors per material and group), `iters` eigenvalue
+    iterations each, two ways: as one solve of the instances side by side
+    (moc_set_instances: every sweep carries all instances' groups along each
+    track, read once; device time of the timed iterations, CUDA events) and
+    in one server pool (each instance its own copy of the tracks; the pool's
+    device time).  Both against one instance alone (its sweep time x the
+    instance count)."""
+    from openmoc_gb300 import GB300Solver, instances, lattice
     from openmoc_gb300.serving import Server, pool_capacity
+    from openmoc_gb300.solver import FISSION_SOURCE
     n = args.batch
+    sets = []
     insts = []
     for i in range(n):
         mats = lattice._fuel_mod(0, p.num_groups, 1, perturb=(7000 + i, 0.05))
-        insts.append(p.with_xs(*lattice.pack_materials(mats)))
+        sets.append(lattice.pack_materials(mats))
+        insts.append(p.with_xs(*sets[-1]))
+    ints_one = p.integrations_per_sweep
+    out = {"instances": n, "iterations_each": iters}
+    # one instance alone
+    s = GB300Solver(insts[0])
+    s.setConvergenceThreshold(1e-30)
+    s.computeEigenvalue(3, FISSION_SOURCE)
+    st, sw = s.benchIterations(iters, FISSION_SOURCE, True)
+    s.close()
+    out["alone"] = {"ms_per_iteration": float(np.mean(st)),
+                    "integrations_per_s": ints_one / (float(np.mean(st)) * 1e-3)}
+    # side by side: one solve of n instances
+    wide = instances(p, sets)
+    s = GB300Solver(wide)
+    s.setInstances(n)
+    s.setConvergenceThreshold(1e-30)
+    lps, slots, kind = s.autotune()
+    s.computeEigenvalue(3, FISSION_SOURCE)
+    st, sw = s.benchIterations(iters, FISSION_SOURCE, True)
+    s.setConvergenceThreshold(1e-30)
+    s.computeEigenvalue(iters, FISSION_SOURCE)
+    keffs = s.getInstanceKeffs().tolist()
+    s.close()
+    t_wide = float(np.mean(st))
+    out["side_by_side"] = {
+        "ms_per_iteration": t_wide, "sweep_ms_per_iteration": float(np.mean(sw)),
+        "integrations_per_s": n * ints_one / (t_wide * 1e-3),
+        "speedup_vs_alone_one_by_one": n * out["alone"]["ms_per_iteration"] / t_wide,
+        "sweep_shape": [lps, slots], "keff": keffs}
+    # one server pool
     srv = Server(iterations_per_poll=iters)
     srv.add_pool(p.num_groups, p.num_polar_half, **pool_capacity(insts, n))
     t0 = time.perf_counter()
@@ -680,13 +714,13 @@ def run_instances(p, args, iters=10):
     st = srv.stats()
     pool = srv.pool_stats(0)
     srv.close()
-    total = sum(r["iterations"] for r in res) * p.integrations_per_sweep
-    return {"instances": n, "iterations_each": iters,
-            "integrations_per_s_device": total / st["gpu_busy_s"],
-            "integrations_per_s_wall": total / wall,
-            "device_s": st["gpu_busy_s"], "wall_s": wall,
-            "sweep_shape": [pool["lanes"], pool["pairs"]],
-            "keff": [r["keff"] for r in res]}
+    total = sum(r["iterations"] for r in res) * ints_one
+    out["pool"] = {"integrations_per_s_device": total / st["gpu_busy_s"],
+                   "integrations_per_s_wall": total / wall,
+                   "device_s": st["gpu_busy_s"], "wall_s": wall,
+                   "sweep_shape": [pool["lanes"], pool["pairs"]],
+                   "keff": [r["keff"] for r in res]}
+    return out
 
 
 # ---------------------------------------------------------------- serving

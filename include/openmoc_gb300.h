@@ -345,6 +345,21 @@ int moc_stabilize_flux(moc_ctx* ctx);
 int moc_compute_fsr_fission_sources(moc_ctx* ctx);
 int moc_compute_fsr_scatter_sources(moc_ctx* ctx);
 
+/** No counterpart in the reference: instances.  The context's problem holds
+ *  num_instances cross-section sets over one track laydown, their groups
+ *  side by side (wide group k * G + g; the materials' arrays of
+ *  moc_upload_materials are [M][K*G] and the scattering matrix block
+ *  diagonal).  moc_compute_eigenvalue then solves them together: one sweep
+ *  per iteration carries every instance's groups along each track, while
+ *  sources, keff and the normalisation stay per instance (the solve stops
+ *  when the largest residual over the wide groups and every instance's keff
+ *  change meet the criterion).  num_instances = 0 returns to one problem.
+ *  Flat-source eigenvalue loop of stored segments only; the source
+ *  contraction runs on the CUDA cores. */
+int moc_set_instances(moc_ctx* ctx, int num_instances);
+/** Each instance's keff after moc_compute_eigenvalue. */
+int moc_get_instance_keffs(moc_ctx* ctx, double* keffs, int num_instances);
+
 /** Solver::setKeffFromNeutronBalance (src/Solver.cpp:2045-2048; used by
  *  CPUSolver::computeKeff and transferBoundaryFlux, src/CPUSolver.cpp:
  *  2258-2330, 2593-2600): on = 1 computes keff = fission / (absorption +

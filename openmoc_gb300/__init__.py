@@ -8,7 +8,7 @@ OpenMOC's Solver interface.
     solver.getKeff(), solver.getFlux(fsr, group)
 """
 from .cmfd import Cmfd  # noqa: F401
-from .problem import Problem, load_packed, save_packed  # noqa: F401
+from .problem import Problem, instances, load_packed, save_packed  # noqa: F401
 from .solver import (EXP_INTRINSIC, EXP_TABLE, FISSION_SOURCE,  # noqa: F401
                      SCALAR_FLUX, TOTAL_SOURCE, GB300LSSolver, GB300Solver)
 

@@ -137,6 +137,8 @@ _SIGS = {
     "moc_get_linear_expansion": ([_P, _P, _P], C.c_int),
     "moc_set_negative_fluxes_allowed": ([_P, C.c_int], C.c_int),
     "moc_set_keff_from_neutron_balance": ([_P, C.c_int], C.c_int),
+    "moc_set_instances": ([_P, C.c_int], C.c_int),
+    "moc_get_instance_keffs": ([_P, _P, C.c_int], C.c_int),
     "moc_set_transport_stabilization": ([_P, C.c_int, C.c_double, C.c_int], C.c_int),
     "moc_compute_stabilizing_flux": ([_P], C.c_int),
     "moc_stabilize_flux": ([_P], C.c_int),

@@ -178,6 +178,11 @@ struct moc_ctx {
   // from the host copies of sigma_t and the scattering diagonal and the
   // materials the FSRs use; the flux saved by the computeStabilizingFlux
   // hook
+  // instances (moc_set_instances): K cross-section sets over one laydown,
+  // inst_groups groups each; 0: one problem
+  int num_instances = 0;
+  int inst_groups = 0;
+  moc::InstState* inst = nullptr;
   int stab_on = 0;
   int stab_type = 0;
   double stab_factor = 0.0;
@@ -283,6 +288,19 @@ bool balance_keff(const moc_ctx* c) {
   return c->keff_balance && !c->ls && !c->otf && !c->cmfd;
 }
 
+// Instances: keff 1, no pending scale, empty accumulators.
+int reset_instances(moc_ctx* c) {
+  moc::InstState h{};
+  for (int k = 0; k < moc::kMaxInstances; k++) {
+    h.keff[k] = h.k_prev[k] = h.factor[k] = 1.0;
+    h.scale[0][k] = h.scale[1][k] = 1.0f;
+  }
+  MOC_CUDA(cudaMemcpyAsync(c->inst, &h, sizeof(h), cudaMemcpyHostToDevice,
+                           c->stream));
+  MOC_CUDA(cudaStreamSynchronize(c->stream));
+  return MOC_OK;
+}
+
 // The transport-stabilization coefficients (c1, c2) per material and group
 // (CPUSolver::computeStabilizingFlux / stabilizeFlux, src/CPUSolver.cpp:
 // 2665-2810), rebuilt after a material or FSR upload.
@@ -368,12 +386,17 @@ moc::SweepArgs sweep_args(moc_ctx* c, int check_done) {
     a.cm_nx = c->cmfd->cfg.nx;
   }
   if (balance_keff(c)) a.leakage = &c->sc->leakage;
+  if (c->num_instances) {
+    a.inst = c->inst;
+    a.inst_groups = c->inst_groups;
+  }
   return a;
 }
 
 // Whether computeFSRSources runs on the tensor cores.
 bool use_tc_sources(const moc_ctx* c) {
   if (!c->tc_b || !c->tc_rows || c->tc_tiles == 0) return false;
+  if (c->num_instances) return false;   // the per-instance fission is FP32
   if (c->source_kind == MOC_SOURCES_TF32X3) return true;
   return c->source_kind == MOC_SOURCES_AUTO && c->d.num_groups >= 70;
 }
@@ -416,6 +439,11 @@ moc::SolverArgs solver_args(moc_ctx* c, int check_done) {
   a.negative_ok = c->negative_ok;
   a.keff_balance = balance_keff(c) ? 1 : 0;
   a.stab = c->stab_on ? c->stab : nullptr;
+  if (c->num_instances) {
+    a.inst = c->inst;
+    a.inst_groups = c->inst_groups;
+    a.num_instances = c->num_instances;
+  }
   if (c->ls) {
     a.mom = c->mom;
     a.qxy = c->qxy;
@@ -721,6 +749,37 @@ int zero_track_fluxes(moc_ctx* c) {
   return MOC_OK;
 }
 
+// addSourceToScalarFlux, computeKeff, stabilizeFlux and the normalisation
+// factor of an eigenvalue iteration (the residual kernel then normalises).
+void enqueue_eigen_update(moc_ctx* c, const moc::SolverArgs& a) {
+  if (c->stab_on) {
+    // keff first; the stabilized flux sets the normalisation
+    enqueue_add_source(c, a, 2);
+    moc::launch_stabilize(a, c->phi_old, 1, c->stream);
+    c->launches++;
+  } else if (c->num_instances) {
+    // each instance's keff and normalisation
+    enqueue_add_source(c, a, 0);
+    moc::launch_instance_rates(a, 0, c->stream);
+    c->launches++;
+  } else {
+    enqueue_add_source(c, a, 1);
+  }
+}
+
+// The starting flux of an eigenvalue solve: flat, normalised (per instance
+// with instances).
+void enqueue_initial_guess(moc_ctx* c, const moc::SolverArgs& a) {
+  moc::launch_fill(c->phi, num_flux(c), 1.0f, c->stream);
+  if (c->num_instances) {
+    moc::launch_instance_rates(a, 1, c->stream);
+  } else {
+    moc::launch_fission_rate(a, 1, c->stream);
+    moc::launch_scale_phi(a, c->stream);
+  }
+  c->launches += 3;
+}
+
 // The device loop: iterations of `kind` until the device reports done.
 int run_iterations(moc_ctx* c, int kind, int res_type) {
   MOC_TRY(ensure_stab(c));
@@ -735,14 +794,10 @@ int run_iterations(moc_ctx* c, int kind, int res_type) {
         enqueue_sources(c, a, -1, 1);
       }
       MOC_TRY(enqueue_sweep(c, 1, true, i));
-      if (kind == moc::kModeEigen && c->stab_on) {
-        // keff first; the stabilized flux sets the normalisation
-        enqueue_add_source(c, a, 2);
-        moc::launch_stabilize(a, c->phi_old, 1, c->stream);
-        c->launches++;
-      } else {
-        enqueue_add_source(c, a, kind == moc::kModeEigen ? 1 : 0);
-      }
+      if (kind == moc::kModeEigen)
+        enqueue_eigen_update(c, a);
+      else
+        enqueue_add_source(c, a, 0);
       moc::launch_residual(a, res_type, kind == moc::kModeEigen ? 1 : 0, 1, 1,
                            c->stream);
       c->launches++;
@@ -1294,6 +1349,7 @@ int moc_destroy(moc_ctx* c) {
   dfree(c->tc_b);
   dfree(c->stab);
   dfree(c->stab_base);
+  dfree(c->inst);
   dfree(c->segs_ls);
   dfree(c->ls_ang);
   dfree(c->ls_dir);
@@ -1772,6 +1828,12 @@ int moc_compute_eigenvalue(moc_ctx* c, int max_iters, int res_type) {
             "without fissionable FSRs");
   MOC_CHECK(c->num_fissionable > 0, MOC_ERR_ARG,
             "an eigenvalue solve needs fissionable material");
+  MOC_CHECK(!c->num_instances || !(c->ls || c->otf || c->cmfd || c->stab_on ||
+                                   c->keff_balance),
+            MOC_ERR_UNSUPPORTED,
+            "instances are built for the flat-source eigenvalue loop of stored "
+            "segments (no linear source, on-the-fly segments, CMFD, "
+            "stabilization or neutron-balance keff)");
   if (c->cmfd) {
     MOC_CHECK(!c->otf, MOC_ERR_UNSUPPORTED,
               "CMFD acceleration of an on-the-fly solve is not supported");
@@ -1782,12 +1844,10 @@ int moc_compute_eigenvalue(moc_ctx* c, int max_iters, int res_type) {
   // zero boundary fluxes (src/Solver.cpp:1710-1757)
   MOC_TRY(zero_track_fluxes(c));
   MOC_TRY(begin_solve(c, moc::kModeEigen, max_iters, res_type, 1.0));
+  if (c->num_instances) MOC_TRY(reset_instances(c));
   moc::SolverArgs a = solver_args(c, 0);
-  moc::launch_fill(c->phi, num_flux(c), 1.0f, c->stream);
+  enqueue_initial_guess(c, a);
   MOC_TRY(zero_moments(c));
-  moc::launch_fission_rate(a, 1, c->stream);
-  moc::launch_scale_phi(a, c->stream);
-  c->launches += 3;
   MOC_CUDA(cudaMemcpyAsync(c->phi_old, c->phi, 4 * num_flux(c),
                            cudaMemcpyDeviceToDevice, c->stream));
   MOC_CUDA(cudaGetLastError());
@@ -1802,6 +1862,8 @@ int moc_compute_eigenvalue(moc_ctx* c, int max_iters, int res_type) {
 int moc_compute_source(moc_ctx* c, int max_iters, double k_eff,
                        int res_type) {
   MOC_TRY(ready(c));
+  MOC_CHECK(!c->num_instances, MOC_ERR_UNSUPPORTED,
+            "instances are solved by moc_compute_eigenvalue only");
   MOC_CHECK(max_iters >= 1, MOC_ERR_ARG, "max_iters must be positive");
   MOC_CHECK(k_eff > 0.0, MOC_ERR_ARG,
             "The Solver is unable to compute the source with a non-positive "
@@ -1823,6 +1885,8 @@ int moc_compute_source(moc_ctx* c, int max_iters, double k_eff,
 
 int moc_compute_flux(moc_ctx* c, int max_iters, int only_fixed_source) {
   MOC_TRY(ready(c));
+  MOC_CHECK(!c->num_instances, MOC_ERR_UNSUPPORTED,
+            "instances are solved by moc_compute_eigenvalue only");
   MOC_CHECK(max_iters >= 1, MOC_ERR_ARG, "max_iters must be positive");
   MOC_CHECK(only_fixed_source, MOC_ERR_UNSUPPORTED,
             "computeFlux without only_fixed_source needs a previous "
@@ -1865,11 +1929,11 @@ int moc_bench_iterations(moc_ctx* c, int steps, int res_type, int flush_l2,
   MOC_TRY(begin_solve(c, moc::kModeEigen, 1 << 30, res_type, 1.0));
   c->hsc->threshold = -1.0;  // never converged: every iteration runs
   MOC_TRY(push(c));
+  if (c->num_instances) MOC_TRY(reset_instances(c));
+  MOC_TRY(ensure_stab(c));
   moc::SolverArgs a = solver_args(c, 1);
-  moc::launch_fill(c->phi, num_flux(c), 1.0f, c->stream);
+  enqueue_initial_guess(c, a);
   MOC_TRY(zero_moments(c));
-  moc::launch_fission_rate(a, 1, c->stream);
-  moc::launch_scale_phi(a, c->stream);
   MOC_CUDA(cudaMemcpyAsync(c->phi_old, c->phi, 4 * num_flux(c),
                            cudaMemcpyDeviceToDevice, c->stream));
   std::vector<cudaEvent_t> ev(4 * steps);
@@ -1881,7 +1945,7 @@ int moc_bench_iterations(moc_ctx* c, int steps, int res_type, int flush_l2,
     MOC_CUDA(cudaEventRecord(ev[4 * i + 1], c->stream));
     MOC_TRY(enqueue_sweep(c, 1, false, 0));
     MOC_CUDA(cudaEventRecord(ev[4 * i + 2], c->stream));
-    enqueue_add_source(c, a, 1);
+    enqueue_eigen_update(c, a);
     moc::launch_residual(a, res_type, 1, 1, 1, c->stream);
     MOC_CUDA(cudaEventRecord(ev[4 * i + 3], c->stream));
     c->launches++;
@@ -2112,6 +2176,8 @@ int moc_store_fsr_fluxes(moc_ctx* c) {
 
 int moc_normalize_fluxes(moc_ctx* c, double* factor) {
   MOC_TRY(ready(c));
+  MOC_CHECK(!c->num_instances, MOC_ERR_UNSUPPORTED,
+            "instances are solved by moc_compute_eigenvalue only");
   moc::SolverArgs a = solver_args(c, 0);
   moc::launch_fission_rate(a, 1, c->stream);
   moc::launch_scale_phi(a, c->stream);
@@ -2158,6 +2224,8 @@ int moc_add_source_to_scalar_flux(moc_ctx* c) {
 
 int moc_compute_keff(moc_ctx* c) {
   MOC_TRY(ready(c));
+  MOC_CHECK(!c->num_instances, MOC_ERR_UNSUPPORTED,
+            "instances are solved by moc_compute_eigenvalue only");
   moc::SolverArgs a = solver_args(c, 0);
   moc::launch_fission_rate(a, 0, c->stream);
   c->launches++;
@@ -2398,6 +2466,36 @@ int moc_compute_fsr_scatter_sources(moc_ctx* c) {
   moc::launch_partial_sources(a, 1, c->stream);
   c->launches++;
   MOC_CUDA(cudaGetLastError());
+  return MOC_OK;
+}
+
+int moc_set_instances(moc_ctx* c, int num_instances) {
+  MOC_CHECK(c, MOC_ERR_ARG, "null context");
+  if (num_instances == 0) {
+    c->num_instances = 0;
+    c->inst_groups = 0;
+    return MOC_OK;
+  }
+  MOC_CHECK(num_instances >= 1 && num_instances <= moc::kMaxInstances,
+            MOC_ERR_ARG, "1 to 16 instances");
+  MOC_CHECK(c->d.num_groups % num_instances == 0, MOC_ERR_ARG,
+            "the problem's groups must be the instances' groups side by side "
+            "(num_groups a multiple of the instance count)");
+  if (!c->inst) MOC_TRY(dalloc(&c->inst, 1));
+  c->num_instances = num_instances;
+  c->inst_groups = c->d.num_groups / num_instances;
+  return reset_instances(c);
+}
+
+int moc_get_instance_keffs(moc_ctx* c, double* keffs, int num_instances) {
+  MOC_CHECK(c && keffs, MOC_ERR_ARG, "null argument");
+  MOC_CHECK(c->num_instances > 0 && num_instances == c->num_instances,
+            MOC_ERR_ARG, "num_instances must be the context's instance count");
+  moc::InstState h;
+  MOC_CUDA(cudaMemcpyAsync(&h, c->inst, sizeof(h), cudaMemcpyDeviceToHost,
+                           c->stream));
+  MOC_CUDA(cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < num_instances; k++) keffs[k] = h.keff[k];
   return MOC_OK;
 }
 

@@ -62,6 +62,21 @@ struct DevScalars {
 
 enum SolveMode { kModeEigen = 0, kModeSource = 1, kModeFlux = 2, kModeHook = 3 };
 
+// Instances: K cross-section sets solved together over one track laydown.
+// The problem's groups are the K instances' groups side by side (wide group
+// k * G + g); the sweep treats them as one wide group set, while sources,
+// keff and the normalisation stay per instance.
+constexpr int kMaxInstances = 16;
+struct InstState {
+  double keff[kMaxInstances];
+  double k_prev[kMaxInstances];
+  double factor[kMaxInstances];
+  double accum[kMaxInstances];       // fission-rate accumulators
+  float scale[2][kMaxInstances];     // pending angular-flux scale per buffer
+  unsigned int ticket;
+  int dk;                            // largest |1e5 (k - k_prev)| this iteration
+};
+
 struct SweepArgs {
   const int2* segs;          // [S] {float length bits, fsr}
   const int64_t* seg_off;    // [T+1]
@@ -117,6 +132,10 @@ struct SweepArgs {
   int cm_nx;
   // keff from the neutron balance: the leakage tally (null: not tallied)
   double* leakage;
+  // instances (null: one problem): each wide group's angular flux takes the
+  // pending scale of its instance, group / inst_groups
+  InstState* inst;
+  int inst_groups;
 };
 
 constexpr int kMaxHotFsrs = 8;
@@ -180,6 +199,11 @@ struct SolverArgs {
   // (c1, c2) of phi = (phi + c1 * phi_start) * c2, phi_start the flux at
   // the start of the iteration
   const float2* stab;        // [M][ld]
+  // instances (null: one problem): per-instance keff, normalisation and
+  // angular-flux scales; inst_groups groups per instance
+  InstState* inst;
+  int inst_groups;
+  int num_instances;
 };
 
 // Rows (FSRs) per tile of the tensor-core source kernel: the MMA's M.
@@ -235,6 +259,10 @@ void launch_stabilize(const SolverArgs& a, const float* base, int in_loop,
 // source alone into qt (CPUSolver::computeFSRFissionSources /
 // computeFSRScatterSources)
 void launch_partial_sources(const SolverArgs& a, int which, cudaStream_t s);
+// instances: each instance's fission-rate total; what = 0: the eigenvalue
+// update (keff, normalisation factor, angular-flux scale, largest dk);
+// what = 1: the normalisation of the starting flux (phi scaled in place)
+void launch_instance_rates(const SolverArgs& a, int what, cudaStream_t s);
 void launch_scale_phi(const SolverArgs& a, cudaStream_t s);
 void launch_zero_phi(const SolverArgs& a, cudaStream_t s);
 void launch_fill(float* p, int64_t n, float v, cudaStream_t s);

@@ -114,6 +114,52 @@ __device__ __forceinline__ int64_t row_step() {
 }
 
 // ---------------------------------------------------------------- sources
+// Instances (a.inst set): for each of the lane's destination groups, the
+// fission rate of its own instance (the groups [k G_i, (k+1) G_i)) times
+// that instance's 1 / keff.  A segmented inclusive scan of nu_sigma_f * phi
+// over each instance's groups by shuffles, the instance's total read at its
+// last group; only the instance's own terms enter its sum.
+template <int S>
+__device__ __forceinline__ void instance_fission(const SolverArgs& a,
+                                                 const float* nf,
+                                                 const float (&ph)[S],
+                                                 bool fissile,
+                                                 const float* s_ik,
+                                                 float (&out)[S]) {
+  const int G = a.num_groups, ig = a.inst_groups;
+  const int lane = threadIdx.x & 31;
+  float scan[S];
+  float carry = 0.0f;
+#pragma unroll
+  for (int j = 0; j < S; j++) {
+    const int g = lane + 32 * j;
+    float v = (fissile && g < G) ? nf[g] * ph[j] : 0.0f;
+    const int start = (g / ig) * ig;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const float t = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o && g - o >= start) v += t;
+    }
+    // the instance that runs across the chunk boundary carries on
+    if (start < 32 * j) v += carry;
+    scan[j] = v;
+    carry = __shfl_sync(0xffffffffu, v, 31);
+  }
+#pragma unroll
+  for (int j = 0; j < S; j++) {
+    const int g = lane + 32 * j;
+    const int k = min(g, G - 1) / ig;
+    const int last = min((k + 1) * ig, G) - 1;
+    float tot = 0.0f;
+#pragma unroll
+    for (int jj = 0; jj < S; jj++) {
+      const float t = __shfl_sync(0xffffffffu, scan[jj], last & 31);
+      if (jj == (last >> 5)) tot = t;
+    }
+    out[j] = tot * s_ik[k];
+  }
+}
+
 // One warp per FSR: the flux row sits in registers (lane l holds groups
 // l, l+32, ...) and is broadcast group by group with shuffles; the
 // transposed scattering matrices of all materials ([m][orig][dest]) are
@@ -129,11 +175,12 @@ __device__ __forceinline__ void source_rows(const SolverArgs& a,
                                             int on_mask, int zero_phi,
                                             int it0, int it1, float ik0,
                                             float ik1,
-                                            unsigned long long& negatives) {
+                                            unsigned long long& negatives,
+                                            const float* s_ik = nullptr) {
   const int G = a.num_groups;
   const int GG = G * G;
   const int lane = threadIdx.x & 31;
-  float ph[2][S], acc[2][S], fr[2];
+  float ph[2][S], acc[2][S], fr[2], fi[2][S];
   const float* mT[2];
   int mat[2];
 #pragma unroll
@@ -162,6 +209,10 @@ __device__ __forceinline__ void source_rows(const SolverArgs& a,
         if (lane + 32 * j < G) fr[i] = fmaf(nf[lane + 32 * j], ph[i][j], fr[i]);
     }
     fr[i] = warp_sum_all(fr[i]);
+    if (s_ik) {
+      const float* nf = a.nu_sigma_f + (int64_t) mat[i] * G;
+      instance_fission<S>(a, nf, ph[i], on && a.fissile[mat[i]], s_ik, fi[i]);
+    }
     mT[i] = ssT + (int64_t) mat[i] * GG + lane;
   }
 #pragma unroll
@@ -193,7 +244,7 @@ __device__ __forceinline__ void source_rows(const SolverArgs& a,
     for (int j = 0; j < S; j++) {
       const int gd = lane + 32 * j;
       if (gd >= G) continue;
-      float q = chi[gd] * fk;
+      float q = chi[gd] * (s_ik ? fi[i][j] : fk);
       q += acc[i][j];
       if (a.fixed) q += a.fixed[r * a.ld + gd];
       q *= (float) kOneOverFourPi;
@@ -224,6 +275,16 @@ compute_sources_kernel(const SolverArgs a, int iteration, int zero_phi,
   const float* ssT =
       staged ? reinterpret_cast<const float*>(s_ss4) : a.sigma_s_T;
   const float inv_k1 = a.row_slot ? 0.0f : (float) (1.0 / a.sc->keff);
+  // instances: each instance's 1 / keff
+  __shared__ float s_ik[kMaxInstances];
+  const bool inst = a.inst && !a.row_slot;
+  if (inst) {
+    if (threadIdx.x < kMaxInstances)
+      s_ik[threadIdx.x] = threadIdx.x < a.num_instances
+                              ? (float) (1.0 / a.inst->keff[threadIdx.x])
+                              : 0.0f;
+    __syncthreads();
+  }
   // iteration < 0: the device iteration counter of the running solve
   if (iteration < 0 && !a.row_slot) iteration = a.sc->iteration;
   unsigned long long negatives = 0;
@@ -268,7 +329,8 @@ compute_sources_kernel(const SolverArgs a, int iteration, int zero_phi,
       ik0 = __shfl_sync(0xffffffffu, ik0, 0);
       ik1 = __shfl_sync(0xffffffffu, ik1, 0);
     }
-    source_rows<S>(a, ssT, r, on, zero_phi, it0, it1, ik0, ik1, negatives);
+    source_rows<S>(a, ssT, r, on, zero_phi, it0, it1, ik0, ik1, negatives,
+                   inst ? s_ik : nullptr);
   }
   if (negatives) atomicAdd(&a.sc->neg_sources, negatives);
 }
@@ -400,7 +462,8 @@ residual_kernel(const SolverArgs a, int normalise, int store, int finish) {
       if (g >= G) continue;
       float v = vv[j];
       if (normalise) {
-        v *= factor;
+        // instances: each group takes its own instance's factor
+        v *= a.inst ? (float) a.inst->factor[g / a.inst_groups] : factor;
         phi[g] = v;
       }
       const float o = oo[j];
@@ -448,7 +511,9 @@ residual_kernel(const SolverArgs a, int normalise, int store, int finish) {
     if (finish) {
       const int i = sc->iteration;
       if (sc->mode == kModeEigen) {
-        const int dk = (int) (1e5 * (sc->keff - sc->k_prev));
+        // instances: the largest change of the instances' keff
+        const int dk =
+            a.inst ? a.inst->dk : (int) (1e5 * (sc->keff - sc->k_prev));
         sc->dk = dk;
         sc->k_prev = sc->keff;
         sc->iteration = i + 1;
@@ -566,6 +631,90 @@ stabilize_kernel(const SolverArgs a, const float* base, int in_loop) {
     sc->accum_rate = 0.0;
     sc->ticket_rate = 0;
     __threadfence();
+  }
+}
+
+// ------------------------------------------------------------- instances
+// Each instance's fission-rate total sum_r V_r sum over its groups of
+// nu_sigma_f phi: per row and instance a warp sum, lane k keeping instance
+// k's running total; per block through shared memory, one FP64 atomic per
+// instance and block.  The last block finishes: what = 0, the eigenvalue
+// update of every instance (keff *= total / R, factor = R / total, the
+// pending angular-flux scale, the largest keff change in 1e-5 units, the
+// first instance's keff as the solve's); what = 1, the factors alone (the
+// starting flux is then scaled by instance_scale_phi_kernel).
+__global__ void __launch_bounds__(kRowThreads)
+instance_rates_kernel(const SolverArgs a, int what) {
+  if (skip(a)) return;
+  InstState* in = a.inst;
+  const int G = a.num_groups, ig = a.inst_groups, K = a.num_instances;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double mine = 0.0;   // lane k: instance k
+  for (int64_t r = first_row(); r < a.num_fsrs; r += row_step()) {
+    const int m = a.fsr_mat[r];
+    if (!a.fissile[m]) continue;
+    const float* nf = a.nu_sigma_f + (int64_t) m * G;
+    const float* phi = a.phi + r * a.ld;
+    const double vol = (double) a.fsr_vol[r];
+    for (int k = 0; k < K; k++) {
+      double p = 0.0;
+      for (int g = k * ig + lane; g < (k + 1) * ig; g += 32)
+        p += (double) (nf[g] * phi[g]);
+      p = warp_sum_all_d(p);
+      if (lane == k) mine += p * vol;
+    }
+  }
+  __shared__ double part[kRowThreads / 32][kMaxInstances];
+  __shared__ int last;
+  if (lane < kMaxInstances) part[warp][lane] = lane < K ? mine : 0.0;
+  __syncthreads();
+  if (threadIdx.x < K) {
+    double t = 0.0;
+    for (int w = 0; w < kRowThreads / 32; w++) t += part[w][threadIdx.x];
+    atomicAdd(&in->accum[threadIdx.x], t);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(&in->ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  __shared__ int s_dk[kMaxInstances];
+  const double R = (double) a.num_fsrs;
+  if (threadIdx.x < K) {
+    const int k = threadIdx.x;
+    const double total = *(volatile double*) &in->accum[k];
+    in->accum[k] = 0.0;
+    in->factor[k] = R / total;
+    if (what == 0) {
+      in->keff[k] = in->keff[k] * (total / R);
+      in->scale[a.sc->cur][k] *= (float) in->factor[k];
+      s_dk[k] = abs((int) (1e5 * (in->keff[k] - in->k_prev[k])));
+      in->k_prev[k] = in->keff[k];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (what == 0) {
+      int dk = 0;
+      for (int k = 0; k < K; k++) dk = max(dk, s_dk[k]);
+      in->dk = dk;
+      a.sc->keff = in->keff[0];
+    }
+    in->ticket = 0;
+    __threadfence();
+  }
+}
+
+__global__ void instance_scale_phi_kernel(const SolverArgs a) {
+  const int64_t n = a.num_fsrs * a.ld;
+  for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t) gridDim.x * blockDim.x) {
+    const int g = (int) (i % a.ld);
+    if (g < a.num_groups)
+      a.phi[i] = (float) ((double) a.phi[i] * a.inst->factor[g / a.inst_groups]);
   }
 }
 
@@ -1245,6 +1394,13 @@ void launch_stabilize(const SolverArgs& a, const float* base, int in_loop,
                       cudaStream_t s) {
   stabilize_kernel<<<row_grid(a.num_fsrs), kRowThreads, 0, s>>>(a, base,
                                                                in_loop);
+}
+
+void launch_instance_rates(const SolverArgs& a, int what, cudaStream_t s) {
+  instance_rates_kernel<<<row_grid(a.num_fsrs), kRowThreads, 0, s>>>(a, what);
+  if (what == 1)
+    instance_scale_phi_kernel<<<grid_for(a.num_fsrs * a.ld, kThreads), kThreads,
+                                0, s>>>(a);
 }
 
 void launch_partial_sources(const SolverArgs& a, int which, cudaStream_t s) {

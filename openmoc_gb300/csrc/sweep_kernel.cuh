@@ -306,10 +306,16 @@ sweep_kernel(const SweepArgs a) {
 #pragma unroll
     for (int s = 0; s < PS; s++) {
       const int g0 = 2 * (sub + s * LPS);
+      // with instances each group takes its own instance's pending scale
+      float sx = scale, sy = scale;
+      if (!POOL && a.inst && g0 < G) {
+        sx = a.inst->scale[cur][g0 / a.inst_groups];
+        if (g0 + 1 < G) sy = a.inst->scale[cur][(g0 + 1) / a.inst_groups];
+      }
 #pragma unroll
       for (int p = 0; p < PH; p++) {
-        psi[s][p].x = (g0 < G) ? pin[p * G + g0] * scale : 0.0f;
-        psi[s][p].y = (g0 + 1 < G) ? pin[p * G + g0 + 1] * scale : 0.0f;
+        psi[s][p].x = (g0 < G) ? pin[p * G + g0] * sx : 0.0f;
+        psi[s][p].y = (g0 + 1 < G) ? pin[p * G + g0 + 1] * sy : 0.0f;
       }
     }
 
@@ -550,6 +556,9 @@ sweep_kernel(const SweepArgs a) {
     if (POOL)
       for (int i = threadIdx.x; i < a.num_slots; i += blockDim.x)
         a.slots[i].scale[cur ^ 1] = 1.0f;
+    if (!POOL && a.inst)
+      for (int i = threadIdx.x; i < kMaxInstances; i += blockDim.x)
+        a.inst->scale[cur ^ 1][i] = 1.0f;
     if (threadIdx.x == 0) {
       sc->ticket_sweep = 0;
       sc->scale[cur ^ 1] = 1.0f;

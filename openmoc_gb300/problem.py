@@ -204,6 +204,33 @@ class Problem:
         return p
 
 
+def instances(problem: Problem, xs_sets) -> Problem:
+    """One problem holding K cross-section sets over ``problem``'s tracks
+    and FSRs, for ``GB300Solver.setInstances(K)``: the groups of the K sets
+    side by side (wide group k * G + g), the scattering matrix block
+    diagonal.  ``xs_sets`` is a list of (sigma_t, sigma_s, nu_sigma_f, chi)
+    in the layout of ``Problem`` (the same materials, G groups each), e.g.
+    from ``lattice.pack_materials``."""
+    K = len(xs_sets)
+    M = problem.num_materials
+    st0 = np.asarray(xs_sets[0][0], np.float32).reshape(M, -1)
+    G = st0.shape[1]
+    W = K * G
+    st = np.zeros((M, W), np.float32)
+    nf = np.zeros((M, W), np.float32)
+    ch = np.zeros((M, W), np.float32)
+    ss = np.zeros((M, W, W), np.float32)
+    for k, (a, b, c, d) in enumerate(xs_sets):
+        sl = slice(k * G, (k + 1) * G)
+        st[:, sl] = np.asarray(a, np.float32).reshape(M, G)
+        ss[:, sl, sl] = np.asarray(b, np.float32).reshape(M, G, G)
+        nf[:, sl] = np.asarray(c, np.float32).reshape(M, G)
+        ch[:, sl] = np.asarray(d, np.float32).reshape(M, G)
+    wide = problem.with_xs(st, ss, nf, ch)
+    wide.meta = dict(problem.meta, instances=K, instance_groups=G)
+    return wide
+
+
 def load_packed(base: str) -> Tuple[Problem, Dict[str, float], Dict[str, np.ndarray]]:
     """Reads ``<base>.json`` + ``<base>.bin`` (the format written by
     tests/golden/make_fixtures.cpp).  Returns the problem, the scalar

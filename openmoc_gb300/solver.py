@@ -61,6 +61,7 @@ class GB300Solver:
         self._negative_ok = False
         self._keff_balance = False
         self._stabilization = None
+        self._instances = 0
         self._formation = "explicit"
         self._cmfd = None
         self._cmfd_keep = None
@@ -129,6 +130,8 @@ class GB300Solver:
             self._call("moc_set_keff_from_neutron_balance", 1)
         if self._stabilization is not None:
             self._call("moc_set_transport_stabilization", 1, *self._stabilization)
+        if self._instances:
+            self._call("moc_set_instances", self._instances)
         if self._formation == "otf":
             self._set_otf()
         if self._cmfd is not None:
@@ -244,6 +247,28 @@ class GB300Solver:
         self._keff_balance = True
         if self._ctx is not None:
             self._call("moc_set_keff_from_neutron_balance", 1)
+
+    def setInstances(self, num_instances: int) -> None:
+        """Solves the problem's groups as ``num_instances`` cross-section
+        sets side by side (a problem made by ``problem.instances``): one
+        sweep per iteration for all of them, sources, keff and the
+        normalisation per instance.  No counterpart in OpenMOC."""
+        self._instances = int(num_instances)
+        if self._ctx is not None:
+            self._call("moc_set_instances", self._instances)
+
+    def getInstanceKeffs(self) -> np.ndarray:
+        self._need_ctx()
+        k = np.zeros(self._instances, np.float64)
+        self._call("moc_get_instance_keffs", _ptr(k), self._instances)
+        return k
+
+    def getInstanceFluxes(self) -> np.ndarray:
+        """[instances, R, G] scalar fluxes."""
+        f = self.getFluxes()
+        K = self._instances
+        return np.ascontiguousarray(
+            f.reshape(f.shape[0], K, -1).transpose(1, 0, 2))
 
     _STABILIZATION = {"DIAGONAL": 0, "YAMAMOTO": 1, "GLOBAL": 2}
 
