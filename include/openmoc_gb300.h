@@ -245,6 +245,12 @@ int moc_bench_iterations(moc_ctx* ctx, int steps, int res_type, int flush_l2,
 int moc_eval_attenuation(moc_ctx* ctx, int kind, const float* x, float* g,
                          int64_t n);
 
+/** No counterpart in the reference.  Contexts keep the device memory they
+ *  free (up to 16 GiB), so that a context created and destroyed per request
+ *  reuses it without cudaMalloc / cudaFree; this returns all of it to the
+ *  driver.  Call it with no context in use. */
+int moc_release_cached_memory(void);
+
 /** Largest num_fsrs that moc_fission_source_total_noalloc accepts. */
 #define MOC_NOALLOC_MAX_FSRS (1 << 19)
 

@@ -76,6 +76,7 @@ _P = C.c_void_p
 _SIGS = {
     "moc_last_error": ([], C.c_char_p),
     "moc_version": ([], C.c_char_p),
+    "moc_release_cached_memory": ([], C.c_int),
     "moc_create": ([C.POINTER(Dims), C.POINTER(C.c_void_p)], C.c_int),
     "moc_destroy": ([_P], C.c_int),
     "moc_upload_tracks": ([_P, _P, _P, _P, _P, _P, _P], C.c_int),

@@ -50,24 +50,117 @@ int fail(int code, const std::string& msg) {
     if (s_ != MOC_OK) return s_; \
   } while (0)
 
+// Device memory of the contexts is kept for reuse.  A context created,
+// solved and destroyed per request (the end-to-end path) gets its buffers
+// back from this cache instead of from cudaMalloc / cudaFree, whose driver
+// work and implicit device synchronisation cost about a millisecond per
+// context.  A block goes back to the cache only when no work can still use
+// it: dfree synchronises the device first, as cudaFree would, unless the
+// caller has (moc_destroy, after its stream).  At most kMaxIdleBytes stay
+// cached; moc_release_cached_memory returns them to the driver.
+struct DeviceBlockCache {
+  std::mutex mu;
+  std::map<void*, std::pair<int, size_t>> live;       // block -> device, bytes
+  std::multimap<std::pair<int, size_t>, void*> idle;  // (device, bytes) -> block
+  size_t idle_bytes = 0;
+};
+DeviceBlockCache g_blocks;
+constexpr size_t kMaxIdleBytes = size_t(16) << 30;
+thread_local bool g_device_idle = false;   // set while moc_destroy frees
+// pinned host copies of the device scalars, kept likewise
+std::mutex g_pinned_mu;
+std::vector<void*> g_pinned_scalars;
+
+// Frees every idle block of `device` (all devices: -1).
+void release_idle(int device) {
+  std::lock_guard<std::mutex> lk(g_blocks.mu);
+  for (auto it = g_blocks.idle.begin(); it != g_blocks.idle.end();) {
+    if (device >= 0 && it->first.first != device) {
+      ++it;
+      continue;
+    }
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(it->first.first);
+    cudaFree(it->second);
+    cudaSetDevice(cur);
+    g_blocks.idle_bytes -= it->first.second;
+    it = g_blocks.idle.erase(it);
+  }
+}
+
+size_t idle_bytes_on(int device) {
+  std::lock_guard<std::mutex> lk(g_blocks.mu);
+  size_t n = 0;
+  for (const auto& kv : g_blocks.idle)
+    if (kv.first.first == device) n += kv.first.second;
+  return n;
+}
+
 template <typename T>
 int dalloc(T** p, size_t n) {
   *p = nullptr;
   if (n == 0) n = 1;
-  cudaError_t e = cudaMalloc((void**) p, n * sizeof(T));
+  const size_t bytes = (n * sizeof(T) + 255) & ~(size_t) 255;
+  int dev = 0;
+  MOC_CUDA(cudaGetDevice(&dev));
+  {
+    // an idle block of this device at most twice the size
+    std::lock_guard<std::mutex> lk(g_blocks.mu);
+    auto it = g_blocks.idle.lower_bound({dev, bytes});
+    if (it != g_blocks.idle.end() && it->first.first == dev &&
+        it->first.second <= 2 * bytes) {
+      *p = static_cast<T*>(it->second);
+      g_blocks.live[it->second] = it->first;
+      g_blocks.idle_bytes -= it->first.second;
+      g_blocks.idle.erase(it);
+      return MOC_OK;
+    }
+  }
+  cudaError_t e = cudaMalloc((void**) p, bytes);
   if (e == cudaErrorMemoryAllocation) {
     cudaGetLastError();
+    release_idle(dev);
+    e = cudaMalloc((void**) p, bytes);
+  }
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    *p = nullptr;
     return fail(MOC_ERR_MEMORY, "device memory exhausted allocating " +
                                     std::to_string(n * sizeof(T)) + " bytes");
   }
   MOC_CUDA(e);
+  std::lock_guard<std::mutex> lk(g_blocks.mu);
+  g_blocks.live[(void*) *p] = {dev, bytes};
   return MOC_OK;
 }
 
 template <typename T>
 void dfree(T*& p) {
-  if (p) cudaFree((void*) p);
+  if (!p) return;
+  void* v = (void*) p;
   p = nullptr;
+  std::pair<int, size_t> blk{-1, 0};
+  {
+    std::lock_guard<std::mutex> lk(g_blocks.mu);
+    auto it = g_blocks.live.find(v);
+    if (it != g_blocks.live.end()) {
+      blk = it->second;
+      g_blocks.live.erase(it);
+    }
+  }
+  if (blk.first < 0 || blk.second > kMaxIdleBytes) {
+    cudaFree(v);
+    return;
+  }
+  if (!g_device_idle) cudaDeviceSynchronize();
+  std::lock_guard<std::mutex> lk(g_blocks.mu);
+  if (g_blocks.idle_bytes + blk.second > kMaxIdleBytes) {
+    cudaFree(v);
+    return;
+  }
+  g_blocks.idle.insert({blk, v});
+  g_blocks.idle_bytes += blk.second;
 }
 
 }  // namespace
@@ -1237,6 +1330,14 @@ const char* moc_last_error(void) { return g_error.c_str(); }
 
 const char* moc_version(void) { return "openmoc_gb300 0.1 (sm_103a)"; }
 
+int moc_release_cached_memory(void) {
+  release_idle(-1);
+  std::lock_guard<std::mutex> lk(g_pinned_mu);
+  for (void* h : g_pinned_scalars) cudaFreeHost(h);
+  g_pinned_scalars.clear();
+  return MOC_OK;
+}
+
 int moc_create(const moc_dims* dims, moc_ctx** out) {
   MOC_CHECK(dims != nullptr && out != nullptr, MOC_ERR_ARG, "null argument");
   *out = nullptr;
@@ -1277,7 +1378,8 @@ int moc_create(const moc_dims* dims, moc_ctx** out) {
                 (sizeof(int64_t) + 4 * sizeof(int32_t) + 1) *
                     (size_t) d.num_tracks;
   size_t free_b = 0, total_b = 0;
-  if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && need > free_b)
+  if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess &&
+      need > free_b + idle_bytes_on(d.device))
     return bail(fail(MOC_ERR_MEMORY,
                      "problem needs " + std::to_string(need) +
                          " bytes of device memory, " +
@@ -1288,8 +1390,15 @@ int moc_create(const moc_dims* dims, moc_ctx** out) {
       (st = dalloc(&c->exp_table, 2 * moc::kExpTableSize)) ||
       (st = dalloc(&c->rates, R)) || (st = dalloc(&c->sc, 1)))
     return bail(st);
-  if (cudaMallocHost((void**) &c->hsc, sizeof(moc::DevScalars)) !=
-      cudaSuccess)
+  {
+    std::lock_guard<std::mutex> lk(g_pinned_mu);
+    if (!g_pinned_scalars.empty()) {
+      c->hsc = static_cast<moc::DevScalars*>(g_pinned_scalars.back());
+      g_pinned_scalars.pop_back();
+    }
+  }
+  if (!c->hsc && cudaMallocHost((void**) &c->hsc, sizeof(moc::DevScalars)) !=
+                     cudaSuccess)
     return bail(fail(MOC_ERR_CUDA, "cudaMallocHost failed"));
   std::memset(c->hsc, 0, sizeof(moc::DevScalars));
   c->hsc->keff = 1.0;
@@ -1317,6 +1426,12 @@ int moc_destroy(moc_ctx* c) {
   if (!c) return MOC_OK;
   cudaSetDevice(c->d.device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  // nothing of this context runs any more: its blocks go back to the cache
+  // without a device synchronisation each
+  struct IdleScope {
+    IdleScope() { g_device_idle = true; }
+    ~IdleScope() { g_device_idle = false; }
+  } idle_scope;
   dfree(c->segs);
   dfree(c->seg_off);
   dfree(c->order);
@@ -1368,7 +1483,11 @@ int moc_destroy(moc_ctx* c) {
   dfree(c->otf_order);
   cmfd_release(c);
   dfree(c->sc);
-  if (c->hsc) cudaFreeHost(c->hsc);
+  if (c->hsc) {
+    std::lock_guard<std::mutex> lk(g_pinned_mu);
+    if (g_pinned_scalars.size() < 64) g_pinned_scalars.push_back(c->hsc);
+    else cudaFreeHost(c->hsc);
+  }
   for (cudaEvent_t e : c->ev) cudaEventDestroy(e);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
