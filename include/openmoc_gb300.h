@@ -449,7 +449,11 @@ typedef struct {
                                   FP32 (as the reference's single-precision
                                   build), with no host round trip; 1: on the
                                   host in FP64, tallies read back every
-                                  iteration */
+                                  iteration; 2: on the GPU on one block;
+                                  3: on the GPU cell-parallel (one thread per
+                                  coarse cell over a cluster of blocks; up to
+                                  8 coarse groups).  0 takes 3 where it
+                                  applies, else 2. */
   int32_t k_nearest;           /* 0: each FSR takes its cell's ratio;
                                   1..9: Cmfd::setKNearest, the ratio
                                   weighted over the nearest of the 3 x 3

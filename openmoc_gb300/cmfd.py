@@ -37,6 +37,7 @@ class Cmfd:
         self._unbounded = 0             # src/Cmfd.cpp:35
         self._edc = True
         self._host = False
+        self._device_solve = 0
         self._k_nearest = 0
         self._fsr_cell: Optional[np.ndarray] = None
 
@@ -113,6 +114,17 @@ class Cmfd:
         the host and the ratios back every iteration) instead of on the GPU
         in FP32 (the default: one block, no host round trip)."""
         self._host = bool(on)
+
+    def setDeviceSolver(self, kind: str) -> None:
+        """Which device kernel runs the coarse power iteration: "auto" (the
+        cell-parallel solve, one thread per coarse cell over a cluster of
+        blocks, for up to 8 coarse groups and meshes it can map; else one
+        block), "block" (one block, any mesh) or "cells" (the cell-parallel
+        solve, an error where it does not apply)."""
+        kinds = {"auto": 0, "block": 2, "cells": 3}
+        if kind not in kinds:
+            raise _native.MOCError(-1, f"unknown CMFD device solver {kind!r}")
+        self._device_solve = kinds[kind]
 
     def setKNearest(self, k: int) -> None:
         """Cmfd::setKNearest (src/Cmfd.cpp:3417): each FSR's update ratio
@@ -194,7 +206,7 @@ class Cmfd:
                              E, ptr(group_of), int(mu.size), ptr(mu), ptr(w),
                              self._relaxation, self._sor,
                              1 if self._flux_limiting else 0, self._unbounded,
-                             1 if self._host else 0, self._k_nearest, ptr(cen),
+                             1 if self._host else self._device_solve, self._k_nearest, ptr(cen),
                              float(bounds[0]), float(bounds[2]))
         return m, keep
 

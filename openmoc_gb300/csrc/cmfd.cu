@@ -13,6 +13,8 @@
 // LINALG_TOL 1e-7); block-wide sums are compensated FP32 within a thread,
 // FP32 within a warp and FP64 across warps, and the scalar work after them
 // runs in one thread, since FP64 issues at a small fraction of the FP32 rate.
+#include <cooperative_groups.h>
+
 #include <algorithm>
 #include <cfloat>
 
@@ -697,6 +699,491 @@ __device__ bool dd_linear_solve(const CmfdArgs& a, const Work& k,
   return true;
 }
 
+// ---------------------------------------------------------------------------
+// The cell-parallel coarse solve.  One thread holds one coarse cell for the
+// whole solve, with the cell's row of the system in registers: A's
+// off-diagonal part within the cell, the diagonal and the SOR factors, the
+// four couplings to its neighbours, its iterate and its right side.  A half
+// sweep then reads from shared memory only the neighbours' iterates, and the
+// fission products, totals and residuals are per-thread work plus one
+// reduction.  Meshes larger than a block (cmfd_cells_threads) split over a
+// thread-block cluster by runs of cells: a block keeps, after its own cells'
+// slots, copies of the other blocks' cells that border its own, which their
+// owners write into its shared memory (distributed shared memory) after
+// each of their updates; the hardware cluster barrier after a half sweep
+// orders those writes before the reads of the next.  Each block's threads
+// hold red cells first, then black ones, so a half sweep leaves whole warps
+// idle rather than half of every warp.
+//
+// Every branch of the solve follows a value all blocks compute identically:
+// a block total is written into every block's shared memory, and each
+// block's thread 0 adds the totals in block order and judges them, so the
+// blocks run the same sweeps and meet at the same cluster barriers.
+
+// Shared-memory stride of a cell's iterate: its E floats in one or two
+// 16-byte loads, padded so that eight consecutive cells fall on distinct
+// banks.
+__host__ __device__ constexpr int cells_xs_stride(int E) {
+  return E <= 2 ? E : E <= 4 ? 4 : 12;
+}
+// Per-thread vectors in shared memory, [kCellVecs][E][threads]: the linear
+// solve's old and new fission sources, the diagonally dominant solve's old
+// and new sources, its right side and its diagonal increments.
+constexpr int kCellVecs = 6;
+
+// The convergence state of the nested solves, kept by thread 0 alone (in
+// shared memory, so that it holds no registers in the other threads).
+struct CellsJudge {
+  double linit, inv_linit, min_res, stall_res, tol;      // linear solve
+  double dd_initial, dd_inv_initial, dd_min_res, dd_stall_res;
+  double initial, inv_initial, e_stall_res, inv_c;       // power iteration
+  int stall_li, stall_it, stall_p;
+};
+
+template <int EC>
+__global__ void __launch_bounds__(cmfd_cells_threads(EC), 1)
+cmfd_cells_kernel(const CmfdArgs a) {
+  namespace cg = cooperative_groups;
+  DevScalars* sc = a.sc;
+  if (*(volatile int*) &sc->done) return;    // the same for every block
+  constexpr int XS = cells_xs_stride(EC);
+  constexpr int EO = EC > 1 ? EC - 1 : 1;
+  const int NB = a.map_nb, T = blockDim.x, t = threadIdx.x;
+  const int rank = NB > 1 ? (int) cg::this_cluster().block_rank() : 0;
+  const int NT = NB * T, gid = rank * T + t;
+  const int C = a.C;
+  extern __shared__ float4 s_dyn[];
+  float* xs = reinterpret_cast<float*>(s_dyn);       // [slots][XS]
+  float* mm = xs + a.map_slots * XS;                  // [EC * EC][T]
+  float* vec = mm + EC * EC * T;                      // [kCellVecs][EC][T]
+  __shared__ double red[33];
+  __shared__ double part[2][kCmfdMaxClusterBlocks];   // block totals
+  __shared__ CellsJudge J;
+  int buf = 0;
+  auto V = [&](int v, int e) -> float& { return vec[(v * EC + e) * T + t]; };
+  auto barrier = [&]() {
+    if (NB > 1) cg::this_cluster().sync();
+    else __syncthreads();
+  };
+
+  // every block of the cluster runs before any writes into another's
+  // shared memory
+  if (NB > 1) cg::this_cluster().sync();
+  const Work g = carve(a.work, C, EC);   // as the build kernel wrote it
+  const int j = a.map_j[gid];
+  const bool has = j >= 0;
+  const int colour = has ? (j >= a.n_color0 ? 1 : 0) : -1;
+  int nsl[4], push[2];
+#pragma unroll
+  for (int f = 0; f < 4; f++) nsl[f] = a.map_nslot[f * NT + gid];
+#pragma unroll
+  for (int q = 0; q < 2; q++) push[q] = a.map_push[q * NT + gid];
+  float x[EC], b[EC], diag[EC], sa[EC], sb[EC], nbc[4][EC], aoff[EC][EO];
+#pragma unroll
+  for (int e = 0; e < EC; e++) {
+    x[e] = has ? g.x[e * C + j] : 0.0f;
+    b[e] = 0.0f;
+    diag[e] = has ? g.A[(e * EC + e) * C + j] : 1.0f;
+#pragma unroll
+    for (int q = 0; q < EO; q++) {
+      const int gg = q < e ? q : q + 1;
+      aoff[e][q] = (has && EC > 1) ? g.A[(e * EC + gg) * C + j] : 0.0f;
+    }
+#pragma unroll
+    for (int f = 0; f < 4; f++)
+      nbc[f][e] = has ? g.nb[(f * EC + e) * C + j] : 0.0f;
+#pragma unroll
+    for (int gg = 0; gg < EC; gg++)
+      mm[(e * EC + gg) * T + t] = has ? g.M[(e * EC + gg) * C + j] : 0.0f;
+  }
+  const float w = a.sor;
+
+  // this cell's iterate into its slot and into the copies other blocks hold
+  auto publish = [&]() {
+    if (!has) return;
+    float* me = xs + t * XS;
+#pragma unroll
+    for (int e = 0; e < EC; e++) me[e] = x[e];
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      if (push[q] < 0) continue;
+      float* rem = cg::this_cluster().map_shared_rank(xs, push[q] >> 24) +
+                   (push[q] & 0xFFFFFF) * XS;
+#pragma unroll
+      for (int e = 0; e < EC; e++) rem[e] = x[e];
+    }
+  };
+  // one red-black half sweep (sor_half's arithmetic for this cell)
+  auto half = [&](int h) {
+    if (colour != h) return;
+    float u[EC];
+#pragma unroll
+    for (int e = 0; e < EC; e++) {
+      float v = b[e];
+#pragma unroll
+      for (int f = 0; f < 4; f++) v -= nbc[f][e] * xs[nsl[f] * XS + e];
+      u[e] = v;
+    }
+#pragma unroll
+    for (int e = 0; e < EC; e++) {
+      float s0 = 0.0f, s1 = 0.0f;
+#pragma unroll
+      for (int gg = 0; gg < EC; gg++)
+        if (gg != e) {
+          const float v = aoff[e][gg < e ? gg : gg - 1] * x[gg];
+          if (gg & 1) s1 -= v;
+          else s0 -= v;
+        }
+      x[e] = (sa[e] * x[e] + (u[e] + (s0 + s1))) * sb[e];
+    }
+    publish();
+  };
+  auto sor_factors = [&]() {
+#pragma unroll
+    for (int e = 0; e < EC; e++) {
+      sa[e] = (1.0f - w) * (diag[e] / w);
+      sb[e] = w / diag[e];
+    }
+  };
+  // out = M v for this cell
+  auto fission = [&](const float (&v)[EC], float (&out)[EC]) {
+#pragma unroll
+    for (int e = 0; e < EC; e++) {
+      float s = 0.0f;
+#pragma unroll
+      for (int gg = 0; gg < EC; gg++) s += mm[(e * EC + gg) * T + t] * v[gg];
+      out[e] = s;
+    }
+  };
+  auto fission_to = [&](int vi) {
+    float o[EC];
+    fission(x, o);
+#pragma unroll
+    for (int e = 0; e < EC; e++) V(vi, e) = o[e];
+  };
+  // finish(the sum over all cells of every thread's v) for every thread:
+  // FP32 within a warp, FP64 across warps and blocks (blocks in order)
+  auto total = [&](float v, auto&& finish) -> double {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int wi = t >> 5, lane = t & 31;
+    if (lane == 0) red[wi] = (double) v;
+    __syncthreads();
+    double s = 0.0;
+    if (wi == 0) {
+      s = lane < (T >> 5) ? red[lane] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    }
+    if (NB > 1) {
+      if (t == 0)
+        for (int r = 0; r < NB; r++)
+          cg::this_cluster().map_shared_rank(&part[0][0], r)[buf * kCmfdMaxClusterBlocks + rank] = s;
+      cg::this_cluster().sync();
+      if (t == 0) {
+        s = 0.0;
+        for (int r = 0; r < NB; r++) s += part[buf][r];
+      }
+      buf ^= 1;
+    }
+    if (t == 0) red[32] = finish(s);
+    __syncthreads();
+    return red[32];
+  };
+  auto cell_sum = [&](const float (&v)[EC]) {
+    FSum s;
+#pragma unroll
+    for (int e = 0; e < EC; e++) s.add(v[e]);
+    return has ? s.value() : 0.0f;
+  };
+  if (t == 0) J.inv_c = 1.0 / (double) max(C, 1);
+  // computeRMSE of this cell's change from y to xv, judged by thread 0
+  auto rmse = [&](const float (&xv)[EC], const float (&y)[EC], auto&& judge) {
+    float r2 = 0.0f;
+    if (has) {
+      float d = 0.0f, tt = 0.0f;
+#pragma unroll
+      for (int e = 0; e < EC; e++) {
+        d += xv[e] - y[e];
+        tt += y[e];
+      }
+      if (fabsf(tt) > (float) kFluxEps) {
+        const float r = d / tt;
+        r2 = r * r;
+      }
+    }
+    return total(r2, [&](double tot) {
+      return judge((double) sqrtf((float) (tot * J.inv_c)));
+    });
+  };
+  auto load = [&](int vi, float (&o)[EC]) {
+#pragma unroll
+    for (int e = 0; e < EC; e++) o[e] = V(vi, e);
+  };
+
+  int sweeps = 0, power = 0;
+  // linearSolve (src/linalg.cpp:179-385), as linear_solve
+  auto linear = [&](double tol) -> bool {
+    if (t == 0) {
+      J.tol = fmax(kLinalgTol, tol);
+      J.linit = 0.0;
+      J.inv_linit = INFINITY;
+      J.min_res = 1e6;
+      J.stall_res = INFINITY;
+      J.stall_li = 0;
+    }
+    int ls_old = 0, ls_new = 1;
+    sor_factors();
+    fission_to(ls_old);
+    int li = 0;
+    while (li < kMaxLinearIters) {
+      half(0);
+      barrier();
+      half(1);
+      barrier();
+      sweeps++;
+      float fo[EC], fn[EC];
+      if (li == 0 || li + 1 >= kMinIters) fission_to(ls_new);
+      if (li == 0) {
+        load(ls_new, fn);
+        load(ls_old, fo);
+        rmse(fn, fo, [&](double r) {
+          J.inv_linit = r > 0.0 ? 1.0 / r : INFINITY;
+          return J.linit = r;
+        });
+      }
+      li++;
+      if (li > kMinIters) {
+        load(ls_new, fn);
+        load(ls_old, fo);
+        const double verdict = rmse(fn, fo, [&](double r) {
+          J.min_res = fmin(J.min_res, r);
+          if ((r > 1e3 * J.min_res && J.min_res > kNoiseFloor) || !isfinite(r))
+            return -1.0;
+          const double q = J.linit > 0.0 ? r * J.inv_linit : INFINITY;
+          if (q < 0.1 || r < J.tol) return 1.0;
+          if (li - J.stall_li >= kStallWindow) {
+            if (r < kStallMax && r > 0.5 * J.stall_res) return 1.0;
+            J.stall_res = r;
+            J.stall_li = li;
+          }
+          return 0.0;
+        });
+        if (verdict < 0.0) return false;
+        if (verdict > 0.0) return true;
+      }
+      if (li > kMinIters - 1 && li < kMaxLinearIters) {
+        const int tmp = ls_old;
+        ls_old = ls_new;
+        ls_new = tmp;
+      }
+      if (sweeps >= kMaxSweeps) return false;
+    }
+    return false;
+  };
+  // ddLinearSolve (src/linalg.cpp:717-900), as dd_linear_solve; the
+  // increments in vector 5, the plain right side in vector 4
+  auto dd_linear = [&](double tol) -> bool {
+#pragma unroll
+    for (int e = 0; e < EC; e++) {
+      double s = 0.0;
+#pragma unroll
+      for (int q = 0; q < EO; q++)
+        if (EC > 1) s += fabsf(aoff[e][q]);
+#pragma unroll
+      for (int f = 0; f < 4; f++) s += fabsf(nbc[f][e]);
+      const float dd = s > (double) diag[e] ? (float) (s - diag[e]) : 0.0f;
+      V(5, e) = dd;
+      diag[e] = diag[e] + dd;
+      V(4, e) = b[e];
+    }
+    int old_src = 2, new_src = 3;
+    fission_to(new_src);
+    if (t == 0) {
+      J.dd_initial = 0.0;
+      J.dd_inv_initial = 0.0;
+      J.dd_min_res = 1e6;
+      J.dd_stall_res = INFINITY;
+      J.stall_it = 0;
+    }
+    for (int it = 0; it < kMaxLinearIters; it++) {
+      const int tmp = old_src;
+      old_src = new_src;
+      new_src = tmp;
+#pragma unroll
+      for (int e = 0; e < EC; e++) b[e] = V(4, e) + V(5, e) * x[e];
+      linear(tol);   // a failure is only noted
+      fission_to(new_src);
+      float fn[EC], fo[EC];
+      load(new_src, fn);
+      load(old_src, fo);
+      const double verdict = rmse(fn, fo, [&](double res) {
+        if (it == 0) {
+          J.dd_initial = res < 1e-14 ? 1e-10 : res;
+          J.dd_inv_initial = 1.0 / J.dd_initial;
+        }
+        J.dd_min_res = fmin(J.dd_min_res, res);
+        if ((res > 1e3 * J.dd_min_res && J.dd_min_res > kNoiseFloor) || !isfinite(res))
+          return -1.0;
+        if (res * J.dd_inv_initial < 0.1 || res < tol) return 1.0;
+        if (it - J.stall_it >= kStallWindow) {
+          if (res < kStallMax && res > 0.5 * J.dd_stall_res) return 1.0;
+          J.dd_stall_res = res;
+          J.stall_it = it;
+        }
+        return 0.0;
+      });
+      if (verdict < 0.0) return false;
+      if (verdict > 0.0) break;
+      if (sweeps >= kMaxSweeps) return false;
+    }
+#pragma unroll
+    for (int e = 0; e < EC; e++) {
+      diag[e] = diag[e] - V(5, e);
+      b[e] = V(4, e);
+    }
+    return true;
+  };
+
+  CmfdDevState* cm = a.cm;
+  const int it = sc->iteration;
+  double src_thr = 0.1 * sc->threshold;
+  if (it > 0) src_thr = 0.01 * (sc->residual > 0.0 ? sc->residual : 1e-6);
+  double keff = cm->keff;
+  const double rows = (double) C * EC;
+  const double tol = fmax(kLinalgTol, src_thr);
+  const double lin_tol = fmax(kLinalgTol, tol * 1e-1);
+  // ---- eigenvalueSolve (src/linalg.cpp:25-176), as cmfd_solve_kernel
+  fission(x, b);
+  const double s0 = total(cell_sum(b), [](double s) { return s; });
+  bool failed = !(s0 > 0.0) || !isfinite(s0);
+  if (!failed) {
+#pragma unroll
+    for (int e = 0; e < EC; e++) {
+      b[e] = (float) (b[e] * (rows / s0));
+      x[e] = (float) (x[e] * (rows * keff / s0));
+    }
+    if (t == 0) {
+      J.initial = 0.0;
+      J.inv_initial = 0.0;
+      J.e_stall_res = INFINITY;
+      J.stall_p = 0;
+    }
+    publish();
+    barrier();
+    bool dd_mode = false;
+    for (power = 0; power < kMaxPowerIters; power++) {
+      bool ok = false;
+      if (!dd_mode) ok = linear(lin_tol);
+      if (!ok) {
+        dd_mode = true;
+        ok = dd_linear(lin_tol);
+      }
+      if (!ok) {
+        failed = true;
+        break;
+      }
+      float sn[EC];
+      fission(x, sn);
+      keff = total(cell_sum(sn), [&](double s) { return s / rows; });
+      const float kf = (float) keff;
+#pragma unroll
+      for (int e = 0; e < EC; e++) sn[e] /= kf;
+      const double stop = rmse(sn, b, [&](double res) {
+        if (power == 0) {
+          J.initial = res < 1e-14 ? 1e-10 : res;
+          J.inv_initial = 1.0 / J.initial;
+        }
+        if ((res * J.inv_initial < 0.03 || res < kLinalgTol) && power > kMinIters)
+          return 1.0;
+        if (power > kMinIters && power - J.stall_p >= kStallWindow) {
+          if (res < kStallMax && res > 0.5 * J.e_stall_res) return 1.0;
+          J.e_stall_res = res;
+          J.stall_p = power;
+        }
+        return 0.0;
+      });
+#pragma unroll
+      for (int e = 0; e < EC; e++) b[e] = sn[e];
+      if (stop > 0.0) {
+        power++;
+        break;
+      }
+    }
+    if (!(fabs(keff + 1.0) > FLT_EPSILON) || !isfinite(keff)) failed = true;
+  }
+
+  if (failed) {
+    if (has)
+#pragma unroll
+      for (int e = 0; e < EC; e++) a.ratio[a.color_cells[j] * EC + e] = 1.0f;
+    if (gid == 0) {
+      cm->failed = 1;
+      cm->power_iters = power;
+      cm->linear_iters = sweeps;
+      cm->max_ratio = 1.0f;
+      cm->valid = 1;
+      sc->keff = cm->keff;
+    }
+    if (NB > 1) cg::this_cluster().sync();   // no block leaves while others may write to it
+    return;
+  }
+  // ---- Cmfd::rescaleFlux and the ratios of Cmfd::updateMOCFlux
+  float pt[EC], fa[EC], fb[EC];
+#pragma unroll
+  for (int e = 0; e < EC; e++) pt[e] = has ? g.phi_t[e * C + j] : 0.0f;
+  fission(x, fa);
+  fission(pt, fb);
+  const auto inverse = [](double s) { return 1.0 / s; };
+  const double sn = total(cell_sum(fa), inverse);
+  const double so = total(cell_sum(fb), inverse);
+  float far = 1.0f;
+  if (has) {
+#pragma unroll
+    for (int e = 0; e < EC; e++) {
+      const int out = a.color_cells[j] * EC + e;
+      const float xn = (float) (x[e] * sn);
+      const float xo = (float) (pt[e] * so);
+      const float q = fabs((double) xo) > kFluxEps ? xn / xo : 0.0f;
+      a.ratio[out] = q;
+      a.flux_new[out] = xn;
+      a.flux_old[out] = xo;
+      if (q > 0.0f && fabsf(logf(q)) > fabsf(logf(far))) far = q;
+    }
+  }
+  // the ratio farthest from 1 (log distance): warps, then blocks in order
+  for (int o = 16; o > 0; o >>= 1) {
+    const float y = __shfl_xor_sync(0xffffffffu, far, o);
+    if (fabsf(logf(y)) > fabsf(logf(far))) far = y;
+  }
+  if ((t & 31) == 0) red[t >> 5] = (double) far;
+  __syncthreads();
+  if (t == 0) {
+    float best = 1.0f;
+    for (int i = 0; i < (T >> 5); i++) {
+      const float y = (float) red[i];
+      if (fabsf(logf(y)) > fabsf(logf(best))) best = y;
+    }
+    if (NB > 1)
+      cg::this_cluster().map_shared_rank(&part[0][0], 0)[buf * kCmfdMaxClusterBlocks + rank] = best;
+    else
+      part[buf][0] = best;
+  }
+  if (NB > 1) cg::this_cluster().sync();
+  if (gid == 0) {
+    float best = 1.0f;
+    for (int r = 0; r < NB; r++) {
+      const float y = (float) part[buf][r];
+      if (fabsf(logf(y)) > fabsf(logf(best))) best = y;
+    }
+    cm->max_ratio = best;
+    cm->failed = 0;
+    cm->power_iters = power;
+    cm->linear_iters = sweeps;
+    cm->valid = 1;
+    cm->keff = keff;
+    sc->keff = keff;
+  }
+}
+
 // Cmfd::collapseXS over the whole GPU, one thread per (cell, coarse group).
 __global__ void __launch_bounds__(256)
 cmfd_collapse_kernel(const CmfdArgs a) {
@@ -915,13 +1402,65 @@ void launch_cmfd_pair_sums(const float* phi, const float* vol,
                                                         sc);
 }
 
-void launch_cmfd_solve(const CmfdArgs& a, cudaStream_t s) {
-  // one thread per cell of a colour, at least four warps
-  // collapse and matrices over the GPU, then the solve on one block
+int64_t cmfd_cells_smem(int E, int threads, int slots) {
+  return 4 * ((int64_t) slots * cells_xs_stride(E) + (int64_t) E * E * threads +
+              (int64_t) kCellVecs * E * threads);
+}
+
+namespace {
+
+template <int EC>
+bool cells_instance(const CmfdArgs& a, cudaStream_t s) {
+  static bool configured = false;
+  if (!configured) {
+    cudaFuncSetAttribute(cmfd_cells_kernel<EC>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kSolveSmemMax);
+    configured = true;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned) a.map_nb);
+  cfg.blockDim = dim3((unsigned) a.map_threads);
+  cfg.dynamicSmemBytes = (size_t) cmfd_cells_smem(EC, a.map_threads, a.map_slots);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned) a.map_nb;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (cudaLaunchKernelEx(&cfg, cmfd_cells_kernel<EC>, a) == cudaSuccess)
+    return true;
+  cudaGetLastError();   // a launch-configuration error is not sticky
+  return false;
+}
+
+bool launch_cells(const CmfdArgs& a, cudaStream_t s) {
+  switch (a.E) {
+    case 1: return cells_instance<1>(a, s);
+    case 2: return cells_instance<2>(a, s);
+    case 3: return cells_instance<3>(a, s);
+    case 4: return cells_instance<4>(a, s);
+    case 5: return cells_instance<5>(a, s);
+    case 6: return cells_instance<6>(a, s);
+    case 7: return cells_instance<7>(a, s);
+    case 8: return cells_instance<8>(a, s);
+    default: return false;
+  }
+}
+
+}  // namespace
+
+bool launch_cmfd_solve(const CmfdArgs& a, cudaStream_t s) {
+  // collapse and matrices over the GPU, then the solve: cell-parallel when
+  // the cells are mapped onto a cluster, else on one block (one thread per
+  // cell of a colour, at least four warps)
   const int CE = a.C * a.E;
   const int nb = (int) std::min<int64_t>((CE + 255) / 256, (int64_t) 4 * sm_count());
   cmfd_collapse_kernel<<<std::max(nb, 1), 256, 0, s>>>(a);
   cmfd_build_kernel<<<std::max(nb, 1), 256, 0, s>>>(a);
+  if (a.map_nb > 0 && a.solve_kind == 0 && launch_cells(a, s)) return true;
   int threads = (std::max(a.n_color0, a.C - a.n_color0) + 31) / 32 * 32;
   threads = std::max(128, std::min(solve_threads(a.E <= 8 ? a.E : 0), threads));
   int64_t bytes = 0;
@@ -938,6 +1477,7 @@ void launch_cmfd_solve(const CmfdArgs& a, cudaStream_t s) {
     case 8: solve_instance<8>(a, threads, smem, level, s); break;
     default: solve_instance<0>(a, threads, smem, level, s); break;
   }
+  return !(a.map_nb > 0 && a.solve_kind == 0);
 }
 
 void launch_cmfd_prolong(float* phi, float* mom, const int32_t* fsr_cell,

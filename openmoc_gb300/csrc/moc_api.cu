@@ -338,6 +338,14 @@ struct moc_ctx {
   int32_t* cm_cell_pos = nullptr;
   int32_t* cm_nbr_j = nullptr;
   int cm_n_color0 = 0;
+  // the cell-parallel coarse solve's map (moc::CmfdArgs::map_*; nb 0: the
+  // mesh is solved on one block) and the solve asked for (0 automatic,
+  // 2 one block, 3 cell-parallel)
+  int32_t* cm_map_j = nullptr;
+  int32_t* cm_map_nslot = nullptr;
+  int32_t* cm_map_push = nullptr;
+  int cm_map_nb = 0, cm_map_threads = 0, cm_map_slots = 0;
+  int cm_solve_kind = 0;
   int32_t* cm_pair_mat = nullptr;
   float* cm_chi_m = nullptr;
   float* cm_ss_m = nullptr;
@@ -946,6 +954,10 @@ void cmfd_release(moc_ctx* c) {
   dfree(c->cm_color_cells);
   dfree(c->cm_cell_pos);
   dfree(c->cm_nbr_j);
+  dfree(c->cm_map_j);
+  dfree(c->cm_map_nslot);
+  dfree(c->cm_map_push);
+  c->cm_map_nb = 0;
   dfree(c->cm_pair_mat);
   dfree(c->cm_chi_m);
   dfree(c->cm_ss_m);
@@ -1088,6 +1100,80 @@ int cmfd_prepare(moc_ctx* c) {
   }
   MOC_TRY(up(&c->cm_cell_pos, pos));
   MOC_TRY(up(&c->cm_nbr_j, nbr_j));
+  // the cell-parallel solve: cells in runs of cell order over the blocks
+  // of a cluster, each block's red cells first
+  c->cm_map_nb = 0;
+  if (E <= moc::kCmfdMaxCellGroups) {
+    const int cap = moc::cmfd_cells_threads(E);
+    const int nb = (C + cap - 1) / cap;
+    const int per = (C + nb - 1) / std::max(nb, 1);
+    std::vector<int> owner(C), slot(C);
+    std::vector<std::vector<int>> own(nb);
+    for (int k = 0; k < 2; k++)
+      for (int cell = 0; cell < C; cell++)
+        if (((cell % cf.nx) + (cell / cf.nx)) % 2 == k) {
+          const int r = cell / per;
+          owner[cell] = r;
+          slot[cell] = (int) own[r].size();
+          own[r].push_back(cell);
+        }
+    int threads = 32;
+    for (int r = 0; r < nb; r++)
+      threads = std::max(threads, ((int) own[r].size() + 31) / 32 * 32);
+    // halo copies: each block's copy of a bordering cell of another block
+    std::vector<std::vector<std::pair<int, int>>> copies(C);   // (block, slot)
+    std::vector<int> halo(nb, 0);
+    std::vector<std::vector<int>> halo_slot(nb);
+    bool ok = nb <= moc::kCmfdMaxClusterBlocks;
+    const int NT = nb * threads;
+    std::vector<int32_t> mj(NT, -1), mns(4 * (size_t) NT), mpush(2 * (size_t) NT, -1);
+    for (int r = 0; ok && r < nb; r++) {
+      std::vector<int> local(C, -1);   // slot in block r of each cell it reads
+      for (int q = 0; q < (int) own[r].size(); q++) local[own[r][q]] = q;
+      for (int q = 0; q < (int) own[r].size(); q++) {
+        const int cell = own[r][q], ix = cell % cf.nx, iy = cell / cf.nx;
+        const int nbc[4] = {ix > 0 ? cell - 1 : -1, iy > 0 ? cell - cf.nx : -1,
+                            ix + 1 < cf.nx ? cell + 1 : -1,
+                            iy + 1 < cf.ny ? cell + cf.nx : -1};
+        const int gid = r * threads + q;
+        mj[gid] = pos[cell];
+        for (int f = 0; f < 4; f++) {
+          int sl = q;
+          if (nbc[f] >= 0) {
+            if (local[nbc[f]] < 0) {
+              local[nbc[f]] = threads + halo[r]++;
+              copies[nbc[f]].push_back({r, local[nbc[f]]});
+            }
+            sl = local[nbc[f]];
+          }
+          mns[(size_t) f * NT + gid] = sl;
+        }
+      }
+      for (int q = (int) own[r].size(); q < threads; q++)
+        for (int f = 0; f < 4; f++) mns[(size_t) f * NT + r * threads + q] = q;
+    }
+    for (int cell = 0; ok && cell < C; cell++) {
+      if (copies[cell].size() > 2) { ok = false; break; }
+      const int gid = owner[cell] * threads + slot[cell];
+      for (size_t q = 0; q < copies[cell].size(); q++)
+        mpush[q * NT + gid] = (copies[cell][q].first << 24) | copies[cell][q].second;
+    }
+    int slots = threads;
+    for (int r = 0; r < nb; r++) slots = std::max(slots, threads + halo[r]);
+    if (ok && moc::cmfd_cells_smem(E, threads, slots) > 200 * 1024) ok = false;
+    if (ok) {
+      MOC_TRY(up(&c->cm_map_j, mj));
+      MOC_TRY(up(&c->cm_map_nslot, mns));
+      MOC_TRY(up(&c->cm_map_push, mpush));
+      c->cm_map_nb = nb;
+      c->cm_map_threads = threads;
+      c->cm_map_slots = slots;
+    }
+  }
+  MOC_CHECK(c->cm_solve_kind != 3 || c->cm_map_nb > 0, MOC_ERR_UNSUPPORTED,
+            "the cell-parallel coarse solve takes up to " +
+                std::to_string(moc::kCmfdMaxCellGroups) + " coarse groups and " +
+                std::to_string(moc::kCmfdMaxClusterBlocks) + " blocks of cells");
   MOC_TRY(up(&c->cm_pair_mat, F.pair_mat));
   MOC_TRY(up(&c->cm_chi_m, chi_m));
   MOC_TRY(up(&c->cm_ss_m, ss_m));
@@ -1142,6 +1228,13 @@ moc::CmfdArgs cmfd_args(moc_ctx* c) {
   a.cell_pos = c->cm_cell_pos;
   a.nbr_j = c->cm_nbr_j;
   a.n_color0 = c->cm_n_color0;
+  a.map_j = c->cm_map_j;
+  a.map_nslot = c->cm_map_nslot;
+  a.map_push = c->cm_map_push;
+  a.map_nb = c->cm_map_nb;
+  a.map_threads = c->cm_map_threads;
+  a.map_slots = c->cm_map_slots;
+  a.solve_kind = c->cm_solve_kind == 2 ? 2 : 0;
   a.pair_mat = c->cm_pair_mat;
   a.st = c->sigma_t;
   a.nf = c->nu_sigma_f;
@@ -1210,8 +1303,12 @@ int run_cmfd_iterations(moc_ctx* c, int res_type) {
         MOC_CUDA(cudaMemcpyAsync(&c->sc->keff, &c->hsc->keff, sizeof(double),
                                  cudaMemcpyHostToDevice, c->stream));
       } else {
-        moc::launch_cmfd_solve(ca, c->stream);   // collapse, build, solve
+        // collapse, build, solve
+        const bool as_asked = moc::launch_cmfd_solve(ca, c->stream);
         c->launches += 3;
+        MOC_CUDA(cudaGetLastError());
+        MOC_CHECK(as_asked || c->cm_solve_kind != 3, MOC_ERR_CUDA,
+                  "the cell-parallel coarse solve could not be launched");
       }
       moc::launch_cmfd_prolong(c->phi, c->ls ? c->mom : nullptr, c->cm_cell,
                                c->cm_group, c->cm_ratio,
@@ -2913,6 +3010,9 @@ int moc_set_cmfd(moc_ctx* c, const moc_cmfd_mesh* m) {
             MOC_ERR_ARG, "the SOR factor must be in (0, 2)");
   MOC_CHECK(m->num_unbounded_iterations >= 0, MOC_ERR_ARG,
             "negative number of unbounded iterations");
+  MOC_CHECK(m->solve_on_host >= 0 && m->solve_on_host <= 3, MOC_ERR_ARG,
+            "solve_on_host must be 0 (device, automatic), 1 (host), 2 (device, "
+            "one block) or 3 (device, cell-parallel)");
   MOC_CHECK(m->k_nearest >= 0 && m->k_nearest <= 9, MOC_ERR_ARG,
             "k_nearest must be in 0..9 (Cmfd::setKNearest takes 1..9)");
   MOC_CHECK(m->k_nearest == 0 || m->fsr_centroid, MOC_ERR_ARG,
@@ -2941,7 +3041,8 @@ int moc_set_cmfd(moc_ctx* c, const moc_cmfd_mesh* m) {
   cf.flux_limiting = m->flux_limiting != 0;
   cf.unbounded = m->num_unbounded_iterations;
   c->cmfd = S;
-  c->cm_host = m->solve_on_host != 0;
+  c->cm_host = m->solve_on_host == 1;
+  c->cm_solve_kind = m->solve_on_host;
   c->h_cm_cell.assign(m->fsr_cell, m->fsr_cell + R);
   const int ld = row_stride(c);
   const int64_t ncur = (int64_t) C * moc_cmfd::kFaces * ld;

@@ -407,14 +407,41 @@ struct CmfdArgs {
   float* flux_new;              // [C][E]
   CmfdDevState* cm;
   DevScalars* sc;
+  // The cell-parallel coarse solve (one thread per cell over a cluster of
+  // map_nb blocks of map_threads threads; map_nb = 0: not available):
+  // thread gid = block * map_threads + t holds the cell at colour position
+  // map_j[gid] (-1: none); map_nslot[f][gid] is the slot of its face-f
+  // neighbour's iterate in the block's shared memory (its own cell's slot t
+  // when there is none), slots past map_threads holding copies of cells of
+  // other blocks; map_push[k][gid] (k < 2) = block << 24 | slot of a copy
+  // of this cell in another block (-1: none).
+  const int32_t* map_j;
+  const int32_t* map_nslot;
+  const int32_t* map_push;
+  int map_nb, map_threads, map_slots;
+  int solve_kind;               // 0 cell-parallel when mapped, 2 one block
 };
+
+// Threads a block of the cell-parallel coarse solve may hold for E coarse
+// groups (one cell each, its coefficients in registers), and the blocks of
+// a cluster at most.
+constexpr int cmfd_cells_threads(int E) {
+  return E <= 2 ? 768 : E <= 4 ? 512 : E <= 6 ? 384 : 320;
+}
+constexpr int kCmfdMaxClusterBlocks = 8;
+constexpr int kCmfdMaxCellGroups = 8;
+// Dynamic shared memory (bytes) of a block of the cell-parallel solve.
+int64_t cmfd_cells_smem(int E, int threads, int slots);
 
 // Scratch floats the device coarse solve needs for C cells, E groups.
 int64_t cmfd_work_floats(int C, int E);
-// One coarse solve (Cmfd::computeKeff) on one block: collapse, matrices,
-// power iteration with red-black SOR, ratios; sets sc->keff.  Returns at
-// once when the solve is done.
-void launch_cmfd_solve(const CmfdArgs& a, cudaStream_t s);
+// One coarse solve (Cmfd::computeKeff): collapse and matrices over the GPU,
+// then the power iteration with red-black SOR and the ratios, cell-parallel
+// over a cluster when the map is set and solve_kind is 0, else on one
+// block; sets sc->keff.  Returns at once when the solve is done.  Returns
+// false when the cell-parallel kernel could not be launched (the one-block
+// solve ran instead).
+bool launch_cmfd_solve(const CmfdArgs& a, cudaStream_t s);
 
 // CMFD (cmfd.cu): per (coarse cell, material) pair the sums of phi * volume
 // over its FSRs, [P][G] FP64, from the CSR list pair_off [P + 1] /
