@@ -773,6 +773,20 @@ cmfd_cells_kernel(const CmfdArgs a) {
   const int j = a.map_j[gid];
   const bool has = j >= 0;
   const int colour = has ? (j >= a.n_color0 ? 1 : 0) : -1;
+  // the barrier after a half sweep of colour h: the threads that updated a
+  // cell (and wrote its iterate here and into other blocks) release their
+  // writes, the others arrive without ordering; all acquire
+  auto sweep_barrier = [&](int h) {
+    if (NB > 1) {
+      if (colour == h)
+        asm volatile("barrier.cluster.arrive.release;" ::: "memory");
+      else
+        asm volatile("barrier.cluster.arrive.relaxed;" ::: "memory");
+      asm volatile("barrier.cluster.wait.acquire;" ::: "memory");
+    } else {
+      __syncthreads();
+    }
+  };
   int nsl[4], push[2];
 #pragma unroll
   for (int f = 0; f < 4; f++) nsl[f] = a.map_nslot[f * NT + gid];
@@ -813,28 +827,28 @@ cmfd_cells_kernel(const CmfdArgs a) {
       for (int e = 0; e < EC; e++) rem[e] = x[e];
     }
   };
-  // one red-black half sweep (sor_half's arithmetic for this cell)
+  // One red-black half sweep for this cell: row e of the SOR update,
+  //   x_e <- ((1 - w) d_e / w x_e + b_e - sum_f c_fe y_fe - sum_g A_eg x_g) w / d_e,
+  // groups in order (x_g new for g < e).  Each row's sum over the old
+  // iterates (g > e) is formed first; each new x_e then enters the later
+  // rows at once, so that a row waits on one multiply-add of the previous.
   auto half = [&](int h) {
     if (colour != h) return;
-    float u[EC];
+    float r[EC];
 #pragma unroll
     for (int e = 0; e < EC; e++) {
       float v = b[e];
 #pragma unroll
       for (int f = 0; f < 4; f++) v -= nbc[f][e] * xs[nsl[f] * XS + e];
-      u[e] = v;
+#pragma unroll
+      for (int gg = e + 1; gg < EC; gg++) v -= aoff[e][gg - 1] * x[gg];
+      r[e] = v;
     }
 #pragma unroll
     for (int e = 0; e < EC; e++) {
-      float s0 = 0.0f, s1 = 0.0f;
+      x[e] = (sa[e] * x[e] + r[e]) * sb[e];
 #pragma unroll
-      for (int gg = 0; gg < EC; gg++)
-        if (gg != e) {
-          const float v = aoff[e][gg < e ? gg : gg - 1] * x[gg];
-          if (gg & 1) s1 -= v;
-          else s0 -= v;
-        }
-      x[e] = (sa[e] * x[e] + (u[e] + (s0 + s1))) * sb[e];
+      for (int ee = e + 1; ee < EC; ee++) r[ee] -= aoff[ee][e] * x[e];
     }
     publish();
   };
@@ -936,9 +950,9 @@ cmfd_cells_kernel(const CmfdArgs a) {
     int li = 0;
     while (li < kMaxLinearIters) {
       half(0);
-      barrier();
+      sweep_barrier(0);
       half(1);
-      barrier();
+      sweep_barrier(1);
       sweeps++;
       float fo[EC], fn[EC];
       if (li == 0 || li + 1 >= kMinIters) fission_to(ls_new);

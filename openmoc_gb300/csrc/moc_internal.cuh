@@ -425,8 +425,11 @@ struct CmfdArgs {
 // Threads a block of the cell-parallel coarse solve may hold for E coarse
 // groups (one cell each, its coefficients in registers), and the blocks of
 // a cluster at most.
+#ifndef MOC_CMFD_CELLS_THREADS_HI
+#define MOC_CMFD_CELLS_THREADS_HI 320
+#endif
 constexpr int cmfd_cells_threads(int E) {
-  return E <= 2 ? 768 : E <= 4 ? 512 : E <= 6 ? 384 : 320;
+  return E <= 2 ? 768 : E <= 4 ? 512 : E <= 6 ? 384 : MOC_CMFD_CELLS_THREADS_HI;
 }
 constexpr int kCmfdMaxClusterBlocks = 8;
 constexpr int kCmfdMaxCellGroups = 8;
