@@ -495,6 +495,9 @@ def run_gpu(args):
                 core = lat.core_51x51(device=local)
             out["cmfd"] = cmfd_acceleration(core, local, label="51x51 core, 7 groups",
                                             groups=[[1, 2, 3], [4, 5, 6, 7]])
+            # and the assembly whose sweeps are cheap (8 coarse groups)
+            out["cmfd_assembly"] = cmfd_acceleration(p, local, coarse_groups=8,
+                                                     label="17x17 assembly, 70 groups")
         if world == 1 and not args.no_serving and args.workload == "assembly70":
             # the second half of the headline: the request stream through the
             # batched server against the plain per-solve loop
@@ -512,7 +515,8 @@ def cmfd_acceleration(p, device, tol=1e-5, coarse_groups=8, label=None, groups=N
     """Time to solution, computeEigenvalue to a 1e-5 fission-source
     residual, without and with CMFD (pin-cell mesh, the groups condensed to
     `coarse_groups` contiguous bands): iterations, wall seconds, and the
-    coarse solve's power iterations and SOR sweeps."""
+    coarse solve's power iterations and SOR sweeps; the CMFD solve with the
+    coarse power iteration cell-parallel (the default) and on one block."""
     from openmoc_gb300 import Cmfd, GB300Solver
     G = p.num_groups
     bands = ([np.array(g) for g in groups] if groups is not None
@@ -521,13 +525,15 @@ def cmfd_acceleration(p, device, tol=1e-5, coarse_groups=8, label=None, groups=N
                                  f"{G} groups")
                        + f"; CMFD on the pin mesh with {len(bands)} coarse groups",
            "tolerance": tol}
-    for name, use in (("plain", False), ("cmfd", True)):
+    for name, use, kind in (("plain", False, None), ("cmfd", True, "auto"),
+                            ("cmfd_one_block", True, "block")):
         s = GB300Solver(p, device=device)
         s.setConvergenceThreshold(tol)
         if use:
             c = Cmfd()
             c.setLatticeStructure(int(p.meta.get("nx", 17)), int(p.meta.get("ny", 17)))
             c.setGroupStructure([b.tolist() for b in bands])
+            c.setDeviceSolver(kind)
             s.setCmfd(c)
         s.computeEigenvalue(5, 1)                 # tuning and module load
         t0 = time.perf_counter()
@@ -542,26 +548,39 @@ def cmfd_acceleration(p, device, tol=1e-5, coarse_groups=8, label=None, groups=N
             res[name]["coarse_sor_sweeps_last"] = info["linear_iterations"]
         s.close()
     res["speedup"] = res["plain"]["seconds"] / res["cmfd"]["seconds"]
+    res["speedup_one_block"] = res["plain"]["seconds"] / res["cmfd_one_block"]["seconds"]
     res["keff_difference"] = res["cmfd"]["keff"] - res["plain"]["keff"]
     return res
 
 
-def cmfd_core_solve(device=0):
-    """The CMFD-accelerated solve of cmfd_acceleration's core alone (pin
-    mesh, two coarse groups, 1e-5), on a device-traced core."""
+def cmfd_solve_only(workload="core", kind="auto", device=0):
+    """One CMFD-accelerated solve alone (for profiling), to 1e-5: the 51x51
+    core traced on the device (pin mesh, two coarse groups) or the 17x17
+    70-group assembly (pin mesh, 8 coarse groups), with the coarse power
+    iteration cell-parallel ("cells"), on one block ("block") or chosen
+    ("auto"); after a 5-iteration warm-up solve."""
     from openmoc_gb300 import Cmfd, GB300Solver
     from openmoc_gb300 import lattice as lat
-    p = lat.core_51x51(device=device)
+    if workload == "core":
+        p, n = lat.core_51x51(device=device), 51
+        bands = [[1, 2, 3], [4, 5, 6, 7]]
+        label = "51x51 core, 7 groups; CMFD on the pin mesh with 2 coarse groups"
+    else:
+        p, n = lat.assembly_17x17(), 17
+        bands = [b.tolist() for b in np.array_split(np.arange(1, 71), 8)]
+        label = "17x17 assembly, 70 groups; CMFD on the pin mesh with 8 coarse groups"
     s = GB300Solver(p, device=device)
     s.setConvergenceThreshold(1e-5)
     c = Cmfd()
-    c.setLatticeStructure(51, 51)
-    c.setGroupStructure([[1, 2, 3], [4, 5, 6, 7]])
+    c.setLatticeStructure(n, n)
+    c.setGroupStructure(bands)
+    c.setDeviceSolver(kind)
     s.setCmfd(c)
+    s.computeEigenvalue(5, 1)
     t0 = time.perf_counter()
     s.computeEigenvalue(1000, 1)
     dt = time.perf_counter() - t0
-    out = {"workload": "51x51 core, 7 groups; CMFD on the pin mesh with 2 coarse groups",
+    out = {"workload": label, "device_solver": kind,
            "iterations": s.getNumIterations(), "seconds": dt, "keff": s.getKeff(),
            "cmfd": s.getCmfdInfo()}
     s.close()
@@ -974,17 +993,19 @@ def main():
                     help="skip the track-generation timing (host vs device ray tracing)")
     ap.add_argument("--no-cmfd", action="store_true",
                     help="leave the CMFD time-to-solution comparison out")
-    ap.add_argument("--cmfd-only", action="store_true",
-                    help="only the CMFD-accelerated solve of the 51x51 core (for "
-                         "profiling): prints its iterations, seconds and coarse-solve "
-                         "statistics")
+    ap.add_argument("--cmfd-only", nargs="?", const="core", choices=("core", "assembly"),
+                    help="only one CMFD-accelerated solve (for profiling): the 51x51 "
+                         "core (default) or the 17x17 70-group assembly; prints its "
+                         "iterations, seconds and coarse-solve statistics")
+    ap.add_argument("--cmfd-solver", default="auto", choices=("auto", "cells", "block"),
+                    help="with --cmfd-only: the device coarse solve")
     ap.add_argument("--no-serving", action="store_true",
                     help="leave the request-stream benchmark out of the default line")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.cmfd_only:
-        print(json.dumps(cmfd_core_solve()), flush=True)
+        print(json.dumps(cmfd_solve_only(args.cmfd_only, args.cmfd_solver)), flush=True)
     elif args.impl == "reference":
         run_reference(args)
     elif args.serving:

@@ -366,8 +366,16 @@ __device__ void collapse_one(const CmfdArgs& a, const Work& k, int c, int e) {
     chi_t += (double) a.chi_m[m * E + e] * prod;
     prod_tot += prod;
   }
+  // the cell's coarse scattering row, accumulated in registers for up to
+  // kRowRegs coarse groups (else in place)
+  constexpr int kRowRegs = 8;
   float* ss_row = k.sig_s + (int64_t) ce * E;
-  for (int g = 0; g < E; g++) ss_row[g] = 0.0f;
+  float acc[kRowRegs];
+  const bool in_regs = E <= kRowRegs;
+#pragma unroll
+  for (int g = 0; g < kRowRegs; g++) acc[g] = 0.0f;
+  if (!in_regs)
+    for (int g = 0; g < E; g++) ss_row[g] = 0.0f;
   double total = 0.0, nuf = 0.0, rxn = 0.0, dsum = 0.0;
   for (int h = a.gstart[e]; h < a.gstart[e + 1]; h++) {
     double r = 0.0, t = 0.0;
@@ -378,12 +386,22 @@ __device__ void collapse_one(const CmfdArgs& a, const Work& k, int c, int e) {
       t += (double) a.st[m * G + h] * s;
       nuf += (double) a.nf[m * G + h] * s;
       const float* sr = a.ss_m + ((int64_t) m * G + h) * E;
-      for (int g = 0; g < E; g++) ss_row[g] += (float) ((double) sr[g] * s);
+      if (in_regs) {
+#pragma unroll
+        for (int g = 0; g < kRowRegs; g++)
+          if (g < E) acc[g] += (float) ((double) sr[g] * s);
+      } else {
+        for (int g = 0; g < E; g++) ss_row[g] += (float) ((double) sr[g] * s);
+      }
     }
     total += t;
     rxn += r;
     if (fabs(t) > fabs(r) * (double) FLT_EPSILON) dsum += r / (3.0 * (t / r));
   }
+  if (in_regs)
+#pragma unroll
+    for (int g = 0; g < kRowRegs; g++)
+      if (g < E) ss_row[g] = acc[g];
   if (rxn <= 0.0) {
     rxn = kZeroSigmaT;
     dsum = kZeroSigmaT;
@@ -726,19 +744,87 @@ __device__ bool dd_linear_solve(const CmfdArgs& a, const Work& k,
 __host__ __device__ constexpr int cells_xs_stride(int E) {
   return E <= 2 ? E : E <= 4 ? 4 : 12;
 }
-// Per-thread vectors in shared memory, [kCellVecs][E][threads]: the linear
-// solve's old and new fission sources, the diagonally dominant solve's old
-// and new sources, its right side and its diagonal increments.
-constexpr int kCellVecs = 6;
+// Each thread's own rows in shared memory, contiguous so that they move in
+// 16-byte (8-byte for E = 2) vectors: the cell's fission matrix M [E][EP],
+// kCellVecs vectors of EP floats (the linear solve's old and new fission
+// sources, and A's diagonal, read where the SOR factors are formed), and
+// from 7 coarse groups on the couplings to the four neighbours [4][EP]
+// (which then leave the registers).  EP pads E to the vector width; the
+// thread stride is padded to an odd number of vectors so that consecutive
+// threads fall on distinct banks.
+constexpr int kCellVecs = 3;
+constexpr int kDiagVec = 2;
+__host__ __device__ constexpr bool cells_nbc_shared(int E) { return E >= 7; }
+__host__ __device__ constexpr int cells_ep(int E) {
+  return E <= 2 ? E : 4 * ((E + 3) / 4);
+}
+__host__ __device__ constexpr int cells_row_words(int E) {
+  return (E + kCellVecs + (cells_nbc_shared(E) ? 4 : 0)) * cells_ep(E);
+}
+__host__ __device__ constexpr int cells_row_stride(int E) {
+  return E == 1 ? cells_row_words(E)
+         : E == 2 ? ((cells_row_words(E) / 2) % 2 == 0 ? cells_row_words(E) + 2
+                                                        : cells_row_words(E))
+         : ((cells_row_words(E) / 4) % 2 == 0 ? cells_row_words(E) + 4
+                                               : cells_row_words(E));
+}
+
+// A cell's EC iterates at p (a slot, cells_xs_stride(EC) floats, 8- or
+// 16-byte aligned): in one or two vector accesses.
+template <int EC>
+__device__ __forceinline__ void load_cell(const float* p, float (&v)[EC]) {
+  if constexpr (EC == 1) {
+    v[0] = p[0];
+  } else if constexpr (EC == 2) {
+    const float2 q = *reinterpret_cast<const float2*>(p);
+    v[0] = q.x;
+    v[1] = q.y;
+  } else {
+#pragma unroll
+    for (int k = 0; k < (EC + 3) / 4; k++) {
+      const float4 q = reinterpret_cast<const float4*>(p)[k];
+      const float qq[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+        if (4 * k + i < EC) v[4 * k + i] = qq[i];
+    }
+  }
+}
+template <int EC>
+__device__ __forceinline__ void store_cell(float* p, const float (&v)[EC]) {
+  if constexpr (EC == 1) {
+    p[0] = v[0];
+  } else if constexpr (EC == 2) {
+    *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < (EC + 3) / 4; k++) {
+      float qq[4];
+#pragma unroll
+      for (int i = 0; i < 4; i++) qq[i] = (4 * k + i < EC) ? v[4 * k + i] : 0.0f;
+      reinterpret_cast<float4*>(p)[k] = make_float4(qq[0], qq[1], qq[2], qq[3]);
+    }
+  }
+}
 
 // The convergence state of the nested solves, kept by thread 0 alone (in
 // shared memory, so that it holds no registers in the other threads).
+// The judgements are threshold tests on residuals formed from FP32 sums,
+// so they run in FP32 (an SM issues FP64 at a small fraction of that rate,
+// and thread 0's chain of them held every block).
 struct CellsJudge {
-  double linit, inv_linit, min_res, stall_res, tol;      // linear solve
-  double dd_initial, dd_inv_initial, dd_min_res, dd_stall_res;
-  double initial, inv_initial, e_stall_res, inv_c;       // power iteration
+  float linit, inv_linit, min_res, stall_res, tol;      // linear solve
+  float dd_initial, dd_inv_initial, dd_min_res, dd_stall_res;
+  float initial, inv_initial, e_stall_res, inv_c;       // power iteration
   int stall_li, stall_it, stall_p;
 };
+
+// a + b = s + e exactly (Knuth's TwoSum)
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
 
 template <int EC>
 __global__ void __launch_bounds__(cmfd_cells_threads(EC), 1)
@@ -753,14 +839,17 @@ cmfd_cells_kernel(const CmfdArgs a) {
   const int NT = NB * T, gid = rank * T + t;
   const int C = a.C;
   extern __shared__ float4 s_dyn[];
+  constexpr int EP = cells_ep(EC), RS = cells_row_stride(EC);
   float* xs = reinterpret_cast<float*>(s_dyn);       // [slots][XS]
-  float* mm = xs + a.map_slots * XS;                  // [EC * EC][T]
-  float* vec = mm + EC * EC * T;                      // [kCellVecs][EC][T]
+  // this thread's rows: M [EC][EP], then the vectors
+  float* row = xs + a.map_slots * XS + t * RS;
+  float* mm = row;
   __shared__ double red[33];
+  __shared__ float2 red2[32];
   __shared__ double part[2][kCmfdMaxClusterBlocks];   // block totals
   __shared__ CellsJudge J;
   int buf = 0;
-  auto V = [&](int v, int e) -> float& { return vec[(v * EC + e) * T + t]; };
+  auto vrow = [&](int v) { return row + EC * EP + v * EP; };
   auto barrier = [&]() {
     if (NB > 1) cg::this_cluster().sync();
     else __syncthreads();
@@ -792,39 +881,42 @@ cmfd_cells_kernel(const CmfdArgs a) {
   for (int f = 0; f < 4; f++) nsl[f] = a.map_nslot[f * NT + gid];
 #pragma unroll
   for (int q = 0; q < 2; q++) push[q] = a.map_push[q * NT + gid];
-  float x[EC], b[EC], diag[EC], sa[EC], sb[EC], nbc[4][EC], aoff[EC][EO];
+  constexpr bool kNbcShared = cells_nbc_shared(EC);
+  float* nbs = row + (EC + kCellVecs) * EP;   // [4][EP] when kNbcShared
+  float x[EC], b[EC], sa[EC], sb[EC], nbc[kNbcShared ? 1 : 4][EC], aoff[EC][EO];
 #pragma unroll
   for (int e = 0; e < EC; e++) {
     x[e] = has ? g.x[e * C + j] : 0.0f;
     b[e] = 0.0f;
-    diag[e] = has ? g.A[(e * EC + e) * C + j] : 1.0f;
+    vrow(kDiagVec)[e] = has ? g.A[(e * EC + e) * C + j] : 1.0f;
 #pragma unroll
     for (int q = 0; q < EO; q++) {
       const int gg = q < e ? q : q + 1;
       aoff[e][q] = (has && EC > 1) ? g.A[(e * EC + gg) * C + j] : 0.0f;
     }
 #pragma unroll
-    for (int f = 0; f < 4; f++)
-      nbc[f][e] = has ? g.nb[(f * EC + e) * C + j] : 0.0f;
+    for (int f = 0; f < 4; f++) {
+      const float v = has ? g.nb[(f * EC + e) * C + j] : 0.0f;
+      if constexpr (kNbcShared) nbs[f * EP + e] = v;
+      else nbc[f][e] = v;
+    }
+    float mr[EC];
 #pragma unroll
-    for (int gg = 0; gg < EC; gg++)
-      mm[(e * EC + gg) * T + t] = has ? g.M[(e * EC + gg) * C + j] : 0.0f;
+    for (int gg = 0; gg < EC; gg++) mr[gg] = has ? g.M[(e * EC + gg) * C + j] : 0.0f;
+    store_cell<EC>(mm + e * EP, mr);
   }
   const float w = a.sor;
 
   // this cell's iterate into its slot and into the copies other blocks hold
   auto publish = [&]() {
     if (!has) return;
-    float* me = xs + t * XS;
-#pragma unroll
-    for (int e = 0; e < EC; e++) me[e] = x[e];
+    store_cell<EC>(xs + t * XS, x);
 #pragma unroll
     for (int q = 0; q < 2; q++) {
       if (push[q] < 0) continue;
-      float* rem = cg::this_cluster().map_shared_rank(xs, push[q] >> 24) +
-                   (push[q] & 0xFFFFFF) * XS;
-#pragma unroll
-      for (int e = 0; e < EC; e++) rem[e] = x[e];
+      store_cell<EC>(cg::this_cluster().map_shared_rank(xs, push[q] >> 24) +
+                         (push[q] & 0xFFFFFF) * XS,
+                     x);
     }
   };
   // One red-black half sweep for this cell: row e of the SOR update,
@@ -834,12 +926,27 @@ cmfd_cells_kernel(const CmfdArgs a) {
   // rows at once, so that a row waits on one multiply-add of the previous.
   auto half = [&](int h) {
     if (colour != h) return;
+    float y[4][EC];   // the neighbours' iterates
+#pragma unroll
+    for (int f = 0; f < 4; f++) load_cell<EC>(xs + nsl[f] * XS, y[f]);
     float r[EC];
 #pragma unroll
-    for (int e = 0; e < EC; e++) {
-      float v = b[e];
+    for (int e = 0; e < EC; e++) r[e] = b[e];
 #pragma unroll
-      for (int f = 0; f < 4; f++) v -= nbc[f][e] * xs[nsl[f] * XS + e];
+    for (int f = 0; f < 4; f++) {
+      if constexpr (kNbcShared) {
+        float cf[EC];
+        load_cell<EC>(nbs + f * EP, cf);
+#pragma unroll
+        for (int e = 0; e < EC; e++) r[e] -= cf[e] * y[f][e];
+      } else {
+#pragma unroll
+        for (int e = 0; e < EC; e++) r[e] -= nbc[f][e] * y[f][e];
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < EC; e++) {
+      float v = r[e];
 #pragma unroll
       for (int gg = e + 1; gg < EC; gg++) v -= aoff[e][gg - 1] * x[gg];
       r[e] = v;
@@ -855,37 +962,56 @@ cmfd_cells_kernel(const CmfdArgs a) {
   auto sor_factors = [&]() {
 #pragma unroll
     for (int e = 0; e < EC; e++) {
-      sa[e] = (1.0f - w) * (diag[e] / w);
-      sb[e] = w / diag[e];
+      const float d = vrow(kDiagVec)[e];
+      sa[e] = (1.0f - w) * (d / w);
+      sb[e] = w / d;
     }
   };
   // out = M v for this cell
   auto fission = [&](const float (&v)[EC], float (&out)[EC]) {
 #pragma unroll
     for (int e = 0; e < EC; e++) {
+      float mr[EC];
+      load_cell<EC>(mm + e * EP, mr);
       float s = 0.0f;
 #pragma unroll
-      for (int gg = 0; gg < EC; gg++) s += mm[(e * EC + gg) * T + t] * v[gg];
+      for (int gg = 0; gg < EC; gg++) s += mr[gg] * v[gg];
       out[e] = s;
     }
   };
   auto fission_to = [&](int vi) {
     float o[EC];
     fission(x, o);
-#pragma unroll
-    for (int e = 0; e < EC; e++) V(vi, e) = o[e];
+    store_cell<EC>(vrow(vi), o);
   };
   // finish(the sum over all cells of every thread's v) for every thread:
-  // FP32 within a warp, FP64 across warps and blocks (blocks in order)
+  // within a warp and across warps FP32 trees of exact pair sums carrying
+  // the rounding errors, across blocks FP64 (blocks in order)
   auto total = [&](float v, auto&& finish) -> double {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    float c = 0.0f;
+    for (int o = 16; o > 0; o >>= 1) {
+      const float vo = __shfl_xor_sync(0xffffffffu, v, o);
+      const float co = __shfl_xor_sync(0xffffffffu, c, o);
+      float e;
+      two_sum(v, vo, v, e);
+      c += co + e;
+    }
     const int wi = t >> 5, lane = t & 31;
-    if (lane == 0) red[wi] = (double) v;
+    if (lane == 0) red2[wi] = make_float2(v, c);
     __syncthreads();
     double s = 0.0;
     if (wi == 0) {
-      s = lane < (T >> 5) ? red[lane] : 0.0;
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      const float2 q = lane < (T >> 5) ? red2[lane] : make_float2(0.0f, 0.0f);
+      v = q.x;
+      c = q.y;
+      for (int o = 16; o > 0; o >>= 1) {
+        const float vo = __shfl_xor_sync(0xffffffffu, v, o);
+        const float co = __shfl_xor_sync(0xffffffffu, c, o);
+        float e;
+        two_sum(v, vo, v, e);
+        c += co + e;
+      }
+      s = (double) v + (double) c;
     }
     if (NB > 1) {
       if (t == 0)
@@ -908,7 +1034,7 @@ cmfd_cells_kernel(const CmfdArgs a) {
     for (int e = 0; e < EC; e++) s.add(v[e]);
     return has ? s.value() : 0.0f;
   };
-  if (t == 0) J.inv_c = 1.0 / (double) max(C, 1);
+  if (t == 0) J.inv_c = 1.0f / (float) max(C, 1);
   // computeRMSE of this cell's change from y to xv, judged by thread 0
   auto rmse = [&](const float (&xv)[EC], const float (&y)[EC], auto&& judge) {
     float r2 = 0.0f;
@@ -925,22 +1051,19 @@ cmfd_cells_kernel(const CmfdArgs a) {
       }
     }
     return total(r2, [&](double tot) {
-      return judge((double) sqrtf((float) (tot * J.inv_c)));
+      return judge(sqrtf((float) tot * J.inv_c));
     });
   };
-  auto load = [&](int vi, float (&o)[EC]) {
-#pragma unroll
-    for (int e = 0; e < EC; e++) o[e] = V(vi, e);
-  };
+  auto load = [&](int vi, float (&o)[EC]) { load_cell<EC>(vrow(vi), o); };
 
   int sweeps = 0, power = 0;
   // linearSolve (src/linalg.cpp:179-385), as linear_solve
   auto linear = [&](double tol) -> bool {
     if (t == 0) {
-      J.tol = fmax(kLinalgTol, tol);
-      J.linit = 0.0;
+      J.tol = (float) fmax(kLinalgTol, tol);
+      J.linit = 0.0f;
       J.inv_linit = INFINITY;
-      J.min_res = 1e6;
+      J.min_res = 1e6f;
       J.stall_res = INFINITY;
       J.stall_li = 0;
     }
@@ -959,23 +1082,24 @@ cmfd_cells_kernel(const CmfdArgs a) {
       if (li == 0) {
         load(ls_new, fn);
         load(ls_old, fo);
-        rmse(fn, fo, [&](double r) {
-          J.inv_linit = r > 0.0 ? 1.0 / r : INFINITY;
-          return J.linit = r;
+        rmse(fn, fo, [&](float r) {
+          J.inv_linit = r > 0.0f ? 1.0f / r : INFINITY;
+          J.linit = r;
+          return 0.0;
         });
       }
       li++;
       if (li > kMinIters) {
         load(ls_new, fn);
         load(ls_old, fo);
-        const double verdict = rmse(fn, fo, [&](double r) {
-          J.min_res = fmin(J.min_res, r);
-          if ((r > 1e3 * J.min_res && J.min_res > kNoiseFloor) || !isfinite(r))
+        const double verdict = rmse(fn, fo, [&](float r) {
+          J.min_res = fminf(J.min_res, r);
+          if ((r > 1e3f * J.min_res && J.min_res > (float) kNoiseFloor) || !isfinite(r))
             return -1.0;
-          const double q = J.linit > 0.0 ? r * J.inv_linit : INFINITY;
-          if (q < 0.1 || r < J.tol) return 1.0;
+          const float q = J.linit > 0.0f ? r * J.inv_linit : INFINITY;
+          if (q < 0.1f || r < J.tol) return 1.0;
           if (li - J.stall_li >= kStallWindow) {
-            if (r < kStallMax && r > 0.5 * J.stall_res) return 1.0;
+            if (r < (float) kStallMax && r > 0.5f * J.stall_res) return 1.0;
             J.stall_res = r;
             J.stall_li = li;
           }
@@ -996,6 +1120,20 @@ cmfd_cells_kernel(const CmfdArgs a) {
   // ddLinearSolve (src/linalg.cpp:717-900), as dd_linear_solve; the
   // increments in vector 5, the plain right side in vector 4
   auto dd_linear = [&](double tol) -> bool {
+    // the increments, the plain right side and the old / new sources in the
+    // solve's global scratch (colour order), rarely touched
+    auto gv = [&](float* v, int e) -> float& { return v[e * C + j]; };
+    auto fission_g = [&](float* v) {
+      float o[EC];
+      fission(x, o);
+      if (has)
+#pragma unroll
+        for (int e = 0; e < EC; e++) gv(v, e) = o[e];
+    };
+    auto load_g = [&](float* v, float (&o)[EC]) {
+#pragma unroll
+      for (int e = 0; e < EC; e++) o[e] = has ? gv(v, e) : 0.0f;
+    };
 #pragma unroll
     for (int e = 0; e < EC; e++) {
       double s = 0.0;
@@ -1003,43 +1141,52 @@ cmfd_cells_kernel(const CmfdArgs a) {
       for (int q = 0; q < EO; q++)
         if (EC > 1) s += fabsf(aoff[e][q]);
 #pragma unroll
-      for (int f = 0; f < 4; f++) s += fabsf(nbc[f][e]);
-      const float dd = s > (double) diag[e] ? (float) (s - diag[e]) : 0.0f;
-      V(5, e) = dd;
-      diag[e] = diag[e] + dd;
-      V(4, e) = b[e];
+      for (int f = 0; f < 4; f++) {
+        if constexpr (kNbcShared) s += fabsf(nbs[f * EP + e]);
+        else s += fabsf(nbc[f][e]);
+      }
+      const float d = vrow(kDiagVec)[e];
+      const float dd = s > (double) d ? (float) (s - d) : 0.0f;
+      vrow(kDiagVec)[e] = d + dd;
+      if (has) {
+        gv(g.ddv, e) = dd;
+        gv(g.rhs, e) = b[e];
+      }
     }
-    int old_src = 2, new_src = 3;
-    fission_to(new_src);
+    float* old_src = g.dd_a;
+    float* new_src = g.dd_b;
+    fission_g(new_src);
     if (t == 0) {
-      J.dd_initial = 0.0;
-      J.dd_inv_initial = 0.0;
-      J.dd_min_res = 1e6;
+      J.dd_initial = 0.0f;
+      J.dd_inv_initial = 0.0f;
+      J.dd_min_res = 1e6f;
       J.dd_stall_res = INFINITY;
       J.stall_it = 0;
     }
     for (int it = 0; it < kMaxLinearIters; it++) {
-      const int tmp = old_src;
+      float* tmp = old_src;
       old_src = new_src;
       new_src = tmp;
 #pragma unroll
-      for (int e = 0; e < EC; e++) b[e] = V(4, e) + V(5, e) * x[e];
+      for (int e = 0; e < EC; e++)
+        b[e] = has ? gv(g.rhs, e) + gv(g.ddv, e) * x[e] : 0.0f;
       linear(tol);   // a failure is only noted
-      fission_to(new_src);
+      fission_g(new_src);
       float fn[EC], fo[EC];
-      load(new_src, fn);
-      load(old_src, fo);
-      const double verdict = rmse(fn, fo, [&](double res) {
+      load_g(new_src, fn);
+      load_g(old_src, fo);
+      const double verdict = rmse(fn, fo, [&](float res) {
         if (it == 0) {
-          J.dd_initial = res < 1e-14 ? 1e-10 : res;
-          J.dd_inv_initial = 1.0 / J.dd_initial;
+          J.dd_initial = res < 1e-14f ? 1e-10f : res;
+          J.dd_inv_initial = 1.0f / J.dd_initial;
         }
-        J.dd_min_res = fmin(J.dd_min_res, res);
-        if ((res > 1e3 * J.dd_min_res && J.dd_min_res > kNoiseFloor) || !isfinite(res))
+        J.dd_min_res = fminf(J.dd_min_res, res);
+        if ((res > 1e3f * J.dd_min_res && J.dd_min_res > (float) kNoiseFloor) ||
+            !isfinite(res))
           return -1.0;
-        if (res * J.dd_inv_initial < 0.1 || res < tol) return 1.0;
+        if (res * J.dd_inv_initial < 0.1f || res < (float) tol) return 1.0;
         if (it - J.stall_it >= kStallWindow) {
-          if (res < kStallMax && res > 0.5 * J.dd_stall_res) return 1.0;
+          if (res < (float) kStallMax && res > 0.5f * J.dd_stall_res) return 1.0;
           J.dd_stall_res = res;
           J.stall_it = it;
         }
@@ -1051,8 +1198,9 @@ cmfd_cells_kernel(const CmfdArgs a) {
     }
 #pragma unroll
     for (int e = 0; e < EC; e++) {
-      diag[e] = diag[e] - V(5, e);
-      b[e] = V(4, e);
+      const float dd = has ? gv(g.ddv, e) : 0.0f;
+      vrow(kDiagVec)[e] = vrow(kDiagVec)[e] - dd;
+      b[e] = has ? gv(g.rhs, e) : 0.0f;
     }
     return true;
   };
@@ -1076,8 +1224,8 @@ cmfd_cells_kernel(const CmfdArgs a) {
       x[e] = (float) (x[e] * (rows * keff / s0));
     }
     if (t == 0) {
-      J.initial = 0.0;
-      J.inv_initial = 0.0;
+      J.initial = 0.0f;
+      J.inv_initial = 0.0f;
       J.e_stall_res = INFINITY;
       J.stall_p = 0;
     }
@@ -1101,15 +1249,15 @@ cmfd_cells_kernel(const CmfdArgs a) {
       const float kf = (float) keff;
 #pragma unroll
       for (int e = 0; e < EC; e++) sn[e] /= kf;
-      const double stop = rmse(sn, b, [&](double res) {
+      const double stop = rmse(sn, b, [&](float res) {
         if (power == 0) {
-          J.initial = res < 1e-14 ? 1e-10 : res;
-          J.inv_initial = 1.0 / J.initial;
+          J.initial = res < 1e-14f ? 1e-10f : res;
+          J.inv_initial = 1.0f / J.initial;
         }
-        if ((res * J.inv_initial < 0.03 || res < kLinalgTol) && power > kMinIters)
+        if ((res * J.inv_initial < 0.03f || res < (float) kLinalgTol) && power > kMinIters)
           return 1.0;
         if (power > kMinIters && power - J.stall_p >= kStallWindow) {
-          if (res < kStallMax && res > 0.5 * J.e_stall_res) return 1.0;
+          if (res < (float) kStallMax && res > 0.5f * J.e_stall_res) return 1.0;
           J.e_stall_res = res;
           J.stall_p = power;
         }
@@ -1417,8 +1565,8 @@ void launch_cmfd_pair_sums(const float* phi, const float* vol,
 }
 
 int64_t cmfd_cells_smem(int E, int threads, int slots) {
-  return 4 * ((int64_t) slots * cells_xs_stride(E) + (int64_t) E * E * threads +
-              (int64_t) kCellVecs * E * threads);
+  return 4 * ((int64_t) slots * cells_xs_stride(E) +
+              (int64_t) threads * cells_row_stride(E));
 }
 
 namespace {
