@@ -217,7 +217,8 @@ __host__ __device__ inline int64_t smem_item_bytes(int i, int C, int E) {
   switch (i) {
     case 4: return 16 * CE;
     case 5: return C <= 32767 ? 8 * (int64_t) C : 0;
-    case 6: return 4 * CE * (E - 1);
+    // only the instances for up to 8 coarse groups read the copy
+    case 6: return E <= 8 ? 4 * CE * (E - 1) : 0;
     default: return 4 * CE;
   }
 }

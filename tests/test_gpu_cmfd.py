@@ -23,10 +23,14 @@ def _rel(got, ref, floor):
                         np.maximum(np.abs(ref), floor * np.abs(ref).max())))
 
 
-def _cmfd(p, groups, host=False, sor=1.5):
+def _cmfd(p, groups, solver="cells", sor=1.5):
+    """solver: "cells" / "block" (the device coarse solve cell-parallel or
+    on one block) or "host" (FP64 on the host)."""
     from openmoc_gb300 import Cmfd
     c = Cmfd()
-    c.useHostSolver(host)
+    c.useHostSolver(solver == "host")
+    if solver != "host":
+        c.setDeviceSolver(solver)
     nx = p.cmfd_geometry["widths_x"].size
     ny = p.cmfd_geometry["widths_y"].size
     c.setLatticeStructure(nx, ny)
@@ -41,17 +45,17 @@ def _cmfd(p, groups, host=False, sor=1.5):
 
 @pytest.mark.parametrize("case", sorted(CMFD_CASES))
 @pytest.mark.parametrize("precision", ["f32", "f64"])
-@pytest.mark.parametrize("host", [False, True])
-def test_gpu_cmfd_matches_openmoc(case, precision, host):
-    """The coarse solve on the GPU (FP32) or on the host (FP64); the
-    linear-source case through GB300LSSolver (moments prolonged, no Larsen
-    factor)."""
+@pytest.mark.parametrize("solver", ["cells", "block", "host"])
+def test_gpu_cmfd_matches_openmoc(case, precision, solver):
+    """The coarse solve on the GPU in FP32 (cell-parallel or on one block)
+    or on the host in FP64; the linear-source case through GB300LSSolver
+    (moments prolonged, no Larsen factor)."""
     from openmoc_gb300 import GB300LSSolver, GB300Solver
     p, sc, arr = load_case(case, precision)
     s = (GB300LSSolver if p.linear_source is not None else GB300Solver)(device=0)
     s.setConvergenceThreshold(sc["tolerance"])
     s.setTrackGenerator(p)
-    s.setCmfd(_cmfd(p, CMFD_CASES[case], host, CMFD_SOR[case]))
+    s.setCmfd(_cmfd(p, CMFD_CASES[case], solver, CMFD_SOR[case]))
     s.computeEigenvalue(int(sc["max_iters"]), int(sc["res_type"]))
     info = s.getCmfdInfo()
     assert info["enabled"] and info["power_iterations"] > 25
@@ -160,8 +164,9 @@ def test_gpu_cmfd_uses_native_library():
     s.close()
 
 
-@pytest.mark.parametrize("host,k", [(False, 0), (True, 0), (False, 3)])
-def test_gpu_cmfd_matches_oracle_step_by_step(host, k):
+@pytest.mark.parametrize("solver,k", [("cells", 0), ("block", 0), ("host", 0),
+                                      ("cells", 3), ("block", 3)])
+def test_gpu_cmfd_matches_oracle_step_by_step(solver, k):
     """A generated 5 x 5 lattice (vacuum on +x and +y, water pins) on a pin
     mesh with two coarse groups, a fixed number of iterations: keff, fluxes
     and the coarse fluxes of the last coarse solve against the FP64 oracle
@@ -181,7 +186,9 @@ def test_gpu_cmfd_matches_oracle_step_by_step(host, k):
     c = Cmfd()
     c.setLatticeStructure(5, 5)
     c.setGroupStructure(groups)
-    c.useHostSolver(host)
+    c.useHostSolver(solver == "host")
+    if solver != "host":
+        c.setDeviceSolver(solver)
     if k:
         c.setKNearest(k)
     mesh, keep = c.mesh(p)
@@ -271,12 +278,35 @@ def test_gpu_cmfd_generic_instance_converges_to_unaccelerated_answer():
     s.close()
 
 
+def test_gpu_cmfd_cell_parallel_refuses_more_than_eight_coarse_groups():
+    """The cell-parallel coarse solve keeps a cell's row in registers for up
+    to 8 coarse groups: asked for it with 16, the solve is refused; "auto"
+    takes the one-block solve instead."""
+    from openmoc_gb300 import Cmfd, GB300Solver
+    from openmoc_gb300._native import MOCError
+    p = _assembly(16)
+    for kind in ("cells", "auto"):
+        s = GB300Solver(p, device=0)
+        c = Cmfd()
+        c.setLatticeStructure(17, 17)
+        c.setDeviceSolver(kind)
+        s.setCmfd(c)
+        if kind == "cells":
+            with pytest.raises(MOCError, match="cell-parallel"):
+                s.computeEigenvalue(3, 1)
+        else:
+            s.computeEigenvalue(3, 1)
+            assert s.getCmfdInfo()["power_iterations"] > 0
+        s.close()
+
+
 def test_gpu_cmfd_core_mesh_matches_oracle_step_by_step():
     """The regime of the 51 x 51 core's CMFD benchmark: a 51 x 51 pin mesh
-    (2,601 cells, 1,300 and 1,301 of each red-black colour, so each thread
-    of the device coarse solve updates two cells of a colour) with two
-    coarse groups, three fuel sets in a checkerboard of assemblies, vacuum
-    on +x and +y.  A fixed number of iterations (a coarser quadrature than
+    (2,601 cells, 1,300 and 1,301 of each red-black colour: the one-block
+    device solve updates two cells of a colour in a thread, the
+    cell-parallel one spreads the cells over a cluster of four blocks that
+    exchange their border cells) with two coarse groups, three fuel sets in
+    a checkerboard of assemblies, vacuum on +x and +y.  A fixed number of iterations (a coarser quadrature than
     the benchmark's keeps the oracle quick): keff, fluxes, the coarse fluxes
     and the coarse keff of the last coarse solve against the FP64 oracle
     CMFD (oracle/cmfd_oracle.py)."""
@@ -308,9 +338,12 @@ def test_gpu_cmfd_core_mesh_matches_oracle_step_by_step():
     iters = 6
     cmfd_eigenvalue(o, cm, iters, 1, 1e-30)
     R = p.num_fsrs
-    # the FP32 device coarse solve and the FP64 host one
-    for host in (False, True):
-        c.useHostSolver(host)
+    # the FP32 device coarse solve (cell-parallel, one block) and the FP64
+    # host one
+    for solver in ("cells", "block", "host"):
+        c.useHostSolver(solver == "host")
+        if solver != "host":
+            c.setDeviceSolver(solver)
         s = GB300Solver(device=0)
         s.setConvergenceThreshold(1e-30)
         s.setTrackGenerator(p)
@@ -319,11 +352,11 @@ def test_gpu_cmfd_core_mesh_matches_oracle_step_by_step():
         info = s.getCmfdInfo()
         assert s.getNumIterations() == iters
         assert info["enabled"] and not info["failed"]
-        assert abs(s.getKeff() - o.keff) < 2e-6, host
-        assert _rel(s.getFluxes(), o.phi.reshape(R, -1), 1e-4) < 2e-5, host
+        assert abs(s.getKeff() - o.keff) < 2e-6, solver
+        assert _rel(s.getFluxes(), o.phi.reshape(R, -1), 1e-4) < 2e-5, solver
         old, new = s.getCmfdFluxes()
         assert old.shape == (51 * 51, 2)
-        assert np.max(np.abs(new - cm.new_flux)) < 1e-4 * np.abs(cm.new_flux).max(), host
-        assert np.max(np.abs(old - cm.old_flux)) < 1e-4 * np.abs(cm.old_flux).max(), host
-        assert abs(info["keff"] - cm.keff) < 2e-6, host
+        assert np.max(np.abs(new - cm.new_flux)) < 1e-4 * np.abs(cm.new_flux).max(), solver
+        assert np.max(np.abs(old - cm.old_flux)) < 1e-4 * np.abs(cm.old_flux).max(), solver
+        assert abs(info["keff"] - cm.keff) < 2e-6, solver
         s.close()
