@@ -186,6 +186,7 @@ struct moc_ctx {
   int32_t* track_ang = nullptr;
   int32_t* next = nullptr;
   uint8_t* flags = nullptr;
+  moc::TrackRec* trec = nullptr;   // [T] in visiting order
   // quadrature
   float* weights = nullptr;
   float* inv_sin = nullptr;
@@ -449,6 +450,7 @@ int ensure_stab(moc_ctx* c) {
 
 moc::SweepArgs sweep_args(moc_ctx* c, int check_done) {
   moc::SweepArgs a{};
+  a.rec = c->trec;
   a.segs = c->segs;
   a.seg_off = c->seg_off;
   a.order = c->order;
@@ -647,6 +649,7 @@ int enqueue_sweep(moc_ctx* c, int check_done, bool timed, int ev_index) {
   bool ok;
   if (c->otf) {
     a.order = c->otf_order;
+    a.rec = nullptr;
     ok = moc::launch_otf_sweep(a, otf_args(c), c->slots, c->stream);
   } else {
     ok = c->ls ? moc::launch_ls_sweep(a, c->d.num_polar_half, c->slots,
@@ -1535,6 +1538,7 @@ int moc_destroy(moc_ctx* c) {
   dfree(c->track_ang);
   dfree(c->next);
   dfree(c->flags);
+  dfree(c->trec);
   dfree(c->weights);
   dfree(c->inv_sin);
   dfree(c->sigma_t);
@@ -1628,6 +1632,7 @@ int moc_upload_tracks(moc_ctx* c, const float* seg_len, const int32_t* seg_fsr,
   dfree(c->track_ang);
   dfree(c->next);
   dfree(c->flags);
+  dfree(c->trec);
   MOC_TRY(dalloc(&c->segs, S));
   // segments: raw lengths and FSR ids up, packed and checked on the device
   {
@@ -1686,6 +1691,23 @@ int moc_upload_tracks(moc_ctx* c, const float* seg_len, const int32_t* seg_fsr,
                       cudaMemcpyHostToDevice));
   MOC_CUDA(cudaMemcpy(c->order, order.data(), sizeof(int32_t) * T,
                       cudaMemcpyHostToDevice));
+  {
+    std::vector<moc::TrackRec> rec(T);
+    for (int64_t i = 0; i < T; i++) {
+      const int32_t t = order[i];
+      moc::TrackRec& r = rec[i];
+      r.off = seg_off[t];
+      r.t = t;
+      r.n = (int32_t) count[t];
+      r.ang = track_ang[t];
+      r.flags = flags[t];
+      r.next[0] = next32[2 * t];
+      r.next[1] = next32[2 * t + 1];
+    }
+    MOC_TRY(dalloc(&c->trec, T));
+    MOC_CUDA(cudaMemcpy(c->trec, rec.data(), sizeof(moc::TrackRec) * T,
+                        cudaMemcpyHostToDevice));
+  }
   MOC_CUDA(cudaMemcpy(c->track_ang, track_ang, sizeof(int32_t) * T,
                       cudaMemcpyHostToDevice));
   MOC_CUDA(cudaMemcpy(c->next, next32.data(), sizeof(int32_t) * 2 * T,

@@ -77,7 +77,20 @@ struct InstState {
   int dk;                            // largest |1e5 (k - k_prev)| this iteration
 };
 
+// One track as the single-problem sweeps visit it, stored in visiting
+// order (longest first) so that the streams of a warp read theirs in one
+// coalesced access: first segment, track id, segment count, angle row,
+// flags and the two connecting tracks.
+struct alignas(16) TrackRec {
+  int64_t off;
+  int32_t t, n, ang, flags, next[2];
+};
+
 struct SweepArgs {
+  // [T] tracks in visiting order, read by the single-problem one-polar
+  // instances (null, and elsewhere: order / seg_off / track_ang / flags /
+  // next are read per track)
+  const TrackRec* rec;
   const int2* segs;          // [S] {float length bits, fsr}
   const int64_t* seg_off;    // [T+1]
   const int32_t* order;      // [T] tracks by decreasing segment count

@@ -265,9 +265,16 @@ sweep_kernel(const SweepArgs a) {
   // the track and its pending scale; in a pool the solve of the track may
   // be finished (the LPS lanes of a stream share the track, so they agree
   // on skipping it)
+  // The one-polar (3D) instances read their track from its record in
+  // visiting order (coalesced; their tracks are short, so the scattered
+  // per-track reads were a tenth of their DRAM traffic); the 2D ones, whose
+  // long tracks amortise them, read per track.
+  constexpr bool kRec = PH == 1;
   int t = 0;
   float scale = 1.0f;
   bool live = stream < 2 * a.num_tracks;
+  int64_t b = 0;
+  int n = 0, ang = 0;
   if (POOL) {
     if (live) {
       t = a.order[stream >> 1];
@@ -277,13 +284,25 @@ sweep_kernel(const SweepArgs a) {
     }
   } else {
     scale = sc->scale[cur];
-    if (live) t = a.order[stream >> 1];
+    if (live && kRec && a.rec) {
+      // the track's record, in visiting order: one coalesced 32-byte read
+      const int4* rp = reinterpret_cast<const int4*>(a.rec + (stream >> 1));
+      const int4 r0 = __ldg(rp);
+      b = (int64_t) (((uint64_t) (uint32_t) r0.y << 32) | (uint32_t) r0.x);
+      t = r0.z;
+      n = r0.w;
+      ang = __ldg(&a.rec[stream >> 1].ang);
+    } else if (live) {
+      t = a.order[stream >> 1];
+    }
   }
   if (live) {
     const int dir = (int) (stream & 1);
-    const int64_t b = a.seg_off[t];
-    const int n = (int) (a.seg_off[t + 1] - b);
-    const int ang = a.track_ang[t];
+    if (POOL || !kRec || !a.rec) {
+      b = a.seg_off[t];
+      n = (int) (a.seg_off[t + 1] - b);
+      ang = a.track_ang[t];
+    }
     const int F = G * PH;
 
     // the exponent scale of each polar angle: x / h for the table, -x log2 e
@@ -503,7 +522,17 @@ sweep_kernel(const SweepArgs a) {
     // the quadrature weight of the track's polar index, which is 0 for 2D
     // tracks (src/CPUSolver.cpp:2593-2600, src/TrackTraversingAlgorithms.cpp
     // :895-905), summed over the stream's lanes, one FP64 atomic per stream
-    const int f = a.flags[t];
+    // the record's flags and connecting tracks (read again here rather
+    // than held in registers through the segment loop)
+    int4 r1 = make_int4(0, 0, 0, 0);
+    if (!POOL && kRec && a.rec) {
+      // the stream index again from the thread's coordinates (cheaper than
+      // keeping it live through the loop)
+      const int64_t gw = ((int64_t) blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+      const int64_t st2 = gw * (32 / LPS) + (threadIdx.x & 31) / LPS;
+      r1 = __ldg(reinterpret_cast<const int4*>(a.rec + (st2 >> 1)) + 1);
+    }
+    const int f = (!POOL && kRec && a.rec) ? r1.y : a.flags[t];
     if (!(f & (dir ? 8 : 4)) && a.leakage) {
       float2 acc = f2(0.0f);
 #pragma unroll
@@ -522,7 +551,8 @@ sweep_kernel(const SweepArgs a) {
       if (sub == 0) atomicAdd(a.leakage, (double) v);
     }
     if (f & (dir ? 8 : 4)) {
-      const int nt = a.next[2 * t + dir];
+      const int nt =
+          (!POOL && kRec && a.rec) ? (dir ? r1.w : r1.z) : a.next[2 * t + dir];
       const int nd = (f & (dir ? 2 : 1)) ? 0 : 1;
       float* po = psi_out + ((int64_t) nt * 2 + nd) * F;
 #pragma unroll
