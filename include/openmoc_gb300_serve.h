@@ -162,6 +162,11 @@ int moc_server_poll(moc_server* srv, int64_t* tickets, int capacity,
                     int* count);
 
 int moc_server_stats_get(moc_server* srv, moc_server_stats* out);
+/** The message of the last error inside the request loop (the call that
+ *  failed and CUDA's description), which failed the requests of its pool
+ *  with that status; "" when none.  Valid until the next call on the
+ *  server from this thread. */
+const char* moc_server_loop_error(moc_server* srv);
 
 typedef struct {
   int32_t num_groups, num_polar_half;

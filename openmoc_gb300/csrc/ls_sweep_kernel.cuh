@@ -298,10 +298,32 @@ void launch_ls_instance(const SweepArgs& a, cudaStream_t stream) {
   const size_t smem = sizeof(float) * (size_t) a.num_materials * a.ld;
   auto kern = a.cm_cell ? ls_sweep_kernel<PH, LPS, PS, true>
                         : ls_sweep_kernel<PH, LPS, PS, false>;
-  if (smem > 48 * 1024)
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int) smem);
   kern<<<(unsigned) blocks, kSweepThreads, smem, stream>>>(a);
+}
+
+// The shared-memory limit of every instance dispatch_ls_lps can launch.
+template <int PH, int LPS>
+void configure_ls_lps(int optin) {
+  raise_smem_limit(ls_sweep_kernel<PH, LPS, 1, true>, optin);
+  raise_smem_limit(ls_sweep_kernel<PH, LPS, 2, true>, optin);
+  raise_smem_limit(ls_sweep_kernel<PH, LPS, 3, true>, optin);
+  raise_smem_limit(ls_sweep_kernel<PH, LPS, 4, true>, optin);
+  raise_smem_limit(ls_sweep_kernel<PH, LPS, 5, true>, optin);
+  raise_smem_limit(ls_sweep_kernel<PH, LPS, 1, false>, optin);
+  raise_smem_limit(ls_sweep_kernel<PH, LPS, 2, false>, optin);
+  raise_smem_limit(ls_sweep_kernel<PH, LPS, 3, false>, optin);
+  raise_smem_limit(ls_sweep_kernel<PH, LPS, 4, false>, optin);
+  raise_smem_limit(ls_sweep_kernel<PH, LPS, 5, false>, optin);
+}
+
+template <int PH>
+void configure_ls(int optin) {
+  configure_ls_lps<PH, 1>(optin);
+  configure_ls_lps<PH, 2>(optin);
+  configure_ls_lps<PH, 4>(optin);
+  configure_ls_lps<PH, 8>(optin);
+  configure_ls_lps<PH, 16>(optin);
+  configure_ls_lps<PH, 32>(optin);
 }
 
 template <int PH, int LPS>

@@ -8,4 +8,6 @@ bool launch_ls_sweep_p1(const SweepArgs& a, int slots, cudaStream_t s) {
   return dispatch_ls_lps<1>(a, slots, s);
 }
 
+void configure_ls_p1(int optin) { configure_ls<1>(optin); }
+
 }  // namespace moc

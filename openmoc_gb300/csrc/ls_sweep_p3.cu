@@ -8,4 +8,6 @@ bool launch_ls_sweep_p3(const SweepArgs& a, int slots, cudaStream_t s) {
   return dispatch_ls_lps<3>(a, slots, s);
 }
 
+void configure_ls_p3(int optin) { configure_ls<3>(optin); }
+
 }  // namespace moc

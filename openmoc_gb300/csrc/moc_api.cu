@@ -448,6 +448,33 @@ int ensure_stab(moc_ctx* c) {
   return MOC_OK;
 }
 
+}  // namespace (file helpers)
+
+namespace moc {
+
+void configure_kernels() {
+  static std::mutex mu;
+  static std::vector<int> done;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return;
+  std::lock_guard<std::mutex> lk(mu);
+  if (std::find(done.begin(), done.end(), dev) != done.end()) return;
+  int optin = 0;
+  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin,
+                             dev) != cudaSuccess || optin <= 0)
+    return;
+  configure_sweeps(optin);
+  configure_ls_sweeps(optin);
+  configure_otf_sweeps(optin);
+  configure_sources(optin);
+  cudaGetLastError();   // an instance the device cannot run is left as is
+  done.push_back(dev);
+}
+
+}  // namespace moc
+
+namespace {
+
 moc::SweepArgs sweep_args(moc_ctx* c, int check_done) {
   moc::SweepArgs a{};
   a.rec = c->trec;
@@ -1459,6 +1486,7 @@ int moc_create(const moc_dims* dims, moc_ctx** out) {
   MOC_CHECK(d.device >= 0 && d.device < ndev, MOC_ERR_ARG,
             "no CUDA device " + std::to_string(d.device));
   MOC_CUDA(cudaSetDevice(d.device));
+  moc::configure_kernels();
 
   moc_ctx* c = new moc_ctx();
   c->d = d;

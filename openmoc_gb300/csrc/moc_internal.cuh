@@ -153,6 +153,26 @@ struct SweepArgs {
 
 constexpr int kMaxHotFsrs = 8;
 
+// Kernels that may take more than 48 KB of dynamic shared memory (the
+// sweeps, whose tables grow with the materials, and the source kernels)
+// have their limit raised once per device to the device's opt-in maximum,
+// when a context or a server is created: never at launch, since the server
+// launches them inside CUDA-graph captures, where changing a function
+// attribute is not captured and fails the launch.
+template <class K>
+void raise_smem_limit(K* kern, int optin) {
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, kern) != cudaSuccess) return;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       optin - (int) fa.sharedSizeBytes);
+}
+void configure_sweeps(int optin);      // sweep.cu
+void configure_ls_sweeps(int optin);   // ls_sweep_p*.cu via sweep.cu
+void configure_otf_sweeps(int optin);  // otf_sweep.cu
+void configure_sources(int optin);     // solver_kernels.cu
+// Once per device (the current one): the above with its opt-in maximum.
+void configure_kernels();
+
 struct SolverArgs {
   const float* sigma_t;      // [M][G]
   const float* sigma_s;      // [M][G][G] dest-major

@@ -261,10 +261,15 @@ void launch_otf_instance(const SweepArgs& a, const OtfArgs& o,
   const int64_t blocks = (warps + wpb - 1) / wpb;
   const size_t smem = sizeof(float) * (size_t) (a.num_materials + 1) * a.ld;
   auto kern = otf_sweep_kernel<LPS, PS>;
-  if (smem > 48 * 1024)
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int) smem);
   kern<<<(unsigned) blocks, kSweepThreads, smem, stream>>>(a, o);
+}
+
+template <int LPS>
+void configure_otf_lps(int optin) {
+  raise_smem_limit(otf_sweep_kernel<LPS, 1>, optin);
+  raise_smem_limit(otf_sweep_kernel<LPS, 2>, optin);
+  raise_smem_limit(otf_sweep_kernel<LPS, 3>, optin);
+  raise_smem_limit(otf_sweep_kernel<LPS, 4>, optin);
 }
 
 template <int LPS>
@@ -280,6 +285,15 @@ bool launch_otf_pairs(const SweepArgs& a, const OtfArgs& o, int slots,
 }
 
 }  // namespace
+
+void configure_otf_sweeps(int optin) {
+  configure_otf_lps<1>(optin);
+  configure_otf_lps<2>(optin);
+  configure_otf_lps<4>(optin);
+  configure_otf_lps<8>(optin);
+  configure_otf_lps<16>(optin);
+  configure_otf_lps<32>(optin);
+}
 
 bool launch_otf_sweep(const SweepArgs& a, const OtfArgs& o, int slots,
                       cudaStream_t s) {

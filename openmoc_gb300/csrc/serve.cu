@@ -1209,6 +1209,7 @@ int moc_server_create(const moc_server_config* cfg, moc_server** out) {
   SV_CHECK(cfg->device >= 0 && cfg->device < ndev, MOC_ERR_ARG,
            "no CUDA device " + std::to_string(cfg->device));
   SV_CUDA(cudaSetDevice(cfg->device));
+  moc::configure_kernels();   // before any launch is captured into a graph
   moc_server* srv = new moc_server();
   srv->cfg = *cfg;
   // nodes of the attenuation table, as in moc_create
@@ -1385,6 +1386,14 @@ int moc_server_stats_get(moc_server* srv, moc_server_stats* out) {
   std::lock_guard<std::mutex> lk(srv->mu);
   *out = srv->stats;
   return MOC_OK;
+}
+
+const char* moc_server_loop_error(moc_server* srv) {
+  thread_local std::string copy;
+  if (!srv) return "";
+  std::lock_guard<std::mutex> lk(srv->mu);
+  copy = srv->loop_error;
+  return copy.c_str();
 }
 
 }  // extern "C"

@@ -1306,9 +1306,6 @@ void launch_sources_s(const SolverArgs& a, int iteration, int fused,
   const int staged = need <= 160 * 1024;
   const size_t smem = staged ? need : 0;
   auto kern = compute_sources_kernel<S>;
-  if (smem > 48 * 1024)
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int) smem);
   // staging costs one matrix copy per block: keep the grid near one wave
   int64_t blocks = (a.num_fsrs + kWarps - 1) / kWarps;
   if (blocks > 152 * 2) blocks = 152 * 2;
@@ -1503,9 +1500,6 @@ void launch_ls_sources_s(const SolverArgs& a, int iteration, int fused,
   const int staged = need <= 160 * 1024;
   const size_t smem = staged ? need : 0;
   auto kern = ls_sources_kernel<S>;
-  if (smem > 48 * 1024)
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int) smem);
   int64_t blocks = (a.num_fsrs + kWarps - 1) / kWarps;
   if (blocks > 152 * 2) blocks = 152 * 2;
   kern<<<(unsigned) blocks, kThreads, smem, s>>>(a, iteration, fused, staged);
@@ -1543,6 +1537,22 @@ void launch_ls_add_source(const SolverArgs& a, int update, cudaStream_t s) {
 void launch_ls_scale_moments(const SolverArgs& a, cudaStream_t s) {
   ls_scale_moments_kernel<<<grid_for(a.num_fsrs * a.ld / 2, kThreads),
                             kThreads, 0, s>>>(a);
+}
+
+void configure_sources(int optin) {
+  raise_smem_limit(compute_sources_kernel<1>, optin);
+  raise_smem_limit(compute_sources_kernel<2>, optin);
+  raise_smem_limit(compute_sources_kernel<3>, optin);
+  raise_smem_limit(compute_sources_kernel<4>, optin);
+  raise_smem_limit(compute_sources_kernel<5>, optin);
+  raise_smem_limit(compute_sources_kernel<6>, optin);
+  raise_smem_limit(compute_sources_kernel<7>, optin);
+  raise_smem_limit(compute_sources_kernel<12>, optin);
+  raise_smem_limit(ls_sources_kernel<1>, optin);
+  raise_smem_limit(ls_sources_kernel<2>, optin);
+  raise_smem_limit(ls_sources_kernel<3>, optin);
+  raise_smem_limit(ls_sources_kernel<4>, optin);
+  raise_smem_limit(ls_sources_kernel<8>, optin);
 }
 
 }  // namespace moc

@@ -10,6 +10,30 @@ bool launch_sweep_p2_e0(const SweepArgs&, int, cudaStream_t);
 bool launch_sweep_p2_e1(const SweepArgs&, int, cudaStream_t);
 bool launch_sweep_p3_e0(const SweepArgs&, int, cudaStream_t);
 bool launch_sweep_p3_e1(const SweepArgs&, int, cudaStream_t);
+void configure_sweep_p1_e0(int);
+void configure_sweep_p1_e1(int);
+void configure_sweep_p2_e0(int);
+void configure_sweep_p2_e1(int);
+void configure_sweep_p3_e0(int);
+void configure_sweep_p3_e1(int);
+void configure_ls_p1(int);
+void configure_ls_p2(int);
+void configure_ls_p3(int);
+
+void configure_sweeps(int optin) {
+  configure_sweep_p1_e0(optin);
+  configure_sweep_p1_e1(optin);
+  configure_sweep_p2_e0(optin);
+  configure_sweep_p2_e1(optin);
+  configure_sweep_p3_e0(optin);
+  configure_sweep_p3_e1(optin);
+}
+
+void configure_ls_sweeps(int optin) {
+  configure_ls_p1(optin);
+  configure_ls_p2(optin);
+  configure_ls_p3(optin);
+}
 
 __global__ void pack_materials_kernel(int2* segs, int64_t n,
                                       const int32_t* fsr_mat) {

@@ -612,10 +612,42 @@ void launch_sweep_instance(const SweepArgs& a, cudaStream_t stream) {
                  kSweepThreads
            : 0);
   auto kern = sweep_kernel<PH, LPS, PS, EXPK, MODE>;
-  if (smem > 48 * 1024)
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int) smem);
   kern<<<(unsigned) blocks, kSweepThreads, smem, stream>>>(a);
+}
+
+// The shared-memory limit of every instance dispatch_sweep_lps can launch.
+template <int PH, int LPS, int EXPK>
+void configure_sweep_lps(int optin) {
+  raise_smem_limit(sweep_kernel<PH, LPS, 1, EXPK, 0>, optin);
+  raise_smem_limit(sweep_kernel<PH, LPS, 2, EXPK, 0>, optin);
+  raise_smem_limit(sweep_kernel<PH, LPS, 3, EXPK, 0>, optin);
+  raise_smem_limit(sweep_kernel<PH, LPS, 4, EXPK, 0>, optin);
+  raise_smem_limit(sweep_kernel<PH, LPS, 5, EXPK, 0>, optin);
+  raise_smem_limit(sweep_kernel<PH, LPS, 6, EXPK, 0>, optin);
+  if constexpr (EXPK == kExpIntrinsic) {
+    raise_smem_limit(sweep_kernel<PH, LPS, 1, EXPK, 1>, optin);
+    raise_smem_limit(sweep_kernel<PH, LPS, 2, EXPK, 1>, optin);
+    raise_smem_limit(sweep_kernel<PH, LPS, 3, EXPK, 1>, optin);
+    raise_smem_limit(sweep_kernel<PH, LPS, 4, EXPK, 1>, optin);
+    raise_smem_limit(sweep_kernel<PH, LPS, 5, EXPK, 1>, optin);
+    raise_smem_limit(sweep_kernel<PH, LPS, 6, EXPK, 1>, optin);
+    raise_smem_limit(sweep_kernel<PH, LPS, 1, EXPK, 2>, optin);
+    raise_smem_limit(sweep_kernel<PH, LPS, 2, EXPK, 2>, optin);
+    raise_smem_limit(sweep_kernel<PH, LPS, 3, EXPK, 2>, optin);
+    raise_smem_limit(sweep_kernel<PH, LPS, 4, EXPK, 2>, optin);
+    raise_smem_limit(sweep_kernel<PH, LPS, 5, EXPK, 2>, optin);
+    raise_smem_limit(sweep_kernel<PH, LPS, 6, EXPK, 2>, optin);
+  }
+}
+
+template <int PH, int EXPK>
+void configure_sweep(int optin) {
+  configure_sweep_lps<PH, 1, EXPK>(optin);
+  configure_sweep_lps<PH, 2, EXPK>(optin);
+  configure_sweep_lps<PH, 4, EXPK>(optin);
+  configure_sweep_lps<PH, 8, EXPK>(optin);
+  configure_sweep_lps<PH, 16, EXPK>(optin);
+  configure_sweep_lps<PH, 32, EXPK>(optin);
 }
 
 // slots = pairs of groups per lane

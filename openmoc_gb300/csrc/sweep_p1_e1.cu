@@ -8,4 +8,6 @@ bool launch_sweep_p1_e1(const SweepArgs& a, int slots, cudaStream_t s) {
   return dispatch_sweep_lps<1, 1>(a, slots, s);
 }
 
+void configure_sweep_p1_e1(int optin) { configure_sweep<1, 1>(optin); }
+
 }  // namespace moc

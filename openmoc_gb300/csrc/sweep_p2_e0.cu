@@ -8,4 +8,6 @@ bool launch_sweep_p2_e0(const SweepArgs& a, int slots, cudaStream_t s) {
   return dispatch_sweep_lps<2, 0>(a, slots, s);
 }
 
+void configure_sweep_p2_e0(int optin) { configure_sweep<2, 0>(optin); }
+
 }  // namespace moc

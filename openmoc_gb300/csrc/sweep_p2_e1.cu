@@ -8,4 +8,6 @@ bool launch_sweep_p2_e1(const SweepArgs& a, int slots, cudaStream_t s) {
   return dispatch_sweep_lps<2, 1>(a, slots, s);
 }
 
+void configure_sweep_p2_e1(int optin) { configure_sweep<2, 1>(optin); }
+
 }  // namespace moc

@@ -8,4 +8,6 @@ bool launch_sweep_p3_e0(const SweepArgs& a, int slots, cudaStream_t s) {
   return dispatch_sweep_lps<3, 0>(a, slots, s);
 }
 
+void configure_sweep_p3_e0(int optin) { configure_sweep<3, 0>(optin); }
+
 }  // namespace moc

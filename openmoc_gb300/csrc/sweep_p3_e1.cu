@@ -8,6 +8,8 @@ bool launch_sweep_p3_e1(const SweepArgs& a, int slots, cudaStream_t s) {
   return dispatch_sweep_lps<3, 1>(a, slots, s);
 }
 
+void configure_sweep_p3_e1(int optin) { configure_sweep<3, 1>(optin); }
+
 // g(x) = 1 - exp(-x) for an array of x with the sweep's own evaluators
 // (ExpEvaluator::computeExponential, src/ExpEvaluator.h:170-183).
 __global__ void attenuation_kernel(int kind, const float* x, float* g,

@@ -105,6 +105,7 @@ _SIGS = {
     "moc_server_wait": ([_P, C.c_int64, C.c_double, C.POINTER(Result)], C.c_int),
     "moc_server_poll": ([_P, _P, C.c_int, C.POINTER(C.c_int)], C.c_int),
     "moc_server_stats_get": ([_P, C.POINTER(Stats)], C.c_int),
+    "moc_server_loop_error": ([_P], C.c_char_p),
     "moc_server_pool_stats": ([_P, C.c_int, C.POINTER(PoolStats)], C.c_int),
 }
 
@@ -255,7 +256,9 @@ class Server:
             self._h, ticket, -1.0 if timeout is None else float(timeout), C.byref(r)))
         _, _, flux = self._keep.pop(ticket)
         if r.status != 0:
-            raise _native.MOCError(r.status, f"request {ticket} failed")
+            why = self.loop_error()
+            raise _native.MOCError(r.status, f"request {ticket} failed"
+                                   + (f": {why}" if why else ""))
         return dict(keff=r.keff, iterations=r.iterations, converged=bool(r.converged),
                     residual=r.residual, pool=r.pool, flux=flux,
                     t_submit=r.t_submit, t_admit=r.t_admit, t_done=r.t_done)
@@ -269,6 +272,11 @@ class Server:
             out.extend(buf[i] for i in range(n.value))
             if n.value < 1024:
                 return out
+
+    def loop_error(self) -> str:
+        """The last error inside the request loop ("" when none): the call
+        that failed, which failed the requests of its pool."""
+        return (_lib().moc_server_loop_error(self._h) or b"").decode()
 
     def stats(self) -> dict:
         s = Stats()

@@ -43,7 +43,7 @@ def max_rel(a, b):
 # Sweep shapes (lanes per track direction, group pairs per lane) with the
 # hardware-ex2 evaluator: a pool and a single solver given the same
 # evaluator differ only in the order of the tally atomics.
-SHAPES = {2: (1, 1), 7: (4, 1), 16: (8, 1), 70: (8, 5)}
+SHAPES = {2: (1, 1), 7: (4, 1), 16: (8, 1), 70: (8, 5), 80: (8, 5)}
 
 
 def make_server(problems, max_solves, k=8, graphs=True, fixed_shape=True):
@@ -152,6 +152,53 @@ def test_continuous_admission_with_two_slots():
     st = srv.stats()
     assert st["admitted"] == len(ps) and st["completed"] == len(ps)
     assert st["graph_captures"] >= 3    # the set of live solves changed
+    srv.close()
+
+
+def test_wide_pool_with_many_materials_runs_from_graphs():
+    """A 70-group pool holding 56 pin cells at once (112 material rows): the
+    sweep's cross-section table and source ring then take more than 48 KB of
+    dynamic shared memory, and the sweep runs from captured graphs (the shape
+    is fixed, so no autotuning launch precedes the first capture); the
+    request loop reports no error and the solves match the single solver."""
+    base = lattice.pin_cell(70, 8, 0.1)
+    ps = [base.with_xs(*lattice.pack_materials(
+              lattice._fuel_mod(0, 70, 1, perturb=(2000 + i, 0.05)))) for i in range(56)]
+    srv = make_server(ps, 56, k=4)
+    tickets = [srv.submit(p, max_iters=8, threshold=NEVER) for p in ps]
+    srv.run_until_idle()
+    res = [srv.wait(t, timeout=0) for t in tickets]
+    assert srv.loop_error() == ""
+    assert all(r["iterations"] == 8 for r in res)
+    assert srv.stats()["graph_captures"] >= 1
+    for i in (0, 55):
+        ref = single(ps[i], max_iters=8)
+        assert abs(res[i]["keff"] - ref["keff"]) <= 2e-6 * ref["keff"]
+        assert max_rel(res[i]["flux"], ref["flux"]) <= 2e-5
+    srv.close()
+
+
+def test_pools_sharing_a_sweep_instance_replay_their_graphs():
+    """A 70-group and an 80-group pool sweep with the same kernel instance
+    (8 lanes x 5 group pairs) and need different shared memory for it
+    (112 and 90 material rows: about 52 and 49 KB); each replays its
+    captured graph between the other's blocks, and every solve matches the
+    single solver."""
+    def pins(G, n, seed):
+        base = lattice.pin_cell(G, 8, 0.1)
+        return [base.with_xs(*lattice.pack_materials(
+                    lattice._fuel_mod(0, G, 1, perturb=(seed + i, 0.05)))) for i in range(n)]
+    ps = pins(70, 56, 3000) + pins(80, 45, 4000)
+    srv = make_server(ps, 56, k=4)
+    tickets = [srv.submit(p, max_iters=12, threshold=NEVER) for p in ps]
+    srv.run_until_idle()
+    res = [srv.wait(t, timeout=0) for t in tickets]
+    assert srv.loop_error() == ""
+    assert all(r["iterations"] == 12 for r in res)
+    for i in (0, 56):
+        ref = single(ps[i], max_iters=12)
+        assert abs(res[i]["keff"] - ref["keff"]) <= 2e-6 * ref["keff"]
+        assert max_rel(res[i]["flux"], ref["flux"]) <= 2e-5
     srv.close()
 
 
