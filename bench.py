@@ -487,6 +487,15 @@ def run_gpu(args):
         core = None
         if world == 1 and args.workload == "assembly70" and not args.no_raytrace:
             out["ray_tracing"], core = ray_tracing(local)
+        if world == 1 and args.workload == "assembly70" and not args.no_configs:
+            # the other single-solve configurations, measured in the same run
+            from openmoc_gb300 import lattice as lat
+            if core is None:
+                core = lat.core_51x51(device=local)
+            out["configs"] = {
+                "core51": single_config(core, WORKLOADS["core51"], local),
+                "assembly3d": single_config(lat.assembly_17x17_3d(),
+                                            WORKLOADS["assembly3d"], local)}
         if world == 1 and args.workload == "assembly70" and not args.no_cmfd:
             # the regime CMFD is for: a core whose sweeps are expensive and
             # whose plain source iteration needs a thousand iterations
@@ -585,6 +594,27 @@ def cmfd_solve_only(workload="core", kind="auto", device=0):
            "cmfd": s.getCmfdInfo()}
     s.close()
     return out
+
+
+def single_config(p, label, device, steps=10):
+    """One more benchmark configuration solved alone: the autotuned sweep
+    shape and the device-timed source iteration (L2 flushed between
+    iterations, as for the headline), integrations per second."""
+    from openmoc_gb300 import GB300Solver
+    from openmoc_gb300.solver import FISSION_SOURCE
+    s = GB300Solver(p, device=device)
+    lps, slots, exp_kind = s.autotune()
+    s.benchIterations(3, FISSION_SOURCE, True)
+    st, sw = s.benchIterations(steps, FISSION_SOURCE, True)
+    s.close()
+    step = float(np.mean(st))
+    return {"workload": label, "fsrs": int(p.num_fsrs), "tracks": int(p.num_tracks),
+            "segments": int(p.num_segments), "groups": int(p.num_groups),
+            "integrations_per_sweep": int(p.integrations_per_sweep),
+            "sweep_shape": [int(lps), int(slots), "ex2" if exp_kind else "table"],
+            "ms_per_step": step, "sweep_ms_per_step": float(np.mean(sw)),
+            "value": p.integrations_per_sweep / (step * 1e-3),
+            "unit": "integrations/s", "steps": steps}
 
 
 def ray_tracing(device):
@@ -989,6 +1019,8 @@ def main():
     ap.add_argument("--serving-no-priorities", action="store_true")
     ap.add_argument("--serving-hot-mb", type=int, default=32,
                     help="L2 budget of the live solves' sources and tallies")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="leave the 51x51 core and 3D assembly single-solve figures out")
     ap.add_argument("--no-raytrace", action="store_true",
                     help="skip the track-generation timing (host vs device ray tracing)")
     ap.add_argument("--no-cmfd", action="store_true",
