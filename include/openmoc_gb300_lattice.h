@@ -84,14 +84,19 @@ int moc_lattice_export_ls(moc_lattice* lat, float* seg_x, float* seg_y,
  *  below fuel_height, one homogeneous moderator region above; reflective
  *  radially (required of the radial lattice), vacuum at bottom and top;
  *  Gauss-Legendre polar angles (2, 4 or 6) and axial spacing z_spacing.
- *  The workload shape of OpenMOC's TrackGenerator3D with EXPLICIT_3D
- *  segments (src/TrackGenerator3D.cpp), with a laydown of its own whose 3D
- *  links are exact.  The result has one polar value per track (3D layout of
- *  include/openmoc_gb300.h) and is read with moc_lattice_sizes/export. */
+ *  OpenMOC's own 3D laydown (TrackGenerator3D with EXPLICIT_3D segments,
+ *  src/TrackGenerator3D.cpp: corrected polar angles, chains of radial
+ *  tracks, z-stacks, track numbering) over the radial tracks.  The result
+ *  has one polar value per track (3D layout of include/openmoc_gb300.h; an
+ *  angle row per azimuthal and polar angle, a * num_polar + p) and is read
+ *  with moc_lattice_sizes/export. */
 int moc_lattice_extrude(const moc_lattice* radial, double height,
                         double fuel_height, double z_spacing,
                         int32_t num_polar, int32_t num_threads,
                         moc_lattice** out);
+/** Start and end point of every 3D track of an extruded lattice, [T][6]
+ *  (x0, y0, z0, x1, y1, z1). */
+int moc_lattice_export_ends3d(moc_lattice* lat, double* ends);
 
 /** On-the-fly description of an extruded lattice's 3D tracks (the arrays
  *  of moc_otf_tracks in openmoc_gb300.h): per 3D track [T][4] (radial

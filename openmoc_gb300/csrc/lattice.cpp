@@ -349,6 +349,7 @@ extern "C" int moc_lattice_generate(const moc_lattice_spec* sp,
 
   std::vector<std::vector<float>> seg_len_t(T);
   std::vector<std::vector<uint64_t>> seg_key_t(T);
+  std::vector<std::vector<double>> seg_pos_t(T);
 #ifdef _OPENMP
   if (s.num_threads > 0) omp_set_num_threads(s.num_threads);
 #pragma omp parallel for schedule(dynamic, 16)
@@ -376,6 +377,7 @@ extern "C" int moc_lattice_generate(const moc_lattice_spec* sp,
     std::vector<double> pts;
     std::vector<float>& out_len = seg_len_t[t];
     std::vector<uint64_t>& out_key = seg_key_t[t];
+    std::vector<double>& out_pos = seg_pos_t[t];
     for (size_t c = 0; c + 1 < cuts.size(); c++) {
       const double ta = cuts[c], tb = cuts[c + 1];
       if (tb - ta <= 0) continue;
@@ -429,6 +431,7 @@ extern "C" int moc_lattice_generate(const moc_lattice_spec* sp,
         } else {
           out_key.push_back(key);
           out_len.push_back((float) l);
+          out_pos.push_back(pts[k]);
         }
       }
     }
@@ -444,8 +447,12 @@ extern "C" int moc_lattice_generate(const moc_lattice_spec* sp,
   L->S = S;
   L->seg_len.resize(S);
   L->seg_fsr.resize(S);
+  L->seg_pos.resize(S);
   for (int64_t t = 0; t < T; t++) {
     const int64_t base = L->seg_off[t];
+    std::memcpy(L->seg_pos.data() + base, seg_pos_t[t].data(),
+                sizeof(double) * seg_pos_t[t].size());
+    std::vector<double>().swap(seg_pos_t[t]);
     for (size_t k = 0; k < seg_len_t[t].size(); k++) {
       const uint64_t key = seg_key_t[t][k];
       auto it = ids.find(key);
@@ -622,30 +629,45 @@ extern "C" int moc_synthetic_xs(uint64_t seed, int32_t num_groups,
 // ---- axial extrusion into explicit 3D tracks ------------------------------
 // A lattice of height `height`, its pins for z < fuel_height and one
 // homogeneous moderator region above, reflective radially and vacuum at the
-// bottom and top: the shape of an axially extruded 3D benchmark with explicit
-// 3D segments (OpenMOC's TrackGenerator3D with EXPLICIT_3D,
-// src/TrackGenerator3D.cpp).  This is not OpenMOC's 3D laydown: it is a
-// laydown of its own on the same radial tracks, built so that every 3D link
-// is exact.
-//   - Radial tracks with reflective ends form closed cycles of directed 2D
-//     tracks; each cycle is unrolled into one periodic line coordinate s.
-//   - For each polar angle of a Gauss-Legendre set (mu = cos theta, half the
-//     angles upward), lines z = z0 + s cot(theta) start at the bottom (or
-//     top) at s_j = (j + 1/2) ds, with ds = L_cycle / n and
-//     n = round(L_cycle |cot theta| / dz): equally spaced along the cycle,
-//     vertical spacing dz' = ds |cot theta| close to dz.
-//   - A line is cut where it passes from one radial track to the next; each
-//     piece is a 3D track whose forward neighbour is the next piece (entered
-//     forward) and backward neighbour the previous one; the first and last
-//     pieces end on the vacuum bottom / top.
+// bottom and top, with OpenMOC's own 3D laydown (TrackGenerator3D with
+// EXPLICIT_3D segments, src/TrackGenerator3D.cpp) over the radial tracks:
+//   - Gauss-Legendre polar angles (TrackGenerator3D's default GLPolarQuad,
+//     src/Quadrature.cpp:1014-1073: theta_p = acos of the Legendre roots in
+//     ascending order for the upper half, pi - theta for the lower half,
+//     weights half the Gauss-Legendre weights).
+//   - Per azimuthal angle and polar pair, the l / z counts and effective
+//     spacings, and the polar angle corrected to atan(dl / dz)
+//     (TrackGenerator3D::initializeTracks, src/TrackGenerator3D.cpp:683-800).
+//   - Chains of radial tracks linked periodically from the y-min boundary to
+//     the y-max boundary (initialize2DTrackChains, :886-925); along each
+//     chain, for every polar angle, nl + nz lines laid at the effective
+//     spacings (getFirst2DTrackLinkIndex, :975-1097) and cut where they
+//     reach an x / y boundary of a radial track or the bottom / top: each
+//     piece is a 3D track of the stack (azimuthal angle, radial track, polar
+//     angle) it lies over, stacked in the order laid (set3DTrackData,
+//     :1099-1251).  Tracks are numbered azimuthal, radial track, polar
+//     angle, stack index, as get3DTrackID numbers them.
 //   - Segments: the radial segments under the piece, cut at z = fuel_height;
 //     above it the single moderator region (id R2); length = radial length /
 //     sin(theta).
-//   - Weights: one row per (cycle, polar angle): 2 pi w_a w_p d_a dz' sin(theta),
-//     w_a and d_a the azimuthal weight and spacing of the cycle's tracks, w_p
-//     the polar weight normalised to 1 over all polar angles (each 3D track is
-//     swept in both directions); FSR volumes are sum(w / 2 pi * length), as
-//     the radial laydown's volumes are sum(w_a d_a length).
+//   - Connections: a track leaving through a reflective x / y boundary
+//     continues in the stack of the radial track's reflected neighbour
+//     (forward keeps the polar angle, an entry from the end takes the
+//     complementary one), in the track that starts (ends) at the exit point;
+//     the bottom and top are vacuum.
+//   - Weights per (azimuthal, polar) row: 2 pi w_a d_a w_p d_p with d_p the
+//     polar spacing dz sin(theta) (Quadrature::precomputeWeights,
+//     src/Quadrature.cpp:728-743); FSR volumes sum(w / 2 pi * length)
+//     (VolumeKernel, src/MOCKernel.cpp:86-160).
+namespace {
+
+struct Piece {
+  int32_t t2;                 // radial track
+  double x0, y0, z0, x1, y1, z1;
+};
+
+}  // namespace
+
 extern "C" int moc_lattice_extrude(const moc_lattice* L2, double height,
                                    double fuel_height, double z_spacing,
                                    int32_t num_polar, int32_t num_threads,
@@ -661,9 +683,30 @@ extern "C" int moc_lattice_extrude(const moc_lattice* L2, double height,
   for (int64_t t = 0; t < T2; t++)
     if ((L2->flags[t] & 12) != 12)
       return lat_fail("the extrusion needs reflective radial boundaries");
-  if (L2->az_spacing.empty()) return lat_fail("radial lattice has no spacings");
+  if (L2->az_spacing.empty() || (int64_t) L2->tracks.size() != T2 ||
+      !(L2->pitch > 0))
+    return lat_fail("the extrusion needs a radial lattice with its tracks");
 
-  // Gauss-Legendre nodes and weights on [-1, 1] (sum of weights 2)
+  const double W = L2->nx * L2->pitch, H = L2->ny * L2->pitch;
+  const double xmin = L2->xmin, xmax = L2->xmin + W;
+  const double ymin = L2->ymin, ymax = L2->ymin + H;
+  const double zmin = 0.0, zmax = height;
+  const int A = L2->A;                       // azimuthal angles in (0, pi)
+  const int P = num_polar, half = P / 2;
+  // radial tracks per azimuthal angle, and those starting on y = ymin
+  std::vector<int64_t> first(A + 1, 0);
+  std::vector<int> num_x(A, 0);
+  for (int64_t t = 0; t < T2; t++) {
+    const moc_lat::Track& tr = L2->tracks[t];
+    if (tr.a < 0 || tr.a >= A) return lat_fail("radial track angle out of range");
+    first[tr.a + 1]++;
+    if (tr.y0 == ymin) num_x[tr.a]++;
+  }
+  for (int a = 0; a < A; a++) first[a + 1] += first[a];
+  std::vector<int> num_y(A);
+  for (int a = 0; a < A; a++) num_y[a] = (int) (first[a + 1] - first[a]) - num_x[a];
+
+  // Gauss-Legendre nodes (ascending, upper half) and weights on [-1, 1]
   static const double gl_mu[3][3] = {{0.5773502691896258, 0, 0},
                                      {0.3399810435848563, 0.8611363115940526, 0},
                                      {0.2386191860831969, 0.6612093864662645,
@@ -672,241 +715,400 @@ extern "C" int moc_lattice_extrude(const moc_lattice* L2, double height,
                                     {0.6521451548625461, 0.3478548451374538, 0},
                                     {0.4679139345726910, 0.3607615730481386,
                                      0.1713244923791704}};
-  const int P = num_polar, half = P / 2, row = half - 1;
-  std::vector<double> mu(P), wp(P);
-  for (int k = 0; k < half; k++) {
-    mu[half - 1 - k] = -gl_mu[row][k];   // downward, steepest last
-    mu[half + k] = gl_mu[row][k];
-    wp[half - 1 - k] = wp[half + k] = 0.5 * gl_w[row][k];
-  }
-
-  // radial segment boundaries per track
-  std::vector<int64_t> off(L2->seg_off.begin(), L2->seg_off.end());
-  std::vector<double> cum((size_t) L2->S + T2);
-  std::vector<double> len2(T2);
-  for (int64_t t = 0; t < T2; t++) {
-    double c = 0;
-    cum[off[t] + t] = 0;
-    for (int64_t k = off[t]; k < off[t + 1]; k++) {
-      c += (double) L2->seg_len[k];
-      cum[k + 1 + t] = c;
+  const int row = half - 1;
+  // per (azimuthal, polar): corrected theta, l / z counts and spacings
+  std::vector<double> theta((size_t) A * P), dl_eff((size_t) A * P),
+      dz_eff((size_t) A * P), wpol((size_t) A * P);
+  std::vector<int> nl((size_t) A * P), nz((size_t) A * P);
+  for (int a = 0; a < A / 2; a++) {
+    const double phi = L2->tracks[first[a]].phi;
+    for (int j = 0; j < half; j++) {
+      const double th = std::acos(gl_mu[row][j]);
+      const double length = H / std::sin(phi);
+      const int l = (int) std::ceil(length * std::tan(0.5 * kPi - th) / z_spacing);
+      const int z = (int) std::ceil(height * l * std::tan(th) / length);
+      const double dl = H / (std::sin(phi) * l);
+      const double dz = height / z;
+      const double th_new = std::atan(dl / dz);
+      const int sa = A - a - 1, cp = P - j - 1;
+      for (int aa : {a, sa})
+        for (int pp : {j, cp}) {
+          const size_t r = (size_t) aa * P + pp;
+          nl[r] = l;
+          nz[r] = z;
+          dl_eff[r] = dl;
+          dz_eff[r] = dz;
+          theta[r] = (pp == j) ? th_new : kPi - th_new;
+          wpol[r] = 0.5 * gl_w[row][j];
+        }
     }
-    len2[t] = c;
   }
-  // cum of track t: cum[off[t] + t + i], i = 0..n_t
 
-  // cycles of directed tracks (t, d); the reverse cycle is left out
-  struct Cycle {
-    std::vector<int64_t> tr;
-    std::vector<int> dir;
-    std::vector<double> s0;
-    double len = 0;
+  // chains: radial tracks linked periodically from y = ymin up to y = ymax
+  // (the periodic forward neighbour of xy < num_y is xy + num_x)
+  struct Chain {
+    int a;
+    std::vector<int32_t> xy;
   };
-  std::vector<Cycle> cycles;
-  std::vector<uint8_t> seen(2 * T2, 0);
-  for (int64_t t0 = 0; t0 < T2; t0++)
-    for (int d0 = 0; d0 < 2; d0++) {
-      if (seen[2 * t0 + d0]) continue;
-      Cycle c;
-      int64_t t = t0;
-      int d = d0;
-      for (int64_t guard = 0;; guard++) {
-        if (guard > 2 * T2) return lat_fail("radial track links do not close");
-        c.tr.push_back(t);
-        c.dir.push_back(d);
-        c.s0.push_back(c.len);
-        c.len += len2[t];
-        seen[2 * t + d] = 1;
-        seen[2 * t + (1 - d)] = 1;
-        const int64_t nt = L2->next[2 * t + d];
-        const bool fwd = (L2->flags[t] & (d ? 2 : 1)) != 0;
-        t = nt;
-        d = fwd ? 0 : 1;
-        if (t == t0 && d == d0) break;
+  std::vector<Chain> chains;
+  for (int a = 0; a < A; a++)
+    for (int x = 0; x < num_x[a]; x++) {
+      Chain c;
+      c.a = a;
+      int xy = x;
+      c.xy.push_back(xy);
+      while (xy < num_y[a]) {
+        xy += num_x[a];
+        c.xy.push_back(xy);
       }
-      cycles.push_back(std::move(c));
+      chains.push_back(std::move(c));
     }
-  const int64_t R2 = L2->R;
-  const int64_t nitems = (int64_t) cycles.size() * P;
 
-  // one work item per (cycle, polar angle): its tracks and segments
-  struct Item {
-    std::vector<float> seg_len;
-    std::vector<int32_t> seg_fsr;
-    std::vector<int32_t> nseg;
-    std::vector<uint8_t> first, last;   // first / last piece of its line
-    std::vector<int32_t> otf;           // per 3D track: t, first, count, rev
-    std::vector<float> otf_f;           // per 3D track: a0, span, w0, 0
-    double weight = 0;
-    float cot = 0, sin_t = 0;
-  };
-  std::vector<Item> items(nitems);
+  // the pieces of every (chain, polar angle), in the order laid
+  const int64_t nitems = (int64_t) chains.size() * P;
+  std::vector<std::vector<Piece>> laid(nitems);
 #ifdef _OPENMP
   if (num_threads > 0) omp_set_num_threads(num_threads);
 #pragma omp parallel for schedule(dynamic, 1)
 #endif
   for (int64_t it = 0; it < nitems; it++) {
-    const Cycle& c = cycles[it / P];
+    const Chain& ch = chains[it / P];
     const int p = (int) (it % P);
-    Item& out_item = items[it];
-    const double sin_t = std::sqrt(1.0 - mu[p] * mu[p]);
-    const double cot = mu[p] / sin_t;          // dz / ds, signed
-    const double run = height / std::fabs(cot);
-    const int64_t n = std::max<int64_t>(
-        1, (int64_t) std::llround(c.len * std::fabs(cot) / z_spacing));
-    const double ds = c.len / (double) n;
-    const double dz_eff = ds * std::fabs(cot);
-    const int a = L2->track_ang[c.tr[0]];
-    out_item.weight = 2.0 * kPi * L2->az_weight[a] * wp[p] *
-                      L2->az_spacing[a] * dz_eff * sin_t;
-    out_item.cot = (float) cot;
-    out_item.sin_t = (float) sin_t;
-    const size_t ncyc = c.tr.size();
-    for (int64_t j = 0; j < n; j++) {
-      double s = (j + 0.5) * ds;
-      double z = (cot > 0) ? 0.0 : height;
-      double remaining = run;
-      size_t k = (size_t) (std::upper_bound(c.s0.begin(), c.s0.end(), s) -
-                           c.s0.begin()) - 1;
-      bool first_piece = true;
-      while (remaining > 1e-12) {
-        const int64_t t = c.tr[k];
-        const int d = c.dir[k];
-        const double L = len2[t];
-        const double a0 = std::max(0.0, s - c.s0[k]);
-        const double take = std::min(L - a0, remaining);
-        const double a1 = a0 + take;
-        // radial segments under [a0, a1] in traversal order, cut at the
-        // top of the fuel
-        const double* cb = cum.data() + off[t] + t;
-        const int64_t nsg = off[t + 1] - off[t];
-        const size_t seg_start = out_item.seg_len.size();
-        int32_t last_fsr = -1;
-        auto emit = [&](int32_t fsr, double l3) {
-          if (l3 <= 1e-10) return;
-          if (fsr == last_fsr && out_item.seg_len.size() > seg_start) {
-            out_item.seg_len.back() = (float) ((double) out_item.seg_len.back() + l3);
-          } else {
-            out_item.seg_fsr.push_back(fsr);
-            out_item.seg_len.push_back((float) l3);
-            last_fsr = fsr;
-          }
-        };
-        auto piece = [&](int32_t fsr2, double u0, double u1) {
-          // traversal interval [u0, u1] of one radial segment
-          const double z0 = z + (u0 - a0) * cot, z1 = z + (u1 - a0) * cot;
-          const double lo = std::min(z0, z1), hi = std::max(z0, z1);
-          if (hi <= fuel_height) {
-            emit(fsr2, (u1 - u0) / sin_t);
-          } else if (lo >= fuel_height) {
-            emit((int32_t) R2, (u1 - u0) / sin_t);
-          } else {
-            const double uc = u0 + (fuel_height - z0) / cot;
-            const bool below_first = z0 < fuel_height;
-            emit(below_first ? fsr2 : (int32_t) R2, (uc - u0) / sin_t);
-            emit(below_first ? (int32_t) R2 : fsr2, (u1 - uc) / sin_t);
-          }
-        };
-        // the radial segments crossed, for the on-the-fly description
-        int64_t i_first = 0, n_crossed = 0;
-        if (d == 0) {
-          int64_t i = (int64_t) (std::upper_bound(cb, cb + nsg + 1, a0) - cb) - 1;
-          i_first = i;
-          for (; i < nsg && cb[i] < a1; i++) {
-            const double u0 = std::max(a0, cb[i]), u1 = std::min(a1, cb[i + 1]);
-            if (u1 > u0) piece(L2->seg_fsr[off[t] + i], u0, u1);
-            n_crossed++;
-          }
-        } else {
-          // natural coordinate x = L - u
-          const double x0 = L - a1, x1 = L - a0;
-          int64_t i = (int64_t) (std::upper_bound(cb, cb + nsg + 1, x1) - cb) - 1;
-          if (i >= nsg) i = nsg - 1;
-          i_first = i;
-          for (; i >= 0 && cb[i + 1] > x0; i--) {
-            const double v0 = std::max(x0, cb[i]), v1 = std::min(x1, cb[i + 1]);
-            if (v1 > v0) piece(L2->seg_fsr[off[t] + i], L - v1, L - v0);
-            n_crossed++;
-          }
+    const int a = ch.a;
+    const size_t r = (size_t) a * P + p;
+    const int NL = nl[r], NZ = nz[r];
+    const double dz = dz_eff[r], dl = dl_eff[r], th = theta[r];
+    const moc_lat::Track& c0 = L2->tracks[first[a] + ch.xy[0]];
+    const double phi = c0.phi, cphi = std::cos(phi), sphi = std::sin(phi);
+    std::vector<Piece>& outp = laid[it];
+    for (int lz = 0; lz < NL + NZ; lz++) {
+      // start point and link (getFirst2DTrackLinkIndex)
+      double l_start = 0.0;
+      if (p < half && lz < NL)
+        l_start = H / sphi - (lz + 0.5) * dl;
+      else if (p >= half && lz >= NZ)
+        l_start = dl * (lz - NZ + 0.5);
+      double x_ext = c0.x0 - xmin + l_start * cphi;
+      double y_ext = c0.y0 - ymin + l_start * sphi;
+      bool nudged = false;
+      if (std::fabs(l_start) > 1e-12) {
+        if (std::fabs(std::round(x_ext / W) * W - x_ext) < kTinyMove ||
+            std::fabs(std::round(y_ext / H) * H - y_ext) < kTinyMove) {
+          l_start += 10 * kTinyMove;
+          x_ext = c0.x0 - xmin + l_start * cphi;
+          y_ext = c0.y0 - ymin + l_start * sphi;
+          nudged = true;
         }
-        out_item.otf.insert(out_item.otf.end(),
-                            {(int32_t) t, (int32_t) i_first,
-                             (int32_t) n_crossed, (int32_t) d});
-        out_item.otf_f.insert(out_item.otf_f.end(),
-                              {(float) a0, (float) take,
-                               (float) (z - fuel_height), 0.0f});
-        out_item.nseg.push_back(
-            (int32_t) (out_item.seg_len.size() - seg_start));
-        remaining -= take;
-        z += take * cot;
-        out_item.first.push_back(first_piece ? 1 : 0);
-        out_item.last.push_back(remaining > 1e-12 ? 0 : 1);
-        first_piece = false;
-        k = (k + 1) % ncyc;
-        s = c.s0[k];
+      }
+      int link = std::abs((int) std::floor(x_ext / W));
+      double x1 = (x_ext < 0.0) ? std::fmod(x_ext, W) + xmax : std::fmod(x_ext, W) + xmin;
+      double y1 = std::fmod(y_ext, H) + ymin;
+      double z1, zend;
+      if (p < half) {
+        z1 = zmin + std::max(0., (lz - NL + 0.5)) * dz;
+        zend = zmax + std::min(0., (lz - NZ + 0.5)) * dz;
+      } else {
+        z1 = zmax + std::min(0., (lz - NZ + 0.5)) * dz;
+        zend = zmin + std::max(0., (lz - NL + 0.5)) * dz;
+      }
+      if (nudged) {
+        x1 -= 10 * kTinyMove * cphi;
+        y1 -= 10 * kTinyMove * sphi;
+      }
+      // walk the chain (set3DTrackData)
+      const int first_link = link;
+      double x2 = x1, y2 = y1, z2 = z1;
+      bool end_of_chain = false;
+      while (!end_of_chain) {
+        if (link >= (int) ch.xy.size()) break;
+        const int xy = ch.xy[link];
+        const moc_lat::Track& t2 = L2->tracks[first[a] + xy];
+        x1 = x2;
+        y1 = y2;
+        z1 = z2;
+        double dl_xy;
+        if (link == first_link) {
+          const double ddx = t2.x1 - x1, ddy = t2.y1 - y1;
+          dl_xy = std::sqrt(ddx * ddx + ddy * ddy);
+        } else {
+          const double ddx = t2.x1 - t2.x0, ddy = t2.y1 - t2.y0;
+          dl_xy = std::sqrt(ddx * ddx + ddy * ddy);
+        }
+        double dl_z;
+        if (p < half)
+          dl_z = (zend - z1) * std::tan(th);
+        else
+          dl_z = (z1 - zend) / std::tan(th - 0.5 * kPi);
+        const double d = std::min(dl_z, dl_xy);
+        x2 = x1 + d * std::cos(t2.phi);
+        y2 = y1 + d * std::sin(t2.phi);
+        if (p < half)
+          z2 = z1 + d / std::tan(th);
+        else
+          z2 = z1 - d * std::tan(th - 0.5 * kPi);
+        if (std::fabs(x2 - x1) < kTinyMove || std::fabs(y2 - y1) < kTinyMove ||
+            std::fabs(z2 - z1) < kTinyMove)
+          break;
+        if (dl_z < dl_xy || xy >= num_y[a]) end_of_chain = true;
+        Piece pc;
+        pc.t2 = (int32_t) (first[a] + xy);
+        pc.x0 = std::max(xmin, std::min(xmax, x1));
+        pc.y0 = std::max(ymin, std::min(ymax, y1));
+        pc.z0 = std::max(zmin, std::min(zmax, z1));
+        pc.x1 = std::max(xmin, std::min(xmax, x2));
+        pc.y1 = std::max(ymin, std::min(ymax, y2));
+        pc.z1 = std::max(zmin, std::min(zmax, z2));
+        outp.push_back(pc);
+        link++;
+        if (!end_of_chain) x2 = (a < A / 2) ? xmin : xmax;
       }
     }
   }
 
-  // concatenate in item order
+  // stacks (azimuthal angle, radial track, polar angle): the pieces in the
+  // order laid; each stack is filled by one chain
+  std::vector<int64_t> stack_n((size_t) T2 * P, 0);
+  for (int64_t it = 0; it < nitems; it++) {
+    const int p = (int) (it % P);
+    for (const Piece& pc : laid[it]) stack_n[(size_t) pc.t2 * P + p]++;
+  }
+  std::vector<int64_t> stack_first((size_t) T2 * P + 1, 0);
+  for (size_t k = 0; k < (size_t) T2 * P; k++) stack_first[k + 1] = stack_first[k] + stack_n[k];
+  const int64_t T = stack_first[(size_t) T2 * P];
+  if (T >= (1LL << 31)) return lat_fail("extruded problem too large");
+  std::vector<Piece> pieces(T);
+  std::vector<int32_t> prow(T);
+  {
+    std::vector<int64_t> fill(stack_first.begin(), stack_first.end() - 1);
+    for (int64_t it = 0; it < nitems; it++) {
+      const int p = (int) (it % P);
+      for (const Piece& pc : laid[it]) {
+        const size_t k = (size_t) pc.t2 * P + p;
+        pieces[fill[k]] = pc;
+        prow[fill[k]] = (int32_t) L2->tracks[pc.t2].a * P + p;
+        fill[k]++;
+      }
+    }
+  }
+  laid.clear();
+  laid.shrink_to_fit();
+
+  // radial segment boundaries per track: the tracer's double-precision
+  // crossings where it kept them, else the summed lengths
+  std::vector<int64_t> off(L2->seg_off.begin(), L2->seg_off.end());
+  std::vector<double> cum((size_t) L2->S + T2);
+  std::vector<double> len2(T2);
+  const bool exact = (int64_t) L2->seg_pos.size() == L2->S;
+  for (int64_t t = 0; t < T2; t++) {
+    double c = 0;
+    cum[off[t] + t] = 0;
+    for (int64_t k = off[t]; k < off[t + 1]; k++) {
+      c += (double) L2->seg_len[k];
+      if (exact && k > off[t]) cum[k + t] = L2->seg_pos[k];
+      cum[k + 1 + t] = c;
+    }
+    if (exact) {
+      const moc_lat::Track& tr = L2->tracks[t];
+      c = std::hypot(tr.x1 - tr.x0, tr.y1 - tr.y0);
+      if (off[t + 1] > off[t]) cum[off[t + 1] + t] = c;
+    }
+    len2[t] = c;
+  }
+  const int64_t R2 = L2->R;
+  // A piece shorter (in 3D) than the reference tracer's step past a surface
+  // forms no segment; with summed lengths, the boundaries are only good to
+  // their float rounding
+  const double kSliver = exact ? kTinyMove : 1e-6;
+
+  // segments of every 3D track (in parallel, then concatenated)
+  std::vector<std::vector<float>> sl(T);
+  std::vector<std::vector<int32_t>> sf(T);
+  std::vector<int32_t> otf_i((size_t) 4 * T);
+  std::vector<float> otf_f((size_t) 4 * T);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 256)
+#endif
+  for (int64_t t = 0; t < T; t++) {
+    const Piece& pc = pieces[t];
+    const int64_t t2 = pc.t2;
+    const moc_lat::Track& tr = L2->tracks[t2];
+    const double th = theta[prow[t]];
+    const double sin_t = std::sin(th), cot = std::cos(th) / sin_t;
+    // the piece's span along the radial track, from its start point
+    const double a0 = std::hypot(pc.x0 - tr.x0, pc.y0 - tr.y0);
+    const double a1 = std::hypot(pc.x1 - tr.x0, pc.y1 - tr.y0);
+    const double* cb = cum.data() + off[t2] + t2;
+    const int64_t nsg = off[t2 + 1] - off[t2];
+    int32_t last_fsr = -1;
+    auto emit = [&](int32_t fsr, double l3) {
+      if (l3 <= 1e-10) return;
+      if (fsr == last_fsr && !sl[t].empty()) {
+        sl[t].back() = (float) ((double) sl[t].back() + l3);
+      } else {
+        sf[t].push_back(fsr);
+        sl[t].push_back((float) l3);
+        last_fsr = fsr;
+      }
+    };
+    // A track that starts or ends on a radial boundary leaves a sliver of
+    // the neighbouring region at that end; the reference's tracing forms no
+    // such segment, so the radial pieces crossed start after a sliver at a0
+    // and stop before one at a1.
+    int64_t i = (int64_t) (std::upper_bound(cb, cb + nsg + 1, a0) - cb) - 1;
+    if (i < 0) i = 0;
+    if (i + 1 < nsg && cb[i + 1] - a0 < kSliver * sin_t) i++;
+    const int64_t i_first = i;
+    int64_t i_end = i;
+    while (i_end < nsg && cb[i_end] < a1) i_end++;
+    if (i_end - 1 > i_first && a1 - cb[i_end - 1] < kSliver * sin_t) i_end--;
+    const int64_t n_crossed = i_end - i_first;
+    for (; i < i_end; i++) {
+      const double u0 = std::max(a0, cb[i]), u1 = std::min(a1, cb[i + 1]);
+      if (!(u1 > u0)) continue;
+      const int32_t fsr2 = L2->seg_fsr[off[t2] + i];
+      const double z0 = pc.z0 + (u0 - a0) * cot, z1 = pc.z0 + (u1 - a0) * cot;
+      const double lo = std::min(z0, z1), hi = std::max(z0, z1);
+      if (hi <= fuel_height) {
+        emit(fsr2, (u1 - u0) / sin_t);
+      } else if (lo >= fuel_height) {
+        emit((int32_t) R2, (u1 - u0) / sin_t);
+      } else {
+        // cut at the fuel top (a sliver on either side of the cut, where the
+        // track crosses it on a radial boundary, joins the other side)
+        const double uc = u0 + (fuel_height - z0) / cot;
+        const bool below_first = z0 < fuel_height;
+        const int32_t f0 = below_first ? fsr2 : (int32_t) R2;
+        const int32_t f1 = below_first ? (int32_t) R2 : fsr2;
+        if (uc - u0 < kSliver * sin_t) {
+          emit(f1, (u1 - u0) / sin_t);
+        } else if (u1 - uc < kSliver * sin_t) {
+          emit(f0, (u1 - u0) / sin_t);
+        } else {
+          emit(f0, (uc - u0) / sin_t);
+          emit(f1, (u1 - uc) / sin_t);
+        }
+      }
+    }
+    otf_i[4 * t + 0] = (int32_t) t2;
+    otf_i[4 * t + 1] = (int32_t) i_first;
+    otf_i[4 * t + 2] = (int32_t) n_crossed;
+    otf_i[4 * t + 3] = 0;
+    otf_f[4 * t + 0] = (float) a0;
+    otf_f[4 * t + 1] = (float) (a1 - a0);
+    otf_f[4 * t + 2] = (float) (pc.z0 - fuel_height);
+    otf_f[4 * t + 3] = 0.0f;
+  }
+
+  // connections: the track of the reflected stack that starts (forward
+  // entry) or ends (backward entry) at the exit point
+  const double ztol = 1e-9, ptol = 1e-6;
+  auto find_in_stack = [&](int64_t t2n, int pn, bool at_start, double x,
+                           double y, double z) -> int64_t {
+    const size_t k = (size_t) t2n * P + pn;
+    int64_t best = -1;
+    double bd = ptol;
+    for (int64_t u = stack_first[k]; u < stack_first[k + 1]; u++) {
+      const Piece& q = pieces[u];
+      const double qx = at_start ? q.x0 : q.x1, qy = at_start ? q.y0 : q.y1,
+                   qz = at_start ? q.z0 : q.z1;
+      const double dd = std::fabs(qx - x) + std::fabs(qy - y) + std::fabs(qz - z);
+      if (dd < bd) {
+        bd = dd;
+        best = u;
+      }
+    }
+    return best;
+  };
   moc_lattice* L = new moc_lattice();
-  int64_t T = 0, S = 0;
-  for (const Item& m : items) {
-    T += (int64_t) m.nseg.size();
-    S += (int64_t) m.seg_len.size();
+  L->next.assign(2 * T, 0);
+  L->flags.assign(T, 0);
+  int bad = 0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 1024) reduction(+ : bad)
+#endif
+  for (int64_t t = 0; t < T; t++) {
+    const Piece& pc = pieces[t];
+    const int p = prow[t] % P, pcomp = P - p - 1;
+    const int64_t t2 = pc.t2;
+    uint8_t f = 0;
+    int64_t nf = t, nb = t;
+    // forward end
+    if (std::fabs(pc.z1 - zmin) > ztol && std::fabs(pc.z1 - zmax) > ztol) {
+      const bool ff = (L2->flags[t2] & 1) != 0;
+      nf = find_in_stack(L2->next[2 * t2], ff ? p : pcomp, ff, pc.x1, pc.y1, pc.z1);
+      if (nf < 0) {
+        bad++;
+        nf = t;
+      } else {
+        f |= 4;
+        if (ff) f |= 1;
+      }
+    }
+    // backward end
+    if (std::fabs(pc.z0 - zmin) > ztol && std::fabs(pc.z0 - zmax) > ztol) {
+      const bool bf = (L2->flags[t2] & 2) != 0;
+      nb = find_in_stack(L2->next[2 * t2 + 1], bf ? pcomp : p, bf, pc.x0, pc.y0, pc.z0);
+      if (nb < 0) {
+        bad++;
+        nb = t;
+      } else {
+        f |= 8;
+        if (bf) f |= 2;
+      }
+    }
+    L->next[2 * t] = nf;
+    L->next[2 * t + 1] = nb;
+    L->flags[t] = f;
   }
-  if (T >= (1LL << 31) || S >= (1LL << 40)) {
+  if (bad) {
     delete L;
-    return lat_fail("extruded problem too large");
+    return lat_fail("3D tracks whose exit point starts no track of the "
+                    "reflected stack: " + std::to_string(bad));
   }
+
+  // concatenate the segments; weights, volumes, on-the-fly description
+  int64_t S = 0;
+  for (int64_t t = 0; t < T; t++) S += (int64_t) sl[t].size();
+  const int nrows = A * P;
   L->R = R2 + 1;
   L->T = T;
   L->S = S;
-  L->A = (int32_t) nitems;
+  L->A = nrows;
   L->Ph = 1;
   L->M = L2->M;
   L->seg_len.resize(S);
   L->seg_fsr.resize(S);
   L->seg_off.assign(T + 1, 0);
-  L->track_ang.resize(T);
-  L->next.resize(2 * T);
-  L->flags.resize(T);
-  L->weights.resize(nitems);
-  L->inv_sin.assign(nitems, 1.0f);
-  L->otf_trk.resize(4 * (size_t) T);
-  L->otf_trk_f.resize(4 * (size_t) T);
-  L->otf_ang.resize(4 * (size_t) nitems);
-  std::vector<double> vol(R2 + 1, 0.0);
-  int64_t tb = 0, sb = 0;
-  for (int64_t it = 0; it < nitems; it++) {
-    const Item& m = items[it];
-    L->weights[it] = (float) m.weight;
-    L->otf_ang[4 * it + 0] = m.cot;
-    L->otf_ang[4 * it + 1] = 1.0f / m.cot;
-    L->otf_ang[4 * it + 2] = 1.0f / m.sin_t;
-    L->otf_ang[4 * it + 3] = 0.0f;
-    std::memcpy(L->otf_trk.data() + 4 * tb, m.otf.data(), 4 * m.otf.size());
-    std::memcpy(L->otf_trk_f.data() + 4 * tb, m.otf_f.data(),
-                4 * m.otf_f.size());
-    const double wv = m.weight / (2.0 * kPi);
-    std::memcpy(L->seg_len.data() + sb, m.seg_len.data(), 4 * m.seg_len.size());
-    std::memcpy(L->seg_fsr.data() + sb, m.seg_fsr.data(), 4 * m.seg_fsr.size());
-    for (size_t q = 0; q < m.seg_len.size(); q++)
-      vol[m.seg_fsr[q]] += wv * (double) m.seg_len[q];
-    for (size_t q = 0; q < m.nseg.size(); q++) {
-      const int64_t t = tb + (int64_t) q;
-      L->seg_off[t + 1] = L->seg_off[t] + m.nseg[q];
-      L->track_ang[t] = (int32_t) it;
-      uint8_t f = 1;                       // forward exit enters forward
-      if (!m.last[q]) f |= 4;              // transfer forward
-      if (!m.first[q]) f |= 8;             // transfer backward
-      L->flags[t] = f;                     // backward exit enters backward
-      L->next[2 * t] = m.last[q] ? t : t + 1;
-      L->next[2 * t + 1] = m.first[q] ? t : t - 1;
-    }
-    tb += (int64_t) m.nseg.size();
-    sb += (int64_t) m.seg_len.size();
+  L->track_ang.assign(prow.begin(), prow.end());
+  L->weights.resize(nrows);
+  L->inv_sin.assign(nrows, 1.0f);
+  L->otf_ang.resize(4 * (size_t) nrows);
+  std::vector<double> wrow(nrows);
+  for (int rr = 0; rr < nrows; rr++) {
+    const int a = rr / P;
+    const double th = theta[rr];
+    const double dp = dz_eff[rr] * std::sin(th);   // polar spacing
+    wrow[rr] = 2.0 * kPi * L2->az_weight[a] * L2->az_spacing[a] * wpol[rr] * dp;
+    L->weights[rr] = (float) wrow[rr];
+    const double c = std::cos(th) / std::sin(th);
+    L->otf_ang[4 * rr + 0] = (float) c;
+    L->otf_ang[4 * rr + 1] = (float) (1.0 / c);
+    L->otf_ang[4 * rr + 2] = (float) (1.0 / std::sin(th));
+    L->otf_ang[4 * rr + 3] = 0.0f;
   }
+  std::vector<double> vol(R2 + 1, 0.0);
+  int64_t sb = 0;
+  for (int64_t t = 0; t < T; t++) {
+    const double wv = wrow[prow[t]] / (2.0 * kPi);
+    const size_t n = sl[t].size();
+    std::memcpy(L->seg_len.data() + sb, sl[t].data(), 4 * n);
+    std::memcpy(L->seg_fsr.data() + sb, sf[t].data(), 4 * n);
+    for (size_t q = 0; q < n; q++) vol[sf[t][q]] += wv * (double) sl[t][q];
+    sb += (int64_t) n;
+    L->seg_off[t + 1] = sb;
+  }
+  L->otf_trk = std::move(otf_i);
+  L->otf_trk_f = std::move(otf_f);
   L->fsr_mat.assign(L2->fsr_mat.begin(), L2->fsr_mat.end());
   L->fsr_mat.push_back(L2->moderator);
   // the radial segments the on-the-fly tracks are cut from
@@ -923,7 +1125,23 @@ extern "C" int moc_lattice_extrude(const moc_lattice* L2, double height,
   L->above_fsr = (int32_t) R2;
   L->fsr_vol.resize(R2 + 1);
   for (int64_t r = 0; r <= R2; r++) L->fsr_vol[r] = (float) vol[r];
+  // the 3D track ends, for comparisons with the reference laydown
+  L->tracks3d.resize(6 * (size_t) T);
+  for (int64_t t = 0; t < T; t++) {
+    const Piece& pc = pieces[t];
+    double* e = L->tracks3d.data() + 6 * t;
+    e[0] = pc.x0; e[1] = pc.y0; e[2] = pc.z0;
+    e[3] = pc.x1; e[4] = pc.y1; e[5] = pc.z1;
+  }
   *out = L;
+  return 0;
+}
+
+extern "C" int moc_lattice_export_ends3d(moc_lattice* L, double* ends) {
+  if (!L || !ends) return lat_fail("null argument");
+  if ((int64_t) L->tracks3d.size() != 6 * L->T)
+    return lat_fail("not an extruded 3D lattice");
+  std::memcpy(ends, L->tracks3d.data(), sizeof(double) * L->tracks3d.size());
   return 0;
 }
 

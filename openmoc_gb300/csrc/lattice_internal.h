@@ -52,6 +52,9 @@ struct moc_lattice {
   int32_t A = 0, Ph = 0, M = 0;
   std::vector<float> seg_len;
   std::vector<int32_t> seg_fsr;
+  // 2D lattices traced on the host: each segment's start along its track in
+  // double precision (the axial extrusion cuts its 3D tracks there)
+  std::vector<double> seg_pos;
   std::vector<int64_t> seg_off;
   std::vector<int32_t> track_ang;
   std::vector<int64_t> next;
@@ -78,6 +81,8 @@ struct moc_lattice {
   std::vector<int32_t> rad_fsr;
   std::vector<int64_t> rad_off;
   int32_t above_fsr = -1;
+  // Extruded 3D lattices: each 3D track's start and end points [T][6]
+  std::vector<double> tracks3d;
   // 2D lattices: the lattice cell of every FSR (row 0 at the top, as the
   // FSR keys number them) and the lattice's placement, for CMFD meshes
   std::vector<int32_t> fsr_pin;

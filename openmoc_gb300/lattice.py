@@ -88,6 +88,8 @@ def _lib():
         L.moc_lattice_otf_sizes.restype = C.c_int
         L.moc_lattice_export_otf.argtypes = [C.c_void_p] + [C.c_void_p] * 8
         L.moc_lattice_export_otf.restype = C.c_int
+        L.moc_lattice_export_ends3d.argtypes = [C.c_void_p, C.c_void_p]
+        L.moc_lattice_export_ends3d.restype = C.c_int
         L.moc_lattice_export_ls.argtypes = [C.c_void_p] + [C.c_void_p] * 7
         L.moc_lattice_export_ls.restype = C.c_int
         L.moc_lattice_export_cmfd.argtypes = [C.c_void_p] + [C.c_void_p] * 6
@@ -217,6 +219,9 @@ def lattice(nx: int, ny: int, pin_material: np.ndarray, materials: Sequence[Mate
                     "trk", "trk_f", "ang", "rad_len", "rad_fsr", "rad_off",
                     "rad_start", "rad_total")]):
                 raise RuntimeError(L.moc_lattice_last_error().decode())
+            ends = np.empty((T, 6), np.float64)
+            if L.moc_lattice_export_ends3d(h, ends.ctypes.data):
+                raise RuntimeError(L.moc_lattice_last_error().decode())
         ls = None
         if linear_source:
             ls = dict(seg_x=np.empty(S, np.float32), seg_y=np.empty(S, np.float32),
@@ -251,6 +256,8 @@ def lattice(nx: int, ny: int, pin_material: np.ndarray, materials: Sequence[Mate
     p.linear_source = ls
     p.otf = otf
     p.cmfd_geometry = cm
+    if extrude is not None:
+        p.track_ends = ends
     p.meta = dict(nx=nx, ny=ny, num_azim=num_azim, spacing=spacing, pitch=pitch,
                   num_polar=num_polar)
     return p.contiguous()

@@ -110,6 +110,9 @@ class Problem:
     # (xmin, xmax, ymin, ymax of the lattice cell holding each FSR) or a
     # fixed mesh: fsr_cell [R] with widths_x, widths_y.
     cmfd_geometry: Optional[Dict[str, np.ndarray]] = None
+    # Extruded 3D lattices: each track's start and end points [T][6]
+    # (x0, y0, z0, x1, y1, z1), float64
+    track_ends: Optional[np.ndarray] = None
 
     @property
     def fluxes_per_track(self) -> int:

@@ -7,6 +7,7 @@
  *
  *   openmoc_run_<f32|f64> <config> golden <iterations> <out.json>
  *   openmoc_run_<f32|f64> <config> time <warmup> <iterations> <threads>
+ *   openmoc_run_<f32|f64> <config3d> laydown3d <out dir> <threads>
  *
  * Configurations (the same geometry, quadrature and seeded cross sections as
  * openmoc_gb300/lattice.py builds them):
@@ -19,6 +20,24 @@
  * All with the default Tabuchi-Yamamoto quadrature of 6 polar angles
  * (TrackGenerator's default) and single-threaded track generation, so FSR
  * numbering is reproducible (as the reference's test harness does).
+ * 3D configurations (TrackGenerator3D, explicit 3D segments, its default
+ * Gauss-Legendre polar quadrature; the lattice below the fuel height, one
+ * homogeneous moderator cell above, reflective radially, vacuum at the
+ * bottom and top):
+ *   assembly3d  the 17 x 17 assembly, 20 cm tall, fuel below 16 cm, 7
+ *               groups, 16 azimuthal, 6 polar, 0.1 cm radial, 0.5 cm axial
+ *   lattice3d   a 3 x 3 lattice (one water pin), 2 cm tall, fuel below
+ *               1.6 cm, 7 groups, 8 azimuthal, 4 polar, 0.1 cm, 0.4 cm
+ *
+ * laydown3d: the 3D tracks and their explicit segments, written to <out dir>
+ *   as raw little-endian arrays (<name>.bin, listed with dtype and length in
+ *   meta.json), in track UID order: azimuthal, xy, polar and stack index;
+ *   start and end points; segment count, total length and the length above
+ *   the fuel height (segments starting there); the forward / backward
+ *   connecting tracks and flags as the packer forms them; per (azimuthal,
+ *   polar) row the corrected polar angle, polar spacing and weight, the
+ *   azimuthal spacing and weight, the total weight and the l / z counts;
+ *   and the FSR volumes.
  *
  * golden: CPUSolver::computeEigenvalue for exactly <iterations> source
  *   iterations (a convergence threshold of 1e-30 never stops it earlier),
@@ -51,6 +70,7 @@
 #include "CPUSolver.h"
 #include "Geometry.h"
 #include "TrackGenerator.h"
+#include "TrackGenerator3D.h"
 #include "log.h"
 
 #include "../openmoc_gb300/adapter/pack_reference.h"
@@ -199,6 +219,219 @@ static Config make_config(const std::string& name) {
   exit(2);
 }
 
+struct Config3D {
+  Geometry* geo;
+  int num_azim, num_polar;
+  double spacing, z_spacing, fuel_height;
+};
+
+/* The n x n lattice for 0 < z < zf and a moderator cell above up to zt. */
+static Geometry* lattice_box_3d(int n, std::vector<Universe*> u, Material* mod,
+                                double zf, double zt) {
+  const double pitch = 1.26, hw = 0.5 * n * pitch;
+  Lattice* lat = new Lattice();
+  lat->setWidth(pitch, pitch);
+  lat->setUniverses(1, n, n, u.data());
+  XPlane* xmin = new XPlane(-hw);
+  XPlane* xmax = new XPlane(hw);
+  YPlane* ymin = new YPlane(-hw);
+  YPlane* ymax = new YPlane(hw);
+  ZPlane* zmin = new ZPlane(0.0);
+  ZPlane* zmid = new ZPlane(zf);
+  ZPlane* zmax = new ZPlane(zt);
+  xmin->setBoundaryType(REFLECTIVE);
+  xmax->setBoundaryType(REFLECTIVE);
+  ymin->setBoundaryType(REFLECTIVE);
+  ymax->setBoundaryType(REFLECTIVE);
+  zmin->setBoundaryType(VACUUM);
+  zmax->setBoundaryType(VACUUM);
+  Cell* low = new Cell();
+  low->addSurface(+1, xmin);
+  low->addSurface(-1, xmax);
+  low->addSurface(+1, ymin);
+  low->addSurface(-1, ymax);
+  low->addSurface(+1, zmin);
+  low->addSurface(-1, zmid);
+  low->setFill(lat);
+  Cell* top = new Cell();
+  top->addSurface(+1, xmin);
+  top->addSurface(-1, xmax);
+  top->addSurface(+1, ymin);
+  top->addSurface(-1, ymax);
+  top->addSurface(+1, zmid);
+  top->addSurface(-1, zmax);
+  top->setFill(mod);
+  Universe* ru = new Universe();
+  ru->addCell(low);
+  ru->addCell(top);
+  Geometry* g = new Geometry();
+  g->setRootUniverse(ru);
+  return g;
+}
+
+static Config3D make_config_3d(const std::string& name) {
+  if (name == "assembly3d") {
+    Material* fuel = make_material(1, openmoc_gb300::make_synthetic_xs(
+                                          SEED + 4, 7, true));
+    Material* mod = make_material(100, openmoc_gb300::make_synthetic_xs(
+                                           SEED + 1004, 7, false));
+    Universe* pin = make_pin(fuel, mod);
+    Universe* water = make_pin(mod, mod);
+    std::vector<Universe*> u(17 * 17, pin);
+    for (const auto& rc : GUIDE_TUBES) u[rc[0] * 17 + rc[1]] = water;
+    return {lattice_box_3d(17, u, mod, 16.0, 20.0), 16, 6, 0.1, 0.5, 16.0};
+  }
+  if (name == "lattice3d") {
+    Material* fuel = make_material(1, openmoc_gb300::make_synthetic_xs(
+                                          SEED + 0, 7, true));
+    Material* mod = make_material(100, openmoc_gb300::make_synthetic_xs(
+                                           SEED + 1000, 7, false));
+    Universe* pin = make_pin(fuel, mod);
+    Universe* water = make_pin(mod, mod);
+    std::vector<Universe*> u(9, pin);
+    u[4] = water;
+    return {lattice_box_3d(3, u, mod, 1.6, 2.0), 8, 4, 0.1, 0.4, 1.6};
+  }
+  fprintf(stderr, "unknown 3D configuration %s\n", name.c_str());
+  exit(2);
+}
+
+template <typename T>
+static void dump(const std::string& dir, const char* name, const char* dtype,
+                 const std::vector<T>& a, FILE* meta, bool& first) {
+  FILE* f = fopen((dir + "/" + name + ".bin").c_str(), "wb");
+  if (!f) {
+    perror(name);
+    exit(1);
+  }
+  fwrite(a.data(), sizeof(T), a.size(), f);
+  fclose(f);
+  fprintf(meta, "%s\n  \"%s\": [\"%s\", %zu]", first ? "" : ",", name, dtype,
+          a.size());
+  first = false;
+}
+
+static int laydown3d(const std::string& name, const std::string& dir,
+                     int threads) {
+  Config3D c = make_config_3d(name);
+  c.geo->initializeFlatSourceRegions();
+  TrackGenerator3D tg(c.geo, c.num_azim, c.num_polar, c.spacing, c.z_spacing);
+  tg.setSegmentFormation(EXPLICIT_3D);
+  tg.setNumThreads(threads);
+  tg.generateTracks();
+  PackedProblem p;
+  openmoc_gb300::pack_tracks(&tg, p);
+  const long T = tg.getNum3DTracks();
+  const int A = c.num_azim / 2, P = c.num_polar;
+  std::vector<int32_t> ta(T), txy(T), tp(T), tz(T), nseg(T);
+  std::vector<double> start(3 * T), end(3 * T), lsum(T), ltop(T);
+  Track3D**** t3d = tg.get3DTracks();
+  int*** tps = tg.getTracksPerStack();
+  Track** t2 = tg.get2DTracksArray();
+  long n2 = tg.getNum2DTracks();
+  for (long i = 0; i < n2; i++) {
+    const int a = t2[i]->getAzimIndex(), xy = t2[i]->getXYIndex();
+    for (int pp = 0; pp < P; pp++)
+      for (int z = 0; z < tps[a][xy][pp]; z++) {
+        Track3D* t = &t3d[a][xy][pp][z];
+        const long u = t->getUid();
+        ta[u] = a;
+        txy[u] = xy;
+        tp[u] = pp;
+        tz[u] = z;
+        start[3 * u] = t->getStart()->getX();
+        start[3 * u + 1] = t->getStart()->getY();
+        start[3 * u + 2] = t->getStart()->getZ();
+        end[3 * u] = t->getEnd()->getX();
+        end[3 * u + 1] = t->getEnd()->getY();
+        end[3 * u + 2] = t->getEnd()->getZ();
+        nseg[u] = t->getNumSegments();
+        double s = 0, top = 0;
+        for (int k = 0; k < t->getNumSegments(); k++) {
+          segment* sg = t->getSegment(k);
+          s += sg->_length;
+          if (sg->_starting_position[2] >= c.fuel_height - 1e-9)
+            top += sg->_length;
+        }
+        lsum[u] = s;
+        ltop[u] = top;
+      }
+  }
+  Quadrature* q = tg.getQuadrature();
+  std::vector<double> theta(A * P), pspace(A * P), pwgt(A * P), aspace(A * P),
+      awgt(A * P), wtot(A * P);
+  std::vector<int32_t> numl(A * P), numz(A * P);
+  for (int a = 0; a < A; a++)
+    for (int pp = 0; pp < P; pp++) {
+      const int r = a * P + pp;
+      theta[r] = q->getTheta(a, pp);
+      pspace[r] = q->getPolarSpacing(a, pp);
+      pwgt[r] = q->getPolarWeight(a, pp);
+      aspace[r] = q->getAzimSpacing(a);
+      awgt[r] = q->getAzimWeight(a);
+      wtot[r] = q->getWeightInline(a, pp);
+      numl[r] = tg.getNumL(a, pp);
+      numz[r] = tg.getNumZ(a, pp);
+    }
+  const long R = c.geo->getNumFSRs();
+  tg.initializeFSRVolumesBuffer();
+  FP_PRECISION* vols = tg.getFSRVolumes();
+  std::vector<double> vol(vols, vols + R);
+  FILE* meta = fopen((dir + "/meta.json").c_str(), "w");
+  if (!meta) {
+    perror("meta.json");
+    return 1;
+  }
+  fprintf(meta, "{\n  \"config\": [\"%s\", 0]", name.c_str());
+  bool first = false;
+  dump(dir, "azim", "i4", ta, meta, first);
+  dump(dir, "xy", "i4", txy, meta, first);
+  dump(dir, "polar", "i4", tp, meta, first);
+  dump(dir, "stack", "i4", tz, meta, first);
+  dump(dir, "start", "f8", start, meta, first);
+  dump(dir, "end", "f8", end, meta, first);
+  dump(dir, "nseg", "i4", nseg, meta, first);
+  dump(dir, "len_sum", "f8", lsum, meta, first);
+  dump(dir, "len_top", "f8", ltop, meta, first);
+  dump(dir, "next", "i8", p.next, meta, first);
+  dump(dir, "flags", "u1", p.flags, meta, first);
+  dump(dir, "theta", "f8", theta, meta, first);
+  dump(dir, "polar_spacing", "f8", pspace, meta, first);
+  dump(dir, "polar_weight", "f8", pwgt, meta, first);
+  dump(dir, "azim_spacing", "f8", aspace, meta, first);
+  dump(dir, "azim_weight", "f8", awgt, meta, first);
+  dump(dir, "weight", "f8", wtot, meta, first);
+  dump(dir, "num_l", "i4", numl, meta, first);
+  dump(dir, "num_z", "i4", numz, meta, first);
+  dump(dir, "fsr_vol", "f8", vol, meta, first);
+  if (p.num_segments < 10000000) {
+    /* small cases: every segment (length, start height, FSR id), UID order */
+    std::vector<double> sl, sz;
+    std::vector<int32_t> sfsr;
+    std::vector<Track3D*> by_uid(T);
+    for (long i = 0; i < n2; i++) {
+      const int a = t2[i]->getAzimIndex(), xy = t2[i]->getXYIndex();
+      for (int pp = 0; pp < P; pp++)
+        for (int z = 0; z < tps[a][xy][pp]; z++)
+          by_uid[t3d[a][xy][pp][z].getUid()] = &t3d[a][xy][pp][z];
+    }
+    for (long u = 0; u < T; u++)
+      for (int k = 0; k < by_uid[u]->getNumSegments(); k++) {
+        segment* sg = by_uid[u]->getSegment(k);
+        sl.push_back(sg->_length);
+        sz.push_back(sg->_starting_position[2]);
+        sfsr.push_back((int32_t) sg->_region_id);
+      }
+    dump(dir, "seg_len", "f8", sl, meta, first);
+    dump(dir, "seg_z0", "f8", sz, meta, first);
+    dump(dir, "seg_fsr", "i4", sfsr, meta, first);
+  }
+  fprintf(meta, "\n}\n");
+  fclose(meta);
+  printf("%s: R=%ld T=%ld S=%ld\n", name.c_str(), R, T, p.num_segments);
+  return 0;
+}
+
 /* Order-sensitive checksum of an array's bytes taken as little-endian words
  * of the element size: sum over i of (word_i + 1) * (2 i + 1) mod 2^64.
  * tests/test_benchmark_configs.py computes the same with numpy. */
@@ -245,6 +478,8 @@ int main(int argc, char** argv) {
   }
   set_log_level("ERROR");
   const std::string name = argv[1], mode = argv[2];
+  if (mode == "laydown3d")
+    return laydown3d(name, argv[3], argc > 4 ? atoi(argv[4]) : 1);
   const bool golden = mode == "golden";
   if (!golden && (mode != "time" || argc < 6)) {
     fprintf(stderr, "unknown mode or missing arguments\n");

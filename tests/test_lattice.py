@@ -3,6 +3,8 @@ tracks OpenMOC's TrackGenerator produced for the fixtures: integer data
 (FSR ids, segment offsets, links, flags, angles, materials) bit-identical,
 segment lengths bit-identical in float, FSR volumes to float accumulation
 order, and the benchmark-size counts OpenMOC reports."""
+import os
+
 import numpy as np
 import pytest
 
@@ -59,7 +61,9 @@ def _extruded_pin(dz=0.4, polar=4, azim=4, spacing=0.1):
 def test_extrusion_volumes_links_and_regions():
     """The axial extrusion: the same FSRs as OpenMOC's explicit-3D fixture
     (radial FSRs below the fuel top, one moderator region above), volumes
-    that sum to the zones' exact volumes, and links that pair up."""
+    that sum to the zones' exact volumes, and links that pair up: a flux
+    passed on at one end of a track comes back, along the reverse path, to
+    that same end."""
     p = _extruded_pin()
     ref, _, _ = load_case("pin3d_g7")
     assert p.solve_3d == 1 and p.num_polar_half == 1
@@ -74,22 +78,95 @@ def test_extrusion_volumes_links_and_regions():
     nxt = p.next.reshape(T, 2)
     for t in range(T):
         f = p.flags[t]
-        if f & 4:     # forward transfer: enters the next track forward
-            assert f & 1 and nxt[nxt[t, 0], 1] == t and p.flags[nxt[t, 0]] & 8
-        if f & 8:     # backward transfer: enters the previous track backward
-            assert not (f & 2) and nxt[nxt[t, 1], 0] == t
+        if f & 4:     # forward end: into n forward (bit 0) or backward
+            n = nxt[t, 0]
+            if f & 1:
+                assert nxt[n, 1] == t and p.flags[n] & 8 and not p.flags[n] & 2
+            else:
+                assert nxt[n, 0] == t and p.flags[n] & 4 and not p.flags[n] & 1
+        if f & 8:     # backward end: into n forward (bit 1) or backward
+            n = nxt[t, 1]
+            if f & 2:
+                assert nxt[n, 1] == t and p.flags[n] & 8 and p.flags[n] & 2
+            else:
+                assert nxt[n, 0] == t and p.flags[n] & 4 and p.flags[n] & 1
     # every line starts and ends on the vacuum bottom / top
     assert np.count_nonzero((p.flags & 4) == 0) == np.count_nonzero((p.flags & 8) == 0)
 
 
-def test_extrusion_converges_towards_openmoc_3d_keff():
-    """keff of the extruded pin approaches OpenMOC's explicit-3D result as
-    the laydown is refined (the laydowns differ; the physics is the same)."""
+def test_extrusion_is_openmocs_3d_laydown():
+    """The extruded pin with OpenMOC's fixture parameters (4 azimuthal, 4
+    polar, 0.1 cm radial, 0.4 cm axial) is OpenMOC's own explicit-3D
+    laydown (TrackGenerator3D, in the fixture pin3d_g7): the same tracks in
+    the same order, segment by segment the same regions (up to the FSR
+    numbering) and lengths, the same angle rows and weights, and the same
+    connections wherever the flux is passed on."""
+    p = _extruded_pin()
+    ref, _, _ = load_case("pin3d_g7")
+    assert (p.num_tracks, p.num_segments) == (ref.num_tracks, ref.num_segments)
+    assert np.array_equal(p.seg_off, ref.seg_off)
+    assert np.array_equal(p.track_ang, ref.track_ang)
+    assert np.allclose(p.weights, ref.weights, rtol=1e-6, atol=0)
+    assert np.allclose(p.seg_len, ref.seg_len, rtol=1e-6, atol=0)
+    # one FSR of ours for each of OpenMOC's, everywhere
+    pairs = set(zip(p.seg_fsr.tolist(), ref.seg_fsr.tolist()))
+    assert len(pairs) == len({a for a, _ in pairs}) == len({b for _, b in pairs}) == 13
+    for a, b in pairs:
+        assert p.fsr_vol[a] == pytest.approx(ref.fsr_vol[b], rel=1e-5)
+    f, g = ref.flags, p.flags
+    assert np.array_equal(f & 12, g & 12)
+    fwd, bwd = (f & 4) != 0, (f & 8) != 0
+    nr, nm = ref.next.reshape(-1, 2), p.next.reshape(-1, 2)
+    assert np.array_equal(nr[fwd, 0], nm[fwd, 0]) and np.array_equal(f[fwd] & 1, g[fwd] & 1)
+    assert np.array_equal(nr[bwd, 1], nm[bwd, 1]) and np.array_equal(f[bwd] & 2, g[bwd] & 2)
+
+
+def test_assembly3d_is_openmocs_3d_laydown():
+    """The 3D benchmark assembly (17 x 17 extruded to 20 cm, 16 azimuthal,
+    6 polar, 0.1 / 0.5 cm) against OpenMOC's own laydown of it
+    (tests/golden/openmoc_assembly3d_laydown.json, written by
+    make_laydown3d_golden.py from TrackGenerator3D): the track and segment
+    counts, checksums of the segment counts, angle rows, transfer flags and
+    connections in track order, and the lengths, weights and volumes."""
+    from conftest import GOLDEN, track_checksum
+    from openmoc_gb300 import lattice
+    import json
+    with open(os.path.join(GOLDEN, "openmoc_assembly3d_laydown.json")) as fh:
+        g = json.load(fh)
+    p = lattice.assembly_17x17_3d()
+    assert (p.num_fsrs, p.num_tracks, p.num_segments) == (
+        g["num_fsrs"], g["num_tracks"], g["num_segments"])
+    nseg = np.diff(p.seg_off).astype(np.int32)
+    flags, nxt = p.flags, p.next.reshape(-1, 2)
+    fwd, bwd = (flags & 4) != 0, (flags & 8) != 0
+    masked = (flags & 12) | np.where(fwd, flags & 1, 0) | np.where(bwd, flags & 2, 0)
+    c = g["checksums"]
+    assert track_checksum(nseg) == int(c["nseg"])
+    assert track_checksum(p.track_ang.astype(np.int32)) == int(c["row"])
+    assert track_checksum(masked.astype(np.uint8)) == int(c["flags"])
+    assert track_checksum(np.where(fwd, nxt[:, 0], -1).astype(np.int64)) == int(c["next_fwd"])
+    assert track_checksum(np.where(bwd, nxt[:, 1], -1).astype(np.int64)) == int(c["next_bwd"])
+    lsum = np.add.reduceat(p.seg_len.astype(np.float64), p.seg_off[:-1])
+    rows = np.bincount(p.track_ang, weights=lsum, minlength=len(g["row_length"]))
+    assert np.allclose(rows, g["row_length"], rtol=1e-6, atol=0)
+    above = p.seg_len[p.seg_fsr == p.num_fsrs - 1].astype(np.float64).sum()
+    assert above == pytest.approx(g["length_above_fuel"], rel=1e-6)
+    assert np.allclose(p.weights, g["weights"], rtol=1e-6, atol=0)
+    vol = np.sort(p.fsr_vol.astype(np.float64))
+    assert np.allclose(np.quantile(vol, np.linspace(0, 1, 101)), g["volume_quantiles"],
+                       rtol=1e-5, atol=0)
+    assert vol.sum() == pytest.approx(g["volume_total"], rel=1e-6)
+
+
+def test_extrusion_keff_is_openmocs():
+    """On OpenMOC's own laydown the FP64 oracle gives the keff of OpenMOC's
+    explicit-3D run (fixture pin3d_g7, stopped by the same 1e-5 criterion)
+    within the parity bar."""
     from oracle.oracle import Oracle
     _, sc, _ = load_case("pin3d_g7", "f64")
-    o = Oracle(_extruded_pin(0.1, 6, 8, 0.05), "f64", num_threads=2)
-    o.compute_eigenvalue(1000, 1, 1e-6)
-    assert abs(o.keff - sc["keff"]) / sc["keff"] < 0.03
+    o = Oracle(_extruded_pin(), "f64", num_threads=2)
+    o.compute_eigenvalue(int(sc["max_iters"]), int(sc["res_type"]), sc["tolerance"])
+    assert abs(o.keff - sc["keff"]) < 1e-5
 
 
 def _otf_pieces(p):
