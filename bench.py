@@ -514,6 +514,11 @@ def run_gpu(args):
             out["serving"] = {k: sv[k] for k in ("metric", "value", "unit", "config",
                                                  "batched", "plain", "speedup",
                                                  "ceiling", "by_class", "agreement")}
+            if args.serving_ls_requests > 0:
+                sv = run_serving(args, ls=True)
+                out["serving_ls"] = {k: sv[k] for k in (
+                    "metric", "value", "unit", "config", "batched", "plain", "speedup",
+                    "ceiling", "by_class", "agreement")}
         print(json.dumps(out), flush=True)
     s.close()
     if dist:
@@ -781,9 +786,17 @@ SERVING_GROUPS = (2, 7, 16, 70)
 SERVING_AZIM = (16, 32, 48, 64)
 SERVING_SPACING = (0.05, 0.075, 0.1)
 SOURCE_KEFF = 3.0   # fixed eigenvalue of the source solves, above every request's own k
+# the linear-source stream: the same request classes without the 17x17
+# assemblies and the 70-group sets
+SERVING_LS_WORKLOAD = ("linear-source request stream (CPULSSolver): Poisson arrivals, "
+                       "70% eigenvalue / 30% fixed-source; pin cell, 3x3 or 7x7 lattice; "
+                       "2, 7 or 16 groups; lognormal(0, 0.05) cross-section factors; "
+                       "16-64 azimuthal; 0.05-0.1 cm")
+SERVING_LS_GEOMS = ("pin", "3x3", "7x7")
+SERVING_LS_GROUPS = (2, 7, 16)
 
 
-def serving_stream(n, seed, mean_gap_ms):
+def serving_stream(n, seed, mean_gap_ms, geoms=SERVING_GEOMS, groups=SERVING_GROUPS):
     """n requests: arrival time, geometry, groups, quadrature, kind, seed."""
     rng = np.random.default_rng(seed)
     t = 0.0
@@ -791,18 +804,19 @@ def serving_stream(n, seed, mean_gap_ms):
     for i in range(n):
         t += rng.exponential(mean_gap_ms * 1e-3)
         out.append(dict(
-            i=i, arrival=t, geom=SERVING_GEOMS[rng.integers(4)],
-            G=int(SERVING_GROUPS[rng.integers(4)]),
+            i=i, arrival=t, geom=geoms[rng.integers(len(geoms))],
+            G=int(groups[rng.integers(len(groups))]),
             azim=int(SERVING_AZIM[rng.integers(4)]),
             spacing=float(SERVING_SPACING[rng.integers(3)]),
             kind="source" if rng.random() < 0.3 else "eigenvalue"))
     return out
 
 
-def serving_problems(stream):
+def serving_problems(stream, ls=False):
     """Problems of a request stream; track laydowns are generated once per
     (geometry, quadrature) and each request gets its own perturbed cross
-    sections (factor on sigma_t and the same row of scattering)."""
+    sections (factor on sigma_t and the same row of scattering).  ls: with
+    the linear-source geometry."""
     from openmoc_gb300 import lattice
     tracks = {}
     probs = []
@@ -810,12 +824,15 @@ def serving_problems(stream):
         key = (r["geom"], r["azim"], r["spacing"])
         if key not in tracks:
             if r["geom"] == "pin":
-                tracks[key] = lattice.pin_cell(2, r["azim"], r["spacing"])
+                tracks[key] = lattice.pin_cell(2, r["azim"], r["spacing"],
+                                               linear_source=ls)
             elif r["geom"] == "17x17":
-                tracks[key] = lattice.assembly_17x17(2, r["azim"], r["spacing"], config=0)
+                tracks[key] = lattice.assembly_17x17(2, r["azim"], r["spacing"], config=0,
+                                                     linear_source=ls)
             else:
                 n = int(r["geom"][0])
-                tracks[key] = lattice.square_lattice(n, 2, r["azim"], r["spacing"], config=0)
+                tracks[key] = lattice.square_lattice(n, 2, r["azim"], r["spacing"], config=0,
+                                                     linear_source=ls)
         mats = lattice._fuel_mod(0, r["G"], 1, perturb=(1000 + r["i"], 0.05))
         p = tracks[key].with_xs(*lattice.pack_materials(mats))
         fs = None
@@ -826,10 +843,10 @@ def serving_problems(stream):
     return probs
 
 
-def serve_plain(stream, probs, max_iters):
-    """The plain loop: one GB300Solver per request, one at a time, in
-    arrival order (upload, solve, fluxes back)."""
-    from openmoc_gb300 import GB300Solver
+def serve_plain(stream, probs, max_iters, ls=False):
+    """The plain loop: one GB300Solver (GB300LSSolver with ls) per request,
+    one at a time, in arrival order (upload, solve, fluxes back)."""
+    from openmoc_gb300 import GB300LSSolver, GB300Solver
     out = []
     t0 = time.perf_counter()
     clock = 0.0
@@ -838,9 +855,10 @@ def serve_plain(stream, probs, max_iters):
         if now < r["arrival"]:
             time.sleep(r["arrival"] - now)
         t_start = time.perf_counter()
-        s = GB300Solver(p)
+        s = GB300LSSolver(p) if ls else GB300Solver(p)
         s.setAutotune(False)
-        s.useExponentialIntrinsic()
+        if not ls:
+            s.useExponentialIntrinsic()
         s.setConvergenceThreshold(1e-5)
         if fs is not None:
             s.setFixedSources(fs)
@@ -858,9 +876,10 @@ def serve_plain(stream, probs, max_iters):
 
 
 def serve_batched(stream, probs, max_iters, max_solves, k, priorities=True,
-                  hot_bytes=0):
+                  hot_bytes=0, ls=False):
     """The server: requests submitted at their arrival times from this
-    thread while the request loop runs on its own."""
+    thread while the request loop runs on its own (ls: linear-source
+    pools and requests)."""
     from openmoc_gb300.serving import Server, pool_capacity
     srv = Server(iterations_per_poll=k, priorities=priorities, hot_bytes=hot_bytes)
     by_g = {}
@@ -868,7 +887,8 @@ def serve_batched(stream, probs, max_iters, max_solves, k, priorities=True,
         by_g.setdefault(p.num_groups, []).append(p)
     pools = []
     for G, ps in sorted(by_g.items()):
-        pools.append(srv.add_pool(G, ps[0].num_polar_half, **pool_capacity(ps, max_solves)))
+        pools.append(srv.add_pool(G, ps[0].num_polar_half, linear_source=ls,
+                                  **pool_capacity(ps, max_solves)))
     srv.start()
     t0 = time.perf_counter()
     tickets = []
@@ -877,9 +897,10 @@ def serve_batched(stream, probs, max_iters, max_solves, k, priorities=True,
         if now < r["arrival"]:
             time.sleep(r["arrival"] - now)
         if fs is not None:
-            t = srv.submit(p, "source", max_iters, 2, k_eff=SOURCE_KEFF, fixed_source=fs)
+            t = srv.submit(p, "source", max_iters, 2, k_eff=SOURCE_KEFF, fixed_source=fs,
+                           linear_source=ls)
         else:
-            t = srv.submit(p, "eigenvalue", max_iters, 1)
+            t = srv.submit(p, "eigenvalue", max_iters, 1, linear_source=ls)
         tickets.append(t)
     res = [srv.wait(t) for t in tickets]
     clock = time.perf_counter() - t0
@@ -893,19 +914,26 @@ def serve_batched(stream, probs, max_iters, max_solves, k, priorities=True,
     return res, clock, stats
 
 
-def run_serving(args):
+def run_serving(args, ls=False):
+    """The request-stream benchmark; ls: the linear-source stream through
+    linear-source pools against a plain loop of GB300LSSolver."""
     import torch  # noqa: F401  (CUDA context and device checks)
-    stream = serving_stream(args.serving_requests, 0xC0FFEE + 2, args.serving_gap_ms)
+    if ls:
+        stream = serving_stream(args.serving_ls_requests, 0xC0FFEE + 3,
+                                args.serving_ls_gap_ms, SERVING_LS_GEOMS,
+                                SERVING_LS_GROUPS)
+    else:
+        stream = serving_stream(args.serving_requests, 0xC0FFEE + 2, args.serving_gap_ms)
     t_prep = time.perf_counter()
-    probs = serving_problems(stream)
+    probs = serving_problems(stream, ls)
     t_prep = time.perf_counter() - t_prep
     # warm both paths (kernel loading, autotune caches) on a few requests
-    serve_plain(stream[:4], probs[:4], args.serving_iters)
+    serve_plain(stream[:4], probs[:4], args.serving_iters, ls)
     batched, t_b, stats = serve_batched(stream, probs, args.serving_iters,
                                         args.serving_slots, args.serving_k,
                                         not args.serving_no_priorities,
-                                        args.serving_hot_mb << 20)
-    plain, t_p = serve_plain(stream, probs, args.serving_iters)
+                                        args.serving_hot_mb << 20, ls)
+    plain, t_p = serve_plain(stream, probs, args.serving_iters, ls)
     diffs = []
     for r, a, b in zip(stream, batched, plain):
         fa, fb = a["flux"].astype(np.float64), b["flux"].astype(np.float64)
@@ -953,15 +981,18 @@ def run_serving(args):
     ceiling = {"stream_integrations": total_int,
                "best_single_problem_rate": best_rate,
                "min_makespan_s_at_best_rate": total_int / best_rate,
-               "speedup_ceiling_at_best_rate": t_p / (total_int / best_rate),
-               "min_makespan_s_at_fp32_peak": total_int / fp32_rate,
-               "speedup_ceiling_at_fp32_peak": t_p / (total_int / fp32_rate)}
+               "speedup_ceiling_at_best_rate": t_p / (total_int / best_rate)}
+    if not ls:   # the flat sweep's flops per integration
+        ceiling.update({"min_makespan_s_at_fp32_peak": total_int / fp32_rate,
+                        "speedup_ceiling_at_fp32_peak": t_p / (total_int / fp32_rate)})
     out = {
         "metric": "solves/s (batched server vs plain per-solve loop)",
         "value": n / t_b, "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
         "data": "synthetic (seeded cross sections, generated tracks)",
-        "config": {"workload": SERVING_WORKLOAD, "requests": n,
-                   "mean_interarrival_ms": args.serving_gap_ms,
+        "config": {"workload": SERVING_LS_WORKLOAD if ls else SERVING_WORKLOAD,
+                   "requests": n,
+                   "mean_interarrival_ms": (args.serving_ls_gap_ms if ls
+                                            else args.serving_gap_ms),
                    "source_keff": SOURCE_KEFF, "max_iters": args.serving_iters,
                    "solves_per_pool": args.serving_slots,
                    "iterations_per_poll": args.serving_k,
@@ -1012,6 +1043,14 @@ def main():
     ap.add_argument("--serving", action="store_true",
                     help="the request-stream benchmark (batched server vs plain loop)")
     ap.add_argument("--serving-requests", type=int, default=512)
+    ap.add_argument("--serving-ls", action="store_true",
+                    help="the linear-source request stream alone (with --serving)")
+    ap.add_argument("--serving-ls-requests", type=int, default=256,
+                    help="requests of the linear-source stream (0: leave it out "
+                         "of the default line)")
+    ap.add_argument("--serving-ls-gap-ms", type=float, default=0.25,
+                    help="mean interarrival time of the linear-source stream (its "
+                         "solves are short: a 2 ms gap leaves the server idle)")
     ap.add_argument("--serving-gap-ms", type=float, default=2.0)
     ap.add_argument("--serving-iters", type=int, default=1000)
     ap.add_argument("--serving-slots", type=int, default=64)
@@ -1041,7 +1080,7 @@ def main():
     elif args.impl == "reference":
         run_reference(args)
     elif args.serving:
-        print(json.dumps(run_serving(args)), flush=True)
+        print(json.dumps(run_serving(args, ls=args.serving_ls)), flush=True)
     else:
         run_gpu(args)
 

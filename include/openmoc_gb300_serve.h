@@ -8,8 +8,8 @@
  * device-resident request loop that runs many such solves concurrently with
  * the same per-solve results (same loop body, same convergence test):
  *
- *   - a pool holds every live solve of one group count and polar count in
- *     shared device arrays (FSR rows, tracks, segments, materials and angle
+ *   - a pool holds every live solve of one group count, polar count and
+ *     source kind (flat, or linear as CPULSSolver) in shared device arrays (FSR rows, tracks, segments, materials and angle
  *     rows are contiguous ranges handed out by first-fit allocators over the
  *     pool's capacity, which is its device-memory budget);
  *   - one iteration of a pool is six launches for all of its solves
@@ -26,8 +26,9 @@
  *     size class (power of two of live tracks), unless fixed; the timing
  *     sweeps write into scratch buffers, so live state is untouched.
  *
- * Requests reference host arrays owned by the caller, which must stay valid
- * (and flux_out writable) until the request completes.  Every entry point
+ * Requests reference host arrays owned by the caller: the input arrays are
+ * copied by moc_server_submit, flux_out and moments_out must stay writable
+ * until the request completes.  Every entry point
  * returns MOC_OK or a negative MOC_ERR_* status; moc_last_error() gives the
  * text.  moc_server_submit, moc_server_wait, moc_server_poll and
  * moc_server_stats may be called from any thread; moc_server_step only when
@@ -80,6 +81,9 @@ typedef struct {
   int32_t pairs;          /* group pairs per lane (with lanes): the fewest
                              that cover the groups, ceil(ceil(G/2)/lanes) */
   int32_t exp_kind;       /* with lanes: MOC_EXP_INTRINSIC (pools use ex2) */
+  int32_t linear_source;  /* 1: the pool takes linear-source requests
+                             (CPULSSolver, 2D), at most 5 group pairs per
+                             lane; 0: flat-source requests */
 } moc_pool_config;
 
 typedef struct {
@@ -108,6 +112,15 @@ typedef struct {
   double k_eff;      /* MOC_SOLVE_SOURCE: the fixed eigenvalue */
   double threshold;  /* convergence threshold */
   float* flux_out;   /* [R][G] scalar fluxes, written on completion */
+  int32_t allow_negative_fluxes; /* Solver::allowNegativeFluxes */
+  /* linear source (NULL: flat source): the geometry moc_set_linear_source
+     takes; the request goes to its (G, Ph) linear-source pool, which
+     computes the expansion constants when it admits the request */
+  const moc_ls_geometry* linear_source;
+  const float* fixed_source_moments; /* [R][3][G] (x, y, z; z unused) or
+                                        NULL (setFixedSourceMomentByFSR) */
+  float* moments_out;  /* [R][3][G] flux moments (z = 0) written on
+                          completion, or NULL */
 } moc_request;
 
 typedef struct {
@@ -135,7 +148,8 @@ typedef struct {
 int moc_server_create(const moc_server_config* cfg, moc_server** out);
 int moc_server_destroy(moc_server* srv);
 
-/** Adds a pool; requests go to the pool of their (G, Ph). */
+/** Adds a pool; requests go to the pool of their (G, Ph) and source
+ *  kind (flat or linear). */
 int moc_server_add_pool(moc_server* srv, const moc_pool_config* cfg,
                         int* pool);
 

@@ -217,6 +217,40 @@ void launch_ls_refresh_ids(const int2* segs, int4* out, int64_t S,
   ls_refresh_kernel<<<(unsigned) grid_for(S, 256), 256, 0, s>>>(segs, out, S);
 }
 
+void launch_ls_seg_track(const int64_t* seg_off, int64_t T, int32_t* seg_track,
+                         cudaStream_t s) {
+  if (T == 0) return;
+  ls_seg_track_kernel<<<(unsigned) grid_for(32 * T, 256), 256, 0, s>>>(
+      seg_off, T, seg_track);
+}
+
+void launch_ls_constants_bucketed(const int4* segs_ls, const int32_t* list,
+                                  const int64_t* start,
+                                  const int32_t* seg_track,
+                                  const int32_t* track_ang,
+                                  const double* ang_dir, const double* ang_wgt,
+                                  const double* pol_sin, const double* pol_wgt,
+                                  int Ph, const float* sigma_t,
+                                  const float* fsr_vol, const int32_t* fsr_mat,
+                                  int64_t R, int G, int ld, float* ilem,
+                                  float* cst, unsigned int* num_flat,
+                                  cudaStream_t s) {
+  const unsigned blocks = (unsigned) grid_for(32 * R, 256);
+#define MOC_LS_CONST(SS)                                                    \
+  ls_constants_kernel<SS><<<blocks, 256, 0, s>>>(                           \
+      segs_ls, list, start, seg_track, track_ang, ang_dir, ang_wgt,         \
+      pol_sin, pol_wgt, Ph, sigma_t, fsr_vol, fsr_mat, R, G, ld, ilem, cst, \
+      num_flat)
+  switch ((ld + 31) / 32) {
+    case 1: MOC_LS_CONST(1); break;
+    case 2: MOC_LS_CONST(2); break;
+    case 3: MOC_LS_CONST(3); break;
+    case 4: MOC_LS_CONST(4); break;
+    default: MOC_LS_CONST(8); break;
+  }
+#undef MOC_LS_CONST
+}
+
 int launch_ls_constants(const int4* segs_ls, const int64_t* seg_off,
                         const int32_t* track_ang, int64_t T, int64_t S,
                         const double* ang_dir, const double* ang_wgt,
@@ -269,20 +303,10 @@ int launch_ls_constants(const int4* segs_ls, const int64_t* seg_off,
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) {
-    const unsigned blocks = (unsigned) grid_for(32 * R, 256);
-#define MOC_LS_CONST(SS)                                                    \
-  ls_constants_kernel<SS><<<blocks, 256, 0, s>>>(                           \
-      segs_ls, list, startp, seg_track, track_ang, ang_dir, ang_wgt,        \
-      pol_sin, pol_wgt, Ph, sigma_t, fsr_vol, fsr_mat, R, G, ld, ilem, cst, \
-      num_flat)
-    switch ((ld + 31) / 32) {
-      case 1: MOC_LS_CONST(1); break;
-      case 2: MOC_LS_CONST(2); break;
-      case 3: MOC_LS_CONST(3); break;
-      case 4: MOC_LS_CONST(4); break;
-      default: MOC_LS_CONST(8); break;
-    }
-#undef MOC_LS_CONST
+    launch_ls_constants_bucketed(segs_ls, list, startp, seg_track, track_ang,
+                                 ang_dir, ang_wgt, pol_sin, pol_wgt, Ph,
+                                 sigma_t, fsr_vol, fsr_mat, R, G, ld, ilem, cst,
+                                 num_flat, s);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);

@@ -85,7 +85,9 @@ struct LsOccupancy {
 };
 
 // CM: also the CMFD partial currents (a.cm_cell set), as the flat sweep's
-// mode 2.
+// mode 2.  In a pool (a.track_slot set) each track takes the pending
+// angular-flux scale of its solve and is skipped once its solve is done, as
+// in the flat sweep's mode 1.
 template <int PH, int LPS, int PS, bool CM>
 __global__ void __launch_bounds__(kSweepThreads,
                                   (LsOccupancy<PH, PS>::min_blocks))
@@ -106,7 +108,6 @@ ls_sweep_kernel(const SweepArgs a) {
   const int cur = sc->cur;
   const float* psi_in = a.psi[cur];
   float* psi_out = a.psi[cur ^ 1];
-  const float scale = sc->scale[cur];
 
   const int lane = threadIdx.x & 31;
   const int sub = lane & (LPS - 1);
@@ -115,8 +116,19 @@ ls_sweep_kernel(const SweepArgs a) {
   const int64_t stream = gwarp * (32 / LPS) + lane / LPS;
   const int npairs = ld >> 1;
 
-  if (stream < 2 * a.num_tracks) {
-    const int t = a.order[stream >> 1];
+  // the LPS lanes of a stream share its track, so they agree on skipping it
+  bool live = stream < 2 * a.num_tracks;
+  int t = 0;
+  float scale = sc->scale[cur];
+  if (live) {
+    t = a.order[stream >> 1];
+    if (a.track_slot) {
+      const DevScalars* ts = a.slots + a.track_slot[t];
+      live = ts->done == 0;
+      scale = ts->scale[cur];
+    }
+  }
+  if (live) {
     const int dir = (int) (stream & 1);
     const int64_t b = a.seg_off[t];
     const int n = (int) (a.seg_off[t + 1] - b);
@@ -281,11 +293,16 @@ ls_sweep_kernel(const SweepArgs a) {
     last = (ticket == gridDim.x - 1);
   }
   __syncthreads();
-  if (last && threadIdx.x == 0) {
-    sc->ticket_sweep = 0;
-    sc->scale[cur ^ 1] = 1.0f;
-    sc->cur = cur ^ 1;
-    __threadfence();
+  if (last) {
+    if (a.track_slot)
+      for (int i = threadIdx.x; i < a.num_slots; i += blockDim.x)
+        a.slots[i].scale[cur ^ 1] = 1.0f;
+    if (threadIdx.x == 0) {
+      sc->ticket_sweep = 0;
+      sc->scale[cur ^ 1] = 1.0f;
+      sc->cur = cur ^ 1;
+      __threadfence();
+    }
   }
 }
 

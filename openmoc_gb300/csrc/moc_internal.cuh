@@ -53,6 +53,7 @@ struct DevScalars {
   long long row0;
   long long nrows;
   int tc_error;           // a tensor-core source launch gave up waiting
+  int negative_ok;        // pools: this solve allows negative fluxes
   // keff from the neutron balance (Solver::setKeffFromNeutronBalance):
   // absorption-rate accumulator and the leakage the last sweep tallied at
   // vacuum track ends
@@ -352,6 +353,23 @@ int launch_ls_constants(const int4* segs_ls, const int64_t* seg_off,
                         const int32_t* fsr_mat, int64_t R, int G, int ld,
                         float* ilem, float* cst, unsigned int* num_flat,
                         cudaStream_t s);
+// The track of every segment from the segment offsets (seg_off[0] = 0).
+void launch_ls_seg_track(const int64_t* seg_off, int64_t T, int32_t* seg_track,
+                         cudaStream_t s);
+// The same constants from segment buckets the caller built (segment ids
+// of FSR r at list[start[r] .. start[r + 1]), and the track of every
+// segment): one launch, asynchronous, nothing allocated.
+void launch_ls_constants_bucketed(const int4* segs_ls, const int32_t* list,
+                                  const int64_t* start,
+                                  const int32_t* seg_track,
+                                  const int32_t* track_ang,
+                                  const double* ang_dir, const double* ang_wgt,
+                                  const double* pol_sin, const double* pol_wgt,
+                                  int Ph, const float* sigma_t,
+                                  const float* fsr_vol, const int32_t* fsr_mat,
+                                  int64_t R, int G, int ld, float* ilem,
+                                  float* cst, unsigned int* num_flat,
+                                  cudaStream_t s);
 // Builds segs_ls from the packed segments and the start positions.
 void launch_ls_pack_segments(const int2* segs, const float* x, const float* y,
                              int4* out, int64_t S, cudaStream_t s);
@@ -377,14 +395,18 @@ bool launch_ls_sweep(const SweepArgs& a, int polar_half, int slots,
 // rate_finish (one block per solve) updates keff, the normalisation factor
 // and the pending angular-flux scale; residual normalises, leaves each row's
 // residual term in row_val and stores phi_old; residual_finish ends the
-// iteration of every live solve (convergence, counters, done).
+// iteration of every live solve (convergence, counters, done).  In a pool
+// of linear-source solves (a.mom set) the sources and add-source are
+// launch_ls_sources / launch_ls_add_source, which take the same per-row
+// states, and residual also normalises the flux moments.
 void launch_batch_sources(const SolverArgs& a, cudaStream_t s);
 void launch_batch_add_source(const SolverArgs& a, cudaStream_t s);
 void launch_batch_rate_finish(const SolverArgs& a, cudaStream_t s);
 void launch_batch_residual(const SolverArgs& a, cudaStream_t s);
 void launch_batch_residual_finish(const SolverArgs& a, cudaStream_t s);
 // Initial state of one admitted solve: rows [r0, r0 + n) of phi and phi_old
-// set to value, qt zeroed.
+// set to value, qt (and with a linear source the flux and source moments)
+// zeroed.
 void launch_batch_init_rows(const SolverArgs& a, int64_t r0, int64_t n,
                             float value, cudaStream_t s);
 // Rebases one admitted solve's track data from its own numbering to the

@@ -36,6 +36,9 @@ namespace {
 // Group pairs per lane for G groups over lps lanes.
 int pairs_for(int G, int lps) { return ((G + 1) / 2 + lps - 1) / lps; }
 
+// Group pairs per lane of the linear-source sweep instances.
+constexpr int kLsMaxPairs = 5;
+
 #define SV_FAIL(code, msg) moc::set_error(code, std::string(msg).c_str())
 
 #define SV_CHECK(cond, code, msg)          \
@@ -145,6 +148,20 @@ struct Staged {
   std::vector<int32_t> fsr_mat;
   std::vector<float> fsr_vol;
   std::vector<float> fixed;        // [R][ld] or empty
+  // linear source: segment starts relative to the FSR centroids, the angle
+  // data in moc_set_linear_source's layout ([A][2] directions, [A] weights,
+  // [A][Ph] sin(theta), [A][Ph] polar weights), and the fixed source
+  // moments as [R][ld][2] (empty: none)
+  bool ls = false;
+  std::vector<float> seg_x, seg_y;
+  std::vector<double> ls_ang;
+  std::vector<float2> ls_dir;
+  std::vector<float> fixed_xy;
+  // segments bucketed by FSR for the expansion constants (ids of FSR r at
+  // ls_list[ls_start[r] .. ls_start[r + 1]), ascending), built here so that
+  // admission only copies and launches
+  std::vector<int64_t> ls_start;
+  std::vector<int32_t> ls_list;
   long long num_fissionable = 0;
   double init_flux = 1.0;          // flat starting flux (normalised)
   double t_submit = 0.0, t_admit = 0.0;
@@ -165,8 +182,85 @@ struct Staged {
     std::vector<uint8_t>().swap(fissile);
     std::vector<float>().swap(fsr_vol);
     std::vector<float>().swap(fixed);
+    std::vector<float>().swap(seg_x);
+    std::vector<float>().swap(seg_y);
+    std::vector<double>().swap(ls_ang);
+    std::vector<float2>().swap(ls_dir);
+    std::vector<float>().swap(fixed_xy);
+    std::vector<int64_t>().swap(ls_start);
+    std::vector<int32_t>().swap(ls_list);
   }
 };
+
+// The linear-source part of a request, checked as moc_set_linear_source and
+// moc_set_fixed_source_moments check theirs (same limits and messages).
+int stage_linear_source(const moc_request& q, Staged& s) {
+  const moc_ls_geometry* g = q.linear_source;
+  const int64_t S = s.S, R = s.R;
+  const int A = s.A, Ph = s.Ph, G = s.G, ld = s.ld;
+  SV_CHECK(G <= 256, MOC_ERR_UNSUPPORTED,
+           "the linear source takes at most 256 groups and 2^31 segments");
+  SV_CHECK(S == 0 || (g->seg_x && g->seg_y), MOC_ERR_ARG,
+           "null linear-source array");
+  SV_CHECK(g->ang_dir && g->ang_wgt && g->pol_sin && g->pol_wgt, MOC_ERR_ARG,
+           "null linear-source array");
+  s.seg_x.resize(S);
+  s.seg_y.resize(S);
+  for (int64_t i = 0; i < S; i++) {
+    SV_CHECK(std::isfinite(g->seg_x[i]) && std::isfinite(g->seg_y[i]),
+             MOC_ERR_ARG,
+             "non-finite segment start position at segment " +
+                 std::to_string(i));
+    s.seg_x[i] = g->seg_x[i];
+    s.seg_y[i] = g->seg_y[i];
+  }
+  s.ls_ang.assign(3 * (size_t) A + 2 * (size_t) A * Ph, 0.0);
+  s.ls_dir.resize(A);
+  for (int a = 0; a < A; a++) {
+    const double cx = g->ang_dir[2 * a], cy = g->ang_dir[2 * a + 1];
+    SV_CHECK(std::isfinite(cx) && std::isfinite(cy) &&
+                 std::fabs(cx * cx + cy * cy - 1.0) < 1e-6,
+             MOC_ERR_ARG,
+             "track direction of angle " + std::to_string(a) +
+                 " is not a unit vector");
+    SV_CHECK(std::isfinite(g->ang_wgt[a]) && g->ang_wgt[a] > 0.0, MOC_ERR_ARG,
+             "azimuthal weight must be positive");
+    s.ls_ang[2 * a] = cx;
+    s.ls_ang[2 * a + 1] = cy;
+    s.ls_ang[2 * A + a] = g->ang_wgt[a];
+    s.ls_dir[a] = make_float2((float) cx, (float) cy);
+    for (int p = 0; p < Ph; p++) {
+      const double sn = g->pol_sin[a * Ph + p], w = g->pol_wgt[a * Ph + p];
+      SV_CHECK(std::isfinite(sn) && sn > 0.0 && sn <= 1.0, MOC_ERR_ARG,
+               "sin(theta) must lie in (0, 1]");
+      SV_CHECK(std::isfinite(w) && w >= 0.0, MOC_ERR_ARG,
+               "polar weight must be non-negative");
+      s.ls_ang[3 * A + a * Ph + p] = sn;
+      s.ls_ang[3 * A + A * Ph + a * Ph + p] = w;
+    }
+  }
+  if (q.fixed_source_moments) {
+    s.fixed_xy.assign(2 * (size_t) R * ld, 0.0f);
+    for (int64_t r = 0; r < R; r++)
+      for (int gg = 0; gg < G; gg++) {
+        const float x = q.fixed_source_moments[(r * 3 + 0) * G + gg];
+        const float y = q.fixed_source_moments[(r * 3 + 1) * G + gg];
+        SV_CHECK(std::isfinite(x) && std::isfinite(y), MOC_ERR_ARG,
+                 "non-finite moment");
+        s.fixed_xy[2 * (r * ld + gg)] = x;
+        s.fixed_xy[2 * (r * ld + gg) + 1] = y;
+      }
+  }
+  // buckets: a counting sort of the segment ids by FSR
+  s.ls_start.assign(R + 1, 0);
+  for (int64_t i = 0; i < S; i++) s.ls_start[s.segs[i].y + 1]++;
+  for (int64_t r = 0; r < R; r++) s.ls_start[r + 1] += s.ls_start[r];
+  s.ls_list.resize(S);
+  std::vector<int64_t> fill(s.ls_start.begin(), s.ls_start.end() - 1);
+  for (int64_t i = 0; i < S; i++) s.ls_list[fill[s.segs[i].y]++] = (int32_t) i;
+  s.ls = true;
+  return MOC_OK;
+}
 
 // Checks a request as moc_upload_* check a context's inputs and packs it.
 int stage_request(const moc_request& q, Staged& s) {
@@ -197,6 +291,11 @@ int stage_request(const moc_request& q, Staged& s) {
   SV_CHECK(q.kind != MOC_SOLVE_SOURCE || q.k_eff > 0.0, MOC_ERR_ARG,
            "The Solver is unable to compute the source with a non-positive "
            "keff");
+  SV_CHECK(!q.linear_source || q.num_segments < (1LL << 31),
+           MOC_ERR_UNSUPPORTED,
+           "the linear source takes at most 256 groups and 2^31 segments");
+  SV_CHECK(q.linear_source || (!q.fixed_source_moments && !q.moments_out),
+           MOC_ERR_ARG, "flux moments need a linear-source request");
   const int G = q.num_groups, M = q.num_materials, Ph = q.num_polar_half;
   const int64_t R = q.num_fsrs, T = q.num_tracks, S = q.num_segments;
   s.req = q;
@@ -327,7 +426,7 @@ int stage_request(const moc_request& q, Staged& s) {
         s.fixed[r * s.ld + g] = v;
       }
   }
-  return MOC_OK;
+  return q.linear_source ? stage_linear_source(q, s) : MOC_OK;
 }
 
 }  // namespace
@@ -386,6 +485,25 @@ struct Pool {
   moc::DevScalars* slots_h = nullptr;  // pinned: states read back per block
   moc::DevScalars* init_h = nullptr;   // pinned: states written at admission
   float* retire_h = nullptr;           // pinned: fluxes of retired solves
+  // linear source (ls): 16-byte segment words, angle directions, inverse
+  // expansion matrices, source constants, source and flux moments, fixed
+  // source moments; admission scratch (segment starts, angle data, the
+  // count of flat FSRs); the moments of retired solves
+  bool ls = false;
+  int4* segs_ls = nullptr;
+  float2* ang_dir = nullptr;
+  float* ls_ilem = nullptr;
+  float* ls_const = nullptr;
+  float* qxy = nullptr;
+  float* mom = nullptr;
+  float* fixed_xy = nullptr;
+  float* ls_xy = nullptr;
+  double* ls_ang = nullptr;
+  int64_t* ls_start = nullptr;
+  int32_t* ls_list = nullptr;
+  int32_t* ls_seg_track = nullptr;
+  unsigned int* ls_flat = nullptr;
+  float* retire_mom_h = nullptr;
 
   RangeAlloc rows, tracks, segments, mats, angles;
   std::vector<int> free_slots;
@@ -406,6 +524,7 @@ struct Pool {
   // autotuner scratch outputs
   float* tune_psi = nullptr;
   float* tune_phi = nullptr;
+  float* tune_mom = nullptr;
   moc::DevScalars* tune_sc = nullptr;
   moc::DevScalars* tune_slots = nullptr;
   // counters (read under the server mutex)
@@ -466,13 +585,28 @@ void destroy_pool(Pool& p) {
   dev_free(p.slots_d);
   dev_free(p.tune_psi);
   dev_free(p.tune_phi);
+  dev_free(p.tune_mom);
   dev_free(p.tune_sc);
   dev_free(p.tune_slots);
+  dev_free(p.segs_ls);
+  dev_free(p.ang_dir);
+  dev_free(p.ls_ilem);
+  dev_free(p.ls_const);
+  dev_free(p.qxy);
+  dev_free(p.mom);
+  dev_free(p.fixed_xy);
+  dev_free(p.ls_xy);
+  dev_free(p.ls_ang);
+  dev_free(p.ls_start);
+  dev_free(p.ls_list);
+  dev_free(p.ls_seg_track);
+  dev_free(p.ls_flat);
   if (p.slots_h) cudaFreeHost(p.slots_h);
   if (p.init_h) cudaFreeHost(p.init_h);
   if (p.retire_h) cudaFreeHost(p.retire_h);
+  if (p.retire_mom_h) cudaFreeHost(p.retire_mom_h);
   p.slots_h = p.init_h = nullptr;
-  p.retire_h = nullptr;
+  p.retire_h = p.retire_mom_h = nullptr;
   for (cudaEvent_t e : p.tune_ev) cudaEventDestroy(e);
   if (p.block_start) cudaEventDestroy(p.block_start);
   if (p.block_done) cudaEventDestroy(p.block_done);
@@ -494,7 +628,16 @@ int create_pool(moc_server* srv, const moc_pool_config& c, Pool& p) {
   const int ld = c.num_groups + (c.num_groups & 1);
   SV_CHECK((int64_t) c.max_materials * ld * 4 <= 200 * 1024, MOC_ERR_ARG,
            "max_materials x groups exceeds the sweep's shared-memory table");
+  SV_CHECK(c.linear_source == 0 || c.linear_source == 1, MOC_ERR_ARG,
+           "linear_source must be 0 or 1");
+  SV_CHECK(!c.linear_source || c.num_groups <= 256, MOC_ERR_UNSUPPORTED,
+           "the linear source takes at most 256 groups and 2^31 segments");
+  SV_CHECK(!c.linear_source || c.max_segments < (1LL << 31),
+           MOC_ERR_UNSUPPORTED,
+           "the linear source takes at most 256 groups and 2^31 segments");
   if (c.lanes != 0) {
+    SV_CHECK(!c.linear_source || c.pairs <= kLsMaxPairs, MOC_ERR_ARG,
+             "the linear-source sweep takes at most 5 group pairs per lane");
     SV_CHECK(moc::sweep_lps_supported(c.lanes), MOC_ERR_ARG,
              "lanes per track direction must be 1, 2, 4, 8, 16 or 32");
     SV_CHECK(c.pairs >= 1 && c.pairs <= moc::kMaxSlots &&
@@ -511,6 +654,7 @@ int create_pool(moc_server* srv, const moc_pool_config& c, Pool& p) {
   p.Ph = c.num_polar_half;
   p.ld = ld;
   p.F = p.G * p.Ph;
+  p.ls = c.linear_source != 0;
   if (c.lanes != 0) {
     p.lps = c.lanes;
     p.pairs = c.pairs;
@@ -586,6 +730,28 @@ int create_pool(moc_server* srv, const moc_pool_config& c, Pool& p) {
   SV_CUDA(cudaMemset(p.psi[0], 0, sizeof(float) * npsi));
   SV_CUDA(cudaMemset(p.psi[1], 0, sizeof(float) * npsi));
   SV_CUDA(cudaMemset(p.sigma_s_T, 0, sizeof(float) * (MG * p.G + 4)));
+  if (p.ls) {
+    SV_TRY(dev_alloc(&p.segs_ls, S));
+    SV_TRY(dev_alloc(&p.ang_dir, A));
+    SV_TRY(dev_alloc(&p.ls_ilem, 3 * R));
+    SV_TRY(dev_alloc(&p.ls_const, 3 * R * ld));
+    SV_TRY(dev_alloc(&p.qxy, 2 * R * ld));
+    SV_TRY(dev_alloc(&p.mom, 2 * R * ld));
+    SV_TRY(dev_alloc(&p.fixed_xy, 2 * R * ld));
+    SV_TRY(dev_alloc(&p.ls_xy, 2 * S));
+    SV_TRY(dev_alloc(&p.ls_ang, A * (3 + 2 * p.Ph)));
+    SV_TRY(dev_alloc(&p.ls_start, R + 1));
+    SV_TRY(dev_alloc(&p.ls_list, S));
+    SV_TRY(dev_alloc(&p.ls_seg_track, S));
+    SV_TRY(dev_alloc(&p.ls_flat, 1));
+    SV_CUDA(cudaMallocHost((void**) &p.retire_mom_h,
+                           sizeof(float) * 2 * R * ld));
+    SV_CUDA(cudaMemset(p.qxy, 0, sizeof(float) * 2 * R * ld));
+    SV_CUDA(cudaMemset(p.mom, 0, sizeof(float) * 2 * R * ld));
+    SV_CUDA(cudaMemset(p.fixed_xy, 0, sizeof(float) * 2 * R * ld));
+    SV_CUDA(cudaMemset(p.ls_ilem, 0, sizeof(float) * 3 * R));
+    SV_CUDA(cudaMemset(p.ls_const, 0, sizeof(float) * 3 * R * ld));
+  }
   p.rows.reset(R);
   p.tracks.reset(T);
   p.segments.reset(S);
@@ -626,6 +792,12 @@ moc::SweepArgs pool_sweep_args(Pool& p) {
   a.num_slots = p.cfg.max_solves;
   a.hot_base = 0x7FFFFFFF;   // no shared-memory tallies in pools
   a.hot_count = 0;
+  if (p.ls) {
+    a.segs_ls = p.segs_ls;
+    a.ang_dir = p.ang_dir;
+    a.qxy = p.qxy;
+    a.mom = p.mom;
+  }
   return a;
 }
 
@@ -658,6 +830,13 @@ moc::SolverArgs pool_solver_args(Pool& p) {
   a.slots = p.slots_d;
   a.row_val = p.row_val;
   a.num_slots = p.cfg.max_solves;
+  if (p.ls) {
+    a.mom = p.mom;
+    a.qxy = p.qxy;
+    a.ls_ilem = p.ls_ilem;
+    a.ls_const = p.ls_const;
+    a.fixed_xy = p.fixed_xy;
+  }
   return a;
 }
 
@@ -681,8 +860,64 @@ void publish(moc_server* srv, const Staged& st, const moc_result& r) {
 }
 
 // Bytes of a solve that the sweep gathers and scatters by FSR id: its
-// reduced sources and tallies.
-int64_t hot_bytes(const Staged& s) { return 8 * s.R * s.ld; }
+// reduced sources and tallies, and with a linear source their x and y
+// moments too.
+int64_t hot_bytes(const Staged& s) { return (s.ls ? 24 : 8) * s.R * s.ld; }
+
+// The linear-source data of an admitted solve, while its segments and track
+// data are still in its own numbering: the 16-byte segment words, its angle
+// directions and fixed source moments, and its expansion matrices and
+// source constants (CPULSSolver::initializeFSRs with
+// LinearExpansionGenerator, src/CPULSSolver.cpp:136-146), computed over its
+// own segments into its rows from the buckets staged on submission.  All
+// copies and launches are in the pool's stream order, so the admission
+// scratch is reused by the next admission without a synchronisation.
+int upload_linear_source(moc_server* srv, Pool& p, const Slot& sl) {
+  const Staged& s = *sl.st;
+  cudaStream_t st = p.stream;
+  const int64_t S = s.S, R = s.R, ld = p.ld;
+  const int A = s.A, Ph = s.Ph;
+  if (S > 0) {
+    float* dx = p.ls_xy;
+    float* dy = p.ls_xy + S;
+    SV_CUDA(cudaMemcpyAsync(dx, s.seg_x.data(), sizeof(float) * S,
+                            cudaMemcpyHostToDevice, st));
+    SV_CUDA(cudaMemcpyAsync(dy, s.seg_y.data(), sizeof(float) * S,
+                            cudaMemcpyHostToDevice, st));
+    moc::launch_ls_pack_segments(p.segs + sl.s0, dx, dy, p.segs_ls + sl.s0,
+                                 S, st);
+  }
+  SV_CUDA(cudaMemcpyAsync(p.ls_ang, s.ls_ang.data(),
+                          sizeof(double) * s.ls_ang.size(),
+                          cudaMemcpyHostToDevice, st));
+  SV_CUDA(cudaMemcpyAsync(p.ang_dir + sl.a0, s.ls_dir.data(),
+                          sizeof(float2) * A, cudaMemcpyHostToDevice, st));
+  if (s.fixed_xy.empty())
+    SV_CUDA(cudaMemsetAsync(p.fixed_xy + 2 * sl.r0 * ld, 0,
+                            sizeof(float) * 2 * R * ld, st));
+  else
+    SV_CUDA(cudaMemcpyAsync(p.fixed_xy + 2 * sl.r0 * ld, s.fixed_xy.data(),
+                            sizeof(float) * 2 * R * ld,
+                            cudaMemcpyHostToDevice, st));
+  SV_CUDA(cudaMemcpyAsync(p.ls_start, s.ls_start.data(),
+                          sizeof(int64_t) * (R + 1), cudaMemcpyHostToDevice,
+                          st));
+  if (S > 0) {
+    SV_CUDA(cudaMemcpyAsync(p.ls_list, s.ls_list.data(), sizeof(int32_t) * S,
+                            cudaMemcpyHostToDevice, st));
+    moc::launch_ls_seg_track(p.seg_off + sl.t0, s.T, p.ls_seg_track, st);
+  }
+  const double* ang = p.ls_ang;
+  moc::launch_ls_constants_bucketed(
+      p.segs_ls + sl.s0, p.ls_list, p.ls_start, p.ls_seg_track,
+      p.track_ang + sl.t0, ang, ang + 2 * A, ang + 3 * A,
+      ang + 3 * A + A * Ph, Ph, p.sigma_t, p.fsr_vol + sl.r0,
+      p.fsr_mat + sl.r0, R, s.G, (int) ld, p.ls_ilem + 3 * sl.r0,
+      p.ls_const + 3 * sl.r0 * ld, p.ls_flat, st);
+  SV_CUDA(cudaGetLastError());
+  add_launches(srv, S > 0 ? 3 : 1);
+  return MOC_OK;
+}
 
 // Copies a solve's data into the ranges given to it and rebases them.
 int upload_slot(moc_server* srv, Pool& p, int slot_index) {
@@ -734,10 +969,13 @@ int upload_slot(moc_server* srv, Pool& p, int slot_index) {
     SV_CUDA(cudaMemcpyAsync(p.fixed + sl.r0 * p.ld, s.fixed.data(),
                             sizeof(float) * R * p.ld, cudaMemcpyHostToDevice,
                             st));
+  if (p.ls) SV_TRY(upload_linear_source(srv, p, sl));
   moc::launch_batch_rebase(p.segs + sl.s0, S, p.fsr_mat, (int32_t) sl.r0,
                            p.seg_off + sl.t0, p.next + 2 * sl.t0,
                            p.track_ang + sl.t0, p.track_slot + sl.t0, T, sl.s0,
                            (int32_t) sl.t0, (int32_t) sl.a0, slot_index, st);
+  // the linear-source words take the rebased FSR ids and materials
+  if (p.ls) moc::launch_ls_refresh_ids(p.segs + sl.s0, p.segs_ls + sl.s0, S, st);
   SV_CUDA(cudaGetLastError());
   // rows become visible to the row kernels only with their owner set, after
   // the data above in stream order
@@ -775,6 +1013,7 @@ int init_slot(moc_server* srv, Pool& p, int slot_index) {
                                                 : moc::kModeSource;
   d.res_type = s.req.res_type;
   d.num_fissionable = s.num_fissionable;
+  d.negative_ok = s.req.allow_negative_fluxes ? 1 : 0;
   d.row0 = sl.r0;
   d.nrows = s.R;
   SV_CUDA(cudaMemcpyAsync(p.slots_d + slot_index, &d, sizeof(d),
@@ -864,6 +1103,11 @@ int retire(moc_server* srv, Pool& p) {
     SV_CUDA(cudaMemcpyAsync(p.retire_h + sl.r0 * p.ld, p.phi + sl.r0 * p.ld,
                             sizeof(float) * R * p.ld, cudaMemcpyDeviceToHost,
                             p.stream));
+    if (p.ls && sl.st->req.moments_out)
+      SV_CUDA(cudaMemcpyAsync(p.retire_mom_h + 2 * sl.r0 * p.ld,
+                              p.mom + 2 * sl.r0 * p.ld,
+                              sizeof(float) * 2 * R * p.ld,
+                              cudaMemcpyDeviceToHost, p.stream));
     // the rows leave the row kernels' view before they are reused
     SV_CUDA(cudaMemsetAsync(p.row_slot + sl.r0, 0xFF, sizeof(int32_t) * R,
                             p.stream));
@@ -877,6 +1121,17 @@ int retire(moc_server* srv, Pool& p) {
     for (int64_t r = 0; r < s.R; r++)
       std::memcpy(s.req.flux_out + r * s.G, rows + r * p.ld,
                   sizeof(float) * s.G);
+    if (p.ls && s.req.moments_out) {
+      // [R][ld][2] (x, y adjacent) -> [R][3][G] with z = 0
+      const float* m = p.retire_mom_h + 2 * sl.r0 * p.ld;
+      float* out = s.req.moments_out;
+      for (int64_t r = 0; r < s.R; r++)
+        for (int g = 0; g < s.G; g++) {
+          out[(r * 3 + 0) * s.G + g] = m[2 * (r * p.ld + g)];
+          out[(r * 3 + 1) * s.G + g] = m[2 * (r * p.ld + g) + 1];
+          out[(r * 3 + 2) * s.G + g] = 0.0f;
+        }
+    }
     moc_result res{};
     res.status = MOC_OK;
     res.converged = d.converged;
@@ -944,7 +1199,14 @@ int rebuild_order(Pool& p) {
 }
 
 
-// Times every sweep shape with at most kMaxSlots pairs per lane and at
+// The pool's sweep (flat or linear source) with the given shape.
+bool pool_sweep(Pool& p, const moc::SweepArgs& a, int pairs) {
+  if (p.ls) return moc::launch_ls_sweep(a, p.Ph, pairs, p.stream);
+  return moc::launch_sweep(a, p.Ph, pairs, MOC_EXP_INTRINSIC, p.stream);
+}
+
+// Times every sweep shape with at most kMaxSlots pairs per lane (5 with a
+// linear source) and at
 // least half of its lanes busy on the pool's current solves (the faster of
 // two sweeps after a warm-up) and keeps the fastest.  The timing sweeps read
 // the live tracks and sources but write tallies, angular fluxes, the buffer
@@ -962,6 +1224,7 @@ int autotune_pool(moc_server* srv, Pool& p) {
     const int64_t npsi = p.cfg.max_tracks * 2 * p.F;
     SV_TRY(dev_alloc(&p.tune_psi, npsi));
     SV_TRY(dev_alloc(&p.tune_phi, p.cfg.max_fsrs * p.ld));
+    if (p.ls) SV_TRY(dev_alloc(&p.tune_mom, 2 * p.cfg.max_fsrs * p.ld));
     SV_TRY(dev_alloc(&p.tune_sc, 1));
     SV_TRY(dev_alloc(&p.tune_slots, N));
     SV_CUDA(cudaMemsetAsync(p.tune_psi, 0, sizeof(float) * npsi, p.stream));
@@ -972,20 +1235,22 @@ int autotune_pool(moc_server* srv, Pool& p) {
                           cudaMemcpyDeviceToDevice, p.stream));
   float best_ms = 1e30f;
   int best_lps = 0, best_pairs = 0;
+  const int max_pairs = p.ls ? kLsMaxPairs : moc::kMaxSlots;
   for (int lps = 1; lps <= 32; lps *= 2) {
     const int pairs = pairs_for(p.G, lps);
-    if (pairs > moc::kMaxSlots || (double) p.G / (2.0 * lps * pairs) < 0.5)
+    if (pairs > max_pairs || (double) p.G / (2.0 * lps * pairs) < 0.5)
       continue;
     p.lps = lps;
     moc::SweepArgs a = pool_sweep_args(p);
     a.phi = p.tune_phi;
+    if (p.ls) a.mom = p.tune_mom;
     a.psi[0] = a.psi[1] = p.tune_psi;
     a.sc = p.tune_sc;
     a.slots = p.tune_slots;
     float best = 1e30f;
     for (int r = 0; r < 3; r++) {
       SV_CUDA(cudaEventRecord(p.tune_ev[0], p.stream));
-      if (!moc::launch_sweep(a, p.Ph, pairs, MOC_EXP_INTRINSIC, p.stream))
+      if (!pool_sweep(p, a, pairs))
         return SV_FAIL(MOC_ERR_UNSUPPORTED, "no sweep kernel for the pool");
       SV_CUDA(cudaEventRecord(p.tune_ev[1], p.stream));
       SV_CUDA(cudaEventSynchronize(p.tune_ev[1]));
@@ -1040,10 +1305,16 @@ int choose_shape(moc_server* srv, Pool& p) {
 int enqueue_iteration(Pool& p) {
   moc::SolverArgs a = pool_solver_args(p);
   moc::SweepArgs w = pool_sweep_args(p);
-  moc::launch_batch_sources(a, p.stream);
-  if (!moc::launch_sweep(w, p.Ph, p.pairs, p.exp_kind, p.stream))
+  if (p.ls)
+    moc::launch_ls_sources(a, 0, 1, p.stream);
+  else
+    moc::launch_batch_sources(a, p.stream);
+  if (!pool_sweep(p, w, p.pairs))
     return SV_FAIL(MOC_ERR_UNSUPPORTED, "no sweep kernel for the pool");
-  moc::launch_batch_add_source(a, p.stream);
+  if (p.ls)
+    moc::launch_ls_add_source(a, 0, p.stream);
+  else
+    moc::launch_batch_add_source(a, p.stream);
   moc::launch_batch_rate_finish(a, p.stream);
   moc::launch_batch_residual(a, p.stream);
   moc::launch_batch_residual_finish(a, p.stream);
@@ -1239,8 +1510,11 @@ int moc_server_add_pool(moc_server* srv, const moc_pool_config* cfg,
   SV_CHECK(!srv->running.load(), MOC_ERR_STATE,
            "add pools before starting the loop");
   for (auto& p : srv->pools)
-    SV_CHECK(p->G != cfg->num_groups || p->Ph != cfg->num_polar_half,
-             MOC_ERR_ARG, "a pool for this group and polar count exists");
+    SV_CHECK(p->G != cfg->num_groups || p->Ph != cfg->num_polar_half ||
+                 p->ls != (cfg->linear_source != 0),
+             MOC_ERR_ARG,
+             "a pool for this group count, polar count and source kind "
+             "exists");
   SV_CUDA(cudaSetDevice(srv->cfg.device));
   std::unique_ptr<Pool> p(new Pool());
   p->index = (int) srv->pools.size();
@@ -1259,12 +1533,15 @@ int moc_server_submit(moc_server* srv, const moc_request* req,
                       int64_t* ticket) {
   SV_CHECK(srv && req, MOC_ERR_ARG, "null argument");
   Pool* target = nullptr;
+  const bool ls = req->linear_source != nullptr;
   for (auto& p : srv->pools)
-    if (p->G == req->num_groups && p->Ph == req->num_polar_half)
+    if (p->G == req->num_groups && p->Ph == req->num_polar_half && p->ls == ls)
       target = p.get();
   SV_CHECK(target, MOC_ERR_UNSUPPORTED,
-           "no pool for " + std::to_string(req->num_groups) + " groups and " +
-               std::to_string(req->num_polar_half) + " polar angles");
+           "no " + std::string(ls ? "linear-source" : "flat-source") +
+               " pool for " + std::to_string(req->num_groups) +
+               " groups and " + std::to_string(req->num_polar_half) +
+               " polar angles");
   std::unique_ptr<Staged> s(new Staged());
   SV_TRY(stage_request(*req, *s));
   const moc_pool_config& c = target->cfg;

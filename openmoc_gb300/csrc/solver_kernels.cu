@@ -316,14 +316,17 @@ compute_sources_kernel(const SolverArgs a, int iteration, int zero_phi,
       }
       on &= ~keep;
       if (!on) continue;
-      // the FP64 reciprocals in one lane (the rows are the whole warp's)
+      // the FP64 reciprocals in one lane (the rows are the whole warp's);
+      // the flat source reads the iteration only for the clamp of negative
+      // sources in the first 30 iterations, which a solve that allows
+      // negative fluxes never applies
       const bool lane0 = (threadIdx.x & 31) == 0;
       if (on & 1) {
-        it0 = p0->iteration;
+        it0 = p0->negative_ok ? 30 : p0->iteration;
         if (lane0) ik0 = (float) (1.0 / p0->keff);
       }
       if (on & 2) {
-        it1 = p1->iteration;
+        it1 = p1->negative_ok ? 30 : p1->iteration;
         if (lane0) ik1 = (float) (1.0 / p1->keff);
       }
       ik0 = __shfl_sync(0xffffffffu, ik0, 0);
@@ -807,6 +810,15 @@ __global__ void fsr_rates_kernel(const SolverArgs a, double* out, int nu) {
   }
 }
 
+// Batched pools: the state of the solve owning row r; null for unused rows and finished solves.
+__device__ __forceinline__ DevScalars* live_slot(const SolverArgs& a,
+                                                 int64_t r) {
+  const int sl = a.row_slot[r];
+  if (sl < 0) return nullptr;
+  DevScalars* ss = a.slots + sl;
+  return ss->done ? nullptr : ss;
+}
+
 // ----------------------------------------------------------- linear source
 // CPULSSolver::computeFSRSources (src/CPULSSolver.cpp:386-527): one warp per
 // FSR computes the flat source of CPUSolver and, from the same pass over the
@@ -815,7 +827,10 @@ __global__ void fsr_rates_kernel(const SolverArgs a, double* out, int nu) {
 // matrix, times 1/(8 pi), and are zeroed where the flat source is not
 // above 1e-24 during the first 30 iterations (unless negative fluxes are
 // allowed).  Stores Q/sigma_t and (q_x, q_y)/sigma_t for the sweep; fused:
-// zeroes the flux and moment tallies.
+// zeroes the flux and moment tallies.  In a pool (a.row_slot set) each row
+// takes keff, the iteration count and the negative-flux rule of its solve;
+// a computeFlux solve keeps the sources of its first iteration and only has
+// its tallies zeroed.
 template <int S>
 __global__ void __launch_bounds__(kThreads)
 ls_sources_kernel(const SolverArgs a, int iteration, int zero, int staged) {
@@ -831,16 +846,37 @@ ls_sources_kernel(const SolverArgs a, int iteration, int zero, int staged) {
   }
   const float* ssT =
       staged ? reinterpret_cast<const float*>(s_ss4) : a.sigma_s_T;
-  const float inv_k = (float) (1.0 / a.sc->keff);
-  if (iteration < 0) iteration = a.sc->iteration;
+  const bool pool = a.row_slot != nullptr;
+  const float inv_k1 = pool ? 0.0f : (float) (1.0 / a.sc->keff);
+  if (iteration < 0 && !pool) iteration = a.sc->iteration;
   const int GG = G * G;
   const int lane = threadIdx.x & 31;
   const int ld = a.ld;
   unsigned long long negatives = 0;
   for (int64_t r = first_row(); r < a.num_fsrs; r += row_step()) {
-    const int m = a.fsr_mat[r];
     float* phi = a.phi + r * ld;
     float2* mom = reinterpret_cast<float2*>(a.mom + r * 2 * ld);
+    float inv_k = inv_k1;
+    int it = iteration;
+    bool neg_ok = a.negative_ok;
+    if (pool) {
+      const DevScalars* ss = live_slot(a, r);
+      if (!ss) continue;
+      if (ss->mode == kModeFlux && ss->iteration > 0) {
+        if (zero)
+          for (int g = lane; g < G; g += 32) {
+            phi[g] = 0.0f;
+            mom[g] = make_float2(0.f, 0.f);
+          }
+        continue;
+      }
+      it = ss->iteration;
+      neg_ok = ss->negative_ok != 0;
+      // the FP64 reciprocal in one lane (the row is the whole warp's)
+      if (lane == 0) inv_k = (float) (1.0 / ss->keff);
+      inv_k = __shfl_sync(0xffffffffu, inv_k, 0);
+    }
+    const int m = a.fsr_mat[r];
     float ph[S], mx[S], my[S], s0[S], s1[S], s2[S];
 #pragma unroll
     for (int j = 0; j < S; j++) {
@@ -916,7 +952,7 @@ ls_sources_kernel(const SolverArgs a, int iteration, int zero, int staged) {
       q *= (float) kOneOverFourPi;
       if (q < 0.0f) {
         negatives++;
-        if (iteration < 30 && !a.negative_ok) q = kFluxEpsilon;
+        if (it < 30 && !neg_ok) q = kFluxEpsilon;
       }
       float sx = fmaf(chi[gd], f1, s1[j]);
       float sy = fmaf(chi[gd], f2v, s2[j]);
@@ -926,7 +962,7 @@ ls_sources_kernel(const SolverArgs a, int iteration, int zero, int staged) {
         sy += fx.y;
       }
       float rx = 0.0f, ry = 0.0f;
-      if (a.negative_ok || q > 10.0f * kFluxEpsilon || iteration > 29) {
+      if (neg_ok || q > 10.0f * kFluxEpsilon || it > 29) {
         rx = (float) (kOneOverFourPi / 2) * fmaf(il0, sx, il2 * sy);
         ry = (float) (kOneOverFourPi / 2) * fmaf(il2, sx, il1 * sy);
       }
@@ -944,7 +980,9 @@ ls_sources_kernel(const SolverArgs a, int iteration, int zero, int staged) {
 //   m_y = m_y / (sigma_t V) + 8 pi (q_x c_xy + q_y c_yy) / sigma_t,
 // a negative flux (unless allowed) becomes max(old flux, 1e-25) with zero
 // moments.  update = 1 also finishes the keff / normalisation update as
-// add_source_kernel does.
+// add_source_kernel does.  In a pool (a.row_slot set; update = 0) each row
+// follows its solve's negative-flux rule and leaves its FP64 nu-fission
+// term in row_val, as batch_add_source_kernel does.
 template <int S>
 __global__ void __launch_bounds__(kRowThreads)
 ls_add_source_kernel(const SolverArgs a, int update) {
@@ -952,10 +990,17 @@ ls_add_source_kernel(const SolverArgs a, int update) {
   const int G = a.num_groups;
   const int ld = a.ld;
   const int lane = threadIdx.x & 31;
-  double rate = 0.0, arate = 0.0;
+  double rate = 0.0;
   unsigned long long negatives = 0;
-  const bool balance = update && a.keff_balance;
+  const bool pool = a.row_slot != nullptr;
   for (int64_t r = first_row(); r < a.num_fsrs; r += row_step()) {
+    DevScalars* ss = nullptr;
+    bool neg_ok = a.negative_ok;
+    if (pool) {
+      ss = live_slot(a, r);
+      if (!ss) continue;
+      neg_ok = ss->negative_ok != 0;
+    }
     const int m = a.fsr_mat[r];
     const float vol0 = a.fsr_vol[r];
     const float vol = (vol0 < 1.0e-12f) ? 1.0e30f : vol0;
@@ -985,6 +1030,7 @@ ls_add_source_kernel(const SolverArgs a, int update) {
       c2[j] = on ? cst[2 * ld + g] : 0.0f;
     }
     float rr = 0.0f;
+    int row_neg = 0;
 #pragma unroll
     for (int j = 0; j < S; j++) {
       const int g = lane + 32 * j;
@@ -995,16 +1041,26 @@ ls_add_source_kernel(const SolverArgs a, int update) {
                                         fmaf(qq[j].x, c0[j], qq[j].y * c2[j]));
       float my = fmaf(mm[j].y, inv, (float) (2 * kFourPi) *
                                         fmaf(qq[j].x, c2[j], qq[j].y * c1[j]));
-      if (x < 0.0f && !a.negative_ok) {
+      if (x < 0.0f && !neg_ok) {
         x = fmaxf(o[j], kFluxEpsilon);
         mx = 0.0f;
         my = 0.0f;
-        negatives++;
+        row_neg++;
       }
       phi[g] = x;
       mom[g] = make_float2(mx, my);
       rr = fmaf(nf[g], x, rr);
     }
+    if (pool) {
+      const double row_rate = warp_sum_all_d((double) rr * (double) vol0);
+      row_neg = __reduce_add_sync(0xffffffffu, row_neg);
+      if (lane == 0) {
+        a.row_val[r] = row_rate;
+        if (row_neg) atomicAdd(&ss->neg_fluxes, (unsigned long long) row_neg);
+      }
+      continue;
+    }
+    negatives += row_neg;
     if (update) rate += (double) rr * (double) vol0;
   }
   if (negatives) atomicAdd(&a.sc->neg_fluxes, negatives);
@@ -1050,15 +1106,6 @@ __global__ void ls_scale_moments_kernel(const SolverArgs a) {
 // row_val, and one block per solve sums its rows in a fixed order and
 // updates the solve's state.
 
-// State of the solve owning row r; null for unused rows and finished solves.
-__device__ __forceinline__ DevScalars* live_slot(const SolverArgs& a,
-                                                 int64_t r) {
-  const int sl = a.row_slot[r];
-  if (sl < 0) return nullptr;
-  DevScalars* ss = a.slots + sl;
-  return ss->done ? nullptr : ss;
-}
-
 template <int S>
 __global__ void __launch_bounds__(kRowThreads)
 batch_add_source_kernel(const SolverArgs a) {
@@ -1089,7 +1136,7 @@ batch_add_source_kernel(const SolverArgs a) {
       if (g >= G) continue;
       float x = v[j] / (st[g] * vol);
       x += (float) kFourPi * q[j];
-      if (x < 0.0f) {
+      if (x < 0.0f && !ss->negative_ok) {
         x = kFluxEpsilon;
         negatives++;
       }
@@ -1137,8 +1184,10 @@ __global__ void batch_rate_finish_kernel(const SolverArgs a) {
   }
 }
 
-// Residual terms per row: eigenvalue solves are normalised first; phi is
-// stored into phi_old.  The residual type is the solve's own.
+// Residual terms per row: eigenvalue solves are normalised first (with a
+// linear source, the flux moments too: CPULSSolver::normalizeFluxes,
+// src/CPULSSolver.cpp:362-378); phi is stored into phi_old.  The residual
+// type is the solve's own.
 template <int S>
 __global__ void __launch_bounds__(kRowThreads)
 batch_residual_kernel(const SolverArgs a) {
@@ -1155,6 +1204,17 @@ batch_residual_kernel(const SolverArgs a) {
     if (RT == 2) {
       if (lane == 0) inv_k = (float) (1.0 / ss->keff);
       inv_k = __shfl_sync(0xffffffffu, inv_k, 0);
+    }
+    if (a.mom && normalise) {
+      float4* m4 = reinterpret_cast<float4*>(a.mom + r * 2 * a.ld);
+      for (int i = lane; i < (a.ld >> 1); i += 32) {
+        float4 v = m4[i];
+        v.x *= factor;
+        v.y *= factor;
+        v.z *= factor;
+        v.w *= factor;
+        m4[i] = v;
+      }
     }
     const int m = a.fsr_mat[r];
     const bool fis = a.fissile[m] != 0;
@@ -1254,6 +1314,11 @@ __global__ void batch_init_rows_kernel(const SolverArgs a, int64_t r0,
     a.phi[base + i] = value;
     a.phi_old[base + i] = value;
     a.qt[base + i] = 0.0f;
+    if (a.mom) {
+      // the flux moments of a flat flux, and no source moments yet
+      reinterpret_cast<float2*>(a.mom)[base + i] = make_float2(0.f, 0.f);
+      reinterpret_cast<float2*>(a.qxy)[base + i] = make_float2(0.f, 0.f);
+    }
   }
 }
 

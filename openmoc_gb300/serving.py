@@ -4,8 +4,9 @@ of uneven size sharing one GPU (ctypes binding of
 
 OpenMOC runs one problem per ``Solver`` object, one at a time
 (src/Solver.cpp:1352-1700).  A :class:`Server` runs the same loop body for
-every admitted request at once: one pool per (groups, polar) count holds
-its solves in shared device arrays, an iteration is six kernel launches for
+every admitted request at once: one pool per (groups, polar) count and
+source kind (flat, or linear as CPULSSolver) holds its solves in shared
+device arrays, an iteration is six kernel launches for
 all of them, blocks of iterations replay as CUDA graphs, and finished solves
 are retired and queued ones admitted between blocks (continuous batching).
 
@@ -48,6 +49,7 @@ class PoolConfig(C.Structure):
         ("max_angles", C.c_int32), ("max_fsrs", C.c_int64),
         ("max_tracks", C.c_int64), ("max_segments", C.c_int64),
         ("lanes", C.c_int32), ("pairs", C.c_int32), ("exp_kind", C.c_int32),
+        ("linear_source", C.c_int32),
     ]
 
 
@@ -66,7 +68,9 @@ class Request(C.Structure):
         ("fixed_source", C.c_void_p),
         ("kind", C.c_int32), ("max_iters", C.c_int32), ("res_type", C.c_int32),
         ("k_eff", C.c_double), ("threshold", C.c_double),
-        ("flux_out", C.c_void_p),
+        ("flux_out", C.c_void_p), ("allow_negative_fluxes", C.c_int32),
+        ("linear_source", C.POINTER(_native.LSGeometry)),
+        ("fixed_source_moments", C.c_void_p), ("moments_out", C.c_void_p),
     ]
 
 
@@ -168,14 +172,16 @@ class Server:
     def add_pool(self, num_groups: int, num_polar_half: int, max_solves: int,
                  max_materials: int, max_angles: int, max_fsrs: int,
                  max_tracks: int, max_segments: int,
-                 shape: Optional[tuple] = None) -> int:
-        """Adds the pool of (num_groups, num_polar_half).  shape = (lanes,
-        pairs, exp_kind) fixes the sweep shape; None autotunes it on the
-        pool's first batch."""
+                 shape: Optional[tuple] = None,
+                 linear_source: bool = False) -> int:
+        """Adds the pool of (num_groups, num_polar_half) and source kind
+        (linear_source: the pool takes linear-source requests, solved as
+        CPULSSolver).  shape = (lanes, pairs, exp_kind) fixes the sweep
+        shape; None autotunes it on the pool's first batch."""
         lanes, pairs, kind = shape if shape else (0, 0, 0)
         cfg = PoolConfig(num_groups, num_polar_half, max_solves, max_materials,
                          max_angles, max_fsrs, max_tracks, max_segments,
-                         lanes, pairs, kind)
+                         lanes, pairs, kind, 1 if linear_source else 0)
         idx = C.c_int()
         _native.check(_lib().moc_server_add_pool(self._h, C.byref(cfg), C.byref(idx)))
         return idx.value
@@ -183,13 +189,21 @@ class Server:
     # ---- requests ---------------------------------------------------------
     def submit(self, p: Problem, kind: str = "eigenvalue", max_iters: int = 1000,
                res_type: int = 1, k_eff: float = 1.0, threshold: float = 1e-5,
-               fixed_source: Optional[np.ndarray] = None) -> int:
+               fixed_source: Optional[np.ndarray] = None,
+               linear_source=False,
+               fixed_source_moments: Optional[np.ndarray] = None,
+               allow_negative_fluxes: bool = False) -> int:
         """Queues a solve of `p`; returns its ticket.  kind "eigenvalue" is
         Solver.computeEigenvalue(max_iters, res_type); "source" is
         Solver.computeSource(max_iters, k_eff, res_type) with fixed_source
         (default: p.fixed_sources) as [R][G] source; "flux" is
         Solver.computeFlux(max_iters, True): that fixed source alone,
-        SCALAR_FLUX residual."""
+        SCALAR_FLUX residual.  linear_source (True: p.linear_source, or a
+        dict of the same arrays) solves it as CPULSSolver in the linear-
+        source pool of its group and polar count, with fixed_source_moments
+        [R][3][G] (CPULSSolver.setFixedSourceMomentByFSR); the result then
+        carries the flux moments [R][3][G].  allow_negative_fluxes is
+        Solver.allowNegativeFluxes(True)."""
         arrs = dict(
             seg_len=np.ascontiguousarray(p.seg_len, np.float32),
             seg_fsr=np.ascontiguousarray(p.seg_fsr, np.int32),
@@ -211,6 +225,33 @@ class Server:
             arrs["fixed_source"] = np.ascontiguousarray(fs, np.float32).reshape(
                 p.num_fsrs, p.num_groups)
         flux = np.zeros((p.num_fsrs, p.num_groups), np.float32)
+        ls = p.linear_source if linear_source is True else (linear_source or None)
+        if linear_source is True and ls is None:
+            raise _native.MOCError(-1, "the problem has no linear-source geometry")
+        moments = geom = None
+        if ls is not None:
+            for k, dt in (("seg_x", np.float32), ("seg_y", np.float32),
+                          ("ang_dir", np.float64), ("ang_wgt", np.float64),
+                          ("pol_sin", np.float64), ("pol_wgt", np.float64)):
+                if k not in ls:
+                    raise _native.MOCError(-1, f"linear-source geometry lacks {k}")
+                arrs["ls_" + k] = np.ascontiguousarray(ls[k], dt).ravel()
+            for k, n in (("seg_x", p.num_segments), ("seg_y", p.num_segments),
+                         ("ang_dir", 2 * p.num_angles), ("ang_wgt", p.num_angles),
+                         ("pol_sin", p.num_angles * p.num_polar_half),
+                         ("pol_wgt", p.num_angles * p.num_polar_half)):
+                if arrs["ls_" + k].size != n:
+                    raise _native.MOCError(
+                        -1, f"{k} has {arrs['ls_' + k].size} values, expected {n}")
+            geom = _native.LSGeometry(*(arrs["ls_" + k].ctypes.data for k in (
+                "seg_x", "seg_y", "ang_dir", "ang_wgt", "pol_sin", "pol_wgt")))
+            moments = np.zeros((p.num_fsrs, 3, p.num_groups), np.float32)
+            if fixed_source_moments is not None:
+                arrs["fixed_source_moments"] = np.ascontiguousarray(
+                    fixed_source_moments, np.float32).reshape(
+                        p.num_fsrs, 3, p.num_groups)
+        elif fixed_source_moments is not None:
+            raise _native.MOCError(-1, "fixed source moments need a linear source")
         req = Request()
         req.num_groups = p.num_groups
         req.num_polar_half = p.num_polar_half
@@ -220,16 +261,21 @@ class Server:
         req.num_tracks = p.num_tracks
         req.num_segments = p.num_segments
         for k, a in arrs.items():
-            setattr(req, k, a.ctypes.data)
+            if not k.startswith("ls_"):
+                setattr(req, k, a.ctypes.data)
         req.kind = _KINDS[kind]
         req.max_iters = max_iters
         req.res_type = res_type
         req.k_eff = k_eff
         req.threshold = threshold
         req.flux_out = flux.ctypes.data
+        req.allow_negative_fluxes = 1 if allow_negative_fluxes else 0
+        if geom is not None:
+            req.linear_source = C.pointer(geom)
+            req.moments_out = moments.ctypes.data
         t = C.c_int64()
         _native.check(_lib().moc_server_submit(self._h, C.byref(req), C.byref(t)))
-        self._keep[t.value] = (req, arrs, flux)
+        self._keep[t.value] = (req, arrs, geom, flux, moments)
         return t.value
 
     def step(self) -> int:
@@ -254,14 +300,17 @@ class Server:
         r = Result()
         _native.check(_lib().moc_server_wait(
             self._h, ticket, -1.0 if timeout is None else float(timeout), C.byref(r)))
-        _, _, flux = self._keep.pop(ticket)
+        _, _, _, flux, moments = self._keep.pop(ticket)
         if r.status != 0:
             why = self.loop_error()
             raise _native.MOCError(r.status, f"request {ticket} failed"
                                    + (f": {why}" if why else ""))
-        return dict(keff=r.keff, iterations=r.iterations, converged=bool(r.converged),
-                    residual=r.residual, pool=r.pool, flux=flux,
-                    t_submit=r.t_submit, t_admit=r.t_admit, t_done=r.t_done)
+        out = dict(keff=r.keff, iterations=r.iterations, converged=bool(r.converged),
+                   residual=r.residual, pool=r.pool, flux=flux,
+                   t_submit=r.t_submit, t_admit=r.t_admit, t_done=r.t_done)
+        if moments is not None:
+            out["moments"] = moments
+        return out
 
     def poll(self) -> List[int]:
         buf = (C.c_int64 * 1024)()

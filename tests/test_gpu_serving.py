@@ -282,7 +282,7 @@ def test_bad_request_is_refused_on_submit():
     srv = make_server([p], 1)
     with pytest.raises(MOCError, match="threshold"):
         srv.submit(p, "eigenvalue", threshold=-1.0)
-    with pytest.raises(MOCError, match="no pool"):
+    with pytest.raises(MOCError, match="no flat-source pool"):
         srv.submit(lattice.pin_cell(2, 16, 0.1))     # no pool for 2 groups
     big = lattice.square_lattice(3, 7, 16, 0.1, config=0)
     with pytest.raises(MOCError, match="capacity"):
