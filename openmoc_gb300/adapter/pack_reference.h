@@ -78,17 +78,22 @@ struct PackedProblem {
   /* Dense index of every Material, keyed by the Material pointer. */
   std::map<Material*, int> material_index;
 
-  /* Linear-source geometry (pack_linear_source; 2D only):
+  /* Linear-source geometry (pack_linear_source):
    *   seg_x[S], seg_y[S]  float   segment::_starting_position relative to
    *                               the FSR centroid (RecenterSegments,
    *                               src/TrackTraversingAlgorithms.cpp:1320-1331)
    *   ang_dir[A][2]       double  cos(phi), sin(phi) of the tracks of each
-   *                               azimuthal index (Track::getPhi)
+   *                               angle row (Track::getPhi)
    *   ang_wgt[A]          double  Quadrature::getAzimSpacing * getAzimWeight
    *   pol_sin[A][Ph], pol_wgt[A][Ph]  double  getSinTheta, getPolarWeight
-   *   centroid[R][2]      double  Geometry::getFSRCentroid (for reporting) */
-  std::vector<float> seg_x, seg_y;
-  std::vector<double> ang_dir, ang_wgt, pol_sin, pol_wgt, centroid;
+   *   centroid[R][2]      double  Geometry::getFSRCentroid (for reporting)
+   * and for explicit 3D tracks (angle rows a * num_polar + p, Ph = 1):
+   *   seg_z[S]            float   the z of the start, relative likewise
+   *   pol_sin[A], pol_cos[A]  double  sin, cos of Track3D::getTheta
+   *   pol_wgt[A]          double  getPolarSpacing * getPolarWeight
+   *   centroid[R][3]      double */
+  std::vector<float> seg_x, seg_y, seg_z;
+  std::vector<double> ang_dir, ang_wgt, pol_sin, pol_wgt, pol_cos, centroid;
 };
 
 inline bool transfers_flux(boundaryType bc) {
@@ -219,9 +224,13 @@ inline void pack_tracks(TrackGenerator* tg, PackedProblem& out) {
  * centroids (TrackGenerator::generateFSRCentroids, which
  * Solver::initializeFSRs runs, src/Solver.cpp:865).  2D tracks only.
  */
+inline void pack_linear_source_3d(TrackGenerator* tg, PackedProblem& out);
+
 inline void pack_linear_source(TrackGenerator* tg, PackedProblem& out) {
-  if (out.solve_3d)
-    throw std::runtime_error("linear-source packing takes 2D tracks only");
+  if (out.solve_3d) {
+    pack_linear_source_3d(tg, out);
+    return;
+  }
   Geometry* geo = tg->getGeometry();
   if (!geo->containsFSRCentroids())
     throw std::runtime_error("FSR centroids have not been generated");
@@ -267,6 +276,73 @@ inline void pack_linear_source(TrackGenerator* tg, PackedProblem& out) {
     Point* c = geo->getFSRCentroid(r);
     out.centroid[2 * r] = c->getX();
     out.centroid[2 * r + 1] = c->getY();
+  }
+}
+
+/** The explicit 3D tracks' linear-source geometry, in UID order as
+ *  pack_tracks leaves them (the 3D branches of
+ *  LinearExpansionGenerator::onTrack and TransportSweep::onTrack,
+ *  src/TrackTraversingAlgorithms.cpp:680-700, :913-926). */
+inline void pack_linear_source_3d(TrackGenerator* tg, PackedProblem& out) {
+  TrackGenerator3D* tg3 = dynamic_cast<TrackGenerator3D*>(tg);
+  Geometry* geo = tg->getGeometry();
+  if (!tg3 || !geo->containsFSRCentroids())
+    throw std::runtime_error("3D tracks with FSR centroids are needed");
+  Quadrature* quad = tg->getQuadrature();
+  const int num_polar = quad->getNumPolarAngles();
+  const int A = out.num_angles;
+  const long T = out.num_tracks, R = geo->getNumFSRs();
+  out.seg_x.resize(out.num_segments);
+  out.seg_y.resize(out.num_segments);
+  out.seg_z.resize(out.num_segments);
+  out.ang_dir.assign(2 * (size_t) A, 0.0);
+  out.ang_wgt.assign(A, 0.0);
+  out.pol_sin.assign(A, 0.0);
+  out.pol_cos.assign(A, 0.0);
+  out.pol_wgt.assign(A, 0.0);
+  std::vector<char> seen(A, 0);
+  Track3D**** t3d = tg3->get3DTracks();
+  int*** per_stack = tg3->getTracksPerStack();
+  Track** tracks_2d = tg->get2DTracksArray();
+  for (long i2 = 0; i2 < tg->getNum2DTracks(); i2++) {
+    const int a = tracks_2d[i2]->getAzimIndex();
+    const int xy = tracks_2d[i2]->getXYIndex();
+    for (int p = 0; p < num_polar; p++)
+      for (int z = 0; z < per_stack[a][xy][p]; z++) {
+        Track3D* t = &t3d[a][xy][p][z];
+        const long uid = t->getUid();
+        if (uid < 0 || uid >= T)
+          throw std::runtime_error("3D track UID out of range");
+        segment* segs = t->getSegments();
+        const long base = out.seg_off[uid];
+        for (int k = 0; k < t->getNumSegments(); k++) {
+          out.seg_x[base + k] = (float) segs[k]._starting_position[0];
+          out.seg_y[base + k] = (float) segs[k]._starting_position[1];
+          out.seg_z[base + k] = (float) segs[k]._starting_position[2];
+        }
+        const int row = out.track_ang[uid];
+        const double phi = t->getPhi(), theta = t->getTheta();
+        if (!seen[row]) {
+          seen[row] = 1;
+          out.ang_dir[2 * row] = std::cos(phi);
+          out.ang_dir[2 * row + 1] = std::sin(phi);
+          out.pol_sin[row] = std::sin(theta);
+          out.pol_cos[row] = std::cos(theta);
+          out.ang_wgt[row] = quad->getAzimSpacing(a) * quad->getAzimWeight(a);
+          out.pol_wgt[row] = quad->getPolarSpacing(a, p) *
+                             quad->getPolarWeight(a, p);
+        } else if (out.ang_dir[2 * row] != std::cos(phi) ||
+                   out.pol_cos[row] != std::cos(theta)) {
+          throw std::runtime_error("tracks of one angle row differ in angle");
+        }
+      }
+  }
+  out.centroid.resize(3 * (size_t) R);
+  for (long r = 0; r < R; r++) {
+    Point* c = geo->getFSRCentroid(r);
+    out.centroid[3 * r] = c->getX();
+    out.centroid[3 * r + 1] = c->getY();
+    out.centroid[3 * r + 2] = c->getZ();
   }
 }
 

@@ -56,9 +56,11 @@ _ARRAY_DTYPES = {
 }
 
 LS_KEYS = ("seg_x", "seg_y", "ang_dir", "ang_wgt", "pol_sin", "pol_wgt")
+# the explicit 3D tracks' extra linear-source arrays
+LS_KEYS_3D = ("seg_z", "pol_cos")
 LS_DTYPES = {"seg_x": np.float32, "seg_y": np.float32, "ang_dir": np.float64,
              "ang_wgt": np.float64, "pol_sin": np.float64, "pol_wgt": np.float64,
-             "centroid": np.float64}
+             "centroid": np.float64, "seg_z": np.float32, "pol_cos": np.float64}
 
 FLAG_NEXT_FWD_IS_FWD = 1
 FLAG_NEXT_BWD_IS_FWD = 2
@@ -92,10 +94,13 @@ class Problem:
     fsr_vol: np.ndarray
     fixed_sources: Optional[np.ndarray] = None
     meta: Dict[str, float] = field(default_factory=dict)
-    # Linear-source geometry (2D; CPULSSolver): seg_x, seg_y [S] float32
+    # Linear-source geometry (CPULSSolver): seg_x, seg_y [S] float32
     # start of each segment relative to its FSR centroid; ang_dir [A][2]
     # cos/sin phi, ang_wgt [A] azimuthal spacing x weight, pol_sin and
-    # pol_wgt [A][Ph] (float64); optionally centroid [R][2] (float64).
+    # pol_wgt [A][Ph] (float64); optionally centroid [R][2] (float64).  For
+    # explicit 3D tracks also seg_z [S] and pol_cos [A] (cos theta of each
+    # angle row), pol_wgt being polar spacing x polar weight, centroid
+    # [R][3].
     linear_source: Optional[Dict[str, np.ndarray]] = None
     # On-the-fly description of extruded 3D tracks (moc_otf_tracks arrays:
     # trk, trk_f, ang, rad_len, rad_fsr, rad_off, rad_start, rad_total,
@@ -263,7 +268,8 @@ def load_packed(base: str) -> Tuple[Problem, Dict[str, float], Dict[str, np.ndar
         if key in arrays:
             p.fixed_sources = arrays[key]
     if "ls_seg_x" in arrays:
-        p.linear_source = {k: arrays["ls_" + k] for k in LS_KEYS + ("centroid",)
+        p.linear_source = {k: arrays["ls_" + k]
+                           for k in LS_KEYS + LS_KEYS_3D + ("centroid",)
                            if "ls_" + k in arrays}
     if "cm_end_face" in arrays:
         p.cmfd_geometry = {k[3:]: v for k, v in arrays.items() if k.startswith("cm_")}

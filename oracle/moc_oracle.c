@@ -698,11 +698,13 @@ int oracle_compute_flux(const oracle_problem* p, oracle_state* s,
 int oracle_real_size(void) { return (int) sizeof(real); }
 
 /* ================================================================ linear
- * source.  CPULSSolver (src/CPULSSolver.cpp) restated for 2D tracks: the
- * same source iteration with flux and source moments along x and y about
- * each FSR centroid.  Layouts follow the reference: moments [R][3][G] (x, y,
- * z; z stays 0 in 2D), src/CPULSSolver.h:20-23; the linear expansion matrix
- * inverse [R][3] (xx, yy, xy) and the source constants [R][3][G].
+ * source.  CPULSSolver (src/CPULSSolver.cpp) restated for 2D and explicit 3D
+ * tracks: the same source iteration with flux and source moments along x
+ * and y (and z in 3D) about each FSR centroid.  Layouts follow the
+ * reference: moments [R][3][G] (x, y, z; z stays 0 in 2D),
+ * src/CPULSSolver.h:20-23; the linear expansion matrix inverse [R][NC] and
+ * the source constants [R][NC][G], NC = 3 in 2D (xx, yy, xy) and 6 in 3D
+ * (xx, yy, xy, xz, yz, zz), src/TrackTraversingAlgorithms.cpp:470-490.
  *
  * The exponential terms are evaluated in double from their definitions
  * (series below x = 1, closed forms above), where the reference uses
@@ -715,15 +717,18 @@ typedef struct {
   const double* ang_dir;  /* [A][2] cos(phi), sin(phi) */
   const double* ang_wgt;  /* [A] azimuthal spacing x azimuthal weight */
   const double* pol_sin;  /* [A][Ph] sin(theta_p) */
-  const double* pol_wgt;  /* [A][Ph] polar weight */
+  const double* pol_wgt;  /* [A][Ph] polar weight; 3D: polar spacing x
+                             polar weight */
+  const float* seg_z;     /* 3D: [S] z of the start; NULL in 2D */
+  const double* pol_cos;  /* 3D: [A] cos(theta) of each angle row */
 } oracle_ls_geometry;
 
 typedef struct {
-  double* ilem;           /* [R][3] */
-  real* src_const;        /* [R][3][G] */
+  double* ilem;           /* [R][NC] */
+  real* src_const;        /* [R][NC][G] */
   real* mom;              /* [R][3][G] flux moments */
   real* red_xyz;          /* [R][3][G] reduced source moments */
-  const real* fixed_xy;   /* [R][2][G] fixed source moments, or NULL */
+  const real* fixed_xy;   /* [R][2][G] fixed source moments, or NULL (2D) */
   int32_t negative_allowed;
   int32_t num_flat;       /* FSRs whose expansion matrix is singular */
 } oracle_ls_state;
@@ -766,8 +771,12 @@ static double exp_g2(double x) {
  * (src/TrackTraversingAlgorithms.cpp:543-640, :716-826): the volume
  * moments of every FSR, their 2x2 inverse, and the source constants.
  * Returns the number of FSRs left with a flat source (singular matrix). */
+static int ls_constants_3d(const oracle_problem* p, const oracle_ls_geometry* g,
+                           oracle_ls_state* s);
+
 int oracle_ls_constants(const oracle_problem* p, const oracle_ls_geometry* g,
                         oracle_ls_state* s) {
+  if (p->solve_3d) return ls_constants_3d(p, g, s);
   const long R = p->num_fsrs;
   const int G = p->num_groups, Ph = p->num_polar_half;
   double* lem = (double*) calloc((size_t) R * 3, sizeof(double));
@@ -824,6 +833,79 @@ int oracle_ls_constants(const oracle_problem* p, const oracle_ls_geometry* g,
   return flat;
 }
 
+/* The 3D branch of LinearExpansionGenerator::onTrack and execute
+ * (src/TrackTraversingAlgorithms.cpp:543-640, :716-781): direction
+ * (cos phi sin theta, sin phi sin theta, cos theta), the row weight
+ * w_a d_a w_p d_p, G2 at the segment's optical length, six moments and
+ * their 3x3 inverse; flat where the determinant is below 1e-10 or the
+ * volume below 1e-6. */
+static int ls_constants_3d(const oracle_problem* p, const oracle_ls_geometry* g,
+                           oracle_ls_state* s) {
+  const long R = p->num_fsrs;
+  const int G = p->num_groups;
+  double* lem = (double*) calloc((size_t) R * 6, sizeof(double));
+  double* sc = (double*) calloc((size_t) R * 6 * G, sizeof(double));
+  for (long t = 0; t < p->num_tracks; t++) {
+    const int a = p->track_ang[t];
+    const double cph = g->ang_dir[2 * a], sph = g->ang_dir[2 * a + 1];
+    const double sth = g->pol_sin[a], cth = g->pol_cos[a];
+    double wgt = g->ang_wgt[a];
+    wgt *= g->pol_wgt[a];
+    for (long k = p->seg_off[t]; k < p->seg_off[t + 1]; k++) {
+      const long r = p->seg_fsr[k];
+      const float* st = p->sigma_t + (long) p->fsr_mat[r] * G;
+      const double len = p->seg_len[k], vol = p->fsr_vol[r];
+      const double xc = (double) g->seg_x[k] + len * 0.5 * cph * sth;
+      const double yc = (double) g->seg_y[k] + len * 0.5 * sph * sth;
+      const double zc = (double) g->seg_z[k] + len * 0.5 * cth;
+      const double vol_impact = wgt * len / vol;
+      const double src_constant = vol_impact * len / 2.0;
+      for (int e = 0; e < G; e++) {
+        const double tau = len * (double) st[e];
+        const double g2 = exp_g2(tau) * len * src_constant;
+        double* c = sc + r * 6 * G + e;
+        c[0] += vol_impact * xc * xc + cph * cph * g2 * sth * sth;
+        c[G] += vol_impact * yc * yc + sph * sph * g2 * sth * sth;
+        c[2 * G] += vol_impact * xc * yc + sph * cph * g2 * sth * sth;
+        c[3 * G] += vol_impact * xc * zc + cph * cth * g2 * sth;
+        c[4 * G] += vol_impact * yc * zc + sph * cth * g2 * sth;
+        c[5 * G] += vol_impact * zc * zc + cth * cth * g2;
+      }
+      const double w = wgt * len / vol, l2 = len * len;
+      lem[r * 6 + 0] += w * (xc * xc + cph * sth * len * cph * sth * len / 12.0);
+      lem[r * 6 + 1] += w * (yc * yc + sph * sth * len * sph * sth * len / 12.0);
+      lem[r * 6 + 2] += w * (xc * yc + sph * cph * sth * len * sth * len / 12.0);
+      lem[r * 6 + 3] += w * (xc * zc + cph * cth * sth * l2 / 12.0);
+      lem[r * 6 + 4] += w * (yc * zc + sph * cth * sth * l2 / 12.0);
+      lem[r * 6 + 5] += w * (zc * zc + cth * len * cth * len / 12.0);
+    }
+  }
+  int flat = 0;
+  for (long r = 0; r < R; r++) {
+    const double* m = lem + r * 6;
+    double* il = s->ilem + r * 6;
+    const double det = m[0] * m[1] * m[5] + m[2] * m[4] * m[3] +
+                       m[3] * m[2] * m[4] - m[0] * m[4] * m[4] -
+                       m[3] * m[1] * m[3] - m[2] * m[2] * m[5];
+    if (fabs(det) < MIN_DET || p->fsr_vol[r] < 1e-6) {
+      for (int i = 0; i < 6; i++) il[i] = 0.0;
+      flat++;
+    } else {
+      il[0] = (m[1] * m[5] - m[4] * m[4]) / det;
+      il[1] = (m[0] * m[5] - m[3] * m[3]) / det;
+      il[2] = (m[3] * m[4] - m[2] * m[5]) / det;
+      il[3] = (m[2] * m[4] - m[3] * m[1]) / det;
+      il[4] = (m[3] * m[2] - m[0] * m[4]) / det;
+      il[5] = (m[0] * m[1] - m[2] * m[2]) / det;
+    }
+  }
+  for (long i = 0; i < R * 6 * G; i++) s->src_const[i] = (real) sc[i];
+  free(lem);
+  free(sc);
+  s->num_flat = flat;
+  return flat;
+}
+
 /* CPULSSolver::flattenFSRFluxes, src/CPULSSolver.cpp:343-353 */
 void oracle_ls_flatten(const oracle_problem* p, oracle_state* s,
                        oracle_ls_state* ls, double value) {
@@ -843,9 +925,57 @@ double oracle_ls_normalize(const oracle_problem* p, oracle_state* s,
 /* CPULSSolver::computeFSRSources (2D branch), src/CPULSSolver.cpp:386-527:
  * the flat source of CPUSolver, then the x and y source moments through the
  * inverse expansion matrix.  Returns the negative flat sources found. */
+/* The 3D branch: the x, y and z source moments through the 3x3 inverse
+ * (src/CPULSSolver.cpp:466-487). */
+static void ls_sources_3d(const oracle_problem* p, oracle_state* s,
+                          oracle_ls_state* ls, int iteration) {
+  const long R = p->num_fsrs;
+  const int G = p->num_groups;
+  set_threads(p);
+#pragma omp parallel for schedule(static)
+  for (long r = 0; r < R; r++) {
+    real buf[1024];
+    const int m = p->fsr_mat[r];
+    const float* ss = p->sigma_s + (long) m * G * G;
+    const float* nf = p->nu_sigma_f + (long) m * G;
+    const float* ch = p->chi + (long) m * G;
+    const int fissile = mat_fissile(p, m);
+    const double* il = ls->ilem + r * 6;
+    for (int gd = 0; gd < G; gd++) {
+      real src[3];
+      for (int i = 0; i < 3; i++) {
+        const real* mi = ls->mom + (r * 3 + i) * G;
+        double fis = 0.0;
+        if (fissile) {
+          for (int g = 0; g < G; g++) buf[g] = ((real) ch[gd] * (real) nf[g]) * mi[g];
+          fis = pairwise_sum_r(buf, G) / s->keff;
+        }
+        for (int g = 0; g < G; g++) buf[g] = (real) ss[gd * G + g] * mi[g];
+        src[i] = (real) (pairwise_sum_r(buf, G) + fis);
+      }
+      real* q = ls->red_xyz + r * 3 * G + gd;
+      if (ls->negative_allowed || s->reduced[r * G + gd] > 10 * FLUX_EPSILON ||
+          iteration > 29) {
+        q[0] = (real) (ONE_OVER_FOUR_PI / 2 *
+                       (il[0] * src[0] + il[2] * src[1] + il[3] * src[2]));
+        q[G] = (real) (ONE_OVER_FOUR_PI / 2 *
+                       (il[2] * src[0] + il[1] * src[1] + il[4] * src[2]));
+        q[2 * G] = (real) (ONE_OVER_FOUR_PI / 2 *
+                           (il[3] * src[0] + il[4] * src[1] + il[5] * src[2]));
+      } else {
+        q[0] = q[G] = q[2 * G] = 0;
+      }
+    }
+  }
+}
+
 long oracle_ls_compute_sources(const oracle_problem* p, oracle_state* s,
                                oracle_ls_state* ls, int iteration) {
   long neg = oracle_compute_sources(p, s, iteration, ls->negative_allowed);
+  if (p->solve_3d) {
+    ls_sources_3d(p, s, ls, iteration);
+    return neg;
+  }
   const long R = p->num_fsrs;
   const int G = p->num_groups;
   set_threads(p);
@@ -957,12 +1087,138 @@ static void ls_flush(const oracle_problem* p, oracle_state* s,
   memset(by, 0, sizeof(real) * G);
 }
 
-/* CPUSolver::transportSweep with the linear-source tally (2D): as
- * oracle_sweep, the direction of a track from its azimuthal angle
- * (src/TrackTraversingAlgorithms.cpp:913-926), reversed for the backward
- * pass, which starts each segment at its far end. */
+/* The 3D branch of tallyLSScalarFlux (src/CPULSSolver.cpp:555-646): the
+ * segment's own optical length, no polar loop; the quadrature weight is
+ * applied when the buffers are flushed. */
+static void ls_tally_segment_3d(const oracle_problem* p, const oracle_state* s,
+                                const oracle_ls_state* ls, long fsr,
+                                real length, int mat, const real pos[3],
+                                const real dir[3], real* buf, real* bx,
+                                real* by, real* bz, float* psi) {
+  const int G = p->num_groups;
+  const float* st = p->sigma_t + (long) mat * G;
+  real c2[3];
+  for (int i = 0; i < 3; i++) c2[i] = 2 * pos[i] + length * dir[i];
+  const real* q = ls->red_xyz + fsr * 3 * G;
+  for (int g = 0; g < G; g++) {
+    real src_flat = s->reduced[fsr * G + g];
+    for (int i = 0; i < 3; i++) src_flat += q[i * G + g] * c2[i];
+    real src_lin = q[g] * dir[0];
+    src_lin += q[G + g] * dir[1];
+    src_lin += q[2 * G + g] * dir[2];
+    const real tau = length * (real) st[g];
+    const double gg = exp_g(tau > 1e-8 ? (double) tau : 1e-8);
+    const real G_ = (real) gg;
+    const real F1 = 1 - tau * G_;
+    const real F2 = 2 * G_ - F1;
+    real H = F1 - G_;
+    H *= length * (real) psi[g] * tau;
+    const real delta = (tau * (real) psi[g] - length * src_flat) * F1 -
+                       src_lin * length * length * F2;
+    psi[g] = (float) ((real) psi[g] - delta);
+    buf[g] += delta;
+    bx[g] += H * dir[0] + delta * pos[0];
+    by[g] += H * dir[1] + delta * pos[1];
+    bz[g] += H * dir[2] + delta * pos[2];
+  }
+}
+
+/* CPULSSolver::accumulateLinearFluxContribution with the 3D weight. */
+static void ls_flush_3d(const oracle_problem* p, oracle_state* s,
+                        oracle_ls_state* ls, long fsr, real weight, real* buf,
+                        void* locks) {
+  const int G = p->num_groups;
+#ifdef _OPENMP
+  omp_set_lock(&((omp_lock_t*) locks)[fsr]);
+#else
+  (void) locks;
+#endif
+  for (int g = 0; g < G; g++) {
+    s->phi[fsr * G + g] += weight * buf[g];
+    for (int i = 0; i < 3; i++)
+      ls->mom[(fsr * 3 + i) * G + g] += weight * buf[(i + 1) * G + g];
+  }
+#ifdef _OPENMP
+  omp_unset_lock(&((omp_lock_t*) locks)[fsr]);
+#endif
+  memset(buf, 0, sizeof(real) * 4 * G);
+}
+
+static void ls_sweep_3d(const oracle_problem* p, const oracle_ls_geometry* geo,
+                        oracle_state* s, oracle_ls_state* ls) {
+  const long R = p->num_fsrs;
+  const int G = p->num_groups;
+  const long T = p->num_tracks;
+  const int F = fluxes_per_track(p);
+  memset(s->phi, 0, sizeof(real) * R * G);
+  memset(ls->mom, 0, sizeof(real) * R * 3 * G);
+  memcpy(s->boundary, s->start, sizeof(float) * 2 * T * F);
+  set_threads(p);
+  void* locks = NULL;
+#ifdef _OPENMP
+  omp_lock_t* lk = (omp_lock_t*) malloc(sizeof(omp_lock_t) * R);
+  for (long r = 0; r < R; r++) omp_init_lock(&lk[r]);
+  locks = lk;
+#endif
+#pragma omp parallel
+  {
+    real* buf = (real*) calloc(4 * (size_t) G, sizeof(real));
+#pragma omp for schedule(dynamic)
+    for (long t = 0; t < T; t++) {
+      const long b = p->seg_off[t];
+      const int n = (int) (p->seg_off[t + 1] - b);
+      const int ang = p->track_ang[t];
+      const real weight = (real) p->weights[ang];
+      /* TransportSweep::onTrack, src/TrackTraversingAlgorithms.cpp:913-926 */
+      const double sth = geo->pol_sin[ang], cth = geo->pol_cos[ang];
+      real dir[3] = {(real) (geo->ang_dir[2 * ang] * sth),
+                     (real) (geo->ang_dir[2 * ang + 1] * sth), (real) cth};
+      float* psi = s->boundary + (t * 2) * (long) F;
+      for (int k = 0; k < n; k++) {
+        const long fsr = p->seg_fsr[b + k];
+        const real pos[3] = {(real) geo->seg_x[b + k], (real) geo->seg_y[b + k],
+                             (real) geo->seg_z[b + k]};
+        ls_tally_segment_3d(p, s, ls, fsr, (real) p->seg_len[b + k],
+                            p->fsr_mat[fsr], pos, dir, buf, buf + G,
+                            buf + 2 * G, buf + 3 * G, psi);
+        if (k < n - 1 && fsr != p->seg_fsr[b + k + 1])
+          ls_flush_3d(p, s, ls, fsr, weight, buf, locks);
+      }
+      transfer(p, s, t, 1, psi);
+      const real fdir[3] = {dir[0], dir[1], dir[2]};
+      for (int i = 0; i < 3; i++) dir[i] = -dir[i];
+      psi = s->boundary + (t * 2 + 1) * (long) F;
+      for (int k = n - 1; k >= 0; k--) {
+        const long fsr = p->seg_fsr[b + k];
+        const real len = (real) p->seg_len[b + k];
+        const real pos[3] = {(real) geo->seg_x[b + k] + fdir[0] * len,
+                             (real) geo->seg_y[b + k] + fdir[1] * len,
+                             (real) geo->seg_z[b + k] + fdir[2] * len};
+        ls_tally_segment_3d(p, s, ls, fsr, len, p->fsr_mat[fsr], pos, dir,
+                            buf, buf + G, buf + 2 * G, buf + 3 * G, psi);
+        if (k == 0 || fsr != p->seg_fsr[b + k - 1])
+          ls_flush_3d(p, s, ls, fsr, weight, buf, locks);
+      }
+      transfer(p, s, t, 0, psi);
+    }
+    free(buf);
+  }
+#ifdef _OPENMP
+  for (long r = 0; r < R; r++) omp_destroy_lock(&lk[r]);
+  free(lk);
+#endif
+}
+
+/* CPUSolver::transportSweep with the linear-source tally: as oracle_sweep,
+ * the direction of a track from its angles (src/TrackTraversingAlgorithms.
+ * cpp:913-926), reversed for the backward pass, which starts each segment
+ * at its far end. */
 void oracle_ls_sweep(const oracle_problem* p, const oracle_ls_geometry* geo,
                      oracle_state* s, oracle_ls_state* ls) {
+  if (p->solve_3d) {
+    ls_sweep_3d(p, geo, s, ls);
+    return;
+  }
   const long R = p->num_fsrs;
   const int G = p->num_groups;
   const long T = p->num_tracks;
@@ -1023,8 +1279,65 @@ void oracle_ls_sweep(const oracle_problem* p, const oracle_ls_geometry* geo,
 }
 
 /* CPULSSolver::addSourceToScalarFlux (2D), src/CPULSSolver.cpp:787-882 */
+/* The 3D branch: six source constants per group (src/CPULSSolver.cpp:
+ * 824-846). */
+static long ls_add_source_3d(const oracle_problem* p, oracle_state* s,
+                             oracle_ls_state* ls) {
+  const long R = p->num_fsrs;
+  const int G = p->num_groups;
+  long neg = 0;
+  set_threads(p);
+#pragma omp parallel for schedule(static) reduction(+:neg)
+  for (long r = 0; r < R; r++) {
+    real vol = (real) p->fsr_vol[r];
+    if (vol < (real) ZERO_VOLUME) vol = (real) 1e30;
+    const float* st = p->sigma_t + (long) p->fsr_mat[r] * G;
+    const real* c = ls->src_const + r * 6 * G;
+    for (int e = 0; e < G; e++) {
+      const real fc = (real) (FOUR_PI * 2);
+      const real qx = ls->red_xyz[(r * 3 + 0) * G + e];
+      const real qy = ls->red_xyz[(r * 3 + 1) * G + e];
+      const real qz = ls->red_xyz[(r * 3 + 2) * G + e];
+      real v = s->phi[r * G + e];
+      v /= vol;
+      v += (real) FOUR_PI * s->reduced[r * G + e];
+      v /= (real) st[e];
+      real mx = ls->mom[(r * 3 + 0) * G + e];
+      mx /= vol;
+      mx += fc * qx * c[e];
+      mx += fc * qy * c[2 * G + e];
+      real my = ls->mom[(r * 3 + 1) * G + e];
+      my /= vol;
+      my += fc * qx * c[2 * G + e];
+      my += fc * qy * c[G + e];
+      mx += fc * qz * c[3 * G + e];
+      my += fc * qz * c[4 * G + e];
+      real mz = ls->mom[(r * 3 + 2) * G + e];
+      mz /= vol;
+      mz += fc * qx * c[3 * G + e];
+      mz += fc * qy * c[4 * G + e];
+      mz += fc * qz * c[5 * G + e];
+      mx /= (real) st[e];
+      my /= (real) st[e];
+      mz /= (real) st[e];
+      if (v < (real) 0 && !ls->negative_allowed) {
+        neg++;
+        real old = s->phi_old[r * G + e];
+        v = old > FLUX_EPSILON ? old : FLUX_EPSILON;
+        mx = my = mz = 0;
+      }
+      s->phi[r * G + e] = v;
+      ls->mom[(r * 3 + 0) * G + e] = mx;
+      ls->mom[(r * 3 + 1) * G + e] = my;
+      ls->mom[(r * 3 + 2) * G + e] = mz;
+    }
+  }
+  return neg;
+}
+
 long oracle_ls_add_source(const oracle_problem* p, oracle_state* s,
                           oracle_ls_state* ls) {
+  if (p->solve_3d) return ls_add_source_3d(p, s, ls);
   const long R = p->num_fsrs;
   const int G = p->num_groups;
   long neg = 0;

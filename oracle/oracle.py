@@ -47,7 +47,8 @@ class _State(C.Structure):
 class _LSGeometry(C.Structure):
     _fields_ = [("seg_x", C.c_void_p), ("seg_y", C.c_void_p),
                 ("ang_dir", C.c_void_p), ("ang_wgt", C.c_void_p),
-                ("pol_sin", C.c_void_p), ("pol_wgt", C.c_void_p)]
+                ("pol_sin", C.c_void_p), ("pol_wgt", C.c_void_p),
+                ("seg_z", C.c_void_p), ("pol_cos", C.c_void_p)]
 
 
 class _LSState(C.Structure):
@@ -256,11 +257,13 @@ class Oracle:
 
 
 class LSOracle(Oracle):
-    """The linear-source CPU solver (CPULSSolver, 2D) over one packed problem
-    plus its linear-source geometry: ``ls`` maps seg_x, seg_y, ang_dir,
-    ang_wgt, pol_sin, pol_wgt (the arrays of include/openmoc_gb300.h's
-    moc_ls_geometry) and optionally fixed_xy ([R][2][G] fixed source
-    moments)."""
+    """The linear-source CPU solver (CPULSSolver, 2D or explicit 3D) over one
+    packed problem plus its linear-source geometry: ``ls`` maps seg_x,
+    seg_y, ang_dir, ang_wgt, pol_sin, pol_wgt (the arrays of
+    include/openmoc_gb300.h's moc_ls_geometry), in 3D also seg_z and
+    pol_cos, and optionally fixed_xy ([R][2][G] fixed source moments, 2D).
+    The expansion inverse and source constants have NC = 3 coefficients in
+    2D, 6 in 3D."""
 
     def __init__(self, problem, ls, precision: str = "f32", num_threads: int = 0,
                  negative_fluxes_allowed: bool = False):
@@ -274,12 +277,18 @@ class LSOracle(Oracle):
             "pol_sin": np.ascontiguousarray(ls["pol_sin"], np.float64),
             "pol_wgt": np.ascontiguousarray(ls["pol_wgt"], np.float64),
         }
+        self.nc = 3
+        if getattr(problem, "solve_3d", 0):
+            self.nc = 6
+            self.geo_arrays["seg_z"] = np.ascontiguousarray(ls["seg_z"], np.float32)
+            self.geo_arrays["pol_cos"] = np.ascontiguousarray(ls["pol_cos"], np.float64)
         g = self.geo_arrays
         self._cg = _LSGeometry(_ptr(g["seg_x"]), _ptr(g["seg_y"]), _ptr(g["ang_dir"]),
                                _ptr(g["ang_wgt"]), _ptr(g["pol_sin"]),
-                               _ptr(g["pol_wgt"]))
-        self.ilem = np.zeros(R * 3, np.float64)
-        self.src_const = np.zeros(R * 3 * G, self.real)
+                               _ptr(g["pol_wgt"]), _ptr(g.get("seg_z")),
+                               _ptr(g.get("pol_cos")))
+        self.ilem = np.zeros(R * self.nc, np.float64)
+        self.src_const = np.zeros(R * self.nc * G, self.real)
         self.mom = np.zeros(R * 3 * G, self.real)
         self.red_xyz = np.zeros(R * 3 * G, self.real)
         fx = ls.get("fixed_xy")

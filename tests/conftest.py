@@ -25,6 +25,8 @@ STAB_CASES = ["pin7_stab_y", "pin7_stab_g", "lat3_stab_d"]
 # test_2d_gradient_linear_source and test_fixed_linear_source replicas, an
 # eigenvalue pin cell and a computeSource lattice.
 LS_CASES = ["grad2d_ls", "fixls_c5g7", "pin7_ls", "src3_ls"]
+# CPULSSolver on explicit 3D tracks (x, y and z moments)
+LS_CASES_3D = ["pin3d_ls"]
 LS_PROBE_CASES = ["grad2d_ls", "pin7_ls"]
 # CMFD-accelerated eigenvalue solves (Geometry::setCmfd) and the coarse
 # group structure each case set (None: one coarse group per group).
@@ -49,7 +51,8 @@ def ls_arrays(arr):
     """The linear-source geometry of a fixture (and its fixed source moments,
     if any) under the names of the oracle and of the solver API."""
     d = {k[3:]: arr[k] for k in ("ls_seg_x", "ls_seg_y", "ls_ang_dir",
-                                 "ls_ang_wgt", "ls_pol_sin", "ls_pol_wgt")}
+                                 "ls_ang_wgt", "ls_pol_sin", "ls_pol_wgt",
+                                 "ls_seg_z", "ls_pol_cos") if k in arr}
     if "fixed_source_xy" in arr:
         d["fixed_xy"] = arr["fixed_source_xy"]
     return d

@@ -182,14 +182,17 @@ class ProbeLSSolver : public CPULSSolver {
   std::vector<float> moments() const {
     return ProbeSolver::tof(_scalar_flux_xyz, 3 * nflux());
   }
+  /* expansion coefficients per FSR: 3 in 2D, 6 in 3D */
+  int ncoeffs() const { return _SOLVE_3D ? 6 : 3; }
   std::vector<double> lin_exp() const {
     std::vector<double> v(_FSR_lin_exp_matrix,
-                          _FSR_lin_exp_matrix + 3 * _num_FSRs);
+                          _FSR_lin_exp_matrix + ncoeffs() * _num_FSRs);
     return v;
   }
   std::vector<double> src_constants() const {
-    std::vector<double> v(3 * nflux());
-    for (long i = 0; i < 3 * nflux(); i++) v[i] = _FSR_source_constants[i];
+    std::vector<double> v(ncoeffs() * nflux());
+    for (long i = 0; i < ncoeffs() * nflux(); i++)
+      v[i] = _FSR_source_constants[i];
     return v;
   }
 
@@ -681,6 +684,10 @@ static void run_case(const CaseSpec& c, const std::string& outdir) {
     w.arr("ls_pol_sin", "f8", p.pol_sin.data(), p.pol_sin.size());
     w.arr("ls_pol_wgt", "f8", p.pol_wgt.data(), p.pol_wgt.size());
     w.arr("ls_centroid", "f8", p.centroid.data(), p.centroid.size());
+    if (p.solve_3d) {
+      w.arr("ls_seg_z", "f4", p.seg_z.data(), p.seg_z.size());
+      w.arr("ls_pol_cos", "f8", p.pol_cos.data(), p.pol_cos.size());
+    }
     std::vector<double> ilem = ls->lin_exp();
     w.arr("ls_ilem", "f8", ilem.data(), ilem.size());
     std::vector<double> sc = ls->src_constants();
@@ -846,6 +853,19 @@ int main(int argc, char** argv) {
     cases.push_back({"pin3d_g7", pin3d_geometry(fuel, mod, p3, 1.6, 2.0), 4,
                      0.1, 1000, 1e-5, FISSION_SOURCE, EIGEN, 1.0, false, NULL,
                      0.0, 4, 0.4});
+  }
+
+  /* 8b. the 3D pin of case 8 with the linear source (CPULSSolver on
+   *     explicit 3D segments: x, y and z moments) */
+  {
+    Material* fuel = make_material(39, "fuel7zl",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 5, 7, true));
+    Material* mod = make_material(40, "mod7zl",
+        openmoc_gb300::make_synthetic_xs(0xC0FFEEULL + 1005, 7, false));
+    PinSpec p3 = {0.54, 1.26, 2, 4, 4};
+    cases.push_back({"pin3d_ls", pin3d_geometry(fuel, mod, p3, 1.6, 2.0), 4,
+                     0.1, 1000, 1e-5, FISSION_SOURCE, EIGEN, 1.0, false, NULL,
+                     0.0, 4, 0.4, true, false, NULL});
   }
 
   /* 9. tests/test_2d_gradient_linear_source: the 2-group homogeneous

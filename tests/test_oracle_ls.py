@@ -7,7 +7,8 @@ Pins the restatement before it checks the CUDA path:
     results_true.dat, copied into tests/golden/reference_results_ls.json) are
     reproduced by the fixtures OpenMOC's library wrote, and by the oracle;
   * the linear expansion matrix inverse and source constants of
-    LinearExpansionGenerator;
+    LinearExpansionGenerator, 2D and explicit 3D (pin3d_ls: x, y and z
+    moments, six coefficients);
   * every linear-source fixture: iterations, keff, fluxes and flux moments
     against the FP_PRECISION=float and =double builds;
   * hook by hook from the same converged state (sources and source moments,
@@ -23,7 +24,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, LS_CASES, LS_PROBE_CASES, load_case, ls_arrays
+from conftest import GOLDEN, LS_CASES, LS_CASES_3D, LS_PROBE_CASES, load_case, ls_arrays
 from oracle.oracle import LSOracle
 
 
@@ -87,11 +88,11 @@ def test_ls_oracle_matches_reference_goldens(case, precision):
     assert _rel(o.phi, d["fluxes"]) < (2e-4 if precision == "f32" else 3e-5)
 
 
-@pytest.mark.parametrize("case", LS_CASES)
+@pytest.mark.parametrize("case", LS_CASES + LS_CASES_3D)
 def test_ls_constants_match_openmoc(case):
-    """LinearExpansionGenerator: the 2x2 inverse per FSR and the source
-    constants per FSR and group (G2 by its definition here, by a rational
-    accurate to 1e-6 in the reference)."""
+    """LinearExpansionGenerator: the 2x2 (3x3 in 3D) inverse per FSR and the
+    source constants per FSR and group (G2 by its definition here, by a
+    rational accurate to 1e-6 in the reference)."""
     o, p, _, arr = _oracle(case, "f64")
     flat = o.constants()
     assert flat == 0
@@ -99,7 +100,7 @@ def test_ls_constants_match_openmoc(case):
     assert _peak(o.src_const, arr["ls_src_constants"]) < 1e-5
 
 
-@pytest.mark.parametrize("case", LS_CASES)
+@pytest.mark.parametrize("case", LS_CASES + LS_CASES_3D)
 @pytest.mark.parametrize("precision", ["f32", "f64"])
 def test_ls_oracle_solve_matches_openmoc(case, precision):
     o, p, sc, arr = _oracle(case, precision, threads=2)
@@ -165,3 +166,24 @@ def test_ls_fixture_positions_inside_their_regions():
         assert np.max(np.abs(sx / vol) / size) < 1e-5, case
         assert np.max(np.abs(sy / vol) / size) < 1e-5, case
         assert T == len(p.seg_off) - 1
+
+
+def test_ls_3d_fixture_positions_inside_their_regions():
+    """The 3D fixture's re-centred start positions: every FSR's
+    weight-and-length-weighted segment midpoints average to ~0 in x, y and
+    z, and the angle rows hold unit directions."""
+    for case in LS_CASES_3D:
+        p, _, arr = load_case(case, "f64")
+        d = arr["ls_ang_dir"].reshape(-1, 2)
+        sth, cth = arr["ls_pol_sin"], arr["ls_pol_cos"]
+        assert np.allclose(sth ** 2 + cth ** 2, 1.0)
+        a = np.repeat(p.track_ang, np.diff(p.seg_off))
+        L = p.seg_len.astype(np.float64)
+        w = (arr["ls_ang_wgt"] * arr["ls_pol_wgt"])[a] * L
+        vol = np.bincount(p.seg_fsr, w, p.num_fsrs)
+        size = np.cbrt(vol)
+        for key, u in (("ls_seg_x", d[a, 0] * sth[a]), ("ls_seg_y", d[a, 1] * sth[a]),
+                       ("ls_seg_z", cth[a])):
+            m = arr[key].astype(np.float64) + 0.5 * L * u
+            c = np.bincount(p.seg_fsr, w * m, p.num_fsrs) / vol
+            assert np.max(np.abs(c) / size) < 1e-5, (case, key)
