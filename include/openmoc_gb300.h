@@ -280,12 +280,12 @@ int moc_fission_source_total_noalloc(const float* phi, int64_t ld,
                                      int32_t num_groups, void* stream,
                                      double* total);
 
-/* ---- linear source (CPULSSolver, 2D tracks) ------------------------------
+/* ---- linear source (CPULSSolver, 2D and explicit 3D tracks) --------------
  * Switches the context from OpenMOC's CPUSolver to its CPULSSolver
- * semantics (src/CPULSSolver.cpp): flat plus linear (x, y) source and flux
- * moments per FSR and group.  The arrays are what pack_linear_source
- * (openmoc_gb300/adapter/pack_reference.h) reads from OpenMOC once the
- * segments are re-centred on the FSR centroids. */
+ * semantics (src/CPULSSolver.cpp): flat plus linear (x, y; x, y, z on 3D
+ * tracks) source and flux moments per FSR and group.  The arrays are what
+ * pack_linear_source (openmoc_gb300/adapter/pack_reference.h) reads from
+ * OpenMOC once the segments are re-centred on the FSR centroids. */
 typedef struct {
   const float* seg_x;     /* [S] segment::_starting_position[0] relative to
                              its FSR centroid (src/TrackTraversingAlgorithms.
@@ -296,6 +296,12 @@ typedef struct {
   const double* ang_wgt;  /* [A] Quadrature::getAzimSpacing * getAzimWeight */
   const double* pol_sin;  /* [A][Ph] Quadrature::getSinTheta */
   const double* pol_wgt;  /* [A][Ph] Quadrature::getPolarWeight */
+  /* explicit 3D tracks (NULL for 2D); angle rows a * num_polar + p, Ph = 1,
+   * pol_sin the sin of Track3D::getTheta and pol_wgt
+   * getPolarSpacing * getPolarWeight of each row: */
+  const float* seg_z;     /* [S] the z of the start relative to the FSR
+                             centroid */
+  const double* pol_cos;  /* [A] cos of Track3D::getTheta */
 } moc_ls_geometry;
 
 /** Sets the linear-source geometry (g != NULL) and computes the linear
@@ -317,9 +323,10 @@ int moc_get_flux_moments(moc_ctx* ctx, float* out, int64_t n);
 int moc_set_flux_moments(moc_ctx* ctx, const float* in, int64_t n);
 int moc_get_source_moments(moc_ctx* ctx, float* out, int64_t n);
 int moc_set_fixed_source_moments(moc_ctx* ctx, const float* in, int64_t n);
-/** The inverse expansion matrices [R][3] (xx, yy, xy) and the source
- *  constants [R][3][G] (CPULSSolver::getLinearExpansionCoeffsBuffer,
- *  getSourceConstantsBuffer; either pointer may be NULL). */
+/** The inverse expansion matrices [R][NC] and the source constants
+ *  [R][NC][G] (CPULSSolver::getLinearExpansionCoeffsBuffer,
+ *  getSourceConstantsBuffer; either pointer may be NULL), NC = 3 (xx, yy,
+ *  xy) in 2D and 6 (xx, yy, xy, xz, yz, zz) on 3D tracks. */
 int moc_get_linear_expansion(moc_ctx* ctx, double* ilem, float* src_const);
 /** Solver::allowNegativeFluxes (src/Solver.cpp:623): no clamping of
  *  negative sources or fluxes. */

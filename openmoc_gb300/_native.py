@@ -41,10 +41,12 @@ class Dims(C.Structure):
 
 
 class LSGeometry(C.Structure):
-    """moc_ls_geometry: the linear-source arrays (pointers)."""
+    """moc_ls_geometry: the linear-source arrays (pointers; seg_z and
+    pol_cos for explicit 3D tracks, else null)."""
     _fields_ = [("seg_x", C.c_void_p), ("seg_y", C.c_void_p),
                 ("ang_dir", C.c_void_p), ("ang_wgt", C.c_void_p),
-                ("pol_sin", C.c_void_p), ("pol_wgt", C.c_void_p)]
+                ("pol_sin", C.c_void_p), ("pol_wgt", C.c_void_p),
+                ("seg_z", C.c_void_p), ("pol_cos", C.c_void_p)]
 
 
 class OtfTracks(C.Structure):

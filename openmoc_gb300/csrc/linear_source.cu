@@ -189,6 +189,105 @@ __global__ void ls_constants_kernel(const int4* segs, const int32_t* list,
   }
 }
 
+// The 3D branch (src/TrackTraversingAlgorithms.cpp:680-781): the row's
+// direction (cos phi sin theta, sin phi sin theta, cos theta) and weight
+// w_a d_a w_p d_p, G2 at the segment's own optical length (no polar loop),
+// six moments (xx, yy, xy, xz, yz, zz) and the 3x3 inverse; flat where the
+// determinant is below 1e-10 or the volume below 1e-6.
+template <int S_>
+__global__ void ls_constants3d_kernel(const int4* segs, const float* seg_z,
+                                      const int32_t* list,
+                                      const int64_t* start,
+                                      const int32_t* seg_track,
+                                      const int32_t* track_ang,
+                                      const double* ang_dir,
+                                      const double* ang_wgt,
+                                      const double* pol_sin,
+                                      const double* pol_wgt,
+                                      const double* pol_cos,
+                                      const float* sigma_t,
+                                      const float* fsr_vol,
+                                      const int32_t* fsr_mat, int64_t R, int G,
+                                      int ld, float* ilem, float* cst,
+                                      unsigned int* num_flat) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t) gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = ((int64_t) blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+       r < R; r += warps) {
+    double l[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    double c[6][S_];
+    float st[S_];
+    const int m = fsr_mat[r];
+#pragma unroll
+    for (int j = 0; j < S_; j++) {
+      const int g = lane + 32 * j;
+#pragma unroll
+      for (int i = 0; i < 6; i++) c[i][j] = 0.0;
+      st[j] = (g < G) ? sigma_t[(int64_t) m * G + g] : 0.0f;
+    }
+    const double vol = (double) fsr_vol[r];
+    for (int64_t e = start[r]; e < start[r + 1]; e++) {
+      const int k = list[e];
+      const int4 w = segs[k];
+      const int a = track_ang[seg_track[k]];
+      const double cph = ang_dir[2 * a], sph = ang_dir[2 * a + 1];
+      const double sth = pol_sin[a], cth = pol_cos[a];
+      const double wgt = ang_wgt[a] * pol_wgt[a];
+      const float lenf = __int_as_float(w.x);
+      const double len = (double) lenf;
+      const double xc = (double) __int_as_float(w.z) + len * 0.5 * cph * sth;
+      const double yc = (double) __int_as_float(w.w) + len * 0.5 * sph * sth;
+      const double zc = (double) seg_z[k] + len * 0.5 * cth;
+      const double vi = wgt * len / vol;
+      const double half = vi * len / 2.0;
+      const double l12 = len * len / 12.0;
+      l[0] += vi * (xc * xc + cph * cph * sth * sth * l12);
+      l[1] += vi * (yc * yc + sph * sph * sth * sth * l12);
+      l[2] += vi * (xc * yc + sph * cph * sth * sth * l12);
+      l[3] += vi * (xc * zc + cph * cth * sth * l12);
+      l[4] += vi * (yc * zc + sph * cth * sth * l12);
+      l[5] += vi * (zc * zc + cth * cth * l12);
+#pragma unroll
+      for (int j = 0; j < S_; j++) {
+        const double g2 = (double) ls_exp_g2(lenf * st[j]) * len * half;
+        c[0][j] += vi * xc * xc + cph * cph * g2 * sth * sth;
+        c[1][j] += vi * yc * yc + sph * sph * g2 * sth * sth;
+        c[2][j] += vi * xc * yc + sph * cph * g2 * sth * sth;
+        c[3][j] += vi * xc * zc + cph * cth * g2 * sth;
+        c[4][j] += vi * yc * zc + sph * cth * g2 * sth;
+        c[5][j] += vi * zc * zc + cth * cth * g2;
+      }
+    }
+    if (lane == 0) {
+      const double det = l[0] * l[1] * l[5] + l[2] * l[4] * l[3] +
+                         l[3] * l[2] * l[4] - l[0] * l[4] * l[4] -
+                         l[3] * l[1] * l[3] - l[2] * l[2] * l[5];
+      float* il = ilem + 6 * r;
+      if (fabs(det) < kMinDet || vol < 1e-6) {
+        for (int i = 0; i < 6; i++) il[i] = 0.0f;
+        atomicAdd(num_flat, 1u);
+      } else {
+        il[0] = (float) ((l[1] * l[5] - l[4] * l[4]) / det);
+        il[1] = (float) ((l[0] * l[5] - l[3] * l[3]) / det);
+        il[2] = (float) ((l[3] * l[4] - l[2] * l[5]) / det);
+        il[3] = (float) ((l[2] * l[4] - l[3] * l[1]) / det);
+        il[4] = (float) ((l[3] * l[2] - l[0] * l[4]) / det);
+        il[5] = (float) ((l[0] * l[1] - l[2] * l[2]) / det);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < S_; j++) {
+      const int g = lane + 32 * j;
+      if (g < ld) {
+        const bool on = g < G;
+#pragma unroll
+        for (int i = 0; i < 6; i++)
+          cst[(r * 6 + i) * ld + g] = on ? (float) c[i][j] : 0.0f;
+      }
+    }
+  }
+}
+
 __global__ void ls_refresh_kernel(const int2* segs, int4* out, int64_t S) {
   for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < S;
        i += (int64_t) gridDim.x * blockDim.x)
@@ -234,8 +333,25 @@ void launch_ls_constants_bucketed(const int4* segs_ls, const int32_t* list,
                                   const float* fsr_vol, const int32_t* fsr_mat,
                                   int64_t R, int G, int ld, float* ilem,
                                   float* cst, unsigned int* num_flat,
-                                  cudaStream_t s) {
+                                  cudaStream_t s, const float* seg_z,
+                                  const double* pol_cos) {
   const unsigned blocks = (unsigned) grid_for(32 * R, 256);
+  if (seg_z) {
+#define MOC_LS_CONST3(SS)                                                     \
+  ls_constants3d_kernel<SS><<<blocks, 256, 0, s>>>(                           \
+      segs_ls, seg_z, list, start, seg_track, track_ang, ang_dir, ang_wgt,    \
+      pol_sin, pol_wgt, pol_cos, sigma_t, fsr_vol, fsr_mat, R, G, ld, ilem,   \
+      cst, num_flat)
+    switch ((ld + 31) / 32) {
+      case 1: MOC_LS_CONST3(1); break;
+      case 2: MOC_LS_CONST3(2); break;
+      case 3: MOC_LS_CONST3(3); break;
+      case 4: MOC_LS_CONST3(4); break;
+      default: MOC_LS_CONST3(8); break;
+    }
+#undef MOC_LS_CONST3
+    return;
+  }
 #define MOC_LS_CONST(SS)                                                    \
   ls_constants_kernel<SS><<<blocks, 256, 0, s>>>(                           \
       segs_ls, list, start, seg_track, track_ang, ang_dir, ang_wgt,         \
@@ -258,7 +374,8 @@ int launch_ls_constants(const int4* segs_ls, const int64_t* seg_off,
                         const float* sigma_t, const float* fsr_vol,
                         const int32_t* fsr_mat, int64_t R, int G, int ld,
                         float* ilem, float* cst, unsigned int* num_flat,
-                        cudaStream_t s) {
+                        cudaStream_t s, const float* seg_z,
+                        const double* pol_cos) {
   // segment buckets by FSR: counts, exclusive scan on the host, scatter
   int64_t* count = nullptr;
   int64_t* startp = nullptr;
@@ -306,7 +423,7 @@ int launch_ls_constants(const int4* segs_ls, const int64_t* seg_off,
     launch_ls_constants_bucketed(segs_ls, list, startp, seg_track, track_ang,
                                  ang_dir, ang_wgt, pol_sin, pol_wgt, Ph,
                                  sigma_t, fsr_vol, fsr_mat, R, G, ld, ilem, cst,
-                                 num_flat, s);
+                                 num_flat, s, seg_z, pol_cos);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);

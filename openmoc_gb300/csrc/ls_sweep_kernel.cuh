@@ -78,19 +78,25 @@ struct LsExpG {
 };
 
 // Blocks of 128 threads kept resident per SM: the register file bounds the
-// busy instances (PH * PS pair-polar values per lane).
-template <int PH, int PS>
+// busy instances (PH * PS pair-polar values per lane); the 3D instances
+// carry the z source moments and tallies of every pair as well.
+template <int PH, int PS, bool D3>
 struct LsOccupancy {
-  static constexpr int min_blocks = (PH * PS >= 12) ? 4 : (PH * PS >= 6) ? 5 : 6;
+  static constexpr int min_blocks =
+      D3 ? ((PS >= 4) ? 3 : (PS >= 3) ? 4 : 6)
+         : ((PH * PS >= 12) ? 4 : (PH * PS >= 6) ? 5 : 6);
 };
 
 // CM: also the CMFD partial currents (a.cm_cell set), as the flat sweep's
 // mode 2.  In a pool (a.track_slot set) each track takes the pending
 // angular-flux scale of its solve and is skipped once its solve is done, as
-// in the flat sweep's mode 1.
-template <int PH, int LPS, int PS, bool CM>
+// in the flat sweep's mode 1.  D3 (PH = 1): explicit 3D tracks, the 3D
+// branch of tallyLSScalarFlux (src/CPULSSolver.cpp:555-646) -- true
+// lengths (inv_sin = 1), the 3D direction of the angle row, the z start of
+// each segment and the z source moment and tally.
+template <int PH, int LPS, int PS, bool CM, bool D3 = false>
 __global__ void __launch_bounds__(kSweepThreads,
-                                  (LsOccupancy<PH, PS>::min_blocks))
+                                  (LsOccupancy<PH, PS, D3>::min_blocks))
 ls_sweep_kernel(const SweepArgs a) {
   extern __shared__ float smem[];
   DevScalars* sc = a.sc;
@@ -135,9 +141,18 @@ ls_sweep_kernel(const SweepArgs a) {
     const int ang = a.track_ang[t];
     const int F = G * PH;
     // forward direction, and the direction of travel of this stream
-    const float2 fd = a.ang_dir[ang];
+    float2 fd;
+    float fdz = 0.0f;
+    if constexpr (D3) {
+      const float4 d3 = a.ang_dir3[ang];
+      fd = make_float2(d3.x, d3.y);
+      fdz = d3.z;
+    } else {
+      fd = a.ang_dir[ang];
+    }
     const float dx = dir ? -fd.x : fd.x;
     const float dy = dir ? -fd.y : fd.y;
+    const float dz = dir ? -fdz : fdz;
 
     float2 w2[PH], xs2[PH], xw2[PH];
 #pragma unroll
@@ -182,16 +197,33 @@ ls_sweep_kernel(const SweepArgs a) {
     int4 chunk = fetch(sub);
     int4 chunk_next = fetch(LPS + sub);
     int4 wcur = word(chunk, 0);
+    // 3D: the z starts, fetched and broadcast like the words
+    const float* segz = D3 ? a.seg_z + b : nullptr;
+    auto fetchz = [&](int kk) -> float {
+      return (D3 && kk < n) ? __ldg(segz + (dir ? n - 1 - kk : kk)) : 0.0f;
+    };
+    float zchunk = fetchz(sub);
+    float zchunk_next = fetchz(LPS + sub);
+    float zcur = D3 ? __shfl_sync(gmask, zchunk, 0, LPS) : 0.0f;
 
     const float2* qf_base = reinterpret_cast<const float2*>(a.qt) + sub;
     const float4* qm_base = reinterpret_cast<const float4*>(a.qxy) + sub;
+    const float2* qz_base =
+        D3 ? reinterpret_cast<const float2*>(a.qz) + sub : nullptr;
     for (int k = 0; k < n; k++) {
       // the next segment's word: segment k + 1 opens a chunk every LPS
       if (((k + 1) & (LPS - 1)) == 0) {
         chunk = chunk_next;
         chunk_next = fetch(k + 1 + LPS + sub);
+        if constexpr (D3) {
+          zchunk = zchunk_next;
+          zchunk_next = fetchz(k + 1 + LPS + sub);
+        }
       }
       const int4 wnext = word(chunk, k + 1);
+      float znext = 0.0f;
+      if constexpr (D3)
+        znext = __shfl_sync(gmask, zchunk, (k + 1) & (LPS - 1), LPS);
 
       const float len = __int_as_float(wcur.x);
       const int fsr = wcur.y & 0xFFFFFF;
@@ -203,8 +235,11 @@ ls_sweep_kernel(const SweepArgs a) {
       const float sy = dir ? fmaf(fd.y, len, py) : py;
       const float c2x = fmaf(2.0f, px, len * fd.x);
       const float c2y = fmaf(2.0f, py, len * fd.y);
+      const float pz = zcur;
+      const float sz = dir ? fmaf(fdz, len, pz) : pz;
+      const float c2z = fmaf(2.0f, pz, len * fdz);
 
-      float2 qf[PS];
+      float2 qf[PS], qzz[PS];
       float4 qm[PS];
 #pragma unroll
       for (int s = 0; s < PS; s++) {
@@ -213,6 +248,9 @@ ls_sweep_kernel(const SweepArgs a) {
                    : f2(0.0f);
         qm[s] = on ? __ldg(qm_base + (int64_t) fsr * npairs + s * LPS)
                    : make_float4(0.f, 0.f, 0.f, 0.f);
+        qzz[s] = (D3 && on)
+                     ? __ldg(qz_base + (int64_t) fsr * npairs + s * LPS)
+                     : f2(0.0f);
       }
 
       const float2* st =
@@ -220,6 +258,9 @@ ls_sweep_kernel(const SweepArgs a) {
       float2* ph = reinterpret_cast<float2*>(a.phi + (int64_t) fsr * ld) + sub;
       float4* pm =
           reinterpret_cast<float4*>(a.mom + (int64_t) fsr * 2 * ld) + sub;
+      float2* pmz =
+          D3 ? reinterpret_cast<float2*>(a.momz + (int64_t) fsr * ld) + sub
+             : nullptr;
       const float2 len2 = f2(len);
 #pragma unroll
       for (int s = 0; s < PS; s++) {
@@ -227,10 +268,13 @@ ls_sweep_kernel(const SweepArgs a) {
           const float2 tau = __fmul2_rn(st[s * LPS], len2);
           const float2 qx = make_float2(qm[s].x, qm[s].z);
           const float2 qy = make_float2(qm[s].y, qm[s].w);
-          const float2 sf =
-              __ffma2_rn(qy, f2(c2y), __ffma2_rn(qx, f2(c2x), qf[s]));
-          const float2 sl =
-              __fmul2_rn(__ffma2_rn(qy, f2(dy), __fmul2_rn(qx, f2(dx))), len2);
+          float2 sf = __ffma2_rn(qy, f2(c2y), __ffma2_rn(qx, f2(c2x), qf[s]));
+          float2 sdq = __ffma2_rn(qy, f2(dy), __fmul2_rn(qx, f2(dx)));
+          if constexpr (D3) {
+            sf = __ffma2_rn(qzz[s], f2(c2z), sf);
+            sdq = __ffma2_rn(qzz[s], f2(dz), sdq);
+          }
+          const float2 sl = __fmul2_rn(sdq, len2);
           // gn = -G, u = 1 - x G, m = u - 2 G = -(2G - u):
           //   delta = (psi - s_f) x u + (s_l x) m
           //   moment term w l x (u - G) psi = l tau (w / sin) (u + gn) psi
@@ -255,6 +299,9 @@ ls_sweep_kernel(const SweepArgs a) {
           const float2 mx = __ffma2_rn(dacc, f2(sx), __fmul2_rn(hl, f2(dx)));
           const float2 my = __ffma2_rn(dacc, f2(sy), __fmul2_rn(hl, f2(dy)));
           atomicAdd(pm + s * LPS, make_float4(mx.x, my.x, mx.y, my.y));
+          if constexpr (D3)
+            atomicAdd(pmz + s * LPS,
+                      __ffma2_rn(dacc, f2(sz), __fmul2_rn(hl, f2(dz))));
         }
       }
       if constexpr (CM) {
@@ -263,6 +310,7 @@ ls_sweep_kernel(const SweepArgs a) {
                                          sub, npairs, ld, w2, psi);
       }
       wcur = wnext;
+      if constexpr (D3) zcur = znext;
     }
 
     // boundary-flux transfer to the connecting track
@@ -313,6 +361,13 @@ void launch_ls_instance(const SweepArgs& a, cudaStream_t stream) {
   const int wpb = kSweepThreads / 32;
   const int64_t blocks = (warps + wpb - 1) / wpb;
   const size_t smem = sizeof(float) * (size_t) a.num_materials * a.ld;
+  if constexpr (PH == 1) {
+    if (a.momz) {
+      ls_sweep_kernel<1, LPS, PS, false, true>
+          <<<(unsigned) blocks, kSweepThreads, smem, stream>>>(a);
+      return;
+    }
+  }
   auto kern = a.cm_cell ? ls_sweep_kernel<PH, LPS, PS, true>
                         : ls_sweep_kernel<PH, LPS, PS, false>;
   kern<<<(unsigned) blocks, kSweepThreads, smem, stream>>>(a);
@@ -321,6 +376,13 @@ void launch_ls_instance(const SweepArgs& a, cudaStream_t stream) {
 // The shared-memory limit of every instance dispatch_ls_lps can launch.
 template <int PH, int LPS>
 void configure_ls_lps(int optin) {
+  if constexpr (PH == 1) {
+    raise_smem_limit(ls_sweep_kernel<1, LPS, 1, false, true>, optin);
+    raise_smem_limit(ls_sweep_kernel<1, LPS, 2, false, true>, optin);
+    raise_smem_limit(ls_sweep_kernel<1, LPS, 3, false, true>, optin);
+    raise_smem_limit(ls_sweep_kernel<1, LPS, 4, false, true>, optin);
+    raise_smem_limit(ls_sweep_kernel<1, LPS, 5, false, true>, optin);
+  }
   raise_smem_limit(ls_sweep_kernel<PH, LPS, 1, true>, optin);
   raise_smem_limit(ls_sweep_kernel<PH, LPS, 2, true>, optin);
   raise_smem_limit(ls_sweep_kernel<PH, LPS, 3, true>, optin);

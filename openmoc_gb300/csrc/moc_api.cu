@@ -249,13 +249,16 @@ struct moc_ctx {
   // moderator above an extruded lattice): tallied in shared memory by the
   // 3D sweep instances
   int hot_base = 0, hot_count = 0;
-  // Linear source (moc_set_linear_source, 2D): 16-byte segment words with
-  // the start positions, per-angle FP64 data for the expansion constants
-  // (dir [A][2], azimuthal weight [A], sin theta [A][Ph], polar weight
-  // [A][Ph], one buffer), float directions, flux / source moments
-  // [R][ld][2], inverse expansion matrices [R][3], constants [R][3][ld] and
-  // fixed source moments [R][ld][2].
+  // Linear source (moc_set_linear_source): 16-byte segment words with the
+  // start positions, per-angle FP64 data for the expansion constants (dir
+  // [A][2], azimuthal weight [A], sin theta [A][Ph], polar weight [A][Ph],
+  // in 3D cos theta [A]; one buffer), float directions, flux / source
+  // moments [R][ld][2], inverse expansion matrices [R][3], constants
+  // [R][3][ld] and fixed source moments [R][ld][2].  On explicit 3D tracks
+  // (ls3d) also the segments' z starts, 3D directions, the z moments
+  // [R][ld] and six coefficients: [R][6], [R][6][ld].
   bool ls = false;
+  bool ls3d = false;
   int4* segs_ls = nullptr;
   double* ls_ang = nullptr;
   float2* ls_dir = nullptr;
@@ -264,6 +267,11 @@ struct moc_ctx {
   float* ls_ilem = nullptr;
   float* ls_const = nullptr;
   float* fixed_xy = nullptr;
+  float* ls_segz = nullptr;
+  float4* ls_dir3 = nullptr;
+  float* momz = nullptr;
+  float* qz = nullptr;
+  float* fixed_z = nullptr;
   int64_t ls_num_flat = 0;
   int negative_ok = 0;       // Solver::allowNegativeFluxes
   int keff_balance = 0;      // Solver::setKeffFromNeutronBalance
@@ -508,6 +516,12 @@ moc::SweepArgs sweep_args(moc_ctx* c, int check_done) {
     a.ang_dir = c->ls_dir;
     a.qxy = c->qxy;
     a.mom = c->mom;
+    if (c->ls3d) {
+      a.seg_z = c->ls_segz;
+      a.ang_dir3 = c->ls_dir3;
+      a.qz = c->qz;
+      a.momz = c->momz;
+    }
   }
   if (c->cmfd && !c->otf) {
     a.cm_cell = c->cm_cell;
@@ -580,6 +594,11 @@ moc::SolverArgs solver_args(moc_ctx* c, int check_done) {
     a.ls_ilem = c->ls_ilem;
     a.ls_const = c->ls_const;
     a.fixed_xy = c->fixed_xy;
+    if (c->ls3d) {
+      a.momz = c->momz;
+      a.qz = c->qz;
+      a.fixed_z = c->fixed_z;
+    }
   }
   return a;
 }
@@ -819,6 +838,8 @@ int enqueue_zero_tallies(moc_ctx* c, const moc::SolverArgs& a) {
 int zero_moments(moc_ctx* c) {
   if (c->ls)
     MOC_CUDA(cudaMemsetAsync(c->mom, 0, 8 * num_flux(c), c->stream));
+  if (c->ls3d)
+    MOC_CUDA(cudaMemsetAsync(c->momz, 0, 4 * num_flux(c), c->stream));
   return MOC_OK;
 }
 
@@ -1402,6 +1423,12 @@ void ls_release(moc_ctx* c) {
   dfree(c->ls_ilem);
   dfree(c->ls_const);
   dfree(c->fixed_xy);
+  dfree(c->ls_segz);
+  dfree(c->ls_dir3);
+  dfree(c->momz);
+  dfree(c->qz);
+  dfree(c->fixed_z);
+  c->ls3d = false;
   if (c->ls && !c->shape_user_set) c->lps = c->slots = 0;
   if (c->ls) c->tuned = false;
   c->ls = false;
@@ -1421,7 +1448,8 @@ int ls_constants(moc_ctx* c) {
       c->segs_ls, c->seg_off, c->track_ang, T, c->d.num_segments, ang,
       ang + 2 * A, ang + 3 * A, ang + 3 * A + A * Ph, Ph, c->sigma_t,
       c->fsr_vol, c->fsr_mat, R, G, row_stride(c), c->ls_ilem, c->ls_const,
-      nflat, c->stream);
+      nflat, c->stream, c->ls3d ? c->ls_segz : nullptr,
+      c->ls3d ? ang + 3 * A + 2 * A * Ph : nullptr);
   c->launches += 4;
   unsigned int h = 0;
   cudaError_t e = (cudaError_t) rc;
@@ -1602,6 +1630,11 @@ int moc_destroy(moc_ctx* c) {
   dfree(c->ls_ilem);
   dfree(c->ls_const);
   dfree(c->fixed_xy);
+  dfree(c->ls_segz);
+  dfree(c->ls_dir3);
+  dfree(c->momz);
+  dfree(c->qz);
+  dfree(c->fixed_z);
   dfree(c->otf_trk);
   dfree(c->otf_trk_f);
   dfree(c->otf_ang);
@@ -2548,8 +2581,13 @@ int moc_set_linear_source(moc_ctx* c, const moc_ls_geometry* g) {
     ls_release(c);
     return MOC_OK;
   }
-  MOC_CHECK(!c->d.solve_3d, MOC_ERR_UNSUPPORTED,
-            "the linear source takes 2D tracks");
+  const bool d3 = c->d.solve_3d != 0;
+  MOC_CHECK(!d3 || (g->seg_z && g->pol_cos), MOC_ERR_ARG,
+            "the linear source on 3D tracks needs seg_z and pol_cos");
+  MOC_CHECK(!d3 || c->d.num_polar_half == 1, MOC_ERR_UNSUPPORTED,
+            "the linear source on 3D tracks takes one polar value per track");
+  MOC_CHECK(!d3 || !c->otf, MOC_ERR_UNSUPPORTED,
+            "on-the-fly segmentation and the linear source do not combine");
   MOC_CHECK(!c->keff_balance, MOC_ERR_UNSUPPORTED,
             "keff from the neutron balance is built for the flat source");
   MOC_CHECK(!c->stab_on, MOC_ERR_UNSUPPORTED,
@@ -2569,10 +2607,18 @@ int moc_set_linear_source(moc_ctx* c, const moc_ls_geometry* g) {
   const int64_t S = c->d.num_segments, R = c->d.num_fsrs;
   const int A = c->d.num_angles, Ph = c->d.num_polar_half;
   for (int64_t i = 0; i < S; i++)
-    MOC_CHECK(std::isfinite(g->seg_x[i]) && std::isfinite(g->seg_y[i]),
+    MOC_CHECK(std::isfinite(g->seg_x[i]) && std::isfinite(g->seg_y[i]) &&
+                  (!d3 || std::isfinite(g->seg_z[i])),
               MOC_ERR_ARG,
               "non-finite segment start position at segment " +
                   std::to_string(i));
+  for (int a = 0; a < A && d3; a++) {
+    const double sn = g->pol_sin[a], cs = g->pol_cos[a];
+    MOC_CHECK(std::isfinite(cs) && std::fabs(sn * sn + cs * cs - 1.0) < 1e-6,
+              MOC_ERR_ARG,
+              "sin and cos theta of angle row " + std::to_string(a) +
+                  " do not make a unit vector");
+  }
   for (int a = 0; a < A; a++) {
     const double cx = g->ang_dir[2 * a], cy = g->ang_dir[2 * a + 1];
     MOC_CHECK(std::isfinite(cx) && std::isfinite(cy) &&
@@ -2592,9 +2638,10 @@ int moc_set_linear_source(moc_ctx* c, const moc_ls_geometry* g) {
   }
   ls_release(c);
   const int64_t nf = num_flux(c);
-  const size_t nang = 3 * (size_t) A + 2 * (size_t) A * Ph;
+  const size_t nang = 3 * (size_t) A + 2 * (size_t) A * Ph + (d3 ? A : 0);
   std::vector<double> ang(nang);
   std::vector<float2> dir(A);
+  std::vector<float4> dir3(d3 ? A : 0);
   for (int a = 0; a < A; a++) {
     ang[2 * a] = g->ang_dir[2 * a];
     ang[2 * a + 1] = g->ang_dir[2 * a + 1];
@@ -2604,7 +2651,17 @@ int moc_set_linear_source(moc_ctx* c, const moc_ls_geometry* g) {
       ang[3 * A + a * Ph + p] = g->pol_sin[a * Ph + p];
       ang[3 * A + A * Ph + a * Ph + p] = g->pol_wgt[a * Ph + p];
     }
+    if (d3) {
+      // TransportSweep::onTrack: cos(phi) sin(theta), sin(phi) sin(theta),
+      // cos(theta) in double, then rounded
+      // (src/TrackTraversingAlgorithms.cpp:913-926)
+      ang[3 * A + 2 * A * Ph + a] = g->pol_cos[a];
+      dir3[a] = make_float4((float) (g->ang_dir[2 * a] * g->pol_sin[a]),
+                            (float) (g->ang_dir[2 * a + 1] * g->pol_sin[a]),
+                            (float) g->pol_cos[a], 0.0f);
+    }
   }
+  const int NC = d3 ? 6 : 3;
   float* dx = nullptr;
   float* dy = nullptr;
   int st = MOC_OK;
@@ -2614,10 +2671,16 @@ int moc_set_linear_source(moc_ctx* c, const moc_ls_geometry* g) {
   step(dalloc(&c->ls_dir, A));
   step(dalloc(&c->mom, 2 * nf));
   step(dalloc(&c->qxy, 2 * nf));
-  step(dalloc(&c->ls_ilem, 3 * R));
-  step(dalloc(&c->ls_const, 3 * nf));
+  step(dalloc(&c->ls_ilem, NC * R));
+  step(dalloc(&c->ls_const, NC * nf));
   step(dalloc(&dx, S > 0 ? S : 1));
   step(dalloc(&dy, S > 0 ? S : 1));
+  if (d3) {
+    step(dalloc(&c->ls_segz, S > 0 ? S : 1));
+    step(dalloc(&c->ls_dir3, A));
+    step(dalloc(&c->momz, nf));
+    step(dalloc(&c->qz, nf));
+  }
   if (st != MOC_OK) {
     dfree(dx);
     dfree(dy);
@@ -2634,6 +2697,13 @@ int moc_set_linear_source(moc_ctx* c, const moc_ls_geometry* g) {
                    cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(c->mom, 0, 8 * nf);
   if (e == cudaSuccess) e = cudaMemset(c->qxy, 0, 8 * nf);
+  if (d3 && e == cudaSuccess)
+    e = cudaMemcpy(c->ls_segz, g->seg_z, 4 * S, cudaMemcpyHostToDevice);
+  if (d3 && e == cudaSuccess)
+    e = cudaMemcpy(c->ls_dir3, dir3.data(), 16 * (size_t) A,
+                   cudaMemcpyHostToDevice);
+  if (d3 && e == cudaSuccess) e = cudaMemset(c->momz, 0, 4 * nf);
+  if (d3 && e == cudaSuccess) e = cudaMemset(c->qz, 0, 4 * nf);
   if (e == cudaSuccess) {
     moc::launch_ls_pack_segments(c->segs, dx, dy, c->segs_ls, S, c->stream);
     c->launches++;
@@ -2648,6 +2718,7 @@ int moc_set_linear_source(moc_ctx* c, const moc_ls_geometry* g) {
                                   cudaGetErrorString(e));
   }
   c->ls = true;
+  c->ls3d = d3;
   if (!c->shape_user_set) c->lps = c->slots = 0;
   c->tuned = false;
   st = ls_constants(c);
@@ -2776,15 +2847,19 @@ int moc_set_keff_from_neutron_balance(moc_ctx* c, int on) {
 }
 
 // host [R][3][G] (x, y, z) <-> device [R][ld][2] (x, y adjacent per group)
+// and, on 3D tracks, [R][ld] (z; dev_z null: z = 0)
 static int moments_out(moc_ctx* c, const float* dev, float* out, int64_t n,
-                       float scale_by_sigma_t) {
+                       float scale_by_sigma_t, const float* dev_z = nullptr) {
   const int64_t R = c->d.num_fsrs;
   const int G = c->d.num_groups, ld = row_stride(c);
   MOC_CHECK(out && n == 3 * R * G, MOC_ERR_ARG,
             "moments need num_fsrs x 3 x num_groups values");
-  std::vector<float> h((size_t) 2 * R * ld);
+  std::vector<float> h((size_t) 2 * R * ld), hz(dev_z ? (size_t) R * ld : 0);
   MOC_CUDA(cudaMemcpyAsync(h.data(), dev, 8 * (size_t) R * ld,
                            cudaMemcpyDeviceToHost, c->stream));
+  if (dev_z)
+    MOC_CUDA(cudaMemcpyAsync(hz.data(), dev_z, 4 * (size_t) R * ld,
+                             cudaMemcpyDeviceToHost, c->stream));
   std::vector<float> st;
   std::vector<int32_t> fm;
   if (scale_by_sigma_t != 0.0f) {
@@ -2799,34 +2874,43 @@ static int moments_out(moc_ctx* c, const float* dev, float* out, int64_t n,
   for (int64_t r = 0; r < R; r++)
     for (int g = 0; g < G; g++) {
       float x = h[(r * ld + g) * 2], y = h[(r * ld + g) * 2 + 1];
+      float z = dev_z ? hz[r * ld + g] : 0.0f;
       if (scale_by_sigma_t != 0.0f) {
         const float s = st[(size_t) fm[r] * G + g];
         x *= s;
         y *= s;
+        z *= s;
       }
       out[(r * 3 + 0) * G + g] = x;
       out[(r * 3 + 1) * G + g] = y;
-      out[(r * 3 + 2) * G + g] = 0.0f;
+      out[(r * 3 + 2) * G + g] = z;
     }
   return MOC_OK;
 }
 
-static int moments_in(moc_ctx* c, float* dev, const float* in, int64_t n) {
+static int moments_in(moc_ctx* c, float* dev, const float* in, int64_t n,
+                      float* dev_z = nullptr) {
   const int64_t R = c->d.num_fsrs;
   const int G = c->d.num_groups, ld = row_stride(c);
   MOC_CHECK(in && n == 3 * R * G, MOC_ERR_ARG,
             "moments need num_fsrs x 3 x num_groups values");
-  std::vector<float> h((size_t) 2 * R * ld, 0.0f);
+  std::vector<float> h((size_t) 2 * R * ld, 0.0f), hz((size_t) R * ld, 0.0f);
   for (int64_t r = 0; r < R; r++)
     for (int g = 0; g < G; g++) {
       const float x = in[(r * 3 + 0) * G + g], y = in[(r * 3 + 1) * G + g];
-      MOC_CHECK(std::isfinite(x) && std::isfinite(y), MOC_ERR_ARG,
-                "non-finite moment");
+      const float z = in[(r * 3 + 2) * G + g];
+      MOC_CHECK(std::isfinite(x) && std::isfinite(y) &&
+                    (!dev_z || std::isfinite(z)),
+                MOC_ERR_ARG, "non-finite moment");
       h[(r * ld + g) * 2] = x;
       h[(r * ld + g) * 2 + 1] = y;
+      hz[r * ld + g] = z;
     }
   MOC_CUDA(cudaMemcpyAsync(dev, h.data(), 8 * (size_t) R * ld,
                            cudaMemcpyHostToDevice, c->stream));
+  if (dev_z)
+    MOC_CUDA(cudaMemcpyAsync(dev_z, hz.data(), 4 * (size_t) R * ld,
+                             cudaMemcpyHostToDevice, c->stream));
   MOC_CUDA(cudaStreamSynchronize(c->stream));
   return MOC_OK;
 }
@@ -2834,19 +2918,19 @@ static int moments_in(moc_ctx* c, float* dev, const float* in, int64_t n) {
 int moc_get_flux_moments(moc_ctx* c, float* out, int64_t n) {
   MOC_TRY(ready(c));
   MOC_CHECK(c->ls, MOC_ERR_STATE, "no linear source set");
-  return moments_out(c, c->mom, out, n, 0.0f);
+  return moments_out(c, c->mom, out, n, 0.0f, c->ls3d ? c->momz : nullptr);
 }
 
 int moc_set_flux_moments(moc_ctx* c, const float* in, int64_t n) {
   MOC_TRY(ready(c));
   MOC_CHECK(c->ls, MOC_ERR_STATE, "no linear source set");
-  return moments_in(c, c->mom, in, n);
+  return moments_in(c, c->mom, in, n, c->ls3d ? c->momz : nullptr);
 }
 
 int moc_get_source_moments(moc_ctx* c, float* out, int64_t n) {
   MOC_TRY(ready(c));
   MOC_CHECK(c->ls, MOC_ERR_STATE, "no linear source set");
-  return moments_out(c, c->qxy, out, n, 1.0f);
+  return moments_out(c, c->qxy, out, n, 1.0f, c->ls3d ? c->qz : nullptr);
 }
 
 int moc_set_fixed_source_moments(moc_ctx* c, const float* in, int64_t n) {
@@ -2854,10 +2938,12 @@ int moc_set_fixed_source_moments(moc_ctx* c, const float* in, int64_t n) {
   MOC_CHECK(c->ls, MOC_ERR_STATE, "no linear source set");
   if (!in) {
     dfree(c->fixed_xy);
+    dfree(c->fixed_z);
     return MOC_OK;
   }
   if (!c->fixed_xy) MOC_TRY(dalloc(&c->fixed_xy, 2 * num_flux(c)));
-  return moments_in(c, c->fixed_xy, in, n);
+  if (c->ls3d && !c->fixed_z) MOC_TRY(dalloc(&c->fixed_z, num_flux(c)));
+  return moments_in(c, c->fixed_xy, in, n, c->ls3d ? c->fixed_z : nullptr);
 }
 
 int moc_get_linear_expansion(moc_ctx* c, double* ilem, float* src_const) {
@@ -2865,15 +2951,16 @@ int moc_get_linear_expansion(moc_ctx* c, double* ilem, float* src_const) {
   MOC_CHECK(c->ls, MOC_ERR_STATE, "no linear source set");
   const int64_t R = c->d.num_fsrs;
   const int G = c->d.num_groups, ld = row_stride(c);
+  const int NC = c->ls3d ? 6 : 3;
   if (ilem) {
-    std::vector<float> h(3 * (size_t) R);
+    std::vector<float> h(NC * (size_t) R);
     MOC_CUDA(cudaMemcpy(h.data(), c->ls_ilem, 4 * h.size(),
                         cudaMemcpyDeviceToHost));
     for (size_t i = 0; i < h.size(); i++) ilem[i] = h[i];
   }
   if (src_const)
     MOC_CUDA(cudaMemcpy2D(src_const, 4 * G, c->ls_const, 4 * ld, 4 * G,
-                          3 * R, cudaMemcpyDeviceToHost));
+                          NC * R, cudaMemcpyDeviceToHost));
   return MOC_OK;
 }
 

@@ -136,6 +136,14 @@ struct SweepArgs {
   const float2* ang_dir;     // [A]
   const float* qxy;          // [R][ld][2]
   float* mom;                // [R][ld][2]
+  // ... on explicit 3D tracks (null in 2D): each segment's z start, the
+  // angle rows' 3D directions (cos phi sin theta, sin phi sin theta,
+  // cos theta; ang_dir is then unused), the z source moment / sigma_t and
+  // the z moment tallies
+  const float* seg_z;        // [S]
+  const float4* ang_dir3;    // [A]
+  const float* qz;           // [R][ld]
+  float* momz;               // [R][ld]
   // CMFD (null: none): coarse cell of every FSR (iy * cm_nx + ix), outgoing
   // partial currents [cells][4 faces][ld], and per track the boundary face
   // crossed at its forward / backward end where the flux is not
@@ -219,12 +227,18 @@ struct SolverArgs {
   // Linear source (null: flat source): flux moments and reduced source
   // moments / sigma_t ([R][ld][2], x and y adjacent per group), the inverse
   // expansion matrix per FSR (xx, yy, xy), the source constants [R][3][ld]
-  // and the fixed source moments [R][ld][2] (or null).
+  // and the fixed source moments [R][ld][2] (or null).  On explicit 3D
+  // tracks (momz set) also the z moments ([R][ld] each) and six
+  // coefficients (xx, yy, xy, xz, yz, zz) per FSR: ls_ilem [R][6],
+  // ls_const [R][6][ld].
   float* mom;
   float* qxy;
-  const float* ls_ilem;      // [R][3]
-  const float* ls_const;     // [R][3][ld]
+  const float* ls_ilem;      // [R][3] or [R][6]
+  const float* ls_const;     // [R][3][ld] or [R][6][ld]
   const float* fixed_xy;
+  float* momz;               // [R][ld] or null
+  float* qz;                 // [R][ld] or null
+  const float* fixed_z;      // [R][ld] or null
   int negative_ok;           // Solver::allowNegativeFluxes
   // keff = fission / (absorption + leakage) instead of keff *= fission / R
   // (Solver::setKeffFromNeutronBalance); absorption = sigma_t - scat_out
@@ -343,7 +357,9 @@ constexpr int kMaxLsSlots = 5;
 // LinearExpansionGenerator (2D): volume moments and source constants per
 // FSR summed in FP64 over the FSR's segments, then inverted; outputs
 // ilem[R][3] and cst[R][3][ld] (float) and through *num_flat the FSRs whose
-// matrix is singular (flat source there).  Allocates and frees its own
+// matrix is singular (flat source there); with seg_z and pol_cos (explicit
+// 3D tracks: pol_sin, pol_cos and pol_wgt per angle row, Ph = 1) the six
+// 3D coefficients, ilem[R][6] and cst[R][6][ld].  Allocates and frees its own
 // scratch (segment buckets by FSR); returns 0 or the cudaError_t.
 int launch_ls_constants(const int4* segs_ls, const int64_t* seg_off,
                         const int32_t* track_ang, int64_t T, int64_t S,
@@ -352,7 +368,8 @@ int launch_ls_constants(const int4* segs_ls, const int64_t* seg_off,
                         const float* sigma_t, const float* fsr_vol,
                         const int32_t* fsr_mat, int64_t R, int G, int ld,
                         float* ilem, float* cst, unsigned int* num_flat,
-                        cudaStream_t s);
+                        cudaStream_t s, const float* seg_z = nullptr,
+                        const double* pol_cos = nullptr);
 // The track of every segment from the segment offsets (seg_off[0] = 0).
 void launch_ls_seg_track(const int64_t* seg_off, int64_t T, int32_t* seg_track,
                          cudaStream_t s);
@@ -369,7 +386,9 @@ void launch_ls_constants_bucketed(const int4* segs_ls, const int32_t* list,
                                   const float* fsr_vol, const int32_t* fsr_mat,
                                   int64_t R, int G, int ld, float* ilem,
                                   float* cst, unsigned int* num_flat,
-                                  cudaStream_t s);
+                                  cudaStream_t s,
+                                  const float* seg_z = nullptr,
+                                  const double* pol_cos = nullptr);
 // Builds segs_ls from the packed segments and the start positions.
 void launch_ls_pack_segments(const int2* segs, const float* x, const float* y,
                              int4* out, int64_t S, cudaStream_t s);

@@ -775,6 +775,7 @@ __global__ void zero_phi_kernel(const SolverArgs a) {
       a.mom[2 * i] = 0.0f;
       a.mom[2 * i + 1] = 0.0f;
     }
+    if (a.momz) a.momz[i] = 0.0f;
   }
 }
 
@@ -831,7 +832,9 @@ __device__ __forceinline__ DevScalars* live_slot(const SolverArgs& a,
 // takes keff, the iteration count and the negative-flux rule of its solve;
 // a computeFlux solve keeps the sources of its first iteration and only has
 // its tallies zeroed.
-template <int S>
+// D3: explicit 3D tracks -- the z moments too and the 3x3 inverse
+// (src/CPULSSolver.cpp:466-487).
+template <int S, bool D3>
 __global__ void __launch_bounds__(kThreads)
 ls_sources_kernel(const SolverArgs a, int iteration, int zero, int staged) {
   if (skip(a)) return;
@@ -867,6 +870,7 @@ ls_sources_kernel(const SolverArgs a, int iteration, int zero, int staged) {
           for (int g = lane; g < G; g += 32) {
             phi[g] = 0.0f;
             mom[g] = make_float2(0.f, 0.f);
+            if constexpr (D3) a.momz[r * ld + g] = 0.0f;
           }
         continue;
       }
@@ -877,7 +881,8 @@ ls_sources_kernel(const SolverArgs a, int iteration, int zero, int staged) {
       inv_k = __shfl_sync(0xffffffffu, inv_k, 0);
     }
     const int m = a.fsr_mat[r];
-    float ph[S], mx[S], my[S], s0[S], s1[S], s2[S];
+    float* momz = D3 ? a.momz + r * ld : nullptr;
+    float ph[S], mx[S], my[S], mz[S], s0[S], s1[S], s2[S], s3[S];
 #pragma unroll
     for (int j = 0; j < S; j++) {
       const int g = lane + 32 * j;
@@ -885,7 +890,8 @@ ls_sources_kernel(const SolverArgs a, int iteration, int zero, int staged) {
       ph[j] = (g < G) ? phi[g] : 0.0f;
       mx[j] = mm.x;
       my[j] = mm.y;
-      s0[j] = s1[j] = s2[j] = 0.0f;
+      mz[j] = (D3 && g < G) ? momz[g] : 0.0f;
+      s0[j] = s1[j] = s2[j] = s3[j] = 0.0f;
     }
     if (zero) {
 #pragma unroll
@@ -894,10 +900,11 @@ ls_sources_kernel(const SolverArgs a, int iteration, int zero, int staged) {
         if (g < G) {
           phi[g] = 0.0f;
           mom[g] = make_float2(0.f, 0.f);
+          if constexpr (D3) momz[g] = 0.0f;
         }
       }
     }
-    float f0 = 0.0f, f1 = 0.0f, f2v = 0.0f;
+    float f0 = 0.0f, f1 = 0.0f, f2v = 0.0f, f3 = 0.0f;
     if (a.fissile[m]) {
       const float* nf = a.nu_sigma_f + (int64_t) m * G;
 #pragma unroll
@@ -907,12 +914,14 @@ ls_sources_kernel(const SolverArgs a, int iteration, int zero, int staged) {
           f0 = fmaf(nf[g], ph[j], f0);
           f1 = fmaf(nf[g], mx[j], f1);
           f2v = fmaf(nf[g], my[j], f2v);
+          if constexpr (D3) f3 = fmaf(nf[g], mz[j], f3);
         }
       }
     }
     f0 = warp_sum_all(f0) * inv_k;
     f1 = warp_sum_all(f1) * inv_k;
     f2v = warp_sum_all(f2v) * inv_k;
+    if constexpr (D3) f3 = warp_sum_all(f3) * inv_k;
     const float* mT = ssT + (int64_t) m * GG + lane;
 #pragma unroll
     for (int js = 0; js < S; js++) {
@@ -923,6 +932,7 @@ ls_sources_kernel(const SolverArgs a, int iteration, int zero, int staged) {
         const float p0 = __shfl_sync(0xffffffffu, ph[js], l);
         const float p1 = __shfl_sync(0xffffffffu, mx[js], l);
         const float p2 = __shfl_sync(0xffffffffu, my[js], l);
+        const float p3 = D3 ? __shfl_sync(0xffffffffu, mz[js], l) : 0.0f;
         const float* c = mT + (int64_t) (gbase + l) * G;
 #pragma unroll
         for (int j = 0; j < S; j++)
@@ -931,13 +941,21 @@ ls_sources_kernel(const SolverArgs a, int iteration, int zero, int staged) {
             s0[j] = fmaf(cf, p0, s0[j]);
             s1[j] = fmaf(cf, p1, s1[j]);
             s2[j] = fmaf(cf, p2, s2[j]);
+            if constexpr (D3) s3[j] = fmaf(cf, p3, s3[j]);
           }
       }
     }
     const float* chi = a.chi + (int64_t) m * G;
     const float* st = a.sigma_t + (int64_t) m * G;
-    const float il0 = a.ls_ilem[3 * r], il1 = a.ls_ilem[3 * r + 1],
-                il2 = a.ls_ilem[3 * r + 2];
+    constexpr int NC = D3 ? 6 : 3;
+    const float il0 = a.ls_ilem[NC * r], il1 = a.ls_ilem[NC * r + 1],
+                il2 = a.ls_ilem[NC * r + 2];
+    float il3 = 0.0f, il4 = 0.0f, il5 = 0.0f;
+    if constexpr (D3) {
+      il3 = a.ls_ilem[6 * r + 3];
+      il4 = a.ls_ilem[6 * r + 4];
+      il5 = a.ls_ilem[6 * r + 5];
+    }
     float2* qxy = reinterpret_cast<float2*>(a.qxy + r * 2 * ld);
     const float2* fxy =
         a.fixed_xy ? reinterpret_cast<const float2*>(a.fixed_xy + r * 2 * ld)
@@ -956,19 +974,31 @@ ls_sources_kernel(const SolverArgs a, int iteration, int zero, int staged) {
       }
       float sx = fmaf(chi[gd], f1, s1[j]);
       float sy = fmaf(chi[gd], f2v, s2[j]);
+      float sz = D3 ? fmaf(chi[gd], f3, s3[j]) : 0.0f;
       if (fxy) {
         const float2 fx = fxy[gd];
         sx += fx.x;
         sy += fx.y;
       }
-      float rx = 0.0f, ry = 0.0f;
+      if (D3 && a.fixed_z) sz += a.fixed_z[r * ld + gd];
+      float rx = 0.0f, ry = 0.0f, rz = 0.0f;
       if (neg_ok || q > 10.0f * kFluxEpsilon || it > 29) {
-        rx = (float) (kOneOverFourPi / 2) * fmaf(il0, sx, il2 * sy);
-        ry = (float) (kOneOverFourPi / 2) * fmaf(il2, sx, il1 * sy);
+        if constexpr (D3) {
+          rx = (float) (kOneOverFourPi / 2) *
+               fmaf(il0, sx, fmaf(il2, sy, il3 * sz));
+          ry = (float) (kOneOverFourPi / 2) *
+               fmaf(il2, sx, fmaf(il1, sy, il4 * sz));
+          rz = (float) (kOneOverFourPi / 2) *
+               fmaf(il3, sx, fmaf(il4, sy, il5 * sz));
+        } else {
+          rx = (float) (kOneOverFourPi / 2) * fmaf(il0, sx, il2 * sy);
+          ry = (float) (kOneOverFourPi / 2) * fmaf(il2, sx, il1 * sy);
+        }
       }
       const float ist = 1.0f / st[gd];
       a.qt[r * ld + gd] = q * ist;
       qxy[gd] = make_float2(rx * ist, ry * ist);
+      if constexpr (D3) a.qz[r * ld + gd] = rz * ist;
     }
   }
   if (negatives) atomicAdd(&a.sc->neg_sources, negatives);
@@ -983,7 +1013,9 @@ ls_sources_kernel(const SolverArgs a, int iteration, int zero, int staged) {
 // add_source_kernel does.  In a pool (a.row_slot set; update = 0) each row
 // follows its solve's negative-flux rule and leaves its FP64 nu-fission
 // term in row_val, as batch_add_source_kernel does.
-template <int S>
+// D3: explicit 3D tracks -- six source constants per group and the z
+// moment (src/CPULSSolver.cpp:824-846).
+template <int S, bool D3>
 __global__ void __launch_bounds__(kRowThreads)
 ls_add_source_kernel(const SolverArgs a, int update) {
   if (skip(a)) return;
@@ -1013,8 +1045,10 @@ ls_add_source_kernel(const SolverArgs a, int update) {
     float2* __restrict__ mom = reinterpret_cast<float2*>(a.mom + r * 2 * ld);
     const float2* __restrict__ qm =
         reinterpret_cast<const float2*>(a.qxy + r * 2 * ld);
-    const float* __restrict__ cst = a.ls_const + r * 3 * ld;
-    float v[S], q[S], o[S], c0[S], c1[S], c2[S];
+    constexpr int NC = D3 ? 6 : 3;
+    const float* __restrict__ cst = a.ls_const + r * NC * ld;
+    float v[S], q[S], o[S], c0[S], c1[S], c2[S], c3[S], c4[S], c5[S];
+    float mzv[S], qzv[S];
     float2 mm[S], qq[S];
 #pragma unroll
     for (int j = 0; j < S; j++) {
@@ -1028,6 +1062,11 @@ ls_add_source_kernel(const SolverArgs a, int update) {
       c0[j] = on ? cst[g] : 0.0f;
       c1[j] = on ? cst[ld + g] : 0.0f;
       c2[j] = on ? cst[2 * ld + g] : 0.0f;
+      c3[j] = (D3 && on) ? cst[3 * ld + g] : 0.0f;
+      c4[j] = (D3 && on) ? cst[4 * ld + g] : 0.0f;
+      c5[j] = (D3 && on) ? cst[5 * ld + g] : 0.0f;
+      mzv[j] = (D3 && on) ? a.momz[r * ld + g] : 0.0f;
+      qzv[j] = (D3 && on) ? a.qz[r * ld + g] : 0.0f;
     }
     float rr = 0.0f;
     int row_neg = 0;
@@ -1041,14 +1080,25 @@ ls_add_source_kernel(const SolverArgs a, int update) {
                                         fmaf(qq[j].x, c0[j], qq[j].y * c2[j]));
       float my = fmaf(mm[j].y, inv, (float) (2 * kFourPi) *
                                         fmaf(qq[j].x, c2[j], qq[j].y * c1[j]));
+      float mz = 0.0f;
+      if constexpr (D3) {
+        // the z terms of the x and y moments, and the z moment
+        mx = fmaf((float) (2 * kFourPi) * qzv[j], c3[j], mx);
+        my = fmaf((float) (2 * kFourPi) * qzv[j], c4[j], my);
+        mz = fmaf(mzv[j], inv,
+                  (float) (2 * kFourPi) *
+                      fmaf(qq[j].x, c3[j], fmaf(qq[j].y, c4[j], qzv[j] * c5[j])));
+      }
       if (x < 0.0f && !neg_ok) {
         x = fmaxf(o[j], kFluxEpsilon);
         mx = 0.0f;
         my = 0.0f;
+        mz = 0.0f;
         row_neg++;
       }
       phi[g] = x;
       mom[g] = make_float2(mx, my);
+      if constexpr (D3) a.momz[r * ld + g] = mz;
       rr = fmaf(nf[g], x, rr);
     }
     if (pool) {
@@ -1094,6 +1144,16 @@ __global__ void ls_scale_moments_kernel(const SolverArgs a) {
     v.z *= f;
     v.w *= f;
     m4[i] = v;
+  }
+  if (a.momz) {
+    float2* z2 = reinterpret_cast<float2*>(a.momz);
+    for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+         i < n / 4; i += (int64_t) gridDim.x * blockDim.x) {
+      float2 v = z2[i];
+      v.x *= f;
+      v.y *= f;
+      z2[i] = v;
+    }
   }
 }
 
@@ -1564,7 +1624,7 @@ void launch_ls_sources_s(const SolverArgs& a, int iteration, int fused,
        15) & ~(size_t) 15;
   const int staged = need <= 160 * 1024;
   const size_t smem = staged ? need : 0;
-  auto kern = ls_sources_kernel<S>;
+  auto kern = a.momz ? ls_sources_kernel<S, true> : ls_sources_kernel<S, false>;
   int64_t blocks = (a.num_fsrs + kWarps - 1) / kWarps;
   if (blocks > 152 * 2) blocks = 152 * 2;
   kern<<<(unsigned) blocks, kThreads, smem, s>>>(a, iteration, fused, staged);
@@ -1572,7 +1632,8 @@ void launch_ls_sources_s(const SolverArgs& a, int iteration, int fused,
 
 template <int S>
 void launch_ls_add_source_s(const SolverArgs& a, int update, cudaStream_t s) {
-  ls_add_source_kernel<S><<<row_grid(a.num_fsrs), kRowThreads, 0, s>>>(a,
+  auto kern = a.momz ? ls_add_source_kernel<S, true> : ls_add_source_kernel<S, false>;
+  kern<<<row_grid(a.num_fsrs), kRowThreads, 0, s>>>(a,
                                                                        update);
 }
 
@@ -1613,11 +1674,16 @@ void configure_sources(int optin) {
   raise_smem_limit(compute_sources_kernel<6>, optin);
   raise_smem_limit(compute_sources_kernel<7>, optin);
   raise_smem_limit(compute_sources_kernel<12>, optin);
-  raise_smem_limit(ls_sources_kernel<1>, optin);
-  raise_smem_limit(ls_sources_kernel<2>, optin);
-  raise_smem_limit(ls_sources_kernel<3>, optin);
-  raise_smem_limit(ls_sources_kernel<4>, optin);
-  raise_smem_limit(ls_sources_kernel<8>, optin);
+  raise_smem_limit(ls_sources_kernel<1, false>, optin);
+  raise_smem_limit(ls_sources_kernel<1, true>, optin);
+  raise_smem_limit(ls_sources_kernel<2, false>, optin);
+  raise_smem_limit(ls_sources_kernel<2, true>, optin);
+  raise_smem_limit(ls_sources_kernel<3, false>, optin);
+  raise_smem_limit(ls_sources_kernel<3, true>, optin);
+  raise_smem_limit(ls_sources_kernel<4, false>, optin);
+  raise_smem_limit(ls_sources_kernel<4, true>, optin);
+  raise_smem_limit(ls_sources_kernel<8, false>, optin);
+  raise_smem_limit(ls_sources_kernel<8, true>, optin);
 }
 
 }  // namespace moc

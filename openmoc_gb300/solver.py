@@ -688,12 +688,16 @@ class GB300LSSolver(GB300Solver):
         self._need_ctx()
         p = self._problem
         arrs = {}
-        for k, dt, n in (("seg_x", np.float32, p.num_segments),
-                         ("seg_y", np.float32, p.num_segments),
-                         ("ang_dir", np.float64, 2 * p.num_angles),
-                         ("ang_wgt", np.float64, p.num_angles),
-                         ("pol_sin", np.float64, p.num_angles * p.num_polar_half),
-                         ("pol_wgt", np.float64, p.num_angles * p.num_polar_half)):
+        keys = [("seg_x", np.float32, p.num_segments),
+                ("seg_y", np.float32, p.num_segments),
+                ("ang_dir", np.float64, 2 * p.num_angles),
+                ("ang_wgt", np.float64, p.num_angles),
+                ("pol_sin", np.float64, p.num_angles * p.num_polar_half),
+                ("pol_wgt", np.float64, p.num_angles * p.num_polar_half)]
+        if p.solve_3d:   # explicit 3D tracks: z starts and cos theta per row
+            keys += [("seg_z", np.float32, p.num_segments),
+                     ("pol_cos", np.float64, p.num_angles)]
+        for k, dt, n in keys:
             if k not in ls:
                 raise _native.MOCError(-1, f"linear-source geometry lacks {k}")
             a = np.ascontiguousarray(ls[k], dt).ravel()
@@ -701,9 +705,9 @@ class GB300LSSolver(GB300Solver):
                 raise _native.MOCError(-1, f"{k} has {a.size} values, expected {n}")
             arrs[k] = a
         self._ls_arrays = arrs
-        g = _native.LSGeometry(*(_ptr(arrs[k]) for k in ("seg_x", "seg_y", "ang_dir",
-                                                          "ang_wgt", "pol_sin",
-                                                          "pol_wgt")))
+        g = _native.LSGeometry(*(_ptr(arrs[k]) if k in arrs else None for k in (
+            "seg_x", "seg_y", "ang_dir", "ang_wgt", "pol_sin", "pol_wgt",
+            "seg_z", "pol_cos")))
         self._call("moc_set_linear_source", C.byref(g))
         self._fixed_moments = {}
 
@@ -768,23 +772,29 @@ class GB300LSSolver(GB300Solver):
         return self._moments("moc_get_source_moments")
 
     def getLinearExpansion(self):
-        """(inverse expansion matrices [R, 3] (xx, yy, xy), source constants
-        [R, 3, G]): getLinearExpansionCoeffsBuffer /
-        getSourceConstantsBuffer."""
+        """(inverse expansion matrices [R, NC], source constants [R, NC, G]):
+        getLinearExpansionCoeffsBuffer / getSourceConstantsBuffer; NC = 3
+        (xx, yy, xy) in 2D, 6 (xx, yy, xy, xz, yz, zz) on 3D tracks."""
         self._need_ctx()
         p = self._problem
-        il = np.empty(3 * p.num_fsrs, np.float64)
-        sc = np.empty(3 * p.num_fsrs * p.num_groups, np.float32)
+        nc = 6 if p.solve_3d else 3
+        il = np.empty(nc * p.num_fsrs, np.float64)
+        sc = np.empty(nc * p.num_fsrs * p.num_groups, np.float32)
         self._call("moc_get_linear_expansion", _ptr(il), _ptr(sc))
-        return il.reshape(p.num_fsrs, 3), sc.reshape(p.num_fsrs, 3, p.num_groups)
+        return il.reshape(p.num_fsrs, nc), sc.reshape(p.num_fsrs, nc, p.num_groups)
 
     def getFluxByPosition(self, fsr_id: int, dx: float, dy: float,
-                          group: int) -> float:
-        """The linear flux at offset (dx, dy) from the FSR's centroid:
+                          group: int, dz: float = 0.0) -> float:
+        """The linear flux at offset (dx, dy[, dz]) from the FSR's centroid:
         CPULSSolver::getFluxByCoords (src/CPULSSolver.cpp:1082-1133) with the
         point given relative to the centroid."""
         il, _ = self.getLinearExpansion()
         m = self.getFluxMoments()[fsr_id, :, group - 1]
         flat = float(self.getFluxes()[fsr_id, group - 1])
-        a, b, c = il[fsr_id]
-        return flat + dx * (a * m[0] + c * m[1]) + dy * (c * m[0] + b * m[1])
+        if il.shape[1] == 3:
+            a, b, c = il[fsr_id]
+            return flat + dx * (a * m[0] + c * m[1]) + dy * (c * m[0] + b * m[1])
+        xx, yy, xy, xz, yz, zz = il[fsr_id]
+        return (flat + dx * (xx * m[0] + xy * m[1] + xz * m[2])
+                + dy * (xy * m[0] + yy * m[1] + yz * m[2])
+                + dz * (xz * m[0] + yz * m[1] + zz * m[2]))

@@ -10,7 +10,10 @@ and the linear-source oracle.
     test_fixed_linear_source);
   * hook by hook from OpenMOC's converged state;
   * generated lattices against the oracle at fixed iteration counts, for
-    every sweep shape (lanes per track direction x group pairs per lane).
+    every sweep shape (lanes per track direction x group pairs per lane);
+  * explicit 3D tracks (x, y and z moments, six expansion coefficients):
+    OpenMOC's 3D CPULSSolver fixture, its constants and its solve for every
+    sweep shape, and the FP64 oracle at a fixed iteration count.
 """
 import json
 import os
@@ -18,7 +21,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, LS_CASES, LS_PROBE_CASES, load_case, ls_arrays
+from conftest import GOLDEN, LS_CASES, LS_CASES_3D, LS_PROBE_CASES, load_case, ls_arrays
 from oracle.oracle import LSOracle
 
 pytestmark = pytest.mark.gpu
@@ -233,4 +236,59 @@ def test_gpu_ls_uses_native_library():
     n0 = s.getLaunchCount()
     s.computeEigenvalue(3, 1)
     assert s.getLaunchCount() > n0 + 3 * 4
+    s.close()
+
+
+@pytest.mark.parametrize("case", LS_CASES_3D)
+def test_gpu_ls_3d_constants_match_openmoc(case):
+    s, p, _, arr = _solver(case, "f64")
+    assert s.getNumFlatSourceRegions() == 0
+    il, cst = s.getLinearExpansion()
+    R, G = p.num_fsrs, p.num_groups
+    assert il.shape == (R, 6) and cst.shape == (R, 6, G)
+    assert _peak(il, arr["ls_ilem"].reshape(R, 6)) < 2e-6
+    assert _peak(cst, arr["ls_src_constants"].reshape(R, 6, G)) < 1e-5
+    s.close()
+
+
+@pytest.mark.parametrize("case", LS_CASES_3D)
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+@pytest.mark.parametrize("shape", [None, (1, 4), (2, 2), (4, 1), (8, 1)])
+def test_gpu_ls_3d_solve_matches_openmoc(case, precision, shape):
+    """CPULSSolver on explicit 3D tracks through the 3D linear-source sweep
+    (autotuned, then every shape for 7 groups) against OpenMOC FP32 / FP64:
+    iterations, keff 1e-5, fluxes 1e-4, x / y / z moments 5e-4 of the
+    peak."""
+    s, p, sc, arr = _solver(case, precision)
+    if shape:
+        s.setSweepShape(*shape)
+    _solve(s, sc)
+    assert abs(s.getNumIterations() - int(sc["iterations"])) <= 1
+    assert abs(s.getKeff() - sc["keff"]) < 1e-5
+    R, G = p.num_fsrs, p.num_groups
+    assert _rel(s.getFluxes(), arr["flux"].reshape(R, G), 1e-4) < 1e-4
+    mom = s.getFluxMoments()
+    ref = arr["ls_moments"].reshape(R, 3, G)
+    assert _peak(mom, ref) < 5e-4
+    assert np.abs(mom[:, 2, :]).max() > 0.1 * np.abs(ref[:, 2, :]).max()
+    s.close()
+
+
+def test_gpu_ls_3d_matches_oracle_at_fixed_iterations():
+    """The 3D fixture's problem for 10 eigenvalue iterations against the
+    FP64 oracle (no convergence test in between): keff, fluxes and the
+    three moments."""
+    from openmoc_gb300 import GB300LSSolver
+    p, _, arr = load_case("pin3d_ls", "f32")
+    iters = 10
+    o = LSOracle(p, ls_arrays(arr), "f64", num_threads=8)
+    o.compute_eigenvalue(iters, 1, 1e-30)
+    s = GB300LSSolver(p, device=0)
+    s.setConvergenceThreshold(1e-30)
+    s.computeEigenvalue(iters, 1)
+    R, G = p.num_fsrs, p.num_groups
+    assert s.getNumIterations() == iters
+    assert abs(s.getKeff() - o.keff) < 2e-6
+    assert _rel(s.getFluxes(), o.phi.reshape(R, G), 1e-4) < 2e-5
+    assert _peak(s.getFluxMoments(), o.mom.reshape(R, 3, G)) < 1e-4
     s.close()
