@@ -41,6 +41,11 @@ FLOPS_PER_INTEGRATION_3D = 28  # 3D: no 1/sin(theta) scaling
 # F1/F2/H from it, the flat and linear source terms, the update and the
 # scalar-flux and x/y moment tallies, per (segment, group, polar)
 FLOPS_PER_LS_INTEGRATION = 48
+# linear source on explicit 3D tracks, per (segment, group): the same
+# attenuation (44) with no polar angles to share the per-segment terms
+# (optical length, flat and linear source with z, 12) and x / y / z moment
+# tallies (11) -- counted from the 3D sweep instances
+FLOPS_PER_LS_INTEGRATION_3D = 68
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one sweep launch
 # of this workload, from one ncu capture per sweep shape (lanes per track
 # direction, group pairs per lane, exponential kind); the summaries are under
@@ -80,19 +85,21 @@ def load_peaks():
 
 def algorithmic_bytes(p, ls=False, otf=False):
     """Compulsory HBM bytes of one sweep: packed segments read once (8 B;
-    16 B with the linear source's start position), per-track
-    offsets/links/flags (16 B), angular flux in and out for both directions
-    (16 B per track and flux value), sources read and tallies written (8 B
-    per FSR and group; 24 B with the x / y source and flux moments)."""
+    16 B with the linear source's start position, 20 B with its z on 3D
+    tracks), per-track offsets/links/flags (16 B), angular flux in and out
+    for both directions (16 B per track and flux value), sources read and
+    tallies written (8 B per FSR and group; 24 B with the x / y source and
+    flux moments, 32 B with z)."""
     F = p.fluxes_per_track
+    ls3d = ls and bool(p.solve_3d)
     if otf:
         # a 32-byte description per 3D track and the radial segments (12 B)
         # instead of the stored 3D segments
         seg = 32 * p.num_tracks + 12 * p.otf["rad_len"].size
     else:
-        seg = (16 if ls else 8) * p.num_segments
+        seg = (20 if ls3d else 16 if ls else 8) * p.num_segments
     return (seg + 16 * p.num_tracks + 16 * p.num_tracks * F
-            + (24 if ls else 8) * p.num_fsrs * p.num_groups)
+            + (32 if ls3d else 24 if ls else 8) * p.num_fsrs * p.num_groups)
 
 
 class Clocks:
@@ -163,6 +170,9 @@ WORKLOADS = {
                   "7 groups, explicit 3D tracks: 16 azimuthal, 6 polar, 0.1 cm radial, "
                   "0.5 cm axial; reflective radially, vacuum top and bottom",
     "assembly70_ls": WORKLOAD + ", linear source (CPULSSolver)",
+    "assembly3d_ls": "17x17 assembly extruded to 20 cm (fuel below 16 cm, moderator above), "
+                     "7 groups, explicit 3D tracks: 16 azimuthal, 6 polar, 0.1 cm radial, "
+                     "0.5 cm axial; linear source (CPULSSolver, x / y / z moments)",
     "assembly3d_otf": "17x17 assembly extruded to 20 cm (fuel below 16 cm, moderator above), "
                       "7 groups, 16 azimuthal, 6 polar, 0.1 cm radial, 0.5 cm axial; 3D "
                       "tracks cut from the radial segments during the sweep (on-the-fly)",
@@ -181,6 +191,8 @@ def build_problem(workload="assembly70"):
         return lattice.assembly_17x17_3d()
     if workload == "assembly70_ls":
         return lattice.assembly_17x17(linear_source=True)
+    if workload == "assembly3d_ls":
+        return lattice.assembly_17x17_3d(linear_source=True)
     return lattice.assembly_17x17()
 
 
@@ -424,7 +436,8 @@ def run_gpu(args):
     sm_mhz = clocks.get("sm_mhz") or float(peaks.get("sm_max_mhz", 2070.0))
     props = torch.cuda.get_device_properties(local)
     fp32_peak = props.multi_processor_count * 128 * 2 * sm_mhz * 1e6 / 1e12
-    flops_per_int = (FLOPS_PER_LS_INTEGRATION if ls else
+    flops_per_int = ((FLOPS_PER_LS_INTEGRATION_3D if p.solve_3d else
+                      FLOPS_PER_LS_INTEGRATION) if ls else
                      FLOPS_PER_INTEGRATION_3D if p.solve_3d else FLOPS_PER_INTEGRATION)
     fp32_achieved = ints * flops_per_int / (sweep_avg * 1e-3) / 1e12
 

@@ -97,6 +97,15 @@ int moc_lattice_extrude(const moc_lattice* radial, double height,
 /** Start and end point of every 3D track of an extruded lattice, [T][6]
  *  (x0, y0, z0, x1, y1, z1). */
 int moc_lattice_export_ends3d(moc_lattice* lat, double* ends);
+/** Linear-source geometry of an extruded 3D lattice (moc_ls_geometry's 3D
+ *  arrays): each segment's start relative to its FSR centroid (seg_x,
+ *  seg_y, seg_z [S]), the centroids [R][3] (CentroidGenerator's 3D
+ *  branch), per angle row cos / sin phi [A][2], azimuthal spacing x weight
+ *  [A], sin / cos theta [A] and polar spacing x weight [A]. */
+int moc_lattice_export_ls3d(moc_lattice* lat, float* seg_x, float* seg_y,
+                            float* seg_z, double* centroid, double* ang_dir,
+                            double* ang_wgt, double* pol_sin, double* pol_cos,
+                            double* pol_wgt);
 
 /** On-the-fly description of an extruded lattice's 3D tracks (the arrays
  *  of moc_otf_tracks in openmoc_gb300.h): per 3D track [T][4] (radial

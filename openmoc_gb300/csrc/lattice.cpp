@@ -1084,12 +1084,20 @@ extern "C" int moc_lattice_extrude(const moc_lattice* L2, double height,
   L->inv_sin.assign(nrows, 1.0f);
   L->otf_ang.resize(4 * (size_t) nrows);
   std::vector<double> wrow(nrows);
+  L->row_phi.resize(nrows);
+  L->row_theta.resize(nrows);
+  L->row_azw.resize(nrows);
+  L->row_polw.resize(nrows);
   for (int rr = 0; rr < nrows; rr++) {
     const int a = rr / P;
     const double th = theta[rr];
     const double dp = dz_eff[rr] * std::sin(th);   // polar spacing
     wrow[rr] = 2.0 * kPi * L2->az_weight[a] * L2->az_spacing[a] * wpol[rr] * dp;
     L->weights[rr] = (float) wrow[rr];
+    L->row_phi[rr] = L2->tracks[first[a]].phi;
+    L->row_theta[rr] = th;
+    L->row_azw[rr] = L2->az_spacing[a] * L2->az_weight[a];
+    L->row_polw[rr] = dp * wpol[rr];
     const double c = std::cos(th) / std::sin(th);
     L->otf_ang[4 * rr + 0] = (float) c;
     L->otf_ang[4 * rr + 1] = (float) (1.0 / c);
@@ -1134,6 +1142,74 @@ extern "C" int moc_lattice_extrude(const moc_lattice* L2, double height,
     e[3] = pc.x1; e[4] = pc.y1; e[5] = pc.z1;
   }
   *out = L;
+  return 0;
+}
+
+// Linear-source geometry of an extruded 3D lattice (the explicit 3D
+// branches of CentroidGenerator::onTrack and RecenterSegments,
+// src/TrackTraversingAlgorithms.cpp:377-460, :1320-1331): FSR centroids as
+// the segment midpoints weighted by length and w_a d_a w_p d_p over the FSR
+// volume, each segment's start walked from its 3D track's start along
+// (cos phi sin theta, sin phi sin theta, cos theta) and taken relative to
+// its FSR's centroid; per angle row cos / sin phi, w_a d_a, sin / cos theta
+// and w_p d_p.
+extern "C" int moc_lattice_export_ls3d(moc_lattice* L, float* seg_x,
+                                       float* seg_y, float* seg_z,
+                                       double* centroid, double* ang_dir,
+                                       double* ang_wgt, double* pol_sin,
+                                       double* pol_cos, double* pol_wgt) {
+  if (!L) return lat_fail("null lattice");
+  if ((int64_t) L->tracks3d.size() != 6 * L->T ||
+      (int64_t) L->row_theta.size() != L->A)
+    return lat_fail("not an extruded 3D lattice");
+  if (!seg_x || !seg_y || !seg_z || !centroid || !ang_dir || !ang_wgt ||
+      !pol_sin || !pol_cos || !pol_wgt)
+    return lat_fail("null output array");
+  const int64_t T = L->T, R = L->R;
+  std::vector<double> dx(L->A), dy(L->A), dz(L->A), w(L->A);
+  for (int rr = 0; rr < L->A; rr++) {
+    const double sth = std::sin(L->row_theta[rr]);
+    dx[rr] = std::cos(L->row_phi[rr]) * sth;
+    dy[rr] = std::sin(L->row_phi[rr]) * sth;
+    dz[rr] = std::cos(L->row_theta[rr]);
+    w[rr] = L->row_azw[rr] * L->row_polw[rr];
+    ang_dir[2 * rr] = std::cos(L->row_phi[rr]);
+    ang_dir[2 * rr + 1] = std::sin(L->row_phi[rr]);
+    ang_wgt[rr] = L->row_azw[rr];
+    pol_sin[rr] = sth;
+    pol_cos[rr] = dz[rr];
+    pol_wgt[rr] = L->row_polw[rr];
+  }
+  std::vector<double> cx(R, 0.0), cy(R, 0.0), cz(R, 0.0);
+  for (int pass = 0; pass < 2; pass++) {
+    for (int64_t t = 0; t < T; t++) {
+      const int rr = L->track_ang[t];
+      const double* e = L->tracks3d.data() + 6 * t;
+      double x = e[0], y = e[1], z = e[2];
+      for (int64_t k = L->seg_off[t]; k < L->seg_off[t + 1]; k++) {
+        const int32_t r = L->seg_fsr[k];
+        const double l = (double) L->seg_len[k];
+        if (pass == 0) {
+          const double v = (double) L->fsr_vol[r];
+          cx[r] += w[rr] * (x + dx[rr] * l / 2.0) * l / v;
+          cy[r] += w[rr] * (y + dy[rr] * l / 2.0) * l / v;
+          cz[r] += w[rr] * (z + dz[rr] * l / 2.0) * l / v;
+        } else {
+          seg_x[k] = (float) (x - cx[r]);
+          seg_y[k] = (float) (y - cy[r]);
+          seg_z[k] = (float) (z - cz[r]);
+        }
+        x += dx[rr] * l;
+        y += dy[rr] * l;
+        z += dz[rr] * l;
+      }
+    }
+  }
+  for (int64_t r = 0; r < R; r++) {
+    centroid[3 * r] = cx[r];
+    centroid[3 * r + 1] = cy[r];
+    centroid[3 * r + 2] = cz[r];
+  }
   return 0;
 }
 

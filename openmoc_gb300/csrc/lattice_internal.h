@@ -81,8 +81,11 @@ struct moc_lattice {
   std::vector<int32_t> rad_fsr;
   std::vector<int64_t> rad_off;
   int32_t above_fsr = -1;
-  // Extruded 3D lattices: each 3D track's start and end points [T][6]
+  // Extruded 3D lattices: each 3D track's start and end points [T][6], and
+  // per angle row phi, theta, azimuthal spacing x weight and polar spacing
+  // x weight (for the linear-source geometry)
   std::vector<double> tracks3d;
+  std::vector<double> row_phi, row_theta, row_azw, row_polw;
   // 2D lattices: the lattice cell of every FSR (row 0 at the top, as the
   // FSR keys number them) and the lattice's placement, for CMFD meshes
   std::vector<int32_t> fsr_pin;

@@ -103,144 +103,84 @@ __global__ void ls_bucket_kernel(const int4* segs, int64_t S,
   }
 }
 
-// One warp per FSR over its own segments, lanes over groups (S_ groups per
-// lane, G <= 32 S_), sums in FP64 registers: no atomics.  Writes the inverse
-// expansion matrix and the source constants of the FSR.
-template <int S_>
-__global__ void ls_constants_kernel(const int4* segs, const int32_t* list,
-                                    const int64_t* start,
-                                    const int32_t* seg_track,
-                                    const int32_t* track_ang,
-                                    const double* ang_dir,
-                                    const double* ang_wgt,
-                                    const double* pol_sin,
-                                    const double* pol_wgt, int Ph,
-                                    const float* sigma_t, const float* fsr_vol,
-                                    const int32_t* fsr_mat, int64_t R, int G,
-                                    int ld, float* ilem, float* cst,
-                                    unsigned int* num_flat) {
+// The expansion moments and source constants, summed over each FSR's
+// segments in FP64.  The segments are bucketed by FSR; warp w takes list
+// entries [w * chunk, (w + 1) * chunk) -- equal shares of segments,
+// whatever the FSRs' sizes (one region crossed by most tracks, as the
+// moderator above a 3D assembly, would leave one warp walking millions of
+// segments) -- with lanes over groups (S_ groups per lane, G <= 32 S_).  A
+// warp sums its run of an FSR in registers and adds it to the FP64 totals
+// lem[R][NC] and acc[R][NC][ld] with FP64 atomics where the FSR changes.
+// NC = 3 in 2D (xx, yy, xy; the polar loop of the 2D branch), 6 on 3D
+// tracks (xx, yy, xy, xz, yz, zz; the row's 3D direction and weight
+// w_a d_a w_p d_p, G2 at the segment's own optical length).
+template <int S_, bool D3>
+__global__ void ls_moments_kernel(const int4* segs, const float* seg_z,
+                                  const int32_t* list, int64_t S, int chunk,
+                                  const int32_t* seg_track,
+                                  const int32_t* track_ang,
+                                  const double* ang_dir, const double* ang_wgt,
+                                  const double* pol_sin, const double* pol_wgt,
+                                  const double* pol_cos, int Ph,
+                                  const float* sigma_t, const float* fsr_vol,
+                                  const int32_t* fsr_mat, int G, int ld,
+                                  double* lem, double* acc) {
+  constexpr int NC = D3 ? 6 : 3;
   const int lane = threadIdx.x & 31;
-  const int64_t warps = ((int64_t) gridDim.x * blockDim.x) >> 5;
-  for (int64_t r = ((int64_t) blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-       r < R; r += warps) {
-    double l0 = 0.0, l1 = 0.0, l2 = 0.0;
-    double a0[S_], a1[S_], a2[S_];
-    float st[S_];
-    const int m = fsr_mat[r];
+  const int64_t warp = ((int64_t) blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t e0 = warp * chunk;
+  if (e0 >= S) return;
+  const int64_t e1 = (e0 + chunk < S) ? e0 + chunk : S;
+  double l[NC], c[NC][S_];
+  float st[S_];
+  int cur = -1;
+  double vol = 1.0;
+  auto flush = [&]() {
+    if (lane == 0)
+      for (int i = 0; i < NC; i++) atomicAdd(lem + (int64_t) cur * NC + i, l[i]);
 #pragma unroll
     for (int j = 0; j < S_; j++) {
       const int g = lane + 32 * j;
-      a0[j] = a1[j] = a2[j] = 0.0;
-      st[j] = (g < G) ? sigma_t[(int64_t) m * G + g] : 0.0f;
+      if (g < G)
+#pragma unroll
+        for (int i = 0; i < NC; i++)
+          atomicAdd(acc + ((int64_t) cur * NC + i) * ld + g, c[i][j]);
     }
-    const double vol = (double) fsr_vol[r];
-    for (int64_t e = start[r]; e < start[r + 1]; e++) {
-      const int k = list[e];
-      const int4 w = segs[k];
-      const int a = track_ang[seg_track[k]];
-      const double cph = ang_dir[2 * a], sph = ang_dir[2 * a + 1];
-      const double len = (double) __int_as_float(w.x);
-      const double xc = (double) __int_as_float(w.z) + 0.5 * len * cph;
-      const double yc = (double) __int_as_float(w.w) + 0.5 * len * sph;
-      const double vi = ang_wgt[a] * len / vol;
-      const double l12 = len * len / 12.0;
-      l0 += vi * (xc * xc + cph * cph * l12);
-      l1 += vi * (yc * yc + sph * sph * l12);
-      l2 += vi * (xc * yc + sph * cph * l12);
-      // per group: sum_p l G2(l sigma_t / sin_p) (vi l / 2) 2 w_p sin_p
-      const double k2f = len * vi * len / 2.0;
-      const float lenf = __int_as_float(w.x);
+  };
+  for (int64_t e = e0; e < e1; e++) {
+    const int k = list[e];
+    const int4 w = segs[k];
+    const int r = w.y & 0xFFFFFF;
+    if (r != cur) {
+      if (cur >= 0) flush();
+      cur = r;
+      vol = (double) fsr_vol[r];
+      const int m = fsr_mat[r];
+#pragma unroll
+      for (int i = 0; i < NC; i++) {
+        l[i] = 0.0;
+#pragma unroll
+        for (int j = 0; j < S_; j++) c[i][j] = 0.0;
+      }
 #pragma unroll
       for (int j = 0; j < S_; j++) {
-        const float tau = lenf * st[j];
-        float k2 = 0.0f;
-        for (int p = 0; p < Ph; p++) {
-          const float sn = (float) pol_sin[a * Ph + p];
-          k2 = fmaf(ls_exp_g2(tau / sn), (float) (2.0 * pol_wgt[a * Ph + p]) * sn,
-                    k2);
-        }
-        const double kk = k2f * (double) k2;
-        a0[j] += vi * xc * xc + cph * cph * kk;
-        a1[j] += vi * yc * yc + sph * sph * kk;
-        a2[j] += vi * xc * yc + sph * cph * kk;
+        const int g = lane + 32 * j;
+        st[j] = (g < G) ? sigma_t[(int64_t) m * G + g] : 0.0f;
       }
     }
-    if (lane == 0) {
-      const double det = l0 * l1 - l2 * l2;
-      if (fabs(det) < kMinDet) {
-        ilem[3 * r] = ilem[3 * r + 1] = ilem[3 * r + 2] = 0.0f;
-        atomicAdd(num_flat, 1u);
-      } else {
-        ilem[3 * r] = (float) (l1 / det);
-        ilem[3 * r + 1] = (float) (l0 / det);
-        ilem[3 * r + 2] = (float) (-l2 / det);
-      }
-    }
-#pragma unroll
-    for (int j = 0; j < S_; j++) {
-      const int g = lane + 32 * j;
-      if (g < ld) {
-        const bool on = g < G;
-        cst[(r * 3 + 0) * ld + g] = on ? (float) a0[j] : 0.0f;
-        cst[(r * 3 + 1) * ld + g] = on ? (float) a1[j] : 0.0f;
-        cst[(r * 3 + 2) * ld + g] = on ? (float) a2[j] : 0.0f;
-      }
-    }
-  }
-}
-
-// The 3D branch (src/TrackTraversingAlgorithms.cpp:680-781): the row's
-// direction (cos phi sin theta, sin phi sin theta, cos theta) and weight
-// w_a d_a w_p d_p, G2 at the segment's own optical length (no polar loop),
-// six moments (xx, yy, xy, xz, yz, zz) and the 3x3 inverse; flat where the
-// determinant is below 1e-10 or the volume below 1e-6.
-template <int S_>
-__global__ void ls_constants3d_kernel(const int4* segs, const float* seg_z,
-                                      const int32_t* list,
-                                      const int64_t* start,
-                                      const int32_t* seg_track,
-                                      const int32_t* track_ang,
-                                      const double* ang_dir,
-                                      const double* ang_wgt,
-                                      const double* pol_sin,
-                                      const double* pol_wgt,
-                                      const double* pol_cos,
-                                      const float* sigma_t,
-                                      const float* fsr_vol,
-                                      const int32_t* fsr_mat, int64_t R, int G,
-                                      int ld, float* ilem, float* cst,
-                                      unsigned int* num_flat) {
-  const int lane = threadIdx.x & 31;
-  const int64_t warps = ((int64_t) gridDim.x * blockDim.x) >> 5;
-  for (int64_t r = ((int64_t) blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-       r < R; r += warps) {
-    double l[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    double c[6][S_];
-    float st[S_];
-    const int m = fsr_mat[r];
-#pragma unroll
-    for (int j = 0; j < S_; j++) {
-      const int g = lane + 32 * j;
-#pragma unroll
-      for (int i = 0; i < 6; i++) c[i][j] = 0.0;
-      st[j] = (g < G) ? sigma_t[(int64_t) m * G + g] : 0.0f;
-    }
-    const double vol = (double) fsr_vol[r];
-    for (int64_t e = start[r]; e < start[r + 1]; e++) {
-      const int k = list[e];
-      const int4 w = segs[k];
-      const int a = track_ang[seg_track[k]];
-      const double cph = ang_dir[2 * a], sph = ang_dir[2 * a + 1];
+    const int a = track_ang[seg_track[k]];
+    const double cph = ang_dir[2 * a], sph = ang_dir[2 * a + 1];
+    const float lenf = __int_as_float(w.x);
+    const double len = (double) lenf;
+    const double l12 = len * len / 12.0;
+    if constexpr (D3) {
       const double sth = pol_sin[a], cth = pol_cos[a];
       const double wgt = ang_wgt[a] * pol_wgt[a];
-      const float lenf = __int_as_float(w.x);
-      const double len = (double) lenf;
       const double xc = (double) __int_as_float(w.z) + len * 0.5 * cph * sth;
       const double yc = (double) __int_as_float(w.w) + len * 0.5 * sph * sth;
       const double zc = (double) seg_z[k] + len * 0.5 * cth;
       const double vi = wgt * len / vol;
       const double half = vi * len / 2.0;
-      const double l12 = len * len / 12.0;
       l[0] += vi * (xc * xc + cph * cph * sth * sth * l12);
       l[1] += vi * (yc * yc + sph * sph * sth * sth * l12);
       l[2] += vi * (xc * yc + sph * cph * sth * sth * l12);
@@ -257,32 +197,78 @@ __global__ void ls_constants3d_kernel(const int4* segs, const float* seg_z,
         c[4][j] += vi * yc * zc + sph * cth * g2 * sth;
         c[5][j] += vi * zc * zc + cth * cth * g2;
       }
+    } else {
+      const double xc = (double) __int_as_float(w.z) + 0.5 * len * cph;
+      const double yc = (double) __int_as_float(w.w) + 0.5 * len * sph;
+      const double vi = ang_wgt[a] * len / vol;
+      l[0] += vi * (xc * xc + cph * cph * l12);
+      l[1] += vi * (yc * yc + sph * sph * l12);
+      l[2] += vi * (xc * yc + sph * cph * l12);
+      // per group: sum_p l G2(l sigma_t / sin_p) (vi l / 2) 2 w_p sin_p
+      const double k2f = len * vi * len / 2.0;
+#pragma unroll
+      for (int j = 0; j < S_; j++) {
+        const float tau = lenf * st[j];
+        float k2 = 0.0f;
+        for (int p = 0; p < Ph; p++) {
+          const float sn = (float) pol_sin[a * Ph + p];
+          k2 = fmaf(ls_exp_g2(tau / sn), (float) (2.0 * pol_wgt[a * Ph + p]) * sn,
+                    k2);
+        }
+        const double kk = k2f * (double) k2;
+        c[0][j] += vi * xc * xc + cph * cph * kk;
+        c[1][j] += vi * yc * yc + sph * sph * kk;
+        c[2][j] += vi * xc * yc + sph * cph * kk;
+      }
     }
-    if (lane == 0) {
-      const double det = l[0] * l[1] * l[5] + l[2] * l[4] * l[3] +
-                         l[3] * l[2] * l[4] - l[0] * l[4] * l[4] -
-                         l[3] * l[1] * l[3] - l[2] * l[2] * l[5];
-      float* il = ilem + 6 * r;
-      if (fabs(det) < kMinDet || vol < 1e-6) {
+  }
+  if (cur >= 0) flush();
+}
+
+// The inverse expansion matrix of every FSR from its FP64 moments (2x2, or
+// 3x3 on 3D tracks; zeros -- a flat source -- where the determinant is
+// below 1e-10, or in 3D the volume below 1e-6), and the source constants
+// rounded to FP32 (zero in the padding groups).
+template <bool D3>
+__global__ void ls_finish_kernel(const double* lem, const double* acc,
+                                 const float* fsr_vol, int64_t R, int G,
+                                 int ld, float* ilem, float* cst,
+                                 unsigned int* num_flat) {
+  constexpr int NC = D3 ? 6 : 3;
+  const int64_t n = R * NC * ld;
+  for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t) gridDim.x * blockDim.x) {
+    const int g = (int) (i % ld);
+    cst[i] = (g < G) ? (float) acc[i] : 0.0f;
+  }
+  for (int64_t r = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; r < R;
+       r += (int64_t) gridDim.x * blockDim.x) {
+    const double* m = lem + r * NC;
+    float* il = ilem + r * NC;
+    if constexpr (D3) {
+      const double det = m[0] * m[1] * m[5] + m[2] * m[4] * m[3] +
+                         m[3] * m[2] * m[4] - m[0] * m[4] * m[4] -
+                         m[3] * m[1] * m[3] - m[2] * m[2] * m[5];
+      if (fabs(det) < kMinDet || (double) fsr_vol[r] < 1e-6) {
         for (int i = 0; i < 6; i++) il[i] = 0.0f;
         atomicAdd(num_flat, 1u);
       } else {
-        il[0] = (float) ((l[1] * l[5] - l[4] * l[4]) / det);
-        il[1] = (float) ((l[0] * l[5] - l[3] * l[3]) / det);
-        il[2] = (float) ((l[3] * l[4] - l[2] * l[5]) / det);
-        il[3] = (float) ((l[2] * l[4] - l[3] * l[1]) / det);
-        il[4] = (float) ((l[3] * l[2] - l[0] * l[4]) / det);
-        il[5] = (float) ((l[0] * l[1] - l[2] * l[2]) / det);
+        il[0] = (float) ((m[1] * m[5] - m[4] * m[4]) / det);
+        il[1] = (float) ((m[0] * m[5] - m[3] * m[3]) / det);
+        il[2] = (float) ((m[3] * m[4] - m[2] * m[5]) / det);
+        il[3] = (float) ((m[2] * m[4] - m[3] * m[1]) / det);
+        il[4] = (float) ((m[3] * m[2] - m[0] * m[4]) / det);
+        il[5] = (float) ((m[0] * m[1] - m[2] * m[2]) / det);
       }
-    }
-#pragma unroll
-    for (int j = 0; j < S_; j++) {
-      const int g = lane + 32 * j;
-      if (g < ld) {
-        const bool on = g < G;
-#pragma unroll
-        for (int i = 0; i < 6; i++)
-          cst[(r * 6 + i) * ld + g] = on ? (float) c[i][j] : 0.0f;
+    } else {
+      const double det = m[0] * m[1] - m[2] * m[2];
+      if (fabs(det) < kMinDet) {
+        il[0] = il[1] = il[2] = 0.0f;
+        atomicAdd(num_flat, 1u);
+      } else {
+        il[0] = (float) (m[1] / det);
+        il[1] = (float) (m[0] / det);
+        il[2] = (float) (-m[2] / det);
       }
     }
   }
@@ -323,9 +309,13 @@ void launch_ls_seg_track(const int64_t* seg_off, int64_t T, int32_t* seg_track,
       seg_off, T, seg_track);
 }
 
+int64_t ls_constants_scratch(int64_t R, int ld, bool d3) {
+  const int64_t nc = d3 ? 6 : 3;
+  return R * nc * (1 + (int64_t) ld);
+}
+
 void launch_ls_constants_bucketed(const int4* segs_ls, const int32_t* list,
-                                  const int64_t* start,
-                                  const int32_t* seg_track,
+                                  int64_t S, const int32_t* seg_track,
                                   const int32_t* track_ang,
                                   const double* ang_dir, const double* ang_wgt,
                                   const double* pol_sin, const double* pol_wgt,
@@ -333,38 +323,48 @@ void launch_ls_constants_bucketed(const int4* segs_ls, const int32_t* list,
                                   const float* fsr_vol, const int32_t* fsr_mat,
                                   int64_t R, int G, int ld, float* ilem,
                                   float* cst, unsigned int* num_flat,
-                                  cudaStream_t s, const float* seg_z,
-                                  const double* pol_cos) {
-  const unsigned blocks = (unsigned) grid_for(32 * R, 256);
-  if (seg_z) {
-#define MOC_LS_CONST3(SS)                                                     \
-  ls_constants3d_kernel<SS><<<blocks, 256, 0, s>>>(                           \
-      segs_ls, seg_z, list, start, seg_track, track_ang, ang_dir, ang_wgt,    \
-      pol_sin, pol_wgt, pol_cos, sigma_t, fsr_vol, fsr_mat, R, G, ld, ilem,   \
-      cst, num_flat)
-    switch ((ld + 31) / 32) {
-      case 1: MOC_LS_CONST3(1); break;
-      case 2: MOC_LS_CONST3(2); break;
-      case 3: MOC_LS_CONST3(3); break;
-      case 4: MOC_LS_CONST3(4); break;
-      default: MOC_LS_CONST3(8); break;
+                                  double* scratch, cudaStream_t s,
+                                  const float* seg_z, const double* pol_cos) {
+  const bool d3 = seg_z != nullptr;
+  const int64_t nc = d3 ? 6 : 3;
+  double* lem = scratch;
+  double* acc = scratch + R * nc;
+  cudaMemsetAsync(scratch, 0, sizeof(double) * ls_constants_scratch(R, ld, d3),
+                  s);
+  // about 48 warps per SM, at least 32 segments each
+  int64_t chunk = (S + 152 * 48 - 1) / (152 * 48);
+  if (chunk < 32) chunk = 32;
+  const int64_t warps = (S + chunk - 1) / chunk;
+  if (warps > 0) {
+    const unsigned blocks = (unsigned) ((warps * 32 + 255) / 256);
+#define MOC_LS_MOM(SS, D)                                                     \
+  ls_moments_kernel<SS, D><<<blocks, 256, 0, s>>>(                            \
+      segs_ls, seg_z, list, S, (int) chunk, seg_track, track_ang, ang_dir,    \
+      ang_wgt, pol_sin, pol_wgt, pol_cos, Ph, sigma_t, fsr_vol, fsr_mat, G,   \
+      ld, lem, acc)
+#define MOC_LS_MOM_S(D)                   \
+    switch ((ld + 31) / 32) {             \
+      case 1: MOC_LS_MOM(1, D); break;    \
+      case 2: MOC_LS_MOM(2, D); break;    \
+      case 3: MOC_LS_MOM(3, D); break;    \
+      case 4: MOC_LS_MOM(4, D); break;    \
+      default: MOC_LS_MOM(8, D); break;   \
     }
-#undef MOC_LS_CONST3
-    return;
+    if (d3) {
+      MOC_LS_MOM_S(true)
+    } else {
+      MOC_LS_MOM_S(false)
+    }
+#undef MOC_LS_MOM_S
+#undef MOC_LS_MOM
   }
-#define MOC_LS_CONST(SS)                                                    \
-  ls_constants_kernel<SS><<<blocks, 256, 0, s>>>(                           \
-      segs_ls, list, start, seg_track, track_ang, ang_dir, ang_wgt,         \
-      pol_sin, pol_wgt, Ph, sigma_t, fsr_vol, fsr_mat, R, G, ld, ilem, cst, \
-      num_flat)
-  switch ((ld + 31) / 32) {
-    case 1: MOC_LS_CONST(1); break;
-    case 2: MOC_LS_CONST(2); break;
-    case 3: MOC_LS_CONST(3); break;
-    case 4: MOC_LS_CONST(4); break;
-    default: MOC_LS_CONST(8); break;
-  }
-#undef MOC_LS_CONST
+  const unsigned fb = (unsigned) grid_for(R * nc * ld, 256);
+  if (d3)
+    ls_finish_kernel<true><<<fb, 256, 0, s>>>(lem, acc, fsr_vol, R, G, ld,
+                                             ilem, cst, num_flat);
+  else
+    ls_finish_kernel<false><<<fb, 256, 0, s>>>(lem, acc, fsr_vol, R, G, ld,
+                                              ilem, cst, num_flat);
 }
 
 int launch_ls_constants(const int4* segs_ls, const int64_t* seg_off,
@@ -381,11 +381,15 @@ int launch_ls_constants(const int4* segs_ls, const int64_t* seg_off,
   int64_t* startp = nullptr;
   int32_t* list = nullptr;
   int32_t* seg_track = nullptr;
+  double* scratch = nullptr;
   cudaError_t e = cudaMalloc(&count, sizeof(int64_t) * (R + 1));
   if (e == cudaSuccess) e = cudaMalloc(&startp, sizeof(int64_t) * (R + 1));
   if (e == cudaSuccess) e = cudaMalloc(&list, sizeof(int32_t) * (S > 0 ? S : 1));
   if (e == cudaSuccess)
     e = cudaMalloc(&seg_track, sizeof(int32_t) * (S > 0 ? S : 1));
+  if (e == cudaSuccess)
+    e = cudaMalloc(&scratch,
+                   sizeof(double) * ls_constants_scratch(R, ld, seg_z != nullptr));
   std::vector<int64_t> h((size_t) R + 1, 0);
   if (e == cudaSuccess)
     e = cudaMemsetAsync(count, 0, sizeof(int64_t) * (R + 1), s);
@@ -420,10 +424,10 @@ int launch_ls_constants(const int4* segs_ls, const int64_t* seg_off,
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) {
-    launch_ls_constants_bucketed(segs_ls, list, startp, seg_track, track_ang,
+    launch_ls_constants_bucketed(segs_ls, list, S, seg_track, track_ang,
                                  ang_dir, ang_wgt, pol_sin, pol_wgt, Ph,
                                  sigma_t, fsr_vol, fsr_mat, R, G, ld, ilem, cst,
-                                 num_flat, s, seg_z, pol_cos);
+                                 num_flat, scratch, s, seg_z, pol_cos);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -431,6 +435,7 @@ int launch_ls_constants(const int4* segs_ls, const int64_t* seg_off,
   cudaFree(startp);
   cudaFree(list);
   cudaFree(seg_track);
+  cudaFree(scratch);
   return e == cudaSuccess ? 0 : (int) e;
 }
 

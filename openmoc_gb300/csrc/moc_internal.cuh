@@ -374,11 +374,12 @@ int launch_ls_constants(const int4* segs_ls, const int64_t* seg_off,
 void launch_ls_seg_track(const int64_t* seg_off, int64_t T, int32_t* seg_track,
                          cudaStream_t s);
 // The same constants from segment buckets the caller built (segment ids
-// of FSR r at list[start[r] .. start[r + 1]), and the track of every
-// segment): one launch, asynchronous, nothing allocated.
+// sorted by FSR, and the track of every segment) and FP64 scratch of
+// ls_constants_scratch(R, ld, 3D) doubles: asynchronous, nothing
+// allocated.
+int64_t ls_constants_scratch(int64_t R, int ld, bool d3);
 void launch_ls_constants_bucketed(const int4* segs_ls, const int32_t* list,
-                                  const int64_t* start,
-                                  const int32_t* seg_track,
+                                  int64_t S, const int32_t* seg_track,
                                   const int32_t* track_ang,
                                   const double* ang_dir, const double* ang_wgt,
                                   const double* pol_sin, const double* pol_wgt,
@@ -386,7 +387,7 @@ void launch_ls_constants_bucketed(const int4* segs_ls, const int32_t* list,
                                   const float* fsr_vol, const int32_t* fsr_mat,
                                   int64_t R, int G, int ld, float* ilem,
                                   float* cst, unsigned int* num_flat,
-                                  cudaStream_t s,
+                                  double* scratch, cudaStream_t s,
                                   const float* seg_z = nullptr,
                                   const double* pol_cos = nullptr);
 // Builds segs_ls from the packed segments and the start positions.

@@ -157,10 +157,8 @@ struct Staged {
   std::vector<double> ls_ang;
   std::vector<float2> ls_dir;
   std::vector<float> fixed_xy;
-  // segments bucketed by FSR for the expansion constants (ids of FSR r at
-  // ls_list[ls_start[r] .. ls_start[r + 1]), ascending), built here so that
-  // admission only copies and launches
-  std::vector<int64_t> ls_start;
+  // segment ids sorted by FSR (ascending within an FSR) for the expansion
+  // constants, built here so that admission only copies and launches
   std::vector<int32_t> ls_list;
   long long num_fissionable = 0;
   double init_flux = 1.0;          // flat starting flux (normalised)
@@ -187,7 +185,6 @@ struct Staged {
     std::vector<double>().swap(ls_ang);
     std::vector<float2>().swap(ls_dir);
     std::vector<float>().swap(fixed_xy);
-    std::vector<int64_t>().swap(ls_start);
     std::vector<int32_t>().swap(ls_list);
   }
 };
@@ -204,6 +201,8 @@ int stage_linear_source(const moc_request& q, Staged& s) {
            "null linear-source array");
   SV_CHECK(g->ang_dir && g->ang_wgt && g->pol_sin && g->pol_wgt, MOC_ERR_ARG,
            "null linear-source array");
+  SV_CHECK(!g->seg_z && !g->pol_cos, MOC_ERR_UNSUPPORTED,
+           "linear-source pools take 2D tracks");
   s.seg_x.resize(S);
   s.seg_y.resize(S);
   for (int64_t i = 0; i < S; i++) {
@@ -251,12 +250,11 @@ int stage_linear_source(const moc_request& q, Staged& s) {
         s.fixed_xy[2 * (r * ld + gg) + 1] = y;
       }
   }
-  // buckets: a counting sort of the segment ids by FSR
-  s.ls_start.assign(R + 1, 0);
-  for (int64_t i = 0; i < S; i++) s.ls_start[s.segs[i].y + 1]++;
-  for (int64_t r = 0; r < R; r++) s.ls_start[r + 1] += s.ls_start[r];
+  // a counting sort of the segment ids by FSR
+  std::vector<int64_t> fill(R + 1, 0);
+  for (int64_t i = 0; i < S; i++) fill[s.segs[i].y + 1]++;
+  for (int64_t r = 0; r < R; r++) fill[r + 1] += fill[r];
   s.ls_list.resize(S);
-  std::vector<int64_t> fill(s.ls_start.begin(), s.ls_start.end() - 1);
   for (int64_t i = 0; i < S; i++) s.ls_list[fill[s.segs[i].y]++] = (int32_t) i;
   s.ls = true;
   return MOC_OK;
@@ -499,7 +497,7 @@ struct Pool {
   float* fixed_xy = nullptr;
   float* ls_xy = nullptr;
   double* ls_ang = nullptr;
-  int64_t* ls_start = nullptr;
+  double* ls_scratch = nullptr;
   int32_t* ls_list = nullptr;
   int32_t* ls_seg_track = nullptr;
   unsigned int* ls_flat = nullptr;
@@ -597,7 +595,7 @@ void destroy_pool(Pool& p) {
   dev_free(p.fixed_xy);
   dev_free(p.ls_xy);
   dev_free(p.ls_ang);
-  dev_free(p.ls_start);
+  dev_free(p.ls_scratch);
   dev_free(p.ls_list);
   dev_free(p.ls_seg_track);
   dev_free(p.ls_flat);
@@ -740,7 +738,7 @@ int create_pool(moc_server* srv, const moc_pool_config& c, Pool& p) {
     SV_TRY(dev_alloc(&p.fixed_xy, 2 * R * ld));
     SV_TRY(dev_alloc(&p.ls_xy, 2 * S));
     SV_TRY(dev_alloc(&p.ls_ang, A * (3 + 2 * p.Ph)));
-    SV_TRY(dev_alloc(&p.ls_start, R + 1));
+    SV_TRY(dev_alloc(&p.ls_scratch, moc::ls_constants_scratch(R, ld, false)));
     SV_TRY(dev_alloc(&p.ls_list, S));
     SV_TRY(dev_alloc(&p.ls_seg_track, S));
     SV_TRY(dev_alloc(&p.ls_flat, 1));
@@ -899,9 +897,6 @@ int upload_linear_source(moc_server* srv, Pool& p, const Slot& sl) {
     SV_CUDA(cudaMemcpyAsync(p.fixed_xy + 2 * sl.r0 * ld, s.fixed_xy.data(),
                             sizeof(float) * 2 * R * ld,
                             cudaMemcpyHostToDevice, st));
-  SV_CUDA(cudaMemcpyAsync(p.ls_start, s.ls_start.data(),
-                          sizeof(int64_t) * (R + 1), cudaMemcpyHostToDevice,
-                          st));
   if (S > 0) {
     SV_CUDA(cudaMemcpyAsync(p.ls_list, s.ls_list.data(), sizeof(int32_t) * S,
                             cudaMemcpyHostToDevice, st));
@@ -909,11 +904,11 @@ int upload_linear_source(moc_server* srv, Pool& p, const Slot& sl) {
   }
   const double* ang = p.ls_ang;
   moc::launch_ls_constants_bucketed(
-      p.segs_ls + sl.s0, p.ls_list, p.ls_start, p.ls_seg_track,
-      p.track_ang + sl.t0, ang, ang + 2 * A, ang + 3 * A,
-      ang + 3 * A + A * Ph, Ph, p.sigma_t, p.fsr_vol + sl.r0,
-      p.fsr_mat + sl.r0, R, s.G, (int) ld, p.ls_ilem + 3 * sl.r0,
-      p.ls_const + 3 * sl.r0 * ld, p.ls_flat, st);
+      p.segs_ls + sl.s0, p.ls_list, S, p.ls_seg_track, p.track_ang + sl.t0,
+      ang, ang + 2 * A, ang + 3 * A, ang + 3 * A + A * Ph, Ph, p.sigma_t,
+      p.fsr_vol + sl.r0, p.fsr_mat + sl.r0, R, s.G, (int) ld,
+      p.ls_ilem + 3 * sl.r0, p.ls_const + 3 * sl.r0 * ld, p.ls_flat,
+      p.ls_scratch, st);
   SV_CUDA(cudaGetLastError());
   add_launches(srv, S > 0 ? 3 : 1);
   return MOC_OK;

@@ -92,6 +92,8 @@ def _lib():
         L.moc_lattice_export_ends3d.restype = C.c_int
         L.moc_lattice_export_ls.argtypes = [C.c_void_p] + [C.c_void_p] * 7
         L.moc_lattice_export_ls.restype = C.c_int
+        L.moc_lattice_export_ls3d.argtypes = [C.c_void_p] + [C.c_void_p] * 9
+        L.moc_lattice_export_ls3d.restype = C.c_int
         L.moc_lattice_export_cmfd.argtypes = [C.c_void_p] + [C.c_void_p] * 6
         L.moc_lattice_export_cmfd.restype = C.c_int
         L.moc_lattice_destroy.argtypes = [C.c_void_p]
@@ -160,12 +162,11 @@ def lattice(nx: int, ny: int, pin_material: np.ndarray, materials: Sequence[Mate
     fuel_height, z_spacing, num_polar) turns it into explicit 3D tracks of
     the lattice extruded axially (moderator above fuel_height, vacuum at
     bottom and top; ``num_polar`` Gauss-Legendre polar angles).
-    ``linear_source`` also exports the linear-source geometry (2D only):
-    segment starts relative to the FSR centroids and the angle data, as
-    ``Problem.linear_source``.  ``device`` ray-traces on that CUDA device
-    (the same segments and FSR ids; moc_lattice_generate_device)."""
-    if linear_source and extrude is not None:
-        raise ValueError("the linear-source geometry needs 2D tracks")
+    ``linear_source`` also exports the linear-source geometry: segment
+    starts relative to the FSR centroids and the angle data (with z starts
+    and cos theta for extruded 3D tracks), as ``Problem.linear_source``.
+    ``device`` ray-traces on that CUDA device (the same segments and FSR
+    ids; moc_lattice_generate_device)."""
     L = _lib()
     pm = np.ascontiguousarray(np.asarray(pin_material, np.int32).reshape(ny, nx))
     spec = _Spec(nx, ny, pitch, pin_radius, fuel_rings, fuel_sectors, mod_sectors,
@@ -223,7 +224,16 @@ def lattice(nx: int, ny: int, pin_material: np.ndarray, materials: Sequence[Mate
             if L.moc_lattice_export_ends3d(h, ends.ctypes.data):
                 raise RuntimeError(L.moc_lattice_last_error().decode())
         ls = None
-        if linear_source:
+        if linear_source and extrude is not None:
+            ls = dict(seg_x=np.empty(S, np.float32), seg_y=np.empty(S, np.float32),
+                      seg_z=np.empty(S, np.float32), centroid=np.empty(3 * R),
+                      ang_dir=np.empty(2 * A), ang_wgt=np.empty(A),
+                      pol_sin=np.empty(A), pol_cos=np.empty(A), pol_wgt=np.empty(A))
+            if L.moc_lattice_export_ls3d(h, *[ls[k].ctypes.data for k in (
+                    "seg_x", "seg_y", "seg_z", "centroid", "ang_dir", "ang_wgt",
+                    "pol_sin", "pol_cos", "pol_wgt")]):
+                raise RuntimeError(L.moc_lattice_last_error().decode())
+        elif linear_source:
             ls = dict(seg_x=np.empty(S, np.float32), seg_y=np.empty(S, np.float32),
                       centroid=np.empty(2 * R), ang_dir=np.empty(2 * A),
                       ang_wgt=np.empty(A), pol_sin=np.empty(A * Ph),
@@ -308,7 +318,8 @@ def assembly_17x17(num_groups: int = 70, num_azim: int = 64, spacing: float = 0.
 
 def assembly_17x17_3d(num_groups: int = 7, num_azim: int = 16, spacing: float = 0.1,
                       num_polar: int = 6, z_spacing: float = 0.5, height: float = 20.0,
-                      fuel_height: float = 16.0, config: int = 4, perturb=None) -> Problem:
+                      fuel_height: float = 16.0, config: int = 4, perturb=None,
+                      linear_source: bool = False) -> Problem:
     """The 17 x 17 assembly extruded axially: the lattice for z < 16 cm,
     homogeneous moderator up to 20 cm, reflective radially, vacuum at the
     bottom and top, explicit 3D tracks (16 azimuthal, 6 polar, 0.1 cm radial,
@@ -319,7 +330,8 @@ def assembly_17x17_3d(num_groups: int = 7, num_azim: int = 16, spacing: float = 
         pm[r, c] = 1
     return lattice(17, 17, pm, mats, 1, num_azim=num_azim, spacing=spacing,
                    extrude=dict(height=height, fuel_height=fuel_height,
-                                z_spacing=z_spacing, num_polar=num_polar))
+                                z_spacing=z_spacing, num_polar=num_polar),
+                   linear_source=linear_source)
 
 
 def core_51x51(num_groups: int = 7, num_azim: int = 128, spacing: float = 0.03,

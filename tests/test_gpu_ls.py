@@ -292,3 +292,38 @@ def test_gpu_ls_3d_matches_oracle_at_fixed_iterations():
     assert _rel(s.getFluxes(), o.phi.reshape(R, G), 1e-4) < 2e-5
     assert _peak(s.getFluxMoments(), o.mom.reshape(R, 3, G)) < 1e-4
     s.close()
+
+
+@pytest.mark.parametrize("G,shapes", [
+    (7, [(1, 4), (2, 2), (4, 1), (8, 1)]),
+    (16, [(2, 4), (4, 2), (8, 1), (16, 1)]),
+])
+def test_gpu_ls_3d_lattice_matches_oracle_every_shape(G, shapes):
+    """A 2 x 2 lattice extruded into explicit 3D tracks with the generator's
+    3D linear-source geometry (moc_lattice_export_ls3d), vacuum at bottom and
+    top, against the FP64 oracle after 8 eigenvalue iterations, for each
+    sweep shape."""
+    from openmoc_gb300 import GB300LSSolver
+    from openmoc_gb300 import lattice as lat
+    mats = lat._fuel_mod(4, G, 1)
+    pm = np.zeros((2, 2), np.int32)
+    pm[1, 1] = 1
+    p = lat.lattice(2, 2, pm, mats, 1, num_azim=8, spacing=0.1,
+                    extrude=dict(height=4.0, fuel_height=3.2, z_spacing=0.4,
+                                 num_polar=4), linear_source=True)
+    iters = 8
+    o = LSOracle(p, p.linear_source, "f64", num_threads=8)
+    o.compute_eigenvalue(iters, 1, 1e-30)
+    R = p.num_fsrs
+    ref_m = o.mom.reshape(R, 3, G)
+    for lps, pairs in shapes:
+        s = GB300LSSolver(device=0)
+        s.setSweepShape(lps, pairs)
+        s.setConvergenceThreshold(1e-30)
+        s.setTrackGenerator(p)
+        s.computeEigenvalue(iters, 1)
+        assert s.getNumIterations() == iters
+        assert abs(s.getKeff() - o.keff) < 2e-6, (lps, pairs)
+        assert _rel(s.getFluxes(), o.phi.reshape(R, G), 1e-4) < 2e-5, (lps, pairs)
+        assert _peak(s.getFluxMoments(), ref_m) < 1e-4, (lps, pairs)
+        s.close()

@@ -121,6 +121,39 @@ def test_extrusion_is_openmocs_3d_laydown():
     assert np.array_equal(nr[bwd, 1], nm[bwd, 1]) and np.array_equal(f[bwd] & 2, g[bwd] & 2)
 
 
+def test_extrusion_ls_geometry_is_openmocs():
+    """The linear-source geometry of the extruded pin (moc_lattice_export_ls3d)
+    against OpenMOC's own (pin3d_ls: CPULSSolver on TrackGenerator3D's
+    laydown of the same pin): angle rows, weights, sin / cos theta exactly;
+    segment starts relative to the centroids to a float rounding; 3D
+    centroids to 1e-7."""
+    from openmoc_gb300 import lattice
+    mats = [lattice.synthetic_xs(lattice.SEED + 5, 7, True),
+            lattice.synthetic_xs(lattice.SEED + 1005, 7, False)]
+    p = lattice.lattice(1, 1, np.zeros((1, 1), np.int32), mats, 1, num_azim=4,
+                        spacing=0.1, fuel_rings=2, fuel_sectors=4, mod_sectors=4,
+                        extrude=dict(height=2.0, fuel_height=1.6, z_spacing=0.4,
+                                     num_polar=4), linear_source=True)
+    ref, _, arr = load_case("pin3d_ls", "f64")
+    ls = p.linear_source
+    assert np.array_equal(p.seg_off, ref.seg_off)
+    for k in ("ang_dir", "ang_wgt", "pol_sin", "pol_cos"):
+        assert np.array_equal(ls[k], arr["ls_" + k]), k
+    assert np.allclose(ls["pol_wgt"], arr["ls_pol_wgt"], rtol=1e-14, atol=0)
+    for k in ("seg_x", "seg_y", "seg_z"):
+        assert np.max(np.abs(ls[k].astype(np.float64) - arr["ls_" + k])) < 2e-7, k
+    pairs = dict(zip(p.seg_fsr.tolist(), ref.seg_fsr.tolist()))
+    c, cr = ls["centroid"].reshape(-1, 3), arr["ls_centroid"].reshape(-1, 3)
+    assert max(np.abs(c[a] - cr[b]).max() for a, b in pairs.items()) < 1e-7
+    # each 3D track runs along its row's direction
+    d = p.track_ends[:, 3:] - p.track_ends[:, :3]
+    d /= np.linalg.norm(d, axis=1)[:, None]
+    a = p.track_ang
+    u = np.stack([ls["ang_dir"][2 * a] * ls["pol_sin"][a],
+                  ls["ang_dir"][2 * a + 1] * ls["pol_sin"][a], ls["pol_cos"][a]], 1)
+    assert np.abs(d - u).max() < 1e-12
+
+
 def test_assembly3d_is_openmocs_3d_laydown():
     """The 3D benchmark assembly (17 x 17 extruded to 20 cm, 16 azimuthal,
     6 polar, 0.1 / 0.5 cm) against OpenMOC's own laydown of it
