@@ -38,8 +38,16 @@ struct Piece2 {
   int w0, w1;     // fsr | material << 24
 };
 
+// Blocks per SM: 6 (up to 85 registers); MOC_OTF_MIN_BLOCKS for the
+// one-pair instances, whose sweeps wait on loads: 3D 17x17 assembly,
+// 7 groups, 4 lanes x 1 pair, 6 blocks (69 registers) 3.767 ms per sweep,
+// 8 blocks (61 registers) 3.257 ms; 10 spills 52 bytes.
+#ifndef MOC_OTF_MIN_BLOCKS
+#define MOC_OTF_MIN_BLOCKS 8
+#endif
 template <int LPS, int PS>
-__global__ void __launch_bounds__(kSweepThreads, 6)
+__global__ void __launch_bounds__(kSweepThreads,
+                                  (PS == 1 ? MOC_OTF_MIN_BLOCKS : 6))
 otf_sweep_kernel(const SweepArgs a, const OtfArgs o) {
   extern __shared__ float smem[];
   DevScalars* sc = a.sc;

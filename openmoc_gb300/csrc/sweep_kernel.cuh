@@ -139,6 +139,15 @@ __device__ __forceinline__ void cp_async_wait() {
 #ifndef MOC_SWEEP_BIG_MIN_BLOCKS
 #define MOC_SWEEP_BIG_MIN_BLOCKS 5
 #endif
+// Blocks per SM of the one-polar (3D) instances with one group pair per
+// lane: their sweeps wait on loads, so resident warps (loads in flight) set
+// their speed.  3D 17x17 assembly, 7 groups, 4 lanes x 1 pair: 8 blocks
+// (56 registers, 9 resident) 1.692 ms per sweep, 10 blocks 1.723 ms,
+// 12 blocks (40 registers) 1.516 ms; 14 and 16 leave 32 registers and
+// spill 76 bytes.  The two-pair instances spill 60 bytes at 12 and keep 8.
+#ifndef MOC_SWEEP_3D_MIN_BLOCKS
+#define MOC_SWEEP_3D_MIN_BLOCKS 12
+#endif
 // The busy instances of the CMFD mode, which also tally partial currents,
 // take 4 blocks (their registers would spill at 5).
 template <int PH, int PS, int MODE = 0>
@@ -148,6 +157,7 @@ struct SweepOccupancy {
       : (PH * PS > 6 && MODE == 2) ? 4
       : (PH * PS > 6)              ? MOC_SWEEP_BIG_MIN_BLOCKS
       : (PH == 1 && PS > 2)        ? 6
+      : (PH == 1 && PS == 1)       ? MOC_SWEEP_3D_MIN_BLOCKS
                                    : 8;
 };
 
