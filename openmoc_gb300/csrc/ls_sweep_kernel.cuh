@@ -79,11 +79,17 @@ struct LsExpG {
 
 // Blocks of 128 threads kept resident per SM: the register file bounds the
 // busy instances (PH * PS pair-polar values per lane); the 3D instances
-// carry the z source moments and tallies of every pair as well.
+// carry the z source moments and tallies of every pair as well, and their
+// light ones wait on loads (MOC_LS3D_MIN_BLOCKS: 3D 17x17 assembly, 7
+// groups, 4 lanes x 1 pair, 6 blocks (72 registers) 4.277 ms per sweep,
+// 8 blocks (62) 4.205 ms; 10 spills).
+#ifndef MOC_LS3D_MIN_BLOCKS
+#define MOC_LS3D_MIN_BLOCKS 8
+#endif
 template <int PH, int PS, bool D3>
 struct LsOccupancy {
   static constexpr int min_blocks =
-      D3 ? ((PS >= 4) ? 3 : (PS >= 3) ? 4 : 6)
+      D3 ? ((PS >= 4) ? 3 : (PS >= 3) ? 4 : MOC_LS3D_MIN_BLOCKS)
          : ((PH * PS >= 12) ? 4 : (PH * PS >= 6) ? 5 : 6);
 };
 
