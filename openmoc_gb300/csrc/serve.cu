@@ -128,6 +128,54 @@ class RangeAlloc {
   std::map<int64_t, int64_t> free_;
 };
 
+// Page-locked host blocks in power-of-two size classes, kept for reuse:
+// each request's arrays are copied into one on submission (on the
+// submitting thread), so that admission only enqueues asynchronous copies.
+class PinnedCache {
+ public:
+  ~PinnedCache() {
+    for (auto& b : all_) cudaFreeHost(b.first);
+  }
+  char* get(size_t n, size_t* cap) {
+    size_t c = (size_t) 1 << 16;
+    while (c < n) c <<= 1;
+    *cap = c;
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      auto it = free_.find(c);
+      if (it != free_.end()) {
+        char* q = it->second;
+        free_.erase(it);
+        return q;
+      }
+    }
+    void* q = nullptr;
+    if (cudaHostAlloc(&q, c, cudaHostAllocPortable) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    std::lock_guard<std::mutex> lk(mu_);
+    all_.emplace_back((char*) q, c);
+    return (char*) q;
+  }
+  void put(char* q, size_t cap) {
+    if (!q) return;
+    std::lock_guard<std::mutex> lk(mu_);
+    free_.emplace(cap, q);
+  }
+ private:
+  std::mutex mu_;
+  std::multimap<size_t, char*> free_;
+  std::vector<std::pair<char*, size_t>> all_;
+};
+
+// The arrays of a request in its pinned block, in this order.
+enum Part {
+  kSegs, kSegOff, kNext, kTrackAng, kFlags, kWeights, kInvSin, kSigmaT,
+  kSigmaST, kNuSigmaF, kChi, kScatOut, kFissile, kFsrMat, kFsrVol, kFixed,
+  kSegX, kSegY, kLsAng, kLsDir, kFixedXY, kLsList, kNumParts
+};
+
 // A validated request, packed in its own numbering, waiting for or holding
 // a pool slot.
 struct Staged {
@@ -163,6 +211,20 @@ struct Staged {
   long long num_fissionable = 0;
   double init_flux = 1.0;          // flat starting flux (normalised)
   double t_submit = 0.0, t_admit = 0.0;
+  // the pinned copy of the arrays (offset, bytes per Part), until the
+  // copies to the pool have run
+  PinnedCache* cache = nullptr;
+  char* pin = nullptr;
+  size_t pin_cap = 0;
+  size_t off[kNumParts] = {}, len[kNumParts] = {};
+  const char* part(int i) const { return pin + off[i]; }
+  // returns the pinned block (its copies have run: the pool's stream was
+  // waited on since they were enqueued)
+  void release_pin() {
+    if (pin && cache) cache->put(pin, pin_cap);
+    pin = nullptr;
+  }
+  ~Staged() { release_pin(); }
 
   void release_arrays() {
     std::vector<int2>().swap(segs);
@@ -186,8 +248,56 @@ struct Staged {
     std::vector<float2>().swap(ls_dir);
     std::vector<float>().swap(fixed_xy);
     std::vector<int32_t>().swap(ls_list);
+    std::vector<int32_t>().swap(fsr_mat);
   }
 };
+
+// Copies a staged request's arrays into one pinned block (16-byte aligned
+// parts, in Part order) and frees the pageable ones.
+int pin_request(PinnedCache& cache, Staged& s) {
+  const void* src[kNumParts] = {};
+  size_t n[kNumParts] = {};
+  auto set = [&](int i, const void* q, size_t b) {
+    src[i] = q;
+    n[i] = b;
+  };
+  set(kSegs, s.segs.data(), sizeof(int2) * s.segs.size());
+  set(kSegOff, s.seg_off.data(), sizeof(int64_t) * s.seg_off.size());
+  set(kNext, s.next.data(), sizeof(int32_t) * s.next.size());
+  set(kTrackAng, s.track_ang.data(), sizeof(int32_t) * s.track_ang.size());
+  set(kFlags, s.flags.data(), s.flags.size());
+  set(kWeights, s.weights.data(), sizeof(float) * s.weights.size());
+  set(kInvSin, s.inv_sin.data(), sizeof(float) * s.inv_sin.size());
+  set(kSigmaT, s.sigma_t.data(), sizeof(float) * s.sigma_t.size());
+  set(kSigmaST, s.sigma_s_T.data(), sizeof(float) * s.sigma_s_T.size());
+  set(kNuSigmaF, s.nu_sigma_f.data(), sizeof(float) * s.nu_sigma_f.size());
+  set(kChi, s.chi.data(), sizeof(float) * s.chi.size());
+  set(kScatOut, s.scat_out.data(), sizeof(float) * s.scat_out.size());
+  set(kFissile, s.fissile.data(), s.fissile.size());
+  set(kFsrMat, s.fsr_mat.data(), sizeof(int32_t) * s.fsr_mat.size());
+  set(kFsrVol, s.fsr_vol.data(), sizeof(float) * s.fsr_vol.size());
+  set(kFixed, s.fixed.data(), sizeof(float) * s.fixed.size());
+  set(kSegX, s.seg_x.data(), sizeof(float) * s.seg_x.size());
+  set(kSegY, s.seg_y.data(), sizeof(float) * s.seg_y.size());
+  set(kLsAng, s.ls_ang.data(), sizeof(double) * s.ls_ang.size());
+  set(kLsDir, s.ls_dir.data(), sizeof(float2) * s.ls_dir.size());
+  set(kFixedXY, s.fixed_xy.data(), sizeof(float) * s.fixed_xy.size());
+  set(kLsList, s.ls_list.data(), sizeof(int32_t) * s.ls_list.size());
+  size_t total = 0;
+  for (int i = 0; i < kNumParts; i++) {
+    s.off[i] = total;
+    s.len[i] = n[i];
+    total += (n[i] + 15) & ~(size_t) 15;
+  }
+  s.cache = &cache;
+  s.pin = cache.get(total > 0 ? total : 16, &s.pin_cap);
+  SV_CHECK(s.pin, MOC_ERR_MEMORY,
+           "no page-locked host memory for the request's arrays");
+  for (int i = 0; i < kNumParts; i++)
+    if (n[i]) std::memcpy(s.pin + s.off[i], src[i], n[i]);
+  s.release_arrays();
+  return MOC_OK;
+}
 
 // The linear-source part of a request, checked as moc_set_linear_source and
 // moc_set_fixed_source_moments check theirs (same limits and messages).
@@ -533,6 +643,7 @@ struct Pool {
 }  // namespace
 
 struct moc_server {
+  PinnedCache pinned;                // requests' host arrays (outlives pools)
   moc_server_config cfg{};
   int64_t hot_live = 0;              // sweep-gathered bytes of live solves
   std::vector<std::unique_ptr<Pool>> pools;
@@ -862,6 +973,25 @@ void publish(moc_server* srv, const Staged& st, const moc_result& r) {
 // moments too.
 int64_t hot_bytes(const Staged& s) { return (s.ls ? 24 : 8) * s.R * s.ld; }
 
+// The pool material numbers of an admitted solve's FSRs (its own + m0),
+// and the owner of its rows.
+__global__ void offset_i32_kernel(int32_t* v, int64_t n, int32_t add) {
+  for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t) gridDim.x * blockDim.x)
+    v[i] += add;
+}
+
+__global__ void fill_i32_kernel(int32_t* v, int64_t n, int32_t value) {
+  for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t) gridDim.x * blockDim.x)
+    v[i] = value;
+}
+
+unsigned small_grid(int64_t n) {
+  int64_t b = (n + 255) / 256;
+  return (unsigned) (b < 1 ? 1 : b > 1024 ? 1024 : b);
+}
+
 // The linear-source data of an admitted solve, while its segments and track
 // data are still in its own numbering: the 16-byte segment words, its angle
 // directions and fixed source moments, and its expansion matrices and
@@ -875,31 +1005,29 @@ int upload_linear_source(moc_server* srv, Pool& p, const Slot& sl) {
   cudaStream_t st = p.stream;
   const int64_t S = s.S, R = s.R, ld = p.ld;
   const int A = s.A, Ph = s.Ph;
+  auto put = [&](void* dst, int part) -> int {
+    if (s.len[part])
+      SV_CUDA(cudaMemcpyAsync(dst, s.part(part), s.len[part],
+                              cudaMemcpyHostToDevice, st));
+    return MOC_OK;
+  };
   if (S > 0) {
     float* dx = p.ls_xy;
     float* dy = p.ls_xy + S;
-    SV_CUDA(cudaMemcpyAsync(dx, s.seg_x.data(), sizeof(float) * S,
-                            cudaMemcpyHostToDevice, st));
-    SV_CUDA(cudaMemcpyAsync(dy, s.seg_y.data(), sizeof(float) * S,
-                            cudaMemcpyHostToDevice, st));
+    SV_TRY(put(dx, kSegX));
+    SV_TRY(put(dy, kSegY));
     moc::launch_ls_pack_segments(p.segs + sl.s0, dx, dy, p.segs_ls + sl.s0,
                                  S, st);
   }
-  SV_CUDA(cudaMemcpyAsync(p.ls_ang, s.ls_ang.data(),
-                          sizeof(double) * s.ls_ang.size(),
-                          cudaMemcpyHostToDevice, st));
-  SV_CUDA(cudaMemcpyAsync(p.ang_dir + sl.a0, s.ls_dir.data(),
-                          sizeof(float2) * A, cudaMemcpyHostToDevice, st));
-  if (s.fixed_xy.empty())
+  SV_TRY(put(p.ls_ang, kLsAng));
+  SV_TRY(put(p.ang_dir + sl.a0, kLsDir));
+  if (s.len[kFixedXY] == 0)
     SV_CUDA(cudaMemsetAsync(p.fixed_xy + 2 * sl.r0 * ld, 0,
                             sizeof(float) * 2 * R * ld, st));
   else
-    SV_CUDA(cudaMemcpyAsync(p.fixed_xy + 2 * sl.r0 * ld, s.fixed_xy.data(),
-                            sizeof(float) * 2 * R * ld,
-                            cudaMemcpyHostToDevice, st));
+    SV_TRY(put(p.fixed_xy + 2 * sl.r0 * ld, kFixedXY));
   if (S > 0) {
-    SV_CUDA(cudaMemcpyAsync(p.ls_list, s.ls_list.data(), sizeof(int32_t) * S,
-                            cudaMemcpyHostToDevice, st));
+    SV_TRY(put(p.ls_list, kLsList));
     moc::launch_ls_seg_track(p.seg_off + sl.t0, s.T, p.ls_seg_track, st);
   }
   const double* ang = p.ls_ang;
@@ -914,56 +1042,41 @@ int upload_linear_source(moc_server* srv, Pool& p, const Slot& sl) {
   return MOC_OK;
 }
 
-// Copies a solve's data into the ranges given to it and rebases them.
+// Copies a solve's data from its pinned block into the ranges given to it
+// (asynchronous copies only) and rebases them.
 int upload_slot(moc_server* srv, Pool& p, int slot_index) {
   Slot& sl = p.slots[slot_index];
   Staged& s = *sl.st;
   cudaStream_t st = p.stream;
   const int64_t T = s.T, S = s.S, R = s.R, G = s.G;
-  const int64_t MG = (int64_t) s.M * G;
-  std::vector<int32_t> mat(s.fsr_mat.size());
-  for (size_t i = 0; i < mat.size(); i++) mat[i] = s.fsr_mat[i] + (int32_t) sl.m0;
-  std::vector<int32_t> owner(R, slot_index);
-  if (S > 0)
-    SV_CUDA(cudaMemcpyAsync(p.segs + sl.s0, s.segs.data(), sizeof(int2) * S,
-                            cudaMemcpyHostToDevice, st));
-  SV_CUDA(cudaMemcpyAsync(p.seg_off + sl.t0, s.seg_off.data(),
-                          sizeof(int64_t) * (T + 1), cudaMemcpyHostToDevice, st));
-  SV_CUDA(cudaMemcpyAsync(p.next + 2 * sl.t0, s.next.data(),
-                          sizeof(int32_t) * 2 * T, cudaMemcpyHostToDevice, st));
-  SV_CUDA(cudaMemcpyAsync(p.track_ang + sl.t0, s.track_ang.data(),
-                          sizeof(int32_t) * T, cudaMemcpyHostToDevice, st));
-  SV_CUDA(cudaMemcpyAsync(p.flags + sl.t0, s.flags.data(), T + 1,
-                          cudaMemcpyHostToDevice, st));
-  SV_CUDA(cudaMemcpyAsync(p.weights + sl.a0 * p.Ph, s.weights.data(),
-                          sizeof(float) * s.weights.size(),
-                          cudaMemcpyHostToDevice, st));
-  SV_CUDA(cudaMemcpyAsync(p.inv_sin + sl.a0 * p.Ph, s.inv_sin.data(),
-                          sizeof(float) * s.inv_sin.size(),
-                          cudaMemcpyHostToDevice, st));
-  SV_CUDA(cudaMemcpyAsync(p.sigma_t + sl.m0 * G, s.sigma_t.data(),
-                          sizeof(float) * MG, cudaMemcpyHostToDevice, st));
-  SV_CUDA(cudaMemcpyAsync(p.sigma_s_T + sl.m0 * G * G, s.sigma_s_T.data(),
-                          sizeof(float) * MG * G, cudaMemcpyHostToDevice, st));
-  SV_CUDA(cudaMemcpyAsync(p.nu_sigma_f + sl.m0 * G, s.nu_sigma_f.data(),
-                          sizeof(float) * MG, cudaMemcpyHostToDevice, st));
-  SV_CUDA(cudaMemcpyAsync(p.chi + sl.m0 * G, s.chi.data(), sizeof(float) * MG,
-                          cudaMemcpyHostToDevice, st));
-  SV_CUDA(cudaMemcpyAsync(p.scat_out + sl.m0 * G, s.scat_out.data(),
-                          sizeof(float) * MG, cudaMemcpyHostToDevice, st));
-  SV_CUDA(cudaMemcpyAsync(p.fissile + sl.m0, s.fissile.data(), s.M,
-                          cudaMemcpyHostToDevice, st));
-  SV_CUDA(cudaMemcpyAsync(p.fsr_mat + sl.r0, mat.data(), sizeof(int32_t) * R,
-                          cudaMemcpyHostToDevice, st));
-  SV_CUDA(cudaMemcpyAsync(p.fsr_vol + sl.r0, s.fsr_vol.data(),
-                          sizeof(float) * R, cudaMemcpyHostToDevice, st));
-  if (s.fixed.empty())
+  auto put = [&](void* dst, int part) -> int {
+    if (s.len[part])
+      SV_CUDA(cudaMemcpyAsync(dst, s.part(part), s.len[part],
+                              cudaMemcpyHostToDevice, st));
+    return MOC_OK;
+  };
+  SV_TRY(put(p.segs + sl.s0, kSegs));
+  SV_TRY(put(p.seg_off + sl.t0, kSegOff));
+  SV_TRY(put(p.next + 2 * sl.t0, kNext));
+  SV_TRY(put(p.track_ang + sl.t0, kTrackAng));
+  SV_TRY(put(p.flags + sl.t0, kFlags));
+  SV_TRY(put(p.weights + sl.a0 * p.Ph, kWeights));
+  SV_TRY(put(p.inv_sin + sl.a0 * p.Ph, kInvSin));
+  SV_TRY(put(p.sigma_t + sl.m0 * G, kSigmaT));
+  SV_TRY(put(p.sigma_s_T + sl.m0 * G * G, kSigmaST));
+  SV_TRY(put(p.nu_sigma_f + sl.m0 * G, kNuSigmaF));
+  SV_TRY(put(p.chi + sl.m0 * G, kChi));
+  SV_TRY(put(p.scat_out + sl.m0 * G, kScatOut));
+  SV_TRY(put(p.fissile + sl.m0, kFissile));
+  SV_TRY(put(p.fsr_mat + sl.r0, kFsrMat));
+  offset_i32_kernel<<<small_grid(R), 256, 0, st>>>(p.fsr_mat + sl.r0, R,
+                                                   (int32_t) sl.m0);
+  SV_TRY(put(p.fsr_vol + sl.r0, kFsrVol));
+  if (s.len[kFixed] == 0)
     SV_CUDA(cudaMemsetAsync(p.fixed + sl.r0 * p.ld, 0,
                             sizeof(float) * R * p.ld, st));
   else
-    SV_CUDA(cudaMemcpyAsync(p.fixed + sl.r0 * p.ld, s.fixed.data(),
-                            sizeof(float) * R * p.ld, cudaMemcpyHostToDevice,
-                            st));
+    SV_TRY(put(p.fixed + sl.r0 * p.ld, kFixed));
   if (p.ls) SV_TRY(upload_linear_source(srv, p, sl));
   moc::launch_batch_rebase(p.segs + sl.s0, S, p.fsr_mat, (int32_t) sl.r0,
                            p.seg_off + sl.t0, p.next + 2 * sl.t0,
@@ -971,12 +1084,12 @@ int upload_slot(moc_server* srv, Pool& p, int slot_index) {
                            (int32_t) sl.t0, (int32_t) sl.a0, slot_index, st);
   // the linear-source words take the rebased FSR ids and materials
   if (p.ls) moc::launch_ls_refresh_ids(p.segs + sl.s0, p.segs_ls + sl.s0, S, st);
-  SV_CUDA(cudaGetLastError());
   // rows become visible to the row kernels only with their owner set, after
   // the data above in stream order
-  SV_CUDA(cudaMemcpyAsync(p.row_slot + sl.r0, owner.data(),
-                          sizeof(int32_t) * R, cudaMemcpyHostToDevice, st));
-  add_launches(srv, 1);
+  fill_i32_kernel<<<small_grid(R), 256, 0, st>>>(p.row_slot + sl.r0, R,
+                                                 slot_index);
+  SV_CUDA(cudaGetLastError());
+  add_launches(srv, 3);
   return MOC_OK;
 }
 
@@ -1076,8 +1189,6 @@ int admit(moc_server* srv, Pool& p) {
     if (!sl.live || sl.uploaded) continue;
     SV_TRY(upload_slot(srv, p, i));
     sl.uploaded = true;
-    // pageable copies are staged by the time cudaMemcpyAsync returns
-    sl.st->release_arrays();
   }
   return MOC_OK;
 }
@@ -1411,6 +1522,9 @@ int service(moc_server* srv, Pool& p, bool wait, bool* progressed) {
       SV_CUDA(e);
     }
     p.in_flight = false;
+    // the copies of the solves admitted before this block have run
+    for (Slot& sl : p.slots)
+      if (sl.live && sl.uploaded) sl.st->release_pin();
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, p.block_start, p.block_done) == cudaSuccess) {
       std::lock_guard<std::mutex> lk(srv->mu);
@@ -1544,6 +1658,7 @@ int moc_server_submit(moc_server* srv, const moc_request* req,
                s->S <= c.max_segments && s->M <= c.max_materials &&
                s->A <= c.max_angles,
            MOC_ERR_MEMORY, "request exceeds its pool's capacity");
+  SV_TRY(pin_request(srv->pinned, *s));
   s->pool = target->index;
   s->t_submit = now_s();
   std::lock_guard<std::mutex> lk(srv->mu);
