@@ -508,7 +508,13 @@ def run_gpu(args):
             out["configs"] = {
                 "core51": single_config(core, WORKLOADS["core51"], local),
                 "assembly3d": single_config(lat.assembly_17x17_3d(),
-                                            WORKLOADS["assembly3d"], local)}
+                                            WORKLOADS["assembly3d"], local),
+                "assembly70_ls": single_config(
+                    lat.assembly_17x17(linear_source=True),
+                    WORKLOADS["assembly70_ls"], local),
+                "assembly3d_ls": single_config(
+                    lat.assembly_17x17_3d(linear_source=True),
+                    WORKLOADS["assembly3d_ls"], local)}
         if world == 1 and args.workload == "assembly70" and not args.no_cmfd:
             # the regime CMFD is for: a core whose sweeps are expensive and
             # whose plain source iteration needs a thousand iterations
@@ -617,10 +623,12 @@ def cmfd_solve_only(workload="core", kind="auto", device=0):
 def single_config(p, label, device, steps=10):
     """One more benchmark configuration solved alone: the autotuned sweep
     shape and the device-timed source iteration (L2 flushed between
-    iterations, as for the headline), integrations per second."""
-    from openmoc_gb300 import GB300Solver
+    iterations, as for the headline), integrations per second; with the
+    linear source (CPULSSolver) when the problem carries its geometry."""
+    from openmoc_gb300 import GB300LSSolver, GB300Solver
     from openmoc_gb300.solver import FISSION_SOURCE
-    s = GB300Solver(p, device=device)
+    s = (GB300LSSolver if p.linear_source is not None else GB300Solver)(
+        p, device=device)
     lps, slots, exp_kind = s.autotune()
     s.benchIterations(3, FISSION_SOURCE, True)
     st, sw = s.benchIterations(steps, FISSION_SOURCE, True)
@@ -629,7 +637,9 @@ def single_config(p, label, device, steps=10):
     return {"workload": label, "fsrs": int(p.num_fsrs), "tracks": int(p.num_tracks),
             "segments": int(p.num_segments), "groups": int(p.num_groups),
             "integrations_per_sweep": int(p.integrations_per_sweep),
-            "sweep_shape": [int(lps), int(slots), "ex2" if exp_kind else "table"],
+            "sweep_shape": [int(lps), int(slots),
+                            "rational G(x)" if p.linear_source is not None else
+                            "ex2" if exp_kind else "table"],
             "ms_per_step": step, "sweep_ms_per_step": float(np.mean(sw)),
             "value": p.integrations_per_sweep / (step * 1e-3),
             "unit": "integrations/s", "steps": steps}
