@@ -265,11 +265,21 @@ sweep_kernel(const SweepArgs a) {
   // instances the others need no test and no branch.  The light instances
   // test every pair (holding the predicate costs them a spill).
   const bool last_live = sub + (PS - 1) * LPS < npairs;
+  // Lane sub of a stream owns the group pairs pidx(s), s < PS: interleaved
+  // with the stream's other lanes (sub + s LPS), or in the light two-pair
+  // instances adjacent (2 sub + s), so that when the rows are padded to a
+  // multiple of four floats one 16-byte gather and one 16-byte reduction
+  // serve both pairs (the light instances' per-segment accesses, one line
+  // per stream each, bound them by L1TEX throughput).
+  constexpr bool kAdj =
+      PS == 2 && !SweepRing<PH, LPS, PS>::staged && MODE != 2;
+  auto pidx = [&](int s) { return kAdj ? PS * sub + s : sub + s * LPS; };
+  const bool vec4 = kAdj && (ld & 3) == 0;
   auto live_pair = [&](int s) {
     if constexpr (SweepRing<PH, LPS, PS>::staged)
       return s < PS - 1 || last_live;
     else
-      return sub + s * LPS < npairs;
+      return pidx(s) < npairs;
   };
 
   // the track and its pending scale; in a pool the solve of the track may
@@ -334,7 +344,7 @@ sweep_kernel(const SweepArgs a) {
     const float* pin = psi_in + ((int64_t) t * 2 + dir) * F;
 #pragma unroll
     for (int s = 0; s < PS; s++) {
-      const int g0 = 2 * (sub + s * LPS);
+      const int g0 = 2 * pidx(s);
       // with instances each group takes its own instance's pending scale
       float sx = scale, sy = scale;
       if (!POOL && a.inst && g0 < G) {
@@ -417,10 +427,27 @@ sweep_kernel(const SweepArgs a) {
       return r;
     };
     auto gather = [&](float2* qq, int f, bool valid) {
-      const float2* qrow = qbase + (int64_t) f * npairs;
+      if constexpr (kAdj) {
+        const float2* qrow = reinterpret_cast<const float2*>(a.qt) +
+                             (int64_t) f * npairs + PS * sub;
+        if (vec4) {
+          // npairs even: a lane's second pair is live with its first
+          const float4 v = (valid && live_pair(0))
+                               ? __ldg(reinterpret_cast<const float4*>(qrow))
+                               : make_float4(0.f, 0.f, 0.f, 0.f);
+          qq[0] = make_float2(v.x, v.y);
+          qq[1] = make_float2(v.z, v.w);
+        } else {
 #pragma unroll
-      for (int s = 0; s < PS; s++)
-        qq[s] = (live_pair(s) && valid) ? __ldg(qrow + s * LPS) : f2(0.0f);
+          for (int s = 0; s < PS; s++)
+            qq[s] = (live_pair(s) && valid) ? __ldg(qrow + s) : f2(0.0f);
+        }
+      } else {
+        const float2* qrow = qbase + (int64_t) f * npairs;
+#pragma unroll
+        for (int s = 0; s < PS; s++)
+          qq[s] = (live_pair(s) && valid) ? __ldg(qrow + s * LPS) : f2(0.0f);
+      }
     };
     float len = 0.0f;
     int fsr = 0, mat = 0;
@@ -465,17 +492,19 @@ sweep_kernel(const SweepArgs a) {
       }
 
       const float2* st =
-          reinterpret_cast<const float2*>(s_st + mat * ld) + sub;
-      float2* ph = reinterpret_cast<float2*>(a.phi + (int64_t) fsr * ld) + sub;
+          reinterpret_cast<const float2*>(s_st + mat * ld) + pidx(0);
+      float2* ph =
+          reinterpret_cast<float2*>(a.phi + (int64_t) fsr * ld) + pidx(0);
       // a region crossed by most tracks tallies into this block's copy
       // (3D problems only, PH == 1: one moderator region above the fuel)
       const int hot = (PH == 1) ? fsr - a.hot_base : -1;
       const float2 len2 = f2(len);
+      float2 tl0 = f2(0.0f);   // the first adjacent pair's tally, sent with the second
 #pragma unroll
       for (int s = 0; s < PS; s++) {
         if (live_pair(s)) {
           const float2 qs = kStaged ? *slot(k, s) : q[s];
-          const float2 tau = __fmul2_rn(st[s * LPS], len2);
+          const float2 tau = __fmul2_rn(st[pidx(s) - pidx(0)], len2);
           float2 tally = f2(0.0f);
 #pragma unroll
           for (int p = 0; p < PH; p++) {
@@ -491,14 +520,23 @@ sweep_kernel(const SweepArgs a) {
             tally = __ffma2_rn(w2[p], d, tally);
           }
           if (PH == 1 && hot >= 0) {
-            float* hp = s_hot + hot * ld + 2 * (sub + s * LPS);
+            float* hp = s_hot + hot * ld + 2 * pidx(s);
             atomicAdd(hp, tally.x);
             atomicAdd(hp + 1, tally.y);
+          } else if constexpr (kAdj) {
+            if (!vec4)
+              atomicAdd(ph + s, tally);
+            else if (s == 0)
+              tl0 = tally;
+            else
+              atomicAdd(reinterpret_cast<float4*>(ph),
+                        make_float4(tl0.x, tl0.y, tally.x, tally.y));
           } else {
             atomicAdd(ph + s * LPS, tally);
           }
         }
       }
+
       if constexpr (CMFD) {
         // partial current out of the coarse cell when the next segment lies
         // in another one (through an intermediate cell at a corner), or out
@@ -547,7 +585,7 @@ sweep_kernel(const SweepArgs a) {
       float2 acc = f2(0.0f);
 #pragma unroll
       for (int s = 0; s < PS; s++) {
-        const int g0 = 2 * (sub + s * LPS);
+        const int g0 = 2 * pidx(s);
 #pragma unroll
         for (int p = 0; p < PH; p++) {
           if (g0 < G) acc.x += psi[s][p].x;
@@ -567,7 +605,7 @@ sweep_kernel(const SweepArgs a) {
       float* po = psi_out + ((int64_t) nt * 2 + nd) * F;
 #pragma unroll
       for (int s = 0; s < PS; s++) {
-        const int g0 = 2 * (sub + s * LPS);
+        const int g0 = 2 * pidx(s);
 #pragma unroll
         for (int p = 0; p < PH; p++) {
           if (g0 < G) po[p * G + g0] = psi[s][p].x;
