@@ -164,19 +164,22 @@ struct SweepOccupancy {
 // CMFD partial currents (mode 2 of the sweeps): faces 0 x-, 1 y-, 2 x+,
 // 3 y+ of cell iy * nx + ix; a crossing adds sum_p w_p psi_p of the lane's
 // group pairs (Cmfd::tallyCurrent, src/Cmfd.h:572-660).
-template <int PH, int LPS, int PS>
+// ADJ: the lane's pairs are adjacent (2 sub + s2), as in the sweep's light
+// two-pair instances, instead of interleaved (sub + s2 LPS).
+template <int PH, int LPS, int PS, bool ADJ = false>
 __device__ __forceinline__ void cmfd_add_current(
     const SweepArgs& a, int cell, int face, float frac, int sub, int npairs,
     int ld, const float2 (&w2)[PH], const float2 (&psi)[PS][PH]) {
   float2* cp = reinterpret_cast<float2*>(
-                   a.cm_cur + ((int64_t) cell * 4 + face) * ld) + sub;
+                   a.cm_cur + ((int64_t) cell * 4 + face) * ld) +
+               (ADJ ? PS * sub : sub);
 #pragma unroll
   for (int s2 = 0; s2 < PS; s2++) {
-    if (sub + s2 * LPS < npairs) {
+    if ((ADJ ? PS * sub + s2 : sub + s2 * LPS) < npairs) {
       float2 j = f2(0.0f);
 #pragma unroll
       for (int p = 0; p < PH; p++) j = __ffma2_rn(w2[p], psi[s2][p], j);
-      atomicAdd(cp + s2 * LPS, __fmul2_rn(j, f2(frac)));
+      atomicAdd(cp + (ADJ ? s2 : s2 * LPS), __fmul2_rn(j, f2(frac)));
     }
   }
 }
@@ -185,7 +188,7 @@ __device__ __forceinline__ void cmfd_add_current(
 // lies in another (a corner crossing half by each neighbouring cell,
 // Cmfd::splitEdgeCurrents, src/Cmfd.cpp:2249-2345), or, at the end of the
 // track (f1 < 0), through the boundary face of the track end.
-template <int PH, int LPS, int PS>
+template <int PH, int LPS, int PS, bool ADJ = false>
 __device__ __forceinline__ void cmfd_tally_crossing(
     const SweepArgs& a, int t, int dir, int f0, int f1, bool at_end, int sub,
     int npairs, int ld, const float2 (&w2)[PH], const float2 (&psi)[PS][PH]) {
@@ -197,20 +200,20 @@ __device__ __forceinline__ void cmfd_tally_crossing(
     const int dy = c1 / a.cm_nx - c0 / a.cm_nx;
     const int fx = dx > 0 ? 2 : 0, fy = dy > 0 ? 3 : 1;
     if (dx != 0 && dy != 0) {
-      cmfd_add_current<PH, LPS, PS>(a, c0, fx, 0.5f, sub, npairs, ld, w2, psi);
-      cmfd_add_current<PH, LPS, PS>(a, c0 + dx, fy, 0.5f, sub, npairs, ld, w2,
+      cmfd_add_current<PH, LPS, PS, ADJ>(a, c0, fx, 0.5f, sub, npairs, ld, w2, psi);
+      cmfd_add_current<PH, LPS, PS, ADJ>(a, c0 + dx, fy, 0.5f, sub, npairs, ld, w2,
                                     psi);
-      cmfd_add_current<PH, LPS, PS>(a, c0, fy, 0.5f, sub, npairs, ld, w2, psi);
-      cmfd_add_current<PH, LPS, PS>(a, c0 + dy * a.cm_nx, fx, 0.5f, sub,
+      cmfd_add_current<PH, LPS, PS, ADJ>(a, c0, fy, 0.5f, sub, npairs, ld, w2, psi);
+      cmfd_add_current<PH, LPS, PS, ADJ>(a, c0 + dy * a.cm_nx, fx, 0.5f, sub,
                                     npairs, ld, w2, psi);
     } else {
-      cmfd_add_current<PH, LPS, PS>(a, c0, dx != 0 ? fx : fy, 1.0f, sub, npairs,
+      cmfd_add_current<PH, LPS, PS, ADJ>(a, c0, dx != 0 ? fx : fy, 1.0f, sub, npairs,
                                     ld, w2, psi);
     }
   } else if (at_end) {
     const int face = a.cm_end[2 * t + dir];
     if (face >= 0)
-      cmfd_add_current<PH, LPS, PS>(a, c0, face, 1.0f, sub, npairs, ld, w2,
+      cmfd_add_current<PH, LPS, PS, ADJ>(a, c0, face, 1.0f, sub, npairs, ld, w2,
                                     psi);
   }
 }
@@ -271,8 +274,7 @@ sweep_kernel(const SweepArgs a) {
   // multiple of four floats one 16-byte gather and one 16-byte reduction
   // serve both pairs (the light instances' per-segment accesses, one line
   // per stream each, bound them by L1TEX throughput).
-  constexpr bool kAdj =
-      PS == 2 && !SweepRing<PH, LPS, PS>::staged && MODE != 2;
+  constexpr bool kAdj = PS == 2 && !SweepRing<PH, LPS, PS>::staged;
   auto pidx = [&](int s) { return kAdj ? PS * sub + s : sub + s * LPS; };
   const bool vec4 = kAdj && (ld & 3) == 0;
   auto live_pair = [&](int s) {
@@ -453,8 +455,8 @@ sweep_kernel(const SweepArgs a) {
     int fsr = 0, mat = 0;
     float2 q[PS];
     auto tally_current = [&](int f0, int f1, bool at_end) {
-      cmfd_tally_crossing<PH, LPS, PS>(a, t, dir, f0, f1, at_end, sub, npairs,
-                                       ld, w2, psi);
+      cmfd_tally_crossing<PH, LPS, PS, kAdj>(a, t, dir, f0, f1, at_end, sub,
+                                             npairs, ld, w2, psi);
     };
     if constexpr (kStaged) {
 #pragma unroll
