@@ -148,6 +148,13 @@ __device__ __forceinline__ void cp_async_wait() {
 #ifndef MOC_SWEEP_3D_MIN_BLOCKS
 #define MOC_SWEEP_3D_MIN_BLOCKS 12
 #endif
+// ... and of the one-polar two-pair instances (adjacent pairs; the 3D
+// assembly's autotuned 2 lanes x 2 pairs: 8 blocks, 62 registers, 1.394 ms
+// per sweep; 10 blocks, 48 registers and 12 bytes spilled, 1.370 ms; 12
+// blocks spill 64 bytes)
+#ifndef MOC_SWEEP_3D_PAIRS2_MIN_BLOCKS
+#define MOC_SWEEP_3D_PAIRS2_MIN_BLOCKS 10
+#endif
 // The busy instances of the CMFD mode, which also tally partial currents,
 // take 4 blocks (their registers would spill at 5).
 template <int PH, int PS, int MODE = 0>
@@ -158,6 +165,7 @@ struct SweepOccupancy {
       : (PH * PS > 6)              ? MOC_SWEEP_BIG_MIN_BLOCKS
       : (PH == 1 && PS > 2)        ? 6
       : (PH == 1 && PS == 1)       ? MOC_SWEEP_3D_MIN_BLOCKS
+      : (PH == 1 && PS == 2)       ? MOC_SWEEP_3D_PAIRS2_MIN_BLOCKS
                                    : 8;
 };
 
