@@ -89,7 +89,7 @@ struct LsExpG {
 template <int PH, int PS, bool D3>
 struct LsOccupancy {
   static constexpr int min_blocks =
-      D3 ? ((PS >= 4) ? 3 : (PS >= 3) ? 4 : MOC_LS3D_MIN_BLOCKS)
+      D3 ? ((PS >= 4) ? 3 : (PS >= 3) ? 4 : (PS == 2) ? 6 : MOC_LS3D_MIN_BLOCKS)
          : ((PH * PS >= 12) ? 4 : (PH * PS >= 6) ? 5 : 6);
 };
 
@@ -127,6 +127,13 @@ ls_sweep_kernel(const SweepArgs a) {
       ((int64_t) blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t stream = gwarp * (32 / LPS) + lane / LPS;
   const int npairs = ld >> 1;
+  // lane sub owns the group pairs pidx(s): interleaved (sub + s LPS), or in
+  // the two-pair instances adjacent (2 sub + s), so that with rows padded to
+  // a multiple of four floats the flat and z sources and their tallies of
+  // both pairs travel in 16-byte accesses (as in the flat sweep)
+  constexpr bool kAdj = PS == 2;
+  auto pidx = [&](int s) { return kAdj ? PS * sub + s : sub + s * LPS; };
+  const bool vec4 = kAdj && (ld & 3) == 0;
 
   // the LPS lanes of a stream share its track, so they agree on skipping it
   bool live = stream < 2 * a.num_tracks;
@@ -174,7 +181,7 @@ ls_sweep_kernel(const SweepArgs a) {
     const float* pin = psi_in + ((int64_t) t * 2 + dir) * F;
 #pragma unroll
     for (int s = 0; s < PS; s++) {
-      const int g0 = 2 * (sub + s * LPS);
+      const int g0 = 2 * pidx(s);
 #pragma unroll
       for (int p = 0; p < PH; p++) {
         psi[s][p].x = (g0 < G) ? pin[p * G + g0] * scale : 0.0f;
@@ -212,10 +219,10 @@ ls_sweep_kernel(const SweepArgs a) {
     float zchunk_next = fetchz(LPS + sub);
     float zcur = D3 ? __shfl_sync(gmask, zchunk, 0, LPS) : 0.0f;
 
-    const float2* qf_base = reinterpret_cast<const float2*>(a.qt) + sub;
-    const float4* qm_base = reinterpret_cast<const float4*>(a.qxy) + sub;
+    const float2* qf_base = reinterpret_cast<const float2*>(a.qt) + pidx(0);
+    const float4* qm_base = reinterpret_cast<const float4*>(a.qxy) + pidx(0);
     const float2* qz_base =
-        D3 ? reinterpret_cast<const float2*>(a.qz) + sub : nullptr;
+        D3 ? reinterpret_cast<const float2*>(a.qz) + pidx(0) : nullptr;
     for (int k = 0; k < n; k++) {
       // the next segment's word: segment k + 1 opens a chunk every LPS
       if (((k + 1) & (LPS - 1)) == 0) {
@@ -249,29 +256,50 @@ ls_sweep_kernel(const SweepArgs a) {
       float4 qm[PS];
 #pragma unroll
       for (int s = 0; s < PS; s++) {
-        const bool on = sub + s * LPS < npairs;
-        qf[s] = on ? __ldg(qf_base + (int64_t) fsr * npairs + s * LPS)
-                   : f2(0.0f);
-        qm[s] = on ? __ldg(qm_base + (int64_t) fsr * npairs + s * LPS)
+        const int ds = pidx(s) - pidx(0);
+        const bool on = pidx(s) < npairs;
+        qm[s] = on ? __ldg(qm_base + (int64_t) fsr * npairs + ds)
                    : make_float4(0.f, 0.f, 0.f, 0.f);
-        qzz[s] = (D3 && on)
-                     ? __ldg(qz_base + (int64_t) fsr * npairs + s * LPS)
-                     : f2(0.0f);
+        if (!vec4) {
+          qf[s] = on ? __ldg(qf_base + (int64_t) fsr * npairs + ds) : f2(0.0f);
+          qzz[s] = (D3 && on) ? __ldg(qz_base + (int64_t) fsr * npairs + ds)
+                              : f2(0.0f);
+        }
+      }
+      if (vec4) {
+        // npairs even: a lane's second pair is live with its first
+        const bool on = pidx(0) < npairs;
+        const float4 f4 =
+            on ? __ldg(reinterpret_cast<const float4*>(qf_base +
+                                                       (int64_t) fsr * npairs))
+               : make_float4(0.f, 0.f, 0.f, 0.f);
+        qf[0] = make_float2(f4.x, f4.y);
+        qf[1 % PS] = make_float2(f4.z, f4.w);
+        float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (D3 && on)
+          z4 = __ldg(reinterpret_cast<const float4*>(qz_base +
+                                                     (int64_t) fsr * npairs));
+        qzz[0] = make_float2(z4.x, z4.y);
+        qzz[1 % PS] = make_float2(z4.z, z4.w);
       }
 
       const float2* st =
-          reinterpret_cast<const float2*>(s_st + mat * ld) + sub;
-      float2* ph = reinterpret_cast<float2*>(a.phi + (int64_t) fsr * ld) + sub;
+          reinterpret_cast<const float2*>(s_st + mat * ld) + pidx(0);
+      float2* ph =
+          reinterpret_cast<float2*>(a.phi + (int64_t) fsr * ld) + pidx(0);
       float4* pm =
-          reinterpret_cast<float4*>(a.mom + (int64_t) fsr * 2 * ld) + sub;
+          reinterpret_cast<float4*>(a.mom + (int64_t) fsr * 2 * ld) + pidx(0);
       float2* pmz =
-          D3 ? reinterpret_cast<float2*>(a.momz + (int64_t) fsr * ld) + sub
+          D3 ? reinterpret_cast<float2*>(a.momz + (int64_t) fsr * ld) + pidx(0)
              : nullptr;
       const float2 len2 = f2(len);
+      // the first adjacent pair's flux and z tallies, sent with the second's
+      float2 ph0 = f2(0.0f), pz0 = f2(0.0f);
 #pragma unroll
       for (int s = 0; s < PS; s++) {
-        if (sub + s * LPS < npairs) {
-          const float2 tau = __fmul2_rn(st[s * LPS], len2);
+        const int ds = pidx(s) - pidx(0);
+        if (pidx(s) < npairs) {
+          const float2 tau = __fmul2_rn(st[ds], len2);
           const float2 qx = make_float2(qm[s].x, qm[s].z);
           const float2 qy = make_float2(qm[s].y, qm[s].w);
           float2 sf = __ffma2_rn(qy, f2(c2y), __ffma2_rn(qx, f2(c2x), qf[s]));
@@ -300,20 +328,33 @@ ls_sweep_kernel(const SweepArgs a) {
             psi[s][p] = __ffma2_rn(d, f2(-1.0f), psi[s][p]);
             dacc = __ffma2_rn(w2[p], d, dacc);
           }
-          atomicAdd(ph + s * LPS, dacc);
           const float2 hl = __fmul2_rn(__fmul2_rn(hacc, tau), len2);
           const float2 mx = __ffma2_rn(dacc, f2(sx), __fmul2_rn(hl, f2(dx)));
           const float2 my = __ffma2_rn(dacc, f2(sy), __fmul2_rn(hl, f2(dy)));
-          atomicAdd(pm + s * LPS, make_float4(mx.x, my.x, mx.y, my.y));
+          atomicAdd(pm + ds, make_float4(mx.x, my.x, mx.y, my.y));
+          float2 mz = f2(0.0f);
           if constexpr (D3)
-            atomicAdd(pmz + s * LPS,
-                      __ffma2_rn(dacc, f2(sz), __fmul2_rn(hl, f2(dz))));
+            mz = __ffma2_rn(dacc, f2(sz), __fmul2_rn(hl, f2(dz)));
+          if (!vec4) {
+            atomicAdd(ph + ds, dacc);
+            if constexpr (D3) atomicAdd(pmz + ds, mz);
+          } else if (s == 0) {
+            ph0 = dacc;
+            pz0 = mz;
+          } else {
+            atomicAdd(reinterpret_cast<float4*>(ph),
+                      make_float4(ph0.x, ph0.y, dacc.x, dacc.y));
+            if constexpr (D3)
+              atomicAdd(reinterpret_cast<float4*>(pmz),
+                        make_float4(pz0.x, pz0.y, mz.x, mz.y));
+          }
         }
       }
       if constexpr (CM) {
         const int fsr_next = (k + 1 < n) ? (wnext.y & 0xFFFFFF) : -1;
-        cmfd_tally_crossing<PH, LPS, PS>(a, t, dir, fsr, fsr_next, k + 1 == n,
-                                         sub, npairs, ld, w2, psi);
+        cmfd_tally_crossing<PH, LPS, PS, kAdj>(a, t, dir, fsr, fsr_next,
+                                               k + 1 == n, sub, npairs, ld, w2,
+                                               psi);
       }
       wcur = wnext;
       if constexpr (D3) zcur = znext;
@@ -328,7 +369,7 @@ ls_sweep_kernel(const SweepArgs a) {
       float* po = psi_out + ((int64_t) nt * 2 + nd) * F;
 #pragma unroll
       for (int s = 0; s < PS; s++) {
-        const int g0 = 2 * (sub + s * LPS);
+        const int g0 = 2 * pidx(s);
 #pragma unroll
         for (int p = 0; p < PH; p++) {
           if (g0 < G) po[p * G + g0] = psi[s][p].x;
