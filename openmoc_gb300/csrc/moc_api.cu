@@ -70,6 +70,12 @@ thread_local bool g_device_idle = false;   // set while moc_destroy frees
 // pinned host copies of the device scalars, kept likewise
 std::mutex g_pinned_mu;
 std::vector<void*> g_pinned_scalars;
+// a page-locked bounce buffer for row copies to pageable host memory (a
+// device-to-pageable copy that also changes the row pitch runs at a
+// fraction of the link's rate); grown on demand, guarded by its mutex
+std::mutex g_bounce_mu;
+void* g_bounce = nullptr;
+size_t g_bounce_bytes = 0;
 
 // Frees every idle block of `device` (all devices: -1).
 void release_idle(int device) {
@@ -1487,6 +1493,12 @@ const char* moc_version(void) { return "openmoc_gb300 0.1 (sm_103a)"; }
 
 int moc_release_cached_memory(void) {
   release_idle(-1);
+  {
+    std::lock_guard<std::mutex> lk(g_bounce_mu);
+    if (g_bounce) cudaFreeHost(g_bounce);
+    g_bounce = nullptr;
+    g_bounce_bytes = 0;
+  }
   std::lock_guard<std::mutex> lk(g_pinned_mu);
   for (void* h : g_pinned_scalars) cudaFreeHost(h);
   g_pinned_scalars.clear();
@@ -2317,8 +2329,41 @@ static int copy_rows_out(moc_ctx* c, const float* src, float* out, int64_t n) {
             "expected " + std::to_string(num_host_flux(c)) + " values, got " +
                 std::to_string(n));
   const int G = c->d.num_groups, ld = row_stride(c);
+  const int64_t R = c->d.num_fsrs;
   MOC_CUDA(cudaSetDevice(c->d.device));
-  MOC_CUDA(cudaMemcpy2DAsync(out, 4 * G, src, 4 * ld, 4 * G, c->d.num_fsrs,
+  cudaPointerAttributes attr;
+  const bool locked = cudaPointerGetAttributes(&attr, out) == cudaSuccess &&
+                      attr.type == cudaMemoryTypeHost;
+  cudaGetLastError();
+  const size_t bytes = sizeof(float) * (size_t) R * ld;
+  if (!locked) {
+    // the rows as they lie into the bounce buffer, then de-pitched here
+    std::lock_guard<std::mutex> lk(g_bounce_mu);
+    if (g_bounce_bytes < bytes) {
+      if (g_bounce) cudaFreeHost(g_bounce);
+      g_bounce = nullptr;
+      g_bounce_bytes = 0;
+      if (cudaMallocHost(&g_bounce, bytes) == cudaSuccess) {
+        g_bounce_bytes = bytes;
+      } else {
+        cudaGetLastError();
+        g_bounce = nullptr;
+      }
+    }
+    if (g_bounce) {
+      MOC_CUDA(cudaMemcpyAsync(g_bounce, src, bytes, cudaMemcpyDeviceToHost,
+                               c->stream));
+      MOC_CUDA(cudaStreamSynchronize(c->stream));
+      const float* b = static_cast<const float*>(g_bounce);
+      if (ld == G)
+        std::memcpy(out, b, sizeof(float) * (size_t) R * G);
+      else
+        for (int64_t r = 0; r < R; r++)
+          std::memcpy(out + r * G, b + r * ld, sizeof(float) * G);
+      return MOC_OK;
+    }
+  }
+  MOC_CUDA(cudaMemcpy2DAsync(out, 4 * G, src, 4 * ld, 4 * G, R,
                              cudaMemcpyDeviceToHost, c->stream));
   MOC_CUDA(cudaStreamSynchronize(c->stream));
   return MOC_OK;
