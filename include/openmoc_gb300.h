@@ -247,8 +247,10 @@ int moc_eval_attenuation(moc_ctx* ctx, int kind, const float* x, float* g,
 
 /** No counterpart in the reference.  Contexts keep the device memory they
  *  free (up to 16 GiB), so that a context created and destroyed per request
- *  reuses it without cudaMalloc / cudaFree; this returns all of it to the
- *  driver.  Call it with no context in use. */
+ *  reuses it without cudaMalloc / cudaFree, and row copies to pageable host
+ *  memory go through a kept page-locked bounce buffer; this returns all of
+ *  it (and the page-locked scalar buffers) to the driver.  Call it with no
+ *  context in use. */
 int moc_release_cached_memory(void);
 
 /** Largest num_fsrs that moc_fission_source_total_noalloc accepts. */
