@@ -344,12 +344,17 @@ int moc_set_negative_fluxes_allowed(moc_ctx* ctx, int allowed);
  *  with the flux at the start of the iteration
  *  (CPUSolver::computeStabilizingFlux + stabilizeFlux,
  *  src/CPUSolver.cpp:2665-2810) before the normalisation.  on = 0 turns it
- *  off.  Flat source only. */
+ *  off.  With a linear source the flux moments take the same correction
+ *  against their own start-of-iteration values (CPULSSolver::
+ *  computeStabilizingFlux / stabilizeFlux, src/CPULSSolver.cpp:886-1049),
+ *  except under YAMAMOTO, whose moment branch in the reference leaves them
+ *  as they are. */
 int moc_set_transport_stabilization(moc_ctx* ctx, int on, double factor,
                                     int type);
 /** The protected hooks: CPUSolver::computeStabilizingFlux keeps the current
- *  flux as the base of the correction; stabilizeFlux applies it
- *  (src/CPUSolver.cpp:2665-2810). */
+ *  flux (and a linear source's moments) as the base of the correction;
+ *  stabilizeFlux applies it (src/CPUSolver.cpp:2665-2810,
+ *  src/CPULSSolver.cpp:886-1049). */
 int moc_compute_stabilizing_flux(moc_ctx* ctx);
 int moc_stabilize_flux(moc_ctx* ctx);
 /** CPUSolver::computeFSRFissionSources / computeFSRScatterSources

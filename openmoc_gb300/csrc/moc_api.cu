@@ -297,6 +297,10 @@ struct moc_ctx {
   bool stab_dirty = true;
   float2* stab = nullptr;
   float* stab_base = nullptr;
+  // the linear source's flux moments (xy, z) at the start of the iteration,
+  // the base of their stabilization
+  float* stab_mom = nullptr;
+  float* stab_momz = nullptr;
   std::vector<float> h_sigma_t, h_scat_diag;
   std::vector<uint8_t> h_mat_used;
   // On-the-fly 3D segmentation (moc_set_otf_tracks): 3D track descriptors,
@@ -822,7 +826,7 @@ void enqueue_add_source(moc_ctx* c, const moc::SolverArgs& a, int update) {
   if (c->ls) {
     moc::launch_ls_add_source(a, update, c->stream);
     c->launches++;
-    if (update) {
+    if (update == 1) {
       moc::launch_ls_scale_moments(a, c->stream);
       c->launches++;
     }
@@ -907,14 +911,45 @@ int zero_track_fluxes(moc_ctx* c) {
   return MOC_OK;
 }
 
+// Whether the linear source's moments are stabilized: CPULSSolver's
+// YAMAMOTO branch for the moments assigns `ratio = max_ratio` where the flat
+// branch raises max_ratio, so its ratio stays 0 and the moments are left as
+// they are (src/CPULSSolver.cpp:924-941, 1010-1031).
+bool stab_moments(const moc_ctx* c) {
+  return c->stab_on && c->ls && c->stab_type != MOC_STABILIZE_YAMAMOTO;
+}
+
+// The flux moments at the start of an eigenvalue iteration, kept as the base
+// of their stabilization (CPULSSolver::computeStabilizingFlux takes them
+// before the sources of the iteration; the flat flux's base is phi_old).
+int enqueue_stab_moments_base(moc_ctx* c) {
+  if (!stab_moments(c)) return MOC_OK;
+  if (!c->stab_mom) MOC_TRY(dalloc(&c->stab_mom, 2 * num_flux(c)));
+  MOC_CUDA(cudaMemcpyAsync(c->stab_mom, c->mom, 8 * num_flux(c),
+                           cudaMemcpyDeviceToDevice, c->stream));
+  if (c->ls3d) {
+    if (!c->stab_momz) MOC_TRY(dalloc(&c->stab_momz, num_flux(c)));
+    MOC_CUDA(cudaMemcpyAsync(c->stab_momz, c->momz, 4 * num_flux(c),
+                             cudaMemcpyDeviceToDevice, c->stream));
+  }
+  return MOC_OK;
+}
+
 // addSourceToScalarFlux, computeKeff, stabilizeFlux and the normalisation
 // factor of an eigenvalue iteration (the residual kernel then normalises).
 void enqueue_eigen_update(moc_ctx* c, const moc::SolverArgs& a) {
   if (c->stab_on) {
-    // keff first; the stabilized flux sets the normalisation
+    // keff first; the stabilized flux sets the normalisation, which then
+    // scales the stabilized moments of a linear source
     enqueue_add_source(c, a, 2);
-    moc::launch_stabilize(a, c->phi_old, 1, c->stream);
+    moc::launch_stabilize(a, c->phi_old, 1, c->stream,
+                          stab_moments(c) ? c->stab_mom : nullptr,
+                          stab_moments(c) && c->ls3d ? c->stab_momz : nullptr);
     c->launches++;
+    if (c->ls) {
+      moc::launch_ls_scale_moments(a, c->stream);
+      c->launches++;
+    }
   } else if (c->num_instances) {
     // each instance's keff and normalisation
     enqueue_add_source(c, a, 0);
@@ -949,6 +984,7 @@ int run_iterations(moc_ctx* c, int kind, int res_type) {
       if (kind == moc::kModeFlux) {
         MOC_TRY(enqueue_zero_tallies(c, a));
       } else {
+        if (kind == moc::kModeEigen) MOC_TRY(enqueue_stab_moments_base(c));
         enqueue_sources(c, a, -1, 1);
       }
       MOC_TRY(enqueue_sweep(c, 1, true, i));
@@ -1633,6 +1669,8 @@ int moc_destroy(moc_ctx* c) {
   dfree(c->tc_b);
   dfree(c->stab);
   dfree(c->stab_base);
+  dfree(c->stab_mom);
+  dfree(c->stab_momz);
   dfree(c->inst);
   dfree(c->segs_ls);
   dfree(c->ls_ang);
@@ -2252,6 +2290,7 @@ int moc_bench_iterations(moc_ctx* c, int steps, int res_type, int flush_l2,
   for (int i = 0; i < steps; i++) {
     if (flush_l2) moc::launch_fill(c->flush, c->flush_n, (float) i, c->stream);
     MOC_CUDA(cudaEventRecord(ev[4 * i], c->stream));
+    MOC_TRY(enqueue_stab_moments_base(c));
     enqueue_sources(c, a, -1, 1);
     MOC_CUDA(cudaEventRecord(ev[4 * i + 1], c->stream));
     MOC_TRY(enqueue_sweep(c, 1, false, 0));
@@ -2635,8 +2674,6 @@ int moc_set_linear_source(moc_ctx* c, const moc_ls_geometry* g) {
             "on-the-fly segmentation and the linear source do not combine");
   MOC_CHECK(!c->keff_balance, MOC_ERR_UNSUPPORTED,
             "keff from the neutron balance is built for the flat source");
-  MOC_CHECK(!c->stab_on, MOC_ERR_UNSUPPORTED,
-            "transport stabilization is built for the flat source");
   MOC_CHECK(c->d.num_polar_half >= 1 && c->d.num_polar_half <= 3,
             MOC_ERR_UNSUPPORTED,
             "the linear-source sweep takes 1 to 3 polar angles per half space");
@@ -2796,8 +2833,6 @@ int moc_set_transport_stabilization(moc_ctx* c, int on, double factor,
   MOC_CHECK(type == MOC_STABILIZE_DIAGONAL || type == MOC_STABILIZE_YAMAMOTO ||
                 type == MOC_STABILIZE_GLOBAL,
             MOC_ERR_ARG, "unknown stabilization type");
-  MOC_CHECK(!c->ls, MOC_ERR_UNSUPPORTED,
-            "transport stabilization is built for the flat source");
   if (c->stab && c->d.num_materials > 0) {
     // the coefficients depend on the factor and type
     dfree(c->stab);
@@ -2817,6 +2852,7 @@ int moc_compute_stabilizing_flux(moc_ctx* c) {
   if (!c->stab_base) MOC_TRY(dalloc(&c->stab_base, num_flux(c)));
   MOC_CUDA(cudaMemcpyAsync(c->stab_base, c->phi, 4 * num_flux(c),
                            cudaMemcpyDeviceToDevice, c->stream));
+  MOC_TRY(enqueue_stab_moments_base(c));
   return MOC_OK;
 }
 
@@ -2827,7 +2863,11 @@ int moc_stabilize_flux(moc_ctx* c) {
             "computeStabilizingFlux must come before stabilizeFlux");
   MOC_TRY(ensure_stab(c));
   moc::SolverArgs a = solver_args(c, 0);
-  moc::launch_stabilize(a, c->stab_base, 0, c->stream);
+  MOC_CHECK(!stab_moments(c) || c->stab_mom, MOC_ERR_STATE,
+            "computeStabilizingFlux must come before stabilizeFlux");
+  moc::launch_stabilize(a, c->stab_base, 0, c->stream,
+                        stab_moments(c) ? c->stab_mom : nullptr,
+                        stab_moments(c) && c->ls3d ? c->stab_momz : nullptr);
   c->launches++;
   MOC_CUDA(cudaGetLastError());
   return MOC_OK;

@@ -300,9 +300,12 @@ void launch_fission_rate(const SolverArgs& a, int what, cudaStream_t s);
 // transport stabilization of phi from `base` (the flux at the start of the
 // iteration); in_loop: only from the second iteration on, and the
 // normalisation factor of the stabilized flux is computed as
-// launch_fission_rate(what = 1) does
+// launch_fission_rate(what = 1) does; base_mom / base_momz: the flux
+// moments at the start of the iteration, stabilized alongside (null: the
+// moments are left as they are)
 void launch_stabilize(const SolverArgs& a, const float* base, int in_loop,
-                      cudaStream_t s);
+                      cudaStream_t s, const float* base_mom = nullptr,
+                      const float* base_momz = nullptr);
 // the fission (which = 0) or scattering (which = 1) part of the reduced
 // source alone into qt (CPUSolver::computeFSRFissionSources /
 // computeFSRScatterSources)

@@ -598,9 +598,13 @@ fission_rate_kernel(const SolverArgs a, int what) {
 // c2 = 1 / (1 + c1); GLOBAL: c1 = 1 / f - 1, c2 = f).  In the eigenvalue
 // loop (in_loop) it applies from the second iteration on and then computes
 // the normalisation factor of the stabilized flux (normalizeFluxes follows
-// stabilizeFlux, src/Solver.cpp:1632-1640).
+// stabilizeFlux, src/Solver.cpp:1632-1640).  With base_mom set, the flux
+// moments of the linear source take the same coefficients against their
+// own start-of-iteration values (CPULSSolver::computeStabilizingFlux /
+// stabilizeFlux, src/CPULSSolver.cpp:886-1049; base_momz: the z moment).
 __global__ void __launch_bounds__(kRowThreads)
-stabilize_kernel(const SolverArgs a, const float* base, int in_loop) {
+stabilize_kernel(const SolverArgs a, const float* base, int in_loop,
+                 const float* base_mom, const float* base_momz) {
   if (skip(a)) return;
   DevScalars* sc = a.sc;
   const int G = a.num_groups;
@@ -622,6 +626,22 @@ stabilize_kernel(const SolverArgs a, const float* base, int in_loop) {
         phi[g] = x;
       }
       s += (double) (nf[g] * x);
+    }
+    if (base_mom && apply) {
+      float2* mom = reinterpret_cast<float2*>(a.mom + r * 2 * a.ld);
+      const float2* bm = reinterpret_cast<const float2*>(base_mom + r * 2 * a.ld);
+      for (int g = lane; g < G; g += 32) {
+        const float2 c = cf[g];
+        const float2 b = bm[g];
+        float2 v = mom[g];
+        v.x = (v.x + c.x * b.x) * c.y;
+        v.y = (v.y + c.x * b.y) * c.y;
+        mom[g] = v;
+        if (base_momz) {
+          float* z = a.momz + r * a.ld + g;
+          *z = (*z + c.x * base_momz[r * a.ld + g]) * c.y;
+        }
+      }
     }
     rate += s * (double) a.fsr_vol[r];
   }
@@ -1121,8 +1141,10 @@ ls_add_source_kernel(const SolverArgs a, int update) {
     const double total = *(volatile double*) &sc->accum_rate;
     const double R = (double) a.num_fsrs;
     sc->keff = sc->keff * (total / R);
-    sc->factor = R / total;
-    sc->scale[sc->cur] *= (float) sc->factor;
+    if (update != 2) {   // 2: the stabilized flux sets the normalisation
+      sc->factor = R / total;
+      sc->scale[sc->cur] *= (float) sc->factor;
+    }
     sc->accum_rate = 0.0;
     sc->ticket_rate = 0;
     __threadfence();
@@ -1513,9 +1535,10 @@ void launch_fission_rate(const SolverArgs& a, int what, cudaStream_t s) {
 }
 
 void launch_stabilize(const SolverArgs& a, const float* base, int in_loop,
-                      cudaStream_t s) {
-  stabilize_kernel<<<row_grid(a.num_fsrs), kRowThreads, 0, s>>>(a, base,
-                                                               in_loop);
+                      cudaStream_t s, const float* base_mom,
+                      const float* base_momz) {
+  stabilize_kernel<<<row_grid(a.num_fsrs), kRowThreads, 0, s>>>(
+      a, base, in_loop, base_mom, base_momz);
 }
 
 void launch_instance_rates(const SolverArgs& a, int what, cudaStream_t s) {

@@ -731,6 +731,8 @@ typedef struct {
   const real* fixed_xy;   /* [R][2][G] fixed source moments, or NULL (2D) */
   int32_t negative_allowed;
   int32_t num_flat;       /* FSRs whose expansion matrix is singular */
+  real* stab_xyz;         /* [R][3][G] stabilizing flux moments, or NULL:
+                             the moments are not stabilized */
 } oracle_ls_state;
 
 #define MIN_DET 1E-10     /* src/constants.h:70 */
@@ -1381,6 +1383,74 @@ long oracle_ls_add_source(const oracle_problem* p, oracle_state* s,
   return neg;
 }
 
+/* CPULSSolver::computeStabilizingFlux, moment part
+ * (src/CPULSSolver.cpp:886-965), after the flat part.  DIAGONAL: where the
+ * in-group scattering is negative, -f sigma_s,gg / sigma_t,g times each
+ * moment; GLOBAL: (1 / f - 1) times each moment.  YAMAMOTO: the reference's
+ * moment branch assigns `ratio = max_ratio` where the flat branch raises
+ * max_ratio, so its ratio stays 0 and the stabilizing moments are zero. */
+void oracle_ls_compute_stabilizing_moments(const oracle_problem* p,
+                                           const oracle_state* s,
+                                           oracle_ls_state* ls) {
+  const long R = p->num_fsrs;
+  const int G = p->num_groups;
+  if (!ls->stab_xyz) return;
+  if (s->stab_type == 0) {
+    for (long r = 0; r < R; r++) {
+      const int m = p->fsr_mat[r];
+      for (int e = 0; e < G; e++) {
+        const real sigma_s = (real) p->sigma_s[((long) m * G + e) * G + e];
+        const real sigma_t = (real) p->sigma_t[(long) m * G + e];
+        if (sigma_s < 0.0)
+          for (int i = 0; i < 3; i++)
+            ls->stab_xyz[(r * 3 + i) * G + e] =
+                (real) (-ls->mom[(r * 3 + i) * G + e] * s->stab_factor *
+                        sigma_s / sigma_t);
+      }
+    }
+  } else if (s->stab_type == 1) {
+    const real max_ratio = 0.0;
+    for (long i = 0; i < R * 3 * G; i++) ls->stab_xyz[i] = ls->mom[i] * max_ratio;
+  } else {
+    const real mult = (real) (1.0 / s->stab_factor - 1.0);
+    for (long i = 0; i < R * 3 * G; i++) ls->stab_xyz[i] = ls->mom[i] * mult;
+  }
+}
+
+/* CPULSSolver::stabilizeFlux, moment part (src/CPULSSolver.cpp:970-1049):
+ * the stabilizing moments added and the sum scaled as the flat flux is
+ * (DIAGONAL 1 / (1 - f sigma_s,gg / sigma_t,g) where sigma_s,gg < 0,
+ * YAMAMOTO 1 / (1 + 0), GLOBAL f). */
+void oracle_ls_stabilize_moments(const oracle_problem* p, const oracle_state* s,
+                                 oracle_ls_state* ls) {
+  const long R = p->num_fsrs;
+  const int G = p->num_groups;
+  if (!ls->stab_xyz) return;
+  for (long r = 0; r < R; r++) {
+    const int m = p->fsr_mat[r];
+    for (int e = 0; e < G; e++) {
+      const real sigma_s = (real) p->sigma_s[((long) m * G + e) * G + e];
+      const real sigma_t = (real) p->sigma_t[(long) m * G + e];
+      for (int i = 0; i < 3; i++) {
+        real* x = &ls->mom[(r * 3 + i) * G + e];
+        const real add = ls->stab_xyz[(r * 3 + i) * G + e];
+        if (s->stab_type == 0) {
+          if (sigma_s < 0.0) {
+            *x += add;
+            *x = (real) (*x / (1.0 - s->stab_factor * sigma_s / sigma_t));
+          }
+        } else if (s->stab_type == 1) {
+          *x += add;
+          *x = (real) (*x / (1.0 + 0.0));
+        } else {
+          *x += add;
+          *x = (real) (*x * s->stab_factor);
+        }
+      }
+    }
+  }
+}
+
 /* Solver::computeEigenvalue with the linear-source hooks. */
 int oracle_ls_compute_eigenvalue(const oracle_problem* p,
                                  const oracle_ls_geometry* geo,
@@ -1396,11 +1466,23 @@ int oracle_ls_compute_eigenvalue(const oracle_problem* p,
   double k_prev = s->keff;
   double residual = 0.0;
   int iters = 0;
+  if (s->stab_flux)
+    memset(s->stab_flux, 0, sizeof(real) * p->num_fsrs * p->num_groups);
+  if (ls->stab_xyz)
+    memset(ls->stab_xyz, 0, sizeof(real) * p->num_fsrs * 3 * p->num_groups);
   for (int i = 0; i < max_iters; i++) {
+    if (i > 0 && s->stab_flux) {
+      oracle_compute_stabilizing_flux(p, s);
+      oracle_ls_compute_stabilizing_moments(p, s, ls);
+    }
     oracle_ls_compute_sources(p, s, ls, i);
     oracle_ls_sweep(p, geo, s, ls);
     oracle_ls_add_source(p, s, ls);
     oracle_compute_keff(p, s);
+    if (i > 0 && s->stab_flux) {
+      oracle_stabilize_flux(p, s);
+      oracle_ls_stabilize_moments(p, s, ls);
+    }
     oracle_ls_normalize(p, s, ls);
     residual = oracle_residual(p, s, res_type);
     int dk = (int) (1e5 * (s->keff - k_prev));

@@ -55,7 +55,7 @@ class _LSState(C.Structure):
     _fields_ = [("ilem", C.c_void_p), ("src_const", C.c_void_p),
                 ("mom", C.c_void_p), ("red_xyz", C.c_void_p),
                 ("fixed_xy", C.c_void_p), ("negative_allowed", C.c_int32),
-                ("num_flat", C.c_int32)]
+                ("num_flat", C.c_int32), ("stab_xyz", C.c_void_p)]
 
 
 def build() -> None:
@@ -296,6 +296,14 @@ class LSOracle(Oracle):
         self._cl = _LSState(_ptr(self.ilem), _ptr(self.src_const), _ptr(self.mom),
                             _ptr(self.red_xyz), _ptr(self.fixed_xy),
                             1 if negative_fluxes_allowed else 0, 0)
+
+    def stabilize_transport(self, factor: float, kind: int) -> None:
+        """Solver::stabilizeTransport on CPULSSolver, which stabilizes the
+        flux moments too (_stabilize_moments is set in its constructor,
+        src/CPULSSolver.cpp:19)."""
+        super().stabilize_transport(factor, kind)
+        self.stab_xyz = np.zeros(self.p.num_fsrs * 3 * self.p.num_groups, self.real)
+        self._cl.stab_xyz = _ptr(self.stab_xyz)
 
     def constants(self) -> int:
         return self.lib.oracle_ls_constants(C.byref(self._cp), C.byref(self._cg),

@@ -327,3 +327,62 @@ def test_gpu_ls_3d_lattice_matches_oracle_every_shape(G, shapes):
         assert _rel(s.getFluxes(), o.phi.reshape(R, G), 1e-4) < 2e-5, (lps, pairs)
         assert _peak(s.getFluxMoments(), ref_m) < 1e-4, (lps, pairs)
         s.close()
+
+
+def _negative_in_group_scattering(p):
+    """p with the water's within-group scattering made negative (as the
+    transport-stabilization fixtures' moderator has it)."""
+    M, G = p.num_materials, p.num_groups
+    ss = np.array(p.sigma_s, np.float32).reshape(M, G, G)
+    for g in range(G):
+        ss[M - 1, g, g] = -0.05 * abs(ss[M - 1, g, g])
+    p.sigma_s = ss.ravel()
+    return p
+
+
+@pytest.mark.parametrize("kind,factor", [("DIAGONAL", 1.0), ("YAMAMOTO", 0.5),
+                                         ("GLOBAL", 0.5)])
+def test_gpu_ls_stabilization_matches_oracle(kind, factor):
+    """Transport stabilization of a linear-source solve (the flat flux and
+    the flux moments, CPULSSolver::computeStabilizingFlux / stabilizeFlux)
+    against the FP64 oracle after 12 eigenvalue iterations; the moments
+    differ from the unstabilized solve's except under YAMAMOTO, whose
+    moment branch in the reference leaves them as they are."""
+    from openmoc_gb300 import GB300LSSolver
+    from openmoc_gb300.lattice import REFLECTIVE, VACUUM
+    G, iters = 7, 12
+    p = _negative_in_group_scattering(
+        _lattice_ls(3, G, bc=(REFLECTIVE, VACUUM, REFLECTIVE, VACUUM)))
+    o = LSOracle(p, p.linear_source, "f64", num_threads=8)
+    o.stabilize_transport(factor, {"DIAGONAL": 0, "YAMAMOTO": 1, "GLOBAL": 2}[kind])
+    o.compute_eigenvalue(iters, 1, 1e-30)
+    s = GB300LSSolver(p, device=0)
+    s.stabilizeTransport(factor, kind)
+    s.setConvergenceThreshold(1e-30)
+    s.computeEigenvalue(iters, 1)
+    R = p.num_fsrs
+    assert s.getNumIterations() == iters
+    assert abs(s.getKeff() - o.keff) < 2e-6
+    assert _rel(s.getFluxes(), o.phi.reshape(R, G), 1e-4) < 2e-5
+    assert _peak(s.getFluxMoments(), o.mom.reshape(R, 3, G)) < 1e-4
+    s.close()
+
+
+def test_gpu_ls_3d_stabilization_matches_oracle():
+    """GLOBAL stabilization on the 3D fixture's problem (x, y and z
+    moments) against the FP64 oracle after 10 eigenvalue iterations."""
+    from openmoc_gb300 import GB300LSSolver
+    p, _, arr = load_case("pin3d_ls", "f32")
+    iters = 10
+    o = LSOracle(p, ls_arrays(arr), "f64", num_threads=8)
+    o.stabilize_transport(0.5, 2)
+    o.compute_eigenvalue(iters, 1, 1e-30)
+    s = GB300LSSolver(p, device=0)
+    s.stabilizeTransport(0.5, "GLOBAL")
+    s.setConvergenceThreshold(1e-30)
+    s.computeEigenvalue(iters, 1)
+    R, G = p.num_fsrs, p.num_groups
+    assert abs(s.getKeff() - o.keff) < 2e-6
+    assert _rel(s.getFluxes(), o.phi.reshape(R, G), 1e-4) < 2e-5
+    assert _peak(s.getFluxMoments(), o.mom.reshape(R, 3, G)) < 1e-4
+    s.close()

@@ -187,3 +187,23 @@ def test_ls_3d_fixture_positions_inside_their_regions():
             m = arr[key].astype(np.float64) + 0.5 * L * u
             c = np.bincount(p.seg_fsr, w * m, p.num_fsrs) / vol
             assert np.max(np.abs(c) / size) < 1e-5, (case, key)
+
+
+def test_ls_oracle_stabilization_identities():
+    """The oracle's moment stabilization: GLOBAL with factor 1 (a zero
+    stabilizing flux, scaled by 1) and DIAGONAL on a problem without
+    negative within-group scattering change nothing; GLOBAL with factor 0.5
+    changes the moments."""
+    o0 = _oracle("pin7_ls", "f64")[0]
+    o0.compute_eigenvalue(6, 1, 1e-30)
+    for kind, factor in ((2, 1.0), (0, 1.0)):
+        o = _oracle("pin7_ls", "f64")[0]
+        o.stabilize_transport(factor, kind)
+        o.compute_eigenvalue(6, 1, 1e-30)
+        assert o.keff == o0.keff
+        np.testing.assert_array_equal(o.mom, o0.mom)
+        np.testing.assert_array_equal(o.phi, o0.phi)
+    o = _oracle("pin7_ls", "f64")[0]
+    o.stabilize_transport(0.5, 2)
+    o.compute_eigenvalue(6, 1, 1e-30)
+    assert np.abs(o.mom - o0.mom).max() > 0
