@@ -1355,6 +1355,7 @@ moc::CmfdArgs cmfd_args(moc_ctx* c) {
 // (the host checks the state once per block of iterations, as without
 // CMFD); the host solve reads the tallies back every iteration.
 int run_cmfd_iterations(moc_ctx* c, int res_type) {
+  MOC_TRY(ensure_stab(c));
   moc_cmfd::Solver& S = *c->cmfd;
   moc::SolverArgs a = solver_args(c, 1);
   const int C = S.cfg.cells(), E = S.cfg.E;
@@ -1365,6 +1366,7 @@ int run_cmfd_iterations(moc_ctx* c, int res_type) {
   for (;;) {
     const int k = c->cm_host ? 1 : c->iters_per_sync;
     for (int i = 0; i < k; i++) {
+      MOC_TRY(enqueue_stab_moments_base(c));
       enqueue_sources(c, a, -1, 1);
       MOC_CUDA(cudaMemsetAsync(c->cm_cur, 0, 4 * ncur, c->stream));
       MOC_TRY(enqueue_sweep(c, 1, true, i));
@@ -1409,7 +1411,13 @@ int run_cmfd_iterations(moc_ctx* c, int res_type) {
                                                 c->cm_pro_coef},
                                c->d.num_fsrs, c->d.num_groups, ld, E,
                                S.cfg.unbounded, c->sc, c->stream);
-      moc::launch_fission_rate(a, 1, c->stream);
+      if (c->stab_on)   // stabilizeFlux follows the CMFD update; the
+                        // normalisation factor is the stabilized flux's
+        moc::launch_stabilize(a, c->phi_old, 1, c->stream,
+                              stab_moments(c) ? c->stab_mom : nullptr,
+                              stab_moments(c) && c->ls3d ? c->stab_momz : nullptr);
+      else
+        moc::launch_fission_rate(a, 1, c->stream);
       c->launches += 2;
       if (c->ls) {     // normalizeFluxes scales the moments too
         moc::launch_ls_scale_moments(a, c->stream);

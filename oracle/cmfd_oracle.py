@@ -396,7 +396,12 @@ def cmfd_eigenvalue(oracle, cm: CmfdOracle, max_iters=1000, res_type=1, tol=1e-5
     k_prev = 1.0
     cur = np.zeros((cm.C, 4, G))
     its = 0
+    stab = getattr(oracle, "stab_flux", None) is not None
+    if stab:
+        oracle.stab_flux[:] = 0.0
     for i in range(max_iters):
+        if i > 0 and stab:      # Solver::computeEigenvalue, src/Solver.cpp:1616-1619
+            oracle.compute_stabilizing_flux()
         oracle.compute_sources(i)
         cur[:] = 0.0
         oracle.sweep_currents(cm.cell, cm.end_face, cm.nx, cur)
@@ -406,6 +411,8 @@ def cmfd_eigenvalue(oracle, cm: CmfdOracle, max_iters=1000, res_type=1, tol=1e-5
         oracle.keff = k
         scaled = phi * cm.update_ratios(i, ratio)[:, cm.group_of]
         oracle.phi[:] = scaled.ravel().astype(oracle.phi.dtype)
+        if i > 0 and stab:      # after the CMFD update, src/Solver.cpp:1632-1635
+            oracle.stabilize_flux()
         oracle.normalize()
         residual = oracle.residual_of(res_type)
         dk = int(1e5 * (k - k_prev))

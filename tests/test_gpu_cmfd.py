@@ -360,3 +360,45 @@ def test_gpu_cmfd_core_mesh_matches_oracle_step_by_step():
         assert np.max(np.abs(old - cm.old_flux)) < 1e-4 * np.abs(cm.old_flux).max(), solver
         assert abs(info["keff"] - cm.keff) < 2e-6, solver
         s.close()
+
+
+@pytest.mark.parametrize("kind,factor", [("GLOBAL", 0.5), ("YAMAMOTO", 0.5)])
+def test_gpu_cmfd_with_stabilization_matches_oracle(kind, factor):
+    """Transport stabilization inside the CMFD loop (stabilizeFlux after the
+    CMFD update, before the normalisation, src/Solver.cpp:1616-1640): the
+    5 x 5 lattice of the step-by-step test, 8 iterations, against the FP64
+    oracle CMFD with the oracle's stabilization hooks."""
+    from openmoc_gb300 import Cmfd, GB300Solver
+    from openmoc_gb300 import lattice as lat
+    from openmoc_gb300.lattice import REFLECTIVE, VACUUM
+    from oracle.cmfd_oracle import CmfdOracle, cmfd_eigenvalue
+    from oracle.oracle import Oracle
+    mats = lat._fuel_mod(2, 7, 1)
+    pm = np.zeros((5, 5), np.int32)
+    for (r, c) in [(1, 1), (2, 3), (3, 2)]:
+        pm[r, c] = 1
+    p = lat.lattice(5, 5, pm, mats, 1, num_azim=16, spacing=0.1,
+                    bc=(REFLECTIVE, VACUUM, REFLECTIVE, VACUUM))
+    c = Cmfd()
+    c.setLatticeStructure(5, 5)
+    c.setGroupStructure([[1, 2, 3], [4, 5, 6, 7]])
+    mesh, keep = c.mesh(p)
+    g = p.cmfd_geometry
+    cm = CmfdOracle(p, 5, 5, keep[0], keep[1], keep[2], g["end_face"], g["bc"],
+                    keep[4], g["edc_mu"], g["edc_w"], k_nearest=0,
+                    centroid=g["fsr_centroid"], origin=(g["bounds"][0], g["bounds"][2]))
+    o = Oracle(p, "f64", num_threads=8)
+    o.stabilize_transport(factor, {"YAMAMOTO": 1, "GLOBAL": 2}[kind])
+    iters = 8
+    cmfd_eigenvalue(o, cm, iters, 1, 1e-30)
+    s = GB300Solver(device=0)
+    s.setConvergenceThreshold(1e-30)
+    s.setTrackGenerator(p)
+    s.setCmfd(c)
+    s.stabilizeTransport(factor, kind)
+    s.computeEigenvalue(iters, 1)
+    assert s.getNumIterations() == iters
+    assert abs(s.getKeff() - o.keff) < 2e-6
+    R = p.num_fsrs
+    assert _rel(s.getFluxes(), o.phi.reshape(R, -1), 1e-4) < 2e-5
+    s.close()
